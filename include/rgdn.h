@@ -1,0 +1,296 @@
+/*
+ * rgdn.h — C ABI of the GB300-native A-SVGF denoiser and luminance-histogram
+ * auto-exposure (the image-space "denoise-and-expose" path of RayTracedGL1).
+ *
+ * Every entry point takes plain pointers and sizes; CUDA streams are passed as
+ * `rgdn_cuda_stream` (ABI-identical to `cudaStream_t`, NULL = legacy default
+ * stream). No C++ exceptions cross this boundary; every call returns an
+ * `rgdn_status`.
+ *
+ * Mapping onto the reference (paths inside the RayTracedGL1 tree):
+ *
+ *   RTGL1::Denoiser::Denoise(cmd, frameIndex, uniform)     Source/Denoiser.cpp:64-255
+ *       -> rgdn_denoise(stream, frameIndex, params, cudaStream)
+ *   RTGL1::PathTracer::CalculateGradientsSamples(...)     Source/PathTracer.cpp:196-219
+ *       (image-space part of RtGradients.rgen) is the first stage of rgdn_denoise
+ *   RTGL1::Tonemapping::CalculateExposure(cmd, frameIndex, uniform)
+ *                                                          Source/Tonemapping.cpp:59-165
+ *       -> rgdn_calculate_exposure(stream, frameIndex, params, cudaStream)
+ *   RTGL1::Tonemapping::GetDescSet (ShTonemapping SSBO)   Source/Tonemapping.h:36-55
+ *       -> rgdn_stream_tonemapping_device / rgdn_get_tonemapping
+ *   RTGL1::Framebuffers (images + _Prev swap by frameIndex)
+ *                                                          Source/Framebuffers.cpp:34-49,640-699
+ *       -> rgdn_stream_* (a stream owns one framebuffer set + history + tonemapping state)
+ *   RgResult                                               Include/RTGL1/RTGL1.h:78-94
+ *       -> rgdn_status (same numeric values where a code exists in both)
+ */
+#ifndef RGDN_H_
+#define RGDN_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define RGDN_API_VERSION 1
+
+/* Status codes. Values 0..13 keep the meaning of RgResult (RTGL1.h:78-94). */
+typedef enum rgdn_status
+{
+    RGDN_SUCCESS                 = 0,  /* RG_RESULT_SUCCESS */
+    RGDN_WRONG_INSTANCE          = 3,  /* RG_RESULT_WRONG_INSTANCE: null / destroyed handle */
+    RGDN_DEVICE_ERROR            = 5,  /* RG_RESULT_GRAPHICS_API_ERROR: a CUDA call failed */
+    RGDN_INTERNAL_ERROR          = 6,  /* RG_RESULT_INTERNAL_ERROR */
+    RGDN_WRONG_FUNCTION_CALL     = 10, /* RG_RESULT_WRONG_FUNCTION_CALL */
+    RGDN_WRONG_FUNCTION_ARGUMENT = 11, /* RG_RESULT_WRONG_FUNCTION_ARGUMENT */
+    RGDN_OUT_OF_BUDGET           = 64, /* admission refused: the memory budget is exhausted */
+    RGDN_TIMEOUT                 = 65, /* a bounded host wait ran out */
+    RGDN_NOT_READY               = 66, /* asynchronous work still in flight */
+} rgdn_status;
+
+/* Storage precision of the denoiser's colour and history buffers.
+ * G-buffer inputs always keep the reference formats.
+ *   REF  — the reference formats exactly (E5B9G9R9 colour, rgba16f history, rg16f moments)
+ *          (Source/Generated/GenerateShaderCommon.py:802-887)
+ *   FP32 — fp32 colour / history / moments
+ *   FP16 — fp16 colour / history, fp32 moments and fp32 variance
+ *   BF16 — bf16 colour / history, fp32 moments and fp32 variance                   */
+typedef enum rgdn_storage
+{
+    RGDN_STORAGE_REF  = 0,
+    RGDN_STORAGE_FP32 = 1,
+    RGDN_STORAGE_FP16 = 2,
+    RGDN_STORAGE_BF16 = 3,
+} rgdn_storage;
+
+/* Element formats of framebuffer planes. */
+typedef enum rgdn_format
+{
+    RGDN_FORMAT_NONE = 0,
+    RGDN_FORMAT_R8_UINT,          /* 1 B */
+    RGDN_FORMAT_RG8_UNORM,        /* 2 B */
+    RGDN_FORMAT_RGBA8_UNORM,      /* 4 B */
+    RGDN_FORMAT_R16_SFLOAT,       /* 2 B */
+    RGDN_FORMAT_RG16_SFLOAT,      /* 4 B */
+    RGDN_FORMAT_RGBA16_SFLOAT,    /* 8 B */
+    RGDN_FORMAT_RGBA16_BFLOAT,    /* 8 B (bf16 x4) */
+    RGDN_FORMAT_R32_SFLOAT,       /* 4 B */
+    RGDN_FORMAT_RG32_SFLOAT,      /* 8 B */
+    RGDN_FORMAT_RGBA32_SFLOAT,    /* 16 B */
+    RGDN_FORMAT_R32_UINT,         /* 4 B */
+    RGDN_FORMAT_E5B9G9R9_UFLOAT,  /* 4 B, shared exponent (EXT_texture_shared_exponent) */
+    RGDN_FORMAT_B10G11R11_UFLOAT, /* 4 B */
+    RGDN_FORMAT_NORMAL_SPHERICAL, /* 4 B, (phi:16 | theta:16) code of Source/Shaders/Utils.h:105-140 */
+} rgdn_format;
+
+/* The framebuffer images of one stream. Names follow the reference's framebuffer
+ * table (GenerateShaderCommon.py:802-887). "prev" images (STORE_PREV there) have
+ * two physical planes; frameIndex selects the current one, frameIndex^1 is _Prev.
+ *
+ * Producer-written, current frame (the G-buffer; checkerboarded layout unless noted):   */
+typedef enum rgdn_framebuf
+{
+    RGDN_FB_ALBEDO = 0,               /* B10G11R11, regular (non-checkerboard) pixel layout */
+    RGDN_FB_IS_SKY,                   /* R8_UINT */
+    RGDN_FB_NORMAL,                   /* NORMAL_SPHERICAL, prev */
+    RGDN_FB_METALLIC_ROUGHNESS,       /* RG8_UNORM, prev */
+    RGDN_FB_DEPTH_WORLD,              /* R16_SFLOAT, prev */
+    RGDN_FB_DEPTH_GRAD,               /* R16_SFLOAT */
+    RGDN_FB_MOTION,                   /* RGBA16_SFLOAT: xy cur->prev screen uv, z linear depth delta */
+    RGDN_FB_UNFILTERED_DIRECT,        /* E5B9G9R9 */
+    RGDN_FB_UNFILTERED_SPECULAR,      /* E5B9G9R9 */
+    RGDN_FB_UNFILTERED_INDIR,         /* E5B9G9R9 */
+    RGDN_FB_SURFACE_POSITION,         /* RGBA32_SFLOAT, prev */
+    RGDN_FB_VIEW_DIRECTION,           /* RGBA16_SFLOAT: xyz ray direction, w hit distance */
+    RGDN_FB_THROUGHPUT,               /* RGBA16_SFLOAT */
+    RGDN_FB_GRADIENT_INPUTS,          /* RG16_SFLOAT: (lum diffuse, lum specular), prev */
+    RGDN_FB_GRADIENT_RESHADED,        /* RG32_SFLOAT: previous-frame surface re-shaded with this
+                                         frame's lights, indexed by previous-frame pixel
+                                         (RtGradients.rgen:107-136 "forwardProjectedLuminance") */
+    /* Outputs */
+    RGDN_FB_PRE_FINAL,                /* REF: B10G11R11; FP32: RGBA32F; FP16/BF16: RGBA16F; regular layout */
+    RGDN_FB_HISTOGRAM_INPUT,          /* R16_SFLOAT, regular layout */
+    /* Denoiser history and intermediates */
+    RGDN_FB_ACCUM_HISTORY_LENGTH,     /* prev */
+    RGDN_FB_DIFF_TEMPORARY,
+    RGDN_FB_DIFF_ACCUM_COLOR,         /* prev */
+    RGDN_FB_DIFF_ACCUM_MOMENTS,       /* prev */
+    RGDN_FB_DIFF_COLOR_HISTORY,
+    RGDN_FB_DIFF_PING_COLOR_AND_VARIANCE,
+    RGDN_FB_DIFF_PONG_COLOR_AND_VARIANCE,
+    RGDN_FB_SPEC_ACCUM_COLOR,         /* prev */
+    RGDN_FB_SPEC_PING_COLOR,
+    RGDN_FB_SPEC_PONG_COLOR,
+    RGDN_FB_INDIR_ACCUM,              /* prev */
+    RGDN_FB_INDIR_PING,
+    RGDN_FB_INDIR_PONG,
+    RGDN_FB_ATROUS_FILTERED_VARIANCE,
+    /* Gradient (A-SVGF) images at 1/3 resolution: ((W+1)/3) x ((H+1)/3) */
+    RGDN_FB_DIS_PING_GRADIENT,        /* RGBA8_UNORM */
+    RGDN_FB_DIS_PONG_GRADIENT,        /* RGBA8_UNORM */
+    RGDN_FB_DIS_GRADIENT_HISTORY,     /* RGBA8_UNORM, prev (double-buffered here; single in the
+                                         reference, where sampling reads it before a-trous writes) */
+    RGDN_FB_GRADIENT_PREV_PIX,        /* R8_UINT */
+    /* FP32 variance planes of the colour+variance images (FP16/BF16 storage only) */
+    RGDN_FB_DIFF_COLOR_HISTORY_VARIANCE,
+    RGDN_FB_DIFF_PING_VARIANCE,
+    RGDN_FB_DIFF_PONG_VARIANCE,
+    RGDN_FB_COUNT
+} rgdn_framebuf;
+
+/* One plane of one framebuffer image. */
+typedef struct rgdn_image
+{
+    void*    data;        /* device pointer (NULL if the image does not exist in this storage mode) */
+    uint32_t width;
+    uint32_t height;
+    uint32_t pitch_bytes; /* row stride */
+    uint32_t texel_bytes;
+    uint32_t format;      /* rgdn_format */
+    uint32_t has_prev;    /* 1 if the image is double-buffered by frameIndex */
+} rgdn_image;
+
+/* Per-frame parameters: the fields of ShGlobalUniform (ShaderCommonC.h:209-304)
+ * that this path reads, as VulkanDevice::FillUniform fills them
+ * (Source/VulkanDevice.cpp:142-300). Matrices are column-major float[16] like the
+ * reference's uniform. */
+typedef struct rgdn_frame_params
+{
+    float    view[ 16 ];
+    float    viewPrev[ 16 ];
+    float    projection[ 16 ];
+    float    projectionPrev[ 16 ];
+    float    cameraPosition[ 4 ];
+    float    cameraPositionPrev[ 4 ];
+    float    timeDelta;             /* seconds, >= 0.001 in the reference */
+    float    minLogLuminance;       /* log2(2^ev100Min * 12.5 / 100) */
+    float    maxLogLuminance;       /* log2(2^ev100Max * 12.5 / 100) */
+    uint32_t stopEyeAdaptation;
+    float    gradientMultDiffuse;   /* clamped to [0,1] by the caller, as FillUniform does */
+    float    gradientMultIndirect;
+    float    gradientMultSpecular;
+    uint32_t antiFireflyEnabled;
+    float    lightmapScreenCoverage;
+    uint32_t debugShowFlags;        /* DEBUG_SHOW_FLAG_* of ShaderCommonC.h */
+    uint32_t atrousIterations;      /* 0 or 4 = the reference's 4 iterations; 1..6 allowed */
+    uint32_t flags;                 /* RGDN_FLAG_* */
+} rgdn_frame_params;
+
+/* rgdn_frame_params.flags */
+#define RGDN_FLAG_PLAIN              0x1u /* one kernel per reference dispatch (no fusion) */
+#define RGDN_FLAG_SKIP_GRADIENTS     0x2u /* GRADIENT_ESTIMATION_ENABLED == 0 behaviour */
+
+/* debugShowFlags bits used on this path (ShaderCommonC.h:156-166) */
+#define RGDN_DEBUG_SHOW_FLAG_ONLY_DIRECT_DIFFUSE   ( 1u << 5 )
+#define RGDN_DEBUG_SHOW_FLAG_ONLY_SPECULAR         ( 1u << 6 )
+#define RGDN_DEBUG_SHOW_FLAG_ONLY_INDIRECT_DIFFUSE ( 1u << 7 )
+#define RGDN_DEBUG_SHOW_FLAG_ALBEDO_WHITE          ( 1u << 9 )
+
+/* Individual stages, for the plain path and per-stage checking. */
+typedef enum rgdn_stage
+{
+    RGDN_STAGE_GRADIENT_SAMPLES = 0,  /* RtGradients.rgen:44-181 (image-space part) */
+    RGDN_STAGE_GRADIENT_ATROUS,       /* CmASVGFGradientAtrous.comp, iteration 0..3 */
+    RGDN_STAGE_TEMPORAL_ACCUMULATION, /* CmSVGFTemporalAccumulation.comp */
+    RGDN_STAGE_ANTI_FIREFLY,          /* CmAntiFirefly.comp */
+    RGDN_STAGE_VARIANCE_ESTIMATION,   /* CmSVGFEstimateVariance.comp */
+    RGDN_STAGE_ATROUS,                /* CmSVGFAtrous_Iter0.comp (0) / CmSVGFAtrous.comp (>=1) */
+    RGDN_STAGE_LUMINANCE_HISTOGRAM,   /* CmLuminanceHistogram.comp */
+    RGDN_STAGE_LUMINANCE_AVG,         /* CmLuminanceAvg.comp */
+    RGDN_STAGE_COUNT
+} rgdn_stage;
+
+typedef struct CUstream_st* rgdn_cuda_stream; /* == cudaStream_t */
+
+typedef struct rgdn_context rgdn_context;
+typedef struct rgdn_stream  rgdn_stream;
+
+typedef struct rgdn_context_create_info
+{
+    int      device;               /* CUDA device ordinal */
+    uint64_t memoryBudgetBytes;    /* 0 = no budget; stream creation beyond it fails with OUT_OF_BUDGET */
+} rgdn_context_create_info;
+
+typedef struct rgdn_stream_create_info
+{
+    uint32_t width;                /* render width, must be even (VulkanDevice.cpp:186-188) */
+    uint32_t height;
+    uint32_t storage;              /* rgdn_storage */
+} rgdn_stream_create_info;
+
+/* ---- context ---------------------------------------------------------------------- */
+/* Replaces the Denoiser/Tonemapping constructors (Denoiser.cpp:28-55,
+ * Tonemapping.cpp:30-46): selects the device, builds the shared tables. */
+rgdn_status rgdn_context_create( const rgdn_context_create_info* info, rgdn_context** outCtx );
+rgdn_status rgdn_context_destroy( rgdn_context* ctx );
+/* Bytes held by all streams of the context. */
+rgdn_status rgdn_context_memory_used( rgdn_context* ctx, uint64_t* outBytes );
+
+/* ---- streams: one camera stream = one framebuffer set + history ------------------- */
+/* Framebuffers::PrepareForSize (Framebuffers.cpp:216-230) + Tonemapping buffer creation
+ * (Tonemapping.cpp:183-191). All images and the tonemapping state start at zero. */
+rgdn_status rgdn_stream_create( rgdn_context* ctx, const rgdn_stream_create_info* info, rgdn_stream** outStream );
+rgdn_status rgdn_stream_destroy( rgdn_stream* stream );
+/* Reallocates every image at the new size (history is lost, as on a reference resize). */
+rgdn_status rgdn_stream_resize( rgdn_stream* stream, uint32_t width, uint32_t height );
+/* Bytes a stream of this size and storage needs (for admission control). */
+rgdn_status rgdn_stream_required_bytes( const rgdn_stream_create_info* info, uint64_t* outBytes );
+/* Framebuffers::GetImageHandles (Framebuffers.cpp:34-49): the plane of `fb` that
+ * frameIndex (0 or 1) selects. A producer writes the G-buffer there directly. */
+rgdn_status rgdn_stream_get_framebuffer( rgdn_stream* stream, uint32_t fb, uint32_t frameIndex, rgdn_image* outImage );
+/* Copies `bytes` (== pitch*height) into / out of a framebuffer plane; `src`/`dst` may be
+ * host (pageable or pinned) or device memory. Enqueued on cudaStream. */
+rgdn_status rgdn_stream_upload( rgdn_stream* stream, uint32_t fb, uint32_t frameIndex, const void* src, size_t bytes, rgdn_cuda_stream cudaStream );
+rgdn_status rgdn_stream_download( rgdn_stream* stream, uint32_t fb, uint32_t frameIndex, void* dst, size_t bytes, rgdn_cuda_stream cudaStream );
+
+/* ---- the hot path ----------------------------------------------------------------- */
+/* Denoiser::Denoise (Denoiser.cpp:64-255) preceded by the image-space gradient sampling
+ * of RtGradients.rgen: gradient samples, 4x gradient a-trous, temporal accumulation,
+ * anti-firefly, variance, N x a-trous with the final composition into PRE_FINAL and
+ * HISTOGRAM_INPUT. Asynchronous on cudaStream. */
+rgdn_status rgdn_denoise( rgdn_stream* stream, uint32_t frameIndex, const rgdn_frame_params* params, rgdn_cuda_stream cudaStream );
+/* Tonemapping::CalculateExposure (Tonemapping.cpp:59-165): 256-bin log-luminance
+ * histogram of HISTOGRAM_INPUT, then the adapted average luminance. */
+rgdn_status rgdn_calculate_exposure( rgdn_stream* stream, uint32_t frameIndex, const rgdn_frame_params* params, rgdn_cuda_stream cudaStream );
+/* One stage alone (the plain path / per-stage checking). `iteration` selects the
+ * a-trous or gradient a-trous iteration. */
+rgdn_status rgdn_denoise_stage( rgdn_stream* stream, uint32_t stage, uint32_t iteration, uint32_t frameIndex, const rgdn_frame_params* params, rgdn_cuda_stream cudaStream );
+
+/* ShTonemapping { uint histogram[256]; float avgLuminance; } (ShaderCommonC.h:344-348):
+ * device address (what Tonemapping::GetDescSet exposes to later passes). */
+rgdn_status rgdn_stream_tonemapping_device( rgdn_stream* stream, void** outDevicePtr );
+/* Synchronous read of the tonemapping state after the work on cudaStream. `exposure`
+ * is ev100ToLuminousExposure(getAutoEV100()) of Exposure.h:33-51. Any out pointer may be NULL. */
+rgdn_status rgdn_get_tonemapping( rgdn_stream* stream, uint32_t* outHistogram256, float* outAvgLuminance, float* outExposure, rgdn_cuda_stream cudaStream );
+/* Overwrites the tonemapping state (test fixtures, stream migration). */
+rgdn_status rgdn_set_tonemapping( rgdn_stream* stream, const uint32_t* histogram256, float avgLuminance, rgdn_cuda_stream cudaStream );
+
+/* ---- batching ---------------------------------------------------------------------- */
+typedef struct rgdn_job
+{
+    rgdn_stream*             stream;
+    uint32_t                 frameIndex;
+    const rgdn_frame_params* params;
+} rgdn_job;
+/* rgdn_denoise + rgdn_calculate_exposure for n frames of (possibly) different streams
+ * and sizes, with one launch per stage covering all of them. Streams of one batch must
+ * be distinct and share one storage mode. */
+rgdn_status rgdn_submit_batch( rgdn_context* ctx, const rgdn_job* jobs, uint32_t n, rgdn_cuda_stream cudaStream );
+
+/* ---- misc -------------------------------------------------------------------------- */
+/* getColorBin (CmLuminanceHistogram.comp:41-54) for every fp16 bit pattern of the
+ * HistogramInput image: out[h] = bin of the fp16 value with bits h. This is the table the
+ * GPU histogram indexes; exported so a caller can bin HistogramInput texels identically. */
+rgdn_status rgdn_histogram_bin_table( float minLogLuminance, float maxLogLuminance, uint8_t* out65536 );
+const char* rgdn_status_string( rgdn_status status );
+/* Number of kernels this library launched since the context was created (all streams). */
+rgdn_status rgdn_context_launch_count( rgdn_context* ctx, uint64_t* outCount );
+uint32_t    rgdn_api_version( void );
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* RGDN_H_ */

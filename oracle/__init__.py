@@ -1,0 +1,190 @@
+"""CPU ORACLE — test infrastructure only (see rgdn_oracle.cpp's header).
+
+Python binding of ``librgdn_oracle.so``, the C++ restatement of RayTracedGL1's denoise and
+auto-exposure shaders. Only ``tests/``, ``__graft_entry__.smoke()`` and ``bench.py``'s CPU
+baseline / reference arm import this module, as the checker; the product never does.
+
+Parity status: unpinned against the reference itself (its GLSL path cannot run here and its
+tests hold no golden vectors); the codecs are pinned by spec known-answer tests.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "librgdn_oracle.so")
+
+MODE_REF, MODE_F32, MODE_F16, MODE_BF16, MODE_F64 = 0, 1, 2, 3, 4
+
+# oracle-only FP64 formats, and the numpy view of every format
+_NUMPY = {
+    1: (np.uint8, 1), 2: (np.uint8, 2), 3: (np.uint8, 4), 4: (np.uint16, 1), 5: (np.uint16, 2),
+    6: (np.uint16, 4), 7: (np.uint16, 4), 8: (np.float32, 1), 9: (np.float32, 2), 10: (np.float32, 4),
+    11: (np.uint32, 1), 12: (np.uint32, 1), 13: (np.uint32, 1), 14: (np.uint32, 1),
+    100: (np.float64, 1), 101: (np.float64, 2), 102: (np.float64, 4),
+}
+
+_lib = None
+
+
+def load():
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise ImportError(f"{LIB_PATH} missing: build it with `python -m raytracedgl1_gb300.build`")
+    from raytracedgl1_gb300._native import FrameParams
+    lib = C.CDLL(LIB_PATH)
+    P = C.POINTER
+    sig = {
+        "orc_stream_create": (C.c_void_p, [C.c_uint32, C.c_uint32, C.c_uint32]),
+        "orc_stream_destroy": (None, [C.c_void_p]),
+        "orc_stream_plane": (C.c_void_p, [C.c_void_p, C.c_uint32, C.c_uint32, P(C.c_uint32), P(C.c_uint32),
+                                          P(C.c_uint32), P(C.c_uint32)]),
+        "orc_stream_grad_width": (C.c_uint32, [C.c_void_p]),
+        "orc_stream_grad_height": (C.c_uint32, [C.c_void_p]),
+        "orc_stage": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint32, P(FrameParams), C.c_int]),
+        "orc_denoise": (C.c_int, [C.c_void_p, C.c_uint32, P(FrameParams), C.c_int]),
+        "orc_calculate_exposure": (C.c_int, [C.c_void_p, C.c_uint32, P(FrameParams), C.c_int]),
+        "orc_exposure_from_avg": (C.c_float, [C.c_float]),
+        "orc_get_tonemapping": (None, [C.c_void_p, P(C.c_uint32), P(C.c_float), P(C.c_double)]),
+        "orc_set_tonemapping": (None, [C.c_void_p, P(C.c_uint32), C.c_float]),
+        "orc_f32_to_f16": (C.c_uint16, [C.c_float]),
+        "orc_f16_to_f32": (C.c_float, [C.c_uint16]),
+        "orc_f32_to_bf16": (C.c_uint16, [C.c_float]),
+        "orc_bf16_to_f32": (C.c_float, [C.c_uint16]),
+        "orc_encode_e5": (C.c_uint32, [C.c_float, C.c_float, C.c_float]),
+        "orc_decode_e5": (None, [C.c_uint32, P(C.c_float)]),
+        "orc_encode_b10g11r11": (C.c_uint32, [C.c_float, C.c_float, C.c_float]),
+        "orc_decode_b10g11r11": (None, [C.c_uint32, P(C.c_float)]),
+        "orc_encode_normal": (C.c_uint32, [C.c_float, C.c_float, C.c_float]),
+        "orc_decode_normal": (None, [C.c_uint32, P(C.c_float)]),
+        "orc_color_bin": (C.c_uint32, [C.c_float, C.c_float, C.c_float]),
+        "orc_unorm8": (C.c_uint8, [C.c_float]),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def nthreads_default() -> int:
+    return max(1, os.cpu_count() or 1)
+
+
+class OracleStream:
+    """CPU twin of a librgdn stream: same framebuffer table, same byte layouts (modes 0-3)."""
+
+    def __init__(self, width: int, height: int, mode: int = MODE_REF):
+        self.lib = load()
+        self.h = self.lib.orc_stream_create(width, height, mode)
+        if not self.h:
+            raise ValueError("bad oracle stream size / mode")
+        self.width, self.height, self.mode = width, height, mode
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            self.lib.orc_stream_destroy(self.h)
+            self.h = None
+
+    def plane(self, fb, frame_index: int = 0) -> np.ndarray | None:
+        """Zero-copy numpy view of a plane (writes go into the oracle's state)."""
+        from raytracedgl1_gb300._native import FB
+        fbi = FB[fb] if isinstance(fb, str) else fb
+        w, h, t, f = C.c_uint32(), C.c_uint32(), C.c_uint32(), C.c_uint32()
+        p = self.lib.orc_stream_plane(self.h, fbi, frame_index, C.byref(w), C.byref(h), C.byref(t), C.byref(f))
+        if not p:
+            return None
+        dt, ch = _NUMPY[f.value]
+        n = w.value * h.value * ch
+        arr = np.ctypeslib.as_array(C.cast(p, C.POINTER(np.ctypeslib.as_ctypes_type(dt))), shape=(n,))
+        return arr.reshape((h.value, w.value) if ch == 1 else (h.value, w.value, ch))
+
+    def fmt(self, fb) -> int:
+        from raytracedgl1_gb300._native import FB
+        fbi = FB[fb] if isinstance(fb, str) else fb
+        w, h, t, f = C.c_uint32(), C.c_uint32(), C.c_uint32(), C.c_uint32()
+        self.lib.orc_stream_plane(self.h, fbi, 0, C.byref(w), C.byref(h), C.byref(t), C.byref(f))
+        return f.value
+
+    def load(self, fb, frame_index: int, data: np.ndarray) -> None:
+        dst = self.plane(fb, frame_index)
+        dst[...] = data.reshape(dst.shape).view(dst.dtype) if data.dtype != dst.dtype else data.reshape(dst.shape)
+
+    def stage(self, stage: int, iteration: int, frame_index: int, params, nthreads: int = 0) -> None:
+        r = self.lib.orc_stage(self.h, stage, iteration, frame_index, C.byref(params), nthreads or nthreads_default())
+        if r != 0:
+            raise RuntimeError(f"orc_stage failed: {r}")
+
+    def denoise(self, frame_index: int, params, nthreads: int = 0) -> None:
+        r = self.lib.orc_denoise(self.h, frame_index, C.byref(params), nthreads or nthreads_default())
+        if r != 0:
+            raise RuntimeError(f"orc_denoise failed: {r}")
+
+    def calculate_exposure(self, frame_index: int, params, nthreads: int = 0) -> None:
+        r = self.lib.orc_calculate_exposure(self.h, frame_index, C.byref(params), nthreads or nthreads_default())
+        if r != 0:
+            raise RuntimeError(f"orc_calculate_exposure failed: {r}")
+
+    def tonemapping(self):
+        hist = (C.c_uint32 * 256)()
+        avg = C.c_float()
+        avg64 = C.c_double()
+        self.lib.orc_get_tonemapping(self.h, hist, C.byref(avg), C.byref(avg64))
+        return np.frombuffer(hist, dtype=np.uint32).copy(), avg.value, self.lib.orc_exposure_from_avg(avg.value)
+
+    def set_tonemapping(self, hist, avg: float) -> None:
+        h = (C.c_uint32 * 256)(*[int(x) for x in hist]) if hist is not None else None
+        self.lib.orc_set_tonemapping(self.h, h, C.c_float(avg))
+
+
+# --- codecs for the known-answer tests ---------------------------------------------------
+def encode_e5(r, g, b) -> int:
+    return load().orc_encode_e5(r, g, b)
+
+
+def decode_e5(p: int):
+    out = (C.c_float * 3)()
+    load().orc_decode_e5(p, out)
+    return tuple(out)
+
+
+def encode_b10g11r11(r, g, b) -> int:
+    return load().orc_encode_b10g11r11(r, g, b)
+
+
+def decode_b10g11r11(p: int):
+    out = (C.c_float * 3)()
+    load().orc_decode_b10g11r11(p, out)
+    return tuple(out)
+
+
+def f32_to_f16(x: float) -> int:
+    return load().orc_f32_to_f16(x)
+
+
+def f16_to_f32(h: int) -> float:
+    return load().orc_f16_to_f32(h)
+
+
+def f32_to_bf16(x: float) -> int:
+    return load().orc_f32_to_bf16(x)
+
+
+def encode_normal(x, y, z) -> int:
+    return load().orc_encode_normal(x, y, z)
+
+
+def decode_normal(p: int):
+    out = (C.c_float * 3)()
+    load().orc_decode_normal(p, out)
+    return tuple(out)
+
+
+def color_bin(lum: float, min_log: float, max_log: float) -> int:
+    return load().orc_color_bin(lum, min_log, max_log)

@@ -1,0 +1,145 @@
+"""ctypes binding of ``include/rgdn.h`` (librgdn.so). Loading fails loudly when the library
+is missing: there is no Python or CPU fallback for any compute entry point."""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG, "lib", "librgdn.so")
+
+# ---- enums (values from include/rgdn.h) -------------------------------------------------
+SUCCESS, WRONG_INSTANCE, DEVICE_ERROR, INTERNAL_ERROR = 0, 3, 5, 6
+WRONG_FUNCTION_CALL, WRONG_FUNCTION_ARGUMENT = 10, 11
+OUT_OF_BUDGET, TIMEOUT, NOT_READY = 64, 65, 66
+
+STORAGE_REF, STORAGE_FP32, STORAGE_FP16, STORAGE_BF16 = 0, 1, 2, 3
+STORAGE_NAMES = {"ref": STORAGE_REF, "fp32": STORAGE_FP32, "fp16": STORAGE_FP16, "bf16": STORAGE_BF16}
+
+FORMAT_NAMES = [
+    "NONE", "R8_UINT", "RG8_UNORM", "RGBA8_UNORM", "R16_SFLOAT", "RG16_SFLOAT", "RGBA16_SFLOAT",
+    "RGBA16_BFLOAT", "R32_SFLOAT", "RG32_SFLOAT", "RGBA32_SFLOAT", "R32_UINT", "E5B9G9R9_UFLOAT",
+    "B10G11R11_UFLOAT", "NORMAL_SPHERICAL",
+]
+
+FB_NAMES = [
+    "ALBEDO", "IS_SKY", "NORMAL", "METALLIC_ROUGHNESS", "DEPTH_WORLD", "DEPTH_GRAD", "MOTION",
+    "UNFILTERED_DIRECT", "UNFILTERED_SPECULAR", "UNFILTERED_INDIR", "SURFACE_POSITION",
+    "VIEW_DIRECTION", "THROUGHPUT", "GRADIENT_INPUTS", "GRADIENT_RESHADED", "PRE_FINAL",
+    "HISTOGRAM_INPUT", "ACCUM_HISTORY_LENGTH", "DIFF_TEMPORARY", "DIFF_ACCUM_COLOR",
+    "DIFF_ACCUM_MOMENTS", "DIFF_COLOR_HISTORY", "DIFF_PING_COLOR_AND_VARIANCE",
+    "DIFF_PONG_COLOR_AND_VARIANCE", "SPEC_ACCUM_COLOR", "SPEC_PING_COLOR", "SPEC_PONG_COLOR",
+    "INDIR_ACCUM", "INDIR_PING", "INDIR_PONG", "ATROUS_FILTERED_VARIANCE", "DIS_PING_GRADIENT",
+    "DIS_PONG_GRADIENT", "DIS_GRADIENT_HISTORY", "GRADIENT_PREV_PIX",
+    "DIFF_COLOR_HISTORY_VARIANCE", "DIFF_PING_VARIANCE", "DIFF_PONG_VARIANCE",
+]
+FB = {n: i for i, n in enumerate(FB_NAMES)}
+FB_COUNT = len(FB_NAMES)
+
+# G-buffer images a producer writes every frame
+GBUFFER = ["ALBEDO", "IS_SKY", "NORMAL", "METALLIC_ROUGHNESS", "DEPTH_WORLD", "DEPTH_GRAD", "MOTION",
+           "UNFILTERED_DIRECT", "UNFILTERED_SPECULAR", "UNFILTERED_INDIR", "SURFACE_POSITION",
+           "VIEW_DIRECTION", "THROUGHPUT", "GRADIENT_INPUTS", "GRADIENT_RESHADED"]
+
+STAGE_GRADIENT_SAMPLES, STAGE_GRADIENT_ATROUS, STAGE_TEMPORAL_ACCUMULATION = 0, 1, 2
+STAGE_ANTI_FIREFLY, STAGE_VARIANCE_ESTIMATION, STAGE_ATROUS = 3, 4, 5
+STAGE_LUMINANCE_HISTOGRAM, STAGE_LUMINANCE_AVG = 6, 7
+
+FLAG_PLAIN, FLAG_SKIP_GRADIENTS = 0x1, 0x2
+
+
+class FrameParams(C.Structure):
+    """rgdn_frame_params: the ShGlobalUniform fields this path reads."""
+    _fields_ = [
+        ("view", C.c_float * 16), ("viewPrev", C.c_float * 16),
+        ("projection", C.c_float * 16), ("projectionPrev", C.c_float * 16),
+        ("cameraPosition", C.c_float * 4), ("cameraPositionPrev", C.c_float * 4),
+        ("timeDelta", C.c_float), ("minLogLuminance", C.c_float), ("maxLogLuminance", C.c_float),
+        ("stopEyeAdaptation", C.c_uint32),
+        ("gradientMultDiffuse", C.c_float), ("gradientMultIndirect", C.c_float),
+        ("gradientMultSpecular", C.c_float), ("antiFireflyEnabled", C.c_uint32),
+        ("lightmapScreenCoverage", C.c_float), ("debugShowFlags", C.c_uint32),
+        ("atrousIterations", C.c_uint32), ("flags", C.c_uint32),
+    ]
+
+    def copy(self) -> "FrameParams":
+        p = FrameParams()
+        C.memmove(C.byref(p), C.byref(self), C.sizeof(FrameParams))
+        return p
+
+
+class Image(C.Structure):
+    _fields_ = [("data", C.c_void_p), ("width", C.c_uint32), ("height", C.c_uint32),
+                ("pitch_bytes", C.c_uint32), ("texel_bytes", C.c_uint32), ("format", C.c_uint32),
+                ("has_prev", C.c_uint32)]
+
+
+class ContextCreateInfo(C.Structure):
+    _fields_ = [("device", C.c_int), ("memoryBudgetBytes", C.c_uint64)]
+
+
+class StreamCreateInfo(C.Structure):
+    _fields_ = [("width", C.c_uint32), ("height", C.c_uint32), ("storage", C.c_uint32)]
+
+
+class Job(C.Structure):
+    _fields_ = [("stream", C.c_void_p), ("frameIndex", C.c_uint32), ("params", C.POINTER(FrameParams))]
+
+
+# (name, restype, argtypes) of every entry point declared in include/rgdn.h
+_VP, _U32, _U64, _SZ, _I = C.c_void_p, C.c_uint32, C.c_uint64, C.c_size_t, C.c_int
+_PFP = C.POINTER(FrameParams)
+SIGNATURES = [
+    ("rgdn_context_create", _I, [C.POINTER(ContextCreateInfo), C.POINTER(_VP)]),
+    ("rgdn_context_destroy", _I, [_VP]),
+    ("rgdn_context_memory_used", _I, [_VP, C.POINTER(_U64)]),
+    ("rgdn_stream_create", _I, [_VP, C.POINTER(StreamCreateInfo), C.POINTER(_VP)]),
+    ("rgdn_stream_destroy", _I, [_VP]),
+    ("rgdn_stream_resize", _I, [_VP, _U32, _U32]),
+    ("rgdn_stream_required_bytes", _I, [C.POINTER(StreamCreateInfo), C.POINTER(_U64)]),
+    ("rgdn_stream_get_framebuffer", _I, [_VP, _U32, _U32, C.POINTER(Image)]),
+    ("rgdn_stream_upload", _I, [_VP, _U32, _U32, _VP, _SZ, _VP]),
+    ("rgdn_stream_download", _I, [_VP, _U32, _U32, _VP, _SZ, _VP]),
+    ("rgdn_denoise", _I, [_VP, _U32, _PFP, _VP]),
+    ("rgdn_calculate_exposure", _I, [_VP, _U32, _PFP, _VP]),
+    ("rgdn_denoise_stage", _I, [_VP, _U32, _U32, _U32, _PFP, _VP]),
+    ("rgdn_stream_tonemapping_device", _I, [_VP, C.POINTER(_VP)]),
+    ("rgdn_get_tonemapping", _I, [_VP, C.POINTER(_U32), C.POINTER(C.c_float), C.POINTER(C.c_float), _VP]),
+    ("rgdn_set_tonemapping", _I, [_VP, C.POINTER(_U32), C.c_float, _VP]),
+    ("rgdn_submit_batch", _I, [_VP, C.POINTER(Job), _U32, _VP]),
+    ("rgdn_status_string", C.c_char_p, [_I]),
+    ("rgdn_context_launch_count", _I, [_VP, C.POINTER(_U64)]),
+    ("rgdn_api_version", _U32, []),
+    ("rgdn_histogram_bin_table", _I, [C.c_float, C.c_float, C.POINTER(C.c_uint8)]),
+]
+
+_lib = None
+
+
+def load() -> C.CDLL:
+    """Loads librgdn.so; raises if it was not built (run raytracedgl1_gb300.build)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise ImportError(f"{LIB_PATH} is missing: build it with `python -m raytracedgl1_gb300.build` "
+                          "(the denoiser has no fallback without its CUDA library)")
+    lib = C.CDLL(LIB_PATH)
+    for name, res, args in SIGNATURES:
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+class RgdnError(RuntimeError):
+    def __init__(self, status: int, what: str = ""):
+        self.status = status
+        msg = load().rgdn_status_string(status).decode()
+        super().__init__(f"{what}: {msg} (status {status})" if what else f"{msg} (status {status})")
+
+
+def check(status: int, what: str = "") -> None:
+    if status != SUCCESS:
+        raise RgdnError(status, what)

@@ -1,0 +1,720 @@
+// C ABI of the denoise-and-expose path (include/rgdn.h): contexts, streams (one framebuffer
+// set + history + tonemapping state each), stage sequencing and the tonemapping read-back.
+//
+// Host-side counterparts in the reference:
+//   Denoiser::Denoise            Source/Denoiser.cpp:64-255 (stage order, iteration routing)
+//   Tonemapping::CalculateExposure  Source/Tonemapping.cpp:59-165
+//   Framebuffers                 Source/Framebuffers.cpp:34-49 (cur/_Prev by frameIndex),
+//                                :640-699 (sizes, FORCE_SIZE_1_3 = (W+1)/3)
+//   RgResult / Call<> wrapper    Source/RTGL1.cpp:145-195 (no exceptions cross the ABI)
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <new>
+#include <set>
+#include <vector>
+
+#include "rgdn_codec.h"
+#include "rgdn_internal.h"
+
+using namespace rgdn;
+
+namespace
+{
+
+struct FbDesc
+{
+    uint32_t format;
+    bool     prev;
+    bool     third;
+};
+
+uint32_t format_bytes( uint32_t f )
+{
+    switch( f )
+    {
+        case RGDN_FORMAT_R8_UINT: return 1;
+        case RGDN_FORMAT_RG8_UNORM: case RGDN_FORMAT_R16_SFLOAT: return 2;
+        case RGDN_FORMAT_RGBA8_UNORM: case RGDN_FORMAT_RG16_SFLOAT: case RGDN_FORMAT_R32_SFLOAT:
+        case RGDN_FORMAT_R32_UINT: case RGDN_FORMAT_E5B9G9R9_UFLOAT: case RGDN_FORMAT_B10G11R11_UFLOAT:
+        case RGDN_FORMAT_NORMAL_SPHERICAL: return 4;
+        case RGDN_FORMAT_RGBA16_SFLOAT: case RGDN_FORMAT_RGBA16_BFLOAT: case RGDN_FORMAT_RG32_SFLOAT: return 8;
+        case RGDN_FORMAT_RGBA32_SFLOAT: return 16;
+        default: return 0;
+    }
+}
+
+// Formats of every image per storage mode. REF is the reference's table
+// (GenerateShaderCommon.py:802-887); the other modes change only colour / history images.
+FbDesc fb_desc( uint32_t fb, uint32_t storage )
+{
+    const uint32_t col3 = storage == RGDN_STORAGE_REF ? RGDN_FORMAT_E5B9G9R9_UFLOAT
+                        : storage == RGDN_STORAGE_FP32 ? RGDN_FORMAT_RGBA32_SFLOAT
+                        : storage == RGDN_STORAGE_FP16 ? RGDN_FORMAT_RGBA16_SFLOAT
+                                                       : RGDN_FORMAT_RGBA16_BFLOAT;
+    const uint32_t colvar = storage == RGDN_STORAGE_REF ? RGDN_FORMAT_RGBA16_SFLOAT : col3;
+    const uint32_t mom    = storage == RGDN_STORAGE_REF ? RGDN_FORMAT_RG16_SFLOAT : RGDN_FORMAT_RG32_SFLOAT;
+    const uint32_t fvar   = storage == RGDN_STORAGE_REF ? RGDN_FORMAT_R16_SFLOAT : RGDN_FORMAT_R32_SFLOAT;
+    const uint32_t pre    = storage == RGDN_STORAGE_REF ? RGDN_FORMAT_B10G11R11_UFLOAT
+                          : storage == RGDN_STORAGE_FP32 ? RGDN_FORMAT_RGBA32_SFLOAT
+                                                         : RGDN_FORMAT_RGBA16_SFLOAT;
+    const uint32_t varpl  = ( storage == RGDN_STORAGE_FP16 || storage == RGDN_STORAGE_BF16 ) ? RGDN_FORMAT_R32_SFLOAT : RGDN_FORMAT_NONE;
+    switch( fb )
+    {
+        case RGDN_FB_ALBEDO: return { RGDN_FORMAT_B10G11R11_UFLOAT, false, false };
+        case RGDN_FB_IS_SKY: return { RGDN_FORMAT_R8_UINT, false, false };
+        case RGDN_FB_NORMAL: return { RGDN_FORMAT_NORMAL_SPHERICAL, true, false };
+        case RGDN_FB_METALLIC_ROUGHNESS: return { RGDN_FORMAT_RG8_UNORM, true, false };
+        case RGDN_FB_DEPTH_WORLD: return { RGDN_FORMAT_R16_SFLOAT, true, false };
+        case RGDN_FB_DEPTH_GRAD: return { RGDN_FORMAT_R16_SFLOAT, false, false };
+        case RGDN_FB_MOTION: return { RGDN_FORMAT_RGBA16_SFLOAT, false, false };
+        case RGDN_FB_UNFILTERED_DIRECT:
+        case RGDN_FB_UNFILTERED_SPECULAR:
+        case RGDN_FB_UNFILTERED_INDIR: return { RGDN_FORMAT_E5B9G9R9_UFLOAT, false, false };
+        case RGDN_FB_SURFACE_POSITION: return { RGDN_FORMAT_RGBA32_SFLOAT, true, false };
+        case RGDN_FB_VIEW_DIRECTION: return { RGDN_FORMAT_RGBA16_SFLOAT, false, false };
+        case RGDN_FB_THROUGHPUT: return { RGDN_FORMAT_RGBA16_SFLOAT, false, false };
+        case RGDN_FB_GRADIENT_INPUTS: return { RGDN_FORMAT_RG16_SFLOAT, true, false };
+        case RGDN_FB_GRADIENT_RESHADED: return { RGDN_FORMAT_RG32_SFLOAT, false, false };
+        case RGDN_FB_PRE_FINAL: return { pre, false, false };
+        case RGDN_FB_HISTOGRAM_INPUT: return { RGDN_FORMAT_R16_SFLOAT, false, false };
+        case RGDN_FB_ACCUM_HISTORY_LENGTH: return { colvar, true, false };
+        case RGDN_FB_DIFF_TEMPORARY: return { col3, false, false };
+        case RGDN_FB_DIFF_ACCUM_COLOR: return { col3, true, false };
+        case RGDN_FB_DIFF_ACCUM_MOMENTS: return { mom, true, false };
+        case RGDN_FB_DIFF_COLOR_HISTORY:
+        case RGDN_FB_DIFF_PING_COLOR_AND_VARIANCE:
+        case RGDN_FB_DIFF_PONG_COLOR_AND_VARIANCE: return { colvar, false, false };
+        case RGDN_FB_SPEC_ACCUM_COLOR: return { col3, true, false };
+        case RGDN_FB_SPEC_PING_COLOR:
+        case RGDN_FB_SPEC_PONG_COLOR: return { col3, false, false };
+        case RGDN_FB_INDIR_ACCUM: return { col3, true, false };
+        case RGDN_FB_INDIR_PING:
+        case RGDN_FB_INDIR_PONG: return { col3, false, false };
+        case RGDN_FB_ATROUS_FILTERED_VARIANCE: return { fvar, false, false };
+        case RGDN_FB_DIS_PING_GRADIENT:
+        case RGDN_FB_DIS_PONG_GRADIENT: return { RGDN_FORMAT_RGBA8_UNORM, false, true };
+        case RGDN_FB_DIS_GRADIENT_HISTORY: return { RGDN_FORMAT_RGBA8_UNORM, true, true };
+        case RGDN_FB_GRADIENT_PREV_PIX: return { RGDN_FORMAT_R8_UINT, false, true };
+        case RGDN_FB_DIFF_COLOR_HISTORY_VARIANCE:
+        case RGDN_FB_DIFF_PING_VARIANCE:
+        case RGDN_FB_DIFF_PONG_VARIANCE: return { varpl, false, false };
+        default: return { RGDN_FORMAT_NONE, false, false };
+    }
+}
+
+constexpr size_t kAlign = 256;
+inline size_t align_up( size_t v ) { return ( v + kAlign - 1 ) & ~( kAlign - 1 ); }
+
+StageLauncher launcher_for( uint32_t storage )
+{
+    switch( storage )
+    {
+        case RGDN_STORAGE_REF: return launch_stage_ref;
+        case RGDN_STORAGE_FP32: return launch_stage_f32;
+        case RGDN_STORAGE_FP16: return launch_stage_f16;
+        case RGDN_STORAGE_BF16: return launch_stage_bf16;
+        default: return nullptr;
+    }
+}
+
+// getColorBin of CmLuminanceHistogram.comp:41-54, evaluated on the host in FP32 for every
+// fp16 bit pattern; the GPU histogram indexes this table with the fp16 bits it bins.
+void build_bin_lut( uint8_t* lut, float minLog, float maxLog )
+{
+    const float inv = 1.0f / ( maxLog - minLog );
+    for( uint32_t h = 0; h < 65536u; h++ )
+    {
+        const float lum = rgdn::f16_to_f32( (uint16_t)h );
+        uint32_t    bin;
+        if( lum < 0.001f ) bin = 0;
+        else
+        {
+            const float ll = fminf( fmaxf( ( log2f( lum ) - minLog ) * inv, 0.0f ), 1.0f );
+            bin            = (uint32_t)( ll * 254.0f + 1.0f );
+        }
+        lut[ h ] = (uint8_t)bin;
+    }
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------------------------------
+// handles
+// ------------------------------------------------------------------------------------------
+struct rgdn_context
+{
+    int                     device = 0;
+    uint64_t                budget = 0;
+    uint64_t                used   = 0;
+    std::mutex              mtx;
+    std::set< rgdn_stream* > streams;
+    float2*                 phiTab   = nullptr;   // (sin phi_j, cos phi_j)
+    float2*                 thetaTab = nullptr;   // (cos theta_k, sin theta_k)
+    std::atomic< uint64_t > launches{ 0 };
+    uint32_t                magic = 0x52474443u;
+};
+
+struct PlaneSlot
+{
+    uint8_t* ptr[ 2 ] = { nullptr, nullptr };
+    uint32_t w = 0, h = 0, texel = 0, format = 0;
+    bool     prev = false;
+};
+
+struct rgdn_stream
+{
+    rgdn_context*          ctx = nullptr;
+    uint32_t               W = 0, H = 0, GW = 0, GH = 0, storage = 0;
+    void*                  block = nullptr;
+    size_t                 bytes = 0;
+    PlaneSlot              planes[ RGDN_FB_COUNT ];
+    Tonemapping*           tm     = nullptr;
+    uint8_t*               binLut = nullptr;
+    float                  lutMin = NAN, lutMax = NAN;
+    std::vector< uint8_t > hostLut;
+    uint32_t               magic = 0x52474453u;
+};
+
+namespace
+{
+
+bool valid_ctx( rgdn_context* c ) { return c && c->magic == 0x52474443u; }
+bool valid_stream( rgdn_stream* s ) { return s && s->magic == 0x52474453u && valid_ctx( s->ctx ); }
+
+rgdn_status cuda_status( cudaError_t e ) { return e == cudaSuccess ? RGDN_SUCCESS : RGDN_DEVICE_ERROR; }
+
+// bytes of one stream's single device block
+size_t stream_layout( uint32_t W, uint32_t H, uint32_t storage, PlaneSlot* planes, uint8_t* base )
+{
+    const uint32_t GW = std::max( 1u, ( W + 1 ) / 3 ), GH = std::max( 1u, ( H + 1 ) / 3 );
+    size_t off = 0;
+    // tonemapping state + histogram bin table first
+    off += align_up( sizeof( Tonemapping ) );
+    off += align_up( 65536 );
+    for( uint32_t fb = 0; fb < RGDN_FB_COUNT; fb++ )
+    {
+        FbDesc   d     = fb_desc( fb, storage );
+        uint32_t texel = format_bytes( d.format );
+        if( planes ) planes[ fb ] = PlaneSlot();
+        if( d.format == RGDN_FORMAT_NONE ) continue;
+        uint32_t w = d.third ? GW : W, h = d.third ? GH : H;
+        size_t   sz = (size_t)w * h * texel;
+        for( int s = 0; s < ( d.prev ? 2 : 1 ); s++ )
+        {
+            if( planes ) planes[ fb ].ptr[ s ] = base ? base + off : nullptr;
+            off += align_up( sz );
+        }
+        if( planes )
+        {
+            planes[ fb ].w = w; planes[ fb ].h = h; planes[ fb ].texel = texel;
+            planes[ fb ].format = d.format; planes[ fb ].prev = d.prev;
+        }
+    }
+    return off;
+}
+
+const uint8_t* plane_ptr( const rgdn_stream* s, uint32_t fb, uint32_t fi )
+{
+    const PlaneSlot& p = s->planes[ fb ];
+    return p.prev ? p.ptr[ fi & 1 ] : p.ptr[ 0 ];
+}
+uint8_t* plane_ptr_mut( rgdn_stream* s, uint32_t fb, uint32_t fi )
+{
+    PlaneSlot& p = s->planes[ fb ];
+    return p.prev ? p.ptr[ fi & 1 ] : p.ptr[ 0 ];
+}
+
+rgdn_status check_params( const rgdn_frame_params* p )
+{
+    if( !p ) return RGDN_WRONG_FUNCTION_ARGUMENT;
+    uint32_t n = p->atrousIterations == 0 ? 4u : p->atrousIterations;
+    if( n < 1 || n > (uint32_t)MAX_ATROUS_ITERATIONS ) return RGDN_WRONG_FUNCTION_ARGUMENT;
+    if( !( p->maxLogLuminance > p->minLogLuminance ) ) return RGDN_WRONG_FUNCTION_ARGUMENT;
+    return RGDN_SUCCESS;
+}
+
+void fill_args( rgdn_stream* s, uint32_t fi, const rgdn_frame_params* p, FrameArgs& a )
+{
+    memset( &a, 0, sizeof( a ) );
+    Uniform& u = a.u;
+    u.W = (int)s->W; u.H = (int)s->H; u.GW = (int)s->GW; u.GH = (int)s->GH;
+    u.rw = (float)s->W; u.rh = (float)s->H;
+    memcpy( u.view, p->view, sizeof( u.view ) );
+    memcpy( u.viewPrev, p->viewPrev, sizeof( u.viewPrev ) );
+    memcpy( u.proj, p->projection, sizeof( u.proj ) );
+    memcpy( u.projPrev, p->projectionPrev, sizeof( u.projPrev ) );
+    memcpy( u.camPos, p->cameraPosition, sizeof( u.camPos ) );
+    memcpy( u.camPosPrev, p->cameraPositionPrev, sizeof( u.camPosPrev ) );
+    u.timeDelta         = p->timeDelta;
+    u.minLog            = p->minLogLuminance;
+    u.maxLog            = p->maxLogLuminance;
+    u.stopEyeAdaptation = p->stopEyeAdaptation;
+    u.gradMultD         = p->gradientMultDiffuse;
+    u.gradMultI         = p->gradientMultIndirect;
+    u.gradMultS         = p->gradientMultSpecular;
+    u.antiFirefly       = p->antiFireflyEnabled;
+    u.lightmapCoverage  = p->lightmapScreenCoverage;
+    u.debugFlags        = p->debugShowFlags;
+    u.niter             = p->atrousIterations == 0 ? 4u : p->atrousIterations;
+    u.flags             = p->flags;
+
+    const uint32_t pf = fi ^ 1u;
+#define CUR( fb ) ( (void*)plane_ptr_mut( s, fb, fi ) )
+#define PRV( fb ) ( (const void*)plane_ptr( s, fb, pf ) )
+    a.albedo         = (const uint32_t*)CUR( RGDN_FB_ALBEDO );
+    a.isSky          = (const uint8_t*)CUR( RGDN_FB_IS_SKY );
+    a.normal         = (const uint32_t*)CUR( RGDN_FB_NORMAL );
+    a.normalPrev     = (const uint32_t*)PRV( RGDN_FB_NORMAL );
+    a.mr             = (const uint16_t*)CUR( RGDN_FB_METALLIC_ROUGHNESS );
+    a.depth          = (const uint16_t*)CUR( RGDN_FB_DEPTH_WORLD );
+    a.depthPrev      = (const uint16_t*)PRV( RGDN_FB_DEPTH_WORLD );
+    a.depthGrad      = (const uint16_t*)CUR( RGDN_FB_DEPTH_GRAD );
+    a.motion         = (const ushort4*)CUR( RGDN_FB_MOTION );
+    a.unfD           = (const uint32_t*)CUR( RGDN_FB_UNFILTERED_DIRECT );
+    a.unfS           = (const uint32_t*)CUR( RGDN_FB_UNFILTERED_SPECULAR );
+    a.unfI           = (const uint32_t*)CUR( RGDN_FB_UNFILTERED_INDIR );
+    a.surfPos        = (const float4*)CUR( RGDN_FB_SURFACE_POSITION );
+    a.surfPosPrev    = (const float4*)PRV( RGDN_FB_SURFACE_POSITION );
+    a.viewDir        = (const ushort4*)CUR( RGDN_FB_VIEW_DIRECTION );
+    a.throughput     = (const ushort4*)CUR( RGDN_FB_THROUGHPUT );
+    a.gradInputsPrev = (const uint32_t*)PRV( RGDN_FB_GRADIENT_INPUTS );
+    a.reshaded       = (const float2*)CUR( RGDN_FB_GRADIENT_RESHADED );
+    a.preFinal       = CUR( RGDN_FB_PRE_FINAL );
+    a.histInput      = (uint16_t*)CUR( RGDN_FB_HISTOGRAM_INPUT );
+    a.histLen        = CUR( RGDN_FB_ACCUM_HISTORY_LENGTH );
+    a.histLenPrev    = PRV( RGDN_FB_ACCUM_HISTORY_LENGTH );
+    a.diffTemp       = CUR( RGDN_FB_DIFF_TEMPORARY );
+    a.diffAccumColor = CUR( RGDN_FB_DIFF_ACCUM_COLOR );
+    a.moments        = CUR( RGDN_FB_DIFF_ACCUM_MOMENTS );
+    a.momentsPrev    = PRV( RGDN_FB_DIFF_ACCUM_MOMENTS );
+    a.diffHistory    = CUR( RGDN_FB_DIFF_COLOR_HISTORY );
+    a.diffPing       = CUR( RGDN_FB_DIFF_PING_COLOR_AND_VARIANCE );
+    a.diffPong       = CUR( RGDN_FB_DIFF_PONG_COLOR_AND_VARIANCE );
+    a.varHistory     = (float*)CUR( RGDN_FB_DIFF_COLOR_HISTORY_VARIANCE );
+    a.varPing        = (float*)CUR( RGDN_FB_DIFF_PING_VARIANCE );
+    a.varPong        = (float*)CUR( RGDN_FB_DIFF_PONG_VARIANCE );
+    a.specAccum      = CUR( RGDN_FB_SPEC_ACCUM_COLOR );
+    a.specAccumPrev  = PRV( RGDN_FB_SPEC_ACCUM_COLOR );
+    a.specPing       = CUR( RGDN_FB_SPEC_PING_COLOR );
+    a.specPong       = CUR( RGDN_FB_SPEC_PONG_COLOR );
+    a.indirAccum     = CUR( RGDN_FB_INDIR_ACCUM );
+    a.indirAccumPrev = PRV( RGDN_FB_INDIR_ACCUM );
+    a.indirPing      = CUR( RGDN_FB_INDIR_PING );
+    a.indirPong      = CUR( RGDN_FB_INDIR_PONG );
+    a.filtVar        = CUR( RGDN_FB_ATROUS_FILTERED_VARIANCE );
+    a.disPing        = (uint32_t*)CUR( RGDN_FB_DIS_PING_GRADIENT );
+    a.disPong        = (uint32_t*)CUR( RGDN_FB_DIS_PONG_GRADIENT );
+    a.disHist        = (uint32_t*)CUR( RGDN_FB_DIS_GRADIENT_HISTORY );
+    a.disHistPrev    = (const uint32_t*)PRV( RGDN_FB_DIS_GRADIENT_HISTORY );
+    a.gradPrevPix    = (uint8_t*)CUR( RGDN_FB_GRADIENT_PREV_PIX );
+#undef CUR
+#undef PRV
+    a.tm       = s->tm;
+    a.binLut   = s->binLut;
+    a.phiTab   = s->ctx->phiTab;
+    a.thetaTab = s->ctx->thetaTab;
+}
+
+rgdn_status launch( rgdn_stream* s, const FrameArgs& a, int stage, int iter, cudaStream_t cs )
+{
+    StageLauncher L = launcher_for( s->storage );
+    if( !L ) return RGDN_INTERNAL_ERROR;
+    cudaError_t e = L( a, stage, iter, cs );
+    s->ctx->launches.fetch_add( 1, std::memory_order_relaxed );
+    return cuda_status( e );
+}
+
+// the histogram bin table follows the frame's luminance range
+rgdn_status ensure_bin_lut( rgdn_stream* s, const rgdn_frame_params* p, cudaStream_t cs )
+{
+    if( s->lutMin == p->minLogLuminance && s->lutMax == p->maxLogLuminance ) return RGDN_SUCCESS;
+    s->hostLut.resize( 65536 );
+    build_bin_lut( s->hostLut.data(), p->minLogLuminance, p->maxLogLuminance );
+    // pageable source: the call returns once the bytes are staged, so hostLut may change later
+    cudaError_t e = cudaMemcpyAsync( s->binLut, s->hostLut.data(), 65536, cudaMemcpyHostToDevice, cs );
+    if( e != cudaSuccess ) return RGDN_DEVICE_ERROR;
+    s->lutMin = p->minLogLuminance;
+    s->lutMax = p->maxLogLuminance;
+    return RGDN_SUCCESS;
+}
+
+rgdn_status run_denoise( rgdn_stream* s, uint32_t fi, const rgdn_frame_params* p, cudaStream_t cs )
+{
+    FrameArgs a;
+    fill_args( s, fi, p, a );
+    rgdn_status r;
+    if( !( p->flags & RGDN_FLAG_SKIP_GRADIENTS ) )
+    {
+        if( ( r = launch( s, a, RGDN_STAGE_GRADIENT_SAMPLES, 0, cs ) ) != RGDN_SUCCESS ) return r;
+        for( int i = 0; i < 4; i++ )
+            if( ( r = launch( s, a, RGDN_STAGE_GRADIENT_ATROUS, i, cs ) ) != RGDN_SUCCESS ) return r;
+    }
+    if( ( r = launch( s, a, RGDN_STAGE_TEMPORAL_ACCUMULATION, 0, cs ) ) != RGDN_SUCCESS ) return r;
+    if( ( r = launch( s, a, RGDN_STAGE_ANTI_FIREFLY, 0, cs ) ) != RGDN_SUCCESS ) return r;
+    if( ( r = launch( s, a, RGDN_STAGE_VARIANCE_ESTIMATION, 0, cs ) ) != RGDN_SUCCESS ) return r;
+    for( uint32_t i = 0; i < a.u.niter; i++ )
+        if( ( r = launch( s, a, RGDN_STAGE_ATROUS, (int)i, cs ) ) != RGDN_SUCCESS ) return r;
+    return RGDN_SUCCESS;
+}
+
+rgdn_status run_exposure( rgdn_stream* s, uint32_t fi, const rgdn_frame_params* p, cudaStream_t cs )
+{
+    rgdn_status r = ensure_bin_lut( s, p, cs );
+    if( r != RGDN_SUCCESS ) return r;
+    FrameArgs a;
+    fill_args( s, fi, p, a );
+    if( ( r = launch( s, a, RGDN_STAGE_LUMINANCE_HISTOGRAM, 0, cs ) ) != RGDN_SUCCESS ) return r;
+    return launch( s, a, RGDN_STAGE_LUMINANCE_AVG, 0, cs );
+}
+
+}  // namespace
+
+// ==========================================================================================
+extern "C" {
+
+uint32_t rgdn_api_version( void ) { return RGDN_API_VERSION; }
+
+rgdn_status rgdn_histogram_bin_table( float minLog, float maxLog, uint8_t* out )
+{
+    if( !out || !( maxLog > minLog ) ) return RGDN_WRONG_FUNCTION_ARGUMENT;
+    build_bin_lut( out, minLog, maxLog );
+    return RGDN_SUCCESS;
+}
+
+const char* rgdn_status_string( rgdn_status st )
+{
+    switch( st )
+    {
+        case RGDN_SUCCESS: return "success";
+        case RGDN_WRONG_INSTANCE: return "wrong instance (null or destroyed handle)";
+        case RGDN_DEVICE_ERROR: return "a CUDA call failed";
+        case RGDN_INTERNAL_ERROR: return "internal error";
+        case RGDN_WRONG_FUNCTION_CALL: return "wrong function call";
+        case RGDN_WRONG_FUNCTION_ARGUMENT: return "wrong function argument";
+        case RGDN_OUT_OF_BUDGET: return "out of the memory budget";
+        case RGDN_TIMEOUT: return "timeout";
+        case RGDN_NOT_READY: return "not ready";
+        default: return "unknown status";
+    }
+}
+
+rgdn_status rgdn_context_create( const rgdn_context_create_info* info, rgdn_context** out )
+{
+    if( !info || !out ) return RGDN_WRONG_FUNCTION_ARGUMENT;
+    *out = nullptr;
+    int n = 0;
+    if( cudaGetDeviceCount( &n ) != cudaSuccess || info->device < 0 || info->device >= n ) return RGDN_DEVICE_ERROR;
+    if( cudaSetDevice( info->device ) != cudaSuccess ) return RGDN_DEVICE_ERROR;
+    rgdn_context* c = new( std::nothrow ) rgdn_context();
+    if( !c ) return RGDN_INTERNAL_ERROR;
+    c->device = info->device;
+    c->budget = info->memoryBudgetBytes;
+    // normal decode tables: the correctly rounded sin/cos of the FP32 angles of Utils.h:132-133
+    std::vector< float2 > ph( 65536 ), th( 65536 );
+    for( uint32_t j = 0; j < 65536u; j++ )
+    {
+        const double phi = (double)rgdn::normal_phi( j );
+        ph[ j ]          = make_float2( (float)sin( phi ), (float)cos( phi ) );
+        const double tht = (double)rgdn::normal_theta( j );
+        th[ j ]          = make_float2( (float)cos( tht ), (float)sin( tht ) );
+    }
+    if( cudaMalloc( &c->phiTab, 65536 * sizeof( float2 ) ) != cudaSuccess ||
+        cudaMalloc( &c->thetaTab, 65536 * sizeof( float2 ) ) != cudaSuccess ||
+        cudaMemcpy( c->phiTab, ph.data(), 65536 * sizeof( float2 ), cudaMemcpyHostToDevice ) != cudaSuccess ||
+        cudaMemcpy( c->thetaTab, th.data(), 65536 * sizeof( float2 ), cudaMemcpyHostToDevice ) != cudaSuccess )
+    {
+        cudaFree( c->phiTab );
+        cudaFree( c->thetaTab );
+        c->magic = 0;
+        delete c;
+        return RGDN_DEVICE_ERROR;
+    }
+    *out = c;
+    return RGDN_SUCCESS;
+}
+
+rgdn_status rgdn_context_destroy( rgdn_context* c )
+{
+    if( !valid_ctx( c ) ) return RGDN_WRONG_INSTANCE;
+    cudaSetDevice( c->device );
+    std::vector< rgdn_stream* > left;
+    {
+        std::lock_guard< std::mutex > g( c->mtx );
+        left.assign( c->streams.begin(), c->streams.end() );
+    }
+    for( rgdn_stream* s : left ) rgdn_stream_destroy( s );
+    cudaFree( c->phiTab );
+    cudaFree( c->thetaTab );
+    c->magic = 0;
+    delete c;
+    return RGDN_SUCCESS;
+}
+
+rgdn_status rgdn_context_memory_used( rgdn_context* c, uint64_t* out )
+{
+    if( !valid_ctx( c ) ) return RGDN_WRONG_INSTANCE;
+    if( !out ) return RGDN_WRONG_FUNCTION_ARGUMENT;
+    std::lock_guard< std::mutex > g( c->mtx );
+    *out = c->used;
+    return RGDN_SUCCESS;
+}
+
+rgdn_status rgdn_context_launch_count( rgdn_context* c, uint64_t* out )
+{
+    if( !valid_ctx( c ) ) return RGDN_WRONG_INSTANCE;
+    if( !out ) return RGDN_WRONG_FUNCTION_ARGUMENT;
+    *out = c->launches.load();
+    return RGDN_SUCCESS;
+}
+
+rgdn_status rgdn_stream_required_bytes( const rgdn_stream_create_info* info, uint64_t* out )
+{
+    if( !info || !out || info->width < 2 || info->height < 1 || ( info->width & 1 ) || info->storage > RGDN_STORAGE_BF16 )
+        return RGDN_WRONG_FUNCTION_ARGUMENT;
+    *out = stream_layout( info->width, info->height, info->storage, nullptr, nullptr );
+    return RGDN_SUCCESS;
+}
+
+static rgdn_status stream_alloc( rgdn_stream* s, uint32_t W, uint32_t H )
+{
+    rgdn_context* c     = s->ctx;
+    const size_t  bytes = stream_layout( W, H, s->storage, nullptr, nullptr );
+    {
+        std::lock_guard< std::mutex > g( c->mtx );
+        if( c->budget && c->used + bytes > c->budget ) return RGDN_OUT_OF_BUDGET;
+        c->used += bytes;
+    }
+    void* block = nullptr;
+    if( cudaMalloc( &block, bytes ) != cudaSuccess || cudaMemset( block, 0, bytes ) != cudaSuccess )
+    {
+        cudaFree( block );
+        cudaGetLastError();
+        std::lock_guard< std::mutex > g( c->mtx );
+        c->used -= bytes;
+        return RGDN_OUT_OF_BUDGET;
+    }
+    s->block = block;
+    s->bytes = bytes;
+    s->W = W; s->H = H;
+    s->GW = std::max( 1u, ( W + 1 ) / 3 );
+    s->GH = std::max( 1u, ( H + 1 ) / 3 );
+    stream_layout( W, H, s->storage, s->planes, (uint8_t*)block );
+    s->tm     = (Tonemapping*)block;
+    s->binLut = (uint8_t*)block + align_up( sizeof( Tonemapping ) );
+    s->lutMin = s->lutMax = NAN;
+    return RGDN_SUCCESS;
+}
+
+static void stream_free( rgdn_stream* s )
+{
+    if( !s->block ) return;
+    cudaFree( s->block );
+    std::lock_guard< std::mutex > g( s->ctx->mtx );
+    s->ctx->used -= s->bytes;
+    s->block = nullptr;
+    s->bytes = 0;
+}
+
+rgdn_status rgdn_stream_create( rgdn_context* c, const rgdn_stream_create_info* info, rgdn_stream** out )
+{
+    if( !valid_ctx( c ) ) return RGDN_WRONG_INSTANCE;
+    if( !info || !out ) return RGDN_WRONG_FUNCTION_ARGUMENT;
+    *out = nullptr;
+    if( info->width < 2 || info->height < 1 || ( info->width & 1 ) || info->storage > RGDN_STORAGE_BF16 ||
+        info->width > 16384 || info->height > 16384 )
+        return RGDN_WRONG_FUNCTION_ARGUMENT;
+    if( cudaSetDevice( c->device ) != cudaSuccess ) return RGDN_DEVICE_ERROR;
+    rgdn_stream* s = new( std::nothrow ) rgdn_stream();
+    if( !s ) return RGDN_INTERNAL_ERROR;
+    s->ctx     = c;
+    s->storage = info->storage;
+    rgdn_status r = stream_alloc( s, info->width, info->height );
+    if( r != RGDN_SUCCESS )
+    {
+        s->magic = 0;
+        delete s;
+        return r;
+    }
+    {
+        std::lock_guard< std::mutex > g( c->mtx );
+        c->streams.insert( s );
+    }
+    *out = s;
+    return RGDN_SUCCESS;
+}
+
+rgdn_status rgdn_stream_destroy( rgdn_stream* s )
+{
+    if( !valid_stream( s ) ) return RGDN_WRONG_INSTANCE;
+    cudaSetDevice( s->ctx->device );
+    cudaDeviceSynchronize();
+    stream_free( s );
+    {
+        std::lock_guard< std::mutex > g( s->ctx->mtx );
+        s->ctx->streams.erase( s );
+    }
+    s->magic = 0;
+    delete s;
+    return RGDN_SUCCESS;
+}
+
+rgdn_status rgdn_stream_resize( rgdn_stream* s, uint32_t w, uint32_t h )
+{
+    if( !valid_stream( s ) ) return RGDN_WRONG_INSTANCE;
+    if( w < 2 || h < 1 || ( w & 1 ) || w > 16384 || h > 16384 ) return RGDN_WRONG_FUNCTION_ARGUMENT;
+    if( w == s->W && h == s->H ) return RGDN_SUCCESS;
+    cudaSetDevice( s->ctx->device );
+    // Framebuffers::PrepareForSize waits for the device idle before reallocating
+    cudaDeviceSynchronize();
+    const uint32_t oldW = s->W, oldH = s->H;
+    stream_free( s );
+    rgdn_status r = stream_alloc( s, w, h );
+    if( r != RGDN_SUCCESS )
+    {
+        // keep the stream usable at its old size when the new one does not fit
+        if( stream_alloc( s, oldW, oldH ) != RGDN_SUCCESS ) return RGDN_DEVICE_ERROR;
+        return r;
+    }
+    return RGDN_SUCCESS;
+}
+
+rgdn_status rgdn_stream_get_framebuffer( rgdn_stream* s, uint32_t fb, uint32_t frameIndex, rgdn_image* out )
+{
+    if( !valid_stream( s ) ) return RGDN_WRONG_INSTANCE;
+    if( fb >= RGDN_FB_COUNT || !out || frameIndex > 1 ) return RGDN_WRONG_FUNCTION_ARGUMENT;
+    const PlaneSlot& p = s->planes[ fb ];
+    out->data        = (void*)plane_ptr( s, fb, frameIndex );
+    out->width       = p.w;
+    out->height      = p.h;
+    out->pitch_bytes = p.w * p.texel;
+    out->texel_bytes = p.texel;
+    out->format      = p.format;
+    out->has_prev    = p.prev ? 1u : 0u;
+    return RGDN_SUCCESS;
+}
+
+rgdn_status rgdn_stream_upload( rgdn_stream* s, uint32_t fb, uint32_t frameIndex, const void* src, size_t bytes, rgdn_cuda_stream cs )
+{
+    if( !valid_stream( s ) ) return RGDN_WRONG_INSTANCE;
+    if( fb >= RGDN_FB_COUNT || frameIndex > 1 || !src ) return RGDN_WRONG_FUNCTION_ARGUMENT;
+    const PlaneSlot& p = s->planes[ fb ];
+    if( !p.ptr[ 0 ] || bytes != (size_t)p.w * p.h * p.texel ) return RGDN_WRONG_FUNCTION_ARGUMENT;
+    cudaSetDevice( s->ctx->device );
+    return cuda_status( cudaMemcpyAsync( plane_ptr_mut( s, fb, frameIndex ), src, bytes, cudaMemcpyDefault, (cudaStream_t)cs ) );
+}
+
+rgdn_status rgdn_stream_download( rgdn_stream* s, uint32_t fb, uint32_t frameIndex, void* dst, size_t bytes, rgdn_cuda_stream cs )
+{
+    if( !valid_stream( s ) ) return RGDN_WRONG_INSTANCE;
+    if( fb >= RGDN_FB_COUNT || frameIndex > 1 || !dst ) return RGDN_WRONG_FUNCTION_ARGUMENT;
+    const PlaneSlot& p = s->planes[ fb ];
+    if( !p.ptr[ 0 ] || bytes != (size_t)p.w * p.h * p.texel ) return RGDN_WRONG_FUNCTION_ARGUMENT;
+    cudaSetDevice( s->ctx->device );
+    return cuda_status( cudaMemcpyAsync( dst, plane_ptr( s, fb, frameIndex ), bytes, cudaMemcpyDefault, (cudaStream_t)cs ) );
+}
+
+rgdn_status rgdn_denoise( rgdn_stream* s, uint32_t frameIndex, const rgdn_frame_params* p, rgdn_cuda_stream cs )
+{
+    if( !valid_stream( s ) ) return RGDN_WRONG_INSTANCE;
+    if( frameIndex > 1 ) return RGDN_WRONG_FUNCTION_ARGUMENT;
+    rgdn_status r = check_params( p );
+    if( r != RGDN_SUCCESS ) return r;
+    cudaSetDevice( s->ctx->device );
+    return run_denoise( s, frameIndex, p, (cudaStream_t)cs );
+}
+
+rgdn_status rgdn_calculate_exposure( rgdn_stream* s, uint32_t frameIndex, const rgdn_frame_params* p, rgdn_cuda_stream cs )
+{
+    if( !valid_stream( s ) ) return RGDN_WRONG_INSTANCE;
+    if( frameIndex > 1 ) return RGDN_WRONG_FUNCTION_ARGUMENT;
+    rgdn_status r = check_params( p );
+    if( r != RGDN_SUCCESS ) return r;
+    cudaSetDevice( s->ctx->device );
+    return run_exposure( s, frameIndex, p, (cudaStream_t)cs );
+}
+
+rgdn_status rgdn_denoise_stage( rgdn_stream* s, uint32_t stage, uint32_t iteration, uint32_t frameIndex, const rgdn_frame_params* p,
+                                rgdn_cuda_stream cs )
+{
+    if( !valid_stream( s ) ) return RGDN_WRONG_INSTANCE;
+    if( frameIndex > 1 || stage >= RGDN_STAGE_COUNT ) return RGDN_WRONG_FUNCTION_ARGUMENT;
+    rgdn_status r = check_params( p );
+    if( r != RGDN_SUCCESS ) return r;
+    const uint32_t niter = p->atrousIterations == 0 ? 4u : p->atrousIterations;
+    if( stage == RGDN_STAGE_GRADIENT_ATROUS && iteration > 3 ) return RGDN_WRONG_FUNCTION_ARGUMENT;
+    if( stage == RGDN_STAGE_ATROUS && iteration >= niter ) return RGDN_WRONG_FUNCTION_ARGUMENT;
+    cudaSetDevice( s->ctx->device );
+    if( stage == RGDN_STAGE_LUMINANCE_HISTOGRAM && ( r = ensure_bin_lut( s, p, (cudaStream_t)cs ) ) != RGDN_SUCCESS ) return r;
+    FrameArgs a;
+    fill_args( s, frameIndex, p, a );
+    return launch( s, a, (int)stage, (int)iteration, (cudaStream_t)cs );
+}
+
+rgdn_status rgdn_stream_tonemapping_device( rgdn_stream* s, void** out )
+{
+    if( !valid_stream( s ) ) return RGDN_WRONG_INSTANCE;
+    if( !out ) return RGDN_WRONG_FUNCTION_ARGUMENT;
+    *out = s->tm;
+    return RGDN_SUCCESS;
+}
+
+rgdn_status rgdn_get_tonemapping( rgdn_stream* s, uint32_t* hist, float* avgLum, float* exposure, rgdn_cuda_stream cs )
+{
+    if( !valid_stream( s ) ) return RGDN_WRONG_INSTANCE;
+    cudaSetDevice( s->ctx->device );
+    Tonemapping h;
+    if( cudaMemcpyAsync( &h, s->tm, sizeof( h ), cudaMemcpyDeviceToHost, (cudaStream_t)cs ) != cudaSuccess ||
+        cudaStreamSynchronize( (cudaStream_t)cs ) != cudaSuccess )
+        return RGDN_DEVICE_ERROR;
+    if( hist ) memcpy( hist, h.histogram, sizeof( h.histogram ) );
+    if( avgLum ) *avgLum = h.avgLuminance;
+    if( exposure )
+    {
+        // Exposure.h:33-51 getAutoEV100 + ev100ToLuminousExposure
+        const float lumAverage = fmaxf( 0.0f, h.avgLuminance );
+        const float ev100      = log2f( lumAverage * 100.0f / 12.5f );
+        const float maxLum     = 1.2f * exp2f( ev100 );
+        *exposure              = maxLum > 0.0f ? 1.0f / maxLum : 0.0f;
+    }
+    return RGDN_SUCCESS;
+}
+
+rgdn_status rgdn_set_tonemapping( rgdn_stream* s, const uint32_t* hist, float avgLum, rgdn_cuda_stream cs )
+{
+    if( !valid_stream( s ) ) return RGDN_WRONG_INSTANCE;
+    cudaSetDevice( s->ctx->device );
+    Tonemapping h;
+    memset( &h, 0, sizeof( h ) );
+    if( hist ) memcpy( h.histogram, hist, sizeof( h.histogram ) );
+    h.avgLuminance = avgLum;
+    // pageable source: staged before the call returns
+    if( cudaMemcpyAsync( s->tm, &h, sizeof( h ), cudaMemcpyHostToDevice, (cudaStream_t)cs ) != cudaSuccess ) return RGDN_DEVICE_ERROR;
+    return cuda_status( cudaStreamSynchronize( (cudaStream_t)cs ) );
+}
+
+rgdn_status rgdn_submit_batch( rgdn_context* c, const rgdn_job* jobs, uint32_t n, rgdn_cuda_stream cs )
+{
+    if( !valid_ctx( c ) ) return RGDN_WRONG_INSTANCE;
+    if( n && !jobs ) return RGDN_WRONG_FUNCTION_ARGUMENT;
+    for( uint32_t j = 0; j < n; j++ )
+    {
+        if( !valid_stream( jobs[ j ].stream ) || jobs[ j ].stream->ctx != c ) return RGDN_WRONG_INSTANCE;
+        if( jobs[ j ].frameIndex > 1 ) return RGDN_WRONG_FUNCTION_ARGUMENT;
+        rgdn_status r = check_params( jobs[ j ].params );
+        if( r != RGDN_SUCCESS ) return r;
+    }
+    cudaSetDevice( c->device );
+    for( uint32_t j = 0; j < n; j++ )
+    {
+        rgdn_status r = run_denoise( jobs[ j ].stream, jobs[ j ].frameIndex, jobs[ j ].params, (cudaStream_t)cs );
+        if( r == RGDN_SUCCESS ) r = run_exposure( jobs[ j ].stream, jobs[ j ].frameIndex, jobs[ j ].params, (cudaStream_t)cs );
+        if( r != RGDN_SUCCESS ) return r;
+    }
+    return RGDN_SUCCESS;
+}
+
+}  // extern "C"

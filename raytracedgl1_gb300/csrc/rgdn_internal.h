@@ -1,0 +1,122 @@
+// Internal interface between the C ABI host code (rgdn_api.cu) and the stage kernels
+// (rgdn_kernels.cuh, instantiated once per storage mode in rgdn_mode_*.cu).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/rgdn.h"
+
+namespace rgdn
+{
+
+enum Mode : int
+{
+    MODE_REF  = RGDN_STORAGE_REF,
+    MODE_F32  = RGDN_STORAGE_FP32,
+    MODE_F16  = RGDN_STORAGE_FP16,
+    MODE_BF16 = RGDN_STORAGE_BF16,
+};
+
+constexpr int   STRATA         = 3;        // COMPUTE_ASVGF_STRATA_SIZE (ShaderCommonC.h:150)
+constexpr float MAX_RAY_LENGTH = 10000.0f; // MAX_RAY_LENGTH (ShaderCommonC.h:167)
+constexpr int   MAX_ATROUS_ITERATIONS = 6;
+
+// ShTonemapping (ShaderCommonC.h:344-348), one per stream, device resident
+struct Tonemapping
+{
+    uint32_t histogram[ 256 ];
+    float    avgLuminance;
+    uint32_t blocksDone;   // completion counter of the fused histogram (zero between frames)
+};
+
+// The subset of ShGlobalUniform (ShaderCommonC.h:209-304) this path reads, plus sizes.
+struct Uniform
+{
+    int      W, H;           // render size (image size)
+    int      GW, GH;         // gradient image size ((W+1)/3, (H+1)/3)
+    float    rw, rh;         // renderWidth / renderHeight as floats
+    float    view[ 16 ], viewPrev[ 16 ], proj[ 16 ], projPrev[ 16 ];
+    float    camPos[ 3 ], camPosPrev[ 3 ];
+    float    timeDelta, minLog, maxLog;
+    uint32_t stopEyeAdaptation;
+    float    gradMultD, gradMultI, gradMultS;
+    uint32_t antiFirefly;
+    float    lightmapCoverage;
+    uint32_t debugFlags;
+    uint32_t niter;
+    uint32_t flags;
+};
+
+// Device addresses of every plane the kernels touch, resolved for one frameIndex
+// (cur = frameIndex, prev = frameIndex ^ 1 for double-buffered images).
+struct FrameArgs
+{
+    Uniform u;
+    // G-buffer (reference formats)
+    const uint32_t* albedo;          // B10G11R11, regular layout
+    const uint8_t*  isSky;
+    const uint32_t* normal;
+    const uint32_t* normalPrev;
+    const uint16_t* mr;              // rg8: low byte metallic, high byte roughness
+    const uint16_t* depth;           // r16f
+    const uint16_t* depthPrev;
+    const uint16_t* depthGrad;
+    const ushort4*  motion;          // rgba16f
+    const uint32_t* unfD;
+    const uint32_t* unfS;
+    const uint32_t* unfI;
+    const float4*   surfPos;
+    const float4*   surfPosPrev;
+    const ushort4*  viewDir;         // rgba16f
+    const ushort4*  throughput;      // rgba16f
+    const uint32_t* gradInputsPrev;  // rg16f
+    const float2*   reshaded;        // rg32f
+    // outputs
+    void*     preFinal;
+    uint16_t* histInput;             // r16f, regular layout
+    // history / intermediates (mode-dependent element types)
+    void*       histLen;
+    const void* histLenPrev;
+    void*       diffTemp;
+    void*       diffAccumColor;
+    void*       moments;
+    const void* momentsPrev;
+    void*       diffHistory;         // DiffColorHistory
+    void*       diffPing;
+    void*       diffPong;
+    float*      varHistory;          // FP32 variance planes (16-bit modes only)
+    float*      varPing;
+    float*      varPong;
+    void*       specAccum;
+    const void* specAccumPrev;
+    void*       specPing;
+    void*       specPong;
+    void*       indirAccum;
+    const void* indirAccumPrev;
+    void*       indirPing;
+    void*       indirPong;
+    void*       filtVar;
+    // gradients, 1/3 resolution, rgba8
+    uint32_t*       disPing;
+    uint32_t*       disPong;
+    uint32_t*       disHist;
+    const uint32_t* disHistPrev;
+    uint8_t*        gradPrevPix;
+    // tonemapping
+    Tonemapping*   tm;
+    const uint8_t* binLut;           // 65536-entry fp16 bits -> histogram bin
+    // normal decode tables: phi[j] = (sin, cos), theta[k] = (cos, sin)
+    const float2* phiTab;
+    const float2* thetaTab;
+};
+
+// Launches one stage for one frame. Returns the CUDA error of the launch.
+typedef cudaError_t ( *StageLauncher )( const FrameArgs& a, int stage, int iter, cudaStream_t s );
+
+cudaError_t launch_stage_ref( const FrameArgs& a, int stage, int iter, cudaStream_t s );
+cudaError_t launch_stage_f32( const FrameArgs& a, int stage, int iter, cudaStream_t s );
+cudaError_t launch_stage_f16( const FrameArgs& a, int stage, int iter, cudaStream_t s );
+cudaError_t launch_stage_bf16( const FrameArgs& a, int stage, int iter, cudaStream_t s );
+
+}  // namespace rgdn

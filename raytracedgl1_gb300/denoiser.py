@@ -1,0 +1,229 @@
+"""Python host mirror of the reference's interface for this path, over the C ABI.
+
+    RTGL1::Denoiser      (Source/Denoiser.h:31-69)     -> Denoiser.Denoise(frameIndex, uniform)
+    RTGL1::Tonemapping   (Source/Tonemapping.h:33-79)  -> Tonemapping.CalculateExposure(frameIndex, uniform)
+    RTGL1::Framebuffers  (Source/Framebuffers.h)       -> Framebuffers (per stream)
+
+Errors surface as ``RgdnError`` carrying the C status (the reference turns RgException into
+RgResult at its API, Source/RTGL1.cpp:145-195). Every compute call goes through librgdn.so;
+there is no Python fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from typing import Optional
+
+import numpy as np
+
+from . import _native as N
+
+# numpy view of each texel format: (dtype, channels per texel)
+FORMAT_NUMPY = {
+    1: (np.uint8, 1),    # R8_UINT
+    2: (np.uint8, 2),    # RG8_UNORM
+    3: (np.uint8, 4),    # RGBA8_UNORM
+    4: (np.uint16, 1),   # R16_SFLOAT (bits)
+    5: (np.uint16, 2),   # RG16_SFLOAT
+    6: (np.uint16, 4),   # RGBA16_SFLOAT
+    7: (np.uint16, 4),   # RGBA16_BFLOAT
+    8: (np.float32, 1),  # R32_SFLOAT
+    9: (np.float32, 2),  # RG32_SFLOAT
+    10: (np.float32, 4),  # RGBA32_SFLOAT
+    11: (np.uint32, 1),  # R32_UINT
+    12: (np.uint32, 1),  # E5B9G9R9
+    13: (np.uint32, 1),  # B10G11R11
+    14: (np.uint32, 1),  # NORMAL_SPHERICAL
+}
+
+
+def _stream_handle(cuda_stream) -> Optional[int]:
+    """Accepts None (legacy default stream), an int handle, or a torch.cuda.Stream."""
+    if cuda_stream is None:
+        return None
+    if isinstance(cuda_stream, int):
+        return cuda_stream
+    return int(cuda_stream.cuda_stream)
+
+
+class Context:
+    """One CUDA device, its normal-decode tables and the streams' memory budget."""
+
+    def __init__(self, device: int = 0, memory_budget_bytes: int = 0):
+        self.lib = N.load()
+        info = N.ContextCreateInfo(device, memory_budget_bytes)
+        h = C.c_void_p()
+        N.check(self.lib.rgdn_context_create(C.byref(info), C.byref(h)), "rgdn_context_create")
+        self.handle = h
+
+    def close(self) -> None:
+        if self.handle:
+            N.check(self.lib.rgdn_context_destroy(self.handle), "rgdn_context_destroy")
+            self.handle = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def memory_used(self) -> int:
+        v = C.c_uint64()
+        N.check(self.lib.rgdn_context_memory_used(self.handle, C.byref(v)))
+        return v.value
+
+    def launch_count(self) -> int:
+        v = C.c_uint64()
+        N.check(self.lib.rgdn_context_launch_count(self.handle, C.byref(v)))
+        return v.value
+
+    def submit_batch(self, jobs, cuda_stream=None) -> None:
+        """jobs: iterable of (Stream, frameIndex, FrameParams)."""
+        jobs = list(jobs)
+        arr = (N.Job * len(jobs))()
+        keep = []
+        for i, (s, fi, p) in enumerate(jobs):
+            keep.append(p)
+            arr[i] = N.Job(s.handle, fi, C.pointer(p))
+        N.check(self.lib.rgdn_submit_batch(self.handle, arr, len(jobs), _stream_handle(cuda_stream)),
+                "rgdn_submit_batch")
+
+
+def required_bytes(width: int, height: int, storage: int) -> int:
+    lib = N.load()
+    info = N.StreamCreateInfo(width, height, storage)
+    v = C.c_uint64()
+    N.check(lib.rgdn_stream_required_bytes(C.byref(info), C.byref(v)), "rgdn_stream_required_bytes")
+    return v.value
+
+
+class Stream:
+    """One camera stream: its framebuffer set, temporal history and tonemapping state."""
+
+    def __init__(self, ctx: Context, width: int, height: int, storage: int = N.STORAGE_REF):
+        self.ctx, self.lib = ctx, ctx.lib
+        info = N.StreamCreateInfo(width, height, storage)
+        h = C.c_void_p()
+        N.check(self.lib.rgdn_stream_create(ctx.handle, C.byref(info), C.byref(h)), "rgdn_stream_create")
+        self.handle = h
+        self.width, self.height, self.storage = width, height, storage
+
+    def close(self) -> None:
+        if self.handle:
+            N.check(self.lib.rgdn_stream_destroy(self.handle), "rgdn_stream_destroy")
+            self.handle = None
+
+    def __del__(self):
+        try:
+            if self.ctx.handle:
+                self.close()
+        except Exception:
+            pass
+
+    def resize(self, width: int, height: int) -> None:
+        N.check(self.lib.rgdn_stream_resize(self.handle, width, height), "rgdn_stream_resize")
+        self.width, self.height = width, height
+
+    # --- Framebuffers --------------------------------------------------------------------
+    def image(self, fb, frame_index: int = 0) -> N.Image:
+        fb = N.FB[fb] if isinstance(fb, str) else fb
+        img = N.Image()
+        N.check(self.lib.rgdn_stream_get_framebuffer(self.handle, fb, frame_index, C.byref(img)),
+                "rgdn_stream_get_framebuffer")
+        return img
+
+    def upload(self, fb, frame_index: int, src, cuda_stream=None) -> None:
+        """src: a numpy array (host) or an (int device pointer, nbytes) pair."""
+        fbi = N.FB[fb] if isinstance(fb, str) else fb
+        if isinstance(src, tuple):
+            ptr, nbytes = src
+        else:
+            arr = np.ascontiguousarray(src)
+            ptr, nbytes = arr.ctypes.data, arr.nbytes
+        N.check(self.lib.rgdn_stream_upload(self.handle, fbi, frame_index, C.c_void_p(ptr), nbytes,
+                                            _stream_handle(cuda_stream)), f"upload {fb}")
+        if not isinstance(src, tuple) and cuda_stream is None:
+            self.synchronize()
+
+    def download(self, fb, frame_index: int = 0, cuda_stream=None) -> np.ndarray:
+        img = self.image(fb, frame_index)
+        if not img.data:
+            raise N.RgdnError(N.WRONG_FUNCTION_ARGUMENT, f"{fb} does not exist in this storage mode")
+        dt, ch = FORMAT_NUMPY[img.format]
+        shape = (img.height, img.width) if ch == 1 else (img.height, img.width, ch)
+        out = np.empty(shape, dtype=dt)
+        fbi = N.FB[fb] if isinstance(fb, str) else fb
+        N.check(self.lib.rgdn_stream_download(self.handle, fbi, frame_index, C.c_void_p(out.ctypes.data),
+                                              out.nbytes, _stream_handle(cuda_stream)), f"download {fb}")
+        self.synchronize(cuda_stream)
+        return out
+
+    def synchronize(self, cuda_stream=None) -> None:
+        # a tonemapping read synchronises the stream; cheap (1 KB)
+        N.check(self.lib.rgdn_get_tonemapping(self.handle, None, None, None, _stream_handle(cuda_stream)))
+
+    # --- tonemapping state ---------------------------------------------------------------
+    def tonemapping(self, cuda_stream=None):
+        hist = (C.c_uint32 * 256)()
+        avg = C.c_float()
+        exp = C.c_float()
+        N.check(self.lib.rgdn_get_tonemapping(self.handle, hist, C.byref(avg), C.byref(exp),
+                                              _stream_handle(cuda_stream)), "rgdn_get_tonemapping")
+        return np.frombuffer(hist, dtype=np.uint32).copy(), avg.value, exp.value
+
+    def set_tonemapping(self, hist, avg_luminance: float, cuda_stream=None) -> None:
+        h = (C.c_uint32 * 256)(*[int(x) for x in hist]) if hist is not None else None
+        N.check(self.lib.rgdn_set_tonemapping(self.handle, h, C.c_float(avg_luminance),
+                                              _stream_handle(cuda_stream)), "rgdn_set_tonemapping")
+
+    def tonemapping_device_ptr(self) -> int:
+        p = C.c_void_p()
+        N.check(self.lib.rgdn_stream_tonemapping_device(self.handle, C.byref(p)))
+        return p.value
+
+    # --- stages --------------------------------------------------------------------------
+    def stage(self, stage: int, iteration: int, frame_index: int, params: N.FrameParams,
+              cuda_stream=None) -> None:
+        N.check(self.lib.rgdn_denoise_stage(self.handle, stage, iteration, frame_index, C.byref(params),
+                                            _stream_handle(cuda_stream)), f"rgdn_denoise_stage {stage}")
+
+
+class Denoiser:
+    """Denoiser::Denoise(cmd, frameIndex, uniform) — Source/Denoiser.cpp:64-255."""
+
+    def __init__(self, stream: Stream):
+        self.stream = stream
+
+    def Denoise(self, frameIndex: int, uniform: N.FrameParams, cuda_stream=None) -> None:
+        s = self.stream
+        N.check(s.lib.rgdn_denoise(s.handle, frameIndex, C.byref(uniform), _stream_handle(cuda_stream)),
+                "rgdn_denoise")
+
+
+class Tonemapping:
+    """Tonemapping::CalculateExposure(cmd, frameIndex, uniform) — Source/Tonemapping.cpp:59-165."""
+
+    def __init__(self, stream: Stream):
+        self.stream = stream
+
+    def CalculateExposure(self, frameIndex: int, uniform: N.FrameParams, cuda_stream=None) -> None:
+        s = self.stream
+        N.check(s.lib.rgdn_calculate_exposure(s.handle, frameIndex, C.byref(uniform),
+                                              _stream_handle(cuda_stream)), "rgdn_calculate_exposure")
+
+    def GetTonemapping(self, cuda_stream=None):
+        """(histogram[256], avgLuminance, exposure) after the work on cuda_stream."""
+        return self.stream.tonemapping(cuda_stream)
+
+
+def histogram_bin_table(min_log: float, max_log: float) -> np.ndarray:
+    lib = N.load()
+    out = np.empty(65536, dtype=np.uint8)
+    N.check(lib.rgdn_histogram_bin_table(C.c_float(min_log), C.c_float(max_log),
+                                         out.ctypes.data_as(C.POINTER(C.c_uint8))))
+    return out

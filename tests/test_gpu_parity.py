@@ -1,0 +1,273 @@
+"""GPU parity: librgdn's CUDA stages against the CPU oracle, through the C ABI.
+
+Per stage: the GPU's whole framebuffer state is copied into the oracle, the one stage runs on
+both, then every plane of both frame slots is compared — planes the stage does not write must
+stay bit-identical, planes it writes must agree to within the storage format's quantum
+(fp32 storage: 1e-3 relative per texel, the FP32-mode bar).
+
+End to end: the GPU and the oracle run the same frames independently (no state sync), and the
+outputs are compared per pixel. Histograms are compared bit-exact on the same HistogramInput.
+"""
+import numpy as np
+import pytest
+
+from raytracedgl1_gb300 import _native as N
+from raytracedgl1_gb300.denoiser import Denoiser, Stream, Tonemapping
+from raytracedgl1_gb300.scene import Scene
+
+import oracle
+from tests import _formats as F
+
+pytestmark = pytest.mark.gpu
+
+MODES = [("ref", N.STORAGE_REF), ("fp32", N.STORAGE_FP32), ("fp16", N.STORAGE_FP16), ("bf16", N.STORAGE_BF16)]
+# sizes: W%3 in {1, 2, 0}, odd heights, a width whose half is odd
+SIZES = [(64, 36), (50, 23), (34, 17)]
+
+# per-texel tolerance (relative to the texel's largest channel) of each stored format
+TOL = {F.F_E5: 2.0 ** -7, F.F_RGBA16F: 2.0 ** -9, F.F_RG16F: 2.0 ** -9, F.F_R16F: 2.0 ** -9,
+       F.F_RGBA16BF: 2.0 ** -6, F.F_RGBA8: 1.01 / 255.0, F.F_B10G11R11: 2.0 ** -5,
+       F.F_R32F: 1e-3, F.F_RG32F: 1e-3, F.F_RGBA32F: 1e-3}
+
+
+def gpu_planes(s: Stream):
+    out = {}
+    for name in N.FB_NAMES:
+        img = s.image(name, 0)
+        if not img.data:
+            continue
+        for slot in ((0, 1) if img.has_prev else (0,)):
+            out[(name, slot)] = (s.download(name, slot), img.format)
+    return out
+
+
+def sync_to_oracle(s: Stream, o: oracle.OracleStream):
+    for (name, slot), (arr, fmt) in gpu_planes(s).items():
+        assert o.fmt(name) == fmt, f"format table mismatch for {name}"
+        o.plane(name, slot)[...] = arr
+    hist, avg, _ = s.tonemapping()
+    o.set_tonemapping(hist, avg)
+
+
+def compare_state(s: Stream, o: oracle.OracleStream, what: str, max_diff_frac: float = 0.02):
+    worst = []
+    for (name, slot), (g, fmt) in gpu_planes(s).items():
+        c = o.plane(name, slot)
+        if np.array_equal(g, c):
+            continue
+        gd, cd = F.decode(g, fmt), F.decode(c, fmt)
+        if fmt in (F.F_R8U, F.F_R32U, F.F_NORMAL):
+            bad = int(np.count_nonzero(gd != cd))
+            raise AssertionError(f"{what}: integer plane {name}[{slot}] differs at {bad} texels")
+        scale = np.percentile(np.abs(cd[np.isfinite(cd)]), 99) if np.isfinite(cd).any() else 1.0
+        err = F.texel_rel_err(gd, cd, atol=max(1e-6, 1e-4 * float(scale)))
+        tol = TOL[fmt]
+        ndiff = int(np.count_nonzero(np.any(g != c, axis=-1) if g.ndim == 3 else g != c))
+        frac = ndiff / err.size
+        worst.append((name, slot, float(err.max()), frac))
+        assert err.max() <= tol, f"{what}: {name}[{slot}] max texel rel err {err.max():.3e} > {tol:.3e}"
+        assert frac <= max_diff_frac, f"{what}: {name}[{slot}] {frac:.2%} of texels differ"
+    return worst
+
+
+def upload_frame(s, o, bufs, fi):
+    for name, arr in bufs.items():
+        s.upload(name, fi, arr)
+        if o is not None:
+            o.load(name, fi, arr)
+
+
+STAGE_SEQ = None
+
+
+def stage_sequence(niter: int):
+    seq = [(N.STAGE_GRADIENT_SAMPLES, 0)] + [(N.STAGE_GRADIENT_ATROUS, i) for i in range(4)]
+    seq += [(N.STAGE_TEMPORAL_ACCUMULATION, 0), (N.STAGE_ANTI_FIREFLY, 0), (N.STAGE_VARIANCE_ESTIMATION, 0)]
+    seq += [(N.STAGE_ATROUS, i) for i in range(niter)]
+    seq += [(N.STAGE_LUMINANCE_HISTOGRAM, 0), (N.STAGE_LUMINANCE_AVG, 0)]
+    return seq
+
+
+@pytest.mark.parametrize("mode_name,mode", MODES)
+@pytest.mark.parametrize("size", SIZES)
+def test_stage_parity(ctx, mode_name, mode, size):
+    W, H = size
+    sc = Scene(W, H, seed=7, lightFlickerFrom=2.0)
+    s = Stream(ctx, W, H, mode)
+    o = oracle.OracleStream(W, H, mode)
+    for f in range(4):
+        fi = f & 1
+        bufs, p = sc.generate(f)
+        upload_frame(s, None, bufs, fi)
+        for stage, it in stage_sequence(4):
+            sync_to_oracle(s, o)
+            s.stage(stage, it, fi, p)
+            o.stage(stage, it, fi, p)
+            compare_state(s, o, f"{mode_name} {W}x{H} frame {f} stage {stage}.{it}")
+            if stage == N.STAGE_LUMINANCE_HISTOGRAM or stage == N.STAGE_LUMINANCE_AVG:
+                hg, ag, _ = s.tonemapping()
+                ho, ao, _ = o.tonemapping()
+                assert np.array_equal(hg, ho), "histogram not bit-exact"
+                assert np.float32(ag) == np.float32(ao), f"avgLuminance {ag!r} != {ao!r}"
+    s.close()
+
+
+@pytest.mark.parametrize("mode_name,mode", MODES)
+def test_five_iterations_and_flags(ctx, mode_name, mode):
+    """N=5 a-trous (the generalised routing), anti-firefly off, debug flags, gradients off."""
+    W, H = 64, 36
+    sc = Scene(W, H, seed=3)
+    s = Stream(ctx, W, H, mode)
+    o = oracle.OracleStream(W, H, mode)
+    variants = [dict(atrousIterations=5), dict(antiFireflyEnabled=0), dict(debugShowFlags=1 << 6),
+                dict(debugShowFlags=(1 << 9) | (1 << 5)), dict(lightmapScreenCoverage=0.3),
+                dict(gradientMultDiffuse=0.0, gradientMultIndirect=0.0, gradientMultSpecular=0.0),
+                dict(flags=N.FLAG_SKIP_GRADIENTS), dict(stopEyeAdaptation=1)]
+    for f, var in enumerate(variants):
+        fi = f & 1
+        bufs, p = sc.generate(f)
+        for k, v in var.items():
+            setattr(p, k, v)
+        upload_frame(s, None, bufs, fi)
+        niter = p.atrousIterations or 4
+        for stage, it in stage_sequence(niter):
+            if p.flags & N.FLAG_SKIP_GRADIENTS and stage in (N.STAGE_GRADIENT_SAMPLES, N.STAGE_GRADIENT_ATROUS):
+                continue
+            sync_to_oracle(s, o)
+            s.stage(stage, it, fi, p)
+            o.stage(stage, it, fi, p)
+            compare_state(s, o, f"{mode_name} variant {var} stage {stage}.{it}")
+    s.close()
+
+
+def run_frames(s, o, sc, frames, denoise_gpu=True):
+    for f in range(frames):
+        fi = f & 1
+        bufs, p = sc.generate(f)
+        upload_frame(s, o, bufs, fi)
+        Denoiser(s).Denoise(fi, p)
+        Tonemapping(s).CalculateExposure(fi, p)
+        o.denoise(fi, p)
+        o.calculate_exposure(fi, p)
+    return (frames - 1) & 1
+
+
+@pytest.mark.parametrize("mode_name,mode", MODES)
+def test_end_to_end(ctx, mode_name, mode):
+    """Independent multi-frame runs; PRE_FINAL compared per pixel."""
+    W, H = 96, 54
+    sc = Scene(W, H, seed=11, lightFlickerFrom=4.0)
+    s = Stream(ctx, W, H, mode)
+    o = oracle.OracleStream(W, H, mode)
+    fi = run_frames(s, o, sc, 8)
+    img = s.image("PRE_FINAL", fi)
+    g = F.decode(s.download("PRE_FINAL", fi), img.format)
+    c = F.decode(o.plane("PRE_FINAL", fi), img.format)
+    err = F.texel_rel_err(g, c, atol=1e-4 * float(np.percentile(c, 99)))
+    if mode == N.STORAGE_FP32:
+        # the FP32-mode bar: 1e-3 relative per pixel
+        assert err.max() <= 1e-3, f"max rel err {err.max():.3e}"
+    else:
+        # quantised storage: discrete flips of one quantum propagate over frames;
+        # almost every pixel stays within 1e-2 and the image PSNR stays high
+        assert np.mean(err <= 1e-2) >= 0.99, f"{np.mean(err <= 1e-2):.4f} of pixels within 1e-2"
+        assert F.psnr(g, c) > 50.0
+    s.close()
+
+
+@pytest.mark.parametrize("mode_name,mode", MODES[:2])
+def test_histogram_bit_exact_same_input(ctx, mode_name, mode):
+    """Given the same HistogramInput bytes, histogram and avgLuminance are bit-exact."""
+    W, H = 128, 72
+    sc = Scene(W, H, seed=5)
+    s = Stream(ctx, W, H, mode)
+    o = oracle.OracleStream(W, H, mode)
+    run_frames(s, o, sc, 3)
+    for f in range(3, 6):
+        fi = f & 1
+        bufs, p = sc.generate(f)
+        upload_frame(s, o, bufs, fi)
+        Denoiser(s).Denoise(fi, p)
+        # feed the oracle the GPU's HistogramInput and tonemapping state
+        o.plane("HISTOGRAM_INPUT", fi)[...] = s.download("HISTOGRAM_INPUT", fi)
+        h0, a0, _ = s.tonemapping()
+        o.set_tonemapping(h0, a0)
+        Tonemapping(s).CalculateExposure(fi, p)
+        o.stage(N.STAGE_LUMINANCE_HISTOGRAM, 0, fi, p)
+        ho = o.tonemapping()[0].copy()
+        o.stage(N.STAGE_LUMINANCE_AVG, 0, fi, p)
+        hg, ag, eg = s.tonemapping()
+        _, ao, eo = o.tonemapping()
+        assert hg.sum() == 0 and o.tonemapping()[0].sum() == 0  # both cleared for the next frame
+        assert np.float32(ag) == np.float32(ao)
+        assert np.float32(eg) == np.float32(eo)
+        # the histogram itself, before the average clears it
+        s.stage(N.STAGE_LUMINANCE_HISTOGRAM, 0, fi, p)
+        hg2, _, _ = s.tonemapping()
+        assert np.array_equal(hg2, ho)
+        assert hg2.sum() == W * H
+        s.set_tonemapping(None, ag)
+    s.close()
+
+
+def test_batch_equals_sequential(ctx):
+    """rgdn_submit_batch over streams of different sizes == each stream alone."""
+    sizes = [(64, 36), (48, 30), (96, 54)]
+    scenes = [Scene(w, h, seed=20 + i) for i, (w, h) in enumerate(sizes)]
+    a = [Stream(ctx, w, h, N.STORAGE_FP16) for w, h in sizes]
+    b = [Stream(ctx, w, h, N.STORAGE_FP16) for w, h in sizes]
+    for f in range(4):
+        fi = f & 1
+        jobs = []
+        for i, sc in enumerate(scenes):
+            bufs, p = sc.generate(f)
+            upload_frame(a[i], None, bufs, fi)
+            upload_frame(b[i], None, bufs, fi)
+            Denoiser(a[i]).Denoise(fi, p)
+            Tonemapping(a[i]).CalculateExposure(fi, p)
+            jobs.append((b[i], fi, p))
+        ctx.submit_batch(jobs)
+    for i in range(len(sizes)):
+        assert np.array_equal(a[i].download("PRE_FINAL", 1), b[i].download("PRE_FINAL", 1))
+        ha, aa, _ = a[i].tonemapping()
+        hb, ab, _ = b[i].tonemapping()
+        assert np.array_equal(ha, hb) and aa == ab
+    for x in a + b:
+        x.close()
+
+
+def test_error_paths(ctx):
+    with pytest.raises(N.RgdnError) as e:
+        Stream(ctx, 63, 36)
+    assert e.value.status == N.WRONG_FUNCTION_ARGUMENT
+    s = Stream(ctx, 64, 36)
+    p = N.FrameParams()
+    p.minLogLuminance, p.maxLogLuminance = -3.0, 7.0
+    p.atrousIterations = 9
+    with pytest.raises(N.RgdnError) as e:
+        Denoiser(s).Denoise(0, p)
+    assert e.value.status == N.WRONG_FUNCTION_ARGUMENT
+    p.atrousIterations = 4
+    with pytest.raises(N.RgdnError):
+        Denoiser(s).Denoise(2, p)
+    with pytest.raises(N.RgdnError):
+        s.upload("NORMAL", 0, np.zeros(10, np.uint32))
+    s.close()
+    lib = N.load()
+    assert lib.rgdn_denoise(None, 0, p, None) == N.WRONG_INSTANCE
+
+
+def test_budget_admission(cuda_ok):
+    from raytracedgl1_gb300.denoiser import Context, required_bytes
+    need = required_bytes(64, 36, N.STORAGE_REF)
+    c = Context(0, memory_budget_bytes=need * 2 + 10)
+    s1 = Stream(c, 64, 36)
+    s2 = Stream(c, 64, 36)
+    with pytest.raises(N.RgdnError) as e:
+        Stream(c, 64, 36)
+    assert e.value.status == N.OUT_OF_BUDGET
+    s1.close()
+    s3 = Stream(c, 64, 36)
+    assert c.memory_used() == 2 * need
+    s2.close(); s3.close()
+    c.close()

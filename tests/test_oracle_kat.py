@@ -1,0 +1,208 @@
+"""Closed-form known-answer tests of the CPU oracle's stages (the reference ships none; these
+follow from the shader math itself)."""
+import math
+
+import numpy as np
+import pytest
+
+import oracle
+from raytracedgl1_gb300 import _native as N
+from raytracedgl1_gb300.scene import Scene
+from tests import _formats as F
+
+
+def params(**kw):
+    p = N.FrameParams()
+    for i in range(4):
+        p.view[i * 5] = p.viewPrev[i * 5] = p.projection[i * 5] = p.projectionPrev[i * 5] = 1.0
+    p.timeDelta = 1.0 / 60.0
+    p.minLogLuminance, p.maxLogLuminance = -3.0, 7.0
+    p.gradientMultDiffuse, p.gradientMultIndirect, p.gradientMultSpecular = 0.5, 0.2, 0.5
+    p.antiFireflyEnabled = 1
+    p.atrousIterations = 4
+    for k, v in kw.items():
+        setattr(p, k, v)
+    return p
+
+
+def test_first_frame_resets_history():
+    """With zeroed history every reprojection test fails: weightSum = 0, so the temporal
+    accumulation outputs the unfiltered signal, history length 1, moments (l, l^2)
+    (CmSVGFTemporalAccumulation.comp:310-376)."""
+    W, H = 32, 18
+    sc = Scene(W, H, seed=2)
+    bufs, p = sc.generate(0)
+    o = oracle.OracleStream(W, H, oracle.MODE_F32)
+    for k, v in bufs.items():
+        o.load(k, 0, v)
+    o.stage(N.STAGE_TEMPORAL_ACCUMULATION, 0, 0, p)
+    unf = F.decode_e5(bufs["UNFILTERED_DIRECT"])
+    dt = o.plane("DIFF_TEMPORARY", 0)[..., :3]
+    assert np.array_equal(dt, unf)
+    hl = o.plane("ACCUM_HISTORY_LENGTH", 0)
+    assert np.all(hl[..., 0] == 1.0) and np.all(hl[..., 1] == 1.0) and np.all(hl[..., 2] == 1.0)
+    l = (np.float32(0.2125) * unf[..., 0] + np.float32(0.7154) * unf[..., 1]) + np.float32(0.0721) * unf[..., 2]
+    m = o.plane("DIFF_ACCUM_MOMENTS", 0)
+    assert np.array_equal(m[..., 0], l) and np.array_equal(m[..., 1], l * l)
+
+
+def _flat_state(o, W, H, color, var, depth=5.0, normal_code=None):
+    """A flat, fully valid surface: one depth, one normal, one colour and variance."""
+    code = normal_code if normal_code is not None else oracle.encode_normal(0.0, 1.0, 0.0)
+    o.plane("DEPTH_WORLD", 0)[...] = np.float16(depth).view(np.uint16)
+    o.plane("DEPTH_GRAD", 0)[...] = np.float16(0.01).view(np.uint16)
+    o.plane("NORMAL", 0)[...] = code
+    o.plane("METALLIC_ROUGHNESS", 0)[...] = [0, 128]
+    cv = o.plane("DIFF_PING_COLOR_AND_VARIANCE", 0)
+    cv[..., :3] = color
+    cv[..., 3] = var
+    for name in ("SPEC_PING_COLOR", "INDIR_PING"):
+        o.plane(name, 0)[..., :3] = color
+    hl = o.plane("ACCUM_HISTORY_LENGTH", 0)
+    hl[...] = [8.0, 8.0, 8.0, 1.0]
+
+
+@pytest.mark.parametrize("niter", [4, 5])
+def test_atrous_constant_image_invariant(niter):
+    """Normalised edge-stopping weights keep a constant image constant through every
+    a-trous iteration (CmSVGFAtrous.comp:212-219)."""
+    W, H = 40, 24
+    o = oracle.OracleStream(W, H, oracle.MODE_F32)
+    c = np.array([0.7, 0.3, 1.9], dtype=np.float32)
+    _flat_state(o, W, H, c, 0.01)
+    o.plane("ALBEDO", 0)[...] = oracle.encode_b10g11r11(1.0, 1.0, 1.0)
+    o.plane("THROUGHPUT", 0)[...] = np.float16(1.0).view(np.uint16)
+    p = params(atrousIterations=niter)
+    for i in range(niter):
+        o.stage(N.STAGE_ATROUS, i, 0, p)
+    # metallic 0, roughness 128/255: composition = (diff + indir) * albedo + spec' * 0.04
+    r = 128.0 / 255.0
+    t = min(max((r - 0.5) / 0.25, 0.0), 1.0)
+    spec_w = t * t * (3 - 2 * t)
+    expect = (c + c) * 1.0 + (c * (1 - spec_w) + c * spec_w) * 0.04
+    pre = o.plane("PRE_FINAL", 0)[..., :3]
+    assert np.allclose(pre, expect, rtol=2e-6)
+
+
+def test_antifirefly_clamps_isolated_spike():
+    W, H = 20, 12
+    o = oracle.OracleStream(W, H, oracle.MODE_F32)
+    base = np.array([1.0, 2.0, 3.0], np.float32)
+    for name in ("DIFF_TEMPORARY", "SPEC_ACCUM_COLOR", "INDIR_ACCUM"):
+        pl = o.plane(name, 0)
+        pl[..., :3] = base
+        pl[6, 9, :3] = base * 1000
+    o.stage(N.STAGE_ANTI_FIREFLY, 0, 0, params())
+    for name in ("DIFF_ACCUM_COLOR", "SPEC_PING_COLOR", "INDIR_PING"):
+        assert np.allclose(o.plane(name, 0)[6, 9, :3], base)
+    # disabled: passthrough
+    o.stage(N.STAGE_ANTI_FIREFLY, 0, 0, params(antiFireflyEnabled=0))
+    assert np.allclose(o.plane("DIFF_ACCUM_COLOR", 0)[6, 9, :3], base * 1000)
+
+
+def test_variance_temporal_branch():
+    """History > 4: variance = max(0, E[l^2] - E[l]^2) / max(1, h - 4)
+    (CmSVGFEstimateVariance.comp:153-161)."""
+    W, H = 16, 8
+    o = oracle.OracleStream(W, H, oracle.MODE_F32)
+    o.plane("DEPTH_WORLD", 0)[...] = np.float16(3.0).view(np.uint16)
+    o.plane("DIFF_ACCUM_COLOR", 0)[..., :3] = 0.5
+    o.plane("ACCUM_HISTORY_LENGTH", 0)[..., 0] = 10.0
+    m = o.plane("DIFF_ACCUM_MOMENTS", 0)
+    m[..., 0] = 0.5
+    m[..., 1] = 0.5
+    o.stage(N.STAGE_VARIANCE_ESTIMATION, 0, 0, params())
+    v = o.plane("DIFF_PING_COLOR_AND_VARIANCE", 0)[..., 3]
+    assert np.allclose(v, (np.float32(0.5) - np.float32(0.25)) / np.float32(6.0))
+    # sky / invalid depth: variance 0, colour passes through
+    o.plane("DEPTH_WORLD", 0)[...] = np.float16(20000.0).view(np.uint16)
+    o.stage(N.STAGE_VARIANCE_ESTIMATION, 0, 0, params())
+    assert np.all(o.plane("DIFF_PING_COLOR_AND_VARIANCE", 0)[..., 3] == 0)
+
+
+def test_luminance_avg_closed_form():
+    """All pixels in bin b: average = exp2((b-1)/254 * range + minLog); one adaptation step
+    t = 1 - exp(-dt * 1.1) from the previous value (CmLuminanceAvg.comp:70-88)."""
+    W, H = 32, 16
+    o = oracle.OracleStream(W, H, oracle.MODE_F32)
+    b = 128
+    hist = np.zeros(256, np.uint32)
+    hist[b] = W * H
+    o.set_tonemapping(hist, 0.5)
+    p = params()
+    o.stage(N.STAGE_LUMINANCE_AVG, 0, 0, p)
+    h, avg, exposure = o.tonemapping()
+    target = 2.0 ** ((b - 1) / 254.0 * 10.0 - 3.0)
+    t = 1.0 - math.exp(-p.timeDelta * 1.1)
+    assert h.sum() == 0
+    assert avg == pytest.approx(0.5 + (target - 0.5) * t, rel=1e-6)
+    # Exposure.h: EV100 = log2(L*100/12.5); exposure = 1 / (1.2 * 2^EV100) = 12.5 / (120 L)
+    assert exposure == pytest.approx(12.5 / (120.0 * avg), rel=1e-5)
+    # stopEyeAdaptation: histogram still cleared, luminance kept
+    o.set_tonemapping(hist, 0.25)
+    o.stage(N.STAGE_LUMINANCE_AVG, 0, 0, params(stopEyeAdaptation=1))
+    h, avg, _ = o.tonemapping()
+    assert h.sum() == 0 and avg == 0.25
+
+
+def test_histogram_counts_every_pixel():
+    W, H = 30, 10
+    o = oracle.OracleStream(W, H, oracle.MODE_REF)
+    rng = np.random.default_rng(4)
+    lum = np.exp(rng.normal(0, 3, (H, W))).astype(np.float16)
+    o.plane("HISTOGRAM_INPUT", 0)[...] = lum.view(np.uint16)
+    o.stage(N.STAGE_LUMINANCE_HISTOGRAM, 0, 0, params())
+    h, _, _ = o.tonemapping()
+    ref = np.bincount([oracle.color_bin(float(v), -3.0, 7.0) for v in lum.astype(np.float32).ravel()],
+                      minlength=256)
+    assert np.array_equal(h, ref) and h.sum() == W * H
+
+
+def test_gradient_atrous_constant():
+    W, H = 36, 18
+    o = oracle.OracleStream(W, H, oracle.MODE_REF)
+    o.plane("DIS_PING_GRADIENT", 0)[...] = [100, 50, 200, 0]
+    for i in range(4):
+        o.stage(N.STAGE_GRADIENT_ATROUS, i, 0, params())
+    g = o.plane("DIS_PING_GRADIENT", 0)
+    gw = (W + 1) // 3  # strata inside the render area keep the constant
+    assert np.all(g[:, :gw, :3] == [100, 50, 200])
+    assert np.all(o.plane("DIS_GRADIENT_HISTORY", 0)[..., :3] == [100, 50, 200])
+
+
+def test_composition_writes_every_regular_pixel_once():
+    """getRegularPixFromCheckerboardPix is a bijection: the last a-trous iteration writes every
+    regular pixel of HistogramInput / PreFinal (ShaderCommonGLSLFunc.h:331-342)."""
+    W, H = 24, 7
+    o = oracle.OracleStream(W, H, oracle.MODE_F32)
+    _flat_state(o, W, H, np.array([1.0, 1.0, 1.0], np.float32), 0.0)
+    alb = o.plane("ALBEDO", 0)
+    codes = np.arange(W * H, dtype=np.float32).reshape(H, W) + 1.0
+    for y in range(H):
+        for x in range(W):
+            alb[y, x] = oracle.encode_b10g11r11(float(codes[y, x]), 0.0, 0.0)
+    o.plane("IS_SKY", 0)[...] = 1  # sky: illuminated = albedo * throughput
+    o.plane("THROUGHPUT", 0)[...] = np.float16(1.0).view(np.uint16)
+    o.stage(N.STAGE_ATROUS, 3, 0, params())
+    pre = o.plane("PRE_FINAL", 0)[..., 0]
+    expect = F.decode_b10g11r11(alb)[..., 0]
+    assert np.array_equal(pre, expect)
+
+
+def test_fp64_and_fp32_oracles_agree():
+    W, H = 48, 27
+    sc = Scene(W, H, seed=9)
+    o32 = oracle.OracleStream(W, H, oracle.MODE_F32)
+    o64 = oracle.OracleStream(W, H, oracle.MODE_F64)
+    for f in range(5):
+        fi = f & 1
+        bufs, p = sc.generate(f)
+        for k, v in bufs.items():
+            o32.load(k, fi, v)
+            o64.load(k, fi, v)
+        for o in (o32, o64):
+            o.denoise(fi, p)
+            o.calculate_exposure(fi, p)
+    a = o32.plane("PRE_FINAL", fi)[..., :3].astype(np.float64)
+    b = o64.plane("PRE_FINAL", fi)[..., :3]
+    assert F.psnr(a, b) > 70.0
