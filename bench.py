@@ -1,0 +1,465 @@
+#!/usr/bin/env python
+"""Benchmark of the A-SVGF denoise + luminance-histogram auto-exposure path on GB300.
+
+Workload (one step = one frame through the whole path): 1 stream of 1920x1080, fp16 colour
+and history storage (fp32 moments and variance), gradient sampling + 4 gradient a-trous,
+temporal accumulation, anti-firefly, variance, 5 edge-aware a-trous passes with composition,
+then the 256-bin histogram and eye adaptation. Inputs are a seeded 60-frame synthetic
+sequence (analytic spheres and planes, camera 2 px/frame, a sphere moving 8 px/frame,
+log-normal radiance sigma 1 with 0.1 % fireflies x100), generated before the timed region;
+they stand in for captured frames, which the reference does not ship.
+
+  value    Mpix/s with every frame's G-buffer already resident in HBM (bound to the stream
+           without a copy), device time of K steps with CUDA events;
+  e2e      the same through the C ABI from pinned HOST buffers: every step uploads the frame's
+           G-buffer (rgdn_stream_upload), denoises, computes exposure, and reads PreFinal and
+           the tonemapping state back to the host, synchronised per frame;
+  roofline the dominant kernel's algorithmic bytes / its CUDA-event duration vs measured HBM;
+  cpu_baseline  the CPU oracle (C++ restatement of the reference shaders) on the host cores.
+
+`--impl reference` times the reference's own arithmetic on the host CPU (the oracle: the
+reference's GLSL path cannot run here — no Vulkan or software renderer), per step one frame of
+a 1920x120 band of the same workload, using every host core.
+
+Multi-GPU (`torchrun --nproc-per-node N`): independent replicas, one stream per rank
+(streams shard with no collective); value = all ranks' pixels / max time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Mpix/s + p99 latency, served/batched vs plain A-SVGF on 1 GB300 at rel err≤1e-3"
+STORAGE = {"ref": 0, "fp32": 1, "fp16": 2, "bf16": 3}
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=600)
+    ap.add_argument("--warmup", type=int, default=10)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--width", type=int, default=1920)
+    ap.add_argument("--height", type=int, default=1080)
+    ap.add_argument("--storage", default="fp16", choices=list(STORAGE))
+    ap.add_argument("--iters", type=int, default=5, help="a-trous passes")
+    ap.add_argument("--frames", type=int, default=60, help="distinct frames in the sequence")
+    ap.add_argument("--e2e-steps", type=int, default=120)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+# ------------------------------------------------------------------------------------------
+# distributed helpers (replicas; a barrier and a max-reduction of the timings only)
+# ------------------------------------------------------------------------------------------
+class Dist:
+    def __init__(self):
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.local = int(os.environ.get("LOCAL_RANK", "0"))
+        self.pg = None
+        if self.world > 1:
+            import torch
+            import torch.distributed as dist
+            torch.cuda.set_device(self.local)
+            dist.init_process_group("nccl", device_id=torch.device("cuda", self.local))
+            self.pg = dist
+
+    def barrier(self):
+        if self.pg:
+            self.pg.barrier()
+
+    def max(self, x: float) -> float:
+        if not self.pg:
+            return x
+        import torch
+        t = torch.tensor([x], dtype=torch.float64, device=f"cuda:{self.local}")
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.pg:
+            self.pg.destroy_process_group()
+
+
+# ------------------------------------------------------------------------------------------
+# clocks sampled during the timed region
+# ------------------------------------------------------------------------------------------
+class ClockSampler:
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device, self.samples, self.proc = device, [], None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.device}", f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            threading.Thread(target=self._read, daemon=True).start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 7:
+                self.samples.append(parts)
+
+    def stop(self) -> dict:
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for s in self.samples for i in range(4) if s[3 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.samples)}
+
+
+# ------------------------------------------------------------------------------------------
+# algorithmic bytes per pixel of each kernel (each distinct texel read once, each output
+# written once), from the framebuffer formats of the storage mode
+# ------------------------------------------------------------------------------------------
+def stage_bytes(storage: str) -> dict:
+    col3 = {"ref": 4, "fp32": 16, "fp16": 8, "bf16": 8}[storage]
+    cv = {"ref": 8, "fp32": 16, "fp16": 12, "bf16": 12}[storage]        # colour + variance
+    cv_rgb = {"ref": 8, "fp32": 16, "fp16": 8, "bf16": 8}[storage]      # colour part only
+    mom = {"ref": 4, "fp32": 8, "fp16": 8, "bf16": 8}[storage]
+    hl = {"ref": 8, "fp32": 16, "fp16": 8, "bf16": 8}[storage]
+    fv = {"ref": 2, "fp32": 4, "fp16": 4, "bf16": 4}[storage]
+    pre = {"ref": 4, "fp32": 16, "fp16": 8, "bf16": 8}[storage]
+    g = 1.0 / 9.0  # gradient images are 1/3 x 1/3
+    b = {}
+    # RtGradients image-space part: per stratum 9 motion + 8 GradientInputs_Prev reads, IsSky,
+    # reshaded, IndirAccum_Prev, DISGradientHistory; writes DISPing + prev pix
+    b["gradient_samples"] = 8 + 4 + g * (1 + 8 + col3 + 4 + 1) + g * (4 + 1)
+    b["gradient_atrous"] = g * (4 + 4)
+    # temporal accumulation: cur G-buffer + prev history (bilinear taps counted once) + writes
+    b["temporal_accumulation"] = (12 + 8 + 8 + 2 + 4 + 2 + 16 + g * 4) + \
+        (2 + 4 + cv_rgb + mom + hl + col3 + col3 + 16) + (col3 + mom + hl + col3 + col3)
+    b["anti_firefly"] = 3 * col3 + 3 * col3
+    b["variance_estimation"] = (col3 + 4 + 2 + hl + mom) + cv
+    b["atrous0"] = (cv + 2 * col3 + 2 + 2 + 2 + 4 + hl) + (cv + 2 * col3 + fv)
+    b["atrous"] = (cv + 2 * col3 + 2 + 2 + 2 + 4 + hl + fv) + (cv + 2 * col3)
+    b["atrous_last"] = (cv + 2 * col3 + 2 + 2 + 2 + 4 + hl + fv) + (4 + 8 + 1) + (pre + 2)
+    b["luminance_histogram"] = 2
+    b["luminance_avg"] = 0
+    return b
+
+
+def kernel_bytes(name: str, it: int, niter: int, per_px: dict) -> float:
+    if name == "atrous":
+        return per_px["atrous0"] if it == 0 else per_px["atrous_last"] if it == niter - 1 else per_px["atrous"]
+    return per_px[name]
+
+
+def load_peaks() -> tuple[float, str]:
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def profile_traffic(kernel: str):
+    """DRAM bytes per launch of the dominant kernel from the committed ncu summary, if any."""
+    path = os.path.join(ROOT, "profiles", "dram_traffic.md")
+    try:
+        for line in open(path):
+            cells = [c.strip() for c in line.strip().strip("|").split("|")]
+            if len(cells) >= 3 and cells[0] == kernel:
+                return float(cells[2])
+    except Exception:
+        pass
+    return None
+
+
+# ------------------------------------------------------------------------------------------
+# CPU oracle timing (cpu_baseline in our line; the whole reference arm)
+# ------------------------------------------------------------------------------------------
+def oracle_time(width: int, height: int, storage: str, iters: int, frames: int, seed: int = 1):
+    """Runs `frames` frames of the oracle (all host cores); returns seconds of the last frame."""
+    import oracle
+    from raytracedgl1_gb300.scene import Scene
+    sc = Scene(width, height, seed=seed)
+    o = oracle.OracleStream(width, height, STORAGE[storage])
+    nthreads = os.cpu_count() or 1
+    last = None
+    for f in range(frames):
+        fi = f & 1
+        bufs, p = sc.generate(f)
+        p.atrousIterations = iters
+        for k, v in bufs.items():
+            o.load(k, fi, v)
+        t0 = time.perf_counter()
+        o.denoise(fi, p, nthreads)
+        o.calculate_exposure(fi, p, nthreads)
+        last = time.perf_counter() - t0
+    return last, nthreads
+
+
+def run_reference(args, dist: Dist):
+    if dist.rank != 0:
+        return
+    from raytracedgl1_gb300 import build
+    build.build_oracle()
+    build.build_scene()
+    import oracle
+    from raytracedgl1_gb300.scene import Scene
+    W, H = args.width, min(120, args.height)
+    sc = Scene(W, H, seed=1)
+    o = oracle.OracleStream(W, H, STORAGE[args.storage])
+    nthreads = os.cpu_count() or 1
+    frames = [sc.generate(f) for f in range(min(args.frames, 8))]
+    times = []
+    for step in range(args.warmup + args.steps):
+        f = step % len(frames)
+        fi = step & 1
+        bufs, p = frames[f]
+        p.atrousIterations = args.iters
+        for k, v in bufs.items():
+            o.load(k, fi, v)
+        t0 = time.perf_counter()
+        o.denoise(fi, p, nthreads)
+        o.calculate_exposure(fi, p, nthreads)
+        dt = time.perf_counter() - t0
+        if step >= args.warmup:
+            times.append(dt)
+    total = sum(times)
+    mpix = W * H * len(times) / total / 1e6
+    times.sort()
+    line = {
+        "impl": "reference", "metric": METRIC, "value": round(mpix, 4), "unit": "Mpix/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(1e3 * total / len(times), 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "p50_ms": round(1e3 * times[len(times) // 2], 3), "p99_ms": round(1e3 * times[int(0.99 * (len(times) - 1))], 3),
+        "config": config_dict(args),
+        "cpu_baseline": {"value": round(mpix, 4), "unit": "Mpix/s", "cores": nthreads, "kind": "port",
+                         "sample": f"one frame of a {W}x{H} band of the workload per step (same per-pixel work)"},
+        "e2e": {"value": round(mpix, 4), "unit": "Mpix/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "reference GLSL/Vulkan path unavailable on this box (no graphics stack); the CPU "
+                "restatement of its shaders (oracle/) is the reference's implementation timed here",
+    }
+    print(json.dumps(line), flush=True)
+
+
+def config_dict(args) -> dict:
+    return {"workload": f"A-SVGF denoise + auto-exposure, 1 stream {args.width}x{args.height}, "
+                        f"{args.storage} storage, {args.iters} a-trous passes + gradient a-trous, "
+                        f"{args.frames}-frame synthetic sequence",
+            "streams_per_gpu": 1, "width": args.width, "height": args.height, "storage": args.storage,
+            "atrous_iterations": args.iters, "frames": args.frames,
+            "l2": "inputs larger than L2: each step touches its own frame's G-buffer (>160 MB) and the "
+                  "stream's history (>500 MB), both above the 129 MB L2"}
+
+
+# ------------------------------------------------------------------------------------------
+# our arm
+# ------------------------------------------------------------------------------------------
+def run_ours(args, dist: Dist):
+    import numpy as np
+    import torch
+
+    from raytracedgl1_gb300 import _native as N
+    from raytracedgl1_gb300 import build
+    from raytracedgl1_gb300.denoiser import Context, Denoiser, Stream, Tonemapping
+    from raytracedgl1_gb300.scene import Scene
+
+    build.build_all()
+    dev = dist.local
+    torch.cuda.set_device(dev)
+    W, H = args.width, args.height
+    storage = STORAGE[args.storage]
+    ctx = Context(dev)
+    st = Stream(ctx, W, H, storage)
+    cs = torch.cuda.Stream(device=dev)
+    sc = Scene(W, H, seed=1 + dist.rank)
+
+    # --- the frame sequence, resident in HBM -------------------------------------------
+    frames = []
+    host_frames = []
+    for f in range(args.frames):
+        bufs, p = sc.generate(f)
+        p.atrousIterations = args.iters
+        dev_bufs = {}
+        for name, arr in bufs.items():
+            t = torch.from_numpy(np.ascontiguousarray(arr).view(np.uint8).reshape(-1)).to(f"cuda:{dev}")
+            dev_bufs[name] = t
+        frames.append((dev_bufs, p))
+        if f < 8:
+            host_frames.append((bufs, p))
+    torch.cuda.synchronize()
+    gbytes_per_frame = sum(t.numel() for t in frames[0][0].values())
+
+    den, tm = Denoiser(st), Tonemapping(st)
+
+    def step(k: int):
+        f = k % len(frames)
+        fi = k & 1
+        bufs, p = frames[f]
+        for name, t in bufs.items():
+            st.bind(name, fi, t.data_ptr())
+        den.Denoise(fi, p, cs)
+        tm.CalculateExposure(fi, p, cs)
+
+    with torch.cuda.stream(cs):
+        for k in range(args.warmup):
+            step(k)
+    cs.synchronize()
+
+    clocks = ClockSampler(dev)
+    clocks.start()
+    time.sleep(0.3)
+    launches0 = ctx.launch_count()
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
+    dist.barrier()
+    torch.cuda.synchronize()
+    with torch.cuda.stream(cs):
+        ev[0].record(cs)
+        for k in range(args.steps):
+            step(args.warmup + k)
+            ev[k + 1].record(cs)
+    cs.synchronize()
+    torch.cuda.synchronize()
+    dist.barrier()
+    launches = ctx.launch_count() - launches0
+    total_ms = ev[0].elapsed_time(ev[-1])
+    step_ms = sorted(ev[k].elapsed_time(ev[k + 1]) for k in range(args.steps))
+    clk = clocks.stop()
+    total_ms_max = dist.max(total_ms)
+    pixels = W * H * args.steps * dist.world
+    value = pixels / (total_ms_max / 1e3) / 1e6
+
+    # --- per-kernel durations over the same steps (library-side events) ------------------
+    st.set_timing(True)
+    with torch.cuda.stream(cs):
+        for k in range(args.steps):
+            step(args.warmup + args.steps + k)
+    cs.synchronize()
+    timing = st.read_timing()
+    st.set_timing(False)
+    per_px = stage_bytes(args.storage)
+    kern = []
+    for (name, it), (n, ms) in timing.items():
+        alg = kernel_bytes(name, it, args.iters, per_px) * W * H
+        kern.append({"kernel": f"{name}[{it}]", "launches": n, "avg_us": 1e3 * ms / n,
+                     "alg_bytes": alg, "gbs": alg / (ms / n / 1e3) / 1e9})
+    kern.sort(key=lambda d: -d["avg_us"] * d["launches"])
+    kernel_total_us = sum(d["avg_us"] * d["launches"] for d in kern) / args.steps
+    top = kern[0]
+    peak, peak_kind = load_peaks()
+
+    # --- end to end from pinned host buffers through the C ABI ----------------------------
+    pinned = []
+    for bufs, p in host_frames:
+        hb = {}
+        for name, arr in bufs.items():
+            t = torch.from_numpy(np.ascontiguousarray(arr).view(np.uint8).reshape(-1)).pin_memory()
+            hb[name] = t
+        pinned.append((hb, p))
+    pre_img = st.image("PRE_FINAL", 0)
+    pre_bytes = pre_img.pitch_bytes * pre_img.height
+    out_host = torch.empty(pre_bytes, dtype=torch.uint8).pin_memory()
+    for name in N.GBUFFER:
+        st.bind(name, 0, None)
+        st.bind(name, 1, None)
+    h2d = sum(t.numel() for t in pinned[0][0].values())
+    d2h = pre_bytes + 256 * 4 + 4
+
+    def e2e_step(k: int):
+        f = k % len(pinned)
+        fi = k & 1
+        hb, p = pinned[f]
+        for name, t in hb.items():
+            st.upload(name, fi, (t.data_ptr(), t.numel()), cs)
+        den.Denoise(fi, p, cs)
+        tm.CalculateExposure(fi, p, cs)
+        N.check(st.lib.rgdn_stream_download(st.handle, N.FB["PRE_FINAL"], fi, out_host.data_ptr(), pre_bytes,
+                                            cs.cuda_stream))
+        return st.tonemapping(cs)   # synchronous read of histogram + avgLuminance + exposure
+
+    for k in range(4):
+        e2e_step(k)
+    dist.barrier()
+    lat = []
+    t0 = time.perf_counter()
+    for k in range(args.e2e_steps):
+        a = time.perf_counter()
+        e2e_step(k)
+        lat.append(time.perf_counter() - a)
+    e2e_s = dist.max(time.perf_counter() - t0)
+    e2e_value = W * H * args.e2e_steps * dist.world / e2e_s / 1e6
+    lat.sort()
+
+    # --- CPU baseline (rank 0, N=1) --------------------------------------------------------
+    cpu = None
+    if dist.rank == 0 and dist.world == 1 and not args.no_cpu_baseline:
+        sec, threads = oracle_time(W, H, args.storage, args.iters, 2)
+        cpu = {"value": round(W * H / sec / 1e6, 4), "unit": "Mpix/s", "cores": threads, "kind": "port",
+               "sample": f"frame 2 of the {W}x{H} sequence through the CPU oracle (frame 1 untimed)"}
+
+    st.close()
+    ctx.close()
+    if dist.rank != 0:
+        return
+    line = {
+        "metric": METRIC, "value": round(value, 2), "unit": "Mpix/s", "n_gpus": dist.world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(total_ms_max / args.steps, 4),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic (seeded analytic scene; see bench.py docstring)",
+        "p50_ms": round(step_ms[len(step_ms) // 2], 4), "p99_ms": round(step_ms[int(0.99 * (len(step_ms) - 1))], 4),
+        "config": config_dict(args),
+        "gpu_launches": int(launches),
+        "roofline": {"bound": "hbm", "kernel": top["kernel"], "achieved": round(top["gbs"], 1),
+                     "peak": peak, "unit": "GB/s", "frac": round(top["gbs"] / peak, 4),
+                     "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else "fallback",
+                     "traffic": profile_traffic(top["kernel"]),
+                     "alg_bytes_per_launch": top["alg_bytes"]},
+        "kernels": [{k: (round(v, 2) if isinstance(v, float) else v) for k, v in d.items()} for d in kern],
+        "kernel_sum_us_per_step": round(kernel_total_us, 2),
+        "path_alg_gbs": round(sum(d["alg_bytes"] * d["launches"] for d in kern) / args.steps /
+                              (total_ms_max / args.steps / 1e3) / 1e9, 1),
+        "e2e": {"value": round(e2e_value, 2), "unit": "Mpix/s", "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h), "p50_ms": round(1e3 * lat[len(lat) // 2], 3),
+                "p99_ms": round(1e3 * lat[int(0.99 * (len(lat) - 1))], 3), "steps": args.e2e_steps},
+        "clocks": clk,
+        "cpu_baseline": cpu,
+        "gbuffer_bytes_per_frame": int(gbytes_per_frame),
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    dist = Dist()
+    try:
+        if args.impl == "reference":
+            run_reference(args, dist)
+        else:
+            run_ours(args, dist)
+    finally:
+        dist.close()
+
+
+if __name__ == "__main__":
+    main()

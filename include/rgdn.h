@@ -240,6 +240,12 @@ rgdn_status rgdn_stream_required_bytes( const rgdn_stream_create_info* info, uin
 /* Framebuffers::GetImageHandles (Framebuffers.cpp:34-49): the plane of `fb` that
  * frameIndex (0 or 1) selects. A producer writes the G-buffer there directly. */
 rgdn_status rgdn_stream_get_framebuffer( rgdn_stream* stream, uint32_t fb, uint32_t frameIndex, rgdn_image* outImage );
+/* Points a producer-written G-buffer image (RGDN_FB_ALBEDO .. RGDN_FB_GRADIENT_RESHADED) of
+ * slot frameIndex at caller-owned device memory (dense rows, 16-byte aligned), so a renderer
+ * that already holds its G-buffer in HBM hands it over without a copy — the role of the
+ * reference's shared Framebuffers images (PathTracer writes, Denoiser reads). NULL restores
+ * the stream's own plane. The memory must stay valid while work using it is in flight. */
+rgdn_status rgdn_stream_bind_framebuffer( rgdn_stream* stream, uint32_t fb, uint32_t frameIndex, void* devicePtr );
 /* Copies `bytes` (== pitch*height) into / out of a framebuffer plane; `src`/`dst` may be
  * host (pageable or pinned) or device memory. Enqueued on cudaStream. */
 rgdn_status rgdn_stream_upload( rgdn_stream* stream, uint32_t fb, uint32_t frameIndex, const void* src, size_t bytes, rgdn_cuda_stream cudaStream );
@@ -278,6 +284,21 @@ typedef struct rgdn_job
  * and sizes, with one launch per stage covering all of them. Streams of one batch must
  * be distinct and share one storage mode. */
 rgdn_status rgdn_submit_batch( rgdn_context* ctx, const rgdn_job* jobs, uint32_t n, rgdn_cuda_stream cudaStream );
+
+/* ---- per-kernel timing (tracing) ----------------------------------------------------- */
+/* With timing on, every kernel the stream launches is bracketed by two CUDA events on the
+ * launching stream. rgdn_stream_read_timing waits for them and returns, per (stage,
+ * iteration), the launches and the summed device time since the last read. The reference
+ * only labels its dispatches (CmdLabel, Source/Denoiser.cpp:90-205); this is the timed form. */
+typedef struct rgdn_stage_timing
+{
+    uint32_t stage;       /* rgdn_stage */
+    uint32_t iteration;
+    uint32_t launches;
+    float    totalMs;
+} rgdn_stage_timing;
+rgdn_status rgdn_stream_set_timing( rgdn_stream* stream, uint32_t enable );
+rgdn_status rgdn_stream_read_timing( rgdn_stream* stream, rgdn_stage_timing* out, uint32_t capacity, uint32_t* outCount );
 
 /* ---- misc -------------------------------------------------------------------------- */
 /* getColorBin (CmLuminanceHistogram.comp:41-54) for every fp16 bit pattern of the

@@ -82,6 +82,11 @@ class StreamCreateInfo(C.Structure):
     _fields_ = [("width", C.c_uint32), ("height", C.c_uint32), ("storage", C.c_uint32)]
 
 
+class StageTiming(C.Structure):
+    _fields_ = [("stage", C.c_uint32), ("iteration", C.c_uint32), ("launches", C.c_uint32),
+                ("totalMs", C.c_float)]
+
+
 class Job(C.Structure):
     _fields_ = [("stream", C.c_void_p), ("frameIndex", C.c_uint32), ("params", C.POINTER(FrameParams))]
 
@@ -98,6 +103,7 @@ SIGNATURES = [
     ("rgdn_stream_resize", _I, [_VP, _U32, _U32]),
     ("rgdn_stream_required_bytes", _I, [C.POINTER(StreamCreateInfo), C.POINTER(_U64)]),
     ("rgdn_stream_get_framebuffer", _I, [_VP, _U32, _U32, C.POINTER(Image)]),
+    ("rgdn_stream_bind_framebuffer", _I, [_VP, _U32, _U32, _VP]),
     ("rgdn_stream_upload", _I, [_VP, _U32, _U32, _VP, _SZ, _VP]),
     ("rgdn_stream_download", _I, [_VP, _U32, _U32, _VP, _SZ, _VP]),
     ("rgdn_denoise", _I, [_VP, _U32, _PFP, _VP]),
@@ -111,7 +117,12 @@ SIGNATURES = [
     ("rgdn_context_launch_count", _I, [_VP, C.POINTER(_U64)]),
     ("rgdn_api_version", _U32, []),
     ("rgdn_histogram_bin_table", _I, [C.c_float, C.c_float, C.POINTER(C.c_uint8)]),
+    ("rgdn_stream_set_timing", _I, [_VP, _U32]),
+    ("rgdn_stream_read_timing", _I, [_VP, C.POINTER(StageTiming), _U32, C.POINTER(_U32)]),
 ]
+
+STAGE_NAMES = ["gradient_samples", "gradient_atrous", "temporal_accumulation", "anti_firefly",
+               "variance_estimation", "atrous", "luminance_histogram", "luminance_avg"]
 
 _lib = None
 

@@ -13,8 +13,10 @@
 #include <cstdio>
 #include <cstring>
 #include <mutex>
+#include <map>
 #include <new>
 #include <set>
+#include <utility>
 #include <vector>
 
 #include "rgdn_codec.h"
@@ -160,7 +162,8 @@ struct rgdn_context
 
 struct PlaneSlot
 {
-    uint8_t* ptr[ 2 ] = { nullptr, nullptr };
+    uint8_t* ptr[ 2 ] = { nullptr, nullptr };   // in use (own plane or a bound caller plane)
+    uint8_t* own[ 2 ] = { nullptr, nullptr };   // the stream's own planes
     uint32_t w = 0, h = 0, texel = 0, format = 0;
     bool     prev = false;
 };
@@ -176,7 +179,16 @@ struct rgdn_stream
     uint8_t*               binLut = nullptr;
     float                  lutMin = NAN, lutMax = NAN;
     std::vector< uint8_t > hostLut;
-    uint32_t               magic = 0x52474453u;
+    // per-kernel timing
+    struct Pending
+    {
+        int         stage, iter;
+        cudaEvent_t a, b;
+    };
+    bool                        timing = false;
+    std::vector< Pending >      pending;
+    std::vector< cudaEvent_t >  eventPool;
+    uint32_t                    magic = 0x52474453u;
 };
 
 namespace
@@ -205,7 +217,7 @@ size_t stream_layout( uint32_t W, uint32_t H, uint32_t storage, PlaneSlot* plane
         size_t   sz = (size_t)w * h * texel;
         for( int s = 0; s < ( d.prev ? 2 : 1 ); s++ )
         {
-            if( planes ) planes[ fb ].ptr[ s ] = base ? base + off : nullptr;
+            if( planes ) planes[ fb ].ptr[ s ] = planes[ fb ].own[ s ] = base ? base + off : nullptr;
             off += align_up( sz );
         }
         if( planes )
@@ -319,12 +331,38 @@ void fill_args( rgdn_stream* s, uint32_t fi, const rgdn_frame_params* p, FrameAr
     a.thetaTab = s->ctx->thetaTab;
 }
 
+cudaEvent_t take_event( rgdn_stream* s )
+{
+    if( !s->eventPool.empty() )
+    {
+        cudaEvent_t e = s->eventPool.back();
+        s->eventPool.pop_back();
+        return e;
+    }
+    cudaEvent_t e = nullptr;
+    if( cudaEventCreate( &e ) != cudaSuccess ) return nullptr;
+    return e;
+}
+
 rgdn_status launch( rgdn_stream* s, const FrameArgs& a, int stage, int iter, cudaStream_t cs )
 {
     StageLauncher L = launcher_for( s->storage );
     if( !L ) return RGDN_INTERNAL_ERROR;
+    cudaEvent_t ea = nullptr, eb = nullptr;
+    if( s->timing )
+    {
+        ea = take_event( s );
+        eb = take_event( s );
+        if( !ea || !eb ) return RGDN_DEVICE_ERROR;
+        cudaEventRecord( ea, cs );
+    }
     cudaError_t e = L( a, stage, iter, cs );
     s->ctx->launches.fetch_add( 1, std::memory_order_relaxed );
+    if( s->timing )
+    {
+        cudaEventRecord( eb, cs );
+        s->pending.push_back( { stage, iter, ea, eb } );
+    }
     return cuda_status( e );
 }
 
@@ -553,6 +591,12 @@ rgdn_status rgdn_stream_destroy( rgdn_stream* s )
     cudaSetDevice( s->ctx->device );
     cudaDeviceSynchronize();
     stream_free( s );
+    for( auto& pd : s->pending )
+    {
+        cudaEventDestroy( pd.a );
+        cudaEventDestroy( pd.b );
+    }
+    for( cudaEvent_t e : s->eventPool ) cudaEventDestroy( e );
     {
         std::lock_guard< std::mutex > g( s->ctx->mtx );
         s->ctx->streams.erase( s );
@@ -594,6 +638,16 @@ rgdn_status rgdn_stream_get_framebuffer( rgdn_stream* s, uint32_t fb, uint32_t f
     out->texel_bytes = p.texel;
     out->format      = p.format;
     out->has_prev    = p.prev ? 1u : 0u;
+    return RGDN_SUCCESS;
+}
+
+rgdn_status rgdn_stream_bind_framebuffer( rgdn_stream* s, uint32_t fb, uint32_t frameIndex, void* devicePtr )
+{
+    if( !valid_stream( s ) ) return RGDN_WRONG_INSTANCE;
+    if( fb > RGDN_FB_GRADIENT_RESHADED || frameIndex > 1 || ( (uintptr_t)devicePtr & 15u ) ) return RGDN_WRONG_FUNCTION_ARGUMENT;
+    PlaneSlot& p    = s->planes[ fb ];
+    const int  slot = p.prev ? (int)frameIndex : 0;
+    p.ptr[ slot ]   = devicePtr ? (uint8_t*)devicePtr : p.own[ slot ];
     return RGDN_SUCCESS;
 }
 
@@ -652,6 +706,41 @@ rgdn_status rgdn_denoise_stage( rgdn_stream* s, uint32_t stage, uint32_t iterati
     FrameArgs a;
     fill_args( s, frameIndex, p, a );
     return launch( s, a, (int)stage, (int)iteration, (cudaStream_t)cs );
+}
+
+rgdn_status rgdn_stream_set_timing( rgdn_stream* s, uint32_t enable )
+{
+    if( !valid_stream( s ) ) return RGDN_WRONG_INSTANCE;
+    s->timing = enable != 0;
+    return RGDN_SUCCESS;
+}
+
+rgdn_status rgdn_stream_read_timing( rgdn_stream* s, rgdn_stage_timing* out, uint32_t capacity, uint32_t* outCount )
+{
+    if( !valid_stream( s ) ) return RGDN_WRONG_INSTANCE;
+    if( !outCount || ( capacity && !out ) ) return RGDN_WRONG_FUNCTION_ARGUMENT;
+    cudaSetDevice( s->ctx->device );
+    std::map< std::pair< int, int >, std::pair< uint32_t, double > > agg;
+    rgdn_status r = RGDN_SUCCESS;
+    for( auto& pd : s->pending )
+    {
+        float ms = 0.0f;
+        if( cudaEventSynchronize( pd.b ) != cudaSuccess || cudaEventElapsedTime( &ms, pd.a, pd.b ) != cudaSuccess ) r = RGDN_DEVICE_ERROR;
+        auto& slot = agg[ { pd.stage, pd.iter } ];
+        slot.first++;
+        slot.second += ms;
+        s->eventPool.push_back( pd.a );
+        s->eventPool.push_back( pd.b );
+    }
+    s->pending.clear();
+    uint32_t n = 0;
+    for( auto& kv : agg )
+    {
+        if( n < capacity ) out[ n ] = { (uint32_t)kv.first.first, (uint32_t)kv.first.second, kv.second.first, (float)kv.second.second };
+        n++;
+    }
+    *outCount = n;
+    return r;
 }
 
 rgdn_status rgdn_stream_tonemapping_device( rgdn_stream* s, void** out )

@@ -137,6 +137,13 @@ class Stream:
                 "rgdn_stream_get_framebuffer")
         return img
 
+    def bind(self, fb, frame_index: int, device_ptr: int | None) -> None:
+        """Zero-copy: the G-buffer image `fb` of slot frame_index reads caller device memory."""
+        fbi = N.FB[fb] if isinstance(fb, str) else fb
+        N.check(self.lib.rgdn_stream_bind_framebuffer(self.handle, fbi, frame_index,
+                                                      C.c_void_p(device_ptr) if device_ptr else None),
+                f"bind {fb}")
+
     def upload(self, fb, frame_index: int, src, cuda_stream=None) -> None:
         """src: a numpy array (host) or an (int device pointer, nbytes) pair."""
         fbi = N.FB[fb] if isinstance(fb, str) else fb
@@ -185,6 +192,18 @@ class Stream:
         p = C.c_void_p()
         N.check(self.lib.rgdn_stream_tonemapping_device(self.handle, C.byref(p)))
         return p.value
+
+    # --- per-kernel timing ----------------------------------------------------------------
+    def set_timing(self, enable: bool) -> None:
+        N.check(self.lib.rgdn_stream_set_timing(self.handle, 1 if enable else 0))
+
+    def read_timing(self) -> dict:
+        """{(stage name, iteration): (launches, total ms)} since the last read."""
+        cap = 64
+        buf = (N.StageTiming * cap)()
+        n = C.c_uint32()
+        N.check(self.lib.rgdn_stream_read_timing(self.handle, buf, cap, C.byref(n)), "rgdn_stream_read_timing")
+        return {(N.STAGE_NAMES[t.stage], t.iteration): (t.launches, t.totalMs) for t in buf[:min(n.value, cap)]}
 
     # --- stages --------------------------------------------------------------------------
     def stage(self, stage: int, iteration: int, frame_index: int, params: N.FrameParams,

@@ -66,7 +66,10 @@ def compare_state(s: Stream, o: oracle.OracleStream, what: str, max_diff_frac: f
         frac = ndiff / err.size
         worst.append((name, slot, float(err.max()), frac))
         assert err.max() <= tol, f"{what}: {name}[{slot}] max texel rel err {err.max():.3e} > {tol:.3e}"
-        assert frac <= max_diff_frac, f"{what}: {name}[{slot}] {frac:.2%} of texels differ"
+        if fmt not in (F.F_R32F, F.F_RG32F, F.F_RGBA32F):
+            # quantised planes: ulp-level differences of the transcendentals flip a stored
+            # quantum only rarely; fp32 planes are held to the 1e-3 relative bar alone
+            assert frac <= max_diff_frac, f"{what}: {name}[{slot}] {frac:.2%} of texels differ"
     return worst
 
 
