@@ -54,6 +54,8 @@ def parse():
     ap.add_argument("--iters", type=int, default=5, help="a-trous passes")
     ap.add_argument("--frames", type=int, default=60, help="distinct frames in the sequence")
     ap.add_argument("--e2e-steps", type=int, default=120)
+    ap.add_argument("--path", default="fused", choices=["fused", "plain"],
+                    help="fused: the default kernels; plain: one kernel per reference dispatch")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     return ap.parse_args()
 
@@ -163,11 +165,15 @@ def stage_bytes(storage: str) -> dict:
     b["atrous_last"] = (cv + 2 * col3 + 2 + 2 + 2 + 4 + hl + fv) + (4 + 8 + 1) + (pre + 2)
     b["luminance_histogram"] = 2
     b["luminance_avg"] = 0
+    # fused kernels
+    b["gradient_fused"] = b["gradient_samples"] + 4 * b["gradient_atrous"]
+    b["temporal_fast"] = b["temporal_accumulation"]
+    b["af_variance"] = b["af_variance_fast"] = 3 * col3 + (2 + 4 + hl + mom) + 2 * col3 + cv
     return b
 
 
 def kernel_bytes(name: str, it: int, niter: int, per_px: dict) -> float:
-    if name == "atrous":
+    if name in ("atrous", "atrous_fast", "atrous_fast_hist", "atrous_exact_hist"):
         return per_px["atrous0"] if it == 0 else per_px["atrous_last"] if it == niter - 1 else per_px["atrous"]
     return per_px[name]
 
@@ -267,6 +273,7 @@ def config_dict(args) -> dict:
     return {"workload": f"A-SVGF denoise + auto-exposure, 1 stream {args.width}x{args.height}, "
                         f"{args.storage} storage, {args.iters} a-trous passes + gradient a-trous, "
                         f"{args.frames}-frame synthetic sequence",
+            "path": getattr(args, "path", "fused"),
             "streams_per_gpu": 1, "width": args.width, "height": args.height, "storage": args.storage,
             "atrous_iterations": args.iters, "frames": args.frames,
             "l2": "inputs larger than L2: each step touches its own frame's G-buffer (>160 MB) and the "
@@ -301,6 +308,8 @@ def run_ours(args, dist: Dist):
     for f in range(args.frames):
         bufs, p = sc.generate(f)
         p.atrousIterations = args.iters
+        if args.path == "plain":
+            p.flags |= N.FLAG_PLAIN
         dev_bufs = {}
         for name, arr in bufs.items():
             t = torch.from_numpy(np.ascontiguousarray(arr).view(np.uint8).reshape(-1)).to(f"cuda:{dev}")

@@ -179,8 +179,11 @@ typedef struct rgdn_frame_params
 } rgdn_frame_params;
 
 /* rgdn_frame_params.flags */
-#define RGDN_FLAG_PLAIN              0x1u /* one kernel per reference dispatch (no fusion) */
+#define RGDN_FLAG_PLAIN              0x1u /* one kernel per reference dispatch, IEEE math (no fusion) */
 #define RGDN_FLAG_SKIP_GRADIENTS     0x2u /* GRADIENT_ESTIMATION_ENABLED == 0 behaviour */
+#define RGDN_FLAG_EXACT_MATH         0x4u /* fused kernels, but the plain path's IEEE math: the same
+                                             results as RGDN_FLAG_PLAIN bit for bit (the default
+                                             path uses hardware exp2/log2 for continuous weights) */
 
 /* debugShowFlags bits used on this path (ShaderCommonC.h:156-166) */
 #define RGDN_DEBUG_SHOW_FLAG_ONLY_DIRECT_DIFFUSE   ( 1u << 5 )

@@ -45,7 +45,7 @@ STAGE_GRADIENT_SAMPLES, STAGE_GRADIENT_ATROUS, STAGE_TEMPORAL_ACCUMULATION = 0, 
 STAGE_ANTI_FIREFLY, STAGE_VARIANCE_ESTIMATION, STAGE_ATROUS = 3, 4, 5
 STAGE_LUMINANCE_HISTOGRAM, STAGE_LUMINANCE_AVG = 6, 7
 
-FLAG_PLAIN, FLAG_SKIP_GRADIENTS = 0x1, 0x2
+FLAG_PLAIN, FLAG_SKIP_GRADIENTS, FLAG_EXACT_MATH = 0x1, 0x2, 0x4
 
 
 class FrameParams(C.Structure):
@@ -123,6 +123,11 @@ SIGNATURES = [
 
 STAGE_NAMES = ["gradient_samples", "gradient_atrous", "temporal_accumulation", "anti_firefly",
                "variance_estimation", "atrous", "luminance_histogram", "luminance_avg"]
+# kernels of the default fused path (ids above the rgdn_stage range, see rgdn_internal.h)
+KERNEL_NAMES = dict(enumerate(STAGE_NAMES))
+KERNEL_NAMES.update({100: "atrous_fast", 101: "atrous_fast_hist", 102: "temporal_fast",
+                     103: "af_variance", 104: "af_variance_fast", 105: "gradient_fused",
+                     106: "atrous_exact_hist"})
 
 _lib = None
 

@@ -186,6 +186,7 @@ struct rgdn_stream
         cudaEvent_t a, b;
     };
     bool                        timing = false;
+    bool                        histPending = false;   // a fused denoise accumulated this frame's histogram
     std::vector< Pending >      pending;
     std::vector< cudaEvent_t >  eventPool;
     uint32_t                    magic = 0x52474453u;
@@ -380,8 +381,11 @@ rgdn_status ensure_bin_lut( rgdn_stream* s, const rgdn_frame_params* p, cudaStre
     return RGDN_SUCCESS;
 }
 
+rgdn_status run_denoise_fused( rgdn_stream* s, uint32_t fi, const rgdn_frame_params* p, cudaStream_t cs );
+
 rgdn_status run_denoise( rgdn_stream* s, uint32_t fi, const rgdn_frame_params* p, cudaStream_t cs )
 {
+    if( !( p->flags & RGDN_FLAG_PLAIN ) ) return run_denoise_fused( s, fi, p, cs );
     FrameArgs a;
     fill_args( s, fi, p, a );
     rgdn_status r;
@@ -399,13 +403,41 @@ rgdn_status run_denoise( rgdn_stream* s, uint32_t fi, const rgdn_frame_params* p
     return RGDN_SUCCESS;
 }
 
+// Default path: gradient chain in one cooperative launch, temporal accumulation, anti-firefly
+// fused with variance (DiffAccumColor is not materialised: nothing reads it after the
+// variance), the a-trous iterations, and the histogram accumulated by the last iteration
+// (HistogramInput is still written). Continuous weights use FAST math.
+rgdn_status run_denoise_fused( rgdn_stream* s, uint32_t fi, const rgdn_frame_params* p, cudaStream_t cs )
+{
+    rgdn_status r = ensure_bin_lut( s, p, cs );
+    if( r != RGDN_SUCCESS ) return r;
+    FrameArgs a;
+    fill_args( s, fi, p, a );
+    const bool exact = ( p->flags & RGDN_FLAG_EXACT_MATH ) != 0;
+    if( !( p->flags & RGDN_FLAG_SKIP_GRADIENTS ) && ( r = launch( s, a, KF_GRADIENT_FUSED, 0, cs ) ) != RGDN_SUCCESS ) return r;
+    if( ( r = launch( s, a, exact ? (int)RGDN_STAGE_TEMPORAL_ACCUMULATION : (int)KF_TEMPORAL_FAST, 0, cs ) ) != RGDN_SUCCESS ) return r;
+    if( ( r = launch( s, a, exact ? KF_AF_VARIANCE : KF_AF_VARIANCE_FAST, 0, cs ) ) != RGDN_SUCCESS ) return r;
+    // a histogram no exposure pass consumed is discarded: this frame's replaces it
+    if( s->histPending && cudaMemsetAsync( s->tm->histogram, 0, sizeof( s->tm->histogram ), cs ) != cudaSuccess )
+        return RGDN_DEVICE_ERROR;
+    for( uint32_t i = 0; i < a.u.niter; i++ )
+    {
+        const bool last = i + 1 == a.u.niter;
+        const int k = exact ? ( last ? KF_ATROUS_EXACT_HIST : (int)RGDN_STAGE_ATROUS ) : ( last ? KF_ATROUS_FAST_HIST : KF_ATROUS_FAST );
+        if( ( r = launch( s, a, k, (int)i, cs ) ) != RGDN_SUCCESS ) return r;
+    }
+    s->histPending = true;
+    return RGDN_SUCCESS;
+}
+
 rgdn_status run_exposure( rgdn_stream* s, uint32_t fi, const rgdn_frame_params* p, cudaStream_t cs )
 {
     rgdn_status r = ensure_bin_lut( s, p, cs );
     if( r != RGDN_SUCCESS ) return r;
     FrameArgs a;
     fill_args( s, fi, p, a );
-    if( ( r = launch( s, a, RGDN_STAGE_LUMINANCE_HISTOGRAM, 0, cs ) ) != RGDN_SUCCESS ) return r;
+    if( !s->histPending && ( r = launch( s, a, RGDN_STAGE_LUMINANCE_HISTOGRAM, 0, cs ) ) != RGDN_SUCCESS ) return r;
+    s->histPending = false;
     return launch( s, a, RGDN_STAGE_LUMINANCE_AVG, 0, cs );
 }
 

@@ -111,6 +111,18 @@ struct FrameArgs
     const float2* thetaTab;
 };
 
+// Kernels of the default (fused, fast-math) path, beyond the per-stage rgdn_stage ids.
+enum FusedKernel : int
+{
+    KF_ATROUS_FAST      = 100,   // a-trous iteration with FAST weights
+    KF_ATROUS_FAST_HIST = 101,   // last iteration + composition + fused histogram
+    KF_TEMPORAL_FAST    = 102,   // temporal accumulation, FAST specular weights
+    KF_AF_VARIANCE      = 103,   // anti-firefly + variance in one kernel
+    KF_AF_VARIANCE_FAST = 104,
+    KF_GRADIENT_FUSED   = 105,   // gradient samples + 4 gradient a-trous, one cooperative launch
+    KF_ATROUS_EXACT_HIST = 106,  // last iteration + fused histogram, IEEE math
+};
+
 // Launches one stage for one frame. Returns the CUDA error of the launch.
 typedef cudaError_t ( *StageLauncher )( const FrameArgs& a, int stage, int iter, cudaStream_t s );
 

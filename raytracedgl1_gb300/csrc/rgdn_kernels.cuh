@@ -11,6 +11,7 @@
 // threads map x -> threadIdx.x so that a warp reads 32 consecutive texels of a row.
 #pragma once
 
+#include <cooperative_groups.h>
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
 
@@ -21,6 +22,7 @@ namespace rgdn
 {
 namespace dev
 {
+namespace cg = cooperative_groups;
 
 // ------------------------------------------------------------------------------------------
 // GLSL semantics
@@ -79,6 +81,37 @@ __device__ __forceinline__ float3 e5( uint32_t p )
     rgdn::f3 c = decode_e5( p );
     return make_float3( c.x, c.y, c.z );
 }
+
+// Math policy of the continuous weights. EXACT follows the shader expressions in IEEE binary32;
+// FAST replaces only functions whose results feed continuous weights (no threshold follows):
+// pow(x,128) by seven squarings, pow(x,y) by exp2(y*log2(x)) with an accurate log2 and the
+// hardware exp2, exp by the hardware exp2, divisions by reciprocal multiplies, and fused
+// multiply-adds in the sums. Every deviation is a few ulp of a weight.
+__device__ __forceinline__ float ex2_approx( float x )
+{
+    float r;
+    asm( "ex2.approx.ftz.f32 %0, %1;" : "=f"( r ) : "f"( x ) );
+    return r;
+}
+template< bool FAST > struct Wm;
+template<> struct Wm< false >
+{
+    __device__ static float pow128( float x ) { return powf( x, 128.0f ); }
+    __device__ static float powv( float x, float y ) { return powf( x, y ); }
+    __device__ static float expn( float x ) { return expf( x ); }
+    __device__ static float madd( float a, float b, float c ) { return a * b + c; }
+};
+template<> struct Wm< true >
+{
+    __device__ static float pow128( float x )
+    {
+        x = x * x; x = x * x; x = x * x; x = x * x; x = x * x; x = x * x; x = x * x;
+        return x;
+    }
+    __device__ static float powv( float x, float y ) { return ex2_approx( y * log2f( x ) ); }
+    __device__ static float expn( float x ) { return ex2_approx( x * 1.44269504088896341f ); }
+    __device__ static float madd( float a, float b, float c ) { return __fmaf_rn( a, b, c ); }
+};
 
 // ------------------------------------------------------------------------------------------
 // Storage policy: element types of the colour / history images per mode
@@ -247,16 +280,22 @@ __device__ __forceinline__ float4 ld_rgba8z( const Uniform& u, const uint32_t* p
 }
 
 // ==========================================================================================
-// RtGradients.rgen:44-181 — image-space part of the gradient samples (one thread per stratum)
+// RtGradients.rgen:44-181 — image-space part of the gradient samples, one stratum
 // ==========================================================================================
-template< int M > __global__ void __launch_bounds__( 256 ) k_gradient_samples( const FrameArgs a )
+// unorm8 -> float through a table of the exact values u / 255
+__device__ __forceinline__ float4 unpack_rgba8_t( uint32_t c, const float* u8 )
+{
+    return make_float4( u8[ c & 0xFFu ], u8[ ( c >> 8 ) & 0xFFu ], u8[ ( c >> 16 ) & 0xFFu ], u8[ c >> 24 ] );
+}
+__device__ __forceinline__ float4 ld_rgba8t( const Uniform& u, const uint32_t* p, int x, int y, const float* u8 )
+{
+    return ( x >= 0 && y >= 0 && x < u.GW && y < u.GH ) ? unpack_rgba8_t( p[ y * u.GW + x ], u8 ) : make_float4( 0, 0, 0, 0 );
+}
+
+template< int M > __device__ __forceinline__ void gradient_sample_px( const FrameArgs& a, const int gx, const int gy, const float* u8 )
 {
     const Uniform& u  = a.u;
-    const int      gx = blockIdx.x * blockDim.x + threadIdx.x;
-    const int      gy = blockIdx.y * blockDim.y + threadIdx.y;
-    if( gx >= u.GW || gy >= u.GH || gx * STRATA >= u.W || gy * STRATA >= u.H ) return;
-    const size_t gi = (size_t)gy * u.GW + gx;
-
+    const int      gi = gy * u.GW + gx;
     if( u.gradMultD < 0.001f && u.gradMultI < 0.001f && u.gradMultS < 0.001f )
     {
         a.disPing[ gi ]     = 0u;
@@ -276,16 +315,16 @@ template< int M > __global__ void __launch_bounds__( 256 ) k_gradient_samples( c
             float2    m  = make_float2( 0, 0 );
             if( inside( u, cx, cy ) )
             {
-                ushort4 mo = a.motion[ idx( u, cx, cy ) ];
-                m          = make_float2( h2f( mo.x ), h2f( mo.y ) );
+                const ushort4 mo = a.motion[ cy * u.W + cx ];
+                m                = make_float2( h2f( mo.x ), h2f( mo.y ) );
             }
             const float2 pp = prev_screen_pos( u, m, cx, cy );
             const int2   ip = make_int2( (int)floorf( pp.x ), (int)floorf( pp.y ) );
             float2       il = make_float2( 0, 0 );
             if( inside( u, ip.x, ip.y ) )
             {
-                uint32_t g = a.gradInputsPrev[ idx( u, ip.x, ip.y ) ];
-                il         = make_float2( h2f( (uint16_t)( g & 0xFFFFu ) ), h2f( (uint16_t)( g >> 16 ) ) );
+                const uint32_t g = a.gradInputsPrev[ ip.y * u.W + ip.x ];
+                il               = make_float2( h2f( (uint16_t)( g & 0xFFFFu ) ), h2f( (uint16_t)( g >> 16 ) ) );
             }
             if( fmaxf( il.x, il.y ) > fmaxf( prevLum.x, prevLum.y ) )
             {
@@ -296,7 +335,7 @@ template< int M > __global__ void __launch_bounds__( 256 ) k_gradient_samples( c
             }
         }
     }
-    const bool skyCur = inside( u, curShadingPix.x, curShadingPix.y ) && a.isSky[ idx( u, curShadingPix.x, curShadingPix.y ) ] != 0;
+    const bool skyCur = inside( u, curShadingPix.x, curShadingPix.y ) && a.isSky[ curShadingPix.y * u.W + curShadingPix.x ] != 0;
     if( !in_area( prevShadingPix.x, prevShadingPix.y, cb_area( u, curShadingPix.x ) ) || skyCur ||
         ( prevLum.x <= 0.0f && prevLum.y <= 0.0f ) )
     {
@@ -304,31 +343,32 @@ template< int M > __global__ void __launch_bounds__( 256 ) k_gradient_samples( c
         a.gradPrevPix[ gi ] = STRATA * STRATA + 1;
         return;
     }
+    // in the render area, so inside the image
+    const int    pi  = prevShadingPix.y * u.W + prevShadingPix.x;
     // the re-shaded luminance is a boundary input (RtGradients.rgen:107-136)
-    const float2 fpl = a.reshaded[ idx( u, prevShadingPix.x, prevShadingPix.y ) ];
+    const float2 fpl = a.reshaded[ pi ];
     float g0, g1, g2;
     {
-        float gs = fpl.x - prevLum.x;
-        float nf = fmaxf( fpl.x, prevLum.x );
-        g0       = antilag( gs, nf );
+        const float gs = fpl.x - prevLum.x;
+        const float nf = fmaxf( fpl.x, prevLum.x );
+        g0             = antilag( gs, nf );
     }
     {
-        float  gs = fmaxf( 0.0f, prevLum.x - fpl.x );
-        float  nf = fmaxf( fpl.x, prevLum.x );
-        float3 ip = Sto< M >::ld3( a.indirAccumPrev, idx( u, prevShadingPix.x, prevShadingPix.y ) );
-        float  brightness = luminance( ip );
+        float        gs         = fmaxf( 0.0f, prevLum.x - fpl.x );
+        const float  nf         = fmaxf( fpl.x, prevLum.x );
+        const float  brightness = luminance( Sto< M >::ld3( a.indirAccumPrev, (size_t)pi ) );
         gs = gs * ( 1.0f - gsmoothstep( 1.0f, 10.0f, brightness ) );
         g1 = antilag( gs, nf );
     }
     {
-        float gs = fpl.y - prevLum.y;
-        float nf = fmaxf( fpl.y, prevLum.y );
-        g2       = antilag( gs, nf );
+        const float gs = fpl.y - prevLum.y;
+        const float nf = fmaxf( fpl.y, prevLum.y );
+        g2             = antilag( gs, nf );
     }
     g0 = g0 * u.gradMultD;
     g1 = g1 * u.gradMultI;
     g2 = g2 * u.gradMultS;
-    const float4 gp = ld_rgba8z( u, a.disHistPrev, prevShadingPix.x / STRATA, prevShadingPix.y / STRATA );
+    const float4 gp = ld_rgba8t( u, a.disHistPrev, prevShadingPix.x / STRATA, prevShadingPix.y / STRATA, u8 );
     g0 = gmix( g0, gp.x, 0.5f );
     g1 = gmix( g1, gp.y, 0.5f );
     g2 = gmix( g2, gp.z, 0.5f );
@@ -336,15 +376,10 @@ template< int M > __global__ void __launch_bounds__( 256 ) k_gradient_samples( c
     a.gradPrevPix[ gi ] = (uint8_t)curStrataPos;
 }
 
-// ==========================================================================================
-// CmASVGFGradientAtrous.comp:42-105 — one iteration (one thread per stratum)
-// ==========================================================================================
-template< int M > __global__ void __launch_bounds__( 256 ) k_gradient_atrous( const FrameArgs a, const int iter )
+// CmASVGFGradientAtrous.comp:42-105 — one iteration, one stratum
+__device__ __forceinline__ void gradient_atrous_px( const FrameArgs& a, const int gx, const int gy, const int iter, const float* u8 )
 {
-    const Uniform& u  = a.u;
-    const int      gx = blockIdx.x * blockDim.x + threadIdx.x;
-    const int      gy = blockIdx.y * blockDim.y + threadIdx.y;
-    if( gx >= u.GW || gy >= u.GH || gx * STRATA >= u.W || gy * STRATA >= u.H ) return;
+    const Uniform&  u    = a.u;
     const uint32_t* src  = ( iter % 2 == 0 ) ? a.disPing : a.disPong;
     uint32_t*       dst  = ( iter % 2 == 0 ) ? a.disPong : a.disPing;
     const int       step = 1 << iter;
@@ -360,7 +395,7 @@ template< int M > __global__ void __launch_bounds__( 256 ) k_gradient_atrous( co
         for( int xx = -1; xx <= 1; xx++ )
         {
             const int    qx = gx + xx * step, qy = gy + yy * step;
-            const float4 g  = ld_rgba8z( u, src, qx, qy );
+            const float4 g  = ld_rgba8t( u, src, qx, qy, u8 );
             const float  w  = kern[ yy < 0 ? -yy : yy ][ xx < 0 ? -xx : xx ] * ( in_area( qx, qy, ga ) ? 1.0f : 0.0f );
             out = add( out, mul( f3( g.x, g.y, g.z ), w ) );
             ws  = ws + w;
@@ -368,9 +403,64 @@ template< int M > __global__ void __launch_bounds__( 256 ) k_gradient_atrous( co
     }
     out = divs( out, ws );
     const uint32_t packed = pack_rgba8( out.x, out.y, out.z, 0.0f );
-    const size_t   gi     = (size_t)gy * u.GW + gx;
+    const int      gi     = gy * u.GW + gx;
     dst[ gi ] = packed;
     if( iter == 0 ) a.disHist[ gi ] = packed;
+}
+
+__device__ __forceinline__ void fill_u8( float* u8, int t )
+{
+    u8[ t ] = (float)t / 255.0f;
+}
+
+template< int M > __global__ void __launch_bounds__( 256 ) k_gradient_samples( const FrameArgs a )
+{
+    __shared__ float u8[ 256 ];
+    fill_u8( u8, threadIdx.y * blockDim.x + threadIdx.x );
+    __syncthreads();
+    const int gx = blockIdx.x * blockDim.x + threadIdx.x;
+    const int gy = blockIdx.y * blockDim.y + threadIdx.y;
+    if( gx >= a.u.GW || gy >= a.u.GH || gx * STRATA >= a.u.W || gy * STRATA >= a.u.H ) return;
+    gradient_sample_px< M >( a, gx, gy, u8 );
+}
+
+template< int M > __global__ void __launch_bounds__( 256 ) k_gradient_atrous( const FrameArgs a, const int iter )
+{
+    __shared__ float u8[ 256 ];
+    fill_u8( u8, threadIdx.y * blockDim.x + threadIdx.x );
+    __syncthreads();
+    const int gx = blockIdx.x * blockDim.x + threadIdx.x;
+    const int gy = blockIdx.y * blockDim.y + threadIdx.y;
+    if( gx >= a.u.GW || gy >= a.u.GH || gx * STRATA >= a.u.W || gy * STRATA >= a.u.H ) return;
+    gradient_atrous_px( a, gx, gy, iter, u8 );
+}
+
+// The whole gradient chain in one cooperative launch: samples, then the 4 a-trous
+// iterations, separated by grid-wide barriers (every block is co-resident; the
+// launch fails instead of starting if the grid does not fit).
+template< int M > __global__ void __launch_bounds__( 256 ) k_gradient_fused( const FrameArgs a )
+{
+    __shared__ float u8[ 256 ];
+    fill_u8( u8, threadIdx.x );
+    __syncthreads();
+    cg::grid_group grid   = cg::this_grid();
+    const Uniform& u      = a.u;
+    const int      n      = u.GW * u.GH;
+    const int      stride = gridDim.x * blockDim.x;
+    for( int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += stride )
+    {
+        const int gx = k % u.GW, gy = k / u.GW;
+        if( gx * STRATA < u.W && gy * STRATA < u.H ) gradient_sample_px< M >( a, gx, gy, u8 );
+    }
+    for( int iter = 0; iter < 4; iter++ )
+    {
+        grid.sync();
+        for( int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += stride )
+        {
+            const int gx = k % u.GW, gy = k / u.GW;
+            if( gx * STRATA < u.W && gy * STRATA < u.H ) gradient_atrous_px( a, gx, gy, iter, u8 );
+        }
+    }
 }
 
 // ==========================================================================================
@@ -382,22 +472,23 @@ __device__ __forceinline__ float spec_min_accum( const Uniform& u )
     const float fps = td <= 0.0f ? 0.0f : 1.0f / td;
     return gclamp( 0.2f * fps, 0.0f, 128.0f );
 }
-__device__ __forceinline__ float spec_accum_speed( const Uniform& u, float Amax, float r, float NoV, float par )
+template< bool FAST > __device__ __forceinline__ float spec_accum_speed( const Uniform& u, float Amax, float r, float NoV, float par )
 {
+    using X              = Wm< FAST >;
     const float acos01sq = 1.0f - NoV;
-    const float aa       = powf( gsat( acos01sq ), 0.66f );
+    const float aa       = X::powv( gsat( acos01sq ), 0.66f );
     const float b        = 1.1f + r * r;
     const float ps       = ( b + aa ) / ( b - aa );
     const float powScale = 1.0f + par * ps;
-    float       f        = 1.0f - exp2f( -200.0f * r * r );
-    f                    = f * powf( gsat( r ), 0.5f * powScale );
+    float       f        = 1.0f - ( FAST ? ex2_approx( -200.0f * r * r ) : exp2f( -200.0f * r * r ) );
+    f                    = f * X::powv( gsat( r ), 0.5f * powScale );
     const float A        = 256.0f * f;
     return gclamp( A, spec_min_accum( u ), Amax );
 }
-__device__ __forceinline__ float spec_dominant( float nv, float r )
+template< bool FAST > __device__ __forceinline__ float spec_dominant( float nv, float r )
 {
-    const float aa = 0.298475f * logf( 39.4115f - 39.0029f * r );
-    const float f  = powf( gclamp( 1.0f - nv, 0.0f, 1.0f ), 10.8649f ) * ( 1.0f - aa ) + aa;
+    const float aa = 0.298475f * ( FAST ? __logf( 39.4115f - 39.0029f * r ) : logf( 39.4115f - 39.0029f * r ) );
+    const float f  = Wm< FAST >::powv( gclamp( 1.0f - nv, 0.0f, 1.0f ), 10.8649f ) * ( 1.0f - aa ) + aa;
     return gclamp( f, 0.0f, 1.0f );
 }
 __device__ __forceinline__ float parallax( const Uniform& u, float3 pos, float3 posPrev )
@@ -410,7 +501,7 @@ __device__ __forceinline__ float parallax( const Uniform& u, float3 pos, float3 
     return par * 60.0f;
 }
 
-template< int M > __global__ void __launch_bounds__( 256 ) k_temporal( const FrameArgs a )
+template< int M, bool FAST > __global__ void __launch_bounds__( 256 ) k_temporal( const FrameArgs a )
 {
     using S          = Sto< M >;
     const Uniform& u = a.u;
@@ -511,9 +602,10 @@ template< int M > __global__ void __launch_bounds__( 256 ) k_temporal( const Fra
         }
         const float nv = fmaxf( 0.0f, dot3( normal, f3( -rayInfo.x, -rayInfo.y, -rayInfo.z ) ) );
 
-        const float A       = gclamp( 1.0f + specHistoryLength * powf( 1.0f - aS, 5.0f ), spec_min_accum( u ), 256.0f );
+        const float A       = gclamp( 1.0f + specHistoryLength * Wm< FAST >::powv( 1.0f - aS, 5.0f ), spec_min_accum( u ), 256.0f );
         const float par     = parallax( u, surfPos, surfPosPrev );
-        const float AOnSurf = spec_accum_speed( u, A, roughness, nv, par );
+        const float AOnSurf = spec_accum_speed< FAST >( u, A, roughness, nv, par );
+        const float domin   = spec_dominant< FAST >( nv, roughness );
 
         const float3 specOnSurf    = vmix( specPrevOnSurf, unfilteredSpec, 1.0f / ( 1.0f + AOnSurf ) );
         const float  hitDistOnSurf = gmix( specHitDistancePrev, rayInfo.w, 1.0f / ( 1.0f + AOnSurf ) );
@@ -523,7 +615,7 @@ template< int M > __global__ void __launch_bounds__( 256 ) k_temporal( const Fra
         specHitDistanceAccum   = hitDistOnSurf;
 
         const float3 rayDir     = f3( rayInfo.x, rayInfo.y, rayInfo.z );
-        const float3 virtualPos = add( surfPos, mul( mul( rayDir, hitDistOnSurf ), spec_dominant( nv, roughness ) ) );
+        const float3 virtualPos = add( surfPos, mul( mul( rayDir, hitDistOnSurf ), domin ) );
 
         int2   pixPrevS;
         float2 subPixS;
@@ -565,14 +657,14 @@ template< int M > __global__ void __launch_bounds__( 256 ) k_temporal( const Fra
         }
         if( weightSumVirtual > 0.0001f )
         {
-            float       Avirt      = spec_accum_speed( u, A, roughness, nv, 0.0f );
+            float       Avirt      = spec_accum_speed< FAST >( u, A, roughness, nv, 0.0f );
             const float confidence = 1.0f;
             const float Amin       = fminf( Avirt, 3.0f * sqrtf( roughness ) );
             float       aa         = gmix( 1.0f / ( 1.0f + Amin ), 1.0f / ( 1.0f + Avirt ), confidence );
             Avirt                  = 1.0f / aa - 1.0f;
             const float Ahitdist   = fminf( Avirt, 16.0f );
             const float3 specVirt  = vmix( specPrevOnSurf, unfilteredSpec, 1.0f / ( 1.0f + Avirt ) );
-            const float amount     = spec_dominant( nv, roughness );
+            const float amount     = domin;
             aa                     = gmix( 1.0f / ( 1.0f + AOnSurf ), 1.0f / ( 1.0f + Avirt ), amount );
             specColorAccum         = vmix( specOnSurf, specVirt, amount );
             specHistoryLengthAccum = 1.0f / aa - 1.0f;
@@ -676,29 +768,30 @@ template< int M > __global__ void __launch_bounds__( 256 ) k_antifirefly( const 
 // ==========================================================================================
 // CmSVGFEstimateVariance.comp:129-206
 // ==========================================================================================
-template< int M > __global__ void __launch_bounds__( 256 ) k_variance( const FrameArgs a )
+// colourAt(dx, dy) returns DiffAccumColor at (px+dx, py+dy), zero outside the image
+template< int M, bool FAST, class ColorAt >
+__device__ __forceinline__ void variance_px( const FrameArgs& a, const int px, const int py, const int i, ColorAt colorAt, float3& outC,
+                                             float& outV )
 {
     using S          = Sto< M >;
-    const Uniform& u = a.u;
-    const int      px = blockIdx.x * blockDim.x + threadIdx.x;
-    const int      py = blockIdx.y * blockDim.y + threadIdx.y;
-    if( px >= u.W || py >= u.H ) return;
-    const size_t i   = idx( u, px, py );
-    const float  cz  = h2f( a.depth[ i ] );
-    float3       pc  = S::ld3( a.diffAccumColor, i );
+    using X          = Wm< FAST >;
+    const float cz   = h2f( a.depth[ i ] );
+    float3      pc   = colorAt( 0, 0 );
     if( cz < 0.0f || cz > MAX_RAY_LENGTH )
     {
-        S::stcv( a.diffPing, a.varPing, i, pc, 0.0f );
+        outC = pc;
+        outV = 0.0f;
         return;
     }
-    const float  histLen = S::ld4( a.histLen, i ).x;
-    const float2 tm      = S::ld2( a.moments, i );
+    const float  histLen = S::ld4( a.histLen, (size_t)i ).x;
+    const float2 tm      = S::ld2( a.moments, (size_t)i );
     const float  THR     = 4.0f;
     if( histLen > THR )
     {
         float tv = fmaxf( 0.0f, tm.y - tm.x * tm.x );
         tv       = tv / fmaxf( 1.0f, histLen - THR );
-        S::stcv( a.diffPing, a.varPing, i, pc, tv );
+        outC     = pc;
+        outV     = tv;
         return;
     }
     const float  l   = luminance( pc );
@@ -713,13 +806,15 @@ template< int M > __global__ void __launch_bounds__( 256 ) k_variance( const Fra
         {
             if( xx == 0 && yy == 0 ) continue;
             const int    qx  = px + xx, qy = py + yy;
-            const float3 cq  = ld3z< M >( a, a.diffAccumColor, qx, qy );
+            const float3 cq  = colorAt( xx, yy );
             const float  lq  = luminance( cq );
-            const float  zq  = ld_depth( a, a.depth, qx, qy );
+            const bool   in  = inside( a.u, qx, qy );
+            const int    q   = in ? qy * a.u.W + qx : 0;
+            const float  zq  = in ? h2f( a.depth[ q ] ) : 0.0f;
             const float  mz  = fmaxf( cz, zq );
             const float  rcp = mz <= 0.0f ? 0.0f : 1.0f / mz;
-            const float  wz  = expf( -fabsf( cz - zq ) * rcp );
-            const float  wn  = powf( fmaxf( 0.0f, dot3( cnd, decode_normal( a, ld_u32( a, a.normal, qx, qy ) ) ) ), 128.0f );
+            const float  wz  = X::expn( -fabsf( cz - zq ) * rcp );
+            const float  wn  = X::pow128( fmaxf( 0.0f, dot3( cnd, decode_normal( a, in ? a.normal[ q ] : 0u ) ) ) );
             const float  w   = wz * wn;
             if( !isnan( w ) )
             {
@@ -731,9 +826,134 @@ template< int M > __global__ void __launch_bounds__( 256 ) k_variance( const Fra
     }
     const float inv = ws <= 0.0f ? 0.0f : 1.0f / ws;
     sm              = make_float2( sm.x * inv, sm.y * inv );
-    pc              = mul( pc, inv );
-    const float sv  = fmaxf( 0.0f, sm.y - sm.x * sm.x ) * ( 1.0f + 2.0f * ( 1.0f - histLen / THR ) );
-    S::stcv( a.diffPing, a.varPing, i, pc, sv );
+    outC            = mul( pc, inv );
+    outV            = fmaxf( 0.0f, sm.y - sm.x * sm.x ) * ( 1.0f + 2.0f * ( 1.0f - histLen / THR ) );
+}
+
+template< int M > __global__ void __launch_bounds__( 256 ) k_variance( const FrameArgs a )
+{
+    using S          = Sto< M >;
+    const Uniform& u = a.u;
+    const int      px = blockIdx.x * blockDim.x + threadIdx.x;
+    const int      py = blockIdx.y * blockDim.y + threadIdx.y;
+    if( px >= u.W || py >= u.H ) return;
+    const int i = py * u.W + px;
+    float3    c;
+    float     v;
+    variance_px< M, false >( a, px, py, i, [ & ]( int dx, int dy ) { return ld3z< M >( a, a.diffAccumColor, px + dx, py + dy ); }, c, v );
+    S::stcv( a.diffPing, a.varPing, (size_t)i, c, v );
+}
+
+// ==========================================================================================
+// Anti-firefly + variance in one kernel (CmAntiFirefly.comp + CmSVGFEstimateVariance.comp).
+// A 32x8 tile: the three signals are staged with a 3-texel halo, the 5x5 ring minimum and
+// maximum come from row extrema (min over the 4 rows above/below of the 5-wide row extremum,
+// and the 4 same-row neighbours), the anti-firefly diffuse result on a 1-texel halo is
+// quantised through the storage format exactly as if it had been stored to DiffAccumColor,
+// and the variance reads it from shared memory. Results equal the two separate kernels.
+// ==========================================================================================
+constexpr int AFV_TX = 32, AFV_TY = 8;
+constexpr int AFV_IW = AFV_TX + 6, AFV_IH = AFV_TY + 6;   // staged inputs: tile +-3
+constexpr int AFV_AW = AFV_TX + 2, AFV_AH = AFV_TY + 2;   // anti-firefly results: tile +-1
+
+template< int M > __device__ __forceinline__ float3 quantize3( float3 v )
+{
+    if( M == MODE_REF ) return e5( encode_e5( v.x, v.y, v.z ) );
+    return v;  // fp32 / fp16 / bf16 channels of a clamp are already representable
+}
+
+template< int M, bool FAST > __global__ void __launch_bounds__( 256 ) k_af_variance( const FrameArgs a )
+{
+    using S = Sto< M >;
+    __shared__ float v[ 3 ][ AFV_IH ][ AFV_IW ];
+    __shared__ float rmn[ 3 ][ AFV_IH ][ AFV_AW ];
+    __shared__ float rmx[ 3 ][ AFV_IH ][ AFV_AW ];
+    __shared__ float afd[ 3 ][ AFV_AH ][ AFV_AW ];
+    const Uniform& u   = a.u;
+    const int      t   = threadIdx.y * AFV_TX + threadIdx.x;
+    const int      x0  = blockIdx.x * AFV_TX, y0 = blockIdx.y * AFV_TY;
+    const bool     af  = u.antiFirefly != 0;
+    const float    MAXF = 1000000.0f;
+
+    for( int sig = 0; sig < 3; sig++ )
+    {
+        const void* src = sig == 0 ? a.diffTemp : sig == 1 ? a.specAccum : a.indirAccum;
+        for( int k = t; k < AFV_IW * AFV_IH; k += 256 )
+        {
+            const int    lx = k % AFV_IW, ly = k / AFV_IW;
+            const float3 c  = ld3z< M >( a, src, x0 - 3 + lx, y0 - 3 + ly );
+            v[ 0 ][ ly ][ lx ] = c.x;
+            v[ 1 ][ ly ][ lx ] = c.y;
+            v[ 2 ][ ly ][ lx ] = c.z;
+        }
+        __syncthreads();
+        if( af )
+        {
+            for( int k = t; k < AFV_AW * AFV_IH; k += 256 )
+            {
+                const int rx = k % AFV_AW, ry = k / AFV_AW;
+#pragma unroll
+                for( int c = 0; c < 3; c++ )
+                {
+                    const float* r = &v[ c ][ ry ][ rx ];
+                    rmn[ c ][ ry ][ rx ] = fminf( fminf( fminf( r[ 0 ], r[ 1 ] ), fminf( r[ 2 ], r[ 3 ] ) ), r[ 4 ] );
+                    rmx[ c ][ ry ][ rx ] = fmaxf( fmaxf( fmaxf( r[ 0 ], r[ 1 ] ), fmaxf( r[ 2 ], r[ 3 ] ) ), r[ 4 ] );
+                }
+            }
+            __syncthreads();
+        }
+        for( int k = t; k < AFV_AW * AFV_AH; k += 256 )
+        {
+            const int ax = k % AFV_AW, ay = k / AFV_AW;
+            const int gx = x0 - 1 + ax, gy = y0 - 1 + ay;
+            float3    res;
+            float*    ctr[ 3 ];
+            float     o[ 3 ];
+#pragma unroll
+            for( int c = 0; c < 3; c++ )
+            {
+                const float center = v[ c ][ ay + 2 ][ ax + 2 ];
+                if( af )
+                {
+                    const float* row = &v[ c ][ ay + 2 ][ ax ];
+                    float mn = fminf( fminf( fminf( rmn[ c ][ ay ][ ax ], rmn[ c ][ ay + 1 ][ ax ] ), fminf( rmn[ c ][ ay + 3 ][ ax ], rmn[ c ][ ay + 4 ][ ax ] ) ),
+                                      fminf( fminf( row[ 0 ], row[ 1 ] ), fminf( row[ 3 ], row[ 4 ] ) ) );
+                    float mx = fmaxf( fmaxf( fmaxf( rmx[ c ][ ay ][ ax ], rmx[ c ][ ay + 1 ][ ax ] ), fmaxf( rmx[ c ][ ay + 3 ][ ax ], rmx[ c ][ ay + 4 ][ ax ] ) ),
+                                      fmaxf( fmaxf( row[ 0 ], row[ 1 ] ), fmaxf( row[ 3 ], row[ 4 ] ) ) );
+                    mn   = fminf( MAXF, mn );
+                    mx   = fmaxf( -MAXF, mx );
+                    o[ c ] = fminf( fmaxf( center, mn ), mx );
+                }
+                else o[ c ] = center;
+                (void)ctr;
+            }
+            res = f3( o[ 0 ], o[ 1 ], o[ 2 ] );
+            const bool in = inside( u, gx, gy );
+            if( sig == 0 )
+            {
+                const float3 q = in ? quantize3< M >( res ) : f3( 0, 0, 0 );
+                afd[ 0 ][ ay ][ ax ] = q.x;
+                afd[ 1 ][ ay ][ ax ] = q.y;
+                afd[ 2 ][ ay ][ ax ] = q.z;
+            }
+            else if( in && ax >= 1 && ax <= AFV_TX && ay >= 1 && ay <= AFV_TY )
+                S::st3( sig == 1 ? a.specPing : a.indirPing, (size_t)( gy * u.W + gx ), res );
+        }
+        __syncthreads();
+    }
+
+    const int px = x0 + threadIdx.x, py = y0 + threadIdx.y;
+    if( px >= u.W || py >= u.H ) return;
+    const int i = py * u.W + px;
+    float3    c;
+    float     var;
+    variance_px< M, FAST >( a, px, py, i,
+                            [ & ]( int dx, int dy ) {
+                                const int ax = threadIdx.x + 1 + dx, ay = threadIdx.y + 1 + dy;
+                                return f3( afd[ 0 ][ ay ][ ax ], afd[ 1 ][ ay ][ ax ], afd[ 2 ][ ay ][ ax ] );
+                            },
+                            c, var );
+    S::stcv( a.diffPing, a.varPing, (size_t)i, c, var );
 }
 
 // ==========================================================================================
@@ -822,26 +1042,33 @@ template< int M > __device__ __forceinline__ uint16_t compose( const FrameArgs& 
     return hin;
 }
 
-template< int M > __global__ void __launch_bounds__( 256 ) k_atrous( const FrameArgs a, const int iter )
+// FP16 pairs through the packed converter
+__device__ __forceinline__ float4 ld_h4( const ushort4* p, int i )
+{
+    const ushort4 h  = p[ i ];
+    const float2  lo = __half22float2( __halves2half2( __ushort_as_half( h.x ), __ushort_as_half( h.y ) ) );
+    const float2  hi = __half22float2( __halves2half2( __ushort_as_half( h.z ), __ushort_as_half( h.w ) ) );
+    return make_float4( lo.x, lo.y, hi.x, hi.y );
+}
+
+// one a-trous iteration for one pixel (CmSVGFAtrous_Iter0.comp:196-304, CmSVGFAtrous.comp:71-220)
+template< int M, bool FAST >
+__device__ __forceinline__ void atrous_px( const FrameArgs& a, const AtrousIO& io, const int iter, const int px, const int py,
+                                           const int i, const float* u8, float3& outDiff, float& outVar, float3& outSpec,
+                                           float3& outInd )
 {
     using S          = Sto< M >;
+    using X          = Wm< FAST >;
     const Uniform& u = a.u;
-    const int      px = blockIdx.x * blockDim.x + threadIdx.x;
-    const int      py = blockIdx.y * blockDim.y + threadIdx.y;
-    if( px >= u.W || py >= u.H ) return;
-    const size_t   i    = idx( u, px, py );
-    const AtrousIO io   = atrous_io< M >( a, iter );
-    const bool     last = iter + 1 == (int)u.niter;
-    const int      step = 1 << iter;
-
-    const Area   chArea  = cb_area( u, px );
-    const float4 cv      = S::ldcv( io.diffSrc, io.varSrc, i );
-    float3       outDiff = f3( cv.x, cv.y, cv.z );
-    float        outVar  = cv.w;
-    float3       outSpec = S::ld3( io.specSrc, i );
-    float3       outInd  = S::ld3( io.indirSrc, i );
-    const float  z       = h2f( a.depth[ i ] );
-    const float  gradDepth = h2f( a.depthGrad[ i ] );
+    const int      step   = 1 << iter;
+    const Area     chArea = cb_area( u, px );
+    const float4   cv     = S::ldcv( io.diffSrc, io.varSrc, (size_t)i );
+    outDiff = f3( cv.x, cv.y, cv.z );
+    outVar  = cv.w;
+    outSpec = S::ld3( io.specSrc, (size_t)i );
+    outInd  = S::ld3( io.indirSrc, (size_t)i );
+    const float z         = h2f( a.depth[ i ] );
+    const float gradDepth = h2f( a.depthGrad[ i ] );
 
     if( z < 0.0f || z > MAX_RAY_LENGTH )
     {
@@ -849,96 +1076,134 @@ template< int M > __global__ void __launch_bounds__( 256 ) k_atrous( const Frame
         {
             outDiff = f3( 0, 0, 0 ); outVar = 0.0f; outSpec = f3( 0, 0, 0 ); outInd = f3( 0, 0, 0 );
         }
+        return;
     }
-    else
+    const float3 normal = decode_normal( a, a.normal[ i ] );
+    const float  l      = luminance( outDiff );
+    float        prefVar;
+    if( iter == 0 )
     {
-        const float3 normal = decode_normal( a, a.normal[ i ] );
-        const float  l      = luminance( outDiff );
-        float        prefVar;
-        if( iter == 0 )
-        {
-            // prefilterLuminanceVariance (CmSVGFAtrous_Iter0.comp:158-187)
-            const float g[ 2 ][ 2 ] = { { 0.25f, 0.125f }, { 0.125f, 0.0625f } };
-            float r = 0.0f;
-#pragma unroll
-            for( int yy = -1; yy <= 1; yy++ )
-            {
-#pragma unroll
-                for( int xx = -1; xx <= 1; xx++ )
-                    r = r + ldcvz< M >( a, io.diffSrc, io.varSrc, px + xx, py + yy ).w * g[ xx < 0 ? -xx : xx ][ yy < 0 ? -yy : yy ];
-            }
-            r = sqrtf( fmaxf( r, 0.0f ) );
-            S::st1( a.filtVar, i, r );
-            prefVar = r;
-        }
-        else prefVar = S::ld1( a.filtVar, i );
-
-        const float wLumMul   = 1.0f / ( 4.0f * prefVar + 0.00001f );
-        const float roughness = unorm8_to_f32( a.mr[ i ] >> 8 );
-        const float wRoughMul = gclamp( roughness * 30.0f - (float)iter, 0.0f, 1.0f );
-        const float hS        = S::ld4( a.histLen, i ).z;
-        const float nws       = gclamp( hS / 8.0f, 0.0f, 1.0f );
-        float       nwSpec    = spec_power( roughness * roughness );
-        nwSpec                = gclamp( nwSpec, 8.0f, 1024.0f );
-        nwSpec                = nwSpec * nws;
-
-        const float kern[ 2 ][ 2 ] = { { 1.0f, 0.5f }, { 0.5f, 0.25f } };
-        float ws = 1.0f, wsS = 1.0f, wsI = 1.0f;
+        // prefilterLuminanceVariance (CmSVGFAtrous_Iter0.comp:158-187)
+        const float g[ 2 ][ 2 ] = { { 0.25f, 0.125f }, { 0.125f, 0.0625f } };
+        float r = 0.0f;
 #pragma unroll
         for( int yy = -1; yy <= 1; yy++ )
         {
 #pragma unroll
             for( int xx = -1; xx <= 1; xx++ )
-            {
-                if( xx == 0 && yy == 0 ) continue;
-                const int    qx  = px + xx * step, qy = py + yy * step;
-                const bool   in  = inside( u, qx, qy );
-                const size_t q   = in ? idx( u, qx, qy ) : 0;
-                const float  rq  = in ? unorm8_to_f32( a.mr[ q ] >> 8 ) : 0.0f;
-                const float3 nq  = decode_normal( a, in ? a.normal[ q ] : 0u );
-                const float  zq  = in ? h2f( a.depth[ q ] ) : 0.0f;
-                const float3 sq  = in ? S::ld3( io.specSrc, q ) : f3( 0, 0, 0 );
-                const float4 cvq = in ? S::ldcv( io.diffSrc, io.varSrc, q ) : make_float4( 0, 0, 0, 0 );
-                const float3 dq  = f3( cvq.x, cvq.y, cvq.z );
-                const float  lq  = luminance( dq );
-                const float  nn  = fmaxf( 0.0f, dot3( normal, nq ) );
-                const float3 iq  = in ? S::ld3( io.indirSrc, q ) : f3( 0, 0, 0 );
-
-                const float w_z = fabsf( z - zq ) / fmaxf( gradDepth * (float)( ( xx < 0 ? -xx : xx ) + ( yy < 0 ? -yy : yy ) ), 0.01f );
-                const float w_n = powf( nn, 128.0f );
-                const float w_l = fabsf( l - lq ) * wLumMul;
-                float       w_r = fmaxf( 0.0f, 1.0f - 10.0f * fabsf( roughness - rq ) ) * wRoughMul;
-                if( nwSpec > 0.0f ) w_r = w_r * powf( nn, nwSpec );
-                const float waveletW = kern[ yy < 0 ? -yy : yy ][ xx < 0 ? -xx : xx ];
-                const float insideA  = in_area( qx, qy, chArea ) ? 1.0f : 0.0f;
-                const float wBase    = expf( -w_z * w_z ) * w_n * waveletW * insideA;
-                const float wDiff    = wBase * expf( -w_l );
-                const float wSpec    = wBase * w_r;
-                const float wInd     = wBase;
-
-                outDiff = add( outDiff, mul( dq, wDiff ) );
-                outSpec = add( outSpec, mul( sq, wSpec ) );
-                outInd  = add( outInd, mul( iq, wInd ) );
-                outVar  = outVar + cvq.w * wDiff * wDiff;
-                ws      = ws + wDiff;
-                wsS     = wsS + wSpec;
-                wsI     = wsI + wInd;
-            }
+                r = r + ldcvz< M >( a, io.diffSrc, io.varSrc, px + xx, py + yy ).w * g[ xx < 0 ? -xx : xx ][ yy < 0 ? -yy : yy ];
         }
-        const float inv = 1.0f / ws, invS = 1.0f / wsS, invI = 1.0f / wsI;
-        outDiff = mul( outDiff, inv );
-        outVar  = outVar * inv * inv;
-        outSpec = mul( outSpec, invS );
-        outInd  = mul( outInd, invI );
+        r = sqrtf( fmaxf( r, 0.0f ) );
+        S::st1( a.filtVar, (size_t)i, r );
+        prefVar = r;
     }
+    else prefVar = S::ld1( a.filtVar, (size_t)i );
 
-    if( !last )
+    const float wLumMul   = 1.0f / ( 4.0f * prefVar + 0.00001f );
+    const float roughness = u8[ a.mr[ i ] >> 8 ];
+    const float wRoughMul = gclamp( roughness * 30.0f - (float)iter, 0.0f, 1.0f );
+    const float hS        = S::ld4( a.histLen, (size_t)i ).z;
+    const float nws       = gclamp( hS / 8.0f, 0.0f, 1.0f );
+    float       nwSpec    = spec_power( roughness * roughness );
+    nwSpec                = gclamp( nwSpec, 8.0f, 1024.0f );
+    nwSpec                = nwSpec * nws;
+    // FAST: one reciprocal per tap distance class (|x|+|y| = 1 or 2)
+    const float rz1 = FAST ? 1.0f / fmaxf( gradDepth * 1.0f, 0.01f ) : 0.0f;
+    const float rz2 = FAST ? 1.0f / fmaxf( gradDepth * 2.0f, 0.01f ) : 0.0f;
+
+    const float kern[ 2 ][ 2 ] = { { 1.0f, 0.5f }, { 0.5f, 0.25f } };
+    float ws = 1.0f, wsS = 1.0f, wsI = 1.0f;
+#pragma unroll
+    for( int yy = -1; yy <= 1; yy++ )
     {
-        S::stcv( io.diffDst, io.varDst, i, outDiff, outVar );
-        S::st3( io.specDst, i, outSpec );
-        S::st3( io.indirDst, i, outInd );
+#pragma unroll
+        for( int xx = -1; xx <= 1; xx++ )
+        {
+            if( xx == 0 && yy == 0 ) continue;
+            const int    qx  = px + xx * step, qy = py + yy * step;
+            const bool   in  = inside( u, qx, qy );
+            const int    q   = in ? qy * u.W + qx : 0;
+            const float  rq  = in ? u8[ a.mr[ q ] >> 8 ] : 0.0f;
+            const float3 nq  = decode_normal( a, in ? a.normal[ q ] : 0u );
+            const float  zq  = in ? h2f( a.depth[ q ] ) : 0.0f;
+            const float3 sq  = in ? S::ld3( io.specSrc, (size_t)q ) : f3( 0, 0, 0 );
+            const float4 cvq = in ? S::ldcv( io.diffSrc, io.varSrc, (size_t)q ) : make_float4( 0, 0, 0, 0 );
+            const float3 dq  = f3( cvq.x, cvq.y, cvq.z );
+            const float  lq  = luminance( dq );
+            const float  nn  = fmaxf( 0.0f, dot3( normal, nq ) );
+            const float3 iq  = in ? S::ld3( io.indirSrc, (size_t)q ) : f3( 0, 0, 0 );
+            const int    man = ( xx < 0 ? -xx : xx ) + ( yy < 0 ? -yy : yy );
+
+            const float w_z = FAST ? fabsf( z - zq ) * ( man == 1 ? rz1 : rz2 )
+                                   : fabsf( z - zq ) / fmaxf( gradDepth * (float)man, 0.01f );
+            const float w_n = X::pow128( nn );
+            const float w_l = fabsf( l - lq ) * wLumMul;
+            float       w_r = fmaxf( 0.0f, 1.0f - 10.0f * fabsf( roughness - rq ) ) * wRoughMul;
+            if( nwSpec > 0.0f ) w_r = w_r * X::powv( nn, nwSpec );
+            const float waveletW = kern[ yy < 0 ? -yy : yy ][ xx < 0 ? -xx : xx ];
+            const float insideA  = in_area( qx, qy, chArea ) ? 1.0f : 0.0f;
+            const float wBase    = X::expn( -w_z * w_z ) * w_n * waveletW * insideA;
+            const float wDiff    = wBase * X::expn( -w_l );
+            const float wSpec    = wBase * w_r;
+            const float wInd     = wBase;
+
+            outDiff = f3( X::madd( dq.x, wDiff, outDiff.x ), X::madd( dq.y, wDiff, outDiff.y ), X::madd( dq.z, wDiff, outDiff.z ) );
+            outSpec = f3( X::madd( sq.x, wSpec, outSpec.x ), X::madd( sq.y, wSpec, outSpec.y ), X::madd( sq.z, wSpec, outSpec.z ) );
+            outInd  = f3( X::madd( iq.x, wInd, outInd.x ), X::madd( iq.y, wInd, outInd.y ), X::madd( iq.z, wInd, outInd.z ) );
+            outVar  = X::madd( cvq.w * wDiff, wDiff, outVar );
+            ws      = ws + wDiff;
+            wsS     = wsS + wSpec;
+            wsI     = wsI + wInd;
+        }
     }
-    else compose< M >( a, px, py, i, outDiff, outSpec, outInd );
+    const float inv = 1.0f / ws, invS = 1.0f / wsS, invI = 1.0f / wsI;
+    outDiff = mul( outDiff, inv );
+    outVar  = outVar * inv * inv;
+    outSpec = mul( outSpec, invS );
+    outInd  = mul( outInd, invI );
+}
+
+// One a-trous iteration over the frame. HIST: the last iteration also accumulates the
+// luminance histogram of the HistogramInput values it writes (CmLuminanceHistogram.comp,
+// fused: no second read of the image).
+template< int M, bool FAST, bool HIST > __global__ void __launch_bounds__( 256 ) k_atrous( const FrameArgs a, const int iter )
+{
+    using S = Sto< M >;
+    __shared__ float    u8[ 256 ];
+    __shared__ uint32_t hist[ HIST ? 256 : 1 ];
+    const int t = threadIdx.y * blockDim.x + threadIdx.x;
+    u8[ t ]     = (float)t / 255.0f;
+    if( HIST ) hist[ t ] = 0u;
+    __syncthreads();
+
+    const Uniform& u  = a.u;
+    const int      px = blockIdx.x * blockDim.x + threadIdx.x;
+    const int      py = blockIdx.y * blockDim.y + threadIdx.y;
+    if( px < u.W && py < u.H )
+    {
+        const int      i    = py * u.W + px;
+        const AtrousIO io   = atrous_io< M >( a, iter );
+        const bool     last = iter + 1 == (int)u.niter;
+        float3         outDiff, outSpec, outInd;
+        float          outVar;
+        atrous_px< M, FAST >( a, io, iter, px, py, i, u8, outDiff, outVar, outSpec, outInd );
+        if( !last )
+        {
+            S::stcv( io.diffDst, io.varDst, (size_t)i, outDiff, outVar );
+            S::st3( io.specDst, (size_t)i, outSpec );
+            S::st3( io.indirDst, (size_t)i, outInd );
+        }
+        else
+        {
+            const uint16_t hin = compose< M >( a, px, py, (size_t)i, outDiff, outSpec, outInd );
+            if( HIST ) atomicAdd( &hist[ __ldg( &a.binLut[ hin ] ) ], 1u );
+        }
+    }
+    if( HIST )
+    {
+        __syncthreads();
+        if( hist[ t ] ) atomicAdd( &a.tm->histogram[ t ], hist[ t ] );
+    }
 }
 
 // ==========================================================================================
@@ -1004,12 +1269,35 @@ template< int M > cudaError_t launch_stage_t( const FrameArgs& a, int stage, int
     {
         case RGDN_STAGE_GRADIENT_SAMPLES: dev::k_gradient_samples< M ><<< gridG, blk, 0, s >>>( a ); break;
         case RGDN_STAGE_GRADIENT_ATROUS: dev::k_gradient_atrous< M ><<< gridG, blk, 0, s >>>( a, iter ); break;
-        case RGDN_STAGE_TEMPORAL_ACCUMULATION: dev::k_temporal< M ><<< grid, blk, 0, s >>>( a ); break;
+        case RGDN_STAGE_TEMPORAL_ACCUMULATION: dev::k_temporal< M, false ><<< grid, blk, 0, s >>>( a ); break;
+        case KF_TEMPORAL_FAST: dev::k_temporal< M, true ><<< grid, blk, 0, s >>>( a ); break;
+        case KF_AF_VARIANCE: dev::k_af_variance< M, false ><<< grid, blk, 0, s >>>( a ); break;
+        case KF_AF_VARIANCE_FAST: dev::k_af_variance< M, true ><<< grid, blk, 0, s >>>( a ); break;
+        case KF_GRADIENT_FUSED:
+        {
+            // one co-resident wave: blocks per SM from the occupancy calculator
+            static int blocksPerGrid = 0;
+            if( blocksPerGrid == 0 )
+            {
+                int dev = 0, sms = 0, perSm = 0;
+                cudaGetDevice( &dev );
+                cudaDeviceGetAttribute( &sms, cudaDevAttrMultiProcessorCount, dev );
+                cudaOccupancyMaxActiveBlocksPerMultiprocessor( &perSm, dev::k_gradient_fused< M >, 256, 0 );
+                blocksPerGrid = sms * ( perSm > 0 ? perSm : 1 );
+            }
+            const int need   = ( a.u.GW * a.u.GH + 255 ) / 256;
+            const int blocks = need < blocksPerGrid ? ( need > 0 ? need : 1 ) : blocksPerGrid;
+            void*     args[] = { (void*)&a };
+            return cudaLaunchCooperativeKernel( (const void*)dev::k_gradient_fused< M >, dim3( blocks ), dim3( 256 ), args, 0, s );
+        }
         case RGDN_STAGE_ANTI_FIREFLY: dev::k_antifirefly< M ><<< grid, blk, 0, s >>>( a ); break;
         case RGDN_STAGE_VARIANCE_ESTIMATION: dev::k_variance< M ><<< grid, blk, 0, s >>>( a ); break;
-        case RGDN_STAGE_ATROUS: dev::k_atrous< M ><<< grid, blk, 0, s >>>( a, iter ); break;
+        case RGDN_STAGE_ATROUS: dev::k_atrous< M, false, false ><<< grid, blk, 0, s >>>( a, iter ); break;
         case RGDN_STAGE_LUMINANCE_HISTOGRAM: dev::k_histogram< M ><<< grid, blk, 0, s >>>( a ); break;
         case RGDN_STAGE_LUMINANCE_AVG: dev::k_luminance_avg< M ><<< 1, 256, 0, s >>>( a ); break;
+        case KF_ATROUS_FAST: dev::k_atrous< M, true, false ><<< grid, blk, 0, s >>>( a, iter ); break;
+        case KF_ATROUS_FAST_HIST: dev::k_atrous< M, true, true ><<< grid, blk, 0, s >>>( a, iter ); break;
+        case KF_ATROUS_EXACT_HIST: dev::k_atrous< M, false, true ><<< grid, blk, 0, s >>>( a, iter ); break;
         default: return cudaErrorInvalidValue;
     }
     return cudaGetLastError();

@@ -203,7 +203,8 @@ class Stream:
         buf = (N.StageTiming * cap)()
         n = C.c_uint32()
         N.check(self.lib.rgdn_stream_read_timing(self.handle, buf, cap, C.byref(n)), "rgdn_stream_read_timing")
-        return {(N.STAGE_NAMES[t.stage], t.iteration): (t.launches, t.totalMs) for t in buf[:min(n.value, cap)]}
+        return {(N.KERNEL_NAMES.get(t.stage, str(t.stage)), t.iteration): (t.launches, t.totalMs)
+                for t in buf[:min(n.value, cap)]}
 
     # --- stages --------------------------------------------------------------------------
     def stage(self, stage: int, iteration: int, frame_index: int, params: N.FrameParams,

@@ -178,9 +178,12 @@ def test_end_to_end(ctx, mode_name, mode):
     s.close()
 
 
+@pytest.mark.parametrize("path", ["plain", "fused"])
 @pytest.mark.parametrize("mode_name,mode", MODES[:2])
-def test_histogram_bit_exact_same_input(ctx, mode_name, mode):
-    """Given the same HistogramInput bytes, histogram and avgLuminance are bit-exact."""
+def test_histogram_bit_exact_same_input(ctx, mode_name, mode, path):
+    """Given the same HistogramInput bytes, the histogram and avgLuminance are bit-exact —
+    for the separate histogram kernel (plain path) and for the histogram fused into the last
+    a-trous iteration (default path)."""
     W, H = 128, 72
     sc = Scene(W, H, seed=5)
     s = Stream(ctx, W, H, mode)
@@ -189,28 +192,99 @@ def test_histogram_bit_exact_same_input(ctx, mode_name, mode):
     for f in range(3, 6):
         fi = f & 1
         bufs, p = sc.generate(f)
+        if path == "plain":
+            p.flags = N.FLAG_PLAIN
         upload_frame(s, o, bufs, fi)
-        Denoiser(s).Denoise(fi, p)
-        # feed the oracle the GPU's HistogramInput and tonemapping state
-        o.plane("HISTOGRAM_INPUT", fi)[...] = s.download("HISTOGRAM_INPUT", fi)
         h0, a0, _ = s.tonemapping()
+        assert h0.sum() == 0   # cleared by the previous exposure pass
+        Denoiser(s).Denoise(fi, p)
+        hd, _, _ = s.tonemapping()   # fused: this frame's histogram already accumulated
+        # the oracle bins the GPU's HistogramInput from the same starting state
+        o.plane("HISTOGRAM_INPUT", fi)[...] = s.download("HISTOGRAM_INPUT", fi)
         o.set_tonemapping(h0, a0)
-        Tonemapping(s).CalculateExposure(fi, p)
         o.stage(N.STAGE_LUMINANCE_HISTOGRAM, 0, fi, p)
         ho = o.tonemapping()[0].copy()
+        assert ho.sum() == W * H
+        if path == "fused":
+            assert np.array_equal(hd, ho), "fused histogram differs"
+        else:
+            assert hd.sum() == 0
+        Tonemapping(s).CalculateExposure(fi, p)
         o.stage(N.STAGE_LUMINANCE_AVG, 0, fi, p)
         hg, ag, eg = s.tonemapping()
-        _, ao, eo = o.tonemapping()
-        assert hg.sum() == 0 and o.tonemapping()[0].sum() == 0  # both cleared for the next frame
+        hc, ao, eo = o.tonemapping()
+        assert hg.sum() == 0 and hc.sum() == 0  # both cleared for the next frame
         assert np.float32(ag) == np.float32(ao)
         assert np.float32(eg) == np.float32(eo)
-        # the histogram itself, before the average clears it
-        s.stage(N.STAGE_LUMINANCE_HISTOGRAM, 0, fi, p)
-        hg2, _, _ = s.tonemapping()
-        assert np.array_equal(hg2, ho)
-        assert hg2.sum() == W * H
-        s.set_tonemapping(None, ag)
+        if path == "plain":
+            # the separate histogram kernel alone, on the same input
+            s.set_tonemapping(None, ag)
+            s.stage(N.STAGE_LUMINANCE_HISTOGRAM, 0, fi, p)
+            assert np.array_equal(s.tonemapping()[0], ho)
+            s.set_tonemapping(None, ag)
     s.close()
+
+
+@pytest.mark.parametrize("mode_name,mode", MODES)
+def test_fused_exact_equals_plain(ctx, mode_name, mode):
+    """The fused kernels with IEEE math reproduce the one-kernel-per-dispatch path bit for
+    bit on every plane (DiffAccumColor is not materialised by the fused path)."""
+    W, H = 82, 46
+    sc = Scene(W, H, seed=13, lightFlickerFrom=3.0)
+    a = Stream(ctx, W, H, mode)
+    b = Stream(ctx, W, H, mode)
+    for f in range(6):
+        fi = f & 1
+        bufs, p = sc.generate(f)
+        p.atrousIterations = 5 if f % 2 else 4
+        upload_frame(a, None, bufs, fi)
+        upload_frame(b, None, bufs, fi)
+        pa, pb = p.copy(), p.copy()
+        pa.flags = N.FLAG_PLAIN
+        pb.flags = N.FLAG_EXACT_MATH
+        Denoiser(a).Denoise(fi, pa)
+        Tonemapping(a).CalculateExposure(fi, pa)
+        Denoiser(b).Denoise(fi, pb)
+        Tonemapping(b).CalculateExposure(fi, pb)
+        ga, gb = gpu_planes(a), gpu_planes(b)
+        for key in ga:
+            if key[0] == "DIFF_ACCUM_COLOR":
+                continue
+            assert np.array_equal(ga[key][0], gb[key][0]), f"frame {f}: {key} differs"
+        ta, tb = a.tonemapping(), b.tonemapping()
+        assert np.array_equal(ta[0], tb[0]) and ta[1] == tb[1]
+    a.close()
+    b.close()
+
+
+@pytest.mark.parametrize("mode_name,mode", MODES)
+def test_fast_math_close_to_exact(ctx, mode_name, mode):
+    """The default path (hardware exp2/log2 in continuous weights) stays within the parity
+    tolerance of the exact path over a frame sequence."""
+    W, H = 96, 54
+    sc = Scene(W, H, seed=17, lightFlickerFrom=3.0)
+    a = Stream(ctx, W, H, mode)
+    b = Stream(ctx, W, H, mode)
+    for f in range(8):
+        fi = f & 1
+        bufs, p = sc.generate(f)
+        upload_frame(a, None, bufs, fi)
+        upload_frame(b, None, bufs, fi)
+        pa = p.copy()
+        pa.flags = N.FLAG_PLAIN
+        for s, q in ((a, pa), (b, p)):
+            Denoiser(s).Denoise(fi, q)
+            Tonemapping(s).CalculateExposure(fi, q)
+    img = a.image("PRE_FINAL", fi)
+    ga = F.decode(a.download("PRE_FINAL", fi), img.format)
+    gb = F.decode(b.download("PRE_FINAL", fi), img.format)
+    err = F.texel_rel_err(gb, ga, atol=1e-4 * float(np.percentile(ga, 99)))
+    if mode == N.STORAGE_FP32:
+        assert err.max() <= 1e-3, f"max rel err {err.max():.3e}"
+    else:
+        assert np.mean(err <= 1e-2) >= 0.99
+    a.close()
+    b.close()
 
 
 def test_batch_equals_sequential(ctx):
