@@ -288,6 +288,23 @@ typedef struct rgdn_job
  * be distinct and share one storage mode. */
 rgdn_status rgdn_submit_batch( rgdn_context* ctx, const rgdn_job* jobs, uint32_t n, rgdn_cuda_stream cudaStream );
 
+/* ---- without device allocation ----------------------------------------------------------- */
+/* No counterpart in the reference. The four gradient a-trous iterations
+ * (CmASVGFGradientAtrous.comp, as RGDN_STAGE_GRADIENT_ATROUS 0..3) for a caller that may not
+ * allocate device memory — a host application that owns every allocation through a fixed
+ * budget, or a frame loop that cannot afford the device synchronisation of cudaMalloc /
+ * cudaFree. The caller passes its own images (rgba8 per stratum, ((W+1)/3) x ((H+1)/3), dense
+ * rows, 4-byte aligned): `samples` (read only), `filtered` (the result, the reference's final
+ * DISPingGradient) and `history` (iteration 0's output, DISGradientHistory). The one
+ * intermediate image lives in a fixed array inside the library: at most 1280 x 720 strata
+ * (3840x2160 renders); larger sizes return RGDN_WRONG_FUNCTION_ARGUMENT. Nothing is allocated.
+ * The first call on a device looks the array up (cudaGetSymbolAddress) with that device
+ * current; make that first call before capturing a stream. All calls share the one array:
+ * calls whose work overlaps on the GPU (other streams, other threads) race on it and must be
+ * serialised by the caller. `filtered` must not alias `samples` or `history`. */
+rgdn_status rgdn_gradient_atrous_noalloc( const uint32_t* samples, uint32_t* filtered, uint32_t* history, uint32_t renderWidth,
+                                          uint32_t renderHeight, rgdn_cuda_stream cudaStream );
+
 /* ---- per-kernel timing (tracing) ----------------------------------------------------- */
 /* With timing on, every kernel the stream launches is bracketed by two CUDA events on the
  * launching stream. rgdn_stream_read_timing waits for them and returns, per (stage,

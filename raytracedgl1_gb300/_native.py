@@ -117,6 +117,7 @@ SIGNATURES = [
     ("rgdn_context_launch_count", _I, [_VP, C.POINTER(_U64)]),
     ("rgdn_api_version", _U32, []),
     ("rgdn_histogram_bin_table", _I, [C.c_float, C.c_float, C.POINTER(C.c_uint8)]),
+    ("rgdn_gradient_atrous_noalloc", _I, [_VP, _VP, _VP, _U32, _U32, _VP]),
     ("rgdn_stream_set_timing", _I, [_VP, _U32]),
     ("rgdn_stream_read_timing", _I, [_VP, C.POINTER(StageTiming), _U32, C.POINTER(_U32)]),
 ]

@@ -30,7 +30,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-lineinfo", "-O3", "--fmad=false", "-std=c++17", "-Xcompiler", "-fPIC",
                      "-Xcompiler", "-O3", "-I" + INCLUDE, "-I" + CSRC]
 CU_SOURCES = ["rgdn_api.cu", "rgdn_mode_ref.cu", "rgdn_mode_f32.cu", "rgdn_mode_f16.cu",
-              "rgdn_mode_bf16.cu"]
+              "rgdn_mode_bf16.cu", "rgdn_noalloc.cu"]
 HEADERS = ["rgdn_internal.h", "rgdn_kernels.cuh", "rgdn_codec.h"]
 
 LIB_RGDN = os.path.join(LIBDIR, "librgdn.so")

@@ -376,16 +376,15 @@ template< int M > __device__ __forceinline__ void gradient_sample_px( const Fram
     a.gradPrevPix[ gi ] = (uint8_t)curStrataPos;
 }
 
-// CmASVGFGradientAtrous.comp:42-105 — one iteration, one stratum
-__device__ __forceinline__ void gradient_atrous_px( const FrameArgs& a, const int gx, const int gy, const int iter, const float* u8 )
+// CmASVGFGradientAtrous.comp:42-105 — one iteration, one stratum, from `src` into `dst`
+// (and `hist` on iteration 0), all GW x GH rgba8 images
+__device__ __forceinline__ void gradient_atrous_core( const Uniform& u, const uint32_t* src, uint32_t* dst, uint32_t* hist, const int gx,
+                                                      const int gy, const int iter, const float* u8 )
 {
-    const Uniform&  u    = a.u;
-    const uint32_t* src  = ( iter % 2 == 0 ) ? a.disPing : a.disPong;
-    uint32_t*       dst  = ( iter % 2 == 0 ) ? a.disPong : a.disPing;
-    const int       step = 1 << iter;
-    const Area      a0   = cb_area( u, gx * STRATA );
-    const Area      ga   = { a0.l / STRATA, a0.r / STRATA, a0.h / STRATA };
-    const float     kern[ 2 ][ 2 ] = { { 1.0f, 0.5f }, { 0.5f, 0.25f } };
+    const int   step = 1 << iter;
+    const Area  a0   = cb_area( u, gx * STRATA );
+    const Area  ga   = { a0.l / STRATA, a0.r / STRATA, a0.h / STRATA };
+    const float kern[ 2 ][ 2 ] = { { 1.0f, 0.5f }, { 0.5f, 0.25f } };
     float3 out = f3( 0, 0, 0 );
     float  ws  = 0.0f;
 #pragma unroll
@@ -405,7 +404,15 @@ __device__ __forceinline__ void gradient_atrous_px( const FrameArgs& a, const in
     const uint32_t packed = pack_rgba8( out.x, out.y, out.z, 0.0f );
     const int      gi     = gy * u.GW + gx;
     dst[ gi ] = packed;
-    if( iter == 0 ) a.disHist[ gi ] = packed;
+    if( iter == 0 && hist ) hist[ gi ] = packed;
+}
+
+// the stream's ping-pong routing (CmASVGFGradientAtrous.comp:89-104)
+__device__ __forceinline__ void gradient_atrous_px( const FrameArgs& a, const int gx, const int gy, const int iter, const float* u8 )
+{
+    const uint32_t* src = ( iter % 2 == 0 ) ? a.disPing : a.disPong;
+    uint32_t*       dst = ( iter % 2 == 0 ) ? a.disPong : a.disPing;
+    gradient_atrous_core( a.u, src, dst, a.disHist, gx, gy, iter, u8 );
 }
 
 __device__ __forceinline__ void fill_u8( float* u8, int t )
