@@ -166,15 +166,22 @@ def stage_bytes(storage: str) -> dict:
     b["luminance_histogram"] = 2
     b["luminance_avg"] = 0
     # fused kernels
-    b["gradient_fused"] = b["gradient_samples"] + 4 * b["gradient_atrous"]
-    b["temporal_fast"] = b["temporal_accumulation"]
-    b["af_variance"] = b["af_variance_fast"] = 3 * col3 + (2 + 4 + hl + mom) + 2 * col3 + cv
+    b["temporal_fast"] = b["temporal_exact_geom"] = b["temporal_accumulation"] + 16   # + record write
+    # with the previous record: 16 B instead of depth (2) + normal (4) at the prev taps
+    b["temporal_fast_gp"] = b["temporal_exact_geom_gp"] = b["temporal_accumulation"] + 16 + 10
+    # fused kernels read the 16-byte geometry record instead of normal + depth + metallic-roughness
+    b["anti_firefly_fast"] = b["anti_firefly"]
+    b["variance_fast"] = b["variance_exact_geom"] = (col3 + 16 + hl + mom) + cv
     return b
 
 
 def kernel_bytes(name: str, it: int, niter: int, per_px: dict) -> float:
-    if name in ("atrous", "atrous_fast", "atrous_fast_hist", "atrous_exact_hist"):
+    if name == "atrous":
         return per_px["atrous0"] if it == 0 else per_px["atrous_last"] if it == niter - 1 else per_px["atrous"]
+    if name in ("atrous_fast", "atrous_fast_hist", "atrous_exact", "atrous_exact_hist"):
+        # the geometry record (16 B) replaces normal (4) + depth (2) + metallic-roughness (2)
+        base = per_px["atrous0"] if it == 0 else per_px["atrous_last"] if it == niter - 1 else per_px["atrous"]
+        return base + 8
     return per_px[name]
 
 

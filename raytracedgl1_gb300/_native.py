@@ -127,8 +127,9 @@ STAGE_NAMES = ["gradient_samples", "gradient_atrous", "temporal_accumulation", "
 # kernels of the default fused path (ids above the rgdn_stage range, see rgdn_internal.h)
 KERNEL_NAMES = dict(enumerate(STAGE_NAMES))
 KERNEL_NAMES.update({100: "atrous_fast", 101: "atrous_fast_hist", 102: "temporal_fast",
-                     103: "af_variance", 104: "af_variance_fast", 105: "gradient_fused",
-                     106: "atrous_exact_hist"})
+                     103: "anti_firefly_fast", 104: "variance_fast", 106: "atrous_exact_hist",
+                     107: "atrous_exact", 108: "temporal_exact_geom", 109: "variance_exact_geom",
+                     110: "temporal_fast_gp", 111: "temporal_exact_geom_gp"})
 
 _lib = None
 

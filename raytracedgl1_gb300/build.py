@@ -30,7 +30,10 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-lineinfo", "-O3", "--fmad=false", "-std=c++17", "-Xcompiler", "-fPIC",
                      "-Xcompiler", "-O3", "-I" + INCLUDE, "-I" + CSRC]
 CU_SOURCES = ["rgdn_api.cu", "rgdn_mode_ref.cu", "rgdn_mode_f32.cu", "rgdn_mode_f16.cu",
-              "rgdn_mode_bf16.cu", "rgdn_noalloc.cu"]
+              "rgdn_mode_bf16.cu", "rgdn_noalloc.cu", "rgdn_fast_ref.cu", "rgdn_fast_f32.cu",
+              "rgdn_fast_f16.cu", "rgdn_fast_bf16.cu"]
+# the FAST kernels carry no threshold decisions: contraction to fused multiply-add allowed
+FMAD_TRUE = {"rgdn_fast_ref.cu", "rgdn_fast_f32.cu", "rgdn_fast_f16.cu", "rgdn_fast_bf16.cu"}
 HEADERS = ["rgdn_internal.h", "rgdn_kernels.cuh", "rgdn_codec.h"]
 
 LIB_RGDN = os.path.join(LIBDIR, "librgdn.so")
@@ -69,7 +72,8 @@ def build_rgdn(force: bool = False, jobs: int | None = None) -> str:
         o = os.path.join(OBJDIR, src.replace(".cu", ".o"))
         objs.append(o)
         if force or _stale(o, [s] + hdrs):
-            todo.append([nvcc] + NVCC_FLAGS + ["-c", s, "-o", o])
+            flags = [f if f != "--fmad=false" or src not in FMAD_TRUE else "--fmad=true" for f in NVCC_FLAGS]
+            todo.append([nvcc] + flags + ["-c", s, "-o", o])
     if todo:
         with ThreadPoolExecutor(max_workers=jobs or min(len(todo), os.cpu_count() or 4)) as ex:
             list(ex.map(_run, todo))

@@ -111,14 +111,15 @@ FbDesc fb_desc( uint32_t fb, uint32_t storage )
 constexpr size_t kAlign = 256;
 inline size_t align_up( size_t v ) { return ( v + kAlign - 1 ) & ~( kAlign - 1 ); }
 
-StageLauncher launcher_for( uint32_t storage )
+StageLauncher launcher_for( uint32_t storage, int stage )
 {
+    const bool fast = is_fast_kernel( stage );
     switch( storage )
     {
-        case RGDN_STORAGE_REF: return launch_stage_ref;
-        case RGDN_STORAGE_FP32: return launch_stage_f32;
-        case RGDN_STORAGE_FP16: return launch_stage_f16;
-        case RGDN_STORAGE_BF16: return launch_stage_bf16;
+        case RGDN_STORAGE_REF: return fast ? launch_fast_ref : launch_stage_ref;
+        case RGDN_STORAGE_FP32: return fast ? launch_fast_f32 : launch_stage_f32;
+        case RGDN_STORAGE_FP16: return fast ? launch_fast_f16 : launch_stage_f16;
+        case RGDN_STORAGE_BF16: return fast ? launch_fast_bf16 : launch_stage_bf16;
         default: return nullptr;
     }
 }
@@ -177,6 +178,8 @@ struct rgdn_stream
     PlaneSlot              planes[ RGDN_FB_COUNT ];
     Tonemapping*           tm     = nullptr;
     uint8_t*               binLut = nullptr;
+    float4*                geom[ 2 ] = { nullptr, nullptr };
+    bool                   geomValid[ 2 ] = { false, false };   // slot holds its frame's record
     float                  lutMin = NAN, lutMax = NAN;
     std::vector< uint8_t > hostLut;
     // per-kernel timing
@@ -205,9 +208,10 @@ size_t stream_layout( uint32_t W, uint32_t H, uint32_t storage, PlaneSlot* plane
 {
     const uint32_t GW = std::max( 1u, ( W + 1 ) / 3 ), GH = std::max( 1u, ( H + 1 ) / 3 );
     size_t off = 0;
-    // tonemapping state + histogram bin table first
+    // tonemapping state, histogram bin table, geometry records of the default path (2 slots)
     off += align_up( sizeof( Tonemapping ) );
     off += align_up( 65536 );
+    off += 2 * align_up( (size_t)W * H * 16 );
     for( uint32_t fb = 0; fb < RGDN_FB_COUNT; fb++ )
     {
         FbDesc   d     = fb_desc( fb, storage );
@@ -256,6 +260,21 @@ void fill_args( rgdn_stream* s, uint32_t fi, const rgdn_frame_params* p, FrameAr
     Uniform& u = a.u;
     u.W = (int)s->W; u.H = (int)s->H; u.GW = (int)s->GW; u.GH = (int)s->GH;
     u.rw = (float)s->W; u.rh = (float)s->H;
+    u.isx = 1.0f / ( u.rw / 2.0f );
+    u.isy = 1.0f / u.rh;
+    // proj * view, column-major, for the FAST virtual-motion reprojection
+    for( int c = 0; c < 4; c++ )
+        for( int r = 0; r < 4; r++ )
+        {
+            double v = 0.0, vPrev = 0.0;
+            for( int k = 0; k < 4; k++ )
+            {
+                v += (double)p->projection[ k * 4 + r ] * (double)p->view[ c * 4 + k ];
+                vPrev += (double)p->projectionPrev[ k * 4 + r ] * (double)p->viewPrev[ c * 4 + k ];
+            }
+            u.vp[ c * 4 + r ]     = (float)v;
+            u.vpPrev[ c * 4 + r ] = (float)vPrev;
+        }
     memcpy( u.view, p->view, sizeof( u.view ) );
     memcpy( u.viewPrev, p->viewPrev, sizeof( u.viewPrev ) );
     memcpy( u.proj, p->projection, sizeof( u.proj ) );
@@ -327,6 +346,8 @@ void fill_args( rgdn_stream* s, uint32_t fi, const rgdn_frame_params* p, FrameAr
 #undef CUR
 #undef PRV
     a.tm       = s->tm;
+    a.geom     = s->geom[ fi & 1 ];
+    a.geomPrev = s->geom[ ( fi & 1 ) ^ 1 ];
     a.binLut   = s->binLut;
     a.phiTab   = s->ctx->phiTab;
     a.thetaTab = s->ctx->thetaTab;
@@ -347,7 +368,9 @@ cudaEvent_t take_event( rgdn_stream* s )
 
 rgdn_status launch( rgdn_stream* s, const FrameArgs& a, int stage, int iter, cudaStream_t cs )
 {
-    StageLauncher L = launcher_for( s->storage );
+    // the plain temporal pass does not write the geometry record of its slot
+    if( stage == RGDN_STAGE_TEMPORAL_ACCUMULATION ) s->geomValid[ a.geom == s->geom[ 0 ] ? 0 : 1 ] = false;
+    StageLauncher L = launcher_for( s->storage, stage );
     if( !L ) return RGDN_INTERNAL_ERROR;
     cudaEvent_t ea = nullptr, eb = nullptr;
     if( s->timing )
@@ -403,10 +426,10 @@ rgdn_status run_denoise( rgdn_stream* s, uint32_t fi, const rgdn_frame_params* p
     return RGDN_SUCCESS;
 }
 
-// Default path: gradient chain in one cooperative launch, temporal accumulation, anti-firefly
-// fused with variance (DiffAccumColor is not materialised: nothing reads it after the
-// variance), the a-trous iterations, and the histogram accumulated by the last iteration
-// (HistogramInput is still written). Continuous weights use FAST math.
+// Default path: gradient samples and the 4 gradient a-trous iterations, temporal accumulation
+// (which also writes the per-pixel geometry record the later passes read), anti-firefly on
+// packed values, variance, the a-trous iterations, and the histogram accumulated by the last
+// iteration (HistogramInput is still written). Continuous weights use FAST math.
 rgdn_status run_denoise_fused( rgdn_stream* s, uint32_t fi, const rgdn_frame_params* p, cudaStream_t cs )
 {
     rgdn_status r = ensure_bin_lut( s, p, cs );
@@ -414,16 +437,25 @@ rgdn_status run_denoise_fused( rgdn_stream* s, uint32_t fi, const rgdn_frame_par
     FrameArgs a;
     fill_args( s, fi, p, a );
     const bool exact = ( p->flags & RGDN_FLAG_EXACT_MATH ) != 0;
-    if( !( p->flags & RGDN_FLAG_SKIP_GRADIENTS ) && ( r = launch( s, a, KF_GRADIENT_FUSED, 0, cs ) ) != RGDN_SUCCESS ) return r;
-    if( ( r = launch( s, a, exact ? (int)RGDN_STAGE_TEMPORAL_ACCUMULATION : (int)KF_TEMPORAL_FAST, 0, cs ) ) != RGDN_SUCCESS ) return r;
-    if( ( r = launch( s, a, exact ? KF_AF_VARIANCE : KF_AF_VARIANCE_FAST, 0, cs ) ) != RGDN_SUCCESS ) return r;
+    if( !( p->flags & RGDN_FLAG_SKIP_GRADIENTS ) )
+    {
+        if( ( r = launch( s, a, RGDN_STAGE_GRADIENT_SAMPLES, 0, cs ) ) != RGDN_SUCCESS ) return r;
+        for( int i = 0; i < 4; i++ )
+            if( ( r = launch( s, a, RGDN_STAGE_GRADIENT_ATROUS, i, cs ) ) != RGDN_SUCCESS ) return r;
+    }
+    const bool gp = s->geomValid[ fi ^ 1u ];
+    const int  ta = exact ? ( gp ? KF_TEMPORAL_EXACT_GEOM_GP : KF_TEMPORAL_EXACT_GEOM ) : ( gp ? KF_TEMPORAL_FAST_GP : KF_TEMPORAL_FAST );
+    if( ( r = launch( s, a, ta, 0, cs ) ) != RGDN_SUCCESS ) return r;
+    s->geomValid[ fi ] = true;
+    if( ( r = launch( s, a, KF_ANTI_FIREFLY_FAST, 0, cs ) ) != RGDN_SUCCESS ) return r;
+    if( ( r = launch( s, a, exact ? KF_VARIANCE_EXACT_GEOM : KF_VARIANCE_FAST, 0, cs ) ) != RGDN_SUCCESS ) return r;
     // a histogram no exposure pass consumed is discarded: this frame's replaces it
     if( s->histPending && cudaMemsetAsync( s->tm->histogram, 0, sizeof( s->tm->histogram ), cs ) != cudaSuccess )
         return RGDN_DEVICE_ERROR;
     for( uint32_t i = 0; i < a.u.niter; i++ )
     {
         const bool last = i + 1 == a.u.niter;
-        const int k = exact ? ( last ? KF_ATROUS_EXACT_HIST : (int)RGDN_STAGE_ATROUS ) : ( last ? KF_ATROUS_FAST_HIST : KF_ATROUS_FAST );
+        const int k = exact ? ( last ? KF_ATROUS_EXACT_HIST : KF_ATROUS_EXACT ) : ( last ? KF_ATROUS_FAST_HIST : KF_ATROUS_FAST );
         if( ( r = launch( s, a, k, (int)i, cs ) ) != RGDN_SUCCESS ) return r;
     }
     s->histPending = true;
@@ -575,6 +607,9 @@ static rgdn_status stream_alloc( rgdn_stream* s, uint32_t W, uint32_t H )
     stream_layout( W, H, s->storage, s->planes, (uint8_t*)block );
     s->tm     = (Tonemapping*)block;
     s->binLut = (uint8_t*)block + align_up( sizeof( Tonemapping ) );
+    s->geom[ 0 ] = (float4*)( (uint8_t*)block + align_up( sizeof( Tonemapping ) ) + align_up( 65536 ) );
+    s->geom[ 1 ] = (float4*)( (uint8_t*)s->geom[ 0 ] + align_up( (size_t)W * H * 16 ) );
+    s->geomValid[ 0 ] = s->geomValid[ 1 ] = false;
     s->lutMin = s->lutMax = NAN;
     return RGDN_SUCCESS;
 }
@@ -680,6 +715,7 @@ rgdn_status rgdn_stream_bind_framebuffer( rgdn_stream* s, uint32_t fb, uint32_t 
     PlaneSlot& p    = s->planes[ fb ];
     const int  slot = p.prev ? (int)frameIndex : 0;
     p.ptr[ slot ]   = devicePtr ? (uint8_t*)devicePtr : p.own[ slot ];
+    if( fb == RGDN_FB_NORMAL || fb == RGDN_FB_DEPTH_WORLD || fb == RGDN_FB_METALLIC_ROUGHNESS ) s->geomValid[ frameIndex ] = false;
     return RGDN_SUCCESS;
 }
 
@@ -690,6 +726,7 @@ rgdn_status rgdn_stream_upload( rgdn_stream* s, uint32_t fb, uint32_t frameIndex
     const PlaneSlot& p = s->planes[ fb ];
     if( !p.ptr[ 0 ] || bytes != (size_t)p.w * p.h * p.texel ) return RGDN_WRONG_FUNCTION_ARGUMENT;
     cudaSetDevice( s->ctx->device );
+    if( fb == RGDN_FB_NORMAL || fb == RGDN_FB_DEPTH_WORLD || fb == RGDN_FB_METALLIC_ROUGHNESS ) s->geomValid[ frameIndex ] = false;
     return cuda_status( cudaMemcpyAsync( plane_ptr_mut( s, fb, frameIndex ), src, bytes, cudaMemcpyDefault, (cudaStream_t)cs ) );
 }
 

@@ -1,0 +1,11 @@
+// FAST kernels (continuous arithmetic only) for the bf16 storage mode; compiled with
+// fused multiply-add contraction.
+#include "rgdn_kernels.cuh"
+
+namespace rgdn
+{
+cudaError_t launch_fast_bf16( const FrameArgs& a, int stage, int iter, cudaStream_t s )
+{
+    return launch_fast_t< MODE_BF16 >( a, stage, iter, s );
+}
+}  // namespace rgdn

@@ -1,0 +1,11 @@
+// FAST kernels (continuous arithmetic only) for the ref storage mode; compiled with
+// fused multiply-add contraction.
+#include "rgdn_kernels.cuh"
+
+namespace rgdn
+{
+cudaError_t launch_fast_ref( const FrameArgs& a, int stage, int iter, cudaStream_t s )
+{
+    return launch_fast_t< MODE_REF >( a, stage, iter, s );
+}
+}  // namespace rgdn

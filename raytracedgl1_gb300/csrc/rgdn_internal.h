@@ -36,7 +36,9 @@ struct Uniform
     int      W, H;           // render size (image size)
     int      GW, GH;         // gradient image size ((W+1)/3, (H+1)/3)
     float    rw, rh;         // renderWidth / renderHeight as floats
+    float    isx, isy;       // 1 / (renderWidth / 2), 1 / renderHeight (ShaderCommonGLSLFunc.h:273-274)
     float    view[ 16 ], viewPrev[ 16 ], proj[ 16 ], projPrev[ 16 ];
+    float    vp[ 16 ], vpPrev[ 16 ];   // proj * view, projPrev * viewPrev (FAST path only)
     float    camPos[ 3 ], camPosPrev[ 3 ];
     float    timeDelta, minLog, maxLog;
     uint32_t stopEyeAdaptation;
@@ -103,6 +105,10 @@ struct FrameArgs
     uint32_t*       disHist;
     const uint32_t* disHistPrev;
     uint8_t*        gradPrevPix;
+    // per-pixel geometry record of the current frame, written by the fused temporal pass:
+    // (decoded normal xyz, bits: depth fp16 | metallic-roughness rg8 << 16)
+    float4*       geom;
+    const float4* geomPrev;   // the previous frame's record (valid when the host says so)
     // tonemapping
     Tonemapping*   tm;
     const uint8_t* binLut;           // 65536-entry fp16 bits -> histogram bin
@@ -117,10 +123,14 @@ enum FusedKernel : int
     KF_ATROUS_FAST      = 100,   // a-trous iteration with FAST weights
     KF_ATROUS_FAST_HIST = 101,   // last iteration + composition + fused histogram
     KF_TEMPORAL_FAST    = 102,   // temporal accumulation, FAST specular weights
-    KF_AF_VARIANCE      = 103,   // anti-firefly + variance in one kernel
-    KF_AF_VARIANCE_FAST = 104,
-    KF_GRADIENT_FUSED   = 105,   // gradient samples + 4 gradient a-trous, one cooperative launch
+    KF_ANTI_FIREFLY_FAST = 103,  // anti-firefly, packed min/max (exact)
+    KF_VARIANCE_FAST     = 104,  // variance reading the geometry record, FAST weights
     KF_ATROUS_EXACT_HIST = 106,  // last iteration + fused histogram, IEEE math
+    KF_ATROUS_EXACT      = 107,  // a-trous iteration reading the geometry record, IEEE math
+    KF_TEMPORAL_EXACT_GEOM = 108,  // temporal accumulation writing the geometry record, IEEE math
+    KF_VARIANCE_EXACT_GEOM = 109,  // variance reading the geometry record, IEEE math
+    KF_TEMPORAL_FAST_GP    = 110,  // KF_TEMPORAL_FAST reading the previous frame's geometry record
+    KF_TEMPORAL_EXACT_GEOM_GP = 111,
 };
 
 // Launches one stage for one frame. Returns the CUDA error of the launch.
@@ -130,5 +140,11 @@ cudaError_t launch_stage_ref( const FrameArgs& a, int stage, int iter, cudaStrea
 cudaError_t launch_stage_f32( const FrameArgs& a, int stage, int iter, cudaStream_t s );
 cudaError_t launch_stage_f16( const FrameArgs& a, int stage, int iter, cudaStream_t s );
 cudaError_t launch_stage_bf16( const FrameArgs& a, int stage, int iter, cudaStream_t s );
+// the FAST kernels (KF_ATROUS_FAST, KF_ATROUS_FAST_HIST, KF_VARIANCE_FAST)
+cudaError_t launch_fast_ref( const FrameArgs& a, int stage, int iter, cudaStream_t s );
+cudaError_t launch_fast_f32( const FrameArgs& a, int stage, int iter, cudaStream_t s );
+cudaError_t launch_fast_f16( const FrameArgs& a, int stage, int iter, cudaStream_t s );
+cudaError_t launch_fast_bf16( const FrameArgs& a, int stage, int iter, cudaStream_t s );
+inline bool is_fast_kernel( int stage ) { return stage == KF_ATROUS_FAST || stage == KF_ATROUS_FAST_HIST || stage == KF_VARIANCE_FAST; }
 
 }  // namespace rgdn

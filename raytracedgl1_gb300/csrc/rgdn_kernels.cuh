@@ -11,7 +11,6 @@
 // threads map x -> threadIdx.x so that a warp reads 32 consecutive texels of a row.
 #pragma once
 
-#include <cooperative_groups.h>
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
 
@@ -22,7 +21,6 @@ namespace rgdn
 {
 namespace dev
 {
-namespace cg = cooperative_groups;
 
 // ------------------------------------------------------------------------------------------
 // GLSL semantics
@@ -76,6 +74,28 @@ __device__ __forceinline__ float3 decode_normal( const FrameArgs& a, uint32_t p 
     return f3( ph.x * th.x, ph.x * th.y, ph.y );
 }
 
+// Geometry record (fused path): decoded normal + raw depth (fp16 bits) + metallic-roughness (rg8)
+// — exactly the values the separate images decode to, fetched with one 16-byte load.
+struct Geo
+{
+    float3   n;
+    uint32_t bits;   // depth fp16 | mr << 16
+};
+__device__ __forceinline__ float4 geo_pack( float3 n, uint16_t depthBits, uint16_t mr )
+{
+    return make_float4( n.x, n.y, n.z, __uint_as_float( (uint32_t)depthBits | ( (uint32_t)mr << 16 ) ) );
+}
+__device__ __forceinline__ Geo geo_load( const float4* g, int i )
+{
+    const float4 r = g[ i ];
+    return { make_float3( r.x, r.y, r.z ), __float_as_uint( r.w ) };
+}
+// the record of an all-zero texel (outside the image): normal code 0 decodes to (0, 0, 1)
+__device__ __forceinline__ Geo geo_zero() { return { make_float3( 0.0f, 0.0f, 1.0f ), 0u }; }
+__device__ __forceinline__ float geo_depth( const Geo& g ) { return __half2float( __ushort_as_half( (uint16_t)( g.bits & 0xFFFFu ) ) ); }
+__device__ __forceinline__ uint32_t geo_rough8( const Geo& g ) { return g.bits >> 24; }
+__device__ __forceinline__ uint32_t geo_metal8( const Geo& g ) { return ( g.bits >> 16 ) & 0xFFu; }
+
 __device__ __forceinline__ float3 e5( uint32_t p )
 {
     rgdn::f3 c = decode_e5( p );
@@ -98,6 +118,7 @@ template<> struct Wm< false >
 {
     __device__ static float pow128( float x ) { return powf( x, 128.0f ); }
     __device__ static float powv( float x, float y ) { return powf( x, y ); }
+    __device__ static float pow01( float x, float y ) { return powf( x, y ); }
     __device__ static float expn( float x ) { return expf( x ); }
     __device__ static float madd( float a, float b, float c ) { return a * b + c; }
 };
@@ -109,6 +130,18 @@ template<> struct Wm< true >
         return x;
     }
     __device__ static float powv( float x, float y ) { return ex2_approx( y * log2f( x ) ); }
+    // x^y for x in [0, 1], y > 0: near 1 (d = 1 - x < 1/16, exact) ln x = -(d + d^2/2 + d^3/3 +
+    // d^4/4 + d^5/5) to 1e-8 absolute; elsewhere the accurate log2
+    __device__ static float pow01( float x, float y )
+    {
+        const float d = 1.0f - x;
+        if( d < 0.0625f )
+        {
+            const float ln = -d * ( 1.0f + d * ( 0.5f + d * ( 0.33333334f + d * ( 0.25f + d * 0.2f ) ) ) );
+            return ex2_approx( y * ln * 1.44269504088896341f );
+        }
+        return ex2_approx( y * log2f( x ) );
+    }
     __device__ static float expn( float x ) { return ex2_approx( x * 1.44269504088896341f ); }
     __device__ static float madd( float a, float b, float c ) { return __fmaf_rn( a, b, c ); }
 };
@@ -253,8 +286,8 @@ __device__ __forceinline__ int2 regular_from_cb( const Uniform& u, int cx, int c
 __device__ __forceinline__ float2 prev_screen_pos( const Uniform& u, float2 m, int px, int py )
 {
     const float sx = u.rw / 2.0f, sy = u.rh;
-    const float isx = 1.0f / sx, isy = 1.0f / sy;
-    return make_float2( ( ( (float)px + 0.5f ) * isx + m.x ) * sx, ( ( (float)py + 0.5f ) * isy + m.y ) * sy );
+    // u.isx = 1 / sx and u.isy = 1 / sy, divided once on the host (IEEE, the same bits)
+    return make_float2( ( ( (float)px + 0.5f ) * u.isx + m.x ) * sx, ( ( (float)py + 0.5f ) * u.isy + m.y ) * sy );
 }
 // ShaderCommonGLSLFunc.h:368-390
 __device__ __forceinline__ bool test_depth( float z, float zPrev, float zMotion ) { return fabsf( z - zPrev + zMotion ) / fabsf( z ) < 0.1f; }
@@ -292,54 +325,67 @@ __device__ __forceinline__ float4 ld_rgba8t( const Uniform& u, const uint32_t* p
     return ( x >= 0 && y >= 0 && x < u.GW && y < u.GH ) ? unpack_rgba8_t( p[ y * u.GW + x ], u8 ) : make_float4( 0, 0, 0, 0 );
 }
 
-template< int M > __device__ __forceinline__ void gradient_sample_px( const FrameArgs& a, const int gx, const int gy, const float* u8 )
+template< int M >
+__device__ __forceinline__ void gradient_sample_px( const FrameArgs& a, uint32_t* dst, const int gx, const int gy, const float* u8 )
 {
     const Uniform& u  = a.u;
     const int      gi = gy * u.GW + gx;
     if( u.gradMultD < 0.001f && u.gradMultI < 0.001f && u.gradMultS < 0.001f )
     {
-        a.disPing[ gi ]     = 0u;
+        dst[ gi ]           = 0u;
         a.gradPrevPix[ gi ] = STRATA * STRATA + 1;
         return;
     }
     const uint32_t prevStrataPos = a.gradPrevPix[ gi ];
+    // the 9 stratum positions: motion first, then the previous frame's luminance at the
+    // forward-projected pixel (two rounds of independent loads instead of 18 in sequence)
+    int2   ipos[ STRATA * STRATA ];
+    float2 ilum[ STRATA * STRATA ];
+#pragma unroll
+    for( int k = 0; k < STRATA * STRATA; k++ )
+    {
+        const int cx = gx * STRATA + k % STRATA, cy = gy * STRATA + k / STRATA;
+        float2    m  = make_float2( 0, 0 );
+        if( inside( u, cx, cy ) )
+        {
+            const ushort4 mo = a.motion[ cy * u.W + cx ];
+            m                = make_float2( h2f( mo.x ), h2f( mo.y ) );
+        }
+        const float2 pp = prev_screen_pos( u, m, cx, cy );
+        ipos[ k ]       = make_int2( (int)floorf( pp.x ), (int)floorf( pp.y ) );
+    }
+#pragma unroll
+    for( int k = 0; k < STRATA * STRATA; k++ )
+    {
+        float2 il = make_float2( 0, 0 );
+        if( inside( u, ipos[ k ].x, ipos[ k ].y ) )
+        {
+            const uint32_t g = a.gradInputsPrev[ ipos[ k ].y * u.W + ipos[ k ].x ];
+            il               = make_float2( h2f( (uint16_t)( g & 0xFFFFu ) ), h2f( (uint16_t)( g >> 16 ) ) );
+        }
+        ilum[ k ] = il;
+    }
     int2     prevShadingPix = make_int2( 0, 0 ), curShadingPix = make_int2( 0, 0 );
     uint32_t curStrataPos   = 0;
     float2   prevLum        = make_float2( 0, 0 );
-    for( int yy = 0; yy < STRATA; yy++ )
+    // (a) the brightest sample of the stratum, skipping last frame's position (RtGradients.rgen:65-96)
+#pragma unroll
+    for( int k = 0; k < STRATA * STRATA; k++ )
     {
-        for( int xx = 0; xx < STRATA; xx++ )
+        if( (uint32_t)k == prevStrataPos ) continue;
+        if( fmaxf( ilum[ k ].x, ilum[ k ].y ) > fmaxf( prevLum.x, prevLum.y ) )
         {
-            if( (uint32_t)( yy * STRATA + xx ) == prevStrataPos ) continue;
-            const int cx = gx * STRATA + xx, cy = gy * STRATA + yy;
-            float2    m  = make_float2( 0, 0 );
-            if( inside( u, cx, cy ) )
-            {
-                const ushort4 mo = a.motion[ cy * u.W + cx ];
-                m                = make_float2( h2f( mo.x ), h2f( mo.y ) );
-            }
-            const float2 pp = prev_screen_pos( u, m, cx, cy );
-            const int2   ip = make_int2( (int)floorf( pp.x ), (int)floorf( pp.y ) );
-            float2       il = make_float2( 0, 0 );
-            if( inside( u, ip.x, ip.y ) )
-            {
-                const uint32_t g = a.gradInputsPrev[ ip.y * u.W + ip.x ];
-                il               = make_float2( h2f( (uint16_t)( g & 0xFFFFu ) ), h2f( (uint16_t)( g >> 16 ) ) );
-            }
-            if( fmaxf( il.x, il.y ) > fmaxf( prevLum.x, prevLum.y ) )
-            {
-                prevShadingPix = ip;
-                curShadingPix  = make_int2( cx, cy );
-                curStrataPos   = (uint32_t)( yy * STRATA + xx );
-                prevLum        = il;
-            }
+            prevShadingPix = ipos[ k ];
+            curShadingPix  = make_int2( gx * STRATA + k % STRATA, gy * STRATA + k / STRATA );
+            curStrataPos   = (uint32_t)k;
+            prevLum        = ilum[ k ];
         }
     }
     const bool skyCur = inside( u, curShadingPix.x, curShadingPix.y ) && a.isSky[ curShadingPix.y * u.W + curShadingPix.x ] != 0;
     if( !in_area( prevShadingPix.x, prevShadingPix.y, cb_area( u, curShadingPix.x ) ) || skyCur ||
         ( prevLum.x <= 0.0f && prevLum.y <= 0.0f ) )
     {
-        a.disPing[ gi ]     = 0u;
+        dst[ gi ]           = 0u;
         a.gradPrevPix[ gi ] = STRATA * STRATA + 1;
         return;
     }
@@ -372,7 +418,7 @@ template< int M > __device__ __forceinline__ void gradient_sample_px( const Fram
     g0 = gmix( g0, gp.x, 0.5f );
     g1 = gmix( g1, gp.y, 0.5f );
     g2 = gmix( g2, gp.z, 0.5f );
-    a.disPing[ gi ]     = pack_rgba8( g0, g1, g2, 0.0f );
+    dst[ gi ]           = pack_rgba8( g0, g1, g2, 0.0f );
     a.gradPrevPix[ gi ] = (uint8_t)curStrataPos;
 }
 
@@ -420,7 +466,7 @@ __device__ __forceinline__ void fill_u8( float* u8, int t )
     u8[ t ] = (float)t / 255.0f;
 }
 
-template< int M > __global__ void __launch_bounds__( 256 ) k_gradient_samples( const FrameArgs a )
+template< int M > __global__ void __launch_bounds__( 256 ) k_gradient_samples( const FrameArgs a, uint32_t* dst )
 {
     __shared__ float u8[ 256 ];
     fill_u8( u8, threadIdx.y * blockDim.x + threadIdx.x );
@@ -428,7 +474,7 @@ template< int M > __global__ void __launch_bounds__( 256 ) k_gradient_samples( c
     const int gx = blockIdx.x * blockDim.x + threadIdx.x;
     const int gy = blockIdx.y * blockDim.y + threadIdx.y;
     if( gx >= a.u.GW || gy >= a.u.GH || gx * STRATA >= a.u.W || gy * STRATA >= a.u.H ) return;
-    gradient_sample_px< M >( a, gx, gy, u8 );
+    gradient_sample_px< M >( a, dst, gx, gy, u8 );
 }
 
 template< int M > __global__ void __launch_bounds__( 256 ) k_gradient_atrous( const FrameArgs a, const int iter )
@@ -440,34 +486,6 @@ template< int M > __global__ void __launch_bounds__( 256 ) k_gradient_atrous( co
     const int gy = blockIdx.y * blockDim.y + threadIdx.y;
     if( gx >= a.u.GW || gy >= a.u.GH || gx * STRATA >= a.u.W || gy * STRATA >= a.u.H ) return;
     gradient_atrous_px( a, gx, gy, iter, u8 );
-}
-
-// The whole gradient chain in one cooperative launch: samples, then the 4 a-trous
-// iterations, separated by grid-wide barriers (every block is co-resident; the
-// launch fails instead of starting if the grid does not fit).
-template< int M > __global__ void __launch_bounds__( 256 ) k_gradient_fused( const FrameArgs a )
-{
-    __shared__ float u8[ 256 ];
-    fill_u8( u8, threadIdx.x );
-    __syncthreads();
-    cg::grid_group grid   = cg::this_grid();
-    const Uniform& u      = a.u;
-    const int      n      = u.GW * u.GH;
-    const int      stride = gridDim.x * blockDim.x;
-    for( int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += stride )
-    {
-        const int gx = k % u.GW, gy = k / u.GW;
-        if( gx * STRATA < u.W && gy * STRATA < u.H ) gradient_sample_px< M >( a, gx, gy, u8 );
-    }
-    for( int iter = 0; iter < 4; iter++ )
-    {
-        grid.sync();
-        for( int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += stride )
-        {
-            const int gx = k % u.GW, gy = k / u.GW;
-            if( gx * STRATA < u.W && gy * STRATA < u.H ) gradient_atrous_px( a, gx, gy, iter, u8 );
-        }
-    }
 }
 
 // ==========================================================================================
@@ -508,9 +526,15 @@ __device__ __forceinline__ float parallax( const Uniform& u, float3 pos, float3 
     return par * 60.0f;
 }
 
-template< int M, bool FAST > __global__ void __launch_bounds__( 256 ) k_temporal( const FrameArgs a )
+// FAST: continuous specular terms in hardware exp2/log2, shared subexpressions and the
+// precombined view-projection matrices. GEOM: write this frame's geometry record. GEOMPREV:
+// read the previous frame's record (decoded normal + depth, the same values) at the taps.
+template< int M, bool FAST, bool GEOM, bool GEOMPREV > __global__ void __launch_bounds__( 256 ) k_temporal( const FrameArgs a )
 {
     using S          = Sto< M >;
+    __shared__ float u8[ 256 ];
+    fill_u8( u8, threadIdx.y * blockDim.x + threadIdx.x );
+    __syncthreads();
     const Uniform& u = a.u;
     const int      px = blockIdx.x * blockDim.x + threadIdx.x;
     const int      py = blockIdx.y * blockDim.y + threadIdx.y;
@@ -527,7 +551,9 @@ template< int M, bool FAST > __global__ void __launch_bounds__( 256 ) k_temporal
     const float   motionZ         = h2f( mo.z );
     const float   z               = h2f( a.depth[ i ] );
     const float3  normal          = decode_normal( a, a.normal[ i ] );
-    const float   roughness       = unorm8_to_f32( a.mr[ i ] >> 8 );
+    const uint16_t mrBits         = a.mr[ i ];
+    const float   roughness       = u8[ mrBits >> 8 ];
+    if( GEOM ) a.geom[ i ] = geo_pack( normal, a.depth[ i ], mrBits );
 
     const float l = luminance( unfilteredDiff );
     const float2 moments = make_float2( l, l * l );
@@ -561,8 +587,19 @@ template< int M, bool FAST > __global__ void __launch_bounds__( 256 ) k_temporal
             const int   qx = pixPrev.x + xx, qy = pixPrev.y + yy;
             const bool  in = inside( u, qx, qy );
             const size_t q = in ? idx( u, qx, qy ) : 0;
-            const float  dP = in ? h2f( a.depthPrev[ q ] ) : 0.0f;
-            const float3 nP = decode_normal( a, in ? a.normalPrev[ q ] : 0u );
+            float        dP;
+            float3       nP;
+            if( GEOMPREV )
+            {
+                const Geo gp = in ? geo_load( a.geomPrev, (int)q ) : geo_zero();
+                dP           = geo_depth( gp );
+                nP           = gp.n;
+            }
+            else
+            {
+                dP = in ? h2f( a.depthPrev[ q ] ) : 0.0f;
+                nP = decode_normal( a, in ? a.normalPrev[ q ] : 0u );
+            }
             const bool ok = in_area( qx, qy, chArea ) && test_depth( z, dP, motionZ ) && test_normal( normal, nP );
             if( ok )
             {
@@ -586,7 +623,7 @@ template< int M, bool FAST > __global__ void __launch_bounds__( 256 ) k_temporal
     float aD = 0.0f, aI = 0.0f, aS = 0.0f;
     if( !( u.flags & RGDN_FLAG_SKIP_GRADIENTS ) )
     {
-        const float4 g = ld_rgba8z( u, a.disPing, px / STRATA, py / STRATA );
+        const float4 g = ld_rgba8t( u, a.disPing, px / STRATA, py / STRATA, u8 );
         aD = g.x; aI = g.y; aS = g.z;
     }
 
@@ -608,74 +645,163 @@ template< int M, bool FAST > __global__ void __launch_bounds__( 256 ) k_temporal
             surfPosPrev      = f3( spp.x, spp.y, spp.z );
         }
         const float nv = fmaxf( 0.0f, dot3( normal, f3( -rayInfo.x, -rayInfo.y, -rayInfo.z ) ) );
-
-        const float A       = gclamp( 1.0f + specHistoryLength * Wm< FAST >::powv( 1.0f - aS, 5.0f ), spec_min_accum( u ), 256.0f );
-        const float par     = parallax( u, surfPos, surfPosPrev );
-        const float AOnSurf = spec_accum_speed< FAST >( u, A, roughness, nv, par );
-        const float domin   = spec_dominant< FAST >( nv, roughness );
-
-        const float3 specOnSurf    = vmix( specPrevOnSurf, unfilteredSpec, 1.0f / ( 1.0f + AOnSurf ) );
-        const float  hitDistOnSurf = gmix( specHitDistancePrev, rayInfo.w, 1.0f / ( 1.0f + AOnSurf ) );
-
-        specColorAccum         = specOnSurf;
-        specHistoryLengthAccum = AOnSurf;
-        specHitDistanceAccum   = hitDistOnSurf;
-
-        const float3 rayDir     = f3( rayInfo.x, rayInfo.y, rayInfo.z );
-        const float3 virtualPos = add( surfPos, mul( mul( rayDir, hitDistOnSurf ), domin ) );
-
-        int2   pixPrevS;
-        float2 subPixS;
+        if constexpr( FAST )
         {
-            const float4 vp   = make_float4( virtualPos.x, virtualPos.y, virtualPos.z, 1.0f );
-            const float4 vsc  = mat_mul( u.view, vp );
-            const float4 vsp  = mat_mul( u.viewPrev, vp );
-            const float4 csc  = mat_mul( u.proj, vsc );
-            const float4 csp  = mat_mul( u.projPrev, vsp );
-            const float3 ndcC = f3( csc.x / csc.w, csc.y / csc.w, csc.z / csc.w );
-            const float3 ndcP = f3( csp.x / csp.w, csp.y / csp.w, csp.z / csp.w );
-            const float2 ssC  = make_float2( ndcC.x * 0.5f + 0.5f, ndcC.y * 0.5f + 0.5f );
-            const float2 ssP  = make_float2( ndcP.x * 0.5f + 0.5f, ndcP.y * 0.5f + 0.5f );
-            const float2 spp  = prev_screen_pos( u, make_float2( ssP.x - ssC.x, ssP.y - ssC.y ), px, py );
+            const float minA = spec_min_accum( u );
+            const float oma  = 1.0f - aS;
+            const float A    = gclamp( 1.0f + specHistoryLength * ( oma * oma * oma * oma * oma ), minA, 256.0f );
+            // getParallax (:58-69): normalize(pos) . normalize(posPrev - cameraDelta)
+            const float3 camDelta = f3( u.camPosPrev[ 0 ] - u.camPos[ 0 ], u.camPosPrev[ 1 ] - u.camPos[ 1 ], u.camPosPrev[ 2 ] - u.camPos[ 2 ] );
+            const float3 pp   = sub( surfPosPrev, camDelta );
+            const float  cosa = gsat( dot3( surfPos, pp ) * rsqrtf( dot3( surfPos, surfPos ) ) * rsqrtf( dot3( pp, pp ) ) );
+            const float  par  = __fdividef( sqrtf( 1.0f - cosa * cosa ), fmaxf( cosa, 1e-6f ) ) * 60.0f;
+            // getSpecAccumSpeed (:80-92) for the surface and the virtual motion share every
+            // term but the parallax
+            const float aa = ex2_approx( 0.66f * __log2f( gsat( 1.0f - nv ) ) );
+            const float b  = 1.1f + roughness * roughness;
+            const float ps = __fdividef( b + aa, b - aa );
+            const float f0 = 1.0f - ex2_approx( -200.0f * roughness * roughness );
+            const float lr = __log2f( gsat( roughness ) );
+            const float AOnSurf = gclamp( 256.0f * ( f0 * ex2_approx( 0.5f * ( 1.0f + par * ps ) * lr ) ), minA, A );
+            // getSpecularDominantFactor (:93-99)
+            const float da    = 0.298475f * __logf( 39.4115f - 39.0029f * roughness );
+            const float domin = gclamp( ex2_approx( 10.8649f * __log2f( gclamp( 1.0f - nv, 0.0f, 1.0f ) ) ) * ( 1.0f - da ) + da, 0.0f, 1.0f );
+
+            const float  invA          = __fdividef( 1.0f, 1.0f + AOnSurf );
+            const float3 specOnSurf    = vmix( specPrevOnSurf, unfilteredSpec, invA );
+            const float  hitDistOnSurf = gmix( specHitDistancePrev, rayInfo.w, invA );
+            specColorAccum         = specOnSurf;
+            specHistoryLengthAccum = AOnSurf;
+            specHitDistanceAccum   = hitDistOnSurf;
+
+            const float3 rayDir = f3( rayInfo.x, rayInfo.y, rayInfo.z );
+            const float3 v      = add( surfPos, mul( mul( rayDir, hitDistOnSurf ), domin ) );
+            // screen-space motion of the virtual position through proj*view (only x, y, w)
+            const float cxC = u.vp[ 0 ] * v.x + u.vp[ 4 ] * v.y + u.vp[ 8 ] * v.z + u.vp[ 12 ];
+            const float cyC = u.vp[ 1 ] * v.x + u.vp[ 5 ] * v.y + u.vp[ 9 ] * v.z + u.vp[ 13 ];
+            const float cwC = u.vp[ 3 ] * v.x + u.vp[ 7 ] * v.y + u.vp[ 11 ] * v.z + u.vp[ 15 ];
+            const float cxP = u.vpPrev[ 0 ] * v.x + u.vpPrev[ 4 ] * v.y + u.vpPrev[ 8 ] * v.z + u.vpPrev[ 12 ];
+            const float cyP = u.vpPrev[ 1 ] * v.x + u.vpPrev[ 5 ] * v.y + u.vpPrev[ 9 ] * v.z + u.vpPrev[ 13 ];
+            const float cwP = u.vpPrev[ 3 ] * v.x + u.vpPrev[ 7 ] * v.y + u.vpPrev[ 11 ] * v.z + u.vpPrev[ 15 ];
+            const float rC = __fdividef( 1.0f, cwC ), rP = __fdividef( 1.0f, cwP );
+            const float2 specMotion = make_float2( ( cxP * rP * 0.5f + 0.5f ) - ( cxC * rC * 0.5f + 0.5f ),
+                                                   ( cyP * rP * 0.5f + 0.5f ) - ( cyC * rC * 0.5f + 0.5f ) );
+            const float2 spp = prev_screen_pos( u, specMotion, px, py );
             const float  fx = floorf( spp.x - 0.5f ), fy = floorf( spp.y - 0.5f );
-            pixPrevS = make_int2( (int)fx, (int)fy );
-            subPixS  = make_float2( ( spp.x - 0.5f ) - fx, ( spp.y - 0.5f ) - fy );
-        }
-        const float bws[ 2 ][ 2 ] = {
-            { ( 1.0f - subPixS.x ) * ( 1.0f - subPixS.y ), subPixS.x * ( 1.0f - subPixS.y ) },
-            { ( 1.0f - subPixS.x ) * subPixS.y, subPixS.x * subPixS.y },
-        };
-        float weightSumVirtual = 0.0f;
+            const int2   pixPrevS = make_int2( (int)fx, (int)fy );
+            const float2 subPixS  = make_float2( ( spp.x - 0.5f ) - fx, ( spp.y - 0.5f ) - fy );
+            float weightSumVirtual = 0.0f;
 #pragma unroll
-        for( int yy = 0; yy <= 1; yy++ )
-        {
-#pragma unroll
-            for( int xx = 0; xx <= 1; xx++ )
+            for( int yy = 0; yy <= 1; yy++ )
             {
-                const int    qx = pixPrevS.x + xx, qy = pixPrevS.y + yy;
-                const bool   in = inside( u, qx, qy );
-                const size_t q  = in ? idx( u, qx, qy ) : 0;
-                const float  dP = in ? h2f( a.depthPrev[ q ] ) : 0.0f;
-                const float3 nP = decode_normal( a, in ? a.normalPrev[ q ] : 0u );
-                const bool ok = in_area( qx, qy, chArea ) && test_depth( z, dP, motionZ ) && test_normal( normal, nP );
-                // the shader also accumulates SpecAccumColor_Prev here but never uses the sum
-                if( ok ) weightSumVirtual = weightSumVirtual + bws[ yy ][ xx ];
+#pragma unroll
+                for( int xx = 0; xx <= 1; xx++ )
+                {
+                    const int  qx = pixPrevS.x + xx, qy = pixPrevS.y + yy;
+                    const bool in = inside( u, qx, qy );
+                    const int  q  = in ? qy * u.W + qx : 0;
+                    float      dP;
+                    float3     nP;
+                    if( GEOMPREV )
+                    {
+                        const Geo gp = in ? geo_load( a.geomPrev, q ) : geo_zero();
+                        dP           = geo_depth( gp );
+                        nP           = gp.n;
+                    }
+                    else
+                    {
+                        dP = in ? h2f( a.depthPrev[ q ] ) : 0.0f;
+                        nP = decode_normal( a, in ? a.normalPrev[ q ] : 0u );
+                    }
+                    const bool ok = in_area( qx, qy, chArea ) && test_depth( z, dP, motionZ ) && test_normal( normal, nP );
+                    const float w = ( xx ? subPixS.x : 1.0f - subPixS.x ) * ( yy ? subPixS.y : 1.0f - subPixS.y );
+                    if( ok ) weightSumVirtual = weightSumVirtual + w;
+                }
+            }
+            if( weightSumVirtual > 0.0001f )
+            {
+                float       Avirt    = gclamp( 256.0f * ( f0 * ex2_approx( 0.5f * lr ) ), minA, A );
+                const float Amin     = fminf( Avirt, 3.0f * sqrtf( roughness ) );
+                float       aa2      = gmix( __fdividef( 1.0f, 1.0f + Amin ), __fdividef( 1.0f, 1.0f + Avirt ), 1.0f );
+                Avirt                = __fdividef( 1.0f, aa2 ) - 1.0f;
+                const float Ahitdist = fminf( Avirt, 16.0f );
+                const float3 specVirt = vmix( specPrevOnSurf, unfilteredSpec, __fdividef( 1.0f, 1.0f + Avirt ) );
+                aa2                    = gmix( invA, __fdividef( 1.0f, 1.0f + Avirt ), domin );
+                specColorAccum         = vmix( specOnSurf, specVirt, domin );
+                specHistoryLengthAccum = __fdividef( 1.0f, aa2 ) - 1.0f;
+                specHitDistanceAccum   = gmix( specHitDistancePrev, rayInfo.w, __fdividef( 1.0f, 1.0f + Ahitdist ) );
             }
         }
-        if( weightSumVirtual > 0.0001f )
+        else
         {
-            float       Avirt      = spec_accum_speed< FAST >( u, A, roughness, nv, 0.0f );
-            const float confidence = 1.0f;
-            const float Amin       = fminf( Avirt, 3.0f * sqrtf( roughness ) );
-            float       aa         = gmix( 1.0f / ( 1.0f + Amin ), 1.0f / ( 1.0f + Avirt ), confidence );
-            Avirt                  = 1.0f / aa - 1.0f;
-            const float Ahitdist   = fminf( Avirt, 16.0f );
-            const float3 specVirt  = vmix( specPrevOnSurf, unfilteredSpec, 1.0f / ( 1.0f + Avirt ) );
-            const float amount     = domin;
-            aa                     = gmix( 1.0f / ( 1.0f + AOnSurf ), 1.0f / ( 1.0f + Avirt ), amount );
-            specColorAccum         = vmix( specOnSurf, specVirt, amount );
-            specHistoryLengthAccum = 1.0f / aa - 1.0f;
-            specHitDistanceAccum   = gmix( specHitDistancePrev, rayInfo.w, 1.0f / ( 1.0f + Ahitdist ) );
+            const float A       = gclamp( 1.0f + specHistoryLength * Wm< FAST >::powv( 1.0f - aS, 5.0f ), spec_min_accum( u ), 256.0f );
+            const float par     = parallax( u, surfPos, surfPosPrev );
+            const float AOnSurf = spec_accum_speed< FAST >( u, A, roughness, nv, par );
+            const float domin   = spec_dominant< FAST >( nv, roughness );
+
+            const float3 specOnSurf    = vmix( specPrevOnSurf, unfilteredSpec, 1.0f / ( 1.0f + AOnSurf ) );
+            const float  hitDistOnSurf = gmix( specHitDistancePrev, rayInfo.w, 1.0f / ( 1.0f + AOnSurf ) );
+
+            specColorAccum         = specOnSurf;
+            specHistoryLengthAccum = AOnSurf;
+            specHitDistanceAccum   = hitDistOnSurf;
+
+            const float3 rayDir     = f3( rayInfo.x, rayInfo.y, rayInfo.z );
+            const float3 virtualPos = add( surfPos, mul( mul( rayDir, hitDistOnSurf ), domin ) );
+
+            int2   pixPrevS;
+            float2 subPixS;
+            {
+                const float4 vp   = make_float4( virtualPos.x, virtualPos.y, virtualPos.z, 1.0f );
+                const float4 vsc  = mat_mul( u.view, vp );
+                const float4 vsp  = mat_mul( u.viewPrev, vp );
+                const float4 csc  = mat_mul( u.proj, vsc );
+                const float4 csp  = mat_mul( u.projPrev, vsp );
+                const float3 ndcC = f3( csc.x / csc.w, csc.y / csc.w, csc.z / csc.w );
+                const float3 ndcP = f3( csp.x / csp.w, csp.y / csp.w, csp.z / csp.w );
+                const float2 ssC  = make_float2( ndcC.x * 0.5f + 0.5f, ndcC.y * 0.5f + 0.5f );
+                const float2 ssP  = make_float2( ndcP.x * 0.5f + 0.5f, ndcP.y * 0.5f + 0.5f );
+                const float2 spp  = prev_screen_pos( u, make_float2( ssP.x - ssC.x, ssP.y - ssC.y ), px, py );
+                const float  fx = floorf( spp.x - 0.5f ), fy = floorf( spp.y - 0.5f );
+                pixPrevS = make_int2( (int)fx, (int)fy );
+                subPixS  = make_float2( ( spp.x - 0.5f ) - fx, ( spp.y - 0.5f ) - fy );
+            }
+            const float bws[ 2 ][ 2 ] = {
+                { ( 1.0f - subPixS.x ) * ( 1.0f - subPixS.y ), subPixS.x * ( 1.0f - subPixS.y ) },
+                { ( 1.0f - subPixS.x ) * subPixS.y, subPixS.x * subPixS.y },
+            };
+            float weightSumVirtual = 0.0f;
+    #pragma unroll
+            for( int yy = 0; yy <= 1; yy++ )
+            {
+    #pragma unroll
+                for( int xx = 0; xx <= 1; xx++ )
+                {
+                    const int    qx = pixPrevS.x + xx, qy = pixPrevS.y + yy;
+                    const bool   in = inside( u, qx, qy );
+                    const size_t q  = in ? idx( u, qx, qy ) : 0;
+                    const float  dP = in ? h2f( a.depthPrev[ q ] ) : 0.0f;
+                    const float3 nP = decode_normal( a, in ? a.normalPrev[ q ] : 0u );
+                    const bool ok = in_area( qx, qy, chArea ) && test_depth( z, dP, motionZ ) && test_normal( normal, nP );
+                    // the shader also accumulates SpecAccumColor_Prev here but never uses the sum
+                    if( ok ) weightSumVirtual = weightSumVirtual + bws[ yy ][ xx ];
+                }
+            }
+            if( weightSumVirtual > 0.0001f )
+            {
+                float       Avirt      = spec_accum_speed< FAST >( u, A, roughness, nv, 0.0f );
+                const float confidence = 1.0f;
+                const float Amin       = fminf( Avirt, 3.0f * sqrtf( roughness ) );
+                float       aa         = gmix( 1.0f / ( 1.0f + Amin ), 1.0f / ( 1.0f + Avirt ), confidence );
+                Avirt                  = 1.0f / aa - 1.0f;
+                const float Ahitdist   = fminf( Avirt, 16.0f );
+                const float3 specVirt  = vmix( specPrevOnSurf, unfilteredSpec, 1.0f / ( 1.0f + Avirt ) );
+                const float amount     = domin;
+                aa                     = gmix( 1.0f / ( 1.0f + AOnSurf ), 1.0f / ( 1.0f + Avirt ), amount );
+                specColorAccum         = vmix( specOnSurf, specVirt, amount );
+                specHistoryLengthAccum = 1.0f / aa - 1.0f;
+                specHitDistanceAccum   = gmix( specHitDistancePrev, rayInfo.w, 1.0f / ( 1.0f + Ahitdist ) );
+            }
         }
     }
     else
@@ -776,13 +902,14 @@ template< int M > __global__ void __launch_bounds__( 256 ) k_antifirefly( const 
 // CmSVGFEstimateVariance.comp:129-206
 // ==========================================================================================
 // colourAt(dx, dy) returns DiffAccumColor at (px+dx, py+dy), zero outside the image
-template< int M, bool FAST, class ColorAt >
+template< int M, bool FAST, bool GEOMIN, class ColorAt >
 __device__ __forceinline__ void variance_px( const FrameArgs& a, const int px, const int py, const int i, ColorAt colorAt, float3& outC,
                                              float& outV )
 {
     using S          = Sto< M >;
     using X          = Wm< FAST >;
-    const float cz   = h2f( a.depth[ i ] );
+    const Geo   gc   = GEOMIN ? geo_load( a.geom, i ) : geo_zero();
+    const float cz   = GEOMIN ? geo_depth( gc ) : h2f( a.depth[ i ] );
     float3      pc   = colorAt( 0, 0 );
     if( cz < 0.0f || cz > MAX_RAY_LENGTH )
     {
@@ -804,7 +931,7 @@ __device__ __forceinline__ void variance_px( const FrameArgs& a, const int px, c
     const float  l   = luminance( pc );
     float2       sm  = make_float2( l + tm.x, l * l + tm.y );
     float        ws  = 1.0f;
-    const float3 cnd = decode_normal( a, a.normal[ i ] );
+    const float3 cnd = GEOMIN ? gc.n : decode_normal( a, a.normal[ i ] );
 #pragma unroll
     for( int yy = -1; yy <= 1; yy++ )
     {
@@ -817,11 +944,23 @@ __device__ __forceinline__ void variance_px( const FrameArgs& a, const int px, c
             const float  lq  = luminance( cq );
             const bool   in  = inside( a.u, qx, qy );
             const int    q   = in ? qy * a.u.W + qx : 0;
-            const float  zq  = in ? h2f( a.depth[ q ] ) : 0.0f;
+            float        zq;
+            float3       nq;
+            if( GEOMIN )
+            {
+                const Geo gq = in ? geo_load( a.geom, q ) : geo_zero();
+                zq           = geo_depth( gq );
+                nq           = gq.n;
+            }
+            else
+            {
+                zq = in ? h2f( a.depth[ q ] ) : 0.0f;
+                nq = decode_normal( a, in ? a.normal[ q ] : 0u );
+            }
             const float  mz  = fmaxf( cz, zq );
             const float  rcp = mz <= 0.0f ? 0.0f : 1.0f / mz;
             const float  wz  = X::expn( -fabsf( cz - zq ) * rcp );
-            const float  wn  = X::pow128( fmaxf( 0.0f, dot3( cnd, decode_normal( a, in ? a.normal[ q ] : 0u ) ) ) );
+            const float  wn  = X::pow128( fmaxf( 0.0f, dot3( cnd, nq ) ) );
             const float  w   = wz * wn;
             if( !isnan( w ) )
             {
@@ -847,120 +986,149 @@ template< int M > __global__ void __launch_bounds__( 256 ) k_variance( const Fra
     const int i = py * u.W + px;
     float3    c;
     float     v;
-    variance_px< M, false >( a, px, py, i, [ & ]( int dx, int dy ) { return ld3z< M >( a, a.diffAccumColor, px + dx, py + dy ); }, c, v );
+    variance_px< M, false, false >( a, px, py, i, [ & ]( int dx, int dy ) { return ld3z< M >( a, a.diffAccumColor, px + dx, py + dy ); }, c, v );
     S::stcv( a.diffPing, a.varPing, (size_t)i, c, v );
 }
 
 // ==========================================================================================
-// Anti-firefly + variance in one kernel (CmAntiFirefly.comp + CmSVGFEstimateVariance.comp).
-// A 32x8 tile: the three signals are staged with a 3-texel halo, the 5x5 ring minimum and
-// maximum come from row extrema (min over the 4 rows above/below of the 5-wide row extremum,
-// and the 4 same-row neighbours), the anti-firefly diffuse result on a 1-texel halo is
-// quantised through the storage format exactly as if it had been stored to DiffAccumColor,
-// and the variance reads it from shared memory. Results equal the two separate kernels.
+// Anti-firefly for the default path (CmAntiFirefly.comp:120-158), the same results as
+// k_antifirefly: min / max are exact in any representation of the stored values, so 16-bit
+// storage clamps on packed half2 / bf16x2 pairs without converting, fp32 on floats, and the
+// shared-exponent storage on decoded floats. Blocks whose 5x5 footprint lies inside the image
+// skip the bounds tests. Every stored colour is non-negative and finite, so the shader's
+// +-1e6 initial extrema never survive the 24 taps and the first tap seeds them.
 // ==========================================================================================
-constexpr int AFV_TX = 32, AFV_TY = 8;
-constexpr int AFV_IW = AFV_TX + 6, AFV_IH = AFV_TY + 6;   // staged inputs: tile +-3
-constexpr int AFV_AW = AFV_TX + 2, AFV_AH = AFV_TY + 2;   // anti-firefly results: tile +-1
-
-template< int M > __device__ __forceinline__ float3 quantize3( float3 v )
+template< int M > struct AfOps;
+template<> struct AfOps< MODE_F16 >
 {
-    if( M == MODE_REF ) return e5( encode_e5( v.x, v.y, v.z ) );
-    return v;  // fp32 / fp16 / bf16 channels of a clamp are already representable
+    using V = uint2;   // (r,g) (b,0) as two half2
+    __device__ static V ld( const void* p, int i ) { return static_cast< const uint2* >( p )[ i ]; }
+    __device__ static V zero() { return make_uint2( 0u, 0u ); }
+    __device__ static uint32_t mn2( uint32_t a, uint32_t b )
+    {
+        __half2 r = __hmin2( *reinterpret_cast< __half2* >( &a ), *reinterpret_cast< __half2* >( &b ) );
+        return *reinterpret_cast< uint32_t* >( &r );
+    }
+    __device__ static uint32_t mx2( uint32_t a, uint32_t b )
+    {
+        __half2 r = __hmax2( *reinterpret_cast< __half2* >( &a ), *reinterpret_cast< __half2* >( &b ) );
+        return *reinterpret_cast< uint32_t* >( &r );
+    }
+    __device__ static V mn( V a, V b ) { return make_uint2( mn2( a.x, b.x ), mn2( a.y, b.y ) ); }
+    __device__ static V mx( V a, V b ) { return make_uint2( mx2( a.x, b.x ), mx2( a.y, b.y ) ); }
+    __device__ static void st( void* p, int i, V v ) { static_cast< uint2* >( p )[ i ] = v; }
+};
+template<> struct AfOps< MODE_BF16 >
+{
+    using V = uint2;
+    __device__ static V ld( const void* p, int i ) { return static_cast< const uint2* >( p )[ i ]; }
+    __device__ static V zero() { return make_uint2( 0u, 0u ); }
+    __device__ static uint32_t mn2( uint32_t a, uint32_t b )
+    {
+        __nv_bfloat162 r = __hmin2( *reinterpret_cast< __nv_bfloat162* >( &a ), *reinterpret_cast< __nv_bfloat162* >( &b ) );
+        return *reinterpret_cast< uint32_t* >( &r );
+    }
+    __device__ static uint32_t mx2( uint32_t a, uint32_t b )
+    {
+        __nv_bfloat162 r = __hmax2( *reinterpret_cast< __nv_bfloat162* >( &a ), *reinterpret_cast< __nv_bfloat162* >( &b ) );
+        return *reinterpret_cast< uint32_t* >( &r );
+    }
+    __device__ static V mn( V a, V b ) { return make_uint2( mn2( a.x, b.x ), mn2( a.y, b.y ) ); }
+    __device__ static V mx( V a, V b ) { return make_uint2( mx2( a.x, b.x ), mx2( a.y, b.y ) ); }
+    __device__ static void st( void* p, int i, V v ) { static_cast< uint2* >( p )[ i ] = v; }
+};
+template<> struct AfOps< MODE_F32 >
+{
+    using V = float4;
+    __device__ static V ld( const void* p, int i ) { return static_cast< const float4* >( p )[ i ]; }
+    __device__ static V zero() { return make_float4( 0, 0, 0, 0 ); }
+    __device__ static V mn( V a, V b ) { return make_float4( fminf( a.x, b.x ), fminf( a.y, b.y ), fminf( a.z, b.z ), 0.0f ); }
+    __device__ static V mx( V a, V b ) { return make_float4( fmaxf( a.x, b.x ), fmaxf( a.y, b.y ), fmaxf( a.z, b.z ), 0.0f ); }
+    __device__ static void st( void* p, int i, V v ) { static_cast< float4* >( p )[ i ] = make_float4( v.x, v.y, v.z, 0.0f ); }
+};
+template<> struct AfOps< MODE_REF >
+{
+    using V = float3;
+    __device__ static V ld( const void* p, int i ) { return e5( static_cast< const uint32_t* >( p )[ i ] ); }
+    __device__ static V zero() { return f3( 0, 0, 0 ); }
+    __device__ static V mn( V a, V b ) { return vmin( a, b ); }
+    __device__ static V mx( V a, V b ) { return vmax( a, b ); }
+    __device__ static void st( void* p, int i, V v ) { static_cast< uint32_t* >( p )[ i ] = encode_e5( v.x, v.y, v.z ); }
+};
+
+template< int M, bool INTERIOR >
+__device__ __forceinline__ void af_signal( const FrameArgs& a, const void* src, void* dst, int px, int py, int i )
+{
+    using O          = AfOps< M >;
+    using V          = typename O::V;
+    const Uniform& u = a.u;
+    V c = O::ld( src, i );
+    if( u.antiFirefly != 0 )
+    {
+        V mn = c, mx = c;
+        bool first = true;
+#pragma unroll
+        for( int oy = -2; oy <= 2; oy++ )
+        {
+#pragma unroll
+            for( int ox = -2; ox <= 2; ox++ )
+            {
+                if( ox == 0 && oy == 0 ) continue;
+                const int qx = px + ox, qy = py + oy;
+                const V   v  = ( INTERIOR || inside( u, qx, qy ) ) ? O::ld( src, qy * u.W + qx ) : O::zero();
+                if( first )
+                {
+                    mn = mx = v;
+                    first = false;
+                }
+                else
+                {
+                    mn = O::mn( mn, v );
+                    mx = O::mx( mx, v );
+                }
+            }
+        }
+        c = O::mn( O::mx( c, mn ), mx );
+    }
+    O::st( dst, i, c );
 }
 
-template< int M, bool FAST > __global__ void __launch_bounds__( 256 ) k_af_variance( const FrameArgs a )
+template< int M > __global__ void __launch_bounds__( 256 ) k_antifirefly_fast( const FrameArgs a )
 {
-    using S = Sto< M >;
-    __shared__ float v[ 3 ][ AFV_IH ][ AFV_IW ];
-    __shared__ float rmn[ 3 ][ AFV_IH ][ AFV_AW ];
-    __shared__ float rmx[ 3 ][ AFV_IH ][ AFV_AW ];
-    __shared__ float afd[ 3 ][ AFV_AH ][ AFV_AW ];
-    const Uniform& u   = a.u;
-    const int      t   = threadIdx.y * AFV_TX + threadIdx.x;
-    const int      x0  = blockIdx.x * AFV_TX, y0 = blockIdx.y * AFV_TY;
-    const bool     af  = u.antiFirefly != 0;
-    const float    MAXF = 1000000.0f;
-
-    for( int sig = 0; sig < 3; sig++ )
+    const Uniform& u  = a.u;
+    const int      px = blockIdx.x * blockDim.x + threadIdx.x;
+    const int      py = blockIdx.y * blockDim.y + threadIdx.y;
+    if( px >= u.W || py >= u.H ) return;
+    const int  i        = py * u.W + px;
+    const int  bx0      = blockIdx.x * blockDim.x, by0 = blockIdx.y * blockDim.y;
+    const bool interior = bx0 >= 2 && by0 >= 2 && bx0 + (int)blockDim.x + 2 <= u.W && by0 + (int)blockDim.y + 2 <= u.H;
+    if( interior )
     {
-        const void* src = sig == 0 ? a.diffTemp : sig == 1 ? a.specAccum : a.indirAccum;
-        for( int k = t; k < AFV_IW * AFV_IH; k += 256 )
-        {
-            const int    lx = k % AFV_IW, ly = k / AFV_IW;
-            const float3 c  = ld3z< M >( a, src, x0 - 3 + lx, y0 - 3 + ly );
-            v[ 0 ][ ly ][ lx ] = c.x;
-            v[ 1 ][ ly ][ lx ] = c.y;
-            v[ 2 ][ ly ][ lx ] = c.z;
-        }
-        __syncthreads();
-        if( af )
-        {
-            for( int k = t; k < AFV_AW * AFV_IH; k += 256 )
-            {
-                const int rx = k % AFV_AW, ry = k / AFV_AW;
-#pragma unroll
-                for( int c = 0; c < 3; c++ )
-                {
-                    const float* r = &v[ c ][ ry ][ rx ];
-                    rmn[ c ][ ry ][ rx ] = fminf( fminf( fminf( r[ 0 ], r[ 1 ] ), fminf( r[ 2 ], r[ 3 ] ) ), r[ 4 ] );
-                    rmx[ c ][ ry ][ rx ] = fmaxf( fmaxf( fmaxf( r[ 0 ], r[ 1 ] ), fmaxf( r[ 2 ], r[ 3 ] ) ), r[ 4 ] );
-                }
-            }
-            __syncthreads();
-        }
-        for( int k = t; k < AFV_AW * AFV_AH; k += 256 )
-        {
-            const int ax = k % AFV_AW, ay = k / AFV_AW;
-            const int gx = x0 - 1 + ax, gy = y0 - 1 + ay;
-            float3    res;
-            float*    ctr[ 3 ];
-            float     o[ 3 ];
-#pragma unroll
-            for( int c = 0; c < 3; c++ )
-            {
-                const float center = v[ c ][ ay + 2 ][ ax + 2 ];
-                if( af )
-                {
-                    const float* row = &v[ c ][ ay + 2 ][ ax ];
-                    float mn = fminf( fminf( fminf( rmn[ c ][ ay ][ ax ], rmn[ c ][ ay + 1 ][ ax ] ), fminf( rmn[ c ][ ay + 3 ][ ax ], rmn[ c ][ ay + 4 ][ ax ] ) ),
-                                      fminf( fminf( row[ 0 ], row[ 1 ] ), fminf( row[ 3 ], row[ 4 ] ) ) );
-                    float mx = fmaxf( fmaxf( fmaxf( rmx[ c ][ ay ][ ax ], rmx[ c ][ ay + 1 ][ ax ] ), fmaxf( rmx[ c ][ ay + 3 ][ ax ], rmx[ c ][ ay + 4 ][ ax ] ) ),
-                                      fmaxf( fmaxf( row[ 0 ], row[ 1 ] ), fmaxf( row[ 3 ], row[ 4 ] ) ) );
-                    mn   = fminf( MAXF, mn );
-                    mx   = fmaxf( -MAXF, mx );
-                    o[ c ] = fminf( fmaxf( center, mn ), mx );
-                }
-                else o[ c ] = center;
-                (void)ctr;
-            }
-            res = f3( o[ 0 ], o[ 1 ], o[ 2 ] );
-            const bool in = inside( u, gx, gy );
-            if( sig == 0 )
-            {
-                const float3 q = in ? quantize3< M >( res ) : f3( 0, 0, 0 );
-                afd[ 0 ][ ay ][ ax ] = q.x;
-                afd[ 1 ][ ay ][ ax ] = q.y;
-                afd[ 2 ][ ay ][ ax ] = q.z;
-            }
-            else if( in && ax >= 1 && ax <= AFV_TX && ay >= 1 && ay <= AFV_TY )
-                S::st3( sig == 1 ? a.specPing : a.indirPing, (size_t)( gy * u.W + gx ), res );
-        }
-        __syncthreads();
+        af_signal< M, true >( a, a.diffTemp, a.diffAccumColor, px, py, i );
+        af_signal< M, true >( a, a.specAccum, a.specPing, px, py, i );
+        af_signal< M, true >( a, a.indirAccum, a.indirPing, px, py, i );
     }
+    else
+    {
+        af_signal< M, false >( a, a.diffTemp, a.diffAccumColor, px, py, i );
+        af_signal< M, false >( a, a.specAccum, a.specPing, px, py, i );
+        af_signal< M, false >( a, a.indirAccum, a.indirPing, px, py, i );
+    }
+}
 
-    const int px = x0 + threadIdx.x, py = y0 + threadIdx.y;
+// Variance for the default path: the geometry record instead of the depth / normal images
+template< int M, bool FAST > __global__ void __launch_bounds__( 256 ) k_variance_geo( const FrameArgs a )
+{
+    using S          = Sto< M >;
+    const Uniform& u = a.u;
+    const int      px = blockIdx.x * blockDim.x + threadIdx.x;
+    const int      py = blockIdx.y * blockDim.y + threadIdx.y;
     if( px >= u.W || py >= u.H ) return;
     const int i = py * u.W + px;
     float3    c;
-    float     var;
-    variance_px< M, FAST >( a, px, py, i,
-                            [ & ]( int dx, int dy ) {
-                                const int ax = threadIdx.x + 1 + dx, ay = threadIdx.y + 1 + dy;
-                                return f3( afd[ 0 ][ ay ][ ax ], afd[ 1 ][ ay ][ ax ], afd[ 2 ][ ay ][ ax ] );
-                            },
-                            c, var );
-    S::stcv( a.diffPing, a.varPing, (size_t)i, c, var );
+    float     v;
+    variance_px< M, FAST, true >( a, px, py, i, [ & ]( int dx, int dy ) { return ld3z< M >( a, a.diffAccumColor, px + dx, py + dy ); }, c, v );
+    S::stcv( a.diffPing, a.varPing, (size_t)i, c, v );
 }
 
 // ==========================================================================================
@@ -1059,7 +1227,10 @@ __device__ __forceinline__ float4 ld_h4( const ushort4* p, int i )
 }
 
 // one a-trous iteration for one pixel (CmSVGFAtrous_Iter0.comp:196-304, CmSVGFAtrous.comp:71-220)
-template< int M, bool FAST >
+// INTERIOR: every tap of the pixel lies inside the image and inside the pixel's checkerboard
+// half, so the bounds and render-area tests are statically true (the caller checks this for
+// the whole block)
+template< int M, bool FAST, bool INTERIOR, bool GEOMIN >
 __device__ __forceinline__ void atrous_px( const FrameArgs& a, const AtrousIO& io, const int iter, const int px, const int py,
                                            const int i, const float* u8, float3& outDiff, float& outVar, float3& outSpec,
                                            float3& outInd )
@@ -1074,7 +1245,8 @@ __device__ __forceinline__ void atrous_px( const FrameArgs& a, const AtrousIO& i
     outVar  = cv.w;
     outSpec = S::ld3( io.specSrc, (size_t)i );
     outInd  = S::ld3( io.indirSrc, (size_t)i );
-    const float z         = h2f( a.depth[ i ] );
+    const Geo   gc        = GEOMIN ? geo_load( a.geom, i ) : geo_zero();
+    const float z         = GEOMIN ? geo_depth( gc ) : h2f( a.depth[ i ] );
     const float gradDepth = h2f( a.depthGrad[ i ] );
 
     if( z < 0.0f || z > MAX_RAY_LENGTH )
@@ -1085,7 +1257,7 @@ __device__ __forceinline__ void atrous_px( const FrameArgs& a, const AtrousIO& i
         }
         return;
     }
-    const float3 normal = decode_normal( a, a.normal[ i ] );
+    const float3 normal = GEOMIN ? gc.n : decode_normal( a, a.normal[ i ] );
     const float  l      = luminance( outDiff );
     float        prefVar;
     if( iter == 0 )
@@ -1107,7 +1279,7 @@ __device__ __forceinline__ void atrous_px( const FrameArgs& a, const AtrousIO& i
     else prefVar = S::ld1( a.filtVar, (size_t)i );
 
     const float wLumMul   = 1.0f / ( 4.0f * prefVar + 0.00001f );
-    const float roughness = u8[ a.mr[ i ] >> 8 ];
+    const float roughness = u8[ GEOMIN ? geo_rough8( gc ) : ( a.mr[ i ] >> 8 ) ];
     const float wRoughMul = gclamp( roughness * 30.0f - (float)iter, 0.0f, 1.0f );
     const float hS        = S::ld4( a.histLen, (size_t)i ).z;
     const float nws       = gclamp( hS / 8.0f, 0.0f, 1.0f );
@@ -1128,11 +1300,23 @@ __device__ __forceinline__ void atrous_px( const FrameArgs& a, const AtrousIO& i
         {
             if( xx == 0 && yy == 0 ) continue;
             const int    qx  = px + xx * step, qy = py + yy * step;
-            const bool   in  = inside( u, qx, qy );
+            const bool   in  = INTERIOR || inside( u, qx, qy );
             const int    q   = in ? qy * u.W + qx : 0;
-            const float  rq  = in ? u8[ a.mr[ q ] >> 8 ] : 0.0f;
-            const float3 nq  = decode_normal( a, in ? a.normal[ q ] : 0u );
-            const float  zq  = in ? h2f( a.depth[ q ] ) : 0.0f;
+            float        rq, zq;
+            float3       nq;
+            if( GEOMIN )
+            {
+                const Geo gq = in ? geo_load( a.geom, q ) : geo_zero();
+                rq           = u8[ geo_rough8( gq ) ];
+                nq           = gq.n;
+                zq           = geo_depth( gq );
+            }
+            else
+            {
+                rq = in ? u8[ a.mr[ q ] >> 8 ] : 0.0f;
+                nq = decode_normal( a, in ? a.normal[ q ] : 0u );
+                zq = in ? h2f( a.depth[ q ] ) : 0.0f;
+            }
             const float3 sq  = in ? S::ld3( io.specSrc, (size_t)q ) : f3( 0, 0, 0 );
             const float4 cvq = in ? S::ldcv( io.diffSrc, io.varSrc, (size_t)q ) : make_float4( 0, 0, 0, 0 );
             const float3 dq  = f3( cvq.x, cvq.y, cvq.z );
@@ -1146,9 +1330,10 @@ __device__ __forceinline__ void atrous_px( const FrameArgs& a, const AtrousIO& i
             const float w_n = X::pow128( nn );
             const float w_l = fabsf( l - lq ) * wLumMul;
             float       w_r = fmaxf( 0.0f, 1.0f - 10.0f * fabsf( roughness - rq ) ) * wRoughMul;
-            if( nwSpec > 0.0f ) w_r = w_r * X::powv( nn, nwSpec );
+            // pow(nn, p) is finite for nn in [0,1], so a zero w_r stays zero without it
+            if( nwSpec > 0.0f && w_r > 0.0f ) w_r = w_r * X::pow01( nn, nwSpec );
             const float waveletW = kern[ yy < 0 ? -yy : yy ][ xx < 0 ? -xx : xx ];
-            const float insideA  = in_area( qx, qy, chArea ) ? 1.0f : 0.0f;
+            const float insideA  = ( INTERIOR || in_area( qx, qy, chArea ) ) ? 1.0f : 0.0f;
             const float wBase    = X::expn( -w_z * w_z ) * w_n * waveletW * insideA;
             const float wDiff    = wBase * X::expn( -w_l );
             const float wSpec    = wBase * w_r;
@@ -1173,7 +1358,7 @@ __device__ __forceinline__ void atrous_px( const FrameArgs& a, const AtrousIO& i
 // One a-trous iteration over the frame. HIST: the last iteration also accumulates the
 // luminance histogram of the HistogramInput values it writes (CmLuminanceHistogram.comp,
 // fused: no second read of the image).
-template< int M, bool FAST, bool HIST > __global__ void __launch_bounds__( 256 ) k_atrous( const FrameArgs a, const int iter )
+template< int M, bool FAST, bool HIST, bool GEOMIN > __global__ void __launch_bounds__( 256, 3 ) k_atrous( const FrameArgs a, const int iter )
 {
     using S = Sto< M >;
     __shared__ float    u8[ 256 ];
@@ -1193,7 +1378,14 @@ template< int M, bool FAST, bool HIST > __global__ void __launch_bounds__( 256 )
         const bool     last = iter + 1 == (int)u.niter;
         float3         outDiff, outSpec, outInd;
         float          outVar;
-        atrous_px< M, FAST >( a, io, iter, px, py, i, u8, outDiff, outVar, outSpec, outInd );
+        // block-uniform: the block's taps are all inside the image and inside one checkerboard half
+        const int  step = 1 << iter, sep = u.W / 2;
+        const int  bx0 = blockIdx.x * blockDim.x, bx1 = bx0 + blockDim.x - 1;
+        const int  by0 = blockIdx.y * blockDim.y, by1 = by0 + blockDim.y - 1;
+        const bool interior = bx0 - step >= 0 && by0 - step >= 0 && bx1 + step < u.W && by1 + step < u.H &&
+                              ( bx1 + step < sep || bx0 - step >= sep );
+        if( interior ) atrous_px< M, FAST, true, GEOMIN >( a, io, iter, px, py, i, u8, outDiff, outVar, outSpec, outInd );
+        else atrous_px< M, FAST, false, GEOMIN >( a, io, iter, px, py, i, u8, outDiff, outVar, outSpec, outInd );
         if( !last )
         {
             S::stcv( io.diffDst, io.varDst, (size_t)i, outDiff, outVar );
@@ -1203,7 +1395,13 @@ template< int M, bool FAST, bool HIST > __global__ void __launch_bounds__( 256 )
         else
         {
             const uint16_t hin = compose< M >( a, px, py, (size_t)i, outDiff, outSpec, outInd );
-            if( HIST ) atomicAdd( &hist[ __ldg( &a.binLut[ hin ] ) ], 1u );
+            if( HIST )
+            {
+                // one shared atomic per distinct bin of the warp
+                const uint32_t bin    = __ldg( &a.binLut[ hin ] );
+                const uint32_t peers  = __match_any_sync( __activemask(), bin );
+                if( ( threadIdx.x & 31 ) == (uint32_t)( __ffs( peers ) - 1 ) ) atomicAdd( &hist[ bin ], (uint32_t)__popc( peers ) );
+            }
         }
     }
     if( HIST )
@@ -1274,37 +1472,38 @@ template< int M > cudaError_t launch_stage_t( const FrameArgs& a, int stage, int
     const dim3 gridG( ( a.u.GW + 31 ) / 32, ( a.u.GH + 7 ) / 8 );
     switch( stage )
     {
-        case RGDN_STAGE_GRADIENT_SAMPLES: dev::k_gradient_samples< M ><<< gridG, blk, 0, s >>>( a ); break;
+        case RGDN_STAGE_GRADIENT_SAMPLES: dev::k_gradient_samples< M ><<< gridG, blk, 0, s >>>( a, a.disPing ); break;
         case RGDN_STAGE_GRADIENT_ATROUS: dev::k_gradient_atrous< M ><<< gridG, blk, 0, s >>>( a, iter ); break;
-        case RGDN_STAGE_TEMPORAL_ACCUMULATION: dev::k_temporal< M, false ><<< grid, blk, 0, s >>>( a ); break;
-        case KF_TEMPORAL_FAST: dev::k_temporal< M, true ><<< grid, blk, 0, s >>>( a ); break;
-        case KF_AF_VARIANCE: dev::k_af_variance< M, false ><<< grid, blk, 0, s >>>( a ); break;
-        case KF_AF_VARIANCE_FAST: dev::k_af_variance< M, true ><<< grid, blk, 0, s >>>( a ); break;
-        case KF_GRADIENT_FUSED:
-        {
-            // one co-resident wave: blocks per SM from the occupancy calculator
-            static int blocksPerGrid = 0;
-            if( blocksPerGrid == 0 )
-            {
-                int dev = 0, sms = 0, perSm = 0;
-                cudaGetDevice( &dev );
-                cudaDeviceGetAttribute( &sms, cudaDevAttrMultiProcessorCount, dev );
-                cudaOccupancyMaxActiveBlocksPerMultiprocessor( &perSm, dev::k_gradient_fused< M >, 256, 0 );
-                blocksPerGrid = sms * ( perSm > 0 ? perSm : 1 );
-            }
-            const int need   = ( a.u.GW * a.u.GH + 255 ) / 256;
-            const int blocks = need < blocksPerGrid ? ( need > 0 ? need : 1 ) : blocksPerGrid;
-            void*     args[] = { (void*)&a };
-            return cudaLaunchCooperativeKernel( (const void*)dev::k_gradient_fused< M >, dim3( blocks ), dim3( 256 ), args, 0, s );
-        }
+        case RGDN_STAGE_TEMPORAL_ACCUMULATION: dev::k_temporal< M, false, false, false ><<< grid, blk, 0, s >>>( a ); break;
+        case KF_TEMPORAL_EXACT_GEOM: dev::k_temporal< M, false, true, false ><<< grid, blk, 0, s >>>( a ); break;
+        case KF_TEMPORAL_EXACT_GEOM_GP: dev::k_temporal< M, false, true, true ><<< grid, blk, 0, s >>>( a ); break;
+        case KF_TEMPORAL_FAST: dev::k_temporal< M, true, true, false ><<< grid, blk, 0, s >>>( a ); break;
+        case KF_TEMPORAL_FAST_GP: dev::k_temporal< M, true, true, true ><<< grid, blk, 0, s >>>( a ); break;
+        case KF_ANTI_FIREFLY_FAST: dev::k_antifirefly_fast< M ><<< grid, blk, 0, s >>>( a ); break;
+        case KF_VARIANCE_EXACT_GEOM: dev::k_variance_geo< M, false ><<< grid, blk, 0, s >>>( a ); break;
         case RGDN_STAGE_ANTI_FIREFLY: dev::k_antifirefly< M ><<< grid, blk, 0, s >>>( a ); break;
         case RGDN_STAGE_VARIANCE_ESTIMATION: dev::k_variance< M ><<< grid, blk, 0, s >>>( a ); break;
-        case RGDN_STAGE_ATROUS: dev::k_atrous< M, false, false ><<< grid, blk, 0, s >>>( a, iter ); break;
+        case RGDN_STAGE_ATROUS: dev::k_atrous< M, false, false, false ><<< grid, blk, 0, s >>>( a, iter ); break;
+        case KF_ATROUS_EXACT: dev::k_atrous< M, false, false, true ><<< grid, blk, 0, s >>>( a, iter ); break;
         case RGDN_STAGE_LUMINANCE_HISTOGRAM: dev::k_histogram< M ><<< grid, blk, 0, s >>>( a ); break;
         case RGDN_STAGE_LUMINANCE_AVG: dev::k_luminance_avg< M ><<< 1, 256, 0, s >>>( a ); break;
-        case KF_ATROUS_FAST: dev::k_atrous< M, true, false ><<< grid, blk, 0, s >>>( a, iter ); break;
-        case KF_ATROUS_FAST_HIST: dev::k_atrous< M, true, true ><<< grid, blk, 0, s >>>( a, iter ); break;
-        case KF_ATROUS_EXACT_HIST: dev::k_atrous< M, false, true ><<< grid, blk, 0, s >>>( a, iter ); break;
+        case KF_ATROUS_EXACT_HIST: dev::k_atrous< M, false, true, true ><<< grid, blk, 0, s >>>( a, iter ); break;
+        default: return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+}
+
+// Kernels whose results are continuous in every arithmetic operation (no threshold follows
+// them): compiled in their own translation units with fused multiply-add contraction on.
+template< int M > cudaError_t launch_fast_t( const FrameArgs& a, int stage, int iter, cudaStream_t s )
+{
+    const dim3 blk( 32, 8 );
+    const dim3 grid( ( a.u.W + 31 ) / 32, ( a.u.H + 7 ) / 8 );
+    switch( stage )
+    {
+        case KF_ATROUS_FAST: dev::k_atrous< M, true, false, true ><<< grid, blk, 0, s >>>( a, iter ); break;
+        case KF_ATROUS_FAST_HIST: dev::k_atrous< M, true, true, true ><<< grid, blk, 0, s >>>( a, iter ); break;
+        case KF_VARIANCE_FAST: dev::k_variance_geo< M, true ><<< grid, blk, 0, s >>>( a ); break;
         default: return cudaErrorInvalidValue;
     }
     return cudaGetLastError();
