@@ -178,7 +178,7 @@ def stage_bytes(storage: str) -> dict:
 def kernel_bytes(name: str, it: int, niter: int, per_px: dict) -> float:
     if name == "atrous":
         return per_px["atrous0"] if it == 0 else per_px["atrous_last"] if it == niter - 1 else per_px["atrous"]
-    if name in ("atrous_fast", "atrous_fast_hist", "atrous_exact", "atrous_exact_hist"):
+    if name in ("atrous_fast", "atrous_fast_hist", "atrous_exact", "atrous_exact_hist", "atrous_tma", "atrous_tma_hist"):
         # the geometry record (16 B) replaces normal (4) + depth (2) + metallic-roughness (2)
         base = per_px["atrous0"] if it == 0 else per_px["atrous_last"] if it == niter - 1 else per_px["atrous"]
         return base + 8

@@ -184,6 +184,9 @@ typedef struct rgdn_frame_params
 #define RGDN_FLAG_EXACT_MATH         0x4u /* fused kernels, but the plain path's IEEE math: the same
                                              results as RGDN_FLAG_PLAIN bit for bit (the default
                                              path uses hardware exp2/log2 for continuous weights) */
+#define RGDN_FLAG_TMA_STAGING        0x8u /* a-trous taps staged in shared memory by the Tensor
+                                             Memory Accelerator (widths divisible by 4, up to 5
+                                             iterations); the same results as the default kernels */
 
 /* debugShowFlags bits used on this path (ShaderCommonC.h:156-166) */
 #define RGDN_DEBUG_SHOW_FLAG_ONLY_DIRECT_DIFFUSE   ( 1u << 5 )

@@ -45,7 +45,7 @@ STAGE_GRADIENT_SAMPLES, STAGE_GRADIENT_ATROUS, STAGE_TEMPORAL_ACCUMULATION = 0, 
 STAGE_ANTI_FIREFLY, STAGE_VARIANCE_ESTIMATION, STAGE_ATROUS = 3, 4, 5
 STAGE_LUMINANCE_HISTOGRAM, STAGE_LUMINANCE_AVG = 6, 7
 
-FLAG_PLAIN, FLAG_SKIP_GRADIENTS, FLAG_EXACT_MATH = 0x1, 0x2, 0x4
+FLAG_PLAIN, FLAG_SKIP_GRADIENTS, FLAG_EXACT_MATH, FLAG_TMA_STAGING = 0x1, 0x2, 0x4, 0x8
 
 
 class FrameParams(C.Structure):
@@ -129,7 +129,8 @@ KERNEL_NAMES = dict(enumerate(STAGE_NAMES))
 KERNEL_NAMES.update({100: "atrous_fast", 101: "atrous_fast_hist", 102: "temporal_fast",
                      103: "anti_firefly_fast", 104: "variance_fast", 106: "atrous_exact_hist",
                      107: "atrous_exact", 108: "temporal_exact_geom", 109: "variance_exact_geom",
-                     110: "temporal_fast_gp", 111: "temporal_exact_geom_gp"})
+                     110: "temporal_fast_gp", 111: "temporal_exact_geom_gp", 112: "atrous_tma",
+                     113: "atrous_tma_hist"})
 
 _lib = None
 

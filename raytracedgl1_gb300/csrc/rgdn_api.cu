@@ -19,10 +19,35 @@
 #include <utility>
 #include <vector>
 
+#include <tuple>
+
 #include "rgdn_codec.h"
 #include "rgdn_internal.h"
 
 using namespace rgdn;
+
+namespace
+{
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no libcuda link)
+typedef CUresult ( *EncodeTiledFn )( CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*, const cuuint64_t*,
+                                     const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave, CUtensorMapSwizzle,
+                                     CUtensorMapL2promotion, CUtensorMapFloatOOBfill );
+EncodeTiledFn encode_tiled_fn()
+{
+    static EncodeTiledFn fn   = nullptr;
+    static bool          done = false;
+    if( !done )
+    {
+        void*                           p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if( cudaGetDriverEntryPointByVersion( "cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q ) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess )
+            fn = (EncodeTiledFn)p;
+        done = true;
+    }
+    return fn;
+}
+}  // namespace
 
 namespace
 {
@@ -190,6 +215,8 @@ struct rgdn_stream
     };
     bool                        timing = false;
     bool                        histPending = false;   // a fused denoise accumulated this frame's histogram
+    // tensor maps of the TMA-staged a-trous, keyed by (plane, texel words, box width, box height)
+    std::map< std::tuple< const void*, int, int, int >, CUtensorMap > tmaps;
     std::vector< Pending >      pending;
     std::vector< cudaEvent_t >  eventPool;
     uint32_t                    magic = 0x52474453u;
@@ -405,6 +432,8 @@ rgdn_status ensure_bin_lut( rgdn_stream* s, const rgdn_frame_params* p, cudaStre
 }
 
 rgdn_status run_denoise_fused( rgdn_stream* s, uint32_t fi, const rgdn_frame_params* p, cudaStream_t cs );
+bool        tma_atrous_ok( const rgdn_stream* s, int iter );
+rgdn_status launch_atrous_tma( rgdn_stream* s, const FrameArgs& a, int iter, bool hist, cudaStream_t cs );
 
 rgdn_status run_denoise( rgdn_stream* s, uint32_t fi, const rgdn_frame_params* p, cudaStream_t cs )
 {
@@ -455,11 +484,91 @@ rgdn_status run_denoise_fused( rgdn_stream* s, uint32_t fi, const rgdn_frame_par
     for( uint32_t i = 0; i < a.u.niter; i++ )
     {
         const bool last = i + 1 == a.u.niter;
+        if( !exact && ( p->flags & RGDN_FLAG_TMA_STAGING ) && tma_atrous_ok( s, (int)i ) )
+        {
+            if( ( r = launch_atrous_tma( s, a, (int)i, last, cs ) ) != RGDN_SUCCESS ) return r;
+            continue;
+        }
         const int k = exact ? ( last ? KF_ATROUS_EXACT_HIST : KF_ATROUS_EXACT ) : ( last ? KF_ATROUS_FAST_HIST : KF_ATROUS_FAST );
         if( ( r = launch( s, a, k, (int)i, cs ) ) != RGDN_SUCCESS ) return r;
     }
     s->histPending = true;
     return RGDN_SUCCESS;
+}
+
+// a 2D map of a dense W x H plane of `tw` 4-byte words per texel, boxes of bw x bh texels
+bool tensor_map( rgdn_stream* s, const void* plane, int tw, int bw, int bh, CUtensorMap& out )
+{
+    const auto key = std::make_tuple( plane, tw, bw, bh );
+    auto       it  = s->tmaps.find( key );
+    if( it != s->tmaps.end() )
+    {
+        out = it->second;
+        return true;
+    }
+    EncodeTiledFn fn = encode_tiled_fn();
+    if( !fn ) return false;
+    const cuuint64_t dims[ 2 ]    = { (cuuint64_t)s->W * tw, (cuuint64_t)s->H };
+    const cuuint64_t strides[ 1 ] = { (cuuint64_t)s->W * tw * 4 };
+    const cuuint32_t box[ 2 ]     = { (cuuint32_t)( bw * tw ), (cuuint32_t)bh };
+    const cuuint32_t es[ 2 ]      = { 1, 1 };
+    CUtensorMap      m;
+    if( fn( &m, CU_TENSOR_MAP_DATA_TYPE_UINT32, 2, const_cast< void* >( plane ), dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+            CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE ) != CUDA_SUCCESS )
+        return false;
+    s->tmaps[ key ] = m;
+    out             = m;
+    return true;
+}
+
+// The TMA-staged a-trous needs 16-byte row pitches of every staged plane (W % 4 == 0 covers
+// the 4-byte ones), steps up to 16, and the driver's tensor-map encoder.
+bool tma_atrous_ok( const rgdn_stream* s, int iter )
+{
+    return ( s->W % 4 ) == 0 && iter <= 4 && encode_tiled_fn() != nullptr && atrous_tma_smem( (int)s->storage, iter ) <= 200 * 1024;
+}
+
+rgdn_status launch_atrous_tma( rgdn_stream* s, const FrameArgs& a, int iter, bool hist, cudaStream_t cs )
+{
+    // the sources of this iteration (the routing of atrous_io, CmSVGFAtrous.comp:237-276)
+    const bool  odd = ( iter & 1 ) != 0;
+    const void* cv  = iter == 0 ? a.diffPing : iter == 1 ? a.diffHistory : ( odd ? a.diffPong : a.diffPing );
+    const void* var = iter == 0 ? a.varPing : iter == 1 ? a.varHistory : ( odd ? a.varPong : a.varPing );
+    const void* sp  = iter == 0 ? a.specPing : ( odd ? a.specPong : a.specPing );
+    const void* in  = iter == 0 ? a.indirPing : ( odd ? a.indirPong : a.indirPing );
+    const int   st  = 1 << iter, sx = ( st + 3 ) & ~3;
+    const int   bw  = 32 + 2 * sx, bh = st > 8 ? 8 : 8 + 2 * st;
+    const int   tCv = s->storage == RGDN_STORAGE_FP32 ? 4 : 2;
+    const int   tCol = s->storage == RGDN_STORAGE_REF ? 1 : s->storage == RGDN_STORAGE_FP32 ? 4 : 2;
+    AtrousMaps  m;
+    if( !tensor_map( s, cv, tCv, bw, bh, m.cv ) || !tensor_map( s, sp, tCol, bw, bh, m.spec ) || !tensor_map( s, in, tCol, bw, bh, m.indir ) ||
+        !tensor_map( s, a.geom, 4, bw, bh, m.geo ) )
+        return RGDN_DEVICE_ERROR;
+    if( var ) { if( !tensor_map( s, var, 1, bw, bh, m.var ) ) return RGDN_DEVICE_ERROR; }
+    else m.var = m.cv;
+    cudaEvent_t ea = nullptr, eb = nullptr;
+    if( s->timing )
+    {
+        ea = take_event( s );
+        eb = take_event( s );
+        if( !ea || !eb ) return RGDN_DEVICE_ERROR;
+        cudaEventRecord( ea, cs );
+    }
+    cudaError_t e;
+    switch( s->storage )
+    {
+        case RGDN_STORAGE_REF: e = launch_atrous_tma_ref( a, iter, hist, &m, cs ); break;
+        case RGDN_STORAGE_FP32: e = launch_atrous_tma_f32( a, iter, hist, &m, cs ); break;
+        case RGDN_STORAGE_FP16: e = launch_atrous_tma_f16( a, iter, hist, &m, cs ); break;
+        default: e = launch_atrous_tma_bf16( a, iter, hist, &m, cs ); break;
+    }
+    s->ctx->launches.fetch_add( 1, std::memory_order_relaxed );
+    if( s->timing )
+    {
+        cudaEventRecord( eb, cs );
+        s->pending.push_back( { hist ? KF_ATROUS_TMA_HIST : KF_ATROUS_TMA, iter, ea, eb } );
+    }
+    return cuda_status( e );
 }
 
 rgdn_status run_exposure( rgdn_stream* s, uint32_t fi, const rgdn_frame_params* p, cudaStream_t cs )
@@ -610,6 +719,7 @@ static rgdn_status stream_alloc( rgdn_stream* s, uint32_t W, uint32_t H )
     s->geom[ 0 ] = (float4*)( (uint8_t*)block + align_up( sizeof( Tonemapping ) ) + align_up( 65536 ) );
     s->geom[ 1 ] = (float4*)( (uint8_t*)s->geom[ 0 ] + align_up( (size_t)W * H * 16 ) );
     s->geomValid[ 0 ] = s->geomValid[ 1 ] = false;
+    s->tmaps.clear();
     s->lutMin = s->lutMax = NAN;
     return RGDN_SUCCESS;
 }

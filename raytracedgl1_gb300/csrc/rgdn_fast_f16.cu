@@ -8,4 +8,8 @@ cudaError_t launch_fast_f16( const FrameArgs& a, int stage, int iter, cudaStream
 {
     return launch_fast_t< MODE_F16 >( a, stage, iter, s );
 }
+cudaError_t launch_atrous_tma_f16( const FrameArgs& a, int iter, bool hist, const void* maps, cudaStream_t s )
+{
+    return launch_atrous_tma_t< MODE_F16 >( a, iter, hist, maps, s );
+}
 }  // namespace rgdn

@@ -2,6 +2,7 @@
 // (rgdn_kernels.cuh, instantiated once per storage mode in rgdn_mode_*.cu).
 #pragma once
 
+#include <cuda.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -27,7 +28,7 @@ struct Tonemapping
 {
     uint32_t histogram[ 256 ];
     float    avgLuminance;
-    uint32_t blocksDone;   // completion counter of the fused histogram (zero between frames)
+    uint32_t errorFlags;   // device-side failures (bit 0: a bounded wait for staged data ran out)
 };
 
 // The subset of ShGlobalUniform (ShaderCommonC.h:209-304) this path reads, plus sizes.
@@ -131,6 +132,8 @@ enum FusedKernel : int
     KF_VARIANCE_EXACT_GEOM = 109,  // variance reading the geometry record, IEEE math
     KF_TEMPORAL_FAST_GP    = 110,  // KF_TEMPORAL_FAST reading the previous frame's geometry record
     KF_TEMPORAL_EXACT_GEOM_GP = 111,
+    KF_ATROUS_TMA          = 112,  // TMA-staged a-trous iteration (timing label)
+    KF_ATROUS_TMA_HIST     = 113,  // TMA-staged last iteration + fused histogram (timing label)
 };
 
 // Launches one stage for one frame. Returns the CUDA error of the launch.
@@ -145,6 +148,20 @@ cudaError_t launch_fast_ref( const FrameArgs& a, int stage, int iter, cudaStream
 cudaError_t launch_fast_f32( const FrameArgs& a, int stage, int iter, cudaStream_t s );
 cudaError_t launch_fast_f16( const FrameArgs& a, int stage, int iter, cudaStream_t s );
 cudaError_t launch_fast_bf16( const FrameArgs& a, int stage, int iter, cudaStream_t s );
+// Tensor maps of the five images one TMA-staged a-trous iteration reads
+struct AtrousMaps
+{
+    CUtensorMap cv, var, spec, indir, geo;
+};
+
+// TMA-staged a-trous iteration (FAST weights) with the tensor maps of its sources
+// (`maps` points to the kernels' AtrousMaps: 5 CUtensorMap for colour+variance, variance,
+// specular, indirect, geometry), and the dynamic shared memory one launch needs
+cudaError_t launch_atrous_tma_ref( const FrameArgs& a, int iter, bool hist, const void* maps, cudaStream_t s );
+cudaError_t launch_atrous_tma_f32( const FrameArgs& a, int iter, bool hist, const void* maps, cudaStream_t s );
+cudaError_t launch_atrous_tma_f16( const FrameArgs& a, int iter, bool hist, const void* maps, cudaStream_t s );
+cudaError_t launch_atrous_tma_bf16( const FrameArgs& a, int iter, bool hist, const void* maps, cudaStream_t s );
+int atrous_tma_smem( int storage, int iter );
 inline bool is_fast_kernel( int stage ) { return stage == KF_ATROUS_FAST || stage == KF_ATROUS_FAST_HIST || stage == KF_VARIANCE_FAST; }
 
 }  // namespace rgdn

@@ -11,6 +11,7 @@
 // threads map x -> threadIdx.x so that a warp reads 32 consecutive texels of a row.
 #pragma once
 
+#include <cuda.h>
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
 
@@ -1412,6 +1413,344 @@ template< int M, bool FAST, bool HIST, bool GEOMIN > __global__ void __launch_bo
 }
 
 // ==========================================================================================
+// A-trous with shared-memory staging by the Tensor Memory Accelerator (default path).
+//
+// A 32x8 output tile reads its 3x3 dilated taps from shared memory. The tap footprint of each
+// source image (colour+variance, variance plane, specular, indirect, geometry record) is
+// copied by TMA (cp.async.bulk.tensor.2d) before any arithmetic: one box of
+// (32 + 2 sx) x (8 + 2 s) texels for steps s <= 8, or three 8-row bands (rows -s, 0, +s) for
+// s = 16, with sx = s rounded up to 4 texels so every box starts on a 16-byte boundary.
+// Texels outside the image arrive as zeros (TMA out-of-bounds fill), which is the zero-texel
+// rule; only the geometry record needs a patch there (a zero normal code decodes to (0,0,1)).
+// Completion is an mbarrier transaction count; the wait is bounded and a timeout sets an
+// error bit in the stream's tonemapping block instead of hanging.
+// ==========================================================================================
+__device__ __forceinline__ uint32_t smem_u32( const void* p ) { return (uint32_t)__cvta_generic_to_shared( p ); }
+__device__ __forceinline__ void mbar_init( uint64_t* bar, uint32_t count )
+{
+    asm volatile( "mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"( smem_u32( bar ) ), "r"( count ) : "memory" );
+}
+__device__ __forceinline__ void fence_async_shared() { asm volatile( "fence.proxy.async.shared::cta;" ::: "memory" ); }
+__device__ __forceinline__ void mbar_arrive_expect_tx( uint64_t* bar, uint32_t bytes )
+{
+    asm volatile( "mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"( smem_u32( bar ) ), "r"( bytes ) : "memory" );
+}
+__device__ __forceinline__ void tma_load_2d( void* dst, const CUtensorMap* tm, int x, int y, uint64_t* bar )
+{
+    asm volatile( "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
+                      smem_u32( dst ) ),
+                  "l"( (uint64_t)tm ), "r"( x ), "r"( y ), "r"( smem_u32( bar ) )
+                  : "memory" );
+}
+__device__ __forceinline__ bool mbar_try_wait( uint64_t* bar, uint32_t phase )
+{
+    uint32_t ok;
+    asm volatile( "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+                  : "=r"( ok )
+                  : "r"( smem_u32( bar ) ), "r"( phase )
+                  : "memory" );
+    return ok != 0;
+}
+// bounded wait: false after the limit (the error bit is then set by the caller)
+__device__ __forceinline__ bool mbar_wait_bounded( uint64_t* bar, uint32_t phase )
+{
+    for( int k = 0; k < ( 1 << 22 ); k++ )
+        if( mbar_try_wait( bar, phase ) ) return true;
+    return false;
+}
+
+// texel bytes of the staged planes per mode: colour+variance, variance plane, colour
+template< int M > struct TmaTexel;
+template<> struct TmaTexel< MODE_REF > { static constexpr int cv = 8, var = 0, col = 4; };
+template<> struct TmaTexel< MODE_F32 > { static constexpr int cv = 16, var = 0, col = 16; };
+template<> struct TmaTexel< MODE_F16 > { static constexpr int cv = 8, var = 4, col = 8; };
+template<> struct TmaTexel< MODE_BF16 > { static constexpr int cv = 8, var = 4, col = 8; };
+
+// shared-memory geometry of one step (the host computes the same for the launch size)
+struct TmaGeom
+{
+    int s, sx, rw, rh, nb;   // step, column halo, box width / height, boxes (1 or 3 bands)
+    int offCv, offVar, offSpec, offInd, offGeo, bytes;
+};
+__host__ __device__ __forceinline__ int tma_align128( int v ) { return ( v + 127 ) & ~127; }
+template< int M > __host__ __device__ __forceinline__ TmaGeom tma_geom( int iter )
+{
+    TmaGeom g;
+    g.s  = 1 << iter;
+    g.sx = ( g.s + 3 ) & ~3;
+    g.rw = 32 + 2 * g.sx;
+    g.nb = g.s > 8 ? 3 : 1;
+    g.rh = g.s > 8 ? 8 : 8 + 2 * g.s;
+    const int texels = g.rw * g.rh * g.nb;
+    int off = 0;
+    g.offCv   = off; off = tma_align128( off + texels * TmaTexel< M >::cv );
+    g.offVar  = off; off = tma_align128( off + texels * TmaTexel< M >::var );
+    g.offSpec = off; off = tma_align128( off + texels * TmaTexel< M >::col );
+    g.offInd  = off; off = tma_align128( off + texels * TmaTexel< M >::col );
+    g.offGeo  = off; off = tma_align128( off + texels * 16 );
+    g.bytes   = off;
+    return g;
+}
+
+template< int M > struct TmaLd;
+template<> struct TmaLd< MODE_REF >
+{
+    __device__ static float4 cv( const uint8_t* b, const uint8_t*, int k )
+    {
+        const ushort4 h = reinterpret_cast< const ushort4* >( b )[ k ];
+        return make_float4( h2f( h.x ), h2f( h.y ), h2f( h.z ), h2f( h.w ) );
+    }
+    __device__ static float3 col( const uint8_t* b, int k ) { return e5( reinterpret_cast< const uint32_t* >( b )[ k ] ); }
+};
+template<> struct TmaLd< MODE_F32 >
+{
+    __device__ static float4 cv( const uint8_t* b, const uint8_t*, int k ) { return reinterpret_cast< const float4* >( b )[ k ]; }
+    __device__ static float3 col( const uint8_t* b, int k )
+    {
+        const float4 v = reinterpret_cast< const float4* >( b )[ k ];
+        return f3( v.x, v.y, v.z );
+    }
+};
+template< bool BF > struct TmaLd16
+{
+    __device__ static float cvt( uint16_t h ) { return BF ? b2f( h ) : h2f( h ); }
+    __device__ static float4 cv( const uint8_t* b, const uint8_t* var, int k )
+    {
+        const ushort4 h = reinterpret_cast< const ushort4* >( b )[ k ];
+        return make_float4( cvt( h.x ), cvt( h.y ), cvt( h.z ), reinterpret_cast< const float* >( var )[ k ] );
+    }
+    __device__ static float3 col( const uint8_t* b, int k )
+    {
+        const ushort4 h = reinterpret_cast< const ushort4* >( b )[ k ];
+        return f3( cvt( h.x ), cvt( h.y ), cvt( h.z ) );
+    }
+};
+template<> struct TmaLd< MODE_F16 > : TmaLd16< false > {};
+template<> struct TmaLd< MODE_BF16 > : TmaLd16< true > {};
+
+template< int M, bool FAST, bool INTERIOR >
+__device__ __forceinline__ void atrous_px_tma( const FrameArgs& a, const AtrousIO& io, const TmaGeom& g, const uint8_t* sm, const int iter,
+                                               const int px, const int py, const int tx, const int ty, const int i, const float* u8,
+                                               float3& outDiff, float& outVar, float3& outSpec, float3& outInd )
+{
+    using S          = Sto< M >;
+    using L          = TmaLd< M >;
+    using X          = Wm< FAST >;
+    const Uniform& u = a.u;
+    const int      step = g.s;
+    // shared-memory texel index of tap (dx, dy) of this thread's pixel
+    auto kidx = [ & ]( int dx, int dy ) {
+        const int row = g.nb == 3 ? ( dy + 1 ) * 8 + ty : step + ty + dy * step;
+        return row * g.rw + g.sx + tx + dx * step;
+    };
+    const uint8_t* bCv  = sm + g.offCv;
+    const uint8_t* bVar = sm + g.offVar;
+    const uint8_t* bSp  = sm + g.offSpec;
+    const uint8_t* bIn  = sm + g.offInd;
+    const float4*  bGeo = reinterpret_cast< const float4* >( sm + g.offGeo );
+    const int      k0   = kidx( 0, 0 );
+    const float4   cv   = L::cv( bCv, bVar, k0 );
+    outDiff = f3( cv.x, cv.y, cv.z );
+    outVar  = cv.w;
+    outSpec = L::col( bSp, k0 );
+    outInd  = L::col( bIn, k0 );
+    const float4 gc4 = bGeo[ k0 ];
+    const Geo    gc  = { make_float3( gc4.x, gc4.y, gc4.z ), __float_as_uint( gc4.w ) };
+    const float  z   = geo_depth( gc );
+    const float  gradDepth = h2f( a.depthGrad[ i ] );
+    if( z < 0.0f || z > MAX_RAY_LENGTH )
+    {
+        if( iter == 0 )
+        {
+            outDiff = f3( 0, 0, 0 ); outVar = 0.0f; outSpec = f3( 0, 0, 0 ); outInd = f3( 0, 0, 0 );
+        }
+        return;
+    }
+    const Area   chArea = cb_area( u, px );
+    const float3 normal = gc.n;
+    const float  l      = luminance( outDiff );
+    float        prefVar;
+    if( iter == 0 )
+    {
+        // prefilterLuminanceVariance (CmSVGFAtrous_Iter0.comp:158-187); the staged footprint
+        // covers +-1 and holds zeros outside the image
+        const float gk[ 2 ][ 2 ] = { { 0.25f, 0.125f }, { 0.125f, 0.0625f } };
+        float r = 0.0f;
+#pragma unroll
+        for( int yy = -1; yy <= 1; yy++ )
+        {
+#pragma unroll
+            for( int xx = -1; xx <= 1; xx++ ) r = r + L::cv( bCv, bVar, kidx( xx, yy ) ).w * gk[ xx < 0 ? -xx : xx ][ yy < 0 ? -yy : yy ];
+        }
+        r = sqrtf( fmaxf( r, 0.0f ) );
+        S::st1( a.filtVar, (size_t)i, r );
+        prefVar = r;
+    }
+    else prefVar = S::ld1( a.filtVar, (size_t)i );
+
+    const float wLumMul   = 1.0f / ( 4.0f * prefVar + 0.00001f );
+    const float roughness = u8[ geo_rough8( gc ) ];
+    const float wRoughMul = gclamp( roughness * 30.0f - (float)iter, 0.0f, 1.0f );
+    const float hS        = S::ld4( a.histLen, (size_t)i ).z;
+    const float nws       = gclamp( hS / 8.0f, 0.0f, 1.0f );
+    float       nwSpec    = spec_power( roughness * roughness );
+    nwSpec                = gclamp( nwSpec, 8.0f, 1024.0f );
+    nwSpec                = nwSpec * nws;
+    const float rz1 = FAST ? 1.0f / fmaxf( gradDepth * 1.0f, 0.01f ) : 0.0f;
+    const float rz2 = FAST ? 1.0f / fmaxf( gradDepth * 2.0f, 0.01f ) : 0.0f;
+
+    const float kern[ 2 ][ 2 ] = { { 1.0f, 0.5f }, { 0.5f, 0.25f } };
+    float ws = 1.0f, wsS = 1.0f, wsI = 1.0f;
+#pragma unroll
+    for( int yy = -1; yy <= 1; yy++ )
+    {
+#pragma unroll
+        for( int xx = -1; xx <= 1; xx++ )
+        {
+            if( xx == 0 && yy == 0 ) continue;
+            const int    qx  = px + xx * step, qy = py + yy * step;
+            const int    k   = kidx( xx, yy );
+            const float4 gq4 = bGeo[ k ];
+            Geo          gq  = { make_float3( gq4.x, gq4.y, gq4.z ), __float_as_uint( gq4.w ) };
+            if( !INTERIOR && !inside( u, qx, qy ) ) gq = geo_zero();
+            const float  rq  = u8[ geo_rough8( gq ) ];
+            const float3 nq  = gq.n;
+            const float  zq  = geo_depth( gq );
+            const float3 sq  = L::col( bSp, k );
+            const float4 cvq = L::cv( bCv, bVar, k );
+            const float3 dq  = f3( cvq.x, cvq.y, cvq.z );
+            const float  lq  = luminance( dq );
+            const float  nn  = fmaxf( 0.0f, dot3( normal, nq ) );
+            const float3 iq  = L::col( bIn, k );
+            const int    man = ( xx < 0 ? -xx : xx ) + ( yy < 0 ? -yy : yy );
+
+            const float w_z = FAST ? fabsf( z - zq ) * ( man == 1 ? rz1 : rz2 )
+                                   : fabsf( z - zq ) / fmaxf( gradDepth * (float)man, 0.01f );
+            const float w_n = X::pow128( nn );
+            const float w_l = fabsf( l - lq ) * wLumMul;
+            float       w_r = fmaxf( 0.0f, 1.0f - 10.0f * fabsf( roughness - rq ) ) * wRoughMul;
+            if( nwSpec > 0.0f && w_r > 0.0f ) w_r = w_r * X::pow01( nn, nwSpec );
+            const float waveletW = kern[ yy < 0 ? -yy : yy ][ xx < 0 ? -xx : xx ];
+            const float insideA  = ( INTERIOR || in_area( qx, qy, chArea ) ) ? 1.0f : 0.0f;
+            const float wBase    = X::expn( -w_z * w_z ) * w_n * waveletW * insideA;
+            const float wDiff    = wBase * X::expn( -w_l );
+            const float wSpec    = wBase * w_r;
+            const float wInd     = wBase;
+
+            outDiff = f3( X::madd( dq.x, wDiff, outDiff.x ), X::madd( dq.y, wDiff, outDiff.y ), X::madd( dq.z, wDiff, outDiff.z ) );
+            outSpec = f3( X::madd( sq.x, wSpec, outSpec.x ), X::madd( sq.y, wSpec, outSpec.y ), X::madd( sq.z, wSpec, outSpec.z ) );
+            outInd  = f3( X::madd( iq.x, wInd, outInd.x ), X::madd( iq.y, wInd, outInd.y ), X::madd( iq.z, wInd, outInd.z ) );
+            outVar  = X::madd( cvq.w * wDiff, wDiff, outVar );
+            ws      = ws + wDiff;
+            wsS     = wsS + wSpec;
+            wsI     = wsI + wInd;
+        }
+    }
+    const float inv = 1.0f / ws, invS = 1.0f / wsS, invI = 1.0f / wsI;
+    outDiff = mul( outDiff, inv );
+    outVar  = outVar * inv * inv;
+    outSpec = mul( outSpec, invS );
+    outInd  = mul( outInd, invI );
+}
+
+template< int M, bool FAST, bool HIST >
+__global__ void __launch_bounds__( 256, 2 ) k_atrous_tma( const FrameArgs a, const int iter, const __grid_constant__ AtrousMaps maps )
+{
+    using S = Sto< M >;
+    extern __shared__ __align__( 128 ) uint8_t sm[];
+    __shared__ __align__( 8 ) uint64_t bar;
+    __shared__ float    u8[ 256 ];
+    __shared__ uint32_t hist[ HIST ? 256 : 1 ];
+    const Uniform& u  = a.u;
+    const int      t  = threadIdx.y * blockDim.x + threadIdx.x;
+    const TmaGeom  g  = tma_geom< M >( iter );
+    const int      x0 = blockIdx.x * 32, y0 = blockIdx.y * 8;
+    if( t == 0 )
+    {
+        mbar_init( &bar, 1 );
+        fence_async_shared();
+    }
+    __syncthreads();
+    if( t == 0 )
+    {
+        constexpr int tCv = TmaTexel< M >::cv, tVar = TmaTexel< M >::var, tCol = TmaTexel< M >::col;
+        const int boxTexels = g.rw * g.rh;
+        mbar_arrive_expect_tx( &bar, (uint32_t)( boxTexels * g.nb * ( tCv + tVar + 2 * tCol + 16 ) ) );
+        for( int b = 0; b < g.nb; b++ )
+        {
+            const int y  = g.nb == 3 ? y0 + ( b - 1 ) * g.s : y0 - g.s;
+            const int xt = x0 - g.sx;   // texels; the maps address 4-byte words
+            const int o  = b * boxTexels;
+            tma_load_2d( sm + g.offCv + o * tCv, &maps.cv, xt * ( tCv / 4 ), y, &bar );
+            if( tVar ) tma_load_2d( sm + g.offVar + o * tVar, &maps.var, xt * ( tVar / 4 ), y, &bar );
+            tma_load_2d( sm + g.offSpec + o * tCol, &maps.spec, xt * ( tCol / 4 ), y, &bar );
+            tma_load_2d( sm + g.offInd + o * tCol, &maps.indir, xt * ( tCol / 4 ), y, &bar );
+            tma_load_2d( sm + g.offGeo + o * 16, &maps.geo, xt * 4, y, &bar );
+        }
+    }
+    u8[ t ] = (float)t / 255.0f;
+    if( HIST ) hist[ t ] = 0u;
+    // block-uniform readiness: every thread leaves together or computes together
+    const bool ready = __syncthreads_and( mbar_wait_bounded( &bar, 0 ) ? 1 : 0 ) != 0;
+    if( !ready )
+    {
+        // the copies did not complete: flag the stream and keep the outputs untouched
+        if( t == 0 ) atomicOr( &a.tm->errorFlags, 1u );
+        return;
+    }
+    const int px = x0 + threadIdx.x, py = y0 + threadIdx.y;
+    if( px < u.W && py < u.H )
+    {
+        const int      i    = py * u.W + px;
+        const AtrousIO io   = atrous_io< M >( a, iter );
+        const bool     last = iter + 1 == (int)u.niter;
+        float3         outDiff, outSpec, outInd;
+        float          outVar;
+        const int  sep      = u.W / 2;
+        const bool interior = x0 - g.s >= 0 && y0 - g.s >= 0 && x0 + 31 + g.s < u.W && y0 + 7 + g.s < u.H &&
+                              ( x0 + 31 + g.s < sep || x0 - g.s >= sep );
+        if( interior ) atrous_px_tma< M, FAST, true >( a, io, g, sm, iter, px, py, threadIdx.x, threadIdx.y, i, u8, outDiff, outVar, outSpec, outInd );
+        else atrous_px_tma< M, FAST, false >( a, io, g, sm, iter, px, py, threadIdx.x, threadIdx.y, i, u8, outDiff, outVar, outSpec, outInd );
+        if( !last )
+        {
+            S::stcv( io.diffDst, io.varDst, (size_t)i, outDiff, outVar );
+            S::st3( io.specDst, (size_t)i, outSpec );
+            S::st3( io.indirDst, (size_t)i, outInd );
+        }
+        else
+        {
+            const uint16_t hin = compose< M >( a, px, py, (size_t)i, outDiff, outSpec, outInd );
+            if( HIST )
+            {
+                const uint32_t bin   = __ldg( &a.binLut[ hin ] );
+                const uint32_t peers = __match_any_sync( __activemask(), bin );
+                if( ( threadIdx.x & 31 ) == (uint32_t)( __ffs( peers ) - 1 ) ) atomicAdd( &hist[ bin ], (uint32_t)__popc( peers ) );
+            }
+        }
+    }
+    if( HIST )
+    {
+        __syncthreads();
+        if( hist[ t ] ) atomicAdd( &a.tm->histogram[ t ], hist[ t ] );
+    }
+}
+
+template< int M, bool FAST, bool HIST > cudaError_t launch_atrous_tma( const FrameArgs& a, int iter, const AtrousMaps& maps, cudaStream_t s )
+{
+    const TmaGeom g = tma_geom< M >( iter );
+    static int    attrBytes = 0;
+    if( attrBytes < g.bytes )
+    {
+        cudaError_t e = cudaFuncSetAttribute( k_atrous_tma< M, FAST, HIST >, cudaFuncAttributeMaxDynamicSharedMemorySize, g.bytes );
+        if( e != cudaSuccess ) return e;
+        attrBytes = g.bytes;
+    }
+    const dim3 grid( ( a.u.W + 31 ) / 32, ( a.u.H + 7 ) / 8 );
+    k_atrous_tma< M, FAST, HIST ><<< grid, dim3( 32, 8 ), g.bytes, s >>>( a, iter, maps );
+    return cudaGetLastError();
+}
+
+// ==========================================================================================
 // CmLuminanceHistogram.comp:60-86 — 256-bin histogram of HistogramInput. Bins come from a
 // 65536-entry table indexed by the fp16 bits (built on the host from getColorBin, :41-54).
 // ==========================================================================================
@@ -1508,5 +1847,12 @@ template< int M > cudaError_t launch_fast_t( const FrameArgs& a, int stage, int 
     }
     return cudaGetLastError();
 }
+
+template< int M > cudaError_t launch_atrous_tma_t( const FrameArgs& a, int iter, bool hist, const void* maps, cudaStream_t s )
+{
+    const AtrousMaps& m = *static_cast< const AtrousMaps* >( maps );
+    return hist ? dev::launch_atrous_tma< M, true, true >( a, iter, m, s ) : dev::launch_atrous_tma< M, true, false >( a, iter, m, s );
+}
+template< int M > int atrous_tma_smem_t( int iter ) { return dev::tma_geom< M >( iter ).bytes; }
 
 }  // namespace rgdn

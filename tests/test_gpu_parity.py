@@ -285,6 +285,32 @@ def test_fast_math_close_to_exact(ctx, mode_name, mode):
     b.close()
 
 
+@pytest.mark.parametrize("mode_name,mode", MODES)
+def test_tma_staging_equals_default(ctx, mode_name, mode):
+    """The TMA-staged a-trous computes the default kernels' arithmetic: identical planes."""
+    W, H = 96, 54   # width divisible by 4: every iteration takes the TMA path
+    sc = Scene(W, H, seed=19, lightFlickerFrom=2.0)
+    a = Stream(ctx, W, H, mode)
+    b = Stream(ctx, W, H, mode)
+    for f in range(5):
+        fi = f & 1
+        bufs, p = sc.generate(f)
+        p.atrousIterations = 5 if f % 2 else 4
+        upload_frame(a, None, bufs, fi)
+        upload_frame(b, None, bufs, fi)
+        pb = p.copy()
+        pb.flags = N.FLAG_TMA_STAGING
+        for s, q in ((a, p), (b, pb)):
+            Denoiser(s).Denoise(fi, q)
+            Tonemapping(s).CalculateExposure(fi, q)
+        ga, gb = gpu_planes(a), gpu_planes(b)
+        for key in ga:
+            assert np.array_equal(ga[key][0], gb[key][0]), f"frame {f}: {key} differs"
+        assert np.array_equal(a.tonemapping()[0], b.tonemapping()[0])
+    a.close()
+    b.close()
+
+
 def test_batch_equals_sequential(ctx):
     """rgdn_submit_batch over streams of different sizes == each stream alone."""
     sizes = [(64, 36), (48, 30), (96, 54)]
