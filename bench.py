@@ -57,6 +57,18 @@ def parse():
     ap.add_argument("--path", default="fused", choices=["fused", "plain"],
                     help="fused: the default kernels; plain: one kernel per reference dispatch")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-batched", action="store_true", help="skip the 32-stream batched measurement")
+    ap.add_argument("--batch-steps", type=int, default=30)
+    ap.add_argument("--batch-frames", type=int, default=4, help="distinct resident frames per batched stream")
+    ap.add_argument("--batch-per-res", type=int, default=8, help="batched streams per resolution")
+    ap.add_argument("--no-serving", action="store_true", help="skip the 64-stream serving measurement")
+    ap.add_argument("--serve-seconds", type=float, default=3.0)
+    ap.add_argument("--serve-hz", type=float, nargs="+", default=[60.0, 15.0],
+                    help="per-stream Poisson frame rates to serve (the configured 60 Hz first)")
+    ap.add_argument("--serve-step-mpix", type=float, default=8.0, help="pixel bound of one serving step (Mpix)")
+    ap.add_argument("--precision-sweep", action="store_true",
+                    help="instead of the benchmark: fp32/fp16/bf16 storage against the FP64 oracle "
+                         "(use with --width 3840 --height 2160 --frames 30)")
     return ap.parse_args()
 
 
@@ -288,6 +300,253 @@ def config_dict(args) -> dict:
 
 
 # ------------------------------------------------------------------------------------------
+# batched: 32 streams of mixed resolution advance one frame per step (rgdn_submit_batch)
+# ------------------------------------------------------------------------------------------
+BATCH_MIX = [(640, 360), (1280, 720), (1920, 1080), (2560, 1440)]
+
+
+def run_batched(args, dist: Dist, dev: int, cs) -> dict:
+    """Mpix/s of batched steps over 8 streams each of 640x360, 1280x720, 1920x1080 and
+    2560x1440 (fp16 storage), beside the same frames one stream per call on the default path
+    and on the plain path (one kernel per reference dispatch). G-buffers are resident in HBM
+    and bound without a copy; `batch_frames` distinct frames per stream cycle."""
+    import numpy as np
+    import torch
+
+    from raytracedgl1_gb300 import _native as N
+    from raytracedgl1_gb300.denoiser import Context, Denoiser, Stream, Tonemapping
+    from raytracedgl1_gb300.scene import Scene
+
+    ctx = Context(dev)
+    storage = STORAGE["fp16"]
+    streams, seqs = [], []
+    for r, (W, H) in enumerate(BATCH_MIX):
+        for k in range(args.batch_per_res):
+            sid = r * args.batch_per_res + k
+            sc = Scene(W, H, seed=100 + sid + 1000 * dist.rank)
+            s = Stream(ctx, W, H, storage)
+            frames = []
+            for f in range(args.batch_frames):
+                bufs, p = sc.generate(f)
+                p.atrousIterations = args.iters
+                frames.append(({name: torch.from_numpy(np.ascontiguousarray(a).view(np.uint8).reshape(-1)).to(f"cuda:{dev}")
+                                for name, a in bufs.items()}, p))
+            streams.append(s)
+            seqs.append(frames)
+    torch.cuda.synchronize()
+    px = sum(s.width * s.height for s in streams)
+
+    def jobs_for(k: int, flags: int = 0):
+        jobs = []
+        for s, frames in zip(streams, seqs):
+            bufs, p = frames[k % len(frames)]
+            fi = k & 1
+            for name, t in bufs.items():
+                s.bind(name, fi, t.data_ptr())
+            if flags:
+                p = p.copy()
+                p.flags |= flags
+            jobs.append((s, fi, p))
+        return jobs
+
+    def batched(k):
+        ctx.submit_batch(jobs_for(k), cs)
+
+    def one_by_one(k, flags):
+        for s, fi, p in jobs_for(k, flags):
+            Denoiser(s).Denoise(fi, p, cs)
+            Tonemapping(s).CalculateExposure(fi, p, cs)
+
+    def timed(fn, steps: int, first: int):
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(steps + 1)]
+        dist.barrier()
+        torch.cuda.synchronize()
+        with torch.cuda.stream(cs):
+            ev[0].record(cs)
+            for k in range(steps):
+                fn(first + k)
+                ev[k + 1].record(cs)
+        cs.synchronize()
+        dist.barrier()
+        per = sorted(ev[k].elapsed_time(ev[k + 1]) for k in range(steps))
+        return dist.max(ev[0].elapsed_time(ev[-1])), per
+
+    k = 0
+    with torch.cuda.stream(cs):
+        for _ in range(24):          # autotuning (18 steps) + graph capture
+            batched(k)
+            k += 1
+    cs.synchronize()
+    cfg = ctx.batch_config(storage)
+    launches0 = ctx.launch_count()
+    t_b, per_b = timed(batched, args.batch_steps, k)
+    launches = ctx.launch_count() - launches0
+    k += args.batch_steps
+    # per-launch device time of batched steps (direct launches with events)
+    ctx.set_batch_timing(True)
+    with torch.cuda.stream(cs):
+        for _ in range(3):
+            batched(k)
+            k += 1
+    cs.synchronize()
+    tim = ctx.read_batch_timing()
+    ctx.set_batch_timing(False)
+    steps_cmp = max(3, args.batch_steps // 5)
+    with torch.cuda.stream(cs):
+        one_by_one(k, 0)
+    t_s, _ = timed(lambda j: one_by_one(j, 0), steps_cmp, k + 1)
+    k += 1 + steps_cmp
+    with torch.cuda.stream(cs):
+        one_by_one(k, N.FLAG_PLAIN)
+    t_p, _ = timed(lambda j: one_by_one(j, N.FLAG_PLAIN), steps_cmp, k + 1)
+
+    per_px = stage_bytes("fp16")
+    kern = []
+    for (name, it), (n, ms) in tim.items():
+        if name == "atrous":
+            alg = kernel_bytes("atrous_fast", it, args.iters, per_px) * px
+        elif name in ("gradient_samples", "gradient_atrous"):
+            alg = per_px[name] * px
+        else:
+            alg = per_px.get({"temporal_accumulation": "temporal_fast_gp", "anti_firefly": "anti_firefly_fast",
+                              "variance_estimation": "variance_fast"}.get(name, name), 0.0) * px
+        kern.append({"kernel": f"batched_{name}[{it}]", "launches": n, "avg_us": round(1e3 * ms / n, 2),
+                     "alg_bytes": alg, "gbs": round(alg / (ms / n / 1e3) / 1e9, 1)})
+    kern.sort(key=lambda d: -d["avg_us"] * d["launches"])
+    out = {
+        "workload": f"{len(streams)} streams: {args.batch_per_res} each of "
+                    + ", ".join(f"{w}x{h}" for w, h in BATCH_MIX)
+                    + f", fp16 storage, {args.iters} a-trous passes + gradient a-trous, one frame per stream per step",
+        "mpix_per_step": round(px / 1e6, 3),
+        "value": round(px * args.batch_steps * dist.world / (t_b / 1e3) / 1e6, 1), "unit": "Mpix/s",
+        "ms_per_step": round(t_b / args.batch_steps, 3),
+        "p50_ms": round(per_b[len(per_b) // 2], 3), "p99_ms": round(per_b[int(0.99 * (len(per_b) - 1))], 3),
+        "steps": args.batch_steps, "gpu_launches": int(launches),
+        "one_stream_per_call_mpix_s": round(px * steps_cmp * dist.world / (t_s / 1e3) / 1e6, 1),
+        "plain_path_mpix_s": round(px * steps_cmp * dist.world / (t_p / 1e3) / 1e6, 1),
+        "tuned_config": {"temporal": int(cfg.temporalTile), "anti_firefly": int(cfg.antiFireflyTile),
+                         "variance": int(cfg.varianceTile), "atrous": [int(v) for v in cfg.atrousTile][:args.iters],
+                         "atrous_two_blocks": [int(v) for v in cfg.atrousTwoBlocks][:args.iters],
+                         "graphs": int(cfg.useGraphs), "tile_names": ["32x8", "16x16", "64x4"]},
+        "kernels": kern,
+    }
+    out["vs_plain"] = round(out["value"] / out["plain_path_mpix_s"], 3)
+    for s in streams:
+        s.close()
+    ctx.close()
+    return out
+
+
+# ------------------------------------------------------------------------------------------
+# serving: 64 camera streams (720p / 1080p / 1440p drawn uniformly), Poisson frame arrivals
+# ------------------------------------------------------------------------------------------
+SERVE_RES = [(1280, 720), (1920, 1080), (2560, 1440)]
+
+
+def run_serving(args, dist: Dist, dev: int) -> dict:
+    """rgdn_server under per-stream Poisson arrivals (the configured 60 Hz, then lower rates),
+    with history resident and admission under a 120 GB budget. Each request carries device
+    pointers to a frame already resident in HBM (RGDN_REQUEST_BIND; 4 frames per resolution
+    cycle), or, for the e2e run, pinned host G-buffers copied in the step with PRE_FINAL read
+    back to pinned host memory. A stream keeps at most one waiting frame: an older waiting
+    frame is dropped when a newer one arrives. Latency is submission -> completion on the
+    host clock."""
+    import numpy as np
+    import torch
+
+    from raytracedgl1_gb300 import _native as N
+    from raytracedgl1_gb300.denoiser import Context, Server
+    from raytracedgl1_gb300.scene import Scene
+
+    storage = STORAGE["fp16"]
+    ctx = Context(dev, memory_budget_bytes=120 * (1 << 30))
+    rng = np.random.default_rng(7 + dist.rank)
+    res = [SERVE_RES[i] for i in rng.integers(0, len(SERVE_RES), size=64)]
+    frames, host = {}, {}
+    for W, H in SERVE_RES:
+        sc = Scene(W, H, seed=300 + W)
+        fr, hf = [], []
+        for f in range(4):
+            bufs, p = sc.generate(f)
+            p.atrousIterations = args.iters
+            fr.append(({n: torch.from_numpy(np.ascontiguousarray(a).view(np.uint8).reshape(-1)).to(f"cuda:{dev}")
+                        for n, a in bufs.items()}, p))
+            hf.append(({n: torch.from_numpy(np.ascontiguousarray(a).view(np.uint8).reshape(-1)).pin_memory()
+                        for n, a in bufs.items()}, p))
+        frames[(W, H)], host[(W, H)] = fr, hf
+    torch.cuda.synchronize()
+    out_host = {r: torch.empty(r[0] * r[1] * 8, dtype=torch.uint8).pin_memory() for r in SERVE_RES}
+
+    def serve(hz: float, e2e: bool) -> dict:
+        sv = Server(ctx, storage, max_frames_per_step=64, max_pixels_per_step=int(args.serve_step_mpix * 1e6),
+                    max_queued_per_stream=1, steps_in_flight=2)
+        sids = [sv.open_stream(w, h) for w, h in res]
+        reqs = []
+        for i, sid in enumerate(sids):
+            src = host[res[i]] if e2e else frames[res[i]]
+            reqs.append([Server.request(sid, p, {n: t.data_ptr() for n, t in b.items()},
+                                        N.REQUEST_COPY if e2e else N.REQUEST_BIND,
+                                        out_host[res[i]].data_ptr() if e2e else None) for b, p in src])
+        # warm-up: admission of every stream, the autotuner's steps, graph capture
+        for rnd in range(3):
+            ts = [sv.submit(reqs[i][rnd % 4]) for i in range(len(sids))]
+            for t in ts:
+                sv.wait(t)
+        for rnd in range(24):
+            sv.wait(sv.submit(reqs[rnd % len(sids)][rnd % 4]))
+        sv.drain()
+        arrivals = []
+        for i in range(len(sids)):
+            t = rng.exponential(1.0 / hz)
+            while t < args.serve_seconds:
+                arrivals.append((t, i))
+                t += rng.exponential(1.0 / hz)
+        arrivals.sort()
+        sv.reset_stats()
+        count = [0] * len(sids)
+        tickets = []
+        t0 = time.perf_counter()
+        for ta, i in arrivals:
+            while True:
+                dt = ta - (time.perf_counter() - t0)
+                if dt <= 0:
+                    break
+                if dt > 2e-3:
+                    time.sleep(dt - 1e-3)
+            tickets.append(sv.submit(reqs[i][count[i] % 4]))
+            count[i] += 1
+        sv.drain()
+        elapsed = time.perf_counter() - t0
+        st = sv.stats()
+        lat_1080 = []
+        for t, (_, i) in zip(tickets, arrivals):
+            r = sv.wait(t, 0)
+            if r.state == N.FRAME_DONE and res[i] == (1920, 1080):
+                lat_1080.append(r.latencyMs)
+        lat_1080.sort()
+        offered = sum(res[i][0] * res[i][1] for _, i in arrivals)
+        sv.close()
+        return {"per_stream_hz": hz, "seconds": round(elapsed, 3), "requests": len(arrivals),
+                "offered_mpix_s": round(offered / args.serve_seconds / 1e6, 1),
+                "value": round(st["pixelsDone"] / elapsed / 1e6, 1), "unit": "Mpix/s",
+                "frames_done": int(st["framesDone"]), "frames_dropped": int(st["framesDropped"]),
+                "p50_ms": round(st["p50Ms"], 3), "p99_ms": round(st["p99Ms"], 3), "max_ms": round(st["maxMs"], 3),
+                "p99_ms_1080p": round(lat_1080[int(0.99 * (len(lat_1080) - 1))], 3) if lat_1080 else None,
+                "mean_frames_per_step": round(st["meanFramesPerStep"], 2), "steps": int(st["steps"]),
+                "gpu_busy_frac": round(st["busySeconds"] / elapsed, 3),
+                "resident_gb": round(st["residentBytes"] / 1e9, 2)}
+
+    runs = [serve(hz, False) for hz in args.serve_hz]
+    e2e = serve(args.serve_hz[-1], True)
+    ctx.close()
+    return {"workload": "64 camera streams, resolutions drawn uniformly from 1280x720 / 1920x1080 / 2560x1440 "
+                        "(seeded), per-stream Poisson arrivals, fp16 storage, 120 GB admission budget, "
+                        f"{args.iters} a-trous passes; steps bounded to {args.serve_step_mpix} Mpix; "
+                        "at most one waiting frame per stream (older dropped)",
+            "runs": runs, "e2e": e2e}
+
+
+# ------------------------------------------------------------------------------------------
 # our arm
 # ------------------------------------------------------------------------------------------
 def run_ours(args, dist: Dist):
@@ -436,6 +695,11 @@ def run_ours(args, dist: Dist):
 
     st.close()
     ctx.close()
+    del frames
+    torch.cuda.empty_cache()
+    batched = None if args.no_batched else run_batched(args, dist, dev, cs)
+    torch.cuda.empty_cache()
+    serving = None if args.no_serving else run_serving(args, dist, dev)
     if dist.rank != 0:
         return
     line = {
@@ -461,15 +725,102 @@ def run_ours(args, dist: Dist):
         "clocks": clk,
         "cpu_baseline": cpu,
         "gbuffer_bytes_per_frame": int(gbytes_per_frame),
+        "batched": batched,
+        "serving": serving,
     }
     print(json.dumps(line), flush=True)
+
+
+def run_precision(args, dist: Dist):
+    """fp32 / fp16 / bf16 storage against the FP64 oracle on the precision-sweep scene
+    (radiance sigma 2, 1 % fireflies x1000): max-rel and PSNR of PRE_FINAL after every tenth
+    frame and the last, and each stage's algorithmic HBM GB/s per storage mode."""
+    import numpy as np
+
+    import oracle
+    from raytracedgl1_gb300 import build
+    from raytracedgl1_gb300.denoiser import Context, Denoiser, Stream, Tonemapping
+    from raytracedgl1_gb300.scene import Scene
+
+    if dist.rank != 0:
+        return
+    build.build_all()
+    W, H, frames = args.width, args.height, args.frames
+    sc = Scene(W, H, seed=5, sigma=2.0, fireflyProb=0.01, fireflyMult=1000.0)
+    o = oracle.OracleStream(W, H, oracle.MODE_F64)
+    ctx = Context(0)
+    modes = ["fp32", "fp16", "bf16"]
+    gpu = {m: Stream(ctx, W, H, STORAGE[m]) for m in modes}
+    nthreads = os.cpu_count() or 1
+
+    def decode(arr, fmt):
+        if fmt == 13:   # B10G11R11 is not used by these modes
+            raise ValueError(fmt)
+        if fmt in (4, 5, 6):
+            return arr.view(np.float16).astype(np.float64)
+        return arr.astype(np.float64)
+
+    def metrics(x, ref):
+        x, ref = x[..., :3], ref[..., :3]
+        atol = 1e-3 * float(np.percentile(np.abs(ref), 99))
+        d = np.abs(x - ref).max(axis=-1)
+        scale = np.maximum(np.abs(ref).max(axis=-1), atol)
+        mse = float(np.mean((x - ref) ** 2))
+        peak = float(np.abs(ref).max()) or 1.0
+        return {"max_rel": float((d / scale).max()), "psnr_db": round(10 * np.log10(peak * peak / mse), 2) if mse else None}
+
+    report = {m: [] for m in modes}
+    stage_gbs = {}
+    t_oracle = 0.0
+    for f in range(frames):
+        fi = f & 1
+        bufs, p = sc.generate(f)
+        p.atrousIterations = args.iters
+        for k, v in bufs.items():
+            o.load(k, fi, v)
+        t0 = time.perf_counter()
+        o.denoise(fi, p, nthreads)
+        o.calculate_exposure(fi, p, nthreads)
+        t_oracle += time.perf_counter() - t0
+        last = f == frames - 1
+        for m, s in gpu.items():
+            for k, v in bufs.items():
+                s.upload(k, fi, v)
+            s.set_timing(last)
+            Denoiser(s).Denoise(fi, p)
+            Tonemapping(s).CalculateExposure(fi, p)
+            if last:
+                per_px = stage_bytes(m)
+                stage_gbs[m] = {f"{name}[{it}]": round(kernel_bytes(name, it, args.iters, per_px) * W * H / (ms / n / 1e3) / 1e9, 1)
+                                for (name, it), (n, ms) in s.read_timing().items()}
+                s.set_timing(False)
+        if f % 10 == 9 or last:
+            ref = o.plane("PRE_FINAL", fi).astype(np.float64)
+            for m, s in gpu.items():
+                img = s.image("PRE_FINAL", fi)
+                r = metrics(decode(s.download("PRE_FINAL", fi), img.format), ref)
+                r["frame"] = f
+                report[m].append(r)
+            print(f"frame {f}: " + ", ".join(f"{m} {report[m][-1]}" for m in modes), file=sys.stderr, flush=True)
+    line = {"metric": "PRE_FINAL error of each storage mode against the FP64 oracle", "unit": "max-rel / dB",
+            "config": {"workload": f"precision sweep, 1 stream {W}x{H}, {frames} frames, radiance sigma 2, "
+                                   f"1% fireflies x1000, {args.iters} a-trous passes, default (FAST) kernels",
+                       "width": W, "height": H, "frames": frames},
+            "data": "synthetic (seeded analytic scene)", "errors": report, "stage_alg_gbs": stage_gbs,
+            "oracle_seconds_per_frame": round(t_oracle / frames, 2), "oracle_threads": nthreads}
+    print(json.dumps(line), flush=True)
+    for s in gpu.values():
+        s.close()
+    ctx.close()
 
 
 def main():
     args = parse()
     dist = Dist()
     try:
-        if args.impl == "reference":
+        if args.precision_sweep:
+            run_precision(args, dist)
+        elif args.impl == "reference":
             run_reference(args, dist)
         else:
             run_ours(args, dist)

@@ -287,9 +287,123 @@ typedef struct rgdn_job
     const rgdn_frame_params* params;
 } rgdn_job;
 /* rgdn_denoise + rgdn_calculate_exposure for n frames of (possibly) different streams
- * and sizes, with one launch per stage covering all of them. Streams of one batch must
- * be distinct and share one storage mode. */
+ * and sizes, with one launch per stage covering all of them. No reference counterpart: the
+ * reference records one stream's dispatches per call (Denoiser.cpp:64-255).
+ *
+ * Jobs run in order; consecutive default-path jobs (no PLAIN, EXACT_MATH or TMA_STAGING
+ * flag) of one storage mode on distinct streams form a step of up to 64 frames. A step is
+ * one persistent launch per stage (gradient samples, 4 gradient a-trous, temporal
+ * accumulation, anti-firefly, variance, each a-trous iteration, luminance average) whose
+ * blocks loop over the tiles of all its frames; the frames' arguments are copied to the
+ * device at the start of the step. Once the autotuner has settled, a step replays a captured
+ * CUDA graph. Other jobs run as rgdn_denoise + rgdn_calculate_exposure. The results are those
+ * of the single-stream calls, bit for bit. Up to 3 steps are in flight; a fourth waits on the
+ * host for the oldest. */
 rgdn_status rgdn_submit_batch( rgdn_context* ctx, const rgdn_job* jobs, uint32_t n, rgdn_cuda_stream cudaStream );
+
+/* Tile shapes of the batched kernels (256 threads per block). */
+#define RGDN_TILE_32X8  0u
+#define RGDN_TILE_16X16 1u
+#define RGDN_TILE_64X4  2u
+/* The launch configuration of batched steps for one storage mode. The autotuner starts from
+ * 32x8 tiles everywhere and, over the first steps, times every candidate of every launch
+ * on the work being submitted (candidates give identical results), then keeps the fastest
+ * and switches to graph replay. */
+typedef struct rgdn_batch_config
+{
+    uint32_t temporalTile;        /* RGDN_TILE_* */
+    uint32_t antiFireflyTile;
+    uint32_t varianceTile;
+    uint32_t atrousTile[ 6 ];     /* per a-trous iteration */
+    uint32_t atrousTwoBlocks[ 6 ];/* 1: the a-trous kernel built for 2 resident blocks per SM
+                                     (more registers per thread) instead of 3 */
+    uint32_t useGraphs;           /* replay a captured graph per step (off while timing) */
+    uint32_t tuned;               /* read: the autotuner has settled (set_config settles it) */
+} rgdn_batch_config;
+rgdn_status rgdn_batch_get_config( rgdn_context* ctx, uint32_t storage, rgdn_batch_config* outConfig );
+/* Fixes the configuration of a storage mode and ends its autotuning. */
+rgdn_status rgdn_batch_set_config( rgdn_context* ctx, uint32_t storage, const rgdn_batch_config* config );
+
+/* ---- serving ---------------------------------------------------------------------------- */
+/* No reference counterpart (the reference renders one camera per process). A request loop
+ * that denoises frames of many camera streams with continuous batching: a frame submitted
+ * while earlier steps run on the GPU joins the next step, which is enqueued at once, so steps
+ * follow each other on the device without a gap (and overlap, on two CUDA streams, when no
+ * camera stream is in both). Each stream's history stays resident. A stream's memory is
+ * allocated when its first frame is scheduled and the context's budget
+ * (rgdn_context_create_info.memoryBudgetBytes) admits it; until then its frames wait.
+ * A step takes the oldest frame of each of up to maxFramesPerStep streams, in arrival
+ * order, while the step's pixels stay within maxPixelsPerStep. The frames of one stream run
+ * in submission order, one per step. Results are those of rgdn_denoise +
+ * rgdn_calculate_exposure on the stream alone, bit for bit. */
+typedef struct rgdn_server rgdn_server;
+typedef struct rgdn_server_create_info
+{
+    uint32_t storage;            /* rgdn_storage of every stream of the server */
+    uint32_t maxFramesPerStep;   /* 1..64 (0 = 64) */
+    uint64_t maxPixelsPerStep;   /* bound on one step's work, i.e. its latency (0 = none) */
+    uint32_t maxQueuedPerStream; /* a stream's frames waiting beyond this many are dropped,
+                                    oldest first (a late frame is stale); 0 = keep all */
+    uint32_t stepsInFlight;      /* steps enqueued ahead of the GPU: 1..3 (0 = 2) */
+    uint32_t evictIdleMs;        /* a stream idle this long may lose its memory (and history)
+                                    to admit another; 0 = never evict */
+} rgdn_server_create_info;
+
+/* G-buffer source of a request: planes RGDN_FB_ALBEDO .. RGDN_FB_GRADIENT_RESHADED */
+#define RGDN_GBUFFER_PLANES 15
+#define RGDN_REQUEST_COPY 0u   /* gbuffer[] are host (pinned or pageable) or device pointers; copied
+                                  into the stream's planes inside the step */
+#define RGDN_REQUEST_BIND 1u   /* gbuffer[] are device pointers used in place (no copy); they must
+                                  stay valid until the frame completes */
+typedef struct rgdn_frame_request
+{
+    uint32_t          stream;                           /* id from rgdn_server_open_stream */
+    uint32_t          gbufferMode;                      /* RGDN_REQUEST_* */
+    const void*       gbuffer[ RGDN_GBUFFER_PLANES ];   /* dense rows; NULL keeps the plane */
+    void*             preFinalOut;                      /* optional destination of PRE_FINAL
+                                                           (host or device, dense rows) */
+    rgdn_frame_params params;
+} rgdn_frame_request;
+
+/* rgdn_server_wait result states */
+#define RGDN_FRAME_DONE    0u
+#define RGDN_FRAME_DROPPED 1u   /* superseded by newer frames of the stream (maxQueuedPerStream) */
+typedef struct rgdn_frame_result
+{
+    uint32_t state;          /* RGDN_FRAME_* */
+    uint32_t frameIndex;     /* the stream's frame slot the frame ran in */
+    float    latencyMs;      /* submission to completion seen by the host */
+    float    queueMs;        /* submission to the step's enqueue */
+} rgdn_frame_result;
+
+typedef struct rgdn_server_stats
+{
+    uint64_t framesDone, framesDropped, steps, pixelsDone;
+    uint32_t residentStreams, queuedFrames;
+    uint64_t residentBytes;
+    float    p50Ms, p99Ms, maxMs;     /* latency of the frames done since the last reset */
+    float    meanFramesPerStep;
+    double   busySeconds;             /* wall time with at least one step on the GPU */
+} rgdn_server_stats;
+
+rgdn_status rgdn_server_create( rgdn_context* ctx, const rgdn_server_create_info* info, rgdn_server** outServer );
+/* Completes every submitted frame, then frees the server's streams. */
+rgdn_status rgdn_server_destroy( rgdn_server* server );
+rgdn_status rgdn_server_open_stream( rgdn_server* server, uint32_t width, uint32_t height, uint32_t* outStreamId );
+/* Waits for the stream's frames, then frees its memory. */
+rgdn_status rgdn_server_close_stream( rgdn_server* server, uint32_t streamId );
+/* Queues one frame; thread-safe. The request's buffers must stay valid until it completes. */
+rgdn_status rgdn_server_submit( rgdn_server* server, const rgdn_frame_request* request, uint64_t* outTicket );
+/* Waits up to timeoutMs (0 = poll) for a ticket: RGDN_SUCCESS with the result (the ticket is
+ * then released), RGDN_TIMEOUT, or RGDN_WRONG_FUNCTION_ARGUMENT for an unknown ticket. */
+rgdn_status rgdn_server_wait( rgdn_server* server, uint64_t ticket, uint32_t timeoutMs, rgdn_frame_result* outResult );
+/* Blocks until every frame submitted so far has completed or been dropped. */
+rgdn_status rgdn_server_drain( rgdn_server* server );
+rgdn_status rgdn_server_stats_get( rgdn_server* server, rgdn_server_stats* outStats );
+rgdn_status rgdn_server_stats_reset( rgdn_server* server );
+/* The stream behind an id (NULL until admitted), for reading its images and tonemapping state
+ * between frames. */
+rgdn_status rgdn_server_get_stream( rgdn_server* server, uint32_t streamId, rgdn_stream** outStream );
 
 /* ---- without device allocation ----------------------------------------------------------- */
 /* No counterpart in the reference. The four gradient a-trous iterations
@@ -322,6 +436,10 @@ typedef struct rgdn_stage_timing
 } rgdn_stage_timing;
 rgdn_status rgdn_stream_set_timing( rgdn_stream* stream, uint32_t enable );
 rgdn_status rgdn_stream_read_timing( rgdn_stream* stream, rgdn_stage_timing* out, uint32_t capacity, uint32_t* outCount );
+/* Per-launch device timing of batched steps (as rgdn_stream_set_timing; stage ids are
+ * rgdn_stage, totals per (stage, iteration)). Timed steps use direct launches, not graphs. */
+rgdn_status rgdn_batch_set_timing( rgdn_context* ctx, uint32_t enable );
+rgdn_status rgdn_batch_read_timing( rgdn_context* ctx, rgdn_stage_timing* out, uint32_t capacity, uint32_t* outCount );
 
 /* ---- misc -------------------------------------------------------------------------- */
 /* getColorBin (CmLuminanceHistogram.comp:41-54) for every fp16 bit pattern of the

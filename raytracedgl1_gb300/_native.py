@@ -87,6 +87,41 @@ class StageTiming(C.Structure):
                 ("totalMs", C.c_float)]
 
 
+class BatchConfig(C.Structure):
+    """rgdn_batch_config: launch configuration of batched steps for one storage mode."""
+    _fields_ = [("temporalTile", C.c_uint32), ("antiFireflyTile", C.c_uint32),
+                ("varianceTile", C.c_uint32), ("atrousTile", C.c_uint32 * 6),
+                ("atrousTwoBlocks", C.c_uint32 * 6), ("useGraphs", C.c_uint32), ("tuned", C.c_uint32)]
+
+
+TILE_32X8, TILE_16X16, TILE_64X4 = 0, 1, 2
+
+GBUFFER_PLANES = 15
+REQUEST_COPY, REQUEST_BIND = 0, 1
+FRAME_DONE, FRAME_DROPPED = 0, 1
+
+
+class ServerCreateInfo(C.Structure):
+    _fields_ = [("storage", C.c_uint32), ("maxFramesPerStep", C.c_uint32), ("maxPixelsPerStep", C.c_uint64),
+                ("maxQueuedPerStream", C.c_uint32), ("stepsInFlight", C.c_uint32), ("evictIdleMs", C.c_uint32)]
+
+
+class FrameRequest(C.Structure):
+    _fields_ = [("stream", C.c_uint32), ("gbufferMode", C.c_uint32), ("gbuffer", C.c_void_p * 15),
+                ("preFinalOut", C.c_void_p), ("params", FrameParams)]
+
+
+class FrameResult(C.Structure):
+    _fields_ = [("state", C.c_uint32), ("frameIndex", C.c_uint32), ("latencyMs", C.c_float), ("queueMs", C.c_float)]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [("framesDone", C.c_uint64), ("framesDropped", C.c_uint64), ("steps", C.c_uint64),
+                ("pixelsDone", C.c_uint64), ("residentStreams", C.c_uint32), ("queuedFrames", C.c_uint32),
+                ("residentBytes", C.c_uint64), ("p50Ms", C.c_float), ("p99Ms", C.c_float), ("maxMs", C.c_float),
+                ("meanFramesPerStep", C.c_float), ("busySeconds", C.c_double)]
+
+
 class Job(C.Structure):
     _fields_ = [("stream", C.c_void_p), ("frameIndex", C.c_uint32), ("params", C.POINTER(FrameParams))]
 
@@ -120,6 +155,20 @@ SIGNATURES = [
     ("rgdn_gradient_atrous_noalloc", _I, [_VP, _VP, _VP, _U32, _U32, _VP]),
     ("rgdn_stream_set_timing", _I, [_VP, _U32]),
     ("rgdn_stream_read_timing", _I, [_VP, C.POINTER(StageTiming), _U32, C.POINTER(_U32)]),
+    ("rgdn_batch_get_config", _I, [_VP, _U32, C.POINTER(BatchConfig)]),
+    ("rgdn_batch_set_config", _I, [_VP, _U32, C.POINTER(BatchConfig)]),
+    ("rgdn_batch_set_timing", _I, [_VP, _U32]),
+    ("rgdn_batch_read_timing", _I, [_VP, C.POINTER(StageTiming), _U32, C.POINTER(_U32)]),
+    ("rgdn_server_create", _I, [_VP, C.POINTER(ServerCreateInfo), C.POINTER(_VP)]),
+    ("rgdn_server_destroy", _I, [_VP]),
+    ("rgdn_server_open_stream", _I, [_VP, _U32, _U32, C.POINTER(_U32)]),
+    ("rgdn_server_close_stream", _I, [_VP, _U32]),
+    ("rgdn_server_submit", _I, [_VP, C.POINTER(FrameRequest), C.POINTER(_U64)]),
+    ("rgdn_server_wait", _I, [_VP, _U64, _U32, C.POINTER(FrameResult)]),
+    ("rgdn_server_drain", _I, [_VP]),
+    ("rgdn_server_stats_get", _I, [_VP, C.POINTER(ServerStats)]),
+    ("rgdn_server_stats_reset", _I, [_VP]),
+    ("rgdn_server_get_stream", _I, [_VP, _U32, C.POINTER(_VP)]),
 ]
 
 STAGE_NAMES = ["gradient_samples", "gradient_atrous", "temporal_accumulation", "anti_firefly",

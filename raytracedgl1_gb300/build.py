@@ -30,11 +30,11 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-lineinfo", "-O3", "--fmad=false", "-std=c++17", "-Xcompiler", "-fPIC",
                      "-Xcompiler", "-O3", "-I" + INCLUDE, "-I" + CSRC]
 CU_SOURCES = ["rgdn_api.cu", "rgdn_mode_ref.cu", "rgdn_mode_f32.cu", "rgdn_mode_f16.cu",
-              "rgdn_mode_bf16.cu", "rgdn_noalloc.cu", "rgdn_fast_ref.cu", "rgdn_fast_f32.cu",
+              "rgdn_mode_bf16.cu", "rgdn_noalloc.cu", "rgdn_batch.cu", "rgdn_serve.cu", "rgdn_fast_ref.cu", "rgdn_fast_f32.cu",
               "rgdn_fast_f16.cu", "rgdn_fast_bf16.cu"]
 # the FAST kernels carry no threshold decisions: contraction to fused multiply-add allowed
 FMAD_TRUE = {"rgdn_fast_ref.cu", "rgdn_fast_f32.cu", "rgdn_fast_f16.cu", "rgdn_fast_bf16.cu"}
-HEADERS = ["rgdn_internal.h", "rgdn_kernels.cuh", "rgdn_codec.h"]
+HEADERS = ["rgdn_internal.h", "rgdn_kernels.cuh", "rgdn_codec.h", "rgdn_host.h"]
 
 LIB_RGDN = os.path.join(LIBDIR, "librgdn.so")
 LIB_SCENE = os.path.join(LIBDIR, "librgdn_scene.so")

@@ -22,7 +22,7 @@
 #include <tuple>
 
 #include "rgdn_codec.h"
-#include "rgdn_internal.h"
+#include "rgdn_host.h"
 
 using namespace rgdn;
 
@@ -170,65 +170,9 @@ void build_bin_lut( uint8_t* lut, float minLog, float maxLog )
 
 }  // namespace
 
-// ------------------------------------------------------------------------------------------
-// handles
-// ------------------------------------------------------------------------------------------
-struct rgdn_context
-{
-    int                     device = 0;
-    uint64_t                budget = 0;
-    uint64_t                used   = 0;
-    std::mutex              mtx;
-    std::set< rgdn_stream* > streams;
-    float2*                 phiTab   = nullptr;   // (sin phi_j, cos phi_j)
-    float2*                 thetaTab = nullptr;   // (cos theta_k, sin theta_k)
-    std::atomic< uint64_t > launches{ 0 };
-    uint32_t                magic = 0x52474443u;
-};
-
-struct PlaneSlot
-{
-    uint8_t* ptr[ 2 ] = { nullptr, nullptr };   // in use (own plane or a bound caller plane)
-    uint8_t* own[ 2 ] = { nullptr, nullptr };   // the stream's own planes
-    uint32_t w = 0, h = 0, texel = 0, format = 0;
-    bool     prev = false;
-};
-
-struct rgdn_stream
-{
-    rgdn_context*          ctx = nullptr;
-    uint32_t               W = 0, H = 0, GW = 0, GH = 0, storage = 0;
-    void*                  block = nullptr;
-    size_t                 bytes = 0;
-    PlaneSlot              planes[ RGDN_FB_COUNT ];
-    Tonemapping*           tm     = nullptr;
-    uint8_t*               binLut = nullptr;
-    float4*                geom[ 2 ] = { nullptr, nullptr };
-    bool                   geomValid[ 2 ] = { false, false };   // slot holds its frame's record
-    float                  lutMin = NAN, lutMax = NAN;
-    std::vector< uint8_t > hostLut;
-    // per-kernel timing
-    struct Pending
-    {
-        int         stage, iter;
-        cudaEvent_t a, b;
-    };
-    bool                        timing = false;
-    bool                        histPending = false;   // a fused denoise accumulated this frame's histogram
-    // tensor maps of the TMA-staged a-trous, keyed by (plane, texel words, box width, box height)
-    std::map< std::tuple< const void*, int, int, int >, CUtensorMap > tmaps;
-    std::vector< Pending >      pending;
-    std::vector< cudaEvent_t >  eventPool;
-    uint32_t                    magic = 0x52474453u;
-};
-
-namespace
+namespace rgdn
 {
 
-bool valid_ctx( rgdn_context* c ) { return c && c->magic == 0x52474443u; }
-bool valid_stream( rgdn_stream* s ) { return s && s->magic == 0x52474453u && valid_ctx( s->ctx ); }
-
-rgdn_status cuda_status( cudaError_t e ) { return e == cudaSuccess ? RGDN_SUCCESS : RGDN_DEVICE_ERROR; }
 
 // bytes of one stream's single device block
 size_t stream_layout( uint32_t W, uint32_t H, uint32_t storage, PlaneSlot* planes, uint8_t* base )
@@ -582,7 +526,7 @@ rgdn_status run_exposure( rgdn_stream* s, uint32_t fi, const rgdn_frame_params* 
     return launch( s, a, RGDN_STAGE_LUMINANCE_AVG, 0, cs );
 }
 
-}  // namespace
+}  // namespace rgdn
 
 // ==========================================================================================
 extern "C" {
@@ -657,6 +601,7 @@ rgdn_status rgdn_context_destroy( rgdn_context* c )
         std::lock_guard< std::mutex > g( c->mtx );
         left.assign( c->streams.begin(), c->streams.end() );
     }
+    batch_destroy( c );
     for( rgdn_stream* s : left ) rgdn_stream_destroy( s );
     cudaFree( c->phiTab );
     cudaFree( c->thetaTab );
@@ -975,14 +920,40 @@ rgdn_status rgdn_submit_batch( rgdn_context* c, const rgdn_job* jobs, uint32_t n
         rgdn_status r = check_params( jobs[ j ].params );
         if( r != RGDN_SUCCESS ) return r;
     }
+    if( n == 0 ) return RGDN_SUCCESS;
     cudaSetDevice( c->device );
-    for( uint32_t j = 0; j < n; j++ )
-    {
-        rgdn_status r = run_denoise( jobs[ j ].stream, jobs[ j ].frameIndex, jobs[ j ].params, (cudaStream_t)cs );
-        if( r == RGDN_SUCCESS ) r = run_exposure( jobs[ j ].stream, jobs[ j ].frameIndex, jobs[ j ].params, (cudaStream_t)cs );
-        if( r != RGDN_SUCCESS ) return r;
-    }
-    return RGDN_SUCCESS;
+    return batch_submit( c, jobs, n, (cudaStream_t)cs );
+}
+
+rgdn_status rgdn_batch_get_config( rgdn_context* c, uint32_t storage, rgdn_batch_config* out )
+{
+    if( !valid_ctx( c ) ) return RGDN_WRONG_INSTANCE;
+    if( !out || storage > RGDN_STORAGE_BF16 ) return RGDN_WRONG_FUNCTION_ARGUMENT;
+    cudaSetDevice( c->device );
+    return batch_get_config( c, storage, out );
+}
+
+rgdn_status rgdn_batch_set_config( rgdn_context* c, uint32_t storage, const rgdn_batch_config* in )
+{
+    if( !valid_ctx( c ) ) return RGDN_WRONG_INSTANCE;
+    if( !in || storage > RGDN_STORAGE_BF16 ) return RGDN_WRONG_FUNCTION_ARGUMENT;
+    cudaSetDevice( c->device );
+    return batch_set_config( c, storage, in );
+}
+
+rgdn_status rgdn_batch_set_timing( rgdn_context* c, uint32_t enable )
+{
+    if( !valid_ctx( c ) ) return RGDN_WRONG_INSTANCE;
+    cudaSetDevice( c->device );
+    return batch_set_timing( c, enable != 0 );
+}
+
+rgdn_status rgdn_batch_read_timing( rgdn_context* c, rgdn_stage_timing* out, uint32_t capacity, uint32_t* outCount )
+{
+    if( !valid_ctx( c ) ) return RGDN_WRONG_INSTANCE;
+    if( !outCount || ( capacity && !out ) ) return RGDN_WRONG_FUNCTION_ARGUMENT;
+    cudaSetDevice( c->device );
+    return batch_read_timing( c, out, capacity, outCount );
 }
 
 }  // extern "C"

@@ -1,0 +1,606 @@
+// Batch executor behind rgdn_submit_batch: many streams' frames of uneven size advance one
+// frame each in one step, with one persistent launch per stage.
+//
+// The reference denoises one camera stream per call (Denoiser::Denoise, Source/Denoiser.cpp:
+// 64-255, then Tonemapping::CalculateExposure, Source/Tonemapping.cpp:59-165); a step here runs
+// the same stages in the same order for up to MAX_BATCH frames:
+//
+//   H2D copy of the step table (BatchSched + FrameArgs of every frame, pinned -> device)
+//   gradient samples, gradient a-trous 0..3        (frames with gradients)
+//   temporal accumulation, anti-firefly, variance  (every frame)
+//   a-trous 0 .. max(niter)-1                      (frames with niter > i; a frame's last
+//                                                   iteration composes and bins its histogram)
+//   luminance average                              (every frame)
+//
+// Every launch has a fixed grid (resident blocks per SM x SMs) and reads its tile table from
+// the step table, so the captured graph of a step is valid for any set of frames with the same
+// launch sequence; a step then costs one H2D copy and one graph launch. The host keeps up to
+// kSlots steps in flight, each with its own pinned table, device table and graph.
+//
+// Autotuning: the first steps of a storage mode time every candidate tile shape (and, for the
+// a-trous kernel, both register budgets) per launch on the frames being submitted. Candidates
+// compute identical values per pixel, so tuning changes no result. Then the fastest candidate
+// per launch is kept and steps switch to graph replay.
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
+#include "rgdn_host.h"
+
+namespace rgdn
+{
+namespace
+{
+
+constexpr int kSlots      = 3;
+constexpr int kTuneRounds = 3;
+const dim3    kShapes[ 3 ] = { dim3( 32, 8 ), dim3( 16, 16 ), dim3( 64, 4 ) };
+
+size_t sched_bytes() { return ( sizeof( BatchSched ) + 255 ) & ~size_t( 255 ); }
+size_t table_bytes( int n ) { return sched_bytes() + sizeof( FrameArgs ) * (size_t)n; }
+
+// the launch sequence of a step: what a captured graph depends on
+struct GraphKey
+{
+    int storage, anyGrad, maxIter;
+    int hm[ MAX_ATROUS_ITERATIONS ];
+    int shape[ BS_COUNT ];
+    int two[ BS_COUNT ];
+};
+bool same_key( const GraphKey& a, const GraphKey& b ) { return memcmp( &a, &b, sizeof( GraphKey ) ) == 0; }
+
+struct Slot
+{
+    uint8_t*        host     = nullptr;   // pinned step table
+    uint8_t*        dev      = nullptr;   // device step table
+    cudaEvent_t     done     = nullptr;   // recorded after the step's last launch
+    bool            inFlight = false;
+    cudaGraphExec_t exec     = nullptr;
+    GraphKey        key;
+};
+
+struct Config
+{
+    int  shape[ BS_COUNT ];   // index into kShapes (BS_GRADIENT stays 32x8)
+    int  two[ BS_COUNT ];     // a-trous kinds: 1 = the 2-blocks-per-SM kernel
+    bool graphs;
+};
+
+struct Probe
+{
+    int         kind, cand;
+    double      pixels;
+    cudaEvent_t a, b;
+};
+
+struct Tuner
+{
+    bool                 settled = false;
+    int                  step    = 0;
+    std::vector< Probe > probes;
+};
+
+int n_candidates( int kind ) { return kind >= BS_ATROUS0 ? 6 : kind == BS_GRADIENT ? 1 : 3; }
+int max_candidates() { return 6; }
+void candidate( int kind, int c, int& shape, int& two )
+{
+    shape = kind == BS_GRADIENT ? 0 : c % 3;
+    two   = kind >= BS_ATROUS0 ? c / 3 : 0;
+}
+
+struct Pending
+{
+    int         stage, iter;
+    cudaEvent_t a, b;
+};
+
+typedef cudaError_t ( *BatchLauncher )( int, int, const BatchSched*, const FrameArgs*, dim3, int, cudaStream_t );
+typedef int ( *BpsFn )( int );
+
+BatchLauncher batch_launcher( uint32_t storage, int stage )
+{
+    const bool fast = is_batch_fast_stage( stage );
+    switch( storage )
+    {
+        case RGDN_STORAGE_REF: return fast ? launch_batch_fast_ref : launch_batch_ref;
+        case RGDN_STORAGE_FP32: return fast ? launch_batch_fast_f32 : launch_batch_f32;
+        case RGDN_STORAGE_FP16: return fast ? launch_batch_fast_f16 : launch_batch_f16;
+        case RGDN_STORAGE_BF16: return fast ? launch_batch_fast_bf16 : launch_batch_bf16;
+        default: return nullptr;
+    }
+}
+BpsFn bps_fn( uint32_t storage, int stage )
+{
+    const bool fast = is_batch_fast_stage( stage );
+    switch( storage )
+    {
+        case RGDN_STORAGE_REF: return fast ? batch_blocks_per_sm_fast_ref : batch_blocks_per_sm_ref;
+        case RGDN_STORAGE_FP32: return fast ? batch_blocks_per_sm_fast_f32 : batch_blocks_per_sm_f32;
+        case RGDN_STORAGE_FP16: return fast ? batch_blocks_per_sm_fast_f16 : batch_blocks_per_sm_f16;
+        case RGDN_STORAGE_BF16: return fast ? batch_blocks_per_sm_fast_bf16 : batch_blocks_per_sm_bf16;
+        default: return nullptr;
+    }
+}
+
+int ceil_div( int a, int b ) { return ( a + b - 1 ) / b; }
+
+}  // namespace
+
+struct BatchExec
+{
+    int                        sms     = 0;
+    cudaStream_t               capture = nullptr;   // private stream the graphs are captured on
+    Slot                       slot[ kSlots ];
+    int                        next = 0;
+    Config                     cfg[ 4 ];
+    Tuner                      tuner[ 4 ];
+    int                        bps[ 4 ][ RGDN_STAGE_COUNT ][ 2 ];   // resident blocks per SM, -1 = unknown
+    bool                       timing = false;
+    std::vector< Pending >     pending;
+    std::vector< cudaEvent_t > eventPool;
+};
+
+namespace
+{
+
+cudaEvent_t take_event( BatchExec& ex )
+{
+    if( !ex.eventPool.empty() )
+    {
+        cudaEvent_t e = ex.eventPool.back();
+        ex.eventPool.pop_back();
+        return e;
+    }
+    cudaEvent_t e = nullptr;
+    return cudaEventCreate( &e ) == cudaSuccess ? e : nullptr;
+}
+
+int blocks_per_sm( BatchExec& ex, uint32_t storage, int stage, int two )
+{
+    int& v = ex.bps[ storage ][ stage ][ two ];
+    if( v < 0 )
+    {
+        BpsFn f = bps_fn( storage, stage );
+        v       = f ? f( stage | ( two ? 0x400 : 0 ) ) : 0;
+    }
+    return v;
+}
+
+BatchExec* create_exec( int device )
+{
+    BatchExec* ex = new( std::nothrow ) BatchExec();
+    if( !ex ) return nullptr;
+    bool ok = cudaDeviceGetAttribute( &ex->sms, cudaDevAttrMultiProcessorCount, device ) == cudaSuccess && ex->sms > 0;
+    ok      = ok && cudaStreamCreateWithFlags( &ex->capture, cudaStreamNonBlocking ) == cudaSuccess;
+    for( int i = 0; ok && i < kSlots; i++ )
+    {
+        ok = cudaMallocHost( &ex->slot[ i ].host, table_bytes( MAX_BATCH ) ) == cudaSuccess &&
+             cudaMalloc( &ex->slot[ i ].dev, table_bytes( MAX_BATCH ) ) == cudaSuccess &&
+             cudaEventCreateWithFlags( &ex->slot[ i ].done, cudaEventDisableTiming ) == cudaSuccess;
+        if( ok ) memset( ex->slot[ i ].host, 0, table_bytes( MAX_BATCH ) );
+    }
+    for( int s = 0; s < 4; s++ )
+    {
+        for( int k = 0; k < BS_COUNT; k++ ) ex->cfg[ s ].shape[ k ] = ex->cfg[ s ].two[ k ] = 0;
+        ex->cfg[ s ].graphs = true;
+        for( int st = 0; st < RGDN_STAGE_COUNT; st++ ) ex->bps[ s ][ st ][ 0 ] = ex->bps[ s ][ st ][ 1 ] = -1;
+    }
+    if( !ok )
+    {
+        batch_exec_free( ex );
+        return nullptr;
+    }
+    return ex;
+}
+
+}  // namespace
+
+void batch_exec_free( BatchExec* ex )
+{
+    if( !ex ) return;
+    for( int i = 0; i < kSlots; i++ )
+    {
+        Slot& s = ex->slot[ i ];
+        if( s.inFlight ) cudaEventSynchronize( s.done );
+        if( s.exec ) cudaGraphExecDestroy( s.exec );
+        if( s.done ) cudaEventDestroy( s.done );
+        if( s.host ) cudaFreeHost( s.host );
+        if( s.dev ) cudaFree( s.dev );
+    }
+    for( auto& t : ex->tuner )
+        for( auto& p : t.probes )
+        {
+            cudaEventSynchronize( p.b );
+            cudaEventDestroy( p.a );
+            cudaEventDestroy( p.b );
+        }
+    for( auto& p : ex->pending )
+    {
+        cudaEventSynchronize( p.b );
+        cudaEventDestroy( p.a );
+        cudaEventDestroy( p.b );
+    }
+    for( cudaEvent_t e : ex->eventPool ) cudaEventDestroy( e );
+    if( ex->capture ) cudaStreamDestroy( ex->capture );
+    delete ex;
+}
+
+namespace
+{
+
+// Enqueues the step's copy and launches on `cs`. `timed`: events around every launch, into
+// the tuner's probes (tuning) and the user's timing list (ex.timing).
+rgdn_status enqueue_step( rgdn_context* c, BatchExec& ex, const Slot& sl, const GraphKey& key, int n, const double* pixels,
+                          int tuneCand, cudaStream_t cs, bool capturing )
+{
+    const uint32_t    st    = (uint32_t)key.storage;
+    const BatchSched* dsch  = reinterpret_cast< const BatchSched* >( sl.dev );
+    const FrameArgs*  djobs = reinterpret_cast< const FrameArgs* >( sl.dev + sched_bytes() );
+    // a graph copies the whole table (its node is fixed); a direct step only its n frames
+    if( cudaMemcpyAsync( sl.dev, sl.host, capturing ? table_bytes( MAX_BATCH ) : table_bytes( n ), cudaMemcpyHostToDevice, cs ) != cudaSuccess )
+        return RGDN_DEVICE_ERROR;
+    Tuner&     tu     = ex.tuner[ st ];
+    const bool tuning = !capturing && !tu.settled;
+    const bool user   = !capturing && ex.timing;
+
+    auto run = [ & ]( int kind, int stage, int iter, int shape, int two, int cand ) -> rgdn_status {
+        BatchLauncher L = batch_launcher( st, stage );
+        if( !L ) return RGDN_INTERNAL_ERROR;
+        const int bps  = stage == RGDN_STAGE_LUMINANCE_AVG ? 0 : blocks_per_sm( ex, st, stage, two );
+        const int grid = stage == RGDN_STAGE_LUMINANCE_AVG ? MAX_BATCH : bps * ex.sms;
+        if( grid <= 0 ) return RGDN_DEVICE_ERROR;
+        cudaEvent_t ta = nullptr, tb = nullptr, ua = nullptr, ub = nullptr;
+        if( tuning && kind >= 0 )
+        {
+            ta = take_event( ex );
+            tb = take_event( ex );
+            if( !ta || !tb ) return RGDN_DEVICE_ERROR;
+            cudaEventRecord( ta, cs );
+        }
+        if( user )
+        {
+            ua = take_event( ex );
+            ub = take_event( ex );
+            if( !ua || !ub ) return RGDN_DEVICE_ERROR;
+            cudaEventRecord( ua, cs );
+        }
+        int arg = iter;
+        if( stage == RGDN_STAGE_ATROUS ) arg |= ( key.hm[ iter ] << 8 ) | ( two << 10 );
+        const cudaError_t e = L( stage, arg, dsch, djobs, kShapes[ shape ], grid, cs );
+        if( user )
+        {
+            cudaEventRecord( ub, cs );
+            ex.pending.push_back( { stage, iter, ua, ub } );
+        }
+        if( ta )
+        {
+            cudaEventRecord( tb, cs );
+            tu.probes.push_back( { kind, cand, pixels[ kind ], ta, tb } );
+        }
+        if( !capturing ) c->launches.fetch_add( 1, std::memory_order_relaxed );
+        return cuda_status( e );
+    };
+
+    rgdn_status r;
+    if( key.anyGrad )
+    {
+        if( ( r = run( -1, RGDN_STAGE_GRADIENT_SAMPLES, 0, 0, 0, 0 ) ) != RGDN_SUCCESS ) return r;
+        for( int i = 0; i < 4; i++ )
+            if( ( r = run( -1, RGDN_STAGE_GRADIENT_ATROUS, i, 0, 0, 0 ) ) != RGDN_SUCCESS ) return r;
+    }
+    const int stages[ 3 ] = { RGDN_STAGE_TEMPORAL_ACCUMULATION, RGDN_STAGE_ANTI_FIREFLY, RGDN_STAGE_VARIANCE_ESTIMATION };
+    for( int k = 0; k < 3; k++ )
+    {
+        const int kind = BS_TEMPORAL + k;
+        if( ( r = run( kind, stages[ k ], 0, key.shape[ kind ], 0, tuneCand % n_candidates( kind ) ) ) != RGDN_SUCCESS ) return r;
+    }
+    for( int i = 0; i < key.maxIter; i++ )
+    {
+        const int kind = BS_ATROUS0 + i;
+        if( ( r = run( kind, RGDN_STAGE_ATROUS, i, key.shape[ kind ], key.two[ kind ], tuneCand % n_candidates( kind ) ) ) != RGDN_SUCCESS )
+            return r;
+    }
+    return run( -1, RGDN_STAGE_LUMINANCE_AVG, 0, 0, 0, 0 );
+}
+
+int kernels_in( const GraphKey& key ) { return ( key.anyGrad ? 5 : 0 ) + 3 + key.maxIter + 1; }
+
+// Picks the fastest candidate of every launch kind from the tuning steps' probes.
+rgdn_status settle( BatchExec& ex, uint32_t st )
+{
+    Tuner& tu = ex.tuner[ st ];
+    std::vector< double > best( BS_COUNT * max_candidates(), 1e30 );
+    rgdn_status r = RGDN_SUCCESS;
+    for( auto& p : tu.probes )
+    {
+        float ms = 0.0f;
+        if( cudaEventSynchronize( p.b ) != cudaSuccess || cudaEventElapsedTime( &ms, p.a, p.b ) != cudaSuccess ) r = RGDN_DEVICE_ERROR;
+        else if( p.pixels > 0.0 )
+        {
+            double& b = best[ p.kind * max_candidates() + p.cand ];
+            b         = std::min( b, (double)ms / p.pixels );
+        }
+        ex.eventPool.push_back( p.a );
+        ex.eventPool.push_back( p.b );
+    }
+    tu.probes.clear();
+    for( int kind = BS_TEMPORAL; kind < BS_COUNT; kind++ )
+    {
+        int bestC = 0;
+        for( int cnd = 1; cnd < n_candidates( kind ); cnd++ )
+            if( best[ kind * max_candidates() + cnd ] < best[ kind * max_candidates() + bestC ] ) bestC = cnd;
+        // kinds no tuning step ran (more iterations later) keep their configuration
+        if( best[ kind * max_candidates() + bestC ] >= 1e30 ) continue;
+        candidate( kind, bestC, ex.cfg[ st ].shape[ kind ], ex.cfg[ st ].two[ kind ] );
+    }
+    tu.settled = true;
+    return r;
+}
+
+bool batchable( const rgdn_job& j )
+{
+    return !( j.params->flags & ( RGDN_FLAG_PLAIN | RGDN_FLAG_EXACT_MATH | RGDN_FLAG_TMA_STAGING ) );
+}
+
+// One step over jobs[0..n) (distinct streams, one storage mode, all batchable).
+rgdn_status run_step( rgdn_context* c, BatchExec& ex, const rgdn_job* jobs, int n, cudaStream_t cs )
+{
+    const uint32_t st = jobs[ 0 ].stream->storage;
+    Slot&          sl = ex.slot[ ex.next ];
+    ex.next           = ( ex.next + 1 ) % kSlots;
+    if( sl.inFlight )
+    {
+        // the slot's previous step must have read its table before the host rewrites it
+        if( cudaEventSynchronize( sl.done ) != cudaSuccess ) return RGDN_DEVICE_ERROR;
+        sl.inFlight = false;
+    }
+    Tuner&       tu     = ex.tuner[ st ];
+    const bool   tuning = !tu.settled;
+    const int    tcand  = tu.step;
+    Config       cfg    = ex.cfg[ st ];
+    if( tuning )
+        for( int kind = BS_TEMPORAL; kind < BS_COUNT; kind++ ) candidate( kind, tcand % n_candidates( kind ), cfg.shape[ kind ], cfg.two[ kind ] );
+
+    BatchSched* sch = reinterpret_cast< BatchSched* >( sl.host );
+    FrameArgs*  fa  = reinterpret_cast< FrameArgs* >( sl.host + sched_bytes() );
+    memset( sch, 0, sizeof( BatchSched ) );
+    sch->n = n;
+    GraphKey key;
+    memset( &key, 0, sizeof( key ) );
+    key.storage = (int)st;
+    for( int k = 0; k < n; k++ )
+    {
+        rgdn_stream*             s  = jobs[ k ].stream;
+        const uint32_t           fi = jobs[ k ].frameIndex;
+        const rgdn_frame_params* p  = jobs[ k ].params;
+        rgdn_status              r  = ensure_bin_lut( s, p, cs );
+        if( r != RGDN_SUCCESS ) return r;
+        fill_args( s, fi, p, fa[ k ] );
+        sch->jobFlags[ k ] = ( s->geomValid[ fi ^ 1u ] ? BATCH_JOB_GEOM_PREV : 0u ) | ( s->histPending ? BATCH_JOB_CLEAR_HIST : 0u );
+        s->geomValid[ fi ] = true;
+        s->histPending     = false;
+        key.maxIter        = std::max( key.maxIter, (int)fa[ k ].u.niter );
+        if( !( p->flags & RGDN_FLAG_SKIP_GRADIENTS ) ) key.anyGrad = 1;
+    }
+    // tile tables and pixels per launch kind
+    double pixels[ BS_COUNT ] = {};
+    for( int kind = 0; kind < BS_COUNT; kind++ )
+    {
+        const dim3 sh  = kShapes[ kind == BS_GRADIENT ? 0 : cfg.shape[ kind ] ];
+        int        acc = 0;
+        for( int k = 0; k < n; k++ )
+        {
+            sch->tiles[ kind ].start[ k ] = acc;
+            const Uniform& u = fa[ k ].u;
+            bool           runs;
+            if( kind == BS_GRADIENT ) runs = !( u.flags & RGDN_FLAG_SKIP_GRADIENTS );
+            else if( kind >= BS_ATROUS0 ) runs = (int)u.niter > kind - BS_ATROUS0;
+            else runs = true;
+            if( !runs ) continue;
+            const int w = kind == BS_GRADIENT ? u.GW : u.W, h = kind == BS_GRADIENT ? u.GH : u.H;
+            acc += ceil_div( w, (int)sh.x ) * ceil_div( h, (int)sh.y );
+            pixels[ kind ] += (double)w * h;
+        }
+        sch->tiles[ kind ].start[ n ] = acc;
+    }
+    for( int i = 0; i < key.maxIter; i++ )
+    {
+        int runs = 0, last = 0;
+        for( int k = 0; k < n; k++ )
+        {
+            if( (int)fa[ k ].u.niter > i ) runs++;
+            if( (int)fa[ k ].u.niter == i + 1 ) last++;
+        }
+        key.hm[ i ] = last == 0 ? 0 : last == runs ? 1 : 2;
+    }
+    for( int kind = 0; kind < BS_COUNT; kind++ )
+    {
+        key.shape[ kind ] = kind == BS_GRADIENT ? 0 : cfg.shape[ kind ];
+        key.two[ kind ]   = cfg.two[ kind ];
+    }
+
+    rgdn_status r = RGDN_SUCCESS;
+    if( cfg.graphs && !tuning && !ex.timing )
+    {
+        if( !sl.exec || !same_key( sl.key, key ) )
+        {
+            cudaGraph_t g = nullptr;
+            if( cudaStreamBeginCapture( ex.capture, cudaStreamCaptureModeThreadLocal ) != cudaSuccess ) return RGDN_DEVICE_ERROR;
+            r                 = enqueue_step( c, ex, sl, key, n, pixels, 0, ex.capture, true );
+            cudaError_t e     = cudaStreamEndCapture( ex.capture, &g );
+            if( r == RGDN_SUCCESS && e != cudaSuccess ) r = RGDN_DEVICE_ERROR;
+            if( r == RGDN_SUCCESS )
+            {
+                if( sl.exec )
+                {
+                    cudaGraphExecUpdateResultInfo info;
+                    if( cudaGraphExecUpdate( sl.exec, g, &info ) != cudaSuccess )
+                    {
+                        cudaGetLastError();
+                        cudaGraphExecDestroy( sl.exec );
+                        sl.exec = nullptr;
+                    }
+                }
+                if( !sl.exec && cudaGraphInstantiate( &sl.exec, g, 0 ) != cudaSuccess )
+                {
+                    sl.exec = nullptr;
+                    r       = RGDN_DEVICE_ERROR;
+                }
+                sl.key = key;
+            }
+            if( g ) cudaGraphDestroy( g );
+            if( r != RGDN_SUCCESS ) return r;
+        }
+        if( cudaGraphLaunch( sl.exec, cs ) != cudaSuccess ) return RGDN_DEVICE_ERROR;
+        c->launches.fetch_add( (uint64_t)kernels_in( key ), std::memory_order_relaxed );
+    }
+    else if( ( r = enqueue_step( c, ex, sl, key, n, pixels, tcand, cs, false ) ) != RGDN_SUCCESS )
+        return r;
+    if( cudaEventRecord( sl.done, cs ) != cudaSuccess ) return RGDN_DEVICE_ERROR;
+    sl.inFlight = true;
+    if( tuning && ++tu.step >= kTuneRounds * max_candidates() ) r = settle( ex, st );
+    return r;
+}
+
+BatchExec* exec_of( rgdn_context* c )
+{
+    if( !c->batch ) c->batch = create_exec( c->device );
+    return c->batch;
+}
+
+}  // namespace
+
+rgdn_status batch_submit( rgdn_context* c, const rgdn_job* jobs, uint32_t n, cudaStream_t cs )
+{
+    std::lock_guard< std::mutex > g( c->batchMtx );
+    BatchExec*                    ex = exec_of( c );
+    if( !ex ) return RGDN_DEVICE_ERROR;
+    uint32_t i = 0;
+    while( i < n )
+    {
+        if( !batchable( jobs[ i ] ) )
+        {
+            rgdn_status r = run_denoise( jobs[ i ].stream, jobs[ i ].frameIndex, jobs[ i ].params, cs );
+            if( r == RGDN_SUCCESS ) r = run_exposure( jobs[ i ].stream, jobs[ i ].frameIndex, jobs[ i ].params, cs );
+            if( r != RGDN_SUCCESS ) return r;
+            i++;
+            continue;
+        }
+        // a step: consecutive batchable jobs of one storage mode on distinct streams
+        uint32_t end = i;
+        while( end < n && end - i < (uint32_t)MAX_BATCH && batchable( jobs[ end ] ) &&
+               jobs[ end ].stream->storage == jobs[ i ].stream->storage )
+        {
+            bool dup = false;
+            for( uint32_t k = i; k < end && !dup; k++ ) dup = jobs[ k ].stream == jobs[ end ].stream;
+            if( dup ) break;
+            end++;
+        }
+        rgdn_status r = run_step( c, *ex, jobs + i, (int)( end - i ), cs );
+        if( r != RGDN_SUCCESS ) return r;
+        i = end;
+    }
+    return RGDN_SUCCESS;
+}
+
+void batch_destroy( rgdn_context* c )
+{
+    std::lock_guard< std::mutex > g( c->batchMtx );
+    batch_exec_free( c->batch );
+    c->batch = nullptr;
+}
+
+rgdn_status batch_get_config( rgdn_context* c, uint32_t storage, rgdn_batch_config* out )
+{
+    std::lock_guard< std::mutex > g( c->batchMtx );
+    BatchExec*                    ex = exec_of( c );
+    if( !ex ) return RGDN_DEVICE_ERROR;
+    const Config& cf = ex->cfg[ storage ];
+    memset( out, 0, sizeof( *out ) );
+    out->temporalTile    = (uint32_t)cf.shape[ BS_TEMPORAL ];
+    out->antiFireflyTile = (uint32_t)cf.shape[ BS_ANTI_FIREFLY ];
+    out->varianceTile    = (uint32_t)cf.shape[ BS_VARIANCE ];
+    for( int i = 0; i < MAX_ATROUS_ITERATIONS; i++ )
+    {
+        out->atrousTile[ i ]      = (uint32_t)cf.shape[ BS_ATROUS0 + i ];
+        out->atrousTwoBlocks[ i ] = (uint32_t)cf.two[ BS_ATROUS0 + i ];
+    }
+    out->useGraphs = cf.graphs ? 1u : 0u;
+    out->tuned     = ex->tuner[ storage ].settled ? 1u : 0u;
+    return RGDN_SUCCESS;
+}
+
+rgdn_status batch_set_config( rgdn_context* c, uint32_t storage, const rgdn_batch_config* in )
+{
+    auto ok_shape = []( uint32_t v ) { return v <= RGDN_TILE_64X4; };
+    if( !ok_shape( in->temporalTile ) || !ok_shape( in->antiFireflyTile ) || !ok_shape( in->varianceTile ) )
+        return RGDN_WRONG_FUNCTION_ARGUMENT;
+    for( int i = 0; i < MAX_ATROUS_ITERATIONS; i++ )
+        if( !ok_shape( in->atrousTile[ i ] ) || in->atrousTwoBlocks[ i ] > 1 ) return RGDN_WRONG_FUNCTION_ARGUMENT;
+    std::lock_guard< std::mutex > g( c->batchMtx );
+    BatchExec*                    ex = exec_of( c );
+    if( !ex ) return RGDN_DEVICE_ERROR;
+    Config& cf                   = ex->cfg[ storage ];
+    cf.shape[ BS_TEMPORAL ]      = (int)in->temporalTile;
+    cf.shape[ BS_ANTI_FIREFLY ]  = (int)in->antiFireflyTile;
+    cf.shape[ BS_VARIANCE ]      = (int)in->varianceTile;
+    for( int i = 0; i < MAX_ATROUS_ITERATIONS; i++ )
+    {
+        cf.shape[ BS_ATROUS0 + i ] = (int)in->atrousTile[ i ];
+        cf.two[ BS_ATROUS0 + i ]   = (int)in->atrousTwoBlocks[ i ];
+    }
+    cf.graphs = in->useGraphs != 0;
+    Tuner& tu = ex->tuner[ storage ];
+    for( auto& p : tu.probes )
+    {
+        cudaEventSynchronize( p.b );
+        ex->eventPool.push_back( p.a );
+        ex->eventPool.push_back( p.b );
+    }
+    tu.probes.clear();
+    tu.settled = true;
+    return RGDN_SUCCESS;
+}
+
+rgdn_status batch_set_timing( rgdn_context* c, bool enable )
+{
+    std::lock_guard< std::mutex > g( c->batchMtx );
+    BatchExec*                    ex = exec_of( c );
+    if( !ex ) return RGDN_DEVICE_ERROR;
+    ex->timing = enable;
+    return RGDN_SUCCESS;
+}
+
+rgdn_status batch_read_timing( rgdn_context* c, rgdn_stage_timing* out, uint32_t capacity, uint32_t* outCount )
+{
+    std::lock_guard< std::mutex > g( c->batchMtx );
+    BatchExec*                    ex = exec_of( c );
+    if( !ex ) return RGDN_DEVICE_ERROR;
+    std::vector< rgdn_stage_timing > agg;
+    rgdn_status                      r = RGDN_SUCCESS;
+    for( auto& pd : ex->pending )
+    {
+        float ms = 0.0f;
+        if( cudaEventSynchronize( pd.b ) != cudaSuccess || cudaEventElapsedTime( &ms, pd.a, pd.b ) != cudaSuccess ) r = RGDN_DEVICE_ERROR;
+        auto it = std::find_if( agg.begin(), agg.end(), [ & ]( const rgdn_stage_timing& t ) {
+            return t.stage == (uint32_t)pd.stage && t.iteration == (uint32_t)pd.iter;
+        } );
+        if( it == agg.end() ) agg.push_back( { (uint32_t)pd.stage, (uint32_t)pd.iter, 1u, ms } );
+        else
+        {
+            it->launches++;
+            it->totalMs += ms;
+        }
+        ex->eventPool.push_back( pd.a );
+        ex->eventPool.push_back( pd.b );
+    }
+    ex->pending.clear();
+    std::sort( agg.begin(), agg.end(), []( const rgdn_stage_timing& a, const rgdn_stage_timing& b ) {
+        return a.stage != b.stage ? a.stage < b.stage : a.iteration < b.iteration;
+    } );
+    for( uint32_t k = 0; k < agg.size() && k < capacity; k++ ) out[ k ] = agg[ k ];
+    *outCount = (uint32_t)agg.size();
+    return r;
+}
+
+}  // namespace rgdn

@@ -52,8 +52,9 @@ struct Uniform
 };
 
 // Device addresses of every plane the kernels touch, resolved for one frameIndex
-// (cur = frameIndex, prev = frameIndex ^ 1 for double-buffered images).
-struct FrameArgs
+// (cur = frameIndex, prev = frameIndex ^ 1 for double-buffered images). 16-byte aligned and
+// sized: the batched kernels copy it into shared memory as int4.
+struct alignas( 16 ) FrameArgs
 {
     Uniform u;
     // G-buffer (reference formats)
@@ -163,5 +164,65 @@ cudaError_t launch_atrous_tma_f16( const FrameArgs& a, int iter, bool hist, cons
 cudaError_t launch_atrous_tma_bf16( const FrameArgs& a, int iter, bool hist, const void* maps, cudaStream_t s );
 int atrous_tma_smem( int storage, int iter );
 inline bool is_fast_kernel( int stage ) { return stage == KF_ATROUS_FAST || stage == KF_ATROUS_FAST_HIST || stage == KF_VARIANCE_FAST; }
+
+// ------------------------------------------------------------------------------------------
+// Batched steps: one persistent launch per stage covers the frames of many streams.
+// The step's schedule and its jobs' FrameArgs live in device memory (copied from pinned host
+// memory at the start of the step), so a captured graph of the step's launches stays valid
+// for any set of up to MAX_BATCH frames.
+// ------------------------------------------------------------------------------------------
+constexpr int MAX_BATCH = 64;
+
+// tile tables of a step, one per launch kind
+enum BatchSlot : int
+{
+    BS_GRADIENT = 0,     // gradient samples and gradient a-trous (over the 1/3-resolution image)
+    BS_TEMPORAL,
+    BS_ANTI_FIREFLY,
+    BS_VARIANCE,
+    BS_ATROUS0,          // a-trous iteration i uses BS_ATROUS0 + i
+    BS_COUNT = BS_ATROUS0 + MAX_ATROUS_ITERATIONS
+};
+
+// Tile j of a launch belongs to the job k with start[k] <= j < start[k+1]; a job without work
+// in that launch has start[k] == start[k+1]. The tiles of one job run row-major over its image,
+// blockDim.x x blockDim.y pixels each.
+struct BatchTiles
+{
+    int start[ MAX_BATCH + 1 ];
+};
+
+constexpr uint32_t BATCH_JOB_GEOM_PREV  = 1u;   // the previous frame's geometry record is valid
+constexpr uint32_t BATCH_JOB_CLEAR_HIST = 2u;   // discard a histogram no exposure pass consumed
+
+struct BatchSched
+{
+    int        n;
+    uint32_t   jobFlags[ MAX_BATCH ];
+    BatchTiles tiles[ BS_COUNT ];
+};
+
+// One stage of a batched step: `grid` persistent blocks of `block` threads (256 in all).
+// Stages: RGDN_STAGE_GRADIENT_SAMPLES, _GRADIENT_ATROUS (iter 0..3), _TEMPORAL_ACCUMULATION,
+// _ANTI_FIREFLY, _LUMINANCE_AVG (launch_batch_*) and _VARIANCE_ESTIMATION, _ATROUS
+// (launch_batch_fast_*: the FAST translation units).
+cudaError_t launch_batch_ref( int stage, int iter, const BatchSched* sch, const FrameArgs* jobs, dim3 block, int grid, cudaStream_t s );
+cudaError_t launch_batch_f32( int stage, int iter, const BatchSched* sch, const FrameArgs* jobs, dim3 block, int grid, cudaStream_t s );
+cudaError_t launch_batch_f16( int stage, int iter, const BatchSched* sch, const FrameArgs* jobs, dim3 block, int grid, cudaStream_t s );
+cudaError_t launch_batch_bf16( int stage, int iter, const BatchSched* sch, const FrameArgs* jobs, dim3 block, int grid, cudaStream_t s );
+cudaError_t launch_batch_fast_ref( int stage, int iter, const BatchSched* sch, const FrameArgs* jobs, dim3 block, int grid, cudaStream_t s );
+cudaError_t launch_batch_fast_f32( int stage, int iter, const BatchSched* sch, const FrameArgs* jobs, dim3 block, int grid, cudaStream_t s );
+cudaError_t launch_batch_fast_f16( int stage, int iter, const BatchSched* sch, const FrameArgs* jobs, dim3 block, int grid, cudaStream_t s );
+cudaError_t launch_batch_fast_bf16( int stage, int iter, const BatchSched* sch, const FrameArgs* jobs, dim3 block, int grid, cudaStream_t s );
+// resident blocks per SM of a batched stage's kernel (256-thread blocks), 0 on error
+int batch_blocks_per_sm_ref( int stage );
+int batch_blocks_per_sm_f32( int stage );
+int batch_blocks_per_sm_f16( int stage );
+int batch_blocks_per_sm_bf16( int stage );
+int batch_blocks_per_sm_fast_ref( int stage );
+int batch_blocks_per_sm_fast_f32( int stage );
+int batch_blocks_per_sm_fast_f16( int stage );
+int batch_blocks_per_sm_fast_bf16( int stage );
+inline bool is_batch_fast_stage( int stage ) { return stage == RGDN_STAGE_VARIANCE_ESTIMATION || stage == RGDN_STAGE_ATROUS; }
 
 }  // namespace rgdn

@@ -467,15 +467,30 @@ __device__ __forceinline__ void fill_u8( float* u8, int t )
     u8[ t ] = (float)t / 255.0f;
 }
 
+// Tile functions: one thread per pixel (or stratum) of the blockDim-sized tile (bx, by) of
+// frame `a`. The single-frame kernels run one tile per block; the batched kernels loop a
+// persistent block over the tiles of many frames.
+template< int M > __device__ __forceinline__ void gradient_samples_tile( const FrameArgs& a, uint32_t* dst, int bx, int by, const float* u8 )
+{
+    const int gx = bx * blockDim.x + threadIdx.x;
+    const int gy = by * blockDim.y + threadIdx.y;
+    if( gx >= a.u.GW || gy >= a.u.GH || gx * STRATA >= a.u.W || gy * STRATA >= a.u.H ) return;
+    gradient_sample_px< M >( a, dst, gx, gy, u8 );
+}
+__device__ __forceinline__ void gradient_atrous_tile( const FrameArgs& a, int iter, int bx, int by, const float* u8 )
+{
+    const int gx = bx * blockDim.x + threadIdx.x;
+    const int gy = by * blockDim.y + threadIdx.y;
+    if( gx >= a.u.GW || gy >= a.u.GH || gx * STRATA >= a.u.W || gy * STRATA >= a.u.H ) return;
+    gradient_atrous_px( a, gx, gy, iter, u8 );
+}
+
 template< int M > __global__ void __launch_bounds__( 256 ) k_gradient_samples( const FrameArgs a, uint32_t* dst )
 {
     __shared__ float u8[ 256 ];
     fill_u8( u8, threadIdx.y * blockDim.x + threadIdx.x );
     __syncthreads();
-    const int gx = blockIdx.x * blockDim.x + threadIdx.x;
-    const int gy = blockIdx.y * blockDim.y + threadIdx.y;
-    if( gx >= a.u.GW || gy >= a.u.GH || gx * STRATA >= a.u.W || gy * STRATA >= a.u.H ) return;
-    gradient_sample_px< M >( a, dst, gx, gy, u8 );
+    gradient_samples_tile< M >( a, dst, blockIdx.x, blockIdx.y, u8 );
 }
 
 template< int M > __global__ void __launch_bounds__( 256 ) k_gradient_atrous( const FrameArgs a, const int iter )
@@ -483,10 +498,7 @@ template< int M > __global__ void __launch_bounds__( 256 ) k_gradient_atrous( co
     __shared__ float u8[ 256 ];
     fill_u8( u8, threadIdx.y * blockDim.x + threadIdx.x );
     __syncthreads();
-    const int gx = blockIdx.x * blockDim.x + threadIdx.x;
-    const int gy = blockIdx.y * blockDim.y + threadIdx.y;
-    if( gx >= a.u.GW || gy >= a.u.GH || gx * STRATA >= a.u.W || gy * STRATA >= a.u.H ) return;
-    gradient_atrous_px( a, gx, gy, iter, u8 );
+    gradient_atrous_tile( a, iter, blockIdx.x, blockIdx.y, u8 );
 }
 
 // ==========================================================================================
@@ -530,15 +542,13 @@ __device__ __forceinline__ float parallax( const Uniform& u, float3 pos, float3 
 // FAST: continuous specular terms in hardware exp2/log2, shared subexpressions and the
 // precombined view-projection matrices. GEOM: write this frame's geometry record. GEOMPREV:
 // read the previous frame's record (decoded normal + depth, the same values) at the taps.
-template< int M, bool FAST, bool GEOM, bool GEOMPREV > __global__ void __launch_bounds__( 256 ) k_temporal( const FrameArgs a )
+template< int M, bool FAST, bool GEOM, bool GEOMPREV >
+__device__ __forceinline__ void temporal_tile( const FrameArgs& a, int bx, int by, const float* u8 )
 {
     using S          = Sto< M >;
-    __shared__ float u8[ 256 ];
-    fill_u8( u8, threadIdx.y * blockDim.x + threadIdx.x );
-    __syncthreads();
     const Uniform& u = a.u;
-    const int      px = blockIdx.x * blockDim.x + threadIdx.x;
-    const int      py = blockIdx.y * blockDim.y + threadIdx.y;
+    const int      px = bx * blockDim.x + threadIdx.x;
+    const int      py = by * blockDim.y + threadIdx.y;
     if( px >= u.W || py >= u.H ) return;
     const size_t i = idx( u, px, py );
 
@@ -859,6 +869,14 @@ template< int M, bool FAST, bool GEOM, bool GEOMPREV > __global__ void __launch_
     S::st3( a.indirAccum, i, indirAccum );
 }
 
+template< int M, bool FAST, bool GEOM, bool GEOMPREV > __global__ void __launch_bounds__( 256 ) k_temporal( const FrameArgs a )
+{
+    __shared__ float u8[ 256 ];
+    fill_u8( u8, threadIdx.y * blockDim.x + threadIdx.x );
+    __syncthreads();
+    temporal_tile< M, FAST, GEOM, GEOMPREV >( a, blockIdx.x, blockIdx.y, u8 );
+}
+
 // ==========================================================================================
 // CmAntiFirefly.comp:96-158 — 5x5 min/max clamp (the centre excluded)
 // ==========================================================================================
@@ -1094,14 +1112,14 @@ __device__ __forceinline__ void af_signal( const FrameArgs& a, const void* src, 
     O::st( dst, i, c );
 }
 
-template< int M > __global__ void __launch_bounds__( 256 ) k_antifirefly_fast( const FrameArgs a )
+template< int M > __device__ __forceinline__ void antifirefly_fast_tile( const FrameArgs& a, int bx, int by )
 {
     const Uniform& u  = a.u;
-    const int      px = blockIdx.x * blockDim.x + threadIdx.x;
-    const int      py = blockIdx.y * blockDim.y + threadIdx.y;
+    const int      px = bx * blockDim.x + threadIdx.x;
+    const int      py = by * blockDim.y + threadIdx.y;
     if( px >= u.W || py >= u.H ) return;
     const int  i        = py * u.W + px;
-    const int  bx0      = blockIdx.x * blockDim.x, by0 = blockIdx.y * blockDim.y;
+    const int  bx0      = bx * blockDim.x, by0 = by * blockDim.y;
     const bool interior = bx0 >= 2 && by0 >= 2 && bx0 + (int)blockDim.x + 2 <= u.W && by0 + (int)blockDim.y + 2 <= u.H;
     if( interior )
     {
@@ -1116,20 +1134,28 @@ template< int M > __global__ void __launch_bounds__( 256 ) k_antifirefly_fast( c
         af_signal< M, false >( a, a.indirAccum, a.indirPing, px, py, i );
     }
 }
+template< int M > __global__ void __launch_bounds__( 256 ) k_antifirefly_fast( const FrameArgs a )
+{
+    antifirefly_fast_tile< M >( a, blockIdx.x, blockIdx.y );
+}
 
 // Variance for the default path: the geometry record instead of the depth / normal images
-template< int M, bool FAST > __global__ void __launch_bounds__( 256 ) k_variance_geo( const FrameArgs a )
+template< int M, bool FAST > __device__ __forceinline__ void variance_geo_tile( const FrameArgs& a, int bx, int by )
 {
     using S          = Sto< M >;
     const Uniform& u = a.u;
-    const int      px = blockIdx.x * blockDim.x + threadIdx.x;
-    const int      py = blockIdx.y * blockDim.y + threadIdx.y;
+    const int      px = bx * blockDim.x + threadIdx.x;
+    const int      py = by * blockDim.y + threadIdx.y;
     if( px >= u.W || py >= u.H ) return;
     const int i = py * u.W + px;
     float3    c;
     float     v;
     variance_px< M, FAST, true >( a, px, py, i, [ & ]( int dx, int dy ) { return ld3z< M >( a, a.diffAccumColor, px + dx, py + dy ); }, c, v );
     S::stcv( a.diffPing, a.varPing, (size_t)i, c, v );
+}
+template< int M, bool FAST > __global__ void __launch_bounds__( 256 ) k_variance_geo( const FrameArgs a )
+{
+    variance_geo_tile< M, FAST >( a, blockIdx.x, blockIdx.y );
 }
 
 // ==========================================================================================
@@ -1359,19 +1385,15 @@ __device__ __forceinline__ void atrous_px( const FrameArgs& a, const AtrousIO& i
 // One a-trous iteration over the frame. HIST: the last iteration also accumulates the
 // luminance histogram of the HistogramInput values it writes (CmLuminanceHistogram.comp,
 // fused: no second read of the image).
-template< int M, bool FAST, bool HIST, bool GEOMIN > __global__ void __launch_bounds__( 256, 3 ) k_atrous( const FrameArgs a, const int iter )
+// The tile of one a-trous iteration. HIST adds the bins of this tile's HistogramInput values
+// to the block's shared histogram `hist` (the caller zeroes and flushes it).
+template< int M, bool FAST, bool HIST, bool GEOMIN >
+__device__ __forceinline__ void atrous_tile( const FrameArgs& a, const int iter, int bx, int by, const float* u8, uint32_t* hist )
 {
     using S = Sto< M >;
-    __shared__ float    u8[ 256 ];
-    __shared__ uint32_t hist[ HIST ? 256 : 1 ];
-    const int t = threadIdx.y * blockDim.x + threadIdx.x;
-    u8[ t ]     = (float)t / 255.0f;
-    if( HIST ) hist[ t ] = 0u;
-    __syncthreads();
-
     const Uniform& u  = a.u;
-    const int      px = blockIdx.x * blockDim.x + threadIdx.x;
-    const int      py = blockIdx.y * blockDim.y + threadIdx.y;
+    const int      px = bx * blockDim.x + threadIdx.x;
+    const int      py = by * blockDim.y + threadIdx.y;
     if( px < u.W && py < u.H )
     {
         const int      i    = py * u.W + px;
@@ -1381,8 +1403,8 @@ template< int M, bool FAST, bool HIST, bool GEOMIN > __global__ void __launch_bo
         float          outVar;
         // block-uniform: the block's taps are all inside the image and inside one checkerboard half
         const int  step = 1 << iter, sep = u.W / 2;
-        const int  bx0 = blockIdx.x * blockDim.x, bx1 = bx0 + blockDim.x - 1;
-        const int  by0 = blockIdx.y * blockDim.y, by1 = by0 + blockDim.y - 1;
+        const int  bx0 = bx * blockDim.x, bx1 = bx0 + blockDim.x - 1;
+        const int  by0 = by * blockDim.y, by1 = by0 + blockDim.y - 1;
         const bool interior = bx0 - step >= 0 && by0 - step >= 0 && bx1 + step < u.W && by1 + step < u.H &&
                               ( bx1 + step < sep || bx0 - step >= sep );
         if( interior ) atrous_px< M, FAST, true, GEOMIN >( a, io, iter, px, py, i, u8, outDiff, outVar, outSpec, outInd );
@@ -1401,10 +1423,22 @@ template< int M, bool FAST, bool HIST, bool GEOMIN > __global__ void __launch_bo
                 // one shared atomic per distinct bin of the warp
                 const uint32_t bin    = __ldg( &a.binLut[ hin ] );
                 const uint32_t peers  = __match_any_sync( __activemask(), bin );
-                if( ( threadIdx.x & 31 ) == (uint32_t)( __ffs( peers ) - 1 ) ) atomicAdd( &hist[ bin ], (uint32_t)__popc( peers ) );
+                if( ( ( threadIdx.y * blockDim.x + threadIdx.x ) & 31 ) == (uint32_t)( __ffs( peers ) - 1 ) )
+                    atomicAdd( &hist[ bin ], (uint32_t)__popc( peers ) );
             }
         }
     }
+}
+
+template< int M, bool FAST, bool HIST, bool GEOMIN > __global__ void __launch_bounds__( 256, 3 ) k_atrous( const FrameArgs a, const int iter )
+{
+    __shared__ float    u8[ 256 ];
+    __shared__ uint32_t hist[ HIST ? 256 : 1 ];
+    const int t = threadIdx.y * blockDim.x + threadIdx.x;
+    u8[ t ]     = (float)t / 255.0f;
+    if( HIST ) hist[ t ] = 0u;
+    __syncthreads();
+    atrous_tile< M, FAST, HIST, GEOMIN >( a, iter, blockIdx.x, blockIdx.y, u8, hist );
     if( HIST )
     {
         __syncthreads();
@@ -1769,10 +1803,8 @@ template< int M > __global__ void __launch_bounds__( 256 ) k_histogram( const Fr
 }
 
 // CmLuminanceAvg.comp:39-89 — weighted average bin, eye adaptation, histogram clear
-template< int M > __global__ void __launch_bounds__( 256 ) k_luminance_avg( const FrameArgs a )
+__device__ __forceinline__ void luminance_avg_job( const FrameArgs& a, uint32_t* sh, uint32_t& count0 )
 {
-    __shared__ uint32_t sh[ 256 ];
-    __shared__ uint32_t count0;
     const Uniform& u  = a.u;
     Tonemapping*   tm = a.tm;
     const int      t  = threadIdx.x;
@@ -1797,6 +1829,181 @@ template< int M > __global__ void __launch_bounds__( 256 ) k_luminance_avg( cons
     const float tt         = 1.0f - (float)exp( (double)( -u.timeDelta * 1.1f ) );
     const float adapted    = last + ( wal - last ) * tt;
     tm->avgLuminance       = fminf( adapted, (float)exp2( (double)maxL ) );
+}
+template< int M > __global__ void __launch_bounds__( 256 ) k_luminance_avg( const FrameArgs a )
+{
+    __shared__ uint32_t sh[ 256 ];
+    __shared__ uint32_t count0;
+    luminance_avg_job( a, sh, count0 );
+}
+
+// ==========================================================================================
+// Batched steps: persistent kernels, one per stage, looping over the tiles of every frame of
+// the step. The tile tables and the frames' arguments are read from device memory.
+// ==========================================================================================
+
+// the job of tile t: the last k with start[k] <= t (jobs without tiles are passed over)
+__device__ __forceinline__ int batch_job( const int* start, int n, int t )
+{
+    int lo = 0, hi = n - 1;
+    while( lo < hi )
+    {
+        const int mid = ( lo + hi + 1 ) >> 1;
+        if( start[ mid ] <= t ) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+// Loads the tile table into shared memory (one barrier, which also publishes whatever the
+// caller wrote to shared memory before), then runs body(args, job, tile index within the job)
+// for the block's tiles. The job's FrameArgs are copied into shared memory `sa` whenever the
+// block moves to another job: the tile code then reads them from an address space that no
+// global store can alias. Every thread of the block runs every iteration: body may use barriers.
+template< class F >
+__device__ __forceinline__ void batch_tiles( const BatchSched* __restrict__ sch, const FrameArgs* __restrict__ jobs, int slot, int* sStart,
+                                             FrameArgs& sa, F&& body )
+{
+    static_assert( sizeof( FrameArgs ) % 16 == 0, "FrameArgs is copied as int4" );
+    const int n  = sch->n;
+    const int t  = threadIdx.y * blockDim.x + threadIdx.x;
+    const int nt = blockDim.x * blockDim.y;
+    for( int k = t; k <= n; k += nt ) sStart[ k ] = sch->tiles[ slot ].start[ k ];
+    __syncthreads();
+    if( n <= 0 ) return;
+    const int total = sStart[ n ];
+    int       cur   = -1;
+    for( int tile = blockIdx.x; tile < total; tile += gridDim.x )
+    {
+        const int j = batch_job( sStart, n, tile );
+        if( j != cur )
+        {
+            __syncthreads();   // the previous job's arguments are no longer read
+            const int4* src = reinterpret_cast< const int4* >( jobs + j );
+            int4*       dst = reinterpret_cast< int4* >( &sa );
+            for( int k = t; k < (int)( sizeof( FrameArgs ) / 16 ); k += nt ) dst[ k ] = __ldg( src + k );
+            __syncthreads();
+            cur = j;
+        }
+        body( static_cast< const FrameArgs& >( sa ), j, tile - sStart[ j ] );
+    }
+}
+
+__device__ __forceinline__ int tiles_x( int w ) { return ( w + (int)blockDim.x - 1 ) / (int)blockDim.x; }
+
+template< int M > __global__ void __launch_bounds__( 256 ) kb_gradient_samples( const BatchSched* __restrict__ sch, const FrameArgs* __restrict__ jobs )
+{
+    __shared__ float u8[ 256 ];
+    __shared__ int   sStart[ MAX_BATCH + 1 ];
+    __shared__ FrameArgs sa;
+    fill_u8( u8, threadIdx.y * blockDim.x + threadIdx.x );
+    batch_tiles( sch, jobs, BS_GRADIENT, sStart, sa, [ & ]( const FrameArgs& a, int, int lt ) {
+        const int tx = tiles_x( a.u.GW );
+        gradient_samples_tile< M >( a, a.disPing, lt % tx, lt / tx, u8 );
+    } );
+}
+
+template< int M > __global__ void __launch_bounds__( 256 ) kb_gradient_atrous( const BatchSched* __restrict__ sch, const FrameArgs* __restrict__ jobs, const int iter )
+{
+    __shared__ float u8[ 256 ];
+    __shared__ int   sStart[ MAX_BATCH + 1 ];
+    __shared__ FrameArgs sa;
+    fill_u8( u8, threadIdx.y * blockDim.x + threadIdx.x );
+    batch_tiles( sch, jobs, BS_GRADIENT, sStart, sa, [ & ]( const FrameArgs& a, int, int lt ) {
+        const int tx = tiles_x( a.u.GW );
+        gradient_atrous_tile( a, iter, lt % tx, lt / tx, u8 );
+    } );
+}
+
+// FAST temporal accumulation writing the geometry record; each job reads the previous
+// frame's record where it is valid. The block of a job's first tile also clears a histogram
+// that no exposure pass consumed (before the last a-trous iteration adds this frame's).
+template< int M > __global__ void __launch_bounds__( 256 ) kb_temporal( const BatchSched* __restrict__ sch, const FrameArgs* __restrict__ jobs )
+{
+    __shared__ float u8[ 256 ];
+    __shared__ int   sStart[ MAX_BATCH + 1 ];
+    __shared__ FrameArgs sa;
+    const int t = threadIdx.y * blockDim.x + threadIdx.x;
+    fill_u8( u8, t );
+    batch_tiles( sch, jobs, BS_TEMPORAL, sStart, sa, [ & ]( const FrameArgs& a, int j, int lt ) {
+        const uint32_t   f  = sch->jobFlags[ j ];
+        const int        tx = tiles_x( a.u.W );
+        if( lt == 0 && ( f & BATCH_JOB_CLEAR_HIST ) ) a.tm->histogram[ t ] = 0u;
+        if( f & BATCH_JOB_GEOM_PREV ) temporal_tile< M, true, true, true >( a, lt % tx, lt / tx, u8 );
+        else temporal_tile< M, true, true, false >( a, lt % tx, lt / tx, u8 );
+    } );
+}
+
+template< int M > __global__ void __launch_bounds__( 256 ) kb_antifirefly( const BatchSched* __restrict__ sch, const FrameArgs* __restrict__ jobs )
+{
+    __shared__ int       sStart[ MAX_BATCH + 1 ];
+    __shared__ FrameArgs sa;
+    batch_tiles( sch, jobs, BS_ANTI_FIREFLY, sStart, sa, [ & ]( const FrameArgs& a, int, int lt ) {
+        const int tx = tiles_x( a.u.W );
+        antifirefly_fast_tile< M >( a, lt % tx, lt / tx );
+    } );
+}
+
+template< int M > __global__ void __launch_bounds__( 256 ) kb_variance( const BatchSched* __restrict__ sch, const FrameArgs* __restrict__ jobs )
+{
+    __shared__ int       sStart[ MAX_BATCH + 1 ];
+    __shared__ FrameArgs sa;
+    batch_tiles( sch, jobs, BS_VARIANCE, sStart, sa, [ & ]( const FrameArgs& a, int, int lt ) {
+        const int tx = tiles_x( a.u.W );
+        variance_geo_tile< M, true >( a, lt % tx, lt / tx );
+    } );
+}
+
+// A-trous iteration `iter` over the jobs that run it. A job's last iteration composes PreFinal
+// and bins its HistogramInput into the block's shared histogram, which is flushed into that
+// job's tonemapping state when the block moves to another job and at the end.
+// HM: 0 = the iteration is no job's last, 1 = it is every job's last, 2 = it depends on the job.
+template< int M, int HM, int MINB >
+__global__ void __launch_bounds__( 256, MINB ) kb_atrous( const BatchSched* __restrict__ sch, const FrameArgs* __restrict__ jobs, const int iter )
+{
+    __shared__ float    u8[ 256 ];
+    __shared__ uint32_t hist[ HM ? 256 : 1 ];
+    __shared__ int      sStart[ MAX_BATCH + 1 ];
+    __shared__ FrameArgs sa;
+    const int t = threadIdx.y * blockDim.x + threadIdx.x;
+    u8[ t ]     = (float)t / 255.0f;
+    if( HM ) hist[ t ] = 0u;
+    int  histJob = -1;
+    auto flush   = [ & ]() {
+        __syncthreads();
+        const uint32_t c = hist[ t ];
+        if( c ) atomicAdd( &jobs[ histJob ].tm->histogram[ t ], c );
+        hist[ t ] = 0u;
+        __syncthreads();
+    };
+    batch_tiles( sch, jobs, BS_ATROUS0 + iter, sStart, sa, [ & ]( const FrameArgs& a, int j, int lt ) {
+        const int tx = tiles_x( a.u.W );
+        if( HM == 0 ) atrous_tile< M, true, false, true >( a, iter, lt % tx, lt / tx, u8, hist );
+        else if( HM == 1 || iter + 1 == (int)a.u.niter )
+        {
+            if( histJob != j )
+            {
+                if( histJob >= 0 ) flush();
+                histJob = j;
+            }
+            atrous_tile< M, true, true, true >( a, iter, lt % tx, lt / tx, u8, hist );
+        }
+        else atrous_tile< M, true, false, true >( a, iter, lt % tx, lt / tx, u8, hist );
+    } );
+    if( HM && histJob >= 0 ) flush();
+}
+
+// one block per job (strided), as k_luminance_avg
+template< int M > __global__ void __launch_bounds__( 256 ) kb_luminance_avg( const BatchSched* __restrict__ sch, const FrameArgs* __restrict__ jobs )
+{
+    __shared__ uint32_t sh[ 256 ];
+    __shared__ uint32_t count0;
+    const int n = sch->n;
+    for( int j = blockIdx.x; j < n; j += gridDim.x )
+    {
+        __syncthreads();
+        luminance_avg_job( jobs[ j ], sh, count0 );
+    }
 }
 
 }  // namespace dev
@@ -1846,6 +2053,74 @@ template< int M > cudaError_t launch_fast_t( const FrameArgs& a, int stage, int 
         default: return cudaErrorInvalidValue;
     }
     return cudaGetLastError();
+}
+
+template< int M > cudaError_t launch_batch_t( int stage, int iter, const BatchSched* sch, const FrameArgs* jobs, dim3 block, int grid, cudaStream_t s )
+{
+    switch( stage )
+    {
+        case RGDN_STAGE_GRADIENT_SAMPLES: dev::kb_gradient_samples< M ><<< grid, block, 0, s >>>( sch, jobs ); break;
+        case RGDN_STAGE_GRADIENT_ATROUS: dev::kb_gradient_atrous< M ><<< grid, block, 0, s >>>( sch, jobs, iter ); break;
+        case RGDN_STAGE_TEMPORAL_ACCUMULATION: dev::kb_temporal< M ><<< grid, block, 0, s >>>( sch, jobs ); break;
+        case RGDN_STAGE_ANTI_FIREFLY: dev::kb_antifirefly< M ><<< grid, block, 0, s >>>( sch, jobs ); break;
+        case RGDN_STAGE_LUMINANCE_AVG: dev::kb_luminance_avg< M ><<< grid, 256, 0, s >>>( sch, jobs ); break;
+        default: return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+}
+template< int M > cudaError_t launch_batch_fast_t( int stage, int iter, const BatchSched* sch, const FrameArgs* jobs, dim3 block, int grid, cudaStream_t s )
+{
+    switch( stage )
+    {
+        case RGDN_STAGE_VARIANCE_ESTIMATION: dev::kb_variance< M ><<< grid, block, 0, s >>>( sch, jobs ); break;
+        // iter carries the histogram mode (bits 8-9) and the occupancy variant (bit 10)
+        case RGDN_STAGE_ATROUS:
+        {
+            const int hm = ( iter >> 8 ) & 3, occ2 = ( iter >> 10 ) & 1, it = iter & 0xff;
+            if( occ2 )
+            {
+                if( hm == 0 ) dev::kb_atrous< M, 0, 2 ><<< grid, block, 0, s >>>( sch, jobs, it );
+                else if( hm == 1 ) dev::kb_atrous< M, 1, 2 ><<< grid, block, 0, s >>>( sch, jobs, it );
+                else dev::kb_atrous< M, 2, 2 ><<< grid, block, 0, s >>>( sch, jobs, it );
+            }
+            else
+            {
+                if( hm == 0 ) dev::kb_atrous< M, 0, 3 ><<< grid, block, 0, s >>>( sch, jobs, it );
+                else if( hm == 1 ) dev::kb_atrous< M, 1, 3 ><<< grid, block, 0, s >>>( sch, jobs, it );
+                else dev::kb_atrous< M, 2, 3 ><<< grid, block, 0, s >>>( sch, jobs, it );
+            }
+            break;
+        }
+        default: return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+}
+template< class K > int blocks_per_sm( K kernel )
+{
+    int n = 0;
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor( &n, kernel, 256, 0 ) == cudaSuccess ? n : 0;
+}
+template< int M > int batch_blocks_per_sm_t( int stage )
+{
+    switch( stage )
+    {
+        case RGDN_STAGE_GRADIENT_SAMPLES: return blocks_per_sm( dev::kb_gradient_samples< M > );
+        case RGDN_STAGE_GRADIENT_ATROUS: return blocks_per_sm( dev::kb_gradient_atrous< M > );
+        case RGDN_STAGE_TEMPORAL_ACCUMULATION: return blocks_per_sm( dev::kb_temporal< M > );
+        case RGDN_STAGE_ANTI_FIREFLY: return blocks_per_sm( dev::kb_antifirefly< M > );
+        case RGDN_STAGE_LUMINANCE_AVG: return blocks_per_sm( dev::kb_luminance_avg< M > );
+        default: return 0;
+    }
+}
+template< int M > int batch_blocks_per_sm_fast_t( int stage )
+{
+    switch( stage )
+    {
+        case RGDN_STAGE_VARIANCE_ESTIMATION: return blocks_per_sm( dev::kb_variance< M > );
+        case RGDN_STAGE_ATROUS: return blocks_per_sm( dev::kb_atrous< M, 2, 3 > );
+        case RGDN_STAGE_ATROUS | 0x400: return blocks_per_sm( dev::kb_atrous< M, 2, 2 > );
+        default: return 0;
+    }
 }
 
 template< int M > cudaError_t launch_atrous_tma_t( const FrameArgs& a, int iter, bool hist, const void* maps, cudaStream_t s )

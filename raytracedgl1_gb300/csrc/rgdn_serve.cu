@@ -1,0 +1,566 @@
+// Serving loop behind rgdn_server_*: continuous batching of frame requests from many camera
+// streams onto the batch executor (rgdn_batch.cu).
+//
+// Threads: callers submit (any thread); a scheduler thread forms steps and enqueues them; a
+// completion thread waits for steps in order and stamps their frames done.
+//
+// Scheduling (the scheduler thread, one step per pass):
+//   * a step is started whenever frames are waiting and fewer than stepsInFlight steps are on
+//     the GPU, so new frames join the next step while the previous one runs;
+//   * candidates are the oldest waiting frame of each stream, in arrival order; a frame whose
+//     stream has no memory yet is admitted if the context budget allows (idle streams may be
+//     evicted, oldest first), otherwise it waits for memory to free up;
+//   * the step takes candidates while it has fewer than maxFramesPerStep frames and its pixels
+//     stay within maxPixelsPerStep (the first candidate is always taken);
+//   * steps alternate between two CUDA streams; a step waits (cudaStreamWaitEvent) only for an
+//     unfinished earlier step on the other CUDA stream that holds one of its camera streams.
+// A frame's G-buffer is copied into (or bound to) the stream's planes at the head of its step,
+// and PRE_FINAL is copied out after the step when the request asks for it.
+#include <algorithm>
+#include <chrono>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <map>
+#include <mutex>
+#include <thread>
+#include <unordered_map>
+#include <vector>
+
+#include "rgdn_host.h"
+
+namespace
+{
+
+using Clock = std::chrono::steady_clock;
+double now_s() { return std::chrono::duration< double >( Clock::now().time_since_epoch() ).count(); }
+
+enum ReqState : uint32_t
+{
+    REQ_QUEUED = 100,
+    REQ_RUNNING,
+    REQ_DONE = RGDN_FRAME_DONE,
+    REQ_DROPPED = RGDN_FRAME_DROPPED,
+};
+
+struct ServeReq
+{
+    rgdn_frame_request req;
+    uint32_t           state = REQ_QUEUED;
+    uint32_t           fi    = 0;
+    double             tSubmit = 0, tEnqueue = 0, tDone = 0;
+};
+
+struct ServeStream
+{
+    uint32_t               id = 0, W = 0, H = 0;
+    rgdn_stream*           s = nullptr;
+    uint32_t               nextFi  = 0;
+    std::deque< uint64_t > queue;            // waiting tickets, oldest first
+    uint32_t               running = 0;      // frames of this stream in unfinished steps
+    int64_t                lastStep = -1;    // step index of its latest scheduled frame
+    double                 lastUse  = 0;
+    bool                   closing  = false;
+};
+
+struct StepRec
+{
+    int64_t                 index;
+    int                     lane;           // which CUDA stream
+    cudaEvent_t             done;
+    std::vector< uint64_t > tickets;
+    std::vector< uint32_t > streams;
+    uint64_t                pixels;
+};
+
+}  // namespace
+
+struct rgdn_server
+{
+    rgdn_context*           ctx = nullptr;
+    rgdn_server_create_info info{};
+    std::mutex              m;
+    std::condition_variable cvWork, cvDone;
+    std::map< uint32_t, ServeStream >       streams;
+    std::unordered_map< uint64_t, ServeReq > reqs;
+    std::deque< uint64_t >  arrival;         // waiting tickets in arrival order
+    uint32_t                nextStreamId = 1;
+    uint64_t                nextTicket   = 1;
+    int64_t                 nextStep     = 0;
+    std::deque< StepRec >   inflight;
+    std::vector< cudaEvent_t > eventPool;
+    cudaStream_t            lane[ 2 ] = { nullptr, nullptr };
+    std::thread             scheduler, completer;
+    bool                    stop = false;
+    uint64_t                changes   = 0;      // submissions, completions, closes
+    uint64_t                stalledAt = ~0ull;  // `changes` when a pass found nothing to run
+    bool                    stalled   = false;  // ... with nothing in flight either
+    rgdn_status             error = RGDN_SUCCESS;   // first asynchronous failure
+    // statistics
+    uint64_t                framesDone = 0, framesDropped = 0, steps = 0, pixelsDone = 0, framesInSteps = 0;
+    std::vector< float >    latencies;
+    double                  busyStart = -1, busySeconds = 0;
+    uint32_t                magic = 0x52475356u;
+};
+
+namespace
+{
+
+bool valid_server( rgdn_server* s ) { return s && s->magic == 0x52475356u; }
+
+cudaEvent_t take_event( rgdn_server* sv )
+{
+    if( !sv->eventPool.empty() )
+    {
+        cudaEvent_t e = sv->eventPool.back();
+        sv->eventPool.pop_back();
+        return e;
+    }
+    cudaEvent_t e = nullptr;
+    return cudaEventCreateWithFlags( &e, cudaEventDisableTiming ) == cudaSuccess ? e : nullptr;
+}
+
+uint64_t stream_bytes( rgdn_server* sv, const ServeStream& st )
+{
+    rgdn_stream_create_info ci = { st.W, st.H, sv->info.storage };
+    uint64_t                b  = 0;
+    rgdn_stream_required_bytes( &ci, &b );
+    return b;
+}
+
+// Admission of a stream without memory (lock held). Evicts idle streams, least recently
+// used first, when the budget is short and eviction is enabled.
+bool admit( rgdn_server* sv, ServeStream& st )
+{
+    rgdn_stream_create_info ci = { st.W, st.H, sv->info.storage };
+    for( ;; )
+    {
+        rgdn_status r = rgdn_stream_create( sv->ctx, &ci, &st.s );
+        if( r == RGDN_SUCCESS )
+        {
+            st.nextFi = 0;
+            return true;
+        }
+        st.s = nullptr;
+        if( r != RGDN_OUT_OF_BUDGET || !sv->info.evictIdleMs ) return false;
+        const double t      = now_s();
+        ServeStream* victim = nullptr;
+        for( auto& kv : sv->streams )
+        {
+            ServeStream& o = kv.second;
+            if( &o == &st || !o.s || o.running || !o.queue.empty() ) continue;
+            if( ( t - o.lastUse ) * 1e3 < (double)sv->info.evictIdleMs ) continue;
+            if( !victim || o.lastUse < victim->lastUse ) victim = &o;
+        }
+        if( !victim ) return false;
+        rgdn_stream_destroy( victim->s );
+        victim->s = nullptr;
+    }
+}
+
+void record_done( rgdn_server* sv, ServeReq& r, uint32_t state, double t )
+{
+    r.state = state;
+    r.tDone = t;
+    if( state == REQ_DONE )
+    {
+        sv->framesDone++;
+        sv->latencies.push_back( (float)( ( t - r.tSubmit ) * 1e3 ) );
+    }
+    else sv->framesDropped++;
+}
+
+// Enqueues one step (no lock held). Returns the step's completion event.
+rgdn_status enqueue_step( rgdn_server* sv, StepRec& rec, std::vector< rgdn_job >& jobs, std::vector< rgdn_stream* >& sts,
+                          std::vector< ServeReq* >& rq, std::vector< cudaEvent_t >& waits )
+{
+    cudaStream_t cs = sv->lane[ rec.lane ];
+    for( cudaEvent_t e : waits )
+        if( cudaStreamWaitEvent( cs, e, 0 ) != cudaSuccess ) return RGDN_DEVICE_ERROR;
+    for( size_t k = 0; k < jobs.size(); k++ )
+    {
+        const rgdn_frame_request& q = rq[ k ]->req;
+        for( uint32_t fb = 0; fb < RGDN_GBUFFER_PLANES; fb++ )
+        {
+            if( q.gbufferMode == RGDN_REQUEST_BIND )
+            {
+                // NULL restores the stream's own plane
+                rgdn_status r = rgdn_stream_bind_framebuffer( sts[ k ], fb, jobs[ k ].frameIndex, const_cast< void* >( q.gbuffer[ fb ] ) );
+                if( r != RGDN_SUCCESS ) return r;
+                continue;
+            }
+            if( !q.gbuffer[ fb ] ) continue;
+            rgdn_image img;
+            rgdn_status r = rgdn_stream_get_framebuffer( sts[ k ], fb, jobs[ k ].frameIndex, &img );
+            if( r != RGDN_SUCCESS ) return r;
+            if( cudaMemcpyAsync( img.data, q.gbuffer[ fb ], (size_t)img.pitch_bytes * img.height, cudaMemcpyDefault, cs ) != cudaSuccess )
+                return RGDN_DEVICE_ERROR;
+        }
+    }
+    rgdn_status r = rgdn_submit_batch( sv->ctx, jobs.data(), (uint32_t)jobs.size(), (rgdn_cuda_stream)cs );
+    if( r != RGDN_SUCCESS ) return r;
+    for( size_t k = 0; k < jobs.size(); k++ )
+    {
+        if( !rq[ k ]->req.preFinalOut ) continue;
+        rgdn_image img;
+        if( ( r = rgdn_stream_get_framebuffer( sts[ k ], RGDN_FB_PRE_FINAL, jobs[ k ].frameIndex, &img ) ) != RGDN_SUCCESS ) return r;
+        if( cudaMemcpyAsync( rq[ k ]->req.preFinalOut, img.data, (size_t)img.pitch_bytes * img.height, cudaMemcpyDefault, cs ) != cudaSuccess )
+            return RGDN_DEVICE_ERROR;
+    }
+    return cudaEventRecord( rec.done, cs ) == cudaSuccess ? RGDN_SUCCESS : RGDN_DEVICE_ERROR;
+}
+
+void scheduler_loop( rgdn_server* sv )
+{
+    cudaSetDevice( sv->ctx->device );
+    const uint32_t maxFrames = sv->info.maxFramesPerStep ? std::min( sv->info.maxFramesPerStep, (uint32_t)rgdn::MAX_BATCH ) : (uint32_t)rgdn::MAX_BATCH;
+    const uint32_t inFlight  = sv->info.stepsInFlight ? std::min( sv->info.stepsInFlight, 3u ) : 2u;
+    std::unique_lock< std::mutex > lk( sv->m );
+    for( ;; )
+    {
+        sv->cvWork.wait( lk, [ & ] {
+            return sv->stop || ( !sv->arrival.empty() && sv->inflight.size() < inFlight && sv->changes != sv->stalledAt );
+        } );
+        if( sv->stop )
+        {
+            // frames that could never be admitted: dropped
+            const double t = now_s();
+            for( uint64_t tk : sv->arrival )
+            {
+                ServeReq& q = sv->reqs[ tk ];
+                sv->streams[ q.req.stream ].queue.clear();
+                record_done( sv, q, REQ_DROPPED, t );
+            }
+            sv->arrival.clear();
+            sv->cvDone.notify_all();
+            break;
+        }
+
+        // form the step
+        StepRec rec;
+        rec.index  = sv->nextStep;
+        rec.lane   = (int)( rec.index & 1 );
+        rec.pixels = 0;
+        std::vector< rgdn_job >     jobs;
+        std::vector< rgdn_stream* > sts;
+        std::vector< ServeReq* >    rq;
+        std::vector< cudaEvent_t >  waits;
+        std::vector< uint64_t >     keep;
+        bool                        full = false;
+        for( uint64_t t : sv->arrival )
+        {
+            ServeReq&    r  = sv->reqs[ t ];
+            ServeStream& st = sv->streams[ r.req.stream ];
+            const bool   oldest = st.queue.front() == t;
+            bool         take   = !full && oldest && st.lastStep != rec.index;
+            if( take && !st.s && !admit( sv, st ) ) take = false;
+            const uint64_t px = (uint64_t)st.W * st.H;
+            if( take && !jobs.empty() &&
+                ( jobs.size() >= maxFrames || ( sv->info.maxPixelsPerStep && rec.pixels + px > sv->info.maxPixelsPerStep ) ) )
+            {
+                take = false;
+                full = true;
+            }
+            if( !take )
+            {
+                keep.push_back( t );
+                continue;
+            }
+            // a step on the other lane still holding this stream must finish first
+            for( const StepRec& o : sv->inflight )
+                if( o.lane != rec.lane && o.index == st.lastStep &&
+                    std::find( waits.begin(), waits.end(), o.done ) == waits.end() )
+                    waits.push_back( o.done );
+            r.state    = REQ_RUNNING;
+            r.fi       = st.nextFi;
+            r.tEnqueue = now_s();
+            st.nextFi ^= 1u;
+            st.queue.pop_front();
+            st.running++;
+            st.lastStep = rec.index;
+            st.lastUse  = r.tEnqueue;
+            jobs.push_back( { st.s, r.fi, &r.req.params } );
+            sts.push_back( st.s );
+            rq.push_back( &r );
+            rec.tickets.push_back( t );
+            rec.streams.push_back( st.id );
+            rec.pixels += px;
+        }
+        if( jobs.empty() )
+        {
+            // nothing admissible now: wait for a change (a completion frees memory, a stream
+            // closes, a frame arrives)
+            sv->stalledAt = sv->changes;
+            sv->stalled   = sv->inflight.empty();
+            sv->cvDone.notify_all();
+            continue;
+        }
+        sv->stalled = false;
+        sv->arrival.assign( keep.begin(), keep.end() );
+        rec.done = take_event( sv );
+        sv->nextStep++;
+        lk.unlock();
+        rgdn_status r = rec.done ? enqueue_step( sv, rec, jobs, sts, rq, waits ) : RGDN_DEVICE_ERROR;
+        lk.lock();
+        if( r != RGDN_SUCCESS )
+        {
+            // the frames cannot complete: report them dropped and remember the failure
+            if( sv->error == RGDN_SUCCESS ) sv->error = r;
+            const double t = now_s();
+            for( size_t k = 0; k < rec.tickets.size(); k++ )
+            {
+                ServeReq& q = sv->reqs[ rec.tickets[ k ] ];
+                record_done( sv, q, REQ_DROPPED, t );
+                sv->streams[ rec.streams[ k ] ].running--;
+            }
+            if( rec.done ) sv->eventPool.push_back( rec.done );
+            sv->cvDone.notify_all();
+            continue;
+        }
+        if( sv->inflight.empty() ) sv->busyStart = now_s();
+        sv->inflight.push_back( std::move( rec ) );
+        sv->cvDone.notify_all();   // wakes the completion thread
+    }
+}
+
+void completion_loop( rgdn_server* sv )
+{
+    cudaSetDevice( sv->ctx->device );
+    std::unique_lock< std::mutex > lk( sv->m );
+    for( ;; )
+    {
+        sv->cvDone.wait( lk, [ & ] { return sv->stop || !sv->inflight.empty(); } );
+        if( sv->inflight.empty() )
+        {
+            if( sv->stop ) break;
+            continue;
+        }
+        cudaEvent_t e = sv->inflight.front().done;
+        lk.unlock();
+        const cudaError_t ce = cudaEventSynchronize( e );
+        const double      t  = now_s();
+        lk.lock();
+        StepRec rec = std::move( sv->inflight.front() );
+        sv->inflight.pop_front();
+        if( ce != cudaSuccess && sv->error == RGDN_SUCCESS ) sv->error = RGDN_DEVICE_ERROR;
+        for( size_t k = 0; k < rec.tickets.size(); k++ )
+        {
+            ServeReq& q = sv->reqs[ rec.tickets[ k ] ];
+            record_done( sv, q, ce == cudaSuccess ? REQ_DONE : REQ_DROPPED, t );
+            ServeStream& st = sv->streams[ rec.streams[ k ] ];
+            st.running--;
+        }
+        sv->steps++;
+        sv->framesInSteps += rec.tickets.size();
+        sv->pixelsDone += rec.pixels;
+        if( sv->inflight.empty() && sv->busyStart >= 0 )
+        {
+            sv->busySeconds += t - sv->busyStart;
+            sv->busyStart = -1;
+        }
+        sv->eventPool.push_back( rec.done );
+        sv->changes++;
+        sv->cvDone.notify_all();
+        sv->cvWork.notify_all();
+    }
+}
+
+float percentile( std::vector< float > v, double q )
+{
+    if( v.empty() ) return 0.0f;
+    std::sort( v.begin(), v.end() );
+    const size_t i = (size_t)( q * (double)( v.size() - 1 ) + 0.5 );
+    return v[ std::min( i, v.size() - 1 ) ];
+}
+
+}  // namespace
+
+extern "C" {
+
+rgdn_status rgdn_server_create( rgdn_context* ctx, const rgdn_server_create_info* info, rgdn_server** out )
+{
+    if( !rgdn::valid_ctx( ctx ) ) return RGDN_WRONG_INSTANCE;
+    if( !info || !out || info->storage > RGDN_STORAGE_BF16 || info->maxFramesPerStep > (uint32_t)rgdn::MAX_BATCH || info->stepsInFlight > 3 )
+        return RGDN_WRONG_FUNCTION_ARGUMENT;
+    cudaSetDevice( ctx->device );
+    rgdn_server* sv = new( std::nothrow ) rgdn_server();
+    if( !sv ) return RGDN_INTERNAL_ERROR;
+    sv->ctx  = ctx;
+    sv->info = *info;
+    for( int i = 0; i < 2; i++ )
+        if( cudaStreamCreateWithFlags( &sv->lane[ i ], cudaStreamNonBlocking ) != cudaSuccess )
+        {
+            for( int k = 0; k < i; k++ ) cudaStreamDestroy( sv->lane[ k ] );
+            delete sv;
+            return RGDN_DEVICE_ERROR;
+        }
+    sv->scheduler = std::thread( scheduler_loop, sv );
+    sv->completer = std::thread( completion_loop, sv );
+    *out          = sv;
+    return RGDN_SUCCESS;
+}
+
+rgdn_status rgdn_server_drain( rgdn_server* sv )
+{
+    if( !valid_server( sv ) ) return RGDN_WRONG_INSTANCE;
+    std::unique_lock< std::mutex > lk( sv->m );
+    sv->cvDone.wait( lk, [ & ] { return sv->inflight.empty() && ( sv->arrival.empty() || ( sv->stalled && sv->stalledAt == sv->changes ) ); } );
+    if( sv->error != RGDN_SUCCESS ) return sv->error;
+    // frames left waiting can run only after memory frees up (rgdn_server_close_stream)
+    return sv->arrival.empty() ? RGDN_SUCCESS : RGDN_OUT_OF_BUDGET;
+}
+
+rgdn_status rgdn_server_destroy( rgdn_server* sv )
+{
+    if( !valid_server( sv ) ) return RGDN_WRONG_INSTANCE;
+    rgdn_server_drain( sv );
+    {
+        std::lock_guard< std::mutex > g( sv->m );
+        sv->stop = true;
+    }
+    sv->cvWork.notify_all();
+    sv->cvDone.notify_all();
+    sv->scheduler.join();
+    sv->completer.join();
+    cudaSetDevice( sv->ctx->device );
+    for( auto& kv : sv->streams )
+        if( kv.second.s ) rgdn_stream_destroy( kv.second.s );
+    for( cudaEvent_t e : sv->eventPool ) cudaEventDestroy( e );
+    for( int i = 0; i < 2; i++ ) cudaStreamDestroy( sv->lane[ i ] );
+    sv->magic = 0;
+    delete sv;
+    return RGDN_SUCCESS;
+}
+
+rgdn_status rgdn_server_open_stream( rgdn_server* sv, uint32_t width, uint32_t height, uint32_t* outId )
+{
+    if( !valid_server( sv ) ) return RGDN_WRONG_INSTANCE;
+    if( !outId || width < 2 || height < 1 || ( width & 1 ) ) return RGDN_WRONG_FUNCTION_ARGUMENT;
+    std::lock_guard< std::mutex > g( sv->m );
+    ServeStream st;
+    st.id = sv->nextStreamId++;
+    st.W  = width;
+    st.H  = height;
+    sv->streams[ st.id ] = st;
+    *outId               = st.id;
+    return RGDN_SUCCESS;
+}
+
+rgdn_status rgdn_server_close_stream( rgdn_server* sv, uint32_t id )
+{
+    if( !valid_server( sv ) ) return RGDN_WRONG_INSTANCE;
+    std::unique_lock< std::mutex > lk( sv->m );
+    auto it = sv->streams.find( id );
+    if( it == sv->streams.end() || it->second.closing ) return RGDN_WRONG_FUNCTION_ARGUMENT;
+    it->second.closing = true;
+    sv->cvDone.wait( lk, [ & ] { return it->second.queue.empty() && it->second.running == 0; } );
+    if( it->second.s )
+    {
+        cudaSetDevice( sv->ctx->device );
+        rgdn_stream_destroy( it->second.s );
+    }
+    sv->streams.erase( it );
+    sv->changes++;
+    sv->cvWork.notify_all();   // memory freed: waiting admissions may proceed
+    return RGDN_SUCCESS;
+}
+
+rgdn_status rgdn_server_submit( rgdn_server* sv, const rgdn_frame_request* req, uint64_t* outTicket )
+{
+    if( !valid_server( sv ) ) return RGDN_WRONG_INSTANCE;
+    if( !req || !outTicket || req->gbufferMode > RGDN_REQUEST_BIND ) return RGDN_WRONG_FUNCTION_ARGUMENT;
+    rgdn_status r = rgdn::check_params( &req->params );
+    if( r != RGDN_SUCCESS ) return r;
+    if( req->params.flags & ( RGDN_FLAG_PLAIN | RGDN_FLAG_EXACT_MATH | RGDN_FLAG_TMA_STAGING ) ) return RGDN_WRONG_FUNCTION_ARGUMENT;
+    std::lock_guard< std::mutex > g( sv->m );
+    auto it = sv->streams.find( req->stream );
+    if( it == sv->streams.end() || it->second.closing ) return RGDN_WRONG_FUNCTION_ARGUMENT;
+    ServeStream& st = it->second;
+    const double t  = now_s();
+    // latest frames win: drop the oldest waiting frames beyond the stream's allowance
+    while( sv->info.maxQueuedPerStream && st.queue.size() >= sv->info.maxQueuedPerStream )
+    {
+        const uint64_t old = st.queue.front();
+        st.queue.pop_front();
+        sv->arrival.erase( std::find( sv->arrival.begin(), sv->arrival.end(), old ) );
+        record_done( sv, sv->reqs[ old ], REQ_DROPPED, t );
+    }
+    const uint64_t ticket = sv->nextTicket++;
+    ServeReq&      q      = sv->reqs[ ticket ];
+    q.req                 = *req;
+    q.tSubmit             = t;
+    st.queue.push_back( ticket );
+    sv->arrival.push_back( ticket );
+    *outTicket = ticket;
+    sv->changes++;
+    sv->cvWork.notify_one();
+    sv->cvDone.notify_all();
+    return RGDN_SUCCESS;
+}
+
+rgdn_status rgdn_server_wait( rgdn_server* sv, uint64_t ticket, uint32_t timeoutMs, rgdn_frame_result* out )
+{
+    if( !valid_server( sv ) ) return RGDN_WRONG_INSTANCE;
+    if( !out ) return RGDN_WRONG_FUNCTION_ARGUMENT;
+    std::unique_lock< std::mutex > lk( sv->m );
+    auto it = sv->reqs.find( ticket );
+    if( it == sv->reqs.end() ) return RGDN_WRONG_FUNCTION_ARGUMENT;
+    auto finished = [ & ] { return it->second.state == REQ_DONE || it->second.state == REQ_DROPPED; };
+    if( !sv->cvDone.wait_for( lk, std::chrono::milliseconds( timeoutMs ), finished ) ) return RGDN_TIMEOUT;
+    const ServeReq& q = it->second;
+    out->state        = q.state;
+    out->frameIndex   = q.fi;
+    out->latencyMs    = (float)( ( q.tDone - q.tSubmit ) * 1e3 );
+    out->queueMs      = q.tEnqueue > 0 ? (float)( ( q.tEnqueue - q.tSubmit ) * 1e3 ) : out->latencyMs;
+    sv->reqs.erase( it );
+    return RGDN_SUCCESS;
+}
+
+rgdn_status rgdn_server_stats_get( rgdn_server* sv, rgdn_server_stats* out )
+{
+    if( !valid_server( sv ) ) return RGDN_WRONG_INSTANCE;
+    if( !out ) return RGDN_WRONG_FUNCTION_ARGUMENT;
+    std::lock_guard< std::mutex > g( sv->m );
+    memset( out, 0, sizeof( *out ) );
+    out->framesDone    = sv->framesDone;
+    out->framesDropped = sv->framesDropped;
+    out->steps         = sv->steps;
+    out->pixelsDone    = sv->pixelsDone;
+    out->queuedFrames  = (uint32_t)sv->arrival.size();
+    for( auto& kv : sv->streams )
+        if( kv.second.s )
+        {
+            out->residentStreams++;
+            out->residentBytes += stream_bytes( sv, kv.second );
+        }
+    out->p50Ms             = percentile( sv->latencies, 0.50 );
+    out->p99Ms             = percentile( sv->latencies, 0.99 );
+    out->maxMs             = percentile( sv->latencies, 1.0 );
+    out->meanFramesPerStep = sv->steps ? (float)sv->framesInSteps / (float)sv->steps : 0.0f;
+    out->busySeconds       = sv->busySeconds + ( sv->busyStart >= 0 ? now_s() - sv->busyStart : 0.0 );
+    return RGDN_SUCCESS;
+}
+
+rgdn_status rgdn_server_stats_reset( rgdn_server* sv )
+{
+    if( !valid_server( sv ) ) return RGDN_WRONG_INSTANCE;
+    std::lock_guard< std::mutex > g( sv->m );
+    sv->framesDone = sv->framesDropped = sv->steps = sv->pixelsDone = sv->framesInSteps = 0;
+    sv->latencies.clear();
+    sv->busySeconds = 0;
+    if( sv->busyStart >= 0 ) sv->busyStart = now_s();
+    return RGDN_SUCCESS;
+}
+
+rgdn_status rgdn_server_get_stream( rgdn_server* sv, uint32_t id, rgdn_stream** out )
+{
+    if( !valid_server( sv ) ) return RGDN_WRONG_INSTANCE;
+    if( !out ) return RGDN_WRONG_FUNCTION_ARGUMENT;
+    std::lock_guard< std::mutex > g( sv->m );
+    auto it = sv->streams.find( id );
+    if( it == sv->streams.end() ) return RGDN_WRONG_FUNCTION_ARGUMENT;
+    *out = it->second.s;
+    return RGDN_SUCCESS;
+}
+
+}  // extern "C"

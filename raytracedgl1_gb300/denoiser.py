@@ -93,6 +93,25 @@ class Context:
         N.check(self.lib.rgdn_submit_batch(self.handle, arr, len(jobs), _stream_handle(cuda_stream)),
                 "rgdn_submit_batch")
 
+    def batch_config(self, storage: int) -> "N.BatchConfig":
+        cfg = N.BatchConfig()
+        N.check(self.lib.rgdn_batch_get_config(self.handle, storage, C.byref(cfg)), "rgdn_batch_get_config")
+        return cfg
+
+    def set_batch_config(self, storage: int, cfg: "N.BatchConfig") -> None:
+        N.check(self.lib.rgdn_batch_set_config(self.handle, storage, C.byref(cfg)), "rgdn_batch_set_config")
+
+    def set_batch_timing(self, enable: bool) -> None:
+        N.check(self.lib.rgdn_batch_set_timing(self.handle, 1 if enable else 0), "rgdn_batch_set_timing")
+
+    def read_batch_timing(self) -> dict:
+        """{(stage name, iteration): (launches, total ms)} of the timed batched launches."""
+        buf = (N.StageTiming * 64)()
+        n = C.c_uint32()
+        N.check(self.lib.rgdn_batch_read_timing(self.handle, buf, 64, C.byref(n)), "rgdn_batch_read_timing")
+        return {(N.KERNEL_NAMES.get(buf[i].stage, str(buf[i].stage)), buf[i].iteration): (buf[i].launches, buf[i].totalMs)
+                for i in range(min(n.value, 64))}
+
 
 def required_bytes(width: int, height: int, storage: int) -> int:
     lib = N.load()
@@ -113,10 +132,19 @@ class Stream:
         self.handle = h
         self.width, self.height, self.storage = width, height, storage
 
+    @classmethod
+    def borrowed(cls, ctx: Context, handle, width: int, height: int, storage: int) -> "Stream":
+        """A view of a stream another owner (a Server) created and destroys."""
+        s = cls.__new__(cls)
+        s.ctx, s.lib, s.handle = ctx, ctx.lib, handle
+        s.width, s.height, s.storage = width, height, storage
+        s._borrowed = True
+        return s
+
     def close(self) -> None:
-        if self.handle:
+        if self.handle and not getattr(self, "_borrowed", False):
             N.check(self.lib.rgdn_stream_destroy(self.handle), "rgdn_stream_destroy")
-            self.handle = None
+        self.handle = None
 
     def __del__(self):
         try:
@@ -247,3 +275,80 @@ def histogram_bin_table(min_log: float, max_log: float) -> np.ndarray:
     N.check(lib.rgdn_histogram_bin_table(C.c_float(min_log), C.c_float(max_log),
                                          out.ctypes.data_as(C.POINTER(C.c_uint8))))
     return out
+
+
+class Server:
+    """rgdn_server: continuous batching of frame requests from many camera streams, each
+    stream's history resident on the device, admission under the context's memory budget."""
+
+    def __init__(self, ctx: Context, storage: int, max_frames_per_step: int = 64, max_pixels_per_step: int = 0,
+                 max_queued_per_stream: int = 0, steps_in_flight: int = 2, evict_idle_ms: int = 0):
+        self.ctx, self.lib, self.storage = ctx, ctx.lib, storage
+        info = N.ServerCreateInfo(storage, max_frames_per_step, max_pixels_per_step, max_queued_per_stream,
+                                  steps_in_flight, evict_idle_ms)
+        h = C.c_void_p()
+        N.check(self.lib.rgdn_server_create(ctx.handle, C.byref(info), C.byref(h)), "rgdn_server_create")
+        self.handle = h
+        self.sizes = {}
+
+    def close(self) -> None:
+        if self.handle:
+            N.check(self.lib.rgdn_server_destroy(self.handle), "rgdn_server_destroy")
+            self.handle = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def open_stream(self, width: int, height: int) -> int:
+        v = C.c_uint32()
+        N.check(self.lib.rgdn_server_open_stream(self.handle, width, height, C.byref(v)), "rgdn_server_open_stream")
+        self.sizes[v.value] = (width, height)
+        return v.value
+
+    def close_stream(self, sid: int) -> None:
+        N.check(self.lib.rgdn_server_close_stream(self.handle, sid), "rgdn_server_close_stream")
+        self.sizes.pop(sid, None)
+
+    @staticmethod
+    def request(sid: int, params: N.FrameParams, gbuffer: dict, mode: int = N.REQUEST_COPY,
+                pre_final_out: int | None = None) -> N.FrameRequest:
+        """gbuffer: {G-buffer image name: pointer (host or device int)}."""
+        r = N.FrameRequest()
+        r.stream, r.gbufferMode = sid, mode
+        for name, ptr in gbuffer.items():
+            r.gbuffer[N.GBUFFER.index(name)] = ptr
+        r.preFinalOut = pre_final_out
+        C.memmove(C.byref(r.params), C.byref(params), C.sizeof(N.FrameParams))
+        return r
+
+    def submit(self, request: N.FrameRequest) -> int:
+        t = C.c_uint64()
+        N.check(self.lib.rgdn_server_submit(self.handle, C.byref(request), C.byref(t)), "rgdn_server_submit")
+        return t.value
+
+    def wait(self, ticket: int, timeout_ms: int = 60000) -> N.FrameResult:
+        res = N.FrameResult()
+        N.check(self.lib.rgdn_server_wait(self.handle, ticket, timeout_ms, C.byref(res)), "rgdn_server_wait")
+        return res
+
+    def drain(self) -> None:
+        N.check(self.lib.rgdn_server_drain(self.handle), "rgdn_server_drain")
+
+    def stats(self) -> dict:
+        st = N.ServerStats()
+        N.check(self.lib.rgdn_server_stats_get(self.handle, C.byref(st)), "rgdn_server_stats_get")
+        return {name: getattr(st, name) for name, _ in N.ServerStats._fields_}
+
+    def reset_stats(self) -> None:
+        N.check(self.lib.rgdn_server_stats_reset(self.handle), "rgdn_server_stats_reset")
+
+    def stream(self, sid: int) -> Optional[Stream]:
+        h = C.c_void_p()
+        N.check(self.lib.rgdn_server_get_stream(self.handle, sid, C.byref(h)), "rgdn_server_get_stream")
+        if not h.value:
+            return None
+        w, hh = self.sizes[sid]
+        return Stream.borrowed(self.ctx, h, w, hh, self.storage)
