@@ -426,7 +426,7 @@ def run_batched(args, dist: Dist, dev: int, cs) -> dict:
         "plain_path_mpix_s": round(px * steps_cmp * dist.world / (t_p / 1e3) / 1e6, 1),
         "tuned_config": {"temporal": int(cfg.temporalTile), "anti_firefly": int(cfg.antiFireflyTile),
                          "variance": int(cfg.varianceTile), "atrous": [int(v) for v in cfg.atrousTile][:args.iters],
-                         "atrous_two_blocks": [int(v) for v in cfg.atrousTwoBlocks][:args.iters],
+                         "atrous_blocks_per_sm": [int(v) for v in cfg.atrousBlocksPerSM][:args.iters],
                          "graphs": int(cfg.useGraphs), "tile_names": ["32x8", "16x16", "64x4"]},
         "kernels": kern,
     }
@@ -478,7 +478,7 @@ def run_serving(args, dist: Dist, dev: int) -> dict:
     out_host = {r: torch.empty(r[0] * r[1] * 8, dtype=torch.uint8).pin_memory() for r in SERVE_RES}
 
     def serve(hz: float, e2e: bool) -> dict:
-        sv = Server(ctx, storage, max_frames_per_step=64, max_pixels_per_step=int(args.serve_step_mpix * 1e6),
+        sv = Server(ctx, storage, max_frames_per_step=32, max_pixels_per_step=int(args.serve_step_mpix * 1e6),
                     max_queued_per_stream=1, steps_in_flight=2)
         sids = [sv.open_stream(w, h) for w, h in res]
         reqs = []

@@ -291,14 +291,15 @@ typedef struct rgdn_job
  * reference records one stream's dispatches per call (Denoiser.cpp:64-255).
  *
  * Jobs run in order; consecutive default-path jobs (no PLAIN, EXACT_MATH or TMA_STAGING
- * flag) of one storage mode on distinct streams form a step of up to 64 frames. A step is
+ * flag) of one storage mode on distinct streams form a step of up to 32 frames. A step is
  * one persistent launch per stage (gradient samples, 4 gradient a-trous, temporal
  * accumulation, anti-firefly, variance, each a-trous iteration, luminance average) whose
  * blocks loop over the tiles of all its frames; the frames' arguments are copied to the
  * device at the start of the step. Once the autotuner has settled, a step replays a captured
  * CUDA graph. Other jobs run as rgdn_denoise + rgdn_calculate_exposure. The results are those
- * of the single-stream calls, bit for bit. Up to 3 steps are in flight; a fourth waits on the
- * host for the oldest. */
+ * of the single-stream calls, bit for bit. Up to 2 steps per device are in flight (the
+ * process shares two constant-memory job tables per device); a third waits on the host for
+ * the oldest. */
 rgdn_status rgdn_submit_batch( rgdn_context* ctx, const rgdn_job* jobs, uint32_t n, rgdn_cuda_stream cudaStream );
 
 /* Tile shapes of the batched kernels (256 threads per block). */
@@ -306,17 +307,18 @@ rgdn_status rgdn_submit_batch( rgdn_context* ctx, const rgdn_job* jobs, uint32_t
 #define RGDN_TILE_16X16 1u
 #define RGDN_TILE_64X4  2u
 /* The launch configuration of batched steps for one storage mode. The autotuner starts from
- * 32x8 tiles everywhere and, over the first steps, times every candidate of every launch
- * on the work being submitted (candidates give identical results), then keeps the fastest
- * and switches to graph replay. */
+ * 32x8 tiles everywhere and, over the first 18 steps, times every candidate of every launch
+ * (tile shape; for a-trous also the register budget) on the work being submitted (candidates
+ * give identical results), then keeps the fastest and switches to graph replay. */
 typedef struct rgdn_batch_config
 {
     uint32_t temporalTile;        /* RGDN_TILE_* */
     uint32_t antiFireflyTile;
     uint32_t varianceTile;
     uint32_t atrousTile[ 6 ];     /* per a-trous iteration */
-    uint32_t atrousTwoBlocks[ 6 ];/* 1: the a-trous kernel built for 2 resident blocks per SM
-                                     (more registers per thread) instead of 3 */
+    uint32_t atrousBlocksPerSM[ 6 ];/* register budget of each a-trous iteration's kernel: built
+                                     for 2, 3 or 4 resident blocks per SM (128, 80 or 64
+                                     registers per thread); 0 = 3 */
     uint32_t useGraphs;           /* replay a captured graph per step (off while timing) */
     uint32_t tuned;               /* read: the autotuner has settled (set_config settles it) */
 } rgdn_batch_config;
@@ -340,11 +342,12 @@ typedef struct rgdn_server rgdn_server;
 typedef struct rgdn_server_create_info
 {
     uint32_t storage;            /* rgdn_storage of every stream of the server */
-    uint32_t maxFramesPerStep;   /* 1..64 (0 = 64) */
+    uint32_t maxFramesPerStep;   /* 1..32 (0 = 32) */
     uint64_t maxPixelsPerStep;   /* bound on one step's work, i.e. its latency (0 = none) */
     uint32_t maxQueuedPerStream; /* a stream's frames waiting beyond this many are dropped,
                                     oldest first (a late frame is stale); 0 = keep all */
-    uint32_t stepsInFlight;      /* steps enqueued ahead of the GPU: 1..3 (0 = 2) */
+    uint32_t stepsInFlight;      /* steps enqueued ahead of the GPU: 1..3 (0 = 2); more than 2
+                                    also wait for the two job tables of the device */
     uint32_t evictIdleMs;        /* a stream idle this long may lose its memory (and history)
                                     to admit another; 0 = never evict */
 } rgdn_server_create_info;

@@ -5,7 +5,7 @@
 // 64-255, then Tonemapping::CalculateExposure, Source/Tonemapping.cpp:59-165); a step here runs
 // the same stages in the same order for up to MAX_BATCH frames:
 //
-//   H2D copy of the step table (BatchSched + FrameArgs of every frame, pinned -> device)
+//   H2D copy of the step table (BatchConst) into the constant slot of the two kernel modules
 //   gradient samples, gradient a-trous 0..3        (frames with gradients)
 //   temporal accumulation, anti-firefly, variance  (every frame)
 //   a-trous 0 .. max(niter)-1                      (frames with niter > i; a frame's last
@@ -13,16 +13,21 @@
 //   luminance average                              (every frame)
 //
 // Every launch has a fixed grid (resident blocks per SM x SMs) and reads its tile table from
-// the step table, so the captured graph of a step is valid for any set of frames with the same
-// launch sequence; a step then costs one H2D copy and one graph launch. The host keeps up to
-// kSlots steps in flight, each with its own pinned table, device table and graph.
+// the slot, so the captured graph of a step is valid for any set of frames with the same launch
+// sequence; a step then costs the two table copies and one graph launch.
+//
+// Slots: each kernel module has BATCH_SLOTS constant slots. They and their pinned host tables
+// are a per-device resource shared by every context of the process; steps take them in turn,
+// and a step waits on the host until the slot's previous step has finished.
 //
 // Autotuning: the first steps of a storage mode time every candidate tile shape (and, for the
-// a-trous kernel, both register budgets) per launch on the frames being submitted. Candidates
+// a-trous kernel, three register budgets) per launch on the frames being submitted. Candidates
 // compute identical values per pixel, so tuning changes no result. Then the fastest candidate
 // per launch is kept and steps switch to graph replay.
 #include <algorithm>
+#include <cstddef>
 #include <cstring>
+#include <mutex>
 #include <vector>
 
 #include "rgdn_host.h"
@@ -32,37 +37,96 @@ namespace rgdn
 namespace
 {
 
-constexpr int kSlots      = 3;
-constexpr int kTuneRounds = 3;
+constexpr int kTuneRounds = 2;
 const dim3    kShapes[ 3 ] = { dim3( 32, 8 ), dim3( 16, 16 ), dim3( 64, 4 ) };
 
-size_t sched_bytes() { return ( sizeof( BatchSched ) + 255 ) & ~size_t( 255 ); }
-size_t table_bytes( int n ) { return sched_bytes() + sizeof( FrameArgs ) * (size_t)n; }
+size_t table_bytes( int n ) { return offsetof( BatchConst, jobs ) + sizeof( FrameArgs ) * (size_t)n; }
 
 // the launch sequence of a step: what a captured graph depends on
 struct GraphKey
 {
-    int storage, anyGrad, maxIter;
+    int storage, anyGrad, maxIter, gpm;
     int hm[ MAX_ATROUS_ITERATIONS ];
     int shape[ BS_COUNT ];
-    int two[ BS_COUNT ];
+    int occ[ BS_COUNT ];
 };
 bool same_key( const GraphKey& a, const GraphKey& b ) { return memcmp( &a, &b, sizeof( GraphKey ) ) == 0; }
 
-struct Slot
+// per-device constant slots and their pinned host tables
+struct DeviceSlots
 {
-    uint8_t*        host     = nullptr;   // pinned step table
-    uint8_t*        dev      = nullptr;   // device step table
-    cudaEvent_t     done     = nullptr;   // recorded after the step's last launch
-    bool            inFlight = false;
-    cudaGraphExec_t exec     = nullptr;
-    GraphKey        key;
+    std::mutex  m;
+    bool        ready = false;
+    int         next  = 0;
+    BatchConst* host[ BATCH_SLOTS ] = {};
+    cudaEvent_t done[ BATCH_SLOTS ] = {};
+    bool        used[ BATCH_SLOTS ] = {};
+    void*       mode[ 4 ][ BATCH_SLOTS ] = {};   // c_batch slot of each storage's mode module
+    void*       fast[ 4 ][ BATCH_SLOTS ] = {};   // ... and of its FAST module
 };
+constexpr int kMaxDevices = 64;
+DeviceSlots   g_slots[ kMaxDevices ];
+
+typedef cudaError_t ( *BatchLauncher )( int, int, int, dim3, int, cudaStream_t );
+typedef int ( *BpsFn )( int );
+typedef void* ( *SlotFn )( int );
+
+BatchLauncher batch_launcher( uint32_t storage, int stage )
+{
+    const bool fast = is_batch_fast_stage( stage );
+    switch( storage )
+    {
+        case RGDN_STORAGE_REF: return fast ? launch_batch_fast_ref : launch_batch_ref;
+        case RGDN_STORAGE_FP32: return fast ? launch_batch_fast_f32 : launch_batch_f32;
+        case RGDN_STORAGE_FP16: return fast ? launch_batch_fast_f16 : launch_batch_f16;
+        case RGDN_STORAGE_BF16: return fast ? launch_batch_fast_bf16 : launch_batch_bf16;
+        default: return nullptr;
+    }
+}
+BpsFn bps_fn( uint32_t storage, int stage )
+{
+    const bool fast = is_batch_fast_stage( stage & 0xff );
+    switch( storage )
+    {
+        case RGDN_STORAGE_REF: return fast ? batch_blocks_per_sm_fast_ref : batch_blocks_per_sm_ref;
+        case RGDN_STORAGE_FP32: return fast ? batch_blocks_per_sm_fast_f32 : batch_blocks_per_sm_f32;
+        case RGDN_STORAGE_FP16: return fast ? batch_blocks_per_sm_fast_f16 : batch_blocks_per_sm_f16;
+        case RGDN_STORAGE_BF16: return fast ? batch_blocks_per_sm_fast_bf16 : batch_blocks_per_sm_bf16;
+        default: return nullptr;
+    }
+}
+
+// slot set-up on the current device (lock held)
+bool slots_ready( DeviceSlots& ds )
+{
+    if( ds.ready ) return true;
+    const SlotFn modeFn[ 4 ] = { batch_slot_ref, batch_slot_f32, batch_slot_f16, batch_slot_bf16 };
+    const SlotFn fastFn[ 4 ] = { batch_slot_fast_ref, batch_slot_fast_f32, batch_slot_fast_f16, batch_slot_fast_bf16 };
+    for( int s = 0; s < BATCH_SLOTS; s++ )
+    {
+        if( !ds.host[ s ] )
+        {
+            void* p = nullptr;
+            if( cudaMallocHost( &p, sizeof( BatchConst ) ) != cudaSuccess ) return false;
+            memset( p, 0, sizeof( BatchConst ) );
+            ds.host[ s ] = static_cast< BatchConst* >( p );
+        }
+        if( !ds.done[ s ] && cudaEventCreateWithFlags( &ds.done[ s ], cudaEventDisableTiming ) != cudaSuccess ) return false;
+        for( int m = 0; m < 4; m++ )
+        {
+            ds.mode[ m ][ s ] = modeFn[ m ]( s );
+            ds.fast[ m ][ s ] = fastFn[ m ]( s );
+            if( !ds.mode[ m ][ s ] || !ds.fast[ m ][ s ] ) return false;
+        }
+    }
+    ds.ready = true;
+    return true;
+}
 
 struct Config
 {
     int  shape[ BS_COUNT ];   // index into kShapes (BS_GRADIENT stays 32x8)
-    int  two[ BS_COUNT ];     // a-trous kinds: 1 = the 2-blocks-per-SM kernel
+    int  occ[ BS_COUNT ];     // a-trous kinds: resident blocks per SM the kernel is built for (2, 3, 4)
     bool graphs;
 };
 
@@ -80,12 +144,14 @@ struct Tuner
     std::vector< Probe > probes;
 };
 
-int n_candidates( int kind ) { return kind >= BS_ATROUS0 ? 6 : kind == BS_GRADIENT ? 1 : 3; }
-int max_candidates() { return 6; }
-void candidate( int kind, int c, int& shape, int& two )
+int n_candidates( int kind ) { return kind >= BS_ATROUS0 ? 9 : kind == BS_GRADIENT ? 1 : 3; }
+int max_candidates() { return 9; }
+// candidate c of a launch kind: tile shape c % 3; for a-trous, budget 3, 2, 4 blocks per SM
+void candidate( int kind, int c, int& shape, int& occ )
 {
+    static const int kOcc[ 3 ] = { 3, 2, 4 };
     shape = kind == BS_GRADIENT ? 0 : c % 3;
-    two   = kind >= BS_ATROUS0 ? c / 3 : 0;
+    occ   = kind >= BS_ATROUS0 ? kOcc[ ( c / 3 ) % 3 ] : 0;
 }
 
 struct Pending
@@ -94,47 +160,19 @@ struct Pending
     cudaEvent_t a, b;
 };
 
-typedef cudaError_t ( *BatchLauncher )( int, int, const BatchSched*, const FrameArgs*, dim3, int, cudaStream_t );
-typedef int ( *BpsFn )( int );
-
-BatchLauncher batch_launcher( uint32_t storage, int stage )
-{
-    const bool fast = is_batch_fast_stage( stage );
-    switch( storage )
-    {
-        case RGDN_STORAGE_REF: return fast ? launch_batch_fast_ref : launch_batch_ref;
-        case RGDN_STORAGE_FP32: return fast ? launch_batch_fast_f32 : launch_batch_f32;
-        case RGDN_STORAGE_FP16: return fast ? launch_batch_fast_f16 : launch_batch_f16;
-        case RGDN_STORAGE_BF16: return fast ? launch_batch_fast_bf16 : launch_batch_bf16;
-        default: return nullptr;
-    }
-}
-BpsFn bps_fn( uint32_t storage, int stage )
-{
-    const bool fast = is_batch_fast_stage( stage );
-    switch( storage )
-    {
-        case RGDN_STORAGE_REF: return fast ? batch_blocks_per_sm_fast_ref : batch_blocks_per_sm_ref;
-        case RGDN_STORAGE_FP32: return fast ? batch_blocks_per_sm_fast_f32 : batch_blocks_per_sm_f32;
-        case RGDN_STORAGE_FP16: return fast ? batch_blocks_per_sm_fast_f16 : batch_blocks_per_sm_f16;
-        case RGDN_STORAGE_BF16: return fast ? batch_blocks_per_sm_fast_bf16 : batch_blocks_per_sm_bf16;
-        default: return nullptr;
-    }
-}
-
 int ceil_div( int a, int b ) { return ( a + b - 1 ) / b; }
 
 }  // namespace
 
 struct BatchExec
 {
-    int                        sms     = 0;
+    int                        device = 0, sms = 0;
     cudaStream_t               capture = nullptr;   // private stream the graphs are captured on
-    Slot                       slot[ kSlots ];
-    int                        next = 0;
+    cudaGraphExec_t            exec[ BATCH_SLOTS ] = {};
+    GraphKey                   key[ BATCH_SLOTS ];
     Config                     cfg[ 4 ];
     Tuner                      tuner[ 4 ];
-    int                        bps[ 4 ][ RGDN_STAGE_COUNT ][ 2 ];   // resident blocks per SM, -1 = unknown
+    int                        bps[ 4 ][ RGDN_STAGE_COUNT ][ 5 ];   // resident blocks per SM by variant, -1 = unknown
     bool                       timing = false;
     std::vector< Pending >     pending;
     std::vector< cudaEvent_t > eventPool;
@@ -155,13 +193,13 @@ cudaEvent_t take_event( BatchExec& ex )
     return cudaEventCreate( &e ) == cudaSuccess ? e : nullptr;
 }
 
-int blocks_per_sm( BatchExec& ex, uint32_t storage, int stage, int two )
+int blocks_per_sm( BatchExec& ex, uint32_t storage, int stage, int occ )
 {
-    int& v = ex.bps[ storage ][ stage ][ two ];
+    int& v = ex.bps[ storage ][ stage ][ occ ];
     if( v < 0 )
     {
         BpsFn f = bps_fn( storage, stage );
-        v       = f ? f( stage | ( two ? 0x400 : 0 ) ) : 0;
+        v       = f ? f( stage | ( occ << 10 ) ) : 0;
     }
     return v;
 }
@@ -170,20 +208,19 @@ BatchExec* create_exec( int device )
 {
     BatchExec* ex = new( std::nothrow ) BatchExec();
     if( !ex ) return nullptr;
-    bool ok = cudaDeviceGetAttribute( &ex->sms, cudaDevAttrMultiProcessorCount, device ) == cudaSuccess && ex->sms > 0;
-    ok      = ok && cudaStreamCreateWithFlags( &ex->capture, cudaStreamNonBlocking ) == cudaSuccess;
-    for( int i = 0; ok && i < kSlots; i++ )
-    {
-        ok = cudaMallocHost( &ex->slot[ i ].host, table_bytes( MAX_BATCH ) ) == cudaSuccess &&
-             cudaMalloc( &ex->slot[ i ].dev, table_bytes( MAX_BATCH ) ) == cudaSuccess &&
-             cudaEventCreateWithFlags( &ex->slot[ i ].done, cudaEventDisableTiming ) == cudaSuccess;
-        if( ok ) memset( ex->slot[ i ].host, 0, table_bytes( MAX_BATCH ) );
-    }
+    ex->device = device;
+    bool ok    = cudaDeviceGetAttribute( &ex->sms, cudaDevAttrMultiProcessorCount, device ) == cudaSuccess && ex->sms > 0;
+    ok         = ok && cudaStreamCreateWithFlags( &ex->capture, cudaStreamNonBlocking ) == cudaSuccess;
     for( int s = 0; s < 4; s++ )
     {
-        for( int k = 0; k < BS_COUNT; k++ ) ex->cfg[ s ].shape[ k ] = ex->cfg[ s ].two[ k ] = 0;
+        for( int k = 0; k < BS_COUNT; k++ )
+        {
+            ex->cfg[ s ].shape[ k ] = 0;
+            ex->cfg[ s ].occ[ k ]   = k >= BS_ATROUS0 ? 3 : 0;
+        }
         ex->cfg[ s ].graphs = true;
-        for( int st = 0; st < RGDN_STAGE_COUNT; st++ ) ex->bps[ s ][ st ][ 0 ] = ex->bps[ s ][ st ][ 1 ] = -1;
+        for( int st = 0; st < RGDN_STAGE_COUNT; st++ )
+            for( int o = 0; o < 5; o++ ) ex->bps[ s ][ st ][ o ] = -1;
     }
     if( !ok )
     {
@@ -198,15 +235,8 @@ BatchExec* create_exec( int device )
 void batch_exec_free( BatchExec* ex )
 {
     if( !ex ) return;
-    for( int i = 0; i < kSlots; i++ )
-    {
-        Slot& s = ex->slot[ i ];
-        if( s.inFlight ) cudaEventSynchronize( s.done );
-        if( s.exec ) cudaGraphExecDestroy( s.exec );
-        if( s.done ) cudaEventDestroy( s.done );
-        if( s.host ) cudaFreeHost( s.host );
-        if( s.dev ) cudaFree( s.dev );
-    }
+    for( int s = 0; s < BATCH_SLOTS; s++ )
+        if( ex->exec[ s ] ) cudaGraphExecDestroy( ex->exec[ s ] );
     for( auto& t : ex->tuner )
         for( auto& p : t.probes )
         {
@@ -228,26 +258,23 @@ void batch_exec_free( BatchExec* ex )
 namespace
 {
 
-// Enqueues the step's copy and launches on `cs`. `timed`: events around every launch, into
-// the tuner's probes (tuning) and the user's timing list (ex.timing).
-rgdn_status enqueue_step( rgdn_context* c, BatchExec& ex, const Slot& sl, const GraphKey& key, int n, const double* pixels,
+// Enqueues the step's table copies and launches on `cs` (the captured stream when capturing).
+rgdn_status enqueue_step( rgdn_context* c, BatchExec& ex, DeviceSlots& ds, int slot, const GraphKey& key, int n, const double* pixels,
                           int tuneCand, cudaStream_t cs, bool capturing )
 {
-    const uint32_t    st    = (uint32_t)key.storage;
-    const BatchSched* dsch  = reinterpret_cast< const BatchSched* >( sl.dev );
-    const FrameArgs*  djobs = reinterpret_cast< const FrameArgs* >( sl.dev + sched_bytes() );
-    // a graph copies the whole table (its node is fixed); a direct step only its n frames
-    if( cudaMemcpyAsync( sl.dev, sl.host, capturing ? table_bytes( MAX_BATCH ) : table_bytes( n ), cudaMemcpyHostToDevice, cs ) != cudaSuccess )
+    const uint32_t st    = (uint32_t)key.storage;
+    const size_t   bytes = capturing ? sizeof( BatchConst ) : table_bytes( n );
+    if( cudaMemcpyAsync( ds.mode[ st ][ slot ], ds.host[ slot ], bytes, cudaMemcpyHostToDevice, cs ) != cudaSuccess ||
+        cudaMemcpyAsync( ds.fast[ st ][ slot ], ds.host[ slot ], bytes, cudaMemcpyHostToDevice, cs ) != cudaSuccess )
         return RGDN_DEVICE_ERROR;
     Tuner&     tu     = ex.tuner[ st ];
     const bool tuning = !capturing && !tu.settled;
     const bool user   = !capturing && ex.timing;
 
-    auto run = [ & ]( int kind, int stage, int iter, int shape, int two, int cand ) -> rgdn_status {
+    auto run = [ & ]( int kind, int stage, int arg, int shape, int occ, int cand ) -> rgdn_status {
         BatchLauncher L = batch_launcher( st, stage );
         if( !L ) return RGDN_INTERNAL_ERROR;
-        const int bps  = stage == RGDN_STAGE_LUMINANCE_AVG ? 0 : blocks_per_sm( ex, st, stage, two );
-        const int grid = stage == RGDN_STAGE_LUMINANCE_AVG ? MAX_BATCH : bps * ex.sms;
+        const int grid = stage == RGDN_STAGE_LUMINANCE_AVG ? MAX_BATCH : blocks_per_sm( ex, st, stage, occ ) * ex.sms;
         if( grid <= 0 ) return RGDN_DEVICE_ERROR;
         cudaEvent_t ta = nullptr, tb = nullptr, ua = nullptr, ub = nullptr;
         if( tuning && kind >= 0 )
@@ -264,13 +291,11 @@ rgdn_status enqueue_step( rgdn_context* c, BatchExec& ex, const Slot& sl, const 
             if( !ua || !ub ) return RGDN_DEVICE_ERROR;
             cudaEventRecord( ua, cs );
         }
-        int arg = iter;
-        if( stage == RGDN_STAGE_ATROUS ) arg |= ( key.hm[ iter ] << 8 ) | ( two << 10 );
-        const cudaError_t e = L( stage, arg, dsch, djobs, kShapes[ shape ], grid, cs );
+        const cudaError_t e = L( stage, arg, slot, kShapes[ shape ], grid, cs );
         if( user )
         {
             cudaEventRecord( ub, cs );
-            ex.pending.push_back( { stage, iter, ua, ub } );
+            ex.pending.push_back( { stage, arg & 0xff, ua, ub } );
         }
         if( ta )
         {
@@ -292,12 +317,14 @@ rgdn_status enqueue_step( rgdn_context* c, BatchExec& ex, const Slot& sl, const 
     for( int k = 0; k < 3; k++ )
     {
         const int kind = BS_TEMPORAL + k;
-        if( ( r = run( kind, stages[ k ], 0, key.shape[ kind ], 0, tuneCand % n_candidates( kind ) ) ) != RGDN_SUCCESS ) return r;
+        const int arg  = k == 0 ? ( key.gpm << 8 ) : 0;
+        if( ( r = run( kind, stages[ k ], arg, key.shape[ kind ], 0, tuneCand % n_candidates( kind ) ) ) != RGDN_SUCCESS ) return r;
     }
     for( int i = 0; i < key.maxIter; i++ )
     {
         const int kind = BS_ATROUS0 + i;
-        if( ( r = run( kind, RGDN_STAGE_ATROUS, i, key.shape[ kind ], key.two[ kind ], tuneCand % n_candidates( kind ) ) ) != RGDN_SUCCESS )
+        const int arg  = i | ( key.hm[ i ] << 8 ) | ( key.occ[ kind ] << 10 );
+        if( ( r = run( kind, RGDN_STAGE_ATROUS, arg, key.shape[ kind ], key.occ[ kind ], tuneCand % n_candidates( kind ) ) ) != RGDN_SUCCESS )
             return r;
     }
     return run( -1, RGDN_STAGE_LUMINANCE_AVG, 0, 0, 0, 0 );
@@ -308,9 +335,9 @@ int kernels_in( const GraphKey& key ) { return ( key.anyGrad ? 5 : 0 ) + 3 + key
 // Picks the fastest candidate of every launch kind from the tuning steps' probes.
 rgdn_status settle( BatchExec& ex, uint32_t st )
 {
-    Tuner& tu = ex.tuner[ st ];
+    Tuner&                tu = ex.tuner[ st ];
     std::vector< double > best( BS_COUNT * max_candidates(), 1e30 );
-    rgdn_status r = RGDN_SUCCESS;
+    rgdn_status           r = RGDN_SUCCESS;
     for( auto& p : tu.probes )
     {
         float ms = 0.0f;
@@ -331,7 +358,7 @@ rgdn_status settle( BatchExec& ex, uint32_t st )
             if( best[ kind * max_candidates() + cnd ] < best[ kind * max_candidates() + bestC ] ) bestC = cnd;
         // kinds no tuning step ran (more iterations later) keep their configuration
         if( best[ kind * max_candidates() + bestC ] >= 1e30 ) continue;
-        candidate( kind, bestC, ex.cfg[ st ].shape[ kind ], ex.cfg[ st ].two[ kind ] );
+        candidate( kind, bestC, ex.cfg[ st ].shape[ kind ], ex.cfg[ st ].occ[ kind ] );
     }
     tu.settled = true;
     return r;
@@ -346,28 +373,32 @@ bool batchable( const rgdn_job& j )
 rgdn_status run_step( rgdn_context* c, BatchExec& ex, const rgdn_job* jobs, int n, cudaStream_t cs )
 {
     const uint32_t st = jobs[ 0 ].stream->storage;
-    Slot&          sl = ex.slot[ ex.next ];
-    ex.next           = ( ex.next + 1 ) % kSlots;
-    if( sl.inFlight )
+    if( ex.device < 0 || ex.device >= kMaxDevices ) return RGDN_DEVICE_ERROR;
+    DeviceSlots&                  ds = g_slots[ ex.device ];
+    std::lock_guard< std::mutex > g( ds.m );
+    if( !slots_ready( ds ) ) return RGDN_DEVICE_ERROR;
+    const int slot = ds.next;
+    ds.next        = ( ds.next + 1 ) % BATCH_SLOTS;
+    if( ds.used[ slot ] )
     {
-        // the slot's previous step must have read its table before the host rewrites it
-        if( cudaEventSynchronize( sl.done ) != cudaSuccess ) return RGDN_DEVICE_ERROR;
-        sl.inFlight = false;
+        // the slot's previous step must be done with its constant slot and host table
+        if( cudaEventSynchronize( ds.done[ slot ] ) != cudaSuccess ) return RGDN_DEVICE_ERROR;
+        ds.used[ slot ] = false;
     }
-    Tuner&       tu     = ex.tuner[ st ];
-    const bool   tuning = !tu.settled;
-    const int    tcand  = tu.step;
-    Config       cfg    = ex.cfg[ st ];
+    Tuner&     tu     = ex.tuner[ st ];
+    const bool tuning = !tu.settled;
+    const int  tcand  = tu.step;
+    Config     cfg    = ex.cfg[ st ];
     if( tuning )
-        for( int kind = BS_TEMPORAL; kind < BS_COUNT; kind++ ) candidate( kind, tcand % n_candidates( kind ), cfg.shape[ kind ], cfg.two[ kind ] );
+        for( int kind = BS_TEMPORAL; kind < BS_COUNT; kind++ ) candidate( kind, tcand % n_candidates( kind ), cfg.shape[ kind ], cfg.occ[ kind ] );
 
-    BatchSched* sch = reinterpret_cast< BatchSched* >( sl.host );
-    FrameArgs*  fa  = reinterpret_cast< FrameArgs* >( sl.host + sched_bytes() );
-    memset( sch, 0, sizeof( BatchSched ) );
-    sch->n = n;
+    BatchConst* tab = ds.host[ slot ];
+    memset( tab, 0, offsetof( BatchConst, jobs ) );
+    tab->n = n;
     GraphKey key;
     memset( &key, 0, sizeof( key ) );
     key.storage = (int)st;
+    int gpValid = 0;
     for( int k = 0; k < n; k++ )
     {
         rgdn_stream*             s  = jobs[ k ].stream;
@@ -375,13 +406,16 @@ rgdn_status run_step( rgdn_context* c, BatchExec& ex, const rgdn_job* jobs, int 
         const rgdn_frame_params* p  = jobs[ k ].params;
         rgdn_status              r  = ensure_bin_lut( s, p, cs );
         if( r != RGDN_SUCCESS ) return r;
-        fill_args( s, fi, p, fa[ k ] );
-        sch->jobFlags[ k ] = ( s->geomValid[ fi ^ 1u ] ? BATCH_JOB_GEOM_PREV : 0u ) | ( s->histPending ? BATCH_JOB_CLEAR_HIST : 0u );
+        fill_args( s, fi, p, tab->jobs[ k ] );
+        const bool gp      = s->geomValid[ fi ^ 1u ];
+        tab->jobFlags[ k ] = ( gp ? BATCH_JOB_GEOM_PREV : 0u ) | ( s->histPending ? BATCH_JOB_CLEAR_HIST : 0u );
+        gpValid += gp ? 1 : 0;
         s->geomValid[ fi ] = true;
         s->histPending     = false;
-        key.maxIter        = std::max( key.maxIter, (int)fa[ k ].u.niter );
+        key.maxIter        = std::max( key.maxIter, (int)tab->jobs[ k ].u.niter );
         if( !( p->flags & RGDN_FLAG_SKIP_GRADIENTS ) ) key.anyGrad = 1;
     }
+    key.gpm = gpValid == 0 ? 0 : gpValid == n ? 1 : 2;
     // tile tables and pixels per launch kind
     double pixels[ BS_COUNT ] = {};
     for( int kind = 0; kind < BS_COUNT; kind++ )
@@ -390,8 +424,8 @@ rgdn_status run_step( rgdn_context* c, BatchExec& ex, const rgdn_job* jobs, int 
         int        acc = 0;
         for( int k = 0; k < n; k++ )
         {
-            sch->tiles[ kind ].start[ k ] = acc;
-            const Uniform& u = fa[ k ].u;
+            tab->start[ kind ][ k ] = acc;
+            const Uniform& u        = tab->jobs[ k ].u;
             bool           runs;
             if( kind == BS_GRADIENT ) runs = !( u.flags & RGDN_FLAG_SKIP_GRADIENTS );
             else if( kind >= BS_ATROUS0 ) runs = (int)u.niter > kind - BS_ATROUS0;
@@ -401,63 +435,64 @@ rgdn_status run_step( rgdn_context* c, BatchExec& ex, const rgdn_job* jobs, int 
             acc += ceil_div( w, (int)sh.x ) * ceil_div( h, (int)sh.y );
             pixels[ kind ] += (double)w * h;
         }
-        sch->tiles[ kind ].start[ n ] = acc;
+        tab->start[ kind ][ n ] = acc;
     }
     for( int i = 0; i < key.maxIter; i++ )
     {
         int runs = 0, last = 0;
         for( int k = 0; k < n; k++ )
         {
-            if( (int)fa[ k ].u.niter > i ) runs++;
-            if( (int)fa[ k ].u.niter == i + 1 ) last++;
+            if( (int)tab->jobs[ k ].u.niter > i ) runs++;
+            if( (int)tab->jobs[ k ].u.niter == i + 1 ) last++;
         }
         key.hm[ i ] = last == 0 ? 0 : last == runs ? 1 : 2;
     }
     for( int kind = 0; kind < BS_COUNT; kind++ )
     {
         key.shape[ kind ] = kind == BS_GRADIENT ? 0 : cfg.shape[ kind ];
-        key.two[ kind ]   = cfg.two[ kind ];
+        key.occ[ kind ]   = cfg.occ[ kind ];
     }
 
     rgdn_status r = RGDN_SUCCESS;
     if( cfg.graphs && !tuning && !ex.timing )
     {
-        if( !sl.exec || !same_key( sl.key, key ) )
+        cudaGraphExec_t& exec = ex.exec[ slot ];
+        if( !exec || !same_key( ex.key[ slot ], key ) )
         {
             cudaGraph_t g = nullptr;
             if( cudaStreamBeginCapture( ex.capture, cudaStreamCaptureModeThreadLocal ) != cudaSuccess ) return RGDN_DEVICE_ERROR;
-            r                 = enqueue_step( c, ex, sl, key, n, pixels, 0, ex.capture, true );
-            cudaError_t e     = cudaStreamEndCapture( ex.capture, &g );
+            r             = enqueue_step( c, ex, ds, slot, key, n, pixels, 0, ex.capture, true );
+            cudaError_t e = cudaStreamEndCapture( ex.capture, &g );
             if( r == RGDN_SUCCESS && e != cudaSuccess ) r = RGDN_DEVICE_ERROR;
             if( r == RGDN_SUCCESS )
             {
-                if( sl.exec )
+                if( exec )
                 {
                     cudaGraphExecUpdateResultInfo info;
-                    if( cudaGraphExecUpdate( sl.exec, g, &info ) != cudaSuccess )
+                    if( cudaGraphExecUpdate( exec, g, &info ) != cudaSuccess )
                     {
                         cudaGetLastError();
-                        cudaGraphExecDestroy( sl.exec );
-                        sl.exec = nullptr;
+                        cudaGraphExecDestroy( exec );
+                        exec = nullptr;
                     }
                 }
-                if( !sl.exec && cudaGraphInstantiate( &sl.exec, g, 0 ) != cudaSuccess )
+                if( !exec && cudaGraphInstantiate( &exec, g, 0 ) != cudaSuccess )
                 {
-                    sl.exec = nullptr;
-                    r       = RGDN_DEVICE_ERROR;
+                    exec = nullptr;
+                    r    = RGDN_DEVICE_ERROR;
                 }
-                sl.key = key;
+                ex.key[ slot ] = key;
             }
             if( g ) cudaGraphDestroy( g );
             if( r != RGDN_SUCCESS ) return r;
         }
-        if( cudaGraphLaunch( sl.exec, cs ) != cudaSuccess ) return RGDN_DEVICE_ERROR;
+        if( cudaGraphLaunch( exec, cs ) != cudaSuccess ) return RGDN_DEVICE_ERROR;
         c->launches.fetch_add( (uint64_t)kernels_in( key ), std::memory_order_relaxed );
     }
-    else if( ( r = enqueue_step( c, ex, sl, key, n, pixels, tcand, cs, false ) ) != RGDN_SUCCESS )
+    else if( ( r = enqueue_step( c, ex, ds, slot, key, n, pixels, tcand, cs, false ) ) != RGDN_SUCCESS )
         return r;
-    if( cudaEventRecord( sl.done, cs ) != cudaSuccess ) return RGDN_DEVICE_ERROR;
-    sl.inFlight = true;
+    if( cudaEventRecord( ds.done[ slot ], cs ) != cudaSuccess ) return RGDN_DEVICE_ERROR;
+    ds.used[ slot ] = true;
     if( tuning && ++tu.step >= kTuneRounds * max_candidates() ) r = settle( ex, st );
     return r;
 }
@@ -506,6 +541,14 @@ rgdn_status batch_submit( rgdn_context* c, const rgdn_job* jobs, uint32_t n, cud
 void batch_destroy( rgdn_context* c )
 {
     std::lock_guard< std::mutex > g( c->batchMtx );
+    if( c->batch && c->batch->device >= 0 && c->batch->device < kMaxDevices )
+    {
+        // steps of this context may still use the device's slots
+        DeviceSlots&                  ds = g_slots[ c->batch->device ];
+        std::lock_guard< std::mutex > gs( ds.m );
+        for( int s = 0; s < BATCH_SLOTS; s++ )
+            if( ds.used[ s ] ) cudaEventSynchronize( ds.done[ s ] );
+    }
     batch_exec_free( c->batch );
     c->batch = nullptr;
 }
@@ -522,8 +565,8 @@ rgdn_status batch_get_config( rgdn_context* c, uint32_t storage, rgdn_batch_conf
     out->varianceTile    = (uint32_t)cf.shape[ BS_VARIANCE ];
     for( int i = 0; i < MAX_ATROUS_ITERATIONS; i++ )
     {
-        out->atrousTile[ i ]      = (uint32_t)cf.shape[ BS_ATROUS0 + i ];
-        out->atrousTwoBlocks[ i ] = (uint32_t)cf.two[ BS_ATROUS0 + i ];
+        out->atrousTile[ i ]        = (uint32_t)cf.shape[ BS_ATROUS0 + i ];
+        out->atrousBlocksPerSM[ i ] = (uint32_t)cf.occ[ BS_ATROUS0 + i ];
     }
     out->useGraphs = cf.graphs ? 1u : 0u;
     out->tuned     = ex->tuner[ storage ].settled ? 1u : 0u;
@@ -536,18 +579,19 @@ rgdn_status batch_set_config( rgdn_context* c, uint32_t storage, const rgdn_batc
     if( !ok_shape( in->temporalTile ) || !ok_shape( in->antiFireflyTile ) || !ok_shape( in->varianceTile ) )
         return RGDN_WRONG_FUNCTION_ARGUMENT;
     for( int i = 0; i < MAX_ATROUS_ITERATIONS; i++ )
-        if( !ok_shape( in->atrousTile[ i ] ) || in->atrousTwoBlocks[ i ] > 1 ) return RGDN_WRONG_FUNCTION_ARGUMENT;
+        if( !ok_shape( in->atrousTile[ i ] ) || ( in->atrousBlocksPerSM[ i ] && ( in->atrousBlocksPerSM[ i ] < 2 || in->atrousBlocksPerSM[ i ] > 4 ) ) )
+            return RGDN_WRONG_FUNCTION_ARGUMENT;
     std::lock_guard< std::mutex > g( c->batchMtx );
     BatchExec*                    ex = exec_of( c );
     if( !ex ) return RGDN_DEVICE_ERROR;
-    Config& cf                   = ex->cfg[ storage ];
-    cf.shape[ BS_TEMPORAL ]      = (int)in->temporalTile;
-    cf.shape[ BS_ANTI_FIREFLY ]  = (int)in->antiFireflyTile;
-    cf.shape[ BS_VARIANCE ]      = (int)in->varianceTile;
+    Config& cf                  = ex->cfg[ storage ];
+    cf.shape[ BS_TEMPORAL ]     = (int)in->temporalTile;
+    cf.shape[ BS_ANTI_FIREFLY ] = (int)in->antiFireflyTile;
+    cf.shape[ BS_VARIANCE ]     = (int)in->varianceTile;
     for( int i = 0; i < MAX_ATROUS_ITERATIONS; i++ )
     {
         cf.shape[ BS_ATROUS0 + i ] = (int)in->atrousTile[ i ];
-        cf.two[ BS_ATROUS0 + i ]   = (int)in->atrousTwoBlocks[ i ];
+        cf.occ[ BS_ATROUS0 + i ]   = in->atrousBlocksPerSM[ i ] ? (int)in->atrousBlocksPerSM[ i ] : 3;
     }
     cf.graphs = in->useGraphs != 0;
     Tuner& tu = ex->tuner[ storage ];

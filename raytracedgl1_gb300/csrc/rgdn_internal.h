@@ -167,14 +167,20 @@ inline bool is_fast_kernel( int stage ) { return stage == KF_ATROUS_FAST || stag
 
 // ------------------------------------------------------------------------------------------
 // Batched steps: one persistent launch per stage covers the frames of many streams.
-// The step's schedule and its jobs' FrameArgs live in device memory (copied from pinned host
-// memory at the start of the step), so a captured graph of the step's launches stays valid
-// for any set of up to MAX_BATCH frames.
+//
+// A step's job table (tile tables and every frame's FrameArgs) is copied from pinned host
+// memory into one of BATCH_SLOTS __constant__ slots of each kernel module at the head of the
+// step. The kernels index their slot with a warp-uniform job index, so the compiler keeps the
+// frame arguments in uniform registers and constant-bank operands, as it does for the
+// single-frame kernels' parameters, instead of spending per-thread registers on them. A
+// captured graph of a step (two copies + the launches) is valid for any set of up to MAX_BATCH
+// frames with the same launch sequence.
 // ------------------------------------------------------------------------------------------
-constexpr int MAX_BATCH = 64;
+constexpr int MAX_BATCH   = 32;
+constexpr int BATCH_SLOTS = 2;
 
 // tile tables of a step, one per launch kind
-enum BatchSlot : int
+enum BatchKind : int
 {
     BS_GRADIENT = 0,     // gradient samples and gradient a-trous (over the 1/3-resolution image)
     BS_TEMPORAL,
@@ -184,36 +190,34 @@ enum BatchSlot : int
     BS_COUNT = BS_ATROUS0 + MAX_ATROUS_ITERATIONS
 };
 
-// Tile j of a launch belongs to the job k with start[k] <= j < start[k+1]; a job without work
-// in that launch has start[k] == start[k+1]. The tiles of one job run row-major over its image,
-// blockDim.x x blockDim.y pixels each.
-struct BatchTiles
-{
-    int start[ MAX_BATCH + 1 ];
-};
-
 constexpr uint32_t BATCH_JOB_GEOM_PREV  = 1u;   // the previous frame's geometry record is valid
 constexpr uint32_t BATCH_JOB_CLEAR_HIST = 2u;   // discard a histogram no exposure pass consumed
 
-struct BatchSched
+// Tile t of launch kind k belongs to the job j with start[k][j] <= t < start[k][j+1]; a job
+// without work in that launch has start[k][j] == start[k][j+1]. A job's tiles run row-major
+// over its image, blockDim.x x blockDim.y pixels each.
+struct BatchConst
 {
-    int        n;
-    uint32_t   jobFlags[ MAX_BATCH ];
-    BatchTiles tiles[ BS_COUNT ];
+    int       n;
+    uint32_t  jobFlags[ MAX_BATCH ];
+    int       start[ BS_COUNT ][ MAX_BATCH + 1 ];
+    FrameArgs jobs[ MAX_BATCH ];
 };
+static_assert( BATCH_SLOTS * sizeof( BatchConst ) <= 63 * 1024, "the job-table slots must fit the 64 KiB constant bank" );
 
-// One stage of a batched step: `grid` persistent blocks of `block` threads (256 in all).
-// Stages: RGDN_STAGE_GRADIENT_SAMPLES, _GRADIENT_ATROUS (iter 0..3), _TEMPORAL_ACCUMULATION,
-// _ANTI_FIREFLY, _LUMINANCE_AVG (launch_batch_*) and _VARIANCE_ESTIMATION, _ATROUS
-// (launch_batch_fast_*: the FAST translation units).
-cudaError_t launch_batch_ref( int stage, int iter, const BatchSched* sch, const FrameArgs* jobs, dim3 block, int grid, cudaStream_t s );
-cudaError_t launch_batch_f32( int stage, int iter, const BatchSched* sch, const FrameArgs* jobs, dim3 block, int grid, cudaStream_t s );
-cudaError_t launch_batch_f16( int stage, int iter, const BatchSched* sch, const FrameArgs* jobs, dim3 block, int grid, cudaStream_t s );
-cudaError_t launch_batch_bf16( int stage, int iter, const BatchSched* sch, const FrameArgs* jobs, dim3 block, int grid, cudaStream_t s );
-cudaError_t launch_batch_fast_ref( int stage, int iter, const BatchSched* sch, const FrameArgs* jobs, dim3 block, int grid, cudaStream_t s );
-cudaError_t launch_batch_fast_f32( int stage, int iter, const BatchSched* sch, const FrameArgs* jobs, dim3 block, int grid, cudaStream_t s );
-cudaError_t launch_batch_fast_f16( int stage, int iter, const BatchSched* sch, const FrameArgs* jobs, dim3 block, int grid, cudaStream_t s );
-cudaError_t launch_batch_fast_bf16( int stage, int iter, const BatchSched* sch, const FrameArgs* jobs, dim3 block, int grid, cudaStream_t s );
+// One stage of a batched step over constant slot `slot`: `grid` persistent blocks of `block`
+// threads (256 in all). Stages: RGDN_STAGE_GRADIENT_SAMPLES, _GRADIENT_ATROUS (iter 0..3),
+// _TEMPORAL_ACCUMULATION, _ANTI_FIREFLY, _LUMINANCE_AVG (launch_batch_*) and
+// _VARIANCE_ESTIMATION, _ATROUS (launch_batch_fast_*: the FAST translation units). `iter` also
+// carries launch variants in its high bits (see launch_batch_t).
+cudaError_t launch_batch_ref( int stage, int iter, int slot, dim3 block, int grid, cudaStream_t s );
+cudaError_t launch_batch_f32( int stage, int iter, int slot, dim3 block, int grid, cudaStream_t s );
+cudaError_t launch_batch_f16( int stage, int iter, int slot, dim3 block, int grid, cudaStream_t s );
+cudaError_t launch_batch_bf16( int stage, int iter, int slot, dim3 block, int grid, cudaStream_t s );
+cudaError_t launch_batch_fast_ref( int stage, int iter, int slot, dim3 block, int grid, cudaStream_t s );
+cudaError_t launch_batch_fast_f32( int stage, int iter, int slot, dim3 block, int grid, cudaStream_t s );
+cudaError_t launch_batch_fast_f16( int stage, int iter, int slot, dim3 block, int grid, cudaStream_t s );
+cudaError_t launch_batch_fast_bf16( int stage, int iter, int slot, dim3 block, int grid, cudaStream_t s );
 // resident blocks per SM of a batched stage's kernel (256-thread blocks), 0 on error
 int batch_blocks_per_sm_ref( int stage );
 int batch_blocks_per_sm_f32( int stage );
@@ -223,6 +227,15 @@ int batch_blocks_per_sm_fast_ref( int stage );
 int batch_blocks_per_sm_fast_f32( int stage );
 int batch_blocks_per_sm_fast_f16( int stage );
 int batch_blocks_per_sm_fast_bf16( int stage );
+// device address of a translation unit's constant slot (the current device), nullptr on error
+void* batch_slot_ref( int slot );
+void* batch_slot_f32( int slot );
+void* batch_slot_f16( int slot );
+void* batch_slot_bf16( int slot );
+void* batch_slot_fast_ref( int slot );
+void* batch_slot_fast_f32( int slot );
+void* batch_slot_fast_f16( int slot );
+void* batch_slot_fast_bf16( int slot );
 inline bool is_batch_fast_stage( int stage ) { return stage == RGDN_STAGE_VARIANCE_ESTIMATION || stage == RGDN_STAGE_ATROUS; }
 
 }  // namespace rgdn

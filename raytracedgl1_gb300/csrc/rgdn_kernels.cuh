@@ -1839,146 +1839,115 @@ template< int M > __global__ void __launch_bounds__( 256 ) k_luminance_avg( cons
 
 // ==========================================================================================
 // Batched steps: persistent kernels, one per stage, looping over the tiles of every frame of
-// the step. The tile tables and the frames' arguments are read from device memory.
+// the step. The step's tile tables and frame arguments are in this module's constant slot
+// c_batch[slot] (internal linkage: every translation unit has its own copy, which the host
+// fills for the kernels it launches). Every index into it is warp-uniform (derived from
+// blockIdx, gridDim and constant data), so the frame arguments live in uniform registers.
 // ==========================================================================================
+static __constant__ BatchConst c_batch[ BATCH_SLOTS ];
 
-// the job of tile t: the last k with start[k] <= t (jobs without tiles are passed over)
-__device__ __forceinline__ int batch_job( const int* start, int n, int t )
+// Runs body(args, job, tile x, tile y) for the block's tiles of launch kind `kind`: tile t of
+// the launch goes to block t mod gridDim.x. The loop runs job by job, so a job's arguments are
+// resolved once per job and the tile coordinates advance by a fixed stride without a division
+// per tile. GRAD: tiles cover the gradient image (GW x GH) instead of the render (W x H).
+// Every thread of the block runs every iteration, so body may use barriers.
+template< bool GRAD, class F > __device__ __forceinline__ void batch_tiles( const int slot, const int kind, F&& body )
 {
-    int lo = 0, hi = n - 1;
-    while( lo < hi )
+    const BatchConst& bc = c_batch[ slot ];
+    const int         n  = bc.n;
+    const int         G  = (int)gridDim.x;
+    for( int j = 0; j < n; j++ )
     {
-        const int mid = ( lo + hi + 1 ) >> 1;
-        if( start[ mid ] <= t ) lo = mid;
-        else hi = mid - 1;
-    }
-    return lo;
-}
-
-// Loads the tile table into shared memory (one barrier, which also publishes whatever the
-// caller wrote to shared memory before), then runs body(args, job, tile index within the job)
-// for the block's tiles. The job's FrameArgs are copied into shared memory `sa` whenever the
-// block moves to another job: the tile code then reads them from an address space that no
-// global store can alias. Every thread of the block runs every iteration: body may use barriers.
-template< class F >
-__device__ __forceinline__ void batch_tiles( const BatchSched* __restrict__ sch, const FrameArgs* __restrict__ jobs, int slot, int* sStart,
-                                             FrameArgs& sa, F&& body )
-{
-    static_assert( sizeof( FrameArgs ) % 16 == 0, "FrameArgs is copied as int4" );
-    const int n  = sch->n;
-    const int t  = threadIdx.y * blockDim.x + threadIdx.x;
-    const int nt = blockDim.x * blockDim.y;
-    for( int k = t; k <= n; k += nt ) sStart[ k ] = sch->tiles[ slot ].start[ k ];
-    __syncthreads();
-    if( n <= 0 ) return;
-    const int total = sStart[ n ];
-    int       cur   = -1;
-    for( int tile = blockIdx.x; tile < total; tile += gridDim.x )
-    {
-        const int j = batch_job( sStart, n, tile );
-        if( j != cur )
+        const int s0 = bc.start[ kind ][ j ], s1 = bc.start[ kind ][ j + 1 ];
+        int       r  = ( (int)blockIdx.x - s0 ) % G;
+        r            = r < 0 ? r + G : r;
+        if( s0 + r >= s1 ) continue;
+        const FrameArgs& a  = bc.jobs[ j ];
+        const int        tx = ( ( GRAD ? a.u.GW : a.u.W ) + (int)blockDim.x - 1 ) / (int)blockDim.x;
+        const int        gq = G / tx, gr = G - gq * tx;
+        int              by = r / tx, bx = r - by * tx;
+        for( int lt = r; lt < s1 - s0; lt += G )
         {
-            __syncthreads();   // the previous job's arguments are no longer read
-            const int4* src = reinterpret_cast< const int4* >( jobs + j );
-            int4*       dst = reinterpret_cast< int4* >( &sa );
-            for( int k = t; k < (int)( sizeof( FrameArgs ) / 16 ); k += nt ) dst[ k ] = __ldg( src + k );
-            __syncthreads();
-            cur = j;
+            body( a, j, bx, by );
+            bx += gr;
+            by += gq;
+            if( bx >= tx )
+            {
+                bx -= tx;
+                by++;
+            }
         }
-        body( static_cast< const FrameArgs& >( sa ), j, tile - sStart[ j ] );
     }
 }
 
-__device__ __forceinline__ int tiles_x( int w ) { return ( w + (int)blockDim.x - 1 ) / (int)blockDim.x; }
-
-template< int M > __global__ void __launch_bounds__( 256 ) kb_gradient_samples( const BatchSched* __restrict__ sch, const FrameArgs* __restrict__ jobs )
+template< int M > __global__ void __launch_bounds__( 256 ) kb_gradient_samples( const int slot )
 {
     __shared__ float u8[ 256 ];
-    __shared__ int   sStart[ MAX_BATCH + 1 ];
-    __shared__ FrameArgs sa;
     fill_u8( u8, threadIdx.y * blockDim.x + threadIdx.x );
-    batch_tiles( sch, jobs, BS_GRADIENT, sStart, sa, [ & ]( const FrameArgs& a, int, int lt ) {
-        const int tx = tiles_x( a.u.GW );
-        gradient_samples_tile< M >( a, a.disPing, lt % tx, lt / tx, u8 );
-    } );
+    __syncthreads();
+    batch_tiles< true >( slot, BS_GRADIENT, [ & ]( const FrameArgs& a, int, int bx, int by ) { gradient_samples_tile< M >( a, a.disPing, bx, by, u8 ); } );
 }
 
-template< int M > __global__ void __launch_bounds__( 256 ) kb_gradient_atrous( const BatchSched* __restrict__ sch, const FrameArgs* __restrict__ jobs, const int iter )
+template< int M > __global__ void __launch_bounds__( 256 ) kb_gradient_atrous( const int slot, const int iter )
 {
     __shared__ float u8[ 256 ];
-    __shared__ int   sStart[ MAX_BATCH + 1 ];
-    __shared__ FrameArgs sa;
     fill_u8( u8, threadIdx.y * blockDim.x + threadIdx.x );
-    batch_tiles( sch, jobs, BS_GRADIENT, sStart, sa, [ & ]( const FrameArgs& a, int, int lt ) {
-        const int tx = tiles_x( a.u.GW );
-        gradient_atrous_tile( a, iter, lt % tx, lt / tx, u8 );
-    } );
+    __syncthreads();
+    batch_tiles< true >( slot, BS_GRADIENT, [ & ]( const FrameArgs& a, int, int bx, int by ) { gradient_atrous_tile( a, iter, bx, by, u8 ); } );
 }
 
-// FAST temporal accumulation writing the geometry record; each job reads the previous
-// frame's record where it is valid. The block of a job's first tile also clears a histogram
-// that no exposure pass consumed (before the last a-trous iteration adds this frame's).
-template< int M > __global__ void __launch_bounds__( 256 ) kb_temporal( const BatchSched* __restrict__ sch, const FrameArgs* __restrict__ jobs )
+// FAST temporal accumulation writing the geometry record. GPM: 0 = no job has a valid previous
+// record, 1 = every job has one, 2 = it depends on the job. The block of a job's first tile also
+// clears a histogram that no exposure pass consumed (before the last a-trous iteration adds
+// this frame's).
+template< int M, int GPM > __global__ void __launch_bounds__( 256 ) kb_temporal( const int slot )
 {
     __shared__ float u8[ 256 ];
-    __shared__ int   sStart[ MAX_BATCH + 1 ];
-    __shared__ FrameArgs sa;
     const int t = threadIdx.y * blockDim.x + threadIdx.x;
     fill_u8( u8, t );
-    batch_tiles( sch, jobs, BS_TEMPORAL, sStart, sa, [ & ]( const FrameArgs& a, int j, int lt ) {
-        const uint32_t   f  = sch->jobFlags[ j ];
-        const int        tx = tiles_x( a.u.W );
-        if( lt == 0 && ( f & BATCH_JOB_CLEAR_HIST ) ) a.tm->histogram[ t ] = 0u;
-        if( f & BATCH_JOB_GEOM_PREV ) temporal_tile< M, true, true, true >( a, lt % tx, lt / tx, u8 );
-        else temporal_tile< M, true, true, false >( a, lt % tx, lt / tx, u8 );
+    __syncthreads();
+    batch_tiles< false >( slot, BS_TEMPORAL, [ & ]( const FrameArgs& a, int j, int bx, int by ) {
+        const uint32_t f = c_batch[ slot ].jobFlags[ j ];
+        if( bx == 0 && by == 0 && ( f & BATCH_JOB_CLEAR_HIST ) ) a.tm->histogram[ t ] = 0u;
+        if( GPM == 1 || ( GPM == 2 && ( f & BATCH_JOB_GEOM_PREV ) ) ) temporal_tile< M, true, true, true >( a, bx, by, u8 );
+        else temporal_tile< M, true, true, false >( a, bx, by, u8 );
     } );
 }
 
-template< int M > __global__ void __launch_bounds__( 256 ) kb_antifirefly( const BatchSched* __restrict__ sch, const FrameArgs* __restrict__ jobs )
+template< int M > __global__ void __launch_bounds__( 256 ) kb_antifirefly( const int slot )
 {
-    __shared__ int       sStart[ MAX_BATCH + 1 ];
-    __shared__ FrameArgs sa;
-    batch_tiles( sch, jobs, BS_ANTI_FIREFLY, sStart, sa, [ & ]( const FrameArgs& a, int, int lt ) {
-        const int tx = tiles_x( a.u.W );
-        antifirefly_fast_tile< M >( a, lt % tx, lt / tx );
-    } );
+    batch_tiles< false >( slot, BS_ANTI_FIREFLY, [ & ]( const FrameArgs& a, int, int bx, int by ) { antifirefly_fast_tile< M >( a, bx, by ); } );
 }
 
-template< int M > __global__ void __launch_bounds__( 256 ) kb_variance( const BatchSched* __restrict__ sch, const FrameArgs* __restrict__ jobs )
+template< int M > __global__ void __launch_bounds__( 256 ) kb_variance( const int slot )
 {
-    __shared__ int       sStart[ MAX_BATCH + 1 ];
-    __shared__ FrameArgs sa;
-    batch_tiles( sch, jobs, BS_VARIANCE, sStart, sa, [ & ]( const FrameArgs& a, int, int lt ) {
-        const int tx = tiles_x( a.u.W );
-        variance_geo_tile< M, true >( a, lt % tx, lt / tx );
-    } );
+    batch_tiles< false >( slot, BS_VARIANCE, [ & ]( const FrameArgs& a, int, int bx, int by ) { variance_geo_tile< M, true >( a, bx, by ); } );
 }
 
 // A-trous iteration `iter` over the jobs that run it. A job's last iteration composes PreFinal
 // and bins its HistogramInput into the block's shared histogram, which is flushed into that
 // job's tonemapping state when the block moves to another job and at the end.
 // HM: 0 = the iteration is no job's last, 1 = it is every job's last, 2 = it depends on the job.
+// MINB: resident blocks per SM the kernel is built for (the register budget).
 template< int M, int HM, int MINB >
-__global__ void __launch_bounds__( 256, MINB ) kb_atrous( const BatchSched* __restrict__ sch, const FrameArgs* __restrict__ jobs, const int iter )
+__global__ void __launch_bounds__( 256, MINB ) kb_atrous( const int slot, const int iter )
 {
     __shared__ float    u8[ 256 ];
     __shared__ uint32_t hist[ HM ? 256 : 1 ];
-    __shared__ int      sStart[ MAX_BATCH + 1 ];
-    __shared__ FrameArgs sa;
     const int t = threadIdx.y * blockDim.x + threadIdx.x;
     u8[ t ]     = (float)t / 255.0f;
     if( HM ) hist[ t ] = 0u;
+    __syncthreads();
     int  histJob = -1;
     auto flush   = [ & ]() {
         __syncthreads();
         const uint32_t c = hist[ t ];
-        if( c ) atomicAdd( &jobs[ histJob ].tm->histogram[ t ], c );
+        if( c ) atomicAdd( &c_batch[ slot ].jobs[ histJob ].tm->histogram[ t ], c );
         hist[ t ] = 0u;
         __syncthreads();
     };
-    batch_tiles( sch, jobs, BS_ATROUS0 + iter, sStart, sa, [ & ]( const FrameArgs& a, int j, int lt ) {
-        const int tx = tiles_x( a.u.W );
-        if( HM == 0 ) atrous_tile< M, true, false, true >( a, iter, lt % tx, lt / tx, u8, hist );
+    batch_tiles< false >( slot, BS_ATROUS0 + iter, [ & ]( const FrameArgs& a, int j, int bx, int by ) {
+        if( HM == 0 ) atrous_tile< M, true, false, true >( a, iter, bx, by, u8, hist );
         else if( HM == 1 || iter + 1 == (int)a.u.niter )
         {
             if( histJob != j )
@@ -1986,23 +1955,23 @@ __global__ void __launch_bounds__( 256, MINB ) kb_atrous( const BatchSched* __re
                 if( histJob >= 0 ) flush();
                 histJob = j;
             }
-            atrous_tile< M, true, true, true >( a, iter, lt % tx, lt / tx, u8, hist );
+            atrous_tile< M, true, true, true >( a, iter, bx, by, u8, hist );
         }
-        else atrous_tile< M, true, false, true >( a, iter, lt % tx, lt / tx, u8, hist );
+        else atrous_tile< M, true, false, true >( a, iter, bx, by, u8, hist );
     } );
     if( HM && histJob >= 0 ) flush();
 }
 
 // one block per job (strided), as k_luminance_avg
-template< int M > __global__ void __launch_bounds__( 256 ) kb_luminance_avg( const BatchSched* __restrict__ sch, const FrameArgs* __restrict__ jobs )
+template< int M > __global__ void __launch_bounds__( 256 ) kb_luminance_avg( const int slot )
 {
     __shared__ uint32_t sh[ 256 ];
     __shared__ uint32_t count0;
-    const int n = sch->n;
+    const int n = c_batch[ slot ].n;
     for( int j = blockIdx.x; j < n; j += gridDim.x )
     {
         __syncthreads();
-        luminance_avg_job( jobs[ j ], sh, count0 );
+        luminance_avg_job( c_batch[ slot ].jobs[ j ], sh, count0 );
     }
 }
 
@@ -2055,39 +2024,47 @@ template< int M > cudaError_t launch_fast_t( const FrameArgs& a, int stage, int 
     return cudaGetLastError();
 }
 
-template< int M > cudaError_t launch_batch_t( int stage, int iter, const BatchSched* sch, const FrameArgs* jobs, dim3 block, int grid, cudaStream_t s )
+// Batched launches. `iter` carries variants in its high bits: for the temporal pass the
+// previous-record mode GPM (bits 8-9); for a-trous the histogram mode HM (bits 8-9) and the
+// resident blocks per SM it is built for (bits 10-12: 2, 3 or 4, i.e. 128, 80 or 64 registers).
+template< int M > cudaError_t launch_batch_t( int stage, int iter, int slot, dim3 block, int grid, cudaStream_t s )
 {
+    const int v = ( iter >> 8 ) & 3, it = iter & 0xff;
     switch( stage )
     {
-        case RGDN_STAGE_GRADIENT_SAMPLES: dev::kb_gradient_samples< M ><<< grid, block, 0, s >>>( sch, jobs ); break;
-        case RGDN_STAGE_GRADIENT_ATROUS: dev::kb_gradient_atrous< M ><<< grid, block, 0, s >>>( sch, jobs, iter ); break;
-        case RGDN_STAGE_TEMPORAL_ACCUMULATION: dev::kb_temporal< M ><<< grid, block, 0, s >>>( sch, jobs ); break;
-        case RGDN_STAGE_ANTI_FIREFLY: dev::kb_antifirefly< M ><<< grid, block, 0, s >>>( sch, jobs ); break;
-        case RGDN_STAGE_LUMINANCE_AVG: dev::kb_luminance_avg< M ><<< grid, 256, 0, s >>>( sch, jobs ); break;
+        case RGDN_STAGE_GRADIENT_SAMPLES: dev::kb_gradient_samples< M ><<< grid, block, 0, s >>>( slot ); break;
+        case RGDN_STAGE_GRADIENT_ATROUS: dev::kb_gradient_atrous< M ><<< grid, block, 0, s >>>( slot, it ); break;
+        case RGDN_STAGE_TEMPORAL_ACCUMULATION:
+            if( v == 0 ) dev::kb_temporal< M, 0 ><<< grid, block, 0, s >>>( slot );
+            else if( v == 1 ) dev::kb_temporal< M, 1 ><<< grid, block, 0, s >>>( slot );
+            else dev::kb_temporal< M, 2 ><<< grid, block, 0, s >>>( slot );
+            break;
+        case RGDN_STAGE_ANTI_FIREFLY: dev::kb_antifirefly< M ><<< grid, block, 0, s >>>( slot ); break;
+        case RGDN_STAGE_LUMINANCE_AVG: dev::kb_luminance_avg< M ><<< grid, 256, 0, s >>>( slot ); break;
         default: return cudaErrorInvalidValue;
     }
     return cudaGetLastError();
 }
-template< int M > cudaError_t launch_batch_fast_t( int stage, int iter, const BatchSched* sch, const FrameArgs* jobs, dim3 block, int grid, cudaStream_t s )
+template< int M > cudaError_t launch_batch_fast_t( int stage, int iter, int slot, dim3 block, int grid, cudaStream_t s )
 {
     switch( stage )
     {
-        case RGDN_STAGE_VARIANCE_ESTIMATION: dev::kb_variance< M ><<< grid, block, 0, s >>>( sch, jobs ); break;
-        // iter carries the histogram mode (bits 8-9) and the occupancy variant (bit 10)
+        case RGDN_STAGE_VARIANCE_ESTIMATION: dev::kb_variance< M ><<< grid, block, 0, s >>>( slot ); break;
         case RGDN_STAGE_ATROUS:
         {
-            const int hm = ( iter >> 8 ) & 3, occ2 = ( iter >> 10 ) & 1, it = iter & 0xff;
-            if( occ2 )
+            const int hm = ( iter >> 8 ) & 3, occ = ( iter >> 10 ) & 7, it = iter & 0xff;
+            switch( occ * 4 + hm )
             {
-                if( hm == 0 ) dev::kb_atrous< M, 0, 2 ><<< grid, block, 0, s >>>( sch, jobs, it );
-                else if( hm == 1 ) dev::kb_atrous< M, 1, 2 ><<< grid, block, 0, s >>>( sch, jobs, it );
-                else dev::kb_atrous< M, 2, 2 ><<< grid, block, 0, s >>>( sch, jobs, it );
-            }
-            else
-            {
-                if( hm == 0 ) dev::kb_atrous< M, 0, 3 ><<< grid, block, 0, s >>>( sch, jobs, it );
-                else if( hm == 1 ) dev::kb_atrous< M, 1, 3 ><<< grid, block, 0, s >>>( sch, jobs, it );
-                else dev::kb_atrous< M, 2, 3 ><<< grid, block, 0, s >>>( sch, jobs, it );
+                case 8: dev::kb_atrous< M, 0, 2 ><<< grid, block, 0, s >>>( slot, it ); break;
+                case 9: dev::kb_atrous< M, 1, 2 ><<< grid, block, 0, s >>>( slot, it ); break;
+                case 10: dev::kb_atrous< M, 2, 2 ><<< grid, block, 0, s >>>( slot, it ); break;
+                case 12: dev::kb_atrous< M, 0, 3 ><<< grid, block, 0, s >>>( slot, it ); break;
+                case 13: dev::kb_atrous< M, 1, 3 ><<< grid, block, 0, s >>>( slot, it ); break;
+                case 14: dev::kb_atrous< M, 2, 3 ><<< grid, block, 0, s >>>( slot, it ); break;
+                case 16: dev::kb_atrous< M, 0, 4 ><<< grid, block, 0, s >>>( slot, it ); break;
+                case 17: dev::kb_atrous< M, 1, 4 ><<< grid, block, 0, s >>>( slot, it ); break;
+                case 18: dev::kb_atrous< M, 2, 4 ><<< grid, block, 0, s >>>( slot, it ); break;
+                default: return cudaErrorInvalidValue;
             }
             break;
         }
@@ -2106,7 +2083,7 @@ template< int M > int batch_blocks_per_sm_t( int stage )
     {
         case RGDN_STAGE_GRADIENT_SAMPLES: return blocks_per_sm( dev::kb_gradient_samples< M > );
         case RGDN_STAGE_GRADIENT_ATROUS: return blocks_per_sm( dev::kb_gradient_atrous< M > );
-        case RGDN_STAGE_TEMPORAL_ACCUMULATION: return blocks_per_sm( dev::kb_temporal< M > );
+        case RGDN_STAGE_TEMPORAL_ACCUMULATION: return blocks_per_sm( dev::kb_temporal< M, 2 > );
         case RGDN_STAGE_ANTI_FIREFLY: return blocks_per_sm( dev::kb_antifirefly< M > );
         case RGDN_STAGE_LUMINANCE_AVG: return blocks_per_sm( dev::kb_luminance_avg< M > );
         default: return 0;
@@ -2117,10 +2094,19 @@ template< int M > int batch_blocks_per_sm_fast_t( int stage )
     switch( stage )
     {
         case RGDN_STAGE_VARIANCE_ESTIMATION: return blocks_per_sm( dev::kb_variance< M > );
-        case RGDN_STAGE_ATROUS: return blocks_per_sm( dev::kb_atrous< M, 2, 3 > );
-        case RGDN_STAGE_ATROUS | 0x400: return blocks_per_sm( dev::kb_atrous< M, 2, 2 > );
+        case RGDN_STAGE_ATROUS | ( 2 << 10 ): return blocks_per_sm( dev::kb_atrous< M, 2, 2 > );
+        case RGDN_STAGE_ATROUS | ( 3 << 10 ): return blocks_per_sm( dev::kb_atrous< M, 2, 3 > );
+        case RGDN_STAGE_ATROUS | ( 4 << 10 ): return blocks_per_sm( dev::kb_atrous< M, 2, 4 > );
         default: return 0;
     }
+}
+// device address of this module's constant slot (for the host's copy of a step's table);
+// internal linkage, like c_batch: every translation unit answers for its own module
+static inline void* batch_slot_t( int slot )
+{
+    void* p = nullptr;
+    if( slot < 0 || slot >= BATCH_SLOTS || cudaGetSymbolAddress( &p, dev::c_batch ) != cudaSuccess ) return nullptr;
+    return static_cast< BatchConst* >( p ) + slot;
 }
 
 template< int M > cudaError_t launch_atrous_tma_t( const FrameArgs& a, int iter, bool hist, const void* maps, cudaStream_t s )

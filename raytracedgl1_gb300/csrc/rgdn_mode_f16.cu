@@ -7,9 +7,10 @@ cudaError_t launch_stage_f16( const FrameArgs& a, int stage, int iter, cudaStrea
 {
     return launch_stage_t< MODE_F16 >( a, stage, iter, s );
 }
-cudaError_t launch_batch_f16( int stage, int iter, const BatchSched* sch, const FrameArgs* jobs, dim3 block, int grid, cudaStream_t s )
+cudaError_t launch_batch_f16( int stage, int iter, int slot, dim3 block, int grid, cudaStream_t s )
 {
-    return launch_batch_t< MODE_F16 >( stage, iter, sch, jobs, block, grid, s );
+    return launch_batch_t< MODE_F16 >( stage, iter, slot, block, grid, s );
 }
+void* batch_slot_f16( int slot ) { return batch_slot_t( slot ); }
 int batch_blocks_per_sm_f16( int stage ) { return batch_blocks_per_sm_t< MODE_F16 >( stage ); }
 }  // namespace rgdn

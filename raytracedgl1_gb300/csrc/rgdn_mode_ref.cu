@@ -7,9 +7,10 @@ cudaError_t launch_stage_ref( const FrameArgs& a, int stage, int iter, cudaStrea
 {
     return launch_stage_t< MODE_REF >( a, stage, iter, s );
 }
-cudaError_t launch_batch_ref( int stage, int iter, const BatchSched* sch, const FrameArgs* jobs, dim3 block, int grid, cudaStream_t s )
+cudaError_t launch_batch_ref( int stage, int iter, int slot, dim3 block, int grid, cudaStream_t s )
 {
-    return launch_batch_t< MODE_REF >( stage, iter, sch, jobs, block, grid, s );
+    return launch_batch_t< MODE_REF >( stage, iter, slot, block, grid, s );
 }
+void* batch_slot_ref( int slot ) { return batch_slot_t( slot ); }
 int batch_blocks_per_sm_ref( int stage ) { return batch_blocks_per_sm_t< MODE_REF >( stage ); }
 }  // namespace rgdn

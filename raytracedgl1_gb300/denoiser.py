@@ -281,7 +281,7 @@ class Server:
     """rgdn_server: continuous batching of frame requests from many camera streams, each
     stream's history resident on the device, admission under the context's memory budget."""
 
-    def __init__(self, ctx: Context, storage: int, max_frames_per_step: int = 64, max_pixels_per_step: int = 0,
+    def __init__(self, ctx: Context, storage: int, max_frames_per_step: int = 0, max_pixels_per_step: int = 0,
                  max_queued_per_stream: int = 0, steps_in_flight: int = 2, evict_idle_ms: int = 0):
         self.ctx, self.lib, self.storage = ctx, ctx.lib, storage
         info = N.ServerCreateInfo(storage, max_frames_per_step, max_pixels_per_step, max_queued_per_stream,

@@ -113,19 +113,19 @@ def test_batch_splits_steps_and_falls_back():
     ctx.close()
 
 
-@pytest.mark.parametrize("shape,two", [(0, 0), (1, 1), (2, 0), (2, 1)])
-def test_batch_fixed_configs(shape, two):
+@pytest.mark.parametrize("shape,occ", [(0, 3), (1, 2), (2, 4), (2, 2), (0, 4)])
+def test_batch_fixed_configs(shape, occ):
     """A configuration set through rgdn_batch_set_config (no tuning) gives the same results."""
     ctx = Context(0)
     cfg = N.BatchConfig()
     cfg.temporalTile = cfg.antiFireflyTile = cfg.varianceTile = shape
     for i in range(6):
         cfg.atrousTile[i] = (shape + i) % 3
-        cfg.atrousTwoBlocks[i] = two
+        cfg.atrousBlocksPerSM[i] = occ
     cfg.useGraphs = 1
     ctx.set_batch_config(N.STORAGE_BF16, cfg)
     got = ctx.batch_config(N.STORAGE_BF16)
-    assert got.tuned == 1 and got.temporalTile == shape and list(got.atrousTwoBlocks) == [two] * 6
+    assert got.tuned == 1 and got.temporalTile == shape and list(got.atrousBlocksPerSM) == [occ] * 6
     sizes = SIZES[:3]
     scenes = [Scene(w, h, seed=70 + i) for i, (w, h) in enumerate(sizes)]
     seq = [Stream(ctx, w, h, N.STORAGE_BF16) for w, h in sizes]
