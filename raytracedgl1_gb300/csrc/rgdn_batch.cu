@@ -20,8 +20,8 @@
 // are a per-device resource shared by every context of the process; steps take them in turn,
 // and a step waits on the host until the slot's previous step has finished.
 //
-// Autotuning: the first steps of a storage mode time every candidate tile shape (and, for the
-// a-trous kernel, three register budgets) per launch on the frames being submitted. Candidates
+// Autotuning: the first 18 steps of a storage mode time every candidate tile shape (and, for
+// the a-trous kernel, three register budgets) per launch on the frames being submitted. Candidates
 // compute identical values per pixel, so tuning changes no result. Then the fastest candidate
 // per launch is kept and steps switch to graph replay.
 #include <algorithm>
@@ -37,7 +37,9 @@ namespace rgdn
 namespace
 {
 
-constexpr int kTuneRounds = 2;
+// tuning steps: kTuneRounds passes over the candidates; the first pass only warms up (module
+// loading, clocks) and is not scored
+constexpr int kTuneRounds = 3;
 const dim3    kShapes[ 3 ] = { dim3( 32, 8 ), dim3( 16, 16 ), dim3( 64, 4 ) };
 
 size_t table_bytes( int n ) { return offsetof( BatchConst, jobs ) + sizeof( FrameArgs ) * (size_t)n; }
@@ -135,6 +137,7 @@ struct Probe
     int         kind, cand;
     double      pixels;
     cudaEvent_t a, b;
+    bool        scored;
 };
 
 struct Tuner
@@ -144,14 +147,15 @@ struct Tuner
     std::vector< Probe > probes;
 };
 
-int n_candidates( int kind ) { return kind >= BS_ATROUS0 ? 9 : kind == BS_GRADIENT ? 1 : 3; }
-int max_candidates() { return 9; }
-// candidate c of a launch kind: tile shape c % 3; for a-trous, budget 3, 2, 4 blocks per SM
+// Candidates of a launch kind: tile shapes 32x8 and 16x16 (64x4 never won on GB300 and is
+// left to rgdn_batch_set_config); for a-trous also the budget of 3, 4 or 2 blocks per SM.
+int n_candidates( int kind ) { return kind >= BS_ATROUS0 ? 6 : kind == BS_GRADIENT ? 1 : 2; }
+int max_candidates() { return 6; }
 void candidate( int kind, int c, int& shape, int& occ )
 {
-    static const int kOcc[ 3 ] = { 3, 2, 4 };
-    shape = kind == BS_GRADIENT ? 0 : c % 3;
-    occ   = kind >= BS_ATROUS0 ? kOcc[ ( c / 3 ) % 3 ] : 0;
+    static const int kOcc[ 3 ] = { 3, 4, 2 };
+    shape = kind == BS_GRADIENT ? 0 : c % 2;
+    occ   = kind >= BS_ATROUS0 ? kOcc[ ( c / 2 ) % 3 ] : 0;
 }
 
 struct Pending
@@ -300,7 +304,7 @@ rgdn_status enqueue_step( rgdn_context* c, BatchExec& ex, DeviceSlots& ds, int s
         if( ta )
         {
             cudaEventRecord( tb, cs );
-            tu.probes.push_back( { kind, cand, pixels[ kind ], ta, tb } );
+            tu.probes.push_back( { kind, cand, pixels[ kind ], ta, tb, tuneCand >= max_candidates() } );
         }
         if( !capturing ) c->launches.fetch_add( 1, std::memory_order_relaxed );
         return cuda_status( e );
@@ -342,7 +346,7 @@ rgdn_status settle( BatchExec& ex, uint32_t st )
     {
         float ms = 0.0f;
         if( cudaEventSynchronize( p.b ) != cudaSuccess || cudaEventElapsedTime( &ms, p.a, p.b ) != cudaSuccess ) r = RGDN_DEVICE_ERROR;
-        else if( p.pixels > 0.0 )
+        else if( p.scored && p.pixels > 0.0 )
         {
             double& b = best[ p.kind * max_candidates() + p.cand ];
             b         = std::min( b, (double)ms / p.pixels );

@@ -1914,12 +1914,13 @@ template< int M, int GPM > __global__ void __launch_bounds__( 256 ) kb_temporal(
     } );
 }
 
-template< int M > __global__ void __launch_bounds__( 256 ) kb_antifirefly( const int slot )
+// register caps: the occupancy of the single-frame kernels (7 and 5 blocks of 256 per SM)
+template< int M > __global__ void __launch_bounds__( 256, 7 ) kb_antifirefly( const int slot )
 {
     batch_tiles< false >( slot, BS_ANTI_FIREFLY, [ & ]( const FrameArgs& a, int, int bx, int by ) { antifirefly_fast_tile< M >( a, bx, by ); } );
 }
 
-template< int M > __global__ void __launch_bounds__( 256 ) kb_variance( const int slot )
+template< int M > __global__ void __launch_bounds__( 256, 5 ) kb_variance( const int slot )
 {
     batch_tiles< false >( slot, BS_VARIANCE, [ & ]( const FrameArgs& a, int, int bx, int by ) { variance_geo_tile< M, true >( a, bx, by ); } );
 }
