@@ -307,7 +307,7 @@ rgdn_status rgdn_submit_batch( rgdn_context* ctx, const rgdn_job* jobs, uint32_t
 #define RGDN_TILE_16X16 1u
 #define RGDN_TILE_64X4  2u
 /* The launch configuration of batched steps for one storage mode. The autotuner starts from
- * 32x8 tiles everywhere and, over the first 18 steps, times every candidate of every launch
+ * 32x8 tiles everywhere and, over the first 12 steps, times every candidate of every launch
  * (tile shape; for a-trous also the register budget) on the work being submitted (candidates
  * give identical results), then keeps the fastest and switches to graph replay. */
 typedef struct rgdn_batch_config
@@ -317,8 +317,8 @@ typedef struct rgdn_batch_config
     uint32_t varianceTile;
     uint32_t atrousTile[ 6 ];     /* per a-trous iteration */
     uint32_t atrousBlocksPerSM[ 6 ];/* register budget of each a-trous iteration's kernel: built
-                                     for 2, 3 or 4 resident blocks per SM (128, 80 or 64
-                                     registers per thread); 0 = 3 */
+                                     for 3 or 4 resident blocks per SM (80 or 64 registers per
+                                     thread); 0 = 3 */
     uint32_t useGraphs;           /* replay a captured graph per step (off while timing) */
     uint32_t tuned;               /* read: the autotuner has settled (set_config settles it) */
 } rgdn_batch_config;

@@ -32,8 +32,10 @@ NVCC_FLAGS = ARCH + ["-lineinfo", "-O3", "--fmad=false", "-std=c++17", "-Xcompil
 CU_SOURCES = ["rgdn_api.cu", "rgdn_mode_ref.cu", "rgdn_mode_f32.cu", "rgdn_mode_f16.cu",
               "rgdn_mode_bf16.cu", "rgdn_noalloc.cu", "rgdn_batch.cu", "rgdn_serve.cu", "rgdn_fast_ref.cu", "rgdn_fast_f32.cu",
               "rgdn_fast_f16.cu", "rgdn_fast_bf16.cu"]
-# the FAST kernels carry no threshold decisions: contraction to fused multiply-add allowed
-FMAD_TRUE = {"rgdn_fast_ref.cu", "rgdn_fast_f32.cu", "rgdn_fast_f16.cu", "rgdn_fast_bf16.cu"}
+# No translation unit lets the compiler contract a*b+c on its own: where the kernels want a
+# fused multiply-add they say so (__fmaf_rn), so every instantiation of a kernel body (the
+# single-frame and the batched kernels) computes the same bits.
+FMAD_TRUE: set[str] = set()
 HEADERS = ["rgdn_internal.h", "rgdn_kernels.cuh", "rgdn_codec.h", "rgdn_host.h"]
 
 LIB_RGDN = os.path.join(LIBDIR, "librgdn.so")

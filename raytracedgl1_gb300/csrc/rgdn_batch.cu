@@ -20,8 +20,8 @@
 // are a per-device resource shared by every context of the process; steps take them in turn,
 // and a step waits on the host until the slot's previous step has finished.
 //
-// Autotuning: the first 18 steps of a storage mode time every candidate tile shape (and, for
-// the a-trous kernel, three register budgets) per launch on the frames being submitted. Candidates
+// Autotuning: the first 12 steps of a storage mode time every candidate tile shape (and, for
+// the a-trous kernel, two register budgets) per launch on the frames being submitted. Candidates
 // compute identical values per pixel, so tuning changes no result. Then the fastest candidate
 // per launch is kept and steps switch to graph replay.
 #include <algorithm>
@@ -128,7 +128,7 @@ bool slots_ready( DeviceSlots& ds )
 struct Config
 {
     int  shape[ BS_COUNT ];   // index into kShapes (BS_GRADIENT stays 32x8)
-    int  occ[ BS_COUNT ];     // a-trous kinds: resident blocks per SM the kernel is built for (2, 3, 4)
+    int  occ[ BS_COUNT ];     // a-trous kinds: resident blocks per SM the kernel is built for (3, 4)
     bool graphs;
 };
 
@@ -148,14 +148,13 @@ struct Tuner
 };
 
 // Candidates of a launch kind: tile shapes 32x8 and 16x16 (64x4 never won on GB300 and is
-// left to rgdn_batch_set_config); for a-trous also the budget of 3, 4 or 2 blocks per SM.
-int n_candidates( int kind ) { return kind >= BS_ATROUS0 ? 6 : kind == BS_GRADIENT ? 1 : 2; }
-int max_candidates() { return 6; }
+// left to rgdn_batch_set_config); for a-trous also the budget of 3 or 4 blocks per SM.
+int n_candidates( int kind ) { return kind >= BS_ATROUS0 ? 4 : kind == BS_GRADIENT ? 1 : 2; }
+int max_candidates() { return 4; }
 void candidate( int kind, int c, int& shape, int& occ )
 {
-    static const int kOcc[ 3 ] = { 3, 4, 2 };
     shape = kind == BS_GRADIENT ? 0 : c % 2;
-    occ   = kind >= BS_ATROUS0 ? kOcc[ ( c / 2 ) % 3 ] : 0;
+    occ   = kind >= BS_ATROUS0 ? 3 + ( c / 2 ) % 2 : 0;
 }
 
 struct Pending
@@ -583,7 +582,7 @@ rgdn_status batch_set_config( rgdn_context* c, uint32_t storage, const rgdn_batc
     if( !ok_shape( in->temporalTile ) || !ok_shape( in->antiFireflyTile ) || !ok_shape( in->varianceTile ) )
         return RGDN_WRONG_FUNCTION_ARGUMENT;
     for( int i = 0; i < MAX_ATROUS_ITERATIONS; i++ )
-        if( !ok_shape( in->atrousTile[ i ] ) || ( in->atrousBlocksPerSM[ i ] && ( in->atrousBlocksPerSM[ i ] < 2 || in->atrousBlocksPerSM[ i ] > 4 ) ) )
+        if( !ok_shape( in->atrousTile[ i ] ) || ( in->atrousBlocksPerSM[ i ] && ( in->atrousBlocksPerSM[ i ] < 3 || in->atrousBlocksPerSM[ i ] > 4 ) ) )
             return RGDN_WRONG_FUNCTION_ARGUMENT;
     std::lock_guard< std::mutex > g( c->batchMtx );
     BatchExec*                    ex = exec_of( c );

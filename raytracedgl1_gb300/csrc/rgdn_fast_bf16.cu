@@ -1,5 +1,5 @@
-// FAST kernels (continuous arithmetic only) for the bf16 storage mode; compiled with
-// fused multiply-add contraction.
+// FAST kernels (continuous arithmetic only: the a-trous weights and the variance) for the bf16
+// storage mode, in their own translation unit.
 #include "rgdn_kernels.cuh"
 
 namespace rgdn

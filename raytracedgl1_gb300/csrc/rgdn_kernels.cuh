@@ -122,6 +122,9 @@ template<> struct Wm< false >
     __device__ static float pow01( float x, float y ) { return powf( x, y ); }
     __device__ static float expn( float x ) { return expf( x ); }
     __device__ static float madd( float a, float b, float c ) { return a * b + c; }
+    __device__ static float lum( float3 c ) { return luminance( c ); }
+    __device__ static float dot( float3 a, float3 b ) { return dot3( a, b ); }
+    __device__ static float one_minus( float k, float x ) { return 1.0f - k * x; }
 };
 template<> struct Wm< true >
 {
@@ -138,13 +141,18 @@ template<> struct Wm< true >
         const float d = 1.0f - x;
         if( d < 0.0625f )
         {
-            const float ln = -d * ( 1.0f + d * ( 0.5f + d * ( 0.33333334f + d * ( 0.25f + d * 0.2f ) ) ) );
-            return ex2_approx( y * ln * 1.44269504088896341f );
+            const float p  = __fmaf_rn( d, __fmaf_rn( d, __fmaf_rn( d, __fmaf_rn( d, 0.2f, 0.25f ), 0.33333334f ), 0.5f ), 1.0f );
+            return ex2_approx( y * ( -d * p ) * 1.44269504088896341f );
         }
         return ex2_approx( y * log2f( x ) );
     }
     __device__ static float expn( float x ) { return ex2_approx( x * 1.44269504088896341f ); }
     __device__ static float madd( float a, float b, float c ) { return __fmaf_rn( a, b, c ); }
+    // luminance and dot products as fused multiply-add chains
+    __device__ static float lum( float3 c ) { return __fmaf_rn( 0.0721f, c.z, __fmaf_rn( 0.7154f, c.y, 0.2125f * c.x ) ); }
+    __device__ static float dot( float3 a, float3 b ) { return __fmaf_rn( a.z, b.z, __fmaf_rn( a.y, b.y, a.x * b.x ) ); }
+    // 1 - k * x
+    __device__ static float one_minus( float k, float x ) { return __fmaf_rn( -k, x, 1.0f ); }
 };
 
 // ------------------------------------------------------------------------------------------
@@ -1257,36 +1265,104 @@ __device__ __forceinline__ float4 ld_h4( const ushort4* p, int i )
 // INTERIOR: every tap of the pixel lies inside the image and inside the pixel's checkerboard
 // half, so the bounds and render-area tests are statically true (the caller checks this for
 // the whole block)
-template< int M, bool FAST, bool INTERIOR, bool GEOMIN >
-__device__ __forceinline__ void atrous_px( const FrameArgs& a, const AtrousIO& io, const int iter, const int px, const int py,
-                                           const int i, const float* u8, float3& outDiff, float& outVar, float3& outSpec,
-                                           float3& outInd )
+// The centre pixel's terms every tap's weights use, and the running sums.
+struct AtrousCtr
+{
+    float3 normal;
+    float  z, l, wLumMul, roughness, wRoughMul, nwSpec, gradDepth, rz1, rz2;
+    Area   chArea;
+};
+struct AtrousAcc
+{
+    float3 d, s, i;
+    float  var, ws, wsS, wsI;
+};
+
+// One tap (xx, yy) of the dilated 3x3 stencil (CmSVGFAtrous.comp:163-235): its edge-stopping
+// weights and its contribution to the sums. Both a-trous loops below run this same code, so
+// their results are identical.
+template< bool FAST, bool INTERIOR >
+__device__ __forceinline__ void atrous_accum( const AtrousCtr& c, AtrousAcc& acc, const int xx, const int yy, const int qx, const int qy,
+                                              const float rq, const float3 nq, const float zq, const float4 cvq, const float3 sq,
+                                              const float3 iq )
+{
+    using X = Wm< FAST >;
+    const float kern[ 2 ][ 2 ] = { { 1.0f, 0.5f }, { 0.5f, 0.25f } };
+    const float3 dq  = f3( cvq.x, cvq.y, cvq.z );
+    const float  lq  = X::lum( dq );
+    const float  nn  = fmaxf( 0.0f, X::dot( c.normal, nq ) );
+    const int    man = ( xx < 0 ? -xx : xx ) + ( yy < 0 ? -yy : yy );
+
+    const float w_z = FAST ? fabsf( c.z - zq ) * ( man == 1 ? c.rz1 : c.rz2 )
+                           : fabsf( c.z - zq ) / fmaxf( c.gradDepth * (float)man, 0.01f );
+    const float w_n = X::pow128( nn );
+    const float w_l = fabsf( c.l - lq ) * c.wLumMul;
+    float       w_r = fmaxf( 0.0f, X::one_minus( 10.0f, fabsf( c.roughness - rq ) ) ) * c.wRoughMul;
+    // pow(nn, p) is finite for nn in [0,1], so a zero w_r stays zero without it
+    if( c.nwSpec > 0.0f && w_r > 0.0f ) w_r = w_r * X::pow01( nn, c.nwSpec );
+    const float waveletW = kern[ yy < 0 ? -yy : yy ][ xx < 0 ? -xx : xx ];
+    const float insideA  = ( INTERIOR || in_area( qx, qy, c.chArea ) ) ? 1.0f : 0.0f;
+    const float wBase    = X::expn( -w_z * w_z ) * w_n * waveletW * insideA;
+    const float wDiff    = wBase * X::expn( -w_l );
+    const float wSpec    = wBase * w_r;
+    const float wInd     = wBase;
+
+    acc.d   = f3( X::madd( dq.x, wDiff, acc.d.x ), X::madd( dq.y, wDiff, acc.d.y ), X::madd( dq.z, wDiff, acc.d.z ) );
+    acc.s   = f3( X::madd( sq.x, wSpec, acc.s.x ), X::madd( sq.y, wSpec, acc.s.y ), X::madd( sq.z, wSpec, acc.s.z ) );
+    acc.i   = f3( X::madd( iq.x, wInd, acc.i.x ), X::madd( iq.y, wInd, acc.i.y ), X::madd( iq.z, wInd, acc.i.z ) );
+    acc.var = X::madd( cvq.w * wDiff, wDiff, acc.var );
+    acc.ws  = acc.ws + wDiff;
+    acc.wsS = acc.wsS + wSpec;
+    acc.wsI = acc.wsI + wInd;
+}
+
+// The centre pixel's weight terms, from its colour (acc.d), normal, depth, depth gradient (in
+// c), roughness byte, prefiltered variance and specular history length; resets the weight sums.
+template< bool FAST >
+__device__ __forceinline__ void atrous_terms( AtrousCtr& c, AtrousAcc& acc, const float* u8, const uint32_t rough8, const float prefVar,
+                                              const float hS, const int iter )
+{
+    c.l             = Wm< FAST >::lum( acc.d );
+    c.wLumMul       = 1.0f / ( 4.0f * prefVar + 0.00001f );
+    c.roughness     = u8[ rough8 ];
+    c.wRoughMul     = gclamp( c.roughness * 30.0f - (float)iter, 0.0f, 1.0f );
+    const float nws = gclamp( hS / 8.0f, 0.0f, 1.0f );
+    c.nwSpec        = gclamp( spec_power( c.roughness * c.roughness ), 8.0f, 1024.0f ) * nws;
+    // FAST: one reciprocal per tap distance class (|x|+|y| = 1 or 2)
+    c.rz1  = FAST ? 1.0f / fmaxf( c.gradDepth * 1.0f, 0.01f ) : 0.0f;
+    c.rz2  = FAST ? 1.0f / fmaxf( c.gradDepth * 2.0f, 0.01f ) : 0.0f;
+    acc.ws = acc.wsS = acc.wsI = 1.0f;
+}
+
+// The centre pixel: loads, the invalid-depth early out and the per-pixel weight terms
+// (CmSVGFAtrous_Iter0.comp:158-243 / CmSVGFAtrous.comp:71-160). Returns false when the pixel
+// keeps its own values (invalid depth).
+template< int M, bool FAST, bool GEOMIN >
+__device__ __forceinline__ bool atrous_centre( const FrameArgs& a, const AtrousIO& io, const int iter, const int px, const int py, const int i,
+                                               const float* u8, AtrousCtr& c, AtrousAcc& acc )
 {
     using S          = Sto< M >;
-    using X          = Wm< FAST >;
     const Uniform& u = a.u;
-    const int      step   = 1 << iter;
-    const Area     chArea = cb_area( u, px );
-    const float4   cv     = S::ldcv( io.diffSrc, io.varSrc, (size_t)i );
-    outDiff = f3( cv.x, cv.y, cv.z );
-    outVar  = cv.w;
-    outSpec = S::ld3( io.specSrc, (size_t)i );
-    outInd  = S::ld3( io.indirSrc, (size_t)i );
-    const Geo   gc        = GEOMIN ? geo_load( a.geom, i ) : geo_zero();
-    const float z         = GEOMIN ? geo_depth( gc ) : h2f( a.depth[ i ] );
-    const float gradDepth = h2f( a.depthGrad[ i ] );
+    c.chArea         = cb_area( u, px );
+    const float4 cv  = S::ldcv( io.diffSrc, io.varSrc, (size_t)i );
+    acc.d            = f3( cv.x, cv.y, cv.z );
+    acc.var          = cv.w;
+    acc.s            = S::ld3( io.specSrc, (size_t)i );
+    acc.i            = S::ld3( io.indirSrc, (size_t)i );
+    const Geo gc     = GEOMIN ? geo_load( a.geom, i ) : geo_zero();
+    c.z              = GEOMIN ? geo_depth( gc ) : h2f( a.depth[ i ] );
+    c.gradDepth      = h2f( a.depthGrad[ i ] );
 
-    if( z < 0.0f || z > MAX_RAY_LENGTH )
+    if( c.z < 0.0f || c.z > MAX_RAY_LENGTH )
     {
         if( iter == 0 )
         {
-            outDiff = f3( 0, 0, 0 ); outVar = 0.0f; outSpec = f3( 0, 0, 0 ); outInd = f3( 0, 0, 0 );
+            acc.d = f3( 0, 0, 0 ); acc.var = 0.0f; acc.s = f3( 0, 0, 0 ); acc.i = f3( 0, 0, 0 );
         }
-        return;
+        return false;
     }
-    const float3 normal = GEOMIN ? gc.n : decode_normal( a, a.normal[ i ] );
-    const float  l      = luminance( outDiff );
-    float        prefVar;
+    c.normal = GEOMIN ? gc.n : decode_normal( a, a.normal[ i ] );
+    float prefVar;
     if( iter == 0 )
     {
         // prefilterLuminanceVariance (CmSVGFAtrous_Iter0.comp:158-187)
@@ -1304,21 +1380,34 @@ __device__ __forceinline__ void atrous_px( const FrameArgs& a, const AtrousIO& i
         prefVar = r;
     }
     else prefVar = S::ld1( a.filtVar, (size_t)i );
+    atrous_terms< FAST >( c, acc, u8, GEOMIN ? geo_rough8( gc ) : ( a.mr[ i ] >> 8 ), prefVar, S::ld4( a.histLen, (size_t)i ).z, iter );
+    return true;
+}
 
-    const float wLumMul   = 1.0f / ( 4.0f * prefVar + 0.00001f );
-    const float roughness = u8[ GEOMIN ? geo_rough8( gc ) : ( a.mr[ i ] >> 8 ) ];
-    const float wRoughMul = gclamp( roughness * 30.0f - (float)iter, 0.0f, 1.0f );
-    const float hS        = S::ld4( a.histLen, (size_t)i ).z;
-    const float nws       = gclamp( hS / 8.0f, 0.0f, 1.0f );
-    float       nwSpec    = spec_power( roughness * roughness );
-    nwSpec                = gclamp( nwSpec, 8.0f, 1024.0f );
-    nwSpec                = nwSpec * nws;
-    // FAST: one reciprocal per tap distance class (|x|+|y| = 1 or 2)
-    const float rz1 = FAST ? 1.0f / fmaxf( gradDepth * 1.0f, 0.01f ) : 0.0f;
-    const float rz2 = FAST ? 1.0f / fmaxf( gradDepth * 2.0f, 0.01f ) : 0.0f;
+__device__ __forceinline__ void atrous_finish( AtrousAcc& acc, float3& outDiff, float& outVar, float3& outSpec, float3& outInd )
+{
+    const float inv = 1.0f / acc.ws, invS = 1.0f / acc.wsS, invI = 1.0f / acc.wsI;
+    outDiff = mul( acc.d, inv );
+    outVar  = acc.var * inv * inv;
+    outSpec = mul( acc.s, invS );
+    outInd  = mul( acc.i, invI );
+}
 
-    const float kern[ 2 ][ 2 ] = { { 1.0f, 0.5f }, { 0.5f, 0.25f } };
-    float ws = 1.0f, wsS = 1.0f, wsI = 1.0f;
+template< int M, bool FAST, bool INTERIOR, bool GEOMIN >
+__device__ __forceinline__ void atrous_px( const FrameArgs& a, const AtrousIO& io, const int iter, const int px, const int py,
+                                           const int i, const float* u8, float3& outDiff, float& outVar, float3& outSpec,
+                                           float3& outInd )
+{
+    using S          = Sto< M >;
+    const Uniform& u = a.u;
+    const int      step = 1 << iter;
+    AtrousCtr      c;
+    AtrousAcc      acc;
+    if( !atrous_centre< M, FAST, GEOMIN >( a, io, iter, px, py, i, u8, c, acc ) )
+    {
+        outDiff = acc.d; outVar = acc.var; outSpec = acc.s; outInd = acc.i;
+        return;
+    }
 #pragma unroll
     for( int yy = -1; yy <= 1; yy++ )
     {
@@ -1326,11 +1415,11 @@ __device__ __forceinline__ void atrous_px( const FrameArgs& a, const AtrousIO& i
         for( int xx = -1; xx <= 1; xx++ )
         {
             if( xx == 0 && yy == 0 ) continue;
-            const int    qx  = px + xx * step, qy = py + yy * step;
-            const bool   in  = INTERIOR || inside( u, qx, qy );
-            const int    q   = in ? qy * u.W + qx : 0;
-            float        rq, zq;
-            float3       nq;
+            const int  qx = px + xx * step, qy = py + yy * step;
+            const bool in = INTERIOR || inside( u, qx, qy );
+            const int  q  = in ? qy * u.W + qx : 0;
+            float      rq, zq;
+            float3     nq;
             if( GEOMIN )
             {
                 const Geo gq = in ? geo_load( a.geom, q ) : geo_zero();
@@ -1346,45 +1435,13 @@ __device__ __forceinline__ void atrous_px( const FrameArgs& a, const AtrousIO& i
             }
             const float3 sq  = in ? S::ld3( io.specSrc, (size_t)q ) : f3( 0, 0, 0 );
             const float4 cvq = in ? S::ldcv( io.diffSrc, io.varSrc, (size_t)q ) : make_float4( 0, 0, 0, 0 );
-            const float3 dq  = f3( cvq.x, cvq.y, cvq.z );
-            const float  lq  = luminance( dq );
-            const float  nn  = fmaxf( 0.0f, dot3( normal, nq ) );
             const float3 iq  = in ? S::ld3( io.indirSrc, (size_t)q ) : f3( 0, 0, 0 );
-            const int    man = ( xx < 0 ? -xx : xx ) + ( yy < 0 ? -yy : yy );
-
-            const float w_z = FAST ? fabsf( z - zq ) * ( man == 1 ? rz1 : rz2 )
-                                   : fabsf( z - zq ) / fmaxf( gradDepth * (float)man, 0.01f );
-            const float w_n = X::pow128( nn );
-            const float w_l = fabsf( l - lq ) * wLumMul;
-            float       w_r = fmaxf( 0.0f, 1.0f - 10.0f * fabsf( roughness - rq ) ) * wRoughMul;
-            // pow(nn, p) is finite for nn in [0,1], so a zero w_r stays zero without it
-            if( nwSpec > 0.0f && w_r > 0.0f ) w_r = w_r * X::pow01( nn, nwSpec );
-            const float waveletW = kern[ yy < 0 ? -yy : yy ][ xx < 0 ? -xx : xx ];
-            const float insideA  = ( INTERIOR || in_area( qx, qy, chArea ) ) ? 1.0f : 0.0f;
-            const float wBase    = X::expn( -w_z * w_z ) * w_n * waveletW * insideA;
-            const float wDiff    = wBase * X::expn( -w_l );
-            const float wSpec    = wBase * w_r;
-            const float wInd     = wBase;
-
-            outDiff = f3( X::madd( dq.x, wDiff, outDiff.x ), X::madd( dq.y, wDiff, outDiff.y ), X::madd( dq.z, wDiff, outDiff.z ) );
-            outSpec = f3( X::madd( sq.x, wSpec, outSpec.x ), X::madd( sq.y, wSpec, outSpec.y ), X::madd( sq.z, wSpec, outSpec.z ) );
-            outInd  = f3( X::madd( iq.x, wInd, outInd.x ), X::madd( iq.y, wInd, outInd.y ), X::madd( iq.z, wInd, outInd.z ) );
-            outVar  = X::madd( cvq.w * wDiff, wDiff, outVar );
-            ws      = ws + wDiff;
-            wsS     = wsS + wSpec;
-            wsI     = wsI + wInd;
+            atrous_accum< FAST, INTERIOR >( c, acc, xx, yy, qx, qy, rq, nq, zq, cvq, sq, iq );
         }
     }
-    const float inv = 1.0f / ws, invS = 1.0f / wsS, invI = 1.0f / wsI;
-    outDiff = mul( outDiff, inv );
-    outVar  = outVar * inv * inv;
-    outSpec = mul( outSpec, invS );
-    outInd  = mul( outInd, invI );
+    atrous_finish( acc, outDiff, outVar, outSpec, outInd );
 }
 
-// One a-trous iteration over the frame. HIST: the last iteration also accumulates the
-// luminance histogram of the HistogramInput values it writes (CmLuminanceHistogram.comp,
-// fused: no second read of the image).
 // The tile of one a-trous iteration. HIST adds the bins of this tile's HistogramInput values
 // to the block's shared histogram `hist` (the caller zeroes and flushes it).
 template< int M, bool FAST, bool HIST, bool GEOMIN >
@@ -1569,7 +1626,6 @@ __device__ __forceinline__ void atrous_px_tma( const FrameArgs& a, const AtrousI
 {
     using S          = Sto< M >;
     using L          = TmaLd< M >;
-    using X          = Wm< FAST >;
     const Uniform& u = a.u;
     const int      step = g.s;
     // shared-memory texel index of tap (dx, dy) of this thread's pixel
@@ -1584,26 +1640,28 @@ __device__ __forceinline__ void atrous_px_tma( const FrameArgs& a, const AtrousI
     const float4*  bGeo = reinterpret_cast< const float4* >( sm + g.offGeo );
     const int      k0   = kidx( 0, 0 );
     const float4   cv   = L::cv( bCv, bVar, k0 );
-    outDiff = f3( cv.x, cv.y, cv.z );
-    outVar  = cv.w;
-    outSpec = L::col( bSp, k0 );
-    outInd  = L::col( bIn, k0 );
+    AtrousCtr      c;
+    AtrousAcc      acc;
+    acc.d            = f3( cv.x, cv.y, cv.z );
+    acc.var          = cv.w;
+    acc.s            = L::col( bSp, k0 );
+    acc.i            = L::col( bIn, k0 );
     const float4 gc4 = bGeo[ k0 ];
     const Geo    gc  = { make_float3( gc4.x, gc4.y, gc4.z ), __float_as_uint( gc4.w ) };
-    const float  z   = geo_depth( gc );
-    const float  gradDepth = h2f( a.depthGrad[ i ] );
-    if( z < 0.0f || z > MAX_RAY_LENGTH )
+    c.z              = geo_depth( gc );
+    c.gradDepth      = h2f( a.depthGrad[ i ] );
+    if( c.z < 0.0f || c.z > MAX_RAY_LENGTH )
     {
         if( iter == 0 )
         {
-            outDiff = f3( 0, 0, 0 ); outVar = 0.0f; outSpec = f3( 0, 0, 0 ); outInd = f3( 0, 0, 0 );
+            acc.d = f3( 0, 0, 0 ); acc.var = 0.0f; acc.s = f3( 0, 0, 0 ); acc.i = f3( 0, 0, 0 );
         }
+        outDiff = acc.d; outVar = acc.var; outSpec = acc.s; outInd = acc.i;
         return;
     }
-    const Area   chArea = cb_area( u, px );
-    const float3 normal = gc.n;
-    const float  l      = luminance( outDiff );
-    float        prefVar;
+    c.chArea = cb_area( u, px );
+    c.normal = gc.n;
+    float prefVar;
     if( iter == 0 )
     {
         // prefilterLuminanceVariance (CmSVGFAtrous_Iter0.comp:158-187); the staged footprint
@@ -1621,20 +1679,8 @@ __device__ __forceinline__ void atrous_px_tma( const FrameArgs& a, const AtrousI
         prefVar = r;
     }
     else prefVar = S::ld1( a.filtVar, (size_t)i );
+    atrous_terms< FAST >( c, acc, u8, geo_rough8( gc ), prefVar, S::ld4( a.histLen, (size_t)i ).z, iter );
 
-    const float wLumMul   = 1.0f / ( 4.0f * prefVar + 0.00001f );
-    const float roughness = u8[ geo_rough8( gc ) ];
-    const float wRoughMul = gclamp( roughness * 30.0f - (float)iter, 0.0f, 1.0f );
-    const float hS        = S::ld4( a.histLen, (size_t)i ).z;
-    const float nws       = gclamp( hS / 8.0f, 0.0f, 1.0f );
-    float       nwSpec    = spec_power( roughness * roughness );
-    nwSpec                = gclamp( nwSpec, 8.0f, 1024.0f );
-    nwSpec                = nwSpec * nws;
-    const float rz1 = FAST ? 1.0f / fmaxf( gradDepth * 1.0f, 0.01f ) : 0.0f;
-    const float rz2 = FAST ? 1.0f / fmaxf( gradDepth * 2.0f, 0.01f ) : 0.0f;
-
-    const float kern[ 2 ][ 2 ] = { { 1.0f, 0.5f }, { 0.5f, 0.25f } };
-    float ws = 1.0f, wsS = 1.0f, wsI = 1.0f;
 #pragma unroll
     for( int yy = -1; yy <= 1; yy++ )
     {
@@ -1647,44 +1693,11 @@ __device__ __forceinline__ void atrous_px_tma( const FrameArgs& a, const AtrousI
             const float4 gq4 = bGeo[ k ];
             Geo          gq  = { make_float3( gq4.x, gq4.y, gq4.z ), __float_as_uint( gq4.w ) };
             if( !INTERIOR && !inside( u, qx, qy ) ) gq = geo_zero();
-            const float  rq  = u8[ geo_rough8( gq ) ];
-            const float3 nq  = gq.n;
-            const float  zq  = geo_depth( gq );
-            const float3 sq  = L::col( bSp, k );
-            const float4 cvq = L::cv( bCv, bVar, k );
-            const float3 dq  = f3( cvq.x, cvq.y, cvq.z );
-            const float  lq  = luminance( dq );
-            const float  nn  = fmaxf( 0.0f, dot3( normal, nq ) );
-            const float3 iq  = L::col( bIn, k );
-            const int    man = ( xx < 0 ? -xx : xx ) + ( yy < 0 ? -yy : yy );
-
-            const float w_z = FAST ? fabsf( z - zq ) * ( man == 1 ? rz1 : rz2 )
-                                   : fabsf( z - zq ) / fmaxf( gradDepth * (float)man, 0.01f );
-            const float w_n = X::pow128( nn );
-            const float w_l = fabsf( l - lq ) * wLumMul;
-            float       w_r = fmaxf( 0.0f, 1.0f - 10.0f * fabsf( roughness - rq ) ) * wRoughMul;
-            if( nwSpec > 0.0f && w_r > 0.0f ) w_r = w_r * X::pow01( nn, nwSpec );
-            const float waveletW = kern[ yy < 0 ? -yy : yy ][ xx < 0 ? -xx : xx ];
-            const float insideA  = ( INTERIOR || in_area( qx, qy, chArea ) ) ? 1.0f : 0.0f;
-            const float wBase    = X::expn( -w_z * w_z ) * w_n * waveletW * insideA;
-            const float wDiff    = wBase * X::expn( -w_l );
-            const float wSpec    = wBase * w_r;
-            const float wInd     = wBase;
-
-            outDiff = f3( X::madd( dq.x, wDiff, outDiff.x ), X::madd( dq.y, wDiff, outDiff.y ), X::madd( dq.z, wDiff, outDiff.z ) );
-            outSpec = f3( X::madd( sq.x, wSpec, outSpec.x ), X::madd( sq.y, wSpec, outSpec.y ), X::madd( sq.z, wSpec, outSpec.z ) );
-            outInd  = f3( X::madd( iq.x, wInd, outInd.x ), X::madd( iq.y, wInd, outInd.y ), X::madd( iq.z, wInd, outInd.z ) );
-            outVar  = X::madd( cvq.w * wDiff, wDiff, outVar );
-            ws      = ws + wDiff;
-            wsS     = wsS + wSpec;
-            wsI     = wsI + wInd;
+            atrous_accum< FAST, INTERIOR >( c, acc, xx, yy, qx, qy, u8[ geo_rough8( gq ) ], gq.n, geo_depth( gq ), L::cv( bCv, bVar, k ),
+                                            L::col( bSp, k ), L::col( bIn, k ) );
         }
     }
-    const float inv = 1.0f / ws, invS = 1.0f / wsS, invI = 1.0f / wsI;
-    outDiff = mul( outDiff, inv );
-    outVar  = outVar * inv * inv;
-    outSpec = mul( outSpec, invS );
-    outInd  = mul( outInd, invI );
+    atrous_finish( acc, outDiff, outVar, outSpec, outInd );
 }
 
 template< int M, bool FAST, bool HIST >
@@ -2010,7 +2023,8 @@ template< int M > cudaError_t launch_stage_t( const FrameArgs& a, int stage, int
 }
 
 // Kernels whose results are continuous in every arithmetic operation (no threshold follows
-// them): compiled in their own translation units with fused multiply-add contraction on.
+// them), in their own translation units (rgdn_fast_*.cu); their weighted sums use explicit
+// fused multiply-adds.
 template< int M > cudaError_t launch_fast_t( const FrameArgs& a, int stage, int iter, cudaStream_t s )
 {
     const dim3 blk( 32, 8 );
@@ -2027,7 +2041,7 @@ template< int M > cudaError_t launch_fast_t( const FrameArgs& a, int stage, int 
 
 // Batched launches. `iter` carries variants in its high bits: for the temporal pass the
 // previous-record mode GPM (bits 8-9); for a-trous the histogram mode HM (bits 8-9) and the
-// resident blocks per SM it is built for (bits 10-12: 2, 3 or 4, i.e. 128, 80 or 64 registers).
+// resident blocks per SM it is built for (bits 10-12: 3 or 4, i.e. 80 or 64 registers).
 template< int M > cudaError_t launch_batch_t( int stage, int iter, int slot, dim3 block, int grid, cudaStream_t s )
 {
     const int v = ( iter >> 8 ) & 3, it = iter & 0xff;
@@ -2056,9 +2070,6 @@ template< int M > cudaError_t launch_batch_fast_t( int stage, int iter, int slot
             const int hm = ( iter >> 8 ) & 3, occ = ( iter >> 10 ) & 7, it = iter & 0xff;
             switch( occ * 4 + hm )
             {
-                case 8: dev::kb_atrous< M, 0, 2 ><<< grid, block, 0, s >>>( slot, it ); break;
-                case 9: dev::kb_atrous< M, 1, 2 ><<< grid, block, 0, s >>>( slot, it ); break;
-                case 10: dev::kb_atrous< M, 2, 2 ><<< grid, block, 0, s >>>( slot, it ); break;
                 case 12: dev::kb_atrous< M, 0, 3 ><<< grid, block, 0, s >>>( slot, it ); break;
                 case 13: dev::kb_atrous< M, 1, 3 ><<< grid, block, 0, s >>>( slot, it ); break;
                 case 14: dev::kb_atrous< M, 2, 3 ><<< grid, block, 0, s >>>( slot, it ); break;
@@ -2095,7 +2106,6 @@ template< int M > int batch_blocks_per_sm_fast_t( int stage )
     switch( stage )
     {
         case RGDN_STAGE_VARIANCE_ESTIMATION: return blocks_per_sm( dev::kb_variance< M > );
-        case RGDN_STAGE_ATROUS | ( 2 << 10 ): return blocks_per_sm( dev::kb_atrous< M, 2, 2 > );
         case RGDN_STAGE_ATROUS | ( 3 << 10 ): return blocks_per_sm( dev::kb_atrous< M, 2, 3 > );
         case RGDN_STAGE_ATROUS | ( 4 << 10 ): return blocks_per_sm( dev::kb_atrous< M, 2, 4 > );
         default: return 0;
