@@ -54,8 +54,9 @@ def parse():
     ap.add_argument("--iters", type=int, default=5, help="a-trous passes")
     ap.add_argument("--frames", type=int, default=60, help="distinct frames in the sequence")
     ap.add_argument("--e2e-steps", type=int, default=120)
-    ap.add_argument("--path", default="fused", choices=["fused", "plain"],
-                    help="fused: the default kernels; plain: one kernel per reference dispatch")
+    ap.add_argument("--path", default="fused", choices=["fused", "plain", "tma"],
+                    help="fused: the default kernels; plain: one kernel per reference dispatch; "
+                         "tma: the default kernels with TMA-staged a-trous")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batched", action="store_true", help="skip the 32-stream batched measurement")
     ap.add_argument("--batch-steps", type=int, default=30)
@@ -576,6 +577,8 @@ def run_ours(args, dist: Dist):
         p.atrousIterations = args.iters
         if args.path == "plain":
             p.flags |= N.FLAG_PLAIN
+        elif args.path == "tma":
+            p.flags |= N.FLAG_TMA_STAGING
         dev_bufs = {}
         for name, arr in bufs.items():
             t = torch.from_numpy(np.ascontiguousarray(arr).view(np.uint8).reshape(-1)).to(f"cuda:{dev}")

@@ -440,7 +440,9 @@ rgdn_status run_denoise_fused( rgdn_stream* s, uint32_t fi, const rgdn_frame_par
     return RGDN_SUCCESS;
 }
 
-// a 2D map of a dense W x H plane of `tw` 4-byte words per texel, boxes of bw x bh texels
+// A map of a dense W x H plane of `tw` 4-byte words per texel with boxes of bw x bh texels:
+// 2-D over words for texels up to 8 bytes, 3-D (word, x, y) for 16-byte texels, so no box
+// dimension exceeds 256 elements.
 bool tensor_map( rgdn_stream* s, const void* plane, int tw, int bw, int bh, CUtensorMap& out )
 {
     const auto key = std::make_tuple( plane, tw, bw, bh );
@@ -452,43 +454,54 @@ bool tensor_map( rgdn_stream* s, const void* plane, int tw, int bw, int bh, CUte
     }
     EncodeTiledFn fn = encode_tiled_fn();
     if( !fn ) return false;
-    const cuuint64_t dims[ 2 ]    = { (cuuint64_t)s->W * tw, (cuuint64_t)s->H };
-    const cuuint64_t strides[ 1 ] = { (cuuint64_t)s->W * tw * 4 };
-    const cuuint32_t box[ 2 ]     = { (cuuint32_t)( bw * tw ), (cuuint32_t)bh };
-    const cuuint32_t es[ 2 ]      = { 1, 1 };
     CUtensorMap      m;
-    if( fn( &m, CU_TENSOR_MAP_DATA_TYPE_UINT32, 2, const_cast< void* >( plane ), dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
-            CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE ) != CUDA_SUCCESS )
-        return false;
+    const cuuint32_t es[ 3 ] = { 1, 1, 1 };
+    CUresult         r;
+    if( tw == 4 )
+    {
+        const cuuint64_t dims[ 3 ]    = { 4, (cuuint64_t)s->W, (cuuint64_t)s->H };
+        const cuuint64_t strides[ 2 ] = { 16, (cuuint64_t)s->W * 16 };
+        const cuuint32_t box[ 3 ]     = { 4, (cuuint32_t)bw, (cuuint32_t)bh };
+        r = fn( &m, CU_TENSOR_MAP_DATA_TYPE_UINT32, 3, const_cast< void* >( plane ), dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE );
+    }
+    else
+    {
+        const cuuint64_t dims[ 2 ]    = { (cuuint64_t)s->W * tw, (cuuint64_t)s->H };
+        const cuuint64_t strides[ 1 ] = { (cuuint64_t)s->W * tw * 4 };
+        const cuuint32_t box[ 2 ]     = { (cuuint32_t)( bw * tw ), (cuuint32_t)bh };
+        r = fn( &m, CU_TENSOR_MAP_DATA_TYPE_UINT32, 2, const_cast< void* >( plane ), dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE );
+    }
+    if( r != CUDA_SUCCESS ) return false;
     s->tmaps[ key ] = m;
     out             = m;
     return true;
 }
 
 // The TMA-staged a-trous needs 16-byte row pitches of every staged plane (W % 4 == 0 covers
-// the 4-byte ones), steps up to 16, and the driver's tensor-map encoder.
+// the 4-byte ones), steps up to 16, the driver's tensor-map encoder, and two stages that fit
+// the 227 KB of shared memory a block may use.
 bool tma_atrous_ok( const rgdn_stream* s, int iter )
 {
-    return ( s->W % 4 ) == 0 && iter <= 4 && encode_tiled_fn() != nullptr && atrous_tma_smem( (int)s->storage, iter ) <= 200 * 1024;
+    return ( s->W % 4 ) == 0 && iter <= 4 && encode_tiled_fn() != nullptr && atrous_tma_smem( (int)s->storage, iter ) <= 220 * 1024;
 }
 
 rgdn_status launch_atrous_tma( rgdn_stream* s, const FrameArgs& a, int iter, bool hist, cudaStream_t cs )
 {
     // the sources of this iteration (the routing of atrous_io, CmSVGFAtrous.comp:237-276)
-    const bool  odd = ( iter & 1 ) != 0;
-    const void* cv  = iter == 0 ? a.diffPing : iter == 1 ? a.diffHistory : ( odd ? a.diffPong : a.diffPing );
-    const void* var = iter == 0 ? a.varPing : iter == 1 ? a.varHistory : ( odd ? a.varPong : a.varPing );
-    const void* sp  = iter == 0 ? a.specPing : ( odd ? a.specPong : a.specPing );
-    const void* in  = iter == 0 ? a.indirPing : ( odd ? a.indirPong : a.indirPing );
-    const int   st  = 1 << iter, sx = ( st + 3 ) & ~3;
-    const int   bw  = 32 + 2 * sx, bh = st > 8 ? 8 : 8 + 2 * st;
-    const int   tCv = s->storage == RGDN_STORAGE_FP32 ? 4 : 2;
-    const int   tCol = s->storage == RGDN_STORAGE_REF ? 1 : s->storage == RGDN_STORAGE_FP32 ? 4 : 2;
-    AtrousMaps  m;
-    if( !tensor_map( s, cv, tCv, bw, bh, m.cv ) || !tensor_map( s, sp, tCol, bw, bh, m.spec ) || !tensor_map( s, in, tCol, bw, bh, m.indir ) ||
-        !tensor_map( s, a.geom, 4, bw, bh, m.geo ) )
+    const bool     odd = ( iter & 1 ) != 0;
+    const void*    cv  = iter == 0 ? a.diffPing : iter == 1 ? a.diffHistory : ( odd ? a.diffPong : a.diffPing );
+    const void*    var = iter == 0 ? a.varPing : iter == 1 ? a.varHistory : ( odd ? a.varPong : a.varPing );
+    const void*    sp  = iter == 0 ? a.specPing : ( odd ? a.specPong : a.specPing );
+    const void*    in  = iter == 0 ? a.indirPing : ( odd ? a.indirPong : a.indirPing );
+    const TmaGeom  g   = tma_geometry( (int)s->storage, iter );
+    const TmaTexel tx  = tma_texel( (int)s->storage );
+    AtrousMaps     m;
+    if( !tensor_map( s, cv, tx.cv / 4, g.rw, g.rh, m.cv ) || !tensor_map( s, sp, tx.col / 4, g.rw, g.rh, m.spec ) ||
+        !tensor_map( s, in, tx.col / 4, g.rw, g.rh, m.indir ) || !tensor_map( s, a.geom, 4, g.rw, g.rh, m.geo ) )
         return RGDN_DEVICE_ERROR;
-    if( var ) { if( !tensor_map( s, var, 1, bw, bh, m.var ) ) return RGDN_DEVICE_ERROR; }
+    if( tx.var ) { if( !var || !tensor_map( s, var, tx.var / 4, g.rw, g.rh, m.var ) ) return RGDN_DEVICE_ERROR; }
     else m.var = m.cv;
     cudaEvent_t ea = nullptr, eb = nullptr;
     if( s->timing )

@@ -155,6 +155,55 @@ struct AtrousMaps
     CUtensorMap cv, var, spec, indir, geo;
 };
 
+// Shared-memory staging of one TMA-staged a-trous iteration (kernel and host agree on it).
+// The output tile is tw x th pixels (one per thread). Each source plane's tap footprint is one
+// box of rw x rh texels (steps up to 8: rows -s..th+s) or three bands of rw x th texels
+// (step 16: rows -s, 0, +s), with a column halo sx = s rounded up to 4 texels so every box
+// starts on a 16-byte boundary. Planes of 16-byte texels are addressed through 3-D maps
+// (4 words x W x H), the others through 2-D maps of 4-byte words, so no box dimension exceeds
+// the TMA limit of 256 elements. The kernel keeps two stages of `bytes` each.
+struct TmaGeom
+{
+    int s, sx, tw, th, rw, rh, nb;
+    int offCv, offVar, offSpec, offInd, offGeo, bytes;
+};
+// texel bytes of the staged planes per storage mode: colour+variance, variance plane, colour
+struct TmaTexel
+{
+    int cv, var, col;
+};
+__host__ __device__ inline TmaTexel tma_texel( int storage )
+{
+    switch( storage )
+    {
+        case RGDN_STORAGE_REF: return { 8, 0, 4 };
+        case RGDN_STORAGE_FP32: return { 16, 0, 16 };
+        default: return { 8, 4, 8 };
+    }
+}
+__host__ __device__ inline int tma_align128( int v ) { return ( v + 127 ) & ~127; }
+__host__ __device__ inline TmaGeom tma_geometry( int storage, int iter )
+{
+    TmaGeom g;
+    g.s  = 1 << iter;
+    g.sx = ( g.s + 3 ) & ~3;
+    g.tw = g.s > 8 ? 64 : 32;
+    g.th = g.s > 8 ? 4 : 8;
+    g.nb = g.s > 8 ? 3 : 1;
+    g.rh = g.s > 8 ? g.th : g.th + 2 * g.s;
+    g.rw = g.tw + 2 * g.sx;
+    const TmaTexel tx     = tma_texel( storage );
+    const int      texels = g.rw * g.rh * g.nb;
+    int            off    = 0;
+    g.offCv   = off; off = tma_align128( off + texels * tx.cv );
+    g.offVar  = off; off = tma_align128( off + texels * tx.var );
+    g.offSpec = off; off = tma_align128( off + texels * tx.col );
+    g.offInd  = off; off = tma_align128( off + texels * tx.col );
+    g.offGeo  = off; off = tma_align128( off + texels * 16 );
+    g.bytes   = off;
+    return g;
+}
+
 // TMA-staged a-trous iteration (FAST weights) with the tensor maps of its sources
 // (`maps` points to the kernels' AtrousMaps: 5 CUtensorMap for colour+variance, variance,
 // specular, indirect, geometry), and the dynamic shared memory one launch needs

@@ -1533,6 +1533,13 @@ __device__ __forceinline__ void tma_load_2d( void* dst, const CUtensorMap* tm, i
                   "l"( (uint64_t)tm ), "r"( x ), "r"( y ), "r"( smem_u32( bar ) )
                   : "memory" );
 }
+__device__ __forceinline__ void tma_load_3d( void* dst, const CUtensorMap* tm, int x, int y, int z, uint64_t* bar )
+{
+    asm volatile( "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(
+                      smem_u32( dst ) ),
+                  "l"( (uint64_t)tm ), "r"( x ), "r"( y ), "r"( z ), "r"( smem_u32( bar ) )
+                  : "memory" );
+}
 __device__ __forceinline__ bool mbar_try_wait( uint64_t* bar, uint32_t phase )
 {
     uint32_t ok;
@@ -1550,38 +1557,7 @@ __device__ __forceinline__ bool mbar_wait_bounded( uint64_t* bar, uint32_t phase
     return false;
 }
 
-// texel bytes of the staged planes per mode: colour+variance, variance plane, colour
-template< int M > struct TmaTexel;
-template<> struct TmaTexel< MODE_REF > { static constexpr int cv = 8, var = 0, col = 4; };
-template<> struct TmaTexel< MODE_F32 > { static constexpr int cv = 16, var = 0, col = 16; };
-template<> struct TmaTexel< MODE_F16 > { static constexpr int cv = 8, var = 4, col = 8; };
-template<> struct TmaTexel< MODE_BF16 > { static constexpr int cv = 8, var = 4, col = 8; };
-
-// shared-memory geometry of one step (the host computes the same for the launch size)
-struct TmaGeom
-{
-    int s, sx, rw, rh, nb;   // step, column halo, box width / height, boxes (1 or 3 bands)
-    int offCv, offVar, offSpec, offInd, offGeo, bytes;
-};
-__host__ __device__ __forceinline__ int tma_align128( int v ) { return ( v + 127 ) & ~127; }
-template< int M > __host__ __device__ __forceinline__ TmaGeom tma_geom( int iter )
-{
-    TmaGeom g;
-    g.s  = 1 << iter;
-    g.sx = ( g.s + 3 ) & ~3;
-    g.rw = 32 + 2 * g.sx;
-    g.nb = g.s > 8 ? 3 : 1;
-    g.rh = g.s > 8 ? 8 : 8 + 2 * g.s;
-    const int texels = g.rw * g.rh * g.nb;
-    int off = 0;
-    g.offCv   = off; off = tma_align128( off + texels * TmaTexel< M >::cv );
-    g.offVar  = off; off = tma_align128( off + texels * TmaTexel< M >::var );
-    g.offSpec = off; off = tma_align128( off + texels * TmaTexel< M >::col );
-    g.offInd  = off; off = tma_align128( off + texels * TmaTexel< M >::col );
-    g.offGeo  = off; off = tma_align128( off + texels * 16 );
-    g.bytes   = off;
-    return g;
-}
+template< int M > __host__ __device__ __forceinline__ TmaGeom tma_geom( int iter ) { return tma_geometry( M, iter ); }
 
 template< int M > struct TmaLd;
 template<> struct TmaLd< MODE_REF >
@@ -1630,7 +1606,7 @@ __device__ __forceinline__ void atrous_px_tma( const FrameArgs& a, const AtrousI
     const int      step = g.s;
     // shared-memory texel index of tap (dx, dy) of this thread's pixel
     auto kidx = [ & ]( int dx, int dy ) {
-        const int row = g.nb == 3 ? ( dy + 1 ) * 8 + ty : step + ty + dy * step;
+        const int row = g.nb == 3 ? ( dy + 1 ) * g.th + ty : step + ty + dy * step;
         return row * g.rw + g.sx + tx + dx * step;
     };
     const uint8_t* bCv  = sm + g.offCv;
@@ -1700,100 +1676,144 @@ __device__ __forceinline__ void atrous_px_tma( const FrameArgs& a, const AtrousI
     atrous_finish( acc, outDiff, outVar, outSpec, outInd );
 }
 
+// Issues the TMA copies of tile (x0, y0)'s footprint into one stage (thread 0 only).
+template< int M >
+__device__ __forceinline__ void tma_issue_tile( const TmaGeom& g, const AtrousMaps& maps, uint8_t* st, uint64_t* bar, int x0, int y0 )
+{
+    constexpr TmaTexel tx   = { M == MODE_REF ? 8 : M == MODE_F32 ? 16 : 8, ( M == MODE_F16 || M == MODE_BF16 ) ? 4 : 0,
+                                M == MODE_REF ? 4 : M == MODE_F32 ? 16 : 8 };
+    const int          box  = g.rw * g.rh;
+    mbar_arrive_expect_tx( bar, (uint32_t)( box * g.nb * ( tx.cv + tx.var + 2 * tx.col + 16 ) ) );
+    // one plane: nb bands of rw x rh texels; 16-byte texels through a 3-D map (word, x, y),
+    // the others through a 2-D map of 4-byte words
+    auto plane = [ & ]( int off, const CUtensorMap* m, int texBytes ) {
+        const int xt = x0 - g.sx;
+        for( int b = 0; b < g.nb; b++ )
+        {
+            const int y = g.nb == 3 ? y0 + ( b - 1 ) * g.s : y0 - g.s;
+            if( texBytes == 16 ) tma_load_3d( st + off + b * box * texBytes, m, 0, xt, y, bar );
+            else tma_load_2d( st + off + b * box * texBytes, m, xt * ( texBytes / 4 ), y, bar );
+        }
+    };
+    plane( g.offCv, &maps.cv, tx.cv );
+    if( tx.var ) plane( g.offVar, &maps.var, tx.var );
+    plane( g.offSpec, &maps.spec, tx.col );
+    plane( g.offInd, &maps.indir, tx.col );
+    plane( g.offGeo, &maps.geo, 16 );
+}
+
+// Persistent TMA-staged a-trous iteration: block b computes tiles b, b + gridDim.x, ... Each
+// tile's footprint is staged in shared memory by TMA; while the block computes tile k from one
+// stage, the copies of tile k+1 fill the other, so the taps never wait on global memory.
+// Waits are bounded: a timeout sets bit 0 of the stream's error flags, waits (bounded) for the
+// block's copies still in flight and returns.
 template< int M, bool FAST, bool HIST >
-__global__ void __launch_bounds__( 256, 2 ) k_atrous_tma( const FrameArgs a, const int iter, const __grid_constant__ AtrousMaps maps )
+__global__ void __launch_bounds__( 256, 3 ) k_atrous_tma( const FrameArgs a, const int iter, const __grid_constant__ AtrousMaps maps )
 {
     using S = Sto< M >;
     extern __shared__ __align__( 128 ) uint8_t sm[];
-    __shared__ __align__( 8 ) uint64_t bar;
+    __shared__ __align__( 8 ) uint64_t bar[ 2 ];
     __shared__ float    u8[ 256 ];
     __shared__ uint32_t hist[ HIST ? 256 : 1 ];
-    const Uniform& u  = a.u;
-    const int      t  = threadIdx.y * blockDim.x + threadIdx.x;
-    const TmaGeom  g  = tma_geom< M >( iter );
-    const int      x0 = blockIdx.x * 32, y0 = blockIdx.y * 8;
+    const Uniform& u      = a.u;
+    const int      t      = threadIdx.y * blockDim.x + threadIdx.x;
+    const TmaGeom  g      = tma_geom< M >( iter );
+    const int      tilesX = ( u.W + g.tw - 1 ) / g.tw;
+    const int      total  = tilesX * ( ( u.H + g.th - 1 ) / g.th );
+    const int      G      = (int)gridDim.x;
     if( t == 0 )
     {
-        mbar_init( &bar, 1 );
+        mbar_init( &bar[ 0 ], 1 );
+        mbar_init( &bar[ 1 ], 1 );
         fence_async_shared();
-    }
-    __syncthreads();
-    if( t == 0 )
-    {
-        constexpr int tCv = TmaTexel< M >::cv, tVar = TmaTexel< M >::var, tCol = TmaTexel< M >::col;
-        const int boxTexels = g.rw * g.rh;
-        mbar_arrive_expect_tx( &bar, (uint32_t)( boxTexels * g.nb * ( tCv + tVar + 2 * tCol + 16 ) ) );
-        for( int b = 0; b < g.nb; b++ )
-        {
-            const int y  = g.nb == 3 ? y0 + ( b - 1 ) * g.s : y0 - g.s;
-            const int xt = x0 - g.sx;   // texels; the maps address 4-byte words
-            const int o  = b * boxTexels;
-            tma_load_2d( sm + g.offCv + o * tCv, &maps.cv, xt * ( tCv / 4 ), y, &bar );
-            if( tVar ) tma_load_2d( sm + g.offVar + o * tVar, &maps.var, xt * ( tVar / 4 ), y, &bar );
-            tma_load_2d( sm + g.offSpec + o * tCol, &maps.spec, xt * ( tCol / 4 ), y, &bar );
-            tma_load_2d( sm + g.offInd + o * tCol, &maps.indir, xt * ( tCol / 4 ), y, &bar );
-            tma_load_2d( sm + g.offGeo + o * 16, &maps.geo, xt * 4, y, &bar );
-        }
     }
     u8[ t ] = (float)t / 255.0f;
     if( HIST ) hist[ t ] = 0u;
-    // block-uniform readiness: every thread leaves together or computes together
-    const bool ready = __syncthreads_and( mbar_wait_bounded( &bar, 0 ) ? 1 : 0 ) != 0;
-    if( !ready )
+    __syncthreads();
+    const int first = (int)blockIdx.x;
+    if( t == 0 && first < total ) tma_issue_tile< M >( g, maps, sm, &bar[ 0 ], ( first % tilesX ) * g.tw, ( first / tilesX ) * g.th );
+
+    const AtrousIO io   = atrous_io< M >( a, iter );
+    const bool     last = iter + 1 == (int)u.niter;
+    const int      sep  = u.W / 2;
+    int            k    = 0;
+    for( int tile = first; tile < total; tile += G, k++ )
     {
-        // the copies did not complete: flag the stream and keep the outputs untouched
-        if( t == 0 ) atomicOr( &a.tm->errorFlags, 1u );
-        return;
-    }
-    const int px = x0 + threadIdx.x, py = y0 + threadIdx.y;
-    if( px < u.W && py < u.H )
-    {
-        const int      i    = py * u.W + px;
-        const AtrousIO io   = atrous_io< M >( a, iter );
-        const bool     last = iter + 1 == (int)u.niter;
-        float3         outDiff, outSpec, outInd;
-        float          outVar;
-        const int  sep      = u.W / 2;
-        const bool interior = x0 - g.s >= 0 && y0 - g.s >= 0 && x0 + 31 + g.s < u.W && y0 + 7 + g.s < u.H &&
-                              ( x0 + 31 + g.s < sep || x0 - g.s >= sep );
-        if( interior ) atrous_px_tma< M, FAST, true >( a, io, g, sm, iter, px, py, threadIdx.x, threadIdx.y, i, u8, outDiff, outVar, outSpec, outInd );
-        else atrous_px_tma< M, FAST, false >( a, io, g, sm, iter, px, py, threadIdx.x, threadIdx.y, i, u8, outDiff, outVar, outSpec, outInd );
-        if( !last )
+        const int st   = k & 1;
+        const int next = tile + G;
+        // the other stage was released by the barrier that ended the previous tile
+        if( t == 0 && next < total )
+            tma_issue_tile< M >( g, maps, sm + ( st ^ 1 ) * g.bytes, &bar[ st ^ 1 ], ( next % tilesX ) * g.tw, ( next / tilesX ) * g.th );
+        const bool ready = __syncthreads_and( mbar_wait_bounded( &bar[ st ], ( k >> 1 ) & 1 ) ? 1 : 0 ) != 0;
+        if( !ready )
         {
-            S::stcv( io.diffDst, io.varDst, (size_t)i, outDiff, outVar );
-            S::st3( io.specDst, (size_t)i, outSpec );
-            S::st3( io.indirDst, (size_t)i, outInd );
-        }
-        else
-        {
-            const uint16_t hin = compose< M >( a, px, py, (size_t)i, outDiff, outSpec, outInd );
-            if( HIST )
+            // the copies did not complete: flag the stream, leave the outputs untouched and let
+            // the copies already issued for the next tile land before the block exits
+            if( t == 0 )
             {
-                const uint32_t bin   = __ldg( &a.binLut[ hin ] );
-                const uint32_t peers = __match_any_sync( __activemask(), bin );
-                if( ( threadIdx.x & 31 ) == (uint32_t)( __ffs( peers ) - 1 ) ) atomicAdd( &hist[ bin ], (uint32_t)__popc( peers ) );
+                atomicOr( &a.tm->errorFlags, 1u );
+                if( next < total ) mbar_wait_bounded( &bar[ st ^ 1 ], ( ( k + 1 ) >> 1 ) & 1 );
+            }
+            return;
+        }
+        const uint8_t* stage = sm + st * g.bytes;
+        const int      x0 = ( tile % tilesX ) * g.tw, y0 = ( tile / tilesX ) * g.th;
+        const int      px = x0 + threadIdx.x, py = y0 + threadIdx.y;
+        if( px < u.W && py < u.H )
+        {
+            const int  i = py * u.W + px;
+            float3     outDiff, outSpec, outInd;
+            float      outVar;
+            const bool interior = x0 - g.s >= 0 && y0 - g.s >= 0 && x0 + g.tw - 1 + g.s < u.W && y0 + g.th - 1 + g.s < u.H &&
+                                  ( x0 + g.tw - 1 + g.s < sep || x0 - g.s >= sep );
+            if( interior )
+                atrous_px_tma< M, FAST, true >( a, io, g, stage, iter, px, py, threadIdx.x, threadIdx.y, i, u8, outDiff, outVar, outSpec, outInd );
+            else
+                atrous_px_tma< M, FAST, false >( a, io, g, stage, iter, px, py, threadIdx.x, threadIdx.y, i, u8, outDiff, outVar, outSpec, outInd );
+            if( !last )
+            {
+                S::stcv( io.diffDst, io.varDst, (size_t)i, outDiff, outVar );
+                S::st3( io.specDst, (size_t)i, outSpec );
+                S::st3( io.indirDst, (size_t)i, outInd );
+            }
+            else
+            {
+                const uint16_t hin = compose< M >( a, px, py, (size_t)i, outDiff, outSpec, outInd );
+                if( HIST )
+                {
+                    const uint32_t bin   = __ldg( &a.binLut[ hin ] );
+                    const uint32_t peers = __match_any_sync( __activemask(), bin );
+                    if( ( t & 31 ) == (uint32_t)( __ffs( peers ) - 1 ) ) atomicAdd( &hist[ bin ], (uint32_t)__popc( peers ) );
+                }
             }
         }
+        __syncthreads();   // every thread is done with this stage before it is refilled
     }
-    if( HIST )
-    {
-        __syncthreads();
-        if( hist[ t ] ) atomicAdd( &a.tm->histogram[ t ], hist[ t ] );
-    }
+    if( HIST && hist[ t ] ) atomicAdd( &a.tm->histogram[ t ], hist[ t ] );
 }
 
 template< int M, bool FAST, bool HIST > cudaError_t launch_atrous_tma( const FrameArgs& a, int iter, const AtrousMaps& maps, cudaStream_t s )
 {
     const TmaGeom g = tma_geom< M >( iter );
-    static int    attrBytes = 0;
-    if( attrBytes < g.bytes )
+    // per iteration: the dynamic shared memory attribute and the resident blocks per SM
+    static int attrBytes = 0, perSM[ MAX_ATROUS_ITERATIONS ] = {}, sms = 0;
+    if( attrBytes < 2 * g.bytes )
     {
-        cudaError_t e = cudaFuncSetAttribute( k_atrous_tma< M, FAST, HIST >, cudaFuncAttributeMaxDynamicSharedMemorySize, g.bytes );
+        cudaError_t e = cudaFuncSetAttribute( k_atrous_tma< M, FAST, HIST >, cudaFuncAttributeMaxDynamicSharedMemorySize, 2 * g.bytes );
         if( e != cudaSuccess ) return e;
-        attrBytes = g.bytes;
+        attrBytes = 2 * g.bytes;
     }
-    const dim3 grid( ( a.u.W + 31 ) / 32, ( a.u.H + 7 ) / 8 );
-    k_atrous_tma< M, FAST, HIST ><<< grid, dim3( 32, 8 ), g.bytes, s >>>( a, iter, maps );
+    if( !perSM[ iter ] )
+    {
+        int dev = 0;
+        if( cudaGetDevice( &dev ) != cudaSuccess || cudaDeviceGetAttribute( &sms, cudaDevAttrMultiProcessorCount, dev ) != cudaSuccess ||
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor( &perSM[ iter ], k_atrous_tma< M, FAST, HIST >, 256, 2 * g.bytes ) != cudaSuccess ||
+            perSM[ iter ] <= 0 )
+            return cudaErrorInvalidConfiguration;
+    }
+    const int total = ( ( a.u.W + g.tw - 1 ) / g.tw ) * ( ( a.u.H + g.th - 1 ) / g.th );
+    const int grid  = total < perSM[ iter ] * sms ? total : perSM[ iter ] * sms;
+    k_atrous_tma< M, FAST, HIST ><<< grid, dim3( g.tw, g.th ), 2 * g.bytes, s >>>( a, iter, maps );
     return cudaGetLastError();
 }
 
@@ -2125,6 +2145,6 @@ template< int M > cudaError_t launch_atrous_tma_t( const FrameArgs& a, int iter,
     const AtrousMaps& m = *static_cast< const AtrousMaps* >( maps );
     return hist ? dev::launch_atrous_tma< M, true, true >( a, iter, m, s ) : dev::launch_atrous_tma< M, true, false >( a, iter, m, s );
 }
-template< int M > int atrous_tma_smem_t( int iter ) { return dev::tma_geom< M >( iter ).bytes; }
+template< int M > int atrous_tma_smem_t( int iter ) { return 2 * dev::tma_geom< M >( iter ).bytes; }
 
 }  // namespace rgdn
