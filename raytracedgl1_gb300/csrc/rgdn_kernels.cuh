@@ -114,6 +114,12 @@ __device__ __forceinline__ float ex2_approx( float x )
     asm( "ex2.approx.ftz.f32 %0, %1;" : "=f"( r ) : "f"( x ) );
     return r;
 }
+__device__ __forceinline__ float lg2_approx( float x )
+{
+    float r;
+    asm( "lg2.approx.ftz.f32 %0, %1;" : "=f"( r ) : "f"( x ) );
+    return r;
+}
 template< bool FAST > struct Wm;
 template<> struct Wm< false >
 {
@@ -1272,6 +1278,8 @@ struct AtrousCtr
     float  z, l, wLumMul, roughness, wRoughMul, nwSpec, gradDepth, rz1, rz2;
     Area   chArea;
 };
+constexpr float kLog2e     = 1.44269504088896341f;   // log2(e)
+constexpr float kSqrtLog2e = 1.20112240878644913f;   // sqrt(log2(e))
 struct AtrousAcc
 {
     float3 d, s, i;
@@ -1281,12 +1289,44 @@ struct AtrousAcc
 // One tap (xx, yy) of the dilated 3x3 stencil (CmSVGFAtrous.comp:163-235): its edge-stopping
 // weights and its contribution to the sums. Both a-trous loops below run this same code, so
 // their results are identical.
+//
+// FAST evaluates every weight in the exponent domain (one hardware exp2 per weight): with
+// L = log2 max(n.n_q, 0) (clamped at -126, where every weight it enters is 0 in FP32),
+//   wBase = 2^( -(w_z sqrt(log2 e))^2 + 128 L + log2 kernel ),
+//   wDiff = 2^( that - w_l log2 e ),   wSpec = w_r' 2^( that + p L ),
+// the same products as exp(-w_z^2) * n^128 * kernel, exp(-w_l) and n^p. atrous_terms folds the
+// constant factors into rz1, rz2 and wLumMul.
 template< bool FAST, bool INTERIOR >
 __device__ __forceinline__ void atrous_accum( const AtrousCtr& c, AtrousAcc& acc, const int xx, const int yy, const int qx, const int qy,
                                               const float rq, const float3 nq, const float zq, const float4 cvq, const float3 sq,
                                               const float3 iq )
 {
     using X = Wm< FAST >;
+    if constexpr( FAST )
+    {
+        const float3 dq    = f3( cvq.x, cvq.y, cvq.z );
+        const float  lq    = X::lum( dq );
+        const float  nn    = fmaxf( 0.0f, X::dot( c.normal, nq ) );
+        const int    man   = ( xx < 0 ? -xx : xx ) + ( yy < 0 ? -yy : yy );
+        const float  L     = fmaxf( lg2_approx( nn ), -126.0f );
+        const float  wz    = fabsf( c.z - zq ) * ( man == 1 ? c.rz1 : c.rz2 );
+        // log2 of the wavelet kernel {1, 0.5, 0.25} by Manhattan distance
+        const float  eBase = __fmaf_rn( -wz, wz, __fmaf_rn( 128.0f, L, -(float)man ) );
+        float        w_r   = fmaxf( 0.0f, X::one_minus( 10.0f, fabsf( c.roughness - rq ) ) ) * c.wRoughMul;
+        const float  insideA = ( INTERIOR || in_area( qx, qy, c.chArea ) ) ? 1.0f : 0.0f;
+        const float  wBase = ex2_approx( eBase ) * insideA;
+        const float  wDiff = ex2_approx( eBase - fabsf( c.l - lq ) * c.wLumMul ) * insideA;
+        const float  wSpec = w_r * ex2_approx( __fmaf_rn( c.nwSpec, L, eBase ) ) * insideA;
+        const float  wInd  = wBase;
+        acc.d   = f3( __fmaf_rn( dq.x, wDiff, acc.d.x ), __fmaf_rn( dq.y, wDiff, acc.d.y ), __fmaf_rn( dq.z, wDiff, acc.d.z ) );
+        acc.s   = f3( __fmaf_rn( sq.x, wSpec, acc.s.x ), __fmaf_rn( sq.y, wSpec, acc.s.y ), __fmaf_rn( sq.z, wSpec, acc.s.z ) );
+        acc.i   = f3( __fmaf_rn( iq.x, wInd, acc.i.x ), __fmaf_rn( iq.y, wInd, acc.i.y ), __fmaf_rn( iq.z, wInd, acc.i.z ) );
+        acc.var = __fmaf_rn( cvq.w * wDiff, wDiff, acc.var );
+        acc.ws  = acc.ws + wDiff;
+        acc.wsS = acc.wsS + wSpec;
+        acc.wsI = acc.wsI + wInd;
+        return;
+    }
     const float kern[ 2 ][ 2 ] = { { 1.0f, 0.5f }, { 0.5f, 0.25f } };
     const float3 dq  = f3( cvq.x, cvq.y, cvq.z );
     const float  lq  = X::lum( dq );
@@ -1323,14 +1363,15 @@ __device__ __forceinline__ void atrous_terms( AtrousCtr& c, AtrousAcc& acc, cons
                                               const float hS, const int iter )
 {
     c.l             = Wm< FAST >::lum( acc.d );
-    c.wLumMul       = 1.0f / ( 4.0f * prefVar + 0.00001f );
+    c.wLumMul       = ( FAST ? kLog2e : 1.0f ) / ( 4.0f * prefVar + 0.00001f );
     c.roughness     = u8[ rough8 ];
     c.wRoughMul     = gclamp( c.roughness * 30.0f - (float)iter, 0.0f, 1.0f );
     const float nws = gclamp( hS / 8.0f, 0.0f, 1.0f );
     c.nwSpec        = gclamp( spec_power( c.roughness * c.roughness ), 8.0f, 1024.0f ) * nws;
-    // FAST: one reciprocal per tap distance class (|x|+|y| = 1 or 2)
-    c.rz1  = FAST ? 1.0f / fmaxf( c.gradDepth * 1.0f, 0.01f ) : 0.0f;
-    c.rz2  = FAST ? 1.0f / fmaxf( c.gradDepth * 2.0f, 0.01f ) : 0.0f;
+    // FAST: one reciprocal per tap distance class (|x|+|y| = 1 or 2), scaled for the exponent
+    // domain
+    c.rz1  = FAST ? kSqrtLog2e / fmaxf( c.gradDepth * 1.0f, 0.01f ) : 0.0f;
+    c.rz2  = FAST ? kSqrtLog2e / fmaxf( c.gradDepth * 2.0f, 0.01f ) : 0.0f;
     acc.ws = acc.wsS = acc.wsI = 1.0f;
 }
 
