@@ -313,7 +313,7 @@ rgdn_status rgdn_submit_batch( rgdn_context* ctx, const rgdn_job* jobs, uint32_t
 typedef struct rgdn_batch_config
 {
     uint32_t temporalTile;        /* RGDN_TILE_* */
-    uint32_t antiFireflyTile;
+    uint32_t antiFireflyTile;     /* always RGDN_TILE_32X8 (its shared-memory tile) */
     uint32_t varianceTile;
     uint32_t atrousTile[ 6 ];     /* per a-trous iteration */
     uint32_t atrousBlocksPerSM[ 6 ];/* register budget of each a-trous iteration's kernel: built

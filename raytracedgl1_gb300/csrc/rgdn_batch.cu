@@ -149,11 +149,12 @@ struct Tuner
 
 // Candidates of a launch kind: tile shapes 32x8 and 16x16 (64x4 never won on GB300 and is
 // left to rgdn_batch_set_config); for a-trous also the budget of 3 or 4 blocks per SM.
-int n_candidates( int kind ) { return kind >= BS_ATROUS0 ? 4 : kind == BS_GRADIENT ? 1 : 2; }
+// (anti-firefly keeps 32x8: its shared-memory tile is laid out for it)
+int n_candidates( int kind ) { return kind >= BS_ATROUS0 ? 4 : ( kind == BS_GRADIENT || kind == BS_ANTI_FIREFLY ) ? 1 : 2; }
 int max_candidates() { return 4; }
 void candidate( int kind, int c, int& shape, int& occ )
 {
-    shape = kind == BS_GRADIENT ? 0 : c % 2;
+    shape = ( kind == BS_GRADIENT || kind == BS_ANTI_FIREFLY ) ? 0 : c % 2;
     occ   = kind >= BS_ATROUS0 ? 3 + ( c / 2 ) % 2 : 0;
 }
 
@@ -589,7 +590,7 @@ rgdn_status batch_set_config( rgdn_context* c, uint32_t storage, const rgdn_batc
     if( !ex ) return RGDN_DEVICE_ERROR;
     Config& cf                  = ex->cfg[ storage ];
     cf.shape[ BS_TEMPORAL ]     = (int)in->temporalTile;
-    cf.shape[ BS_ANTI_FIREFLY ] = (int)in->antiFireflyTile;
+    cf.shape[ BS_ANTI_FIREFLY ] = 0;   // the shared-memory tile is 32x8
     cf.shape[ BS_VARIANCE ]     = (int)in->varianceTile;
     for( int i = 0; i < MAX_ATROUS_ITERATIONS; i++ )
     {

@@ -657,9 +657,11 @@ __device__ __forceinline__ void temporal_tile( const FrameArgs& a, int bx, int b
 
     if( weightSum > 0.0001f )
     {
-        specPrevOnSurf                = divs( specPrevOnSurf, weightSum );
-        const float specHistoryLength   = histLenDIS.z / weightSum;
-        const float specHitDistancePrev = histLenDIS.w / weightSum;
+        // FAST: one IEEE reciprocal for the averages that feed only continuous terms
+        const float invW                = FAST ? 1.0f / weightSum : 0.0f;
+        specPrevOnSurf                  = FAST ? mul( specPrevOnSurf, invW ) : divs( specPrevOnSurf, weightSum );
+        const float specHistoryLength   = FAST ? histLenDIS.z * invW : histLenDIS.z / weightSum;
+        const float specHitDistancePrev = FAST ? histLenDIS.w * invW : histLenDIS.w / weightSum;
 
         const float4 sp4     = a.surfPos[ i ];
         const float3 surfPos = f3( sp4.x, sp4.y, sp4.z );
@@ -848,10 +850,13 @@ __device__ __forceinline__ void temporal_tile( const FrameArgs& a, int bx, int b
         float dHL       = histLenDIS.x * inv;
         float iHL       = histLenDIS.y * inv;
         {
+            // the history length stays IEEE (variance switches on it); its reciprocal only
+            // blends, so FAST takes the hardware one
             dHL = dHL * powf( 1.0f - aD, 10.0f );
             dHL = gclamp( dHL + 1.0f, 1.0f, 256.0f );
-            float alphaColor   = fmaxf( 0.01f, 1.0f / dHL );
-            float alphaMoments = fmaxf( 0.01f, 1.0f / dHL );
+            const float rD     = FAST ? __fdividef( 1.0f, dHL ) : 1.0f / dHL;
+            float alphaColor   = fmaxf( 0.01f, rD );
+            float alphaMoments = fmaxf( 0.01f, rD );
             alphaColor         = gmix( alphaColor, 1.0f, aD );
             alphaMoments       = gmix( alphaMoments, 1.0f, aD );
             diffColorAccum     = vmix( diffPrev, unfilteredDiff, alphaColor );
@@ -861,7 +866,7 @@ __device__ __forceinline__ void temporal_tile( const FrameArgs& a, int bx, int b
         {
             iHL = iHL * powf( 1.0f - aI, 10.0f );
             iHL = gclamp( iHL + 1.0f, 1.0f, 256.0f );
-            float alphaColor = fmaxf( 0.01f, 1.0f / iHL );
+            float alphaColor = fmaxf( 0.01f, FAST ? __fdividef( 1.0f, iHL ) : 1.0f / iHL );
             alphaColor       = gmix( alphaColor, 1.0f, aI );
             indirAccum       = vmix( indirPrev, unfilteredIndir, alphaColor );
             indirHL          = iHL;
@@ -1072,11 +1077,15 @@ template<> struct AfOps< MODE_BF16 >
 };
 template<> struct AfOps< MODE_F32 >
 {
-    using V = float4;
-    __device__ static V ld( const void* p, int i ) { return static_cast< const float4* >( p )[ i ]; }
-    __device__ static V zero() { return make_float4( 0, 0, 0, 0 ); }
-    __device__ static V mn( V a, V b ) { return make_float4( fminf( a.x, b.x ), fminf( a.y, b.y ), fminf( a.z, b.z ), 0.0f ); }
-    __device__ static V mx( V a, V b ) { return make_float4( fmaxf( a.x, b.x ), fmaxf( a.y, b.y ), fmaxf( a.z, b.z ), 0.0f ); }
+    using V = float3;   // rgb of the rgba32f texel (alpha is written 0)
+    __device__ static V ld( const void* p, int i )
+    {
+        const float4 v = static_cast< const float4* >( p )[ i ];
+        return f3( v.x, v.y, v.z );
+    }
+    __device__ static V zero() { return f3( 0, 0, 0 ); }
+    __device__ static V mn( V a, V b ) { return vmin( a, b ); }
+    __device__ static V mx( V a, V b ) { return vmax( a, b ); }
     __device__ static void st( void* p, int i, V v ) { static_cast< float4* >( p )[ i ] = make_float4( v.x, v.y, v.z, 0.0f ); }
 };
 template<> struct AfOps< MODE_REF >
@@ -1126,31 +1135,93 @@ __device__ __forceinline__ void af_signal( const FrameArgs& a, const void* src, 
     O::st( dst, i, c );
 }
 
-template< int M > __device__ __forceinline__ void antifirefly_fast_tile( const FrameArgs& a, int bx, int by )
+// Shared-memory form of the 5x5 clamp for a 32x8 tile (blockDim 32 x 8). The (32+4) x (8+4)
+// footprints of the three signals are loaded once (zeros outside the image); then 5-wide row
+// minima / maxima are taken for every footprint row, and a pixel combines the two rows above
+// and below it with the four other texels of its own row. min and max are exact, so this is
+// the 24-tap clamp of af_signal value for value.
+template< int M > struct AfShared
 {
-    const Uniform& u  = a.u;
-    const int      px = bx * blockDim.x + threadIdx.x;
-    const int      py = by * blockDim.y + threadIdx.y;
-    if( px >= u.W || py >= u.H ) return;
-    const int  i        = py * u.W + px;
-    const int  bx0      = bx * blockDim.x, by0 = by * blockDim.y;
-    const bool interior = bx0 >= 2 && by0 >= 2 && bx0 + (int)blockDim.x + 2 <= u.W && by0 + (int)blockDim.y + 2 <= u.H;
-    if( interior )
+    using V = typename AfOps< M >::V;
+    static constexpr int TW = 32, TH = 8, RW = TW + 4, RH = TH + 4;
+    V tile[ 3 ][ RH ][ RW ];
+    V hmin[ 3 ][ RH ][ TW ];
+    V hmax[ 3 ][ RH ][ TW ];
+};
+static_assert( sizeof( AfShared< MODE_F32 > ) <= 48 * 1024 && sizeof( AfShared< MODE_REF > ) <= 48 * 1024,
+               "the anti-firefly tile must fit static shared memory" );
+
+template< int M > __device__ __forceinline__ void antifirefly_fast_tile( const FrameArgs& a, int bx, int by, AfShared< M >& sh )
+{
+    using O          = AfOps< M >;
+    using V          = typename O::V;
+    using SH         = AfShared< M >;
+    const Uniform& u = a.u;
+    const int      tx = threadIdx.x, ty = threadIdx.y;
+    const int      bx0 = bx * SH::TW, by0 = by * SH::TH;
+    const void*    src[ 3 ] = { a.diffTemp, a.specAccum, a.indirAccum };
+    void*          dst[ 3 ] = { a.diffAccumColor, a.specPing, a.indirPing };
+    const bool     interior = bx0 >= 2 && by0 >= 2 && bx0 + SH::TW + 2 <= u.W && by0 + SH::TH + 2 <= u.H;
+#pragma unroll
+    for( int r = ty; r < SH::RH; r += SH::TH )
     {
-        af_signal< M, true >( a, a.diffTemp, a.diffAccumColor, px, py, i );
-        af_signal< M, true >( a, a.specAccum, a.specPing, px, py, i );
-        af_signal< M, true >( a, a.indirAccum, a.indirPing, px, py, i );
+#pragma unroll
+        for( int c = tx; c < SH::RW; c += SH::TW )
+        {
+            const int  x = bx0 - 2 + c, y = by0 - 2 + r;
+            const bool in = interior || inside( u, x, y );
+#pragma unroll
+            for( int k = 0; k < 3; k++ ) sh.tile[ k ][ r ][ c ] = in ? O::ld( src[ k ], y * u.W + x ) : O::zero();
+        }
     }
-    else
+    __syncthreads();
+#pragma unroll
+    for( int r = ty; r < SH::RH; r += SH::TH )
     {
-        af_signal< M, false >( a, a.diffTemp, a.diffAccumColor, px, py, i );
-        af_signal< M, false >( a, a.specAccum, a.specPing, px, py, i );
-        af_signal< M, false >( a, a.indirAccum, a.indirPing, px, py, i );
+#pragma unroll
+        for( int k = 0; k < 3; k++ )
+        {
+            const V* row = &sh.tile[ k ][ r ][ tx ];
+            V        mn = row[ 0 ], mx = row[ 0 ];
+#pragma unroll
+            for( int d = 1; d < 5; d++ )
+            {
+                mn = O::mn( mn, row[ d ] );
+                mx = O::mx( mx, row[ d ] );
+            }
+            sh.hmin[ k ][ r ][ tx ] = mn;
+            sh.hmax[ k ][ r ][ tx ] = mx;
+        }
+    }
+    __syncthreads();
+    const int px = bx0 + tx, py = by0 + ty;
+    if( px >= u.W || py >= u.H ) return;
+#pragma unroll
+    for( int k = 0; k < 3; k++ )
+    {
+        const V* row = &sh.tile[ k ][ ty + 2 ][ tx ];
+        V        c   = row[ 2 ];
+        if( u.antiFirefly != 0 )
+        {
+            V mn = O::mn( O::mn( row[ 0 ], row[ 1 ] ), O::mn( row[ 3 ], row[ 4 ] ) );
+            V mx = O::mx( O::mx( row[ 0 ], row[ 1 ] ), O::mx( row[ 3 ], row[ 4 ] ) );
+#pragma unroll
+            for( int dy = -2; dy <= 2; dy++ )
+            {
+                if( dy == 0 ) continue;
+                mn = O::mn( mn, sh.hmin[ k ][ ty + 2 + dy ][ tx ] );
+                mx = O::mx( mx, sh.hmax[ k ][ ty + 2 + dy ][ tx ] );
+            }
+            c = O::mn( O::mx( c, mn ), mx );
+        }
+        O::st( dst[ k ], py * u.W + px, c );
     }
 }
+
 template< int M > __global__ void __launch_bounds__( 256 ) k_antifirefly_fast( const FrameArgs a )
 {
-    antifirefly_fast_tile< M >( a, blockIdx.x, blockIdx.y );
+    __shared__ AfShared< M > sh;
+    antifirefly_fast_tile< M >( a, blockIdx.x, blockIdx.y, sh );
 }
 
 // Variance for the default path: the geometry record instead of the depth / normal images
@@ -1988,11 +2059,18 @@ template< int M, int GPM > __global__ void __launch_bounds__( 256 ) kb_temporal(
     } );
 }
 
-// register caps: the occupancy of the single-frame kernels (7 and 5 blocks of 256 per SM)
-template< int M > __global__ void __launch_bounds__( 256, 7 ) kb_antifirefly( const int slot )
+// 32x8 tiles only (the shared-memory layout); a barrier ends each tile before the next reuses
+// the buffers
+template< int M > __global__ void __launch_bounds__( 256 ) kb_antifirefly( const int slot )
 {
-    batch_tiles< false >( slot, BS_ANTI_FIREFLY, [ & ]( const FrameArgs& a, int, int bx, int by ) { antifirefly_fast_tile< M >( a, bx, by ); } );
+    __shared__ AfShared< M > sh;
+    batch_tiles< false >( slot, BS_ANTI_FIREFLY, [ & ]( const FrameArgs& a, int, int bx, int by ) {
+        antifirefly_fast_tile< M >( a, bx, by, sh );
+        __syncthreads();
+    } );
 }
+
+// register cap: the occupancy of the single-frame kernel (5 blocks of 256 per SM)
 
 template< int M > __global__ void __launch_bounds__( 256, 5 ) kb_variance( const int slot )
 {
