@@ -12,6 +12,7 @@
 #pragma once
 
 #include <cuda.h>
+#include <utility>
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
 
@@ -20,6 +21,24 @@
 
 namespace rgdn
 {
+// A launch that lets the kernel start while its predecessor in the stream drains
+// (programmatic stream serialization; the kernels order their memory accesses with pdl_wait).
+template< class... KP, class... A >
+cudaError_t launch_pdl( void ( *kernel )( KP... ), dim3 grid, dim3 block, size_t smem, cudaStream_t s, A&&... args )
+{
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim            = grid;
+    cfg.blockDim           = block;
+    cfg.dynamicSmemBytes   = smem;
+    cfg.stream             = s;
+    cudaLaunchAttribute at;
+    at.id                                         = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at.val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs                                     = &at;
+    cfg.numAttrs                                  = 1;
+    return cudaLaunchKernelEx( &cfg, kernel, std::forward< A >( args )... );
+}
+
 namespace dev
 {
 
@@ -481,6 +500,13 @@ __device__ __forceinline__ void fill_u8( float* u8, int t )
     u8[ t ] = (float)t / 255.0f;
 }
 
+// Programmatic dependent launch. Every kernel of the path lets its successor's blocks be
+// scheduled once all of its own blocks have started (they then fill the SMs freed by this
+// grid's last wave), and waits for its predecessor's grid to complete, with its writes visible,
+// before the first global-memory access. Without a programmatic dependency both are no-ops.
+__device__ __forceinline__ void pdl_launch_dependents() { asm volatile( "griddepcontrol.launch_dependents;" ::: "memory" ); }
+__device__ __forceinline__ void pdl_wait() { asm volatile( "griddepcontrol.wait;" ::: "memory" ); }
+
 // Tile functions: one thread per pixel (or stratum) of the blockDim-sized tile (bx, by) of
 // frame `a`. The single-frame kernels run one tile per block; the batched kernels loop a
 // persistent block over the tiles of many frames.
@@ -502,7 +528,9 @@ __device__ __forceinline__ void gradient_atrous_tile( const FrameArgs& a, int it
 template< int M > __global__ void __launch_bounds__( 256 ) k_gradient_samples( const FrameArgs a, uint32_t* dst )
 {
     __shared__ float u8[ 256 ];
+    pdl_launch_dependents();
     fill_u8( u8, threadIdx.y * blockDim.x + threadIdx.x );
+    pdl_wait();
     __syncthreads();
     gradient_samples_tile< M >( a, dst, blockIdx.x, blockIdx.y, u8 );
 }
@@ -510,7 +538,9 @@ template< int M > __global__ void __launch_bounds__( 256 ) k_gradient_samples( c
 template< int M > __global__ void __launch_bounds__( 256 ) k_gradient_atrous( const FrameArgs a, const int iter )
 {
     __shared__ float u8[ 256 ];
+    pdl_launch_dependents();
     fill_u8( u8, threadIdx.y * blockDim.x + threadIdx.x );
+    pdl_wait();
     __syncthreads();
     gradient_atrous_tile( a, iter, blockIdx.x, blockIdx.y, u8 );
 }
@@ -891,7 +921,9 @@ __device__ __forceinline__ void temporal_tile( const FrameArgs& a, int bx, int b
 template< int M, bool FAST, bool GEOM, bool GEOMPREV > __global__ void __launch_bounds__( 256 ) k_temporal( const FrameArgs a )
 {
     __shared__ float u8[ 256 ];
+    pdl_launch_dependents();
     fill_u8( u8, threadIdx.y * blockDim.x + threadIdx.x );
+    pdl_wait();
     __syncthreads();
     temporal_tile< M, FAST, GEOM, GEOMPREV >( a, blockIdx.x, blockIdx.y, u8 );
 }
@@ -1221,6 +1253,8 @@ template< int M > __device__ __forceinline__ void antifirefly_fast_tile( const F
 template< int M > __global__ void __launch_bounds__( 256 ) k_antifirefly_fast( const FrameArgs a )
 {
     __shared__ AfShared< M > sh;
+    pdl_launch_dependents();
+    pdl_wait();
     antifirefly_fast_tile< M >( a, blockIdx.x, blockIdx.y, sh );
 }
 
@@ -1240,6 +1274,8 @@ template< int M, bool FAST > __device__ __forceinline__ void variance_geo_tile( 
 }
 template< int M, bool FAST > __global__ void __launch_bounds__( 256 ) k_variance_geo( const FrameArgs a )
 {
+    pdl_launch_dependents();
+    pdl_wait();
     variance_geo_tile< M, FAST >( a, blockIdx.x, blockIdx.y );
 }
 
@@ -1604,8 +1640,10 @@ template< int M, bool FAST, bool HIST, bool GEOMIN > __global__ void __launch_bo
     __shared__ float    u8[ 256 ];
     __shared__ uint32_t hist[ HIST ? 256 : 1 ];
     const int t = threadIdx.y * blockDim.x + threadIdx.x;
+    pdl_launch_dependents();
     u8[ t ]     = (float)t / 255.0f;
     if( HIST ) hist[ t ] = 0u;
+    pdl_wait();
     __syncthreads();
     atrous_tile< M, FAST, HIST, GEOMIN >( a, iter, blockIdx.x, blockIdx.y, u8, hist );
     if( HIST )
@@ -1833,6 +1871,8 @@ __global__ void __launch_bounds__( 256, 3 ) k_atrous_tma( const FrameArgs a, con
     const int      tilesX = ( u.W + g.tw - 1 ) / g.tw;
     const int      total  = tilesX * ( ( u.H + g.th - 1 ) / g.th );
     const int      G      = (int)gridDim.x;
+    pdl_launch_dependents();
+    pdl_wait();
     if( t == 0 )
     {
         mbar_init( &bar[ 0 ], 1 );
@@ -1925,8 +1965,7 @@ template< int M, bool FAST, bool HIST > cudaError_t launch_atrous_tma( const Fra
     }
     const int total = ( ( a.u.W + g.tw - 1 ) / g.tw ) * ( ( a.u.H + g.th - 1 ) / g.th );
     const int grid  = total < perSM[ iter ] * sms ? total : perSM[ iter ] * sms;
-    k_atrous_tma< M, FAST, HIST ><<< grid, dim3( g.tw, g.th ), 2 * g.bytes, s >>>( a, iter, maps );
-    return cudaGetLastError();
+    return launch_pdl( k_atrous_tma< M, FAST, HIST >, grid, dim3( g.tw, g.th ), 2 * g.bytes, s, a, iter, maps );
 }
 
 // ==========================================================================================
@@ -1979,12 +2018,16 @@ template< int M > __global__ void __launch_bounds__( 256 ) k_luminance_avg( cons
 {
     __shared__ uint32_t sh[ 256 ];
     __shared__ uint32_t count0;
+    pdl_launch_dependents();
+    pdl_wait();
     luminance_avg_job( a, sh, count0 );
 }
 
 // ==========================================================================================
 // Batched steps: persistent kernels, one per stage, looping over the tiles of every frame of
-// the step. The step's tile tables and frame arguments are in this module's constant slot
+// the step. Their grids are a single wave, so each block lets the next stage launch only when it
+// has finished its tiles (pdl_launch_dependents at the end): the next stage's blocks then take
+// over the SMs as this stage's blocks drain. The step's tile tables and frame arguments are in this module's constant slot
 // c_batch[slot] (internal linkage: every translation unit has its own copy, which the host
 // fills for the kernels it launches). Every index into it is warp-uniform (derived from
 // blockIdx, gridDim and constant data), so the frame arguments live in uniform registers.
@@ -2029,16 +2072,20 @@ template< int M > __global__ void __launch_bounds__( 256 ) kb_gradient_samples( 
 {
     __shared__ float u8[ 256 ];
     fill_u8( u8, threadIdx.y * blockDim.x + threadIdx.x );
+    pdl_wait();
     __syncthreads();
     batch_tiles< true >( slot, BS_GRADIENT, [ & ]( const FrameArgs& a, int, int bx, int by ) { gradient_samples_tile< M >( a, a.disPing, bx, by, u8 ); } );
+    pdl_launch_dependents();
 }
 
 template< int M > __global__ void __launch_bounds__( 256 ) kb_gradient_atrous( const int slot, const int iter )
 {
     __shared__ float u8[ 256 ];
     fill_u8( u8, threadIdx.y * blockDim.x + threadIdx.x );
+    pdl_wait();
     __syncthreads();
     batch_tiles< true >( slot, BS_GRADIENT, [ & ]( const FrameArgs& a, int, int bx, int by ) { gradient_atrous_tile( a, iter, bx, by, u8 ); } );
+    pdl_launch_dependents();
 }
 
 // FAST temporal accumulation writing the geometry record. GPM: 0 = no job has a valid previous
@@ -2050,6 +2097,7 @@ template< int M, int GPM > __global__ void __launch_bounds__( 256 ) kb_temporal(
     __shared__ float u8[ 256 ];
     const int t = threadIdx.y * blockDim.x + threadIdx.x;
     fill_u8( u8, t );
+    pdl_wait();
     __syncthreads();
     batch_tiles< false >( slot, BS_TEMPORAL, [ & ]( const FrameArgs& a, int j, int bx, int by ) {
         const uint32_t f = c_batch[ slot ].jobFlags[ j ];
@@ -2057,6 +2105,7 @@ template< int M, int GPM > __global__ void __launch_bounds__( 256 ) kb_temporal(
         if( GPM == 1 || ( GPM == 2 && ( f & BATCH_JOB_GEOM_PREV ) ) ) temporal_tile< M, true, true, true >( a, bx, by, u8 );
         else temporal_tile< M, true, true, false >( a, bx, by, u8 );
     } );
+    pdl_launch_dependents();
 }
 
 // 32x8 tiles only (the shared-memory layout); a barrier ends each tile before the next reuses
@@ -2064,17 +2113,21 @@ template< int M, int GPM > __global__ void __launch_bounds__( 256 ) kb_temporal(
 template< int M > __global__ void __launch_bounds__( 256 ) kb_antifirefly( const int slot )
 {
     __shared__ AfShared< M > sh;
+    pdl_wait();
     batch_tiles< false >( slot, BS_ANTI_FIREFLY, [ & ]( const FrameArgs& a, int, int bx, int by ) {
         antifirefly_fast_tile< M >( a, bx, by, sh );
         __syncthreads();
     } );
+    pdl_launch_dependents();
 }
 
 // register cap: the occupancy of the single-frame kernel (5 blocks of 256 per SM)
 
 template< int M > __global__ void __launch_bounds__( 256, 5 ) kb_variance( const int slot )
 {
+    pdl_wait();
     batch_tiles< false >( slot, BS_VARIANCE, [ & ]( const FrameArgs& a, int, int bx, int by ) { variance_geo_tile< M, true >( a, bx, by ); } );
+    pdl_launch_dependents();
 }
 
 // A-trous iteration `iter` over the jobs that run it. A job's last iteration composes PreFinal
@@ -2090,6 +2143,7 @@ __global__ void __launch_bounds__( 256, MINB ) kb_atrous( const int slot, const 
     const int t = threadIdx.y * blockDim.x + threadIdx.x;
     u8[ t ]     = (float)t / 255.0f;
     if( HM ) hist[ t ] = 0u;
+    pdl_wait();
     __syncthreads();
     int  histJob = -1;
     auto flush   = [ & ]() {
@@ -2113,6 +2167,7 @@ __global__ void __launch_bounds__( 256, MINB ) kb_atrous( const int slot, const 
         else atrous_tile< M, true, false, true >( a, iter, bx, by, u8, hist );
     } );
     if( HM && histJob >= 0 ) flush();
+    pdl_launch_dependents();
 }
 
 // one block per job (strided), as k_luminance_avg
@@ -2120,45 +2175,49 @@ template< int M > __global__ void __launch_bounds__( 256 ) kb_luminance_avg( con
 {
     __shared__ uint32_t sh[ 256 ];
     __shared__ uint32_t count0;
+    pdl_wait();
     const int n = c_batch[ slot ].n;
     for( int j = blockIdx.x; j < n; j += gridDim.x )
     {
         __syncthreads();
         luminance_avg_job( c_batch[ slot ].jobs[ j ], sh, count0 );
     }
+    pdl_launch_dependents();
 }
 
 }  // namespace dev
+
 
 // ------------------------------------------------------------------------------------------
 // launcher for one mode
 // ------------------------------------------------------------------------------------------
 template< int M > cudaError_t launch_stage_t( const FrameArgs& a, int stage, int iter, cudaStream_t s )
 {
+    cudaError_t e = cudaSuccess;
     const dim3 blk( 32, 8 );
     const dim3 grid( ( a.u.W + 31 ) / 32, ( a.u.H + 7 ) / 8 );
     const dim3 gridG( ( a.u.GW + 31 ) / 32, ( a.u.GH + 7 ) / 8 );
     switch( stage )
     {
-        case RGDN_STAGE_GRADIENT_SAMPLES: dev::k_gradient_samples< M ><<< gridG, blk, 0, s >>>( a, a.disPing ); break;
-        case RGDN_STAGE_GRADIENT_ATROUS: dev::k_gradient_atrous< M ><<< gridG, blk, 0, s >>>( a, iter ); break;
-        case RGDN_STAGE_TEMPORAL_ACCUMULATION: dev::k_temporal< M, false, false, false ><<< grid, blk, 0, s >>>( a ); break;
-        case KF_TEMPORAL_EXACT_GEOM: dev::k_temporal< M, false, true, false ><<< grid, blk, 0, s >>>( a ); break;
-        case KF_TEMPORAL_EXACT_GEOM_GP: dev::k_temporal< M, false, true, true ><<< grid, blk, 0, s >>>( a ); break;
-        case KF_TEMPORAL_FAST: dev::k_temporal< M, true, true, false ><<< grid, blk, 0, s >>>( a ); break;
-        case KF_TEMPORAL_FAST_GP: dev::k_temporal< M, true, true, true ><<< grid, blk, 0, s >>>( a ); break;
-        case KF_ANTI_FIREFLY_FAST: dev::k_antifirefly_fast< M ><<< grid, blk, 0, s >>>( a ); break;
-        case KF_VARIANCE_EXACT_GEOM: dev::k_variance_geo< M, false ><<< grid, blk, 0, s >>>( a ); break;
+        case RGDN_STAGE_GRADIENT_SAMPLES: e = launch_pdl( dev::k_gradient_samples< M >, gridG, blk, 0, s, a, a.disPing ); break;
+        case RGDN_STAGE_GRADIENT_ATROUS: e = launch_pdl( dev::k_gradient_atrous< M >, gridG, blk, 0, s, a, iter ); break;
+        case RGDN_STAGE_TEMPORAL_ACCUMULATION: e = launch_pdl( dev::k_temporal< M, false, false, false >, grid, blk, 0, s, a ); break;
+        case KF_TEMPORAL_EXACT_GEOM: e = launch_pdl( dev::k_temporal< M, false, true, false >, grid, blk, 0, s, a ); break;
+        case KF_TEMPORAL_EXACT_GEOM_GP: e = launch_pdl( dev::k_temporal< M, false, true, true >, grid, blk, 0, s, a ); break;
+        case KF_TEMPORAL_FAST: e = launch_pdl( dev::k_temporal< M, true, true, false >, grid, blk, 0, s, a ); break;
+        case KF_TEMPORAL_FAST_GP: e = launch_pdl( dev::k_temporal< M, true, true, true >, grid, blk, 0, s, a ); break;
+        case KF_ANTI_FIREFLY_FAST: e = launch_pdl( dev::k_antifirefly_fast< M >, grid, blk, 0, s, a ); break;
+        case KF_VARIANCE_EXACT_GEOM: e = launch_pdl( dev::k_variance_geo< M, false >, grid, blk, 0, s, a ); break;
         case RGDN_STAGE_ANTI_FIREFLY: dev::k_antifirefly< M ><<< grid, blk, 0, s >>>( a ); break;
         case RGDN_STAGE_VARIANCE_ESTIMATION: dev::k_variance< M ><<< grid, blk, 0, s >>>( a ); break;
-        case RGDN_STAGE_ATROUS: dev::k_atrous< M, false, false, false ><<< grid, blk, 0, s >>>( a, iter ); break;
-        case KF_ATROUS_EXACT: dev::k_atrous< M, false, false, true ><<< grid, blk, 0, s >>>( a, iter ); break;
+        case RGDN_STAGE_ATROUS: e = launch_pdl( dev::k_atrous< M, false, false, false >, grid, blk, 0, s, a, iter ); break;
+        case KF_ATROUS_EXACT: e = launch_pdl( dev::k_atrous< M, false, false, true >, grid, blk, 0, s, a, iter ); break;
         case RGDN_STAGE_LUMINANCE_HISTOGRAM: dev::k_histogram< M ><<< grid, blk, 0, s >>>( a ); break;
-        case RGDN_STAGE_LUMINANCE_AVG: dev::k_luminance_avg< M ><<< 1, 256, 0, s >>>( a ); break;
-        case KF_ATROUS_EXACT_HIST: dev::k_atrous< M, false, true, true ><<< grid, blk, 0, s >>>( a, iter ); break;
+        case RGDN_STAGE_LUMINANCE_AVG: e = launch_pdl( dev::k_luminance_avg< M >, 1, 256, 0, s, a ); break;
+        case KF_ATROUS_EXACT_HIST: e = launch_pdl( dev::k_atrous< M, false, true, true >, grid, blk, 0, s, a, iter ); break;
         default: return cudaErrorInvalidValue;
     }
-    return cudaGetLastError();
+    return e != cudaSuccess ? e : cudaGetLastError();
 }
 
 // Kernels whose results are continuous in every arithmetic operation (no threshold follows
@@ -2166,16 +2225,17 @@ template< int M > cudaError_t launch_stage_t( const FrameArgs& a, int stage, int
 // fused multiply-adds.
 template< int M > cudaError_t launch_fast_t( const FrameArgs& a, int stage, int iter, cudaStream_t s )
 {
+    cudaError_t e = cudaSuccess;
     const dim3 blk( 32, 8 );
     const dim3 grid( ( a.u.W + 31 ) / 32, ( a.u.H + 7 ) / 8 );
     switch( stage )
     {
-        case KF_ATROUS_FAST: dev::k_atrous< M, true, false, true ><<< grid, blk, 0, s >>>( a, iter ); break;
-        case KF_ATROUS_FAST_HIST: dev::k_atrous< M, true, true, true ><<< grid, blk, 0, s >>>( a, iter ); break;
-        case KF_VARIANCE_FAST: dev::k_variance_geo< M, true ><<< grid, blk, 0, s >>>( a ); break;
+        case KF_ATROUS_FAST: e = launch_pdl( dev::k_atrous< M, true, false, true >, grid, blk, 0, s, a, iter ); break;
+        case KF_ATROUS_FAST_HIST: e = launch_pdl( dev::k_atrous< M, true, true, true >, grid, blk, 0, s, a, iter ); break;
+        case KF_VARIANCE_FAST: e = launch_pdl( dev::k_variance_geo< M, true >, grid, blk, 0, s, a ); break;
         default: return cudaErrorInvalidValue;
     }
-    return cudaGetLastError();
+    return e != cudaSuccess ? e : cudaGetLastError();
 }
 
 // Batched launches. `iter` carries variants in its high bits: for the temporal pass the
@@ -2183,45 +2243,47 @@ template< int M > cudaError_t launch_fast_t( const FrameArgs& a, int stage, int 
 // resident blocks per SM it is built for (bits 10-12: 3 or 4, i.e. 80 or 64 registers).
 template< int M > cudaError_t launch_batch_t( int stage, int iter, int slot, dim3 block, int grid, cudaStream_t s )
 {
+    cudaError_t e = cudaSuccess;
     const int v = ( iter >> 8 ) & 3, it = iter & 0xff;
     switch( stage )
     {
-        case RGDN_STAGE_GRADIENT_SAMPLES: dev::kb_gradient_samples< M ><<< grid, block, 0, s >>>( slot ); break;
-        case RGDN_STAGE_GRADIENT_ATROUS: dev::kb_gradient_atrous< M ><<< grid, block, 0, s >>>( slot, it ); break;
+        case RGDN_STAGE_GRADIENT_SAMPLES: e = launch_pdl( dev::kb_gradient_samples< M >, grid, block, 0, s, slot ); break;
+        case RGDN_STAGE_GRADIENT_ATROUS: e = launch_pdl( dev::kb_gradient_atrous< M >, grid, block, 0, s, slot, it ); break;
         case RGDN_STAGE_TEMPORAL_ACCUMULATION:
-            if( v == 0 ) dev::kb_temporal< M, 0 ><<< grid, block, 0, s >>>( slot );
-            else if( v == 1 ) dev::kb_temporal< M, 1 ><<< grid, block, 0, s >>>( slot );
-            else dev::kb_temporal< M, 2 ><<< grid, block, 0, s >>>( slot );
+            if( v == 0 ) e = launch_pdl( dev::kb_temporal< M, 0 >, grid, block, 0, s, slot );
+            else if( v == 1 ) e = launch_pdl( dev::kb_temporal< M, 1 >, grid, block, 0, s, slot );
+            else e = launch_pdl( dev::kb_temporal< M, 2 >, grid, block, 0, s, slot );
             break;
-        case RGDN_STAGE_ANTI_FIREFLY: dev::kb_antifirefly< M ><<< grid, block, 0, s >>>( slot ); break;
-        case RGDN_STAGE_LUMINANCE_AVG: dev::kb_luminance_avg< M ><<< grid, 256, 0, s >>>( slot ); break;
+        case RGDN_STAGE_ANTI_FIREFLY: e = launch_pdl( dev::kb_antifirefly< M >, grid, block, 0, s, slot ); break;
+        case RGDN_STAGE_LUMINANCE_AVG: e = launch_pdl( dev::kb_luminance_avg< M >, grid, 256, 0, s, slot ); break;
         default: return cudaErrorInvalidValue;
     }
-    return cudaGetLastError();
+    return e != cudaSuccess ? e : cudaGetLastError();
 }
 template< int M > cudaError_t launch_batch_fast_t( int stage, int iter, int slot, dim3 block, int grid, cudaStream_t s )
 {
+    cudaError_t e = cudaSuccess;
     switch( stage )
     {
-        case RGDN_STAGE_VARIANCE_ESTIMATION: dev::kb_variance< M ><<< grid, block, 0, s >>>( slot ); break;
+        case RGDN_STAGE_VARIANCE_ESTIMATION: e = launch_pdl( dev::kb_variance< M >, grid, block, 0, s, slot ); break;
         case RGDN_STAGE_ATROUS:
         {
             const int hm = ( iter >> 8 ) & 3, occ = ( iter >> 10 ) & 7, it = iter & 0xff;
             switch( occ * 4 + hm )
             {
-                case 12: dev::kb_atrous< M, 0, 3 ><<< grid, block, 0, s >>>( slot, it ); break;
-                case 13: dev::kb_atrous< M, 1, 3 ><<< grid, block, 0, s >>>( slot, it ); break;
-                case 14: dev::kb_atrous< M, 2, 3 ><<< grid, block, 0, s >>>( slot, it ); break;
-                case 16: dev::kb_atrous< M, 0, 4 ><<< grid, block, 0, s >>>( slot, it ); break;
-                case 17: dev::kb_atrous< M, 1, 4 ><<< grid, block, 0, s >>>( slot, it ); break;
-                case 18: dev::kb_atrous< M, 2, 4 ><<< grid, block, 0, s >>>( slot, it ); break;
+                case 12: e = launch_pdl( dev::kb_atrous< M, 0, 3 >, grid, block, 0, s, slot, it ); break;
+                case 13: e = launch_pdl( dev::kb_atrous< M, 1, 3 >, grid, block, 0, s, slot, it ); break;
+                case 14: e = launch_pdl( dev::kb_atrous< M, 2, 3 >, grid, block, 0, s, slot, it ); break;
+                case 16: e = launch_pdl( dev::kb_atrous< M, 0, 4 >, grid, block, 0, s, slot, it ); break;
+                case 17: e = launch_pdl( dev::kb_atrous< M, 1, 4 >, grid, block, 0, s, slot, it ); break;
+                case 18: e = launch_pdl( dev::kb_atrous< M, 2, 4 >, grid, block, 0, s, slot, it ); break;
                 default: return cudaErrorInvalidValue;
             }
             break;
         }
         default: return cudaErrorInvalidValue;
     }
-    return cudaGetLastError();
+    return e != cudaSuccess ? e : cudaGetLastError();
 }
 template< class K > int blocks_per_sm( K kernel )
 {
