@@ -276,6 +276,10 @@ rgdn_status rgdn_stream_tonemapping_device( rgdn_stream* stream, void** outDevic
 /* Synchronous read of the tonemapping state after the work on cudaStream. `exposure`
  * is ev100ToLuminousExposure(getAutoEV100()) of Exposure.h:33-51. Any out pointer may be NULL. */
 rgdn_status rgdn_get_tonemapping( rgdn_stream* stream, uint32_t* outHistogram256, float* outAvgLuminance, float* outExposure, rgdn_cuda_stream cudaStream );
+/* Asynchronous copy, in cudaStream order, of { uint histogram[256]; float avgLuminance; }
+ * (1028 bytes) to dst (host, pinned for overlap, or device). No reference counterpart: later
+ * passes of the reference read the SSBO on the GPU. */
+rgdn_status rgdn_stream_copy_tonemapping( rgdn_stream* stream, void* dst, rgdn_cuda_stream cudaStream );
 /* Overwrites the tonemapping state (test fixtures, stream migration). */
 rgdn_status rgdn_set_tonemapping( rgdn_stream* stream, const uint32_t* histogram256, float avgLuminance, rgdn_cuda_stream cudaStream );
 

@@ -147,6 +147,7 @@ SIGNATURES = [
     ("rgdn_stream_tonemapping_device", _I, [_VP, C.POINTER(_VP)]),
     ("rgdn_get_tonemapping", _I, [_VP, C.POINTER(_U32), C.POINTER(C.c_float), C.POINTER(C.c_float), _VP]),
     ("rgdn_set_tonemapping", _I, [_VP, C.POINTER(_U32), C.c_float, _VP]),
+    ("rgdn_stream_copy_tonemapping", _I, [_VP, _VP, _VP]),
     ("rgdn_submit_batch", _I, [_VP, C.POINTER(Job), _U32, _VP]),
     ("rgdn_status_string", C.c_char_p, [_I]),
     ("rgdn_context_launch_count", _I, [_VP, C.POINTER(_U64)]),

@@ -8,6 +8,7 @@
 //                                :640-699 (sizes, FORCE_SIZE_1_3 = (W+1)/3)
 //   RgResult / Call<> wrapper    Source/RTGL1.cpp:145-195 (no exceptions cross the ABI)
 #include <algorithm>
+#include <cstddef>
 #include <atomic>
 #include <cmath>
 #include <cstdio>
@@ -907,6 +908,15 @@ rgdn_status rgdn_get_tonemapping( rgdn_stream* s, uint32_t* hist, float* avgLum,
         *exposure              = maxLum > 0.0f ? 1.0f / maxLum : 0.0f;
     }
     return RGDN_SUCCESS;
+}
+
+rgdn_status rgdn_stream_copy_tonemapping( rgdn_stream* s, void* dst, rgdn_cuda_stream cs )
+{
+    if( !valid_stream( s ) ) return RGDN_WRONG_INSTANCE;
+    if( !dst ) return RGDN_WRONG_FUNCTION_ARGUMENT;
+    cudaSetDevice( s->ctx->device );
+    const size_t bytes = offsetof( Tonemapping, avgLuminance ) + sizeof( float );
+    return cuda_status( cudaMemcpyAsync( dst, s->tm, bytes, cudaMemcpyDefault, (cudaStream_t)cs ) );
 }
 
 rgdn_status rgdn_set_tonemapping( rgdn_stream* s, const uint32_t* hist, float avgLum, rgdn_cuda_stream cs )
