@@ -659,17 +659,21 @@ __device__ __forceinline__ void temporal_tile( const FrameArgs& a, int bx, int b
             if( ok )
             {
                 // in_area implies inside the image
+                // FAST: fused multiply-adds for the continuous sums; the diffuse history length
+                // (the variance pass switches on it) and the weight sum stay IEEE
+                using X         = Wm< FAST >;
                 const float  w  = bw[ yy ][ xx ];
                 const float4 dc = S::ldcv( a.diffHistory, a.varHistory, q );
-                diffPrev        = add( diffPrev, mul( f3( dc.x, dc.y, dc.z ), w ) );
+                diffPrev        = f3( X::madd( dc.x, w, diffPrev.x ), X::madd( dc.y, w, diffPrev.y ), X::madd( dc.z, w, diffPrev.z ) );
                 const float2 m  = S::ld2( a.momentsPrev, q );
-                momentsPrev     = make_float2( momentsPrev.x + w * m.x, momentsPrev.y + w * m.y );
+                momentsPrev     = make_float2( X::madd( w, m.x, momentsPrev.x ), X::madd( w, m.y, momentsPrev.y ) );
                 const float4 hl = S::ld4( a.histLenPrev, q );
-                histLenDIS = make_float4( histLenDIS.x + w * hl.x, histLenDIS.y + w * hl.y, histLenDIS.z + w * hl.z, histLenDIS.w + w * hl.w );
+                histLenDIS = make_float4( histLenDIS.x + w * hl.x, X::madd( w, hl.y, histLenDIS.y ), X::madd( w, hl.z, histLenDIS.z ),
+                                          X::madd( w, hl.w, histLenDIS.w ) );
                 const float3 sp = S::ld3( a.specAccumPrev, q );
-                specPrevOnSurf  = add( specPrevOnSurf, f3( w * sp.x, w * sp.y, w * sp.z ) );
+                specPrevOnSurf  = f3( X::madd( w, sp.x, specPrevOnSurf.x ), X::madd( w, sp.y, specPrevOnSurf.y ), X::madd( w, sp.z, specPrevOnSurf.z ) );
                 const float3 ip = S::ld3( a.indirAccumPrev, q );
-                indirPrev       = add( indirPrev, f3( w * ip.x, w * ip.y, w * ip.z ) );
+                indirPrev       = f3( X::madd( w, ip.x, indirPrev.x ), X::madd( w, ip.y, indirPrev.y ), X::madd( w, ip.z, indirPrev.z ) );
                 weightSum       = weightSum + w;
             }
         }
