@@ -48,6 +48,22 @@ EncodeTiledFn encode_tiled_fn()
     }
     return fn;
 }
+
+// The temporal pass's history-length decay pow(1 - g, 10) (CmSVGFTemporalAccumulation.comp:
+// 339, 356) for the 256 unorm8 gradient values g = k / 255: the expression the exact kernels
+// evaluate inline, in the same FP32 operations, so the fast kernels read the same bits.
+__global__ void k_fill_decay( float* t )
+{
+    const int   k = threadIdx.x;
+    const float g = (float)k / 255.0f;
+    t[ k ]        = powf( 1.0f - g, 10.0f );
+}
+cudaError_t fill_decay_table( float* t )
+{
+    k_fill_decay<<< 1, 256 >>>( t );
+    const cudaError_t e = cudaGetLastError();
+    return e != cudaSuccess ? e : cudaDeviceSynchronize();
+}
 }  // namespace
 
 namespace
@@ -323,6 +339,7 @@ void fill_args( rgdn_stream* s, uint32_t fi, const rgdn_frame_params* p, FrameAr
     a.binLut   = s->binLut;
     a.phiTab   = s->ctx->phiTab;
     a.thetaTab = s->ctx->thetaTab;
+    a.decay10  = s->ctx->decayTab;
 }
 
 cudaEvent_t take_event( rgdn_stream* s )
@@ -593,11 +610,14 @@ rgdn_status rgdn_context_create( const rgdn_context_create_info* info, rgdn_cont
     }
     if( cudaMalloc( &c->phiTab, 65536 * sizeof( float2 ) ) != cudaSuccess ||
         cudaMalloc( &c->thetaTab, 65536 * sizeof( float2 ) ) != cudaSuccess ||
+        cudaMalloc( &c->decayTab, 256 * sizeof( float ) ) != cudaSuccess ||
         cudaMemcpy( c->phiTab, ph.data(), 65536 * sizeof( float2 ), cudaMemcpyHostToDevice ) != cudaSuccess ||
-        cudaMemcpy( c->thetaTab, th.data(), 65536 * sizeof( float2 ), cudaMemcpyHostToDevice ) != cudaSuccess )
+        cudaMemcpy( c->thetaTab, th.data(), 65536 * sizeof( float2 ), cudaMemcpyHostToDevice ) != cudaSuccess ||
+        fill_decay_table( c->decayTab ) != cudaSuccess )
     {
         cudaFree( c->phiTab );
         cudaFree( c->thetaTab );
+        cudaFree( c->decayTab );
         c->magic = 0;
         delete c;
         return RGDN_DEVICE_ERROR;
@@ -619,6 +639,7 @@ rgdn_status rgdn_context_destroy( rgdn_context* c )
     for( rgdn_stream* s : left ) rgdn_stream_destroy( s );
     cudaFree( c->phiTab );
     cudaFree( c->thetaTab );
+    cudaFree( c->decayTab );
     c->magic = 0;
     delete c;
     return RGDN_SUCCESS;

@@ -28,6 +28,7 @@ struct rgdn_context
     std::set< rgdn_stream* > streams;
     float2*                 phiTab   = nullptr;   // (sin phi_j, cos phi_j)
     float2*                 thetaTab = nullptr;   // (cos theta_k, sin theta_k)
+    float*                  decayTab = nullptr;   // pow(1 - k/255, 10), k = 0..255
     std::atomic< uint64_t > launches{ 0 };
     std::mutex              batchMtx;              // guards `batch`
     rgdn::BatchExec*        batch = nullptr;       // created by the first batched submission

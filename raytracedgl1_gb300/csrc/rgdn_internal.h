@@ -117,6 +117,9 @@ struct alignas( 16 ) FrameArgs
     // normal decode tables: phi[j] = (sin, cos), theta[k] = (cos, sin)
     const float2* phiTab;
     const float2* thetaTab;
+    // pow(1 - k/255, 10) for the 256 unorm8 gradient values k, computed on the device with the
+    // powf the exact path calls inline (the same bits): the history-length decay
+    const float* decay10;
 };
 
 // Kernels of the default (fused, fast-math) path, beyond the per-stage rgdn_stage ids.

@@ -139,9 +139,23 @@ __device__ __forceinline__ float lg2_approx( float x )
     asm( "lg2.approx.ftz.f32 %0, %1;" : "=f"( r ) : "f"( x ) );
     return r;
 }
+__device__ __forceinline__ float rcp_approx( float x )
+{
+    float r;
+    asm( "rcp.approx.ftz.f32 %0, %1;" : "=f"( r ) : "f"( x ) );
+    return r;
+}
+__device__ __forceinline__ float sqrt_approx( float x )
+{
+    float r;
+    asm( "sqrt.approx.ftz.f32 %0, %1;" : "=f"( r ) : "f"( x ) );
+    return r;
+}
 template< bool FAST > struct Wm;
 template<> struct Wm< false >
 {
+    __device__ static float  mix( float x, float y, float a ) { return gmix( x, y, a ); }
+    __device__ static float3 vmix( float3 x, float3 y, float a ) { return ::rgdn::dev::vmix( x, y, a ); }
     __device__ static float pow128( float x ) { return powf( x, 128.0f ); }
     __device__ static float powv( float x, float y ) { return powf( x, y ); }
     __device__ static float pow01( float x, float y ) { return powf( x, y ); }
@@ -173,6 +187,9 @@ template<> struct Wm< true >
     }
     __device__ static float expn( float x ) { return ex2_approx( x * 1.44269504088896341f ); }
     __device__ static float madd( float a, float b, float c ) { return __fmaf_rn( a, b, c ); }
+    // x + a (y - x)
+    __device__ static float  mix( float x, float y, float a ) { return __fmaf_rn( a, y - x, x ); }
+    __device__ static float3 vmix( float3 x, float3 y, float a ) { return f3( mix( x.x, y.x, a ), mix( x.y, y.y, a ), mix( x.z, y.z, a ) ); }
     // luminance and dot products as fused multiply-add chains
     __device__ static float lum( float3 c ) { return __fmaf_rn( 0.0721f, c.z, __fmaf_rn( 0.7154f, c.y, 0.2125f * c.x ) ); }
     __device__ static float dot( float3 a, float3 b ) { return __fmaf_rn( a.z, b.z, __fmaf_rn( a.y, b.y, a.x * b.x ) ); }
@@ -326,6 +343,18 @@ __device__ __forceinline__ float2 prev_screen_pos( const Uniform& u, float2 m, i
 // ShaderCommonGLSLFunc.h:368-390
 __device__ __forceinline__ bool test_depth( float z, float zPrev, float zMotion ) { return fabsf( z - zPrev + zMotion ) / fabsf( z ) < 0.1f; }
 __device__ __forceinline__ bool test_normal( float3 n, float3 np ) { return dot3( n, np ) > 0.95f; }
+// test_depth's decision from rz = rcp.approx(|z|) (relative error below 2^-22): the product
+// n * rz lies within 2^-21 (relative) of the quotient n / |z|, so outside a band of 1e-6
+// (relative) around 0.1 it decides as the rounded quotient would; inside the band, and for
+// NaN, the IEEE quotient decides.
+__device__ __forceinline__ bool test_depth_r( float z, float rz, float zPrev, float zMotion )
+{
+    const float n = fabsf( z - zPrev + zMotion );
+    const float t = n * rz;
+    if( t < 0.0999999f ) return true;
+    if( t > 0.1000001f ) return false;
+    return n / fabsf( z ) < 0.1f;
+}
 __device__ __forceinline__ float antilag( float g, float nf )
 {
     float lambda = nf > 0.0001f ? gclamp( fabsf( g ) / nf, 0.0f, 1.0f ) : 0.0f;
@@ -583,34 +612,40 @@ __device__ __forceinline__ float parallax( const Uniform& u, float3 pos, float3 
     return par * 60.0f;
 }
 
-// FAST: continuous specular terms in hardware exp2/log2, shared subexpressions and the
-// precombined view-projection matrices. GEOM: write this frame's geometry record. GEOMPREV:
-// read the previous frame's record (decoded normal + depth, the same values) at the taps.
+// FAST: continuous specular terms in hardware exp2/log2/sqrt, shared subexpressions, the
+// precombined view-projection matrices, fused multiply-adds in the continuous sums and blends,
+// the depth test through a reciprocal (exact near its threshold) and the history-length decay
+// from the device table (the same bits as the inline powf). GEOM: write this frame's geometry
+// record. GEOMPREV: read the previous frame's record (decoded normal + depth, the same values)
+// at the taps.
 template< int M, bool FAST, bool GEOM, bool GEOMPREV >
 __device__ __forceinline__ void temporal_tile( const FrameArgs& a, int bx, int by, const float* u8 )
 {
     using S          = Sto< M >;
+    using X          = Wm< FAST >;
     const Uniform& u = a.u;
     const int      px = bx * blockDim.x + threadIdx.x;
     const int      py = by * blockDim.y + threadIdx.y;
     if( px >= u.W || py >= u.H ) return;
-    const size_t i = idx( u, px, py );
+    const int i = py * u.W + px;
 
-    const float3  unfilteredDiff  = e5( a.unfD[ i ] );
-    const float3  unfilteredIndir = e5( a.unfI[ i ] );
-    const float3  unfilteredSpec  = e5( a.unfS[ i ] );
-    const ushort4 rv              = a.viewDir[ i ];
-    const float4  rayInfo         = make_float4( h2f( rv.x ), h2f( rv.y ), h2f( rv.z ), h2f( rv.w ) );
-    const Area    chArea          = cb_area( u, px );
-    const ushort4 mo              = a.motion[ i ];
-    const float   motionZ         = h2f( mo.z );
-    const float   z               = h2f( a.depth[ i ] );
-    const float3  normal          = decode_normal( a, a.normal[ i ] );
-    const uint16_t mrBits         = a.mr[ i ];
-    const float   roughness       = u8[ mrBits >> 8 ];
-    if( GEOM ) a.geom[ i ] = geo_pack( normal, a.depth[ i ], mrBits );
+    const float3   unfilteredDiff  = e5( a.unfD[ i ] );
+    const float3   unfilteredIndir = e5( a.unfI[ i ] );
+    const float3   unfilteredSpec  = e5( a.unfS[ i ] );
+    const ushort4  rv              = a.viewDir[ i ];
+    const float4   rayInfo         = make_float4( h2f( rv.x ), h2f( rv.y ), h2f( rv.z ), h2f( rv.w ) );
+    const Area     chArea          = cb_area( u, px );
+    const ushort4  mo              = a.motion[ i ];
+    const float    motionZ         = h2f( mo.z );
+    const uint16_t zBits           = a.depth[ i ];
+    const float    z               = h2f( zBits );
+    const float    rz              = FAST ? rcp_approx( fabsf( z ) ) : 0.0f;
+    const float3   normal          = decode_normal( a, a.normal[ i ] );
+    const uint16_t mrBits          = a.mr[ i ];
+    const float    roughness       = u8[ mrBits >> 8 ];
+    if( GEOM ) a.geom[ i ] = geo_pack( normal, zBits, mrBits );
 
-    const float l = luminance( unfilteredDiff );
+    const float  l       = X::lum( unfilteredDiff );
     const float2 moments = make_float2( l, l * l );
 
     int2   pixPrev;
@@ -625,6 +660,11 @@ __device__ __forceinline__ void temporal_tile( const FrameArgs& a, int bx, int b
         { ( 1.0f - subPix.x ) * ( 1.0f - subPix.y ), subPix.x * ( 1.0f - subPix.y ) },
         { ( 1.0f - subPix.x ) * subPix.y, subPix.x * subPix.y },
     };
+    // the surface positions the specular terms read once a tap is accepted, loaded with the
+    // taps rather than after them
+    const float4 sp4 = a.surfPos[ i ];
+    const float4 spp4 =
+        inside( u, pixPrev.x, pixPrev.y ) ? a.surfPosPrev[ pixPrev.y * u.W + pixPrev.x ] : make_float4( 0, 0, 0, 0 );
 
     float4 histLenDIS     = make_float4( 0, 0, 0, 0 );
     float3 diffPrev       = f3( 0, 0, 0 );
@@ -639,114 +679,143 @@ __device__ __forceinline__ void temporal_tile( const FrameArgs& a, int bx, int b
 #pragma unroll
         for( int xx = 0; xx <= 1; xx++ )
         {
-            const int   qx = pixPrev.x + xx, qy = pixPrev.y + yy;
-            const bool  in = inside( u, qx, qy );
-            const size_t q = in ? idx( u, qx, qy ) : 0;
-            float        dP;
-            float3       nP;
+            const int qx = pixPrev.x + xx, qy = pixPrev.y + yy;
+            // in_area implies inside the image; a tap outside the area is rejected whatever
+            // its texel holds
+            if( !in_area( qx, qy, chArea ) ) continue;
+            const int q = qy * u.W + qx;
+            float     dP;
+            float3    nP;
             if( GEOMPREV )
             {
-                const Geo gp = in ? geo_load( a.geomPrev, (int)q ) : geo_zero();
+                const Geo gp = geo_load( a.geomPrev, q );
                 dP           = geo_depth( gp );
                 nP           = gp.n;
             }
             else
             {
-                dP = in ? h2f( a.depthPrev[ q ] ) : 0.0f;
-                nP = decode_normal( a, in ? a.normalPrev[ q ] : 0u );
+                dP = h2f( a.depthPrev[ q ] );
+                nP = decode_normal( a, a.normalPrev[ q ] );
             }
-            const bool ok = in_area( qx, qy, chArea ) && test_depth( z, dP, motionZ ) && test_normal( normal, nP );
-            if( ok )
+            const bool okDepth = FAST ? test_depth_r( z, rz, dP, motionZ ) : test_depth( z, dP, motionZ );
+            if( okDepth && test_normal( normal, nP ) )
             {
-                // in_area implies inside the image
                 // FAST: fused multiply-adds for the continuous sums; the diffuse history length
                 // (the variance pass switches on it) and the weight sum stay IEEE
-                using X         = Wm< FAST >;
                 const float  w  = bw[ yy ][ xx ];
                 const float4 dc = S::ldcv( a.diffHistory, a.varHistory, q );
-                diffPrev        = f3( X::madd( dc.x, w, diffPrev.x ), X::madd( dc.y, w, diffPrev.y ), X::madd( dc.z, w, diffPrev.z ) );
                 const float2 m  = S::ld2( a.momentsPrev, q );
-                momentsPrev     = make_float2( X::madd( w, m.x, momentsPrev.x ), X::madd( w, m.y, momentsPrev.y ) );
                 const float4 hl = S::ld4( a.histLenPrev, q );
-                histLenDIS = make_float4( histLenDIS.x + w * hl.x, X::madd( w, hl.y, histLenDIS.y ), X::madd( w, hl.z, histLenDIS.z ),
-                                          X::madd( w, hl.w, histLenDIS.w ) );
                 const float3 sp = S::ld3( a.specAccumPrev, q );
-                specPrevOnSurf  = f3( X::madd( w, sp.x, specPrevOnSurf.x ), X::madd( w, sp.y, specPrevOnSurf.y ), X::madd( w, sp.z, specPrevOnSurf.z ) );
                 const float3 ip = S::ld3( a.indirAccumPrev, q );
-                indirPrev       = f3( X::madd( w, ip.x, indirPrev.x ), X::madd( w, ip.y, indirPrev.y ), X::madd( w, ip.z, indirPrev.z ) );
-                weightSum       = weightSum + w;
+                if constexpr( FAST )
+                {
+                    // the fourteen continuous sums as seven packed FP32 FMAs (the bits of the
+                    // scalar FMAs)
+                    const float2 ww = make_float2( w, w );
+                    const float2 p0 = __ffma2_rn( make_float2( dc.x, dc.y ), ww, make_float2( diffPrev.x, diffPrev.y ) );
+                    const float2 p1 = __ffma2_rn( make_float2( dc.z, m.x ), ww, make_float2( diffPrev.z, momentsPrev.x ) );
+                    const float2 p2 = __ffma2_rn( make_float2( m.y, hl.y ), ww, make_float2( momentsPrev.y, histLenDIS.y ) );
+                    const float2 p3 = __ffma2_rn( make_float2( hl.z, hl.w ), ww, make_float2( histLenDIS.z, histLenDIS.w ) );
+                    const float2 p4 = __ffma2_rn( make_float2( sp.x, sp.y ), ww, make_float2( specPrevOnSurf.x, specPrevOnSurf.y ) );
+                    const float2 p5 = __ffma2_rn( make_float2( sp.z, ip.x ), ww, make_float2( specPrevOnSurf.z, indirPrev.x ) );
+                    const float2 p6 = __ffma2_rn( make_float2( ip.y, ip.z ), ww, make_float2( indirPrev.y, indirPrev.z ) );
+                    diffPrev       = f3( p0.x, p0.y, p1.x );
+                    momentsPrev    = make_float2( p1.y, p2.x );
+                    histLenDIS     = make_float4( histLenDIS.x + w * hl.x, p2.y, p3.x, p3.y );
+                    specPrevOnSurf = f3( p4.x, p4.y, p5.x );
+                    indirPrev      = f3( p5.y, p6.x, p6.y );
+                }
+                else
+                {
+                    diffPrev       = f3( dc.x * w + diffPrev.x, dc.y * w + diffPrev.y, dc.z * w + diffPrev.z );
+                    momentsPrev    = make_float2( w * m.x + momentsPrev.x, w * m.y + momentsPrev.y );
+                    histLenDIS     = make_float4( histLenDIS.x + w * hl.x, w * hl.y + histLenDIS.y, w * hl.z + histLenDIS.z, w * hl.w + histLenDIS.w );
+                    specPrevOnSurf = f3( w * sp.x + specPrevOnSurf.x, w * sp.y + specPrevOnSurf.y, w * sp.z + specPrevOnSurf.z );
+                    indirPrev      = f3( w * ip.x + indirPrev.x, w * ip.y + indirPrev.y, w * ip.z + indirPrev.z );
+                }
+                weightSum = weightSum + w;
             }
         }
     }
 
-    float aD = 0.0f, aI = 0.0f, aS = 0.0f;
+    // the filtered gradients (unorm8) and, FAST, their history-length decay from the table
+    float aD = 0.0f, aI = 0.0f, aS = 0.0f, decD = 1.0f, decI = 1.0f;
     if( !( u.flags & RGDN_FLAG_SKIP_GRADIENTS ) )
     {
-        const float4 g = ld_rgba8t( u, a.disPing, px / STRATA, py / STRATA, u8 );
-        aD = g.x; aI = g.y; aS = g.z;
+        const int      gx = px / STRATA, gy = py / STRATA;
+        const uint32_t g  = ( gx < u.GW && gy < u.GH ) ? a.disPing[ gy * u.GW + gx ] : 0u;
+        aD = u8[ g & 0xFFu ];
+        aI = u8[ ( g >> 8 ) & 0xFFu ];
+        aS = u8[ ( g >> 16 ) & 0xFFu ];
+        if( FAST )
+        {
+            decD = __ldg( &a.decay10[ g & 0xFFu ] );
+            decI = __ldg( &a.decay10[ ( g >> 8 ) & 0xFFu ] );
+        }
     }
+
+    const bool hasHistory = weightSum > 0.0001f;
+    // FAST: the one IEEE reciprocal both the continuous averages and the diffuse history
+    // length use
+    const float invWS = ( FAST && hasHistory ) ? 1.0f / weightSum : 0.0f;
 
     float3 specColorAccum;
     float  specHistoryLengthAccum, specHitDistanceAccum;
 
-    if( weightSum > 0.0001f )
+    if( hasHistory )
     {
-        // FAST: one IEEE reciprocal for the averages that feed only continuous terms
-        const float invW                = FAST ? 1.0f / weightSum : 0.0f;
-        specPrevOnSurf                  = FAST ? mul( specPrevOnSurf, invW ) : divs( specPrevOnSurf, weightSum );
-        const float specHistoryLength   = FAST ? histLenDIS.z * invW : histLenDIS.z / weightSum;
-        const float specHitDistancePrev = FAST ? histLenDIS.w * invW : histLenDIS.w / weightSum;
+        specPrevOnSurf                  = FAST ? mul( specPrevOnSurf, invWS ) : divs( specPrevOnSurf, weightSum );
+        const float specHistoryLength   = FAST ? histLenDIS.z * invWS : histLenDIS.z / weightSum;
+        const float specHitDistancePrev = FAST ? histLenDIS.w * invWS : histLenDIS.w / weightSum;
 
-        const float4 sp4     = a.surfPos[ i ];
-        const float3 surfPos = f3( sp4.x, sp4.y, sp4.z );
-        float3       surfPosPrev = f3( 0, 0, 0 );
-        if( inside( u, pixPrev.x, pixPrev.y ) )
-        {
-            const float4 spp = a.surfPosPrev[ idx( u, pixPrev.x, pixPrev.y ) ];
-            surfPosPrev      = f3( spp.x, spp.y, spp.z );
-        }
-        const float nv = fmaxf( 0.0f, dot3( normal, f3( -rayInfo.x, -rayInfo.y, -rayInfo.z ) ) );
+        const float3 surfPos     = f3( sp4.x, sp4.y, sp4.z );
+        const float3 surfPosPrev = f3( spp4.x, spp4.y, spp4.z );
+        const float nv = fmaxf( 0.0f, X::dot( normal, f3( -rayInfo.x, -rayInfo.y, -rayInfo.z ) ) );
         if constexpr( FAST )
         {
-            const float minA = spec_min_accum( u );
+            const float td   = u.timeDelta;
+            const float minA = gclamp( 0.2f * ( td <= 0.0f ? 0.0f : rcp_approx( td ) ), 0.0f, 128.0f );
             const float oma  = 1.0f - aS;
             const float A    = gclamp( 1.0f + specHistoryLength * ( oma * oma * oma * oma * oma ), minA, 256.0f );
             // getParallax (:58-69): normalize(pos) . normalize(posPrev - cameraDelta)
             const float3 camDelta = f3( u.camPosPrev[ 0 ] - u.camPos[ 0 ], u.camPosPrev[ 1 ] - u.camPos[ 1 ], u.camPosPrev[ 2 ] - u.camPos[ 2 ] );
             const float3 pp   = sub( surfPosPrev, camDelta );
-            const float  cosa = gsat( dot3( surfPos, pp ) * rsqrtf( dot3( surfPos, surfPos ) ) * rsqrtf( dot3( pp, pp ) ) );
-            const float  par  = __fdividef( sqrtf( 1.0f - cosa * cosa ), fmaxf( cosa, 1e-6f ) ) * 60.0f;
+            const float  cosa = gsat( X::dot( surfPos, pp ) * rsqrtf( X::dot( surfPos, surfPos ) ) * rsqrtf( X::dot( pp, pp ) ) );
+            const float  par  = __fdividef( sqrt_approx( X::one_minus( cosa, cosa ) ), fmaxf( cosa, 1e-6f ) ) * 60.0f;
             // getSpecAccumSpeed (:80-92) for the surface and the virtual motion share every
             // term but the parallax
             const float aa = ex2_approx( 0.66f * __log2f( gsat( 1.0f - nv ) ) );
-            const float b  = 1.1f + roughness * roughness;
+            const float b  = X::madd( roughness, roughness, 1.1f );
             const float ps = __fdividef( b + aa, b - aa );
             const float f0 = 1.0f - ex2_approx( -200.0f * roughness * roughness );
             const float lr = __log2f( gsat( roughness ) );
-            const float AOnSurf = gclamp( 256.0f * ( f0 * ex2_approx( 0.5f * ( 1.0f + par * ps ) * lr ) ), minA, A );
+            const float AOnSurf = gclamp( 256.0f * ( f0 * ex2_approx( 0.5f * X::madd( par, ps, 1.0f ) * lr ) ), minA, A );
             // getSpecularDominantFactor (:93-99)
-            const float da    = 0.298475f * __logf( 39.4115f - 39.0029f * roughness );
-            const float domin = gclamp( ex2_approx( 10.8649f * __log2f( gclamp( 1.0f - nv, 0.0f, 1.0f ) ) ) * ( 1.0f - da ) + da, 0.0f, 1.0f );
+            const float da    = 0.298475f * __logf( X::madd( -39.0029f, roughness, 39.4115f ) );
+            const float domin = gclamp( X::madd( ex2_approx( 10.8649f * __log2f( gclamp( 1.0f - nv, 0.0f, 1.0f ) ) ), 1.0f - da, da ), 0.0f, 1.0f );
 
             const float  invA          = __fdividef( 1.0f, 1.0f + AOnSurf );
-            const float3 specOnSurf    = vmix( specPrevOnSurf, unfilteredSpec, invA );
-            const float  hitDistOnSurf = gmix( specHitDistancePrev, rayInfo.w, invA );
+            const float3 specOnSurf    = X::vmix( specPrevOnSurf, unfilteredSpec, invA );
+            const float  hitDistOnSurf = X::mix( specHitDistancePrev, rayInfo.w, invA );
             specColorAccum         = specOnSurf;
             specHistoryLengthAccum = AOnSurf;
             specHitDistanceAccum   = hitDistOnSurf;
 
-            const float3 rayDir = f3( rayInfo.x, rayInfo.y, rayInfo.z );
-            const float3 v      = add( surfPos, mul( mul( rayDir, hitDistOnSurf ), domin ) );
+            const float  hd = hitDistOnSurf * domin;
+            const float3 v  = f3( X::madd( rayInfo.x, hd, surfPos.x ), X::madd( rayInfo.y, hd, surfPos.y ), X::madd( rayInfo.z, hd, surfPos.z ) );
             // screen-space motion of the virtual position through proj*view (only x, y, w)
-            const float cxC = u.vp[ 0 ] * v.x + u.vp[ 4 ] * v.y + u.vp[ 8 ] * v.z + u.vp[ 12 ];
-            const float cyC = u.vp[ 1 ] * v.x + u.vp[ 5 ] * v.y + u.vp[ 9 ] * v.z + u.vp[ 13 ];
-            const float cwC = u.vp[ 3 ] * v.x + u.vp[ 7 ] * v.y + u.vp[ 11 ] * v.z + u.vp[ 15 ];
-            const float cxP = u.vpPrev[ 0 ] * v.x + u.vpPrev[ 4 ] * v.y + u.vpPrev[ 8 ] * v.z + u.vpPrev[ 12 ];
-            const float cyP = u.vpPrev[ 1 ] * v.x + u.vpPrev[ 5 ] * v.y + u.vpPrev[ 9 ] * v.z + u.vpPrev[ 13 ];
-            const float cwP = u.vpPrev[ 3 ] * v.x + u.vpPrev[ 7 ] * v.y + u.vpPrev[ 11 ] * v.z + u.vpPrev[ 15 ];
-            const float rC = __fdividef( 1.0f, cwC ), rP = __fdividef( 1.0f, cwP );
-            const float2 specMotion = make_float2( ( cxP * rP * 0.5f + 0.5f ) - ( cxC * rC * 0.5f + 0.5f ),
-                                                   ( cyP * rP * 0.5f + 0.5f ) - ( cyC * rC * 0.5f + 0.5f ) );
+            const float* m  = u.vp;
+            const float* mp = u.vpPrev;
+            const float cxC = X::madd( m[ 0 ], v.x, X::madd( m[ 4 ], v.y, X::madd( m[ 8 ], v.z, m[ 12 ] ) ) );
+            const float cyC = X::madd( m[ 1 ], v.x, X::madd( m[ 5 ], v.y, X::madd( m[ 9 ], v.z, m[ 13 ] ) ) );
+            const float cwC = X::madd( m[ 3 ], v.x, X::madd( m[ 7 ], v.y, X::madd( m[ 11 ], v.z, m[ 15 ] ) ) );
+            const float cxP = X::madd( mp[ 0 ], v.x, X::madd( mp[ 4 ], v.y, X::madd( mp[ 8 ], v.z, mp[ 12 ] ) ) );
+            const float cyP = X::madd( mp[ 1 ], v.x, X::madd( mp[ 5 ], v.y, X::madd( mp[ 9 ], v.z, mp[ 13 ] ) ) );
+            const float cwP = X::madd( mp[ 3 ], v.x, X::madd( mp[ 7 ], v.y, X::madd( mp[ 11 ], v.z, mp[ 15 ] ) ) );
+            const float hC = 0.5f * rcp_approx( cwC ), hP = 0.5f * rcp_approx( cwP );
+            // (ndcPrev * 0.5 + 0.5) - (ndcCur * 0.5 + 0.5)
+            const float2 specMotion = make_float2( X::madd( cxP, hP, -cxC * hC ), X::madd( cyP, hP, -cyC * hC ) );
             const float2 spp = prev_screen_pos( u, specMotion, px, py );
             const float  fx = floorf( spp.x - 0.5f ), fy = floorf( spp.y - 0.5f );
             const int2   pixPrevS = make_int2( (int)fx, (int)fy );
@@ -758,47 +827,45 @@ __device__ __forceinline__ void temporal_tile( const FrameArgs& a, int bx, int b
 #pragma unroll
                 for( int xx = 0; xx <= 1; xx++ )
                 {
-                    const int  qx = pixPrevS.x + xx, qy = pixPrevS.y + yy;
-                    const bool in = inside( u, qx, qy );
-                    const int  q  = in ? qy * u.W + qx : 0;
-                    float      dP;
-                    float3     nP;
+                    const int qx = pixPrevS.x + xx, qy = pixPrevS.y + yy;
+                    if( !in_area( qx, qy, chArea ) ) continue;
+                    const int q = qy * u.W + qx;
+                    float     dP;
+                    float3    nP;
                     if( GEOMPREV )
                     {
-                        const Geo gp = in ? geo_load( a.geomPrev, q ) : geo_zero();
+                        const Geo gp = geo_load( a.geomPrev, q );
                         dP           = geo_depth( gp );
                         nP           = gp.n;
                     }
                     else
                     {
-                        dP = in ? h2f( a.depthPrev[ q ] ) : 0.0f;
-                        nP = decode_normal( a, in ? a.normalPrev[ q ] : 0u );
+                        dP = h2f( a.depthPrev[ q ] );
+                        nP = decode_normal( a, a.normalPrev[ q ] );
                     }
-                    const bool ok = in_area( qx, qy, chArea ) && test_depth( z, dP, motionZ ) && test_normal( normal, nP );
                     const float w = ( xx ? subPixS.x : 1.0f - subPixS.x ) * ( yy ? subPixS.y : 1.0f - subPixS.y );
-                    if( ok ) weightSumVirtual = weightSumVirtual + w;
+                    if( test_depth_r( z, rz, dP, motionZ ) && test_normal( normal, nP ) ) weightSumVirtual = weightSumVirtual + w;
                 }
             }
             if( weightSumVirtual > 0.0001f )
             {
-                float       Avirt    = gclamp( 256.0f * ( f0 * ex2_approx( 0.5f * lr ) ), minA, A );
-                const float Amin     = fminf( Avirt, 3.0f * sqrtf( roughness ) );
-                float       aa2      = gmix( __fdividef( 1.0f, 1.0f + Amin ), __fdividef( 1.0f, 1.0f + Avirt ), 1.0f );
-                Avirt                = __fdividef( 1.0f, aa2 ) - 1.0f;
+                // with the shader's confidence 1, mix(1/(1+Amin), 1/(1+Avirt), 1) leaves Avirt
+                const float Avirt    = gclamp( 256.0f * ( f0 * ex2_approx( 0.5f * lr ) ), minA, A );
+                const float invAv    = __fdividef( 1.0f, 1.0f + Avirt );
                 const float Ahitdist = fminf( Avirt, 16.0f );
-                const float3 specVirt = vmix( specPrevOnSurf, unfilteredSpec, __fdividef( 1.0f, 1.0f + Avirt ) );
-                aa2                    = gmix( invA, __fdividef( 1.0f, 1.0f + Avirt ), domin );
-                specColorAccum         = vmix( specOnSurf, specVirt, domin );
+                const float3 specVirt = X::vmix( specPrevOnSurf, unfilteredSpec, invAv );
+                const float  aa2      = X::mix( invA, invAv, domin );
+                specColorAccum         = X::vmix( specOnSurf, specVirt, domin );
                 specHistoryLengthAccum = __fdividef( 1.0f, aa2 ) - 1.0f;
-                specHitDistanceAccum   = gmix( specHitDistancePrev, rayInfo.w, __fdividef( 1.0f, 1.0f + Ahitdist ) );
+                specHitDistanceAccum   = X::mix( specHitDistancePrev, rayInfo.w, __fdividef( 1.0f, 1.0f + Ahitdist ) );
             }
         }
         else
         {
-            const float A       = gclamp( 1.0f + specHistoryLength * Wm< FAST >::powv( 1.0f - aS, 5.0f ), spec_min_accum( u ), 256.0f );
+            const float A       = gclamp( 1.0f + specHistoryLength * powf( 1.0f - aS, 5.0f ), spec_min_accum( u ), 256.0f );
             const float par     = parallax( u, surfPos, surfPosPrev );
-            const float AOnSurf = spec_accum_speed< FAST >( u, A, roughness, nv, par );
-            const float domin   = spec_dominant< FAST >( nv, roughness );
+            const float AOnSurf = spec_accum_speed< false >( u, A, roughness, nv, par );
+            const float domin   = spec_dominant< false >( nv, roughness );
 
             const float3 specOnSurf    = vmix( specPrevOnSurf, unfilteredSpec, 1.0f / ( 1.0f + AOnSurf ) );
             const float  hitDistOnSurf = gmix( specHitDistancePrev, rayInfo.w, 1.0f / ( 1.0f + AOnSurf ) );
@@ -832,25 +899,24 @@ __device__ __forceinline__ void temporal_tile( const FrameArgs& a, int bx, int b
                 { ( 1.0f - subPixS.x ) * subPixS.y, subPixS.x * subPixS.y },
             };
             float weightSumVirtual = 0.0f;
-    #pragma unroll
+#pragma unroll
             for( int yy = 0; yy <= 1; yy++ )
             {
-    #pragma unroll
+#pragma unroll
                 for( int xx = 0; xx <= 1; xx++ )
                 {
-                    const int    qx = pixPrevS.x + xx, qy = pixPrevS.y + yy;
-                    const bool   in = inside( u, qx, qy );
-                    const size_t q  = in ? idx( u, qx, qy ) : 0;
-                    const float  dP = in ? h2f( a.depthPrev[ q ] ) : 0.0f;
-                    const float3 nP = decode_normal( a, in ? a.normalPrev[ q ] : 0u );
-                    const bool ok = in_area( qx, qy, chArea ) && test_depth( z, dP, motionZ ) && test_normal( normal, nP );
+                    const int qx = pixPrevS.x + xx, qy = pixPrevS.y + yy;
+                    if( !in_area( qx, qy, chArea ) ) continue;
+                    const int    q  = qy * u.W + qx;
+                    const float  dP = h2f( a.depthPrev[ q ] );
+                    const float3 nP = decode_normal( a, a.normalPrev[ q ] );
                     // the shader also accumulates SpecAccumColor_Prev here but never uses the sum
-                    if( ok ) weightSumVirtual = weightSumVirtual + bws[ yy ][ xx ];
+                    if( test_depth( z, dP, motionZ ) && test_normal( normal, nP ) ) weightSumVirtual = weightSumVirtual + bws[ yy ][ xx ];
                 }
             }
             if( weightSumVirtual > 0.0001f )
             {
-                float       Avirt      = spec_accum_speed< FAST >( u, A, roughness, nv, 0.0f );
+                float       Avirt      = spec_accum_speed< false >( u, A, roughness, nv, 0.0f );
                 const float confidence = 1.0f;
                 const float Amin       = fminf( Avirt, 3.0f * sqrtf( roughness ) );
                 float       aa         = gmix( 1.0f / ( 1.0f + Amin ), 1.0f / ( 1.0f + Avirt ), confidence );
@@ -875,9 +941,9 @@ __device__ __forceinline__ void temporal_tile( const FrameArgs& a, int bx, int b
     float3 diffColorAccum, indirAccum;
     float2 diffMomentsAccum;
     float  diffHL, indirHL;
-    if( weightSum > 0.0001f )
+    if( hasHistory )
     {
-        const float inv = 1.0f / weightSum;
+        const float inv = FAST ? invWS : 1.0f / weightSum;
         diffPrev        = mul( diffPrev, inv );
         momentsPrev     = make_float2( momentsPrev.x * inv, momentsPrev.y * inv );
         indirPrev       = mul( indirPrev, inv );
@@ -886,23 +952,23 @@ __device__ __forceinline__ void temporal_tile( const FrameArgs& a, int bx, int b
         {
             // the history length stays IEEE (variance switches on it); its reciprocal only
             // blends, so FAST takes the hardware one
-            dHL = dHL * powf( 1.0f - aD, 10.0f );
+            dHL = dHL * ( FAST ? decD : powf( 1.0f - aD, 10.0f ) );
             dHL = gclamp( dHL + 1.0f, 1.0f, 256.0f );
             const float rD     = FAST ? __fdividef( 1.0f, dHL ) : 1.0f / dHL;
             float alphaColor   = fmaxf( 0.01f, rD );
             float alphaMoments = fmaxf( 0.01f, rD );
-            alphaColor         = gmix( alphaColor, 1.0f, aD );
-            alphaMoments       = gmix( alphaMoments, 1.0f, aD );
-            diffColorAccum     = vmix( diffPrev, unfilteredDiff, alphaColor );
-            diffMomentsAccum   = make_float2( gmix( momentsPrev.x, moments.x, alphaMoments ), gmix( momentsPrev.y, moments.y, alphaMoments ) );
+            alphaColor         = X::mix( alphaColor, 1.0f, aD );
+            alphaMoments       = X::mix( alphaMoments, 1.0f, aD );
+            diffColorAccum     = X::vmix( diffPrev, unfilteredDiff, alphaColor );
+            diffMomentsAccum   = make_float2( X::mix( momentsPrev.x, moments.x, alphaMoments ), X::mix( momentsPrev.y, moments.y, alphaMoments ) );
             diffHL             = dHL;
         }
         {
-            iHL = iHL * powf( 1.0f - aI, 10.0f );
+            iHL = iHL * ( FAST ? decI : powf( 1.0f - aI, 10.0f ) );
             iHL = gclamp( iHL + 1.0f, 1.0f, 256.0f );
             float alphaColor = fmaxf( 0.01f, FAST ? __fdividef( 1.0f, iHL ) : 1.0f / iHL );
-            alphaColor       = gmix( alphaColor, 1.0f, aI );
-            indirAccum       = vmix( indirPrev, unfilteredIndir, alphaColor );
+            alphaColor       = X::mix( alphaColor, 1.0f, aI );
+            indirAccum       = X::vmix( indirPrev, unfilteredIndir, alphaColor );
             indirHL          = iHL;
         }
     }
@@ -994,16 +1060,18 @@ __device__ __forceinline__ void variance_px( const FrameArgs& a, const int px, c
     const float  histLen = S::ld4( a.histLen, (size_t)i ).x;
     const float2 tm      = S::ld2( a.moments, (size_t)i );
     const float  THR     = 4.0f;
+    // FAST: hardware reciprocals and fused multiply-adds in the continuous terms; the history
+    // length switch and the validity tests stay IEEE
     if( histLen > THR )
     {
-        float tv = fmaxf( 0.0f, tm.y - tm.x * tm.x );
-        tv       = tv / fmaxf( 1.0f, histLen - THR );
+        float tv = fmaxf( 0.0f, FAST ? X::madd( -tm.x, tm.x, tm.y ) : tm.y - tm.x * tm.x );
+        tv       = FAST ? tv * rcp_approx( fmaxf( 1.0f, histLen - THR ) ) : tv / fmaxf( 1.0f, histLen - THR );
         outC     = pc;
         outV     = tv;
         return;
     }
-    const float  l   = luminance( pc );
-    float2       sm  = make_float2( l + tm.x, l * l + tm.y );
+    const float  l   = X::lum( pc );
+    float2       sm  = make_float2( l + tm.x, X::madd( l, l, tm.y ) );
     float        ws  = 1.0f;
     const float3 cnd = GEOMIN ? gc.n : decode_normal( a, a.normal[ i ] );
 #pragma unroll
@@ -1015,7 +1083,7 @@ __device__ __forceinline__ void variance_px( const FrameArgs& a, const int px, c
             if( xx == 0 && yy == 0 ) continue;
             const int    qx  = px + xx, qy = py + yy;
             const float3 cq  = colorAt( xx, yy );
-            const float  lq  = luminance( cq );
+            const float  lq  = X::lum( cq );
             const bool   in  = inside( a.u, qx, qy );
             const int    q   = in ? qy * a.u.W + qx : 0;
             float        zq;
@@ -1032,22 +1100,23 @@ __device__ __forceinline__ void variance_px( const FrameArgs& a, const int px, c
                 nq = decode_normal( a, in ? a.normal[ q ] : 0u );
             }
             const float  mz  = fmaxf( cz, zq );
-            const float  rcp = mz <= 0.0f ? 0.0f : 1.0f / mz;
+            const float  rcp = mz <= 0.0f ? 0.0f : ( FAST ? rcp_approx( mz ) : 1.0f / mz );
             const float  wz  = X::expn( -fabsf( cz - zq ) * rcp );
-            const float  wn  = X::pow128( fmaxf( 0.0f, dot3( cnd, nq ) ) );
+            const float  wn  = X::pow128( fmaxf( 0.0f, X::dot( cnd, nq ) ) );
             const float  w   = wz * wn;
             if( !isnan( w ) )
             {
-                sm = make_float2( sm.x + lq * w, sm.y + lq * lq * w );
-                pc = add( pc, mul( cq, w ) );
+                const float lw = lq * w;
+                sm = make_float2( sm.x + lw, FAST ? X::madd( lq, lw, sm.y ) : sm.y + lq * lq * w );
+                pc = f3( X::madd( cq.x, w, pc.x ), X::madd( cq.y, w, pc.y ), X::madd( cq.z, w, pc.z ) );
                 ws = ws + w;
             }
         }
     }
-    const float inv = ws <= 0.0f ? 0.0f : 1.0f / ws;
+    const float inv = ws <= 0.0f ? 0.0f : ( FAST ? rcp_approx( ws ) : 1.0f / ws );
     sm              = make_float2( sm.x * inv, sm.y * inv );
     outC            = mul( pc, inv );
-    outV            = fmaxf( 0.0f, sm.y - sm.x * sm.x ) * ( 1.0f + 2.0f * ( 1.0f - histLen / THR ) );
+    outV            = fmaxf( 0.0f, FAST ? X::madd( -sm.x, sm.x, sm.y ) : sm.y - sm.x * sm.x ) * ( 1.0f + 2.0f * ( 1.0f - histLen / THR ) );
 }
 
 template< int M > __global__ void __launch_bounds__( 256 ) k_variance( const FrameArgs a )
@@ -1332,14 +1401,32 @@ __device__ __forceinline__ float material_ambient( float3 albedo )
 }
 
 // CmSVGFAtrous.comp:278-348; returns the histogram input value (fp16 bits)
-template< int M > __device__ __forceinline__ uint16_t compose( const FrameArgs& a, int px, int py, size_t i, float3 filteredDiff, float3 filteredSpec,
-                                                            float3 filteredIndir )
+// B10G11R11 channel to FP32 by assembling the bits: exponent e in 1..30 becomes e + 112 with the
+// mantissa shifted up; e = 0 gives (2^-14 + m 2^(-14-k)) - 2^-14, an exact difference; e = 31
+// gives Inf or the canonical NaN. The values of rgdn::ufloat_to_f32, without a conversion.
+__device__ __forceinline__ float ufloat_bits( uint32_t v, int mbits )
 {
+    const uint32_t e = v >> mbits, m = v & ( ( 1u << mbits ) - 1u );
+    if( e == 31u ) return __uint_as_float( m ? 0x7FC00000u : 0x7F800000u );
+    const float f = __uint_as_float( ( ( e ? e + 112u : 113u ) << 23 ) | ( m << ( 23 - mbits ) ) );
+    return e ? f : f - 6.103515625e-05f;
+}
+__device__ __forceinline__ float3 decode_b10g11r11_bits( uint32_t p )
+{
+    return f3( ufloat_bits( p & 0x7FFu, 6 ), ufloat_bits( ( p >> 11 ) & 0x7FFu, 6 ), ufloat_bits( ( p >> 22 ) & 0x3FFu, 5 ) );
+}
+
+// FAST: fused multiply-adds and a reciprocal multiply in the continuous terms (the composed
+// colour and the histogram input both are); unorm8 through the table u8 (the same values)
+template< int M, bool FAST >
+__device__ __forceinline__ uint16_t compose( const FrameArgs& a, int px, int py, size_t i, float3 filteredDiff, float3 filteredSpec,
+                                             float3 filteredIndir, const float* u8 )
+{
+    using X           = Wm< FAST >;
     const Uniform& u  = a.u;
     const int2     rp = regular_from_cb( u, px, py );
-    const size_t   ri = idx( u, rp.x, rp.y );
-    const rgdn::f3 al = decode_b10g11r11( a.albedo[ ri ] );
-    float3         albedo = f3( al.x, al.y, al.z );
+    const int      ri = rp.y * u.W + rp.x;
+    float3         albedo = decode_b10g11r11_bits( a.albedo[ ri ] );
     const ushort4  tp = a.throughput[ i ];
     const float3   throughput = f3( h2f( tp.x ), h2f( tp.y ), h2f( tp.z ) );
     if( u.debugFlags & RGDN_DEBUG_SHOW_FLAG_ALBEDO_WHITE ) albedo = f3( 1.0f, 1.0f, 1.0f );
@@ -1347,22 +1434,29 @@ template< int M > __device__ __forceinline__ uint16_t compose( const FrameArgs& 
     if( a.isSky[ i ] == 0 )
     {
         const uint16_t mrb       = a.mr[ i ];
-        const float    metallic  = unorm8_to_f32( mrb & 0xFFu );
-        const float    roughness = unorm8_to_f32( mrb >> 8 );
+        const float    metallic  = u8[ mrb & 0xFFu ];
+        const float    roughness = u8[ mrb >> 8 ];
         const float3   diffuse = filteredDiff, indirect = filteredIndir;
-        const float3   specular = vmix( filteredSpec, indirect, gsmoothstep( 0.5f, 0.5f + 0.25f, roughness ) );
-        const float3   ro_s     = vmix( f3( 0.04f, 0.04f, 0.04f ), albedo, metallic );
+        // smoothstep(0.5, 0.75, roughness): the division by 0.25 is the exact product by 4
+        const float    st       = gsat( ( roughness - 0.5f ) * 4.0f );
+        const float3   specular = X::vmix( filteredSpec, indirect, st * st * ( 3.0f - 2.0f * st ) );
+        const float3   ro_s     = X::vmix( f3( 0.04f, 0.04f, 0.04f ), albedo, metallic );
         const float3   ro_d     = mul( albedo, 1.0f - metallic );
-        ill = add( mul( add( diffuse, indirect ), ro_d ), mul( specular, ro_s ) );
+        const float3   di       = add( diffuse, indirect );
+        ill = f3( X::madd( di.x, ro_d.x, specular.x * ro_s.x ), X::madd( di.y, ro_d.y, specular.y * ro_s.y ),
+                  X::madd( di.z, ro_d.z, specular.z * ro_s.z ) );
         if( u.debugFlags & RGDN_DEBUG_SHOW_FLAG_ONLY_DIRECT_DIFFUSE ) ill = mul( diffuse, albedo );
-        else if( u.debugFlags & RGDN_DEBUG_SHOW_FLAG_ONLY_SPECULAR ) ill = mul( specular, vmix( f3( 0.04f, 0.04f, 0.04f ), albedo, metallic ) );
+        else if( u.debugFlags & RGDN_DEBUG_SHOW_FLAG_ONLY_SPECULAR ) ill = mul( specular, ro_s );
         else if( u.debugFlags & RGDN_DEBUG_SHOW_FLAG_ONLY_INDIRECT_DIFFUSE ) ill = indirect;
         ill = mul( ill, throughput );
-        ill = mul( ill, material_ambient( albedo ) );
+        // MaterialAmbient (BRDF.h:49-64)
+        const float l = X::lum( albedo );
+        const float q = FAST ? ( l - 0.02f ) * 50.0f : ( l - 0.02f ) / 0.02f;
+        ill           = mul( ill, l > 0.02f ? 1.0f : X::one_minus( q, q ) );
     }
     else ill = mul( albedo, throughput );
 
-    const uint16_t hin = f32_to_f16( fmaxf( 0.0f, luminance( ill ) ) );
+    const uint16_t hin = f32_to_f16( fmaxf( 0.0f, X::lum( ill ) ) );
     a.histInput[ ri ] = hin;
     if( (float)rp.x < u.lightmapCoverage * u.rw ) ill = mul( albedo, throughput );
     Sto< M >::stpre( a.preFinal, ri, vmax( f3( 0, 0, 0 ), ill ) );
@@ -1429,12 +1523,22 @@ __device__ __forceinline__ void atrous_accum( const AtrousCtr& c, AtrousAcc& acc
         const float  wDiff = ex2_approx( eBase - fabsf( c.l - lq ) * c.wLumMul ) * insideA;
         const float  wSpec = w_r * ex2_approx( __fmaf_rn( c.nwSpec, L, eBase ) ) * insideA;
         const float  wInd  = wBase;
-        acc.d   = f3( __fmaf_rn( dq.x, wDiff, acc.d.x ), __fmaf_rn( dq.y, wDiff, acc.d.y ), __fmaf_rn( dq.z, wDiff, acc.d.z ) );
-        acc.s   = f3( __fmaf_rn( sq.x, wSpec, acc.s.x ), __fmaf_rn( sq.y, wSpec, acc.s.y ), __fmaf_rn( sq.z, wSpec, acc.s.z ) );
-        acc.i   = f3( __fmaf_rn( iq.x, wInd, acc.i.x ), __fmaf_rn( iq.y, wInd, acc.i.y ), __fmaf_rn( iq.z, wInd, acc.i.z ) );
-        acc.var = __fmaf_rn( cvq.w * wDiff, wDiff, acc.var );
-        acc.ws  = acc.ws + wDiff;
-        acc.wsS = acc.wsS + wSpec;
+        // the sums in packed FP32 pairs (two independent round-to-nearest FMAs or adds per
+        // instruction, the bits of the scalar forms): (d.xy), (d.z, var), (s.xy), (s.z, i.z),
+        // (i.xy), (ws, wsS)
+        const float2 wDD = make_float2( wDiff, wDiff ), wSS = make_float2( wSpec, wSpec ), wII = make_float2( wInd, wInd );
+        const float2 dxy = __ffma2_rn( make_float2( dq.x, dq.y ), wDD, make_float2( acc.d.x, acc.d.y ) );
+        const float2 dzv = __ffma2_rn( make_float2( dq.z, cvq.w * wDiff ), wDD, make_float2( acc.d.z, acc.var ) );
+        const float2 sxy = __ffma2_rn( make_float2( sq.x, sq.y ), wSS, make_float2( acc.s.x, acc.s.y ) );
+        const float2 szi = __ffma2_rn( make_float2( sq.z, iq.z ), make_float2( wSpec, wInd ), make_float2( acc.s.z, acc.i.z ) );
+        const float2 ixy = __ffma2_rn( make_float2( iq.x, iq.y ), wII, make_float2( acc.i.x, acc.i.y ) );
+        const float2 wsp = __fadd2_rn( make_float2( acc.ws, acc.wsS ), make_float2( wDiff, wSpec ) );
+        acc.d   = f3( dxy.x, dxy.y, dzv.x );
+        acc.var = dzv.y;
+        acc.s   = f3( sxy.x, sxy.y, szi.x );
+        acc.i   = f3( ixy.x, ixy.y, szi.y );
+        acc.ws  = wsp.x;
+        acc.wsS = wsp.y;
         acc.wsI = acc.wsI + wInd;
         return;
     }
@@ -1626,7 +1730,7 @@ __device__ __forceinline__ void atrous_tile( const FrameArgs& a, const int iter,
         }
         else
         {
-            const uint16_t hin = compose< M >( a, px, py, (size_t)i, outDiff, outSpec, outInd );
+            const uint16_t hin = compose< M, FAST >( a, px, py, (size_t)i, outDiff, outSpec, outInd, u8 );
             if( HIST )
             {
                 // one shared atomic per distinct bin of the warp
@@ -1934,7 +2038,7 @@ __global__ void __launch_bounds__( 256, 3 ) k_atrous_tma( const FrameArgs a, con
             }
             else
             {
-                const uint16_t hin = compose< M >( a, px, py, (size_t)i, outDiff, outSpec, outInd );
+                const uint16_t hin = compose< M, FAST >( a, px, py, (size_t)i, outDiff, outSpec, outInd, u8 );
                 if( HIST )
                 {
                     const uint32_t bin   = __ldg( &a.binLut[ hin ] );

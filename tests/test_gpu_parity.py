@@ -257,10 +257,61 @@ def test_fused_exact_equals_plain(ctx, mode_name, mode):
 
 @pytest.mark.parametrize("mode_name,mode", MODES)
 def test_fast_math_close_to_exact(ctx, mode_name, mode):
-    """The default path (hardware exp2/log2 in continuous weights) stays within the parity
-    tolerance of the exact path over a frame sequence."""
+    """The default path (hardware exp2/log2/rcp and fused multiply-adds in continuous terms)
+    stays within the parity tolerance of the exact path over a frame sequence, and is as close
+    to the FP64 oracle as the exact path is."""
     W, H = 96, 54
     sc = Scene(W, H, seed=17, lightFlickerFrom=3.0)
+    a = Stream(ctx, W, H, mode)
+    b = Stream(ctx, W, H, mode)
+    o = oracle.OracleStream(W, H, oracle.MODE_F64)
+    for f in range(8):
+        fi = f & 1
+        bufs, p = sc.generate(f)
+        upload_frame(a, o, bufs, fi)
+        upload_frame(b, None, bufs, fi)
+        o.denoise(fi, p)
+        pa = p.copy()
+        pa.flags = N.FLAG_PLAIN
+        for s, q in ((a, pa), (b, p)):
+            Denoiser(s).Denoise(fi, q)
+            Tonemapping(s).CalculateExposure(fi, q)
+    img = a.image("PRE_FINAL", fi)
+    ga = F.decode(a.download("PRE_FINAL", fi), img.format)
+    gb = F.decode(b.download("PRE_FINAL", fi), img.format)
+    err = F.texel_rel_err(gb, ga, atol=1e-4 * float(np.percentile(ga, 99)))
+    ref = F.decode(o.plane("PRE_FINAL", fi), o.fmt("PRE_FINAL"))[..., :3]
+    psnr_exact, psnr_fast = F.psnr(ga[..., :3], ref), F.psnr(gb[..., :3], ref)
+    stats = (f"p99 {np.percentile(err, 99):.3e} p99.9 {np.percentile(err, 99.9):.3e} max {err.max():.3e}; "
+             f"PSNR vs FP64: exact {psnr_exact:.2f} dB, default {psnr_fast:.2f} dB")
+    if mode == N.STORAGE_FP32:
+        assert err.max() <= 1e-3, stats
+    elif mode == N.STORAGE_REF:
+        # The reference formats quantise coarsely: E5B9G9R9 history (9-bit mantissas), unorm8
+        # gradients and a B10G11R11 PreFinal (2^-6 for R and G, 2^-5 for B). An ulp-level
+        # difference can move a stored code, and where it moves the unorm8 indirect gradient
+        # (RtGradients.rgen weighs it by the indirect history's brightness) the indirect
+        # history length of that pixel changes, a local difference of several quanta. So
+        # almost every texel stays within one PreFinal quantum, and the default path is as
+        # accurate against FP64 as the exact path.
+        assert np.mean(err <= 2.0 ** -5) >= 0.99, stats
+        assert psnr_fast >= psnr_exact - 1.5, stats
+    else:
+        assert np.mean(err <= 1e-2) >= 0.99, stats
+        assert np.percentile(err, 99.9) <= 4e-2, stats
+        assert psnr_fast >= psnr_exact - 0.5, stats
+    a.close()
+    b.close()
+
+
+@pytest.mark.parametrize("mode_name,mode", MODES)
+def test_fast_math_keeps_history_length(ctx, mode_name, mode):
+    """The default path approximates only continuous weights: the diffuse history length (the
+    variance pass switches on it, and the temporal pass derives it from the reprojection tests,
+    the gradients and the decay table) is bit-identical to the one-kernel-per-dispatch path's
+    over a sequence with disocclusions and gradient resets."""
+    W, H = 96, 54
+    sc = Scene(W, H, seed=23, lightFlickerFrom=2.0)
     a = Stream(ctx, W, H, mode)
     b = Stream(ctx, W, H, mode)
     for f in range(8):
@@ -272,15 +323,9 @@ def test_fast_math_close_to_exact(ctx, mode_name, mode):
         pa.flags = N.FLAG_PLAIN
         for s, q in ((a, pa), (b, p)):
             Denoiser(s).Denoise(fi, q)
-            Tonemapping(s).CalculateExposure(fi, q)
-    img = a.image("PRE_FINAL", fi)
-    ga = F.decode(a.download("PRE_FINAL", fi), img.format)
-    gb = F.decode(b.download("PRE_FINAL", fi), img.format)
-    err = F.texel_rel_err(gb, ga, atol=1e-4 * float(np.percentile(ga, 99)))
-    if mode == N.STORAGE_FP32:
-        assert err.max() <= 1e-3, f"max rel err {err.max():.3e}"
-    else:
-        assert np.mean(err <= 1e-2) >= 0.99
+        ha = a.download("ACCUM_HISTORY_LENGTH", fi)[..., 0]
+        hb = b.download("ACCUM_HISTORY_LENGTH", fi)[..., 0]
+        assert np.array_equal(ha, hb), f"frame {f}: {int(np.sum(ha != hb))} history lengths differ"
     a.close()
     b.close()
 
