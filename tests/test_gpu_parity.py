@@ -226,10 +226,12 @@ def test_histogram_bit_exact_same_input(ctx, mode_name, mode, path):
 
 
 @pytest.mark.parametrize("mode_name,mode", MODES)
-def test_fused_exact_equals_plain(ctx, mode_name, mode):
+@pytest.mark.parametrize("size", [(82, 46), (250, 151)])
+def test_fused_exact_equals_plain(ctx, mode_name, mode, size):
     """The default path's kernels with IEEE math reproduce the one-kernel-per-dispatch path bit
-    for bit on every plane."""
-    W, H = 82, 46
+    for bit on every plane, on one tile row and on many (250x151: odd height, interior and
+    edge tiles of every kernel)."""
+    W, H = size
     sc = Scene(W, H, seed=13, lightFlickerFrom=3.0)
     a = Stream(ctx, W, H, mode)
     b = Stream(ctx, W, H, mode)
