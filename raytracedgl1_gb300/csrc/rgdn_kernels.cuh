@@ -1416,24 +1416,46 @@ __device__ __forceinline__ float3 decode_b10g11r11_bits( uint32_t p )
     return f3( ufloat_bits( p & 0x7FFu, 6 ), ufloat_bits( ( p >> 11 ) & 0x7FFu, 6 ), ufloat_bits( ( p >> 22 ) & 0x3FFu, 5 ) );
 }
 
+// The G-buffer texels the composition reads, loaded before the last iteration's taps so their
+// latency overlaps the filtering
+struct ComposeIn
+{
+    uint32_t albedo;   // B10G11R11 at the pixel's regular-layout position
+    ushort4  throughput;
+    uint32_t sky;
+    uint32_t mr;
+    int      rx, ri;   // regular-layout column and index
+};
+__device__ __forceinline__ ComposeIn compose_load( const FrameArgs& a, int px, int py, int i )
+{
+    const int2 rp = regular_from_cb( a.u, px, py );
+    ComposeIn  c;
+    c.rx         = rp.x;
+    c.ri         = rp.y * a.u.W + rp.x;
+    c.albedo     = a.albedo[ c.ri ];
+    c.throughput = a.throughput[ i ];
+    c.sky        = a.isSky[ i ];
+    c.mr         = a.mr[ i ];
+    return c;
+}
+
 // FAST: fused multiply-adds and a reciprocal multiply in the continuous terms (the composed
 // colour and the histogram input both are); unorm8 through the table u8 (the same values)
 template< int M, bool FAST >
-__device__ __forceinline__ uint16_t compose( const FrameArgs& a, int px, int py, size_t i, float3 filteredDiff, float3 filteredSpec,
+__device__ __forceinline__ uint16_t compose( const FrameArgs& a, int px, const ComposeIn& in, float3 filteredDiff, float3 filteredSpec,
                                              float3 filteredIndir, const float* u8 )
 {
     using X           = Wm< FAST >;
     const Uniform& u  = a.u;
-    const int2     rp = regular_from_cb( u, px, py );
-    const int      ri = rp.y * u.W + rp.x;
-    float3         albedo = decode_b10g11r11_bits( a.albedo[ ri ] );
-    const ushort4  tp = a.throughput[ i ];
+    const int      ri = in.ri;
+    float3         albedo = decode_b10g11r11_bits( in.albedo );
+    const ushort4  tp = in.throughput;
     const float3   throughput = f3( h2f( tp.x ), h2f( tp.y ), h2f( tp.z ) );
     if( u.debugFlags & RGDN_DEBUG_SHOW_FLAG_ALBEDO_WHITE ) albedo = f3( 1.0f, 1.0f, 1.0f );
     float3 ill;
-    if( a.isSky[ i ] == 0 )
+    if( in.sky == 0 )
     {
-        const uint16_t mrb       = a.mr[ i ];
+        const uint32_t mrb       = in.mr;
         const float    metallic  = u8[ mrb & 0xFFu ];
         const float    roughness = u8[ mrb >> 8 ];
         const float3   diffuse = filteredDiff, indirect = filteredIndir;
@@ -1458,7 +1480,7 @@ __device__ __forceinline__ uint16_t compose( const FrameArgs& a, int px, int py,
 
     const uint16_t hin = f32_to_f16( fmaxf( 0.0f, X::lum( ill ) ) );
     a.histInput[ ri ] = hin;
-    if( (float)rp.x < u.lightmapCoverage * u.rw ) ill = mul( albedo, throughput );
+    if( (float)in.rx < u.lightmapCoverage * u.rw ) ill = mul( albedo, throughput );
     Sto< M >::stpre( a.preFinal, ri, vmax( f3( 0, 0, 0 ), ill ) );
     return hin;
 }
@@ -1720,6 +1742,8 @@ __device__ __forceinline__ void atrous_tile( const FrameArgs& a, const int iter,
         const int  by0 = by * blockDim.y, by1 = by0 + blockDim.y - 1;
         const bool interior = bx0 - step >= 0 && by0 - step >= 0 && bx1 + step < u.W && by1 + step < u.H &&
                               ( bx1 + step < sep || bx0 - step >= sep );
+        ComposeIn cin;
+        if( last ) cin = compose_load( a, px, py, i );
         if( interior ) atrous_px< M, FAST, true, GEOMIN >( a, io, iter, px, py, i, u8, outDiff, outVar, outSpec, outInd );
         else atrous_px< M, FAST, false, GEOMIN >( a, io, iter, px, py, i, u8, outDiff, outVar, outSpec, outInd );
         if( !last )
@@ -1730,7 +1754,7 @@ __device__ __forceinline__ void atrous_tile( const FrameArgs& a, const int iter,
         }
         else
         {
-            const uint16_t hin = compose< M, FAST >( a, px, py, (size_t)i, outDiff, outSpec, outInd, u8 );
+            const uint16_t hin = compose< M, FAST >( a, px, cin, outDiff, outSpec, outInd, u8 );
             if( HIST )
             {
                 // one shared atomic per distinct bin of the warp
@@ -2038,7 +2062,7 @@ __global__ void __launch_bounds__( 256, 3 ) k_atrous_tma( const FrameArgs a, con
             }
             else
             {
-                const uint16_t hin = compose< M, FAST >( a, px, py, (size_t)i, outDiff, outSpec, outInd, u8 );
+                const uint16_t hin = compose< M, FAST >( a, px, compose_load( a, px, py, i ), outDiff, outSpec, outInd, u8 );
                 if( HIST )
                 {
                     const uint32_t bin   = __ldg( &a.binLut[ hin ] );
