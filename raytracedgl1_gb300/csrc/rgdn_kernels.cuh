@@ -660,6 +660,24 @@ __device__ __forceinline__ void temporal_tile( const FrameArgs& a, int bx, int b
         { ( 1.0f - subPix.x ) * ( 1.0f - subPix.y ), subPix.x * ( 1.0f - subPix.y ) },
         { ( 1.0f - subPix.x ) * subPix.y, subPix.x * subPix.y },
     };
+    // FAST: an L2 prefetch of the history rows under the bilinear footprint, so the history
+    // loads that follow the reprojection tests find them on chip
+    if( FAST && pixPrev.x >= 0 && pixPrev.y >= 0 && pixPrev.x + 1 < u.W && pixPrev.y + 1 < u.H )
+    {
+        const TmaTexel tx = tma_texel( M == MODE_REF ? RGDN_STORAGE_REF : M == MODE_F32 ? RGDN_STORAGE_FP32 : RGDN_STORAGE_FP16 );
+        const int      mb = M == MODE_REF ? 4 : 8;   // moments
+#pragma unroll
+        for( int r = 0; r < 2; r++ )
+        {
+            const size_t q = (size_t)( pixPrev.y + r ) * u.W + pixPrev.x;
+            asm volatile( "prefetch.global.L2 [%0];" ::"l"( static_cast< const char* >( a.diffHistory ) + q * tx.cv ) );
+            asm volatile( "prefetch.global.L2 [%0];" ::"l"( static_cast< const char* >( a.momentsPrev ) + q * mb ) );
+            asm volatile( "prefetch.global.L2 [%0];" ::"l"( static_cast< const char* >( a.histLenPrev ) + q * tx.cv ) );
+            asm volatile( "prefetch.global.L2 [%0];" ::"l"( static_cast< const char* >( a.specAccumPrev ) + q * tx.col ) );
+            asm volatile( "prefetch.global.L2 [%0];" ::"l"( static_cast< const char* >( a.indirAccumPrev ) + q * tx.col ) );
+            if( tx.var ) asm volatile( "prefetch.global.L2 [%0];" ::"l"( a.varHistory + q ) );
+        }
+    }
     // the surface positions the specular terms read once a tap is accepted, loaded with the
     // taps rather than after them
     const float4 sp4 = a.surfPos[ i ];
