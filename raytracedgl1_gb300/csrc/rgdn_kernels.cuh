@@ -1006,11 +1006,13 @@ __device__ __forceinline__ void temporal_tile( const FrameArgs& a, int bx, int b
     S::st3( a.indirAccum, i, indirAccum );
 }
 
-template< int M, bool FAST, bool GEOM, bool GEOMPREV > __global__ void __launch_bounds__( 256 ) k_temporal( const FrameArgs a )
+// NT threads per block (32 x NT/32 tiles), MINB resident blocks per SM
+template< int M, bool FAST, bool GEOM, bool GEOMPREV, int NT = 256, int MINB = 1 >
+__global__ void __launch_bounds__( NT, MINB ) k_temporal( const FrameArgs a )
 {
     __shared__ float u8[ 256 ];
     pdl_launch_dependents();
-    fill_u8( u8, threadIdx.y * blockDim.x + threadIdx.x );
+    for( int k = threadIdx.y * blockDim.x + threadIdx.x; k < 256; k += NT ) fill_u8( u8, k );
     pdl_wait();
     __syncthreads();
     temporal_tile< M, FAST, GEOM, GEOMPREV >( a, blockIdx.x, blockIdx.y, u8 );
@@ -1785,21 +1787,29 @@ __device__ __forceinline__ void atrous_tile( const FrameArgs& a, const int iter,
     }
 }
 
-template< int M, bool FAST, bool HIST, bool GEOMIN > __global__ void __launch_bounds__( 256, 3 ) k_atrous( const FrameArgs a, const int iter )
+// NT threads per block (32 x NT/32 tiles), MINB resident blocks per SM
+template< int M, bool FAST, bool HIST, bool GEOMIN, int NT = 256, int MINB = 3 >
+__global__ void __launch_bounds__( NT, MINB ) k_atrous( const FrameArgs a, const int iter )
 {
     __shared__ float    u8[ 256 ];
     __shared__ uint32_t hist[ HIST ? 256 : 1 ];
     const int t = threadIdx.y * blockDim.x + threadIdx.x;
     pdl_launch_dependents();
-    u8[ t ]     = (float)t / 255.0f;
-    if( HIST ) hist[ t ] = 0u;
+#pragma unroll
+    for( int k = t; k < 256; k += NT )
+    {
+        u8[ k ] = (float)k / 255.0f;
+        if( HIST ) hist[ k ] = 0u;
+    }
     pdl_wait();
     __syncthreads();
     atrous_tile< M, FAST, HIST, GEOMIN >( a, iter, blockIdx.x, blockIdx.y, u8, hist );
     if( HIST )
     {
         __syncthreads();
-        if( hist[ t ] ) atomicAdd( &a.tm->histogram[ t ], hist[ t ] );
+#pragma unroll
+        for( int k = t; k < 256; k += NT )
+            if( hist[ k ] ) atomicAdd( &a.tm->histogram[ k ], hist[ k ] );
     }
 }
 
@@ -2354,8 +2364,12 @@ template< int M > cudaError_t launch_stage_t( const FrameArgs& a, int stage, int
         case RGDN_STAGE_TEMPORAL_ACCUMULATION: e = launch_pdl( dev::k_temporal< M, false, false, false >, grid, blk, 0, s, a ); break;
         case KF_TEMPORAL_EXACT_GEOM: e = launch_pdl( dev::k_temporal< M, false, true, false >, grid, blk, 0, s, a ); break;
         case KF_TEMPORAL_EXACT_GEOM_GP: e = launch_pdl( dev::k_temporal< M, false, true, true >, grid, blk, 0, s, a ); break;
-        case KF_TEMPORAL_FAST: e = launch_pdl( dev::k_temporal< M, true, true, false >, grid, blk, 0, s, a ); break;
-        case KF_TEMPORAL_FAST_GP: e = launch_pdl( dev::k_temporal< M, true, true, true >, grid, blk, 0, s, a ); break;
+        case KF_TEMPORAL_FAST:
+            e = launch_pdl( dev::k_temporal< M, true, true, false, 128, 7 >, dim3( grid.x, ( a.u.H + 3 ) / 4 ), dim3( 32, 4 ), 0, s, a );
+            break;
+        case KF_TEMPORAL_FAST_GP:
+            e = launch_pdl( dev::k_temporal< M, true, true, true, 128, 7 >, dim3( grid.x, ( a.u.H + 3 ) / 4 ), dim3( 32, 4 ), 0, s, a );
+            break;
         case KF_ANTI_FIREFLY_FAST: e = launch_pdl( dev::k_antifirefly_fast< M >, grid, blk, 0, s, a ); break;
         case KF_VARIANCE_EXACT_GEOM: e = launch_pdl( dev::k_variance_geo< M, false >, grid, blk, 0, s, a ); break;
         case RGDN_STAGE_ANTI_FIREFLY: dev::k_antifirefly< M ><<< grid, blk, 0, s >>>( a ); break;
@@ -2380,8 +2394,12 @@ template< int M > cudaError_t launch_fast_t( const FrameArgs& a, int stage, int 
     const dim3 grid( ( a.u.W + 31 ) / 32, ( a.u.H + 7 ) / 8 );
     switch( stage )
     {
-        case KF_ATROUS_FAST: e = launch_pdl( dev::k_atrous< M, true, false, true >, grid, blk, 0, s, a, iter ); break;
-        case KF_ATROUS_FAST_HIST: e = launch_pdl( dev::k_atrous< M, true, true, true >, grid, blk, 0, s, a, iter ); break;
+        case KF_ATROUS_FAST:
+            e = launch_pdl( dev::k_atrous< M, true, false, true, 128, 7 >, dim3( grid.x, ( a.u.H + 3 ) / 4 ), dim3( 32, 4 ), 0, s, a, iter );
+            break;
+        case KF_ATROUS_FAST_HIST:
+            e = launch_pdl( dev::k_atrous< M, true, true, true, 128, 7 >, dim3( grid.x, ( a.u.H + 3 ) / 4 ), dim3( 32, 4 ), 0, s, a, iter );
+            break;
         case KF_VARIANCE_FAST: e = launch_pdl( dev::k_variance_geo< M, true >, grid, blk, 0, s, a ); break;
         default: return cudaErrorInvalidValue;
     }
