@@ -431,7 +431,7 @@ def run_batched(args, dist: Dist, dev: int, cs) -> dict:
         "tuned_config": {"temporal": int(cfg.temporalTile), "anti_firefly": int(cfg.antiFireflyTile),
                          "variance": int(cfg.varianceTile), "atrous": [int(v) for v in cfg.atrousTile][:args.iters],
                          "atrous_blocks_per_sm": [int(v) for v in cfg.atrousBlocksPerSM][:args.iters],
-                         "graphs": int(cfg.useGraphs), "tile_names": ["32x8", "16x16", "64x4"]},
+                         "graphs": int(cfg.useGraphs), "tile_names": ["32x8", "16x16", "64x4", "32x4"]},
         "kernels": kern,
     }
     out["vs_plain"] = round(out["value"] / out["plain_path_mpix_s"], 3)

@@ -306,10 +306,13 @@ typedef struct rgdn_job
  * the oldest. */
 rgdn_status rgdn_submit_batch( rgdn_context* ctx, const rgdn_job* jobs, uint32_t n, rgdn_cuda_stream cudaStream );
 
-/* Tile shapes of the batched kernels (256 threads per block). */
+/* Tile shapes of the batched kernels: 256 threads per block, except 32x4 (128 threads, built for
+ * 7 resident blocks per SM; temporal accumulation and a-trous only, set through
+ * rgdn_batch_set_config; the autotuner chooses among 32x8 and 16x16). */
 #define RGDN_TILE_32X8  0u
 #define RGDN_TILE_16X16 1u
 #define RGDN_TILE_64X4  2u
+#define RGDN_TILE_32X4  3u
 /* The launch configuration of batched steps for one storage mode. The autotuner starts from
  * 32x8 tiles everywhere and, over the first 12 steps, times every candidate of every launch
  * (tile shape; for a-trous also the register budget) on the work being submitted (candidates
@@ -322,7 +325,7 @@ typedef struct rgdn_batch_config
     uint32_t atrousTile[ 6 ];     /* per a-trous iteration */
     uint32_t atrousBlocksPerSM[ 6 ];/* register budget of each a-trous iteration's kernel: built
                                      for 3 or 4 resident blocks per SM (80 or 64 registers per
-                                     thread); 0 = 3 */
+                                     thread); 0 = 3. With RGDN_TILE_32X4 it is 7 (0 or 7). */
     uint32_t useGraphs;           /* replay a captured graph per step (off while timing) */
     uint32_t tuned;               /* read: the autotuner has settled (set_config settles it) */
 } rgdn_batch_config;

@@ -94,7 +94,7 @@ class BatchConfig(C.Structure):
                 ("atrousBlocksPerSM", C.c_uint32 * 6), ("useGraphs", C.c_uint32), ("tuned", C.c_uint32)]
 
 
-TILE_32X8, TILE_16X16, TILE_64X4 = 0, 1, 2
+TILE_32X8, TILE_16X16, TILE_64X4, TILE_32X4 = 0, 1, 2, 3
 
 GBUFFER_PLANES = 15
 REQUEST_COPY, REQUEST_BIND = 0, 1

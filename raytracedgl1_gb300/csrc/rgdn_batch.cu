@@ -40,7 +40,9 @@ namespace
 // tuning steps: kTuneRounds passes over the candidates; the first pass only warms up (module
 // loading, clocks) and is not scored
 constexpr int kTuneRounds = 3;
-const dim3    kShapes[ 3 ] = { dim3( 32, 8 ), dim3( 16, 16 ), dim3( 64, 4 ) };
+// RGDN_TILE_*: 32x8, 16x16 and 64x4 tiles of 256 threads; 32x4 tiles of 128 threads, whose
+// kernels are built for 7 resident blocks per SM
+const dim3    kShapes[ 4 ] = { dim3( 32, 8 ), dim3( 16, 16 ), dim3( 64, 4 ), dim3( 32, 4 ) };
 
 size_t table_bytes( int n ) { return offsetof( BatchConst, jobs ) + sizeof( FrameArgs ) * (size_t)n; }
 
@@ -147,9 +149,12 @@ struct Tuner
     std::vector< Probe > probes;
 };
 
-// Candidates of a launch kind: tile shapes 32x8 and 16x16 (64x4 never won on GB300 and is
-// left to rgdn_batch_set_config); for a-trous also the budget of 3 or 4 blocks per SM.
-// (anti-firefly keeps 32x8: its shared-memory tile is laid out for it)
+// Candidates of a launch kind: tile shapes 32x8 and 16x16, and for a-trous also the budget of
+// 3 or 4 blocks per SM. Left to rgdn_batch_set_config: 64x4, which never won on GB300, and the
+// 128-thread 32x4 builds (7 blocks per SM) of the temporal and a-trous kernels. Those run the
+// kernels themselves faster, but a graph-replayed step of persistent blocks over twice as many
+// tiles took longer (18.9 against 18.1 ms for the 32-stream mix). Anti-firefly keeps 32x8: its
+// shared-memory tile is laid out for it.
 int n_candidates( int kind ) { return kind >= BS_ATROUS0 ? 4 : ( kind == BS_GRADIENT || kind == BS_ANTI_FIREFLY ) ? 1 : 2; }
 int max_candidates() { return 4; }
 void candidate( int kind, int c, int& shape, int& occ )
@@ -176,7 +181,7 @@ struct BatchExec
     GraphKey                   key[ BATCH_SLOTS ];
     Config                     cfg[ 4 ];
     Tuner                      tuner[ 4 ];
-    int                        bps[ 4 ][ RGDN_STAGE_COUNT ][ 5 ];   // resident blocks per SM by variant, -1 = unknown
+    int                        bps[ 4 ][ RGDN_STAGE_COUNT ][ 8 ];   // resident blocks per SM by variant, -1 = unknown
     bool                       timing = false;
     std::vector< Pending >     pending;
     std::vector< cudaEvent_t > eventPool;
@@ -224,7 +229,7 @@ BatchExec* create_exec( int device )
         }
         ex->cfg[ s ].graphs = true;
         for( int st = 0; st < RGDN_STAGE_COUNT; st++ )
-            for( int o = 0; o < 5; o++ ) ex->bps[ s ][ st ][ o ] = -1;
+            for( int o = 0; o < 8; o++ ) ex->bps[ s ][ st ][ o ] = -1;
     }
     if( !ok )
     {
@@ -321,8 +326,9 @@ rgdn_status enqueue_step( rgdn_context* c, BatchExec& ex, DeviceSlots& ds, int s
     for( int k = 0; k < 3; k++ )
     {
         const int kind = BS_TEMPORAL + k;
-        const int arg  = k == 0 ? ( key.gpm << 8 ) : 0;
-        if( ( r = run( kind, stages[ k ], arg, key.shape[ kind ], 0, tuneCand % n_candidates( kind ) ) ) != RGDN_SUCCESS ) return r;
+        const int arg  = k == 0 ? ( key.gpm << 8 ) | ( key.occ[ kind ] << 10 ) : 0;
+        if( ( r = run( kind, stages[ k ], arg, key.shape[ kind ], key.occ[ kind ], tuneCand % n_candidates( kind ) ) ) != RGDN_SUCCESS )
+            return r;
     }
     for( int i = 0; i < key.maxIter; i++ )
     {
@@ -579,23 +585,29 @@ rgdn_status batch_get_config( rgdn_context* c, uint32_t storage, rgdn_batch_conf
 
 rgdn_status batch_set_config( rgdn_context* c, uint32_t storage, const rgdn_batch_config* in )
 {
+    // 32x4 (128-thread) tiles exist for the temporal and a-trous kernels only
     auto ok_shape = []( uint32_t v ) { return v <= RGDN_TILE_64X4; };
-    if( !ok_shape( in->temporalTile ) || !ok_shape( in->antiFireflyTile ) || !ok_shape( in->varianceTile ) )
+    auto ok_shape4 = []( uint32_t v ) { return v <= RGDN_TILE_32X4; };
+    if( !ok_shape4( in->temporalTile ) || !ok_shape( in->antiFireflyTile ) || !ok_shape( in->varianceTile ) )
         return RGDN_WRONG_FUNCTION_ARGUMENT;
     for( int i = 0; i < MAX_ATROUS_ITERATIONS; i++ )
-        if( !ok_shape( in->atrousTile[ i ] ) || ( in->atrousBlocksPerSM[ i ] && ( in->atrousBlocksPerSM[ i ] < 3 || in->atrousBlocksPerSM[ i ] > 4 ) ) )
-            return RGDN_WRONG_FUNCTION_ARGUMENT;
+    {
+        const uint32_t b = in->atrousBlocksPerSM[ i ];
+        if( !ok_shape4( in->atrousTile[ i ] ) ) return RGDN_WRONG_FUNCTION_ARGUMENT;
+        if( in->atrousTile[ i ] == RGDN_TILE_32X4 ? ( b && b != 7 ) : ( b && ( b < 3 || b > 4 ) ) ) return RGDN_WRONG_FUNCTION_ARGUMENT;
+    }
     std::lock_guard< std::mutex > g( c->batchMtx );
     BatchExec*                    ex = exec_of( c );
     if( !ex ) return RGDN_DEVICE_ERROR;
     Config& cf                  = ex->cfg[ storage ];
     cf.shape[ BS_TEMPORAL ]     = (int)in->temporalTile;
+    cf.occ[ BS_TEMPORAL ]       = in->temporalTile == RGDN_TILE_32X4 ? 7 : 0;
     cf.shape[ BS_ANTI_FIREFLY ] = 0;   // the shared-memory tile is 32x8
     cf.shape[ BS_VARIANCE ]     = (int)in->varianceTile;
     for( int i = 0; i < MAX_ATROUS_ITERATIONS; i++ )
     {
         cf.shape[ BS_ATROUS0 + i ] = (int)in->atrousTile[ i ];
-        cf.occ[ BS_ATROUS0 + i ]   = in->atrousBlocksPerSM[ i ] ? (int)in->atrousBlocksPerSM[ i ] : 3;
+        cf.occ[ BS_ATROUS0 + i ]   = in->atrousTile[ i ] == RGDN_TILE_32X4 ? 7 : in->atrousBlocksPerSM[ i ] ? (int)in->atrousBlocksPerSM[ i ] : 3;
     }
     cf.graphs = in->useGraphs != 0;
     Tuner& tu = ex->tuner[ storage ];

@@ -113,14 +113,17 @@ def test_batch_splits_steps_and_falls_back():
     ctx.close()
 
 
-@pytest.mark.parametrize("shape,occ", [(0, 3), (1, 4), (2, 4), (2, 3), (0, 4)])
+@pytest.mark.parametrize("shape,occ", [(0, 3), (1, 4), (2, 4), (2, 3), (0, 4), (3, 7)])
 def test_batch_fixed_configs(shape, occ):
-    """A configuration set through rgdn_batch_set_config (no tuning) gives the same results."""
+    """A configuration set through rgdn_batch_set_config (no tuning) gives the same results.
+    Shape 3 is the 128-thread 32x4 tile (temporal and a-trous; variance keeps 32x8)."""
     ctx = Context(0)
     cfg = N.BatchConfig()
-    cfg.temporalTile = cfg.antiFireflyTile = cfg.varianceTile = shape
+    cfg.temporalTile = shape
+    cfg.antiFireflyTile = 0
+    cfg.varianceTile = shape if shape != N.TILE_32X4 else N.TILE_32X8
     for i in range(6):
-        cfg.atrousTile[i] = (shape + i) % 3
+        cfg.atrousTile[i] = (shape + i) % 3 if shape != N.TILE_32X4 else N.TILE_32X4
         cfg.atrousBlocksPerSM[i] = occ
     cfg.useGraphs = 1
     ctx.set_batch_config(N.STORAGE_BF16, cfg)
