@@ -306,9 +306,10 @@ typedef struct rgdn_job
  * the oldest. */
 rgdn_status rgdn_submit_batch( rgdn_context* ctx, const rgdn_job* jobs, uint32_t n, rgdn_cuda_stream cudaStream );
 
-/* Tile shapes of the batched kernels: 256 threads per block, except 32x4 (128 threads, built for
- * 7 resident blocks per SM; temporal accumulation and a-trous only, set through
- * rgdn_batch_set_config; the autotuner chooses among 32x8 and 16x16). */
+/* Tile shapes of the batched kernels. 32x8, 16x16 and 64x4: persistent blocks of 256 threads,
+ * as many as are resident, each looping over tiles. 32x4 (temporal accumulation and a-trous
+ * only): one tile per 128-thread block, 7 resident per SM, the launch shape of the single-frame
+ * kernels. */
 #define RGDN_TILE_32X8  0u
 #define RGDN_TILE_16X16 1u
 #define RGDN_TILE_64X4  2u

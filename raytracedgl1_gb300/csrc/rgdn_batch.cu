@@ -53,6 +53,7 @@ struct GraphKey
     int hm[ MAX_ATROUS_ITERATIONS ];
     int shape[ BS_COUNT ];
     int occ[ BS_COUNT ];
+    int tiles[ BS_COUNT ];   // the grid of one-tile-per-block launches (occ 7), else 0
 };
 bool same_key( const GraphKey& a, const GraphKey& b ) { return memcmp( &a, &b, sizeof( GraphKey ) ) == 0; }
 
@@ -149,18 +150,35 @@ struct Tuner
     std::vector< Probe > probes;
 };
 
-// Candidates of a launch kind: tile shapes 32x8 and 16x16, and for a-trous also the budget of
-// 3 or 4 blocks per SM. Left to rgdn_batch_set_config: 64x4, which never won on GB300, and the
-// 128-thread 32x4 builds (7 blocks per SM) of the temporal and a-trous kernels. Those run the
-// kernels themselves faster, but a graph-replayed step of persistent blocks over twice as many
-// tiles took longer (18.9 against 18.1 ms for the 32-stream mix). Anti-firefly keeps 32x8: its
-// shared-memory tile is laid out for it.
-int n_candidates( int kind ) { return kind >= BS_ATROUS0 ? 4 : ( kind == BS_GRADIENT || kind == BS_ANTI_FIREFLY ) ? 1 : 2; }
+// Candidates of a launch kind (64x4 never won on GB300 and is left to rgdn_batch_set_config;
+// anti-firefly keeps 32x8, its shared-memory tile is laid out for it):
+//   temporal:  persistent 32x8 and 16x16; one 32x4 tile per 128-thread block (occ 7)
+//   variance:  persistent 32x8 and 16x16
+//   a-trous:   persistent 32x8 and 16x16 at 3 blocks per SM, one 32x4 tile per block, 32x8 at 4
+int n_candidates( int kind )
+{
+    return kind >= BS_ATROUS0 ? 4 : kind == BS_TEMPORAL ? 3 : ( kind == BS_GRADIENT || kind == BS_ANTI_FIREFLY ) ? 1 : 2;
+}
 int max_candidates() { return 4; }
 void candidate( int kind, int c, int& shape, int& occ )
 {
-    shape = ( kind == BS_GRADIENT || kind == BS_ANTI_FIREFLY ) ? 0 : c % 2;
-    occ   = kind >= BS_ATROUS0 ? 3 + ( c / 2 ) % 2 : 0;
+    static const int atrousShape[ 4 ] = { RGDN_TILE_32X8, RGDN_TILE_16X16, RGDN_TILE_32X4, RGDN_TILE_32X8 };
+    static const int atrousOcc[ 4 ]   = { 3, 3, 7, 4 };
+    if( kind >= BS_ATROUS0 )
+    {
+        shape = atrousShape[ c % 4 ];
+        occ   = atrousOcc[ c % 4 ];
+    }
+    else if( kind == BS_TEMPORAL )
+    {
+        shape = c % 3 == 2 ? (int)RGDN_TILE_32X4 : c % 3;
+        occ   = c % 3 == 2 ? 7 : 0;
+    }
+    else
+    {
+        shape = ( kind == BS_GRADIENT || kind == BS_ANTI_FIREFLY ) ? 0 : c % 2;
+        occ   = 0;
+    }
 }
 
 struct Pending
@@ -283,7 +301,10 @@ rgdn_status enqueue_step( rgdn_context* c, BatchExec& ex, DeviceSlots& ds, int s
     auto run = [ & ]( int kind, int stage, int arg, int shape, int occ, int cand ) -> rgdn_status {
         BatchLauncher L = batch_launcher( st, stage );
         if( !L ) return RGDN_INTERNAL_ERROR;
-        const int grid = stage == RGDN_STAGE_LUMINANCE_AVG ? MAX_BATCH : blocks_per_sm( ex, st, stage, occ ) * ex.sms;
+        // persistent launches: resident blocks per SM x SMs; one-tile-per-block launches: the tiles
+        const int grid = stage == RGDN_STAGE_LUMINANCE_AVG ? MAX_BATCH
+                       : occ == 7                          ? key.tiles[ kind ]
+                                                           : blocks_per_sm( ex, st, stage, occ ) * ex.sms;
         if( grid <= 0 ) return RGDN_DEVICE_ERROR;
         cudaEvent_t ta = nullptr, tb = nullptr, ua = nullptr, ub = nullptr;
         if( tuning && kind >= 0 )
@@ -446,6 +467,7 @@ rgdn_status run_step( rgdn_context* c, BatchExec& ex, const rgdn_job* jobs, int 
             pixels[ kind ] += (double)w * h;
         }
         tab->start[ kind ][ n ] = acc;
+        if( kind != BS_GRADIENT && cfg.occ[ kind ] == 7 ) key.tiles[ kind ] = acc;
     }
     for( int i = 0; i < key.maxIter; i++ )
     {

@@ -2252,23 +2252,65 @@ template< int M > __global__ void __launch_bounds__( 256 ) kb_gradient_atrous( c
 // record, 1 = every job has one, 2 = it depends on the job. The block of a job's first tile also
 // clears a histogram that no exposure pass consumed (before the last a-trous iteration adds
 // this frame's).
-// MINB 7: 128-thread blocks (32x4 tiles), 7 resident per SM; otherwise 256 threads.
-template< int M, int GPM, int MINB = 1 > __global__ void __launch_bounds__( MINB == 7 ? 128 : 256, MINB ) kb_temporal( const int slot )
+template< int M, int GPM > __global__ void __launch_bounds__( 256 ) kb_temporal( const int slot )
 {
-    constexpr int NT = MINB == 7 ? 128 : 256;
     __shared__ float u8[ 256 ];
     const int t = threadIdx.y * blockDim.x + threadIdx.x;
-    for( int k = t; k < 256; k += NT ) fill_u8( u8, k );
+    fill_u8( u8, t );
     pdl_wait();
     __syncthreads();
     batch_tiles< false >( slot, BS_TEMPORAL, [ & ]( const FrameArgs& a, int j, int bx, int by ) {
         const uint32_t f = c_batch[ slot ].jobFlags[ j ];
-        if( bx == 0 && by == 0 && ( f & BATCH_JOB_CLEAR_HIST ) )
-            for( int k = t; k < 256; k += NT ) a.tm->histogram[ k ] = 0u;
+        if( bx == 0 && by == 0 && ( f & BATCH_JOB_CLEAR_HIST ) ) a.tm->histogram[ t ] = 0u;
         if( GPM == 1 || ( GPM == 2 && ( f & BATCH_JOB_GEOM_PREV ) ) ) temporal_tile< M, true, true, true >( a, bx, by, u8 );
         else temporal_tile< M, true, true, false >( a, bx, by, u8 );
     } );
     pdl_launch_dependents();
+}
+
+// One tile per block instead of persistent blocks: block b of the launch takes tile b of the
+// step's tile table, in the job j with start[kind][j] <= b < start[kind][j + 1] (a block-uniform
+// binary search over the constant table, which skips jobs without tiles of this kind). The
+// execution shape of the single-frame kernels: 128-thread 32x4 tiles, 7 blocks per SM, the
+// dependent launch triggered at the start.
+template< bool GRAD > __device__ __forceinline__ bool batch_tile_of_block( const int slot, const int kind, int& j, int& bx, int& by )
+{
+    const BatchConst& bc = c_batch[ slot ];
+    const int         b  = (int)blockIdx.x;
+    int               lo = 0, hi = bc.n;
+    if( b >= bc.start[ kind ][ hi ] ) return false;
+    while( hi - lo > 1 )
+    {
+        const int mid = ( lo + hi ) >> 1;
+        if( bc.start[ kind ][ mid ] <= b ) lo = mid;
+        else hi = mid;
+    }
+    j                  = lo;
+    const FrameArgs& a = bc.jobs[ j ];
+    const int        t = b - bc.start[ kind ][ j ];
+    const int        tx = ( ( GRAD ? a.u.GW : a.u.W ) + (int)blockDim.x - 1 ) / (int)blockDim.x;
+    by                 = t / tx;
+    bx                 = t - by * tx;
+    return true;
+}
+
+template< int M, int GPM > __global__ void __launch_bounds__( 128, 7 ) kt_temporal( const int slot )
+{
+    __shared__ float u8[ 256 ];
+    const int t = threadIdx.y * blockDim.x + threadIdx.x;
+    pdl_launch_dependents();
+    for( int k = t; k < 256; k += 128 ) fill_u8( u8, k );
+    int        j = 0, bx = 0, by = 0;
+    const bool has = batch_tile_of_block< false >( slot, BS_TEMPORAL, j, bx, by );
+    pdl_wait();
+    __syncthreads();
+    if( !has ) return;
+    const FrameArgs& a = c_batch[ slot ].jobs[ j ];
+    const uint32_t   f = c_batch[ slot ].jobFlags[ j ];
+    if( bx == 0 && by == 0 && ( f & BATCH_JOB_CLEAR_HIST ) )
+        for( int k = t; k < 256; k += 128 ) a.tm->histogram[ k ] = 0u;
+    if( GPM == 1 || ( GPM == 2 && ( f & BATCH_JOB_GEOM_PREV ) ) ) temporal_tile< M, true, true, true >( a, bx, by, u8 );
+    else temporal_tile< M, true, true, false >( a, bx, by, u8 );
 }
 
 // 32x8 tiles only (the shared-memory layout); a barrier ends each tile before the next reuses
@@ -2297,31 +2339,23 @@ template< int M > __global__ void __launch_bounds__( 256, 5 ) kb_variance( const
 // and bins its HistogramInput into the block's shared histogram, which is flushed into that
 // job's tonemapping state when the block moves to another job and at the end.
 // HM: 0 = the iteration is no job's last, 1 = it is every job's last, 2 = it depends on the job.
-// MINB: resident blocks per SM the kernel is built for (the register budget): 3 or 4 blocks of
-// 256 threads, or 7 of 128 (32x4 tiles).
+// MINB: resident blocks per SM the kernel is built for (the register budget).
 template< int M, int HM, int MINB >
-__global__ void __launch_bounds__( MINB == 7 ? 128 : 256, MINB ) kb_atrous( const int slot, const int iter )
+__global__ void __launch_bounds__( 256, MINB ) kb_atrous( const int slot, const int iter )
 {
-    constexpr int       NT = MINB == 7 ? 128 : 256;
     __shared__ float    u8[ 256 ];
     __shared__ uint32_t hist[ HM ? 256 : 1 ];
     const int t = threadIdx.y * blockDim.x + threadIdx.x;
-    for( int k = t; k < 256; k += NT )
-    {
-        u8[ k ] = (float)k / 255.0f;
-        if( HM ) hist[ k ] = 0u;
-    }
+    u8[ t ]     = (float)t / 255.0f;
+    if( HM ) hist[ t ] = 0u;
     pdl_wait();
     __syncthreads();
     int  histJob = -1;
     auto flush   = [ & ]() {
         __syncthreads();
-        for( int k = t; k < 256; k += NT )
-        {
-            const uint32_t c = hist[ k ];
-            if( c ) atomicAdd( &c_batch[ slot ].jobs[ histJob ].tm->histogram[ k ], c );
-            hist[ k ] = 0u;
-        }
+        const uint32_t c = hist[ t ];
+        if( c ) atomicAdd( &c_batch[ slot ].jobs[ histJob ].tm->histogram[ t ], c );
+        hist[ t ] = 0u;
         __syncthreads();
     };
     batch_tiles< false >( slot, BS_ATROUS0 + iter, [ & ]( const FrameArgs& a, int j, int bx, int by ) {
@@ -2339,6 +2373,35 @@ __global__ void __launch_bounds__( MINB == 7 ? 128 : 256, MINB ) kb_atrous( cons
     } );
     if( HM && histJob >= 0 ) flush();
     pdl_launch_dependents();
+}
+
+// One 32x4 tile per 128-thread block (see kt_temporal); a tile of a job's last iteration bins
+// its HistogramInput in the block's shared histogram and flushes it into that job's state.
+template< int M, int HM > __global__ void __launch_bounds__( 128, 7 ) kt_atrous( const int slot, const int iter )
+{
+    __shared__ float    u8[ 256 ];
+    __shared__ uint32_t hist[ HM ? 256 : 1 ];
+    const int t = threadIdx.y * blockDim.x + threadIdx.x;
+    pdl_launch_dependents();
+    for( int k = t; k < 256; k += 128 )
+    {
+        u8[ k ] = (float)k / 255.0f;
+        if( HM ) hist[ k ] = 0u;
+    }
+    int        j = 0, bx = 0, by = 0;
+    const bool has = batch_tile_of_block< false >( slot, BS_ATROUS0 + iter, j, bx, by );
+    pdl_wait();
+    __syncthreads();
+    if( !has ) return;
+    const FrameArgs& a = c_batch[ slot ].jobs[ j ];
+    if( HM == 1 || ( HM == 2 && iter + 1 == (int)a.u.niter ) )
+    {
+        atrous_tile< M, true, true, true >( a, iter, bx, by, u8, hist );
+        __syncthreads();
+        for( int k = t; k < 256; k += 128 )
+            if( hist[ k ] ) atomicAdd( &a.tm->histogram[ k ], hist[ k ] );
+    }
+    else atrous_tile< M, true, false, true >( a, iter, bx, by, u8, hist );
 }
 
 // one block per job (strided), as k_luminance_avg
@@ -2431,9 +2494,9 @@ template< int M > cudaError_t launch_batch_t( int stage, int iter, int slot, dim
         case RGDN_STAGE_TEMPORAL_ACCUMULATION:
             if( ( ( iter >> 10 ) & 7 ) == 7 )
             {
-                if( v == 0 ) e = launch_pdl( dev::kb_temporal< M, 0, 7 >, grid, block, 0, s, slot );
-                else if( v == 1 ) e = launch_pdl( dev::kb_temporal< M, 1, 7 >, grid, block, 0, s, slot );
-                else e = launch_pdl( dev::kb_temporal< M, 2, 7 >, grid, block, 0, s, slot );
+                if( v == 0 ) e = launch_pdl( dev::kt_temporal< M, 0 >, grid, block, 0, s, slot );
+                else if( v == 1 ) e = launch_pdl( dev::kt_temporal< M, 1 >, grid, block, 0, s, slot );
+                else e = launch_pdl( dev::kt_temporal< M, 2 >, grid, block, 0, s, slot );
             }
             else if( v == 0 ) e = launch_pdl( dev::kb_temporal< M, 0 >, grid, block, 0, s, slot );
             else if( v == 1 ) e = launch_pdl( dev::kb_temporal< M, 1 >, grid, block, 0, s, slot );
@@ -2462,9 +2525,9 @@ template< int M > cudaError_t launch_batch_fast_t( int stage, int iter, int slot
                 case 16: e = launch_pdl( dev::kb_atrous< M, 0, 4 >, grid, block, 0, s, slot, it ); break;
                 case 17: e = launch_pdl( dev::kb_atrous< M, 1, 4 >, grid, block, 0, s, slot, it ); break;
                 case 18: e = launch_pdl( dev::kb_atrous< M, 2, 4 >, grid, block, 0, s, slot, it ); break;
-                case 28: e = launch_pdl( dev::kb_atrous< M, 0, 7 >, grid, block, 0, s, slot, it ); break;
-                case 29: e = launch_pdl( dev::kb_atrous< M, 1, 7 >, grid, block, 0, s, slot, it ); break;
-                case 30: e = launch_pdl( dev::kb_atrous< M, 2, 7 >, grid, block, 0, s, slot, it ); break;
+                case 28: e = launch_pdl( dev::kt_atrous< M, 0 >, grid, block, 0, s, slot, it ); break;
+                case 29: e = launch_pdl( dev::kt_atrous< M, 1 >, grid, block, 0, s, slot, it ); break;
+                case 30: e = launch_pdl( dev::kt_atrous< M, 2 >, grid, block, 0, s, slot, it ); break;
                 default: return cudaErrorInvalidValue;
             }
             break;
@@ -2485,7 +2548,7 @@ template< int M > int batch_blocks_per_sm_t( int stage )
         case RGDN_STAGE_GRADIENT_SAMPLES: return blocks_per_sm( dev::kb_gradient_samples< M > );
         case RGDN_STAGE_GRADIENT_ATROUS: return blocks_per_sm( dev::kb_gradient_atrous< M > );
         case RGDN_STAGE_TEMPORAL_ACCUMULATION: return blocks_per_sm( dev::kb_temporal< M, 2 > );
-        case RGDN_STAGE_TEMPORAL_ACCUMULATION | ( 7 << 10 ): return blocks_per_sm( dev::kb_temporal< M, 2, 7 >, 128 );
+        case RGDN_STAGE_TEMPORAL_ACCUMULATION | ( 7 << 10 ): return blocks_per_sm( dev::kt_temporal< M, 2 >, 128 );
         case RGDN_STAGE_ANTI_FIREFLY: return blocks_per_sm( dev::kb_antifirefly< M > );
         case RGDN_STAGE_LUMINANCE_AVG: return blocks_per_sm( dev::kb_luminance_avg< M > );
         default: return 0;
@@ -2498,7 +2561,7 @@ template< int M > int batch_blocks_per_sm_fast_t( int stage )
         case RGDN_STAGE_VARIANCE_ESTIMATION: return blocks_per_sm( dev::kb_variance< M > );
         case RGDN_STAGE_ATROUS | ( 3 << 10 ): return blocks_per_sm( dev::kb_atrous< M, 2, 3 > );
         case RGDN_STAGE_ATROUS | ( 4 << 10 ): return blocks_per_sm( dev::kb_atrous< M, 2, 4 > );
-        case RGDN_STAGE_ATROUS | ( 7 << 10 ): return blocks_per_sm( dev::kb_atrous< M, 2, 7 >, 128 );
+        case RGDN_STAGE_ATROUS | ( 7 << 10 ): return blocks_per_sm( dev::kt_atrous< M, 2 >, 128 );
         default: return 0;
     }
 }
