@@ -451,7 +451,7 @@ rgdn_status run_step( rgdn_context* c, BatchExec& ex, const rgdn_job* jobs, int 
     double pixels[ BS_COUNT ] = {};
     for( int kind = 0; kind < BS_COUNT; kind++ )
     {
-        const dim3 sh  = kShapes[ kind == BS_GRADIENT ? 0 : cfg.shape[ kind ] ];
+        const dim3 sh  = kind == BS_ANTI_FIREFLY ? dim3( 32, af_tile_rows( (int)st ) ) : kShapes[ kind == BS_GRADIENT ? 0 : cfg.shape[ kind ] ];
         int        acc = 0;
         for( int k = 0; k < n; k++ )
         {

@@ -158,6 +158,10 @@ struct AtrousMaps
     CUtensorMap cv, var, spec, indir, geo;
 };
 
+// Rows of the anti-firefly tile (32 columns, 4 rows per thread of a 32 x 8 block; the kernel and
+// the batched tile tables agree on it).
+__host__ __device__ inline int af_tile_rows( int ) { return 32; }
+
 // Shared-memory staging of one TMA-staged a-trous iteration (kernel and host agree on it).
 // The output tile is tw x th pixels (one per thread). Each source plane's tap footprint is one
 // box of rw x rh texels (steps up to 8: rows -s..th+s) or three bands of rw x th texels

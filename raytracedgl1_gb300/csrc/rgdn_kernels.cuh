@@ -1260,86 +1260,124 @@ __device__ __forceinline__ void af_signal( const FrameArgs& a, const void* src, 
     O::st( dst, i, c );
 }
 
-// Shared-memory form of the 5x5 clamp for a 32x8 tile (blockDim 32 x 8). The (32+4) x (8+4)
-// footprints of the three signals are loaded once (zeros outside the image); then 5-wide row
-// minima / maxima are taken for every footprint row, and a pixel combines the two rows above
-// and below it with the four other texels of its own row. min and max are exact, so this is
-// the 24-tap clamp of af_signal value for value.
+// The 5x5 clamp (the centre excluded) of a tile of 32 columns x 8 RP rows, blockDim 32 x 8,
+// one signal after the other:
+//   1. the thread of column x and row group ty loads its column's RP + 4 texels (zeros outside
+//      the image) into registers and forms, for each of its RP rows, the minimum and maximum of
+//      the 5 rows around it (v5) and of the 4 rows without it (v4), from minima of row pairs;
+//   2. v5 of every column, the two halo columns on each side included, goes to shared memory;
+//   3. the pixel combines its own v4 with v5 of the columns x-2, x-1, x+1, x+2 and clamps its
+//      centre, still in registers.
+// min and max are exact, so this is the 24-tap clamp of af_signal value for value. Shared
+// memory carries only the v5 pairs: one 16-byte store and four 16-byte loads per pixel and
+// signal for the packed 16-bit texels.
+template< int M > struct AfOpsRows
+{
+    static constexpr int RP = 4;   // output rows per thread
+};
+template< int M > struct AfPair
+{
+    typename AfOps< M >::V mn, mx;
+};
 template< int M > struct AfShared
 {
-    using V = typename AfOps< M >::V;
-    static constexpr int TW = 32, TH = 8, RW = TW + 4, RH = TH + 4;
-    V tile[ 3 ][ RH ][ RW ];
-    V hmin[ 3 ][ RH ][ TW ];
-    V hmax[ 3 ][ RH ][ TW ];
+    static constexpr int RP = AfOpsRows< M >::RP, TH = 8 * RP, RW = 32 + 4;
+    AfPair< M >          v5[ TH ][ RW ];
 };
-static_assert( sizeof( AfShared< MODE_F32 > ) <= 48 * 1024 && sizeof( AfShared< MODE_REF > ) <= 48 * 1024,
+static_assert( sizeof( AfShared< MODE_F32 > ) <= 48 * 1024 && sizeof( AfShared< MODE_F16 > ) <= 48 * 1024,
                "the anti-firefly tile must fit static shared memory" );
+
+// Rows r0 - 2 .. r0 + RP + 1 of column x of one signal, zeros outside the image: writes v5 of
+// rows r0 .. r0 + RP - 1 to the shared column `col` (rows `row0` ...), and returns v4 and the
+// centre texel of each row (when v4 is non-null).
+template< int M >
+__device__ __forceinline__ void af_column( const Uniform& u, const void* src, const int x, const int r0, AfShared< M >& sh, const int row0,
+                                           const int col, typename AfOps< M >::V* c, AfPair< M >* v4 )
+{
+    using O          = AfOps< M >;
+    using V          = typename O::V;
+    constexpr int RP = AfOpsRows< M >::RP;
+    const bool    colIn = x >= 0 && x < u.W;
+    V             v[ RP + 4 ];
+#pragma unroll
+    for( int k = 0; k < RP + 4; k++ )
+    {
+        const int y = r0 - 2 + k;
+        v[ k ]      = ( colIn && y >= 0 && y < u.H ) ? O::ld( src, y * u.W + x ) : O::zero();
+    }
+#pragma unroll
+    for( int r = 0; r < RP; r++ )
+    {
+        // rows r-2, r-1 and r+1, r+2 around row r (v[r + 2])
+        const V     mn4 = O::mn( O::mn( v[ r ], v[ r + 1 ] ), O::mn( v[ r + 3 ], v[ r + 4 ] ) );
+        const V     mx4 = O::mx( O::mx( v[ r ], v[ r + 1 ] ), O::mx( v[ r + 3 ], v[ r + 4 ] ) );
+        AfPair< M > p5;
+        p5.mn                       = O::mn( mn4, v[ r + 2 ] );
+        p5.mx                       = O::mx( mx4, v[ r + 2 ] );
+        sh.v5[ row0 + r ][ col ] = p5;
+        if( v4 )
+        {
+            v4[ r ].mn = mn4;
+            v4[ r ].mx = mx4;
+            c[ r ]     = v[ r + 2 ];
+        }
+    }
+}
 
 template< int M > __device__ __forceinline__ void antifirefly_fast_tile( const FrameArgs& a, int bx, int by, AfShared< M >& sh )
 {
     using O          = AfOps< M >;
     using V          = typename O::V;
     using SH         = AfShared< M >;
+    constexpr int RP = SH::RP;
     const Uniform& u = a.u;
     const int      tx = threadIdx.x, ty = threadIdx.y;
-    const int      bx0 = bx * SH::TW, by0 = by * SH::TH;
-    const void*    src[ 3 ] = { a.diffTemp, a.specAccum, a.indirAccum };
-    void*          dst[ 3 ] = { a.diffAccumColor, a.specPing, a.indirPing };
-    const bool     interior = bx0 >= 2 && by0 >= 2 && bx0 + SH::TW + 2 <= u.W && by0 + SH::TH + 2 <= u.H;
-#pragma unroll
-    for( int r = ty; r < SH::RH; r += SH::TH )
+    const int      x  = bx * 32 + tx;
+    const int      r0 = by * SH::TH + ty * RP;
+    if( u.antiFirefly == 0 )
     {
+        if( x >= u.W ) return;
 #pragma unroll
-        for( int c = tx; c < SH::RW; c += SH::TW )
+        for( int r = 0; r < RP; r++ )
         {
-            const int  x = bx0 - 2 + c, y = by0 - 2 + r;
-            const bool in = interior || inside( u, x, y );
-#pragma unroll
-            for( int k = 0; k < 3; k++ ) sh.tile[ k ][ r ][ c ] = in ? O::ld( src[ k ], y * u.W + x ) : O::zero();
+            if( r0 + r >= u.H ) break;
+            const int i = ( r0 + r ) * u.W + x;
+            O::st( a.diffAccumColor, i, O::ld( a.diffTemp, i ) );
+            O::st( a.specPing, i, O::ld( a.specAccum, i ) );
+            O::st( a.indirPing, i, O::ld( a.indirAccum, i ) );
         }
+        return;
     }
-    __syncthreads();
-#pragma unroll
-    for( int r = ty; r < SH::RH; r += SH::TH )
-    {
-#pragma unroll
-        for( int k = 0; k < 3; k++ )
-        {
-            const V* row = &sh.tile[ k ][ r ][ tx ];
-            V        mn = row[ 0 ], mx = row[ 0 ];
-#pragma unroll
-            for( int d = 1; d < 5; d++ )
-            {
-                mn = O::mn( mn, row[ d ] );
-                mx = O::mx( mx, row[ d ] );
-            }
-            sh.hmin[ k ][ r ][ tx ] = mn;
-            sh.hmax[ k ][ r ][ tx ] = mx;
-        }
-    }
-    __syncthreads();
-    const int px = bx0 + tx, py = by0 + ty;
-    if( px >= u.W || py >= u.H ) return;
 #pragma unroll
     for( int k = 0; k < 3; k++ )
     {
-        const V* row = &sh.tile[ k ][ ty + 2 ][ tx ];
-        V        c   = row[ 2 ];
-        if( u.antiFirefly != 0 )
+        const void* src = k == 0 ? a.diffTemp : k == 1 ? a.specAccum : a.indirAccum;
+        void*       dst = k == 0 ? a.diffAccumColor : k == 1 ? a.specPing : a.indirPing;
+        V           c[ RP ];
+        AfPair< M > v4[ RP ];
+        af_column< M >( u, src, x, r0, sh, ty * RP, tx + 2, c, v4 );
+        // the halo columns: local 0, 1 (x0 - 2, x0 - 1) and 34, 35 (x0 + 32, x0 + 33)
+        if( tx < 4 )
         {
-            V mn = O::mn( O::mn( row[ 0 ], row[ 1 ] ), O::mn( row[ 3 ], row[ 4 ] ) );
-            V mx = O::mx( O::mx( row[ 0 ], row[ 1 ] ), O::mx( row[ 3 ], row[ 4 ] ) );
-#pragma unroll
-            for( int dy = -2; dy <= 2; dy++ )
-            {
-                if( dy == 0 ) continue;
-                mn = O::mn( mn, sh.hmin[ k ][ ty + 2 + dy ][ tx ] );
-                mx = O::mx( mx, sh.hmax[ k ][ ty + 2 + dy ][ tx ] );
-            }
-            c = O::mn( O::mx( c, mn ), mx );
+            const int lc = tx < 2 ? tx : 32 + tx;
+            af_column< M >( u, src, bx * 32 - 2 + lc, r0, sh, ty * RP, lc, nullptr, nullptr );
         }
-        O::st( dst[ k ], py * u.W + px, c );
+        __syncthreads();
+        if( x < u.W )
+        {
+#pragma unroll
+            for( int r = 0; r < RP; r++ )
+            {
+                if( r0 + r >= u.H ) break;
+                const AfPair< M >* row = &sh.v5[ ty * RP + r ][ tx ];
+                V mn = O::mn( O::mn( row[ 0 ].mn, row[ 1 ].mn ), O::mn( row[ 3 ].mn, row[ 4 ].mn ) );
+                V mx = O::mx( O::mx( row[ 0 ].mx, row[ 1 ].mx ), O::mx( row[ 3 ].mx, row[ 4 ].mx ) );
+                mn   = O::mn( mn, v4[ r ].mn );
+                mx   = O::mx( mx, v4[ r ].mx );
+                O::st( dst, ( r0 + r ) * u.W + x, O::mn( O::mx( c[ r ], mn ), mx ) );
+            }
+        }
+        __syncthreads();   // the next signal reuses the v5 rows
     }
 }
 
@@ -2313,8 +2351,8 @@ template< int M, int GPM > __global__ void __launch_bounds__( 128, 7 ) kt_tempor
     else temporal_tile< M, true, true, false >( a, bx, by, u8 );
 }
 
-// 32x8 tiles only (the shared-memory layout); a barrier ends each tile before the next reuses
-// the buffers
+// blockDim 32 x 8 over tiles of 32 columns x af_tile_rows rows (the tile function's layout); a
+// barrier ends each tile before the next reuses the shared rows
 template< int M > __global__ void __launch_bounds__( 256 ) kb_antifirefly( const int slot )
 {
     __shared__ AfShared< M > sh;
@@ -2444,7 +2482,9 @@ template< int M > cudaError_t launch_stage_t( const FrameArgs& a, int stage, int
         case KF_TEMPORAL_FAST_GP:
             e = launch_pdl( dev::k_temporal< M, true, true, true, 128, 7 >, dim3( grid.x, ( a.u.H + 3 ) / 4 ), dim3( 32, 4 ), 0, s, a );
             break;
-        case KF_ANTI_FIREFLY_FAST: e = launch_pdl( dev::k_antifirefly_fast< M >, grid, blk, 0, s, a ); break;
+        case KF_ANTI_FIREFLY_FAST:
+            e = launch_pdl( dev::k_antifirefly_fast< M >, dim3( grid.x, ( a.u.H + dev::AfShared< M >::TH - 1 ) / dev::AfShared< M >::TH ), blk, 0, s, a );
+            break;
         case KF_VARIANCE_EXACT_GEOM: e = launch_pdl( dev::k_variance_geo< M, false >, grid, blk, 0, s, a ); break;
         case RGDN_STAGE_ANTI_FIREFLY: dev::k_antifirefly< M ><<< grid, blk, 0, s >>>( a ); break;
         case RGDN_STAGE_VARIANCE_ESTIMATION: dev::k_variance< M ><<< grid, blk, 0, s >>>( a ); break;
