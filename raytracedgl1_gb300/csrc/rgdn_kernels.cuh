@@ -2477,10 +2477,10 @@ template< int M > cudaError_t launch_stage_t( const FrameArgs& a, int stage, int
         case KF_TEMPORAL_EXACT_GEOM: e = launch_pdl( dev::k_temporal< M, false, true, false >, grid, blk, 0, s, a ); break;
         case KF_TEMPORAL_EXACT_GEOM_GP: e = launch_pdl( dev::k_temporal< M, false, true, true >, grid, blk, 0, s, a ); break;
         case KF_TEMPORAL_FAST:
-            e = launch_pdl( dev::k_temporal< M, true, true, false, 128, 7 >, dim3( grid.x, ( a.u.H + 3 ) / 4 ), dim3( 32, 4 ), 0, s, a );
+            e = launch_pdl( dev::k_temporal< M, true, true, false, 128, 8 >, dim3( grid.x, ( a.u.H + 3 ) / 4 ), dim3( 32, 4 ), 0, s, a );
             break;
         case KF_TEMPORAL_FAST_GP:
-            e = launch_pdl( dev::k_temporal< M, true, true, true, 128, 7 >, dim3( grid.x, ( a.u.H + 3 ) / 4 ), dim3( 32, 4 ), 0, s, a );
+            e = launch_pdl( dev::k_temporal< M, true, true, true, 128, 8 >, dim3( grid.x, ( a.u.H + 3 ) / 4 ), dim3( 32, 4 ), 0, s, a );
             break;
         case KF_ANTI_FIREFLY_FAST:
             e = launch_pdl( dev::k_antifirefly_fast< M >, dim3( grid.x, ( a.u.H + dev::AfShared< M >::TH - 1 ) / dev::AfShared< M >::TH ), blk, 0, s, a );
