@@ -276,6 +276,13 @@ rgdn_status rgdn_stream_tonemapping_device( rgdn_stream* stream, void** outDevic
 /* Synchronous read of the tonemapping state after the work on cudaStream. `exposure`
  * is ev100ToLuminousExposure(getAutoEV100()) of Exposure.h:33-51. Any out pointer may be NULL. */
 rgdn_status rgdn_get_tonemapping( rgdn_stream* stream, uint32_t* outHistogram256, float* outAvgLuminance, float* outExposure, rgdn_cuda_stream cudaStream );
+/* Device-side failures of the stream's kernels since the last call, read and cleared after the
+ * work on cudaStream (synchronising it). Every wait inside a kernel is bounded; one that runs
+ * out sets a bit and lets the kernel finish, so the frames since the last call are unreliable
+ * but the device is not hung:
+ *   bit 0  a TMA-staged a-trous pass stopped waiting for its copies (RGDN_FLAG_TMA_STAGING) */
+#define RGDN_DEVICE_ERROR_TMA_WAIT 1u
+rgdn_status rgdn_stream_take_device_errors( rgdn_stream* stream, uint32_t* outFlags, rgdn_cuda_stream cudaStream );
 /* Asynchronous copy, in cudaStream order, of { uint histogram[256]; float avgLuminance; }
  * (1028 bytes) to dst (host, pinned for overlap, or device). No reference counterpart: later
  * passes of the reference read the SSBO on the GPU. */

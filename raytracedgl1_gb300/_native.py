@@ -95,6 +95,7 @@ class BatchConfig(C.Structure):
 
 
 TILE_32X8, TILE_16X16, TILE_64X4, TILE_32X4 = 0, 1, 2, 3
+DEVICE_ERROR_TMA_WAIT = 1
 
 GBUFFER_PLANES = 15
 REQUEST_COPY, REQUEST_BIND = 0, 1
@@ -148,6 +149,7 @@ SIGNATURES = [
     ("rgdn_get_tonemapping", _I, [_VP, C.POINTER(_U32), C.POINTER(C.c_float), C.POINTER(C.c_float), _VP]),
     ("rgdn_set_tonemapping", _I, [_VP, C.POINTER(_U32), C.c_float, _VP]),
     ("rgdn_stream_copy_tonemapping", _I, [_VP, _VP, _VP]),
+    ("rgdn_stream_take_device_errors", _I, [_VP, C.POINTER(_U32), _VP]),
     ("rgdn_submit_batch", _I, [_VP, C.POINTER(Job), _U32, _VP]),
     ("rgdn_status_string", C.c_char_p, [_I]),
     ("rgdn_context_launch_count", _I, [_VP, C.POINTER(_U64)]),

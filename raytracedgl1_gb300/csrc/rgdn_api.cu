@@ -931,6 +931,23 @@ rgdn_status rgdn_get_tonemapping( rgdn_stream* s, uint32_t* hist, float* avgLum,
     return RGDN_SUCCESS;
 }
 
+rgdn_status rgdn_stream_take_device_errors( rgdn_stream* s, uint32_t* outFlags, rgdn_cuda_stream cs )
+{
+    if( !valid_stream( s ) ) return RGDN_WRONG_INSTANCE;
+    if( !outFlags ) return RGDN_WRONG_FUNCTION_ARGUMENT;
+    cudaSetDevice( s->ctx->device );
+    uint32_t     flags = 0;
+    cudaStream_t st    = (cudaStream_t)cs;
+    if( cudaMemcpyAsync( &flags, &s->tm->errorFlags, sizeof( flags ), cudaMemcpyDeviceToHost, st ) != cudaSuccess ||
+        cudaStreamSynchronize( st ) != cudaSuccess )
+        return RGDN_DEVICE_ERROR;
+    if( flags && ( cudaMemsetAsync( &s->tm->errorFlags, 0, sizeof( uint32_t ), st ) != cudaSuccess ||
+                   cudaStreamSynchronize( st ) != cudaSuccess ) )
+        return RGDN_DEVICE_ERROR;
+    *outFlags = flags;
+    return RGDN_SUCCESS;
+}
+
 rgdn_status rgdn_stream_copy_tonemapping( rgdn_stream* s, void* dst, rgdn_cuda_stream cs )
 {
     if( !valid_stream( s ) ) return RGDN_WRONG_INSTANCE;

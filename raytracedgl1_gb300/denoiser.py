@@ -203,6 +203,13 @@ class Stream:
         N.check(self.lib.rgdn_get_tonemapping(self.handle, None, None, None, _stream_handle(cuda_stream)))
 
     # --- tonemapping state ---------------------------------------------------------------
+    def take_device_errors(self, cuda_stream=None) -> int:
+        """Device-side failure flags since the last call (N.DEVICE_ERROR_*), cleared."""
+        out = C.c_uint32()
+        N.check(self.lib.rgdn_stream_take_device_errors(self.handle, C.byref(out), _stream_handle(cuda_stream)),
+                "rgdn_stream_take_device_errors")
+        return out.value
+
     def tonemapping(self, cuda_stream=None):
         hist = (C.c_uint32 * 256)()
         avg = C.c_float()

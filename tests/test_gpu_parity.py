@@ -405,6 +405,23 @@ def test_error_paths(ctx):
     assert lib.rgdn_denoise(None, 0, p, None) == N.WRONG_INSTANCE
 
 
+def test_device_errors_clear_on_a_clean_run(ctx):
+    """Every bounded wait inside a kernel that runs out leaves a flag for
+    rgdn_stream_take_device_errors; frames on the default and the TMA-staged paths leave none."""
+    W, H = 96, 54
+    sc = Scene(W, H, seed=29)
+    s = Stream(ctx, W, H, N.STORAGE_FP16)
+    for f in range(4):
+        bufs, p = sc.generate(f)
+        if f >= 2:
+            p.flags |= N.FLAG_TMA_STAGING
+        upload_frame(s, None, bufs, f & 1)
+        Denoiser(s).Denoise(f & 1, p)
+        Tonemapping(s).CalculateExposure(f & 1, p)
+        assert s.take_device_errors() == 0
+    s.close()
+
+
 def test_budget_admission(cuda_ok):
     from raytracedgl1_gb300.denoiser import Context, required_bytes
     need = required_bytes(64, 36, N.STORAGE_REF)
