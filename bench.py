@@ -648,6 +648,29 @@ def run_ours(args, dist: Dist):
                      "alg_bytes": alg, "gbs": alg / (ms / n / 1e3) / 1e9})
     kern.sort(key=lambda d: -d["avg_us"] * d["launches"])
     kernel_total_us = sum(d["avg_us"] * d["launches"] for d in kern) / args.steps
+
+    # --- exposure application and tonemapping (rgdn_prepare_final), after the same steps ------
+    from raytracedgl1_gb300.denoiser import ImageComposition
+    comp = ImageComposition(st)
+    fparams = N.FinalParams.defaults()
+    fparams.lightmapScreenCoverage = 0.0
+    fparams.flags = N.FINAL_APPLY_SCATTERING
+    nfin = max(args.steps, 20)
+    with torch.cuda.stream(cs):
+        for k in range(3):
+            comp.Finalize(k & 1, fparams, cs)
+        fe = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+        fe[0].record(cs)
+        for k in range(nfin):
+            comp.Finalize(k & 1, fparams, cs)
+        fe[1].record(cs)
+    cs.synchronize()
+    fin_us = 1e3 * fe[0].elapsed_time(fe[1]) / nfin
+    pre_b = {"ref": 4, "fp32": 16, "fp16": 8, "bf16": 8}[args.storage]
+    fin_alg = (pre_b + 4 + 8 + 8 + 2 * pre_b) * W * H   # PreFinal, emission, scattering, throughput in; Final, bloom out
+    final = {"kernel": "prepare_final", "what": "CmCheckerboard + CmPrepareFinal (LPM 709, bloom input, scattering on)",
+             "us_per_frame": round(fin_us, 2), "mpix_s": round(W * H / fin_us, 1),
+             "alg_bytes": fin_alg, "gbs": round(fin_alg / (fin_us / 1e6) / 1e9, 1)}
     top = kern[0]
     peak, peak_kind = load_peaks()
 
@@ -770,6 +793,7 @@ def run_ours(args, dist: Dist):
                      "alg_bytes_per_launch": top["alg_bytes"]},
         "kernels": [{k: (round(v, 2) if isinstance(v, float) else v) for k, v in d.items()} for d in kern],
         "kernel_sum_us_per_step": round(kernel_total_us, 2),
+        "prepare_final": final,
         "path_alg_gbs": round(sum(d["alg_bytes"] * d["launches"] for d in kern) / args.steps /
                               (total_ms_max / args.steps / 1e3) / 1e9, 1),
         "e2e": {"value": round(e2e_value, 2), "unit": "Mpix/s", "h2d_bytes_per_step": int(h2d),

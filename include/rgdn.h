@@ -137,6 +137,11 @@ typedef enum rgdn_framebuf
     RGDN_FB_DIFF_COLOR_HISTORY_VARIANCE,
     RGDN_FB_DIFF_PING_VARIANCE,
     RGDN_FB_DIFF_PONG_VARIANCE,
+    /* exposure application and tonemapping (rgdn_prepare_final), regular pixel layout */
+    RGDN_FB_SCREEN_EMIS_RT,           /* B10G11R11: the producer's screen-space emission */
+    RGDN_FB_SCATTERING,               /* RGBA16_SFLOAT: volumetric in-scattering (rgb), transmittance (a) */
+    RGDN_FB_FINAL,                    /* the exposed, tonemapped image (PRE_FINAL's format) */
+    RGDN_FB_BLOOM_INPUT,              /* bloom input (PRE_FINAL's format) */
     RGDN_FB_COUNT
 } rgdn_framebuf;
 
@@ -246,8 +251,8 @@ rgdn_status rgdn_stream_required_bytes( const rgdn_stream_create_info* info, uin
 /* Framebuffers::GetImageHandles (Framebuffers.cpp:34-49): the plane of `fb` that
  * frameIndex (0 or 1) selects. A producer writes the G-buffer there directly. */
 rgdn_status rgdn_stream_get_framebuffer( rgdn_stream* stream, uint32_t fb, uint32_t frameIndex, rgdn_image* outImage );
-/* Points a producer-written G-buffer image (RGDN_FB_ALBEDO .. RGDN_FB_GRADIENT_RESHADED) of
- * slot frameIndex at caller-owned device memory (dense rows, 16-byte aligned), so a renderer
+/* Points a producer-written G-buffer image (RGDN_FB_ALBEDO .. RGDN_FB_GRADIENT_RESHADED,
+ * RGDN_FB_SCREEN_EMIS_RT, RGDN_FB_SCATTERING) of slot frameIndex at caller-owned device memory (dense rows, 16-byte aligned), so a renderer
  * that already holds its G-buffer in HBM hands it over without a copy — the role of the
  * reference's shared Framebuffers images (PathTracer writes, Denoiser reads). NULL restores
  * the stream's own plane. The memory must stay valid while work using it is in flight. */
@@ -266,6 +271,31 @@ rgdn_status rgdn_denoise( rgdn_stream* stream, uint32_t frameIndex, const rgdn_f
 /* Tonemapping::CalculateExposure (Tonemapping.cpp:59-165): 256-bin log-luminance
  * histogram of HISTOGRAM_INPUT, then the adapted average luminance. */
 rgdn_status rgdn_calculate_exposure( rgdn_stream* stream, uint32_t frameIndex, const rgdn_frame_params* params, rgdn_cuda_stream cudaStream );
+/* ---- exposure application and tonemapping ------------------------------------------
+ * ImageComposition::PrepareForRaster + Finalize (ImageComposition.cpp:87-155) without the
+ * rasterised geometry between them, in one kernel per pixel of the regular layout:
+ *   CmCheckerboard.comp      PRE_FINAL and SCREEN_EMIS_RT, resolved from their cross
+ *                            neighbours where the primary ray was split (THROUGHPUT.a > 0.5)
+ *   CmPrepareFinal.comp      volumetric scattering (optional), then finalizeColor: uncharted2
+ *                            under classic shading, else exposure (from the stream's adapted
+ *                            average luminance) + screen emission through AMD LPM (709 -> 709);
+ *                            and the bloom input
+ * into FINAL and BLOOM_INPUT. Call after rgdn_calculate_exposure. The debug views of
+ * processDebug and the SHIPPING_HACK acid fog are not part of it. */
+typedef struct rgdn_final_params
+{
+    float    luminanceWhitePoint;      /* uncharted2 white point (classic shading); reference default 10 */
+    float    emissionMaxScreenColor;   /* screen emission scale; default 1.5 */
+    float    bloomEmissionMultiplier;  /* EV offset of screen emission in the bloom input; default 16 */
+    float    bloomThreshold;           /* bloom input threshold (inputThreshold); default 4 */
+    float    saturation[ 3 ];          /* LPM per-channel saturation (<0 less, >0 more); default 0 */
+    float    crosstalk[ 3 ];           /* LPM crosstalk, one channel 1, others in (0, 1]; default 1 */
+    float    lightmapScreenCoverage;   /* classic shading where x < coverage * width */
+    uint32_t flags;                    /* RGDN_FINAL_* */
+} rgdn_final_params;
+#define RGDN_FINAL_APPLY_SCATTERING 0x1u /* hdr = hdr * scattering.a + scattering.rgb */
+rgdn_status rgdn_prepare_final( rgdn_stream* stream, uint32_t frameIndex, const rgdn_final_params* params, rgdn_cuda_stream cudaStream );
+
 /* One stage alone (the plain path / per-stage checking). `iteration` selects the
  * a-trous or gradient a-trous iteration. */
 rgdn_status rgdn_denoise_stage( rgdn_stream* stream, uint32_t stage, uint32_t iteration, uint32_t frameIndex, const rgdn_frame_params* params, rgdn_cuda_stream cudaStream );

@@ -36,7 +36,7 @@ def load():
         return _lib
     if not os.path.exists(LIB_PATH):
         raise ImportError(f"{LIB_PATH} missing: build it with `python -m raytracedgl1_gb300.build`")
-    from raytracedgl1_gb300._native import FrameParams
+    from raytracedgl1_gb300._native import FinalParams, FrameParams
     lib = C.CDLL(LIB_PATH)
     P = C.POINTER
     sig = {
@@ -50,6 +50,9 @@ def load():
         "orc_denoise": (C.c_int, [C.c_void_p, C.c_uint32, P(FrameParams), C.c_int]),
         "orc_calculate_exposure": (C.c_int, [C.c_void_p, C.c_uint32, P(FrameParams), C.c_int]),
         "orc_exposure_from_avg": (C.c_float, [C.c_float]),
+        "orc_prepare_final": (C.c_int, [C.c_void_p, C.c_uint32, P(FinalParams), C.c_int]),
+        "orc_lpm_setup": (None, [P(C.c_float), P(C.c_float), P(C.c_float)]),
+        "orc_lpm_filter": (None, [P(C.c_float), P(C.c_float), P(C.c_float)]),
         "orc_get_tonemapping": (None, [C.c_void_p, P(C.c_uint32), P(C.c_float), P(C.c_double)]),
         "orc_set_tonemapping": (None, [C.c_void_p, P(C.c_uint32), C.c_float]),
         "orc_f32_to_f16": (C.c_uint16, [C.c_float]),
@@ -131,6 +134,12 @@ class OracleStream:
         if r != 0:
             raise RuntimeError(f"orc_calculate_exposure failed: {r}")
 
+    def prepare_final(self, frame_index: int, params, nthreads: int = 0) -> None:
+        """CmCheckerboard + CmPrepareFinal into FINAL and BLOOM_INPUT (rgdn_final_params)."""
+        r = self.lib.orc_prepare_final(self.h, frame_index, C.byref(params), nthreads or nthreads_default())
+        if r != 0:
+            raise RuntimeError(f"orc_prepare_final failed: {r}")
+
     def tonemapping(self):
         hist = (C.c_uint32 * 256)()
         avg = C.c_float()
@@ -188,3 +197,19 @@ def decode_normal(p: int):
 
 def color_bin(lum: float, min_log: float, max_log: float) -> int:
     return load().orc_color_bin(lum, min_log, max_log)
+
+
+# --- AMD LPM (709 -> 709, no shoulder) for the known-answer tests -------------------------
+def lpm_setup(saturation=(0.0, 0.0, 0.0), crosstalk=(1.0, 1.0, 1.0)) -> dict:
+    """The LpmFilter constants: saturation powers, contrast, tone scale/bias, luma weights."""
+    sat, ct, out = (C.c_float * 3)(*saturation), (C.c_float * 3)(*crosstalk), (C.c_float * 16)()
+    load().orc_lpm_setup(sat, ct, out)
+    v = list(out)
+    return {"saturation": v[0:3], "contrast": v[3], "tone_scale_bias": v[4:6], "luma": v[6:9],
+            "rcp_luma": v[9:12], "crosstalk": v[12:15]}
+
+
+def lpm_filter(rgb, saturation=(0.0, 0.0, 0.0), crosstalk=(1.0, 1.0, 1.0)):
+    sat, ct, c = (C.c_float * 3)(*saturation), (C.c_float * 3)(*crosstalk), (C.c_float * 3)(*rgb)
+    load().orc_lpm_filter(sat, ct, c)
+    return tuple(c)

@@ -425,6 +425,12 @@ FbInfo fb_info( uint32_t fb, uint32_t mode )
         case RGDN_FB_DIFF_COLOR_HISTORY_VARIANCE:
         case RGDN_FB_DIFF_PING_VARIANCE:
         case RGDN_FB_DIFF_PONG_VARIANCE: return { varpl, false, false };
+        // GenerateShaderCommon.py:820-863 ScreenEmisRT, Scattering, Final, BloomInput (the last
+        // two in PreFinal's format per storage mode)
+        case RGDN_FB_SCREEN_EMIS_RT: return { F_B10G11R11, false, false };
+        case RGDN_FB_SCATTERING: return { F_RGBA16F, false, false };
+        case RGDN_FB_FINAL:
+        case RGDN_FB_BLOOM_INPUT: return { pre, false, false };
         default: return { F_NONE, false, false };
     }
 }
@@ -1378,6 +1384,184 @@ template< class T > struct Denoise
     }
 };
 
+
+// ============================================================================================
+//  Exposure application and tonemapping: CmCheckerboard.comp:27-69 + CmPrepareFinal.comp:57-187
+// ============================================================================================
+
+// AMD FidelityFX LPM 1.0 (vendored as Shaders/LPM/ffx_lpm.h), the 709 -> 709 configuration
+// without shoulder tuning that ImageComposition uses. Setup: LpmSetupCustom.inl:40-70;
+// LpmColRgbToXyz / LpmMatInv3x3 (ffx_lpm.h:157-210) for the luma coefficients. Filter:
+// LpmMap (ffx_lpm.h:727-812) with con, soft, con2, clip, scaleOnly and shoulder all false.
+template< class T > struct Lpm
+{
+    T saturation[ 3 ], contrast, tsb[ 2 ], lumaT[ 3 ], rcpLumaT[ 3 ], crosstalk[ 3 ];
+};
+
+template< class T > Lpm< T > lpm_setup( const float sat[ 3 ], const float ct[ 3 ] )
+{
+    Lpm< T > L;
+    const T hdrMax = (T)256, exposure = (T)8, shoulderContrast = (T)1;
+    T       contrast = K( 0.1 ) + (T)1;
+    for( int k = 0; k < 3; k++ ) L.saturation[ k ] = (T)sat[ k ] + contrast;
+    L.contrast     = contrast;
+    const T midIn  = hdrMax * K( 0.18 ) * o_exp2( -exposure );
+    const T midOut = K( 0.18 );
+    const T cs     = contrast * shoulderContrast;
+    const T z0     = -o_pow( midIn, contrast );
+    const T z1     = o_pow( hdrMax, cs ) * o_pow( midIn, contrast );
+    const T z2     = o_pow( hdrMax, contrast ) * o_pow( midIn, cs ) * midOut;
+    const T z3     = o_pow( hdrMax, cs ) * midOut;
+    const T z4     = o_pow( midIn, cs ) * midOut;
+    L.tsb[ 0 ]     = -( ( z0 + ( midOut * ( z1 - z2 ) ) * ( (T)1 / ( z3 - z4 ) ) ) * ( (T)1 / z4 ) );
+    const T w0     = o_pow( hdrMax, cs ) * o_pow( midIn, contrast );
+    const T w1     = o_pow( hdrMax, contrast ) * o_pow( midIn, cs ) * midOut;
+    const T w2     = o_pow( hdrMax, cs ) * midOut;
+    const T w3     = o_pow( midIn, cs ) * midOut;
+    L.tsb[ 1 ]     = ( w0 - w1 ) * ( (T)1 / ( w2 - w3 ) );
+    // RGB -> XYZ of the 709 primaries and the D65 white: the primaries' xyz as columns, scaled
+    // per primary by inverse(columns) . white XYZ (Y = 1); the Y row gives the luma weights
+    const T xy[ 3 ][ 2 ] = { { K( 0.64 ), K( 0.33 ) }, { K( 0.30 ), K( 0.60 ) }, { K( 0.15 ), K( 0.06 ) } };
+    const T wxy[ 2 ]     = { K( 0.3127 ), K( 0.3290 ) };
+    T       m[ 3 ][ 3 ];   // m[row][primary]
+    for( int c = 0; c < 3; c++ )
+    {
+        m[ 0 ][ c ] = xy[ c ][ 0 ];
+        m[ 1 ][ c ] = xy[ c ][ 1 ];
+        m[ 2 ][ c ] = (T)1 - ( xy[ c ][ 0 ] + xy[ c ][ 1 ] );
+    }
+    const T wr = (T)1 / wxy[ 1 ];
+    const T w[ 3 ] = { wxy[ 0 ] * wr, wxy[ 1 ] * wr, ( (T)1 - ( wxy[ 0 ] + wxy[ 1 ] ) ) * wr };
+    // inverse by cofactors
+    const T det = m[ 0 ][ 0 ] * ( m[ 1 ][ 1 ] * m[ 2 ][ 2 ] - m[ 2 ][ 1 ] * m[ 1 ][ 2 ] ) - m[ 0 ][ 1 ] * ( m[ 1 ][ 0 ] * m[ 2 ][ 2 ] - m[ 1 ][ 2 ] * m[ 2 ][ 0 ] ) +
+                  m[ 0 ][ 2 ] * ( m[ 1 ][ 0 ] * m[ 2 ][ 1 ] - m[ 1 ][ 1 ] * m[ 2 ][ 0 ] );
+    const T id = (T)1 / det;
+    T inv[ 3 ][ 3 ];
+    inv[ 0 ][ 0 ] = ( m[ 1 ][ 1 ] * m[ 2 ][ 2 ] - m[ 2 ][ 1 ] * m[ 1 ][ 2 ] ) * id;
+    inv[ 0 ][ 1 ] = ( m[ 0 ][ 2 ] * m[ 2 ][ 1 ] - m[ 0 ][ 1 ] * m[ 2 ][ 2 ] ) * id;
+    inv[ 0 ][ 2 ] = ( m[ 0 ][ 1 ] * m[ 1 ][ 2 ] - m[ 0 ][ 2 ] * m[ 1 ][ 1 ] ) * id;
+    inv[ 1 ][ 0 ] = ( m[ 1 ][ 2 ] * m[ 2 ][ 0 ] - m[ 1 ][ 0 ] * m[ 2 ][ 2 ] ) * id;
+    inv[ 1 ][ 1 ] = ( m[ 0 ][ 0 ] * m[ 2 ][ 2 ] - m[ 0 ][ 2 ] * m[ 2 ][ 0 ] ) * id;
+    inv[ 1 ][ 2 ] = ( m[ 1 ][ 0 ] * m[ 0 ][ 2 ] - m[ 0 ][ 0 ] * m[ 1 ][ 2 ] ) * id;
+    inv[ 2 ][ 0 ] = ( m[ 1 ][ 0 ] * m[ 2 ][ 1 ] - m[ 2 ][ 0 ] * m[ 1 ][ 1 ] ) * id;
+    inv[ 2 ][ 1 ] = ( m[ 2 ][ 0 ] * m[ 0 ][ 1 ] - m[ 0 ][ 0 ] * m[ 2 ][ 1 ] ) * id;
+    inv[ 2 ][ 2 ] = ( m[ 0 ][ 0 ] * m[ 1 ][ 1 ] - m[ 1 ][ 0 ] * m[ 0 ][ 1 ] ) * id;
+    T y[ 3 ];
+    for( int c = 0; c < 3; c++ )
+    {
+        const T sc = inv[ c ][ 0 ] * w[ 0 ] + inv[ c ][ 1 ] * w[ 1 ] + inv[ c ][ 2 ] * w[ 2 ];
+        y[ c ]     = m[ 1 ][ c ] * sc;
+    }
+    const T rs = (T)1 / ( y[ 0 ] + y[ 1 ] + y[ 2 ] );
+    for( int k = 0; k < 3; k++ )
+    {
+        L.lumaT[ k ]     = y[ k ] * rs;
+        L.rcpLumaT[ k ]  = (T)1 / L.lumaT[ k ];
+        L.crosstalk[ k ] = (T)ct[ k ];
+    }
+    return L;
+}
+
+template< class T > V3< T > lpm_filter( V3< T > c, const Lpm< T >& L )
+{
+    const T rcpMax = (T)1 / o_fmax( c.x, o_fmax( c.y, c.z ) );
+    T       rR = c.x * rcpMax, rG = c.y * rcpMax, rB = c.z * rcpMax;
+    rR = o_pow( rR, L.saturation[ 0 ] );
+    rG = o_pow( rG, L.saturation[ 1 ] );
+    rB = o_pow( rB, L.saturation[ 2 ] );
+    T luma = c.y * L.lumaT[ 1 ] + ( c.x * L.lumaT[ 0 ] + ( c.z * L.lumaT[ 2 ] ) );
+    luma   = o_pow( luma, L.contrast );
+    luma   = luma * ( (T)1 / ( luma * L.tsb[ 0 ] + L.tsb[ 1 ] ) );
+    const T lumaRatio  = rR * L.lumaT[ 0 ] + rG * L.lumaT[ 1 ] + rB * L.lumaT[ 2 ];
+    const T ratioScale = gsat( luma * ( (T)1 / lumaRatio ) );
+    T       cR = gsat( rR * ratioScale ), cG = gsat( rG * ratioScale ), cB = gsat( rB * ratioScale );
+    const T capR = -L.crosstalk[ 0 ] * cR + L.crosstalk[ 0 ];
+    const T capG = -L.crosstalk[ 1 ] * cG + L.crosstalk[ 1 ];
+    const T capB = -L.crosstalk[ 2 ] * cB + L.crosstalk[ 2 ];
+    T lumaAdd = gsat( ( -cB ) * L.lumaT[ 2 ] + ( ( -cR ) * L.lumaT[ 0 ] + ( ( -cG ) * L.lumaT[ 1 ] + luma ) ) );
+    const T t = lumaAdd * ( (T)1 / ( capG * L.lumaT[ 1 ] + ( capR * L.lumaT[ 0 ] + ( capB * L.lumaT[ 2 ] ) ) ) );
+    cR      = gsat( t * capR + cR );
+    cG      = gsat( t * capG + cG );
+    cB      = gsat( t * capB + cB );
+    lumaAdd = gsat( ( -cB ) * L.lumaT[ 2 ] + ( ( -cR ) * L.lumaT[ 0 ] + ( ( -cG ) * L.lumaT[ 1 ] + luma ) ) );
+    cR      = gsat( lumaAdd * L.rcpLumaT[ 0 ] + cR );
+    cG      = gsat( lumaAdd * L.rcpLumaT[ 1 ] + cG );
+    cB      = gsat( lumaAdd * L.rcpLumaT[ 2 ] + cB );
+    return { cR, cG, cB };
+}
+
+// uncharted2TonemapOp (CmPrepareFinal.comp:69-80)
+template< class T > T u2_op( T x )
+{
+    const T A = K( 0.15 ), B = K( 0.50 ), C = K( 0.10 ), D = K( 0.20 ), E = K( 0.02 ), F = K( 0.30 );
+    return ( ( x * ( A * x + C * B ) + D * E ) / ( x * ( A * x + B ) + D * F ) ) - E / F;
+}
+
+template< class T > void prepare_final( Stream& s, uint32_t fi, const rgdn_final_params& p, int nthreads )
+{
+    const Lpm< T > L     = lpm_setup< T >( p.saturation, p.crosstalk );
+    const int      W     = s.W, H = s.H, sep = W / 2;
+    Plane&         pre   = s.cur( RGDN_FB_PRE_FINAL, fi );
+    Plane&         emisP = s.cur( RGDN_FB_SCREEN_EMIS_RT, fi );
+    Plane&         scat  = s.cur( RGDN_FB_SCATTERING, fi );
+    Plane&         thr   = s.cur( RGDN_FB_THROUGHPUT, fi );
+    Plane&         outF  = s.cur( RGDN_FB_FINAL, fi );
+    Plane&         outB  = s.cur( RGDN_FB_BLOOM_INPUT, fi );
+    // getAutoEV100 / ev100ToLuminousExposure (Exposure.h:14-51); the tonemapping SSBO holds a float
+    const T avg      = (T)( std::is_same< T, float >::value ? (double)(float)s.avgLum : s.avgLum );
+    const T ev       = o_log2( o_fmax( (T)0, avg ) * (T)100 / K( 12.5 ) );
+    const T maxLum   = K( 1.2 ) * o_exp2( ev );
+    const T exposure = maxLum > (T)0 ? (T)1 / maxLum : (T)0;
+    const T quarter  = K( 0.25 );
+    auto resolve = [ & ]( Plane& src, int x, int y, int cbx, V3< T > c ) {
+        const T lf = ( cbx == 0 || cbx == sep ) ? (T)0 : (T)1;
+        const T rf = ( cbx == sep || cbx == W ) ? (T)0 : (T)1;
+        const V3< T > l = xyz( src.fetch< T >( x - 1, y ) ), r = xyz( src.fetch< T >( x + 1, y ) );
+        const V3< T > d = xyz( src.fetch< T >( x, y + 1 ) ), u = xyz( src.fetch< T >( x, y - 1 ) );
+        const V3< T > cross = { quarter * l.x * lf + quarter * r.x * rf + quarter * d.x + quarter * u.x,
+                                quarter * l.y * lf + quarter * r.y * rf + quarter * d.y + quarter * u.y,
+                                quarter * l.z * lf + quarter * r.z * rf + quarter * d.z + quarter * u.z };
+        return vmix( c, cross, K( 0.5 ) );
+    };
+    parallel_rows( H, nthreads, [ & ]( int y ) {
+        for( int x = 0; x < W; x++ )
+        {
+            const int cbx  = ( ( x + y % 2 ) % 2 ) * sep + x / 2;   // getCheckerboardPix
+            V3< T >   hdr  = xyz( pre.fetch< T >( x, y ) );
+            V3< T >   emis = xyz( emisP.fetch< T >( x, y ) );
+            if( thr.fetch< T >( cbx, y ).w > K( 0.5 ) )   // wasSplit
+            {
+                hdr  = resolve( pre, x, y, cbx, hdr );
+                emis = resolve( emisP, x, y, cbx, emis );
+            }
+            if( p.flags & RGDN_FINAL_APPLY_SCATTERING )
+            {
+                const V4< T > v = scat.fetch< T >( x, y );
+                hdr             = { hdr.x * v.w + v.x, hdr.y * v.w + v.y, hdr.z * v.w + v.z };
+            }
+            V3< T > color;
+            if( (T)x < (T)p.lightmapScreenCoverage * (T)W )   // classicShading
+            {
+                const T w = u2_op< T >( (T)p.luminanceWhitePoint );
+                color     = { u2_op< T >( (T)2 * hdr.x ) / w, u2_op< T >( (T)2 * hdr.y ) / w, u2_op< T >( (T)2 * hdr.z ) / w };
+            }
+            else
+            {
+                const T em = (T)p.emissionMaxScreenColor;
+                color      = lpm_filter< T >( { hdr.x * exposure + emis.x * em, hdr.y * exposure + emis.y * em, hdr.z * exposure + emis.z * em }, L );
+            }
+            const T el    = o_exp2( ev + (T)p.bloomEmissionMultiplier - (T)3 );
+            V3< T > bloom = { ( hdr.x + emis.x * el ) * exposure, ( hdr.y + emis.y * el ) * exposure, ( hdr.z + emis.z * el ) * exposure };
+            if( std::isnan( bloom.x ) || std::isnan( bloom.y ) || std::isnan( bloom.z ) || std::isinf( bloom.x ) || std::isinf( bloom.y ) ||
+                std::isinf( bloom.z ) )
+                bloom = { 0, 0, 0 };
+            bloom = bloom * gsmoothstep( (T)0, (T)p.bloomThreshold, luminance( bloom ) );
+            outF.store< T >( x, y, { color.x, color.y, color.z, (T)0 } );
+            outB.store< T >( x, y, { bloom.x, bloom.y, bloom.z, (T)0 } );
+        }
+    } );
+}
+
 }  // namespace orc
 
 // ============================================================================================
@@ -1479,6 +1663,32 @@ int orc_calculate_exposure( orc_stream* o, uint32_t frameIndex, const rgdn_frame
     int r = run_stage_t( o->s, RGDN_STAGE_LUMINANCE_HISTOGRAM, 0, frameIndex & 1, p, nthreads );
     r |= run_stage_t( o->s, RGDN_STAGE_LUMINANCE_AVG, 0, frameIndex & 1, p, nthreads );
     return r;
+}
+
+// ImageComposition::PrepareForRaster + Finalize: CmCheckerboard + CmPrepareFinal
+int orc_prepare_final( orc_stream* o, uint32_t frameIndex, const rgdn_final_params* p, int nthreads )
+{
+    if( !o || !p ) return RGDN_WRONG_INSTANCE;
+    if( o->s.mode == orc::M_F64 ) orc::prepare_final< double >( o->s, frameIndex & 1, *p, nthreads );
+    else orc::prepare_final< float >( o->s, frameIndex & 1, *p, nthreads );
+    return RGDN_SUCCESS;
+}
+
+// the LPM constants (saturation[3], contrast, toneScaleBias[2], lumaT[3], rcpLumaT[3],
+// crosstalk[3]) and one filtered colour, for the known-answer tests
+void orc_lpm_setup( const float* saturation3, const float* crosstalk3, float* out16 )
+{
+    const orc::Lpm< float > L = orc::lpm_setup< float >( saturation3, crosstalk3 );
+    const float v[ 16 ] = { L.saturation[ 0 ], L.saturation[ 1 ], L.saturation[ 2 ], L.contrast, L.tsb[ 0 ], L.tsb[ 1 ],
+                            L.lumaT[ 0 ], L.lumaT[ 1 ], L.lumaT[ 2 ], L.rcpLumaT[ 0 ], L.rcpLumaT[ 1 ], L.rcpLumaT[ 2 ],
+                            L.crosstalk[ 0 ], L.crosstalk[ 1 ], L.crosstalk[ 2 ], 0.0f };
+    memcpy( out16, v, sizeof( v ) );
+}
+void orc_lpm_filter( const float* saturation3, const float* crosstalk3, float* rgb )
+{
+    const orc::Lpm< float > L = orc::lpm_setup< float >( saturation3, crosstalk3 );
+    const orc::V3< float >  c = orc::lpm_filter< float >( { rgb[ 0 ], rgb[ 1 ], rgb[ 2 ] }, L );
+    rgb[ 0 ] = c.x; rgb[ 1 ] = c.y; rgb[ 2 ] = c.z;
 }
 
 // Exposure.h:33-51, evaluated on the host in FP32

@@ -32,6 +32,7 @@ FB_NAMES = [
     "INDIR_ACCUM", "INDIR_PING", "INDIR_PONG", "ATROUS_FILTERED_VARIANCE", "DIS_PING_GRADIENT",
     "DIS_PONG_GRADIENT", "DIS_GRADIENT_HISTORY", "GRADIENT_PREV_PIX",
     "DIFF_COLOR_HISTORY_VARIANCE", "DIFF_PING_VARIANCE", "DIFF_PONG_VARIANCE",
+    "SCREEN_EMIS_RT", "SCATTERING", "FINAL", "BLOOM_INPUT",
 ]
 FB = {n: i for i, n in enumerate(FB_NAMES)}
 FB_COUNT = len(FB_NAMES)
@@ -46,6 +47,34 @@ STAGE_ANTI_FIREFLY, STAGE_VARIANCE_ESTIMATION, STAGE_ATROUS = 3, 4, 5
 STAGE_LUMINANCE_HISTOGRAM, STAGE_LUMINANCE_AVG = 6, 7
 
 FLAG_PLAIN, FLAG_SKIP_GRADIENTS, FLAG_EXACT_MATH, FLAG_TMA_STAGING = 0x1, 0x2, 0x4, 0x8
+
+
+class FinalParams(C.Structure):
+    """rgdn_final_params: ImageComposition's tonemapping, bloom and emission parameters."""
+    _fields_ = [
+        ("luminanceWhitePoint", C.c_float), ("emissionMaxScreenColor", C.c_float),
+        ("bloomEmissionMultiplier", C.c_float), ("bloomThreshold", C.c_float),
+        ("saturation", C.c_float * 3), ("crosstalk", C.c_float * 3),
+        ("lightmapScreenCoverage", C.c_float), ("flags", C.c_uint32),
+    ]
+
+    @staticmethod
+    def defaults() -> "FinalParams":
+        """The reference's defaults (DrawFrameInfo.h: tonemapping, bloom, textures params)."""
+        p = FinalParams()
+        p.luminanceWhitePoint, p.emissionMaxScreenColor = 10.0, 1.5
+        p.bloomEmissionMultiplier, p.bloomThreshold = 16.0, 4.0
+        p.saturation[:] = (0.0, 0.0, 0.0)
+        p.crosstalk[:] = (1.0, 1.0, 1.0)
+        return p
+
+    def copy(self) -> "FinalParams":
+        c = FinalParams()
+        C.pointer(c)[0] = self
+        return c
+
+
+FINAL_APPLY_SCATTERING = 0x1
 
 
 class FrameParams(C.Structure):
@@ -144,6 +173,7 @@ SIGNATURES = [
     ("rgdn_stream_download", _I, [_VP, _U32, _U32, _VP, _SZ, _VP]),
     ("rgdn_denoise", _I, [_VP, _U32, _PFP, _VP]),
     ("rgdn_calculate_exposure", _I, [_VP, _U32, _PFP, _VP]),
+    ("rgdn_prepare_final", _I, [_VP, _U32, C.POINTER(FinalParams), _VP]),
     ("rgdn_denoise_stage", _I, [_VP, _U32, _U32, _U32, _PFP, _VP]),
     ("rgdn_stream_tonemapping_device", _I, [_VP, C.POINTER(_VP)]),
     ("rgdn_get_tonemapping", _I, [_VP, C.POINTER(_U32), C.POINTER(C.c_float), C.POINTER(C.c_float), _VP]),
@@ -182,7 +212,7 @@ KERNEL_NAMES.update({100: "atrous_fast", 101: "atrous_fast_hist", 102: "temporal
                      103: "anti_firefly_fast", 104: "variance_fast", 106: "atrous_exact_hist",
                      107: "atrous_exact", 108: "temporal_exact_geom", 109: "variance_exact_geom",
                      110: "temporal_fast_gp", 111: "temporal_exact_geom_gp", 112: "atrous_tma",
-                     113: "atrous_tma_hist"})
+                     113: "atrous_tma_hist", 114: "prepare_final"})
 
 _lib = None
 

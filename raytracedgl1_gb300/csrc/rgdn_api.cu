@@ -146,6 +146,10 @@ FbDesc fb_desc( uint32_t fb, uint32_t storage )
         case RGDN_FB_DIFF_COLOR_HISTORY_VARIANCE:
         case RGDN_FB_DIFF_PING_VARIANCE:
         case RGDN_FB_DIFF_PONG_VARIANCE: return { varpl, false, false };
+        case RGDN_FB_SCREEN_EMIS_RT: return { RGDN_FORMAT_B10G11R11_UFLOAT, false, false };
+        case RGDN_FB_SCATTERING: return { RGDN_FORMAT_RGBA16_SFLOAT, false, false };
+        case RGDN_FB_FINAL:
+        case RGDN_FB_BLOOM_INPUT: return { pre, false, false };
         default: return { RGDN_FORMAT_NONE, false, false };
     }
 }
@@ -557,6 +561,72 @@ rgdn_status run_exposure( rgdn_stream* s, uint32_t fi, const rgdn_frame_params* 
     return launch( s, a, RGDN_STAGE_LUMINANCE_AVG, 0, cs );
 }
 
+// The Y row of the RGB -> XYZ matrix of the Rec.709 primaries with the D65 white (Lindbloom's
+// construction: primaries' xyz columns scaled so that RGB (1, 1, 1) maps to the white's XYZ
+// with Y = 1), in double precision.
+static void rec709_luma( double y[ 3 ] )
+{
+    const double px[ 3 ] = { 0.64, 0.30, 0.15 }, py[ 3 ] = { 0.33, 0.60, 0.06 };
+    const double wx = 0.3127, wy = 0.3290;
+    double       m[ 3 ][ 3 ];
+    for( int c = 0; c < 3; c++ )
+    {
+        m[ 0 ][ c ] = px[ c ];
+        m[ 1 ][ c ] = py[ c ];
+        m[ 2 ][ c ] = 1.0 - px[ c ] - py[ c ];
+    }
+    const double w[ 3 ] = { wx / wy, 1.0, ( 1.0 - wx - wy ) / wy };
+    const double det = m[ 0 ][ 0 ] * ( m[ 1 ][ 1 ] * m[ 2 ][ 2 ] - m[ 1 ][ 2 ] * m[ 2 ][ 1 ] ) -
+                       m[ 0 ][ 1 ] * ( m[ 1 ][ 0 ] * m[ 2 ][ 2 ] - m[ 1 ][ 2 ] * m[ 2 ][ 0 ] ) +
+                       m[ 0 ][ 2 ] * ( m[ 1 ][ 0 ] * m[ 2 ][ 1 ] - m[ 1 ][ 1 ] * m[ 2 ][ 0 ] );
+    // s = m^-1 w by Cramer's rule: column c of m replaced by w
+    for( int c = 0; c < 3; c++ )
+    {
+        double a[ 3 ][ 3 ];
+        for( int r = 0; r < 3; r++ )
+            for( int k = 0; k < 3; k++ ) a[ r ][ k ] = k == c ? w[ r ] : m[ r ][ k ];
+        const double dc = a[ 0 ][ 0 ] * ( a[ 1 ][ 1 ] * a[ 2 ][ 2 ] - a[ 1 ][ 2 ] * a[ 2 ][ 1 ] ) -
+                          a[ 0 ][ 1 ] * ( a[ 1 ][ 0 ] * a[ 2 ][ 2 ] - a[ 1 ][ 2 ] * a[ 2 ][ 0 ] ) +
+                          a[ 0 ][ 2 ] * ( a[ 1 ][ 0 ] * a[ 2 ][ 1 ] - a[ 1 ][ 1 ] * a[ 2 ][ 0 ] );
+        y[ c ] = m[ 1 ][ c ] * ( dc / det );
+    }
+}
+
+// LpmSetupCustom.inl:40-70 for the 709 -> 709 arguments ImageComposition::SetupLpmParams
+// passes, in FP32 in the setup's order; the luma coefficients are the Rec.709 Y row normalised
+// to a unit sum
+void lpm_setup_709( const float saturation[ 3 ], const float crosstalk[ 3 ], LpmConsts& o )
+{
+    const float hdrMax = 256.0f, exposure = 8.0f, shoulderContrast = 1.0f;
+    const float contrast = 0.1f + 1.0f;
+    for( int k = 0; k < 3; k++ ) o.saturation[ k ] = saturation[ k ] + contrast;
+    o.contrast         = contrast;
+    const float midIn  = hdrMax * 0.18f * exp2f( -exposure );
+    const float midOut = 0.18f;
+    const float cs     = contrast * shoulderContrast;
+    const float z0 = -powf( midIn, contrast );
+    const float z1 = powf( hdrMax, cs ) * powf( midIn, contrast );
+    const float z2 = powf( hdrMax, contrast ) * powf( midIn, cs ) * midOut;
+    const float z3 = powf( hdrMax, cs ) * midOut;
+    const float z4 = powf( midIn, cs ) * midOut;
+    o.toneScaleBias[ 0 ] = -( ( z0 + ( midOut * ( z1 - z2 ) ) * ( 1.0f / ( z3 - z4 ) ) ) * ( 1.0f / z4 ) );
+    const float w0 = powf( hdrMax, cs ) * powf( midIn, contrast );
+    const float w1 = powf( hdrMax, contrast ) * powf( midIn, cs ) * midOut;
+    const float w2 = powf( hdrMax, cs ) * midOut;
+    const float w3 = powf( midIn, cs ) * midOut;
+    o.toneScaleBias[ 1 ] = ( w0 - w1 ) * ( 1.0f / ( w2 - w3 ) );
+    double y[ 3 ];
+    rec709_luma( y );
+    float l[ 3 ] = { (float)y[ 0 ], (float)y[ 1 ], (float)y[ 2 ] };
+    const float rs = 1.0f / ( l[ 0 ] + l[ 1 ] + l[ 2 ] );
+    for( int k = 0; k < 3; k++ )
+    {
+        o.lumaT[ k ]     = l[ k ] * rs;
+        o.rcpLumaT[ k ]  = 1.0f / o.lumaT[ k ];
+        o.crosstalk[ k ] = crosstalk[ k ];
+    }
+}
+
 }  // namespace rgdn
 
 // ==========================================================================================
@@ -801,7 +871,8 @@ rgdn_status rgdn_stream_get_framebuffer( rgdn_stream* s, uint32_t fb, uint32_t f
 rgdn_status rgdn_stream_bind_framebuffer( rgdn_stream* s, uint32_t fb, uint32_t frameIndex, void* devicePtr )
 {
     if( !valid_stream( s ) ) return RGDN_WRONG_INSTANCE;
-    if( fb > RGDN_FB_GRADIENT_RESHADED || frameIndex > 1 || ( (uintptr_t)devicePtr & 15u ) ) return RGDN_WRONG_FUNCTION_ARGUMENT;
+    const bool producerPlane = fb <= RGDN_FB_GRADIENT_RESHADED || fb == RGDN_FB_SCREEN_EMIS_RT || fb == RGDN_FB_SCATTERING;
+    if( !producerPlane || frameIndex > 1 || ( (uintptr_t)devicePtr & 15u ) ) return RGDN_WRONG_FUNCTION_ARGUMENT;
     PlaneSlot& p    = s->planes[ fb ];
     const int  slot = p.prev ? (int)frameIndex : 0;
     p.ptr[ slot ]   = devicePtr ? (uint8_t*)devicePtr : p.own[ slot ];
@@ -838,6 +909,61 @@ rgdn_status rgdn_denoise( rgdn_stream* s, uint32_t frameIndex, const rgdn_frame_
     if( r != RGDN_SUCCESS ) return r;
     cudaSetDevice( s->ctx->device );
     return run_denoise( s, frameIndex, p, (cudaStream_t)cs );
+}
+
+rgdn_status rgdn_prepare_final( rgdn_stream* s, uint32_t frameIndex, const rgdn_final_params* p, rgdn_cuda_stream cs )
+{
+    if( !valid_stream( s ) ) return RGDN_WRONG_INSTANCE;
+    if( !p || frameIndex > 1 ) return RGDN_WRONG_FUNCTION_ARGUMENT;
+    // LpmSetup: crosstalk in (0, 1] (one channel 1); finite tone parameters
+    for( int k = 0; k < 3; k++ )
+        if( !( p->crosstalk[ k ] > 0.0f && p->crosstalk[ k ] <= 1.0f ) || !std::isfinite( p->saturation[ k ] ) ) return RGDN_WRONG_FUNCTION_ARGUMENT;
+    if( !( p->luminanceWhitePoint > 0.0f ) || !std::isfinite( p->emissionMaxScreenColor ) || !std::isfinite( p->bloomEmissionMultiplier ) ||
+        !( p->bloomThreshold >= 0.0f ) )
+        return RGDN_WRONG_FUNCTION_ARGUMENT;
+    cudaSetDevice( s->ctx->device );
+    FinalArgs f        = {};
+    f.W                = (int)s->W;
+    f.H                = (int)s->H;
+    f.rw               = (float)s->W;
+    f.lightmapCoverage = p->lightmapScreenCoverage;
+    f.whitePoint       = p->luminanceWhitePoint;
+    f.emisMax          = p->emissionMaxScreenColor;
+    f.bloomEvOffset    = p->bloomEmissionMultiplier;
+    f.bloomThreshold   = p->bloomThreshold;
+    f.flags            = p->flags;
+    lpm_setup_709( p->saturation, p->crosstalk, f.lpm );
+    f.preFinal   = plane_ptr( s, RGDN_FB_PRE_FINAL, frameIndex );
+    f.screenEmis = (const uint32_t*)plane_ptr( s, RGDN_FB_SCREEN_EMIS_RT, frameIndex );
+    f.scattering = (const ushort4*)plane_ptr( s, RGDN_FB_SCATTERING, frameIndex );
+    f.throughput = (const ushort4*)plane_ptr( s, RGDN_FB_THROUGHPUT, frameIndex );
+    f.tm         = s->tm;
+    f.finalOut   = plane_ptr_mut( s, RGDN_FB_FINAL, frameIndex );
+    f.bloomOut   = plane_ptr_mut( s, RGDN_FB_BLOOM_INPUT, frameIndex );
+    cudaStream_t st = (cudaStream_t)cs;
+    cudaEvent_t  ea = nullptr, eb = nullptr;
+    if( s->timing )
+    {
+        ea = take_event( s );
+        eb = take_event( s );
+        if( !ea || !eb ) return RGDN_DEVICE_ERROR;
+        cudaEventRecord( ea, st );
+    }
+    cudaError_t e;
+    switch( s->storage )
+    {
+        case RGDN_STORAGE_REF: e = launch_final_ref( f, st ); break;
+        case RGDN_STORAGE_FP32: e = launch_final_f32( f, st ); break;
+        case RGDN_STORAGE_FP16: e = launch_final_f16( f, st ); break;
+        default: e = launch_final_bf16( f, st ); break;
+    }
+    s->ctx->launches.fetch_add( 1, std::memory_order_relaxed );
+    if( s->timing )
+    {
+        cudaEventRecord( eb, st );
+        s->pending.push_back( { KF_PREPARE_FINAL, 0, ea, eb } );
+    }
+    return cuda_status( e );
 }
 
 rgdn_status rgdn_calculate_exposure( rgdn_stream* s, uint32_t frameIndex, const rgdn_frame_params* p, rgdn_cuda_stream cs )

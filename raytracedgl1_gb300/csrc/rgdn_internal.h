@@ -122,6 +122,40 @@ struct alignas( 16 ) FrameArgs
     const float* decay10;
 };
 
+// AMD LPM constants of the 709 -> 709 configuration without shoulder tuning (the ones
+// LpmFilter reads with LPM_CONFIG_709_709): saturation powers, contrast, tone scale / bias,
+// luma coefficients and their reciprocals, crosstalk.
+struct LpmConsts
+{
+    float saturation[ 3 ], contrast, toneScaleBias[ 2 ], lumaT[ 3 ], rcpLumaT[ 3 ], crosstalk[ 3 ];
+};
+// LpmSetup (LpmSetupCustom.inl) for ImageComposition::SetupLpmParams' arguments
+// (ImageComposition.cpp:384-394): 709 primaries and D65 in and out, no soft gap, hdrMax 256,
+// exposure 8 stops, contrast 0.1, shoulder contrast 1.
+void lpm_setup_709( const float saturation[ 3 ], const float crosstalk[ 3 ], LpmConsts& out );
+
+// Arguments of the exposure / tonemapping kernel (rgdn_prepare_final), regular pixel layout.
+struct FinalArgs
+{
+    int             W, H;
+    float           rw;               // render width as float
+    float           lightmapCoverage;
+    float           whitePoint, emisMax, bloomEvOffset, bloomThreshold;
+    uint32_t        flags;            // RGDN_FINAL_*
+    LpmConsts       lpm;
+    const void*     preFinal;         // PRE_FINAL (the storage mode's format)
+    const uint32_t* screenEmis;       // B10G11R11
+    const ushort4*  scattering;       // rgba16f
+    const ushort4*  throughput;       // rgba16f, checkerboard layout
+    const Tonemapping* tm;
+    void*           finalOut;         // PRE_FINAL's format
+    void*           bloomOut;
+};
+cudaError_t launch_final_ref( const FinalArgs& f, cudaStream_t s );
+cudaError_t launch_final_f32( const FinalArgs& f, cudaStream_t s );
+cudaError_t launch_final_f16( const FinalArgs& f, cudaStream_t s );
+cudaError_t launch_final_bf16( const FinalArgs& f, cudaStream_t s );
+
 // Kernels of the default (fused, fast-math) path, beyond the per-stage rgdn_stage ids.
 enum FusedKernel : int
 {
@@ -138,6 +172,7 @@ enum FusedKernel : int
     KF_TEMPORAL_EXACT_GEOM_GP = 111,
     KF_ATROUS_TMA          = 112,  // TMA-staged a-trous iteration (timing label)
     KF_ATROUS_TMA_HIST     = 113,  // TMA-staged last iteration + fused histogram (timing label)
+    KF_PREPARE_FINAL       = 114,  // exposure, tonemapping and bloom input (timing label)
 };
 
 // Launches one stage for one frame. Returns the CUDA error of the launch.

@@ -235,6 +235,11 @@ template<> struct Sto< MODE_REF >
     __device__ static float ld1( const void* p, size_t i ) { return h2f( static_cast< const uint16_t* >( p )[ i ] ); }
     __device__ static void  st1( void* p, size_t i, float v ) { static_cast< uint16_t* >( p )[ i ] = f32_to_f16( v ); }
     __device__ static void  stpre( void* p, size_t i, float3 v ) { static_cast< uint32_t* >( p )[ i ] = encode_b10g11r11( v.x, v.y, v.z ); }
+    __device__ static float3 ldpre( const void* p, size_t i )
+    {
+        const rgdn::f3 c = decode_b10g11r11( static_cast< const uint32_t* >( p )[ i ] );
+        return make_float3( c.x, c.y, c.z );
+    }
 };
 
 template<> struct Sto< MODE_F32 >
@@ -251,6 +256,7 @@ template<> struct Sto< MODE_F32 >
     __device__ static float  ld1( const void* p, size_t i ) { return static_cast< const float* >( p )[ i ]; }
     __device__ static void   st1( void* p, size_t i, float v ) { static_cast< float* >( p )[ i ] = v; }
     __device__ static void   stpre( void* p, size_t i, float3 v ) { static_cast< float4* >( p )[ i ] = make_float4( v.x, v.y, v.z, 0.0f ); }
+    __device__ static float3 ldpre( const void* p, size_t i ) { float4 v = static_cast< const float4* >( p )[ i ]; return f3( v.x, v.y, v.z ); }
 };
 
 // 16-bit colour / history with FP32 moments, FP32 variance planes, FP32 prefiltered variance
@@ -285,6 +291,11 @@ template< bool BF > struct Sto16
     __device__ static void stpre( void* p, size_t i, float3 v )
     {
         static_cast< ushort4* >( p )[ i ] = make_ushort4( f32_to_f16( v.x ), f32_to_f16( v.y ), f32_to_f16( v.z ), 0 );
+    }
+    __device__ static float3 ldpre( const void* p, size_t i )
+    {
+        const ushort4 h = static_cast< const ushort4* >( p )[ i ];
+        return f3( h2f( h.x ), h2f( h.y ), h2f( h.z ) );
     }
 };
 template<> struct Sto< MODE_F16 > : Sto16< false > {};
@@ -2457,6 +2468,121 @@ template< int M > __global__ void __launch_bounds__( 256 ) kb_luminance_avg( con
     pdl_launch_dependents();
 }
 
+
+// ==========================================================================================
+// CmCheckerboard.comp:27-69 and CmPrepareFinal.comp:57-187: the checkerboard resolve of split
+// pixels, volumetric scattering, exposure, tonemapping and the bloom input, per regular pixel.
+// IEEE arithmetic in the shaders' order (a per-pixel pass, off the denoiser's hot loop).
+// ==========================================================================================
+// resolveCheckerboard (CmCheckerboard.comp:27-39): the cross mean of the four neighbours,
+// without a horizontal neighbour across a checkerboard half's edge, mixed half-half with the
+// centre; neighbours outside the image read zero
+template< class Ld > __device__ __forceinline__ float3 cb_resolve( const FinalArgs& f, Ld ld, const int x, const int y, const int cbx, const float3 c )
+{
+    const int    sep = f.W / 2;
+    const float  lf  = ( cbx == 0 || cbx == sep ) ? 0.0f : 1.0f;
+    const float  rf  = ( cbx == sep || cbx == f.W ) ? 0.0f : 1.0f;
+    const float3 l = ld( x - 1, y ), r = ld( x + 1, y ), d = ld( x, y + 1 ), u = ld( x, y - 1 );
+    const float3 cross = f3( 0.25f * l.x * lf + 0.25f * r.x * rf + 0.25f * d.x + 0.25f * u.x,
+                             0.25f * l.y * lf + 0.25f * r.y * rf + 0.25f * d.y + 0.25f * u.y,
+                             0.25f * l.z * lf + 0.25f * r.z * rf + 0.25f * d.z + 0.25f * u.z );
+    return vmix( c, cross, 0.5f );
+}
+
+// uncharted2Tonemap (CmPrepareFinal.comp:69-87)
+__device__ __forceinline__ float u2_op( float x )
+{
+    const float A = 0.15f, B = 0.50f, C = 0.10f, D = 0.20f, E = 0.02f, F = 0.30f;
+    return ( ( x * ( A * x + C * B ) + D * E ) / ( x * ( A * x + B ) + D * F ) ) - E / F;
+}
+
+// LpmMap (ffx_lpm.h, AMD FidelityFX LPM 1.0) with LPM_CONFIG_709_709 and no shoulder: the ratio
+// of the colour to its maximum, raised to the saturation powers; luma tone-mapped by
+// luma^c / (luma^c * scale + bias); the ratio scaled to hit that luma without clipping; then
+// the missing luma of clipped channels moved to the others through the crosstalk capacities,
+// twice. The operation order is the shader's.
+__device__ __forceinline__ float3 lpm_709( float3 c, const LpmConsts& k )
+{
+    const float rcpMax = 1.0f / fmaxf( c.x, fmaxf( c.y, c.z ) );
+    float       rR = c.x * rcpMax, rG = c.y * rcpMax, rB = c.z * rcpMax;
+    rR = powf( rR, k.saturation[ 0 ] );
+    rG = powf( rG, k.saturation[ 1 ] );
+    rB = powf( rB, k.saturation[ 2 ] );
+    float luma = c.y * k.lumaT[ 1 ] + ( c.x * k.lumaT[ 0 ] + ( c.z * k.lumaT[ 2 ] ) );
+    luma       = powf( luma, k.contrast );
+    luma       = luma * ( 1.0f / ( luma * k.toneScaleBias[ 0 ] + k.toneScaleBias[ 1 ] ) );
+    const float lumaRatio  = rR * k.lumaT[ 0 ] + rG * k.lumaT[ 1 ] + rB * k.lumaT[ 2 ];
+    const float ratioScale = gsat( luma * ( 1.0f / lumaRatio ) );
+    float       cR = gsat( rR * ratioScale ), cG = gsat( rG * ratioScale ), cB = gsat( rB * ratioScale );
+    const float capR = -k.crosstalk[ 0 ] * cR + k.crosstalk[ 0 ];
+    const float capG = -k.crosstalk[ 1 ] * cG + k.crosstalk[ 1 ];
+    const float capB = -k.crosstalk[ 2 ] * cB + k.crosstalk[ 2 ];
+    float lumaAdd = gsat( ( -cB ) * k.lumaT[ 2 ] + ( ( -cR ) * k.lumaT[ 0 ] + ( ( -cG ) * k.lumaT[ 1 ] + luma ) ) );
+    const float t = lumaAdd * ( 1.0f / ( capG * k.lumaT[ 1 ] + ( capR * k.lumaT[ 0 ] + ( capB * k.lumaT[ 2 ] ) ) ) );
+    cR      = gsat( t * capR + cR );
+    cG      = gsat( t * capG + cG );
+    cB      = gsat( t * capB + cB );
+    lumaAdd = gsat( ( -cB ) * k.lumaT[ 2 ] + ( ( -cR ) * k.lumaT[ 0 ] + ( ( -cG ) * k.lumaT[ 1 ] + luma ) ) );
+    cR      = gsat( lumaAdd * k.rcpLumaT[ 0 ] + cR );
+    cG      = gsat( lumaAdd * k.rcpLumaT[ 1 ] + cG );
+    cB      = gsat( lumaAdd * k.rcpLumaT[ 2 ] + cB );
+    return f3( cR, cG, cB );
+}
+
+template< int M > __global__ void __launch_bounds__( 256 ) k_prepare_final( const FinalArgs f )
+{
+    using S     = Sto< M >;
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y * blockDim.y + threadIdx.y;
+    pdl_launch_dependents();
+    pdl_wait();
+    if( x >= f.W || y >= f.H ) return;
+    const int i   = y * f.W + x;
+    // getCheckerboardPix (ShaderCommonGLSLFunc.h:321-329)
+    const int sep = f.W / 2;
+    const int odd = ( x + y % 2 ) % 2;
+    const int cbx = odd * sep + x / 2;
+    float3    hdr = S::ldpre( f.preFinal, (size_t)i );
+    float3    emis = decode_b10g11r11_bits( f.screenEmis[ i ] );
+    // needResolveCheckerboard: wasSplit(Throughput.a) (ShaderCommonGLSLFunc.h:435-444)
+    if( h2f( f.throughput[ y * f.W + cbx ].w ) > 0.5f )
+    {
+        auto inImg = [ & ]( int qx, int qy ) { return qx >= 0 && qy >= 0 && qx < f.W && qy < f.H; };
+        hdr  = cb_resolve( f, [ & ]( int qx, int qy ) { return inImg( qx, qy ) ? S::ldpre( f.preFinal, (size_t)( qy * f.W + qx ) ) : f3( 0, 0, 0 ); }, x, y, cbx, hdr );
+        emis = cb_resolve( f, [ & ]( int qx, int qy ) { return inImg( qx, qy ) ? decode_b10g11r11_bits( f.screenEmis[ qy * f.W + qx ] ) : f3( 0, 0, 0 ); }, x, y, cbx, emis );
+    }
+    if( f.flags & RGDN_FINAL_APPLY_SCATTERING )
+    {
+        const ushort4 v = f.scattering[ i ];
+        const float   a = h2f( v.w );
+        hdr             = f3( hdr.x * a + h2f( v.x ), hdr.y * a + h2f( v.y ), hdr.z * a + h2f( v.z ) );
+    }
+    // getAutoEV100, ev100ToLuminousExposure (Exposure.h:14-51)
+    const float ev       = log2f( fmaxf( 0.0f, f.tm->avgLuminance ) * 100.0f / 12.5f );
+    const float maxLum   = 1.2f * exp2f( ev );
+    const float exposure = maxLum > 0.0f ? 1.0f / maxLum : 0.0f;
+    // finalizeColor (CmPrepareFinal.comp:101-113)
+    float3 color;
+    if( (float)x < f.lightmapCoverage * f.rw )
+    {
+        const float w = u2_op( f.whitePoint );
+        color         = f3( u2_op( 2.0f * hdr.x ) / w, u2_op( 2.0f * hdr.y ) / w, u2_op( 2.0f * hdr.z ) / w );
+    }
+    else
+    {
+        const float3 c = f3( hdr.x * exposure + emis.x * f.emisMax, hdr.y * exposure + emis.y * f.emisMax, hdr.z * exposure + emis.z * f.emisMax );
+        color          = lpm_709( c, f.lpm );
+    }
+    // getBloomInput (CmPrepareFinal.comp:116-133)
+    const float  el    = exp2f( ev + f.bloomEvOffset - 3.0f );
+    float3       bloom = f3( ( hdr.x + emis.x * el ) * exposure, ( hdr.y + emis.y * el ) * exposure, ( hdr.z + emis.z * el ) * exposure );
+    if( isnan( bloom.x ) || isnan( bloom.y ) || isnan( bloom.z ) || isinf( bloom.x ) || isinf( bloom.y ) || isinf( bloom.z ) )
+        bloom = f3( 0, 0, 0 );
+    bloom = mul( bloom, gsmoothstep( 0.0f, f.bloomThreshold, luminance( bloom ) ) );
+    S::stpre( f.finalOut, (size_t)i, color );
+    S::stpre( f.bloomOut, (size_t)i, bloom );
+}
+
 }  // namespace dev
 
 
@@ -2495,6 +2621,12 @@ template< int M > cudaError_t launch_stage_t( const FrameArgs& a, int stage, int
         case KF_ATROUS_EXACT_HIST: e = launch_pdl( dev::k_atrous< M, false, true, true >, grid, blk, 0, s, a, iter ); break;
         default: return cudaErrorInvalidValue;
     }
+    return e != cudaSuccess ? e : cudaGetLastError();
+}
+
+template< int M > cudaError_t launch_final_t( const FinalArgs& f, cudaStream_t s )
+{
+    const cudaError_t e = launch_pdl( dev::k_prepare_final< M >, dim3( ( f.W + 31 ) / 32, ( f.H + 7 ) / 8 ), dim3( 32, 8 ), 0, s, f );
     return e != cudaSuccess ? e : cudaGetLastError();
 }
 

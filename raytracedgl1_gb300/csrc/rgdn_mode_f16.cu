@@ -3,6 +3,10 @@
 
 namespace rgdn
 {
+cudaError_t launch_final_f16( const FinalArgs& f, cudaStream_t s )
+{
+    return launch_final_t< MODE_F16 >( f, s );
+}
 cudaError_t launch_stage_f16( const FrameArgs& a, int stage, int iter, cudaStream_t s )
 {
     return launch_stage_t< MODE_F16 >( a, stage, iter, s );

@@ -3,6 +3,10 @@
 
 namespace rgdn
 {
+cudaError_t launch_final_f32( const FinalArgs& f, cudaStream_t s )
+{
+    return launch_final_t< MODE_F32 >( f, s );
+}
 cudaError_t launch_stage_f32( const FrameArgs& a, int stage, int iter, cudaStream_t s )
 {
     return launch_stage_t< MODE_F32 >( a, stage, iter, s );

@@ -3,6 +3,10 @@
 
 namespace rgdn
 {
+cudaError_t launch_final_ref( const FinalArgs& f, cudaStream_t s )
+{
+    return launch_final_t< MODE_REF >( f, s );
+}
 cudaError_t launch_stage_ref( const FrameArgs& a, int stage, int iter, cudaStream_t s )
 {
     return launch_stage_t< MODE_REF >( a, stage, iter, s );

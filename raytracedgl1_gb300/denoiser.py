@@ -260,6 +260,21 @@ class Denoiser:
                 "rgdn_denoise")
 
 
+class ImageComposition:
+    """ImageComposition::PrepareForRaster + Finalize (Source/ImageComposition.cpp:87-155), without
+    rasterised geometry in between: CmCheckerboard.comp + CmPrepareFinal.comp into FINAL and
+    BLOOM_INPUT, from PRE_FINAL, SCREEN_EMIS_RT, SCATTERING and the adapted average luminance."""
+
+    def __init__(self, stream: Stream):
+        self.stream = stream
+
+    def Finalize(self, frameIndex: int, params: N.FinalParams = None, cuda_stream=None) -> None:
+        s = self.stream
+        p = params if params is not None else N.FinalParams.defaults()
+        N.check(s.lib.rgdn_prepare_final(s.handle, frameIndex, C.byref(p), _stream_handle(cuda_stream)),
+                "rgdn_prepare_final")
+
+
 class Tonemapping:
     """Tonemapping::CalculateExposure(cmd, frameIndex, uniform) — Source/Tonemapping.cpp:59-165."""
 

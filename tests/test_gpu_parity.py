@@ -12,7 +12,7 @@ import numpy as np
 import pytest
 
 from raytracedgl1_gb300 import _native as N
-from raytracedgl1_gb300.denoiser import Denoiser, Stream, Tonemapping
+from raytracedgl1_gb300.denoiser import Denoiser, ImageComposition, Stream, Tonemapping
 from raytracedgl1_gb300.scene import Scene
 
 import oracle
@@ -403,6 +403,79 @@ def test_error_paths(ctx):
     s.close()
     lib = N.load()
     assert lib.rgdn_denoise(None, 0, p, None) == N.WRONG_INSTANCE
+
+
+def _final_inputs(W, H, mode, seed):
+    """Identical PRE_FINAL, SCREEN_EMIS_RT, SCATTERING and THROUGHPUT bytes for a GPU stream and
+    the oracle: HDR colours up to 40 (some above the LPM mid level, some clipped), emission,
+    volumetric scattering, and about a fifth of the primary rays split."""
+    rng = np.random.default_rng(seed)
+    o = oracle.OracleStream(W, H, mode)
+    hdr = rng.uniform(0.0, 1.0, (H, W, 3)) ** 3 * 40.0
+    pre = o.plane("PRE_FINAL", 0)
+    if mode == N.STORAGE_REF:
+        pre[...] = np.array([[oracle.encode_b10g11r11(*hdr[y, x]) for x in range(W)] for y in range(H)], np.uint32)
+    elif mode == N.STORAGE_FP32:
+        pre[..., :3] = hdr.astype(np.float32)
+    else:
+        pre[..., :3] = hdr.astype(np.float16).view(np.uint16)
+    em = rng.uniform(0.0, 2.0, (H, W, 3)) * (rng.uniform(size=(H, W, 1)) < 0.3)
+    o.plane("SCREEN_EMIS_RT", 0)[...] = np.array([[oracle.encode_b10g11r11(*em[y, x]) for x in range(W)] for y in range(H)], np.uint32)
+    sc = np.concatenate([rng.uniform(0.0, 0.3, (H, W, 3)), rng.uniform(0.5, 1.0, (H, W, 1))], axis=2)
+    o.plane("SCATTERING", 0)[...] = sc.astype(np.float16).view(np.uint16)
+    thr = np.zeros((H, W, 4), np.float16)
+    thr[..., :3] = 1.0
+    thr[..., 3] = (rng.uniform(size=(H, W)) < 0.2).astype(np.float16)
+    o.plane("THROUGHPUT", 0)[...] = thr.view(np.uint16)
+    return o
+
+
+@pytest.mark.parametrize("mode_name,mode", MODES)
+@pytest.mark.parametrize("size", [(64, 36), (50, 23)])
+def test_prepare_final_parity(ctx, mode_name, mode, size):
+    """rgdn_prepare_final (CmCheckerboard + CmPrepareFinal: split-pixel resolve, scattering,
+    uncharted2 / exposure + emission through LPM, bloom input) against the oracle on the same
+    inputs: classic shading on the left 30 %, non-default LPM saturation and crosstalk, with
+    and without scattering."""
+    W, H = size
+    o = _final_inputs(W, H, mode, seed=W + H)
+    s = Stream(ctx, W, H, mode)
+    for name in ("PRE_FINAL", "SCREEN_EMIS_RT", "SCATTERING", "THROUGHPUT"):
+        s.upload(name, 0, o.plane(name, 0))
+    for avg in (0.35, 2.5):
+        s.set_tonemapping(None, avg)
+        o.set_tonemapping(None, avg)
+        for flags in (0, N.FINAL_APPLY_SCATTERING):
+            p = N.FinalParams.defaults()
+            p.lightmapScreenCoverage = 0.3
+            p.saturation[:] = (-0.1, 0.0, 0.15)
+            p.crosstalk[:] = (1.0, 0.5, 0.25)
+            p.flags = flags
+            ImageComposition(s).Finalize(0, p)
+            o.prepare_final(0, p)
+            for name in ("FINAL", "BLOOM_INPUT"):
+                img = s.image(name, 0)
+                g = F.decode(s.download(name, 0), img.format)
+                c = F.decode(o.plane(name, 0), img.format)
+                err = F.texel_rel_err(g, c, atol=1e-6)
+                assert err.max() <= TOL[img.format], f"{name} avg {avg} flags {flags}: max rel err {err.max():.3e}"
+                if img.format != F.F_RGBA32F:
+                    # quantised outputs: ulp-level differences of pow / exp2 move a code rarely
+                    assert np.mean(err > 0) <= 0.02, f"{name}: {np.mean(err > 0):.2%} of texels differ"
+    s.close()
+
+
+def test_prepare_final_rejects_bad_params(ctx):
+    s = Stream(ctx, 64, 36)
+    p = N.FinalParams.defaults()
+    p.crosstalk[1] = 0.0
+    with pytest.raises(N.RgdnError) as e:
+        ImageComposition(s).Finalize(0, p)
+    assert e.value.status == N.WRONG_FUNCTION_ARGUMENT
+    p = N.FinalParams.defaults()
+    with pytest.raises(N.RgdnError):
+        ImageComposition(s).Finalize(2, p)
+    s.close()
 
 
 def test_device_errors_clear_on_a_clean_run(ctx):

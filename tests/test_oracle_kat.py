@@ -206,3 +206,79 @@ def test_fp64_and_fp32_oracles_agree():
     a = o32.plane("PRE_FINAL", fi)[..., :3].astype(np.float64)
     b = o64.plane("PRE_FINAL", fi)[..., :3]
     assert F.psnr(a, b) > 70.0
+
+
+# --- exposure application and tonemapping (CmCheckerboard + CmPrepareFinal) ----------------
+def test_lpm_setup_709():
+    """LpmSetup for ImageComposition's arguments: luma weights are the Rec.709 Y row (D65),
+    contrast 1 + 0.1, and the luma curve l^c / (l^c s + b) maps the mid level 0.18 to 0.18
+    and hdrMax 256 to 1 (the two conditions its scale and bias are solved from)."""
+    k = oracle.lpm_setup()
+    assert k["luma"] == pytest.approx([0.2126390, 0.7151687, 0.0721923], abs=2e-6)
+    assert sum(k["luma"]) == pytest.approx(1.0, abs=1e-6)
+    assert k["contrast"] == pytest.approx(1.1) and k["saturation"] == pytest.approx([1.1] * 3)
+    s, b = k["tone_scale_bias"]
+    tone = lambda l: l ** 1.1 / (l ** 1.1 * s + b)
+    assert tone(0.18) == pytest.approx(0.18, rel=1e-5)
+    assert tone(256.0) == pytest.approx(1.0, rel=1e-5)
+    assert oracle.lpm_setup(saturation=(-0.1, 0.0, 0.2))["saturation"] == pytest.approx([1.0, 1.1, 1.3])
+
+
+def test_lpm_filter_grey_and_luma():
+    """A grey stays grey on the luma curve; an in-gamut colour keeps its luma on the curve
+    (the filter is luma-preserving); every output lies in [0, 1]."""
+    k = oracle.lpm_setup()
+    s, b = k["tone_scale_bias"]
+    tone = lambda l: l ** 1.1 / (l ** 1.1 * s + b)
+    for v in (0.003, 0.05, 0.18, 1.0, 7.5, 100.0):
+        out = oracle.lpm_filter((v, v, v))
+        assert out == pytest.approx((tone(v),) * 3, rel=2e-5)
+    rgb = (0.3, 0.2, 0.1)
+    out = oracle.lpm_filter(rgb)
+    luma = lambda c: sum(w * x for w, x in zip(k["luma"], c))
+    assert luma(out) == pytest.approx(tone(luma(rgb)), rel=1e-4)
+    for c in ((50.0, 0.1, 0.0), (0.0, 0.0, 3.0), (1e4, 1e4, 0.5)):
+        out = oracle.lpm_filter(c)
+        assert all(0.0 <= x <= 1.0 for x in out)
+
+
+def test_prepare_final_closed_form():
+    """FINAL and BLOOM_INPUT of an fp32 stream against the formulas of CmPrepareFinal:
+    uncharted2 left of the classic-shading edge, LPM of the exposed colour right of it, and
+    the bloom input; one pixel with a split primary ray takes the cross-resolved colour."""
+    W, H = 8, 4
+    o = oracle.OracleStream(W, H, oracle.MODE_F32)
+    rng = np.random.default_rng(3)
+    hdr = rng.uniform(0.0, 6.0, (H, W, 4)).astype(np.float32)
+    hdr[..., 3] = 0
+    o.load("PRE_FINAL", 0, hdr)
+    emis = np.array([[oracle.encode_b10g11r11(0.25, 0.5, 0.0)] * W] * H, np.uint32)
+    o.load("SCREEN_EMIS_RT", 0, emis)
+    thr = np.zeros((H, W, 4), np.uint16)
+    thr[2, 1, 3] = 0x3C00   # throughput.a = 1 at checkerboard pixel (1, 2): regular pixel (2, 2)
+    o.load("THROUGHPUT", 0, thr)
+    avg = 0.4
+    o.set_tonemapping(np.zeros(256), avg)
+    p = N.FinalParams.defaults()
+    p.lightmapScreenCoverage = 0.25   # classic shading for x < 2
+    o.prepare_final(0, p)
+    fin = o.plane("FINAL", 0)[..., :3].astype(np.float64)
+    bloom = o.plane("BLOOM_INPUT", 0)[..., :3].astype(np.float64)
+    exposure = 1.0 / (1.2 * avg * 100.0 / 12.5)
+    e = np.array(oracle.decode_b10g11r11(int(emis[0, 0])))
+    op = lambda x: ((x * (0.15 * x + 0.05) + 0.004) / (x * (0.15 * x + 0.5) + 0.06)) - 0.02 / 0.3
+    for y in range(H):
+        for x in range(W):
+            c = hdr[y, x, :3].astype(np.float64)
+            if (x, y) == (2, 2):
+                cross = 0.25 * (hdr[2, 1, :3] + hdr[2, 3, :3] + hdr[3, 2, :3] + hdr[1, 2, :3])
+                c = 0.5 * c + 0.5 * cross
+            if x < 2:
+                want = op(2.0 * c) / op(10.0)
+            else:
+                want = np.array(oracle.lpm_filter(tuple(c * exposure + e * 1.5)))
+            assert fin[y, x] == pytest.approx(want, rel=2e-5, abs=1e-6), (x, y)
+            b = (c + e * 2.0 ** (math.log2(avg * 8.0) + 16.0 - 3.0)) * exposure
+            l = 0.2125 * b[0] + 0.7154 * b[1] + 0.0721 * b[2]
+            t = min(max(l / 4.0, 0.0), 1.0)
+            assert bloom[y, x] == pytest.approx(b * t * t * (3 - 2 * t), rel=2e-5, abs=1e-6), (x, y)
