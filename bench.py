@@ -671,6 +671,30 @@ def run_ours(args, dist: Dist):
     final = {"kernel": "prepare_final", "what": "CmCheckerboard + CmPrepareFinal (LPM 709, bloom input, scattering on)",
              "us_per_frame": round(fin_us, 2), "mpix_s": round(W * H / fin_us, 1),
              "alg_bytes": fin_alg, "gbs": round(fin_alg / (fin_us / 1e6) / 1e9, 1)}
+
+    # --- bloom pyramid (rgdn_bloom: 8 down, 8 up, apply; 17 launches), after the composition --
+    from raytracedgl1_gb300.denoiser import Bloom
+    bloom = Bloom(st)
+    with torch.cuda.stream(cs):
+        for k in range(3):
+            bloom.Apply(k & 1, 1.0, cs)
+        be = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+        be[0].record(cs)
+        for k in range(nfin):
+            bloom.Apply(k & 1, 1.0, cs)
+        be[1].record(cs)
+    cs.synchronize()
+    bl_us = 1e3 * be[0].elapsed_time(be[1]) / nfin
+    mips = [((W + 1) >> k) * ((H + 1) >> k) for k in range(9)]
+    mips[0] = W * H
+    # each level read once and written once on the way down, read (coarser level and own
+    # texel) and written on the way up, then BLOOM_RESULT read and FINAL read and written
+    bl_texels = sum(mips[k] + mips[k + 1] for k in range(8)) + sum(mips[k + 1] + 2 * mips[k] for k in range(1, 8)) \
+        + mips[1] + W * H + 3 * W * H
+    bl_alg = bl_texels * pre_b
+    bloom_t = {"kernel": "bloom", "what": "8 downsample (13-tap, Karis on the first) + 8 tent upsample + apply, 17 launches",
+               "us_per_frame": round(bl_us, 2), "mpix_s": round(W * H / bl_us, 1),
+               "alg_bytes": bl_alg, "gbs": round(bl_alg / (bl_us / 1e6) / 1e9, 1)}
     top = kern[0]
     peak, peak_kind = load_peaks()
 
@@ -794,6 +818,7 @@ def run_ours(args, dist: Dist):
         "kernels": [{k: (round(v, 2) if isinstance(v, float) else v) for k, v in d.items()} for d in kern],
         "kernel_sum_us_per_step": round(kernel_total_us, 2),
         "prepare_final": final,
+        "bloom": bloom_t,
         "path_alg_gbs": round(sum(d["alg_bytes"] * d["launches"] for d in kern) / args.steps /
                               (total_ms_max / args.steps / 1e3) / 1e9, 1),
         "e2e": {"value": round(e2e_value, 2), "unit": "Mpix/s", "h2d_bytes_per_step": int(h2d),

@@ -142,6 +142,16 @@ typedef enum rgdn_framebuf
     RGDN_FB_SCATTERING,               /* RGBA16_SFLOAT: volumetric in-scattering (rgb), transmittance (a) */
     RGDN_FB_FINAL,                    /* the exposed, tonemapped image (PRE_FINAL's format) */
     RGDN_FB_BLOOM_INPUT,              /* bloom input (PRE_FINAL's format) */
+    /* bloom (rgdn_bloom): mip k is ((W+1) >> k) x ((H+1) >> k), at least 1x1; PRE_FINAL's format */
+    RGDN_FB_BLOOM_MIP1,
+    RGDN_FB_BLOOM_MIP2,
+    RGDN_FB_BLOOM_MIP3,
+    RGDN_FB_BLOOM_MIP4,
+    RGDN_FB_BLOOM_MIP5,
+    RGDN_FB_BLOOM_MIP6,
+    RGDN_FB_BLOOM_MIP7,
+    RGDN_FB_BLOOM_MIP8,
+    RGDN_FB_BLOOM_RESULT,             /* W x H */
     RGDN_FB_COUNT
 } rgdn_framebuf;
 
@@ -295,6 +305,19 @@ typedef struct rgdn_final_params
 } rgdn_final_params;
 #define RGDN_FINAL_APPLY_SCATTERING 0x1u /* hdr = hdr * scattering.a + scattering.rgb */
 rgdn_status rgdn_prepare_final( rgdn_stream* stream, uint32_t frameIndex, const rgdn_final_params* params, rgdn_cuda_stream cudaStream );
+
+/* ---- bloom -------------------------------------------------------------------------
+ * Bloom::Prepare + Apply (Bloom.cpp:94-240): 8 downsampling steps of BLOOM_INPUT
+ * (CmBloomDownsample.comp: 13-tap, partial Karis average on the first) into BLOOM_MIP1..8,
+ * 8 upsampling steps (CmBloomUpsample.comp: 3x3 tent, adding each mip's own downsample) into
+ * BLOOM_MIP7..1 and BLOOM_RESULT, then FINAL += intensity * BLOOM_RESULT (CmBloomApply.comp,
+ * at render size, without the lens-dirt texture term). Bilinear reads are clamp-to-edge in
+ * FP32. Call after rgdn_prepare_final. */
+typedef struct rgdn_bloom_params
+{
+    float bloomIntensity;   /* reference default 1 */
+} rgdn_bloom_params;
+rgdn_status rgdn_bloom( rgdn_stream* stream, uint32_t frameIndex, const rgdn_bloom_params* params, rgdn_cuda_stream cudaStream );
 
 /* One stage alone (the plain path / per-stage checking). `iteration` selects the
  * a-trous or gradient a-trous iteration. */

@@ -51,6 +51,7 @@ def load():
         "orc_calculate_exposure": (C.c_int, [C.c_void_p, C.c_uint32, P(FrameParams), C.c_int]),
         "orc_exposure_from_avg": (C.c_float, [C.c_float]),
         "orc_prepare_final": (C.c_int, [C.c_void_p, C.c_uint32, P(FinalParams), C.c_int]),
+        "orc_bloom": (C.c_int, [C.c_void_p, C.c_uint32, C.c_float]),
         "orc_lpm_setup": (None, [P(C.c_float), P(C.c_float), P(C.c_float)]),
         "orc_lpm_filter": (None, [P(C.c_float), P(C.c_float), P(C.c_float)]),
         "orc_get_tonemapping": (None, [C.c_void_p, P(C.c_uint32), P(C.c_float), P(C.c_double)]),
@@ -139,6 +140,12 @@ class OracleStream:
         r = self.lib.orc_prepare_final(self.h, frame_index, C.byref(params), nthreads or nthreads_default())
         if r != 0:
             raise RuntimeError(f"orc_prepare_final failed: {r}")
+
+    def bloom(self, frame_index: int, intensity: float = 1.0) -> None:
+        """The bloom pyramid of BLOOM_INPUT added to FINAL (rgdn_bloom)."""
+        r = self.lib.orc_bloom(self.h, frame_index, C.c_float(intensity))
+        if r != 0:
+            raise RuntimeError(f"orc_bloom failed: {r}")
 
     def tonemapping(self):
         hist = (C.c_uint32 * 256)()

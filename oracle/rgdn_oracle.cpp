@@ -371,6 +371,7 @@ struct FbInfo
     uint32_t fmt;
     bool     prev;
     bool     third;    // 1/3 resolution
+    int      shift = 0;   // Framebuffers.cpp:669-692 FORCE_SIZE_BLOOM: (size + 1) / 2^shift, at least 1
 };
 
 // The oracle's own format table (the reference's is GenerateShaderCommon.py:802-887).
@@ -430,7 +431,11 @@ FbInfo fb_info( uint32_t fb, uint32_t mode )
         case RGDN_FB_SCREEN_EMIS_RT: return { F_B10G11R11, false, false };
         case RGDN_FB_SCATTERING: return { F_RGBA16F, false, false };
         case RGDN_FB_FINAL:
-        case RGDN_FB_BLOOM_INPUT: return { pre, false, false };
+        case RGDN_FB_BLOOM_INPUT:
+        case RGDN_FB_BLOOM_RESULT: return { pre, false, false };
+        case RGDN_FB_BLOOM_MIP1: case RGDN_FB_BLOOM_MIP2: case RGDN_FB_BLOOM_MIP3: case RGDN_FB_BLOOM_MIP4:
+        case RGDN_FB_BLOOM_MIP5: case RGDN_FB_BLOOM_MIP6: case RGDN_FB_BLOOM_MIP7: case RGDN_FB_BLOOM_MIP8:
+            return { pre, false, false, (int)( fb - RGDN_FB_BLOOM_MIP1 ) + 1 };
         default: return { F_NONE, false, false };
     }
 }
@@ -543,7 +548,9 @@ struct Stream
             for( int s = 0; s < 2; s++ )
             {
                 if( fi.fmt == F_NONE || ( s == 1 && !fi.prev ) ) { planes[ fb ][ s ] = Plane(); continue; }
-                planes[ fb ][ s ].init( fi.third ? GW : W, fi.third ? GH : H, fi.fmt );
+                int pw = fi.third ? GW : W, ph = fi.third ? GH : H;
+                if( fi.shift ) pw = std::max( 1, ( W + 1 ) >> fi.shift ), ph = std::max( 1, ( H + 1 ) >> fi.shift );
+                planes[ fb ][ s ].init( pw, ph, fi.fmt );
             }
         }
         memset( hist, 0, sizeof( hist ) );
@@ -1562,6 +1569,87 @@ template< class T > void prepare_final( Stream& s, uint32_t fi, const rgdn_final
     } );
 }
 
+// --------------------------------------------------------------------------------------------
+//  Bloom: CmBloomDownsample.comp:15-136, CmBloomUpsample.comp:15-104, CmBloomApply.comp:45-76
+//  (without the lens-dirt texture term). textureLod through the framebuffers' bilinear
+//  clamp-to-edge sampler (Framebuffers.cpp:187-209), evaluated exactly in T.
+// --------------------------------------------------------------------------------------------
+template< class T > V3< T > bilinear( const Plane& img, T u, T v )
+{
+    const T   x  = u * (T)img.w - K( 0.5 ), y = v * (T)img.h - K( 0.5 );
+    const T   fx = o_floor( x ), fy = o_floor( y );
+    const T   a  = x - fx, b = y - fy;
+    const int ix = (int)fx, iy = (int)fy;
+    const int x0 = std::min( std::max( ix, 0 ), img.w - 1 ), x1 = std::min( std::max( ix + 1, 0 ), img.w - 1 );
+    const int y0 = std::min( std::max( iy, 0 ), img.h - 1 ), y1 = std::min( std::max( iy + 1, 0 ), img.h - 1 );
+    const V3< T > t00 = xyz( img.fetch< T >( x0, y0 ) ), t10 = xyz( img.fetch< T >( x1, y0 ) );
+    const V3< T > t01 = xyz( img.fetch< T >( x0, y1 ) ), t11 = xyz( img.fetch< T >( x1, y1 ) );
+    return vmix( vmix( t00, t10, a ), vmix( t01, t11, a ), b );
+}
+
+template< class T > void bloom( Stream& s, uint32_t fi, float intensity )
+{
+    const int W = s.W, H = s.H;
+    auto      mip = [ & ]( int k ) -> Plane& { return s.cur( k == 0 ? RGDN_FB_BLOOM_INPUT : RGDN_FB_BLOOM_MIP1 + ( k - 1 ), fi ); };
+    const T   q = K( 0.25 ), h2 = K( 0.5 ), e8 = K( 0.125 );
+    for( int k = 0; k < 8; k++ )
+    {
+        const Plane& src = mip( k );
+        Plane&       dst = mip( k + 1 );
+        const T      idx = (T)( 1 << ( k + 1 ) ) / (T)W, idy = (T)( 1 << ( k + 1 ) ) / (T)H;
+        const T      isx = (T)( 1 << k ) / (T)W, isy = (T)( 1 << k ) / (T)H;
+        for( int y = 0; y < dst.h; y++ )
+            for( int x = 0; x < dst.w; x++ )
+            {
+                const T u = ( (T)x + h2 ) * idx, v = ( (T)y + h2 ) * idy;
+                if( u > (T)1 || v > (T)1 ) continue;
+                auto tap = [ & ]( T ox, T oy ) { return bilinear< T >( src, u + ox * isx, v + oy * isy ); };
+                const V3< T > t0 = tap( -2, -2 ), t1 = tap( 0, -2 ), t2 = tap( 2, -2 ), t3 = tap( -1, -1 ), t4 = tap( 1, -1 );
+                const V3< T > t5 = tap( -2, 0 ), t6 = tap( 0, 0 ), t7 = tap( 2, 0 ), t8 = tap( -1, 1 ), t9 = tap( 1, 1 );
+                const V3< T > t10 = tap( -2, 2 ), t11 = tap( 0, 2 ), t12 = tap( 2, 2 );
+                const V3< T > b0 = ( t3 + t4 + t8 + t9 ) * q, b1 = ( t0 + t1 + t5 + t6 ) * q, b2 = ( t1 + t2 + t6 + t7 ) * q;
+                const V3< T > b3 = ( t5 + t6 + t10 + t11 ) * q, b4 = ( t6 + t7 + t11 + t12 ) * q;
+                V3< T >       r;
+                if( k == 0 )
+                {
+                    auto kw = []( V3< T > bx ) { return (T)1 / ( (T)1 + luminance( bx ) ); };   // getKarisWeight
+                    r       = b0 * ( h2 * kw( b0 ) ) + b1 * ( e8 * kw( b1 ) ) + b2 * ( e8 * kw( b2 ) ) + b3 * ( e8 * kw( b3 ) ) + b4 * ( e8 * kw( b4 ) );
+                }
+                else r = b0 * h2 + b1 * e8 + b2 * e8 + b3 * e8 + b4 * e8;
+                dst.store< T >( x, y, { r.x, r.y, r.z, (T)0 } );
+            }
+    }
+    const T wt[ 3 ][ 3 ] = { { K( 0.0625 ), K( 0.125 ), K( 0.0625 ) }, { K( 0.125 ), K( 0.25 ), K( 0.125 ) }, { K( 0.0625 ), K( 0.125 ), K( 0.0625 ) } };
+    for( int k = 7; k >= 0; k-- )
+    {
+        const Plane& src = mip( k + 1 );
+        Plane&       dst = k == 0 ? s.cur( RGDN_FB_BLOOM_RESULT, fi ) : mip( k );
+        const T      isx = (T)( 1 << ( k + 1 ) ) / (T)W, isy = (T)( 1 << ( k + 1 ) ) / (T)H;
+        const T      iux = (T)( 1 << k ) / (T)W, iuy = (T)( 1 << k ) / (T)H;
+        for( int y = 0; y < dst.h; y++ )
+            for( int x = 0; x < dst.w; x++ )
+            {
+                const T u = ( (T)x + h2 ) * iux + h2 * isx, v = ( (T)y + h2 ) * iuy + h2 * isy;
+                if( u > (T)1 || v > (T)1 ) continue;
+                V3< T > r = { 0, 0, 0 };
+                for( int oy = -1; oy <= 1; oy++ )
+                    for( int ox = -1; ox <= 1; ox++ ) r = r + bilinear< T >( src, u + (T)ox * isx, v + (T)oy * isy ) * wt[ oy + 1 ][ ox + 1 ];
+                if( k > 0 ) r = r + xyz( dst.fetch< T >( x, y ) );
+                dst.store< T >( x, y, { r.x, r.y, r.z, (T)0 } );
+            }
+    }
+    const Plane& res = s.cur( RGDN_FB_BLOOM_RESULT, fi );
+    Plane&       fin = s.cur( RGDN_FB_FINAL, fi );
+    for( int y = 0; y < H; y++ )
+        for( int x = 0; x < W; x++ )
+        {
+            const T u = ( (T)x + h2 ) * ( (T)1 / (T)W ), v = ( (T)y + h2 ) * ( (T)1 / (T)H );
+            if( u > (T)1 || v > (T)1 ) continue;
+            const V3< T > c = xyz( fin.fetch< T >( x, y ) ) + bilinear< T >( res, u, v ) * (T)intensity;
+            fin.store< T >( x, y, { c.x, c.y, c.z, (T)0 } );
+        }
+}
+
 }  // namespace orc
 
 // ============================================================================================
@@ -1671,6 +1759,15 @@ int orc_prepare_final( orc_stream* o, uint32_t frameIndex, const rgdn_final_para
     if( !o || !p ) return RGDN_WRONG_INSTANCE;
     if( o->s.mode == orc::M_F64 ) orc::prepare_final< double >( o->s, frameIndex & 1, *p, nthreads );
     else orc::prepare_final< float >( o->s, frameIndex & 1, *p, nthreads );
+    return RGDN_SUCCESS;
+}
+
+// Bloom::Prepare + Apply
+int orc_bloom( orc_stream* o, uint32_t frameIndex, float intensity )
+{
+    if( !o ) return RGDN_WRONG_INSTANCE;
+    if( o->s.mode == orc::M_F64 ) orc::bloom< double >( o->s, frameIndex & 1, intensity );
+    else orc::bloom< float >( o->s, frameIndex & 1, intensity );
     return RGDN_SUCCESS;
 }
 

@@ -33,6 +33,8 @@ FB_NAMES = [
     "DIS_PONG_GRADIENT", "DIS_GRADIENT_HISTORY", "GRADIENT_PREV_PIX",
     "DIFF_COLOR_HISTORY_VARIANCE", "DIFF_PING_VARIANCE", "DIFF_PONG_VARIANCE",
     "SCREEN_EMIS_RT", "SCATTERING", "FINAL", "BLOOM_INPUT",
+    "BLOOM_MIP1", "BLOOM_MIP2", "BLOOM_MIP3", "BLOOM_MIP4", "BLOOM_MIP5", "BLOOM_MIP6", "BLOOM_MIP7",
+    "BLOOM_MIP8", "BLOOM_RESULT",
 ]
 FB = {n: i for i, n in enumerate(FB_NAMES)}
 FB_COUNT = len(FB_NAMES)
@@ -75,6 +77,11 @@ class FinalParams(C.Structure):
 
 
 FINAL_APPLY_SCATTERING = 0x1
+
+
+class BloomParams(C.Structure):
+    """rgdn_bloom_params."""
+    _fields_ = [("bloomIntensity", C.c_float)]
 
 
 class FrameParams(C.Structure):
@@ -174,6 +181,7 @@ SIGNATURES = [
     ("rgdn_denoise", _I, [_VP, _U32, _PFP, _VP]),
     ("rgdn_calculate_exposure", _I, [_VP, _U32, _PFP, _VP]),
     ("rgdn_prepare_final", _I, [_VP, _U32, C.POINTER(FinalParams), _VP]),
+    ("rgdn_bloom", _I, [_VP, _U32, C.POINTER(BloomParams), _VP]),
     ("rgdn_denoise_stage", _I, [_VP, _U32, _U32, _U32, _PFP, _VP]),
     ("rgdn_stream_tonemapping_device", _I, [_VP, C.POINTER(_VP)]),
     ("rgdn_get_tonemapping", _I, [_VP, C.POINTER(_U32), C.POINTER(C.c_float), C.POINTER(C.c_float), _VP]),
@@ -212,7 +220,7 @@ KERNEL_NAMES.update({100: "atrous_fast", 101: "atrous_fast_hist", 102: "temporal
                      103: "anti_firefly_fast", 104: "variance_fast", 106: "atrous_exact_hist",
                      107: "atrous_exact", 108: "temporal_exact_geom", 109: "variance_exact_geom",
                      110: "temporal_fast_gp", 111: "temporal_exact_geom_gp", 112: "atrous_tma",
-                     113: "atrous_tma_hist", 114: "prepare_final"})
+                     113: "atrous_tma_hist", 114: "prepare_final", 115: "bloom"})
 
 _lib = None
 

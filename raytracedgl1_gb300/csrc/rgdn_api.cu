@@ -74,6 +74,7 @@ struct FbDesc
     uint32_t format;
     bool     prev;
     bool     third;
+    int      shift = 0;   // bloom mips: ((W+1) >> shift) x ((H+1) >> shift), at least 1
 };
 
 uint32_t format_bytes( uint32_t f )
@@ -149,7 +150,11 @@ FbDesc fb_desc( uint32_t fb, uint32_t storage )
         case RGDN_FB_SCREEN_EMIS_RT: return { RGDN_FORMAT_B10G11R11_UFLOAT, false, false };
         case RGDN_FB_SCATTERING: return { RGDN_FORMAT_RGBA16_SFLOAT, false, false };
         case RGDN_FB_FINAL:
-        case RGDN_FB_BLOOM_INPUT: return { pre, false, false };
+        case RGDN_FB_BLOOM_INPUT:
+        case RGDN_FB_BLOOM_RESULT: return { pre, false, false };
+        case RGDN_FB_BLOOM_MIP1: case RGDN_FB_BLOOM_MIP2: case RGDN_FB_BLOOM_MIP3: case RGDN_FB_BLOOM_MIP4:
+        case RGDN_FB_BLOOM_MIP5: case RGDN_FB_BLOOM_MIP6: case RGDN_FB_BLOOM_MIP7: case RGDN_FB_BLOOM_MIP8:
+            return { pre, false, false, (int)( fb - RGDN_FB_BLOOM_MIP1 ) + 1 };
         default: return { RGDN_FORMAT_NONE, false, false };
     }
 }
@@ -211,6 +216,7 @@ size_t stream_layout( uint32_t W, uint32_t H, uint32_t storage, PlaneSlot* plane
         if( planes ) planes[ fb ] = PlaneSlot();
         if( d.format == RGDN_FORMAT_NONE ) continue;
         uint32_t w = d.third ? GW : W, h = d.third ? GH : H;
+        if( d.shift ) w = std::max( 1u, ( W + 1 ) >> d.shift ), h = std::max( 1u, ( H + 1 ) >> d.shift );
         size_t   sz = (size_t)w * h * texel;
         for( int s = 0; s < ( d.prev ? 2 : 1 ); s++ )
         {
@@ -909,6 +915,50 @@ rgdn_status rgdn_denoise( rgdn_stream* s, uint32_t frameIndex, const rgdn_frame_
     if( r != RGDN_SUCCESS ) return r;
     cudaSetDevice( s->ctx->device );
     return run_denoise( s, frameIndex, p, (cudaStream_t)cs );
+}
+
+rgdn_status rgdn_bloom( rgdn_stream* s, uint32_t frameIndex, const rgdn_bloom_params* p, rgdn_cuda_stream cs )
+{
+    if( !valid_stream( s ) ) return RGDN_WRONG_INSTANCE;
+    if( !p || frameIndex > 1 || !std::isfinite( p->bloomIntensity ) ) return RGDN_WRONG_FUNCTION_ARGUMENT;
+    cudaSetDevice( s->ctx->device );
+    BloomArgs b = {};
+    const uint32_t fbs[ 11 ] = { RGDN_FB_BLOOM_INPUT, RGDN_FB_BLOOM_MIP1, RGDN_FB_BLOOM_MIP2, RGDN_FB_BLOOM_MIP3, RGDN_FB_BLOOM_MIP4,
+                                 RGDN_FB_BLOOM_MIP5,  RGDN_FB_BLOOM_MIP6, RGDN_FB_BLOOM_MIP7, RGDN_FB_BLOOM_MIP8, RGDN_FB_BLOOM_RESULT,
+                                 RGDN_FB_FINAL };
+    for( int k = 0; k < 11; k++ )
+    {
+        b.planes[ k ] = plane_ptr_mut( s, fbs[ k ], frameIndex );
+        b.w[ k ]      = (int)s->planes[ fbs[ k ] ].w;
+        b.h[ k ]      = (int)s->planes[ fbs[ k ] ].h;
+    }
+    b.W         = (int)s->W;
+    b.H         = (int)s->H;
+    b.intensity = p->bloomIntensity;
+    cudaStream_t st = (cudaStream_t)cs;
+    cudaEvent_t  ea = nullptr, eb = nullptr;
+    if( s->timing )
+    {
+        ea = take_event( s );
+        eb = take_event( s );
+        if( !ea || !eb ) return RGDN_DEVICE_ERROR;
+        cudaEventRecord( ea, st );
+    }
+    cudaError_t e;
+    switch( s->storage )
+    {
+        case RGDN_STORAGE_REF: e = launch_bloom_ref( b, st ); break;
+        case RGDN_STORAGE_FP32: e = launch_bloom_f32( b, st ); break;
+        case RGDN_STORAGE_FP16: e = launch_bloom_f16( b, st ); break;
+        default: e = launch_bloom_bf16( b, st ); break;
+    }
+    s->ctx->launches.fetch_add( 17, std::memory_order_relaxed );
+    if( s->timing )
+    {
+        cudaEventRecord( eb, st );
+        s->pending.push_back( { KF_BLOOM, 0, ea, eb } );
+    }
+    return cuda_status( e );
 }
 
 rgdn_status rgdn_prepare_final( rgdn_stream* s, uint32_t frameIndex, const rgdn_final_params* p, rgdn_cuda_stream cs )

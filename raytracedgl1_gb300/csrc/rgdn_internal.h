@@ -151,6 +151,18 @@ struct FinalArgs
     void*           finalOut;         // PRE_FINAL's format
     void*           bloomOut;
 };
+// The bloom pyramid's planes: [0] BLOOM_INPUT, [1..8] BLOOM_MIP1..8, [9] BLOOM_RESULT, [10] FINAL
+struct BloomArgs
+{
+    void* planes[ 11 ];
+    int   w[ 11 ], h[ 11 ];
+    int   W, H;
+    float intensity;
+};
+cudaError_t launch_bloom_ref( const BloomArgs& b, cudaStream_t s );
+cudaError_t launch_bloom_f32( const BloomArgs& b, cudaStream_t s );
+cudaError_t launch_bloom_f16( const BloomArgs& b, cudaStream_t s );
+cudaError_t launch_bloom_bf16( const BloomArgs& b, cudaStream_t s );
 cudaError_t launch_final_ref( const FinalArgs& f, cudaStream_t s );
 cudaError_t launch_final_f32( const FinalArgs& f, cudaStream_t s );
 cudaError_t launch_final_f16( const FinalArgs& f, cudaStream_t s );
@@ -173,6 +185,7 @@ enum FusedKernel : int
     KF_ATROUS_TMA          = 112,  // TMA-staged a-trous iteration (timing label)
     KF_ATROUS_TMA_HIST     = 113,  // TMA-staged last iteration + fused histogram (timing label)
     KF_PREPARE_FINAL       = 114,  // exposure, tonemapping and bloom input (timing label)
+    KF_BLOOM               = 115,  // the bloom pyramid and its application (timing label)
 };
 
 // Launches one stage for one frame. Returns the CUDA error of the launch.

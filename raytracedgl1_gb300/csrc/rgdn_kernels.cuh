@@ -2583,6 +2583,98 @@ template< int M > __global__ void __launch_bounds__( 256 ) k_prepare_final( cons
     S::stpre( f.bloomOut, (size_t)i, bloom );
 }
 
+
+// ==========================================================================================
+// CmBloomDownsample.comp, CmBloomUpsample.comp, CmBloomApply.comp: the bloom pyramid over
+// images in PRE_FINAL's format. textureLod with the framebuffers' bilinear clamp-to-edge
+// sampler is evaluated in FP32 (texel centres at +0.5, weights from the fractional position).
+// ==========================================================================================
+template< int M > __device__ __forceinline__ float3 bloom_bilinear( const void* img, const int w, const int h, const float u, const float v )
+{
+    using S         = Sto< M >;
+    const float x   = u * (float)w - 0.5f, y = v * (float)h - 0.5f;
+    const float fx  = floorf( x ), fy = floorf( y );
+    const float a   = x - fx, b = y - fy;
+    const int   ix  = (int)fx, iy = (int)fy;
+    const int   x0  = min( max( ix, 0 ), w - 1 ), x1 = min( max( ix + 1, 0 ), w - 1 );
+    const int   y0  = min( max( iy, 0 ), h - 1 ), y1 = min( max( iy + 1, 0 ), h - 1 );
+    const float3 t00 = S::ldpre( img, (size_t)( y0 * w + x0 ) ), t10 = S::ldpre( img, (size_t)( y0 * w + x1 ) );
+    const float3 t01 = S::ldpre( img, (size_t)( y1 * w + x0 ) ), t11 = S::ldpre( img, (size_t)( y1 * w + x1 ) );
+    return vmix( vmix( t00, t10, a ), vmix( t01, t11, a ), b );
+}
+__device__ __forceinline__ float3 sum4( float3 a, float3 b, float3 c, float3 d ) { return add( add( add( a, b ), c ), d ); }
+
+// step k: src is BLOOM_INPUT (k = 0) or mip k, dst mip k + 1 (CmBloomDownsample.comp:15-136)
+template< int M >
+__global__ void __launch_bounds__( 256 ) k_bloom_down( const void* src, int sw, int sh, void* dst, int dw, int dh, int k, int W, int H )
+{
+    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
+    pdl_launch_dependents();
+    pdl_wait();
+    if( x >= dw || y >= dh ) return;
+    const float  idx = (float)( 1 << ( k + 1 ) ) / (float)W, idy = (float)( 1 << ( k + 1 ) ) / (float)H;
+    const float  u   = ( (float)x + 0.5f ) * idx, v = ( (float)y + 0.5f ) * idy;
+    if( u > 1.0f || v > 1.0f ) return;
+    const float  isx = (float)( 1 << k ) / (float)W, isy = (float)( 1 << k ) / (float)H;
+    auto tap = [ & ]( float ox, float oy ) { return bloom_bilinear< M >( src, sw, sh, u + ox * isx, v + oy * isy ); };
+    const float3 t0 = tap( -2, -2 ), t1 = tap( 0, -2 ), t2 = tap( 2, -2 );
+    const float3 t3 = tap( -1, -1 ), t4 = tap( 1, -1 );
+    const float3 t5 = tap( -2, 0 ), t6 = tap( 0, 0 ), t7 = tap( 2, 0 );
+    const float3 t8 = tap( -1, 1 ), t9 = tap( 1, 1 );
+    const float3 t10 = tap( -2, 2 ), t11 = tap( 0, 2 ), t12 = tap( 2, 2 );
+    const float3 b0 = mul( sum4( t3, t4, t8, t9 ), 0.25f ), b1 = mul( sum4( t0, t1, t5, t6 ), 0.25f );
+    const float3 b2 = mul( sum4( t1, t2, t6, t7 ), 0.25f ), b3 = mul( sum4( t5, t6, t10, t11 ), 0.25f );
+    const float3 b4 = mul( sum4( t6, t7, t11, t12 ), 0.25f );
+    float3 r;
+    if( k == 0 )
+    {
+        // partial Karis average: each box weighted by 1 / (1 + luminance)
+        auto kw = []( float3 bx ) { return 1.0f / ( 1.0f + luminance( bx ) ); };
+        r = add( add( add( add( mul( b0, 0.5f * kw( b0 ) ), mul( b1, 0.125f * kw( b1 ) ) ), mul( b2, 0.125f * kw( b2 ) ) ), mul( b3, 0.125f * kw( b3 ) ) ),
+                 mul( b4, 0.125f * kw( b4 ) ) );
+    }
+    else r = add( add( add( add( mul( b0, 0.5f ), mul( b1, 0.125f ) ), mul( b2, 0.125f ) ), mul( b3, 0.125f ) ), mul( b4, 0.125f ) );
+    Sto< M >::stpre( dst, (size_t)( y * dw + x ), r );
+}
+
+// step k: src mip k + 1, dst mip k (adding its own texel) or BLOOM_RESULT (k = 0)
+// (CmBloomUpsample.comp:15-104)
+template< int M >
+__global__ void __launch_bounds__( 256 ) k_bloom_up( const void* src, int sw, int sh, void* dst, int dw, int dh, int k, int W, int H )
+{
+    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
+    pdl_launch_dependents();
+    pdl_wait();
+    if( x >= dw || y >= dh ) return;
+    const float isx = (float)( 1 << ( k + 1 ) ) / (float)W, isy = (float)( 1 << ( k + 1 ) ) / (float)H;
+    const float iux = (float)( 1 << k ) / (float)W, iuy = (float)( 1 << k ) / (float)H;
+    const float u   = ( (float)x + 0.5f ) * iux + 0.5f * isx, v = ( (float)y + 0.5f ) * iuy + 0.5f * isy;
+    if( u > 1.0f || v > 1.0f ) return;
+    const float wt[ 3 ][ 3 ] = { { 0.0625f, 0.125f, 0.0625f }, { 0.125f, 0.25f, 0.125f }, { 0.0625f, 0.125f, 0.0625f } };
+    float3      r            = f3( 0, 0, 0 );
+#pragma unroll
+    for( int oy = -1; oy <= 1; oy++ )
+#pragma unroll
+        for( int ox = -1; ox <= 1; ox++ )
+            r = add( r, mul( bloom_bilinear< M >( src, sw, sh, u + (float)ox * isx, v + (float)oy * isy ), wt[ oy + 1 ][ ox + 1 ] ) );
+    if( k > 0 ) r = add( r, Sto< M >::ldpre( dst, (size_t)( y * dw + x ) ) );
+    Sto< M >::stpre( dst, (size_t)( y * dw + x ), r );
+}
+
+// FINAL += intensity * BLOOM_RESULT(uv) (CmBloomApply.comp:45-76, lens dirt not included)
+template< int M > __global__ void __launch_bounds__( 256 ) k_bloom_apply( const void* result, void* finalImg, int W, int H, float intensity )
+{
+    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
+    pdl_launch_dependents();
+    pdl_wait();
+    if( x >= W || y >= H ) return;
+    const float  u = ( (float)x + 0.5f ) * ( 1.0f / (float)W ), v = ( (float)y + 0.5f ) * ( 1.0f / (float)H );
+    if( u > 1.0f || v > 1.0f ) return;
+    const float3 bloom = mul( bloom_bilinear< M >( result, W, H, u, v ), intensity );
+    const size_t i     = (size_t)( y * W + x );
+    Sto< M >::stpre( finalImg, i, add( Sto< M >::ldpre( finalImg, i ), bloom ) );
+}
+
 }  // namespace dev
 
 
@@ -2621,6 +2713,27 @@ template< int M > cudaError_t launch_stage_t( const FrameArgs& a, int stage, int
         case KF_ATROUS_EXACT_HIST: e = launch_pdl( dev::k_atrous< M, false, true, true >, grid, blk, 0, s, a, iter ); break;
         default: return cudaErrorInvalidValue;
     }
+    return e != cudaSuccess ? e : cudaGetLastError();
+}
+
+// the bloom pyramid over planes[0] = BLOOM_INPUT, planes[1..8] = mips, planes[9] = BLOOM_RESULT,
+// planes[10] = FINAL; w/h per plane
+template< int M > cudaError_t launch_bloom_t( const BloomArgs& b, cudaStream_t s )
+{
+    const dim3  blk( 32, 8 );
+    auto        grid = []( int w, int h ) { return dim3( ( w + 31 ) / 32, ( h + 7 ) / 8 ); };
+    cudaError_t e    = cudaSuccess;
+    for( int k = 0; k < 8 && e == cudaSuccess; k++ )
+        e = launch_pdl( dev::k_bloom_down< M >, grid( b.w[ k + 1 ], b.h[ k + 1 ] ), blk, 0, s, (const void*)b.planes[ k ], b.w[ k ], b.h[ k ],
+                        b.planes[ k + 1 ], b.w[ k + 1 ], b.h[ k + 1 ], k, b.W, b.H );
+    for( int k = 7; k >= 0 && e == cudaSuccess; k-- )
+    {
+        const int d = k == 0 ? 9 : k;
+        e           = launch_pdl( dev::k_bloom_up< M >, grid( b.w[ d ], b.h[ d ] ), blk, 0, s, (const void*)b.planes[ k + 1 ], b.w[ k + 1 ],
+                                  b.h[ k + 1 ], b.planes[ d ], b.w[ d ], b.h[ d ], k, b.W, b.H );
+    }
+    if( e == cudaSuccess )
+        e = launch_pdl( dev::k_bloom_apply< M >, grid( b.W, b.H ), blk, 0, s, (const void*)b.planes[ 9 ], b.planes[ 10 ], b.W, b.H, b.intensity );
     return e != cudaSuccess ? e : cudaGetLastError();
 }
 

@@ -3,6 +3,10 @@
 
 namespace rgdn
 {
+cudaError_t launch_bloom_bf16( const BloomArgs& b, cudaStream_t s )
+{
+    return launch_bloom_t< MODE_BF16 >( b, s );
+}
 cudaError_t launch_final_bf16( const FinalArgs& f, cudaStream_t s )
 {
     return launch_final_t< MODE_BF16 >( f, s );

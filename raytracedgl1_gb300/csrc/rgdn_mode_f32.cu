@@ -3,6 +3,10 @@
 
 namespace rgdn
 {
+cudaError_t launch_bloom_f32( const BloomArgs& b, cudaStream_t s )
+{
+    return launch_bloom_t< MODE_F32 >( b, s );
+}
 cudaError_t launch_final_f32( const FinalArgs& f, cudaStream_t s )
 {
     return launch_final_t< MODE_F32 >( f, s );

@@ -3,6 +3,10 @@
 
 namespace rgdn
 {
+cudaError_t launch_bloom_ref( const BloomArgs& b, cudaStream_t s )
+{
+    return launch_bloom_t< MODE_REF >( b, s );
+}
 cudaError_t launch_final_ref( const FinalArgs& f, cudaStream_t s )
 {
     return launch_final_t< MODE_REF >( f, s );

@@ -275,6 +275,19 @@ class ImageComposition:
                 "rgdn_prepare_final")
 
 
+class Bloom:
+    """Bloom::Prepare + Apply (Source/Bloom.cpp:94-240): the 8-level bloom pyramid of BLOOM_INPUT,
+    added to FINAL with the given intensity (without the lens-dirt texture term)."""
+
+    def __init__(self, stream: Stream):
+        self.stream = stream
+
+    def Apply(self, frameIndex: int, bloomIntensity: float = 1.0, cuda_stream=None) -> None:
+        s = self.stream
+        p = N.BloomParams(bloomIntensity)
+        N.check(s.lib.rgdn_bloom(s.handle, frameIndex, C.byref(p), _stream_handle(cuda_stream)), "rgdn_bloom")
+
+
 class Tonemapping:
     """Tonemapping::CalculateExposure(cmd, frameIndex, uniform) — Source/Tonemapping.cpp:59-165."""
 

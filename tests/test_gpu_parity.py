@@ -12,7 +12,7 @@ import numpy as np
 import pytest
 
 from raytracedgl1_gb300 import _native as N
-from raytracedgl1_gb300.denoiser import Denoiser, ImageComposition, Stream, Tonemapping
+from raytracedgl1_gb300.denoiser import Bloom, Denoiser, ImageComposition, Stream, Tonemapping
 from raytracedgl1_gb300.scene import Scene
 
 import oracle
@@ -462,6 +462,54 @@ def test_prepare_final_parity(ctx, mode_name, mode, size):
                 if img.format != F.F_RGBA32F:
                     # quantised outputs: ulp-level differences of pow / exp2 move a code rarely
                     assert np.mean(err > 0) <= 0.02, f"{name}: {np.mean(err > 0):.2%} of texels differ"
+    s.close()
+
+
+def _encode_pre(rgb: np.ndarray, fmt: int) -> np.ndarray:
+    """HDR colours as the bytes of a pre-tonemapping plane of the given storage format."""
+    H, W, _ = rgb.shape
+    if fmt == F.F_B10G11R11:
+        return np.array([[oracle.encode_b10g11r11(*rgb[y, x]) for x in range(W)] for y in range(H)], np.uint32)
+    rgba = np.concatenate([rgb, np.zeros((H, W, 1))], axis=2)
+    if fmt == F.F_RGBA32F:
+        return rgba.astype(np.float32)
+    if fmt == F.F_RGBA16F:
+        return rgba.astype(np.float16).view(np.uint16)
+    assert fmt == F.F_RGBA16BF
+    b = rgba.astype(np.float32).view(np.uint32).astype(np.uint64)
+    return ((b + 0x7FFF + ((b >> 16) & 1)) >> 16).astype(np.uint16)
+
+
+BLOOM_PLANES = ["BLOOM_INPUT"] + [f"BLOOM_MIP{k}" for k in range(1, 9)] + ["BLOOM_RESULT", "FINAL"]
+
+
+@pytest.mark.parametrize("mode_name,mode", MODES)
+@pytest.mark.parametrize("size", [(320, 180), (302, 163)])
+def test_bloom_parity(ctx, mode_name, mode, size):
+    """rgdn_bloom (8 downsample steps with the Karis-weighted first one, 8 tent upsample steps,
+    the apply onto FINAL) against the oracle. Every bloom plane starts from the same random
+    bytes on both sides, so the texels the uv > 1 guards skip must keep them; an odd height
+    gives mips whose sizes do not halve evenly."""
+    W, H = size
+    rng = np.random.default_rng(W * 7 + H)
+    o = oracle.OracleStream(W, H, mode)
+    s = Stream(ctx, W, H, mode)
+    for name in BLOOM_PLANES:
+        img = s.image(name, 0)
+        rgb = rng.uniform(0.0, 1.0, (img.height, img.width, 3)) ** 4 * (24.0 if name == "BLOOM_INPUT" else 2.0)
+        data = _encode_pre(rgb, img.format)
+        o.plane(name, 0)[...] = data
+        s.upload(name, 0, data)
+    Bloom(s).Apply(0, 0.7)
+    o.bloom(0, 0.7)
+    for name in BLOOM_PLANES[1:]:
+        img = s.image(name, 0)
+        g = F.decode(s.download(name, 0), img.format)
+        c = F.decode(o.plane(name, 0), img.format)
+        err = F.texel_rel_err(g, c, atol=1e-6)
+        assert err.max() <= TOL[img.format], f"{name}: max rel err {err.max():.3e}"
+        if img.format == F.F_RGBA32F:
+            assert err.max() <= 1e-5, f"{name}: max rel err {err.max():.3e}"
     s.close()
 
 

@@ -282,3 +282,38 @@ def test_prepare_final_closed_form():
             l = 0.2125 * b[0] + 0.7154 * b[1] + 0.0721 * b[2]
             t = min(max(l / 4.0, 0.0), 1.0)
             assert bloom[y, x] == pytest.approx(b * t * t * (3 - 2 * t), rel=2e-5, abs=1e-6), (x, y)
+
+
+def test_bloom_constant_image():
+    """A constant BLOOM_INPUT c through the pyramid of a 1920x1080 frame.
+
+    - The Karis-weighted first downsample gives c' = c / (1 + lum(c)); the later downsamples
+      keep it, so mip 8 (7x4, only ever written by the downsample) is c'.
+    - Each upsample adds its own level, so mip k tops out at (9 - k) c' and BLOOM_RESULT at
+      8 c'. FINAL gains intensity times BLOOM_RESULT.
+    - The upsample's uv > 1 guard (CmBloomUpsample.comp:88-91) leaves the last column and row
+      of every upsampled level unadded. Through the coarse levels (mip 8 spans 7.5 texels of
+      uv but holds 7) this lowers the right and bottom of the frame, while the upper left
+      (rows < 500, columns < 1280) stays exactly 8 c'."""
+    W, H = 1920, 1080
+    o = oracle.OracleStream(W, H, oracle.MODE_F64)
+    c = np.array([0.5, 1.0, 2.0])
+    o.plane("BLOOM_INPUT", 0)[..., :3] = c
+    o.plane("FINAL", 0)[..., :3] = 0.25
+    o.plane("BLOOM_RESULT", 0)[...] = -1.0
+    o.bloom(0, 0.5)
+    lum = 0.2125 * c[0] + 0.7154 * c[1] + 0.0721 * c[2]
+    cp = c / (1 + lum)
+    mip8 = o.plane("BLOOM_MIP8", 0)[..., :3]
+    assert mip8.shape == (4, 7, 3)
+    assert mip8 == pytest.approx(np.broadcast_to(cp, mip8.shape), rel=1e-12)
+    for k in range(1, 8):
+        m = o.plane(f"BLOOM_MIP{k}", 0)[..., :3] / cp
+        assert m.max() == pytest.approx(9 - k, rel=1e-12) and m.min() == pytest.approx(1.0, rel=1e-12), k
+    res = o.plane("BLOOM_RESULT", 0)
+    assert res[:500, :1280, :3] == pytest.approx(np.broadcast_to(8 * cp, (500, 1280, 3)), rel=1e-12)
+    fin = o.plane("FINAL", 0)[..., :3]
+    assert fin[:500, :1280] == pytest.approx(np.broadcast_to(0.25 + 4 * cp, (500, 1280, 3)), rel=1e-12)
+    assert np.all(res[:, W - 1] == -1.0) and np.all(res[H - 1, :] == -1.0)
+    inner = res[: H - 1, : W - 1, :3] / cp
+    assert inner.min() > 1.0 and inner.max() <= 8.0 * (1 + 1e-12)
