@@ -952,7 +952,7 @@ rgdn_status rgdn_bloom( rgdn_stream* s, uint32_t frameIndex, const rgdn_bloom_pa
         case RGDN_STORAGE_FP16: e = launch_bloom_f16( b, st ); break;
         default: e = launch_bloom_bf16( b, st ); break;
     }
-    s->ctx->launches.fetch_add( 17, std::memory_order_relaxed );
+    s->ctx->launches.fetch_add( BLOOM_LAUNCHES, std::memory_order_relaxed );
     if( s->timing )
     {
         cudaEventRecord( eb, st );

@@ -159,6 +159,11 @@ struct BloomArgs
     int   W, H;
     float intensity;
 };
+// 8 downsample launches, 8 upsample launches, the apply
+constexpr int BLOOM_LAUNCHES = 17;
+// levels of at least this many texels take the wide builds (2x2 quads per thread for the
+// upsample, 4 blocks per SM for the downsample)
+constexpr long long BLOOM_LARGE_TEXELS = 65536;
 cudaError_t launch_bloom_ref( const BloomArgs& b, cudaStream_t s );
 cudaError_t launch_bloom_f32( const BloomArgs& b, cudaStream_t s );
 cudaError_t launch_bloom_f16( const BloomArgs& b, cudaStream_t s );

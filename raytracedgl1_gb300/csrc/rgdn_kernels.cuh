@@ -2589,56 +2589,283 @@ template< int M > __global__ void __launch_bounds__( 256 ) k_prepare_final( cons
 // images in PRE_FINAL's format. textureLod with the framebuffers' bilinear clamp-to-edge
 // sampler is evaluated in FP32 (texel centres at +0.5, weights from the fractional position).
 // ==========================================================================================
-template< int M > __device__ __forceinline__ float3 bloom_bilinear( const void* img, const int w, const int h, const float u, const float v )
+// One bloom texel: (r, g) as a pair for the packed FP32x2 operations, b alone. Each packed
+// lane rounds as the scalar operation does (no contraction), so results equal a scalar
+// evaluation bit for bit.
+struct P3
 {
-    using S         = Sto< M >;
-    const float x   = u * (float)w - 0.5f, y = v * (float)h - 0.5f;
-    const float fx  = floorf( x ), fy = floorf( y );
-    const float a   = x - fx, b = y - fy;
-    const int   ix  = (int)fx, iy = (int)fy;
-    const int   x0  = min( max( ix, 0 ), w - 1 ), x1 = min( max( ix + 1, 0 ), w - 1 );
-    const int   y0  = min( max( iy, 0 ), h - 1 ), y1 = min( max( iy + 1, 0 ), h - 1 );
-    const float3 t00 = S::ldpre( img, (size_t)( y0 * w + x0 ) ), t10 = S::ldpre( img, (size_t)( y0 * w + x1 ) );
-    const float3 t01 = S::ldpre( img, (size_t)( y1 * w + x0 ) ), t11 = S::ldpre( img, (size_t)( y1 * w + x1 ) );
-    return vmix( vmix( t00, t10, a ), vmix( t01, t11, a ), b );
+    float2 rg;
+    float  b;
+};
+__device__ __forceinline__ float3 f3of( P3 p ) { return f3( p.rg.x, p.rg.y, p.b ); }
+__device__ __forceinline__ P3     padd( P3 a, P3 b ) { return { __fadd2_rn( a.rg, b.rg ), a.b + b.b }; }
+__device__ __forceinline__ P3     pmul( P3 a, float s ) { return { __fmul2_rn( a.rg, make_float2( s, s ) ), a.b * s }; }
+// gmix per channel: x (1 - a) + y a
+__device__ __forceinline__ P3 pmix( P3 x, P3 y, float a )
+{
+    const float w = 1.0f - a;
+    return { __fadd2_rn( __fmul2_rn( x.rg, make_float2( w, w ) ), __fmul2_rn( y.rg, make_float2( a, a ) ) ), x.b * w + y.b * a };
 }
-__device__ __forceinline__ float3 sum4( float3 a, float3 b, float3 c, float3 d ) { return add( add( add( a, b ), c ), d ); }
+__device__ __forceinline__ float plum( P3 c ) { return 0.2125f * c.rg.x + 0.7154f * c.rg.y + 0.0721f * c.b; }
 
-// step k: src is BLOOM_INPUT (k = 0) or mip k, dst mip k + 1 (CmBloomDownsample.comp:15-136)
+// a texel of an image in PRE_FINAL's format
+template< int M > __device__ __forceinline__ P3 bloom_ld( const void* p, size_t i )
+{
+    const float3 c = Sto< M >::ldpre( p, i );
+    return { make_float2( c.x, c.y ), c.z };
+}
+
+// one coordinate of the bilinear clamp-to-edge sampler: x = u n - 0.5, the texel pair
+// (floor(x), floor(x) + 1) clamped to [0, n - 1] and the weight x - floor(x)
+struct BlAxis
+{
+    int   i0, i1;
+    float f;
+};
+__device__ __forceinline__ BlAxis bl_axis( float u, int n )
+{
+    const float x  = u * (float)n - 0.5f;
+    const float fx = floorf( x );
+    const int   ix = (int)fx;
+    return { min( max( ix, 0 ), n - 1 ), min( max( ix + 1, 0 ), n - 1 ), x - fx };
+}
+template< int M > __device__ __forceinline__ P3 bl_sample( const void* img, int w, const BlAxis& ax, const BlAxis& ay )
+{
+    const P3 t00 = bloom_ld< M >( img, (size_t)( ay.i0 * w + ax.i0 ) ), t10 = bloom_ld< M >( img, (size_t)( ay.i0 * w + ax.i1 ) );
+    const P3 t01 = bloom_ld< M >( img, (size_t)( ay.i1 * w + ax.i0 ) ), t11 = bloom_ld< M >( img, (size_t)( ay.i1 * w + ax.i1 ) );
+    return pmix( pmix( t00, t10, ax.f ), pmix( t01, t11, ax.f ), ay.f );
+}
+
+// One texel of downsample step k (CmBloomDownsample.comp:15-136): src is BLOOM_INPUT (k = 0)
+// or mip k, dst mip k + 1. 13 bilinear taps at offsets of -2..2 source texels, five 2x2 boxes
+// of them, Karis weights 1 / (1 + luminance) on step 0. When each offset's texel pair starts
+// where the previous one's ends (the usual case; rounding near a texel edge can break it) the
+// 6x6 source window is read once, a row at a time, and each row's horizontal lerps serve the
+// taps above and below it. Every tap is the same expression either way.
 template< int M >
-__global__ void __launch_bounds__( 256 ) k_bloom_down( const void* src, int sw, int sh, void* dst, int dw, int dh, int k, int W, int H )
+__device__ __forceinline__ void bloom_down_texel( const void* src, int sw, int sh, void* dst, int dw, int x, int y, int k, int W, int H )
+{
+    const float idx = (float)( 1 << ( k + 1 ) ) / (float)W, idy = (float)( 1 << ( k + 1 ) ) / (float)H;
+    const float u = ( (float)x + 0.5f ) * idx, v = ( (float)y + 0.5f ) * idy;
+    if( u > 1.0f || v > 1.0f ) return;
+    const float isx = (float)( 1 << k ) / (float)W, isy = (float)( 1 << k ) / (float)H;
+    BlAxis      ax[ 5 ], ay[ 5 ];
+    bool        chain = true;
+#pragma unroll
+    for( int j = 0; j < 5; j++ )
+    {
+        ax[ j ] = bl_axis( u + (float)( j - 2 ) * isx, sw );
+        ay[ j ] = bl_axis( v + (float)( j - 2 ) * isy, sh );
+        if( j > 0 ) chain = chain && ax[ j - 1 ].i1 == ax[ j ].i0 && ay[ j - 1 ].i1 == ay[ j ].i0;
+    }
+    // the boxes' sums in tap order: b0 = t3 t4 t8 t9, b1 = t0 t1 t5 t6, b2 = t1 t2 t6 t7,
+    // b3 = t5 t6 t10 t11, b4 = t6 t7 t11 t12 (tap (ox, oy) on the 5x5 offset grid: t0 (-2,-2),
+    // t1 (0,-2), t2 (2,-2), t3 (-1,-1), t4 (1,-1), t5 (-2,0), t6 (0,0), t7 (2,0), t8 (-1,1),
+    // t9 (1,1), t10 (-2,2), t11 (0,2), t12 (2,2))
+    P3 s0, s1, s2, s3, s4;
+    if( chain )
+    {
+        int col[ 6 ];
+#pragma unroll
+        for( int j = 0; j < 5; j++ ) col[ j ] = ax[ j ].i0;
+        col[ 5 ] = ax[ 4 ].i1;
+        P3 hp[ 5 ] = {}, hc[ 5 ] = {};
+#pragma unroll
+        for( int r = 0; r < 6; r++ )
+        {
+            const int row = r < 5 ? ay[ r ].i0 : ay[ 4 ].i1;
+            P3        t[ 6 ];
+#pragma unroll
+            for( int c = 0; c < 6; c++ ) t[ c ] = bloom_ld< M >( src, (size_t)( row * sw + col[ c ] ) );
+#pragma unroll
+            for( int j = 0; j < 5; j++ )
+                if( ( j & 1 ) == 0 || ( r >= 1 && r <= 4 ) ) hc[ j ] = pmix( t[ j ], t[ j + 1 ], ax[ j ].f );
+            if( r > 0 )
+            {
+                const int   yj = r - 1;
+                const float b  = ay[ yj ].f;
+                if( ( yj & 1 ) == 0 )
+                {
+                    const P3 ta = pmix( hp[ 0 ], hc[ 0 ], b ), tb = pmix( hp[ 2 ], hc[ 2 ], b ), tc = pmix( hp[ 4 ], hc[ 4 ], b );
+                    if( yj == 0 ) s1 = padd( ta, tb ), s2 = padd( tb, tc );
+                    else if( yj == 2 ) s1 = padd( padd( s1, ta ), tb ), s2 = padd( padd( s2, tb ), tc ), s3 = padd( ta, tb ), s4 = padd( tb, tc );
+                    else s3 = padd( padd( s3, ta ), tb ), s4 = padd( padd( s4, tb ), tc );
+                }
+                else
+                {
+                    const P3 ta = pmix( hp[ 1 ], hc[ 1 ], b ), tb = pmix( hp[ 3 ], hc[ 3 ], b );
+                    s0 = yj == 1 ? padd( ta, tb ) : padd( padd( s0, ta ), tb );
+                }
+            }
+#pragma unroll
+            for( int j = 0; j < 5; j++ ) hp[ j ] = hc[ j ];
+        }
+    }
+    else
+    {
+        auto     tap = [ & ]( int xj, int yj ) { return bl_sample< M >( src, sw, ax[ xj ], ay[ yj ] ); };
+        const P3 t0 = tap( 0, 0 ), t1 = tap( 2, 0 ), t2 = tap( 4, 0 ), t3 = tap( 1, 1 ), t4 = tap( 3, 1 );
+        const P3 t5 = tap( 0, 2 ), t6 = tap( 2, 2 ), t7 = tap( 4, 2 ), t8 = tap( 1, 3 ), t9 = tap( 3, 3 );
+        const P3 t10 = tap( 0, 4 ), t11 = tap( 2, 4 ), t12 = tap( 4, 4 );
+        s0 = padd( padd( padd( t3, t4 ), t8 ), t9 );
+        s1 = padd( padd( padd( t0, t1 ), t5 ), t6 );
+        s2 = padd( padd( padd( t1, t2 ), t6 ), t7 );
+        s3 = padd( padd( padd( t5, t6 ), t10 ), t11 );
+        s4 = padd( padd( padd( t6, t7 ), t11 ), t12 );
+    }
+    const P3 b0 = pmul( s0, 0.25f ), b1 = pmul( s1, 0.25f ), b2 = pmul( s2, 0.25f ), b3 = pmul( s3, 0.25f ), b4 = pmul( s4, 0.25f );
+    P3       r;
+    if( k == 0 )
+    {
+        // partial Karis average: each box weighted by 1 / (1 + luminance)
+        auto kw = []( P3 bx ) { return 1.0f / ( 1.0f + plum( bx ) ); };
+        r       = padd( padd( padd( padd( pmul( b0, 0.5f * kw( b0 ) ), pmul( b1, 0.125f * kw( b1 ) ) ), pmul( b2, 0.125f * kw( b2 ) ) ),
+                              pmul( b3, 0.125f * kw( b3 ) ) ),
+                        pmul( b4, 0.125f * kw( b4 ) ) );
+    }
+    else r = padd( padd( padd( padd( pmul( b0, 0.5f ), pmul( b1, 0.125f ) ), pmul( b2, 0.125f ) ), pmul( b3, 0.125f ) ), pmul( b4, 0.125f ) );
+    Sto< M >::stpre( dst, (size_t)( y * dw + x ), f3of( r ) );
+}
+
+// One texel of upsample step k (CmBloomUpsample.comp:15-104): a 3x3 tent of bilinear taps of
+// src (mip k + 1) around the texel's centre plus half a source texel, plus dst's own texel for
+// k > 0; dst is mip k, or BLOOM_RESULT for k = 0. The chained case reads the 4x4 source window
+// once and shares each row's lerps between the taps above and below it.
+template< int M >
+__device__ __forceinline__ void bloom_up_texel( const void* src, int sw, int sh, void* dst, int dw, int x, int y, int k, int W, int H )
+{
+    const float isx = (float)( 1 << ( k + 1 ) ) / (float)W, isy = (float)( 1 << ( k + 1 ) ) / (float)H;
+    const float iux = (float)( 1 << k ) / (float)W, iuy = (float)( 1 << k ) / (float)H;
+    const float u = ( (float)x + 0.5f ) * iux + 0.5f * isx, v = ( (float)y + 0.5f ) * iuy + 0.5f * isy;
+    if( u > 1.0f || v > 1.0f ) return;
+    BlAxis ax[ 3 ], ay[ 3 ];
+    bool   chain = true;
+#pragma unroll
+    for( int j = 0; j < 3; j++ )
+    {
+        ax[ j ] = bl_axis( u + (float)( j - 1 ) * isx, sw );
+        ay[ j ] = bl_axis( v + (float)( j - 1 ) * isy, sh );
+        if( j > 0 ) chain = chain && ax[ j - 1 ].i1 == ax[ j ].i0 && ay[ j - 1 ].i1 == ay[ j ].i0;
+    }
+    auto wt = []( int q, int j ) { return ( q == 1 ? 2.0f : 1.0f ) * ( j == 1 ? 0.125f : 0.0625f ); };   // 1 2 1 / 2 4 2 / 1 2 1 over 16
+    P3   r  = { make_float2( 0.0f, 0.0f ), 0.0f };
+    if( chain )
+    {
+        const int col[ 4 ] = { ax[ 0 ].i0, ax[ 1 ].i0, ax[ 2 ].i0, ax[ 2 ].i1 };
+        P3        hp[ 3 ] = {}, hc[ 3 ];
+#pragma unroll
+        for( int rr = 0; rr < 4; rr++ )
+        {
+            const int row = rr < 3 ? ay[ rr ].i0 : ay[ 2 ].i1;
+            P3        t[ 4 ];
+#pragma unroll
+            for( int c = 0; c < 4; c++ ) t[ c ] = bloom_ld< M >( src, (size_t)( row * sw + col[ c ] ) );
+#pragma unroll
+            for( int j = 0; j < 3; j++ ) hc[ j ] = pmix( t[ j ], t[ j + 1 ], ax[ j ].f );
+            if( rr > 0 )
+#pragma unroll
+                for( int j = 0; j < 3; j++ ) r = padd( r, pmul( pmix( hp[ j ], hc[ j ], ay[ rr - 1 ].f ), wt( rr - 1, j ) ) );
+#pragma unroll
+            for( int j = 0; j < 3; j++ ) hp[ j ] = hc[ j ];
+        }
+    }
+    else
+    {
+#pragma unroll
+        for( int q = 0; q < 3; q++ )
+#pragma unroll
+            for( int j = 0; j < 3; j++ ) r = padd( r, pmul( bl_sample< M >( src, sw, ax[ j ], ay[ q ] ), wt( q, j ) ) );
+    }
+    if( k > 0 ) r = padd( r, bloom_ld< M >( dst, (size_t)( y * dw + x ) ) );
+    Sto< M >::stpre( dst, (size_t)( y * dw + x ), f3of( r ) );
+}
+
+// MINB 4 for the large steps (more warps in flight at 64 registers), 1 for the small coarse
+// steps, whose single wave is bound by one texel's chain of dependent loads; the B10G11R11
+// decode of the reference storage mode would spill at 64 registers, so it always takes 1
+template< int M, int MINB >
+__global__ void __launch_bounds__( 256, M == MODE_REF ? 1 : MINB ) k_bloom_down( const void* src, int sw, int sh, void* dst, int dw, int dh, int k, int W, int H )
 {
     const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
     pdl_launch_dependents();
     pdl_wait();
     if( x >= dw || y >= dh ) return;
-    const float  idx = (float)( 1 << ( k + 1 ) ) / (float)W, idy = (float)( 1 << ( k + 1 ) ) / (float)H;
-    const float  u   = ( (float)x + 0.5f ) * idx, v = ( (float)y + 0.5f ) * idy;
-    if( u > 1.0f || v > 1.0f ) return;
-    const float  isx = (float)( 1 << k ) / (float)W, isy = (float)( 1 << k ) / (float)H;
-    auto tap = [ & ]( float ox, float oy ) { return bloom_bilinear< M >( src, sw, sh, u + ox * isx, v + oy * isy ); };
-    const float3 t0 = tap( -2, -2 ), t1 = tap( 0, -2 ), t2 = tap( 2, -2 );
-    const float3 t3 = tap( -1, -1 ), t4 = tap( 1, -1 );
-    const float3 t5 = tap( -2, 0 ), t6 = tap( 0, 0 ), t7 = tap( 2, 0 );
-    const float3 t8 = tap( -1, 1 ), t9 = tap( 1, 1 );
-    const float3 t10 = tap( -2, 2 ), t11 = tap( 0, 2 ), t12 = tap( 2, 2 );
-    const float3 b0 = mul( sum4( t3, t4, t8, t9 ), 0.25f ), b1 = mul( sum4( t0, t1, t5, t6 ), 0.25f );
-    const float3 b2 = mul( sum4( t1, t2, t6, t7 ), 0.25f ), b3 = mul( sum4( t5, t6, t10, t11 ), 0.25f );
-    const float3 b4 = mul( sum4( t6, t7, t11, t12 ), 0.25f );
-    float3 r;
-    if( k == 0 )
-    {
-        // partial Karis average: each box weighted by 1 / (1 + luminance)
-        auto kw = []( float3 bx ) { return 1.0f / ( 1.0f + luminance( bx ) ); };
-        r = add( add( add( add( mul( b0, 0.5f * kw( b0 ) ), mul( b1, 0.125f * kw( b1 ) ) ), mul( b2, 0.125f * kw( b2 ) ) ), mul( b3, 0.125f * kw( b3 ) ) ),
-                 mul( b4, 0.125f * kw( b4 ) ) );
-    }
-    else r = add( add( add( add( mul( b0, 0.5f ), mul( b1, 0.125f ) ), mul( b2, 0.125f ) ), mul( b3, 0.125f ) ), mul( b4, 0.125f ) );
-    Sto< M >::stpre( dst, (size_t)( y * dw + x ), r );
+    bloom_down_texel< M >( src, sw, sh, dst, dw, x, y, k, W, H );
 }
 
-// step k: src mip k + 1, dst mip k (adding its own texel) or BLOOM_RESULT (k = 0)
-// (CmBloomUpsample.comp:15-104)
+// Upsample step k for the 2x2 quad of dst texels at (x0, y0): the four texels' tents read the
+// same 4x4 source window when their texel pairs chain and coincide (the usual case, as dst has
+// twice src's resolution), so the window is read once, each row's lerps serve both rows of the
+// quad, and each texel keeps its own weights. Returns false, having written nothing, when the
+// quad is not complete, a texel is outside the uv <= 1 range or the windows differ.
+template< int M >
+__device__ __forceinline__ bool bloom_up_quad( const void* src, int sw, int sh, void* dst, int dw, int dh, int x0, int y0, int k, int W, int H )
+{
+    if( x0 + 1 >= dw || y0 + 1 >= dh ) return false;
+    const float isx = (float)( 1 << ( k + 1 ) ) / (float)W, isy = (float)( 1 << ( k + 1 ) ) / (float)H;
+    const float iux = (float)( 1 << k ) / (float)W, iuy = (float)( 1 << k ) / (float)H;
+    BlAxis      ax[ 2 ][ 3 ], ay[ 2 ][ 3 ];
+    bool        ok = true;
+#pragma unroll
+    for( int i = 0; i < 2; i++ )
+    {
+        const float u = ( (float)( x0 + i ) + 0.5f ) * iux + 0.5f * isx, v = ( (float)( y0 + i ) + 0.5f ) * iuy + 0.5f * isy;
+        ok            = ok && u <= 1.0f && v <= 1.0f;
+#pragma unroll
+        for( int j = 0; j < 3; j++ )
+        {
+            ax[ i ][ j ] = bl_axis( u + (float)( j - 1 ) * isx, sw );
+            ay[ i ][ j ] = bl_axis( v + (float)( j - 1 ) * isy, sh );
+        }
+        ok = ok && ax[ i ][ 0 ].i1 == ax[ i ][ 1 ].i0 && ax[ i ][ 1 ].i1 == ax[ i ][ 2 ].i0 && ay[ i ][ 0 ].i1 == ay[ i ][ 1 ].i0 &&
+             ay[ i ][ 1 ].i1 == ay[ i ][ 2 ].i0;
+    }
+#pragma unroll
+    for( int j = 0; j < 3; j++ ) ok = ok && ax[ 0 ][ j ].i0 == ax[ 1 ][ j ].i0 && ay[ 0 ][ j ].i0 == ay[ 1 ][ j ].i0;
+    ok = ok && ax[ 0 ][ 2 ].i1 == ax[ 1 ][ 2 ].i1 && ay[ 0 ][ 2 ].i1 == ay[ 1 ][ 2 ].i1;
+    if( !ok ) return false;
+    auto      wt       = []( int q, int j ) { return ( q == 1 ? 2.0f : 1.0f ) * ( j == 1 ? 0.125f : 0.0625f ); };
+    const int col[ 4 ] = { ax[ 0 ][ 0 ].i0, ax[ 0 ][ 1 ].i0, ax[ 0 ][ 2 ].i0, ax[ 0 ][ 2 ].i1 };
+    P3        r[ 2 ][ 2 ];
+#pragma unroll
+    for( int q = 0; q < 4; q++ ) r[ q >> 1 ][ q & 1 ] = { make_float2( 0.0f, 0.0f ), 0.0f };
+    P3 hp[ 2 ][ 3 ] = {}, hc[ 2 ][ 3 ];
+#pragma unroll
+    for( int rr = 0; rr < 4; rr++ )
+    {
+        const int row = rr < 3 ? ay[ 0 ][ rr ].i0 : ay[ 0 ][ 2 ].i1;
+        P3        t[ 4 ];
+#pragma unroll
+        for( int c = 0; c < 4; c++ ) t[ c ] = bloom_ld< M >( src, (size_t)( row * sw + col[ c ] ) );
+#pragma unroll
+        for( int xi = 0; xi < 2; xi++ )
+#pragma unroll
+            for( int j = 0; j < 3; j++ ) hc[ xi ][ j ] = pmix( t[ j ], t[ j + 1 ], ax[ xi ][ j ].f );
+        if( rr > 0 )
+#pragma unroll
+            for( int yi = 0; yi < 2; yi++ )
+#pragma unroll
+                for( int xi = 0; xi < 2; xi++ )
+#pragma unroll
+                    for( int j = 0; j < 3; j++ )
+                        r[ yi ][ xi ] = padd( r[ yi ][ xi ], pmul( pmix( hp[ xi ][ j ], hc[ xi ][ j ], ay[ yi ][ rr - 1 ].f ), wt( rr - 1, j ) ) );
+#pragma unroll
+        for( int xi = 0; xi < 2; xi++ )
+#pragma unroll
+            for( int j = 0; j < 3; j++ ) hp[ xi ][ j ] = hc[ xi ][ j ];
+    }
+#pragma unroll
+    for( int q = 0; q < 4; q++ )
+    {
+        const size_t i = (size_t)( ( y0 + ( q >> 1 ) ) * dw + x0 + ( q & 1 ) );
+        P3           o = r[ q >> 1 ][ q & 1 ];
+        if( k > 0 ) o = padd( o, bloom_ld< M >( dst, i ) );
+        Sto< M >::stpre( dst, i, f3of( o ) );
+    }
+    return true;
+}
+
+// one thread per dst texel (the small coarse steps)
 template< int M >
 __global__ void __launch_bounds__( 256 ) k_bloom_up( const void* src, int sw, int sh, void* dst, int dw, int dh, int k, int W, int H )
 {
@@ -2646,19 +2873,24 @@ __global__ void __launch_bounds__( 256 ) k_bloom_up( const void* src, int sw, in
     pdl_launch_dependents();
     pdl_wait();
     if( x >= dw || y >= dh ) return;
-    const float isx = (float)( 1 << ( k + 1 ) ) / (float)W, isy = (float)( 1 << ( k + 1 ) ) / (float)H;
-    const float iux = (float)( 1 << k ) / (float)W, iuy = (float)( 1 << k ) / (float)H;
-    const float u   = ( (float)x + 0.5f ) * iux + 0.5f * isx, v = ( (float)y + 0.5f ) * iuy + 0.5f * isy;
-    if( u > 1.0f || v > 1.0f ) return;
-    const float wt[ 3 ][ 3 ] = { { 0.0625f, 0.125f, 0.0625f }, { 0.125f, 0.25f, 0.125f }, { 0.0625f, 0.125f, 0.0625f } };
-    float3      r            = f3( 0, 0, 0 );
-#pragma unroll
-    for( int oy = -1; oy <= 1; oy++ )
-#pragma unroll
-        for( int ox = -1; ox <= 1; ox++ )
-            r = add( r, mul( bloom_bilinear< M >( src, sw, sh, u + (float)ox * isx, v + (float)oy * isy ), wt[ oy + 1 ][ ox + 1 ] ) );
-    if( k > 0 ) r = add( r, Sto< M >::ldpre( dst, (size_t)( y * dw + x ) ) );
-    Sto< M >::stpre( dst, (size_t)( y * dw + x ), r );
+    bloom_up_texel< M >( src, sw, sh, dst, dw, x, y, k, W, H );
+}
+
+// one thread per 2x2 quad of dst texels, blocks of 32x4 threads (the large steps)
+template< int M >
+__global__ void __launch_bounds__( 128 ) k_bloom_up_quad( const void* src, int sw, int sh, void* dst, int dw, int dh, int k, int W, int H )
+{
+    const int x0 = 2 * ( blockIdx.x * blockDim.x + threadIdx.x ), y0 = 2 * ( blockIdx.y * blockDim.y + threadIdx.y );
+    pdl_launch_dependents();
+    pdl_wait();
+    if( x0 >= dw || y0 >= dh ) return;
+    if( bloom_up_quad< M >( src, sw, sh, dst, dw, dh, x0, y0, k, W, H ) ) return;
+#pragma unroll 1
+    for( int q = 0; q < 4; q++ )
+    {
+        const int x = x0 + ( q & 1 ), y = y0 + ( q >> 1 );
+        if( x < dw && y < dh ) bloom_up_texel< M >( src, sw, sh, dst, dw, x, y, k, W, H );
+    }
 }
 
 // FINAL += intensity * BLOOM_RESULT(uv) (CmBloomApply.comp:45-76, lens dirt not included)
@@ -2668,11 +2900,11 @@ template< int M > __global__ void __launch_bounds__( 256 ) k_bloom_apply( const 
     pdl_launch_dependents();
     pdl_wait();
     if( x >= W || y >= H ) return;
-    const float  u = ( (float)x + 0.5f ) * ( 1.0f / (float)W ), v = ( (float)y + 0.5f ) * ( 1.0f / (float)H );
+    const float u = ( (float)x + 0.5f ) * ( 1.0f / (float)W ), v = ( (float)y + 0.5f ) * ( 1.0f / (float)H );
     if( u > 1.0f || v > 1.0f ) return;
-    const float3 bloom = mul( bloom_bilinear< M >( result, W, H, u, v ), intensity );
+    const P3     bloom = pmul( bl_sample< M >( result, W, bl_axis( u, W ), bl_axis( v, H ) ), intensity );
     const size_t i     = (size_t)( y * W + x );
-    Sto< M >::stpre( finalImg, i, add( Sto< M >::ldpre( finalImg, i ), bloom ) );
+    Sto< M >::stpre( finalImg, i, f3of( padd( bloom_ld< M >( finalImg, i ), bloom ) ) );
 }
 
 }  // namespace dev
@@ -2721,16 +2953,21 @@ template< int M > cudaError_t launch_stage_t( const FrameArgs& a, int stage, int
 template< int M > cudaError_t launch_bloom_t( const BloomArgs& b, cudaStream_t s )
 {
     const dim3  blk( 32, 8 );
-    auto        grid = []( int w, int h ) { return dim3( ( w + 31 ) / 32, ( h + 7 ) / 8 ); };
-    cudaError_t e    = cudaSuccess;
+    auto        grid  = []( int w, int h ) { return dim3( ( w + 31 ) / 32, ( h + 7 ) / 8 ); };
+    auto        large = [ & ]( int p ) { return (long long)b.w[ p ] * b.h[ p ] >= BLOOM_LARGE_TEXELS; };
+    cudaError_t e     = cudaSuccess;
     for( int k = 0; k < 8 && e == cudaSuccess; k++ )
-        e = launch_pdl( dev::k_bloom_down< M >, grid( b.w[ k + 1 ], b.h[ k + 1 ] ), blk, 0, s, (const void*)b.planes[ k ], b.w[ k ], b.h[ k ],
-                        b.planes[ k + 1 ], b.w[ k + 1 ], b.h[ k + 1 ], k, b.W, b.H );
+        e = launch_pdl( large( k + 1 ) ? dev::k_bloom_down< M, 4 > : dev::k_bloom_down< M, 1 >, grid( b.w[ k + 1 ], b.h[ k + 1 ] ), blk, 0, s,
+                        (const void*)b.planes[ k ], b.w[ k ], b.h[ k ], b.planes[ k + 1 ], b.w[ k + 1 ], b.h[ k + 1 ], k, b.W, b.H );
     for( int k = 7; k >= 0 && e == cudaSuccess; k-- )
     {
         const int d = k == 0 ? 9 : k;
-        e           = launch_pdl( dev::k_bloom_up< M >, grid( b.w[ d ], b.h[ d ] ), blk, 0, s, (const void*)b.planes[ k + 1 ], b.w[ k + 1 ],
-                                  b.h[ k + 1 ], b.planes[ d ], b.w[ d ], b.h[ d ], k, b.W, b.H );
+        if( large( d ) )
+            e = launch_pdl( dev::k_bloom_up_quad< M >, dim3( ( b.w[ d ] + 63 ) / 64, ( b.h[ d ] + 7 ) / 8 ), dim3( 32, 4 ), 0, s,
+                            (const void*)b.planes[ k + 1 ], b.w[ k + 1 ], b.h[ k + 1 ], b.planes[ d ], b.w[ d ], b.h[ d ], k, b.W, b.H );
+        else
+            e = launch_pdl( dev::k_bloom_up< M >, grid( b.w[ d ], b.h[ d ] ), blk, 0, s, (const void*)b.planes[ k + 1 ], b.w[ k + 1 ], b.h[ k + 1 ],
+                            b.planes[ d ], b.w[ d ], b.h[ d ], k, b.W, b.H );
     }
     if( e == cudaSuccess )
         e = launch_pdl( dev::k_bloom_apply< M >, grid( b.W, b.H ), blk, 0, s, (const void*)b.planes[ 9 ], b.planes[ 10 ], b.W, b.H, b.intensity );
