@@ -2505,9 +2505,10 @@ __device__ __forceinline__ float3 lpm_709( float3 c, const LpmConsts& k )
 {
     const float rcpMax = 1.0f / fmaxf( c.x, fmaxf( c.y, c.z ) );
     float       rR = c.x * rcpMax, rG = c.y * rcpMax, rB = c.z * rcpMax;
-    rR = powf( rR, k.saturation[ 0 ] );
-    rG = powf( rG, k.saturation[ 1 ] );
-    rB = powf( rB, k.saturation[ 2 ] );
+    // pow(x, +-0) is 1 for every x, NaN included: the default saturation 0 needs no powf
+    rR = k.saturation[ 0 ] == 0.0f ? 1.0f : powf( rR, k.saturation[ 0 ] );
+    rG = k.saturation[ 1 ] == 0.0f ? 1.0f : powf( rG, k.saturation[ 1 ] );
+    rB = k.saturation[ 2 ] == 0.0f ? 1.0f : powf( rB, k.saturation[ 2 ] );
     float luma = c.y * k.lumaT[ 1 ] + ( c.x * k.lumaT[ 0 ] + ( c.z * k.lumaT[ 2 ] ) );
     luma       = powf( luma, k.contrast );
     luma       = luma * ( 1.0f / ( luma * k.toneScaleBias[ 0 ] + k.toneScaleBias[ 1 ] ) );
@@ -2536,8 +2537,20 @@ template< int M > __global__ void __launch_bounds__( 256 ) k_prepare_final( cons
     const int y = blockIdx.y * blockDim.y + threadIdx.y;
     pdl_launch_dependents();
     pdl_wait();
+    // getAutoEV100, ev100ToLuminousExposure (Exposure.h:14-51): the same for every pixel, so one
+    // thread of the block evaluates them
+    __shared__ float shExp[ 2 ];
+    if( threadIdx.x == 0 && threadIdx.y == 0 )
+    {
+        const float ev     = log2f( fmaxf( 0.0f, f.tm->avgLuminance ) * 100.0f / 12.5f );
+        const float maxLum = 1.2f * exp2f( ev );
+        shExp[ 0 ]         = maxLum > 0.0f ? 1.0f / maxLum : 0.0f;
+        shExp[ 1 ]         = exp2f( ev + f.bloomEvOffset - 3.0f );
+    }
+    __syncthreads();
     if( x >= f.W || y >= f.H ) return;
-    const int i   = y * f.W + x;
+    const float exposure = shExp[ 0 ], el = shExp[ 1 ];
+    const int   i        = y * f.W + x;
     // getCheckerboardPix (ShaderCommonGLSLFunc.h:321-329)
     const int sep = f.W / 2;
     const int odd = ( x + y % 2 ) % 2;
@@ -2557,10 +2570,6 @@ template< int M > __global__ void __launch_bounds__( 256 ) k_prepare_final( cons
         const float   a = h2f( v.w );
         hdr             = f3( hdr.x * a + h2f( v.x ), hdr.y * a + h2f( v.y ), hdr.z * a + h2f( v.z ) );
     }
-    // getAutoEV100, ev100ToLuminousExposure (Exposure.h:14-51)
-    const float ev       = log2f( fmaxf( 0.0f, f.tm->avgLuminance ) * 100.0f / 12.5f );
-    const float maxLum   = 1.2f * exp2f( ev );
-    const float exposure = maxLum > 0.0f ? 1.0f / maxLum : 0.0f;
     // finalizeColor (CmPrepareFinal.comp:101-113)
     float3 color;
     if( (float)x < f.lightmapCoverage * f.rw )
@@ -2574,8 +2583,7 @@ template< int M > __global__ void __launch_bounds__( 256 ) k_prepare_final( cons
         color          = lpm_709( c, f.lpm );
     }
     // getBloomInput (CmPrepareFinal.comp:116-133)
-    const float  el    = exp2f( ev + f.bloomEvOffset - 3.0f );
-    float3       bloom = f3( ( hdr.x + emis.x * el ) * exposure, ( hdr.y + emis.y * el ) * exposure, ( hdr.z + emis.z * el ) * exposure );
+    float3 bloom = f3( ( hdr.x + emis.x * el ) * exposure, ( hdr.y + emis.y * el ) * exposure, ( hdr.z + emis.z * el ) * exposure );
     if( isnan( bloom.x ) || isnan( bloom.y ) || isnan( bloom.z ) || isinf( bloom.x ) || isinf( bloom.y ) || isinf( bloom.z ) )
         bloom = f3( 0, 0, 0 );
     bloom = mul( bloom, gsmoothstep( 0.0f, f.bloomThreshold, luminance( bloom ) ) );
