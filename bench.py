@@ -695,6 +695,37 @@ def run_ours(args, dist: Dist):
     bloom_t = {"kernel": "bloom", "what": "8 downsample (13-tap, Karis on the first) + 8 tent upsample + apply, 17 launches",
                "us_per_frame": round(bl_us, 2), "mpix_s": round(W * H / bl_us, 1),
                "alg_bytes": bl_alg, "gbs": round(bl_alg / (bl_us / 1e6) / 1e9, 1)}
+
+    # --- volumetric scattering (rgdn_process_scattering: volume integration + accumulation) ---
+    from raytracedgl1_gb300.denoiser import Volumetric
+    vparams = N.VolumetricParams()
+    for name in ("invView", "invProjection", "volumeViewProj"):
+        getattr(vparams, name)[:] = np.eye(4, dtype=np.float32).reshape(-1)
+    vparams.cameraPosition[:] = (0.0, 0.0, -1.0, 0.0)
+    vparams.volumeCameraNear, vparams.volumeCameraFar = 0.5, 3.0
+    vparams.maxHistoryLength = 8.0
+    vparams.volumeEnableType = N.VOLUME_ENABLE_VOLUMETRIC
+    volu = Volumetric(st)
+    with torch.cuda.stream(cs):
+        for k in range(3):
+            vparams.frameId = k
+            volu.ProcessScattering(k & 1, vparams, cs)
+        ve = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+        ve[0].record(cs)
+        for k in range(nfin):
+            vparams.frameId = 3 + k
+            volu.ProcessScattering(k & 1, vparams, cs)
+        ve[1].record(cs)
+    cs.synchronize()
+    vol_us = 1e3 * ve[0].elapsed_time(ve[1]) / nfin
+    vol_bytes = 2 * 160 * 88 * 64 * 8
+    # per pixel: motion 8, depth 2, normal 4, NDC depth 4, previous depth 2 and normal 4 (one
+    # texel per pixel over the frame), previous scattering 8 and history 2, outputs 8 + 2
+    vol_alg = vol_bytes + 44 * W * H
+    volumetric_t = {"kernel": "process_scattering",
+                    "what": "CmVolumetricProcess (160x88x64 froxels, in place) + CmScatterAccum (VOLUMETRIC mode)",
+                    "us_per_frame": round(vol_us, 2), "mpix_s": round(W * H / vol_us, 1),
+                    "alg_bytes": vol_alg, "gbs": round(vol_alg / (vol_us / 1e6) / 1e9, 1)}
     top = kern[0]
     peak, peak_kind = load_peaks()
 
@@ -819,6 +850,7 @@ def run_ours(args, dist: Dist):
         "kernel_sum_us_per_step": round(kernel_total_us, 2),
         "prepare_final": final,
         "bloom": bloom_t,
+        "volumetric": volumetric_t,
         "path_alg_gbs": round(sum(d["alg_bytes"] * d["launches"] for d in kern) / args.steps /
                               (total_ms_max / args.steps / 1e3) / 1e9, 1),
         "e2e": {"value": round(e2e_value, 2), "unit": "Mpix/s", "h2d_bytes_per_step": int(h2d),

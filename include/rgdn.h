@@ -139,7 +139,8 @@ typedef enum rgdn_framebuf
     RGDN_FB_DIFF_PONG_VARIANCE,
     /* exposure application and tonemapping (rgdn_prepare_final), regular pixel layout */
     RGDN_FB_SCREEN_EMIS_RT,           /* B10G11R11: the producer's screen-space emission */
-    RGDN_FB_SCATTERING,               /* RGBA16_SFLOAT: volumetric in-scattering (rgb), transmittance (a) */
+    RGDN_FB_SCATTERING,               /* RGBA16_SFLOAT: volumetric in-scattering (rgb), transmittance (a);
+                                         prev (rgdn_process_scattering accumulates it over frames) */
     RGDN_FB_FINAL,                    /* the exposed, tonemapped image (PRE_FINAL's format) */
     RGDN_FB_BLOOM_INPUT,              /* bloom input (PRE_FINAL's format) */
     /* bloom (rgdn_bloom): mip k is ((W+1) >> k) x ((H+1) >> k), at least 1x1; PRE_FINAL's format */
@@ -152,6 +153,14 @@ typedef enum rgdn_framebuf
     RGDN_FB_BLOOM_MIP7,
     RGDN_FB_BLOOM_MIP8,
     RGDN_FB_BLOOM_RESULT,             /* W x H */
+    /* volumetric scattering (rgdn_process_scattering) */
+    RGDN_FB_DEPTH_NDC,                /* R32_SFLOAT: NDC depth of the primary hit, regular layout */
+    RGDN_FB_SCATTERING_HISTORY,       /* R16_SFLOAT: history length of SCATTERING, regular layout, prev */
+    RGDN_FB_SCATTER_VOLUME,           /* RGBA16_SFLOAT froxel volume of RGDN_VOLUME_SIZE_X x _Y x _Z
+                                         cells as an image of X x (Y * Z) texels, z-major slices
+                                         (cell (x, y, z) at row z * Y + y); rgb in-scattered light,
+                                         a extinction along the cell; prev (two slots, as the
+                                         reference's scattering[2]) */
     RGDN_FB_COUNT
 } rgdn_framebuf;
 
@@ -262,7 +271,7 @@ rgdn_status rgdn_stream_required_bytes( const rgdn_stream_create_info* info, uin
  * frameIndex (0 or 1) selects. A producer writes the G-buffer there directly. */
 rgdn_status rgdn_stream_get_framebuffer( rgdn_stream* stream, uint32_t fb, uint32_t frameIndex, rgdn_image* outImage );
 /* Points a producer-written G-buffer image (RGDN_FB_ALBEDO .. RGDN_FB_GRADIENT_RESHADED,
- * RGDN_FB_SCREEN_EMIS_RT, RGDN_FB_SCATTERING) of slot frameIndex at caller-owned device memory (dense rows, 16-byte aligned), so a renderer
+ * RGDN_FB_SCREEN_EMIS_RT, RGDN_FB_SCATTERING, RGDN_FB_DEPTH_NDC, RGDN_FB_SCATTER_VOLUME) of slot frameIndex at caller-owned device memory (dense rows, 16-byte aligned), so a renderer
  * that already holds its G-buffer in HBM hands it over without a copy — the role of the
  * reference's shared Framebuffers images (PathTracer writes, Denoiser reads). NULL restores
  * the stream's own plane. The memory must stay valid while work using it is in flight. */
@@ -318,6 +327,41 @@ typedef struct rgdn_bloom_params
     float bloomIntensity;   /* reference default 1 */
 } rgdn_bloom_params;
 rgdn_status rgdn_bloom( rgdn_stream* stream, uint32_t frameIndex, const rgdn_bloom_params* params, rgdn_cuda_stream cudaStream );
+
+/* ---- volumetric scattering ---------------------------------------------------------
+ * Volumetric::ProcessScattering (Volumetric.cpp:71-190), between rgdn_denoise and
+ * rgdn_calculate_exposure as VulkanDevice::Render orders them:
+ *  1. CmVolumetricProcess.comp: each froxel column of SCATTER_VOLUME[frameIndex] integrated
+ *     front to back in place (rgb: light scattered in so far, a: transmittance exp(-sum a));
+ *  2. CmScatterAccum.comp: per pixel, the previous SCATTERING reprojected (2x2 bilinear with
+ *     the depth and normal tests of the denoiser) and mixed with this frame's value by
+ *     1 / history length into SCATTERING and SCATTERING_HISTORY. This frame's value is the
+ *     processed volume sampled at the pixel's world position with a hashed dither
+ *     (VOLUMETRIC), exponential fog from the ray length (SIMPLE), or (0, 0, 0, 1) (NONE).
+ * The froxel illumination that RtVolumetric.rgen traces is an input: the producer writes
+ * SCATTER_VOLUME. Matrices are column-major, as GLSL mat4. */
+#define RGDN_VOLUME_SIZE_X 160 /* VOLUMETRIC_SIZE_X (ShaderCommonC.h:189-191) */
+#define RGDN_VOLUME_SIZE_Y 88
+#define RGDN_VOLUME_SIZE_Z 64
+#define RGDN_VOLUME_ENABLE_NONE       0u /* VOLUME_ENABLE_* (ShaderCommonC.h:195-197) */
+#define RGDN_VOLUME_ENABLE_SIMPLE     1u
+#define RGDN_VOLUME_ENABLE_VOLUMETRIC 2u
+typedef struct rgdn_volumetric_params
+{
+    float    invView[ 16 ];          /* GlobalUniform::invView */
+    float    invProjection[ 16 ];    /* GlobalUniform::invProjection */
+    float    volumeViewProj[ 16 ];   /* GlobalUniform::volumeViewProj */
+    float    cameraPosition[ 4 ];    /* xyz */
+    float    volumeCameraNear;
+    float    volumeCameraFar;        /* > volumeCameraNear */
+    float    volumeAmbient[ 3 ];     /* SIMPLE mode fog colour */
+    float    volumeScattering;       /* SIMPLE mode density (times 0.00005) */
+    float    maxHistoryLength;       /* RgDrawFrameVolumetricParams::maxHistoryLength; 0 after a
+                                        history reset */
+    uint32_t volumeEnableType;       /* RGDN_VOLUME_ENABLE_* */
+    uint32_t frameId;                /* GlobalUniform::frameId: seeds the per-pixel dither */
+} rgdn_volumetric_params;
+rgdn_status rgdn_process_scattering( rgdn_stream* stream, uint32_t frameIndex, const rgdn_volumetric_params* params, rgdn_cuda_stream cudaStream );
 
 /* One stage alone (the plain path / per-stage checking). `iteration` selects the
  * a-trous or gradient a-trous iteration. */

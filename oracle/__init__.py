@@ -36,7 +36,7 @@ def load():
         return _lib
     if not os.path.exists(LIB_PATH):
         raise ImportError(f"{LIB_PATH} missing: build it with `python -m raytracedgl1_gb300.build`")
-    from raytracedgl1_gb300._native import FinalParams, FrameParams
+    from raytracedgl1_gb300._native import FinalParams, FrameParams, VolumetricParams
     lib = C.CDLL(LIB_PATH)
     P = C.POINTER
     sig = {
@@ -52,6 +52,9 @@ def load():
         "orc_exposure_from_avg": (C.c_float, [C.c_float]),
         "orc_prepare_final": (C.c_int, [C.c_void_p, C.c_uint32, P(FinalParams), C.c_int]),
         "orc_bloom": (C.c_int, [C.c_void_p, C.c_uint32, C.c_float]),
+        "orc_process_scattering": (C.c_int, [C.c_void_p, C.c_uint32, P(VolumetricParams)]),
+        "orc_random_seed": (C.c_uint32, [C.c_int, C.c_int, C.c_uint32]),
+        "orc_wellons_lowbias32": (C.c_uint32, [C.c_uint32]),
         "orc_lpm_setup": (None, [P(C.c_float), P(C.c_float), P(C.c_float)]),
         "orc_lpm_filter": (None, [P(C.c_float), P(C.c_float), P(C.c_float)]),
         "orc_get_tonemapping": (None, [C.c_void_p, P(C.c_uint32), P(C.c_float), P(C.c_double)]),
@@ -140,6 +143,12 @@ class OracleStream:
         r = self.lib.orc_prepare_final(self.h, frame_index, C.byref(params), nthreads or nthreads_default())
         if r != 0:
             raise RuntimeError(f"orc_prepare_final failed: {r}")
+
+    def process_scattering(self, frame_index: int, params) -> None:
+        """The volume integration and the scattering accumulation (rgdn_process_scattering)."""
+        r = self.lib.orc_process_scattering(self.h, frame_index, C.byref(params))
+        if r != 0:
+            raise RuntimeError(f"orc_process_scattering failed: {r}")
 
     def bloom(self, frame_index: int, intensity: float = 1.0) -> None:
         """The bloom pyramid of BLOOM_INPUT added to FINAL (rgdn_bloom)."""

@@ -372,6 +372,7 @@ struct FbInfo
     bool     prev;
     bool     third;    // 1/3 resolution
     int      shift = 0;   // Framebuffers.cpp:669-692 FORCE_SIZE_BLOOM: (size + 1) / 2^shift, at least 1
+    int      fixedW = 0, fixedH = 0;   // a size independent of the render size
 };
 
 // The oracle's own format table (the reference's is GenerateShaderCommon.py:802-887).
@@ -429,7 +430,12 @@ FbInfo fb_info( uint32_t fb, uint32_t mode )
         // GenerateShaderCommon.py:820-863 ScreenEmisRT, Scattering, Final, BloomInput (the last
         // two in PreFinal's format per storage mode)
         case RGDN_FB_SCREEN_EMIS_RT: return { F_B10G11R11, false, false };
-        case RGDN_FB_SCATTERING: return { F_RGBA16F, false, false };
+        case RGDN_FB_SCATTERING: return { F_RGBA16F, true, false };
+        // GenerateShaderCommon.py:810, 854-855 DepthNdc, ScatteringHistory; Volumetric.cpp:31,
+        // 259-290 the scattering volume (RGBA16F, two slots), as an image of X x (Y * Z) texels
+        case RGDN_FB_DEPTH_NDC: return { F_R32F, false, false };
+        case RGDN_FB_SCATTERING_HISTORY: return { F_R16F, true, false };
+        case RGDN_FB_SCATTER_VOLUME: return { F_RGBA16F, true, false, 0, RGDN_VOLUME_SIZE_X, RGDN_VOLUME_SIZE_Y * RGDN_VOLUME_SIZE_Z };
         case RGDN_FB_FINAL:
         case RGDN_FB_BLOOM_INPUT:
         case RGDN_FB_BLOOM_RESULT: return { pre, false, false };
@@ -550,6 +556,7 @@ struct Stream
                 if( fi.fmt == F_NONE || ( s == 1 && !fi.prev ) ) { planes[ fb ][ s ] = Plane(); continue; }
                 int pw = fi.third ? GW : W, ph = fi.third ? GH : H;
                 if( fi.shift ) pw = std::max( 1, ( W + 1 ) >> fi.shift ), ph = std::max( 1, ( H + 1 ) >> fi.shift );
+                if( fi.fixedW ) pw = fi.fixedW, ph = fi.fixedH;
                 planes[ fb ][ s ].init( pw, ph, fi.fmt );
             }
         }
@@ -1650,6 +1657,234 @@ template< class T > void bloom( Stream& s, uint32_t fi, float intensity )
         }
 }
 
+// --------------------------------------------------------------------------------------------
+//  Volumetric::ProcessScattering (Volumetric.cpp:71-190)
+// --------------------------------------------------------------------------------------------
+// CmVolumetricProcess.comp:38-79: each froxel column integrated front to back in place; the
+// running (light, extinction) in T, cell z storing (light, exp(-extinction))
+template< class T > void volume_process( Stream& s, uint32_t fi )
+{
+    Plane&    vol = s.cur( RGDN_FB_SCATTER_VOLUME, fi );
+    const int nx = RGDN_VOLUME_SIZE_X, ny = RGDN_VOLUME_SIZE_Y, nz = RGDN_VOLUME_SIZE_Z;
+    for( int y = 0; y < ny; y++ )
+        for( int x = 0; x < nx; x++ )
+        {
+            V4< T > acc = vol.fetch< T >( x, y );
+            T       e   = o_exp( -acc.w );
+            vol.store< T >( x, y, { acc.x, acc.y, acc.z, e } );
+            for( int z = 1; z < nz; z++ )
+            {
+                const V4< T > v = vol.fetch< T >( x, z * ny + y );
+                const T       t = gsat( e );   // saturate( exp( -front.a ) )
+                acc             = { acc.x + t * v.x, acc.y + t * v.y, acc.z + t * v.z, acc.w + v.w };
+                e               = o_exp( -acc.w );
+                vol.store< T >( x, z * ny + y, { acc.x, acc.y, acc.z, e } );
+            }
+        }
+}
+
+// Random.h:243-251 wellonsLowBias32, 280-287 murmurHash33, 202-208 + 289-300 getRandomSeed
+uint32_t wellons_lowbias32( uint32_t x )
+{
+    x ^= x >> 16;
+    x *= 0x7feb352du;
+    x ^= x >> 15;
+    x *= 0x846ca68bu;
+    x ^= x >> 16;
+    return x;
+}
+void murmur_hash33( const uint32_t in[ 3 ], uint32_t h[ 3 ] )
+{
+    const uint32_t M      = 0x5bd1e995u;
+    uint32_t       src[3] = { in[ 0 ], in[ 1 ], in[ 2 ] };
+    h[ 0 ] = 1190494759u, h[ 1 ] = 2147483647u, h[ 2 ] = 3559788179u;
+    for( int c = 0; c < 3; c++ )
+    {
+        src[ c ] *= M;
+        src[ c ] ^= src[ c ] >> 24;
+        src[ c ] *= M;
+    }
+    for( int k = 0; k < 3; k++ )
+        for( int c = 0; c < 3; c++ )
+        {
+            h[ c ] *= M;
+            h[ c ] ^= src[ k ];
+        }
+    for( int c = 0; c < 3; c++ )
+    {
+        h[ c ] ^= h[ c ] >> 13;
+        h[ c ] *= M;
+        h[ c ] ^= h[ c ] >> 15;
+    }
+}
+uint32_t random_seed( int px, int py, uint32_t frame )
+{
+    const uint32_t in[ 3 ] = { (uint32_t)px, (uint32_t)py, frame };
+    uint32_t       h[ 3 ];
+    murmur_hash33( in, h );
+    return ( ( h[ 2 ] % 128u ) << 14 ) | ( ( h[ 1 ] % 128u ) << 7 ) | ( h[ 0 ] % 128u );
+}
+
+// floor()ed coordinate to an index: NaN to 0, saturated beyond 2^30
+template< class T > int safe_floor_int( T f ) { return f == f ? (int)std::min( std::max( f, (T)-1073741824.0 ), (T)1073741824.0 ) : 0; }
+
+template< class T > V4< T > mat_mul_t( const T* m, V4< T > v )
+{
+    V4< T > r;
+    T*      rp = &r.x;
+    for( int row = 0; row < 4; row++ ) rp[ row ] = m[ row ] * v.x + m[ 4 + row ] * v.y + m[ 8 + row ] * v.z + m[ 12 + row ] * v.w;
+    return r;
+}
+template< class T > V4< T > vmix4( V4< T > x, V4< T > y, T a ) { return { gmix( x.x, y.x, a ), gmix( x.y, y.y, a ), gmix( x.z, y.z, a ), gmix( x.w, y.w, a ) }; }
+
+template< class T > struct Scatter
+{
+    Stream&                       s;
+    uint32_t                      fi;
+    const rgdn_volumetric_params& p;
+    T                             invViewProj[ 16 ], viewProj[ 16 ];
+
+    Scatter( Stream& st, uint32_t f, const rgdn_volumetric_params& pp ) : s( st ), fi( f ), p( pp )
+    {
+        // invView * invProjection (CmScatterAccum.comp:55), each element summed over k in order
+        for( int c = 0; c < 4; c++ )
+            for( int r = 0; r < 4; r++ )
+            {
+                T acc = (T)p.invView[ r ] * (T)p.invProjection[ c * 4 ];
+                for( int k = 1; k < 4; k++ ) acc = acc + (T)p.invView[ k * 4 + r ] * (T)p.invProjection[ c * 4 + k ];
+                invViewProj[ c * 4 + r ] = acc;
+            }
+        for( int k = 0; k < 16; k++ ) viewProj[ k ] = (T)p.volumeViewProj[ k ];
+    }
+
+    // textureLod of the volume, linear clamp-to-edge: x, then y, then z
+    V4< T > trilinear( V3< T > sp )
+    {
+        Plane&    vol = s.cur( RGDN_FB_SCATTER_VOLUME, fi );
+        const int n[ 3 ] = { RGDN_VOLUME_SIZE_X, RGDN_VOLUME_SIZE_Y, RGDN_VOLUME_SIZE_Z };
+        const T   u[ 3 ] = { sp.x, sp.y, sp.z };
+        int       i0[ 3 ], i1[ 3 ];
+        T         f[ 3 ];
+        for( int d = 0; d < 3; d++ )
+        {
+            const T x  = u[ d ] * (T)n[ d ] - K( 0.5 );
+            const T fx = o_floor( x );
+            const int ix = safe_floor_int( fx );
+            i0[ d ] = std::min( std::max( ix, 0 ), n[ d ] - 1 );
+            i1[ d ] = std::min( std::max( ix, -1 ) + 1, n[ d ] - 1 );
+            f[ d ]  = x - fx;
+        }
+        auto t = [ & ]( int x, int y, int z ) { return vol.fetch< T >( x, z * n[ 1 ] + y ); };
+        const V4< T > c00 = vmix4( t( i0[ 0 ], i0[ 1 ], i0[ 2 ] ), t( i1[ 0 ], i0[ 1 ], i0[ 2 ] ), f[ 0 ] );
+        const V4< T > c10 = vmix4( t( i0[ 0 ], i1[ 1 ], i0[ 2 ] ), t( i1[ 0 ], i1[ 1 ], i0[ 2 ] ), f[ 0 ] );
+        const V4< T > c01 = vmix4( t( i0[ 0 ], i0[ 1 ], i1[ 2 ] ), t( i1[ 0 ], i0[ 1 ], i1[ 2 ] ), f[ 0 ] );
+        const V4< T > c11 = vmix4( t( i0[ 0 ], i1[ 1 ], i1[ 2 ] ), t( i1[ 0 ], i1[ 1 ], i1[ 2 ] ), f[ 0 ] );
+        return vmix4( vmix4( c00, c10, f[ 1 ] ), vmix4( c01, c11, f[ 1 ] ), f[ 2 ] );
+    }
+
+    // volume_toSamplePosition_T (Volumetric.h:38-58), VOLUMETRIC_DISTANCE_POW 1
+    V3< T > sample_pos( V3< T > w )
+    {
+        const V4< T > ndc = mat_mul_t( viewProj, V4< T >{ w.x, w.y, w.z, (T)1 } );
+        const T       nx = ndc.x / ndc.w, ny = ndc.y / ndc.w;
+        const T       dx = w.x - (T)p.cameraPosition[ 0 ], dy = w.y - (T)p.cameraPosition[ 1 ], dz = w.z - (T)p.cameraPosition[ 2 ];
+        const T       dist = o_sqrt( dx * dx + dy * dy + dz * dz );
+        const T       z    = gclamp( ( dist - (T)p.volumeCameraNear ) / ( (T)p.volumeCameraFar - (T)p.volumeCameraNear ), (T)0, (T)1 );
+        return { nx * K( 0.5 ) + K( 0.5 ), ny * K( 0.5 ) + K( 0.5 ), z };
+    }
+
+    // fializeScattering (CmScatterAccum.comp:41-95)
+    V4< T > finalize( int rx, int ry, T depthCb )
+    {
+        if( p.volumeEnableType == RGDN_VOLUME_ENABLE_VOLUMETRIC )
+        {
+            const T       sx  = (T)rx / (T)(float)s.W, sy = (T)ry / (T)(float)s.H;
+            const T       dn  = s.cur( RGDN_FB_DEPTH_NDC, fi ).fetch< T >( rx, ry ).x;
+            const V4< T > wp  = mat_mul_t( invViewProj, V4< T >{ sx * K( 2.0 ) - K( 1.0 ), sy * K( 2.0 ) - K( 1.0 ), dn, (T)1 } );
+            const V3< T > pos = { wp.x / wp.w, wp.y / wp.w, wp.z / wp.w };
+            const uint32_t rnd = wellons_lowbias32( random_seed( rx, ry, p.frameId ) );   // rnd8_4( seed, 0 )
+            const T        r0 = (T)( rnd & 0xFFu ) / K( 255.0 ), r1 = (T)( ( rnd >> 8 ) & 0xFFu ) / K( 255.0 );
+            const T        r2 = (T)( ( rnd >> 16 ) & 0xFFu ) / K( 255.0 );
+            // sampleHemisphere (Random.h:73-92), unitBasis = -offset
+            const T u1 = r0 * K( 0.99 ), u2 = r1 * K( 0.99 );
+            const T rr = o_sqrt( u1 ), hz = o_sqrt( (T)1 - u1 );
+            const T phi = ( K( 2.0 ) * K( 3.14159265358979 ) ) * u2;
+            const V3< T > basis = { -( rr * (T)std::cos( phi ) ), -( rr * (T)std::sin( phi ) ), -hz };
+            // volume_sampleDithered (Volumetric.h:92-104), dither radius 2
+            V3< T >  sp = sample_pos( pos );
+            const T  k  = r2 * K( 2.0 );
+            sp          = { sp.x + ( k * basis.x ) / (T)RGDN_VOLUME_SIZE_X, sp.y + ( k * basis.y ) / (T)RGDN_VOLUME_SIZE_Y,
+                            sp.z + ( k * basis.z ) / (T)RGDN_VOLUME_SIZE_Z };
+            return trilinear( sp );
+        }
+        if( p.volumeEnableType == RGDN_VOLUME_ENABLE_SIMPLE )
+        {
+            if( depthCb > (T)MAX_RAY_LENGTH ) return { 0, 0, 0, 1 };
+            const T density = (T)( p.volumeScattering * 0.00005f );
+            const T f       = o_exp( -depthCb * density );
+            return { (T)p.volumeAmbient[ 0 ] * ( (T)1 - f ), (T)p.volumeAmbient[ 1 ] * ( (T)1 - f ), (T)p.volumeAmbient[ 2 ] * ( (T)1 - f ), f };
+        }
+        return { 0, 0, 0, 1 };
+    }
+
+    // CmScatterAccum.comp:97-161
+    void accumulate()
+    {
+        const int W = s.W, H = s.H, sep = W / 2;
+        const T   sxs = (T)(float)s.W / K( 2.0 ), sys = (T)(float)s.H;
+        const T   isx = (T)1 / sxs, isy = (T)1 / sys;
+        Plane &   motion = s.cur( RGDN_FB_MOTION, fi ), &depthC = s.cur( RGDN_FB_DEPTH_WORLD, fi ), &depthP = s.prv( RGDN_FB_DEPTH_WORLD, fi );
+        Plane &   nrmC = s.cur( RGDN_FB_NORMAL, fi ), &nrmP = s.prv( RGDN_FB_NORMAL, fi );
+        Plane &   scP = s.prv( RGDN_FB_SCATTERING, fi ), &hP = s.prv( RGDN_FB_SCATTERING_HISTORY, fi );
+        Plane &   scC = s.cur( RGDN_FB_SCATTERING, fi ), &hC = s.cur( RGDN_FB_SCATTERING_HISTORY, fi );
+        auto      regular = [ & ]( int cx, int cy ) {
+            const int isOdd = cx >= sep ? 1 : 0, x = cx - isOdd * sep;
+            return V2< int >{ x * 2 + ( isOdd + cy ) % 2, cy };
+        };
+        for( int cy = 0; cy < H; cy++ )
+            for( int cx = 0; cx < W; cx++ )
+            {
+                const V4< T > mo     = motion.fetch< T >( cx, cy );
+                const T       depth  = depthC.fetch< T >( cx, cy ).x;
+                const V3< T > normal = decode_normal< T >( nrmC.raw_u32( cx, cy ) );
+                // getPrevScreenPos (ShaderCommonGLSLFunc.h:271-277)
+                const T  ppx = ( ( (T)cx + K( 0.5 ) ) * isx + mo.x ) * sxs, ppy = ( ( (T)cy + K( 0.5 ) ) * isy + mo.y ) * sys;
+                const T  fpx = o_floor( ppx - K( 0.5 ) ), fpy = o_floor( ppy - K( 0.5 ) );
+                const int px = safe_floor_int( fpx ), py = safe_floor_int( fpy );
+                const T  sx = ( ppx - K( 0.5 ) ) - fpx, sy = ( ppy - K( 0.5 ) ) - fpy;
+                const T  bw[ 2 ][ 2 ] = { { ( (T)1 - sx ) * ( (T)1 - sy ), sx * ( (T)1 - sy ) }, { ( (T)1 - sx ) * sy, sx * sy } };
+                const int isOdd = cx >= sep ? 1 : 0, al = isOdd * sep, ar = ( isOdd + 1 ) * sep;
+                V4< T >  acc = { 0, 0, 0, 0 };
+                T        hist = 0, wsum = 0;
+                for( int yy = 0; yy <= 1; yy++ )
+                    for( int xx = 0; xx <= 1; xx++ )
+                    {
+                        const int qx = px + xx, qy = py + yy;
+                        if( !( qy >= 0 && qy < H && qx >= al && qx < ar ) ) continue;
+                        const T       dP = depthP.fetch< T >( qx, qy ).x;
+                        const V3< T > nP = decode_normal< T >( nrmP.raw_u32( qx, qy ) );
+                        if( o_abs( depth - dP + mo.z ) / o_abs( depth ) < K( 0.1 ) && dot3( normal, nP ) > K( 0.95 ) )
+                        {
+                            const T         w = bw[ yy ][ xx ];
+                            const V2< int > r = regular( qx, qy );
+                            const V4< T >   v = scP.fetch< T >( r.x, r.y );
+                            acc               = { acc.x + w * v.x, acc.y + w * v.y, acc.z + w * v.z, acc.w + w * v.w };
+                            hist              = hist + w * hP.fetch< T >( r.x, r.y ).x;
+                            wsum              = wsum + w;
+                        }
+                    }
+                const bool ok = wsum > K( 0.0001 );
+                hist          = ok ? hist / wsum : (T)0;
+                acc           = ok ? V4< T >{ acc.x / wsum, acc.y / wsum, acc.z / wsum, acc.w / wsum } : V4< T >{ 0, 0, 0, 0 };
+                hist          = gclamp( hist + (T)1, (T)1, o_fmax( (T)1, (T)p.maxHistoryLength ) );
+                const V2< int > reg = regular( cx, cy );
+                acc                 = vmix4( acc, finalize( reg.x, reg.y, depth ), (T)1 / hist );
+                scC.store< T >( reg.x, reg.y, acc );
+                hC.store< T >( reg.x, reg.y, { hist, 0, 0, 0 } );
+            }
+    }
+};
+
 }  // namespace orc
 
 // ============================================================================================
@@ -1761,6 +1996,27 @@ int orc_prepare_final( orc_stream* o, uint32_t frameIndex, const rgdn_final_para
     else orc::prepare_final< float >( o->s, frameIndex & 1, *p, nthreads );
     return RGDN_SUCCESS;
 }
+
+// Volumetric::ProcessScattering
+int orc_process_scattering( orc_stream* o, uint32_t frameIndex, const rgdn_volumetric_params* p )
+{
+    if( !o || !p ) return RGDN_WRONG_INSTANCE;
+    const uint32_t fi = frameIndex & 1;
+    if( o->s.mode == orc::M_F64 )
+    {
+        orc::volume_process< double >( o->s, fi );
+        orc::Scatter< double >( o->s, fi, *p ).accumulate();
+    }
+    else
+    {
+        orc::volume_process< float >( o->s, fi );
+        orc::Scatter< float >( o->s, fi, *p ).accumulate();
+    }
+    return RGDN_SUCCESS;
+}
+// getRandomSeed + rnd8_4 (for the known-answer tests)
+uint32_t orc_random_seed( int x, int y, uint32_t frame ) { return orc::random_seed( x, y, frame ); }
+uint32_t orc_wellons_lowbias32( uint32_t x ) { return orc::wellons_lowbias32( x ); }
 
 // Bloom::Prepare + Apply
 int orc_bloom( orc_stream* o, uint32_t frameIndex, float intensity )

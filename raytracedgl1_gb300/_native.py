@@ -35,6 +35,7 @@ FB_NAMES = [
     "SCREEN_EMIS_RT", "SCATTERING", "FINAL", "BLOOM_INPUT",
     "BLOOM_MIP1", "BLOOM_MIP2", "BLOOM_MIP3", "BLOOM_MIP4", "BLOOM_MIP5", "BLOOM_MIP6", "BLOOM_MIP7",
     "BLOOM_MIP8", "BLOOM_RESULT",
+    "DEPTH_NDC", "SCATTERING_HISTORY", "SCATTER_VOLUME",
 ]
 FB = {n: i for i, n in enumerate(FB_NAMES)}
 FB_COUNT = len(FB_NAMES)
@@ -82,6 +83,20 @@ FINAL_APPLY_SCATTERING = 0x1
 class BloomParams(C.Structure):
     """rgdn_bloom_params."""
     _fields_ = [("bloomIntensity", C.c_float)]
+
+
+VOLUME_SIZE = (160, 88, 64)   # RGDN_VOLUME_SIZE_X, _Y, _Z
+VOLUME_ENABLE_NONE, VOLUME_ENABLE_SIMPLE, VOLUME_ENABLE_VOLUMETRIC = 0, 1, 2
+
+
+class VolumetricParams(C.Structure):
+    """rgdn_volumetric_params: the GlobalUniform fields of Volumetric::ProcessScattering."""
+    _fields_ = [
+        ("invView", C.c_float * 16), ("invProjection", C.c_float * 16), ("volumeViewProj", C.c_float * 16),
+        ("cameraPosition", C.c_float * 4), ("volumeCameraNear", C.c_float), ("volumeCameraFar", C.c_float),
+        ("volumeAmbient", C.c_float * 3), ("volumeScattering", C.c_float), ("maxHistoryLength", C.c_float),
+        ("volumeEnableType", C.c_uint32), ("frameId", C.c_uint32),
+    ]
 
 
 class FrameParams(C.Structure):
@@ -182,6 +197,7 @@ SIGNATURES = [
     ("rgdn_calculate_exposure", _I, [_VP, _U32, _PFP, _VP]),
     ("rgdn_prepare_final", _I, [_VP, _U32, C.POINTER(FinalParams), _VP]),
     ("rgdn_bloom", _I, [_VP, _U32, C.POINTER(BloomParams), _VP]),
+    ("rgdn_process_scattering", _I, [_VP, _U32, C.POINTER(VolumetricParams), _VP]),
     ("rgdn_denoise_stage", _I, [_VP, _U32, _U32, _U32, _PFP, _VP]),
     ("rgdn_stream_tonemapping_device", _I, [_VP, C.POINTER(_VP)]),
     ("rgdn_get_tonemapping", _I, [_VP, C.POINTER(_U32), C.POINTER(C.c_float), C.POINTER(C.c_float), _VP]),
@@ -220,7 +236,8 @@ KERNEL_NAMES.update({100: "atrous_fast", 101: "atrous_fast_hist", 102: "temporal
                      103: "anti_firefly_fast", 104: "variance_fast", 106: "atrous_exact_hist",
                      107: "atrous_exact", 108: "temporal_exact_geom", 109: "variance_exact_geom",
                      110: "temporal_fast_gp", 111: "temporal_exact_geom_gp", 112: "atrous_tma",
-                     113: "atrous_tma_hist", 114: "prepare_final", 115: "bloom"})
+                     113: "atrous_tma_hist", 114: "prepare_final", 115: "bloom",
+                     116: "volume_process", 117: "process_scattering"})
 
 _lib = None
 

@@ -75,6 +75,7 @@ struct FbDesc
     bool     prev;
     bool     third;
     int      shift = 0;   // bloom mips: ((W+1) >> shift) x ((H+1) >> shift), at least 1
+    uint32_t fixedW = 0, fixedH = 0;   // a size independent of the render size (the froxel volume)
 };
 
 uint32_t format_bytes( uint32_t f )
@@ -148,7 +149,11 @@ FbDesc fb_desc( uint32_t fb, uint32_t storage )
         case RGDN_FB_DIFF_PING_VARIANCE:
         case RGDN_FB_DIFF_PONG_VARIANCE: return { varpl, false, false };
         case RGDN_FB_SCREEN_EMIS_RT: return { RGDN_FORMAT_B10G11R11_UFLOAT, false, false };
-        case RGDN_FB_SCATTERING: return { RGDN_FORMAT_RGBA16_SFLOAT, false, false };
+        case RGDN_FB_SCATTERING: return { RGDN_FORMAT_RGBA16_SFLOAT, true, false };
+        case RGDN_FB_DEPTH_NDC: return { RGDN_FORMAT_R32_SFLOAT, false, false };
+        case RGDN_FB_SCATTERING_HISTORY: return { RGDN_FORMAT_R16_SFLOAT, true, false };
+        case RGDN_FB_SCATTER_VOLUME:
+            return { RGDN_FORMAT_RGBA16_SFLOAT, true, false, 0, RGDN_VOLUME_SIZE_X, RGDN_VOLUME_SIZE_Y * RGDN_VOLUME_SIZE_Z };
         case RGDN_FB_FINAL:
         case RGDN_FB_BLOOM_INPUT:
         case RGDN_FB_BLOOM_RESULT: return { pre, false, false };
@@ -217,6 +222,7 @@ size_t stream_layout( uint32_t W, uint32_t H, uint32_t storage, PlaneSlot* plane
         if( d.format == RGDN_FORMAT_NONE ) continue;
         uint32_t w = d.third ? GW : W, h = d.third ? GH : H;
         if( d.shift ) w = std::max( 1u, ( W + 1 ) >> d.shift ), h = std::max( 1u, ( H + 1 ) >> d.shift );
+        if( d.fixedW ) w = d.fixedW, h = d.fixedH;
         size_t   sz = (size_t)w * h * texel;
         for( int s = 0; s < ( d.prev ? 2 : 1 ); s++ )
         {
@@ -877,7 +883,8 @@ rgdn_status rgdn_stream_get_framebuffer( rgdn_stream* s, uint32_t fb, uint32_t f
 rgdn_status rgdn_stream_bind_framebuffer( rgdn_stream* s, uint32_t fb, uint32_t frameIndex, void* devicePtr )
 {
     if( !valid_stream( s ) ) return RGDN_WRONG_INSTANCE;
-    const bool producerPlane = fb <= RGDN_FB_GRADIENT_RESHADED || fb == RGDN_FB_SCREEN_EMIS_RT || fb == RGDN_FB_SCATTERING;
+    const bool producerPlane = fb <= RGDN_FB_GRADIENT_RESHADED || fb == RGDN_FB_SCREEN_EMIS_RT || fb == RGDN_FB_SCATTERING ||
+                               fb == RGDN_FB_DEPTH_NDC || fb == RGDN_FB_SCATTER_VOLUME;
     if( !producerPlane || frameIndex > 1 || ( (uintptr_t)devicePtr & 15u ) ) return RGDN_WRONG_FUNCTION_ARGUMENT;
     PlaneSlot& p    = s->planes[ fb ];
     const int  slot = p.prev ? (int)frameIndex : 0;
@@ -957,6 +964,81 @@ rgdn_status rgdn_bloom( rgdn_stream* s, uint32_t frameIndex, const rgdn_bloom_pa
     {
         cudaEventRecord( eb, st );
         s->pending.push_back( { KF_BLOOM, 0, ea, eb } );
+    }
+    return cuda_status( e );
+}
+
+// GLSL mat4 * mat4 (column-major), each element summed over k = 0..3 in FP32 without
+// contraction: CmScatterAccum.comp:55 evaluates invView * invProjection before the vector
+static void mat4_mul_f32( const float* a, const float* b, float* out )
+{
+    for( int c = 0; c < 4; c++ )
+        for( int r = 0; r < 4; r++ )
+        {
+            volatile float acc = a[ 0 * 4 + r ] * b[ c * 4 + 0 ];
+            for( int k = 1; k < 4; k++ )
+            {
+                volatile float prod = a[ k * 4 + r ] * b[ c * 4 + k ];
+                acc                 = acc + prod;
+            }
+            out[ c * 4 + r ] = acc;
+        }
+}
+
+rgdn_status rgdn_process_scattering( rgdn_stream* s, uint32_t frameIndex, const rgdn_volumetric_params* p, rgdn_cuda_stream cs )
+{
+    if( !valid_stream( s ) ) return RGDN_WRONG_INSTANCE;
+    if( !p || frameIndex > 1 || p->volumeEnableType > RGDN_VOLUME_ENABLE_VOLUMETRIC || !std::isfinite( p->maxHistoryLength ) )
+        return RGDN_WRONG_FUNCTION_ARGUMENT;
+    if( p->volumeEnableType == RGDN_VOLUME_ENABLE_VOLUMETRIC && !( p->volumeCameraFar > p->volumeCameraNear ) ) return RGDN_WRONG_FUNCTION_ARGUMENT;
+    cudaSetDevice( s->ctx->device );
+    ScatterArgs a = {};
+    a.u.W         = (int)s->W;
+    a.u.H         = (int)s->H;
+    a.u.rw        = (float)s->W;
+    a.u.rh        = (float)s->H;
+    a.u.isx       = 1.0f / ( a.u.rw / 2.0f );
+    a.u.isy       = 1.0f / a.u.rh;
+    a.volume      = (ushort4*)plane_ptr_mut( s, RGDN_FB_SCATTER_VOLUME, frameIndex );
+    a.nx          = RGDN_VOLUME_SIZE_X;
+    a.ny          = RGDN_VOLUME_SIZE_Y;
+    a.nz          = RGDN_VOLUME_SIZE_Z;
+    a.motion      = (const ushort4*)plane_ptr( s, RGDN_FB_MOTION, frameIndex );
+    a.depth       = (const uint16_t*)plane_ptr( s, RGDN_FB_DEPTH_WORLD, frameIndex );
+    a.depthPrev   = (const uint16_t*)plane_ptr( s, RGDN_FB_DEPTH_WORLD, frameIndex ^ 1 );
+    a.normal      = (const uint32_t*)plane_ptr( s, RGDN_FB_NORMAL, frameIndex );
+    a.normalPrev  = (const uint32_t*)plane_ptr( s, RGDN_FB_NORMAL, frameIndex ^ 1 );
+    a.depthNdc    = (const float*)plane_ptr( s, RGDN_FB_DEPTH_NDC, frameIndex );
+    a.scatterPrev = (const ushort4*)plane_ptr( s, RGDN_FB_SCATTERING, frameIndex ^ 1 );
+    a.historyPrev = (const uint16_t*)plane_ptr( s, RGDN_FB_SCATTERING_HISTORY, frameIndex ^ 1 );
+    a.scatterOut  = (ushort4*)plane_ptr_mut( s, RGDN_FB_SCATTERING, frameIndex );
+    a.historyOut  = (uint16_t*)plane_ptr_mut( s, RGDN_FB_SCATTERING_HISTORY, frameIndex );
+    a.phiTab      = s->ctx->phiTab;
+    a.thetaTab    = s->ctx->thetaTab;
+    mat4_mul_f32( p->invView, p->invProjection, a.invViewProj );
+    memcpy( a.volumeViewProj, p->volumeViewProj, sizeof( a.volumeViewProj ) );
+    for( int k = 0; k < 3; k++ ) a.camPos[ k ] = p->cameraPosition[ k ], a.ambient[ k ] = p->volumeAmbient[ k ];
+    a.volNear          = p->volumeCameraNear;
+    a.volFar           = p->volumeCameraFar;
+    a.density          = p->volumeScattering * 0.00005f;
+    a.maxHistoryLength = p->maxHistoryLength;
+    a.enableType       = p->volumeEnableType;
+    a.frameId          = p->frameId;
+    cudaStream_t st = (cudaStream_t)cs;
+    cudaEvent_t  ea = nullptr, eb = nullptr;
+    if( s->timing )
+    {
+        ea = take_event( s );
+        eb = take_event( s );
+        if( !ea || !eb ) return RGDN_DEVICE_ERROR;
+        cudaEventRecord( ea, st );
+    }
+    const cudaError_t e = launch_process_scattering( a, st );
+    s->ctx->launches.fetch_add( 2, std::memory_order_relaxed );
+    if( s->timing )
+    {
+        cudaEventRecord( eb, st );
+        s->pending.push_back( { KF_SCATTER_ACCUM, 0, ea, eb } );
     }
     return cuda_status( e );
 }

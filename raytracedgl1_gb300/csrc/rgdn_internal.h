@@ -168,6 +168,37 @@ cudaError_t launch_bloom_ref( const BloomArgs& b, cudaStream_t s );
 cudaError_t launch_bloom_f32( const BloomArgs& b, cudaStream_t s );
 cudaError_t launch_bloom_f16( const BloomArgs& b, cudaStream_t s );
 cudaError_t launch_bloom_bf16( const BloomArgs& b, cudaStream_t s );
+// Volumetric::ProcessScattering: the froxel volume (RGBA16F, nx x (ny * nz) texels, z-major
+// slices) integrated in place, then the screen-space accumulation. Fixed formats: the same
+// kernels serve every storage mode.
+struct ScatterArgs
+{
+    Uniform        u;                 // W, H, rw, rh, isx, isy
+    ushort4*       volume;            // SCATTER_VOLUME[frameIndex], processed in place
+    int            nx, ny, nz;
+    const ushort4* motion;            // checkerboard layout
+    const uint16_t* depth;            // DEPTH_WORLD cur / prev, checkerboard layout
+    const uint16_t* depthPrev;
+    const uint32_t* normal;           // NORMAL cur / prev, checkerboard layout
+    const uint32_t* normalPrev;
+    const float*   depthNdc;          // regular layout
+    const ushort4* scatterPrev;       // SCATTERING prev, regular layout
+    const uint16_t* historyPrev;      // SCATTERING_HISTORY prev, regular layout
+    ushort4*       scatterOut;        // SCATTERING cur
+    uint16_t*      historyOut;        // SCATTERING_HISTORY cur
+    const float2*  phiTab;            // normal decode tables
+    const float2*  thetaTab;
+    float          invViewProj[ 16 ]; // invView * invProjection, column-major (FP32 on the host)
+    float          volumeViewProj[ 16 ];
+    float          camPos[ 3 ];
+    float          volNear, volFar;
+    float          ambient[ 3 ];
+    float          density;           // volumeScattering * 0.00005
+    float          maxHistoryLength;
+    uint32_t       enableType;
+    uint32_t       frameId;
+};
+cudaError_t launch_process_scattering( const ScatterArgs& a, cudaStream_t s );
 cudaError_t launch_final_ref( const FinalArgs& f, cudaStream_t s );
 cudaError_t launch_final_f32( const FinalArgs& f, cudaStream_t s );
 cudaError_t launch_final_f16( const FinalArgs& f, cudaStream_t s );
@@ -191,6 +222,8 @@ enum FusedKernel : int
     KF_ATROUS_TMA_HIST     = 113,  // TMA-staged last iteration + fused histogram (timing label)
     KF_PREPARE_FINAL       = 114,  // exposure, tonemapping and bloom input (timing label)
     KF_BLOOM               = 115,  // the bloom pyramid and its application (timing label)
+    KF_VOLUME_PROCESS      = 116,  // froxel columns integrated front to back (timing label)
+    KF_SCATTER_ACCUM       = 117,  // screen-space scattering accumulation (timing label)
 };
 
 // Launches one stage for one frame. Returns the CUDA error of the launch.

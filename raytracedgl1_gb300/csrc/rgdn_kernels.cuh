@@ -2915,6 +2915,221 @@ template< int M > __global__ void __launch_bounds__( 256 ) k_bloom_apply( const 
     Sto< M >::stpre( finalImg, i, f3of( padd( bloom_ld< M >( finalImg, i ), bloom ) ) );
 }
 
+// ==========================================================================================
+// Volumetric::ProcessScattering: CmVolumetricProcess.comp and CmScatterAccum.comp
+// ==========================================================================================
+__device__ __forceinline__ float4 h4f( ushort4 h ) { return make_float4( h2f( h.x ), h2f( h.y ), h2f( h.z ), h2f( h.w ) ); }
+__device__ __forceinline__ ushort4 f4h( float4 v ) { return make_ushort4( f32_to_f16( v.x ), f32_to_f16( v.y ), f32_to_f16( v.z ), f32_to_f16( v.w ) ); }
+__device__ __forceinline__ float4 vmix4( float4 x, float4 y, float a )
+{
+    return make_float4( gmix( x.x, y.x, a ), gmix( x.y, y.y, a ), gmix( x.z, y.z, a ), gmix( x.w, y.w, a ) );
+}
+
+// CmVolumetricProcess.comp:58-79 (accumulateScattering, store): one thread per froxel column,
+// front to back. The running (light, extinction) stays in FP32; cell z stores
+// (light, exp(-extinction)) over the cell's own (in-scatter, extinction), which it has read.
+template< int M > __global__ void __launch_bounds__( 128 ) k_volume_process( ushort4* vol, int nx, int ny, int nz )
+{
+    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
+    pdl_launch_dependents();
+    pdl_wait();
+    if( x >= nx || y >= ny ) return;
+    const size_t  slice = (size_t)nx * ny;
+    ushort4*      col   = vol + (size_t)y * nx + x;
+    // The column is walked in chunks of VP cells, the next chunk's loads issued before the
+    // current chunk's stores: every cell is still read before it is written, and the loads of a
+    // chunk are in flight together instead of one per step.
+    constexpr int VP = 8;
+    ushort4       cur[ VP ], nxt[ VP ];
+#pragma unroll
+    for( int j = 0; j < VP; j++ ) cur[ j ] = j < nz ? col[ j * slice ] : make_ushort4( 0, 0, 0, 0 );
+    float4 acc = make_float4( 0.0f, 0.0f, 0.0f, 0.0f );
+    float  e   = 1.0f;
+    for( int z0 = 0; z0 < nz; z0 += VP )
+    {
+#pragma unroll
+        for( int j = 0; j < VP; j++ ) nxt[ j ] = z0 + VP + j < nz ? col[ ( z0 + VP + j ) * slice ] : make_ushort4( 0, 0, 0, 0 );
+#pragma unroll
+        for( int j = 0; j < VP; j++ )
+        {
+            const int z = z0 + j;
+            if( z >= nz ) break;
+            const float4 v = h4f( cur[ j ] );
+            if( z == 0 ) acc = v;
+            else
+            {
+                const float t = gsat( e );   // saturate( exp( -front.a ) )
+                acc           = make_float4( acc.x + t * v.x, acc.y + t * v.y, acc.z + t * v.z, acc.w + v.w );
+            }
+            e                = expf( -acc.w );
+            col[ z * slice ] = f4h( make_float4( acc.x, acc.y, acc.z, e ) );
+        }
+#pragma unroll
+        for( int j = 0; j < VP; j++ ) cur[ j ] = nxt[ j ];
+    }
+}
+
+// murmurHash33 (Random.h:280-287), the published MurmurHash2 mixing on three lanes
+__device__ __forceinline__ uint3 murmur_hash33( uint3 src )
+{
+    const uint32_t M = 0x5bd1e995u;
+    uint3          h = make_uint3( 1190494759u, 2147483647u, 3559788179u );
+    src              = make_uint3( src.x * M, src.y * M, src.z * M );
+    src              = make_uint3( src.x ^ ( src.x >> 24 ), src.y ^ ( src.y >> 24 ), src.z ^ ( src.z >> 24 ) );
+    src              = make_uint3( src.x * M, src.y * M, src.z * M );
+    auto mulx        = [ & ]( uint32_t k ) {
+        h = make_uint3( h.x * M, h.y * M, h.z * M );
+        h = make_uint3( h.x ^ k, h.y ^ k, h.z ^ k );
+    };
+    mulx( src.x );
+    mulx( src.y );
+    mulx( src.z );
+    h = make_uint3( h.x ^ ( h.x >> 13 ), h.y ^ ( h.y >> 13 ), h.z ^ ( h.z >> 13 ) );
+    h = make_uint3( h.x * M, h.y * M, h.z * M );
+    return make_uint3( h.x ^ ( h.x >> 15 ), h.y ^ ( h.y >> 15 ), h.z ^ ( h.z >> 15 ) );
+}
+// Chris Wellons' lowbias32 (Random.h:243-251)
+__device__ __forceinline__ uint32_t wellons_lowbias32( uint32_t x )
+{
+    x ^= x >> 16;
+    x *= 0x7feb352du;
+    x ^= x >> 15;
+    x *= 0x846ca68bu;
+    x ^= x >> 16;
+    return x;
+}
+// getRandomSeed + packRandomSeed (Random.h:202-208, 289-300): 128 blue-noise layers of 128x128
+__device__ __forceinline__ uint32_t random_seed( int px, int py, uint32_t frame )
+{
+    const uint3 h = murmur_hash33( make_uint3( (uint32_t)px, (uint32_t)py, frame ) );
+    return ( ( h.z % 128u ) << 14 ) | ( ( h.y % 128u ) << 7 ) | ( h.x % 128u );
+}
+
+// an index from a floor()ed coordinate: NaN to 0, magnitudes beyond 2^30 saturated, so that
+// the conversion is defined for every input
+__device__ __forceinline__ int safe_floor_int( float f ) { return f == f ? (int)fminf( fmaxf( f, -1073741824.0f ), 1073741824.0f ) : 0; }
+
+// textureLod of the processed volume with the linear clamp-to-edge sampler (Volumetric.cpp:
+// 236-256): lerps along x, then y, then z, in FP32
+__device__ __forceinline__ float4 volume_trilinear( const ushort4* vol, int nx, int ny, int nz, float3 sp )
+{
+    auto axis = []( float u, int n, int& i0, int& i1, float& f ) {
+        const float x  = u * (float)n - 0.5f;
+        const float fx = floorf( x );
+        const int   ix = safe_floor_int( fx );
+        i0             = min( max( ix, 0 ), n - 1 );
+        i1             = min( max( ix, -1 ) + 1, n - 1 );
+        f              = x - fx;
+    };
+    int   x0, x1, y0, y1, z0, z1;
+    float fx, fy, fz;
+    axis( sp.x, nx, x0, x1, fx );
+    axis( sp.y, ny, y0, y1, fy );
+    axis( sp.z, nz, z0, z1, fz );
+    auto t = [ & ]( int x, int y, int z ) { return h4f( vol[ ( (size_t)z * ny + y ) * nx + x ] ); };
+    const float4 c00 = vmix4( t( x0, y0, z0 ), t( x1, y0, z0 ), fx ), c10 = vmix4( t( x0, y1, z0 ), t( x1, y1, z0 ), fx );
+    const float4 c01 = vmix4( t( x0, y0, z1 ), t( x1, y0, z1 ), fx ), c11 = vmix4( t( x0, y1, z1 ), t( x1, y1, z1 ), fx );
+    return vmix4( vmix4( c00, c10, fy ), vmix4( c01, c11, fy ), fz );
+}
+
+// volume_toSamplePosition_T (Volumetric.h:38-58) with VOLUMETRIC_DISTANCE_POW 1
+__device__ __forceinline__ float3 volume_sample_pos( const ScatterArgs& a, float3 w )
+{
+    const float4 ndc = mat_mul( a.volumeViewProj, make_float4( w.x, w.y, w.z, 1.0f ) );
+    const float  nx = ndc.x / ndc.w, ny = ndc.y / ndc.w;
+    const float  dx = w.x - a.camPos[ 0 ], dy = w.y - a.camPos[ 1 ], dz = w.z - a.camPos[ 2 ];
+    const float  dist = sqrtf( dx * dx + dy * dy + dz * dz );
+    const float  z    = gclamp( ( dist - a.volNear ) / ( a.volFar - a.volNear ), 0.0f, 1.0f );   // pow( z, 1 ) == z
+    return f3( nx * 0.5f + 0.5f, ny * 0.5f + 0.5f, z );
+}
+
+// fializeScattering (CmScatterAccum.comp:41-95) at regular pixel (rx, ry); depthCb is
+// DEPTH_WORLD at its checkerboard position
+__device__ __forceinline__ float4 finalize_scattering( const ScatterArgs& a, int rx, int ry, float depthCb )
+{
+    if( a.enableType == RGDN_VOLUME_ENABLE_VOLUMETRIC )
+    {
+        const float  sx  = (float)rx / a.u.rw, sy = (float)ry / a.u.rh;
+        const float4 ndc = make_float4( sx * 2.0f - 1.0f, sy * 2.0f - 1.0f, a.depthNdc[ (size_t)ry * a.u.W + rx ], 1.0f );
+        const float4 wp  = mat_mul( a.invViewProj, ndc );
+        const float3 pos = f3( wp.x / wp.w, wp.y / wp.w, wp.z / wp.w );
+        // rnd8_4( getRandomSeed( pix, frameId ), 0 ).xyz
+        const uint32_t rnd = wellons_lowbias32( random_seed( rx, ry, a.frameId ) );
+        const float    r0 = (float)( rnd & 0xFFu ) / 255.0f, r1 = (float)( ( rnd >> 8 ) & 0xFFu ) / 255.0f;
+        const float    r2 = (float)( ( rnd >> 16 ) & 0xFFu ) / 255.0f;
+        // sampleHemisphere (Random.h:73-92)
+        const float u1 = r0 * 0.99f, u2 = r1 * 0.99f;
+        const float rr = sqrtf( u1 ), phi = ( 2.0f * 3.14159265358979f ) * u2, hz = sqrtf( 1.0f - u1 );
+        const float3 basis = f3( -( rr * cosf( phi ) ), -( rr * sinf( phi ) ), -hz );
+        // volume_sampleDithered (Volumetric.h:92-104), dither radius 2
+        float3      sp = volume_sample_pos( a, pos );
+        const float k  = r2 * 2.0f;
+        sp             = f3( sp.x + ( k * basis.x ) / (float)a.nx, sp.y + ( k * basis.y ) / (float)a.ny, sp.z + ( k * basis.z ) / (float)a.nz );
+        return volume_trilinear( a.volume, a.nx, a.ny, a.nz, sp );
+    }
+    if( a.enableType == RGDN_VOLUME_ENABLE_SIMPLE )
+    {
+        if( depthCb > MAX_RAY_LENGTH ) return make_float4( 0.0f, 0.0f, 0.0f, 1.0f );
+        const float f = expf( -depthCb * a.density );
+        return make_float4( a.ambient[ 0 ] * ( 1.0f - f ), a.ambient[ 1 ] * ( 1.0f - f ), a.ambient[ 2 ] * ( 1.0f - f ), f );
+    }
+    return make_float4( 0.0f, 0.0f, 0.0f, 1.0f );
+}
+
+// CmScatterAccum.comp:97-161: one thread per checkerboard pixel
+template< int M > __global__ void __launch_bounds__( 256 ) k_scatter_accum( const ScatterArgs a )
+{
+    const int cx = blockIdx.x * blockDim.x + threadIdx.x, cy = blockIdx.y * blockDim.y + threadIdx.y;
+    pdl_launch_dependents();
+    pdl_wait();
+    if( cx >= a.u.W || cy >= a.u.H ) return;
+    const size_t  ci      = (size_t)cy * a.u.W + cx;
+    const float4  mo      = h4f( a.motion[ ci ] );
+    const float   depth   = h2f( a.depth[ ci ] );
+    auto          nrm     = [ & ]( uint32_t p ) {
+        const float2 ph = __ldg( &a.phiTab[ p >> 16 ] ), th = __ldg( &a.thetaTab[ p & 0xFFFFu ] );
+        return f3( ph.x * th.x, ph.x * th.y, ph.y );
+    };
+    const float3 normal = nrm( a.normal[ ci ] );
+    const float2 pp     = prev_screen_pos( a.u, make_float2( mo.x, mo.y ), cx, cy );
+    const float  fpx = floorf( pp.x - 0.5f ), fpy = floorf( pp.y - 0.5f );
+    const int    px = safe_floor_int( fpx ), py = safe_floor_int( fpy );
+    const float  sx = ( pp.x - 0.5f ) - fpx, sy = ( pp.y - 0.5f ) - fpy;
+    const float  bw[ 2 ][ 2 ] = { { ( 1.0f - sx ) * ( 1.0f - sy ), sx * ( 1.0f - sy ) }, { ( 1.0f - sx ) * sy, sx * sy } };
+    const Area   area = cb_area( a.u, cx );
+    float4       acc  = make_float4( 0.0f, 0.0f, 0.0f, 0.0f );
+    float        hist = 0.0f, wsum = 0.0f;
+#pragma unroll
+    for( int yy = 0; yy <= 1; yy++ )
+#pragma unroll
+        for( int xx = 0; xx <= 1; xx++ )
+        {
+            const int qx = px + xx, qy = py + yy;
+            if( !in_area( qx, qy, area ) ) continue;
+            const size_t qi = (size_t)qy * a.u.W + qx;
+            if( test_depth( depth, h2f( a.depthPrev[ qi ] ), mo.z ) && test_normal( normal, nrm( a.normalPrev[ qi ] ) ) )
+            {
+                const float  w  = bw[ yy ][ xx ];
+                const int2   r  = regular_from_cb( a.u, qx, qy );
+                const size_t ri = (size_t)r.y * a.u.W + r.x;
+                const float4 v  = h4f( a.scatterPrev[ ri ] );
+                acc             = make_float4( acc.x + w * v.x, acc.y + w * v.y, acc.z + w * v.z, acc.w + w * v.w );
+                hist            = hist + w * h2f( a.historyPrev[ ri ] );
+                wsum            = wsum + w;
+            }
+        }
+    const bool ok = wsum > 0.0001f;
+    hist          = ok ? hist / wsum : 0.0f;
+    acc           = ok ? make_float4( acc.x / wsum, acc.y / wsum, acc.z / wsum, acc.w / wsum ) : make_float4( 0.0f, 0.0f, 0.0f, 0.0f );
+    hist          = gclamp( hist + 1.0f, 1.0f, fmaxf( 1.0f, a.maxHistoryLength ) );
+    const int2   reg = regular_from_cb( a.u, cx, cy );
+    const float4 fin = finalize_scattering( a, reg.x, reg.y, depth );
+    acc              = vmix4( acc, fin, 1.0f / hist );
+    const size_t ri  = (size_t)reg.y * a.u.W + reg.x;
+    a.scatterOut[ ri ] = f4h( acc );
+    a.historyOut[ ri ] = f32_to_f16( hist );
+}
+
 }  // namespace dev
 
 
@@ -2979,6 +3194,13 @@ template< int M > cudaError_t launch_bloom_t( const BloomArgs& b, cudaStream_t s
     }
     if( e == cudaSuccess )
         e = launch_pdl( dev::k_bloom_apply< M >, grid( b.W, b.H ), blk, 0, s, (const void*)b.planes[ 9 ], b.planes[ 10 ], b.W, b.H, b.intensity );
+    return e != cudaSuccess ? e : cudaGetLastError();
+}
+
+template< int M > cudaError_t launch_scatter_t( const ScatterArgs& a, cudaStream_t s )
+{
+    cudaError_t e = launch_pdl( dev::k_volume_process< M >, dim3( ( a.nx + 31 ) / 32, ( a.ny + 3 ) / 4 ), dim3( 32, 4 ), 0, s, a.volume, a.nx, a.ny, a.nz );
+    if( e == cudaSuccess ) e = launch_pdl( dev::k_scatter_accum< M >, dim3( ( a.u.W + 31 ) / 32, ( a.u.H + 7 ) / 8 ), dim3( 32, 8 ), 0, s, a );
     return e != cudaSuccess ? e : cudaGetLastError();
 }
 

@@ -7,6 +7,11 @@ cudaError_t launch_bloom_f16( const BloomArgs& b, cudaStream_t s )
 {
     return launch_bloom_t< MODE_F16 >( b, s );
 }
+// the volumetric kernels read and write fixed formats: one instantiation serves every mode
+cudaError_t launch_process_scattering( const ScatterArgs& a, cudaStream_t s )
+{
+    return launch_scatter_t< MODE_F16 >( a, s );
+}
 cudaError_t launch_final_f16( const FinalArgs& f, cudaStream_t s )
 {
     return launch_final_t< MODE_F16 >( f, s );

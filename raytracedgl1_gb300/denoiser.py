@@ -288,6 +288,20 @@ class Bloom:
         N.check(s.lib.rgdn_bloom(s.handle, frameIndex, C.byref(p), _stream_handle(cuda_stream)), "rgdn_bloom")
 
 
+class Volumetric:
+    """Volumetric::ProcessScattering (Source/Volumetric.cpp:71-190): the froxel volume of
+    SCATTER_VOLUME integrated front to back in place, then SCATTERING and SCATTERING_HISTORY
+    accumulated over frames per pixel. Call between Denoise and CalculateExposure."""
+
+    def __init__(self, stream: Stream):
+        self.stream = stream
+
+    def ProcessScattering(self, frameIndex: int, params: N.VolumetricParams, cuda_stream=None) -> None:
+        s = self.stream
+        N.check(s.lib.rgdn_process_scattering(s.handle, frameIndex, C.byref(params), _stream_handle(cuda_stream)),
+                "rgdn_process_scattering")
+
+
 class Tonemapping:
     """Tonemapping::CalculateExposure(cmd, frameIndex, uniform) — Source/Tonemapping.cpp:59-165."""
 

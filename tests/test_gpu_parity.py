@@ -12,7 +12,7 @@ import numpy as np
 import pytest
 
 from raytracedgl1_gb300 import _native as N
-from raytracedgl1_gb300.denoiser import Bloom, Denoiser, ImageComposition, Stream, Tonemapping
+from raytracedgl1_gb300.denoiser import Bloom, Denoiser, ImageComposition, Stream, Tonemapping, Volumetric
 from raytracedgl1_gb300.scene import Scene
 
 import oracle
@@ -510,6 +510,80 @@ def test_bloom_parity(ctx, mode_name, mode, size):
         assert err.max() <= TOL[img.format], f"{name}: max rel err {err.max():.3e}"
         if img.format == F.F_RGBA32F:
             assert err.max() <= 1e-5, f"{name}: max rel err {err.max():.3e}"
+    s.close()
+
+
+def _volumetric_params(mode, frame_id):
+    """Matrices that place every pixel's world position inside the froxel volume: world =
+    NDC through a slightly skewed inverse view-projection, a volume projection with a small
+    perspective term, the camera behind the screen."""
+    p = N.VolumetricParams()
+    iv = np.eye(4, dtype=np.float32)
+    iv[3, 0] = 0.05                      # column 3 (translation) x
+    ip = np.eye(4, dtype=np.float32)
+    ip[1, 0] = 0.02                      # column 1, row 0: skew
+    vp = np.eye(4, dtype=np.float32)
+    vp[2, 3] = 0.1                       # column 2, row 3: w = 1 + 0.1 z
+    p.invView[:] = iv.reshape(-1)        # rows of this array are GLSL columns
+    p.invProjection[:] = ip.reshape(-1)
+    p.volumeViewProj[:] = vp.reshape(-1)
+    p.cameraPosition[:] = (0.0, 0.0, -1.0, 0.0)
+    p.volumeCameraNear, p.volumeCameraFar = 0.5, 3.0
+    p.volumeAmbient[:] = (0.2, 0.4, 0.8)
+    p.volumeScattering = 300.0
+    p.maxHistoryLength = 6.0
+    p.volumeEnableType = mode
+    p.frameId = frame_id
+    return p
+
+
+@pytest.mark.parametrize("vmode", [N.VOLUME_ENABLE_NONE, N.VOLUME_ENABLE_SIMPLE, N.VOLUME_ENABLE_VOLUMETRIC])
+@pytest.mark.parametrize("size", [(64, 36), (50, 23)])
+def test_process_scattering_parity(ctx, vmode, size):
+    """rgdn_process_scattering (CmVolumetricProcess + CmScatterAccum) against the oracle over
+    two frames of the synthetic scene: the volume integrated in place, then SCATTERING and
+    SCATTERING_HISTORY reprojected from the previous frame (random history on the first, the
+    first frame's output on the second) and mixed with this frame's fog or volume sample."""
+    W, H = size
+    rng = np.random.default_rng(W * 31 + H + vmode)
+    sc = Scene(W, H, seed=W + vmode)
+    s = Stream(ctx, W, H, N.STORAGE_FP16)
+    o = oracle.OracleStream(W, H, oracle.MODE_F32)
+    nz, ny, nx = N.VOLUME_SIZE[2], N.VOLUME_SIZE[1], N.VOLUME_SIZE[0]
+    for fi in (0, 1):
+        vol = np.concatenate([rng.uniform(0, 0.5, (ny * nz, nx, 3)), rng.uniform(0, 0.1, (ny * nz, nx, 1))], axis=2)
+        upload_frame(s, o, {"SCATTER_VOLUME": vol.astype(np.float16).view(np.uint16)}, fi)
+    prev = np.concatenate([rng.uniform(0, 1, (H, W, 3)), rng.uniform(0.2, 1, (H, W, 1))], axis=2)
+    upload_frame(s, o, {"SCATTERING": prev.astype(np.float16).view(np.uint16),
+                        "SCATTERING_HISTORY": rng.uniform(1, 5, (H, W)).astype(np.float16).view(np.uint16)}, 1)
+    for f in range(2):
+        fi = f & 1
+        bufs, _ = sc.generate(f)
+        upload_frame(s, o, {k: bufs[k] for k in ("NORMAL", "DEPTH_WORLD", "MOTION")}, fi)
+        upload_frame(s, o, {"DEPTH_NDC": rng.uniform(0.1, 0.9, (H, W)).astype(np.float32)}, fi)
+        p = _volumetric_params(vmode, 100 + f)
+        Volumetric(s).ProcessScattering(fi, p)
+        o.process_scattering(fi, p)
+        for name in ("SCATTER_VOLUME", "SCATTERING", "SCATTERING_HISTORY"):
+            img = s.image(name, fi)
+            g = F.decode(s.download(name, fi), img.format)
+            c = F.decode(o.plane(name, fi), img.format)
+            err = F.texel_rel_err(g, c, atol=1e-6)
+            assert err.max() <= TOL[img.format], f"frame {f} {name}: max rel err {err.max():.3e}"
+            assert np.mean(err > 0) <= 0.02, f"frame {f} {name}: {np.mean(err > 0):.2%} of texels differ"
+    s.close()
+
+
+def test_process_scattering_rejects_bad_params(ctx):
+    s = Stream(ctx, 64, 36)
+    p = _volumetric_params(N.VOLUME_ENABLE_VOLUMETRIC, 0)
+    p.volumeCameraFar = p.volumeCameraNear
+    with pytest.raises(N.RgdnError) as e:
+        Volumetric(s).ProcessScattering(0, p)
+    assert e.value.status == N.WRONG_FUNCTION_ARGUMENT
+    p = _volumetric_params(3, 0)
+    with pytest.raises(N.RgdnError):
+        Volumetric(s).ProcessScattering(0, p)
     s.close()
 
 

@@ -317,3 +317,102 @@ def test_bloom_constant_image():
     assert np.all(res[:, W - 1] == -1.0) and np.all(res[H - 1, :] == -1.0)
     inner = res[: H - 1, : W - 1, :3] / cp
     assert inner.min() > 1.0 and inner.max() <= 8.0 * (1 + 1e-12)
+
+
+def _f16(x):
+    return np.asarray(x, np.float16).view(np.uint16)
+
+
+def test_volume_process_closed_form():
+    """CmVolumetricProcess on a volume of constant in-scatter L and extinction d per cell:
+    cell z holds L * sum_{i<=z} exp(-i d) and transmittance exp(-(z + 1) d), within one fp16
+    rounding of the stored cell."""
+    o = oracle.OracleStream(64, 36, oracle.MODE_F64)
+    vol = o.plane("SCATTER_VOLUME", 0)
+    assert vol.shape == (N.VOLUME_SIZE[1] * N.VOLUME_SIZE[2], N.VOLUME_SIZE[0], 4)
+    L, d = np.array([0.5, 0.25, 0.125]), 0.05
+    vol[...] = _f16(np.concatenate([L, [d]]))
+    o.process_scattering(0, N.VolumetricParams())
+    v = vol.view(np.float16).astype(np.float64).reshape(N.VOLUME_SIZE[2], N.VOLUME_SIZE[1], N.VOLUME_SIZE[0], 4)
+    dq, Lq = float(np.float16(d)), L.astype(np.float16).astype(np.float64)
+    for z in range(N.VOLUME_SIZE[2]):
+        rgb = Lq * sum(math.exp(-i * dq) for i in range(z + 1))
+        assert v[z, 3, 7, :3] == pytest.approx(rgb, rel=2.0 ** -10), z
+        assert v[z, 80, 150, 3] == pytest.approx(math.exp(-(z + 1) * dq), rel=2.0 ** -10), z
+
+
+def _scatter_stream(W, H, depth, motion_x=0.0):
+    o = oracle.OracleStream(W, H, oracle.MODE_F32)
+    n = oracle.encode_normal(0.0, 0.0, 1.0)
+    for fi in (0, 1):
+        o.plane("NORMAL", fi)[...] = n
+        o.plane("DEPTH_WORLD", fi)[...] = _f16(depth)
+    mo = np.zeros((H, W, 4), np.float32)
+    mo[..., 0] = motion_x
+    o.plane("MOTION", 0)[...] = _f16(mo)
+    o.plane("MOTION", 1)[...] = _f16(mo)
+    return o
+
+
+def test_scatter_simple_fog_and_history():
+    """CmScatterAccum in SIMPLE mode. A frame without history writes the fog
+    (ambient (1 - f), f), f = exp(-depth * scattering * 0.00005), with history length 1; sky
+    (ray length above MAX_RAY_LENGTH) writes (0, 0, 0, 1). A static next frame finds all four
+    taps valid and mixes with weight 1/2 (history 2), capped by maxHistoryLength."""
+    W, H = 16, 8
+    depth = np.full((H, W), 40.0)
+    depth[:, 3] = 20000.0
+    o = _scatter_stream(W, H, depth, motion_x=5.0)   # reprojects outside the image: no history
+    p = N.VolumetricParams()
+    p.volumeEnableType = N.VOLUME_ENABLE_SIMPLE
+    p.volumeScattering = 100.0
+    p.volumeAmbient[:] = (0.5, 1.0, 2.0)
+    p.maxHistoryLength = 1.5
+    o.process_scattering(0, p)
+    sc = o.plane("SCATTERING", 0).view(np.float16).astype(np.float64)
+    hist = o.plane("SCATTERING_HISTORY", 0).view(np.float16).astype(np.float64)
+    f = math.exp(-float(np.float16(40.0)) * float(np.float32(100.0) * np.float32(0.00005)))
+    fog = np.array([0.5 * (1 - f), 1.0 * (1 - f), 2.0 * (1 - f), f])
+    cb_sky = {(2 * (3 - 0) + (0 + y) % 2, y) for y in range(H)}   # regular pixels of checkerboard column 3
+    for y in range(H):
+        for x in range(W):
+            want = np.array([0, 0, 0, 1.0]) if (x, y) in cb_sky else fog
+            assert sc[y, x] == pytest.approx(want, rel=2.0 ** -10, abs=1e-6), (x, y)
+            assert hist[y, x] == 1.0
+    # static second frame: history of 1 everywhere, mixed with 1 / min(1 + 1, 1.5)
+    o.plane("MOTION", 1)[...] = _f16(np.zeros((H, W, 4), np.float32))
+    o.process_scattering(1, p)
+    sc1 = o.plane("SCATTERING", 1).view(np.float16).astype(np.float64)
+    h1 = o.plane("SCATTERING_HISTORY", 1).view(np.float16).astype(np.float64)
+    assert np.all(h1 == 1.5)
+    assert sc1[4, 8] == pytest.approx(fog, rel=2.0 ** -9)
+
+
+def test_random_seed_restatement():
+    """getRandomSeed / rnd8_4's hashes (Random.h:243-300) against an independent Python
+    restatement of MurmurHash2's mixing and lowbias32."""
+    M, U = 0x5BD1E995, 0xFFFFFFFF
+
+    def murmur33(v):
+        src = [(((c * M) & U) ^ (((c * M) & U) >> 24)) * M & U for c in v]
+        h = [1190494759, 2147483647, 3559788179]
+        for k in src:
+            h = [((x * M) & U) ^ k for x in h]
+        h = [x ^ (x >> 13) for x in h]
+        h = [(x * M) & U for x in h]
+        return [x ^ (x >> 15) for x in h]
+
+    def lowbias32(x):
+        x ^= x >> 16
+        x = (x * 0x7FEB352D) & U
+        x ^= x >> 15
+        x = (x * 0x846CA68B) & U
+        return x ^ (x >> 16)
+
+    lib = oracle.load()
+    for (x, y, f) in [(0, 0, 0), (1, 2, 3), (1919, 1079, 123456), (640, 17, 0xFFFFFFFF)]:
+        h = murmur33([x, y, f])
+        seed = ((h[2] % 128) << 14) | ((h[1] % 128) << 7) | (h[0] % 128)
+        assert lib.orc_random_seed(x, y, f) == seed
+        assert lib.orc_wellons_lowbias32(seed) == lowbias32(seed)
+    assert lowbias32(0) == 0 and lib.orc_wellons_lowbias32(1) == lowbias32(1)
