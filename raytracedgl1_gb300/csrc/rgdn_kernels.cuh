@@ -3045,7 +3045,7 @@ __device__ __forceinline__ float3 volume_sample_pos( const ScatterArgs& a, float
 
 // fializeScattering (CmScatterAccum.comp:41-95) at regular pixel (rx, ry); depthCb is
 // DEPTH_WORLD at its checkerboard position
-__device__ __forceinline__ float4 finalize_scattering( const ScatterArgs& a, int rx, int ry, float depthCb )
+__device__ __forceinline__ float4 finalize_scattering( const ScatterArgs& a, int rx, int ry, float depthCb, const float* inv255 )
 {
     if( a.enableType == RGDN_VOLUME_ENABLE_VOLUMETRIC )
     {
@@ -3054,17 +3054,19 @@ __device__ __forceinline__ float4 finalize_scattering( const ScatterArgs& a, int
         const float4 wp  = mat_mul( a.invViewProj, ndc );
         const float3 pos = f3( wp.x / wp.w, wp.y / wp.w, wp.z / wp.w );
         // rnd8_4( getRandomSeed( pix, frameId ), 0 ).xyz
+        // byte / 255 from a table of the IEEE quotients
         const uint32_t rnd = wellons_lowbias32( random_seed( rx, ry, a.frameId ) );
-        const float    r0 = (float)( rnd & 0xFFu ) / 255.0f, r1 = (float)( ( rnd >> 8 ) & 0xFFu ) / 255.0f;
-        const float    r2 = (float)( ( rnd >> 16 ) & 0xFFu ) / 255.0f;
+        const float    r0 = inv255[ rnd & 0xFFu ], r1 = inv255[ ( rnd >> 8 ) & 0xFFu ], r2 = inv255[ ( rnd >> 16 ) & 0xFFu ];
         // sampleHemisphere (Random.h:73-92)
         const float u1 = r0 * 0.99f, u2 = r1 * 0.99f;
         const float rr = sqrtf( u1 ), phi = ( 2.0f * 3.14159265358979f ) * u2, hz = sqrtf( 1.0f - u1 );
-        const float3 basis = f3( -( rr * cosf( phi ) ), -( rr * sinf( phi ) ), -hz );
-        // volume_sampleDithered (Volumetric.h:92-104), dither radius 2
+        float       sphi, cphi;
+        sincosf( phi, &sphi, &cphi );
+        const float3 basis = f3( -( rr * cphi ), -( rr * sphi ), -hz );
+        // volume_sampleDithered (Volumetric.h:92-104), dither radius 2; / 64 is the exact * 2^-6
         float3      sp = volume_sample_pos( a, pos );
         const float k  = r2 * 2.0f;
-        sp             = f3( sp.x + ( k * basis.x ) / (float)a.nx, sp.y + ( k * basis.y ) / (float)a.ny, sp.z + ( k * basis.z ) / (float)a.nz );
+        sp             = f3( sp.x + ( k * basis.x ) / (float)a.nx, sp.y + ( k * basis.y ) / (float)a.ny, sp.z + ( k * basis.z ) * 0.015625f );
         return volume_trilinear( a.volume, a.nx, a.ny, a.nz, sp );
     }
     if( a.enableType == RGDN_VOLUME_ENABLE_SIMPLE )
@@ -3076,21 +3078,19 @@ __device__ __forceinline__ float4 finalize_scattering( const ScatterArgs& a, int
     return make_float4( 0.0f, 0.0f, 0.0f, 1.0f );
 }
 
-// CmScatterAccum.comp:97-161: one thread per checkerboard pixel
-template< int M > __global__ void __launch_bounds__( 256 ) k_scatter_accum( const ScatterArgs a )
+// CmScatterAccum.comp:97-161 for checkerboard pixel (cx, cy); returns the new scattering and
+// history length
+__device__ __forceinline__ float4 scatter_pixel( const ScatterArgs& a, int cx, int cy, const float* inv255, float& histOut )
 {
-    const int cx = blockIdx.x * blockDim.x + threadIdx.x, cy = blockIdx.y * blockDim.y + threadIdx.y;
-    pdl_launch_dependents();
-    pdl_wait();
-    if( cx >= a.u.W || cy >= a.u.H ) return;
-    const size_t  ci      = (size_t)cy * a.u.W + cx;
-    const float4  mo      = h4f( a.motion[ ci ] );
-    const float   depth   = h2f( a.depth[ ci ] );
-    auto          nrm     = [ & ]( uint32_t p ) {
+    const size_t ci    = (size_t)cy * a.u.W + cx;
+    const float4 mo    = h4f( a.motion[ ci ] );
+    const float  depth = h2f( a.depth[ ci ] );
+    auto         nrm   = [ & ]( uint32_t p ) {
         const float2 ph = __ldg( &a.phiTab[ p >> 16 ] ), th = __ldg( &a.thetaTab[ p & 0xFFFFu ] );
         return f3( ph.x * th.x, ph.x * th.y, ph.y );
     };
     const float3 normal = nrm( a.normal[ ci ] );
+    const float  rz     = rcp_approx( fabsf( depth ) );   // testReprojectedDepth through test_depth_r
     const float2 pp     = prev_screen_pos( a.u, make_float2( mo.x, mo.y ), cx, cy );
     const float  fpx = floorf( pp.x - 0.5f ), fpy = floorf( pp.y - 0.5f );
     const int    px = safe_floor_int( fpx ), py = safe_floor_int( fpy );
@@ -3107,7 +3107,7 @@ template< int M > __global__ void __launch_bounds__( 256 ) k_scatter_accum( cons
             const int qx = px + xx, qy = py + yy;
             if( !in_area( qx, qy, area ) ) continue;
             const size_t qi = (size_t)qy * a.u.W + qx;
-            if( test_depth( depth, h2f( a.depthPrev[ qi ] ), mo.z ) && test_normal( normal, nrm( a.normalPrev[ qi ] ) ) )
+            if( test_depth_r( depth, rz, h2f( a.depthPrev[ qi ] ), mo.z ) && test_normal( normal, nrm( a.normalPrev[ qi ] ) ) )
             {
                 const float  w  = bw[ yy ][ xx ];
                 const int2   r  = regular_from_cb( a.u, qx, qy );
@@ -3122,9 +3122,25 @@ template< int M > __global__ void __launch_bounds__( 256 ) k_scatter_accum( cons
     hist          = ok ? hist / wsum : 0.0f;
     acc           = ok ? make_float4( acc.x / wsum, acc.y / wsum, acc.z / wsum, acc.w / wsum ) : make_float4( 0.0f, 0.0f, 0.0f, 0.0f );
     hist          = gclamp( hist + 1.0f, 1.0f, fmaxf( 1.0f, a.maxHistoryLength ) );
+    const int2 reg = regular_from_cb( a.u, cx, cy );
+    histOut        = hist;
+    return vmix4( acc, finalize_scattering( a, reg.x, reg.y, depth, inv255 ), 1.0f / hist );
+}
+
+// One thread per checkerboard pixel. (One thread per pair (cx, cx + W/2), whose regular pixels
+// are neighbours, wrote full sectors but ran 10 % slower: half the warps to hide latency.)
+template< int M > __global__ void __launch_bounds__( 256 ) k_scatter_accum( const ScatterArgs a )
+{
+    __shared__ float inv255[ 256 ];
+    for( int t = threadIdx.y * blockDim.x + threadIdx.x; t < 256; t += blockDim.x * blockDim.y ) inv255[ t ] = (float)t / 255.0f;
+    __syncthreads();
+    const int cx = blockIdx.x * blockDim.x + threadIdx.x, cy = blockIdx.y * blockDim.y + threadIdx.y;
+    pdl_launch_dependents();
+    pdl_wait();
+    if( cx >= a.u.W || cy >= a.u.H ) return;
+    float        hist;
+    const float4 acc = scatter_pixel( a, cx, cy, inv255, hist );
     const int2   reg = regular_from_cb( a.u, cx, cy );
-    const float4 fin = finalize_scattering( a, reg.x, reg.y, depth );
-    acc              = vmix4( acc, fin, 1.0f / hist );
     const size_t ri  = (size_t)reg.y * a.u.W + reg.x;
     a.scatterOut[ ri ] = f4h( acc );
     a.historyOut[ ri ] = f32_to_f16( hist );
