@@ -629,6 +629,8 @@ __device__ __forceinline__ float parallax( const Uniform& u, float3 pos, float3 
 // from the device table (the same bits as the inline powf). GEOM: write this frame's geometry
 // record. GEOMPREV: read the previous frame's record (decoded normal + depth, the same values)
 // at the taps.
+// the temporal pass reads each in-area tap's history together with its geometry
+constexpr bool kTemporalEarlyHistory = true;
 template< int M, bool FAST, bool GEOM, bool GEOMPREV >
 __device__ __forceinline__ void temporal_tile( const FrameArgs& a, int bx, int by, const float* u8 )
 {
@@ -726,17 +728,26 @@ __device__ __forceinline__ void temporal_tile( const FrameArgs& a, int bx, int b
                 dP = h2f( a.depthPrev[ q ] );
                 nP = decode_normal( a, a.normalPrev[ q ] );
             }
+            // FAST: the tap's history is read with its geometry, before the tests decide
+            // whether it counts, so the two loads are in flight together
+            float4 dc, hl;
+            float2 m;
+            float3 sp, ip;
+            auto   ldHist = [ & ]() {
+                dc = S::ldcv( a.diffHistory, a.varHistory, q );
+                m  = S::ld2( a.momentsPrev, q );
+                hl = S::ld4( a.histLenPrev, q );
+                sp = S::ld3( a.specAccumPrev, q );
+                ip = S::ld3( a.indirAccumPrev, q );
+            };
+            if( FAST && kTemporalEarlyHistory ) ldHist();
             const bool okDepth = FAST ? test_depth_r( z, rz, dP, motionZ ) : test_depth( z, dP, motionZ );
             if( okDepth && test_normal( normal, nP ) )
             {
                 // FAST: fused multiply-adds for the continuous sums; the diffuse history length
                 // (the variance pass switches on it) and the weight sum stay IEEE
-                const float  w  = bw[ yy ][ xx ];
-                const float4 dc = S::ldcv( a.diffHistory, a.varHistory, q );
-                const float2 m  = S::ld2( a.momentsPrev, q );
-                const float4 hl = S::ld4( a.histLenPrev, q );
-                const float3 sp = S::ld3( a.specAccumPrev, q );
-                const float3 ip = S::ld3( a.indirAccumPrev, q );
+                const float w = bw[ yy ][ xx ];
+                if( !( FAST && kTemporalEarlyHistory ) ) ldHist();
                 if constexpr( FAST )
                 {
                     // the fourteen continuous sums as seven packed FP32 FMAs (the bits of the
