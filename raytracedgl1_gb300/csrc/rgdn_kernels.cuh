@@ -1403,7 +1403,7 @@ template< int M > __device__ __forceinline__ void antifirefly_fast_tile( const F
     }
 }
 
-template< int M > __global__ void __launch_bounds__( 256 ) k_antifirefly_fast( const FrameArgs a )
+template< int M > __global__ void __launch_bounds__( 256, ( M == MODE_F16 || M == MODE_BF16 ) ? 4 : 3 ) k_antifirefly_fast( const FrameArgs a )
 {
     __shared__ AfShared< M > sh;
     pdl_launch_dependents();
