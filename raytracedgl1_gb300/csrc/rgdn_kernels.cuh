@@ -565,7 +565,7 @@ __device__ __forceinline__ void gradient_atrous_tile( const FrameArgs& a, int it
     gradient_atrous_px( a, gx, gy, iter, u8 );
 }
 
-template< int M > __global__ void __launch_bounds__( 256 ) k_gradient_samples( const FrameArgs a, uint32_t* dst )
+template< int M > __global__ void __launch_bounds__( 256, 6 ) k_gradient_samples( const FrameArgs a, uint32_t* dst )
 {
     __shared__ float u8[ 256 ];
     pdl_launch_dependents();
@@ -1425,7 +1425,7 @@ template< int M, bool FAST > __device__ __forceinline__ void variance_geo_tile( 
     variance_px< M, FAST, true >( a, px, py, i, [ & ]( int dx, int dy ) { return ld3z< M >( a, a.diffAccumColor, px + dx, py + dy ); }, c, v );
     S::stcv( a.diffPing, a.varPing, (size_t)i, c, v );
 }
-template< int M, bool FAST > __global__ void __launch_bounds__( 256 ) k_variance_geo( const FrameArgs a )
+template< int M, bool FAST > __global__ void __launch_bounds__( 256, 8 ) k_variance_geo( const FrameArgs a )
 {
     pdl_launch_dependents();
     pdl_wait();
