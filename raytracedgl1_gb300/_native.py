@@ -237,7 +237,7 @@ KERNEL_NAMES.update({100: "atrous_fast", 101: "atrous_fast_hist", 102: "temporal
                      107: "atrous_exact", 108: "temporal_exact_geom", 109: "variance_exact_geom",
                      110: "temporal_fast_gp", 111: "temporal_exact_geom_gp", 112: "atrous_tma",
                      113: "atrous_tma_hist", 114: "prepare_final", 115: "bloom",
-                     116: "volume_process", 117: "process_scattering"})
+                     117: "process_scattering"})
 
 _lib = None
 

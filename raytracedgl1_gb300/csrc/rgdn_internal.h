@@ -222,8 +222,7 @@ enum FusedKernel : int
     KF_ATROUS_TMA_HIST     = 113,  // TMA-staged last iteration + fused histogram (timing label)
     KF_PREPARE_FINAL       = 114,  // exposure, tonemapping and bloom input (timing label)
     KF_BLOOM               = 115,  // the bloom pyramid and its application (timing label)
-    KF_VOLUME_PROCESS      = 116,  // froxel columns integrated front to back (timing label)
-    KF_SCATTER_ACCUM       = 117,  // screen-space scattering accumulation (timing label)
+    KF_SCATTER_ACCUM       = 117,  // volume integration + screen-space accumulation (timing label)
 };
 
 // Launches one stage for one frame. Returns the CUDA error of the launch.
