@@ -574,6 +574,60 @@ def test_process_scattering_parity(ctx, vmode, size):
     s.close()
 
 
+def test_bloom_parity_1080p(ctx):
+    """The bloom pyramid at the headline size (1920x1080, fp16 storage): every level of 64K
+    texels or more takes the wide builds (2x2-quad upsample, 4 blocks per SM), the coarse levels
+    the per-texel kernels; all mips, BLOOM_RESULT and FINAL against the oracle."""
+    W, H = 1920, 1080
+    rng = np.random.default_rng(11)
+    o = oracle.OracleStream(W, H, N.STORAGE_FP16)
+    s = Stream(ctx, W, H, N.STORAGE_FP16)
+    for name in BLOOM_PLANES:
+        img = s.image(name, 0)
+        rgb = rng.uniform(0.0, 1.0, (img.height, img.width, 3)) ** 4 * (24.0 if name == "BLOOM_INPUT" else 2.0)
+        data = _encode_pre(rgb, img.format)
+        o.plane(name, 0)[...] = data
+        s.upload(name, 0, data)
+    Bloom(s).Apply(0, 0.8)
+    o.bloom(0, 0.8)
+    for name in BLOOM_PLANES[1:]:
+        img = s.image(name, 0)
+        err = F.texel_rel_err(F.decode(s.download(name, 0), img.format), F.decode(o.plane(name, 0), img.format), atol=1e-6)
+        assert err.max() <= TOL[img.format], f"{name}: max rel err {err.max():.3e}"
+        assert np.mean(err > 0) <= 0.02, f"{name}: {np.mean(err > 0):.2%} of texels differ"
+    s.close()
+
+
+def test_process_scattering_parity_1080p(ctx):
+    """Volumetric scattering (VOLUMETRIC mode) at 1920x1080 on one frame of the synthetic scene
+    with a random froxel volume and history: the integrated volume, SCATTERING and
+    SCATTERING_HISTORY against the oracle."""
+    W, H = 1920, 1080
+    rng = np.random.default_rng(5)
+    sc = Scene(W, H, seed=5)
+    s = Stream(ctx, W, H, N.STORAGE_FP16)
+    o = oracle.OracleStream(W, H, oracle.MODE_F32)
+    nz, ny, nx = N.VOLUME_SIZE[2], N.VOLUME_SIZE[1], N.VOLUME_SIZE[0]
+    vol = np.concatenate([rng.uniform(0, 0.5, (ny * nz, nx, 3)), rng.uniform(0, 0.1, (ny * nz, nx, 1))], axis=2)
+    upload_frame(s, o, {"SCATTER_VOLUME": vol.astype(np.float16).view(np.uint16)}, 0)
+    prev = np.concatenate([rng.uniform(0, 1, (H, W, 3)), rng.uniform(0.2, 1, (H, W, 1))], axis=2)
+    upload_frame(s, o, {"SCATTERING": prev.astype(np.float16).view(np.uint16),
+                        "SCATTERING_HISTORY": rng.uniform(1, 5, (H, W)).astype(np.float16).view(np.uint16)}, 1)
+    for f in range(2):
+        bufs, _ = sc.generate(f)
+        upload_frame(s, o, {k: bufs[k] for k in ("NORMAL", "DEPTH_WORLD", "MOTION")}, f & 1)
+    upload_frame(s, o, {"DEPTH_NDC": rng.uniform(0.1, 0.9, (H, W)).astype(np.float32)}, 0)
+    p = _volumetric_params(N.VOLUME_ENABLE_VOLUMETRIC, 7)
+    Volumetric(s).ProcessScattering(0, p)
+    o.process_scattering(0, p)
+    for name in ("SCATTER_VOLUME", "SCATTERING", "SCATTERING_HISTORY"):
+        img = s.image(name, 0)
+        err = F.texel_rel_err(F.decode(s.download(name, 0), img.format), F.decode(o.plane(name, 0), img.format), atol=1e-6)
+        assert err.max() <= TOL[img.format], f"{name}: max rel err {err.max():.3e}"
+        assert np.mean(err > 0) <= 0.02, f"{name}: {np.mean(err > 0):.2%} of texels differ"
+    s.close()
+
+
 def test_process_scattering_rejects_bad_params(ctx):
     s = Stream(ctx, 64, 36)
     p = _volumetric_params(N.VOLUME_ENABLE_VOLUMETRIC, 0)
