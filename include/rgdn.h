@@ -313,6 +313,10 @@ typedef struct rgdn_final_params
     uint32_t flags;                    /* RGDN_FINAL_* */
 } rgdn_final_params;
 #define RGDN_FINAL_APPLY_SCATTERING 0x1u /* hdr = hdr * scattering.a + scattering.rgb */
+#define RGDN_FINAL_EXACT_MATH       0x2u /* IEEE powf and divisions in the shader's order; the
+                                            default evaluates pow as the hardware exp2(y log2 x)
+                                            and divides by reciprocal multiplies, as a GPU
+                                            compiles the shader */
 rgdn_status rgdn_prepare_final( rgdn_stream* stream, uint32_t frameIndex, const rgdn_final_params* params, rgdn_cuda_stream cudaStream );
 
 /* ---- bloom -------------------------------------------------------------------------
@@ -360,7 +364,12 @@ typedef struct rgdn_volumetric_params
                                         history reset */
     uint32_t volumeEnableType;       /* RGDN_VOLUME_ENABLE_* */
     uint32_t frameId;                /* GlobalUniform::frameId: seeds the per-pixel dither */
+    uint32_t flags;                  /* RGDN_VOLUME_EXACT_MATH */
 } rgdn_volumetric_params;
+#define RGDN_VOLUME_EXACT_MATH 0x1u /* IEEE divisions, square roots, sin/cos and exp in the
+                                       accumulation; the default uses the hardware reciprocal,
+                                       square root, sin/cos and exp2 for its continuous terms
+                                       (the reprojection tests decide exactly either way) */
 rgdn_status rgdn_process_scattering( rgdn_stream* stream, uint32_t frameIndex, const rgdn_volumetric_params* params, rgdn_cuda_stream cudaStream );
 
 /* One stage alone (the plain path / per-stage checking). `iteration` selects the

@@ -78,6 +78,7 @@ class FinalParams(C.Structure):
 
 
 FINAL_APPLY_SCATTERING = 0x1
+FINAL_EXACT_MATH = 0x2
 
 
 class BloomParams(C.Structure):
@@ -87,6 +88,7 @@ class BloomParams(C.Structure):
 
 VOLUME_SIZE = (160, 88, 64)   # RGDN_VOLUME_SIZE_X, _Y, _Z
 VOLUME_ENABLE_NONE, VOLUME_ENABLE_SIMPLE, VOLUME_ENABLE_VOLUMETRIC = 0, 1, 2
+VOLUME_EXACT_MATH = 0x1
 
 
 class VolumetricParams(C.Structure):
@@ -95,7 +97,7 @@ class VolumetricParams(C.Structure):
         ("invView", C.c_float * 16), ("invProjection", C.c_float * 16), ("volumeViewProj", C.c_float * 16),
         ("cameraPosition", C.c_float * 4), ("volumeCameraNear", C.c_float), ("volumeCameraFar", C.c_float),
         ("volumeAmbient", C.c_float * 3), ("volumeScattering", C.c_float), ("maxHistoryLength", C.c_float),
-        ("volumeEnableType", C.c_uint32), ("frameId", C.c_uint32),
+        ("volumeEnableType", C.c_uint32), ("frameId", C.c_uint32), ("flags", C.c_uint32),
     ]
 
 

@@ -1024,6 +1024,10 @@ rgdn_status rgdn_process_scattering( rgdn_stream* s, uint32_t frameIndex, const 
     a.maxHistoryLength = p->maxHistoryLength;
     a.enableType       = p->volumeEnableType;
     a.frameId          = p->frameId;
+    a.flags            = p->flags;
+    a.irw              = 1.0f / a.u.rw;
+    a.irh              = 1.0f / a.u.rh;
+    a.iRange           = 1.0f / ( a.volFar - a.volNear );
     cudaStream_t st = (cudaStream_t)cs;
     cudaEvent_t  ea = nullptr, eb = nullptr;
     if( s->timing )

@@ -192,11 +192,13 @@ struct ScatterArgs
     float          volumeViewProj[ 16 ];
     float          camPos[ 3 ];
     float          volNear, volFar;
+    float          irw, irh, iRange;  // 1 / renderWidth, 1 / renderHeight, 1 / (far - near)
     float          ambient[ 3 ];
     float          density;           // volumeScattering * 0.00005
     float          maxHistoryLength;
     uint32_t       enableType;
     uint32_t       frameId;
+    uint32_t       flags;             // RGDN_VOLUME_EXACT_MATH
 };
 cudaError_t launch_process_scattering( const ScatterArgs& a, cudaStream_t s );
 cudaError_t launch_final_ref( const FinalArgs& f, cudaStream_t s );

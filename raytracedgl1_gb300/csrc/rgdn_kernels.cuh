@@ -2512,25 +2512,29 @@ __device__ __forceinline__ float u2_op( float x )
 // luma^c / (luma^c * scale + bias); the ratio scaled to hit that luma without clipping; then
 // the missing luma of clipped channels moved to the others through the crosstalk capacities,
 // twice. The operation order is the shader's.
-__device__ __forceinline__ float3 lpm_709( float3 c, const LpmConsts& k )
+// FAST: pow(x, y) as the hardware exp2(y log2 x) and the reciprocals by rcp.approx, as the
+// shader's own pow and division compile on a GPU; the result is continuous in each of them
+template< bool FAST > __device__ __forceinline__ float lpm_pow( float x, float y ) { return FAST ? ex2_approx( y * lg2_approx( x ) ) : powf( x, y ); }
+template< bool FAST > __device__ __forceinline__ float lpm_rcp( float x ) { return FAST ? rcp_approx( x ) : 1.0f / x; }
+template< bool FAST > __device__ __forceinline__ float3 lpm_709( float3 c, const LpmConsts& k )
 {
-    const float rcpMax = 1.0f / fmaxf( c.x, fmaxf( c.y, c.z ) );
+    const float rcpMax = lpm_rcp< FAST >( fmaxf( c.x, fmaxf( c.y, c.z ) ) );
     float       rR = c.x * rcpMax, rG = c.y * rcpMax, rB = c.z * rcpMax;
-    // pow(x, +-0) is 1 for every x, NaN included: the default saturation 0 needs no powf
-    rR = k.saturation[ 0 ] == 0.0f ? 1.0f : powf( rR, k.saturation[ 0 ] );
-    rG = k.saturation[ 1 ] == 0.0f ? 1.0f : powf( rG, k.saturation[ 1 ] );
-    rB = k.saturation[ 2 ] == 0.0f ? 1.0f : powf( rB, k.saturation[ 2 ] );
+    // pow(x, +-0) is 1 for every x, NaN included: the default saturation 0 needs no pow
+    rR = k.saturation[ 0 ] == 0.0f ? 1.0f : lpm_pow< FAST >( rR, k.saturation[ 0 ] );
+    rG = k.saturation[ 1 ] == 0.0f ? 1.0f : lpm_pow< FAST >( rG, k.saturation[ 1 ] );
+    rB = k.saturation[ 2 ] == 0.0f ? 1.0f : lpm_pow< FAST >( rB, k.saturation[ 2 ] );
     float luma = c.y * k.lumaT[ 1 ] + ( c.x * k.lumaT[ 0 ] + ( c.z * k.lumaT[ 2 ] ) );
-    luma       = powf( luma, k.contrast );
-    luma       = luma * ( 1.0f / ( luma * k.toneScaleBias[ 0 ] + k.toneScaleBias[ 1 ] ) );
+    luma       = lpm_pow< FAST >( luma, k.contrast );
+    luma       = luma * lpm_rcp< FAST >( luma * k.toneScaleBias[ 0 ] + k.toneScaleBias[ 1 ] );
     const float lumaRatio  = rR * k.lumaT[ 0 ] + rG * k.lumaT[ 1 ] + rB * k.lumaT[ 2 ];
-    const float ratioScale = gsat( luma * ( 1.0f / lumaRatio ) );
+    const float ratioScale = gsat( luma * lpm_rcp< FAST >( lumaRatio ) );
     float       cR = gsat( rR * ratioScale ), cG = gsat( rG * ratioScale ), cB = gsat( rB * ratioScale );
     const float capR = -k.crosstalk[ 0 ] * cR + k.crosstalk[ 0 ];
     const float capG = -k.crosstalk[ 1 ] * cG + k.crosstalk[ 1 ];
     const float capB = -k.crosstalk[ 2 ] * cB + k.crosstalk[ 2 ];
     float lumaAdd = gsat( ( -cB ) * k.lumaT[ 2 ] + ( ( -cR ) * k.lumaT[ 0 ] + ( ( -cG ) * k.lumaT[ 1 ] + luma ) ) );
-    const float t = lumaAdd * ( 1.0f / ( capG * k.lumaT[ 1 ] + ( capR * k.lumaT[ 0 ] + ( capB * k.lumaT[ 2 ] ) ) ) );
+    const float t = lumaAdd * lpm_rcp< FAST >( capG * k.lumaT[ 1 ] + ( capR * k.lumaT[ 0 ] + ( capB * k.lumaT[ 2 ] ) ) );
     cR      = gsat( t * capR + cR );
     cG      = gsat( t * capG + cG );
     cB      = gsat( t * capB + cB );
@@ -2541,7 +2545,7 @@ __device__ __forceinline__ float3 lpm_709( float3 c, const LpmConsts& k )
     return f3( cR, cG, cB );
 }
 
-template< int M > __global__ void __launch_bounds__( 256 ) k_prepare_final( const FinalArgs f )
+template< int M, bool FAST > __global__ void __launch_bounds__( 256 ) k_prepare_final( const FinalArgs f )
 {
     using S     = Sto< M >;
     const int x = blockIdx.x * blockDim.x + threadIdx.x;
@@ -2586,18 +2590,28 @@ template< int M > __global__ void __launch_bounds__( 256 ) k_prepare_final( cons
     if( (float)x < f.lightmapCoverage * f.rw )
     {
         const float w = u2_op( f.whitePoint );
-        color         = f3( u2_op( 2.0f * hdr.x ) / w, u2_op( 2.0f * hdr.y ) / w, u2_op( 2.0f * hdr.z ) / w );
+        if constexpr( FAST )
+        {
+            const float iw = rcp_approx( w );
+            color          = f3( u2_op( 2.0f * hdr.x ) * iw, u2_op( 2.0f * hdr.y ) * iw, u2_op( 2.0f * hdr.z ) * iw );
+        }
+        else color = f3( u2_op( 2.0f * hdr.x ) / w, u2_op( 2.0f * hdr.y ) / w, u2_op( 2.0f * hdr.z ) / w );
     }
     else
     {
         const float3 c = f3( hdr.x * exposure + emis.x * f.emisMax, hdr.y * exposure + emis.y * f.emisMax, hdr.z * exposure + emis.z * f.emisMax );
-        color          = lpm_709( c, f.lpm );
+        color          = lpm_709< FAST >( c, f.lpm );
     }
     // getBloomInput (CmPrepareFinal.comp:116-133)
     float3 bloom = f3( ( hdr.x + emis.x * el ) * exposure, ( hdr.y + emis.y * el ) * exposure, ( hdr.z + emis.z * el ) * exposure );
     if( isnan( bloom.x ) || isnan( bloom.y ) || isnan( bloom.z ) || isinf( bloom.x ) || isinf( bloom.y ) || isinf( bloom.z ) )
         bloom = f3( 0, 0, 0 );
-    bloom = mul( bloom, gsmoothstep( 0.0f, f.bloomThreshold, luminance( bloom ) ) );
+    if constexpr( FAST )
+    {
+        const float st = gsat( luminance( bloom ) * rcp_approx( f.bloomThreshold ) );   // smoothstep( 0, threshold, . )
+        bloom          = mul( bloom, st * st * ( 3.0f - 2.0f * st ) );
+    }
+    else bloom = mul( bloom, gsmoothstep( 0.0f, f.bloomThreshold, luminance( bloom ) ) );
     S::stpre( f.finalOut, (size_t)i, color );
     S::stpre( f.bloomOut, (size_t)i, bloom );
 }
@@ -3044,46 +3058,56 @@ __device__ __forceinline__ float4 volume_trilinear( const ushort4* vol, int nx, 
 }
 
 // volume_toSamplePosition_T (Volumetric.h:38-58) with VOLUMETRIC_DISTANCE_POW 1
-__device__ __forceinline__ float3 volume_sample_pos( const ScatterArgs& a, float3 w )
+// FAST: reciprocal multiplies and the hardware square root (continuous in every term)
+template< bool FAST > __device__ __forceinline__ float3 volume_sample_pos( const ScatterArgs& a, float3 w )
 {
     const float4 ndc = mat_mul( a.volumeViewProj, make_float4( w.x, w.y, w.z, 1.0f ) );
-    const float  nx = ndc.x / ndc.w, ny = ndc.y / ndc.w;
+    const float  iw  = FAST ? rcp_approx( ndc.w ) : 0.0f;
+    const float  nx = FAST ? ndc.x * iw : ndc.x / ndc.w, ny = FAST ? ndc.y * iw : ndc.y / ndc.w;
     const float  dx = w.x - a.camPos[ 0 ], dy = w.y - a.camPos[ 1 ], dz = w.z - a.camPos[ 2 ];
-    const float  dist = sqrtf( dx * dx + dy * dy + dz * dz );
-    const float  z    = gclamp( ( dist - a.volNear ) / ( a.volFar - a.volNear ), 0.0f, 1.0f );   // pow( z, 1 ) == z
+    const float  d2 = dx * dx + dy * dy + dz * dz;
+    const float  dist = FAST ? sqrt_approx( d2 ) : sqrtf( d2 );
+    const float  zr   = FAST ? ( dist - a.volNear ) * a.iRange : ( dist - a.volNear ) / ( a.volFar - a.volNear );
+    const float  z    = gclamp( zr, 0.0f, 1.0f );   // pow( z, 1 ) == z
     return f3( nx * 0.5f + 0.5f, ny * 0.5f + 0.5f, z );
 }
 
 // fializeScattering (CmScatterAccum.comp:41-95) at regular pixel (rx, ry); depthCb is
 // DEPTH_WORLD at its checkerboard position
+template< bool FAST >
 __device__ __forceinline__ float4 finalize_scattering( const ScatterArgs& a, int rx, int ry, float depthCb, const float* inv255 )
 {
     if( a.enableType == RGDN_VOLUME_ENABLE_VOLUMETRIC )
     {
-        const float  sx  = (float)rx / a.u.rw, sy = (float)ry / a.u.rh;
+        const float  sx  = FAST ? (float)rx * a.irw : (float)rx / a.u.rw, sy = FAST ? (float)ry * a.irh : (float)ry / a.u.rh;
         const float4 ndc = make_float4( sx * 2.0f - 1.0f, sy * 2.0f - 1.0f, a.depthNdc[ (size_t)ry * a.u.W + rx ], 1.0f );
         const float4 wp  = mat_mul( a.invViewProj, ndc );
-        const float3 pos = f3( wp.x / wp.w, wp.y / wp.w, wp.z / wp.w );
+        const float  iw  = FAST ? rcp_approx( wp.w ) : 0.0f;
+        const float3 pos = FAST ? f3( wp.x * iw, wp.y * iw, wp.z * iw ) : f3( wp.x / wp.w, wp.y / wp.w, wp.z / wp.w );
         // rnd8_4( getRandomSeed( pix, frameId ), 0 ).xyz
         // byte / 255 from a table of the IEEE quotients
         const uint32_t rnd = wellons_lowbias32( random_seed( rx, ry, a.frameId ) );
         const float    r0 = inv255[ rnd & 0xFFu ], r1 = inv255[ ( rnd >> 8 ) & 0xFFu ], r2 = inv255[ ( rnd >> 16 ) & 0xFFu ];
         // sampleHemisphere (Random.h:73-92)
         const float u1 = r0 * 0.99f, u2 = r1 * 0.99f;
-        const float rr = sqrtf( u1 ), phi = ( 2.0f * 3.14159265358979f ) * u2, hz = sqrtf( 1.0f - u1 );
+        const float rr = FAST ? sqrt_approx( u1 ) : sqrtf( u1 ), phi = ( 2.0f * 3.14159265358979f ) * u2;
+        const float hz = FAST ? sqrt_approx( 1.0f - u1 ) : sqrtf( 1.0f - u1 );
         float       sphi, cphi;
-        sincosf( phi, &sphi, &cphi );
+        if( FAST ) __sincosf( phi, &sphi, &cphi );
+        else sincosf( phi, &sphi, &cphi );
         const float3 basis = f3( -( rr * cphi ), -( rr * sphi ), -hz );
         // volume_sampleDithered (Volumetric.h:92-104), dither radius 2; / 64 is the exact * 2^-6
-        float3      sp = volume_sample_pos( a, pos );
+        float3      sp = volume_sample_pos< FAST >( a, pos );
         const float k  = r2 * 2.0f;
-        sp             = f3( sp.x + ( k * basis.x ) / (float)a.nx, sp.y + ( k * basis.y ) / (float)a.ny, sp.z + ( k * basis.z ) * 0.015625f );
+        const float dx = FAST ? ( k * basis.x ) * ( 1.0f / (float)RGDN_VOLUME_SIZE_X ) : ( k * basis.x ) / (float)a.nx;
+        const float dy = FAST ? ( k * basis.y ) * ( 1.0f / (float)RGDN_VOLUME_SIZE_Y ) : ( k * basis.y ) / (float)a.ny;
+        sp             = f3( sp.x + dx, sp.y + dy, sp.z + ( k * basis.z ) * 0.015625f );
         return volume_trilinear( a.volume, a.nx, a.ny, a.nz, sp );
     }
     if( a.enableType == RGDN_VOLUME_ENABLE_SIMPLE )
     {
         if( depthCb > MAX_RAY_LENGTH ) return make_float4( 0.0f, 0.0f, 0.0f, 1.0f );
-        const float f = expf( -depthCb * a.density );
+        const float f = FAST ? ex2_approx( ( -depthCb * a.density ) * 1.44269504088896341f ) : expf( -depthCb * a.density );
         return make_float4( a.ambient[ 0 ] * ( 1.0f - f ), a.ambient[ 1 ] * ( 1.0f - f ), a.ambient[ 2 ] * ( 1.0f - f ), f );
     }
     return make_float4( 0.0f, 0.0f, 0.0f, 1.0f );
@@ -3091,6 +3115,7 @@ __device__ __forceinline__ float4 finalize_scattering( const ScatterArgs& a, int
 
 // CmScatterAccum.comp:97-161 for checkerboard pixel (cx, cy); returns the new scattering and
 // history length
+template< bool FAST >
 __device__ __forceinline__ float4 scatter_pixel( const ScatterArgs& a, int cx, int cy, const float* inv255, float& histOut )
 {
     const size_t ci    = (size_t)cy * a.u.W + cx;
@@ -3130,17 +3155,26 @@ __device__ __forceinline__ float4 scatter_pixel( const ScatterArgs& a, int cx, i
             }
         }
     const bool ok = wsum > 0.0001f;
-    hist          = ok ? hist / wsum : 0.0f;
-    acc           = ok ? make_float4( acc.x / wsum, acc.y / wsum, acc.z / wsum, acc.w / wsum ) : make_float4( 0.0f, 0.0f, 0.0f, 0.0f );
-    hist          = gclamp( hist + 1.0f, 1.0f, fmaxf( 1.0f, a.maxHistoryLength ) );
+    if( FAST )
+    {
+        const float iws = rcp_approx( wsum );
+        hist            = ok ? hist * iws : 0.0f;
+        acc             = ok ? make_float4( acc.x * iws, acc.y * iws, acc.z * iws, acc.w * iws ) : make_float4( 0.0f, 0.0f, 0.0f, 0.0f );
+    }
+    else
+    {
+        hist = ok ? hist / wsum : 0.0f;
+        acc  = ok ? make_float4( acc.x / wsum, acc.y / wsum, acc.z / wsum, acc.w / wsum ) : make_float4( 0.0f, 0.0f, 0.0f, 0.0f );
+    }
+    hist           = gclamp( hist + 1.0f, 1.0f, fmaxf( 1.0f, a.maxHistoryLength ) );
     const int2 reg = regular_from_cb( a.u, cx, cy );
     histOut        = hist;
-    return vmix4( acc, finalize_scattering( a, reg.x, reg.y, depth, inv255 ), 1.0f / hist );
+    return vmix4( acc, finalize_scattering< FAST >( a, reg.x, reg.y, depth, inv255 ), FAST ? rcp_approx( hist ) : 1.0f / hist );
 }
 
 // One thread per checkerboard pixel. (One thread per pair (cx, cx + W/2), whose regular pixels
 // are neighbours, wrote full sectors but ran 10 % slower: half the warps to hide latency.)
-template< int M > __global__ void __launch_bounds__( 256 ) k_scatter_accum( const ScatterArgs a )
+template< int M, bool FAST > __global__ void __launch_bounds__( 256 ) k_scatter_accum( const ScatterArgs a )
 {
     __shared__ float inv255[ 256 ];
     for( int t = threadIdx.y * blockDim.x + threadIdx.x; t < 256; t += blockDim.x * blockDim.y ) inv255[ t ] = (float)t / 255.0f;
@@ -3150,7 +3184,7 @@ template< int M > __global__ void __launch_bounds__( 256 ) k_scatter_accum( cons
     pdl_wait();
     if( cx >= a.u.W || cy >= a.u.H ) return;
     float        hist;
-    const float4 acc = scatter_pixel( a, cx, cy, inv255, hist );
+    const float4 acc = scatter_pixel< FAST >( a, cx, cy, inv255, hist );
     const int2   reg = regular_from_cb( a.u, cx, cy );
     const size_t ri  = (size_t)reg.y * a.u.W + reg.x;
     a.scatterOut[ ri ] = f4h( acc );
@@ -3227,13 +3261,18 @@ template< int M > cudaError_t launch_bloom_t( const BloomArgs& b, cudaStream_t s
 template< int M > cudaError_t launch_scatter_t( const ScatterArgs& a, cudaStream_t s )
 {
     cudaError_t e = launch_pdl( dev::k_volume_process< M >, dim3( ( a.nx + 31 ) / 32, ( a.ny + 3 ) / 4 ), dim3( 32, 4 ), 0, s, a.volume, a.nx, a.ny, a.nz );
-    if( e == cudaSuccess ) e = launch_pdl( dev::k_scatter_accum< M >, dim3( ( a.u.W + 31 ) / 32, ( a.u.H + 7 ) / 8 ), dim3( 32, 8 ), 0, s, a );
+    const dim3 g( ( a.u.W + 31 ) / 32, ( a.u.H + 7 ) / 8 ), b( 32, 8 );
+    if( e == cudaSuccess )
+        e = ( a.flags & RGDN_VOLUME_EXACT_MATH ) ? launch_pdl( dev::k_scatter_accum< M, false >, g, b, 0, s, a )
+                                                  : launch_pdl( dev::k_scatter_accum< M, true >, g, b, 0, s, a );
     return e != cudaSuccess ? e : cudaGetLastError();
 }
 
 template< int M > cudaError_t launch_final_t( const FinalArgs& f, cudaStream_t s )
 {
-    const cudaError_t e = launch_pdl( dev::k_prepare_final< M >, dim3( ( f.W + 31 ) / 32, ( f.H + 7 ) / 8 ), dim3( 32, 8 ), 0, s, f );
+    const dim3        g( ( f.W + 31 ) / 32, ( f.H + 7 ) / 8 ), b( 32, 8 );
+    const cudaError_t e = ( f.flags & RGDN_FINAL_EXACT_MATH ) ? launch_pdl( dev::k_prepare_final< M, false >, g, b, 0, s, f )
+                                                             : launch_pdl( dev::k_prepare_final< M, true >, g, b, 0, s, f );
     return e != cudaSuccess ? e : cudaGetLastError();
 }
 

@@ -430,13 +430,15 @@ def _final_inputs(W, H, mode, seed):
     return o
 
 
+@pytest.mark.parametrize("exact", [False, True])
 @pytest.mark.parametrize("mode_name,mode", MODES)
 @pytest.mark.parametrize("size", [(64, 36), (50, 23)])
-def test_prepare_final_parity(ctx, mode_name, mode, size):
+def test_prepare_final_parity(ctx, mode_name, mode, size, exact):
     """rgdn_prepare_final (CmCheckerboard + CmPrepareFinal: split-pixel resolve, scattering,
     uncharted2 / exposure + emission through LPM, bloom input) against the oracle on the same
     inputs: classic shading on the left 30 %, non-default LPM saturation and crosstalk, with
-    and without scattering."""
+    and without scattering; in the default hardware pow / reciprocal form and in the IEEE form
+    (RGDN_FINAL_EXACT_MATH), both to the same bounds."""
     W, H = size
     o = _final_inputs(W, H, mode, seed=W + H)
     s = Stream(ctx, W, H, mode)
@@ -450,7 +452,7 @@ def test_prepare_final_parity(ctx, mode_name, mode, size):
             p.lightmapScreenCoverage = 0.3
             p.saturation[:] = (-0.1, 0.0, 0.15)
             p.crosstalk[:] = (1.0, 0.5, 0.25)
-            p.flags = flags
+            p.flags = flags | (N.FINAL_EXACT_MATH if exact else 0)
             ImageComposition(s).Finalize(0, p)
             o.prepare_final(0, p)
             for name in ("FINAL", "BLOOM_INPUT"):
@@ -537,13 +539,16 @@ def _volumetric_params(mode, frame_id):
     return p
 
 
+@pytest.mark.parametrize("exact", [False, True])
 @pytest.mark.parametrize("vmode", [N.VOLUME_ENABLE_NONE, N.VOLUME_ENABLE_SIMPLE, N.VOLUME_ENABLE_VOLUMETRIC])
 @pytest.mark.parametrize("size", [(64, 36), (50, 23)])
-def test_process_scattering_parity(ctx, vmode, size):
+def test_process_scattering_parity(ctx, vmode, size, exact):
     """rgdn_process_scattering (CmVolumetricProcess + CmScatterAccum) against the oracle over
     two frames of the synthetic scene: the volume integrated in place, then SCATTERING and
     SCATTERING_HISTORY reprojected from the previous frame (random history on the first, the
-    first frame's output on the second) and mixed with this frame's fog or volume sample."""
+    first frame's output on the second) and mixed with this frame's fog or volume sample; in the
+    default hardware-math form and the IEEE form (RGDN_VOLUME_EXACT_MATH), both to the same
+    bounds."""
     W, H = size
     rng = np.random.default_rng(W * 31 + H + vmode)
     sc = Scene(W, H, seed=W + vmode)
@@ -562,6 +567,7 @@ def test_process_scattering_parity(ctx, vmode, size):
         upload_frame(s, o, {k: bufs[k] for k in ("NORMAL", "DEPTH_WORLD", "MOTION")}, fi)
         upload_frame(s, o, {"DEPTH_NDC": rng.uniform(0.1, 0.9, (H, W)).astype(np.float32)}, fi)
         p = _volumetric_params(vmode, 100 + f)
+        p.flags = N.VOLUME_EXACT_MATH if exact else 0
         Volumetric(s).ProcessScattering(fi, p)
         o.process_scattering(fi, p)
         for name in ("SCATTER_VOLUME", "SCATTERING", "SCATTERING_HISTORY"):
