@@ -2676,12 +2676,12 @@ template< int M > __device__ __forceinline__ P3 bl_sample( const void* img, int 
 // 6x6 source window is read once, a row at a time, and each row's horizontal lerps serve the
 // taps above and below it. Every tap is the same expression either way.
 template< int M >
-__device__ __forceinline__ void bloom_down_texel( const void* src, int sw, int sh, void* dst, int dw, int x, int y, int k, int W, int H )
+__device__ __forceinline__ void bloom_down_texel( const void* src, int sw, int sh, void* dst, int dw, int x, int y, int k, float4 st )
 {
-    const float idx = (float)( 1 << ( k + 1 ) ) / (float)W, idy = (float)( 1 << ( k + 1 ) ) / (float)H;
+    const float idx = st.x, idy = st.y;
     const float u = ( (float)x + 0.5f ) * idx, v = ( (float)y + 0.5f ) * idy;
     if( u > 1.0f || v > 1.0f ) return;
-    const float isx = (float)( 1 << k ) / (float)W, isy = (float)( 1 << k ) / (float)H;
+    const float isx = st.z, isy = st.w;
     BlAxis      ax[ 5 ], ay[ 5 ];
     bool        chain = true;
 #pragma unroll
@@ -2765,10 +2765,10 @@ __device__ __forceinline__ void bloom_down_texel( const void* src, int sw, int s
 // k > 0; dst is mip k, or BLOOM_RESULT for k = 0. The chained case reads the 4x4 source window
 // once and shares each row's lerps between the taps above and below it.
 template< int M >
-__device__ __forceinline__ void bloom_up_texel( const void* src, int sw, int sh, void* dst, int dw, int x, int y, int k, int W, int H )
+__device__ __forceinline__ void bloom_up_texel( const void* src, int sw, int sh, void* dst, int dw, int x, int y, int k, float4 st )
 {
-    const float isx = (float)( 1 << ( k + 1 ) ) / (float)W, isy = (float)( 1 << ( k + 1 ) ) / (float)H;
-    const float iux = (float)( 1 << k ) / (float)W, iuy = (float)( 1 << k ) / (float)H;
+    const float isx = st.x, isy = st.y;
+    const float iux = st.z, iuy = st.w;
     const float u = ( (float)x + 0.5f ) * iux + 0.5f * isx, v = ( (float)y + 0.5f ) * iuy + 0.5f * isy;
     if( u > 1.0f || v > 1.0f ) return;
     BlAxis ax[ 3 ], ay[ 3 ];
@@ -2817,13 +2817,13 @@ __device__ __forceinline__ void bloom_up_texel( const void* src, int sw, int sh,
 // steps, whose single wave is bound by one texel's chain of dependent loads; the B10G11R11
 // decode of the reference storage mode would spill at 64 registers, so it always takes 1
 template< int M, int MINB >
-__global__ void __launch_bounds__( 256, M == MODE_REF ? 1 : MINB ) k_bloom_down( const void* src, int sw, int sh, void* dst, int dw, int dh, int k, int W, int H )
+__global__ void __launch_bounds__( 256, M == MODE_REF ? 1 : MINB ) k_bloom_down( const void* src, int sw, int sh, void* dst, int dw, int dh, int k, float4 st )
 {
     const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
     pdl_launch_dependents();
     pdl_wait();
     if( x >= dw || y >= dh ) return;
-    bloom_down_texel< M >( src, sw, sh, dst, dw, x, y, k, W, H );
+    bloom_down_texel< M >( src, sw, sh, dst, dw, x, y, k, st );
 }
 
 // Upsample step k for the 2x2 quad of dst texels at (x0, y0): the four texels' tents read the
@@ -2832,11 +2832,11 @@ __global__ void __launch_bounds__( 256, M == MODE_REF ? 1 : MINB ) k_bloom_down(
 // quad, and each texel keeps its own weights. Returns false, having written nothing, when the
 // quad is not complete, a texel is outside the uv <= 1 range or the windows differ.
 template< int M >
-__device__ __forceinline__ bool bloom_up_quad( const void* src, int sw, int sh, void* dst, int dw, int dh, int x0, int y0, int k, int W, int H )
+__device__ __forceinline__ bool bloom_up_quad( const void* src, int sw, int sh, void* dst, int dw, int dh, int x0, int y0, int k, float4 st )
 {
     if( x0 + 1 >= dw || y0 + 1 >= dh ) return false;
-    const float isx = (float)( 1 << ( k + 1 ) ) / (float)W, isy = (float)( 1 << ( k + 1 ) ) / (float)H;
-    const float iux = (float)( 1 << k ) / (float)W, iuy = (float)( 1 << k ) / (float)H;
+    const float isx = st.x, isy = st.y;
+    const float iux = st.z, iuy = st.w;
     BlAxis      ax[ 2 ][ 3 ], ay[ 2 ][ 3 ];
     bool        ok = true;
 #pragma unroll
@@ -2900,40 +2900,40 @@ __device__ __forceinline__ bool bloom_up_quad( const void* src, int sw, int sh, 
 
 // one thread per dst texel (the small coarse steps)
 template< int M >
-__global__ void __launch_bounds__( 256 ) k_bloom_up( const void* src, int sw, int sh, void* dst, int dw, int dh, int k, int W, int H )
+__global__ void __launch_bounds__( 256 ) k_bloom_up( const void* src, int sw, int sh, void* dst, int dw, int dh, int k, float4 st )
 {
     const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
     pdl_launch_dependents();
     pdl_wait();
     if( x >= dw || y >= dh ) return;
-    bloom_up_texel< M >( src, sw, sh, dst, dw, x, y, k, W, H );
+    bloom_up_texel< M >( src, sw, sh, dst, dw, x, y, k, st );
 }
 
 // one thread per 2x2 quad of dst texels, blocks of 32x4 threads (the large steps)
 template< int M >
-__global__ void __launch_bounds__( 128 ) k_bloom_up_quad( const void* src, int sw, int sh, void* dst, int dw, int dh, int k, int W, int H )
+__global__ void __launch_bounds__( 128 ) k_bloom_up_quad( const void* src, int sw, int sh, void* dst, int dw, int dh, int k, float4 st )
 {
     const int x0 = 2 * ( blockIdx.x * blockDim.x + threadIdx.x ), y0 = 2 * ( blockIdx.y * blockDim.y + threadIdx.y );
     pdl_launch_dependents();
     pdl_wait();
     if( x0 >= dw || y0 >= dh ) return;
-    if( bloom_up_quad< M >( src, sw, sh, dst, dw, dh, x0, y0, k, W, H ) ) return;
+    if( bloom_up_quad< M >( src, sw, sh, dst, dw, dh, x0, y0, k, st ) ) return;
 #pragma unroll 1
     for( int q = 0; q < 4; q++ )
     {
         const int x = x0 + ( q & 1 ), y = y0 + ( q >> 1 );
-        if( x < dw && y < dh ) bloom_up_texel< M >( src, sw, sh, dst, dw, x, y, k, W, H );
+        if( x < dw && y < dh ) bloom_up_texel< M >( src, sw, sh, dst, dw, x, y, k, st );
     }
 }
 
 // FINAL += intensity * BLOOM_RESULT(uv) (CmBloomApply.comp:45-76, lens dirt not included)
-template< int M > __global__ void __launch_bounds__( 256 ) k_bloom_apply( const void* result, void* finalImg, int W, int H, float intensity )
+template< int M > __global__ void __launch_bounds__( 256 ) k_bloom_apply( const void* result, void* finalImg, int W, int H, float2 inv, float intensity )
 {
     const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
     pdl_launch_dependents();
     pdl_wait();
     if( x >= W || y >= H ) return;
-    const float u = ( (float)x + 0.5f ) * ( 1.0f / (float)W ), v = ( (float)y + 0.5f ) * ( 1.0f / (float)H );
+    const float u = ( (float)x + 0.5f ) * inv.x, v = ( (float)y + 0.5f ) * inv.y;   // inv = (1 / W, 1 / H)
     if( u > 1.0f || v > 1.0f ) return;
     const P3     bloom = pmul( bl_sample< M >( result, W, bl_axis( u, W ), bl_axis( v, H ) ), intensity );
     const size_t i     = (size_t)( y * W + x );
@@ -3240,21 +3240,28 @@ template< int M > cudaError_t launch_bloom_t( const BloomArgs& b, cudaStream_t s
     auto        grid  = []( int w, int h ) { return dim3( ( w + 31 ) / 32, ( h + 7 ) / 8 ); };
     auto        large = [ & ]( int p ) { return (long long)b.w[ p ] * b.h[ p ] >= BLOOM_LARGE_TEXELS; };
     cudaError_t e     = cudaSuccess;
+    // the texel steps of level k in uv, (2^(k+1) / W, 2^(k+1) / H, 2^k / W, 2^k / H): the IEEE
+    // quotients every texel of the shaders computes, evaluated once
+    auto st = [ & ]( int k ) {
+        return make_float4( (float)( 1 << ( k + 1 ) ) / (float)b.W, (float)( 1 << ( k + 1 ) ) / (float)b.H, (float)( 1 << k ) / (float)b.W,
+                            (float)( 1 << k ) / (float)b.H );
+    };
     for( int k = 0; k < 8 && e == cudaSuccess; k++ )
         e = launch_pdl( large( k + 1 ) ? dev::k_bloom_down< M, 4 > : dev::k_bloom_down< M, 1 >, grid( b.w[ k + 1 ], b.h[ k + 1 ] ), blk, 0, s,
-                        (const void*)b.planes[ k ], b.w[ k ], b.h[ k ], b.planes[ k + 1 ], b.w[ k + 1 ], b.h[ k + 1 ], k, b.W, b.H );
+                        (const void*)b.planes[ k ], b.w[ k ], b.h[ k ], b.planes[ k + 1 ], b.w[ k + 1 ], b.h[ k + 1 ], k, st( k ) );
     for( int k = 7; k >= 0 && e == cudaSuccess; k-- )
     {
         const int d = k == 0 ? 9 : k;
         if( large( d ) )
             e = launch_pdl( dev::k_bloom_up_quad< M >, dim3( ( b.w[ d ] + 63 ) / 64, ( b.h[ d ] + 7 ) / 8 ), dim3( 32, 4 ), 0, s,
-                            (const void*)b.planes[ k + 1 ], b.w[ k + 1 ], b.h[ k + 1 ], b.planes[ d ], b.w[ d ], b.h[ d ], k, b.W, b.H );
+                            (const void*)b.planes[ k + 1 ], b.w[ k + 1 ], b.h[ k + 1 ], b.planes[ d ], b.w[ d ], b.h[ d ], k, st( k ) );
         else
             e = launch_pdl( dev::k_bloom_up< M >, grid( b.w[ d ], b.h[ d ] ), blk, 0, s, (const void*)b.planes[ k + 1 ], b.w[ k + 1 ], b.h[ k + 1 ],
-                            b.planes[ d ], b.w[ d ], b.h[ d ], k, b.W, b.H );
+                            b.planes[ d ], b.w[ d ], b.h[ d ], k, st( k ) );
     }
     if( e == cudaSuccess )
-        e = launch_pdl( dev::k_bloom_apply< M >, grid( b.W, b.H ), blk, 0, s, (const void*)b.planes[ 9 ], b.planes[ 10 ], b.W, b.H, b.intensity );
+        e = launch_pdl( dev::k_bloom_apply< M >, grid( b.W, b.H ), blk, 0, s, (const void*)b.planes[ 9 ], b.planes[ 10 ], b.W, b.H,
+                        make_float2( 1.0f / (float)b.W, 1.0f / (float)b.H ), b.intensity );
     return e != cudaSuccess ? e : cudaGetLastError();
 }
 
