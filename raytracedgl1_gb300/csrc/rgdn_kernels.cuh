@@ -3174,7 +3174,7 @@ __device__ __forceinline__ float4 scatter_pixel( const ScatterArgs& a, int cx, i
 
 // One thread per checkerboard pixel. (One thread per pair (cx, cx + W/2), whose regular pixels
 // are neighbours, wrote full sectors but ran 10 % slower: half the warps to hide latency.)
-template< int M, bool FAST > __global__ void __launch_bounds__( 256 ) k_scatter_accum( const ScatterArgs a )
+template< int M, bool FAST > __global__ void __launch_bounds__( 256, 6 ) k_scatter_accum( const ScatterArgs a )
 {
     __shared__ float inv255[ 256 ];
     for( int t = threadIdx.y * blockDim.x + threadIdx.x; t < 256; t += blockDim.x * blockDim.y ) inv255[ t ] = (float)t / 255.0f;
