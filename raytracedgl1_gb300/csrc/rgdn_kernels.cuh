@@ -2288,7 +2288,7 @@ template< bool GRAD, class F > __device__ __forceinline__ void batch_tiles( cons
     }
 }
 
-template< int M > __global__ void __launch_bounds__( 256 ) kb_gradient_samples( const int slot )
+template< int M > __global__ void __launch_bounds__( 256, 6 ) kb_gradient_samples( const int slot )
 {
     __shared__ float u8[ 256 ];
     fill_u8( u8, threadIdx.y * blockDim.x + threadIdx.x );
