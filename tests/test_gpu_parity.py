@@ -634,6 +634,45 @@ def test_process_scattering_parity_1080p(ctx):
     s.close()
 
 
+def test_process_scattering_bound_inputs(ctx):
+    """A producer that owns its images binds them (rgdn_stream_bind_framebuffer) instead of
+    uploading: the froxel volume (processed in place in the caller's memory), the NDC depth and
+    the G-buffer planes the accumulation reads give SCATTERING bits equal to the uploaded
+    stream's. Output-only images cannot be bound."""
+    torch = pytest.importorskip("torch")
+    W, H = 64, 36
+    rng = np.random.default_rng(21)
+    sc = Scene(W, H, seed=21)
+    up = Stream(ctx, W, H, N.STORAGE_FP16)
+    bd = Stream(ctx, W, H, N.STORAGE_FP16)
+    nz, ny, nx = N.VOLUME_SIZE[2], N.VOLUME_SIZE[1], N.VOLUME_SIZE[0]
+    vol = np.concatenate([rng.uniform(0, 0.5, (ny * nz, nx, 3)), rng.uniform(0, 0.1, (ny * nz, nx, 1))], axis=2)
+    inputs = {"SCATTER_VOLUME": vol.astype(np.float16).view(np.uint16),
+              "DEPTH_NDC": rng.uniform(0.1, 0.9, (H, W)).astype(np.float32)}
+    bufs, _ = sc.generate(0)
+    inputs.update({k: bufs[k] for k in ("NORMAL", "DEPTH_WORLD", "MOTION")})
+    keep = []
+    for name, arr in inputs.items():
+        up.upload(name, 0, arr)
+        t = torch.from_numpy(np.ascontiguousarray(arr).view(np.uint8).reshape(-1).copy()).cuda()
+        keep.append(t)
+        bd.bind(name, 0, t.data_ptr())
+    torch.cuda.synchronize()
+    p = _volumetric_params(N.VOLUME_ENABLE_VOLUMETRIC, 3)
+    Volumetric(up).ProcessScattering(0, p)
+    Volumetric(bd).ProcessScattering(0, p)
+    for name in ("SCATTERING", "SCATTERING_HISTORY"):
+        assert np.array_equal(up.download(name, 0), bd.download(name, 0)), name
+    processed = keep[0].cpu().numpy().view(np.uint16).reshape(up.download("SCATTER_VOLUME", 0).shape)
+    assert np.array_equal(processed, up.download("SCATTER_VOLUME", 0))
+    with pytest.raises(N.RgdnError):
+        bd.bind("SCATTERING_HISTORY", 0, keep[1].data_ptr())
+    for name in inputs:
+        bd.bind(name, 0, None)
+    up.close()
+    bd.close()
+
+
 def test_process_scattering_rejects_bad_params(ctx):
     s = Stream(ctx, 64, 36)
     p = _volumetric_params(N.VOLUME_ENABLE_VOLUMETRIC, 0)
