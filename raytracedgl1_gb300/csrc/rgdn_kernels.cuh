@@ -631,6 +631,8 @@ __device__ __forceinline__ float parallax( const Uniform& u, float3 pos, float3 
 // at the taps.
 // the temporal pass reads each in-area tap's history together with its geometry
 constexpr bool kTemporalEarlyHistory = true;
+// the temporal pass reads the surface positions before the taps rather than where they are used
+constexpr bool kTemporalEarlySurfPos = false;
 template< int M, bool FAST, bool GEOM, bool GEOMPREV >
 __device__ __forceinline__ void temporal_tile( const FrameArgs& a, int bx, int by, const float* u8 )
 {
@@ -691,11 +693,14 @@ __device__ __forceinline__ void temporal_tile( const FrameArgs& a, int bx, int b
             if( tx.var ) asm volatile( "prefetch.global.L2 [%0];" ::"l"( a.varHistory + q ) );
         }
     }
-    // the surface positions the specular terms read once a tap is accepted, loaded with the
-    // taps rather than after them
-    const float4 sp4 = a.surfPos[ i ];
-    const float4 spp4 =
-        inside( u, pixPrev.x, pixPrev.y ) ? a.surfPosPrev[ pixPrev.y * u.W + pixPrev.x ] : make_float4( 0, 0, 0, 0 );
+    // the surface positions the specular terms read once a tap is accepted: loaded with the
+    // taps (kTemporalEarlySurfPos) or where they are used
+    float4 sp4 = make_float4( 0, 0, 0, 0 ), spp4 = make_float4( 0, 0, 0, 0 );
+    auto   ldSurf = [ & ]() {
+        sp4  = a.surfPos[ i ];
+        spp4 = inside( u, pixPrev.x, pixPrev.y ) ? a.surfPosPrev[ pixPrev.y * u.W + pixPrev.x ] : make_float4( 0, 0, 0, 0 );
+    };
+    if( kTemporalEarlySurfPos ) ldSurf();
 
     float4 histLenDIS     = make_float4( 0, 0, 0, 0 );
     float3 diffPrev       = f3( 0, 0, 0 );
@@ -809,6 +814,7 @@ __device__ __forceinline__ void temporal_tile( const FrameArgs& a, int bx, int b
         const float specHistoryLength   = FAST ? histLenDIS.z * invWS : histLenDIS.z / weightSum;
         const float specHitDistancePrev = FAST ? histLenDIS.w * invWS : histLenDIS.w / weightSum;
 
+        if( !kTemporalEarlySurfPos ) ldSurf();
         const float3 surfPos     = f3( sp4.x, sp4.y, sp4.z );
         const float3 surfPosPrev = f3( spp4.x, spp4.y, spp4.z );
         const float nv = fmaxf( 0.0f, X::dot( normal, f3( -rayInfo.x, -rayInfo.y, -rayInfo.z ) ) );
