@@ -633,6 +633,8 @@ __device__ __forceinline__ float parallax( const Uniform& u, float3 pos, float3 
 constexpr bool kTemporalEarlyHistory = true;
 // the temporal pass reads the surface positions before the taps rather than where they are used
 constexpr bool kTemporalEarlySurfPos = false;
+// the temporal pass prefetches the history rows under its bilinear footprint into L2
+constexpr bool kTemporalL2Prefetch = true;
 template< int M, bool FAST, bool GEOM, bool GEOMPREV >
 __device__ __forceinline__ void temporal_tile( const FrameArgs& a, int bx, int by, const float* u8 )
 {
@@ -677,7 +679,7 @@ __device__ __forceinline__ void temporal_tile( const FrameArgs& a, int bx, int b
     };
     // FAST: an L2 prefetch of the history rows under the bilinear footprint, so the history
     // loads that follow the reprojection tests find them on chip
-    if( FAST && pixPrev.x >= 0 && pixPrev.y >= 0 && pixPrev.x + 1 < u.W && pixPrev.y + 1 < u.H )
+    if( FAST && kTemporalL2Prefetch && pixPrev.x >= 0 && pixPrev.y >= 0 && pixPrev.x + 1 < u.W && pixPrev.y + 1 < u.H )
     {
         const TmaTexel tx = tma_texel( M == MODE_REF ? RGDN_STORAGE_REF : M == MODE_F32 ? RGDN_STORAGE_FP32 : RGDN_STORAGE_FP16 );
         const int      mb = M == MODE_REF ? 4 : 8;   // moments
@@ -1808,6 +1810,9 @@ __device__ __forceinline__ void atrous_px( const FrameArgs& a, const AtrousIO& i
 
 // The tile of one a-trous iteration. HIST adds the bins of this tile's HistogramInput values
 // to the block's shared histogram `hist` (the caller zeroes and flushes it).
+// the last a-trous iteration loads the composition's G-buffer texels before its taps (held in
+// registers across the taps: slower) or after them
+constexpr bool kComposeEarlyLoads = false;
 template< int M, bool FAST, bool HIST, bool GEOMIN >
 __device__ __forceinline__ void atrous_tile( const FrameArgs& a, const int iter, int bx, int by, const float* u8, uint32_t* hist )
 {
@@ -1829,9 +1834,10 @@ __device__ __forceinline__ void atrous_tile( const FrameArgs& a, const int iter,
         const bool interior = bx0 - step >= 0 && by0 - step >= 0 && bx1 + step < u.W && by1 + step < u.H &&
                               ( bx1 + step < sep || bx0 - step >= sep );
         ComposeIn cin;
-        if( last ) cin = compose_load( a, px, py, i );
+        if( last && kComposeEarlyLoads ) cin = compose_load( a, px, py, i );
         if( interior ) atrous_px< M, FAST, true, GEOMIN >( a, io, iter, px, py, i, u8, outDiff, outVar, outSpec, outInd );
         else atrous_px< M, FAST, false, GEOMIN >( a, io, iter, px, py, i, u8, outDiff, outVar, outSpec, outInd );
+        if( last && !kComposeEarlyLoads ) cin = compose_load( a, px, py, i );
         if( !last )
         {
             S::stcv( io.diffDst, io.varDst, (size_t)i, outDiff, outVar );
