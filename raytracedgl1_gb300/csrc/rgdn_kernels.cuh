@@ -635,6 +635,8 @@ constexpr bool kTemporalEarlyHistory = true;
 constexpr bool kTemporalEarlySurfPos = false;
 // the temporal pass prefetches the history rows under its bilinear footprint into L2
 constexpr bool kTemporalL2Prefetch = true;
+// the temporal pass reads this frame's unfiltered colours and view ray before its taps
+constexpr bool kTemporalEarlyInputs = true;
 template< int M, bool FAST, bool GEOM, bool GEOMPREV >
 __device__ __forceinline__ void temporal_tile( const FrameArgs& a, int bx, int by, const float* u8 )
 {
@@ -646,11 +648,18 @@ __device__ __forceinline__ void temporal_tile( const FrameArgs& a, int bx, int b
     if( px >= u.W || py >= u.H ) return;
     const int i = py * u.W + px;
 
-    const float3   unfilteredDiff  = e5( a.unfD[ i ] );
-    const float3   unfilteredIndir = e5( a.unfI[ i ] );
-    const float3   unfilteredSpec  = e5( a.unfS[ i ] );
-    const ushort4  rv              = a.viewDir[ i ];
-    const float4   rayInfo         = make_float4( h2f( rv.x ), h2f( rv.y ), h2f( rv.z ), h2f( rv.w ) );
+    // this frame's unfiltered colours and view ray, used only after the taps: read before them
+    // (kTemporalEarlyInputs) or after them, so that they hold no registers across the tap loop
+    float3 unfilteredDiff, unfilteredIndir, unfilteredSpec;
+    float4 rayInfo;
+    auto   ldInputs = [ & ]() {
+        unfilteredDiff     = e5( a.unfD[ i ] );
+        unfilteredIndir    = e5( a.unfI[ i ] );
+        unfilteredSpec     = e5( a.unfS[ i ] );
+        const ushort4 rv   = a.viewDir[ i ];
+        rayInfo            = make_float4( h2f( rv.x ), h2f( rv.y ), h2f( rv.z ), h2f( rv.w ) );
+    };
+    if( kTemporalEarlyInputs ) ldInputs();
     const Area     chArea          = cb_area( u, px );
     const ushort4  mo              = a.motion[ i ];
     const float    motionZ         = h2f( mo.z );
@@ -662,8 +671,6 @@ __device__ __forceinline__ void temporal_tile( const FrameArgs& a, int bx, int b
     const float    roughness       = u8[ mrBits >> 8 ];
     if( GEOM ) a.geom[ i ] = geo_pack( normal, zBits, mrBits );
 
-    const float  l       = X::lum( unfilteredDiff );
-    const float2 moments = make_float2( l, l * l );
 
     int2   pixPrev;
     float2 subPix;
@@ -802,7 +809,10 @@ __device__ __forceinline__ void temporal_tile( const FrameArgs& a, int bx, int b
         }
     }
 
-    const bool hasHistory = weightSum > 0.0001f;
+    if( !kTemporalEarlyInputs ) ldInputs();
+    const float  l          = X::lum( unfilteredDiff );
+    const float2 moments    = make_float2( l, l * l );
+    const bool   hasHistory = weightSum > 0.0001f;
     // FAST: the one IEEE reciprocal both the continuous averages and the diffuse history
     // length use
     const float invWS = ( FAST && hasHistory ) ? 1.0f / weightSum : 0.0f;
