@@ -211,6 +211,11 @@ typedef struct rgdn_frame_params
 #define RGDN_FLAG_TMA_STAGING        0x8u /* a-trous taps staged in shared memory by the Tensor
                                              Memory Accelerator (widths divisible by 4, up to 5
                                              iterations); the same results as the default kernels */
+#define RGDN_FLAG_STAGE_DEFAULT      0x10u /* rgdn_denoise_stage runs the default path's kernel for
+                                             the stage (with RGDN_FLAG_EXACT_MATH: its IEEE form)
+                                             instead of the one-kernel-per-dispatch form; the last
+                                             a-trous iteration then also bins the histogram, and
+                                             RGDN_STAGE_LUMINANCE_HISTOGRAM does nothing */
 
 /* debugShowFlags bits used on this path (ShaderCommonC.h:156-166) */
 #define RGDN_DEBUG_SHOW_FLAG_ONLY_DIRECT_DIFFUSE   ( 1u << 5 )
@@ -372,8 +377,9 @@ typedef struct rgdn_volumetric_params
                                        (the reprojection tests decide exactly either way) */
 rgdn_status rgdn_process_scattering( rgdn_stream* stream, uint32_t frameIndex, const rgdn_volumetric_params* params, rgdn_cuda_stream cudaStream );
 
-/* One stage alone (the plain path / per-stage checking). `iteration` selects the
- * a-trous or gradient a-trous iteration. */
+/* One stage alone (per-stage checking): the plain path's kernel, or with
+ * RGDN_FLAG_STAGE_DEFAULT the default path's. `iteration` selects the a-trous or gradient
+ * a-trous iteration. */
 rgdn_status rgdn_denoise_stage( rgdn_stream* stream, uint32_t stage, uint32_t iteration, uint32_t frameIndex, const rgdn_frame_params* params, rgdn_cuda_stream cudaStream );
 
 /* ShTonemapping { uint histogram[256]; float avgLuminance; } (ShaderCommonC.h:344-348):
@@ -508,6 +514,9 @@ typedef struct rgdn_server_stats
     float    p50Ms, p99Ms, maxMs;     /* latency of the frames done since the last reset */
     float    meanFramesPerStep;
     double   busySeconds;             /* wall time with at least one step on the GPU */
+    float    p99AllMs;                /* p99 over every finished request, a dropped one counting as
+                                         an unbounded latency (+infinity once drops pass 1 %) */
+    float    dropRate;                /* framesDropped / (framesDone + framesDropped) */
 } rgdn_server_stats;
 
 rgdn_status rgdn_server_create( rgdn_context* ctx, const rgdn_server_create_info* info, rgdn_server** outServer );
@@ -540,9 +549,11 @@ rgdn_status rgdn_server_get_stream( rgdn_server* server, uint32_t streamId, rgdn
  * intermediate image lives in a fixed array inside the library: at most 1280 x 720 strata
  * (3840x2160 renders); larger sizes return RGDN_WRONG_FUNCTION_ARGUMENT. Nothing is allocated.
  * The first call on a device looks the array up (cudaGetSymbolAddress) with that device
- * current; make that first call before capturing a stream. All calls share the one array:
- * calls whose work overlaps on the GPU (other streams, other threads) race on it and must be
- * serialised by the caller. `filtered` must not alias `samples` or `history`. */
+ * current, and so does the first call in any other CUDA context (a non-primary context, or the
+ * primary one created again after cudaDeviceReset); make that first call before capturing a
+ * stream. All calls share the one array: calls whose work overlaps on the GPU (other streams,
+ * other threads) race on it and must be serialised by the caller. The three images must not
+ * overlap; equal pointers return RGDN_WRONG_FUNCTION_ARGUMENT. */
 rgdn_status rgdn_gradient_atrous_noalloc( const uint32_t* samples, uint32_t* filtered, uint32_t* history, uint32_t renderWidth,
                                           uint32_t renderHeight, rgdn_cuda_stream cudaStream );
 

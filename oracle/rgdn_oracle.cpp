@@ -1403,6 +1403,21 @@ template< class T > struct Denoise
 //  Exposure application and tonemapping: CmCheckerboard.comp:27-69 + CmPrepareFinal.comp:57-187
 // ============================================================================================
 
+// The LPM setup and filter restated below follow AMD FidelityFX LPM, which carries this notice:
+//   Copyright (c) 2017-2019 Advanced Micro Devices, Inc. All rights reserved.
+//   Permission is hereby granted, free of charge, to any person obtaining a copy of this
+//   software and associated documentation files (the "Software"), to deal in the Software
+//   without restriction, including without limitation the rights to use, copy, modify, merge,
+//   publish, distribute, sublicense, and/or sell copies of the Software, and to permit persons
+//   to whom the Software is furnished to do so, subject to the following conditions:
+//   The above copyright notice and this permission notice shall be included in all copies or
+//   substantial portions of the Software.
+//   THE SOFTWARE IS PROVIDED "AS IS", WITHOUT WARRANTY OF ANY KIND, EXPRESS OR IMPLIED,
+//   INCLUDING BUT NOT LIMITED TO THE WARRANTIES OF MERCHANTABILITY, FITNESS FOR A PARTICULAR
+//   PURPOSE AND NONINFRINGEMENT. IN NO EVENT SHALL THE AUTHORS OR COPYRIGHT HOLDERS BE LIABLE FOR
+//   ANY CLAIM, DAMAGES OR OTHER LIABILITY, WHETHER IN AN ACTION OF CONTRACT, TORT OR OTHERWISE,
+//   ARISING FROM, OUT OF OR IN CONNECTION WITH THE SOFTWARE OR THE USE OR OTHER DEALINGS IN THE
+//   SOFTWARE.
 // AMD FidelityFX LPM 1.0 (vendored as Shaders/LPM/ffx_lpm.h), the 709 -> 709 configuration
 // without shoulder tuning that ImageComposition uses. Setup: LpmSetupCustom.inl:40-70;
 // LpmColRgbToXyz / LpmMatInv3x3 (ffx_lpm.h:157-210) for the luma coefficients. Filter:

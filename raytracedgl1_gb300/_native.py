@@ -49,7 +49,7 @@ STAGE_GRADIENT_SAMPLES, STAGE_GRADIENT_ATROUS, STAGE_TEMPORAL_ACCUMULATION = 0, 
 STAGE_ANTI_FIREFLY, STAGE_VARIANCE_ESTIMATION, STAGE_ATROUS = 3, 4, 5
 STAGE_LUMINANCE_HISTOGRAM, STAGE_LUMINANCE_AVG = 6, 7
 
-FLAG_PLAIN, FLAG_SKIP_GRADIENTS, FLAG_EXACT_MATH, FLAG_TMA_STAGING = 0x1, 0x2, 0x4, 0x8
+FLAG_PLAIN, FLAG_SKIP_GRADIENTS, FLAG_EXACT_MATH, FLAG_TMA_STAGING, FLAG_STAGE_DEFAULT = 0x1, 0x2, 0x4, 0x8, 0x10
 
 
 class FinalParams(C.Structure):
@@ -173,7 +173,8 @@ class ServerStats(C.Structure):
     _fields_ = [("framesDone", C.c_uint64), ("framesDropped", C.c_uint64), ("steps", C.c_uint64),
                 ("pixelsDone", C.c_uint64), ("residentStreams", C.c_uint32), ("queuedFrames", C.c_uint32),
                 ("residentBytes", C.c_uint64), ("p50Ms", C.c_float), ("p99Ms", C.c_float), ("maxMs", C.c_float),
-                ("meanFramesPerStep", C.c_float), ("busySeconds", C.c_double)]
+                ("meanFramesPerStep", C.c_float), ("busySeconds", C.c_double), ("p99AllMs", C.c_float),
+                ("dropRate", C.c_float)]
 
 
 class Job(C.Structure):

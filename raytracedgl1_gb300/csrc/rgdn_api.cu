@@ -433,44 +433,80 @@ rgdn_status run_denoise( rgdn_stream* s, uint32_t fi, const rgdn_frame_params* p
     return RGDN_SUCCESS;
 }
 
-// Default path: gradient samples and the 4 gradient a-trous iterations, temporal accumulation
-// (which also writes the per-pixel geometry record the later passes read), anti-firefly on
-// packed values, variance, the a-trous iterations, and the histogram accumulated by the last
-// iteration (HistogramInput is still written). Continuous weights use FAST math.
+// One reference stage on the default path's kernel (run_denoise_fused, and rgdn_denoise_stage
+// with RGDN_FLAG_STAGE_DEFAULT): the temporal pass also writes the per-pixel geometry record the
+// later passes read, the last a-trous iteration also bins the histogram, and the histogram stage
+// itself is then empty. The caller has filled `a` for frame slot `fi` and made the bin table
+// current.
+rgdn_status launch_default_stage( rgdn_stream* s, const FrameArgs& a, uint32_t fi, const rgdn_frame_params* p, int stage, int iter,
+                                  cudaStream_t cs )
+{
+    const bool exact = ( p->flags & RGDN_FLAG_EXACT_MATH ) != 0;
+    switch( stage )
+    {
+        case RGDN_STAGE_GRADIENT_SAMPLES:
+        case RGDN_STAGE_GRADIENT_ATROUS: return launch( s, a, stage, iter, cs );
+        case RGDN_STAGE_TEMPORAL_ACCUMULATION:
+        {
+            const bool  gp = s->geomValid[ fi ^ 1u ];
+            const int   ta = exact ? ( gp ? KF_TEMPORAL_EXACT_GEOM_GP : KF_TEMPORAL_EXACT_GEOM ) : ( gp ? KF_TEMPORAL_FAST_GP : KF_TEMPORAL_FAST );
+            rgdn_status r  = launch( s, a, ta, 0, cs );
+            if( r == RGDN_SUCCESS ) s->geomValid[ fi ] = true;
+            return r;
+        }
+        case RGDN_STAGE_ANTI_FIREFLY: return launch( s, a, KF_ANTI_FIREFLY_FAST, 0, cs );
+        case RGDN_STAGE_VARIANCE_ESTIMATION: return launch( s, a, exact ? KF_VARIANCE_EXACT_GEOM : KF_VARIANCE_FAST, 0, cs );
+        case RGDN_STAGE_ATROUS:
+        {
+            // a histogram no exposure pass consumed is discarded: this frame's replaces it
+            if( iter == 0 && s->histPending )
+            {
+                if( cudaMemsetAsync( s->tm->histogram, 0, sizeof( s->tm->histogram ), cs ) != cudaSuccess ) return RGDN_DEVICE_ERROR;
+                s->histPending = false;
+            }
+            const bool  last = iter + 1 == (int)a.u.niter;
+            rgdn_status r;
+            if( !exact && ( p->flags & RGDN_FLAG_TMA_STAGING ) && tma_atrous_ok( s, iter ) ) r = launch_atrous_tma( s, a, iter, last, cs );
+            else
+            {
+                const int k = exact ? ( last ? KF_ATROUS_EXACT_HIST : KF_ATROUS_EXACT ) : ( last ? KF_ATROUS_FAST_HIST : KF_ATROUS_FAST );
+                r = launch( s, a, k, iter, cs );
+            }
+            if( r == RGDN_SUCCESS && last ) s->histPending = true;
+            return r;
+        }
+        case RGDN_STAGE_LUMINANCE_HISTOGRAM: return RGDN_SUCCESS;
+        case RGDN_STAGE_LUMINANCE_AVG:
+        {
+            // binned by the last a-trous iteration, or by nothing (an average of an empty
+            // histogram, as the plain path's order would give without its histogram pass)
+            s->histPending = false;
+            return launch( s, a, RGDN_STAGE_LUMINANCE_AVG, 0, cs );
+        }
+        default: return RGDN_WRONG_FUNCTION_ARGUMENT;
+    }
+}
+
+// Default path: gradient samples and the 4 gradient a-trous iterations, temporal accumulation,
+// anti-firefly on packed values, variance, the a-trous iterations, and the histogram
+// accumulated by the last iteration (HistogramInput is still written). Continuous weights use
+// FAST math.
 rgdn_status run_denoise_fused( rgdn_stream* s, uint32_t fi, const rgdn_frame_params* p, cudaStream_t cs )
 {
     rgdn_status r = ensure_bin_lut( s, p, cs );
     if( r != RGDN_SUCCESS ) return r;
     FrameArgs a;
     fill_args( s, fi, p, a );
-    const bool exact = ( p->flags & RGDN_FLAG_EXACT_MATH ) != 0;
     if( !( p->flags & RGDN_FLAG_SKIP_GRADIENTS ) )
     {
-        if( ( r = launch( s, a, RGDN_STAGE_GRADIENT_SAMPLES, 0, cs ) ) != RGDN_SUCCESS ) return r;
+        if( ( r = launch_default_stage( s, a, fi, p, RGDN_STAGE_GRADIENT_SAMPLES, 0, cs ) ) != RGDN_SUCCESS ) return r;
         for( int i = 0; i < 4; i++ )
-            if( ( r = launch( s, a, RGDN_STAGE_GRADIENT_ATROUS, i, cs ) ) != RGDN_SUCCESS ) return r;
+            if( ( r = launch_default_stage( s, a, fi, p, RGDN_STAGE_GRADIENT_ATROUS, i, cs ) ) != RGDN_SUCCESS ) return r;
     }
-    const bool gp = s->geomValid[ fi ^ 1u ];
-    const int  ta = exact ? ( gp ? KF_TEMPORAL_EXACT_GEOM_GP : KF_TEMPORAL_EXACT_GEOM ) : ( gp ? KF_TEMPORAL_FAST_GP : KF_TEMPORAL_FAST );
-    if( ( r = launch( s, a, ta, 0, cs ) ) != RGDN_SUCCESS ) return r;
-    s->geomValid[ fi ] = true;
-    if( ( r = launch( s, a, KF_ANTI_FIREFLY_FAST, 0, cs ) ) != RGDN_SUCCESS ) return r;
-    if( ( r = launch( s, a, exact ? KF_VARIANCE_EXACT_GEOM : KF_VARIANCE_FAST, 0, cs ) ) != RGDN_SUCCESS ) return r;
-    // a histogram no exposure pass consumed is discarded: this frame's replaces it
-    if( s->histPending && cudaMemsetAsync( s->tm->histogram, 0, sizeof( s->tm->histogram ), cs ) != cudaSuccess )
-        return RGDN_DEVICE_ERROR;
+    for( int stage : { (int)RGDN_STAGE_TEMPORAL_ACCUMULATION, (int)RGDN_STAGE_ANTI_FIREFLY, (int)RGDN_STAGE_VARIANCE_ESTIMATION } )
+        if( ( r = launch_default_stage( s, a, fi, p, stage, 0, cs ) ) != RGDN_SUCCESS ) return r;
     for( uint32_t i = 0; i < a.u.niter; i++ )
-    {
-        const bool last = i + 1 == a.u.niter;
-        if( !exact && ( p->flags & RGDN_FLAG_TMA_STAGING ) && tma_atrous_ok( s, (int)i ) )
-        {
-            if( ( r = launch_atrous_tma( s, a, (int)i, last, cs ) ) != RGDN_SUCCESS ) return r;
-            continue;
-        }
-        const int k = exact ? ( last ? KF_ATROUS_EXACT_HIST : KF_ATROUS_EXACT ) : ( last ? KF_ATROUS_FAST_HIST : KF_ATROUS_FAST );
-        if( ( r = launch( s, a, k, (int)i, cs ) ) != RGDN_SUCCESS ) return r;
-    }
-    s->histPending = true;
+        if( ( r = launch_default_stage( s, a, fi, p, RGDN_STAGE_ATROUS, (int)i, cs ) ) != RGDN_SUCCESS ) return r;
     return RGDN_SUCCESS;
 }
 
@@ -604,6 +640,21 @@ static void rec709_luma( double y[ 3 ] )
     }
 }
 
+// The LPM setup and filter restated below follow AMD FidelityFX LPM, which carries this notice:
+//   Copyright (c) 2017-2019 Advanced Micro Devices, Inc. All rights reserved.
+//   Permission is hereby granted, free of charge, to any person obtaining a copy of this
+//   software and associated documentation files (the "Software"), to deal in the Software
+//   without restriction, including without limitation the rights to use, copy, modify, merge,
+//   publish, distribute, sublicense, and/or sell copies of the Software, and to permit persons
+//   to whom the Software is furnished to do so, subject to the following conditions:
+//   The above copyright notice and this permission notice shall be included in all copies or
+//   substantial portions of the Software.
+//   THE SOFTWARE IS PROVIDED "AS IS", WITHOUT WARRANTY OF ANY KIND, EXPRESS OR IMPLIED,
+//   INCLUDING BUT NOT LIMITED TO THE WARRANTIES OF MERCHANTABILITY, FITNESS FOR A PARTICULAR
+//   PURPOSE AND NONINFRINGEMENT. IN NO EVENT SHALL THE AUTHORS OR COPYRIGHT HOLDERS BE LIABLE FOR
+//   ANY CLAIM, DAMAGES OR OTHER LIABILITY, WHETHER IN AN ACTION OF CONTRACT, TORT OR OTHERWISE,
+//   ARISING FROM, OUT OF OR IN CONNECTION WITH THE SOFTWARE OR THE USE OR OTHER DEALINGS IN THE
+//   SOFTWARE.
 // LpmSetupCustom.inl:40-70 for the 709 -> 709 arguments ImageComposition::SetupLpmParams
 // passes, in FP32 in the setup's order; the luma coefficients are the Rec.709 Y row normalised
 // to a unit sum
@@ -1123,9 +1174,11 @@ rgdn_status rgdn_denoise_stage( rgdn_stream* s, uint32_t stage, uint32_t iterati
     if( stage == RGDN_STAGE_GRADIENT_ATROUS && iteration > 3 ) return RGDN_WRONG_FUNCTION_ARGUMENT;
     if( stage == RGDN_STAGE_ATROUS && iteration >= niter ) return RGDN_WRONG_FUNCTION_ARGUMENT;
     cudaSetDevice( s->ctx->device );
-    if( stage == RGDN_STAGE_LUMINANCE_HISTOGRAM && ( r = ensure_bin_lut( s, p, (cudaStream_t)cs ) ) != RGDN_SUCCESS ) return r;
+    const bool def = ( p->flags & RGDN_FLAG_STAGE_DEFAULT ) != 0;
+    if( ( def || stage == RGDN_STAGE_LUMINANCE_HISTOGRAM ) && ( r = ensure_bin_lut( s, p, (cudaStream_t)cs ) ) != RGDN_SUCCESS ) return r;
     FrameArgs a;
     fill_args( s, frameIndex, p, a );
+    if( def ) return launch_default_stage( s, a, frameIndex, p, (int)stage, (int)iteration, (cudaStream_t)cs );
     return launch( s, a, (int)stage, (int)iteration, (cudaStream_t)cs );
 }
 

@@ -2529,6 +2529,21 @@ __device__ __forceinline__ float u2_op( float x )
     return ( ( x * ( A * x + C * B ) + D * E ) / ( x * ( A * x + B ) + D * F ) ) - E / F;
 }
 
+// The LPM setup and filter restated below follow AMD FidelityFX LPM, which carries this notice:
+//   Copyright (c) 2017-2019 Advanced Micro Devices, Inc. All rights reserved.
+//   Permission is hereby granted, free of charge, to any person obtaining a copy of this
+//   software and associated documentation files (the "Software"), to deal in the Software
+//   without restriction, including without limitation the rights to use, copy, modify, merge,
+//   publish, distribute, sublicense, and/or sell copies of the Software, and to permit persons
+//   to whom the Software is furnished to do so, subject to the following conditions:
+//   The above copyright notice and this permission notice shall be included in all copies or
+//   substantial portions of the Software.
+//   THE SOFTWARE IS PROVIDED "AS IS", WITHOUT WARRANTY OF ANY KIND, EXPRESS OR IMPLIED,
+//   INCLUDING BUT NOT LIMITED TO THE WARRANTIES OF MERCHANTABILITY, FITNESS FOR A PARTICULAR
+//   PURPOSE AND NONINFRINGEMENT. IN NO EVENT SHALL THE AUTHORS OR COPYRIGHT HOLDERS BE LIABLE FOR
+//   ANY CLAIM, DAMAGES OR OTHER LIABILITY, WHETHER IN AN ACTION OF CONTRACT, TORT OR OTHERWISE,
+//   ARISING FROM, OUT OF OR IN CONNECTION WITH THE SOFTWARE OR THE USE OR OTHER DEALINGS IN THE
+//   SOFTWARE.
 // LpmMap (ffx_lpm.h, AMD FidelityFX LPM 1.0) with LPM_CONFIG_709_709 and no shoulder: the ratio
 // of the colour to its maximum, raised to the saturation powers; luma tone-mapped by
 // luma^c / (luma^c * scale + bias); the ratio scaled to hit that luma without clipping; then

@@ -11,7 +11,10 @@
 // image is a file-scope __device__ array of fixed capacity (kMaxStrata rgba8 texels, 3.5 MiB),
 // which every GPU that loads the library holds until the process exits. Host code cannot
 // use the array's name as a device address (in host code it names a host-side shadow), so
-// the address is taken once per device with cudaGetSymbolAddress and passed to the kernel.
+// the address is taken with cudaGetSymbolAddress, with the device current, and passed to the
+// kernel. It is looked up once per CUDA context: a context that is not the device's primary
+// one, or the primary context created again after cudaDeviceReset, loads the module anew and
+// may place the array elsewhere, so the cached address is keyed by the context handle.
 #include <mutex>
 
 #include "rgdn_kernels.cuh"
@@ -24,8 +27,28 @@ constexpr int kMaxStrata = 1280 * 720;
 static __device__ __align__( 256 ) uint32_t g_gradientScratch[ kMaxStrata ];
 
 constexpr int kMaxDevices = 64;
+// per device: the context the address was taken in, and the address
+void*         g_scratchContext[ kMaxDevices ] = {};
 void*         g_scratchAddress[ kMaxDevices ] = {};
 std::mutex    g_setupMutex;
+
+// cuCtxGetCurrent through the runtime's driver entry point (the library links only cudart)
+typedef int ( *CtxGetCurrentFn )( void** ctx );
+CtxGetCurrentFn ctx_get_current_fn()
+{
+    static CtxGetCurrentFn fn   = nullptr;
+    static bool            done = false;
+    if( !done )
+    {
+        void*                           p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if( cudaGetDriverEntryPointByVersion( "cuCtxGetCurrent", &p, 12000, cudaEnableDefault, &q ) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess )
+            fn = (CtxGetCurrentFn)p;
+        done = true;
+    }
+    return fn;
+}
 
 __global__ void __launch_bounds__( 256 ) k_gradient_atrous_noalloc( const uint32_t* src, uint32_t* dst, uint32_t* hist,
                                                                      const rgdn::Uniform u, const int iter )
@@ -48,6 +71,11 @@ extern "C" rgdn_status rgdn_gradient_atrous_noalloc( const uint32_t* samples, ui
     if( !samples || !filtered || !history || renderWidth < 2 || renderHeight < 1 || ( renderWidth & 1 ) ||
         ( (uintptr_t)samples & 3 ) || ( (uintptr_t)filtered & 3 ) || ( (uintptr_t)history & 3 ) )
         return RGDN_WRONG_FUNCTION_ARGUMENT;
+    // iteration 0 reads the neighbours of `samples` while it writes `history`, and the later
+    // iterations write `filtered`: three distinct images, as the reference's DISPingGradient /
+    // DISGradientHistory are
+    if( (const void*)samples == (const void*)history || (const void*)filtered == (const void*)samples || filtered == history )
+        return RGDN_WRONG_FUNCTION_ARGUMENT;
     const uint32_t gw = ( renderWidth + 1 ) / 3 > 0 ? ( renderWidth + 1 ) / 3 : 1;
     const uint32_t gh = ( renderHeight + 1 ) / 3 > 0 ? ( renderHeight + 1 ) / 3 : 1;
     // the fixed scratch holds kMaxStrata texels: larger frames are refused, not truncated
@@ -55,15 +83,21 @@ extern "C" rgdn_status rgdn_gradient_atrous_noalloc( const uint32_t* samples, ui
 
     int dev = 0;
     if( cudaGetDevice( &dev ) != cudaSuccess || dev < 0 || dev >= kMaxDevices ) return RGDN_DEVICE_ERROR;
+    const CtxGetCurrentFn getCtx = ctx_get_current_fn();
+    void*                 ctx    = nullptr;
+    if( !getCtx || getCtx( &ctx ) != 0 ) return RGDN_DEVICE_ERROR;
     void* scratch = nullptr;
     {
-        // set-up, once per device, with that device current
+        // set-up, once per device and context, with that device current
         std::lock_guard< std::mutex > g( g_setupMutex );
-        if( !g_scratchAddress[ dev ] )
+        if( !ctx || !g_scratchAddress[ dev ] || g_scratchContext[ dev ] != ctx )
         {
             void* p = nullptr;
             if( cudaGetSymbolAddress( &p, g_gradientScratch ) != cudaSuccess || !p ) return RGDN_DEVICE_ERROR;
+            // with no context current before, the runtime has now made the primary one current
+            if( !ctx && ( getCtx( &ctx ) != 0 || !ctx ) ) return RGDN_DEVICE_ERROR;
             g_scratchAddress[ dev ] = p;
+            g_scratchContext[ dev ] = ctx;
         }
         scratch = g_scratchAddress[ dev ];
     }

@@ -17,6 +17,7 @@
 // A frame's G-buffer is copied into (or bound to) the stream's planes at the head of its step,
 // and PRE_FINAL is copied out after the step when the request asks for it.
 #include <algorithm>
+#include <limits>
 #include <chrono>
 #include <condition_variable>
 #include <cstring>
@@ -373,6 +374,17 @@ float percentile( std::vector< float > v, double q )
     return v[ std::min( i, v.size() - 1 ) ];
 }
 
+// The q-quantile over every finished request, each dropped one counted as an unbounded latency:
+// +infinity once the dropped requests reach past the quantile.
+float percentile_all( std::vector< float > v, uint64_t dropped, double q )
+{
+    const uint64_t n = (uint64_t)v.size() + dropped;
+    if( n == 0 ) return 0.0f;
+    std::sort( v.begin(), v.end() );
+    const uint64_t i = std::min< uint64_t >( (uint64_t)( q * (double)( n - 1 ) + 0.5 ), n - 1 );
+    return i < v.size() ? v[ i ] : std::numeric_limits< float >::infinity();
+}
+
 }  // namespace
 
 extern "C" {
@@ -503,10 +515,17 @@ rgdn_status rgdn_server_wait( rgdn_server* sv, uint64_t ticket, uint32_t timeout
     if( !valid_server( sv ) ) return RGDN_WRONG_INSTANCE;
     if( !out ) return RGDN_WRONG_FUNCTION_ARGUMENT;
     std::unique_lock< std::mutex > lk( sv->m );
-    auto it = sv->reqs.find( ticket );
-    if( it == sv->reqs.end() ) return RGDN_WRONG_FUNCTION_ARGUMENT;
-    auto finished = [ & ] { return it->second.state == REQ_DONE || it->second.state == REQ_DROPPED; };
+    if( sv->reqs.find( ticket ) == sv->reqs.end() ) return RGDN_WRONG_FUNCTION_ARGUMENT;
+    // the ticket is looked up again after every wake-up: a submit on another thread may rehash
+    // the map while the lock is released (invalidating iterators), and another waiter on the
+    // same ticket may already have taken and erased it
+    auto finished = [ & ] {
+        const auto f = sv->reqs.find( ticket );
+        return f == sv->reqs.end() || f->second.state == REQ_DONE || f->second.state == REQ_DROPPED;
+    };
     if( !sv->cvDone.wait_for( lk, std::chrono::milliseconds( timeoutMs ), finished ) ) return RGDN_TIMEOUT;
+    const auto it = sv->reqs.find( ticket );
+    if( it == sv->reqs.end() ) return RGDN_WRONG_FUNCTION_ARGUMENT;
     const ServeReq& q = it->second;
     out->state        = q.state;
     out->frameIndex   = q.fi;
@@ -536,6 +555,10 @@ rgdn_status rgdn_server_stats_get( rgdn_server* sv, rgdn_server_stats* out )
     out->p50Ms             = percentile( sv->latencies, 0.50 );
     out->p99Ms             = percentile( sv->latencies, 0.99 );
     out->maxMs             = percentile( sv->latencies, 1.0 );
+    out->p99AllMs          = percentile_all( sv->latencies, sv->framesDropped, 0.99 );
+    out->dropRate          = ( sv->framesDone + sv->framesDropped )
+                                 ? (float)( (double)sv->framesDropped / (double)( sv->framesDone + sv->framesDropped ) )
+                                 : 0.0f;
     out->meanFramesPerStep = sv->steps ? (float)sv->framesInSteps / (float)sv->steps : 0.0f;
     out->busySeconds       = sv->busySeconds + ( sv->busyStart >= 0 ? now_s() - sv->busyStart : 0.0 );
     return RGDN_SUCCESS;

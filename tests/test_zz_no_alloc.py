@@ -69,11 +69,41 @@ def test_noalloc_matches_stream_path_twice_in_a_row():
     ctx.close()
 
 
+def test_noalloc_at_the_stated_maximum():
+    """3840x2160 (exactly the 1280 x 720 strata the fixed scratch holds) is accepted and gives the
+    stream path's images bit for bit, on seeded random samples."""
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    W, H = 3840, 2160
+    ctx = Context(0)
+    s = Stream(ctx, W, H, N.STORAGE_REF)
+    rng = np.random.default_rng(41)
+    shape = (s.image("DIS_PING_GRADIENT", 0).height, s.image("DIS_PING_GRADIENT", 0).width)
+    assert shape == (720, 1280)
+    samples = rng.integers(0, 2 ** 32, size=shape, dtype=np.uint32)
+    s.upload("DIS_PING_GRADIENT", 0, samples)
+    p = N.FrameParams()
+    p.minLogLuminance, p.maxLogLuminance = -3.0, 7.0
+    for i in range(4):
+        s.stage(N.STAGE_GRADIENT_ATROUS, i, 0, p)
+    ref_filtered, ref_history = s.download("DIS_PING_GRADIENT", 0), s.download("DIS_GRADIENT_HISTORY", 0)
+    s.close()
+    ctx.close()
+    filtered, history = call_noalloc(samples, W, H)
+    assert np.array_equal(filtered, ref_filtered), "filtered gradients differ at the maximum size"
+    assert np.array_equal(history, ref_history), "gradient history differs at the maximum size"
+
+
 def test_noalloc_rejects_oversized_and_bad_arguments():
     lib = N.load()
-    buf = (C.c_uint32 * 4)()
-    p = C.cast(buf, C.c_void_p)
+    bufs = [(C.c_uint32 * 4)() for _ in range(3)]
+    a, b, c = (C.cast(x, C.c_void_p) for x in bufs)
     # 3842 x 2162 needs 1281 x 721 strata, beyond the fixed 1280 x 720 scratch
-    assert lib.rgdn_gradient_atrous_noalloc(p, p, p, 3842, 2162, None) == N.WRONG_FUNCTION_ARGUMENT
-    assert lib.rgdn_gradient_atrous_noalloc(p, p, p, 63, 36, None) == N.WRONG_FUNCTION_ARGUMENT   # odd width
-    assert lib.rgdn_gradient_atrous_noalloc(None, p, p, 64, 36, None) == N.WRONG_FUNCTION_ARGUMENT
+    assert lib.rgdn_gradient_atrous_noalloc(a, b, c, 3842, 2162, None) == N.WRONG_FUNCTION_ARGUMENT
+    assert lib.rgdn_gradient_atrous_noalloc(a, b, c, 63, 36, None) == N.WRONG_FUNCTION_ARGUMENT   # odd width
+    assert lib.rgdn_gradient_atrous_noalloc(None, b, c, 64, 36, None) == N.WRONG_FUNCTION_ARGUMENT
+    # the three images must be distinct
+    assert lib.rgdn_gradient_atrous_noalloc(a, b, a, 64, 36, None) == N.WRONG_FUNCTION_ARGUMENT   # history = samples
+    assert lib.rgdn_gradient_atrous_noalloc(a, a, c, 64, 36, None) == N.WRONG_FUNCTION_ARGUMENT   # filtered = samples
+    assert lib.rgdn_gradient_atrous_noalloc(a, b, b, 64, 36, None) == N.WRONG_FUNCTION_ARGUMENT   # filtered = history
