@@ -54,10 +54,12 @@ def parse():
     ap.add_argument("--iters", type=int, default=5, help="a-trous passes")
     ap.add_argument("--frames", type=int, default=60, help="distinct frames in the sequence")
     ap.add_argument("--e2e-steps", type=int, default=120)
-    ap.add_argument("--path", default="fused", choices=["fused", "plain", "tma"],
+    ap.add_argument("--path", default="fused", choices=["fused", "plain", "tma", "direct", "pair"],
                     help="fused: the default kernels; plain: one kernel per reference dispatch; "
-                         "tma: the default kernels with TMA-staged a-trous")
-    ap.add_argument("--no-cpu-baseline", action="store_true")
+                         "tma: the default kernels with TMA-staged a-trous; direct: the default kernels with "
+                         "the a-trous taps read from global memory")
+    ap.add_argument("--no-cpu-baseline", action="store_true", help="skip the CPU oracle (baseline and parity)")
+    ap.add_argument("--parity-frames", type=int, default=8, help="frames run on GPU and oracle for the parity figures")
     ap.add_argument("--no-batched", action="store_true", help="skip the 32-stream batched measurement")
     ap.add_argument("--batch-steps", type=int, default=30)
     ap.add_argument("--batch-frames", type=int, default=4, help="distinct resident frames per batched stream")
@@ -179,26 +181,68 @@ def stage_bytes(storage: str) -> dict:
     b["atrous0"] = (cv + 2 * col3 + 2 + 2 + 2 + 4 + hl) + (cv + 2 * col3 + fv)
     b["atrous"] = (cv + 2 * col3 + 2 + 2 + 2 + 4 + hl + fv) + (cv + 2 * col3)
     b["atrous_last"] = (cv + 2 * col3 + 2 + 2 + 2 + 4 + hl + fv) + (4 + 8 + 1) + (pre + 2)
+    b["atrous_pair0"] = (cv + 2 * col3 + 2 + 2 + 2 + 4 + hl) + (cv + fv) + (cv + 2 * col3)
+    b["atrous_pair"] = b["atrous"]
     b["luminance_histogram"] = 2
     b["luminance_avg"] = 0
-    # fused kernels
-    b["temporal_fast"] = b["temporal_exact_geom"] = b["temporal_accumulation"] + 16   # + record write
-    # with the previous record: 16 B instead of depth (2) + normal (4) at the prev taps
-    b["temporal_fast_gp"] = b["temporal_exact_geom_gp"] = b["temporal_accumulation"] + 16 + 10
-    # fused kernels read the 16-byte geometry record instead of normal + depth + metallic-roughness
+    # The default path's kernels do the same reference stages, so they are charged the same
+    # compulsory bytes: the 16-byte geometry record they write and read instead of normal,
+    # depth and metallic-roughness is this implementation's choice, not the algorithm's traffic.
+    for k in ("temporal_fast", "temporal_exact_geom", "temporal_fast_gp", "temporal_exact_geom_gp"):
+        b[k] = b["temporal_accumulation"]
     b["anti_firefly_fast"] = b["anti_firefly"]
-    b["variance_fast"] = b["variance_exact_geom"] = (col3 + 16 + hl + mom) + cv
+    b["variance_fast"] = b["variance_exact_geom"] = b["variance_estimation"]
     return b
 
 
+def path_bytes(storage: str) -> float:
+    """Compulsory bytes per pixel of the whole fused chain (gradient samples through the
+    histogram): every distinct input read once, every persistent output written once, the
+    intermediates between stages never leaving the chip. The reference formats give about
+    154.5 B/px; the 16-bit storage modes about 190.5 (16-bit colour and history, FP32 moments and
+    variance)."""
+    col3 = {"ref": 4, "fp32": 16, "fp16": 8, "bf16": 8}[storage]
+    cv = {"ref": 8, "fp32": 16, "fp16": 12, "bf16": 12}[storage]
+    mom = {"ref": 4, "fp32": 8, "fp16": 8, "bf16": 8}[storage]
+    hl = {"ref": 8, "fp32": 16, "fp16": 8, "bf16": 8}[storage]
+    pre = {"ref": 4, "fp32": 16, "fp16": 8, "bf16": 8}[storage]
+    cur = 3 * 4 + 8 + 8 + 2 + 2 + 4 + 2 + 16 + 4 + 8 + 1                 # this frame's G-buffer: 67 B
+    prev = 2 + 4 + 16 + cv + mom + hl + col3 + col3 + 4                  # history and G-buffer _Prev
+    grad = 1.5                                                           # 1/9-resolution gradient state
+    writes = cv + mom + hl + col3 + col3                                 # history for the next frame
+    return cur + prev + grad + writes + pre
+
+
 def kernel_bytes(name: str, it: int, niter: int, per_px: dict) -> float:
-    if name == "atrous":
+    if name in ("atrous", "atrous_fast", "atrous_fast_hist", "atrous_exact", "atrous_exact_hist", "atrous_tma",
+                "atrous_tma_hist", "atrous_sm", "atrous_sm_hist"):
         return per_px["atrous0"] if it == 0 else per_px["atrous_last"] if it == niter - 1 else per_px["atrous"]
-    if name in ("atrous_fast", "atrous_fast_hist", "atrous_exact", "atrous_exact_hist", "atrous_tma", "atrous_tma_hist"):
-        # the geometry record (16 B) replaces normal (4) + depth (2) + metallic-roughness (2)
-        base = per_px["atrous0"] if it == 0 else per_px["atrous_last"] if it == niter - 1 else per_px["atrous"]
-        return base + 8
+    if name in ("atrous_pair", "atrous_pair_hist"):
+        # two iterations in one launch (it, it + 1): the first one's sources and the static
+        # planes read once; the second one's outputs written, and iteration 0's feedback image
+        # and prefiltered variance as well when the pair starts at 0
+        return per_px["atrous_pair0"] if it == 0 else per_px["atrous_pair"]
     return per_px[name]
+
+
+def kernel_groups(kern: list, steps: int) -> list:
+    """Per-launch entries (name[it]) summed per kernel over all its iterations, ranked by device
+    time per step."""
+    groups = {}
+    for d in kern:
+        name = d["kernel"].split("[")[0]
+        g = groups.setdefault(name, {"kernel": name, "launches": 0, "us": 0.0, "alg_bytes": 0.0})
+        g["launches"] += d["launches"]
+        g["us"] += d["avg_us"] * d["launches"]
+        g["alg_bytes"] += d["alg_bytes"] * d["launches"]
+    out = []
+    for g in groups.values():
+        out.append({"kernel": g["kernel"], "launches_per_step": g["launches"] / steps,
+                    "us_per_step": g["us"] / steps, "avg_us": g["us"] / g["launches"],
+                    "alg_bytes_per_launch": g["alg_bytes"] / g["launches"],
+                    "gbs": g["alg_bytes"] / (g["us"] / 1e6) / 1e9})
+    out.sort(key=lambda g: -g["us_per_step"])
+    return out
 
 
 def load_peaks() -> tuple[float, str]:
@@ -209,14 +253,17 @@ def load_peaks() -> tuple[float, str]:
         return 6800.0, "fallback"
 
 
-def profile_traffic(kernel: str):
-    """DRAM bytes per launch of the dominant kernel from the committed ncu summary, if any."""
+def profile_traffic(kernel: str, width: int, height: int, storage: str):
+    """DRAM bytes (read + write) per launch of `kernel` from the committed ncu summary
+    (profiles/dram_traffic.md, written by --ncu-traffic from one capture of this build), scaled
+    from the captured frame size to this one by pixel count. None without a matching row."""
     path = os.path.join(ROOT, "profiles", "dram_traffic.md")
     try:
         for line in open(path):
             cells = [c.strip() for c in line.strip().strip("|").split("|")]
-            if len(cells) >= 3 and cells[0] == kernel:
-                return float(cells[2])
+            if len(cells) >= 5 and cells[0] == kernel and cells[1] == storage:
+                w, h = (int(v) for v in cells[2].split("x"))
+                return float(cells[4]) * (width * height) / (w * h)
     except Exception:
         pass
     return None
@@ -225,25 +272,66 @@ def profile_traffic(kernel: str):
 # ------------------------------------------------------------------------------------------
 # CPU oracle timing (cpu_baseline in our line; the whole reference arm)
 # ------------------------------------------------------------------------------------------
-def oracle_time(width: int, height: int, storage: str, iters: int, frames: int, seed: int = 1):
-    """Runs `frames` frames of the oracle (all host cores); returns seconds of the last frame."""
+def oracle_check(ctx, args, frames: int):
+    """The workload's first `frames` frames on a fresh GPU stream (default kernels) and on the
+    CPU oracle (the same storage mode, all host cores), independently. Returns the oracle's time
+    for the last frame (the CPU baseline) and the last frame's PRE_FINAL error (max-rel, p99.9
+    rel, PSNR) with the histogram counts moved between bins per frame."""
+    import numpy as np
+
     import oracle
+    from raytracedgl1_gb300 import _native as N
+    from raytracedgl1_gb300.denoiser import Denoiser, Stream, Tonemapping
     from raytracedgl1_gb300.scene import Scene
-    sc = Scene(width, height, seed=seed)
-    o = oracle.OracleStream(width, height, STORAGE[storage])
+
+    W, H = args.width, args.height
+    sc = Scene(W, H, seed=1)
+    s = Stream(ctx, W, H, STORAGE[args.storage])
+    o = oracle.OracleStream(W, H, STORAGE[args.storage])
     nthreads = os.cpu_count() or 1
-    last = None
+    moved, last = [], None
     for f in range(frames):
         fi = f & 1
         bufs, p = sc.generate(f)
-        p.atrousIterations = iters
+        p.atrousIterations = args.iters
         for k, v in bufs.items():
+            s.upload(k, fi, v)
             o.load(k, fi, v)
+        Denoiser(s).Denoise(fi, p)
+        hg = s.tonemapping()[0].astype(np.int64)
+        Tonemapping(s).CalculateExposure(fi, p)
         t0 = time.perf_counter()
         o.denoise(fi, p, nthreads)
-        o.calculate_exposure(fi, p, nthreads)
+        o.stage(N.STAGE_LUMINANCE_HISTOGRAM, 0, fi, p, nthreads)
+        ho = o.tonemapping()[0].astype(np.int64)
+        o.stage(N.STAGE_LUMINANCE_AVG, 0, fi, p, nthreads)
         last = time.perf_counter() - t0
-    return last, nthreads
+        moved.append(int(np.abs(hg - ho).sum()) // 2)
+    fi = (frames - 1) & 1
+    img = s.image("PRE_FINAL", fi)
+    fmt16 = img.format in (4, 5, 6)
+    dec = (lambda a: a.view(np.float16).astype(np.float64)) if fmt16 else (lambda a: a.astype(np.float64))
+    if img.format == 13:   # B10G11R11 (ref storage)
+        from tests import _formats as F
+        dec = lambda a: F.decode(a, 13).astype(np.float64)   # noqa: E731
+    g = dec(s.download("PRE_FINAL", fi))[..., :3]
+    c = dec(o.plane("PRE_FINAL", fi))[..., :3]
+    atol = 1e-4 * float(np.percentile(np.abs(c), 99))
+    rel = np.abs(g - c).max(axis=-1) / np.maximum(np.abs(c).max(axis=-1), atol)
+    mse = float(np.mean((g - c) ** 2))
+    peak = float(np.abs(c).max()) or 1.0
+    s.close()
+    cpu = {"value": round(W * H / last / 1e6, 4), "unit": "Mpix/s", "cores": nthreads, "kind": "port",
+           "sample": f"frame {frames - 1} of the {W}x{H} sequence through the CPU oracle (denoise + exposure; "
+                     f"frames 0-{frames - 2} untimed)"}
+    parity = {"against": f"CPU oracle, {args.storage} storage, {frames} frames run independently",
+              "frame": frames - 1, "max_rel": float(rel.max()), "p999_rel": float(np.percentile(rel, 99.9)),
+              "frac_le_1e-3": float(np.mean(rel <= 1e-3)), "frac_le_1e-2": float(np.mean(rel <= 1e-2)),
+              "psnr_db": round(10 * np.log10(peak * peak / mse), 2) if mse else None,
+              "histogram_counts_moved_per_frame": moved,
+              "histogram_note": "bit-exact given the same HistogramInput (tests); from independent runs a value "
+                                "within an fp16 step of a bin edge can land in the neighbouring bin"}
+    return cpu, parity
 
 
 def run_reference(args, dist: Dist):
@@ -282,7 +370,10 @@ def run_reference(args, dist: Dist):
         "ms_per_step": round(1e3 * total / len(times), 3), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "p50_ms": round(1e3 * times[len(times) // 2], 3), "p99_ms": round(1e3 * times[int(0.99 * (len(times) - 1))], 3),
-        "config": config_dict(args),
+        "config": dict(config_dict(args), band=f"{W}x{H}",
+                       sample=f"each step times one {W}x{H} frame (a band of the {args.width}x{args.height} "
+                              f"workload's width, from the same generator and stages, so the same per-pixel "
+                              f"work); Mpix/s is per pixel of that band"),
         "cpu_baseline": {"value": round(mpix, 4), "unit": "Mpix/s", "cores": nthreads, "kind": "port",
                          "sample": f"one frame of a {W}x{H} band of the workload per step (same per-pixel work)"},
         "e2e": {"value": round(mpix, 4), "unit": "Mpix/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -340,9 +431,11 @@ def run_batched(args, dist: Dist, dev: int, cs) -> dict:
     torch.cuda.synchronize()
     px = sum(s.width * s.height for s in streams)
 
-    def jobs_for(k: int, flags: int = 0):
+    def jobs_for(k: int, flags: int = 0, subset=None):
         jobs = []
-        for s, frames in zip(streams, seqs):
+        for idx, (s, frames) in enumerate(zip(streams, seqs)):
+            if subset is not None and idx not in subset:
+                continue
             bufs, p = frames[k % len(frames)]
             fi = k & 1
             for name, t in bufs.items():
@@ -353,11 +446,11 @@ def run_batched(args, dist: Dist, dev: int, cs) -> dict:
             jobs.append((s, fi, p))
         return jobs
 
-    def batched(k):
-        ctx.submit_batch(jobs_for(k), cs)
+    def batched(k, subset=None):
+        ctx.submit_batch(jobs_for(k, 0, subset), cs)
 
-    def one_by_one(k, flags):
-        for s, fi, p in jobs_for(k, flags):
+    def one_by_one(k, flags, subset=None):
+        for s, fi, p in jobs_for(k, flags, subset):
             Denoiser(s).Denoise(fi, p, cs)
             Tonemapping(s).CalculateExposure(fi, p, cs)
 
@@ -404,6 +497,28 @@ def run_batched(args, dist: Dist, dev: int, cs) -> dict:
         one_by_one(k, N.FLAG_PLAIN)
     t_p, _ = timed(lambda j: one_by_one(j, N.FLAG_PLAIN), steps_cmp, k + 1)
 
+    k += 1 + steps_cmp
+    # each resolution class alone: its 8 streams batched against the same frames one stream per
+    # call (the small frames are where launch overhead would show)
+    per_class = []
+    for r, (W, H) in enumerate(BATCH_MIX):
+        sub = set(range(r * args.batch_per_res, (r + 1) * args.batch_per_res))
+        cpx = W * H * len(sub)
+        with torch.cuda.stream(cs):
+            for _ in range(3):
+                batched(k, sub)
+                k += 1
+        t_cb, _ = timed(lambda j: batched(j, sub), steps_cmp, k)
+        k += steps_cmp
+        with torch.cuda.stream(cs):
+            one_by_one(k, 0, sub)
+        t_cs, _ = timed(lambda j: one_by_one(j, 0, sub), steps_cmp, k + 1)
+        k += 1 + steps_cmp
+        vb = cpx * steps_cmp * dist.world / (t_cb / 1e3) / 1e6
+        vs = cpx * steps_cmp * dist.world / (t_cs / 1e3) / 1e6
+        per_class.append({"resolution": f"{W}x{H}", "streams": len(sub), "batched_mpix_s": round(vb, 1),
+                          "one_stream_per_call_mpix_s": round(vs, 1), "vs_one_frame_per_launch": round(vb / vs, 3)})
+
     per_px = stage_bytes("fp16")
     kern = []
     for (name, it), (n, ms) in tim.items():
@@ -435,6 +550,8 @@ def run_batched(args, dist: Dist, dev: int, cs) -> dict:
         "kernels": kern,
     }
     out["vs_plain"] = round(out["value"] / out["plain_path_mpix_s"], 3)
+    out["vs_one_frame_per_launch"] = round(out["value"] / out["one_stream_per_call_mpix_s"], 3)
+    out["per_class"] = per_class
     for s in streams:
         s.close()
     ctx.close()
@@ -536,6 +653,8 @@ def run_serving(args, dist: Dist, dev: int) -> dict:
                 "value": round(st["pixelsDone"] / elapsed / 1e6, 1), "unit": "Mpix/s",
                 "frames_done": int(st["framesDone"]), "frames_dropped": int(st["framesDropped"]),
                 "p50_ms": round(st["p50Ms"], 3), "p99_ms": round(st["p99Ms"], 3), "max_ms": round(st["maxMs"], 3),
+                "p99_all_requests_ms": (round(st["p99AllMs"], 3) if st["p99AllMs"] != float("inf") else "inf"),
+                "drop_rate": round(st["dropRate"], 4),
                 "p99_ms_1080p": round(lat_1080[int(0.99 * (len(lat_1080) - 1))], 3) if lat_1080 else None,
                 "mean_frames_per_step": round(st["meanFramesPerStep"], 2), "steps": int(st["steps"]),
                 "gpu_busy_frac": round(st["busySeconds"] / elapsed, 3),
@@ -583,6 +702,10 @@ def run_ours(args, dist: Dist):
             p.flags |= N.FLAG_PLAIN
         elif args.path == "tma":
             p.flags |= N.FLAG_TMA_STAGING
+        elif args.path == "direct":
+            p.flags |= N.FLAG_ATROUS_DIRECT
+        elif args.path == "pair":
+            p.flags |= N.FLAG_ATROUS_PAIR
         dev_bufs = {}
         for name, arr in bufs.items():
             t = torch.from_numpy(np.ascontiguousarray(arr).view(np.uint8).reshape(-1)).to(f"cuda:{dev}")
@@ -726,7 +849,8 @@ def run_ours(args, dist: Dist):
                     "what": "CmVolumetricProcess (160x88x64 froxels, in place) + CmScatterAccum (VOLUMETRIC mode)",
                     "us_per_frame": round(vol_us, 2), "mpix_s": round(W * H / vol_us, 1),
                     "alg_bytes": vol_alg, "gbs": round(vol_alg / (vol_us / 1e6) / 1e9, 1)}
-    top = kern[0]
+    groups = kernel_groups(kern, args.steps)
+    top = groups[0]
     peak, peak_kind = load_peaks()
 
     # --- end to end from pinned host buffers through the C ABI ----------------------------
@@ -818,11 +942,9 @@ def run_ours(args, dist: Dist):
         st.bind(name, 1, None)
 
     # --- CPU baseline (rank 0, N=1) --------------------------------------------------------
-    cpu = None
+    cpu, parity = None, None
     if dist.rank == 0 and dist.world == 1 and not args.no_cpu_baseline:
-        sec, threads = oracle_time(W, H, args.storage, args.iters, 2)
-        cpu = {"value": round(W * H / sec / 1e6, 4), "unit": "Mpix/s", "cores": threads, "kind": "port",
-               "sample": f"frame 2 of the {W}x{H} sequence through the CPU oracle (frame 1 untimed)"}
+        cpu, parity = oracle_check(ctx, args, args.parity_frames)
 
     st.close()
     ctx.close()
@@ -843,9 +965,17 @@ def run_ours(args, dist: Dist):
         "gpu_launches": int(launches),
         "roofline": {"bound": "hbm", "kernel": top["kernel"], "achieved": round(top["gbs"], 1),
                      "peak": peak, "unit": "GB/s", "frac": round(top["gbs"] / peak, 4),
-                     "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else "fallback",
-                     "traffic": profile_traffic(top["kernel"]),
-                     "alg_bytes_per_launch": top["alg_bytes"]},
+                     "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs, burst copy)" if peak_kind == "measured" else "fallback 6800 GB/s",
+                     "traffic": profile_traffic(top["kernel"], W, H, args.storage),
+                     "alg_bytes_per_launch": round(top["alg_bytes_per_launch"]),
+                     "avg_us_per_launch": round(top["avg_us"], 2), "launches_per_step": top["launches_per_step"],
+                     "kernel_choice": "the kernel with the most device time per step, all its launches of a step summed",
+                     "bytes": "compulsory bytes of the reference stages it runs (each distinct texel read once, each "
+                              "output written once), in the storage mode's formats",
+                     "path_alg_bytes_per_px": path_bytes(args.storage),
+                     "path_achieved": round(path_bytes(args.storage) * W * H / (total_ms_max / args.steps / 1e3) / 1e9, 1),
+                     "path_frac": round(path_bytes(args.storage) * W * H / (total_ms_max / args.steps / 1e3) / 1e9 / peak, 4)},
+        "kernel_groups": [{k: (round(v, 2) if isinstance(v, float) else v) for k, v in g.items()} for g in groups],
         "kernels": [{k: (round(v, 2) if isinstance(v, float) else v) for k, v in d.items()} for d in kern],
         "kernel_sum_us_per_step": round(kernel_total_us, 2),
         "prepare_final": final,
@@ -863,6 +993,7 @@ def run_ours(args, dist: Dist):
                 "synchronous_p99_ms": round(1e3 * lat[int(0.99 * (len(lat) - 1))], 3)},
         "clocks": clk,
         "cpu_baseline": cpu,
+        "parity": parity,
         "gbuffer_bytes_per_frame": int(gbytes_per_frame),
         "batched": batched,
         "serving": serving,

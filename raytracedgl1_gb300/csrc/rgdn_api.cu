@@ -439,7 +439,7 @@ rgdn_status run_denoise( rgdn_stream* s, uint32_t fi, const rgdn_frame_params* p
 // itself is then empty. The caller has filled `a` for frame slot `fi` and made the bin table
 // current.
 rgdn_status launch_default_stage( rgdn_stream* s, const FrameArgs& a, uint32_t fi, const rgdn_frame_params* p, int stage, int iter,
-                                  cudaStream_t cs )
+                                  cudaStream_t cs, bool pairOk = false )
 {
     const bool exact = ( p->flags & RGDN_FLAG_EXACT_MATH ) != 0;
     switch( stage )
@@ -466,10 +466,14 @@ rgdn_status launch_default_stage( rgdn_stream* s, const FrameArgs& a, uint32_t f
             }
             const bool  last = iter + 1 == (int)a.u.niter;
             rgdn_status r;
-            if( !exact && ( p->flags & RGDN_FLAG_TMA_STAGING ) && tma_atrous_ok( s, iter ) ) r = launch_atrous_tma( s, a, iter, last, cs );
+            if( pairOk && iter == 1 ) return RGDN_SUCCESS;   // computed with iteration 0
+            if( pairOk && iter == 0 ) r = launch( s, a, KF_ATROUS_PAIR01, 0, cs );
+            else if( !exact && ( p->flags & RGDN_FLAG_TMA_STAGING ) && tma_atrous_ok( s, iter ) ) r = launch_atrous_tma( s, a, iter, last, cs );
             else
             {
-                const int k = exact ? ( last ? KF_ATROUS_EXACT_HIST : KF_ATROUS_EXACT ) : ( last ? KF_ATROUS_FAST_HIST : KF_ATROUS_FAST );
+                const bool direct = exact || ( p->flags & RGDN_FLAG_ATROUS_DIRECT );
+                const int  k = exact ? ( last ? KF_ATROUS_EXACT_HIST : KF_ATROUS_EXACT )
+                                     : direct ? ( last ? KF_ATROUS_FAST_HIST : KF_ATROUS_FAST ) : ( last ? KF_ATROUS_SM_HIST : KF_ATROUS_SM );
                 r = launch( s, a, k, iter, cs );
             }
             if( r == RGDN_SUCCESS && last ) s->histPending = true;
@@ -505,8 +509,12 @@ rgdn_status run_denoise_fused( rgdn_stream* s, uint32_t fi, const rgdn_frame_par
     }
     for( int stage : { (int)RGDN_STAGE_TEMPORAL_ACCUMULATION, (int)RGDN_STAGE_ANTI_FIREFLY, (int)RGDN_STAGE_VARIANCE_ESTIMATION } )
         if( ( r = launch_default_stage( s, a, fi, p, stage, 0, cs ) ) != RGDN_SUCCESS ) return r;
+    // iterations 0 and 1 in one launch when asked for, with the FAST shared-memory kernels and at
+    // least one more iteration after them
+    const bool pairOk = ( p->flags & RGDN_FLAG_ATROUS_PAIR ) && a.u.niter >= 3 &&
+                        !( p->flags & ( RGDN_FLAG_EXACT_MATH | RGDN_FLAG_ATROUS_DIRECT | RGDN_FLAG_TMA_STAGING ) );
     for( uint32_t i = 0; i < a.u.niter; i++ )
-        if( ( r = launch_default_stage( s, a, fi, p, RGDN_STAGE_ATROUS, (int)i, cs ) ) != RGDN_SUCCESS ) return r;
+        if( ( r = launch_default_stage( s, a, fi, p, RGDN_STAGE_ATROUS, (int)i, cs, pairOk ) ) != RGDN_SUCCESS ) return r;
     return RGDN_SUCCESS;
 }
 

@@ -12,6 +12,8 @@
 #pragma once
 
 #include <cuda.h>
+#include <atomic>
+#include <type_traits>
 #include <utility>
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
@@ -1621,16 +1623,16 @@ struct AtrousAcc
 //   wDiff = 2^( that - w_l log2 e ),   wSpec = w_r' 2^( that + p L ),
 // the same products as exp(-w_z^2) * n^128 * kernel, exp(-w_l) and n^p. atrous_terms folds the
 // constant factors into rz1, rz2 and wLumMul.
+// lq is the tap colour's luminance, Wm< FAST >::lum of (cvq.x, cvq.y, cvq.z)
 template< bool FAST, bool INTERIOR >
-__device__ __forceinline__ void atrous_accum( const AtrousCtr& c, AtrousAcc& acc, const int xx, const int yy, const int qx, const int qy,
-                                              const float rq, const float3 nq, const float zq, const float4 cvq, const float3 sq,
-                                              const float3 iq )
+__device__ __forceinline__ void atrous_accum_l( const AtrousCtr& c, AtrousAcc& acc, const int xx, const int yy, const int qx, const int qy,
+                                                const float rq, const float3 nq, const float zq, const float4 cvq, const float lq,
+                                                const float3 sq, const float3 iq )
 {
     using X = Wm< FAST >;
     if constexpr( FAST )
     {
         const float3 dq    = f3( cvq.x, cvq.y, cvq.z );
-        const float  lq    = X::lum( dq );
         const float  nn    = fmaxf( 0.0f, X::dot( c.normal, nq ) );
         const int    man   = ( xx < 0 ? -xx : xx ) + ( yy < 0 ? -yy : yy );
         const float  L     = fmaxf( lg2_approx( nn ), -126.0f );
@@ -1664,7 +1666,6 @@ __device__ __forceinline__ void atrous_accum( const AtrousCtr& c, AtrousAcc& acc
     }
     const float kern[ 2 ][ 2 ] = { { 1.0f, 0.5f }, { 0.5f, 0.25f } };
     const float3 dq  = f3( cvq.x, cvq.y, cvq.z );
-    const float  lq  = X::lum( dq );
     const float  nn  = fmaxf( 0.0f, X::dot( c.normal, nq ) );
     const int    man = ( xx < 0 ? -xx : xx ) + ( yy < 0 ? -yy : yy );
 
@@ -1690,16 +1691,23 @@ __device__ __forceinline__ void atrous_accum( const AtrousCtr& c, AtrousAcc& acc
     acc.wsS = acc.wsS + wSpec;
     acc.wsI = acc.wsI + wInd;
 }
+template< bool FAST, bool INTERIOR >
+__device__ __forceinline__ void atrous_accum( const AtrousCtr& c, AtrousAcc& acc, const int xx, const int yy, const int qx, const int qy,
+                                              const float rq, const float3 nq, const float zq, const float4 cvq, const float3 sq,
+                                              const float3 iq )
+{
+    atrous_accum_l< FAST, INTERIOR >( c, acc, xx, yy, qx, qy, rq, nq, zq, cvq, Wm< FAST >::lum( f3( cvq.x, cvq.y, cvq.z ) ), sq, iq );
+}
 
 // The centre pixel's weight terms, from its colour (acc.d), normal, depth, depth gradient (in
 // c), roughness byte, prefiltered variance and specular history length; resets the weight sums.
 template< bool FAST >
-__device__ __forceinline__ void atrous_terms( AtrousCtr& c, AtrousAcc& acc, const float* u8, const uint32_t rough8, const float prefVar,
-                                              const float hS, const int iter )
+__device__ __forceinline__ void atrous_terms_r( AtrousCtr& c, AtrousAcc& acc, const float roughness, const float prefVar, const float hS,
+                                                const int iter )
 {
     c.l             = Wm< FAST >::lum( acc.d );
     c.wLumMul       = ( FAST ? kLog2e : 1.0f ) / ( 4.0f * prefVar + 0.00001f );
-    c.roughness     = u8[ rough8 ];
+    c.roughness     = roughness;
     c.wRoughMul     = gclamp( c.roughness * 30.0f - (float)iter, 0.0f, 1.0f );
     const float nws = gclamp( hS / 8.0f, 0.0f, 1.0f );
     c.nwSpec        = gclamp( spec_power( c.roughness * c.roughness ), 8.0f, 1024.0f ) * nws;
@@ -1708,6 +1716,12 @@ __device__ __forceinline__ void atrous_terms( AtrousCtr& c, AtrousAcc& acc, cons
     c.rz1  = FAST ? kSqrtLog2e / fmaxf( c.gradDepth * 1.0f, 0.01f ) : 0.0f;
     c.rz2  = FAST ? kSqrtLog2e / fmaxf( c.gradDepth * 2.0f, 0.01f ) : 0.0f;
     acc.ws = acc.wsS = acc.wsI = 1.0f;
+}
+template< bool FAST >
+__device__ __forceinline__ void atrous_terms( AtrousCtr& c, AtrousAcc& acc, const float* u8, const uint32_t rough8, const float prefVar,
+                                              const float hS, const int iter )
+{
+    atrous_terms_r< FAST >( c, acc, u8[ rough8 ], prefVar, hS, iter );
 }
 
 // The centre pixel: loads, the invalid-depth early out and the per-pixel weight terms
@@ -1896,7 +1910,349 @@ __global__ void __launch_bounds__( NT, MINB ) k_atrous( const FrameArgs a, const
 }
 
 // ==========================================================================================
-// A-trous with shared-memory staging by the Tensor Memory Accelerator (default path).
+// A-trous with the tap footprint decoded once into shared memory (default path).
+//
+// Every texel a block's taps read is loaded once (coalesced rows), decoded to FP32 and kept in
+// four float4 planes of shared memory: (normal, depth), (colour, variance), (specular, colour
+// luminance) and (indirect, roughness). The taps then read shared memory at compile-time
+// offsets (the step is a template parameter), so a tap costs its weights and four 16-byte
+// shared loads; the decode, the address arithmetic and the luminance of a texel are paid once
+// per staged texel instead of once per tap. The arithmetic is atrous_px's, in the same order,
+// so the results equal the direct kernel's bit for bit.
+//
+// The block is 32 x 8 threads and its tile 32 x TH pixels (TH / 8 rows per thread). The staged
+// region is the tile widened by the step on every side; when TH is below the step, its rows
+// are three bands of TH rows (-step, 0, +step), the only rows the dilated stencil reads.
+// ==========================================================================================
+template< int ITER, int TH > struct AtSm
+{
+    static constexpr int  S     = 1 << ITER;
+    static constexpr int  TW    = 32;
+    static constexpr int  PY    = TH / 8;
+    static constexpr bool BANDS = TH < S;
+    static constexpr int  RW    = TW + 2 * S;
+    static constexpr int  RH    = BANDS ? 3 * TH : TH + 2 * S;
+    static constexpr int  N     = RW * RH;
+    static constexpr int  SMEM  = 4 * N * (int)sizeof( float4 );
+    static_assert( TH % 8 == 0 && S <= TW, "tile rows are whole thread rows; columns are one contiguous run" );
+    // texel offset of the tap (dx, dy) from its centre
+    static __host__ __device__ constexpr int off( int dx, int dy ) { return dy * ( BANDS ? TH : S ) * RW + dx * S; }
+    // region row of tile row ty, and image row of region row r
+    static __device__ __forceinline__ int crow( int ty ) { return BANDS ? TH + ty : S + ty; }
+    static __device__ __forceinline__ int grow( int r, int y0 ) { return BANDS ? y0 + ( r / TH - 1 ) * S + r % TH : y0 - S + r; }
+};
+
+// One texel of an a-trous footprint as the staged planes hold it: (normal, depth),
+// (colour, variance), (specular, luminance of the colour), (indirect, roughness). A texel outside
+// the image is the zero texel the direct kernel substitutes (normal code 0 decodes to (0, 0, 1)).
+template< int M >
+__device__ __forceinline__ void atrous_stage_texel( const FrameArgs& a, const AtrousIO& io, const int gx, const int gy, const float* u8,
+                                                    float4& vg, float4& vc, float4& vs, float4& vi )
+{
+    using S = Sto< M >;
+    vg = make_float4( 0.0f, 0.0f, 1.0f, 0.0f );
+    vc = vs = vi = make_float4( 0.0f, 0.0f, 0.0f, 0.0f );
+    if( inside( a.u, gx, gy ) )
+    {
+        const int    q  = gy * a.u.W + gx;
+        const Geo    g  = geo_load( a.geom, q );
+        const float3 sp = S::ld3( io.specSrc, (size_t)q );
+        const float3 in = S::ld3( io.indirSrc, (size_t)q );
+        vc = S::ldcv( io.diffSrc, io.varSrc, (size_t)q );
+        vg = make_float4( g.n.x, g.n.y, g.n.z, geo_depth( g ) );
+        vs = make_float4( sp.x, sp.y, sp.z, Wm< true >::lum( f3( vc.x, vc.y, vc.z ) ) );
+        vi = make_float4( in.x, in.y, in.z, u8[ geo_rough8( g ) ] );
+    }
+}
+
+// The result of one a-trous pixel; `pref` tells whether iteration 0 computed the prefiltered
+// variance (not for an invalid-depth centre, which keeps its values and writes no variance).
+struct AtrousOut
+{
+    float3 d, s, i;
+    float  var, prefVar;
+    bool   pref;
+};
+
+// One pixel of a-trous iteration ITER (step STEP) from staged planes: the colour planes C, Sp, I
+// with centre texel cc and tap offsets dy * RC + dx * STEP, the static plane G with centre cg
+// and tap offsets dy * RG + dx * STEP. The arithmetic and its order are atrous_px's (FAST).
+// Iteration 0 prefilters the variance from C (STEP 1); later iterations take `prefVar`.
+template< int ITER, int STEP, int RC, int RG >
+__device__ __forceinline__ AtrousOut atrous_sm_px( const FrameArgs& a, const int px, const int py, const int i, const bool interior,
+                                                   const float4* G, const float4* C, const float4* Sp, const float4* I, const int cg,
+                                                   const int cc, float prefVar, const float hS )
+{
+    AtrousCtr c;
+    AtrousAcc acc;
+    AtrousOut o;
+    o.pref          = false;
+    c.chArea        = cb_area( a.u, px );
+    const float4 cv = C[ cc ], cs = Sp[ cc ], ci = I[ cc ], cgv = G[ cg ];
+    acc.d           = f3( cv.x, cv.y, cv.z );
+    acc.var         = cv.w;
+    acc.s           = f3( cs.x, cs.y, cs.z );
+    acc.i           = f3( ci.x, ci.y, ci.z );
+    c.z             = cgv.w;
+    c.gradDepth     = h2f( a.depthGrad[ i ] );
+    if( c.z < 0.0f || c.z > MAX_RAY_LENGTH )
+    {
+        // invalid depth keeps its own values (iteration 0: zeros), CmSVGFAtrous_Iter0.comp:208-216
+        if( ITER == 0 ) { acc.d = f3( 0, 0, 0 ); acc.var = 0.0f; acc.s = f3( 0, 0, 0 ); acc.i = f3( 0, 0, 0 ); }
+        o.d = acc.d; o.var = acc.var; o.s = acc.s; o.i = acc.i; o.prefVar = 0.0f;
+        return o;
+    }
+    c.normal = f3( cgv.x, cgv.y, cgv.z );
+    if( ITER == 0 )
+    {
+        // prefilterLuminanceVariance (CmSVGFAtrous_Iter0.comp:158-187), step-1 neighbours
+        const float gw[ 2 ][ 2 ] = { { 0.25f, 0.125f }, { 0.125f, 0.0625f } };
+        float       r            = 0.0f;
+#pragma unroll
+        for( int yy = -1; yy <= 1; yy++ )
+        {
+#pragma unroll
+            for( int xx = -1; xx <= 1; xx++ )
+                r = r + C[ cc + yy * RC + xx ].w * gw[ xx < 0 ? -xx : xx ][ yy < 0 ? -yy : yy ];
+        }
+        prefVar = sqrtf( fmaxf( r, 0.0f ) );
+        o.pref  = true;
+    }
+    o.prefVar = prefVar;
+    atrous_terms_r< true >( c, acc, ci.w, prefVar, hS, ITER );
+    auto taps = [ & ]( auto interiorTag ) {
+        constexpr bool IN = decltype( interiorTag )::value;
+#pragma unroll
+        for( int yy = -1; yy <= 1; yy++ )
+        {
+#pragma unroll
+            for( int xx = -1; xx <= 1; xx++ )
+            {
+                if( xx == 0 && yy == 0 ) continue;
+                const int    ec = cc + yy * RC + xx * STEP, eg = cg + yy * RG + xx * STEP;
+                const float4 tg = G[ eg ], tc = C[ ec ], ts = Sp[ ec ], ti = I[ ec ];
+                atrous_accum_l< true, IN >( c, acc, xx, yy, px + xx * STEP, py + yy * STEP, ti.w, f3( tg.x, tg.y, tg.z ), tg.w, tc, ts.w,
+                                            f3( ts.x, ts.y, ts.z ), f3( ti.x, ti.y, ti.z ) );
+            }
+        }
+    };
+    if( interior ) taps( std::true_type() );
+    else taps( std::false_type() );
+    atrous_finish( acc, o.d, o.var, o.s, o.i );
+    return o;
+}
+
+template< int M, bool HIST, int ITER, int TH, int MINB >
+__global__ void __launch_bounds__( 256, MINB ) k_atrous_sm( const FrameArgs a )
+{
+    using G = AtSm< ITER, TH >;
+    using S = Sto< M >;
+    extern __shared__ float4 smem[];
+    float4* const       sG = smem;          // normal, depth
+    float4* const       sC = sG + G::N;     // colour, variance
+    float4* const       sS = sC + G::N;     // specular, luminance of the colour
+    float4* const       sI = sS + G::N;     // indirect, roughness
+    __shared__ float    u8[ 256 ];
+    __shared__ uint32_t hist[ HIST ? 256 : 1 ];
+    const int           t = threadIdx.y * 32 + threadIdx.x;
+    pdl_launch_dependents();
+    u8[ t ] = (float)t / 255.0f;
+    if( HIST ) hist[ t ] = 0u;
+    pdl_wait();
+    __syncthreads();
+
+    const Uniform& u  = a.u;
+    const AtrousIO io = atrous_io< M >( a, ITER );
+    const int      x0 = blockIdx.x * G::TW, y0 = blockIdx.y * TH;
+#pragma unroll
+    for( int k = 0; k < ( G::N + 255 ) / 256; k++ )
+    {
+        const int e = t + 256 * k;
+        if( e < G::N )
+        {
+            const int r = e / G::RW, c = e - r * G::RW;
+            atrous_stage_texel< M >( a, io, x0 - G::S + c, G::grow( r, y0 ), u8, sG[ e ], sC[ e ], sS[ e ], sI[ e ] );
+        }
+    }
+    __syncthreads();
+
+    // block-uniform: every tap of the tile inside the image and inside one checkerboard half
+    const int  sep = u.W / 2, x1 = x0 + G::TW - 1, y1 = y0 + TH - 1;
+    const bool interior = x0 - G::S >= 0 && y0 - G::S >= 0 && x1 + G::S < u.W && y1 + G::S < u.H &&
+                          ( x1 + G::S < sep || x0 - G::S >= sep );
+    constexpr int RS = G::off( 0, 1 );
+#pragma unroll 1
+    for( int k = 0; k < G::PY; k++ )
+    {
+        const int ty = threadIdx.y + 8 * k;
+        const int px = x0 + threadIdx.x, py = y0 + ty;
+        if( px >= u.W || py >= u.H ) continue;
+        const int       i  = py * u.W + px;
+        const int       ce = G::crow( ty ) * G::RW + threadIdx.x + G::S;
+        const float     pv = ITER == 0 ? 0.0f : S::ld1( a.filtVar, (size_t)i );
+        const AtrousOut o  = atrous_sm_px< ITER, G::S, RS, RS >( a, px, py, i, interior, sG, sC, sS, sI, ce, ce, pv, S::ld4( a.histLen, (size_t)i ).z );
+        if( ITER == 0 && o.pref ) S::st1( a.filtVar, (size_t)i, o.prefVar );
+        if( !HIST )
+        {
+            S::stcv( io.diffDst, io.varDst, (size_t)i, o.d, o.var );
+            S::st3( io.specDst, (size_t)i, o.s );
+            S::st3( io.indirDst, (size_t)i, o.i );
+        }
+        else
+        {
+            const ComposeIn cin = compose_load( a, px, py, i );
+            const uint16_t  hin = compose< M, true >( a, px, cin, o.d, o.s, o.i, u8 );
+            // one shared atomic per distinct bin of the warp
+            const uint32_t bin   = __ldg( &a.binLut[ hin ] );
+            const uint32_t peers = __match_any_sync( __activemask(), bin );
+            if( ( t & 31 ) == (uint32_t)( __ffs( peers ) - 1 ) ) atomicAdd( &hist[ bin ], (uint32_t)__popc( peers ) );
+        }
+    }
+    if( HIST )
+    {
+        __syncthreads();
+        if( hist[ t ] ) atomicAdd( &a.tm->histogram[ t ], hist[ t ] );
+    }
+}
+
+// ==========================================================================================
+// A-trous iterations 0 and 1 in one launch (fusion depth 2).
+//
+// The block stages iteration 0's sources over its 32 x 8 tile widened by 3 (1 for iteration 0's
+// taps, 2 for iteration 1's), computes iteration 0 over the tile widened by 2, keeps those
+// results in shared memory exactly as they would be stored and read back (the storage mode's
+// quantisation), and then computes iteration 1 (step 2) over the tile. Iteration 0's persistent
+// outputs (DiffColorHistory, the prefiltered variance) are written for the tile's own pixels;
+// its specular and indirect results, which only iteration 1 reads, never leave the chip, nor do
+// iteration 1's sources. The arithmetic is the single-iteration kernels', so the planes are the
+// same bit for bit. The extra cost is iteration 0 over (36 x 12) / (32 x 8) = 1.69 times the
+// tile's pixels.
+// ==========================================================================================
+struct AtPair
+{
+    static constexpr int TW = 32, TH = 8;
+    static constexpr int RW0 = TW + 6, RH0 = TH + 6, N0 = RW0 * RH0;   // iteration 0's sources: tile +- 3
+    static constexpr int RW1 = TW + 4, RH1 = TH + 4, N1 = RW1 * RH1;   // iteration 0's results: tile +- 2
+    static constexpr int SMEM = ( 4 * N0 + 3 * N1 ) * (int)sizeof( float4 ) + TW * TH * (int)sizeof( float );
+};
+
+// the value `v` takes once stored in and read back from a colour + variance / colour plane of
+// storage mode M
+template< int M > __device__ __forceinline__ float4 stored_cv( float3 c, float var )
+{
+    alignas( 16 ) uint8_t tex[ 16 ];
+    float                 vv;
+    Sto< M >::stcv( tex, &vv, 0, c, var );
+    return Sto< M >::ldcv( tex, &vv, 0 );
+}
+template< int M > __device__ __forceinline__ float3 stored_c3( float3 c )
+{
+    alignas( 16 ) uint8_t tex[ 16 ];
+    Sto< M >::st3( tex, 0, c );
+    return Sto< M >::ld3( tex, 0 );
+}
+template< int M > __device__ __forceinline__ float stored_1( float v )
+{
+    alignas( 16 ) uint8_t tex[ 4 ];
+    Sto< M >::st1( tex, 0, v );
+    return Sto< M >::ld1( tex, 0 );
+}
+
+template< int M, int MINB >
+__global__ void __launch_bounds__( 256, MINB ) k_atrous_pair01( const FrameArgs a )
+{
+    using P = AtPair;
+    using S = Sto< M >;
+    extern __shared__ float4 smem[];
+    float4* const    sG = smem;           // iteration 0's sources over tile +- 3
+    float4* const    sC = sG + P::N0;
+    float4* const    sS = sC + P::N0;
+    float4* const    sI = sS + P::N0;
+    float4* const    tC = sI + P::N0;     // iteration 0's results over tile +- 2
+    float4* const    tS = tC + P::N1;
+    float4* const    tI = tS + P::N1;
+    float* const     tP = reinterpret_cast< float* >( tI + P::N1 );   // prefiltered variance of the tile
+    __shared__ float u8[ 256 ];
+    const int        t = threadIdx.y * 32 + threadIdx.x;
+    pdl_launch_dependents();
+    u8[ t ] = (float)t / 255.0f;
+    pdl_wait();
+    __syncthreads();
+
+    const Uniform& u   = a.u;
+    const AtrousIO io0 = atrous_io< M >( a, 0 ), io1 = atrous_io< M >( a, 1 );
+    const int      x0 = blockIdx.x * P::TW, y0 = blockIdx.y * P::TH;
+#pragma unroll
+    for( int k = 0; k < ( P::N0 + 255 ) / 256; k++ )
+    {
+        const int e = t + 256 * k;
+        if( e < P::N0 )
+        {
+            const int r = e / P::RW0, c = e - r * P::RW0;
+            atrous_stage_texel< M >( a, io0, x0 - 3 + c, y0 - 3 + r, u8, sG[ e ], sC[ e ], sS[ e ], sI[ e ] );
+        }
+    }
+    __syncthreads();
+
+    const int sep = u.W / 2;
+    // iteration 0 over tile +- 2; a pixel outside the image is the zero texel iteration 1 reads
+    // there (the roughness stays the staged one, which is zero outside the image as well)
+    {
+        const int  xa = x0 - 2, ya = y0 - 2, xb = x0 + P::TW + 1, yb = y0 + P::TH + 1;
+        const bool interior = xa - 1 >= 0 && ya - 1 >= 0 && xb + 1 < u.W && yb + 1 < u.H && ( xb + 1 < sep || xa - 1 >= sep );
+#pragma unroll 1
+        for( int e = t; e < P::N1; e += 256 )
+        {
+            const int r = e / P::RW1, c = e - r * P::RW1;
+            const int px = xa + c, py = ya + r;
+            const int ce = ( r + 1 ) * P::RW0 + c + 1;
+            float4    vc = make_float4( 0.0f, 0.0f, 0.0f, 0.0f ), vs = vc, vi = make_float4( 0.0f, 0.0f, 0.0f, sI[ ce ].w );
+            if( inside( u, px, py ) )
+            {
+                const int       i  = py * u.W + px;
+                const bool      own = c >= 2 && c < 2 + P::TW && r >= 2 && r < 2 + P::TH;
+                const AtrousOut o  = atrous_sm_px< 0, 1, P::RW0, P::RW0 >( a, px, py, i, interior, sG, sC, sS, sI, ce, ce, 0.0f,
+                                                                            S::ld4( a.histLen, (size_t)i ).z );
+                if( own )
+                {
+                    // iteration 0's persistent outputs, for the tile's own pixels
+                    if( o.pref ) S::st1( a.filtVar, (size_t)i, o.prefVar );
+                    S::stcv( io0.diffDst, io0.varDst, (size_t)i, o.d, o.var );
+                    tP[ ( r - 2 ) * P::TW + c - 2 ] = o.pref ? stored_1< M >( o.prefVar ) : 0.0f;
+                }
+                vc = stored_cv< M >( o.d, o.var );
+                const float3 sp = stored_c3< M >( o.s ), in = stored_c3< M >( o.i );
+                vs = make_float4( sp.x, sp.y, sp.z, Wm< true >::lum( f3( vc.x, vc.y, vc.z ) ) );
+                vi = make_float4( in.x, in.y, in.z, vi.w );
+            }
+            tC[ e ] = vc;
+            tS[ e ] = vs;
+            tI[ e ] = vi;
+        }
+    }
+    __syncthreads();
+
+    // iteration 1 (step 2) over the tile
+    {
+        const int  x1 = x0 + P::TW - 1, y1 = y0 + P::TH - 1;
+        const bool interior = x0 - 2 >= 0 && y0 - 2 >= 0 && x1 + 2 < u.W && y1 + 2 < u.H && ( x1 + 2 < sep || x0 - 2 >= sep );
+        const int  px = x0 + threadIdx.x, py = y0 + threadIdx.y;
+        if( px < u.W && py < u.H )
+        {
+            const int       i  = py * u.W + px;
+            const int       cc = ( threadIdx.y + 2 ) * P::RW1 + threadIdx.x + 2;
+            const int       cg = ( threadIdx.y + 3 ) * P::RW0 + threadIdx.x + 3;
+            const AtrousOut o  = atrous_sm_px< 1, 2, 2 * P::RW1, 2 * P::RW0 >( a, px, py, i, interior, sG, tC, tS, tI, cg, cc, tP[ t ],
+                                                                              S::ld4( a.histLen, (size_t)i ).z );
+            S::stcv( io1.diffDst, io1.varDst, (size_t)i, o.d, o.var );
+            S::st3( io1.specDst, (size_t)i, o.s );
+            S::st3( io1.indirDst, (size_t)i, o.i );
+        }
+    }
+}
+
+// ==========================================================================================
+// A-trous with shared-memory staging by the Tensor Memory Accelerator (opt-in).
 //
 // A 32x8 output tile reads its 3x3 dilated taps from shared memory. The tap footprint of each
 // source image (colour+variance, variance plane, specular, indirect, geometry record) is
@@ -1941,10 +2297,10 @@ __device__ __forceinline__ bool mbar_try_wait( uint64_t* bar, uint32_t phase )
                   : "memory" );
     return ok != 0;
 }
-// bounded wait: false after the limit (the error bit is then set by the caller)
-__device__ __forceinline__ bool mbar_wait_bounded( uint64_t* bar, uint32_t phase )
+// bounded wait: false after `limit` polls (the error bit is then set by the caller)
+__device__ __forceinline__ bool mbar_wait_bounded( uint64_t* bar, uint32_t phase, int limit = 1 << 22 )
 {
-    for( int k = 0; k < ( 1 << 22 ); k++ )
+    for( int k = 0; k < limit; k++ )
         if( mbar_try_wait( bar, phase ) ) return true;
     return false;
 }
@@ -2069,13 +2425,16 @@ __device__ __forceinline__ void atrous_px_tma( const FrameArgs& a, const AtrousI
 }
 
 // Issues the TMA copies of tile (x0, y0)'s footprint into one stage (thread 0 only).
+// `extraTx` bytes are expected on top of what the copies deliver: 0, except under
+// RGDN_FLAG_TEST_TMA_TIMEOUT, where the barrier can then never complete
 template< int M >
-__device__ __forceinline__ void tma_issue_tile( const TmaGeom& g, const AtrousMaps& maps, uint8_t* st, uint64_t* bar, int x0, int y0 )
+__device__ __forceinline__ void tma_issue_tile( const TmaGeom& g, const AtrousMaps& maps, uint8_t* st, uint64_t* bar, int x0, int y0,
+                                                uint32_t extraTx )
 {
     constexpr TmaTexel tx   = { M == MODE_REF ? 8 : M == MODE_F32 ? 16 : 8, ( M == MODE_F16 || M == MODE_BF16 ) ? 4 : 0,
                                 M == MODE_REF ? 4 : M == MODE_F32 ? 16 : 8 };
     const int          box  = g.rw * g.rh;
-    mbar_arrive_expect_tx( bar, (uint32_t)( box * g.nb * ( tx.cv + tx.var + 2 * tx.col + 16 ) ) );
+    mbar_arrive_expect_tx( bar, (uint32_t)( box * g.nb * ( tx.cv + tx.var + 2 * tx.col + 16 ) ) + extraTx );
     // one plane: nb bands of rw x rh texels; 16-byte texels through a 3-D map (word, x, y),
     // the others through a 2-D map of 4-byte words
     auto plane = [ & ]( int off, const CUtensorMap* m, int texBytes ) {
@@ -2097,8 +2456,8 @@ __device__ __forceinline__ void tma_issue_tile( const TmaGeom& g, const AtrousMa
 // Persistent TMA-staged a-trous iteration: block b computes tiles b, b + gridDim.x, ... Each
 // tile's footprint is staged in shared memory by TMA; while the block computes tile k from one
 // stage, the copies of tile k+1 fill the other, so the taps never wait on global memory.
-// Waits are bounded: a timeout sets bit 0 of the stream's error flags, waits (bounded) for the
-// block's copies still in flight and returns.
+// Waits are bounded: a timeout sets bit 0 of the stream's error flags and returns once the
+// block's copies are accounted for (see the timeout branch).
 template< int M, bool FAST, bool HIST >
 __global__ void __launch_bounds__( 256, 3 ) k_atrous_tma( const FrameArgs a, const int iter, const __grid_constant__ AtrousMaps maps )
 {
@@ -2113,6 +2472,11 @@ __global__ void __launch_bounds__( 256, 3 ) k_atrous_tma( const FrameArgs a, con
     const int      tilesX = ( u.W + g.tw - 1 ) / g.tw;
     const int      total  = tilesX * ( ( u.H + g.th - 1 ) / g.th );
     const int      G      = (int)gridDim.x;
+    // RGDN_FLAG_TEST_TMA_TIMEOUT: every stage expects 16 bytes more than its copies bring, and
+    // the waits give up after a short limit
+    const bool     testTimeout = ( u.flags & RGDN_FLAG_TEST_TMA_TIMEOUT ) != 0;
+    const uint32_t extraTx     = testTimeout ? 16u : 0u;
+    const int      limit       = testTimeout ? ( 1 << 14 ) : ( 1 << 22 );
     pdl_launch_dependents();
     pdl_wait();
     if( t == 0 )
@@ -2125,7 +2489,7 @@ __global__ void __launch_bounds__( 256, 3 ) k_atrous_tma( const FrameArgs a, con
     if( HIST ) hist[ t ] = 0u;
     __syncthreads();
     const int first = (int)blockIdx.x;
-    if( t == 0 && first < total ) tma_issue_tile< M >( g, maps, sm, &bar[ 0 ], ( first % tilesX ) * g.tw, ( first / tilesX ) * g.th );
+    if( t == 0 && first < total ) tma_issue_tile< M >( g, maps, sm, &bar[ 0 ], ( first % tilesX ) * g.tw, ( first / tilesX ) * g.th, extraTx );
 
     const AtrousIO io   = atrous_io< M >( a, iter );
     const bool     last = iter + 1 == (int)u.niter;
@@ -2137,16 +2501,24 @@ __global__ void __launch_bounds__( 256, 3 ) k_atrous_tma( const FrameArgs a, con
         const int next = tile + G;
         // the other stage was released by the barrier that ended the previous tile
         if( t == 0 && next < total )
-            tma_issue_tile< M >( g, maps, sm + ( st ^ 1 ) * g.bytes, &bar[ st ^ 1 ], ( next % tilesX ) * g.tw, ( next / tilesX ) * g.th );
-        const bool ready = __syncthreads_and( mbar_wait_bounded( &bar[ st ], ( k >> 1 ) & 1 ) ? 1 : 0 ) != 0;
+            tma_issue_tile< M >( g, maps, sm + ( st ^ 1 ) * g.bytes, &bar[ st ^ 1 ], ( next % tilesX ) * g.tw, ( next / tilesX ) * g.th,
+                                 extraTx );
+        const bool ready = __syncthreads_and( mbar_wait_bounded( &bar[ st ], ( k >> 1 ) & 1, limit ) ? 1 : 0 ) != 0;
         if( !ready )
         {
-            // the copies did not complete: flag the stream, leave the outputs untouched and let
-            // the copies already issued for the next tile land before the block exits
+            // The copies did not complete in time: flag the stream and leave the outputs
+            // untouched. The block may not exit while a copy it issued can still write its
+            // shared memory, and at this point two stages may have copies outstanding: this
+            // tile's (the wait just gave up on them) and the next tile's (issued above). Thread 0
+            // waits for both stages again, each up to the full limit, so copies that are only
+            // slow land before the memory is released. (A barrier that expects more bytes than
+            // its copies bring never completes even after they have landed: both waits then run
+            // out, which is the test's case.)
             if( t == 0 )
             {
-                atomicOr( &a.tm->errorFlags, 1u );
-                if( next < total ) mbar_wait_bounded( &bar[ st ^ 1 ], ( ( k + 1 ) >> 1 ) & 1 );
+                atomicOr( &a.tm->errorFlags, RGDN_DEVICE_ERROR_TMA_WAIT );
+                mbar_wait_bounded( &bar[ st ], ( k >> 1 ) & 1, limit );
+                if( next < total ) mbar_wait_bounded( &bar[ st ^ 1 ], ( ( k + 1 ) >> 1 ) & 1, limit );
             }
             return;
         }
@@ -3320,6 +3692,58 @@ template< int M > cudaError_t launch_final_t( const FinalArgs& f, cudaStream_t s
     return e != cudaSuccess ? e : cudaGetLastError();
 }
 
+// The shared-memory a-trous for one iteration: a 32 x TH tile per 256-thread block, MINB blocks
+// per SM. The dynamic shared memory above 48 KB is enabled once per device.
+template< int M, bool HIST, int ITER, int TH, int MINB > cudaError_t launch_atrous_sm_it( const FrameArgs& a, cudaStream_t s )
+{
+    using G     = dev::AtSm< ITER, TH >;
+    auto kernel = dev::k_atrous_sm< M, HIST, ITER, TH, MINB >;
+    static std::atomic< uint64_t > enabled( 0 );
+    int                            d = 0;
+    if( cudaGetDevice( &d ) != cudaSuccess ) return cudaErrorInvalidDevice;
+    const uint64_t bit = 1ull << ( d & 63 );
+    if( !( enabled.load( std::memory_order_relaxed ) & bit ) )
+    {
+        const cudaError_t e = cudaFuncSetAttribute( kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, G::SMEM );
+        if( e != cudaSuccess ) return e;
+        enabled.fetch_or( bit, std::memory_order_relaxed );
+    }
+    return launch_pdl( kernel, dim3( ( a.u.W + G::TW - 1 ) / G::TW, ( a.u.H + TH - 1 ) / TH ), dim3( 32, 8 ), G::SMEM, s, a );
+}
+// tile rows and resident blocks per iteration: 32 x 8 tiles for steps 1 and 2 (22 and 28 KB of
+// shared memory), 32 x 16 for steps 4 and 8 (61 and 98 KB), three 8-row bands for 16 and 32
+template< int M, bool HIST > cudaError_t launch_atrous_sm( const FrameArgs& a, int iter, cudaStream_t s )
+{
+    switch( iter )
+    {
+        case 0: return launch_atrous_sm_it< M, HIST, 0, 8, 4 >( a, s );
+        case 1: return launch_atrous_sm_it< M, HIST, 1, 8, 4 >( a, s );
+        case 2: return launch_atrous_sm_it< M, HIST, 2, 16, 3 >( a, s );
+        case 3: return launch_atrous_sm_it< M, HIST, 3, 16, 2 >( a, s );
+        case 4: return launch_atrous_sm_it< M, HIST, 4, 8, 2 >( a, s );
+        case 5: return launch_atrous_sm_it< M, HIST, 5, 8, 1 >( a, s );
+        default: return cudaErrorInvalidValue;
+    }
+}
+
+// a-trous iterations 0 and 1 in one launch (the caller ensures iteration 1 is not the last)
+template< int M > cudaError_t launch_atrous_pair01( const FrameArgs& a, cudaStream_t s )
+{
+    using P     = dev::AtPair;
+    auto kernel = dev::k_atrous_pair01< M, 3 >;
+    static std::atomic< uint64_t > enabled( 0 );
+    int                            d = 0;
+    if( cudaGetDevice( &d ) != cudaSuccess ) return cudaErrorInvalidDevice;
+    const uint64_t bit = 1ull << ( d & 63 );
+    if( !( enabled.load( std::memory_order_relaxed ) & bit ) )
+    {
+        const cudaError_t e = cudaFuncSetAttribute( kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, P::SMEM );
+        if( e != cudaSuccess ) return e;
+        enabled.fetch_or( bit, std::memory_order_relaxed );
+    }
+    return launch_pdl( kernel, dim3( ( a.u.W + P::TW - 1 ) / P::TW, ( a.u.H + P::TH - 1 ) / P::TH ), dim3( 32, 8 ), P::SMEM, s, a );
+}
+
 // Kernels whose results are continuous in every arithmetic operation (no threshold follows
 // them), in their own translation units (rgdn_fast_*.cu); their weighted sums use explicit
 // fused multiply-adds.
@@ -3337,6 +3761,9 @@ template< int M > cudaError_t launch_fast_t( const FrameArgs& a, int stage, int 
             e = launch_pdl( dev::k_atrous< M, true, true, true, 128, 7 >, dim3( grid.x, ( a.u.H + 3 ) / 4 ), dim3( 32, 4 ), 0, s, a, iter );
             break;
         case KF_VARIANCE_FAST: e = launch_pdl( dev::k_variance_geo< M, true >, grid, blk, 0, s, a ); break;
+        case KF_ATROUS_SM: e = launch_atrous_sm< M, false >( a, iter, s ); break;
+        case KF_ATROUS_SM_HIST: e = launch_atrous_sm< M, true >( a, iter, s ); break;
+        case KF_ATROUS_PAIR01: e = launch_atrous_pair01< M >( a, s ); break;
         default: return cudaErrorInvalidValue;
     }
     return e != cudaSuccess ? e : cudaGetLastError();

@@ -22,7 +22,7 @@ from raytracedgl1_gb300.scene import Scene
 
 import oracle
 from tests import _formats as F
-from tests.test_gpu_parity import compare_state, stage_sequence, sync_to_oracle, upload_frame
+from tests.test_gpu_parity import TOL, gpu_planes, stage_sequence, sync_to_oracle, upload_frame
 
 pytestmark = pytest.mark.gpu
 
@@ -45,6 +45,33 @@ def frame_both(s, o, sc, f, niter, flags=0):
     o.stage(N.STAGE_LUMINANCE_AVG, 0, fi, p)
     ao = o.tonemapping()[1]
     return hg, ho, ag, ao
+
+
+# The default kernels' variance is E[l^2] - E[l]^2 of spatially weighted moments whose weights
+# use hardware exp2 / repeated squaring (relative error about 1e-5): the cancellation scales
+# that by E[l^2] / variance, so the FP32 variance planes get a wider per-texel bound than the
+# other FP32 planes. Every other plane keeps its storage quantum.
+VARIANCE_PLANES = ("DIFF_PING_VARIANCE", "DIFF_PONG_VARIANCE", "DIFF_COLOR_HISTORY_VARIANCE")
+
+
+def stage_errors(s, o):
+    """Per changed plane: (name, slot, max texel rel err, fraction of texels differing,
+    tolerance, integer texels differing)."""
+    out = []
+    for (name, slot), (g, fmt) in gpu_planes(s).items():
+        c = o.plane(name, slot)
+        if np.array_equal(g, c):
+            continue
+        if fmt in (F.F_R8U, F.F_R32U, F.F_NORMAL):
+            out.append((name, slot, float("inf"), 1.0, 0.0, int(np.count_nonzero(g != c))))
+            continue
+        gd, cd = F.decode(g, fmt), F.decode(c, fmt)
+        scale = np.percentile(np.abs(cd[np.isfinite(cd)]), 99) if np.isfinite(cd).any() else 1.0
+        err = F.texel_rel_err(gd, cd, atol=max(1e-6, 1e-4 * float(scale)))
+        ndiff = int(np.count_nonzero(np.any(g != c, axis=-1) if g.ndim == 3 else g != c))
+        tol = 2e-2 if name in VARIANCE_PLANES else TOL[fmt]
+        out.append((name, slot, float(err.max()), ndiff / err.size, tol, 0))
+    return out
 
 
 def pre_final_metrics(s, o, fi):
@@ -79,8 +106,8 @@ def test_config1_640x360_fp32(ctx, niter, math):
     assert m["max_rel"] <= 1e-3, m
     # a moved count needs a HistogramInput within an fp16 rounding step of a bin edge: a few per
     # 230 400 pixels, and the average luminance follows the histogram
-    assert max(moved) <= 64, moved
-    assert max(avg_rel) <= 1e-4, avg_rel
+    assert max(moved) <= 16, moved
+    assert max(avg_rel) <= 1e-5, avg_rel
 
 
 def test_config2_1080p_fp16(ctx):
@@ -96,8 +123,8 @@ def test_config2_1080p_fp16(ctx):
     print(f"\nconfig 2, {frames - 1} independent frames: PRE_FINAL {m}; histogram counts moved per frame {moved}")
     # 16-bit storage: a flip of one stored quantum propagates through the history, so the bar is
     # on the image as a whole
-    assert m["frac_le_1e-2"] >= 0.99 and m["psnr_db"] > 50.0, m
-    assert max(moved) <= 1024, moved
+    assert m["frac_le_1e-2"] >= 0.9999 and m["psnr_db"] > 100.0, m
+    assert max(moved) <= 256, moved
 
     # the last frame, stage by stage on the default kernels, from the GPU's state
     f = frames - 1
@@ -106,7 +133,7 @@ def test_config2_1080p_fp16(ctx):
     p.atrousIterations = niter
     p.flags = N.FLAG_STAGE_DEFAULT
     upload_frame(s, o, bufs, fi)
-    worst = []
+    worst, bad = [], []
     for stage, it in stage_sequence(niter):
         sync_to_oracle(s, o)
         h0 = s.tonemapping()[0].copy()
@@ -121,11 +148,20 @@ def test_config2_1080p_fp16(ctx):
         o.stage(stage, it, fi, p)
         if stage == N.STAGE_ATROUS and it == niter - 1:
             h_before_last = h0
-        worst += compare_state(s, o, f"1080p fp16 frame {f} stage {stage}.{it}")
+        for name, slot, err, frac, tol, nint in stage_errors(s, o):
+            where = f"stage {stage}.{it} {name}[{slot}]"
+            worst.append((where, err, frac))
+            if nint:
+                bad.append(f"{where}: integer plane differs at {nint} texels")
+            elif err > tol:
+                bad.append(f"{where}: max texel rel err {err:.3e} > {tol:.1e}")
+            elif not name.endswith("VARIANCE") and F.QUANTUM.get(s.image(name, slot).format, 0) > 2.0 ** -20 and frac > 0.02:
+                bad.append(f"{where}: {frac:.2%} of texels differ")
         if stage == N.STAGE_LUMINANCE_AVG:
             hg, ag, _ = s.tonemapping()
             hc, ac, _ = o.tonemapping()
             assert np.array_equal(hg, hc) and np.float32(ag) == np.float32(ac), "average luminance differs"
-    worst.sort(key=lambda w: -w[2])
-    print("largest per-stage texel errors:", worst[:6])
+    worst.sort(key=lambda w: -w[1])
+    print("largest per-stage texel errors:", worst[:8])
     s.close()
+    assert not bad, bad

@@ -358,6 +358,39 @@ def test_tma_staging_equals_default(ctx, mode_name, mode):
     b.close()
 
 
+@pytest.mark.parametrize("mode_name,mode", MODES)
+@pytest.mark.parametrize("size", [(96, 54), (250, 151), (330, 97)])
+def test_atrous_shared_equals_direct(ctx, mode_name, mode, size):
+    """The default a-trous (taps decoded once into shared memory) computes the direct kernel's
+    arithmetic: identical planes, with partial tiles on the right and bottom edges and every step
+    from 1 to 32 (4, 5 and 6 iterations)."""
+    W, H = size
+    sc = Scene(W, H, seed=29, lightFlickerFrom=2.0)
+    a = Stream(ctx, W, H, mode)
+    b = Stream(ctx, W, H, mode)
+    for f in range(5):
+        fi = f & 1
+        bufs, p = sc.generate(f)
+        p.atrousIterations = (4, 5, 6)[f % 3]
+        upload_frame(a, None, bufs, fi)
+        upload_frame(b, None, bufs, fi)
+        pb = p.copy()
+        pb.flags = N.FLAG_ATROUS_DIRECT
+        if f % 2:
+            p = p.copy()
+            p.flags = N.FLAG_ATROUS_PAIR   # iterations 0 and 1 in one launch
+        for s, q in ((a, p), (b, pb)):
+            Denoiser(s).Denoise(fi, q)
+            Tonemapping(s).CalculateExposure(fi, q)
+        ga, gb = gpu_planes(a), gpu_planes(b)
+        for key in ga:
+            assert np.array_equal(ga[key][0], gb[key][0]), f"frame {f}: {key} differs"
+        ta, tb = a.tonemapping(), b.tonemapping()
+        assert np.array_equal(ta[0], tb[0]) and ta[1] == tb[1]
+    a.close()
+    b.close()
+
+
 def test_batch_equals_sequential(ctx):
     """rgdn_submit_batch over streams of different sizes == each stream alone."""
     sizes = [(64, 36), (48, 30), (96, 54)]
@@ -713,6 +746,35 @@ def test_device_errors_clear_on_a_clean_run(ctx):
         Denoiser(s).Denoise(f & 1, p)
         Tonemapping(s).CalculateExposure(f & 1, p)
         assert s.take_device_errors() == 0
+    s.close()
+
+
+def test_tma_wait_runs_out_and_reports(ctx):
+    """A TMA-staged a-trous pass whose barriers cannot complete gives up after its bounded wait,
+    sets RGDN_DEVICE_ERROR_TMA_WAIT and returns, and the stream stays usable. The failure is made
+    on purpose without any copy left in flight: under RGDN_FLAG_TEST_TMA_TIMEOUT every stage
+    expects 16 bytes more than its copies deliver, so every copy lands while the barrier phase
+    never completes."""
+    W, H = 96, 54   # width divisible by 4: every iteration takes the TMA path
+    sc = Scene(W, H, seed=31)
+    s = Stream(ctx, W, H, N.STORAGE_FP16)
+    bufs, p = sc.generate(0)
+    upload_frame(s, None, bufs, 0)
+    p.flags |= N.FLAG_TMA_STAGING | N.FLAG_TEST_TMA_TIMEOUT
+    Denoiser(s).Denoise(0, p)
+    s.synchronize()
+    assert s.take_device_errors() & N.DEVICE_ERROR_TMA_WAIT
+    assert s.take_device_errors() == 0   # taken and cleared
+    # the context and the stream still work: a normal frame reports nothing
+    for f in (1, 2):
+        bufs, p = sc.generate(f)
+        upload_frame(s, None, bufs, f & 1)
+        p.flags |= N.FLAG_TMA_STAGING
+        Denoiser(s).Denoise(f & 1, p)
+        Tonemapping(s).CalculateExposure(f & 1, p)
+        assert s.take_device_errors() == 0
+    img = s.image("PRE_FINAL", 0)
+    assert np.isfinite(F.decode(s.download("PRE_FINAL", 0), img.format)).all()
     s.close()
 
 
