@@ -83,6 +83,7 @@ typedef enum rgdn_format
     RGDN_FORMAT_E5B9G9R9_UFLOAT,  /* 4 B, shared exponent (EXT_texture_shared_exponent) */
     RGDN_FORMAT_B10G11R11_UFLOAT, /* 4 B */
     RGDN_FORMAT_NORMAL_SPHERICAL, /* 4 B, (phi:16 | theta:16) code of Source/Shaders/Utils.h:105-140 */
+    RGDN_FORMAT_RGBA32_UINT,      /* 16 B */
 } rgdn_format;
 
 /* The framebuffer images of one stream. Names follow the reference's framebuffer
@@ -161,6 +162,11 @@ typedef enum rgdn_framebuf
                                          (cell (x, y, z) at row z * Y + y); rgb in-scattered light,
                                          a extinction along the cell; prev (two slots, as the
                                          reference's scattering[2]) */
+    /* gradient re-shading on the device (rgdn_stream_set_reshade_scene) */
+    RGDN_FB_RESERVOIRS,               /* RGBA32_UINT: the direct-light reservoir of each pixel as
+                                         packReservoir stores it (Reservoir.h:116-136): x = M << 16 |
+                                         selected light, y = bits of the selected target pdf, z = bits of
+                                         the weight sum; prev (the producer writes it every frame) */
     RGDN_FB_COUNT
 } rgdn_framebuf;
 
@@ -200,6 +206,7 @@ typedef struct rgdn_frame_params
     uint32_t debugShowFlags;        /* DEBUG_SHOW_FLAG_* of ShaderCommonC.h */
     uint32_t atrousIterations;      /* 0 or 4 = the reference's 4 iterations; 1..6 allowed */
     uint32_t flags;                 /* RGDN_FLAG_* */
+    uint32_t frameId;               /* GlobalUniform::frameId: seeds the re-shaded light samples */
 } rgdn_frame_params;
 
 /* rgdn_frame_params.flags */
@@ -388,6 +395,49 @@ typedef struct rgdn_volumetric_params
                                        square root, sin/cos and exp2 for its continuous terms
                                        (the reprojection tests decide exactly either way) */
 rgdn_status rgdn_process_scattering( rgdn_stream* stream, uint32_t frameIndex, const rgdn_volumetric_params* params, rgdn_cuda_stream cudaStream );
+
+/* ---- gradient re-shading on the device --------------------------------------------------
+ * RtGradients.rgen:107-136 re-lights the previous frame's surface at each gradient sample with
+ * this frame's lights (processDirectIllumination with the previous frame's reservoir and random
+ * seed, a shadow ray against the scene). By default the producer supplies that luminance as
+ * RGDN_FB_GRADIENT_RESHADED. With a re-shade scene set, the gradient-samples kernel computes it
+ * itself from RGDN_FB_RESERVOIRS (previous slot), the previous slot's SURFACE_POSITION, NORMAL and
+ * METALLIC_ROUGHNESS, this frame's sphere lights and the scene's analytic occluders, which stand
+ * in for the reference's acceleration structure (no triangle meshes on this path). Every surface
+ * counts as matched by the visibility buffer, since analytic surfaces have exact positions. */
+typedef struct rgdn_sphere_light
+{
+    float center[ 3 ];
+    float radius;
+    float color[ 3 ];
+    float pad;
+} rgdn_sphere_light;   /* SphereLight (Light.h:31-36), ShLightEncoded's LIGHT_TYPE_SPHERE */
+
+#define RGDN_OCCLUDER_SPHERE 0u   /* data: center xyz, radius */
+#define RGDN_OCCLUDER_RECT   1u   /* data: axis (0 = x, 1 = y, 2 = z) as float, plane offset along it,
+                                     then min, max of the first and min, max of the second of the
+                                     other two coordinates in x, y, z order (data[6] unused): an
+                                     axis-aligned rectangle (an unbounded plane with +-inf) */
+typedef struct rgdn_occluder
+{
+    uint32_t type;
+    float    data[ 7 ];
+} rgdn_occluder;
+
+typedef struct rgdn_reshade_scene
+{
+    const rgdn_sphere_light* lights;         /* device: this frame's lights (lightSources) */
+    uint32_t                 lightCount;
+    const uint32_t*          prevToCur;      /* device: lightSources_Index_PrevToCur, prevLightCount
+                                                entries; 0xFFFFFFFF = the light is gone */
+    uint32_t                 prevLightCount;
+    const rgdn_occluder*     occluders;      /* device: shadow-ray geometry */
+    uint32_t                 occluderCount;
+} rgdn_reshade_scene;
+
+/* Sets (scene != NULL) or clears the re-shade scene of a stream; the arrays must stay valid for
+ * every frame denoised with them. The frame's rgdn_frame_params.frameId seeds the samples. */
+rgdn_status rgdn_stream_set_reshade_scene( rgdn_stream* stream, const rgdn_reshade_scene* scene );
 
 /* One stage alone (per-stage checking): the plain path's kernel, or with
  * RGDN_FLAG_STAGE_DEFAULT the default path's. `iteration` selects the a-trous or gradient

@@ -23,7 +23,7 @@ MODE_REF, MODE_F32, MODE_F16, MODE_BF16, MODE_F64 = 0, 1, 2, 3, 4
 _NUMPY = {
     1: (np.uint8, 1), 2: (np.uint8, 2), 3: (np.uint8, 4), 4: (np.uint16, 1), 5: (np.uint16, 2),
     6: (np.uint16, 4), 7: (np.uint16, 4), 8: (np.float32, 1), 9: (np.float32, 2), 10: (np.float32, 4),
-    11: (np.uint32, 1), 12: (np.uint32, 1), 13: (np.uint32, 1), 14: (np.uint32, 1),
+    11: (np.uint32, 1), 12: (np.uint32, 1), 13: (np.uint32, 1), 14: (np.uint32, 1), 15: (np.uint32, 4),
     100: (np.float64, 1), 101: (np.float64, 2), 102: (np.float64, 4),
 }
 
@@ -54,6 +54,8 @@ def load():
         "orc_bloom": (C.c_int, [C.c_void_p, C.c_uint32, C.c_float]),
         "orc_process_scattering": (C.c_int, [C.c_void_p, C.c_uint32, P(VolumetricParams)]),
         "orc_random_seed": (C.c_uint32, [C.c_int, C.c_int, C.c_uint32]),
+        "orc_set_reshade_scene": (None, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.c_uint32, C.c_void_p, C.c_uint32]),
+        "orc_reshade": (C.c_int, [C.c_void_p, C.c_uint32, C.c_int, C.c_int, P(FrameParams), C.c_int, P(C.c_double)]),
         "orc_wellons_lowbias32": (C.c_uint32, [C.c_uint32]),
         "orc_lpm_setup": (None, [P(C.c_float), P(C.c_float), P(C.c_float)]),
         "orc_lpm_filter": (None, [P(C.c_float), P(C.c_float), P(C.c_float)]),
@@ -162,6 +164,26 @@ class OracleStream:
         avg64 = C.c_double()
         self.lib.orc_get_tonemapping(self.h, hist, C.byref(avg), C.byref(avg64))
         return np.frombuffer(hist, dtype=np.uint32).copy(), avg.value, self.lib.orc_exposure_from_avg(avg.value)
+
+    def set_reshade_scene(self, lights=None, prev_to_cur=None, occluders=None) -> None:
+        """Gradient re-shading from these host arrays (numpy structured / ctypes arrays of
+        rgdn_sphere_light, uint32, rgdn_occluder); lights None clears it."""
+        if lights is None:
+            self.lib.orc_set_reshade_scene(self.h, None, 0, None, 0, None, 0)
+            return
+        self._rs = (lights, prev_to_cur, occluders)   # keep the buffers alive
+        self.lib.orc_set_reshade_scene(self.h, C.cast(lights, C.c_void_p), len(lights),
+                                       C.cast(prev_to_cur, C.c_void_p), len(prev_to_cur),
+                                       C.cast(occluders, C.c_void_p) if occluders is not None else None,
+                                       len(occluders) if occluders is not None else 0)
+
+    def reshade(self, frame_index: int, px: int, py: int, params, f64: bool = False):
+        """The re-shaded (diffuse, specular) luminance of previous-frame pixel (px, py)."""
+        out = (C.c_double * 2)()
+        r = self.lib.orc_reshade(self.h, frame_index, px, py, C.byref(params), 1 if f64 else 0, out)
+        if r != 0:
+            raise RuntimeError(f"orc_reshade failed: {r}")
+        return out[0], out[1]
 
     def set_tonemapping(self, hist, avg: float) -> None:
         h = (C.c_uint32 * 256)(*[int(x) for x in hist]) if hist is not None else None

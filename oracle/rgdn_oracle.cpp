@@ -343,6 +343,7 @@ enum Fmt : uint32_t
     F_E5       = RGDN_FORMAT_E5B9G9R9_UFLOAT,
     F_B10G11R11= RGDN_FORMAT_B10G11R11_UFLOAT,
     F_NORMAL   = RGDN_FORMAT_NORMAL_SPHERICAL,
+    F_RGBA32U  = RGDN_FORMAT_RGBA32_UINT,
     // oracle-only, FP64 error reference
     F_R64F     = 100,
     F_RG64F    = 101,
@@ -358,7 +359,7 @@ inline uint32_t fmt_bytes( uint32_t f )
         case F_R16F: return 2;
         case F_RGBA8: case F_RG16F: case F_R32F: case F_R32U: case F_E5: case F_B10G11R11: case F_NORMAL: return 4;
         case F_RGBA16F: case F_RGBA16BF: case F_RG32F: case F_R64F: return 8;
-        case F_RGBA32F: case F_RG64F: return 16;
+        case F_RGBA32F: case F_RG64F: case F_RGBA32U: return 16;
         case F_RGBA64F: return 32;
         default: return 0;
     }
@@ -442,6 +443,8 @@ FbInfo fb_info( uint32_t fb, uint32_t mode )
         case RGDN_FB_BLOOM_MIP1: case RGDN_FB_BLOOM_MIP2: case RGDN_FB_BLOOM_MIP3: case RGDN_FB_BLOOM_MIP4:
         case RGDN_FB_BLOOM_MIP5: case RGDN_FB_BLOOM_MIP6: case RGDN_FB_BLOOM_MIP7: case RGDN_FB_BLOOM_MIP8:
             return { pre, false, false, (int)( fb - RGDN_FB_BLOOM_MIP1 ) + 1 };
+        // GenerateShaderCommon.py Reservoirs (R32G32B32A32_UINT, stored with _Prev)
+        case RGDN_FB_RESERVOIRS: return { F_RGBA32U, true, false };
         default: return { F_NONE, false, false };
     }
 }
@@ -468,6 +471,12 @@ struct Plane
         uint32_t v; memcpy( &v, at( x, y ), 4 ); return v;
     }
     uint32_t raw_u8( int x, int y ) const { return inside( x, y ) ? *at( x, y ) : 0u; }
+    // one 32-bit word k of a texel (RGBA32_UINT)
+    uint32_t raw_word( int x, int y, int k ) const
+    {
+        if( !inside( x, y ) ) return 0;
+        uint32_t v; memcpy( &v, at( x, y ) + 4 * k, 4 ); return v;
+    }
 
     // texelFetch with the OOB-is-zero convention, decoded to T
     template< class T > V4< T > fetch( int x, int y ) const
@@ -542,6 +551,11 @@ struct Stream
     Plane    planes[ RGDN_FB_COUNT ][ 2 ];
     uint32_t hist[ 256 ] = {};
     double   avgLum      = 0.0;
+    // the re-shade scene (rgdn_stream_set_reshade_scene), host copies
+    bool                              rsSet = false;
+    std::vector< rgdn_sphere_light > lights;
+    std::vector< uint32_t >           prevToCur;
+    std::vector< rgdn_occluder >      occluders;
 
     void init( int w, int h, uint32_t m )
     {
@@ -600,6 +614,9 @@ template< class F > void parallel_rows( int h, int nthreads, F&& fn )
 
 constexpr int   STRATA         = 3;        // COMPUTE_ASVGF_STRATA_SIZE (ShaderCommonC.h:150)
 constexpr float MAX_RAY_LENGTH = 10000.0f; // ShaderCommonC.h:167
+
+uint32_t wellons_lowbias32( uint32_t x );
+uint32_t random_seed( int px, int py, uint32_t frame );
 
 template< class T > struct Denoise
 {
@@ -680,6 +697,140 @@ template< class T > struct Denoise
         else C( fb ).template store< T >( x, y, { c.x, c.y, c.z, var } );
     }
 
+    // ---------------------------------------------------------------- RtGradients.rgen:107-136
+    // forwardProjectedLuminance of previous-frame pixel (px, py): the previous surface
+    // (Surface.inl:72-90) lit by this frame's light selected through the previous reservoir
+    // (Reservoir.h:138-146, lightSources_Index_PrevToCur), with the previous frame's seed
+    // (Random.h:289-300) and light point (RaygenCommon.h:624-627, Light.h:244-258), shaded
+    // (RaygenCommon.h:364-380, BRDF.h:34-146) and shadow-tested (RaygenCommon.h:322-359) against
+    // the analytic occluders.
+    static T safe_positive_rcp( T f ) { return f <= (T)0 ? (T)0 : (T)1 / f; }
+    static V3< T > normalize_( V3< T > v ) { return v / o_sqrt( dot3( v, v ) ); }
+    static V3< T > safe_normalize( V3< T > v )
+    {
+        T len = o_sqrt( dot3( v, v ) );
+        return len > K( 0.001 ) ? v / len : V3< T >{ 0, 1, 0 };
+    }
+    static T safe_solid_angle( T a )
+    {
+        return a > (T)0 && !std::isnan( a ) && !std::isinf( a ) ? gclamp( a, (T)0, (T)4 * K( 3.14159265358979323846 ) ) : (T)0;
+    }
+    static T o_cos_( T x ) { if constexpr( std::is_same< T, float >::value ) return cosf( x ); else return cos( x ); }
+    static T o_sin_( T x ) { if constexpr( std::is_same< T, float >::value ) return sinf( x ); else return sin( x ); }
+    V3< T > brdf_smith_ggx( V3< T > n, V3< T > v, V3< T > l, T alpha, V3< T > specColor ) const
+    {
+        const T PI = K( 3.14159265358979323846 );
+        alpha      = o_fmax( alpha, K( 0.005 ) );
+        const T nl = o_fmax( dot3( n, l ), (T)0 );
+        if( nl <= (T)0 ) return { 0, 0, 0 };
+        const T       fr = o_pow( (T)1 - o_fmax( nl, (T)0 ), K( 5.0 ) );
+        const V3< T > F  = { specColor.x + ( (T)1 - specColor.x ) * fr, specColor.y + ( (T)1 - specColor.y ) * fr,
+                             specColor.z + ( (T)1 - specColor.z ) * fr };
+        const V3< T > h       = normalize_( v + l );
+        const T       alphaSq = alpha * alpha;
+        const T       nm      = o_fmax( (T)0, dot3( n, h ) );
+        const T       dd      = nm * nm * ( alphaSq - (T)1 ) + (T)1;
+        const T       D       = alphaSq / PI / ( dd * dd );
+        const T       nv      = o_fmax( dot3( n, v ), (T)0 );
+        const T       G2      = K( 0.5 ) / gmix( (T)2 * nl * nv, nl + nv, alpha );
+        return F * ( G2 * D );
+    }
+    bool shadowed( V3< T > start, V3< T > end ) const
+    {
+        V3< T >  l           = end - start;
+        const T  maxDistance = o_sqrt( dot3( l, l ) );
+        l                    = l / maxDistance;
+        const T tmin = K( 0.001 ), tmax = maxDistance - K( 0.01 );
+        for( const rgdn_occluder& o : s.occluders )
+        {
+            if( o.type == RGDN_OCCLUDER_SPHERE )
+            {
+                const V3< T > oc   = start - V3< T >{ (T)o.data[ 0 ], (T)o.data[ 1 ], (T)o.data[ 2 ] };
+                const T       b    = dot3( oc, l );
+                const T       c    = dot3( oc, oc ) - (T)o.data[ 3 ] * (T)o.data[ 3 ];
+                const T       disc = b * b - c;
+                if( disc <= (T)0 ) continue;
+                const T sq = o_sqrt( disc );
+                const T t0 = -b - sq, t1 = -b + sq;
+                if( ( t0 >= tmin && t0 <= tmax ) || ( t1 >= tmin && t1 <= tmax ) ) return true;
+            }
+            else if( o.type == RGDN_OCCLUDER_RECT )
+            {
+                const int ax = (int)o.data[ 0 ];
+                const T   so = ax == 0 ? start.x : ax == 1 ? start.y : start.z;
+                const T   dl = ax == 0 ? l.x : ax == 1 ? l.y : l.z;
+                if( dl == (T)0 ) continue;
+                const T t = ( (T)o.data[ 1 ] - so ) / dl;
+                if( !( t >= tmin && t <= tmax ) ) continue;
+                const V3< T > q  = start + l * t;
+                const T       u0 = ax == 0 ? q.y : q.x, u1 = ax == 2 ? q.y : q.z;
+                if( u0 >= (T)o.data[ 2 ] && u0 <= (T)o.data[ 3 ] && u1 >= (T)o.data[ 4 ] && u1 <= (T)o.data[ 5 ] ) return true;
+            }
+        }
+        return false;
+    }
+    V2< T > reshade( int px, int py )
+    {
+        const T  PI  = K( 3.14159265358979323846 );
+        Plane&   res = P( RGDN_FB_RESERVOIRS );
+        const uint32_t r0 = res.raw_word( px, py, 0 );
+        const uint32_t selectedPrev = r0 & 65535u, Mres = ( r0 >> 16 ) & 65535u;
+        if( selectedPrev == 32767u || selectedPrev >= s.prevToCur.size() ) return { 0, 0 };   // LIGHT_INDEX_NONE
+        const uint32_t sel = s.prevToCur[ selectedPrev ];
+        if( sel == 0xFFFFFFFFu || sel >= s.lights.size() ) return { 0, 0 };
+        float tpdf, wsum;
+        {
+            uint32_t a = res.raw_word( px, py, 1 ), b = res.raw_word( px, py, 2 );
+            memcpy( &tpdf, &a, 4 );
+            memcpy( &wsum, &b, 4 );
+        }
+        const V4< T > sp   = P( RGDN_FB_SURFACE_POSITION ).template fetch< T >( px, py );
+        const V3< T > pos  = { sp.x, sp.y, sp.z };
+        const V4< T > mr   = P( RGDN_FB_METALLIC_ROUGHNESS ).template fetch< T >( px, py );
+        const T       metallic = mr.x, roughness = mr.y;
+        const T       spc  = K( 0.04 ) * ( (T)1 - metallic ) + (T)1 * metallic;   // getSpecularColor(vec3(1), metallic)
+        const V3< T > n    = fetch_normal( P( RGDN_FB_NORMAL ), px, py );
+        const V3< T > cam  = { (T)p.cameraPositionPrev[ 0 ], (T)p.cameraPositionPrev[ 1 ], (T)p.cameraPositionPrev[ 2 ] };
+        const V3< T > v    = normalize_( cam - pos );
+        const uint32_t seed = random_seed( px, py, p.frameId - 1u );
+        const uint32_t rnd  = wellons_lowbias32( seed + 20u );   // RANDOM_SALT_LIGHT_POINT
+        const T        r1   = (T)( (float)( rnd & 0xFFFFu ) / 65535.0f ) * K( 0.99 );
+        const T        r2   = (T)( (float)( ( rnd & 0xFFFF0000u ) >> 16 ) / 65535.0f ) * K( 0.99 );
+        const rgdn_sphere_light& L = s.lights[ sel ];
+        const V3< T > c   = { (T)L.center[ 0 ], (T)L.center[ 1 ], (T)L.center[ 2 ] };
+        V3< T >       tc  = c - pos;
+        const T       tl  = o_sqrt( dot3( tc, tc ) );
+        tc                = tc / tl;
+        // sampleOrientedHemisphere(-toLightCenter.dir, u1, u2) (Random.h:175-201)
+        V3< T > ln;
+        {
+            T       a   = (T)1 - (T)2 * r1;
+            T       b   = o_sqrt( (T)1 - a * a );
+            const T phi = (T)2 * PI * r2;
+            a = a * K( 0.98 );
+            b = b * K( 0.98 );
+            ln = normalize_( V3< T >{ -tc.x + b * o_cos_( phi ), -tc.y + b * o_sin_( phi ), -tc.z + a } );
+        }
+        const V3< T > lpos = c + ln * (T)L.radius;
+        T             dw;
+        {
+            const T sinTheta = (T)L.radius / o_fmax( (T)L.radius, tl );
+            const T cosTheta = o_sqrt( (T)1 - sinTheta * sinTheta );
+            dw               = safe_solid_angle( (T)2 * PI * ( (T)1 - cosTheta ) );
+        }
+        const V3< T > col = { (T)L.color[ 0 ], (T)L.color[ 1 ], (T)L.color[ 2 ] };
+        const V3< T > l   = safe_normalize( lpos - pos );
+        const T       nl  = dot3( n, l );
+        if( nl <= (T)0 ) return { 0, 0 };
+        const T       w    = safe_positive_rcp( (T)tpdf ) * ( (T)wsum / (T)std::max( 1u, Mres ) );
+        const V3< T > base = col * ( dw * nl );
+        const V3< T > dif  = ( base * ( (T)1 / PI ) ) * w;
+        const V3< T > spe  = ( base * brdf_smith_ggx( n, v, l, roughness, { spc, spc, spc } ) ) * w;
+        if( luminance( dif + spe ) <= (T)0 ) return { 0, 0 };
+        if( shadowed( pos + v * K( 0.01 ), lpos ) ) return { 0, 0 };
+        return { luminance( dif ), luminance( spe ) };
+    }
+
     // ---------------------------------------------------------------- RtGradients.rgen:44-181
     void gradient_samples()
     {
@@ -735,6 +886,12 @@ template< class T > struct Denoise
                     continue;
                 }
                 V4< T > fpl = reshaded.template fetch< T >( prevShadingPix.x, prevShadingPix.y );
+                if( s.rsSet )
+                {
+                    const V2< T > r = reshade( prevShadingPix.x, prevShadingPix.y );
+                    fpl.x = r.x;
+                    fpl.y = r.y;
+                }
                 T g[ 3 ];
                 {
                     T gs = fpl.x - prevLum.x;
@@ -1933,6 +2090,37 @@ void* orc_stream_plane( orc_stream* o, uint32_t fb, uint32_t frameIndex, uint32_
     if( outTexel ) *outTexel = pl.texel;
     if( outFmt ) *outFmt = pl.fmt;
     return pl.bytes.empty() ? nullptr : pl.bytes.data();
+}
+
+// the re-shade scene from host arrays (lights == NULL clears it)
+void orc_set_reshade_scene( orc_stream* o, const rgdn_sphere_light* lights, uint32_t lightCount, const uint32_t* prevToCur,
+                            uint32_t prevLightCount, const rgdn_occluder* occluders, uint32_t occluderCount )
+{
+    if( !o ) return;
+    o->s.rsSet = lights != nullptr;
+    o->s.lights.assign( lights, lights ? lights + lightCount : lights );
+    o->s.prevToCur.assign( prevToCur, prevToCur ? prevToCur + prevLightCount : prevToCur );
+    o->s.occluders.assign( occluders, occluders ? occluders + occluderCount : occluders );
+}
+
+// forwardProjectedLuminance of previous-frame pixel (px, py) for frame slot frameIndex (the
+// re-shading alone, for the known-answer tests)
+int orc_reshade( orc_stream* o, uint32_t frameIndex, int px, int py, const rgdn_frame_params* p, int f64, double out[ 2 ] )
+{
+    if( !o || !p || !out || !o->s.rsSet ) return RGDN_WRONG_FUNCTION_ARGUMENT;
+    if( f64 )
+    {
+        orc::Denoise< double > dn{ o->s, frameIndex, *p, 1 };
+        const auto r = dn.reshade( px, py );
+        out[ 0 ] = r.x; out[ 1 ] = r.y;
+    }
+    else
+    {
+        orc::Denoise< float > dn{ o->s, frameIndex, *p, 1 };
+        const auto r = dn.reshade( px, py );
+        out[ 0 ] = r.x; out[ 1 ] = r.y;
+    }
+    return RGDN_SUCCESS;
 }
 
 uint32_t orc_stream_grad_width( orc_stream* o ) { return o ? (uint32_t)o->s.GW : 0; }

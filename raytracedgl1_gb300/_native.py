@@ -35,7 +35,7 @@ FB_NAMES = [
     "SCREEN_EMIS_RT", "SCATTERING", "FINAL", "BLOOM_INPUT",
     "BLOOM_MIP1", "BLOOM_MIP2", "BLOOM_MIP3", "BLOOM_MIP4", "BLOOM_MIP5", "BLOOM_MIP6", "BLOOM_MIP7",
     "BLOOM_MIP8", "BLOOM_RESULT",
-    "DEPTH_NDC", "SCATTERING_HISTORY", "SCATTER_VOLUME",
+    "DEPTH_NDC", "SCATTERING_HISTORY", "SCATTER_VOLUME", "RESERVOIRS",
 ]
 FB = {n: i for i, n in enumerate(FB_NAMES)}
 FB_COUNT = len(FB_NAMES)
@@ -114,13 +114,32 @@ class FrameParams(C.Structure):
         ("gradientMultDiffuse", C.c_float), ("gradientMultIndirect", C.c_float),
         ("gradientMultSpecular", C.c_float), ("antiFireflyEnabled", C.c_uint32),
         ("lightmapScreenCoverage", C.c_float), ("debugShowFlags", C.c_uint32),
-        ("atrousIterations", C.c_uint32), ("flags", C.c_uint32),
+        ("atrousIterations", C.c_uint32), ("flags", C.c_uint32), ("frameId", C.c_uint32),
     ]
 
     def copy(self) -> "FrameParams":
         p = FrameParams()
         C.memmove(C.byref(p), C.byref(self), C.sizeof(FrameParams))
         return p
+
+
+class SphereLight(C.Structure):
+    """rgdn_sphere_light: SphereLight (Light.h:31-36)."""
+    _fields_ = [("center", C.c_float * 3), ("radius", C.c_float), ("color", C.c_float * 3), ("pad", C.c_float)]
+
+
+OCCLUDER_SPHERE, OCCLUDER_RECT = 0, 1
+
+
+class Occluder(C.Structure):
+    _fields_ = [("type", C.c_uint32), ("data", C.c_float * 7)]
+
+
+class ReshadeScene(C.Structure):
+    """rgdn_reshade_scene: device arrays of this frame's lights, the previous-to-current light
+    index map and the shadow-ray occluders."""
+    _fields_ = [("lights", C.c_void_p), ("lightCount", C.c_uint32), ("prevToCur", C.c_void_p),
+                ("prevLightCount", C.c_uint32), ("occluders", C.c_void_p), ("occluderCount", C.c_uint32)]
 
 
 class Image(C.Structure):
@@ -215,6 +234,7 @@ SIGNATURES = [
     ("rgdn_api_version", _U32, []),
     ("rgdn_histogram_bin_table", _I, [C.c_float, C.c_float, C.POINTER(C.c_uint8)]),
     ("rgdn_gradient_atrous_noalloc", _I, [_VP, _VP, _VP, _U32, _U32, _VP]),
+    ("rgdn_stream_set_reshade_scene", _I, [_VP, C.POINTER(ReshadeScene)]),
     ("rgdn_stream_set_timing", _I, [_VP, _U32]),
     ("rgdn_stream_read_timing", _I, [_VP, C.POINTER(StageTiming), _U32, C.POINTER(_U32)]),
     ("rgdn_batch_get_config", _I, [_VP, _U32, C.POINTER(BatchConfig)]),

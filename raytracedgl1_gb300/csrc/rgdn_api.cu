@@ -88,7 +88,7 @@ uint32_t format_bytes( uint32_t f )
         case RGDN_FORMAT_R32_UINT: case RGDN_FORMAT_E5B9G9R9_UFLOAT: case RGDN_FORMAT_B10G11R11_UFLOAT:
         case RGDN_FORMAT_NORMAL_SPHERICAL: return 4;
         case RGDN_FORMAT_RGBA16_SFLOAT: case RGDN_FORMAT_RGBA16_BFLOAT: case RGDN_FORMAT_RG32_SFLOAT: return 8;
-        case RGDN_FORMAT_RGBA32_SFLOAT: return 16;
+        case RGDN_FORMAT_RGBA32_SFLOAT: case RGDN_FORMAT_RGBA32_UINT: return 16;
         default: return 0;
     }
 }
@@ -157,6 +157,7 @@ FbDesc fb_desc( uint32_t fb, uint32_t storage )
         case RGDN_FB_FINAL:
         case RGDN_FB_BLOOM_INPUT:
         case RGDN_FB_BLOOM_RESULT: return { pre, false, false };
+        case RGDN_FB_RESERVOIRS: return { RGDN_FORMAT_RGBA32_UINT, true, false };
         case RGDN_FB_BLOOM_MIP1: case RGDN_FB_BLOOM_MIP2: case RGDN_FB_BLOOM_MIP3: case RGDN_FB_BLOOM_MIP4:
         case RGDN_FB_BLOOM_MIP5: case RGDN_FB_BLOOM_MIP6: case RGDN_FB_BLOOM_MIP7: case RGDN_FB_BLOOM_MIP8:
             return { pre, false, false, (int)( fb - RGDN_FB_BLOOM_MIP1 ) + 1 };
@@ -210,8 +211,10 @@ size_t stream_layout( uint32_t W, uint32_t H, uint32_t storage, PlaneSlot* plane
 {
     const uint32_t GW = std::max( 1u, ( W + 1 ) / 3 ), GH = std::max( 1u, ( H + 1 ) / 3 );
     size_t off = 0;
-    // tonemapping state, histogram bin table, geometry records of the default path (2 slots)
+    // tonemapping state, re-shade scene, histogram bin table, geometry records of the default
+    // path (2 slots)
     off += align_up( sizeof( Tonemapping ) );
+    off += align_up( sizeof( rgdn_reshade_scene ) );
     off += align_up( 65536 );
     off += 2 * align_up( (size_t)W * H * 16 );
     for( uint32_t fb = 0; fb < RGDN_FB_COUNT; fb++ )
@@ -297,6 +300,7 @@ void fill_args( rgdn_stream* s, uint32_t fi, const rgdn_frame_params* p, FrameAr
     u.debugFlags        = p->debugShowFlags;
     u.niter             = p->atrousIterations == 0 ? 4u : p->atrousIterations;
     u.flags             = p->flags;
+    u.frameId           = p->frameId;
 
     const uint32_t pf = fi ^ 1u;
 #define CUR( fb ) ( (void*)plane_ptr_mut( s, fb, fi ) )
@@ -319,6 +323,9 @@ void fill_args( rgdn_stream* s, uint32_t fi, const rgdn_frame_params* p, FrameAr
     a.throughput     = (const ushort4*)CUR( RGDN_FB_THROUGHPUT );
     a.gradInputsPrev = (const uint32_t*)PRV( RGDN_FB_GRADIENT_INPUTS );
     a.reshaded       = (const float2*)CUR( RGDN_FB_GRADIENT_RESHADED );
+    a.rs             = s->rsSet ? s->rsDev : nullptr;
+    a.reservoirsPrev = (const uint4*)PRV( RGDN_FB_RESERVOIRS );
+    a.mrPrev         = (const uint16_t*)PRV( RGDN_FB_METALLIC_ROUGHNESS );
     a.preFinal       = CUR( RGDN_FB_PRE_FINAL );
     a.histInput      = (uint16_t*)CUR( RGDN_FB_HISTOGRAM_INPUT );
     a.histLen        = CUR( RGDN_FB_ACCUM_HISTORY_LENGTH );
@@ -836,8 +843,9 @@ static rgdn_status stream_alloc( rgdn_stream* s, uint32_t W, uint32_t H )
     s->GH = std::max( 1u, ( H + 1 ) / 3 );
     stream_layout( W, H, s->storage, s->planes, (uint8_t*)block );
     s->tm     = (Tonemapping*)block;
-    s->binLut = (uint8_t*)block + align_up( sizeof( Tonemapping ) );
-    s->geom[ 0 ] = (float4*)( (uint8_t*)block + align_up( sizeof( Tonemapping ) ) + align_up( 65536 ) );
+    s->rsDev  = (rgdn_reshade_scene*)( (uint8_t*)block + align_up( sizeof( Tonemapping ) ) );
+    s->binLut = (uint8_t*)s->rsDev + align_up( sizeof( rgdn_reshade_scene ) );
+    s->geom[ 0 ] = (float4*)( s->binLut + align_up( 65536 ) );
     s->geom[ 1 ] = (float4*)( (uint8_t*)s->geom[ 0 ] + align_up( (size_t)W * H * 16 ) );
     s->geomValid[ 0 ] = s->geomValid[ 1 ] = false;
     s->tmaps.clear();
@@ -943,6 +951,7 @@ rgdn_status rgdn_stream_bind_framebuffer( rgdn_stream* s, uint32_t fb, uint32_t 
 {
     if( !valid_stream( s ) ) return RGDN_WRONG_INSTANCE;
     const bool producerPlane = fb <= RGDN_FB_GRADIENT_RESHADED || fb == RGDN_FB_SCREEN_EMIS_RT || fb == RGDN_FB_SCATTERING ||
+                               fb == RGDN_FB_RESERVOIRS ||
                                fb == RGDN_FB_DEPTH_NDC || fb == RGDN_FB_SCATTER_VOLUME;
     if( !producerPlane || frameIndex > 1 || ( (uintptr_t)devicePtr & 15u ) ) return RGDN_WRONG_FUNCTION_ARGUMENT;
     PlaneSlot& p    = s->planes[ fb ];
@@ -1188,6 +1197,24 @@ rgdn_status rgdn_denoise_stage( rgdn_stream* s, uint32_t stage, uint32_t iterati
     fill_args( s, frameIndex, p, a );
     if( def ) return launch_default_stage( s, a, frameIndex, p, (int)stage, (int)iteration, (cudaStream_t)cs );
     return launch( s, a, (int)stage, (int)iteration, (cudaStream_t)cs );
+}
+
+rgdn_status rgdn_stream_set_reshade_scene( rgdn_stream* s, const rgdn_reshade_scene* scene )
+{
+    if( !valid_stream( s ) ) return RGDN_WRONG_INSTANCE;
+    if( !scene )
+    {
+        s->rsSet = false;
+        return RGDN_SUCCESS;
+    }
+    if( ( scene->lightCount && !scene->lights ) || ( scene->prevLightCount && !scene->prevToCur ) ||
+        ( scene->occluderCount && !scene->occluders ) )
+        return RGDN_WRONG_FUNCTION_ARGUMENT;
+    cudaSetDevice( s->ctx->device );
+    // a synchronous copy: frames already enqueued must not be in flight on another stream
+    if( cudaMemcpy( s->rsDev, scene, sizeof( *scene ), cudaMemcpyHostToDevice ) != cudaSuccess ) return RGDN_DEVICE_ERROR;
+    s->rsSet = true;
+    return RGDN_SUCCESS;
 }
 
 rgdn_status rgdn_stream_set_timing( rgdn_stream* s, uint32_t enable )

@@ -52,6 +52,8 @@ struct rgdn_stream
     PlaneSlot              planes[ RGDN_FB_COUNT ];
     rgdn::Tonemapping*     tm     = nullptr;
     uint8_t*               binLut = nullptr;
+    rgdn_reshade_scene*    rsDev  = nullptr;   // device copy of the re-shade scene (stream block)
+    bool                   rsSet  = false;
     float4*                geom[ 2 ] = { nullptr, nullptr };
     bool                   geomValid[ 2 ] = { false, false };   // slot holds its frame's record
     float                  lutMin = NAN, lutMax = NAN;

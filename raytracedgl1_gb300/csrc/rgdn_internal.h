@@ -49,6 +49,7 @@ struct Uniform
     uint32_t debugFlags;
     uint32_t niter;
     uint32_t flags;
+    uint32_t frameId;        // GlobalUniform::frameId (re-shading seeds)
 };
 
 // Device addresses of every plane the kernels touch, resolved for one frameIndex
@@ -76,6 +77,10 @@ struct alignas( 16 ) FrameArgs
     const ushort4*  throughput;      // rgba16f
     const uint32_t* gradInputsPrev;  // rg16f
     const float2*   reshaded;        // rg32f
+    // gradient re-shading on the device (null: `reshaded` is the producer's image)
+    const rgdn_reshade_scene* rs;
+    const uint4*              reservoirsPrev;   // RGBA32_UINT, previous slot
+    const uint16_t*           mrPrev;           // metallic-roughness, previous slot
     // outputs
     void*     preFinal;
     uint16_t* histInput;             // r16f, regular layout

@@ -215,6 +215,13 @@ template<> struct Sto< MODE_REF >
         ushort4 h = static_cast< const ushort4* >( p )[ i ];
         return make_float4( h2f( h.x ), h2f( h.y ), h2f( h.z ), h2f( h.w ) );
     }
+    // the same values through read-only global loads (ld.global.nc: free to move past shared stores)
+    __device__ static float3 ld3_g( const void* p, size_t i ) { return e5( __ldg( static_cast< const uint32_t* >( p ) + i ) ); }
+    __device__ static float4 ldcv_g( const void* p, const float*, size_t i )
+    {
+        const ushort4 h = __ldg( static_cast< const ushort4* >( p ) + i );
+        return make_float4( h2f( h.x ), h2f( h.y ), h2f( h.z ), h2f( h.w ) );
+    }
     __device__ static void stcv( void* p, float*, size_t i, float3 c, float var )
     {
         static_cast< ushort4* >( p )[ i ] = make_ushort4( f32_to_f16( c.x ), f32_to_f16( c.y ), f32_to_f16( c.z ), f32_to_f16( var ) );
@@ -251,6 +258,8 @@ template<> struct Sto< MODE_F32 >
     __device__ static void   st3( void* p, size_t i, float3 v ) { static_cast< float4* >( p )[ i ] = make_float4( v.x, v.y, v.z, 0.0f ); }
     __device__ static float4 ldcv( const void* p, const float*, size_t i ) { return static_cast< const float4* >( p )[ i ]; }
     __device__ static void   stcv( void* p, float*, size_t i, float3 c, float var ) { static_cast< float4* >( p )[ i ] = make_float4( c.x, c.y, c.z, var ); }
+    __device__ static float3 ld3_g( const void* p, size_t i ) { const float4 v = __ldg( static_cast< const float4* >( p ) + i ); return f3( v.x, v.y, v.z ); }
+    __device__ static float4 ldcv_g( const void* p, const float*, size_t i ) { return __ldg( static_cast< const float4* >( p ) + i ); }
     __device__ static float2 ld2( const void* p, size_t i ) { return static_cast< const float2* >( p )[ i ]; }
     __device__ static void   st2( void* p, size_t i, float2 v ) { static_cast< float2* >( p )[ i ] = v; }
     __device__ static float4 ld4( const void* p, size_t i ) { return static_cast< const float4* >( p )[ i ]; }
@@ -269,6 +278,16 @@ template< bool BF > struct Sto16
     __device__ static uint16_t pk( float f ) { return BF ? f32_to_bf16( f ) : f32_to_f16( f ); }
     __device__ static float3 ld3( const void* p, size_t i ) { ushort4 h = static_cast< const ushort4* >( p )[ i ]; return f3( cv( h.x ), cv( h.y ), cv( h.z ) ); }
     __device__ static void   st3( void* p, size_t i, float3 v ) { static_cast< ushort4* >( p )[ i ] = make_ushort4( pk( v.x ), pk( v.y ), pk( v.z ), 0 ); }
+    __device__ static float3 ld3_g( const void* p, size_t i )
+    {
+        const ushort4 h = __ldg( static_cast< const ushort4* >( p ) + i );
+        return f3( cv( h.x ), cv( h.y ), cv( h.z ) );
+    }
+    __device__ static float4 ldcv_g( const void* p, const float* var, size_t i )
+    {
+        const ushort4 h = __ldg( static_cast< const ushort4* >( p ) + i );
+        return make_float4( cv( h.x ), cv( h.y ), cv( h.z ), __ldg( var + i ) );
+    }
     __device__ static float4 ldcv( const void* p, const float* var, size_t i )
     {
         ushort4 h = static_cast< const ushort4* >( p )[ i ];
@@ -401,6 +420,178 @@ __device__ __forceinline__ float4 ld_rgba8t( const Uniform& u, const uint32_t* p
     return ( x >= 0 && y >= 0 && x < u.GW && y < u.GH ) ? unpack_rgba8_t( p[ y * u.GW + x ], u8 ) : make_float4( 0, 0, 0, 0 );
 }
 
+// murmurHash33 (Random.h:280-287), the published MurmurHash2 mixing on three lanes
+__device__ __forceinline__ uint3 murmur_hash33( uint3 src )
+{
+    const uint32_t M = 0x5bd1e995u;
+    uint3          h = make_uint3( 1190494759u, 2147483647u, 3559788179u );
+    src              = make_uint3( src.x * M, src.y * M, src.z * M );
+    src              = make_uint3( src.x ^ ( src.x >> 24 ), src.y ^ ( src.y >> 24 ), src.z ^ ( src.z >> 24 ) );
+    src              = make_uint3( src.x * M, src.y * M, src.z * M );
+    auto mulx        = [ & ]( uint32_t k ) {
+        h = make_uint3( h.x * M, h.y * M, h.z * M );
+        h = make_uint3( h.x ^ k, h.y ^ k, h.z ^ k );
+    };
+    mulx( src.x );
+    mulx( src.y );
+    mulx( src.z );
+    h = make_uint3( h.x ^ ( h.x >> 13 ), h.y ^ ( h.y >> 13 ), h.z ^ ( h.z >> 13 ) );
+    h = make_uint3( h.x * M, h.y * M, h.z * M );
+    return make_uint3( h.x ^ ( h.x >> 15 ), h.y ^ ( h.y >> 15 ), h.z ^ ( h.z >> 15 ) );
+}
+// Chris Wellons' lowbias32 (Random.h:243-251)
+__device__ __forceinline__ uint32_t wellons_lowbias32( uint32_t x )
+{
+    x ^= x >> 16;
+    x *= 0x7feb352du;
+    x ^= x >> 15;
+    x *= 0x846ca68bu;
+    x ^= x >> 16;
+    return x;
+}
+// getRandomSeed + packRandomSeed (Random.h:202-208, 289-300): 128 blue-noise layers of 128x128
+__device__ __forceinline__ uint32_t random_seed( int px, int py, uint32_t frame )
+{
+    const uint3 h = murmur_hash33( make_uint3( (uint32_t)px, (uint32_t)py, frame ) );
+    return ( ( h.z % 128u ) << 14 ) | ( ( h.y % 128u ) << 7 ) | ( h.x % 128u );
+}
+
+// ------------------------------------------------------------------------------------------
+// Gradient re-shading (RtGradients.rgen:107-136): the previous frame's surface at a gradient
+// sample, lit again by this frame's lights with the previous frame's reservoir and random seed.
+// The light sample, the BRDF and the sample weight follow the shaders in IEEE binary32 and in
+// their expression order; the shadow ray runs against the analytic occluders.
+// ------------------------------------------------------------------------------------------
+constexpr float kPi = 3.14159265358979323846f;   // M_PI (Utils.h:26)
+
+// Utils.h:69-72, 142-146, Light.h:140-151
+__device__ __forceinline__ float safe_positive_rcp( float f ) { return f <= 0.0f ? 0.0f : 1.0f / f; }
+__device__ __forceinline__ float3 safe_normalize( float3 v )
+{
+    const float len = sqrtf( dot3( v, v ) );
+    return len > 0.001f ? divs( v, len ) : f3( 0.0f, 1.0f, 0.0f );
+}
+__device__ __forceinline__ float safe_solid_angle( float a ) { return a > 0.0f && !isnan( a ) && !isinf( a ) ? gclamp( a, 0.0f, 4.0f * kPi ) : 0.0f; }
+__device__ __forceinline__ float solid_angle_sphere( float radius, float dist )
+{
+    const float sinTheta = radius / fmaxf( radius, dist );
+    const float cosTheta = sqrtf( 1.0f - sinTheta * sinTheta );
+    return safe_solid_angle( 2.0f * kPi * ( 1.0f - cosTheta ) );
+}
+// sampleOrientedHemisphere (Random.h:175-201), the direction only
+__device__ __forceinline__ float3 oriented_hemisphere( float3 n, float u1, float u2 )
+{
+    float       a   = 1.0f - 2.0f * u1;
+    float       b   = sqrtf( 1.0f - a * a );
+    const float phi = 2.0f * kPi * u2;
+    a               = a * 0.98f;
+    b               = b * 0.98f;
+    return normalize3( f3( n.x + b * cosf( phi ), n.y + b * sinf( phi ), n.z + a ) );
+}
+// evalBRDFSmithGGX (BRDF.h:116-146) with D_GGX (BRDF.h:87-101) and getFresnelSchlick (BRDF.h:73-76)
+__device__ __forceinline__ float3 brdf_smith_ggx( float3 n, float3 v, float3 l, float alpha, float3 specColor )
+{
+    alpha          = fmaxf( alpha, 0.005f );
+    const float nl = fmaxf( dot3( n, l ), 0.0f );
+    if( nl <= 0.0f ) return f3( 0.0f, 0.0f, 0.0f );
+    const float  fr = powf( 1.0f - fmaxf( nl, 0.0f ), 5.0f );
+    const float3 F  = f3( specColor.x + ( 1.0f - specColor.x ) * fr, specColor.y + ( 1.0f - specColor.y ) * fr,
+                          specColor.z + ( 1.0f - specColor.z ) * fr );
+    const float3 h       = normalize3( add( v, l ) );
+    const float  alphaSq = alpha * alpha;
+    const float  nm      = fmaxf( 0.0f, dot3( n, h ) );
+    const float  dd      = nm * nm * ( alphaSq - 1.0f ) + 1.0f;
+    const float  D       = alphaSq / kPi / ( dd * dd );
+    const float  nv      = fmaxf( dot3( n, v ), 0.0f );
+    const float  G2      = 0.5f / gmix( 2.0f * nl * nv, nl + nv, alpha );
+    return mul( F, G2 * D );
+}
+// traceShadowRay (RaygenCommon.h:322-348) against the occluders: tMin 0.001, tMax the distance
+// to the light point minus SHADOW_RAY_EPS (0.01)
+__device__ __forceinline__ bool shadowed( const rgdn_reshade_scene& sc, float3 start, float3 end )
+{
+    float3      l           = sub( end, start );
+    const float maxDistance = sqrtf( dot3( l, l ) );
+    l                       = divs( l, maxDistance );
+    const float tmin = 0.001f, tmax = maxDistance - 0.01f;
+    for( uint32_t k = 0; k < sc.occluderCount; k++ )
+    {
+        const rgdn_occluder o = sc.occluders[ k ];
+        if( o.type == RGDN_OCCLUDER_SPHERE )
+        {
+            const float3 oc   = sub( start, f3( o.data[ 0 ], o.data[ 1 ], o.data[ 2 ] ) );
+            const float  b    = dot3( oc, l );
+            const float  c    = dot3( oc, oc ) - o.data[ 3 ] * o.data[ 3 ];
+            const float  disc = b * b - c;
+            if( disc <= 0.0f ) continue;
+            const float sq = sqrtf( disc );
+            const float t0 = -b - sq, t1 = -b + sq;
+            if( ( t0 >= tmin && t0 <= tmax ) || ( t1 >= tmin && t1 <= tmax ) ) return true;
+        }
+        else if( o.type == RGDN_OCCLUDER_RECT )
+        {
+            const int   ax = (int)o.data[ 0 ];
+            const float so = ax == 0 ? start.x : ax == 1 ? start.y : start.z;
+            const float dl = ax == 0 ? l.x : ax == 1 ? l.y : l.z;
+            if( dl == 0.0f ) continue;
+            const float t = ( o.data[ 1 ] - so ) / dl;
+            if( !( t >= tmin && t <= tmax ) ) continue;
+            const float3 q  = add( start, mul( l, t ) );
+            const float  u0 = ax == 0 ? q.y : q.x, u1 = ax == 2 ? q.y : q.z;
+            if( u0 >= o.data[ 2 ] && u0 <= o.data[ 3 ] && u1 >= o.data[ 4 ] && u1 <= o.data[ 5 ] ) return true;
+        }
+    }
+    return false;
+}
+// forwardProjectedLuminance of the previous frame's pixel pp (checkerboard layout)
+__device__ __forceinline__ float2 reshade_px( const FrameArgs& a, const int2 pp, const float* u8 )
+{
+    const Uniform&            u  = a.u;
+    const rgdn_reshade_scene& sc = *a.rs;
+    const int                 pi = pp.y * u.W + pp.x;
+    const uint4               rv = a.reservoirsPrev[ pi ];
+    const uint32_t            selectedPrev = rv.x & 65535u, Mres = ( rv.x >> 16 ) & 65535u;
+    // isReservoirValid, then lightSources_Index_PrevToCur
+    if( selectedPrev == 32767u || selectedPrev >= sc.prevLightCount ) return make_float2( 0.0f, 0.0f );
+    const uint32_t sel = sc.prevToCur[ selectedPrev ];
+    if( sel == 0xFFFFFFFFu || sel >= sc.lightCount ) return make_float2( 0.0f, 0.0f );
+    // fetchGbufferSurface_NoAlbedoViewDir_Prev (Surface.inl:72-90) + the toViewerDir fix-up
+    const float4   sp4  = a.surfPosPrev[ pi ];
+    const float3   pos  = f3( sp4.x, sp4.y, sp4.z );
+    const uint16_t mrb  = a.mrPrev[ pi ];
+    const float    metallic = u8[ mrb & 0xFFu ], roughness = u8[ mrb >> 8 ];
+    const float    spc  = 0.04f * ( 1.0f - metallic ) + 1.0f * metallic;   // getSpecularColor(1, metallic)
+    const float3   n    = decode_normal( a, a.normalPrev[ pi ] );
+    const float3   v    = normalize3( sub( f3( u.camPosPrev[ 0 ], u.camPosPrev[ 1 ], u.camPosPrev[ 2 ] ), pos ) );
+    // getRandomSeed(prevShadingPix, frameId - 1), getLightPointRnd (RaygenCommon.h:624-627)
+    const uint32_t seed = random_seed( pp.x, pp.y, u.frameId - 1u );
+    const uint32_t rnd  = wellons_lowbias32( seed + 20u );   // RANDOM_SALT_LIGHT_POINT
+    const float    r1   = (float)( rnd & 0xFFFFu ) / 65535.0f * 0.99f;
+    const float    r2   = (float)( ( rnd & 0xFFFF0000u ) >> 16 ) / 65535.0f * 0.99f;
+    // sampleSphereLight (Light.h:244-258)
+    const rgdn_sphere_light L  = sc.lights[ sel ];
+    const float3            c  = f3( L.center[ 0 ], L.center[ 1 ], L.center[ 2 ] );
+    float3                  tc = sub( c, pos );
+    const float             tl = sqrtf( dot3( tc, tc ) );
+    tc                         = divs( tc, tl );
+    const float3 ln            = oriented_hemisphere( f3( -tc.x, -tc.y, -tc.z ), r1, r2 );
+    const float3 lpos          = add( c, mul( ln, L.radius ) );
+    const float  dw            = solid_angle_sphere( L.radius, tl );
+    const float3 col           = f3( L.color[ 0 ], L.color[ 1 ], L.color[ 2 ] );
+    // shade (RaygenCommon.h:364-380) with calcSelectedSampleWeight (Reservoir.h:47-50)
+    const float3 l  = safe_normalize( sub( lpos, pos ) );
+    const float  nl = dot3( n, l );
+    if( nl <= 0.0f ) return make_float2( 0.0f, 0.0f );
+    const float  w    = safe_positive_rcp( __uint_as_float( rv.y ) ) * ( __uint_as_float( rv.z ) / (float)max( 1u, Mres ) );
+    const float3 base = mul( col, dw * nl );
+    float3       dif  = mul( mul( base, 1.0f / kPi ), w );
+    float3       spe  = mul( mul( base, brdf_smith_ggx( n, v, l, roughness, f3( spc, spc, spc ) ) ), w );
+    if( luminance( add( dif, spe ) ) <= 0.0f ) return make_float2( 0.0f, 0.0f );
+    // traceVisibility (RaygenCommon.h:350-359): from the surface moved towards the viewer
+    if( shadowed( sc, add( pos, mul( v, 0.01f ) ), lpos ) ) return make_float2( 0.0f, 0.0f );
+    return make_float2( luminance( dif ), luminance( spe ) );
+}
+
 template< int M >
 __device__ __forceinline__ void gradient_sample_px( const FrameArgs& a, uint32_t* dst, const int gx, const int gy, const float* u8 )
 {
@@ -467,8 +658,9 @@ __device__ __forceinline__ void gradient_sample_px( const FrameArgs& a, uint32_t
     }
     // in the render area, so inside the image
     const int    pi  = prevShadingPix.y * u.W + prevShadingPix.x;
-    // the re-shaded luminance is a boundary input (RtGradients.rgen:107-136)
-    const float2 fpl = a.reshaded[ pi ];
+    // the re-shaded luminance: computed here from the lights (RtGradients.rgen:107-136), or the
+    // producer's image
+    const float2 fpl = a.rs ? reshade_px( a, prevShadingPix, u8 ) : a.reshaded[ pi ];
     float g0, g1, g2;
     {
         const float gs = fpl.x - prevLum.x;
@@ -1955,10 +2147,11 @@ __device__ __forceinline__ void atrous_stage_texel( const FrameArgs& a, const At
     if( inside( a.u, gx, gy ) )
     {
         const int    q  = gy * a.u.W + gx;
-        const Geo    g  = geo_load( a.geom, q );
-        const float3 sp = S::ld3( io.specSrc, (size_t)q );
-        const float3 in = S::ld3( io.indirSrc, (size_t)q );
-        vc = S::ldcv( io.diffSrc, io.varSrc, (size_t)q );
+        const float4 gr = __ldg( a.geom + q );
+        const Geo    g  = { make_float3( gr.x, gr.y, gr.z ), __float_as_uint( gr.w ) };
+        const float3 sp = S::ld3_g( io.specSrc, (size_t)q );
+        const float3 in = S::ld3_g( io.indirSrc, (size_t)q );
+        vc = S::ldcv_g( io.diffSrc, io.varSrc, (size_t)q );
         vg = make_float4( g.n.x, g.n.y, g.n.z, geo_depth( g ) );
         vs = make_float4( sp.x, sp.y, sp.z, Wm< true >::lum( f3( vc.x, vc.y, vc.z ) ) );
         vi = make_float4( in.x, in.y, in.z, u8[ geo_rough8( g ) ] );
@@ -3401,42 +3594,6 @@ template< int M > __global__ void __launch_bounds__( 128 ) k_volume_process( ush
 #pragma unroll
         for( int j = 0; j < VP; j++ ) cur[ j ] = nxt[ j ];
     }
-}
-
-// murmurHash33 (Random.h:280-287), the published MurmurHash2 mixing on three lanes
-__device__ __forceinline__ uint3 murmur_hash33( uint3 src )
-{
-    const uint32_t M = 0x5bd1e995u;
-    uint3          h = make_uint3( 1190494759u, 2147483647u, 3559788179u );
-    src              = make_uint3( src.x * M, src.y * M, src.z * M );
-    src              = make_uint3( src.x ^ ( src.x >> 24 ), src.y ^ ( src.y >> 24 ), src.z ^ ( src.z >> 24 ) );
-    src              = make_uint3( src.x * M, src.y * M, src.z * M );
-    auto mulx        = [ & ]( uint32_t k ) {
-        h = make_uint3( h.x * M, h.y * M, h.z * M );
-        h = make_uint3( h.x ^ k, h.y ^ k, h.z ^ k );
-    };
-    mulx( src.x );
-    mulx( src.y );
-    mulx( src.z );
-    h = make_uint3( h.x ^ ( h.x >> 13 ), h.y ^ ( h.y >> 13 ), h.z ^ ( h.z >> 13 ) );
-    h = make_uint3( h.x * M, h.y * M, h.z * M );
-    return make_uint3( h.x ^ ( h.x >> 15 ), h.y ^ ( h.y >> 15 ), h.z ^ ( h.z >> 15 ) );
-}
-// Chris Wellons' lowbias32 (Random.h:243-251)
-__device__ __forceinline__ uint32_t wellons_lowbias32( uint32_t x )
-{
-    x ^= x >> 16;
-    x *= 0x7feb352du;
-    x ^= x >> 15;
-    x *= 0x846ca68bu;
-    x ^= x >> 16;
-    return x;
-}
-// getRandomSeed + packRandomSeed (Random.h:202-208, 289-300): 128 blue-noise layers of 128x128
-__device__ __forceinline__ uint32_t random_seed( int px, int py, uint32_t frame )
-{
-    const uint3 h = murmur_hash33( make_uint3( (uint32_t)px, (uint32_t)py, frame ) );
-    return ( ( h.z % 128u ) << 14 ) | ( ( h.y % 128u ) << 7 ) | ( h.x % 128u );
 }
 
 // an index from a floor()ed coordinate: NaN to 0, magnitudes beyond 2^30 saturated, so that

@@ -21,6 +21,7 @@
 #include <cmath>
 #include <cstdint>
 #include <cstring>
+#include <limits>
 #include <thread>
 #include <vector>
 
@@ -111,6 +112,8 @@ typedef struct rgdn_scene_desc
     float    lightFlickerGain;
     uint32_t atrousIterations;
     uint32_t antiFirefly;
+    uint32_t reshadeLights;    // 1: GradientInputs from a sphere light shaded as the reference's direct
+                               // pass does (so the device re-shading reproduces them), and reservoirs
 } rgdn_scene_desc;
 
 void rgdn_scene_desc_default( rgdn_scene_desc* d )
@@ -128,6 +131,7 @@ void rgdn_scene_desc_default( rgdn_scene_desc* d )
     d->lightFlickerGain = 2.0f;
     d->atrousIterations = 4;
     d->antiFirefly      = 1;
+    d->reshadeLights    = 0;
 }
 
 struct rgdn_scene
@@ -271,6 +275,27 @@ struct Sample
 };
 
 const D3 kLightPos = { 3.0, 5.0, 2.0 };
+// the sphere light of the re-shading scenes: kLightPos, radius 0.25, white of this intensity
+// (times the frame's light gain): dw * color / pi matches the point light's 30 / d^2 at range
+constexpr double kLightRadius = 0.25, kLightColor = 480.0;
+
+// Random.h hashes (the host twins of the kernels' getRandomSeed / wellonsLowBias32)
+uint32_t wellons( uint32_t x )
+{
+    x ^= x >> 16; x *= 0x7feb352du; x ^= x >> 15; x *= 0x846ca68bu; x ^= x >> 16;
+    return x;
+}
+uint32_t seed_of( int px, int py, uint32_t frame )
+{
+    const uint32_t M = 0x5bd1e995u;
+    uint32_t       src[ 3 ] = { (uint32_t)px, (uint32_t)py, frame }, h[ 3 ] = { 1190494759u, 2147483647u, 3559788179u };
+    for( auto& v : src ) { v *= M; v ^= v >> 24; v *= M; }
+    for( int k = 0; k < 3; k++ )
+        for( auto& v : h ) { v *= M; v ^= src[ k ]; }
+    for( auto& v : h ) { v ^= v >> 13; v *= M; v ^= v >> 15; }
+    return ( ( h[ 2 ] % 128u ) << 14 ) | ( ( h[ 1 ] % 128u ) << 7 ) | ( h[ 0 ] % 128u );
+}
+
 
 // noisy demodulated radiance of a surface point at frame `frame` for checkerboard pixel `pix`
 Sample shade( const rgdn_scene* s, const Hit& h, D3 viewDir, int frame, uint64_t pixId, double gain )
@@ -303,6 +328,54 @@ Sample shade( const rgdn_scene* s, const Hit& h, D3 viewDir, int frame, uint64_t
         *dst[ sig ] = { c[ 0 ], c[ 1 ], c[ 2 ] };
     }
     return out;
+}
+
+// The direct-light sample of RtRaygenDirect for checkerboard pixel (cx, cy) of `frame` at the
+// surface (p, n) seen from `eye`: the sphere light's point drawn with the pixel's seed
+// (getLightPointRnd), shade() with the Lambertian and Smith-GGX terms, a sample weight of 1
+// (the reservoirs written say so) and the shadow ray against the scene; luminances (diffuse,
+// specular). In double precision, on the quantised metallic / roughness the G-buffer stores.
+void light_sample( const SceneAtFrame& sc, D3 p, D3 n, D3 eye, double metallic, double roughness, int cx, int cy, uint32_t frame,
+                   double gain, double out[ 2 ] )
+{
+    out[ 0 ] = out[ 1 ] = 0.0;
+    const double PI  = 3.14159265358979323846;
+    const uint32_t rnd = wellons( seed_of( cx, cy, frame ) + 20u );
+    const double r1 = (double)( rnd & 0xFFFFu ) / 65535.0 * 0.99, r2 = (double)( rnd >> 16 ) / 65535.0 * 0.99;
+    D3           tc = kLightPos - p;
+    const double tl = len( tc );
+    tc              = tc * ( 1.0 / tl );
+    double a = 1.0 - 2.0 * r1, b = std::sqrt( 1.0 - a * a );
+    const double phi = 2.0 * PI * r2;
+    a *= 0.98; b *= 0.98;
+    const D3     ln   = nrm( D3{ -tc.x + b * std::cos( phi ), -tc.y + b * std::sin( phi ), -tc.z + a } );
+    const D3     lpos = kLightPos + ln * kLightRadius;
+    const double sinT = kLightRadius / std::max( kLightRadius, tl ), cosT = std::sqrt( 1.0 - sinT * sinT );
+    const double dw   = 2.0 * PI * ( 1.0 - cosT );
+    const D3     l    = nrm( lpos - p );
+    const double nl   = dot( n, l );
+    if( nl <= 0.0 ) return;
+    const D3     v     = nrm( eye - p );
+    const double col   = kLightColor * gain;
+    const double dif   = dw * nl * col / PI;
+    const double alpha = std::max( roughness, 0.005 );
+    const double spc   = 0.04 * ( 1.0 - metallic ) + metallic;
+    const double F     = spc + ( 1.0 - spc ) * std::pow( 1.0 - nl, 5.0 );
+    const D3     h     = nrm( v + l );
+    const double nm = std::max( 0.0, dot( n, h ) ), dd = nm * nm * ( alpha * alpha - 1.0 ) + 1.0;
+    const double D  = alpha * alpha / PI / ( dd * dd );
+    const double nv = std::max( dot( n, v ), 0.0 );
+    const double G2 = 0.5 / ( 2.0 * nl * nv * ( 1.0 - alpha ) + ( nl + nv ) * alpha );
+    const double spe = dw * nl * col * F * G2 * D;
+    // shadow ray from the surface moved towards the viewer, tMin 0.001, up to 0.01 short of the light
+    const D3     st = p + v * 0.01;
+    D3           dl = lpos - st;
+    const double md = len( dl );
+    dl              = dl * ( 1.0 / md );
+    const Hit hs    = trace( sc, st, dl );
+    if( hs.hit && hs.t >= 0.001 && hs.t <= md - 0.01 ) return;
+    out[ 0 ] = lum( D3{ dif, dif, dif } );
+    out[ 1 ] = lum( D3{ spe, spe, spe } );
 }
 
 template< class F > void parallel_rows( int h, int nthreads, F&& fn )
@@ -349,6 +422,7 @@ typedef struct rgdn_scene_frame
     uint16_t* throughput;      // rgba16f
     uint16_t* gradientInputs;  // rg16f
     float*    gradientReshaded;// rg32f, indexed by previous-frame pixel
+    uint32_t* reservoirs;      // RGDN_FB_RESERVOIRS, uint32 x4 (written when reshadeLights)
 } rgdn_scene_frame;
 
 // Generates frame `frame` into `out` and fills `params` (may be NULL).
@@ -393,6 +467,7 @@ int rgdn_scene_generate( const rgdn_scene* s, uint32_t frame, rgdn_scene_frame* 
         params->debugShowFlags         = 0;
         params->atrousIterations       = s->d.atrousIterations;
         params->flags                  = 0;
+        params->frameId                = frame;
     }
 
     // primary ray through regular pixel (rx + ox, ry + oy), world space
@@ -451,6 +526,11 @@ int rgdn_scene_generate( const rgdn_scene* s, uint32_t frame, rgdn_scene_frame* 
                     out->throughput[ idx * 4 + 3 ] = 0;
                 }
                 if( out->gradientInputs ) { out->gradientInputs[ idx * 2 ] = 0; out->gradientInputs[ idx * 2 + 1 ] = 0; }
+                if( out->reservoirs )
+                {
+                    out->reservoirs[ idx * 4 + 0 ] = 32767u;   // LIGHT_INDEX_NONE, M 0
+                    out->reservoirs[ idx * 4 + 1 ] = out->reservoirs[ idx * 4 + 2 ] = out->reservoirs[ idx * 4 + 3 ] = 0u;
+                }
             }
             else
             {
@@ -517,8 +597,23 @@ int rgdn_scene_generate( const rgdn_scene* s, uint32_t frame, rgdn_scene_frame* 
                 }
                 if( out->gradientInputs )
                 {
-                    out->gradientInputs[ idx * 2 + 0 ] = rgdn::f32_to_f16( (float)lum( smp.direct ) );
-                    out->gradientInputs[ idx * 2 + 1 ] = rgdn::f32_to_f16( (float)lum( smp.spec ) );
+                    double gl[ 2 ] = { lum( smp.direct ), lum( smp.spec ) };
+                    if( s->d.reshadeLights )
+                    {
+                        // the same quantised metallic / roughness the G-buffer holds
+                        const double metal = (double)rgdn::f32_to_unorm8( (float)m.metallic ) / 255.0;
+                        const double rough = (double)rgdn::f32_to_unorm8( (float)m.roughness ) / 255.0;
+                        light_sample( sc, h.p, h.n, eye, metal, rough, cx, y, frame, gainCur, gl );
+                    }
+                    out->gradientInputs[ idx * 2 + 0 ] = rgdn::f32_to_f16( (float)gl[ 0 ] );
+                    out->gradientInputs[ idx * 2 + 1 ] = rgdn::f32_to_f16( (float)gl[ 1 ] );
+                }
+                if( out->reservoirs )
+                {
+                    // light 0 chosen with a weight of 1: targetPdf 1, weightSum 1, M 1
+                    out->reservoirs[ idx * 4 + 0 ] = ( 1u << 16 ) | 0u;
+                    out->reservoirs[ idx * 4 + 1 ] = out->reservoirs[ idx * 4 + 2 ] = 0x3F800000u;
+                    out->reservoirs[ idx * 4 + 3 ] = 0u;
                 }
             }
 
@@ -546,6 +641,48 @@ int rgdn_scene_generate( const rgdn_scene* s, uint32_t frame, rgdn_scene_frame* 
         }
     } );
     return RGDN_SUCCESS;
+}
+
+// The re-shading scene of `frame`: its sphere light (index 0, the previous frame's light 0 maps
+// to it) and the analytic occluders (the five spheres at this frame, the ground plane, the back
+// wall). Returns the counts; NULL outputs are skipped.
+void rgdn_scene_reshade( const rgdn_scene* s, uint32_t frame, rgdn_sphere_light* light, rgdn_occluder* occluders, uint32_t* occluderCount )
+{
+    if( !s ) return;
+    const double gain = light_gain( s, (int)frame );
+    if( light )
+    {
+        memset( light, 0, sizeof( *light ) );
+        light->center[ 0 ] = (float)kLightPos.x;
+        light->center[ 1 ] = (float)kLightPos.y;
+        light->center[ 2 ] = (float)kLightPos.z;
+        light->radius      = (float)kLightRadius;
+        light->color[ 0 ] = light->color[ 1 ] = light->color[ 2 ] = (float)( kLightColor * gain );
+    }
+    if( occluders )
+    {
+        const SceneAtFrame sc = scene_at( s, (double)frame );
+        uint32_t           k  = 0;
+        for( int i = 0; i < 5; i++, k++ )
+        {
+            occluders[ k ].type = RGDN_OCCLUDER_SPHERE;
+            occluders[ k ].data[ 0 ] = (float)sc.spheres[ i ].x;
+            occluders[ k ].data[ 1 ] = (float)sc.spheres[ i ].y;
+            occluders[ k ].data[ 2 ] = (float)sc.spheres[ i ].z;
+            occluders[ k ].data[ 3 ] = (float)sc.radii[ i ];
+            occluders[ k ].data[ 4 ] = occluders[ k ].data[ 5 ] = occluders[ k ].data[ 6 ] = 0.0f;
+        }
+        const float inf = std::numeric_limits< float >::infinity();
+        occluders[ k ].type = RGDN_OCCLUDER_RECT;   // ground y = 0
+        const float g[ 7 ] = { 1.0f, 0.0f, -inf, inf, -inf, inf, 0.0f };
+        memcpy( occluders[ k ].data, g, sizeof( g ) );
+        k++;
+        occluders[ k ].type = RGDN_OCCLUDER_RECT;   // back wall z = -8, |x| <= 12, 0 <= y <= 6
+        const float w[ 7 ] = { 2.0f, -8.0f, -12.0f, 12.0f, 0.0f, 6.0f, 0.0f };
+        memcpy( occluders[ k ].data, w, sizeof( w ) );
+        k++;
+        if( occluderCount ) *occluderCount = k;
+    }
 }
 
 }  // extern "C"

@@ -33,6 +33,7 @@ FORMAT_NUMPY = {
     12: (np.uint32, 1),  # E5B9G9R9
     13: (np.uint32, 1),  # B10G11R11
     14: (np.uint32, 1),  # NORMAL_SPHERICAL
+    15: (np.uint32, 4),  # RGBA32_UINT
 }
 
 
@@ -240,6 +241,17 @@ class Stream:
         N.check(self.lib.rgdn_stream_read_timing(self.handle, buf, cap, C.byref(n)), "rgdn_stream_read_timing")
         return {(N.KERNEL_NAMES.get(t.stage, str(t.stage)), t.iteration): (t.launches, t.totalMs)
                 for t in buf[:min(n.value, cap)]}
+
+    def set_reshade_scene(self, lights_ptr=None, light_count=0, prev_to_cur_ptr=None, prev_light_count=0,
+                          occluders_ptr=None, occluder_count=0) -> None:
+        """Gradient re-shading on the device from these device arrays (rgdn_sphere_light,
+        uint32 previous-to-current light indices, rgdn_occluder); lights_ptr None clears it, and
+        the producer's RGDN_FB_GRADIENT_RESHADED image is used again."""
+        if lights_ptr is None:
+            N.check(self.lib.rgdn_stream_set_reshade_scene(self.handle, None), "rgdn_stream_set_reshade_scene")
+            return
+        sc = N.ReshadeScene(lights_ptr, light_count, prev_to_cur_ptr, prev_light_count, occluders_ptr, occluder_count)
+        N.check(self.lib.rgdn_stream_set_reshade_scene(self.handle, C.byref(sc)), "rgdn_stream_set_reshade_scene")
 
     # --- stages --------------------------------------------------------------------------
     def stage(self, stage: int, iteration: int, frame_index: int, params: N.FrameParams,

@@ -19,7 +19,7 @@ class SceneDesc(C.Structure):
         ("fireflyMult", C.c_float), ("cameraPxPerFrame", C.c_float), ("spherePxPerFrame", C.c_float),
         ("timeDelta", C.c_float), ("ev100Min", C.c_float), ("ev100Max", C.c_float),
         ("lightFlickerFrom", C.c_float), ("lightFlickerGain", C.c_float),
-        ("atrousIterations", C.c_uint32), ("antiFirefly", C.c_uint32),
+        ("atrousIterations", C.c_uint32), ("antiFirefly", C.c_uint32), ("reshadeLights", C.c_uint32),
     ]
 
 
@@ -27,7 +27,7 @@ class SceneFrame(C.Structure):
     _fields_ = [(n, C.c_void_p) for n in (
         "albedo", "isSky", "normal", "metallicRoughness", "depthWorld", "depthGrad", "motion",
         "unfilteredDirect", "unfilteredSpecular", "unfilteredIndir", "surfacePosition",
-        "viewDirection", "throughput", "gradientInputs", "gradientReshaded")]
+        "viewDirection", "throughput", "gradientInputs", "gradientReshaded", "reservoirs")]
 
 
 # framebuffer name -> (SceneFrame field, dtype, channels)
@@ -47,6 +47,7 @@ _LAYOUT = {
     "THROUGHPUT": ("throughput", np.uint16, 4),
     "GRADIENT_INPUTS": ("gradientInputs", np.uint16, 2),
     "GRADIENT_RESHADED": ("gradientReshaded", np.float32, 2),
+    "RESERVOIRS": ("reservoirs", np.uint32, 4),
 }
 
 _lib = None
@@ -65,6 +66,8 @@ def _load():
         lib.rgdn_scene_generate.restype = C.c_int
         lib.rgdn_scene_generate.argtypes = [C.c_void_p, C.c_uint32, C.POINTER(SceneFrame),
                                             C.POINTER(N.FrameParams), C.c_int]
+        lib.rgdn_scene_reshade.argtypes = [C.c_void_p, C.c_uint32, C.POINTER(N.SphereLight),
+                                           C.POINTER(N.Occluder), C.POINTER(C.c_uint32)]
         _lib = lib
     return _lib
 
@@ -91,10 +94,15 @@ class Scene:
             self.lib.rgdn_scene_destroy(self.handle)
             self.handle = None
 
+    def planes(self) -> list:
+        """The framebuffers this scene writes: RESERVOIRS only for a re-shading scene."""
+        return [n for n in _LAYOUT if n != "RESERVOIRS" or self.desc.reshadeLights]
+
     def alloc(self, pinned=None) -> dict:
         """Host buffers for one frame. `pinned`: optional callable(nbytes) -> numpy uint8 array."""
         out = {}
-        for name, (_, dt, ch) in _LAYOUT.items():
+        for name in self.planes():
+            _, dt, ch = _LAYOUT[name]
             shape = (self.height, self.width) if ch == 1 else (self.height, self.width, ch)
             if pinned is not None:
                 nbytes = int(np.prod(shape)) * np.dtype(dt).itemsize
@@ -108,11 +116,21 @@ class Scene:
         if out is None:
             out = self.alloc()
         sf = SceneFrame()
-        for name, (field, _, _) in _LAYOUT.items():
-            setattr(sf, field, out[name].ctypes.data)
+        for name in self.planes():
+            setattr(sf, _LAYOUT[name][0], out[name].ctypes.data)
         params = N.FrameParams()
         if nthreads <= 0:
             nthreads = min(32, os.cpu_count() or 1)
         r = self.lib.rgdn_scene_generate(self.handle, frame, C.byref(sf), C.byref(params), nthreads)
         N.check(r, "rgdn_scene_generate")
         return out, params
+
+    def reshade(self, frame: int):
+        """The re-shading scene of `frame`: (lights, previous-to-current light map, occluders) as
+        ctypes arrays (one sphere light, light 0 of the previous frame mapped to it, seven
+        occluders), for rgdn_stream_set_reshade_scene (after a copy to the device) and the oracle."""
+        light = (N.SphereLight * 1)()
+        occ = (N.Occluder * 16)()
+        n = C.c_uint32()
+        self.lib.rgdn_scene_reshade(self.handle, frame, light, occ, C.byref(n))
+        return light, (C.c_uint32 * 1)(0), (N.Occluder * n.value)(*occ[:n.value])

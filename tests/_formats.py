@@ -6,6 +6,7 @@ import numpy as np
 
 F_R8U, F_RG8, F_RGBA8, F_R16F, F_RG16F, F_RGBA16F, F_RGBA16BF = 1, 2, 3, 4, 5, 6, 7
 F_R32F, F_RG32F, F_RGBA32F, F_R32U, F_E5, F_B10G11R11, F_NORMAL = 8, 9, 10, 11, 12, 13, 14
+F_RGBA32U = 15
 F_R64F, F_RG64F, F_RGBA64F = 100, 101, 102
 
 
@@ -44,7 +45,7 @@ def decode(arr: np.ndarray, fmt: int) -> np.ndarray:
         return (arr.astype(np.uint32) << 16).view(np.float32)
     if fmt in (F_RG8, F_RGBA8):
         return arr.astype(np.float32) / np.float32(255.0)
-    if fmt in (F_R8U, F_R32U, F_NORMAL):
+    if fmt in (F_R8U, F_R32U, F_NORMAL, F_RGBA32U):
         return arr.astype(np.float64)
     return arr.astype(np.float64) if arr.dtype == np.float64 else arr.astype(np.float32)
 

@@ -62,7 +62,7 @@ def stage_errors(s, o):
         c = o.plane(name, slot)
         if np.array_equal(g, c):
             continue
-        if fmt in (F.F_R8U, F.F_R32U, F.F_NORMAL):
+        if fmt in (F.F_R8U, F.F_R32U, F.F_NORMAL, F.F_RGBA32U):
             out.append((name, slot, float("inf"), 1.0, 0.0, int(np.count_nonzero(g != c))))
             continue
         gd, cd = F.decode(g, fmt), F.decode(c, fmt)

@@ -416,3 +416,92 @@ def test_random_seed_restatement():
         assert lib.orc_random_seed(x, y, f) == seed
         assert lib.orc_wellons_lowbias32(seed) == lowbias32(seed)
     assert lowbias32(0) == 0 and lib.orc_wellons_lowbias32(1) == lowbias32(1)
+
+
+def _reshade_stream(normal=(0.0, 1.0, 0.0), roughness=1.0, metallic=0.0):
+    """An oracle stream whose previous slot holds one surface point at the origin, seen from a
+    camera 5 above and 5 in front, with the reservoir of light 0 (weight 1)."""
+    from raytracedgl1_gb300 import _native as N
+    o = oracle.OracleStream(8, 4, oracle.MODE_F32)
+    prev = 0   # frame slot 1 reads slot 0 as its previous frame
+    o.plane("SURFACE_POSITION", prev)[...] = 0.0
+    o.plane("NORMAL", prev)[...] = oracle.encode_normal(*normal)
+    mr = o.plane("METALLIC_ROUGHNESS", prev)
+    mr[..., 0], mr[..., 1] = round(metallic * 255), round(roughness * 255)
+    res = o.plane("RESERVOIRS", prev)
+    res[..., 0], res[..., 1], res[..., 2], res[..., 3] = (1 << 16) | 0, 0x3F800000, 0x3F800000, 0
+    p = N.FrameParams()
+    p.minLogLuminance, p.maxLogLuminance = -3.0, 7.0
+    p.cameraPositionPrev[:] = (0.0, 5.0, 5.0, 0.0)
+    p.frameId = 7
+    return o, p
+
+
+def _light(center, radius, color):
+    from raytracedgl1_gb300 import _native as N
+    lt = (N.SphereLight * 1)()
+    lt[0].center[:] = center
+    lt[0].radius = radius
+    lt[0].color[:] = (color, color, color)
+    return lt
+
+
+def test_reshade_closed_form_and_its_zero_cases():
+    """RtGradients.rgen:107-136 re-shading (oracle restatement): a surface facing a small sphere
+    light straight above it gets the Lambertian term dw * nl * color / pi with dw the light's solid
+    angle and nl within the light's angular radius of 1; the sample is zero when an occluder
+    blocks the shadow ray, when the reservoir's light is gone or invalid, and for a surface facing
+    away."""
+    import ctypes as C
+    import math
+    from raytracedgl1_gb300 import _native as N
+    o, p = _reshade_stream()
+    lt = _light((0.0, 5.0, 0.0), 0.25, 100.0)
+    o.set_reshade_scene(lt, (C.c_uint32 * 1)(0), (N.Occluder * 0)())
+    d, s = o.reshade(1, 3, 2, p, f64=True)
+    sin_t = 0.25 / 5.0
+    dw = 2.0 * math.pi * (1.0 - math.sqrt(1.0 - sin_t * sin_t))
+    ref = dw * 100.0 / math.pi   # luminance of a white light: the weights sum to 1
+    assert 0.995 * ref <= d <= ref * 1.0000001, (d, ref)
+    assert s > 0.0
+    # FP32: 1 - cos(theta) of a small light cancels (the shader's own arithmetic), about 1e-4
+    d32, _ = o.reshade(1, 3, 2, p, f64=False)
+    assert abs(d32 - d) <= 1e-3 * d
+    # an occluding sphere half way
+    occ = (N.Occluder * 1)()
+    occ[0].type = N.OCCLUDER_SPHERE
+    occ[0].data[:4] = (0.0, 2.5, 0.0, 0.5)
+    o.set_reshade_scene(lt, (C.c_uint32 * 1)(0), occ)
+    assert o.reshade(1, 3, 2, p) == (0.0, 0.0)
+    # a rectangle that misses the ray (beside it) changes nothing
+    occ[0].type = N.OCCLUDER_RECT
+    occ[0].data[:] = (1.0, 2.5, 3.0, 4.0, -1.0, 1.0, 0.0)   # y = 2.5, x in [3, 4], z in [-1, 1]
+    o.set_reshade_scene(lt, (C.c_uint32 * 1)(0), occ)
+    assert o.reshade(1, 3, 2, p, f64=True)[0] == d
+    occ[0].data[:] = (1.0, 2.5, -1.0, 1.0, -1.0, 1.0, 0.0)  # the same plane across the ray
+    o.set_reshade_scene(lt, (C.c_uint32 * 1)(0), occ)
+    assert o.reshade(1, 3, 2, p) == (0.0, 0.0)
+    # the previous frame's light is gone, or the reservoir holds no light
+    o.set_reshade_scene(lt, (C.c_uint32 * 1)(0xFFFFFFFF), (N.Occluder * 0)())
+    assert o.reshade(1, 3, 2, p) == (0.0, 0.0)
+    o.set_reshade_scene(lt, (C.c_uint32 * 1)(0), (N.Occluder * 0)())
+    o.plane("RESERVOIRS", 0)[..., 0] = 32767
+    assert o.reshade(1, 3, 2, p) == (0.0, 0.0)
+    # facing away from the light
+    o2, p2 = _reshade_stream(normal=(0.0, -1.0, 0.0))
+    o2.set_reshade_scene(lt, (C.c_uint32 * 1)(0), (N.Occluder * 0)())
+    assert o2.reshade(1, 3, 2, p2) == (0.0, 0.0)
+
+
+def test_reshade_specular_follows_roughness():
+    """The Smith-GGX term (BRDF.h:116-146): with the camera on the mirror direction of the light,
+    a smooth metal's specular luminance exceeds a rough dielectric's by orders of magnitude."""
+    import ctypes as C
+    from raytracedgl1_gb300 import _native as N
+    lt = _light((0.0, 5.0, -5.0), 0.25, 100.0)
+    spec = []
+    for rough, metal in ((1.0, 0.0), (0.1, 1.0)):
+        o, p = _reshade_stream(roughness=rough, metallic=metal)
+        o.set_reshade_scene(lt, (C.c_uint32 * 1)(0), (N.Occluder * 0)())
+        spec.append(o.reshade(1, 3, 2, p, f64=True)[1])
+    assert spec[1] > 100.0 * spec[0] > 0.0, spec

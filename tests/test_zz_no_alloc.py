@@ -81,7 +81,7 @@ def test_noalloc_at_the_stated_maximum():
     rng = np.random.default_rng(41)
     shape = (s.image("DIS_PING_GRADIENT", 0).height, s.image("DIS_PING_GRADIENT", 0).width)
     assert shape == (720, 1280)
-    samples = rng.integers(0, 2 ** 32, size=shape, dtype=np.uint32)
+    samples = rng.integers(0, 256, size=shape + (4,), dtype=np.uint8)   # rgba8 per stratum
     s.upload("DIS_PING_GRADIENT", 0, samples)
     p = N.FrameParams()
     p.minLogLuminance, p.maxLogLuminance = -3.0, 7.0
