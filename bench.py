@@ -54,10 +54,10 @@ def parse():
     ap.add_argument("--iters", type=int, default=5, help="a-trous passes")
     ap.add_argument("--frames", type=int, default=60, help="distinct frames in the sequence")
     ap.add_argument("--e2e-steps", type=int, default=120)
-    ap.add_argument("--path", default="fused", choices=["fused", "plain", "tma", "direct", "pair"],
+    ap.add_argument("--path", default="fused", choices=["fused", "plain", "tma", "pair"],
                     help="fused: the default kernels; plain: one kernel per reference dispatch; "
-                         "tma: the default kernels with TMA-staged a-trous; direct: the default kernels with "
-                         "the a-trous taps read from global memory")
+                         "tma: the default kernels with TMA-staged a-trous; pair: the default kernels with "
+                         "a-trous iterations 0 and 1 in one launch")
     ap.add_argument("--no-cpu-baseline", action="store_true", help="skip the CPU oracle (baseline and parity)")
     ap.add_argument("--parity-frames", type=int, default=8, help="frames run on GPU and oracle for the parity figures")
     ap.add_argument("--no-batched", action="store_true", help="skip the 32-stream batched measurement")
@@ -72,6 +72,11 @@ def parse():
     ap.add_argument("--serve-inflight", type=int, default=1,
                     help="serving steps enqueued ahead of the GPU (1..3) with resident inputs; the e2e run "
                          "(host inputs) uses at least 2 so copies overlap the kernels")
+    ap.add_argument("--ncu-traffic", nargs="+", metavar="GROUP=CSV",
+                    help="instead of the benchmark: print the profiles/dram_traffic.md rows (DRAM bytes read + "
+                         "written per launch) of each kernel group from an ncu --csv capture of "
+                         "dram__bytes_read.sum and dram__bytes_write.sum for that group's kernel (with --width, "
+                         "--height and --storage of the captured run)")
     ap.add_argument("--precision-sweep", action="store_true",
                     help="instead of the benchmark: fp32/fp16/bf16 storage against the FP64 oracle "
                          "(use with --width 3840 --height 2160 --frames 30)")
@@ -215,7 +220,7 @@ def path_bytes(storage: str) -> float:
 
 def kernel_bytes(name: str, it: int, niter: int, per_px: dict) -> float:
     if name in ("atrous", "atrous_fast", "atrous_fast_hist", "atrous_exact", "atrous_exact_hist", "atrous_tma",
-                "atrous_tma_hist", "atrous_sm", "atrous_sm_hist"):
+                "atrous_tma_hist"):
         return per_px["atrous0"] if it == 0 else per_px["atrous_last"] if it == niter - 1 else per_px["atrous"]
     if name in ("atrous_pair", "atrous_pair_hist"):
         # two iterations in one launch (it, it + 1): the first one's sources and the static
@@ -702,8 +707,6 @@ def run_ours(args, dist: Dist):
             p.flags |= N.FLAG_PLAIN
         elif args.path == "tma":
             p.flags |= N.FLAG_TMA_STAGING
-        elif args.path == "direct":
-            p.flags |= N.FLAG_ATROUS_DIRECT
         elif args.path == "pair":
             p.flags |= N.FLAG_ATROUS_PAIR
         dev_bufs = {}
@@ -1099,8 +1102,33 @@ def run_precision(args, dist: Dist):
     ctx.close()
 
 
+def ncu_traffic(args):
+    """profiles/dram_traffic.md rows from ncu --csv captures (one per kernel group): per launch,
+    the DRAM bytes read + written, averaged over the captured launches."""
+    import csv
+    scale = {"byte": 1, "Kbyte": 1e3, "Mbyte": 1e6, "Gbyte": 1e9, "KB": 1e3, "MB": 1e6, "GB": 1e9}
+    print("| kernel group | storage | frame | launches captured | DRAM bytes per launch (read + write) |")
+    print("|---|---|---|---|---|")
+    for item in args.ncu_traffic:
+        group, path = item.split("=", 1)
+        per = {}
+        with open(path, newline="") as f:
+            lines = [ln for ln in f if ln.startswith('"')]
+        for row in csv.DictReader(lines):
+            name = row.get("Metric Name", "")
+            if name not in ("dram__bytes_read.sum", "dram__bytes_write.sum"):
+                continue
+            v = float(row["Metric Value"].replace(",", "")) * scale.get(row.get("Metric Unit", "byte"), 1)
+            per[row["ID"]] = per.get(row["ID"], 0.0) + v
+        if per:
+            print(f"| {group} | {args.storage} | {args.width}x{args.height} | {len(per)} | {sum(per.values()) / len(per):.0f} |")
+
+
 def main():
     args = parse()
+    if args.ncu_traffic:
+        ncu_traffic(args)
+        return
     dist = Dist()
     try:
         if args.precision_sweep:

@@ -218,12 +218,10 @@ typedef struct rgdn_frame_params
 #define RGDN_FLAG_TMA_STAGING        0x8u /* a-trous taps staged in shared memory by the Tensor
                                              Memory Accelerator (widths divisible by 4, up to 5
                                              iterations); the same results as the default kernels */
-#define RGDN_FLAG_ATROUS_DIRECT      0x20u /* the default path's a-trous reading every tap from global
-                                             memory instead of from the shared-memory footprint;
-                                             the same results bit for bit */
-#define RGDN_FLAG_ATROUS_PAIR        0x40u /* a-trous iterations 0 and 1 in one launch (fusion depth 2;
-                                             with 3 or more iterations, not with RGDN_FLAG_ATROUS_DIRECT);
-                                             the same results bit for bit */
+#define RGDN_FLAG_ATROUS_PAIR        0x40u /* a-trous iterations 0 and 1 in one launch (fusion depth 2,
+                                             with 3 or more iterations): iteration 0 over the tile
+                                             widened by 2 in shared memory, then iteration 1; the
+                                             same results bit for bit */
 #define RGDN_FLAG_TEST_TMA_TIMEOUT   0x80000000u /* tests only, with RGDN_FLAG_TMA_STAGING: every stage of
                                              the TMA-staged a-trous expects 16 bytes more than its
                                              copies deliver, so each block's first bounded wait runs

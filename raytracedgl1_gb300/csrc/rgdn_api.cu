@@ -478,9 +478,7 @@ rgdn_status launch_default_stage( rgdn_stream* s, const FrameArgs& a, uint32_t f
             else if( !exact && ( p->flags & RGDN_FLAG_TMA_STAGING ) && tma_atrous_ok( s, iter ) ) r = launch_atrous_tma( s, a, iter, last, cs );
             else
             {
-                const bool direct = exact || ( p->flags & RGDN_FLAG_ATROUS_DIRECT );
-                const int  k = exact ? ( last ? KF_ATROUS_EXACT_HIST : KF_ATROUS_EXACT )
-                                     : direct ? ( last ? KF_ATROUS_FAST_HIST : KF_ATROUS_FAST ) : ( last ? KF_ATROUS_SM_HIST : KF_ATROUS_SM );
+                const int k = exact ? ( last ? KF_ATROUS_EXACT_HIST : KF_ATROUS_EXACT ) : ( last ? KF_ATROUS_FAST_HIST : KF_ATROUS_FAST );
                 r = launch( s, a, k, iter, cs );
             }
             if( r == RGDN_SUCCESS && last ) s->histPending = true;
@@ -519,7 +517,7 @@ rgdn_status run_denoise_fused( rgdn_stream* s, uint32_t fi, const rgdn_frame_par
     // iterations 0 and 1 in one launch when asked for, with the FAST shared-memory kernels and at
     // least one more iteration after them
     const bool pairOk = ( p->flags & RGDN_FLAG_ATROUS_PAIR ) && a.u.niter >= 3 &&
-                        !( p->flags & ( RGDN_FLAG_EXACT_MATH | RGDN_FLAG_ATROUS_DIRECT | RGDN_FLAG_TMA_STAGING ) );
+                        !( p->flags & ( RGDN_FLAG_EXACT_MATH | RGDN_FLAG_TMA_STAGING ) );
     for( uint32_t i = 0; i < a.u.niter; i++ )
         if( ( r = launch_default_stage( s, a, fi, p, RGDN_STAGE_ATROUS, (int)i, cs, pairOk ) ) != RGDN_SUCCESS ) return r;
     return RGDN_SUCCESS;

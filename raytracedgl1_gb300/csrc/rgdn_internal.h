@@ -230,8 +230,6 @@ enum FusedKernel : int
     KF_PREPARE_FINAL       = 114,  // exposure, tonemapping and bloom input (timing label)
     KF_BLOOM               = 115,  // the bloom pyramid and its application (timing label)
     KF_SCATTER_ACCUM       = 117,  // volume integration + screen-space accumulation (timing label)
-    KF_ATROUS_SM           = 120,  // a-trous iteration, taps decoded once into shared memory
-    KF_ATROUS_SM_HIST      = 121,  // its last iteration + composition + fused histogram
     KF_ATROUS_PAIR01       = 122,  // a-trous iterations 0 and 1 in one launch (fusion depth 2)
 };
 
@@ -316,8 +314,7 @@ cudaError_t launch_atrous_tma_bf16( const FrameArgs& a, int iter, bool hist, con
 int atrous_tma_smem( int storage, int iter );
 inline bool is_fast_kernel( int stage )
 {
-    return stage == KF_ATROUS_FAST || stage == KF_ATROUS_FAST_HIST || stage == KF_VARIANCE_FAST || stage == KF_ATROUS_SM ||
-           stage == KF_ATROUS_SM_HIST || stage == KF_ATROUS_PAIR01;
+    return stage == KF_ATROUS_FAST || stage == KF_ATROUS_FAST_HIST || stage == KF_VARIANCE_FAST || stage == KF_ATROUS_PAIR01;
 }
 
 // ------------------------------------------------------------------------------------------

@@ -2102,38 +2102,14 @@ __global__ void __launch_bounds__( NT, MINB ) k_atrous( const FrameArgs a, const
 }
 
 // ==========================================================================================
-// A-trous with the tap footprint decoded once into shared memory (default path).
+// A-trous from footprints decoded once into shared memory (the fused iterations 0 + 1 below).
 //
-// Every texel a block's taps read is loaded once (coalesced rows), decoded to FP32 and kept in
-// four float4 planes of shared memory: (normal, depth), (colour, variance), (specular, colour
-// luminance) and (indirect, roughness). The taps then read shared memory at compile-time
-// offsets (the step is a template parameter), so a tap costs its weights and four 16-byte
-// shared loads; the decode, the address arithmetic and the luminance of a texel are paid once
-// per staged texel instead of once per tap. The arithmetic is atrous_px's, in the same order,
-// so the results equal the direct kernel's bit for bit.
-//
-// The block is 32 x 8 threads and its tile 32 x TH pixels (TH / 8 rows per thread). The staged
-// region is the tile widened by the step on every side; when TH is below the step, its rows
-// are three bands of TH rows (-step, 0, +step), the only rows the dilated stencil reads.
+// Every texel a block's taps read is loaded once (coalesced rows, read-only loads), decoded to
+// FP32 and kept in four float4 planes of shared memory: (normal, depth), (colour, variance),
+// (specular, colour luminance) and (indirect, roughness). The taps then read shared memory at
+// compile-time offsets. The arithmetic is atrous_px's, in the same order, so the results equal
+// the direct kernel's bit for bit.
 // ==========================================================================================
-template< int ITER, int TH > struct AtSm
-{
-    static constexpr int  S     = 1 << ITER;
-    static constexpr int  TW    = 32;
-    static constexpr int  PY    = TH / 8;
-    static constexpr bool BANDS = TH < S;
-    static constexpr int  RW    = TW + 2 * S;
-    static constexpr int  RH    = BANDS ? 3 * TH : TH + 2 * S;
-    static constexpr int  N     = RW * RH;
-    static constexpr int  SMEM  = 4 * N * (int)sizeof( float4 );
-    static_assert( TH % 8 == 0 && S <= TW, "tile rows are whole thread rows; columns are one contiguous run" );
-    // texel offset of the tap (dx, dy) from its centre
-    static __host__ __device__ constexpr int off( int dx, int dy ) { return dy * ( BANDS ? TH : S ) * RW + dx * S; }
-    // region row of tile row ty, and image row of region row r
-    static __device__ __forceinline__ int crow( int ty ) { return BANDS ? TH + ty : S + ty; }
-    static __device__ __forceinline__ int grow( int r, int y0 ) { return BANDS ? y0 + ( r / TH - 1 ) * S + r % TH : y0 - S + r; }
-};
-
 // One texel of an a-trous footprint as the staged planes hold it: (normal, depth),
 // (colour, variance), (specular, luminance of the colour), (indirect, roughness). A texel outside
 // the image is the zero texel the direct kernel substitutes (normal code 0 decodes to (0, 0, 1)).
@@ -2233,79 +2209,6 @@ __device__ __forceinline__ AtrousOut atrous_sm_px( const FrameArgs& a, const int
     else taps( std::false_type() );
     atrous_finish( acc, o.d, o.var, o.s, o.i );
     return o;
-}
-
-template< int M, bool HIST, int ITER, int TH, int MINB >
-__global__ void __launch_bounds__( 256, MINB ) k_atrous_sm( const FrameArgs a )
-{
-    using G = AtSm< ITER, TH >;
-    using S = Sto< M >;
-    extern __shared__ float4 smem[];
-    float4* const       sG = smem;          // normal, depth
-    float4* const       sC = sG + G::N;     // colour, variance
-    float4* const       sS = sC + G::N;     // specular, luminance of the colour
-    float4* const       sI = sS + G::N;     // indirect, roughness
-    __shared__ float    u8[ 256 ];
-    __shared__ uint32_t hist[ HIST ? 256 : 1 ];
-    const int           t = threadIdx.y * 32 + threadIdx.x;
-    pdl_launch_dependents();
-    u8[ t ] = (float)t / 255.0f;
-    if( HIST ) hist[ t ] = 0u;
-    pdl_wait();
-    __syncthreads();
-
-    const Uniform& u  = a.u;
-    const AtrousIO io = atrous_io< M >( a, ITER );
-    const int      x0 = blockIdx.x * G::TW, y0 = blockIdx.y * TH;
-#pragma unroll
-    for( int k = 0; k < ( G::N + 255 ) / 256; k++ )
-    {
-        const int e = t + 256 * k;
-        if( e < G::N )
-        {
-            const int r = e / G::RW, c = e - r * G::RW;
-            atrous_stage_texel< M >( a, io, x0 - G::S + c, G::grow( r, y0 ), u8, sG[ e ], sC[ e ], sS[ e ], sI[ e ] );
-        }
-    }
-    __syncthreads();
-
-    // block-uniform: every tap of the tile inside the image and inside one checkerboard half
-    const int  sep = u.W / 2, x1 = x0 + G::TW - 1, y1 = y0 + TH - 1;
-    const bool interior = x0 - G::S >= 0 && y0 - G::S >= 0 && x1 + G::S < u.W && y1 + G::S < u.H &&
-                          ( x1 + G::S < sep || x0 - G::S >= sep );
-    constexpr int RS = G::off( 0, 1 );
-#pragma unroll 1
-    for( int k = 0; k < G::PY; k++ )
-    {
-        const int ty = threadIdx.y + 8 * k;
-        const int px = x0 + threadIdx.x, py = y0 + ty;
-        if( px >= u.W || py >= u.H ) continue;
-        const int       i  = py * u.W + px;
-        const int       ce = G::crow( ty ) * G::RW + threadIdx.x + G::S;
-        const float     pv = ITER == 0 ? 0.0f : S::ld1( a.filtVar, (size_t)i );
-        const AtrousOut o  = atrous_sm_px< ITER, G::S, RS, RS >( a, px, py, i, interior, sG, sC, sS, sI, ce, ce, pv, S::ld4( a.histLen, (size_t)i ).z );
-        if( ITER == 0 && o.pref ) S::st1( a.filtVar, (size_t)i, o.prefVar );
-        if( !HIST )
-        {
-            S::stcv( io.diffDst, io.varDst, (size_t)i, o.d, o.var );
-            S::st3( io.specDst, (size_t)i, o.s );
-            S::st3( io.indirDst, (size_t)i, o.i );
-        }
-        else
-        {
-            const ComposeIn cin = compose_load( a, px, py, i );
-            const uint16_t  hin = compose< M, true >( a, px, cin, o.d, o.s, o.i, u8 );
-            // one shared atomic per distinct bin of the warp
-            const uint32_t bin   = __ldg( &a.binLut[ hin ] );
-            const uint32_t peers = __match_any_sync( __activemask(), bin );
-            if( ( t & 31 ) == (uint32_t)( __ffs( peers ) - 1 ) ) atomicAdd( &hist[ bin ], (uint32_t)__popc( peers ) );
-        }
-    }
-    if( HIST )
-    {
-        __syncthreads();
-        if( hist[ t ] ) atomicAdd( &a.tm->histogram[ t ], hist[ t ] );
-    }
 }
 
 // ==========================================================================================
@@ -3849,40 +3752,6 @@ template< int M > cudaError_t launch_final_t( const FinalArgs& f, cudaStream_t s
     return e != cudaSuccess ? e : cudaGetLastError();
 }
 
-// The shared-memory a-trous for one iteration: a 32 x TH tile per 256-thread block, MINB blocks
-// per SM. The dynamic shared memory above 48 KB is enabled once per device.
-template< int M, bool HIST, int ITER, int TH, int MINB > cudaError_t launch_atrous_sm_it( const FrameArgs& a, cudaStream_t s )
-{
-    using G     = dev::AtSm< ITER, TH >;
-    auto kernel = dev::k_atrous_sm< M, HIST, ITER, TH, MINB >;
-    static std::atomic< uint64_t > enabled( 0 );
-    int                            d = 0;
-    if( cudaGetDevice( &d ) != cudaSuccess ) return cudaErrorInvalidDevice;
-    const uint64_t bit = 1ull << ( d & 63 );
-    if( !( enabled.load( std::memory_order_relaxed ) & bit ) )
-    {
-        const cudaError_t e = cudaFuncSetAttribute( kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, G::SMEM );
-        if( e != cudaSuccess ) return e;
-        enabled.fetch_or( bit, std::memory_order_relaxed );
-    }
-    return launch_pdl( kernel, dim3( ( a.u.W + G::TW - 1 ) / G::TW, ( a.u.H + TH - 1 ) / TH ), dim3( 32, 8 ), G::SMEM, s, a );
-}
-// tile rows and resident blocks per iteration: 32 x 8 tiles for steps 1 and 2 (22 and 28 KB of
-// shared memory), 32 x 16 for steps 4 and 8 (61 and 98 KB), three 8-row bands for 16 and 32
-template< int M, bool HIST > cudaError_t launch_atrous_sm( const FrameArgs& a, int iter, cudaStream_t s )
-{
-    switch( iter )
-    {
-        case 0: return launch_atrous_sm_it< M, HIST, 0, 8, 4 >( a, s );
-        case 1: return launch_atrous_sm_it< M, HIST, 1, 8, 4 >( a, s );
-        case 2: return launch_atrous_sm_it< M, HIST, 2, 16, 3 >( a, s );
-        case 3: return launch_atrous_sm_it< M, HIST, 3, 16, 2 >( a, s );
-        case 4: return launch_atrous_sm_it< M, HIST, 4, 8, 2 >( a, s );
-        case 5: return launch_atrous_sm_it< M, HIST, 5, 8, 1 >( a, s );
-        default: return cudaErrorInvalidValue;
-    }
-}
-
 // a-trous iterations 0 and 1 in one launch (the caller ensures iteration 1 is not the last)
 template< int M > cudaError_t launch_atrous_pair01( const FrameArgs& a, cudaStream_t s )
 {
@@ -3918,8 +3787,6 @@ template< int M > cudaError_t launch_fast_t( const FrameArgs& a, int stage, int 
             e = launch_pdl( dev::k_atrous< M, true, true, true, 128, 7 >, dim3( grid.x, ( a.u.H + 3 ) / 4 ), dim3( 32, 4 ), 0, s, a, iter );
             break;
         case KF_VARIANCE_FAST: e = launch_pdl( dev::k_variance_geo< M, true >, grid, blk, 0, s, a ); break;
-        case KF_ATROUS_SM: e = launch_atrous_sm< M, false >( a, iter, s ); break;
-        case KF_ATROUS_SM_HIST: e = launch_atrous_sm< M, true >( a, iter, s ); break;
         case KF_ATROUS_PAIR01: e = launch_atrous_pair01< M >( a, s ); break;
         default: return cudaErrorInvalidValue;
     }

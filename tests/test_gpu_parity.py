@@ -24,6 +24,12 @@ MODES = [("ref", N.STORAGE_REF), ("fp32", N.STORAGE_FP32), ("fp16", N.STORAGE_FP
 # sizes: W%3 in {1, 2, 0}, odd heights, a width whose half is odd
 SIZES = [(64, 36), (50, 23), (34, 17)]
 
+# The FP32 variance planes hold E[l^2] - E[l]^2 of weighted moments: the cancellation scales
+# an ulp of the weights (CUDA's and the host's expf / powf differ by up to one) by
+# E[l^2] / variance, so they get a wider per-texel bound than the other FP32 planes.
+VARIANCE_PLANES = ("DIFF_PING_VARIANCE", "DIFF_PONG_VARIANCE", "DIFF_COLOR_HISTORY_VARIANCE")
+VARIANCE_TOL = 2e-2
+
 # per-texel tolerance (relative to the texel's largest channel) of each stored format
 TOL = {F.F_E5: 2.0 ** -7, F.F_RGBA16F: 2.0 ** -9, F.F_RG16F: 2.0 ** -9, F.F_R16F: 2.0 ** -9,
        F.F_RGBA16BF: 2.0 ** -6, F.F_RGBA8: 1.01 / 255.0, F.F_B10G11R11: 2.0 ** -5,
@@ -61,7 +67,7 @@ def compare_state(s: Stream, o: oracle.OracleStream, what: str, max_diff_frac: f
             raise AssertionError(f"{what}: integer plane {name}[{slot}] differs at {bad} texels")
         scale = np.percentile(np.abs(cd[np.isfinite(cd)]), 99) if np.isfinite(cd).any() else 1.0
         err = F.texel_rel_err(gd, cd, atol=max(1e-6, 1e-4 * float(scale)))
-        tol = TOL[fmt]
+        tol = VARIANCE_TOL if name in VARIANCE_PLANES else TOL[fmt]
         ndiff = int(np.count_nonzero(np.any(g != c, axis=-1) if g.ndim == 3 else g != c))
         frac = ndiff / err.size
         worst.append((name, slot, float(err.max()), frac))
@@ -360,10 +366,11 @@ def test_tma_staging_equals_default(ctx, mode_name, mode):
 
 @pytest.mark.parametrize("mode_name,mode", MODES)
 @pytest.mark.parametrize("size", [(96, 54), (250, 151), (330, 97)])
-def test_atrous_shared_equals_direct(ctx, mode_name, mode, size):
-    """The default a-trous (taps decoded once into shared memory) computes the direct kernel's
-    arithmetic: identical planes, with partial tiles on the right and bottom edges and every step
-    from 1 to 32 (4, 5 and 6 iterations)."""
+def test_atrous_pair_equals_single(ctx, mode_name, mode, size):
+    """A-trous iterations 0 and 1 in one launch (fusion depth 2: iteration 0 over the tile widened
+    by 2 in shared memory, its results quantised as stored) give the single-iteration kernels'
+    planes bit for bit, with partial tiles on the right and bottom edges and 4, 5 and 6
+    iterations."""
     W, H = size
     sc = Scene(W, H, seed=29, lightFlickerFrom=2.0)
     a = Stream(ctx, W, H, mode)
@@ -374,12 +381,9 @@ def test_atrous_shared_equals_direct(ctx, mode_name, mode, size):
         p.atrousIterations = (4, 5, 6)[f % 3]
         upload_frame(a, None, bufs, fi)
         upload_frame(b, None, bufs, fi)
-        pb = p.copy()
-        pb.flags = N.FLAG_ATROUS_DIRECT
-        if f % 2:
-            p = p.copy()
-            p.flags = N.FLAG_ATROUS_PAIR   # iterations 0 and 1 in one launch
-        for s, q in ((a, p), (b, pb)):
+        pa = p.copy()
+        pa.flags = N.FLAG_ATROUS_PAIR   # iterations 0 and 1 in one launch
+        for s, q in ((a, pa), (b, p)):
             Denoiser(s).Denoise(fi, q)
             Tonemapping(s).CalculateExposure(fi, q)
         ga, gb = gpu_planes(a), gpu_planes(b)
