@@ -475,7 +475,7 @@ def run_batched(args, dist: Dist, dev: int, cs) -> dict:
 
     k = 0
     with torch.cuda.stream(cs):
-        for _ in range(24):          # autotuning (18 steps) + graph capture
+        for _ in range(24):          # autotuning (15 steps) + graph capture
             batched(k)
             k += 1
     cs.synchronize()
@@ -551,6 +551,7 @@ def run_batched(args, dist: Dist, dev: int, cs) -> dict:
         "tuned_config": {"temporal": int(cfg.temporalTile), "anti_firefly": int(cfg.antiFireflyTile),
                          "variance": int(cfg.varianceTile), "atrous": [int(v) for v in cfg.atrousTile][:args.iters],
                          "atrous_blocks_per_sm": [int(v) for v in cfg.atrousBlocksPerSM][:args.iters],
+                         "atrous_fusion_depth": int(cfg.atrousFusionDepth),
                          "graphs": int(cfg.useGraphs), "tile_names": ["32x8", "16x16", "64x4", "32x4"]},
         "kernels": kern,
     }

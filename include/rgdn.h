@@ -508,6 +508,10 @@ typedef struct rgdn_batch_config
                                      thread); 0 = 3. With RGDN_TILE_32X4 it is 7 (0 or 7). */
     uint32_t useGraphs;           /* replay a captured graph per step (off while timing) */
     uint32_t tuned;               /* read: the autotuner has settled (set_config settles it) */
+    uint32_t atrousFusionDepth;   /* 1: one launch per a-trous iteration; 2: iterations 0 and 1 in
+                                     one launch (32x8 tiles, iteration 0 recomputed over the tile
+                                     widened by 2) in steps whose frames all run 3 or more
+                                     iterations; 0 = 1 */
 } rgdn_batch_config;
 rgdn_status rgdn_batch_get_config( rgdn_context* ctx, uint32_t storage, rgdn_batch_config* outConfig );
 /* Fixes the configuration of a storage mode and ends its autotuning. */

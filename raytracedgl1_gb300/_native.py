@@ -165,7 +165,8 @@ class BatchConfig(C.Structure):
     """rgdn_batch_config: launch configuration of batched steps for one storage mode."""
     _fields_ = [("temporalTile", C.c_uint32), ("antiFireflyTile", C.c_uint32),
                 ("varianceTile", C.c_uint32), ("atrousTile", C.c_uint32 * 6),
-                ("atrousBlocksPerSM", C.c_uint32 * 6), ("useGraphs", C.c_uint32), ("tuned", C.c_uint32)]
+                ("atrousBlocksPerSM", C.c_uint32 * 6), ("useGraphs", C.c_uint32), ("tuned", C.c_uint32),
+                ("atrousFusionDepth", C.c_uint32)]
 
 
 TILE_32X8, TILE_16X16, TILE_64X4, TILE_32X4 = 0, 1, 2, 3

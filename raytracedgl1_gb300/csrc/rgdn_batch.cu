@@ -154,20 +154,25 @@ struct Tuner
 // anti-firefly keeps 32x8, its shared-memory tile is laid out for it):
 //   temporal:  persistent 32x8 and 16x16; one 32x4 tile per 128-thread block (occ 7)
 //   variance:  persistent 32x8 and 16x16
-//   a-trous:   persistent 32x8 and 16x16 at 3 blocks per SM, one 32x4 tile per block, 32x8 at 4
+//   a-trous:   persistent 32x8 and 16x16 at 3 blocks per SM, one 32x4 tile per block, 32x8 at 4;
+//              for the first iteration also the fusion depth 2 (kOccPair): iterations 0 and 1
+//              in one launch of one 32x8 tile per block, scored against the best first and
+//              second iterations together
+constexpr int kOccPair = 6;
 int n_candidates( int kind )
 {
-    return kind >= BS_ATROUS0 ? 4 : kind == BS_TEMPORAL ? 3 : ( kind == BS_GRADIENT || kind == BS_ANTI_FIREFLY ) ? 1 : 2;
+    return kind == BS_ATROUS0 ? 5 : kind > BS_ATROUS0 ? 4 : kind == BS_TEMPORAL ? 3 : ( kind == BS_GRADIENT || kind == BS_ANTI_FIREFLY ) ? 1 : 2;
 }
-int max_candidates() { return 4; }
+int max_candidates() { return 5; }
 void candidate( int kind, int c, int& shape, int& occ )
 {
-    static const int atrousShape[ 4 ] = { RGDN_TILE_32X8, RGDN_TILE_16X16, RGDN_TILE_32X4, RGDN_TILE_32X8 };
-    static const int atrousOcc[ 4 ]   = { 3, 3, 7, 4 };
+    static const int atrousShape[ 5 ] = { RGDN_TILE_32X8, RGDN_TILE_16X16, RGDN_TILE_32X4, RGDN_TILE_32X8, RGDN_TILE_32X8 };
+    static const int atrousOcc[ 5 ]   = { 3, 3, 7, 4, kOccPair };
     if( kind >= BS_ATROUS0 )
     {
-        shape = atrousShape[ c % 4 ];
-        occ   = atrousOcc[ c % 4 ];
+        const int k = c % n_candidates( kind );
+        shape       = atrousShape[ k ];
+        occ         = atrousOcc[ k ];
     }
     else if( kind == BS_TEMPORAL )
     {
@@ -303,7 +308,7 @@ rgdn_status enqueue_step( rgdn_context* c, BatchExec& ex, DeviceSlots& ds, int s
         if( !L ) return RGDN_INTERNAL_ERROR;
         // persistent launches: resident blocks per SM x SMs; one-tile-per-block launches: the tiles
         const int grid = stage == RGDN_STAGE_LUMINANCE_AVG ? MAX_BATCH
-                       : occ == 7                          ? key.tiles[ kind ]
+                       : ( occ == 7 || occ == kOccPair )   ? key.tiles[ kind ]
                                                            : blocks_per_sm( ex, st, stage, occ ) * ex.sms;
         if( grid <= 0 ) return RGDN_DEVICE_ERROR;
         cudaEvent_t ta = nullptr, tb = nullptr, ua = nullptr, ub = nullptr;
@@ -354,6 +359,8 @@ rgdn_status enqueue_step( rgdn_context* c, BatchExec& ex, DeviceSlots& ds, int s
     for( int i = 0; i < key.maxIter; i++ )
     {
         const int kind = BS_ATROUS0 + i;
+        // fusion depth 2: the first launch ran iterations 0 and 1
+        if( i == 1 && key.occ[ BS_ATROUS0 ] == kOccPair ) continue;
         const int arg  = i | ( key.hm[ i ] << 8 ) | ( key.occ[ kind ] << 10 );
         if( ( r = run( kind, RGDN_STAGE_ATROUS, arg, key.shape[ kind ], key.occ[ kind ], tuneCand % n_candidates( kind ) ) ) != RGDN_SUCCESS )
             return r;
@@ -382,15 +389,24 @@ rgdn_status settle( BatchExec& ex, uint32_t st )
         ex.eventPool.push_back( p.b );
     }
     tu.probes.clear();
+    int bestOf[ BS_COUNT ] = {};
     for( int kind = BS_TEMPORAL; kind < BS_COUNT; kind++ )
     {
-        int bestC = 0;
-        for( int cnd = 1; cnd < n_candidates( kind ); cnd++ )
+        // the first iteration's single-launch candidates; the fused pair is weighed below
+        const int nc    = kind == BS_ATROUS0 ? n_candidates( kind ) - 1 : n_candidates( kind );
+        int       bestC = 0;
+        for( int cnd = 1; cnd < nc; cnd++ )
             if( best[ kind * max_candidates() + cnd ] < best[ kind * max_candidates() + bestC ] ) bestC = cnd;
+        bestOf[ kind ] = bestC;
         // kinds no tuning step ran (more iterations later) keep their configuration
         if( best[ kind * max_candidates() + bestC ] >= 1e30 ) continue;
         candidate( kind, bestC, ex.cfg[ st ].shape[ kind ], ex.cfg[ st ].occ[ kind ] );
     }
+    // fusion depth 2 when the pair beats the best first and second iterations together
+    const double pair = best[ BS_ATROUS0 * max_candidates() + 4 ];
+    const double sep  = best[ BS_ATROUS0 * max_candidates() + bestOf[ BS_ATROUS0 ] ] +
+                       best[ ( BS_ATROUS0 + 1 ) * max_candidates() + bestOf[ BS_ATROUS0 + 1 ] ];
+    if( pair < 1e30 && sep < 1e30 && pair < sep ) candidate( BS_ATROUS0, 4, ex.cfg[ st ].shape[ BS_ATROUS0 ], ex.cfg[ st ].occ[ BS_ATROUS0 ] );
     tu.settled = true;
     return r;
 }
@@ -418,10 +434,19 @@ rgdn_status run_step( rgdn_context* c, BatchExec& ex, const rgdn_job* jobs, int 
     }
     Tuner&     tu     = ex.tuner[ st ];
     const bool tuning = !tu.settled;
-    const int  tcand  = tu.step;
+    int        tcand  = tu.step;
     Config     cfg    = ex.cfg[ st ];
     if( tuning )
         for( int kind = BS_TEMPORAL; kind < BS_COUNT; kind++ ) candidate( kind, tcand % n_candidates( kind ), cfg.shape[ kind ], cfg.occ[ kind ] );
+    // the fused first two iterations need every frame of the step to run at least three
+    int minIter = MAX_ATROUS_ITERATIONS;
+    for( int k = 0; k < n; k++ ) minIter = std::min( minIter, jobs[ k ].params->atrousIterations ? (int)jobs[ k ].params->atrousIterations : 4 );
+    if( cfg.occ[ BS_ATROUS0 ] == kOccPair && minIter < 3 )
+    {
+        candidate( BS_ATROUS0, 0, cfg.shape[ BS_ATROUS0 ], cfg.occ[ BS_ATROUS0 ] );
+        // not scored as the pair: this tuning step counts as a warm-up step
+        if( tuning ) tcand = tcand % max_candidates();
+    }
 
     BatchConst* tab = ds.host[ slot ];
     memset( tab, 0, offsetof( BatchConst, jobs ) );
@@ -467,7 +492,7 @@ rgdn_status run_step( rgdn_context* c, BatchExec& ex, const rgdn_job* jobs, int 
             pixels[ kind ] += (double)w * h;
         }
         tab->start[ kind ][ n ] = acc;
-        if( kind != BS_GRADIENT && cfg.occ[ kind ] == 7 ) key.tiles[ kind ] = acc;
+        if( kind != BS_GRADIENT && ( cfg.occ[ kind ] == 7 || cfg.occ[ kind ] == kOccPair ) ) key.tiles[ kind ] = acc;
     }
     for( int i = 0; i < key.maxIter; i++ )
     {
@@ -600,6 +625,8 @@ rgdn_status batch_get_config( rgdn_context* c, uint32_t storage, rgdn_batch_conf
         out->atrousTile[ i ]        = (uint32_t)cf.shape[ BS_ATROUS0 + i ];
         out->atrousBlocksPerSM[ i ] = (uint32_t)cf.occ[ BS_ATROUS0 + i ];
     }
+    out->atrousFusionDepth = cf.occ[ BS_ATROUS0 ] == kOccPair ? 2u : 1u;
+    if( out->atrousFusionDepth == 2u ) out->atrousBlocksPerSM[ 0 ] = 3;   // the pair kernel's build
     out->useGraphs = cf.graphs ? 1u : 0u;
     out->tuned     = ex->tuner[ storage ].settled ? 1u : 0u;
     return RGDN_SUCCESS;
@@ -618,6 +645,7 @@ rgdn_status batch_set_config( rgdn_context* c, uint32_t storage, const rgdn_batc
         if( !ok_shape4( in->atrousTile[ i ] ) ) return RGDN_WRONG_FUNCTION_ARGUMENT;
         if( in->atrousTile[ i ] == RGDN_TILE_32X4 ? ( b && b != 7 ) : ( b && ( b < 3 || b > 4 ) ) ) return RGDN_WRONG_FUNCTION_ARGUMENT;
     }
+    if( in->atrousFusionDepth > 2 ) return RGDN_WRONG_FUNCTION_ARGUMENT;
     std::lock_guard< std::mutex > g( c->batchMtx );
     BatchExec*                    ex = exec_of( c );
     if( !ex ) return RGDN_DEVICE_ERROR;
@@ -631,6 +659,7 @@ rgdn_status batch_set_config( rgdn_context* c, uint32_t storage, const rgdn_batc
         cf.shape[ BS_ATROUS0 + i ] = (int)in->atrousTile[ i ];
         cf.occ[ BS_ATROUS0 + i ]   = in->atrousTile[ i ] == RGDN_TILE_32X4 ? 7 : in->atrousBlocksPerSM[ i ] ? (int)in->atrousBlocksPerSM[ i ] : 3;
     }
+    if( in->atrousFusionDepth == 2 ) candidate( BS_ATROUS0, 4, cf.shape[ BS_ATROUS0 ], cf.occ[ BS_ATROUS0 ] );
     cf.graphs = in->useGraphs != 0;
     Tuner& tu = ex->tuner[ storage ];
     for( auto& p : tu.probes )

@@ -2254,12 +2254,12 @@ template< int M > __device__ __forceinline__ float stored_1( float v )
     return Sto< M >::ld1( tex, 0 );
 }
 
-template< int M, int MINB >
-__global__ void __launch_bounds__( 256, MINB ) k_atrous_pair01( const FrameArgs a )
+// the pair's tile (bx, by) of frame `a`, one 32 x 8 block; `smem` holds AtPair::SMEM bytes
+template< int M >
+__device__ __forceinline__ void atrous_pair_tile( const FrameArgs& a, const int bx, const int by, float4* smem, const float* u8 )
 {
     using P = AtPair;
     using S = Sto< M >;
-    extern __shared__ float4 smem[];
     float4* const    sG = smem;           // iteration 0's sources over tile +- 3
     float4* const    sC = sG + P::N0;
     float4* const    sS = sC + P::N0;
@@ -2268,16 +2268,11 @@ __global__ void __launch_bounds__( 256, MINB ) k_atrous_pair01( const FrameArgs 
     float4* const    tS = tC + P::N1;
     float4* const    tI = tS + P::N1;
     float* const     tP = reinterpret_cast< float* >( tI + P::N1 );   // prefiltered variance of the tile
-    __shared__ float u8[ 256 ];
     const int        t = threadIdx.y * 32 + threadIdx.x;
-    pdl_launch_dependents();
-    u8[ t ] = (float)t / 255.0f;
-    pdl_wait();
-    __syncthreads();
 
     const Uniform& u   = a.u;
     const AtrousIO io0 = atrous_io< M >( a, 0 ), io1 = atrous_io< M >( a, 1 );
-    const int      x0 = blockIdx.x * P::TW, y0 = blockIdx.y * P::TH;
+    const int      x0 = bx * P::TW, y0 = by * P::TH;
 #pragma unroll
     for( int k = 0; k < ( P::N0 + 255 ) / 256; k++ )
     {
@@ -2345,6 +2340,19 @@ __global__ void __launch_bounds__( 256, MINB ) k_atrous_pair01( const FrameArgs 
             S::st3( io1.indirDst, (size_t)i, o.i );
         }
     }
+}
+
+template< int M, int MINB >
+__global__ void __launch_bounds__( 256, MINB ) k_atrous_pair01( const FrameArgs a )
+{
+    extern __shared__ float4 smem[];
+    __shared__ float         u8[ 256 ];
+    const int                t = threadIdx.y * 32 + threadIdx.x;
+    pdl_launch_dependents();
+    u8[ t ] = (float)t / 255.0f;
+    pdl_wait();
+    __syncthreads();
+    atrous_pair_tile< M >( a, blockIdx.x, blockIdx.y, smem, u8 );
 }
 
 // ==========================================================================================
@@ -2952,6 +2960,23 @@ template< int M, int HM > __global__ void __launch_bounds__( 128, 7 ) kt_atrous(
             if( hist[ k ] ) atomicAdd( &a.tm->histogram[ k ], hist[ k ] );
     }
     else atrous_tile< M, true, false, true >( a, iter, bx, by, u8, hist );
+}
+
+// a-trous iterations 0 and 1 of a batched step in one launch: one 32 x 8 tile of the
+// BS_ATROUS0 table per block (every job runs at least 3 iterations)
+template< int M > __global__ void __launch_bounds__( 256, 3 ) kt_atrous_pair01( const int slot )
+{
+    extern __shared__ float4 smem[];
+    __shared__ float         u8[ 256 ];
+    const int                t = threadIdx.y * 32 + threadIdx.x;
+    pdl_launch_dependents();
+    u8[ t ] = (float)t / 255.0f;
+    int        j = 0, bx = 0, by = 0;
+    const bool has = batch_tile_of_block< false >( slot, BS_ATROUS0, j, bx, by );
+    pdl_wait();
+    __syncthreads();
+    if( !has ) return;
+    atrous_pair_tile< M >( c_batch[ slot ].jobs[ j ], bx, by, smem, u8 );
 }
 
 // one block per job (strided), as k_luminance_avg
@@ -3838,6 +3863,25 @@ template< int M > cudaError_t launch_batch_fast_t( int stage, int iter, int slot
                 case 16: e = launch_pdl( dev::kb_atrous< M, 0, 4 >, grid, block, 0, s, slot, it ); break;
                 case 17: e = launch_pdl( dev::kb_atrous< M, 1, 4 >, grid, block, 0, s, slot, it ); break;
                 case 18: e = launch_pdl( dev::kb_atrous< M, 2, 4 >, grid, block, 0, s, slot, it ); break;
+                case 24:
+                case 25:
+                case 26:
+                {
+                    // occupancy code 6: iterations 0 and 1 in one launch (fusion depth 2)
+                    auto kernel = dev::kt_atrous_pair01< M >;
+                    static std::atomic< uint64_t > enabled( 0 );
+                    int                            d = 0;
+                    if( cudaGetDevice( &d ) != cudaSuccess ) return cudaErrorInvalidDevice;
+                    const uint64_t bit = 1ull << ( d & 63 );
+                    if( !( enabled.load( std::memory_order_relaxed ) & bit ) )
+                    {
+                        if( ( e = cudaFuncSetAttribute( kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, dev::AtPair::SMEM ) ) != cudaSuccess )
+                            return e;
+                        enabled.fetch_or( bit, std::memory_order_relaxed );
+                    }
+                    e = launch_pdl( kernel, grid, block, dev::AtPair::SMEM, s, slot );
+                    break;
+                }
                 case 28: e = launch_pdl( dev::kt_atrous< M, 0 >, grid, block, 0, s, slot, it ); break;
                 case 29: e = launch_pdl( dev::kt_atrous< M, 1 >, grid, block, 0, s, slot, it ); break;
                 case 30: e = launch_pdl( dev::kt_atrous< M, 2 >, grid, block, 0, s, slot, it ); break;

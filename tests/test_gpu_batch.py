@@ -57,7 +57,7 @@ def test_batch_equals_sequential_through_tuning_and_graphs(mode_name, mode):
     scenes = [Scene(w, h, seed=40 + i, lightFlickerFrom=3.0) for i, (w, h) in enumerate(SIZES)]
     seq = [Stream(ctx, w, h, mode) for w, h in SIZES]
     bat = [Stream(ctx, w, h, mode) for w, h in SIZES]
-    frames = 18   # 12 tuning steps, then graph replay
+    frames = 19   # 15 tuning steps (the fused first two a-trous iterations among them), then graph replay
     for f in range(frames):
         fi = f & 1
         jobs = []
@@ -113,10 +113,12 @@ def test_batch_splits_steps_and_falls_back():
     ctx.close()
 
 
-@pytest.mark.parametrize("shape,occ", [(0, 3), (1, 4), (2, 4), (2, 3), (0, 4), (3, 7)])
-def test_batch_fixed_configs(shape, occ):
+@pytest.mark.parametrize("shape,occ,depth", [(0, 3, 1), (1, 4, 1), (2, 4, 1), (2, 3, 1), (0, 4, 1), (3, 7, 1), (0, 3, 2), (3, 7, 2)])
+def test_batch_fixed_configs(shape, occ, depth):
     """A configuration set through rgdn_batch_set_config (no tuning) gives the same results.
-    Shape 3 is the 128-thread 32x4 tile (temporal and a-trous; variance keeps 32x8)."""
+    Shape 3 is the 128-thread 32x4 tile (temporal and a-trous; variance keeps 32x8). Fusion depth
+    2 runs a-trous iterations 0 and 1 in one launch; the last frame has a stream running only
+    two iterations, where the step falls back to one launch per iteration."""
     ctx = Context(0)
     cfg = N.BatchConfig()
     cfg.temporalTile = shape
@@ -126,9 +128,11 @@ def test_batch_fixed_configs(shape, occ):
         cfg.atrousTile[i] = (shape + i) % 3 if shape != N.TILE_32X4 else N.TILE_32X4
         cfg.atrousBlocksPerSM[i] = occ
     cfg.useGraphs = 1
+    cfg.atrousFusionDepth = depth
     ctx.set_batch_config(N.STORAGE_BF16, cfg)
     got = ctx.batch_config(N.STORAGE_BF16)
-    assert got.tuned == 1 and got.temporalTile == shape and list(got.atrousBlocksPerSM) == [occ] * 6
+    assert got.tuned == 1 and got.temporalTile == shape and got.atrousFusionDepth == depth
+    assert list(got.atrousBlocksPerSM)[1:] == [occ] * 5
     sizes = SIZES[:3]
     scenes = [Scene(w, h, seed=70 + i) for i, (w, h) in enumerate(sizes)]
     seq = [Stream(ctx, w, h, N.STORAGE_BF16) for w, h in sizes]
@@ -138,7 +142,7 @@ def test_batch_fixed_configs(shape, occ):
         jobs = []
         for i, sc in enumerate(scenes):
             bufs, p = sc.generate(f)
-            p.atrousIterations = 5
+            p.atrousIterations = 2 if (f == 4 and i == 1) else 5
             for s in (seq[i], bat[i]):
                 for name, arr in bufs.items():
                     s.upload(name, fi, arr)
