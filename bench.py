@@ -66,13 +66,15 @@ def parse():
     ap.add_argument("--batch-per-res", type=int, default=8, help="batched streams per resolution")
     ap.add_argument("--no-serving", action="store_true", help="skip the 64-stream serving measurement")
     ap.add_argument("--serve-seconds", type=float, default=3.0)
+    ap.add_argument("--serve-only", action="store_true",
+                    help="only the serving measurement (its runs and the end-to-end one), as its own JSON line")
     ap.add_argument("--serve-hz", type=float, nargs="+", default=[60.0, 15.0, 10.0],
                     help="per-stream Poisson frame rates to serve (the configured 60 Hz first)")
     ap.add_argument("--serve-step-mpix", type=float, default=8.0, help="pixel bound of one serving step (Mpix)")
     ap.add_argument("--serve-inflight", type=int, default=1,
                     help="serving steps enqueued ahead of the GPU (1..3) with resident inputs; the e2e run "
                          "(host inputs) uses at least 2 so copies overlap the kernels")
-    ap.add_argument("--ncu-traffic", nargs="+", metavar="GROUP=CSV",
+    ap.add_argument("--ncu-traffic", nargs="+", metavar="GROUP=CSV[@NAME]",
                     help="instead of the benchmark: print the profiles/dram_traffic.md rows (DRAM bytes read + "
                          "written per launch) of each kernel group from an ncu --csv capture of "
                          "dram__bytes_read.sum and dram__bytes_write.sum for that group's kernel (with --width, "
@@ -186,7 +188,7 @@ def stage_bytes(storage: str) -> dict:
     b["atrous0"] = (cv + 2 * col3 + 2 + 2 + 2 + 4 + hl) + (cv + 2 * col3 + fv)
     b["atrous"] = (cv + 2 * col3 + 2 + 2 + 2 + 4 + hl + fv) + (cv + 2 * col3)
     b["atrous_last"] = (cv + 2 * col3 + 2 + 2 + 2 + 4 + hl + fv) + (4 + 8 + 1) + (pre + 2)
-    b["atrous_pair0"] = (cv + 2 * col3 + 2 + 2 + 2 + 4 + hl) + (cv + fv) + (cv + 2 * col3)
+    b["atrous_pair0"] = (cv + 2 * col3 + 2 + 2 + 2 + 4 + hl) + (cv + 2 * col3 + fv) + (cv + 2 * col3)
     b["atrous_pair"] = b["atrous"]
     b["luminance_histogram"] = 2
     b["luminance_avg"] = 0
@@ -552,7 +554,7 @@ def run_batched(args, dist: Dist, dev: int, cs) -> dict:
                          "variance": int(cfg.varianceTile), "atrous": [int(v) for v in cfg.atrousTile][:args.iters],
                          "atrous_blocks_per_sm": [int(v) for v in cfg.atrousBlocksPerSM][:args.iters],
                          "atrous_fusion_depth": int(cfg.atrousFusionDepth),
-                         "graphs": int(cfg.useGraphs), "tile_names": ["32x8", "16x16", "64x4", "32x4"]},
+                         "graphs": int(cfg.useGraphs), "tile_names": ["32x8", "16x16", "64x4", "32x4", "32x8 per block"]},
         "kernels": kern,
     }
     out["vs_plain"] = round(out["value"] / out["plain_path_mpix_s"], 3)
@@ -632,7 +634,7 @@ def run_serving(args, dist: Dist, dev: int) -> dict:
         arrivals.sort()
         sv.reset_stats()
         count = [0] * len(sids)
-        tickets = []
+        tickets, late = [], []
         t0 = time.perf_counter()
         for ta, i in arrivals:
             while True:
@@ -641,17 +643,26 @@ def run_serving(args, dist: Dist, dev: int) -> dict:
                     break
                 if dt > 2e-3:
                     time.sleep(dt - 1e-3)
+            late.append(1e3 * ((time.perf_counter() - t0) - ta))   # the feeder's own delay
             tickets.append(sv.submit(reqs[i][count[i] % 4]))
             count[i] += 1
         sv.drain()
         elapsed = time.perf_counter() - t0
         st = sv.stats()
-        lat_1080 = []
+        lat_1080, queue, service = [], [], []
         for t, (_, i) in zip(tickets, arrivals):
             r = sv.wait(t, 0)
-            if r.state == N.FRAME_DONE and res[i] == (1920, 1080):
-                lat_1080.append(r.latencyMs)
+            if r.state == N.FRAME_DONE:
+                # queueing (submission to the step's enqueue) and service (enqueue to completion)
+                queue.append(r.queueMs)
+                service.append(r.latencyMs - r.queueMs)
+                if res[i] == (1920, 1080):
+                    lat_1080.append(r.latencyMs)
         lat_1080.sort()
+
+        def pct(v, q):
+            v = sorted(v)
+            return round(v[int(q * (len(v) - 1))], 3) if v else None
         offered = sum(res[i][0] * res[i][1] for _, i in arrivals)
         sv.close()
         return {"per_stream_hz": hz, "steps_in_flight": inflight, "seconds": round(elapsed, 3), "requests": len(arrivals),
@@ -662,6 +673,9 @@ def run_serving(args, dist: Dist, dev: int) -> dict:
                 "p99_all_requests_ms": (round(st["p99AllMs"], 3) if st["p99AllMs"] != float("inf") else "inf"),
                 "drop_rate": round(st["dropRate"], 4),
                 "p99_ms_1080p": round(lat_1080[int(0.99 * (len(lat_1080) - 1))], 3) if lat_1080 else None,
+                "queue_p50_ms": pct(queue, 0.5), "queue_p99_ms": pct(queue, 0.99),
+                "service_p50_ms": pct(service, 0.5), "service_p99_ms": pct(service, 0.99),
+                "feeder_late_p99_ms": pct(late, 0.99),
                 "mean_frames_per_step": round(st["meanFramesPerStep"], 2), "steps": int(st["steps"]),
                 "gpu_busy_frac": round(st["busySeconds"] / elapsed, 3),
                 "resident_gb": round(st["residentBytes"] / 1e9, 2)}
@@ -679,6 +693,16 @@ def run_serving(args, dist: Dist, dev: int) -> dict:
 # ------------------------------------------------------------------------------------------
 # our arm
 # ------------------------------------------------------------------------------------------
+def run_serve_only(args, dist: Dist):
+    import torch
+    from raytracedgl1_gb300 import build
+    build.build_all()
+    torch.cuda.set_device(dist.local)
+    out = run_serving(args, dist, dist.local)
+    if dist.rank == 0:
+        print(json.dumps({"serving": out}), flush=True)
+
+
 def run_ours(args, dist: Dist):
     import numpy as np
     import torch
@@ -1112,12 +1136,16 @@ def ncu_traffic(args):
     print("|---|---|---|---|---|")
     for item in args.ncu_traffic:
         group, path = item.split("=", 1)
+        # GROUP=CSV@TEXT keeps the launches whose kernel name contains TEXT
+        path, _, only = path.partition("@")
         per = {}
         with open(path, newline="") as f:
             lines = [ln for ln in f if ln.startswith('"')]
         for row in csv.DictReader(lines):
             name = row.get("Metric Name", "")
             if name not in ("dram__bytes_read.sum", "dram__bytes_write.sum"):
+                continue
+            if only and only not in row.get("Kernel Name", ""):
                 continue
             v = float(row["Metric Value"].replace(",", "")) * scale.get(row.get("Metric Unit", "byte"), 1)
             per[row["ID"]] = per.get(row["ID"], 0.0) + v
@@ -1136,6 +1164,8 @@ def main():
             run_precision(args, dist)
         elif args.impl == "reference":
             run_reference(args, dist)
+        elif args.serve_only:
+            run_serve_only(args, dist)
         else:
             run_ours(args, dist)
     finally:

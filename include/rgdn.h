@@ -493,6 +493,7 @@ rgdn_status rgdn_submit_batch( rgdn_context* ctx, const rgdn_job* jobs, uint32_t
 #define RGDN_TILE_16X16 1u
 #define RGDN_TILE_64X4  2u
 #define RGDN_TILE_32X4  3u
+#define RGDN_TILE_32X8_PER_BLOCK 4u   /* variance: one 32x8 tile per 256-thread block */
 /* The launch configuration of batched steps for one storage mode. The autotuner starts from
  * 32x8 tiles everywhere and, over the first 12 steps, times every candidate of every launch
  * (tile shape; for a-trous also the register budget) on the work being submitted (candidates

@@ -169,7 +169,7 @@ class BatchConfig(C.Structure):
                 ("atrousFusionDepth", C.c_uint32)]
 
 
-TILE_32X8, TILE_16X16, TILE_64X4, TILE_32X4 = 0, 1, 2, 3
+TILE_32X8, TILE_16X16, TILE_64X4, TILE_32X4, TILE_32X8_PER_BLOCK = 0, 1, 2, 3, 4
 DEVICE_ERROR_TMA_WAIT = 1
 
 GBUFFER_PLANES = 15

@@ -42,7 +42,7 @@ namespace
 constexpr int kTuneRounds = 3;
 // RGDN_TILE_*: 32x8, 16x16 and 64x4 tiles of 256 threads; 32x4 tiles of 128 threads, whose
 // kernels are built for 7 resident blocks per SM
-const dim3    kShapes[ 4 ] = { dim3( 32, 8 ), dim3( 16, 16 ), dim3( 64, 4 ), dim3( 32, 4 ) };
+const dim3    kShapes[ 5 ] = { dim3( 32, 8 ), dim3( 16, 16 ), dim3( 64, 4 ), dim3( 32, 4 ), dim3( 32, 8 ) };
 
 size_t table_bytes( int n ) { return offsetof( BatchConst, jobs ) + sizeof( FrameArgs ) * (size_t)n; }
 
@@ -153,7 +153,7 @@ struct Tuner
 // Candidates of a launch kind (64x4 never won on GB300 and is left to rgdn_batch_set_config;
 // anti-firefly keeps 32x8, its shared-memory tile is laid out for it):
 //   temporal:  persistent 32x8 and 16x16; one 32x4 tile per 128-thread block (occ 7)
-//   variance:  persistent 32x8 and 16x16
+//   variance:  persistent 32x8 and 16x16; one 32x8 tile per 256-thread block (occ 7)
 //   a-trous:   persistent 32x8 and 16x16 at 3 blocks per SM, one 32x4 tile per block, 32x8 at 4;
 //              for the first iteration also the fusion depth 2 (kOccPair): iterations 0 and 1
 //              in one launch of one 32x8 tile per block, scored against the best first and
@@ -161,7 +161,8 @@ struct Tuner
 constexpr int kOccPair = 6;
 int n_candidates( int kind )
 {
-    return kind == BS_ATROUS0 ? 5 : kind > BS_ATROUS0 ? 4 : kind == BS_TEMPORAL ? 3 : ( kind == BS_GRADIENT || kind == BS_ANTI_FIREFLY ) ? 1 : 2;
+    return kind == BS_ATROUS0 ? 5 : kind > BS_ATROUS0 ? 4 : ( kind == BS_TEMPORAL || kind == BS_VARIANCE ) ? 3
+         : 1;
 }
 int max_candidates() { return 5; }
 void candidate( int kind, int c, int& shape, int& occ )
@@ -177,6 +178,11 @@ void candidate( int kind, int c, int& shape, int& occ )
     else if( kind == BS_TEMPORAL )
     {
         shape = c % 3 == 2 ? (int)RGDN_TILE_32X4 : c % 3;
+        occ   = c % 3 == 2 ? 7 : 0;
+    }
+    else if( kind == BS_VARIANCE )
+    {
+        shape = c % 3 == 2 ? (int)RGDN_TILE_32X8_PER_BLOCK : c % 3;
         occ   = c % 3 == 2 ? 7 : 0;
     }
     else
@@ -352,7 +358,7 @@ rgdn_status enqueue_step( rgdn_context* c, BatchExec& ex, DeviceSlots& ds, int s
     for( int k = 0; k < 3; k++ )
     {
         const int kind = BS_TEMPORAL + k;
-        const int arg  = k == 0 ? ( key.gpm << 8 ) | ( key.occ[ kind ] << 10 ) : 0;
+        const int arg  = k == 0 ? ( key.gpm << 8 ) | ( key.occ[ kind ] << 10 ) : ( key.occ[ kind ] << 10 );
         if( ( r = run( kind, stages[ k ], arg, key.shape[ kind ], key.occ[ kind ], tuneCand % n_candidates( kind ) ) ) != RGDN_SUCCESS )
             return r;
     }
@@ -637,7 +643,8 @@ rgdn_status batch_set_config( rgdn_context* c, uint32_t storage, const rgdn_batc
     // 32x4 (128-thread) tiles exist for the temporal and a-trous kernels only
     auto ok_shape = []( uint32_t v ) { return v <= RGDN_TILE_64X4; };
     auto ok_shape4 = []( uint32_t v ) { return v <= RGDN_TILE_32X4; };
-    if( !ok_shape4( in->temporalTile ) || !ok_shape( in->antiFireflyTile ) || !ok_shape( in->varianceTile ) )
+    if( !ok_shape4( in->temporalTile ) || !ok_shape( in->antiFireflyTile ) ||
+        !( ok_shape( in->varianceTile ) || in->varianceTile == RGDN_TILE_32X8_PER_BLOCK ) )
         return RGDN_WRONG_FUNCTION_ARGUMENT;
     for( int i = 0; i < MAX_ATROUS_ITERATIONS; i++ )
     {
@@ -654,6 +661,7 @@ rgdn_status batch_set_config( rgdn_context* c, uint32_t storage, const rgdn_batc
     cf.occ[ BS_TEMPORAL ]       = in->temporalTile == RGDN_TILE_32X4 ? 7 : 0;
     cf.shape[ BS_ANTI_FIREFLY ] = 0;   // the shared-memory tile is 32x8
     cf.shape[ BS_VARIANCE ]     = (int)in->varianceTile;
+    cf.occ[ BS_VARIANCE ]       = in->varianceTile == RGDN_TILE_32X8_PER_BLOCK ? 7 : 0;
     for( int i = 0; i < MAX_ATROUS_ITERATIONS; i++ )
     {
         cf.shape[ BS_ATROUS0 + i ] = (int)in->atrousTile[ i ];

@@ -2217,12 +2217,11 @@ __device__ __forceinline__ AtrousOut atrous_sm_px( const FrameArgs& a, const int
 // The block stages iteration 0's sources over its 32 x 8 tile widened by 3 (1 for iteration 0's
 // taps, 2 for iteration 1's), computes iteration 0 over the tile widened by 2, keeps those
 // results in shared memory exactly as they would be stored and read back (the storage mode's
-// quantisation), and then computes iteration 1 (step 2) over the tile. Iteration 0's persistent
-// outputs (DiffColorHistory, the prefiltered variance) are written for the tile's own pixels;
-// its specular and indirect results, which only iteration 1 reads, never leave the chip, nor do
-// iteration 1's sources. The arithmetic is the single-iteration kernels', so the planes are the
-// same bit for bit. The extra cost is iteration 0 over (36 x 12) / (32 x 8) = 1.69 times the
-// tile's pixels.
+// quantisation), and then computes iteration 1 (step 2) over the tile. Iteration 0's images are
+// written for the tile's own pixels, but iteration 1 reads none of them back: its sources never
+// leave the chip. The arithmetic is the single-iteration kernels', so the planes are the same
+// bit for bit. The extra cost is iteration 0 over (36 x 12) / (32 x 8) = 1.69 times the tile's
+// pixels.
 // ==========================================================================================
 struct AtPair
 {
@@ -2306,9 +2305,15 @@ __device__ __forceinline__ void atrous_pair_tile( const FrameArgs& a, const int 
                                                                             S::ld4( a.histLen, (size_t)i ).z );
                 if( own )
                 {
-                    // iteration 0's persistent outputs, for the tile's own pixels
+                    // iteration 0's images, for the tile's own pixels: DiffColorHistory and the
+                    // prefiltered variance, which later passes read, and the specular / indirect
+                    // pong images (iteration 1 takes them from shared memory, but with three
+                    // iterations nothing overwrites them, so the frame's planes stay the
+                    // single launches')
                     if( o.pref ) S::st1( a.filtVar, (size_t)i, o.prefVar );
                     S::stcv( io0.diffDst, io0.varDst, (size_t)i, o.d, o.var );
+                    S::st3( io0.specDst, (size_t)i, o.s );
+                    S::st3( io0.indirDst, (size_t)i, o.i );
                     tP[ ( r - 2 ) * P::TW + c - 2 ] = o.pref ? stored_1< M >( o.prefVar ) : 0.0f;
                 }
                 vc = stored_cv< M >( o.d, o.var );
@@ -2891,6 +2896,18 @@ template< int M > __global__ void __launch_bounds__( 256, 5 ) kb_variance( const
     pdl_wait();
     batch_tiles< false >( slot, BS_VARIANCE, [ & ]( const FrameArgs& a, int, int bx, int by ) { variance_geo_tile< M, true >( a, bx, by ); } );
     pdl_launch_dependents();
+}
+
+// Variance with one 32 x 8 tile of the step's table per block, built for 8 blocks per SM as the
+// single-frame kernel (the block finds its job by a search of the tile table)
+template< int M > __global__ void __launch_bounds__( 256, 8 ) kt_variance( const int slot )
+{
+    pdl_launch_dependents();
+    int        j = 0, bx = 0, by = 0;
+    const bool has = batch_tile_of_block< false >( slot, BS_VARIANCE, j, bx, by );
+    pdl_wait();
+    if( !has ) return;
+    variance_geo_tile< M, true >( c_batch[ slot ].jobs[ j ], bx, by );
 }
 
 // A-trous iteration `iter` over the jobs that run it. A job's last iteration composes PreFinal
@@ -3851,7 +3868,10 @@ template< int M > cudaError_t launch_batch_fast_t( int stage, int iter, int slot
     cudaError_t e = cudaSuccess;
     switch( stage )
     {
-        case RGDN_STAGE_VARIANCE_ESTIMATION: e = launch_pdl( dev::kb_variance< M >, grid, block, 0, s, slot ); break;
+        case RGDN_STAGE_VARIANCE_ESTIMATION:
+            e = ( ( iter >> 10 ) & 7 ) == 7 ? launch_pdl( dev::kt_variance< M >, grid, block, 0, s, slot )
+                                            : launch_pdl( dev::kb_variance< M >, grid, block, 0, s, slot );
+            break;
         case RGDN_STAGE_ATROUS:
         {
             const int hm = ( iter >> 8 ) & 3, occ = ( iter >> 10 ) & 7, it = iter & 0xff;

@@ -116,14 +116,16 @@ def test_batch_splits_steps_and_falls_back():
 @pytest.mark.parametrize("shape,occ,depth", [(0, 3, 1), (1, 4, 1), (2, 4, 1), (2, 3, 1), (0, 4, 1), (3, 7, 1), (0, 3, 2), (3, 7, 2)])
 def test_batch_fixed_configs(shape, occ, depth):
     """A configuration set through rgdn_batch_set_config (no tuning) gives the same results.
-    Shape 3 is the 128-thread 32x4 tile (temporal and a-trous; variance keeps 32x8). Fusion depth
+    Shape 3 is the 128-thread 32x4 tile (temporal and a-trous; variance then runs one 32x8 tile
+    per block). Fusion depth
     2 runs a-trous iterations 0 and 1 in one launch; the last frame has a stream running only
     two iterations, where the step falls back to one launch per iteration."""
     ctx = Context(0)
     cfg = N.BatchConfig()
     cfg.temporalTile = shape
     cfg.antiFireflyTile = 0
-    cfg.varianceTile = shape if shape != N.TILE_32X4 else N.TILE_32X8
+    # the 128-thread configurations take the variance's one-tile-per-block form
+    cfg.varianceTile = shape if shape != N.TILE_32X4 else N.TILE_32X8_PER_BLOCK
     for i in range(6):
         cfg.atrousTile[i] = (shape + i) % 3 if shape != N.TILE_32X4 else N.TILE_32X4
         cfg.atrousBlocksPerSM[i] = occ
