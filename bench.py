@@ -71,6 +71,8 @@ def parse():
     ap.add_argument("--serve-hz", type=float, nargs="+", default=[60.0, 15.0, 10.0],
                     help="per-stream Poisson frame rates to serve (the configured 60 Hz first)")
     ap.add_argument("--serve-step-mpix", type=float, default=8.0, help="pixel bound of one serving step (Mpix)")
+    ap.add_argument("--serve-e2e-inflight", type=int, default=2,
+                    help="serving steps enqueued ahead of the GPU in the end-to-end run (host inputs)")
     ap.add_argument("--serve-inflight", type=int, default=1,
                     help="serving steps enqueued ahead of the GPU (1..3) with resident inputs; the e2e run "
                          "(host inputs) uses at least 2 so copies overlap the kernels")
@@ -607,7 +609,7 @@ def run_serving(args, dist: Dist, dev: int) -> dict:
     out_host = {r: torch.empty(r[0] * r[1] * 8, dtype=torch.uint8).pin_memory() for r in SERVE_RES}
 
     def serve(hz: float, e2e: bool) -> dict:
-        inflight = max(2, args.serve_inflight) if e2e else args.serve_inflight
+        inflight = args.serve_e2e_inflight if e2e else args.serve_inflight
         sv = Server(ctx, storage, max_frames_per_step=32, max_pixels_per_step=int(args.serve_step_mpix * 1e6),
                     max_queued_per_stream=1, steps_in_flight=inflight)
         sids = [sv.open_stream(w, h) for w, h in res]
