@@ -1027,6 +1027,16 @@ def run_ours(args, dist: Dist):
         "gbuffer_bytes_per_frame": int(gbytes_per_frame),
         "batched": batched,
         "serving": serving,
+        # the metric's own quantity: the served / batched forms against the plain path, at p99
+        "served_batched": None if not (batched and serving) else {
+            "batched_mpix_s": batched["value"], "batched_p99_step_ms": batched["p99_ms"],
+            "batched_vs_plain_path": batched["vs_plain"],
+            "batched_vs_one_frame_per_launch": batched["vs_one_frame_per_launch"],
+            "served_mpix_s_configured_rate": serving["runs"][0]["value"],
+            "served_p99_all_requests_ms_configured_rate": serving["runs"][0]["p99_all_requests_ms"],
+            "served_drop_rate_configured_rate": serving["runs"][0]["drop_rate"],
+            "served_p99_ms_1080p_lowest_rate": serving["runs"][-1]["p99_ms_1080p"],
+            "plain_path_mpix_s": batched["plain_path_mpix_s"]},
     }
     print(json.dumps(line), flush=True)
 
