@@ -71,6 +71,14 @@ def parse():
     ap.add_argument("--serve-hz", type=float, nargs="+", default=[60.0, 15.0, 10.0],
                     help="per-stream Poisson frame rates to serve (the configured 60 Hz first)")
     ap.add_argument("--serve-step-mpix", type=float, default=8.0, help="pixel bound of one serving step (Mpix)")
+    ap.add_argument("--serve-e2e-repeats", type=int, default=1,
+                    help="end-to-end serving runs back to back in the process (the first is the line's)")
+    ap.add_argument("--serve-keep-pins", action="store_true",
+                    help="end-to-end serving from the host buffers pinned at start-up, not fresh pinned "
+                         "copies made right before each run (pinned buffers that have aged for tens of "
+                         "seconds showed 30-50 ms host-to-device copy stalls on the GB300 boxes)")
+    ap.add_argument("--serve-device-rates", type=int, default=1,
+                    help="0: skip the device-resident serving runs (with --serve-only)")
     ap.add_argument("--serve-e2e-inflight", type=int, default=2,
                     help="serving steps enqueued ahead of the GPU in the end-to-end run (host inputs)")
     ap.add_argument("--serve-inflight", type=int, default=1,
@@ -251,6 +259,52 @@ def kernel_groups(kern: list, steps: int) -> list:
                     "alg_bytes_per_launch": g["alg_bytes"] / g["launches"],
                     "gbs": g["alg_bytes"] / (g["us"] / 1e6) / 1e9})
     out.sort(key=lambda g: -g["us_per_step"])
+    return out
+
+
+def host_link_gbs(dev: int, nbytes: int = 1 << 30, reps: int = 4) -> dict:
+    """The host link's copy rates, measured live: one pinned buffer of `nbytes` copied host ->
+    device, device -> host, and both at once on two streams (each direction's rate), timed
+    with CUDA events after one untimed copy. These bound any end-to-end figure that moves a
+    frame's inputs and outputs across the link."""
+    import torch
+    h = torch.empty(nbytes, dtype=torch.uint8).pin_memory()
+    h2 = torch.empty(nbytes, dtype=torch.uint8).pin_memory()
+    d = torch.empty(nbytes, dtype=torch.uint8, device=f"cuda:{dev}")
+    d2 = torch.empty(nbytes, dtype=torch.uint8, device=f"cuda:{dev}")
+    s1, s2 = torch.cuda.Stream(device=dev), torch.cuda.Stream(device=dev)
+
+    def rate(fn) -> float:
+        fn()
+        torch.cuda.synchronize(dev)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(s1)
+        s2.wait_event(e0)
+        for _ in range(reps):
+            fn()
+        e2 = torch.cuda.Event()
+        e2.record(s2)
+        s1.wait_event(e2)
+        e1.record(s1)
+        e1.synchronize()
+        return round(nbytes * reps / (e0.elapsed_time(e1) * 1e-3) / 1e9, 1)
+
+    def up():
+        with torch.cuda.stream(s1):
+            d.copy_(h, non_blocking=True)
+
+    def down():
+        with torch.cuda.stream(s1):
+            h2.copy_(d2, non_blocking=True)
+
+    def both():
+        with torch.cuda.stream(s1):
+            d.copy_(h, non_blocking=True)
+        with torch.cuda.stream(s2):
+            h2.copy_(d2, non_blocking=True)
+
+    out = {"h2d_gbs": rate(up), "d2h_gbs": rate(down), "bidirectional_each_way_gbs": rate(both)}
+    del h, h2, d, d2
     return out
 
 
@@ -479,7 +533,7 @@ def run_batched(args, dist: Dist, dev: int, cs) -> dict:
 
     k = 0
     with torch.cuda.stream(cs):
-        for _ in range(24):          # autotuning (15 steps) + graph capture
+        for _ in range(28):          # autotuning (15 + 8 steps) + graph capture
             batched(k)
             k += 1
     cs.synchronize()
@@ -538,9 +592,12 @@ def run_batched(args, dist: Dist, dev: int, cs) -> dict:
         else:
             alg = per_px.get({"temporal_accumulation": "temporal_fast_gp", "anti_firefly": "anti_firefly_fast",
                               "variance_estimation": "variance_fast"}.get(name, name), 0.0) * px
-        kern.append({"kernel": f"batched_{name}[{it}]", "launches": n, "avg_us": round(1e3 * ms / n, 2),
-                     "alg_bytes": alg, "gbs": round(alg / (ms / n / 1e3) / 1e9, 1)})
-    kern.sort(key=lambda d: -d["avg_us"] * d["launches"])
+        # 3 timed steps; a step launches each kind once per group of frames
+        us_step = 1e3 * ms / 3
+        kern.append({"kernel": f"batched_{name}[{it}]", "launches_per_step": round(n / 3, 2),
+                     "us_per_step": round(us_step, 2), "us_per_mpix": round(us_step / (px / 1e6), 3),
+                     "alg_bytes_per_step": alg, "gbs": round(alg / (us_step / 1e6) / 1e9, 1)})
+    kern.sort(key=lambda d: -d["us_per_step"])
     out = {
         "workload": f"{len(streams)} streams: {args.batch_per_res} each of "
                     + ", ".join(f"{w}x{h}" for w, h in BATCH_MIX)
@@ -556,6 +613,7 @@ def run_batched(args, dist: Dist, dev: int, cs) -> dict:
                          "variance": int(cfg.varianceTile), "atrous": [int(v) for v in cfg.atrousTile][:args.iters],
                          "atrous_blocks_per_sm": [int(v) for v in cfg.atrousBlocksPerSM][:args.iters],
                          "atrous_fusion_depth": int(cfg.atrousFusionDepth),
+                         "group_pixels": int(cfg.groupPixels),
                          "graphs": int(cfg.useGraphs), "tile_names": ["32x8", "16x16", "64x4", "32x4", "32x8 per block"]},
         "kernels": kern,
     }
@@ -678,12 +736,60 @@ def run_serving(args, dist: Dist, dev: int) -> dict:
                 "queue_p50_ms": pct(queue, 0.5), "queue_p99_ms": pct(queue, 0.99),
                 "service_p50_ms": pct(service, 0.5), "service_p99_ms": pct(service, 0.99),
                 "feeder_late_p99_ms": pct(late, 0.99),
+                "step_parts_ms": {k: round(st[k], 3) for k in ("issueP50Ms", "issueP99Ms", "copyInP50Ms", "copyInP99Ms",
+                                                               "kernelsP50Ms", "kernelsP99Ms", "copyOutP50Ms", "copyOutP99Ms")},
                 "mean_frames_per_step": round(st["meanFramesPerStep"], 2), "steps": int(st["steps"]),
                 "gpu_busy_frac": round(st["busySeconds"] / elapsed, 3),
                 "resident_gb": round(st["residentBytes"] / 1e9, 2)}
 
-    runs = [serve(hz, False) for hz in args.serve_hz]
-    e2e = serve(args.serve_hz[-1], True)
+    runs = [serve(hz, False) for hz in args.serve_hz] if args.serve_device_rates else []
+
+    def frames_h2d_gbs() -> float:
+        """Host -> device rate of the requests' own pinned G-buffers (every plane of every
+        frame once)."""
+        dst = {r: torch.empty(max(t.numel() for t in host[r][0][0].values()), dtype=torch.uint8, device=f"cuda:{dev}")
+               for r in SERVE_RES}
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        nb = 0
+        torch.cuda.synchronize(dev)
+        e0.record()
+        for r in SERVE_RES:
+            for b, _ in host[r]:
+                for t in b.values():
+                    dst[r][:t.numel()].copy_(t, non_blocking=True)
+                    nb += t.numel()
+        e1.record()
+        e1.synchronize()
+        return round(nb / (e0.elapsed_time(e1) * 1e-3) / 1e9, 1)
+
+    # the e2e run moves every frame across the host link: the link's rates, the rate of the
+    # requests' own buffers and the host's load are recorded on both sides of each run
+    e2e_runs, kept = [], []
+    for _ in range(max(1, args.serve_e2e_repeats)):
+        if not args.serve_keep_pins:
+            # the old buffers stay referenced, so the new ones are new pinned allocations
+            kept.append(dict(host))
+            for r in SERVE_RES:
+                host[r] = [({n: t.clone().pin_memory() for n, t in b.items()}, p) for b, p in host[r]]
+        before = dict(host_link_gbs(dev, 1 << 29, 3), frames_h2d_gbs=frames_h2d_gbs(), loadavg=os.getloadavg()[0])
+        clk = ClockSampler(dev)
+        clk.start()
+        r = serve(args.serve_hz[-1], True)
+        r["clocks"] = clk.stop()
+        r["host_link_before"] = before
+        r["host_link_after"] = dict(host_link_gbs(dev, 1 << 29, 3), frames_h2d_gbs=frames_h2d_gbs(), loadavg=os.getloadavg()[0])
+        e2e_runs.append(r)
+    e2e = e2e_runs[0]
+    e2e["host_buffers"] = ("pinned at start-up" if args.serve_keep_pins
+                           else "fresh pinned copies made right before the run")
+    if len(e2e_runs) > 1:
+        e2e["repeats"] = [{k: r[k] for k in ("p50_ms", "p99_ms", "p99_all_requests_ms", "drop_rate", "queue_p99_ms",
+                                              "service_p50_ms", "service_p99_ms", "gpu_busy_frac", "host_link_before",
+                                              "step_parts_ms", "mean_frames_per_step", "clocks")}
+                          for r in e2e_runs[1:]]
+    W0, H0 = SERVE_RES[0]
+    bpp = sum(t.numel() for t in host[(W0, H0)][0][0].values()) / (W0 * H0)
+    e2e["h2d_gb_s_offered"] = round(e2e["offered_mpix_s"] * 1e6 * bpp / 1e9, 1)
     ctx.close()
     return {"workload": "64 camera streams, resolutions drawn uniformly from 1280x720 / 1920x1080 / 2560x1440 "
                         "(seeded), per-stream Poisson arrivals, fp16 storage, 120 GB admission budget, "
@@ -967,6 +1073,10 @@ def run_ours(args, dist: Dist):
     cs.synchronize()
     e2e_s = dist.max(time.perf_counter() - t0)
     e2e_value = W * H * args.e2e_steps * dist.world / e2e_s / 1e6
+    # the host link's own rates: a frame cannot finish faster than its upload at the link's
+    # host -> device rate, so W H / (h2d bytes / rate) is the end-to-end roofline
+    link = host_link_gbs(dev)
+    link_bound = W * H * dist.world / (h2d / (link["h2d_gbs"] * 1e9)) / 1e6
     for name in N.GBUFFER:
         st.bind(name, 0, None)
         st.bind(name, 1, None)
@@ -1020,7 +1130,9 @@ def run_ours(args, dist: Dist):
                         "memory; wall clock over all steps after a final synchronize",
                 "synchronous_mpix_s": round(W * H * args.e2e_steps * dist.world / e2e_sync_s / 1e6, 2),
                 "synchronous_p50_ms": round(1e3 * lat[len(lat) // 2], 3),
-                "synchronous_p99_ms": round(1e3 * lat[int(0.99 * (len(lat) - 1))], 3)},
+                "synchronous_p99_ms": round(1e3 * lat[int(0.99 * (len(lat) - 1))], 3),
+                "host_link": link, "link_bound_mpix_s": round(link_bound, 1),
+                "link_frac": round(e2e_value / link_bound, 4)},
         "clocks": clk,
         "cpu_baseline": cpu,
         "parity": parity,

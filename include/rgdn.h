@@ -495,9 +495,11 @@ rgdn_status rgdn_submit_batch( rgdn_context* ctx, const rgdn_job* jobs, uint32_t
 #define RGDN_TILE_32X4  3u
 #define RGDN_TILE_32X8_PER_BLOCK 4u   /* variance: one 32x8 tile per 256-thread block */
 /* The launch configuration of batched steps for one storage mode. The autotuner starts from
- * 32x8 tiles everywhere and, over the first 12 steps, times every candidate of every launch
- * (tile shape; for a-trous also the register budget) on the work being submitted (candidates
- * give identical results), then keeps the fastest and switches to graph replay. */
+ * 32x8 tiles everywhere and, over the first 15 steps, times every candidate of every launch
+ * (tile shape; for a-trous also the register budget and the fusion depth) on the work being
+ * submitted, keeps the fastest, then times 8 whole steps at each candidate group size
+ * (groupPixels) and keeps the fastest; then steps switch to graph replay. Candidates give
+ * identical results. */
 typedef struct rgdn_batch_config
 {
     uint32_t temporalTile;        /* RGDN_TILE_* */
@@ -513,6 +515,11 @@ typedef struct rgdn_batch_config
                                      one launch (32x8 tiles, iteration 0 recomputed over the tile
                                      widened by 2) in steps whose frames all run 3 or more
                                      iterations; 0 = 1 */
+    uint64_t groupPixels;         /* the step's frames run in groups of consecutive frames of at
+                                     most this many pixels (a larger frame is a group of its own);
+                                     a group runs every stage before the next group starts, so the
+                                     planes one stage writes are still in L2 when the group's next
+                                     stage reads them. 0 = the whole step is one group */
 } rgdn_batch_config;
 rgdn_status rgdn_batch_get_config( rgdn_context* ctx, uint32_t storage, rgdn_batch_config* outConfig );
 /* Fixes the configuration of a storage mode and ends its autotuning. */
@@ -582,6 +589,13 @@ typedef struct rgdn_server_stats
     float    p99AllMs;                /* p99 over every finished request, a dropped one counting as
                                          an unbounded latency (+infinity once drops pass 1 %) */
     float    dropRate;                /* framesDropped / (framesDone + framesDropped) */
+    /* one step's parts, p50 and p99 over the steps done since the last reset: the host time to
+     * enqueue it (plane copies, tables, launches), then on the device the G-buffer copies in,
+     * the kernels and the PRE_FINAL copies out (CUDA events on the step's stream) */
+    float    issueP50Ms, issueP99Ms;
+    float    copyInP50Ms, copyInP99Ms;
+    float    kernelsP50Ms, kernelsP99Ms;
+    float    copyOutP50Ms, copyOutP99Ms;
 } rgdn_server_stats;
 
 rgdn_status rgdn_server_create( rgdn_context* ctx, const rgdn_server_create_info* info, rgdn_server** outServer );
@@ -637,7 +651,10 @@ typedef struct rgdn_stage_timing
 rgdn_status rgdn_stream_set_timing( rgdn_stream* stream, uint32_t enable );
 rgdn_status rgdn_stream_read_timing( rgdn_stream* stream, rgdn_stage_timing* out, uint32_t capacity, uint32_t* outCount );
 /* Per-launch device timing of batched steps (as rgdn_stream_set_timing; stage ids are
- * rgdn_stage, totals per (stage, iteration)). Timed steps use direct launches, not graphs. */
+ * rgdn_stage, totals per (stage, iteration)). Timed steps use direct launches, not graphs.
+ * A group of one frame (rgdn_batch_config.groupPixels) runs on the single-frame kernels and is
+ * timed as a whole under the id RGDN_BATCH_SINGLE_FRAME_GROUP. */
+#define RGDN_BATCH_SINGLE_FRAME_GROUP 200u
 rgdn_status rgdn_batch_set_timing( rgdn_context* ctx, uint32_t enable );
 rgdn_status rgdn_batch_read_timing( rgdn_context* ctx, rgdn_stage_timing* out, uint32_t capacity, uint32_t* outCount );
 

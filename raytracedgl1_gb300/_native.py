@@ -166,7 +166,7 @@ class BatchConfig(C.Structure):
     _fields_ = [("temporalTile", C.c_uint32), ("antiFireflyTile", C.c_uint32),
                 ("varianceTile", C.c_uint32), ("atrousTile", C.c_uint32 * 6),
                 ("atrousBlocksPerSM", C.c_uint32 * 6), ("useGraphs", C.c_uint32), ("tuned", C.c_uint32),
-                ("atrousFusionDepth", C.c_uint32)]
+                ("atrousFusionDepth", C.c_uint32), ("groupPixels", C.c_uint64)]
 
 
 TILE_32X8, TILE_16X16, TILE_64X4, TILE_32X4, TILE_32X8_PER_BLOCK = 0, 1, 2, 3, 4
@@ -196,7 +196,9 @@ class ServerStats(C.Structure):
                 ("pixelsDone", C.c_uint64), ("residentStreams", C.c_uint32), ("queuedFrames", C.c_uint32),
                 ("residentBytes", C.c_uint64), ("p50Ms", C.c_float), ("p99Ms", C.c_float), ("maxMs", C.c_float),
                 ("meanFramesPerStep", C.c_float), ("busySeconds", C.c_double), ("p99AllMs", C.c_float),
-                ("dropRate", C.c_float)]
+                ("dropRate", C.c_float), ("issueP50Ms", C.c_float), ("issueP99Ms", C.c_float),
+                ("copyInP50Ms", C.c_float), ("copyInP99Ms", C.c_float), ("kernelsP50Ms", C.c_float),
+                ("kernelsP99Ms", C.c_float), ("copyOutP50Ms", C.c_float), ("copyOutP99Ms", C.c_float)]
 
 
 class Job(C.Structure):
@@ -263,7 +265,7 @@ KERNEL_NAMES.update({100: "atrous_fast", 101: "atrous_fast_hist", 102: "temporal
                      107: "atrous_exact", 108: "temporal_exact_geom", 109: "variance_exact_geom",
                      110: "temporal_fast_gp", 111: "temporal_exact_geom_gp", 112: "atrous_tma",
                      113: "atrous_tma_hist", 114: "prepare_final", 115: "bloom",
-                     117: "process_scattering", 122: "atrous_pair"})
+                     117: "process_scattering", 122: "atrous_pair", 200: "single_frame_group"})
 
 _lib = None
 

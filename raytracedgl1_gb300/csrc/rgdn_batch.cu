@@ -20,10 +20,20 @@
 // are a per-device resource shared by every context of the process; steps take them in turn,
 // and a step waits on the host until the slot's previous step has finished.
 //
-// Autotuning: the first 12 steps of a storage mode time every candidate tile shape (and, for
-// the a-trous kernel, two register budgets) per launch on the frames being submitted. Candidates
-// compute identical values per pixel, so tuning changes no result. Then the fastest candidate
-// per launch is kept and steps switch to graph replay.
+// Groups: the step's frames run in groups of consecutive frames of at most groupPixels pixels,
+// each group through every stage before the next group starts. A group of one frame runs on the
+// single-frame kernels, whose frame arguments are kernel parameters: read from the constant
+// table with a job index known only at run time, the same fields cost the batched kernels
+// registers (the batched a-trous and variance builds spill 2-7 times the bytes of the
+// single-frame ones) and their large frames ran 5-13 % slower per pixel. A step with such a
+// group is launched directly rather than replayed from a graph, since that group's parameters
+// change every step; at a frame of a million pixels or more the launches stay ahead of the GPU.
+//
+// Autotuning: the first 15 steps of a storage mode time every candidate tile shape (and, for
+// the a-trous kernel, the register budget and the fusion depth) per launch on the frames being
+// submitted; the fastest candidate per launch is kept. The next 8 steps time whole steps at each
+// candidate group size and keep the fastest. Candidates compute identical values per pixel, so
+// tuning changes no result. Then steps switch to graph replay.
 #include <algorithm>
 #include <cstddef>
 #include <cstring>
@@ -46,14 +56,21 @@ const dim3    kShapes[ 5 ] = { dim3( 32, 8 ), dim3( 16, 16 ), dim3( 64, 4 ), dim
 
 size_t table_bytes( int n ) { return offsetof( BatchConst, jobs ) + sizeof( FrameArgs ) * (size_t)n; }
 
-// the launch sequence of a step: what a captured graph depends on
+// the launch sequence of one group of a step's frames (jobs [j0, j1) of the table)
+struct GroupKey
+{
+    int j0, j1, single, anyGrad, maxIter, gpm;   // single: one frame, on the single-frame kernels
+    int hm[ MAX_ATROUS_ITERATIONS ];
+    int tiles[ BS_COUNT ];   // the grid of one-tile-per-block launches (occ 7, pair), else 0
+};
+// the launch sequence of a step: what a captured graph depends on (zero-filled before it is
+// set, so that memcmp compares it)
 struct GraphKey
 {
-    int storage, anyGrad, maxIter, gpm;
-    int hm[ MAX_ATROUS_ITERATIONS ];
-    int shape[ BS_COUNT ];
-    int occ[ BS_COUNT ];
-    int tiles[ BS_COUNT ];   // the grid of one-tile-per-block launches (occ 7), else 0
+    int      storage, ng;
+    int      shape[ BS_COUNT ];
+    int      occ[ BS_COUNT ];
+    GroupKey g[ MAX_BATCH ];
 };
 bool same_key( const GraphKey& a, const GraphKey& b ) { return memcmp( &a, &b, sizeof( GraphKey ) ) == 0; }
 
@@ -130,11 +147,13 @@ bool slots_ready( DeviceSlots& ds )
 
 struct Config
 {
-    int  shape[ BS_COUNT ];   // index into kShapes (BS_GRADIENT stays 32x8)
-    int  occ[ BS_COUNT ];     // a-trous kinds: resident blocks per SM the kernel is built for (3, 4)
-    bool graphs;
+    int      shape[ BS_COUNT ];   // index into kShapes (BS_GRADIENT stays 32x8)
+    int      occ[ BS_COUNT ];     // a-trous kinds: resident blocks per SM the kernel is built for (3, 4)
+    bool     graphs;
+    uint64_t groupPixels;         // 0 = one group per step
 };
 
+// kind -2: a whole step (the group-size phase)
 struct Probe
 {
     int         kind, cand;
@@ -143,10 +162,16 @@ struct Probe
     bool        scored;
 };
 
+// Group sizes the second tuning phase times, as whole steps: one group, then about two 2560x1440
+// frames, one, and one 1920x1080 frame. Phase 1 runs kGroupRounds passes (the first not scored).
+const uint64_t kGroupCand[ 4 ] = { 0ull, 8ull << 20, 4ull << 20, 2ull << 20 };
+constexpr int  kGroupRounds    = 2;
+
 struct Tuner
 {
     bool                 settled = false;
-    int                  step    = 0;
+    int                  phase   = 0;   // 0: launch candidates, 1: group sizes
+    int                  step    = 0;   // tuning steps taken in the phase
     std::vector< Probe > probes;
 };
 
@@ -256,7 +281,8 @@ BatchExec* create_exec( int device )
             ex->cfg[ s ].shape[ k ] = 0;
             ex->cfg[ s ].occ[ k ]   = k >= BS_ATROUS0 ? 3 : 0;
         }
-        ex->cfg[ s ].graphs = true;
+        ex->cfg[ s ].graphs      = true;
+        ex->cfg[ s ].groupPixels = kGroupCand[ 2 ];
         for( int st = 0; st < RGDN_STAGE_COUNT; st++ )
             for( int o = 0; o < 8; o++ ) ex->bps[ s ][ st ][ o ] = -1;
     }
@@ -296,9 +322,10 @@ void batch_exec_free( BatchExec* ex )
 namespace
 {
 
-// Enqueues the step's table copies and launches on `cs` (the captured stream when capturing).
-rgdn_status enqueue_step( rgdn_context* c, BatchExec& ex, DeviceSlots& ds, int slot, const GraphKey& key, int n, const double* pixels,
-                          int tuneCand, cudaStream_t cs, bool capturing )
+// Enqueues the step's table copies and launches on `cs` (the captured stream when capturing):
+// the stage sequence once per group. pixels[g][kind]: the pixels of group g's launch of a kind.
+rgdn_status enqueue_step( rgdn_context* c, BatchExec& ex, DeviceSlots& ds, int slot, const GraphKey& key, const rgdn_job* jobs,
+                          const double ( *pixels )[ BS_COUNT ], int n, int tuneCand, cudaStream_t cs, bool capturing )
 {
     const uint32_t st    = (uint32_t)key.storage;
     const size_t   bytes = capturing ? sizeof( BatchConst ) : table_bytes( n );
@@ -306,95 +333,150 @@ rgdn_status enqueue_step( rgdn_context* c, BatchExec& ex, DeviceSlots& ds, int s
         cudaMemcpyAsync( ds.fast[ st ][ slot ], ds.host[ slot ], bytes, cudaMemcpyHostToDevice, cs ) != cudaSuccess )
         return RGDN_DEVICE_ERROR;
     Tuner&     tu     = ex.tuner[ st ];
-    const bool tuning = !capturing && !tu.settled;
+    const bool tuning = !capturing && !tu.settled && tu.phase == 0;
     const bool user   = !capturing && ex.timing;
 
-    auto run = [ & ]( int kind, int stage, int arg, int shape, int occ, int cand ) -> rgdn_status {
-        BatchLauncher L = batch_launcher( st, stage );
-        if( !L ) return RGDN_INTERNAL_ERROR;
-        // persistent launches: resident blocks per SM x SMs; one-tile-per-block launches: the tiles
-        const int grid = stage == RGDN_STAGE_LUMINANCE_AVG ? MAX_BATCH
-                       : ( occ == 7 || occ == kOccPair )   ? key.tiles[ kind ]
-                                                           : blocks_per_sm( ex, st, stage, occ ) * ex.sms;
-        if( grid <= 0 ) return RGDN_DEVICE_ERROR;
-        cudaEvent_t ta = nullptr, tb = nullptr, ua = nullptr, ub = nullptr;
-        if( tuning && kind >= 0 )
+    for( int gi = 0; gi < key.ng; gi++ )
+    {
+        const GroupKey& gk = key.g[ gi ];
+        if( gk.single )
         {
-            ta = take_event( ex );
-            tb = take_event( ex );
-            if( !ta || !tb ) return RGDN_DEVICE_ERROR;
-            cudaEventRecord( ta, cs );
+            // one frame: the single-frame kernels, with its arguments as kernel parameters
+            const rgdn_job& jb = jobs[ gk.j0 ];
+            cudaEvent_t     ua = nullptr, ub = nullptr;
+            if( user )
+            {
+                ua = take_event( ex );
+                ub = take_event( ex );
+                if( !ua || !ub ) return RGDN_DEVICE_ERROR;
+                cudaEventRecord( ua, cs );
+            }
+            rgdn_status r = run_denoise( jb.stream, jb.frameIndex, jb.params, cs );
+            if( r == RGDN_SUCCESS ) r = run_exposure( jb.stream, jb.frameIndex, jb.params, cs );
+            if( user )
+            {
+                cudaEventRecord( ub, cs );
+                ex.pending.push_back( { (int)RGDN_BATCH_SINGLE_FRAME_GROUP, 0, ua, ub } );
+            }
+            if( r != RGDN_SUCCESS ) return r;
+            continue;
         }
-        if( user )
-        {
-            ua = take_event( ex );
-            ub = take_event( ex );
-            if( !ua || !ub ) return RGDN_DEVICE_ERROR;
-            cudaEventRecord( ua, cs );
-        }
-        const cudaError_t e = L( stage, arg, slot, kShapes[ shape ], grid, cs );
-        if( user )
-        {
-            cudaEventRecord( ub, cs );
-            ex.pending.push_back( { stage, arg & 0xff, ua, ub } );
-        }
-        if( ta )
-        {
-            cudaEventRecord( tb, cs );
-            tu.probes.push_back( { kind, cand, pixels[ kind ], ta, tb, tuneCand >= max_candidates() } );
-        }
-        if( !capturing ) c->launches.fetch_add( 1, std::memory_order_relaxed );
-        return cuda_status( e );
-    };
+        const int sarg = slot | ( gk.j0 << 8 ) | ( gk.j1 << 16 );
+        auto run = [ & ]( int kind, int stage, int arg, int shape, int occ, int cand ) -> rgdn_status {
+            BatchLauncher L = batch_launcher( st, stage );
+            if( !L ) return RGDN_INTERNAL_ERROR;
+            // persistent launches: resident blocks per SM x SMs; one-tile-per-block launches: the
+            // group's tiles; the luminance average: one block per frame
+            const int grid = stage == RGDN_STAGE_LUMINANCE_AVG ? gk.j1 - gk.j0
+                           : ( occ == 7 || occ == kOccPair )   ? gk.tiles[ kind ]
+                                                               : blocks_per_sm( ex, st, stage, occ ) * ex.sms;
+            if( grid <= 0 ) return RGDN_DEVICE_ERROR;
+            cudaEvent_t ta = nullptr, tb = nullptr, ua = nullptr, ub = nullptr;
+            if( tuning && kind >= 0 )
+            {
+                ta = take_event( ex );
+                tb = take_event( ex );
+                if( !ta || !tb ) return RGDN_DEVICE_ERROR;
+                cudaEventRecord( ta, cs );
+            }
+            if( user )
+            {
+                ua = take_event( ex );
+                ub = take_event( ex );
+                if( !ua || !ub ) return RGDN_DEVICE_ERROR;
+                cudaEventRecord( ua, cs );
+            }
+            const cudaError_t e = L( stage, arg, sarg, kShapes[ shape ], grid, cs );
+            if( user )
+            {
+                cudaEventRecord( ub, cs );
+                ex.pending.push_back( { stage, arg & 0xff, ua, ub } );
+            }
+            if( ta )
+            {
+                cudaEventRecord( tb, cs );
+                tu.probes.push_back( { kind, cand, pixels[ gi ][ kind ], ta, tb, tuneCand >= max_candidates() } );
+            }
+            if( !capturing ) c->launches.fetch_add( 1, std::memory_order_relaxed );
+            return cuda_status( e );
+        };
 
-    rgdn_status r;
-    if( key.anyGrad )
-    {
-        if( ( r = run( -1, RGDN_STAGE_GRADIENT_SAMPLES, 0, 0, 0, 0 ) ) != RGDN_SUCCESS ) return r;
-        for( int i = 0; i < 4; i++ )
-            if( ( r = run( -1, RGDN_STAGE_GRADIENT_ATROUS, i, 0, 0, 0 ) ) != RGDN_SUCCESS ) return r;
+        rgdn_status r;
+        if( gk.anyGrad )
+        {
+            if( ( r = run( -1, RGDN_STAGE_GRADIENT_SAMPLES, 0, 0, 0, 0 ) ) != RGDN_SUCCESS ) return r;
+            for( int i = 0; i < 4; i++ )
+                if( ( r = run( -1, RGDN_STAGE_GRADIENT_ATROUS, i, 0, 0, 0 ) ) != RGDN_SUCCESS ) return r;
+        }
+        const int stages[ 3 ] = { RGDN_STAGE_TEMPORAL_ACCUMULATION, RGDN_STAGE_ANTI_FIREFLY, RGDN_STAGE_VARIANCE_ESTIMATION };
+        for( int k = 0; k < 3; k++ )
+        {
+            const int kind = BS_TEMPORAL + k;
+            const int arg  = k == 0 ? ( gk.gpm << 8 ) | ( key.occ[ kind ] << 10 ) : ( key.occ[ kind ] << 10 );
+            if( ( r = run( kind, stages[ k ], arg, key.shape[ kind ], key.occ[ kind ], tuneCand % n_candidates( kind ) ) ) != RGDN_SUCCESS )
+                return r;
+        }
+        for( int i = 0; i < gk.maxIter; i++ )
+        {
+            const int kind = BS_ATROUS0 + i;
+            // fusion depth 2: the first launch ran iterations 0 and 1
+            if( i == 1 && key.occ[ BS_ATROUS0 ] == kOccPair ) continue;
+            const int arg = i | ( gk.hm[ i ] << 8 ) | ( key.occ[ kind ] << 10 );
+            if( ( r = run( kind, RGDN_STAGE_ATROUS, arg, key.shape[ kind ], key.occ[ kind ], tuneCand % n_candidates( kind ) ) ) !=
+                RGDN_SUCCESS )
+                return r;
+        }
+        if( ( r = run( -1, RGDN_STAGE_LUMINANCE_AVG, 0, 0, 0, 0 ) ) != RGDN_SUCCESS ) return r;
     }
-    const int stages[ 3 ] = { RGDN_STAGE_TEMPORAL_ACCUMULATION, RGDN_STAGE_ANTI_FIREFLY, RGDN_STAGE_VARIANCE_ESTIMATION };
-    for( int k = 0; k < 3; k++ )
-    {
-        const int kind = BS_TEMPORAL + k;
-        const int arg  = k == 0 ? ( key.gpm << 8 ) | ( key.occ[ kind ] << 10 ) : ( key.occ[ kind ] << 10 );
-        if( ( r = run( kind, stages[ k ], arg, key.shape[ kind ], key.occ[ kind ], tuneCand % n_candidates( kind ) ) ) != RGDN_SUCCESS )
-            return r;
-    }
-    for( int i = 0; i < key.maxIter; i++ )
-    {
-        const int kind = BS_ATROUS0 + i;
-        // fusion depth 2: the first launch ran iterations 0 and 1
-        if( i == 1 && key.occ[ BS_ATROUS0 ] == kOccPair ) continue;
-        const int arg  = i | ( key.hm[ i ] << 8 ) | ( key.occ[ kind ] << 10 );
-        if( ( r = run( kind, RGDN_STAGE_ATROUS, arg, key.shape[ kind ], key.occ[ kind ], tuneCand % n_candidates( kind ) ) ) != RGDN_SUCCESS )
-            return r;
-    }
-    return run( -1, RGDN_STAGE_LUMINANCE_AVG, 0, 0, 0, 0 );
+    return RGDN_SUCCESS;
 }
 
-int kernels_in( const GraphKey& key ) { return ( key.anyGrad ? 5 : 0 ) + 3 + key.maxIter + 1; }
-
-// Picks the fastest candidate of every launch kind from the tuning steps' probes.
-rgdn_status settle( BatchExec& ex, uint32_t st )
+int kernels_in( const GraphKey& key )
 {
-    Tuner&                tu = ex.tuner[ st ];
-    std::vector< double > best( BS_COUNT * max_candidates(), 1e30 );
-    rgdn_status           r = RGDN_SUCCESS;
+    int k = 0;
+    for( int gi = 0; gi < key.ng; gi++ )
+    {
+        const GroupKey& gk = key.g[ gi ];
+        k += ( gk.anyGrad ? 5 : 0 ) + 3 + gk.maxIter - ( key.occ[ BS_ATROUS0 ] == kOccPair && gk.maxIter >= 2 ? 1 : 0 ) + 1;
+    }
+    return k;
+}
+
+// Sums the scored probes' device time and pixels by kind * stride + candidate (kind -2, a whole
+// step: by candidate) and returns their events to the pool.
+rgdn_status collect_probes( BatchExec& ex, Tuner& tu, std::vector< double >& ms, std::vector< double >& px, int stride )
+{
+    rgdn_status r = RGDN_SUCCESS;
     for( auto& p : tu.probes )
     {
-        float ms = 0.0f;
-        if( cudaEventSynchronize( p.b ) != cudaSuccess || cudaEventElapsedTime( &ms, p.a, p.b ) != cudaSuccess ) r = RGDN_DEVICE_ERROR;
+        float t = 0.0f;
+        if( cudaEventSynchronize( p.b ) != cudaSuccess || cudaEventElapsedTime( &t, p.a, p.b ) != cudaSuccess ) r = RGDN_DEVICE_ERROR;
         else if( p.scored && p.pixels > 0.0 )
         {
-            double& b = best[ p.kind * max_candidates() + p.cand ];
-            b         = std::min( b, (double)ms / p.pixels );
+            const size_t k = (size_t)( p.kind < 0 ? 0 : p.kind * stride ) + (size_t)p.cand;
+            if( k < ms.size() )
+            {
+                ms[ k ] += t;
+                px[ k ] += p.pixels;
+            }
         }
         ex.eventPool.push_back( p.a );
         ex.eventPool.push_back( p.b );
     }
     tu.probes.clear();
+    return r;
+}
+
+// Picks the fastest candidate of every launch kind from the tuning steps' probes.
+rgdn_status settle( BatchExec& ex, uint32_t st )
+{
+    Tuner&                tu = ex.tuner[ st ];
+    std::vector< double > ms( BS_COUNT * max_candidates(), 0.0 ), px( BS_COUNT * max_candidates(), 0.0 );
+    rgdn_status           r = collect_probes( ex, tu, ms, px, max_candidates() );
+    // time per pixel of each (kind, candidate) over its scored launches (all groups, all rounds)
+    std::vector< double > best( BS_COUNT * max_candidates(), 1e30 );
+    for( size_t k = 0; k < best.size(); k++ )
+        if( px[ k ] > 0.0 ) best[ k ] = ms[ k ] / px[ k ];
     int bestOf[ BS_COUNT ] = {};
     for( int kind = BS_TEMPORAL; kind < BS_COUNT; kind++ )
     {
@@ -413,6 +495,22 @@ rgdn_status settle( BatchExec& ex, uint32_t st )
     const double sep  = best[ BS_ATROUS0 * max_candidates() + bestOf[ BS_ATROUS0 ] ] +
                        best[ ( BS_ATROUS0 + 1 ) * max_candidates() + bestOf[ BS_ATROUS0 + 1 ] ];
     if( pair < 1e30 && sep < 1e30 && pair < sep ) candidate( BS_ATROUS0, 4, ex.cfg[ st ].shape[ BS_ATROUS0 ], ex.cfg[ st ].occ[ BS_ATROUS0 ] );
+    // next: the group sizes, as whole steps
+    tu.phase = 1;
+    tu.step  = 0;
+    return r;
+}
+
+// Picks the fastest group size from the whole-step probes of the second phase.
+rgdn_status settle_groups( BatchExec& ex, uint32_t st )
+{
+    Tuner&                tu = ex.tuner[ st ];
+    std::vector< double > ms( 4, 0.0 ), px( 4, 0.0 );
+    rgdn_status           r    = collect_probes( ex, tu, ms, px, 4 );
+    int                   best = -1;
+    for( int k = 0; k < 4; k++ )
+        if( px[ k ] > 0.0 && ( best < 0 || ms[ k ] / px[ k ] < ms[ best ] / px[ best ] ) ) best = k;
+    if( best >= 0 ) ex.cfg[ st ].groupPixels = kGroupCand[ best ];
     tu.settled = true;
     return r;
 }
@@ -438,12 +536,15 @@ rgdn_status run_step( rgdn_context* c, BatchExec& ex, const rgdn_job* jobs, int 
         if( cudaEventSynchronize( ds.done[ slot ] ) != cudaSuccess ) return RGDN_DEVICE_ERROR;
         ds.used[ slot ] = false;
     }
-    Tuner&     tu     = ex.tuner[ st ];
-    const bool tuning = !tu.settled;
-    int        tcand  = tu.step;
-    Config     cfg    = ex.cfg[ st ];
-    if( tuning )
+    Tuner&     tu      = ex.tuner[ st ];
+    const bool tuning  = !tu.settled;
+    const bool tuneLk  = tuning && tu.phase == 0;   // launch candidates
+    const bool tuneGrp = tuning && tu.phase == 1;   // group sizes
+    int        tcand   = tu.step;
+    Config     cfg     = ex.cfg[ st ];
+    if( tuneLk )
         for( int kind = BS_TEMPORAL; kind < BS_COUNT; kind++ ) candidate( kind, tcand % n_candidates( kind ), cfg.shape[ kind ], cfg.occ[ kind ] );
+    if( tuneGrp ) cfg.groupPixels = kGroupCand[ tcand % 4 ];
     // the fused first two iterations need every frame of the step to run at least three
     int minIter = MAX_ATROUS_ITERATIONS;
     for( int k = 0; k < n; k++ ) minIter = std::min( minIter, jobs[ k ].params->atrousIterations ? (int)jobs[ k ].params->atrousIterations : 4 );
@@ -451,7 +552,7 @@ rgdn_status run_step( rgdn_context* c, BatchExec& ex, const rgdn_job* jobs, int 
     {
         candidate( BS_ATROUS0, 0, cfg.shape[ BS_ATROUS0 ], cfg.occ[ BS_ATROUS0 ] );
         // not scored as the pair: this tuning step counts as a warm-up step
-        if( tuning ) tcand = tcand % max_candidates();
+        if( tuneLk ) tcand = tcand % max_candidates();
     }
 
     BatchConst* tab = ds.host[ slot ];
@@ -460,9 +561,43 @@ rgdn_status run_step( rgdn_context* c, BatchExec& ex, const rgdn_job* jobs, int 
     GraphKey key;
     memset( &key, 0, sizeof( key ) );
     key.storage = (int)st;
-    int gpValid = 0;
+    // groups: consecutive frames while their pixels stay within the group size
+    {
+        uint64_t acc = 0;
+        int      j0  = 0;
+        for( int k = 0; k < n; k++ )
+        {
+            const uint64_t px = (uint64_t)jobs[ k ].stream->W * jobs[ k ].stream->H;
+            if( k > j0 && cfg.groupPixels && acc + px > cfg.groupPixels )
+            {
+                key.g[ key.ng ].j0   = j0;
+                key.g[ key.ng++ ].j1 = k;
+                j0                   = k;
+                acc                  = 0;
+            }
+            acc += px;
+        }
+        key.g[ key.ng ].j0   = j0;
+        key.g[ key.ng++ ].j1 = n;
+    }
+    bool anySingle = false;
+    bool single[ MAX_BATCH ] = {};
+    for( int gi = 0; gi < key.ng; gi++ )
+        if( key.g[ gi ].j1 - key.g[ gi ].j0 == 1 )
+        {
+            key.g[ gi ].single       = 1;
+            single[ key.g[ gi ].j0 ] = true;
+            anySingle                = true;
+        }
     for( int k = 0; k < n; k++ )
     {
+        if( single[ k ] )
+        {
+            // the single-frame path fills its own arguments and keeps its stream's state
+            memset( &tab->jobs[ k ], 0, sizeof( FrameArgs ) );
+            tab->jobFlags[ k ] = 0;
+            continue;
+        }
         rgdn_stream*             s  = jobs[ k ].stream;
         const uint32_t           fi = jobs[ k ].frameIndex;
         const rgdn_frame_params* p  = jobs[ k ].params;
@@ -471,44 +606,61 @@ rgdn_status run_step( rgdn_context* c, BatchExec& ex, const rgdn_job* jobs, int 
         fill_args( s, fi, p, tab->jobs[ k ] );
         const bool gp      = s->geomValid[ fi ^ 1u ];
         tab->jobFlags[ k ] = ( gp ? BATCH_JOB_GEOM_PREV : 0u ) | ( s->histPending ? BATCH_JOB_CLEAR_HIST : 0u );
-        gpValid += gp ? 1 : 0;
         s->geomValid[ fi ] = true;
         s->histPending     = false;
-        key.maxIter        = std::max( key.maxIter, (int)tab->jobs[ k ].u.niter );
-        if( !( p->flags & RGDN_FLAG_SKIP_GRADIENTS ) ) key.anyGrad = 1;
     }
-    key.gpm = gpValid == 0 ? 0 : gpValid == n ? 1 : 2;
-    // tile tables and pixels per launch kind
-    double pixels[ BS_COUNT ] = {};
+    // tile tables (numbered over the whole step) and pixels per group and launch kind
+    double pixels[ MAX_BATCH ][ BS_COUNT ] = {};
+    double stepPixels                      = 0.0;
     for( int kind = 0; kind < BS_COUNT; kind++ )
     {
         const dim3 sh  = kind == BS_ANTI_FIREFLY ? dim3( 32, af_tile_rows( (int)st ) ) : kShapes[ kind == BS_GRADIENT ? 0 : cfg.shape[ kind ] ];
         int        acc = 0;
-        for( int k = 0; k < n; k++ )
+        for( int gi = 0; gi < key.ng; gi++ )
         {
-            tab->start[ kind ][ k ] = acc;
-            const Uniform& u        = tab->jobs[ k ].u;
-            bool           runs;
-            if( kind == BS_GRADIENT ) runs = !( u.flags & RGDN_FLAG_SKIP_GRADIENTS );
-            else if( kind >= BS_ATROUS0 ) runs = (int)u.niter > kind - BS_ATROUS0;
-            else runs = true;
-            if( !runs ) continue;
-            const int w = kind == BS_GRADIENT ? u.GW : u.W, h = kind == BS_GRADIENT ? u.GH : u.H;
-            acc += ceil_div( w, (int)sh.x ) * ceil_div( h, (int)sh.y );
-            pixels[ kind ] += (double)w * h;
+            GroupKey& gk = key.g[ gi ];
+            for( int k = gk.j0; k < gk.j1; k++ )
+            {
+                tab->start[ kind ][ k ] = acc;
+                const Uniform& u        = tab->jobs[ k ].u;
+                bool           runs;
+                if( single[ k ] ) runs = false;
+                else if( kind == BS_GRADIENT ) runs = !( u.flags & RGDN_FLAG_SKIP_GRADIENTS );
+                else if( kind >= BS_ATROUS0 ) runs = (int)u.niter > kind - BS_ATROUS0;
+                else runs = true;
+                if( !runs ) continue;
+                const int w = kind == BS_GRADIENT ? u.GW : u.W, h = kind == BS_GRADIENT ? u.GH : u.H;
+                acc += ceil_div( w, (int)sh.x ) * ceil_div( h, (int)sh.y );
+                pixels[ gi ][ kind ] += (double)w * h;
+            }
+            if( kind != BS_GRADIENT && ( cfg.occ[ kind ] == 7 || cfg.occ[ kind ] == kOccPair ) )
+                gk.tiles[ kind ] = acc - tab->start[ kind ][ gk.j0 ];
         }
         tab->start[ kind ][ n ] = acc;
-        if( kind != BS_GRADIENT && ( cfg.occ[ kind ] == 7 || cfg.occ[ kind ] == kOccPair ) ) key.tiles[ kind ] = acc;
     }
-    for( int i = 0; i < key.maxIter; i++ )
+    for( int k = 0; k < n; k++ ) stepPixels += (double)jobs[ k ].stream->W * jobs[ k ].stream->H;
+    for( int gi = 0; gi < key.ng; gi++ )
     {
-        int runs = 0, last = 0;
-        for( int k = 0; k < n; k++ )
+        GroupKey& gk      = key.g[ gi ];
+        int       gpValid = 0;
+        if( gk.single ) continue;
+        for( int k = gk.j0; k < gk.j1; k++ )
         {
-            if( (int)tab->jobs[ k ].u.niter > i ) runs++;
-            if( (int)tab->jobs[ k ].u.niter == i + 1 ) last++;
+            gpValid += ( tab->jobFlags[ k ] & BATCH_JOB_GEOM_PREV ) ? 1 : 0;
+            gk.maxIter = std::max( gk.maxIter, (int)tab->jobs[ k ].u.niter );
+            if( !( tab->jobs[ k ].u.flags & RGDN_FLAG_SKIP_GRADIENTS ) ) gk.anyGrad = 1;
         }
-        key.hm[ i ] = last == 0 ? 0 : last == runs ? 1 : 2;
+        gk.gpm = gpValid == 0 ? 0 : gpValid == gk.j1 - gk.j0 ? 1 : 2;
+        for( int i = 0; i < gk.maxIter; i++ )
+        {
+            int runs = 0, last = 0;
+            for( int k = gk.j0; k < gk.j1; k++ )
+            {
+                if( (int)tab->jobs[ k ].u.niter > i ) runs++;
+                if( (int)tab->jobs[ k ].u.niter == i + 1 ) last++;
+            }
+            gk.hm[ i ] = last == 0 ? 0 : last == runs ? 1 : 2;
+        }
     }
     for( int kind = 0; kind < BS_COUNT; kind++ )
     {
@@ -517,14 +669,16 @@ rgdn_status run_step( rgdn_context* c, BatchExec& ex, const rgdn_job* jobs, int 
     }
 
     rgdn_status r = RGDN_SUCCESS;
-    if( cfg.graphs && !tuning && !ex.timing )
+    // a step with a single-frame group is launched directly: that group's kernel parameters
+    // change every step
+    if( cfg.graphs && !tuning && !ex.timing && !anySingle )
     {
         cudaGraphExec_t& exec = ex.exec[ slot ];
         if( !exec || !same_key( ex.key[ slot ], key ) )
         {
             cudaGraph_t g = nullptr;
             if( cudaStreamBeginCapture( ex.capture, cudaStreamCaptureModeThreadLocal ) != cudaSuccess ) return RGDN_DEVICE_ERROR;
-            r             = enqueue_step( c, ex, ds, slot, key, n, pixels, 0, ex.capture, true );
+            r             = enqueue_step( c, ex, ds, slot, key, jobs, pixels, n, 0, ex.capture, true );
             cudaError_t e = cudaStreamEndCapture( ex.capture, &g );
             if( r == RGDN_SUCCESS && e != cudaSuccess ) r = RGDN_DEVICE_ERROR;
             if( r == RGDN_SUCCESS )
@@ -552,11 +706,27 @@ rgdn_status run_step( rgdn_context* c, BatchExec& ex, const rgdn_job* jobs, int 
         if( cudaGraphLaunch( exec, cs ) != cudaSuccess ) return RGDN_DEVICE_ERROR;
         c->launches.fetch_add( (uint64_t)kernels_in( key ), std::memory_order_relaxed );
     }
-    else if( ( r = enqueue_step( c, ex, ds, slot, key, n, pixels, tcand, cs, false ) ) != RGDN_SUCCESS )
-        return r;
+    else
+    {
+        cudaEvent_t ga = nullptr, gb = nullptr;
+        if( tuneGrp )
+        {
+            ga = take_event( ex );
+            gb = take_event( ex );
+            if( !ga || !gb ) return RGDN_DEVICE_ERROR;
+            cudaEventRecord( ga, cs );
+        }
+        if( ( r = enqueue_step( c, ex, ds, slot, key, jobs, pixels, n, tcand, cs, false ) ) != RGDN_SUCCESS ) return r;
+        if( ga )
+        {
+            cudaEventRecord( gb, cs );
+            tu.probes.push_back( { -2, tcand % 4, stepPixels, ga, gb, tcand >= 4 } );
+        }
+    }
     if( cudaEventRecord( ds.done[ slot ], cs ) != cudaSuccess ) return RGDN_DEVICE_ERROR;
     ds.used[ slot ] = true;
-    if( tuning && ++tu.step >= kTuneRounds * max_candidates() ) r = settle( ex, st );
+    if( tuneLk && ++tu.step >= kTuneRounds * max_candidates() ) r = settle( ex, st );
+    else if( tuneGrp && ++tu.step >= kGroupRounds * 4 ) r = settle_groups( ex, st );
     return r;
 }
 
@@ -633,8 +803,9 @@ rgdn_status batch_get_config( rgdn_context* c, uint32_t storage, rgdn_batch_conf
     }
     out->atrousFusionDepth = cf.occ[ BS_ATROUS0 ] == kOccPair ? 2u : 1u;
     if( out->atrousFusionDepth == 2u ) out->atrousBlocksPerSM[ 0 ] = 3;   // the pair kernel's build
-    out->useGraphs = cf.graphs ? 1u : 0u;
-    out->tuned     = ex->tuner[ storage ].settled ? 1u : 0u;
+    out->useGraphs   = cf.graphs ? 1u : 0u;
+    out->tuned       = ex->tuner[ storage ].settled ? 1u : 0u;
+    out->groupPixels = cf.groupPixels;
     return RGDN_SUCCESS;
 }
 
@@ -668,7 +839,8 @@ rgdn_status batch_set_config( rgdn_context* c, uint32_t storage, const rgdn_batc
         cf.occ[ BS_ATROUS0 + i ]   = in->atrousTile[ i ] == RGDN_TILE_32X4 ? 7 : in->atrousBlocksPerSM[ i ] ? (int)in->atrousBlocksPerSM[ i ] : 3;
     }
     if( in->atrousFusionDepth == 2 ) candidate( BS_ATROUS0, 4, cf.shape[ BS_ATROUS0 ], cf.occ[ BS_ATROUS0 ] );
-    cf.graphs = in->useGraphs != 0;
+    cf.graphs      = in->useGraphs != 0;
+    cf.groupPixels = in->groupPixels;
     Tuner& tu = ex->tuner[ storage ];
     for( auto& p : tu.probes )
     {

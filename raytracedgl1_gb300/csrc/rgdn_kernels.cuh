@@ -2075,10 +2075,13 @@ __device__ __forceinline__ void atrous_tile( const FrameArgs& a, const int iter,
     }
 }
 
-// NT threads per block (32 x NT/32 tiles), MINB resident blocks per SM
-template< int M, bool FAST, bool HIST, bool GEOMIN, int NT = 256, int MINB = 3 >
-__global__ void __launch_bounds__( NT, MINB ) k_atrous( const FrameArgs a, const int iter )
+// NT threads per block (32 x NT/32 tiles), MINB resident blocks per SM. ITER >= 0 builds the
+// kernel for that iteration (the argument `iter` is then ITER): the step is a constant, so the
+// taps of a stencil row share one address and differ by immediate offsets.
+template< int M, bool FAST, bool HIST, bool GEOMIN, int NT = 256, int MINB = 3, int ITER = -1 >
+__global__ void __launch_bounds__( NT, MINB ) k_atrous( const FrameArgs a, const int iterArg )
 {
+    const int iter = ITER >= 0 ? ITER : iterArg;
     __shared__ float    u8[ 256 ];
     __shared__ uint32_t hist[ HIST ? 256 : 1 ];
     const int t = threadIdx.y * blockDim.x + threadIdx.x;
@@ -2757,19 +2760,29 @@ template< int M > __global__ void __launch_bounds__( 256 ) k_luminance_avg( cons
 // ==========================================================================================
 static __constant__ BatchConst c_batch[ BATCH_SLOTS ];
 
+// A batched launch covers the jobs [j0, j1) of its slot's table (one group of the step): the
+// launch argument `sarg` packs slot | j0 << 8 | j1 << 16. Tile numbers of a launch count from
+// the group's first tile, start[kind][j0].
+struct BatchRange
+{
+    int slot, j0, j1;
+};
+__device__ __forceinline__ BatchRange batch_range( const int sarg ) { return { sarg & 0xff, ( sarg >> 8 ) & 0xff, ( sarg >> 16 ) & 0xff }; }
+
 // Runs body(args, job, tile x, tile y) for the block's tiles of launch kind `kind`: tile t of
 // the launch goes to block t mod gridDim.x. The loop runs job by job, so a job's arguments are
 // resolved once per job and the tile coordinates advance by a fixed stride without a division
 // per tile. GRAD: tiles cover the gradient image (GW x GH) instead of the render (W x H).
 // Every thread of the block runs every iteration, so body may use barriers.
-template< bool GRAD, class F > __device__ __forceinline__ void batch_tiles( const int slot, const int kind, F&& body )
+template< bool GRAD, class F > __device__ __forceinline__ void batch_tiles( const int sarg, const int kind, F&& body )
 {
-    const BatchConst& bc = c_batch[ slot ];
-    const int         n  = bc.n;
-    const int         G  = (int)gridDim.x;
-    for( int j = 0; j < n; j++ )
+    const BatchRange  br   = batch_range( sarg );
+    const BatchConst& bc   = c_batch[ br.slot ];
+    const int         base = bc.start[ kind ][ br.j0 ];
+    const int         G    = (int)gridDim.x;
+    for( int j = br.j0; j < br.j1; j++ )
     {
-        const int s0 = bc.start[ kind ][ j ], s1 = bc.start[ kind ][ j + 1 ];
+        const int s0 = bc.start[ kind ][ j ] - base, s1 = bc.start[ kind ][ j + 1 ] - base;
         int       r  = ( (int)blockIdx.x - s0 ) % G;
         r            = r < 0 ? r + G : r;
         if( s0 + r >= s1 ) continue;
@@ -2791,23 +2804,23 @@ template< bool GRAD, class F > __device__ __forceinline__ void batch_tiles( cons
     }
 }
 
-template< int M > __global__ void __launch_bounds__( 256, 6 ) kb_gradient_samples( const int slot )
+template< int M > __global__ void __launch_bounds__( 256, 6 ) kb_gradient_samples( const int sarg )
 {
     __shared__ float u8[ 256 ];
     fill_u8( u8, threadIdx.y * blockDim.x + threadIdx.x );
     pdl_wait();
     __syncthreads();
-    batch_tiles< true >( slot, BS_GRADIENT, [ & ]( const FrameArgs& a, int, int bx, int by ) { gradient_samples_tile< M >( a, a.disPing, bx, by, u8 ); } );
+    batch_tiles< true >( sarg, BS_GRADIENT, [ & ]( const FrameArgs& a, int, int bx, int by ) { gradient_samples_tile< M >( a, a.disPing, bx, by, u8 ); } );
     pdl_launch_dependents();
 }
 
-template< int M > __global__ void __launch_bounds__( 256 ) kb_gradient_atrous( const int slot, const int iter )
+template< int M > __global__ void __launch_bounds__( 256 ) kb_gradient_atrous( const int sarg, const int iter )
 {
     __shared__ float u8[ 256 ];
     fill_u8( u8, threadIdx.y * blockDim.x + threadIdx.x );
     pdl_wait();
     __syncthreads();
-    batch_tiles< true >( slot, BS_GRADIENT, [ & ]( const FrameArgs& a, int, int bx, int by ) { gradient_atrous_tile( a, iter, bx, by, u8 ); } );
+    batch_tiles< true >( sarg, BS_GRADIENT, [ & ]( const FrameArgs& a, int, int bx, int by ) { gradient_atrous_tile( a, iter, bx, by, u8 ); } );
     pdl_launch_dependents();
 }
 
@@ -2815,15 +2828,15 @@ template< int M > __global__ void __launch_bounds__( 256 ) kb_gradient_atrous( c
 // record, 1 = every job has one, 2 = it depends on the job. The block of a job's first tile also
 // clears a histogram that no exposure pass consumed (before the last a-trous iteration adds
 // this frame's).
-template< int M, int GPM > __global__ void __launch_bounds__( 256 ) kb_temporal( const int slot )
+template< int M, int GPM > __global__ void __launch_bounds__( 256 ) kb_temporal( const int sarg )
 {
     __shared__ float u8[ 256 ];
     const int t = threadIdx.y * blockDim.x + threadIdx.x;
     fill_u8( u8, t );
     pdl_wait();
     __syncthreads();
-    batch_tiles< false >( slot, BS_TEMPORAL, [ & ]( const FrameArgs& a, int j, int bx, int by ) {
-        const uint32_t f = c_batch[ slot ].jobFlags[ j ];
+    batch_tiles< false >( sarg, BS_TEMPORAL, [ & ]( const FrameArgs& a, int j, int bx, int by ) {
+        const uint32_t f = c_batch[ sarg & 0xff ].jobFlags[ j ];
         if( bx == 0 && by == 0 && ( f & BATCH_JOB_CLEAR_HIST ) ) a.tm->histogram[ t ] = 0u;
         if( GPM == 1 || ( GPM == 2 && ( f & BATCH_JOB_GEOM_PREV ) ) ) temporal_tile< M, true, true, true >( a, bx, by, u8 );
         else temporal_tile< M, true, true, false >( a, bx, by, u8 );
@@ -2836,11 +2849,12 @@ template< int M, int GPM > __global__ void __launch_bounds__( 256 ) kb_temporal(
 // binary search over the constant table, which skips jobs without tiles of this kind). The
 // execution shape of the single-frame kernels: 128-thread 32x4 tiles, 7 blocks per SM, the
 // dependent launch triggered at the start.
-template< bool GRAD > __device__ __forceinline__ bool batch_tile_of_block( const int slot, const int kind, int& j, int& bx, int& by )
+template< bool GRAD > __device__ __forceinline__ bool batch_tile_of_block( const int sarg, const int kind, int& j, int& bx, int& by )
 {
-    const BatchConst& bc = c_batch[ slot ];
-    const int         b  = (int)blockIdx.x;
-    int               lo = 0, hi = bc.n;
+    const BatchRange  br = batch_range( sarg );
+    const BatchConst& bc = c_batch[ br.slot ];
+    const int         b  = (int)blockIdx.x + bc.start[ kind ][ br.j0 ];
+    int               lo = br.j0, hi = br.j1;
     if( b >= bc.start[ kind ][ hi ] ) return false;
     while( hi - lo > 1 )
     {
@@ -2857,19 +2871,19 @@ template< bool GRAD > __device__ __forceinline__ bool batch_tile_of_block( const
     return true;
 }
 
-template< int M, int GPM > __global__ void __launch_bounds__( 128, 7 ) kt_temporal( const int slot )
+template< int M, int GPM > __global__ void __launch_bounds__( 128, 7 ) kt_temporal( const int sarg )
 {
     __shared__ float u8[ 256 ];
     const int t = threadIdx.y * blockDim.x + threadIdx.x;
     pdl_launch_dependents();
     for( int k = t; k < 256; k += 128 ) fill_u8( u8, k );
     int        j = 0, bx = 0, by = 0;
-    const bool has = batch_tile_of_block< false >( slot, BS_TEMPORAL, j, bx, by );
+    const bool has = batch_tile_of_block< false >( sarg, BS_TEMPORAL, j, bx, by );
     pdl_wait();
     __syncthreads();
     if( !has ) return;
-    const FrameArgs& a = c_batch[ slot ].jobs[ j ];
-    const uint32_t   f = c_batch[ slot ].jobFlags[ j ];
+    const FrameArgs& a = c_batch[ sarg & 0xff ].jobs[ j ];
+    const uint32_t   f = c_batch[ sarg & 0xff ].jobFlags[ j ];
     if( bx == 0 && by == 0 && ( f & BATCH_JOB_CLEAR_HIST ) )
         for( int k = t; k < 256; k += 128 ) a.tm->histogram[ k ] = 0u;
     if( GPM == 1 || ( GPM == 2 && ( f & BATCH_JOB_GEOM_PREV ) ) ) temporal_tile< M, true, true, true >( a, bx, by, u8 );
@@ -2878,11 +2892,11 @@ template< int M, int GPM > __global__ void __launch_bounds__( 128, 7 ) kt_tempor
 
 // blockDim 32 x 8 over tiles of 32 columns x af_tile_rows rows (the tile function's layout); a
 // barrier ends each tile before the next reuses the shared rows
-template< int M > __global__ void __launch_bounds__( 256 ) kb_antifirefly( const int slot )
+template< int M > __global__ void __launch_bounds__( 256 ) kb_antifirefly( const int sarg )
 {
     __shared__ AfShared< M > sh;
     pdl_wait();
-    batch_tiles< false >( slot, BS_ANTI_FIREFLY, [ & ]( const FrameArgs& a, int, int bx, int by ) {
+    batch_tiles< false >( sarg, BS_ANTI_FIREFLY, [ & ]( const FrameArgs& a, int, int bx, int by ) {
         antifirefly_fast_tile< M >( a, bx, by, sh );
         __syncthreads();
     } );
@@ -2891,23 +2905,23 @@ template< int M > __global__ void __launch_bounds__( 256 ) kb_antifirefly( const
 
 // register cap: the occupancy of the single-frame kernel (5 blocks of 256 per SM)
 
-template< int M > __global__ void __launch_bounds__( 256, 5 ) kb_variance( const int slot )
+template< int M > __global__ void __launch_bounds__( 256, 5 ) kb_variance( const int sarg )
 {
     pdl_wait();
-    batch_tiles< false >( slot, BS_VARIANCE, [ & ]( const FrameArgs& a, int, int bx, int by ) { variance_geo_tile< M, true >( a, bx, by ); } );
+    batch_tiles< false >( sarg, BS_VARIANCE, [ & ]( const FrameArgs& a, int, int bx, int by ) { variance_geo_tile< M, true >( a, bx, by ); } );
     pdl_launch_dependents();
 }
 
 // Variance with one 32 x 8 tile of the step's table per block, built for 8 blocks per SM as the
 // single-frame kernel (the block finds its job by a search of the tile table)
-template< int M > __global__ void __launch_bounds__( 256, 8 ) kt_variance( const int slot )
+template< int M > __global__ void __launch_bounds__( 256, 8 ) kt_variance( const int sarg )
 {
     pdl_launch_dependents();
     int        j = 0, bx = 0, by = 0;
-    const bool has = batch_tile_of_block< false >( slot, BS_VARIANCE, j, bx, by );
+    const bool has = batch_tile_of_block< false >( sarg, BS_VARIANCE, j, bx, by );
     pdl_wait();
     if( !has ) return;
-    variance_geo_tile< M, true >( c_batch[ slot ].jobs[ j ], bx, by );
+    variance_geo_tile< M, true >( c_batch[ sarg & 0xff ].jobs[ j ], bx, by );
 }
 
 // A-trous iteration `iter` over the jobs that run it. A job's last iteration composes PreFinal
@@ -2916,7 +2930,7 @@ template< int M > __global__ void __launch_bounds__( 256, 8 ) kt_variance( const
 // HM: 0 = the iteration is no job's last, 1 = it is every job's last, 2 = it depends on the job.
 // MINB: resident blocks per SM the kernel is built for (the register budget).
 template< int M, int HM, int MINB >
-__global__ void __launch_bounds__( 256, MINB ) kb_atrous( const int slot, const int iter )
+__global__ void __launch_bounds__( 256, MINB ) kb_atrous( const int sarg, const int iter )
 {
     __shared__ float    u8[ 256 ];
     __shared__ uint32_t hist[ HM ? 256 : 1 ];
@@ -2929,11 +2943,11 @@ __global__ void __launch_bounds__( 256, MINB ) kb_atrous( const int slot, const 
     auto flush   = [ & ]() {
         __syncthreads();
         const uint32_t c = hist[ t ];
-        if( c ) atomicAdd( &c_batch[ slot ].jobs[ histJob ].tm->histogram[ t ], c );
+        if( c ) atomicAdd( &c_batch[ sarg & 0xff ].jobs[ histJob ].tm->histogram[ t ], c );
         hist[ t ] = 0u;
         __syncthreads();
     };
-    batch_tiles< false >( slot, BS_ATROUS0 + iter, [ & ]( const FrameArgs& a, int j, int bx, int by ) {
+    batch_tiles< false >( sarg, BS_ATROUS0 + iter, [ & ]( const FrameArgs& a, int j, int bx, int by ) {
         if( HM == 0 ) atrous_tile< M, true, false, true >( a, iter, bx, by, u8, hist );
         else if( HM == 1 || iter + 1 == (int)a.u.niter )
         {
@@ -2952,7 +2966,7 @@ __global__ void __launch_bounds__( 256, MINB ) kb_atrous( const int slot, const 
 
 // One 32x4 tile per 128-thread block (see kt_temporal); a tile of a job's last iteration bins
 // its HistogramInput in the block's shared histogram and flushes it into that job's state.
-template< int M, int HM > __global__ void __launch_bounds__( 128, 7 ) kt_atrous( const int slot, const int iter )
+template< int M, int HM > __global__ void __launch_bounds__( 128, 7 ) kt_atrous( const int sarg, const int iter )
 {
     __shared__ float    u8[ 256 ];
     __shared__ uint32_t hist[ HM ? 256 : 1 ];
@@ -2964,11 +2978,11 @@ template< int M, int HM > __global__ void __launch_bounds__( 128, 7 ) kt_atrous(
         if( HM ) hist[ k ] = 0u;
     }
     int        j = 0, bx = 0, by = 0;
-    const bool has = batch_tile_of_block< false >( slot, BS_ATROUS0 + iter, j, bx, by );
+    const bool has = batch_tile_of_block< false >( sarg, BS_ATROUS0 + iter, j, bx, by );
     pdl_wait();
     __syncthreads();
     if( !has ) return;
-    const FrameArgs& a = c_batch[ slot ].jobs[ j ];
+    const FrameArgs& a = c_batch[ sarg & 0xff ].jobs[ j ];
     if( HM == 1 || ( HM == 2 && iter + 1 == (int)a.u.niter ) )
     {
         atrous_tile< M, true, true, true >( a, iter, bx, by, u8, hist );
@@ -2981,7 +2995,7 @@ template< int M, int HM > __global__ void __launch_bounds__( 128, 7 ) kt_atrous(
 
 // a-trous iterations 0 and 1 of a batched step in one launch: one 32 x 8 tile of the
 // BS_ATROUS0 table per block (every job runs at least 3 iterations)
-template< int M > __global__ void __launch_bounds__( 256, 3 ) kt_atrous_pair01( const int slot )
+template< int M > __global__ void __launch_bounds__( 256, 3 ) kt_atrous_pair01( const int sarg )
 {
     extern __shared__ float4 smem[];
     __shared__ float         u8[ 256 ];
@@ -2989,24 +3003,24 @@ template< int M > __global__ void __launch_bounds__( 256, 3 ) kt_atrous_pair01( 
     pdl_launch_dependents();
     u8[ t ] = (float)t / 255.0f;
     int        j = 0, bx = 0, by = 0;
-    const bool has = batch_tile_of_block< false >( slot, BS_ATROUS0, j, bx, by );
+    const bool has = batch_tile_of_block< false >( sarg, BS_ATROUS0, j, bx, by );
     pdl_wait();
     __syncthreads();
     if( !has ) return;
-    atrous_pair_tile< M >( c_batch[ slot ].jobs[ j ], bx, by, smem, u8 );
+    atrous_pair_tile< M >( c_batch[ sarg & 0xff ].jobs[ j ], bx, by, smem, u8 );
 }
 
-// one block per job (strided), as k_luminance_avg
-template< int M > __global__ void __launch_bounds__( 256 ) kb_luminance_avg( const int slot )
+// one block per job of the group (strided), as k_luminance_avg
+template< int M > __global__ void __launch_bounds__( 256 ) kb_luminance_avg( const int sarg )
 {
     __shared__ uint32_t sh[ 256 ];
     __shared__ uint32_t count0;
     pdl_wait();
-    const int n = c_batch[ slot ].n;
-    for( int j = blockIdx.x; j < n; j += gridDim.x )
+    const BatchRange br = batch_range( sarg );
+    for( int j = br.j0 + (int)blockIdx.x; j < br.j1; j += gridDim.x )
     {
         __syncthreads();
-        luminance_avg_job( c_batch[ slot ].jobs[ j ], sh, count0 );
+        luminance_avg_job( c_batch[ br.slot ].jobs[ j ], sh, count0 );
     }
     pdl_launch_dependents();
 }
@@ -3812,6 +3826,22 @@ template< int M > cudaError_t launch_atrous_pair01( const FrameArgs& a, cudaStre
     return launch_pdl( kernel, dim3( ( a.u.W + P::TW - 1 ) / P::TW, ( a.u.H + P::TH - 1 ) / P::TH ), dim3( 32, 8 ), P::SMEM, s, a );
 }
 
+// The default a-trous kernel (32x4 tiles, 7 blocks per SM), built per iteration for the first
+// five iterations (steps 1 to 16)
+template< int M, bool HIST > cudaError_t launch_atrous_fast( const FrameArgs& a, const int iter, cudaStream_t s )
+{
+    const dim3 grid( ( a.u.W + 31 ) / 32, ( a.u.H + 3 ) / 4 ), blk( 32, 4 );
+    switch( iter )
+    {
+        case 0: return launch_pdl( dev::k_atrous< M, true, HIST, true, 128, 7, 0 >, grid, blk, 0, s, a, iter );
+        case 1: return launch_pdl( dev::k_atrous< M, true, HIST, true, 128, 7, 1 >, grid, blk, 0, s, a, iter );
+        case 2: return launch_pdl( dev::k_atrous< M, true, HIST, true, 128, 7, 2 >, grid, blk, 0, s, a, iter );
+        case 3: return launch_pdl( dev::k_atrous< M, true, HIST, true, 128, 7, 3 >, grid, blk, 0, s, a, iter );
+        case 4: return launch_pdl( dev::k_atrous< M, true, HIST, true, 128, 7, 4 >, grid, blk, 0, s, a, iter );
+        default: return launch_pdl( dev::k_atrous< M, true, HIST, true, 128, 7 >, grid, blk, 0, s, a, iter );
+    }
+}
+
 // Kernels whose results are continuous in every arithmetic operation (no threshold follows
 // them), in their own translation units (rgdn_fast_*.cu); their weighted sums use explicit
 // fused multiply-adds.
@@ -3822,12 +3852,8 @@ template< int M > cudaError_t launch_fast_t( const FrameArgs& a, int stage, int 
     const dim3 grid( ( a.u.W + 31 ) / 32, ( a.u.H + 7 ) / 8 );
     switch( stage )
     {
-        case KF_ATROUS_FAST:
-            e = launch_pdl( dev::k_atrous< M, true, false, true, 128, 7 >, dim3( grid.x, ( a.u.H + 3 ) / 4 ), dim3( 32, 4 ), 0, s, a, iter );
-            break;
-        case KF_ATROUS_FAST_HIST:
-            e = launch_pdl( dev::k_atrous< M, true, true, true, 128, 7 >, dim3( grid.x, ( a.u.H + 3 ) / 4 ), dim3( 32, 4 ), 0, s, a, iter );
-            break;
+        case KF_ATROUS_FAST: e = launch_atrous_fast< M, false >( a, iter, s ); break;
+        case KF_ATROUS_FAST_HIST: e = launch_atrous_fast< M, true >( a, iter, s ); break;
         case KF_VARIANCE_FAST: e = launch_pdl( dev::k_variance_geo< M, true >, grid, blk, 0, s, a ); break;
         case KF_ATROUS_PAIR01: e = launch_atrous_pair01< M >( a, s ); break;
         default: return cudaErrorInvalidValue;

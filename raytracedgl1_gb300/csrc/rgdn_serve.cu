@@ -69,6 +69,8 @@ struct StepRec
     int64_t                 index;
     int                     lane;           // which CUDA stream
     cudaEvent_t             done;
+    cudaEvent_t             mark[ 4 ] = {}; // timing: start, copies in, kernels, copies out done
+    double                  issueMs = 0;    // host time in enqueue_step
     std::vector< uint64_t > tickets;
     std::vector< uint32_t > streams;
     uint64_t                pixels;
@@ -96,10 +98,13 @@ struct rgdn_server
     uint64_t                changes   = 0;      // submissions, completions, closes
     uint64_t                stalledAt = ~0ull;  // `changes` when a pass found nothing to run
     bool                    stalled   = false;  // ... with nothing in flight either
+    bool                    forming   = false;  // a step left `arrival` and is not in `inflight` yet
     rgdn_status             error = RGDN_SUCCESS;   // first asynchronous failure
     // statistics
     uint64_t                framesDone = 0, framesDropped = 0, steps = 0, pixelsDone = 0, framesInSteps = 0;
     std::vector< float >    latencies;
+    std::vector< float >    issueMs, copyInMs, kernelsMs, copyOutMs;   // per step
+    std::vector< cudaEvent_t > timingPool;
     double                  busyStart = -1, busySeconds = 0;
     uint32_t                magic = 0x52475356u;
 };
@@ -119,6 +124,18 @@ cudaEvent_t take_event( rgdn_server* sv )
     }
     cudaEvent_t e = nullptr;
     return cudaEventCreateWithFlags( &e, cudaEventDisableTiming ) == cudaSuccess ? e : nullptr;
+}
+
+cudaEvent_t take_timing_event( rgdn_server* sv )
+{
+    if( !sv->timingPool.empty() )
+    {
+        cudaEvent_t e = sv->timingPool.back();
+        sv->timingPool.pop_back();
+        return e;
+    }
+    cudaEvent_t e = nullptr;
+    return cudaEventCreate( &e ) == cudaSuccess ? e : nullptr;
 }
 
 uint64_t stream_bytes( rgdn_server* sv, const ServeStream& st )
@@ -178,6 +195,7 @@ rgdn_status enqueue_step( rgdn_server* sv, StepRec& rec, std::vector< rgdn_job >
     cudaStream_t cs = sv->lane[ rec.lane ];
     for( cudaEvent_t e : waits )
         if( cudaStreamWaitEvent( cs, e, 0 ) != cudaSuccess ) return RGDN_DEVICE_ERROR;
+    if( rec.mark[ 0 ] && cudaEventRecord( rec.mark[ 0 ], cs ) != cudaSuccess ) return RGDN_DEVICE_ERROR;
     for( size_t k = 0; k < jobs.size(); k++ )
     {
         const rgdn_frame_request& q = rq[ k ]->req;
@@ -198,8 +216,10 @@ rgdn_status enqueue_step( rgdn_server* sv, StepRec& rec, std::vector< rgdn_job >
                 return RGDN_DEVICE_ERROR;
         }
     }
+    if( rec.mark[ 1 ] && cudaEventRecord( rec.mark[ 1 ], cs ) != cudaSuccess ) return RGDN_DEVICE_ERROR;
     rgdn_status r = rgdn_submit_batch( sv->ctx, jobs.data(), (uint32_t)jobs.size(), (rgdn_cuda_stream)cs );
     if( r != RGDN_SUCCESS ) return r;
+    if( rec.mark[ 2 ] && cudaEventRecord( rec.mark[ 2 ], cs ) != cudaSuccess ) return RGDN_DEVICE_ERROR;
     for( size_t k = 0; k < jobs.size(); k++ )
     {
         if( !rq[ k ]->req.preFinalOut ) continue;
@@ -208,6 +228,7 @@ rgdn_status enqueue_step( rgdn_server* sv, StepRec& rec, std::vector< rgdn_job >
         if( cudaMemcpyAsync( rq[ k ]->req.preFinalOut, img.data, (size_t)img.pitch_bytes * img.height, cudaMemcpyDefault, cs ) != cudaSuccess )
             return RGDN_DEVICE_ERROR;
     }
+    if( rec.mark[ 3 ] && cudaEventRecord( rec.mark[ 3 ], cs ) != cudaSuccess ) return RGDN_DEVICE_ERROR;
     return cudaEventRecord( rec.done, cs ) == cudaSuccess ? RGDN_SUCCESS : RGDN_DEVICE_ERROR;
 }
 
@@ -299,10 +320,16 @@ void scheduler_loop( rgdn_server* sv )
         sv->stalled = false;
         sv->arrival.assign( keep.begin(), keep.end() );
         rec.done = take_event( sv );
+        for( cudaEvent_t& e : rec.mark ) e = take_timing_event( sv );
         sv->nextStep++;
+        // its frames are in neither `arrival` nor `inflight` while the lock is released
+        sv->forming = true;
         lk.unlock();
-        rgdn_status r = rec.done ? enqueue_step( sv, rec, jobs, sts, rq, waits ) : RGDN_DEVICE_ERROR;
+        const double tIssue = now_s();
+        rgdn_status  r      = rec.done ? enqueue_step( sv, rec, jobs, sts, rq, waits ) : RGDN_DEVICE_ERROR;
+        rec.issueMs         = ( now_s() - tIssue ) * 1e3;
         lk.lock();
+        sv->forming = false;
         if( r != RGDN_SUCCESS )
         {
             // the frames cannot complete: report them dropped and remember the failure
@@ -315,6 +342,8 @@ void scheduler_loop( rgdn_server* sv )
                 sv->streams[ rec.streams[ k ] ].running--;
             }
             if( rec.done ) sv->eventPool.push_back( rec.done );
+            for( cudaEvent_t e : rec.mark )
+                if( e ) sv->timingPool.push_back( e );
             sv->cvDone.notify_all();
             continue;
         }
@@ -351,6 +380,21 @@ void completion_loop( rgdn_server* sv )
             ServeStream& st = sv->streams[ rec.streams[ k ] ];
             st.running--;
         }
+        if( ce == cudaSuccess && rec.mark[ 0 ] && rec.mark[ 1 ] && rec.mark[ 2 ] && rec.mark[ 3 ] )
+        {
+            float a = 0, b = 0, c = 0;
+            if( cudaEventElapsedTime( &a, rec.mark[ 0 ], rec.mark[ 1 ] ) == cudaSuccess &&
+                cudaEventElapsedTime( &b, rec.mark[ 1 ], rec.mark[ 2 ] ) == cudaSuccess &&
+                cudaEventElapsedTime( &c, rec.mark[ 2 ], rec.mark[ 3 ] ) == cudaSuccess )
+            {
+                sv->copyInMs.push_back( a );
+                sv->kernelsMs.push_back( b );
+                sv->copyOutMs.push_back( c );
+            }
+        }
+        sv->issueMs.push_back( (float)rec.issueMs );
+        for( cudaEvent_t e : rec.mark )
+            if( e ) sv->timingPool.push_back( e );
         sv->steps++;
         sv->framesInSteps += rec.tickets.size();
         sv->pixelsDone += rec.pixels;
@@ -416,7 +460,9 @@ rgdn_status rgdn_server_drain( rgdn_server* sv )
 {
     if( !valid_server( sv ) ) return RGDN_WRONG_INSTANCE;
     std::unique_lock< std::mutex > lk( sv->m );
-    sv->cvDone.wait( lk, [ & ] { return sv->inflight.empty() && ( sv->arrival.empty() || ( sv->stalled && sv->stalledAt == sv->changes ) ); } );
+    sv->cvDone.wait( lk, [ & ] {
+        return !sv->forming && sv->inflight.empty() && ( sv->arrival.empty() || ( sv->stalled && sv->stalledAt == sv->changes ) );
+    } );
     if( sv->error != RGDN_SUCCESS ) return sv->error;
     // frames left waiting can run only after memory frees up (rgdn_server_close_stream)
     return sv->arrival.empty() ? RGDN_SUCCESS : RGDN_OUT_OF_BUDGET;
@@ -438,6 +484,7 @@ rgdn_status rgdn_server_destroy( rgdn_server* sv )
     for( auto& kv : sv->streams )
         if( kv.second.s ) rgdn_stream_destroy( kv.second.s );
     for( cudaEvent_t e : sv->eventPool ) cudaEventDestroy( e );
+    for( cudaEvent_t e : sv->timingPool ) cudaEventDestroy( e );
     for( int i = 0; i < 2; i++ ) cudaStreamDestroy( sv->lane[ i ] );
     sv->magic = 0;
     delete sv;
@@ -561,6 +608,14 @@ rgdn_status rgdn_server_stats_get( rgdn_server* sv, rgdn_server_stats* out )
                                  : 0.0f;
     out->meanFramesPerStep = sv->steps ? (float)sv->framesInSteps / (float)sv->steps : 0.0f;
     out->busySeconds       = sv->busySeconds + ( sv->busyStart >= 0 ? now_s() - sv->busyStart : 0.0 );
+    out->issueP50Ms        = percentile( sv->issueMs, 0.50 );
+    out->issueP99Ms        = percentile( sv->issueMs, 0.99 );
+    out->copyInP50Ms       = percentile( sv->copyInMs, 0.50 );
+    out->copyInP99Ms       = percentile( sv->copyInMs, 0.99 );
+    out->kernelsP50Ms      = percentile( sv->kernelsMs, 0.50 );
+    out->kernelsP99Ms      = percentile( sv->kernelsMs, 0.99 );
+    out->copyOutP50Ms      = percentile( sv->copyOutMs, 0.50 );
+    out->copyOutP99Ms      = percentile( sv->copyOutMs, 0.99 );
     return RGDN_SUCCESS;
 }
 
@@ -570,6 +625,10 @@ rgdn_status rgdn_server_stats_reset( rgdn_server* sv )
     std::lock_guard< std::mutex > g( sv->m );
     sv->framesDone = sv->framesDropped = sv->steps = sv->pixelsDone = sv->framesInSteps = 0;
     sv->latencies.clear();
+    sv->issueMs.clear();
+    sv->copyInMs.clear();
+    sv->kernelsMs.clear();
+    sv->copyOutMs.clear();
     sv->busySeconds = 0;
     if( sv->busyStart >= 0 ) sv->busyStart = now_s();
     return RGDN_SUCCESS;

@@ -67,3 +67,43 @@ def test_bin_table_rejects_empty_range():
     lib = N.load()
     buf = (C.c_uint8 * 65536)()
     assert lib.rgdn_histogram_bin_table(C.c_float(1.0), C.c_float(1.0), buf) == N.WRONG_FUNCTION_ARGUMENT
+
+
+# every ctypes mirror of a struct in include/rgdn.h, by its C name
+MIRRORS = {
+    "rgdn_image": N.Image, "rgdn_frame_params": N.FrameParams, "rgdn_context_create_info": N.ContextCreateInfo,
+    "rgdn_stream_create_info": N.StreamCreateInfo, "rgdn_final_params": N.FinalParams, "rgdn_bloom_params": N.BloomParams,
+    "rgdn_volumetric_params": N.VolumetricParams, "rgdn_sphere_light": N.SphereLight, "rgdn_occluder": N.Occluder,
+    "rgdn_reshade_scene": N.ReshadeScene, "rgdn_job": N.Job, "rgdn_batch_config": N.BatchConfig,
+    "rgdn_server_create_info": N.ServerCreateInfo, "rgdn_frame_request": N.FrameRequest,
+    "rgdn_frame_result": N.FrameResult, "rgdn_server_stats": N.ServerStats, "rgdn_stage_timing": N.StageTiming,
+}
+
+
+def test_struct_layouts_match_the_header(tmp_path):
+    """The size and every field offset of each struct, as a C compiler lays it out from the
+    header, equal the ctypes mirror's."""
+    import shutil
+    import subprocess
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if not cc:
+        pytest.skip("no C compiler")
+    lines = ["#include <stdio.h>", "#include <stddef.h>", '#include "rgdn.h"', "int main(void) {"]
+    for cname, py in MIRRORS.items():
+        lines.append(f'printf("{cname} size %zu\\n", sizeof({cname}));')
+        for fname, _ in py._fields_:
+            lines.append(f'printf("{cname} {fname} %zu\\n", offsetof({cname}, {fname}));')
+    lines += ["return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "layout"
+    subprocess.run([cc, "-std=c11", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split("\n")
+    bad = []
+    for line in filter(None, out):
+        cname, field, value = line.split()
+        py = MIRRORS[cname]
+        got = C.sizeof(py) if field == "size" else getattr(py, field).offset
+        if got != int(value):
+            bad.append(f"{cname}.{field}: C {value}, ctypes {got}")
+    assert not bad, bad

@@ -57,7 +57,9 @@ def test_batch_equals_sequential_through_tuning_and_graphs(mode_name, mode):
     scenes = [Scene(w, h, seed=40 + i, lightFlickerFrom=3.0) for i, (w, h) in enumerate(SIZES)]
     seq = [Stream(ctx, w, h, mode) for w, h in SIZES]
     bat = [Stream(ctx, w, h, mode) for w, h in SIZES]
-    frames = 19   # 15 tuning steps (the fused first two a-trous iterations among them), then graph replay
+    # 15 steps tuning the launches (the fused first two a-trous iterations among them), 8 tuning
+    # the group size, then graph replay
+    frames = 27
     for f in range(frames):
         fi = f & 1
         jobs = []
@@ -113,13 +115,15 @@ def test_batch_splits_steps_and_falls_back():
     ctx.close()
 
 
-@pytest.mark.parametrize("shape,occ,depth", [(0, 3, 1), (1, 4, 1), (2, 4, 1), (2, 3, 1), (0, 4, 1), (3, 7, 1), (0, 3, 2), (3, 7, 2)])
-def test_batch_fixed_configs(shape, occ, depth):
+@pytest.mark.parametrize("shape,occ,depth,group", [(0, 3, 1, 0), (1, 4, 1, 0), (2, 4, 1, 1), (2, 3, 1, 0), (0, 4, 1, 2000),
+                                                   (3, 7, 1, 2000), (0, 3, 2, 1), (3, 7, 2, 0), (3, 7, 2, 2000)])
+def test_batch_fixed_configs(shape, occ, depth, group):
     """A configuration set through rgdn_batch_set_config (no tuning) gives the same results.
     Shape 3 is the 128-thread 32x4 tile (temporal and a-trous; variance then runs one 32x8 tile
-    per block). Fusion depth
-    2 runs a-trous iterations 0 and 1 in one launch; the last frame has a stream running only
-    two iterations, where the step falls back to one launch per iteration."""
+    per block). Fusion depth 2 runs a-trous iterations 0 and 1 in one launch; the last frame has
+    a stream running only two iterations, where the step falls back to one launch per iteration.
+    Group size 0 runs the three frames as one group, 2000 pixels as two (64x36 alone, on the
+    single-frame kernels, then 50x23 with 34x17), 1 pixel as three single-frame groups."""
     ctx = Context(0)
     cfg = N.BatchConfig()
     cfg.temporalTile = shape
@@ -131,9 +135,10 @@ def test_batch_fixed_configs(shape, occ, depth):
         cfg.atrousBlocksPerSM[i] = occ
     cfg.useGraphs = 1
     cfg.atrousFusionDepth = depth
+    cfg.groupPixels = group
     ctx.set_batch_config(N.STORAGE_BF16, cfg)
     got = ctx.batch_config(N.STORAGE_BF16)
-    assert got.tuned == 1 and got.temporalTile == shape and got.atrousFusionDepth == depth
+    assert got.tuned == 1 and got.temporalTile == shape and got.atrousFusionDepth == depth and got.groupPixels == group
     assert list(got.atrousBlocksPerSM)[1:] == [occ] * 5
     sizes = SIZES[:3]
     scenes = [Scene(w, h, seed=70 + i) for i, (w, h) in enumerate(sizes)]
@@ -183,5 +188,48 @@ def test_batch_timing_and_launch_count():
     assert all(ms > 0 for _, ms in t.values())
     ctx.set_batch_timing(False)
     for s in streams:
+        s.close()
+    ctx.close()
+
+
+def test_batch_groups_launch_per_group():
+    """Groups of frames: with a group size of 2000 pixels the frames 64x36, 50x23 and 34x17 form
+    the groups {64x36} and {50x23, 34x17}. A group of one frame runs on the single-frame kernels,
+    the other on the batched kernels over jobs 1..2 of the step's table; each launches the whole
+    stage sequence, in order, with the same results as one stream per call."""
+    ctx = Context(0)
+    cfg = ctx.batch_config(N.STORAGE_FP16)
+    cfg.groupPixels = 2000
+    cfg.useGraphs = 1
+    ctx.set_batch_config(N.STORAGE_FP16, cfg)
+    sizes = SIZES[:1] + SIZES[1:3]
+    scenes = [Scene(w, h, seed=90 + i) for i, (w, h) in enumerate(sizes)]
+    seq = [Stream(ctx, w, h, N.STORAGE_FP16) for w, h in sizes]
+    bat = [Stream(ctx, w, h, N.STORAGE_FP16) for w, h in sizes]
+    for f in range(4):
+        timed = f == 3
+        ctx.set_batch_timing(timed)
+        jobs = []
+        for i, sc in enumerate(scenes):
+            bufs, p = sc.generate(f)
+            p.atrousIterations = 5
+            for s in (seq[i], bat[i]):
+                for name, arr in bufs.items():
+                    s.upload(name, f & 1, arr)
+            Denoiser(seq[i]).Denoise(f & 1, p)
+            Tonemapping(seq[i]).CalculateExposure(f & 1, p)
+            jobs.append((bat[i], f & 1, p))
+        before = ctx.launch_count()
+        ctx.submit_batch(jobs)
+        # 14 launches per group (5 gradient, 3, 5 a-trous, 1 luminance average), two groups
+        assert ctx.launch_count() - before == 28
+        if timed:
+            t = ctx.read_batch_timing()
+            assert t[("single_frame_group", 0)][0] == 1 and t[("temporal_accumulation", 0)][0] == 1
+            assert t[("luminance_avg", 0)][0] == 1
+        for i in range(len(sizes)):
+            assert_same(seq[i], bat[i], f"frame {f} stream {i}", full=True)
+    ctx.set_batch_timing(False)
+    for s in seq + bat:
         s.close()
     ctx.close()
