@@ -73,6 +73,10 @@ def parse():
     ap.add_argument("--serve-step-mpix", type=float, default=8.0, help="pixel bound of one serving step (Mpix)")
     ap.add_argument("--serve-e2e-repeats", type=int, default=1,
                     help="end-to-end serving runs back to back in the process (the first is the line's)")
+    ap.add_argument("--serve-host-copy", choices=["engine", "sm"], default="sm",
+                    help="how the end-to-end serving run's pinned G-buffers reach the device: one kernel per "
+                         "frame loading them over the host link (32 blocks), or the copy engines "
+                         "(cudaMemcpyAsync per plane), whose copies stalled for 10-50 ms at times on the GB300 boxes")
     ap.add_argument("--serve-keep-pins", action="store_true",
                     help="end-to-end serving from the host buffers pinned at start-up, not fresh pinned "
                          "copies made right before each run (pinned buffers that have aged for tens of "
@@ -613,7 +617,7 @@ def run_batched(args, dist: Dist, dev: int, cs) -> dict:
                          "variance": int(cfg.varianceTile), "atrous": [int(v) for v in cfg.atrousTile][:args.iters],
                          "atrous_blocks_per_sm": [int(v) for v in cfg.atrousBlocksPerSM][:args.iters],
                          "atrous_fusion_depth": int(cfg.atrousFusionDepth),
-                         "group_pixels": int(cfg.groupPixels),
+                         "group_pixels": int(cfg.groupPixels), "single_frame_pixels": int(cfg.singleFramePixels),
                          "graphs": int(cfg.useGraphs), "tile_names": ["32x8", "16x16", "64x4", "32x4", "32x8 per block"]},
         "kernels": kern,
     }
@@ -669,7 +673,8 @@ def run_serving(args, dist: Dist, dev: int) -> dict:
     def serve(hz: float, e2e: bool) -> dict:
         inflight = args.serve_e2e_inflight if e2e else args.serve_inflight
         sv = Server(ctx, storage, max_frames_per_step=32, max_pixels_per_step=int(args.serve_step_mpix * 1e6),
-                    max_queued_per_stream=1, steps_in_flight=inflight)
+                    max_queued_per_stream=1, steps_in_flight=inflight,
+                    host_copy=N.HOST_COPY_SM if (e2e and args.serve_host_copy == "sm") else N.HOST_COPY_ENGINE)
         sids = [sv.open_stream(w, h) for w, h in res]
         reqs = []
         for i, sid in enumerate(sids):
@@ -782,6 +787,7 @@ def run_serving(args, dist: Dist, dev: int) -> dict:
     e2e = e2e_runs[0]
     e2e["host_buffers"] = ("pinned at start-up" if args.serve_keep_pins
                            else "fresh pinned copies made right before the run")
+    e2e["host_copy"] = args.serve_host_copy
     if len(e2e_runs) > 1:
         e2e["repeats"] = [{k: r[k] for k in ("p50_ms", "p99_ms", "p99_all_requests_ms", "drop_rate", "queue_p99_ms",
                                               "service_p50_ms", "service_p99_ms", "gpu_busy_frac", "host_link_before",

@@ -497,9 +497,9 @@ rgdn_status rgdn_submit_batch( rgdn_context* ctx, const rgdn_job* jobs, uint32_t
 /* The launch configuration of batched steps for one storage mode. The autotuner starts from
  * 32x8 tiles everywhere and, over the first 15 steps, times every candidate of every launch
  * (tile shape; for a-trous also the register budget and the fusion depth) on the work being
- * submitted, keeps the fastest, then times 8 whole steps at each candidate group size
- * (groupPixels) and keeps the fastest; then steps switch to graph replay. Candidates give
- * identical results. */
+ * submitted, keeps the fastest, then times 2 whole steps at each of 4 candidate groupings
+ * (groupPixels, singleFramePixels) and keeps the fastest; then steps switch to graph replay
+ * (steps with a single-frame group are launched directly). Candidates give identical results. */
 typedef struct rgdn_batch_config
 {
     uint32_t temporalTile;        /* RGDN_TILE_* */
@@ -519,7 +519,10 @@ typedef struct rgdn_batch_config
                                      most this many pixels (a larger frame is a group of its own);
                                      a group runs every stage before the next group starts, so the
                                      planes one stage writes are still in L2 when the group's next
-                                     stage reads them. 0 = the whole step is one group */
+                                     stage reads them. 0 = no bound */
+    uint64_t singleFramePixels;   /* a frame of at least this many pixels is a group of its own; a
+                                     group of one frame runs on the single-frame kernels, its
+                                     arguments passed as kernel parameters. 0 = never alone */
 } rgdn_batch_config;
 rgdn_status rgdn_batch_get_config( rgdn_context* ctx, uint32_t storage, rgdn_batch_config* outConfig );
 /* Fixes the configuration of a storage mode and ends its autotuning. */
@@ -549,7 +552,14 @@ typedef struct rgdn_server_create_info
                                     also wait for the two job tables of the device */
     uint32_t evictIdleMs;        /* a stream idle this long may lose its memory (and history)
                                     to admit another; 0 = never evict */
+    uint32_t hostCopy;           /* RGDN_HOST_COPY_*: how RGDN_REQUEST_COPY planes in pinned host
+                                    memory reach the device */
 } rgdn_server_create_info;
+#define RGDN_HOST_COPY_ENGINE 0u /* cudaMemcpyAsync per plane (the copy engines) */
+#define RGDN_HOST_COPY_SM     1u /* one kernel per frame loads the pinned planes over the host link
+                                    (mapped host memory) and stores them to the stream's planes;
+                                    planes that are not device-mapped, or not 16-byte aligned and
+                                    sized, still go through cudaMemcpyAsync */
 
 /* G-buffer source of a request: planes RGDN_FB_ALBEDO .. RGDN_FB_GRADIENT_RESHADED */
 #define RGDN_GBUFFER_PLANES 15

@@ -166,7 +166,8 @@ class BatchConfig(C.Structure):
     _fields_ = [("temporalTile", C.c_uint32), ("antiFireflyTile", C.c_uint32),
                 ("varianceTile", C.c_uint32), ("atrousTile", C.c_uint32 * 6),
                 ("atrousBlocksPerSM", C.c_uint32 * 6), ("useGraphs", C.c_uint32), ("tuned", C.c_uint32),
-                ("atrousFusionDepth", C.c_uint32), ("groupPixels", C.c_uint64)]
+                ("atrousFusionDepth", C.c_uint32), ("groupPixels", C.c_uint64),
+                ("singleFramePixels", C.c_uint64)]
 
 
 TILE_32X8, TILE_16X16, TILE_64X4, TILE_32X4, TILE_32X8_PER_BLOCK = 0, 1, 2, 3, 4
@@ -179,7 +180,11 @@ FRAME_DONE, FRAME_DROPPED = 0, 1
 
 class ServerCreateInfo(C.Structure):
     _fields_ = [("storage", C.c_uint32), ("maxFramesPerStep", C.c_uint32), ("maxPixelsPerStep", C.c_uint64),
-                ("maxQueuedPerStream", C.c_uint32), ("stepsInFlight", C.c_uint32), ("evictIdleMs", C.c_uint32)]
+                ("maxQueuedPerStream", C.c_uint32), ("stepsInFlight", C.c_uint32), ("evictIdleMs", C.c_uint32),
+                ("hostCopy", C.c_uint32)]
+
+
+HOST_COPY_ENGINE, HOST_COPY_SM = 0, 1
 
 
 class FrameRequest(C.Structure):

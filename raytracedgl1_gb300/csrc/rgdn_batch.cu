@@ -21,8 +21,9 @@
 // and a step waits on the host until the slot's previous step has finished.
 //
 // Groups: the step's frames run in groups of consecutive frames of at most groupPixels pixels,
-// each group through every stage before the next group starts. A group of one frame runs on the
-// single-frame kernels, whose frame arguments are kernel parameters: read from the constant
+// each group through every stage before the next group starts. A frame of at least
+// singlePixels pixels is a group of its own and runs on the single-frame kernels, whose frame
+// arguments are kernel parameters: read from the constant
 // table with a job index known only at run time, the same fields cost the batched kernels
 // registers (the batched a-trous and variance builds spill 2-7 times the bytes of the
 // single-frame ones) and their large frames ran 5-13 % slower per pixel. A step with such a
@@ -32,8 +33,8 @@
 // Autotuning: the first 15 steps of a storage mode time every candidate tile shape (and, for
 // the a-trous kernel, the register budget and the fusion depth) per launch on the frames being
 // submitted; the fastest candidate per launch is kept. The next 8 steps time whole steps at each
-// candidate group size and keep the fastest. Candidates compute identical values per pixel, so
-// tuning changes no result. Then steps switch to graph replay.
+// candidate grouping (kGroupCand) and keep the fastest. Candidates compute identical values per
+// pixel, so tuning changes no result. Then steps switch to graph replay.
 #include <algorithm>
 #include <cstddef>
 #include <cstring>
@@ -150,7 +151,8 @@ struct Config
     int      shape[ BS_COUNT ];   // index into kShapes (BS_GRADIENT stays 32x8)
     int      occ[ BS_COUNT ];     // a-trous kinds: resident blocks per SM the kernel is built for (3, 4)
     bool     graphs;
-    uint64_t groupPixels;         // 0 = one group per step
+    uint64_t groupPixels;         // 0 = no bound on a group's pixels
+    uint64_t singlePixels;        // frames of at least this many pixels run alone (0 = never)
 };
 
 // kind -2: a whole step (the group-size phase)
@@ -162,9 +164,15 @@ struct Probe
     bool        scored;
 };
 
-// Group sizes the second tuning phase times, as whole steps: one group, then about two 2560x1440
-// frames, one, and one 1920x1080 frame. Phase 1 runs kGroupRounds passes (the first not scored).
-const uint64_t kGroupCand[ 4 ] = { 0ull, 8ull << 20, 4ull << 20, 2ull << 20 };
+// Groupings the second tuning phase times, as whole steps (group pixels, single-frame pixels):
+// the whole step as one group; groups of about one 2560x1440 frame; frames of 1280x720 and up
+// alone with the smaller ones grouped; frames of 1920x1080 and up alone. Phase 1 runs
+// kGroupRounds passes over them (the first not scored).
+struct Grouping
+{
+    uint64_t group, single;
+};
+const Grouping kGroupCand[ 4 ] = { { 0ull, 0ull }, { 4ull << 20, 0ull }, { 8ull << 20, 512ull << 10 }, { 8ull << 20, 2000000ull } };
 constexpr int  kGroupRounds    = 2;
 
 struct Tuner
@@ -282,7 +290,8 @@ BatchExec* create_exec( int device )
             ex->cfg[ s ].occ[ k ]   = k >= BS_ATROUS0 ? 3 : 0;
         }
         ex->cfg[ s ].graphs      = true;
-        ex->cfg[ s ].groupPixels = kGroupCand[ 2 ];
+        ex->cfg[ s ].groupPixels  = kGroupCand[ 2 ].group;
+        ex->cfg[ s ].singlePixels = kGroupCand[ 2 ].single;
         for( int st = 0; st < RGDN_STAGE_COUNT; st++ )
             for( int o = 0; o < 8; o++ ) ex->bps[ s ][ st ][ o ] = -1;
     }
@@ -329,8 +338,10 @@ rgdn_status enqueue_step( rgdn_context* c, BatchExec& ex, DeviceSlots& ds, int s
 {
     const uint32_t st    = (uint32_t)key.storage;
     const size_t   bytes = capturing ? sizeof( BatchConst ) : table_bytes( n );
-    if( cudaMemcpyAsync( ds.mode[ st ][ slot ], ds.host[ slot ], bytes, cudaMemcpyHostToDevice, cs ) != cudaSuccess ||
-        cudaMemcpyAsync( ds.fast[ st ][ slot ], ds.host[ slot ], bytes, cudaMemcpyHostToDevice, cs ) != cudaSuccess )
+    bool           table = false;   // a group on the batched kernels reads the table
+    for( int gi = 0; gi < key.ng; gi++ ) table = table || !key.g[ gi ].single;
+    if( table && ( cudaMemcpyAsync( ds.mode[ st ][ slot ], ds.host[ slot ], bytes, cudaMemcpyHostToDevice, cs ) != cudaSuccess ||
+                   cudaMemcpyAsync( ds.fast[ st ][ slot ], ds.host[ slot ], bytes, cudaMemcpyHostToDevice, cs ) != cudaSuccess ) )
         return RGDN_DEVICE_ERROR;
     Tuner&     tu     = ex.tuner[ st ];
     const bool tuning = !capturing && !tu.settled && tu.phase == 0;
@@ -510,7 +521,11 @@ rgdn_status settle_groups( BatchExec& ex, uint32_t st )
     int                   best = -1;
     for( int k = 0; k < 4; k++ )
         if( px[ k ] > 0.0 && ( best < 0 || ms[ k ] / px[ k ] < ms[ best ] / px[ best ] ) ) best = k;
-    if( best >= 0 ) ex.cfg[ st ].groupPixels = kGroupCand[ best ];
+    if( best >= 0 )
+    {
+        ex.cfg[ st ].groupPixels  = kGroupCand[ best ].group;
+        ex.cfg[ st ].singlePixels = kGroupCand[ best ].single;
+    }
     tu.settled = true;
     return r;
 }
@@ -544,7 +559,11 @@ rgdn_status run_step( rgdn_context* c, BatchExec& ex, const rgdn_job* jobs, int 
     Config     cfg     = ex.cfg[ st ];
     if( tuneLk )
         for( int kind = BS_TEMPORAL; kind < BS_COUNT; kind++ ) candidate( kind, tcand % n_candidates( kind ), cfg.shape[ kind ], cfg.occ[ kind ] );
-    if( tuneGrp ) cfg.groupPixels = kGroupCand[ tcand % 4 ];
+    if( tuneGrp )
+    {
+        cfg.groupPixels  = kGroupCand[ tcand % 4 ].group;
+        cfg.singlePixels = kGroupCand[ tcand % 4 ].single;
+    }
     // the fused first two iterations need every frame of the step to run at least three
     int minIter = MAX_ATROUS_ITERATIONS;
     for( int k = 0; k < n; k++ ) minIter = std::min( minIter, jobs[ k ].params->atrousIterations ? (int)jobs[ k ].params->atrousIterations : 4 );
@@ -561,34 +580,39 @@ rgdn_status run_step( rgdn_context* c, BatchExec& ex, const rgdn_job* jobs, int 
     GraphKey key;
     memset( &key, 0, sizeof( key ) );
     key.storage = (int)st;
-    // groups: consecutive frames while their pixels stay within the group size
+    // groups: consecutive frames while their pixels stay within the group size; a frame of at
+    // least singlePixels pixels alone
+    bool anySingle           = false;
+    bool single[ MAX_BATCH ] = {};
     {
         uint64_t acc = 0;
         int      j0  = 0;
+        auto     close = [ & ]( int j1, bool alone ) {
+            key.g[ key.ng ].j0     = j0;
+            key.g[ key.ng ].j1     = j1;
+            key.g[ key.ng++ ].single = alone ? 1 : 0;
+            if( alone )
+            {
+                single[ j0 ] = true;
+                anySingle    = true;
+            }
+            j0  = j1;
+            acc = 0;
+        };
         for( int k = 0; k < n; k++ )
         {
             const uint64_t px = (uint64_t)jobs[ k ].stream->W * jobs[ k ].stream->H;
-            if( k > j0 && cfg.groupPixels && acc + px > cfg.groupPixels )
+            if( cfg.singlePixels && px >= cfg.singlePixels )
             {
-                key.g[ key.ng ].j0   = j0;
-                key.g[ key.ng++ ].j1 = k;
-                j0                   = k;
-                acc                  = 0;
+                if( k > j0 ) close( k, false );
+                close( k + 1, true );
+                continue;
             }
+            if( k > j0 && cfg.groupPixels && acc + px > cfg.groupPixels ) close( k, false );
             acc += px;
         }
-        key.g[ key.ng ].j0   = j0;
-        key.g[ key.ng++ ].j1 = n;
+        if( n > j0 ) close( n, false );
     }
-    bool anySingle = false;
-    bool single[ MAX_BATCH ] = {};
-    for( int gi = 0; gi < key.ng; gi++ )
-        if( key.g[ gi ].j1 - key.g[ gi ].j0 == 1 )
-        {
-            key.g[ gi ].single       = 1;
-            single[ key.g[ gi ].j0 ] = true;
-            anySingle                = true;
-        }
     for( int k = 0; k < n; k++ )
     {
         if( single[ k ] )
@@ -723,8 +747,14 @@ rgdn_status run_step( rgdn_context* c, BatchExec& ex, const rgdn_job* jobs, int 
             tu.probes.push_back( { -2, tcand % 4, stepPixels, ga, gb, tcand >= 4 } );
         }
     }
-    if( cudaEventRecord( ds.done[ slot ], cs ) != cudaSuccess ) return RGDN_DEVICE_ERROR;
-    ds.used[ slot ] = true;
+    // the slot's host table is read by the device only when a group ran on the batched kernels
+    bool anyTable = false;
+    for( int gi = 0; gi < key.ng; gi++ ) anyTable = anyTable || !key.g[ gi ].single;
+    if( anyTable )
+    {
+        if( cudaEventRecord( ds.done[ slot ], cs ) != cudaSuccess ) return RGDN_DEVICE_ERROR;
+        ds.used[ slot ] = true;
+    }
     if( tuneLk && ++tu.step >= kTuneRounds * max_candidates() ) r = settle( ex, st );
     else if( tuneGrp && ++tu.step >= kGroupRounds * 4 ) r = settle_groups( ex, st );
     return r;
@@ -806,6 +836,7 @@ rgdn_status batch_get_config( rgdn_context* c, uint32_t storage, rgdn_batch_conf
     out->useGraphs   = cf.graphs ? 1u : 0u;
     out->tuned       = ex->tuner[ storage ].settled ? 1u : 0u;
     out->groupPixels = cf.groupPixels;
+    out->singleFramePixels = cf.singlePixels;
     return RGDN_SUCCESS;
 }
 
@@ -840,7 +871,8 @@ rgdn_status batch_set_config( rgdn_context* c, uint32_t storage, const rgdn_batc
     }
     if( in->atrousFusionDepth == 2 ) candidate( BS_ATROUS0, 4, cf.shape[ BS_ATROUS0 ], cf.occ[ BS_ATROUS0 ] );
     cf.graphs      = in->useGraphs != 0;
-    cf.groupPixels = in->groupPixels;
+    cf.groupPixels  = in->groupPixels;
+    cf.singlePixels = in->singleFramePixels;
     Tuner& tu = ex->tuner[ storage ];
     for( auto& p : tu.probes )
     {

@@ -176,6 +176,63 @@ bool admit( rgdn_server* sv, ServeStream& st )
     }
 }
 
+// ------------------------------------------------------------------------------------------
+// RGDN_HOST_COPY_SM: a frame's pinned host planes copied by one kernel. The planes are split
+// into chunks of kChunkBytes, numbered over the planes in order (plane s holds chunks
+// first[s] .. first[s + 1] - 1); block b copies chunks b, b + grid, ... with 16-byte loads of
+// the device-mapped host pages, four in flight per thread. kGatherBlocks blocks keep about
+// 0.5 MB of loads in flight, enough for the host link's rate, and leave the other SMs to the
+// kernels of the step on the other lane.
+// ------------------------------------------------------------------------------------------
+constexpr int      kGatherThreads = 256;
+constexpr uint32_t kGatherBlocks  = 32;
+constexpr uint64_t kChunkBytes    = 256ull << 10;
+struct GatherList
+{
+    const uint4* src[ RGDN_GBUFFER_PLANES ];
+    uint4*       dst[ RGDN_GBUFFER_PLANES ];
+    uint64_t     n16[ RGDN_GBUFFER_PLANES ];        // 16-byte units of the plane
+    uint32_t     first[ RGDN_GBUFFER_PLANES + 1 ];  // first block of each plane, then the total
+    int          count;
+};
+
+__global__ void __launch_bounds__( kGatherThreads ) k_gather_host( const GatherList L )
+{
+    const uint32_t total = L.first[ L.count ];
+    int            p     = 0;
+    for( uint32_t chunk = blockIdx.x; chunk < total; chunk += gridDim.x )
+    {
+        while( p + 1 < L.count && L.first[ p + 1 ] <= chunk ) p++;
+        const uint64_t per   = kChunkBytes / 16;
+        const uint64_t begin = (uint64_t)( chunk - L.first[ p ] ) * per;
+        const uint64_t end   = begin + per < L.n16[ p ] ? begin + per : L.n16[ p ];
+        const uint4*   src   = L.src[ p ];
+        uint4*         dst   = L.dst[ p ];
+        uint64_t       i     = begin + threadIdx.x;
+        for( ; i + 3 * kGatherThreads < end; i += 4 * kGatherThreads )
+        {
+            const uint4 a = src[ i ], b = src[ i + kGatherThreads ], c = src[ i + 2 * kGatherThreads ], d = src[ i + 3 * kGatherThreads ];
+            dst[ i ]                      = a;
+            dst[ i + kGatherThreads ]     = b;
+            dst[ i + 2 * kGatherThreads ] = c;
+            dst[ i + 3 * kGatherThreads ] = d;
+        }
+        for( ; i < end; i += kGatherThreads ) dst[ i ] = src[ i ];
+    }
+}
+
+// The device address of a pinned, device-mapped host buffer (nullptr otherwise)
+const void* mapped_host( const void* p )
+{
+    cudaPointerAttributes at;
+    if( cudaPointerGetAttributes( &at, p ) != cudaSuccess )
+    {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return at.type == cudaMemoryTypeHost ? at.devicePointer : nullptr;
+}
+
 void record_done( rgdn_server* sv, ServeReq& r, uint32_t state, double t )
 {
     r.state = state;
@@ -199,6 +256,8 @@ rgdn_status enqueue_step( rgdn_server* sv, StepRec& rec, std::vector< rgdn_job >
     for( size_t k = 0; k < jobs.size(); k++ )
     {
         const rgdn_frame_request& q = rq[ k ]->req;
+        GatherList                gl;
+        memset( &gl, 0, sizeof( gl ) );
         for( uint32_t fb = 0; fb < RGDN_GBUFFER_PLANES; fb++ )
         {
             if( q.gbufferMode == RGDN_REQUEST_BIND )
@@ -212,8 +271,27 @@ rgdn_status enqueue_step( rgdn_server* sv, StepRec& rec, std::vector< rgdn_job >
             rgdn_image img;
             rgdn_status r = rgdn_stream_get_framebuffer( sts[ k ], fb, jobs[ k ].frameIndex, &img );
             if( r != RGDN_SUCCESS ) return r;
-            if( cudaMemcpyAsync( img.data, q.gbuffer[ fb ], (size_t)img.pitch_bytes * img.height, cudaMemcpyDefault, cs ) != cudaSuccess )
-                return RGDN_DEVICE_ERROR;
+            const size_t bytes = (size_t)img.pitch_bytes * img.height;
+            if( sv->info.hostCopy == RGDN_HOST_COPY_SM && bytes % 16 == 0 && ( (uintptr_t)img.data & 15 ) == 0 )
+            {
+                const void* m = mapped_host( q.gbuffer[ fb ] );
+                if( m && ( (uintptr_t)m & 15 ) == 0 )
+                {
+                    const int c = gl.count++;
+                    gl.src[ c ]       = static_cast< const uint4* >( m );
+                    gl.dst[ c ]       = static_cast< uint4* >( img.data );
+                    gl.n16[ c ]       = bytes / 16;
+                    gl.first[ c + 1 ] = gl.first[ c ] + (uint32_t)( ( bytes + kChunkBytes - 1 ) / kChunkBytes );
+                    continue;
+                }
+            }
+            if( cudaMemcpyAsync( img.data, q.gbuffer[ fb ], bytes, cudaMemcpyDefault, cs ) != cudaSuccess ) return RGDN_DEVICE_ERROR;
+        }
+        if( gl.count )
+        {
+            k_gather_host<<< std::min( gl.first[ gl.count ], kGatherBlocks ), kGatherThreads, 0, cs >>>( gl );
+            if( cudaGetLastError() != cudaSuccess ) return RGDN_DEVICE_ERROR;
+            sv->ctx->launches.fetch_add( 1, std::memory_order_relaxed );
         }
     }
     if( rec.mark[ 1 ] && cudaEventRecord( rec.mark[ 1 ], cs ) != cudaSuccess ) return RGDN_DEVICE_ERROR;
@@ -436,7 +514,8 @@ extern "C" {
 rgdn_status rgdn_server_create( rgdn_context* ctx, const rgdn_server_create_info* info, rgdn_server** out )
 {
     if( !rgdn::valid_ctx( ctx ) ) return RGDN_WRONG_INSTANCE;
-    if( !info || !out || info->storage > RGDN_STORAGE_BF16 || info->maxFramesPerStep > (uint32_t)rgdn::MAX_BATCH || info->stepsInFlight > 3 )
+    if( !info || !out || info->storage > RGDN_STORAGE_BF16 || info->maxFramesPerStep > (uint32_t)rgdn::MAX_BATCH || info->stepsInFlight > 3 ||
+        info->hostCopy > RGDN_HOST_COPY_SM )
         return RGDN_WRONG_FUNCTION_ARGUMENT;
     cudaSetDevice( ctx->device );
     rgdn_server* sv = new( std::nothrow ) rgdn_server();

@@ -343,10 +343,11 @@ class Server:
     stream's history resident on the device, admission under the context's memory budget."""
 
     def __init__(self, ctx: Context, storage: int, max_frames_per_step: int = 0, max_pixels_per_step: int = 0,
-                 max_queued_per_stream: int = 0, steps_in_flight: int = 2, evict_idle_ms: int = 0):
+                 max_queued_per_stream: int = 0, steps_in_flight: int = 2, evict_idle_ms: int = 0,
+                 host_copy: int = N.HOST_COPY_ENGINE):
         self.ctx, self.lib, self.storage = ctx, ctx.lib, storage
         info = N.ServerCreateInfo(storage, max_frames_per_step, max_pixels_per_step, max_queued_per_stream,
-                                  steps_in_flight, evict_idle_ms)
+                                  steps_in_flight, evict_idle_ms, host_copy)
         h = C.c_void_p()
         N.check(self.lib.rgdn_server_create(ctx.handle, C.byref(info), C.byref(h)), "rgdn_server_create")
         self.handle = h

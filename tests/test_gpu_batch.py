@@ -115,15 +115,17 @@ def test_batch_splits_steps_and_falls_back():
     ctx.close()
 
 
-@pytest.mark.parametrize("shape,occ,depth,group", [(0, 3, 1, 0), (1, 4, 1, 0), (2, 4, 1, 1), (2, 3, 1, 0), (0, 4, 1, 2000),
-                                                   (3, 7, 1, 2000), (0, 3, 2, 1), (3, 7, 2, 0), (3, 7, 2, 2000)])
-def test_batch_fixed_configs(shape, occ, depth, group):
+@pytest.mark.parametrize("shape,occ,depth,group,single", [(0, 3, 1, 0, 0), (1, 4, 1, 0, 0), (2, 4, 1, 1, 0), (2, 3, 1, 0, 0),
+                                                          (0, 4, 1, 2000, 0), (3, 7, 1, 2000, 2000), (0, 3, 2, 1, 1),
+                                                          (3, 7, 2, 0, 0), (3, 7, 2, 2000, 0), (0, 3, 2, 0, 2000)])
+def test_batch_fixed_configs(shape, occ, depth, group, single):
     """A configuration set through rgdn_batch_set_config (no tuning) gives the same results.
     Shape 3 is the 128-thread 32x4 tile (temporal and a-trous; variance then runs one 32x8 tile
     per block). Fusion depth 2 runs a-trous iterations 0 and 1 in one launch; the last frame has
     a stream running only two iterations, where the step falls back to one launch per iteration.
-    Group size 0 runs the three frames as one group, 2000 pixels as two (64x36 alone, on the
-    single-frame kernels, then 50x23 with 34x17), 1 pixel as three single-frame groups."""
+    Group size 0 runs the three frames as one group, 2000 pixels as two (64x36, then 50x23 with
+    34x17), 1 pixel as three; a single-frame size of 2000 pixels runs 64x36 alone on the
+    single-frame kernels, 1 pixel every frame."""
     ctx = Context(0)
     cfg = N.BatchConfig()
     cfg.temporalTile = shape
@@ -136,9 +138,11 @@ def test_batch_fixed_configs(shape, occ, depth, group):
     cfg.useGraphs = 1
     cfg.atrousFusionDepth = depth
     cfg.groupPixels = group
+    cfg.singleFramePixels = single
     ctx.set_batch_config(N.STORAGE_BF16, cfg)
     got = ctx.batch_config(N.STORAGE_BF16)
-    assert got.tuned == 1 and got.temporalTile == shape and got.atrousFusionDepth == depth and got.groupPixels == group
+    assert got.tuned == 1 and got.temporalTile == shape and got.atrousFusionDepth == depth
+    assert got.groupPixels == group and got.singleFramePixels == single
     assert list(got.atrousBlocksPerSM)[1:] == [occ] * 5
     sizes = SIZES[:3]
     scenes = [Scene(w, h, seed=70 + i) for i, (w, h) in enumerate(sizes)]
@@ -193,13 +197,15 @@ def test_batch_timing_and_launch_count():
 
 
 def test_batch_groups_launch_per_group():
-    """Groups of frames: with a group size of 2000 pixels the frames 64x36, 50x23 and 34x17 form
-    the groups {64x36} and {50x23, 34x17}. A group of one frame runs on the single-frame kernels,
-    the other on the batched kernels over jobs 1..2 of the step's table; each launches the whole
-    stage sequence, in order, with the same results as one stream per call."""
+    """Groups of frames: with a group size and a single-frame size of 2000 pixels the frames
+    64x36, 50x23 and 34x17 form the groups {64x36} and {50x23, 34x17}. The first runs on the
+    single-frame kernels, the other on the batched kernels over jobs 1..2 of the step's table;
+    each launches the whole stage sequence, in order, with the same results as one stream per
+    call."""
     ctx = Context(0)
     cfg = ctx.batch_config(N.STORAGE_FP16)
     cfg.groupPixels = 2000
+    cfg.singleFramePixels = 2000
     cfg.useGraphs = 1
     ctx.set_batch_config(N.STORAGE_FP16, cfg)
     sizes = SIZES[:1] + SIZES[1:3]

@@ -145,3 +145,36 @@ def test_stale_frames_are_dropped():
         assert r.state == N.FRAME_DONE and r.frameIndex == 0
         assert sv.stats()["framesDropped"] == 2
     ctx.close()
+
+
+def test_sm_host_copy_equals_copy_engine():
+    """RGDN_HOST_COPY_SM: the planes of requests in pinned host memory are loaded by one kernel
+    per frame instead of the copy engines. The results are the same bit for bit, and the kernel
+    runs (one launch more per frame). The 130x36 frame's 1-byte IS_SKY plane (4680 bytes, not a
+    multiple of 16) still goes through cudaMemcpyAsync."""
+    torch = pytest.importorskip("torch")
+    ctx = Context(0)
+    W, H = 130, 36
+    frames = [Scene(W, H, seed=95).generate(f) for f in range(6)]
+    pinned = [({n: torch.from_numpy(np.ascontiguousarray(a).view(np.uint8).reshape(-1)).pin_memory() for n, a in b.items()}, p)
+              for b, p in frames]
+    results, launches = {}, {}
+    for mode in (N.HOST_COPY_ENGINE, N.HOST_COPY_SM):
+        outs = []
+        before = ctx.launch_count()
+        with Server(ctx, N.STORAGE_FP16, host_copy=mode) as sv:
+            sid = sv.open_stream(W, H)
+            for b, p in pinned:
+                out = torch.zeros(pre_final_bytes(W, H, N.STORAGE_FP16), dtype=torch.uint8).pin_memory()
+                req = Server.request(sid, p, {n: t.data_ptr() for n, t in b.items()}, N.REQUEST_COPY, out.data_ptr())
+                r = sv.wait(sv.submit(req))
+                assert r.state == N.FRAME_DONE
+                hist, avg, _ = sv.stream(sid).tonemapping()
+                outs.append((out.numpy().copy(), hist.copy(), avg))
+        launches[mode] = ctx.launch_count() - before
+        results[mode] = outs
+    for f, ((oa, ha, aa), (ob, hb, ab)) in enumerate(zip(results[N.HOST_COPY_ENGINE], results[N.HOST_COPY_SM])):
+        assert np.array_equal(oa, ob), f"frame {f}: PRE_FINAL differs"
+        assert np.array_equal(ha, hb) and aa == ab, f"frame {f}: tonemapping differs"
+    assert launches[N.HOST_COPY_SM] - launches[N.HOST_COPY_ENGINE] == len(frames)
+    ctx.close()
