@@ -54,11 +54,10 @@ def parse():
     ap.add_argument("--iters", type=int, default=5, help="a-trous passes")
     ap.add_argument("--frames", type=int, default=60, help="distinct frames in the sequence")
     ap.add_argument("--e2e-steps", type=int, default=120)
-    ap.add_argument("--path", default="fused", choices=["fused", "plain", "tma", "pair", "gradchain"],
+    ap.add_argument("--path", default="fused", choices=["fused", "plain", "tma", "pair"],
                     help="fused: the default kernels; plain: one kernel per reference dispatch; "
                          "tma: the default kernels with TMA-staged a-trous; pair: the default kernels with "
-                         "a-trous iterations 0 and 1 in one launch; gradchain: the default kernels with the "
-                         "gradient samples and gradient a-trous in one cooperative launch")
+                         "a-trous iterations 0 and 1 in one launch")
     ap.add_argument("--no-cpu-baseline", action="store_true", help="skip the CPU oracle (baseline and parity)")
     ap.add_argument("--parity-frames", type=int, default=8, help="frames run on GPU and oracle for the parity figures")
     ap.add_argument("--no-batched", action="store_true", help="skip the 32-stream batched measurement")
@@ -195,9 +194,6 @@ def stage_bytes(storage: str) -> dict:
     # reshaded, IndirAccum_Prev, DISGradientHistory; writes DISPing + prev pix
     b["gradient_samples"] = 8 + 4 + g * (1 + 8 + col3 + 4 + 1) + g * (4 + 1)
     b["gradient_atrous"] = g * (4 + 4)
-    # the samples and the four iterations in one launch: the samples' reads, one gradient image
-    # write each for the history, the pong and the ping (the iterations' intermediates stay in L2)
-    b["gradient_chain"] = b["gradient_samples"] + g * (4 + 4 + 4)
     # temporal accumulation: cur G-buffer + prev history (bilinear taps counted once) + writes
     b["temporal_accumulation"] = (12 + 8 + 8 + 2 + 4 + 2 + 16 + g * 4) + \
         (2 + 4 + cv_rgb + mom + hl + col3 + col3 + 16) + (col3 + mom + hl + col3 + col3)
@@ -595,7 +591,7 @@ def run_batched(args, dist: Dist, dev: int, cs) -> dict:
     for (name, it), (n, ms) in tim.items():
         if name == "atrous":
             alg = kernel_bytes("atrous_fast", it, args.iters, per_px) * px
-        elif name in ("gradient_samples", "gradient_atrous", "gradient_chain"):
+        elif name in ("gradient_samples", "gradient_atrous"):
             alg = per_px[name] * px
         else:
             alg = per_px.get({"temporal_accumulation": "temporal_fast_gp", "anti_firefly": "anti_firefly_fast",
@@ -856,8 +852,6 @@ def run_ours(args, dist: Dist):
             p.flags |= N.FLAG_TMA_STAGING
         elif args.path == "pair":
             p.flags |= N.FLAG_ATROUS_PAIR
-        elif args.path == "gradchain":
-            p.flags |= N.FLAG_GRADIENT_ONE_LAUNCH
         dev_bufs = {}
         for name, arr in bufs.items():
             t = torch.from_numpy(np.ascontiguousarray(arr).view(np.uint8).reshape(-1)).to(f"cuda:{dev}")

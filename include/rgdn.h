@@ -228,10 +228,6 @@ typedef struct rgdn_frame_params
                                              out (after a short limit) with all its copies landed:
                                              the pass sets RGDN_DEVICE_ERROR_TMA_WAIT and leaves its
                                              outputs as they were */
-#define RGDN_FLAG_GRADIENT_ONE_LAUNCH 0x20u /* gradient samples and the four gradient a-trous
-                                             iterations in one cooperative launch with grid
-                                             barriers between them (as many blocks as fit on the
-                                             GPU at once); the same images bit for bit */
 #define RGDN_FLAG_STAGE_DEFAULT      0x10u /* rgdn_denoise_stage runs the default path's kernel for
                                              the stage (with RGDN_FLAG_EXACT_MATH: its IEEE form)
                                              instead of the one-kernel-per-dispatch form; the last
@@ -456,11 +452,8 @@ rgdn_status rgdn_get_tonemapping( rgdn_stream* stream, uint32_t* outHistogram256
  * work on cudaStream (synchronising it). Every wait inside a kernel is bounded; one that runs
  * out sets a bit and lets the kernel finish, so the frames since the last call are unreliable
  * but the device is not hung:
- *   bit 0  a TMA-staged a-trous pass stopped waiting for its copies (RGDN_FLAG_TMA_STAGING)
- *   bit 1  a block of the one-launch gradient chain stopped waiting at its grid barrier (that
- *          frame's gradient images are incomplete; the call also resets the barrier) */
+ *   bit 0  a TMA-staged a-trous pass stopped waiting for its copies (RGDN_FLAG_TMA_STAGING) */
 #define RGDN_DEVICE_ERROR_TMA_WAIT 1u
-#define RGDN_DEVICE_ERROR_GRID_BARRIER 2u
 rgdn_status rgdn_stream_take_device_errors( rgdn_stream* stream, uint32_t* outFlags, rgdn_cuda_stream cudaStream );
 /* Asynchronous copy, in cudaStream order, of { uint histogram[256]; float avgLuminance; }
  * (1028 bytes) to dst (host, pinned for overlap, or device). No reference counterpart: later

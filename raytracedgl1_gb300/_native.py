@@ -51,7 +51,6 @@ STAGE_LUMINANCE_HISTOGRAM, STAGE_LUMINANCE_AVG = 6, 7
 
 FLAG_PLAIN, FLAG_SKIP_GRADIENTS, FLAG_EXACT_MATH, FLAG_TMA_STAGING, FLAG_STAGE_DEFAULT = 0x1, 0x2, 0x4, 0x8, 0x10
 FLAG_ATROUS_PAIR = 0x40
-FLAG_GRADIENT_ONE_LAUNCH = 0x20
 FLAG_TEST_TMA_TIMEOUT = 0x80000000
 
 
@@ -173,7 +172,6 @@ class BatchConfig(C.Structure):
 
 TILE_32X8, TILE_16X16, TILE_64X4, TILE_32X4, TILE_32X8_PER_BLOCK = 0, 1, 2, 3, 4
 DEVICE_ERROR_TMA_WAIT = 1
-DEVICE_ERROR_GRID_BARRIER = 2
 
 GBUFFER_PLANES = 15
 REQUEST_COPY, REQUEST_BIND = 0, 1
@@ -272,7 +270,7 @@ KERNEL_NAMES.update({100: "atrous_fast", 101: "atrous_fast_hist", 102: "temporal
                      107: "atrous_exact", 108: "temporal_exact_geom", 109: "variance_exact_geom",
                      110: "temporal_fast_gp", 111: "temporal_exact_geom_gp", 112: "atrous_tma",
                      113: "atrous_tma_hist", 114: "prepare_final", 115: "bloom",
-                     117: "process_scattering", 122: "atrous_pair", 123: "gradient_chain",
+                     117: "process_scattering", 122: "atrous_pair",
                      200: "single_frame_group"})
 
 _lib = None

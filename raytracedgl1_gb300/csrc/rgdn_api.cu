@@ -508,23 +508,9 @@ rgdn_status run_denoise_fused( rgdn_stream* s, uint32_t fi, const rgdn_frame_par
     fill_args( s, fi, p, a );
     if( !( p->flags & RGDN_FLAG_SKIP_GRADIENTS ) )
     {
-        if( ( p->flags & RGDN_FLAG_GRADIENT_ONE_LAUNCH ) && s->ctx->gradientChainOk )
-        {
-            // one cooperative launch; a device that refuses it takes the five launches from then on
-            r = launch( s, a, KF_GRADIENT_CHAIN, 0, cs );
-            if( r != RGDN_SUCCESS )
-            {
-                cudaGetLastError();
-                s->ctx->gradientChainOk = false;
-            }
-        }
-        else r = RGDN_DEVICE_ERROR;
-        if( r != RGDN_SUCCESS )
-        {
-            if( ( r = launch_default_stage( s, a, fi, p, RGDN_STAGE_GRADIENT_SAMPLES, 0, cs ) ) != RGDN_SUCCESS ) return r;
-            for( int i = 0; i < 4; i++ )
-                if( ( r = launch_default_stage( s, a, fi, p, RGDN_STAGE_GRADIENT_ATROUS, i, cs ) ) != RGDN_SUCCESS ) return r;
-        }
+        if( ( r = launch_default_stage( s, a, fi, p, RGDN_STAGE_GRADIENT_SAMPLES, 0, cs ) ) != RGDN_SUCCESS ) return r;
+        for( int i = 0; i < 4; i++ )
+            if( ( r = launch_default_stage( s, a, fi, p, RGDN_STAGE_GRADIENT_ATROUS, i, cs ) ) != RGDN_SUCCESS ) return r;
     }
     for( int stage : { (int)RGDN_STAGE_TEMPORAL_ACCUMULATION, (int)RGDN_STAGE_ANTI_FIREFLY, (int)RGDN_STAGE_VARIANCE_ESTIMATION } )
         if( ( r = launch_default_stage( s, a, fi, p, stage, 0, cs ) ) != RGDN_SUCCESS ) return r;
@@ -1303,11 +1289,8 @@ rgdn_status rgdn_stream_take_device_errors( rgdn_stream* s, uint32_t* outFlags, 
     if( cudaMemcpyAsync( &flags, &s->tm->errorFlags, sizeof( flags ), cudaMemcpyDeviceToHost, st ) != cudaSuccess ||
         cudaStreamSynchronize( st ) != cudaSuccess )
         return RGDN_DEVICE_ERROR;
-    // a grid barrier that ran out may have left arrivals counted: the error word and the
-    // barrier's count are reset together
-    const size_t clear = ( flags & RGDN_DEVICE_ERROR_GRID_BARRIER ) ? offsetof( Tonemapping, barrierGen ) - offsetof( Tonemapping, errorFlags )
-                                                                     : sizeof( uint32_t );
-    if( flags && ( cudaMemsetAsync( &s->tm->errorFlags, 0, clear, st ) != cudaSuccess || cudaStreamSynchronize( st ) != cudaSuccess ) )
+    if( flags && ( cudaMemsetAsync( &s->tm->errorFlags, 0, sizeof( uint32_t ), st ) != cudaSuccess ||
+                   cudaStreamSynchronize( st ) != cudaSuccess ) )
         return RGDN_DEVICE_ERROR;
     *outFlags = flags;
     return RGDN_SUCCESS;

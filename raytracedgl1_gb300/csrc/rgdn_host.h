@@ -30,7 +30,6 @@ struct rgdn_context
     float2*                 thetaTab = nullptr;   // (cos theta_k, sin theta_k)
     float*                  decayTab = nullptr;   // pow(1 - k/255, 10), k = 0..255
     std::atomic< uint64_t > launches{ 0 };
-    std::atomic< bool >     gradientChainOk{ true };   // the device accepts the cooperative gradient chain
     std::mutex              batchMtx;              // guards `batch`
     rgdn::BatchExec*        batch = nullptr;       // created by the first batched submission
     uint32_t                magic = 0x52474443u;

@@ -29,7 +29,6 @@ struct Tonemapping
     uint32_t histogram[ 256 ];
     float    avgLuminance;
     uint32_t errorFlags;   // device-side failures (RGDN_DEVICE_ERROR_*)
-    uint32_t barrierCount, barrierGen;   // the grid barrier of the one-launch gradient chain
 };
 
 // The subset of ShGlobalUniform (ShaderCommonC.h:209-304) this path reads, plus sizes.
@@ -232,7 +231,6 @@ enum FusedKernel : int
     KF_BLOOM               = 115,  // the bloom pyramid and its application (timing label)
     KF_SCATTER_ACCUM       = 117,  // volume integration + screen-space accumulation (timing label)
     KF_ATROUS_PAIR01       = 122,  // a-trous iterations 0 and 1 in one launch (fusion depth 2)
-    KF_GRADIENT_CHAIN      = 123,  // gradient samples + gradient a-trous 0..3, one cooperative launch
 };
 
 // Launches one stage for one frame. Returns the CUDA error of the launch.

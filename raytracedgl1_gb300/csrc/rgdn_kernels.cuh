@@ -779,100 +779,6 @@ template< int M > __global__ void __launch_bounds__( 256, 6 ) k_gradient_samples
     gradient_samples_tile< M >( a, dst, blockIdx.x, blockIdx.y, u8 );
 }
 
-// ------------------------------------------------------------------------------------------
-// Gradient samples and the four gradient a-trous iterations in one cooperative launch.
-//
-// The gradient image is 1/9 of the frame (230 400 texels at 1920x1080), so each of the five
-// separate launches is short and mostly launch and drain. Here every block of a grid that fits
-// on the GPU at once loops over the texels of each phase and meets the others at a grid barrier
-// between phases. A phase reads what other blocks wrote in the phase before through L2
-// (ld.global.cg): an SM's L1 may still hold lines of a ping/pong image from two phases earlier.
-// The per-texel arithmetic is gradient_sample_px's and gradient_atrous_texel's, so the images
-// are those of the five launches bit for bit.
-// ------------------------------------------------------------------------------------------
-constexpr uint32_t kGridBarrierSpins = 1u << 22;   // with 64 ns sleeps: about a quarter second
-
-// A barrier over every block of the grid (which must be resident at once: a cooperative
-// launch). Thread 0 of the block arrives on tm->barrierCount; the last block to arrive resets it
-// and advances tm->barrierGen, which the others wait for. A wait that runs out sets
-// RGDN_DEVICE_ERROR_GRID_BARRIER and makes the barrier return false for the block; `ok` false
-// skips the wait (a block that already failed).
-__device__ __forceinline__ bool grid_barrier( Tonemapping* tm, const bool ok )
-{
-    __shared__ int sOk;
-    __syncthreads();
-    if( threadIdx.x == 0 && threadIdx.y == 0 )
-    {
-        int good = ok ? 1 : 0;
-        if( good )
-        {
-            volatile uint32_t* gen = &tm->barrierGen;
-            const uint32_t     g   = *gen;   // the generation this barrier ends
-            __threadfence();                 // the block's writes, then its arrival
-            if( atomicAdd( &tm->barrierCount, 1u ) == gridDim.x * gridDim.y - 1u )
-            {
-                atomicExch( &tm->barrierCount, 0u );
-                __threadfence();
-                atomicAdd( &tm->barrierGen, 1u );
-            }
-            else
-            {
-                uint32_t spins = 0;
-                while( *gen == g )
-                {
-                    if( ++spins > kGridBarrierSpins )
-                    {
-                        atomicOr( &tm->errorFlags, RGDN_DEVICE_ERROR_GRID_BARRIER );
-                        good = 0;
-                        break;
-                    }
-                    __nanosleep( 64 );
-                }
-            }
-            __threadfence();
-        }
-        sOk = good;
-    }
-    __syncthreads();
-    return sOk != 0;
-}
-
-template< int M > __global__ void __launch_bounds__( 256 ) k_gradient_chain( const FrameArgs a )
-{
-    __shared__ float u8[ 256 ];
-    const int        t = threadIdx.x;
-    pdl_launch_dependents();
-    fill_u8( u8, t );
-    pdl_wait();
-    __syncthreads();
-    const Uniform& u  = a.u;
-    const int      n  = u.GW * u.GH;
-    const int      g0 = blockIdx.x * 256 + t, gs = gridDim.x * 256;
-    for( int e = g0; e < n; e += gs )
-    {
-        const int gy = e / u.GW, gx = e - gy * u.GW;
-        if( gx * STRATA < u.W && gy * STRATA < u.H ) gradient_sample_px< M >( a, a.disPing, gx, gy, u8 );
-    }
-    bool ok = true;
-#pragma unroll 1
-    for( int iter = 0; iter < 4; iter++ )
-    {
-        ok = grid_barrier( a.tm, ok );
-        if( !ok ) return;
-        const uint32_t* src = ( iter % 2 == 0 ) ? a.disPing : a.disPong;
-        uint32_t*       dst = ( iter % 2 == 0 ) ? a.disPong : a.disPing;
-        auto fetch = [ & ]( int x, int y ) { return ( x >= 0 && y >= 0 && x < u.GW && y < u.GH ) ? __ldcg( src + y * u.GW + x ) : 0u; };
-        for( int e = g0; e < n; e += gs )
-        {
-            const int gy = e / u.GW, gx = e - gy * u.GW;
-            if( gx * STRATA >= u.W || gy * STRATA >= u.H ) continue;
-            const uint32_t packed = gradient_atrous_texel( u, fetch, gx, gy, iter, u8 );
-            dst[ e ] = packed;
-            if( iter == 0 ) a.disHist[ e ] = packed;
-        }
-    }
-}
-
 template< int M > __global__ void __launch_bounds__( 256 ) k_gradient_atrous( const FrameArgs a, const int iter )
 {
     __shared__ float u8[ 256 ];
@@ -3823,41 +3729,6 @@ template< int M, bool FAST > __global__ void __launch_bounds__( 256, 6 ) k_scatt
 }  // namespace dev
 
 
-// The gradient chain as one cooperative launch: as many 256-thread blocks as fit on the GPU at
-// once (the occupancy of the kernel times the SMs, cached per device), at most one per 256
-// texels; programmatic dependent launch as the other kernels of the path.
-template< int M > cudaError_t launch_gradient_chain( const FrameArgs& a, cudaStream_t s )
-{
-    static std::atomic< int > resident[ 64 ];
-    int                       d = 0;
-    cudaError_t               e = cudaGetDevice( &d );
-    if( e != cudaSuccess ) return e;
-    int r = resident[ d & 63 ].load( std::memory_order_relaxed );
-    if( r <= 0 )
-    {
-        int perSm = 0, sms = 0;
-        if( ( e = cudaOccupancyMaxActiveBlocksPerMultiprocessor( &perSm, dev::k_gradient_chain< M >, 256, 0 ) ) != cudaSuccess ) return e;
-        if( ( e = cudaDeviceGetAttribute( &sms, cudaDevAttrMultiProcessorCount, d ) ) != cudaSuccess ) return e;
-        r = perSm * sms;
-        if( r <= 0 ) return cudaErrorCooperativeLaunchTooLarge;
-        resident[ d & 63 ].store( r, std::memory_order_relaxed );
-    }
-    const int          texels = a.u.GW * a.u.GH;
-    const int          grid   = std::max( 1, std::min( r, ( texels + 255 ) / 256 ) );
-    cudaLaunchConfig_t cfg    = {};
-    cfg.gridDim               = dim3( grid );
-    cfg.blockDim              = dim3( 256 );
-    cfg.stream                = s;
-    cudaLaunchAttribute at[ 2 ];
-    at[ 0 ].id                                         = cudaLaunchAttributeCooperative;
-    at[ 0 ].val.cooperative                            = 1;
-    at[ 1 ].id                                         = cudaLaunchAttributeProgrammaticStreamSerialization;
-    at[ 1 ].val.programmaticStreamSerializationAllowed = 1;
-    cfg.attrs                                          = at;
-    cfg.numAttrs                                       = 2;
-    return cudaLaunchKernelEx( &cfg, dev::k_gradient_chain< M >, a );
-}
-
 // ------------------------------------------------------------------------------------------
 // launcher for one mode
 // ------------------------------------------------------------------------------------------
@@ -3871,7 +3742,6 @@ template< int M > cudaError_t launch_stage_t( const FrameArgs& a, int stage, int
     {
         case RGDN_STAGE_GRADIENT_SAMPLES: e = launch_pdl( dev::k_gradient_samples< M >, gridG, blk, 0, s, a, a.disPing ); break;
         case RGDN_STAGE_GRADIENT_ATROUS: e = launch_pdl( dev::k_gradient_atrous< M >, gridG, blk, 0, s, a, iter ); break;
-        case KF_GRADIENT_CHAIN: e = launch_gradient_chain< M >( a, s ); break;
         case RGDN_STAGE_TEMPORAL_ACCUMULATION: e = launch_pdl( dev::k_temporal< M, false, false, false >, grid, blk, 0, s, a ); break;
         case KF_TEMPORAL_EXACT_GEOM: e = launch_pdl( dev::k_temporal< M, false, true, false >, grid, blk, 0, s, a ); break;
         case KF_TEMPORAL_EXACT_GEOM_GP: e = launch_pdl( dev::k_temporal< M, false, true, true >, grid, blk, 0, s, a ); break;

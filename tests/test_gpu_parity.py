@@ -395,36 +395,6 @@ def test_atrous_pair_equals_single(ctx, mode_name, mode, size):
     b.close()
 
 
-@pytest.mark.parametrize("mode_name,mode", [("fp16", N.STORAGE_FP16), ("ref", N.STORAGE_REF)])
-@pytest.mark.parametrize("size", [(250, 151), (97, 33), (1920, 1080)])
-def test_gradient_one_launch_equals_five(ctx, mode_name, mode, size):
-    """Gradient samples and the four gradient a-trous iterations in one cooperative launch with
-    grid barriers (RGDN_FLAG_GRADIENT_ONE_LAUNCH) give the five launches' planes bit for bit,
-    frame after frame, and no barrier wait runs out."""
-    W, H = size
-    sc = Scene(W, H, seed=31, lightFlickerFrom=2.0)
-    a = Stream(ctx, W, H, mode)
-    b = Stream(ctx, W, H, mode)
-    for f in range(4):
-        fi = f & 1
-        bufs, p = sc.generate(f)
-        upload_frame(a, None, bufs, fi)
-        upload_frame(b, None, bufs, fi)
-        pa = p.copy()
-        pa.flags = N.FLAG_GRADIENT_ONE_LAUNCH
-        for s, q in ((a, pa), (b, p)):
-            Denoiser(s).Denoise(fi, q)
-            Tonemapping(s).CalculateExposure(fi, q)
-        ga, gb = gpu_planes(a), gpu_planes(b)
-        for key in ga:
-            assert np.array_equal(ga[key][0], gb[key][0]), f"frame {f}: {key} differs"
-        ta, tb = a.tonemapping(), b.tonemapping()
-        assert np.array_equal(ta[0], tb[0]) and ta[1] == tb[1]
-    assert a.take_device_errors() == 0 and b.take_device_errors() == 0
-    a.close()
-    b.close()
-
-
 def reshade_bind(s, o, sc, f):
     """Frame f's re-shading scene: device copies bound to GPU stream s, host arrays to the oracle
     o (None to skip). Returns the device buffers, which must outlive the frames that use them."""
