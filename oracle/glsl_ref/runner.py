@@ -1,0 +1,123 @@
+"""Runs the reference's own shaders (oracle/_ref/librgdn_refshaders.so, built by build.py from
+the reference's GLSL sources) beside the oracle, stage by stage, on the same state: test
+infrastructure that pins the oracle to the reference.
+
+Each stage is dispatched the way Denoiser::Denoise and Tonemapping::CalculateExposure
+dispatch it (Source/Denoiser.cpp:92-253, Source/Tonemapping.cpp:106-165): 16x16 groups over the
+render size, the gradient a-trous over renderWidth / 3 (a float, rounded up), the luminance
+average as one group of 256. The reference's framebuffers are bound by name to copies of the
+oracle's planes (frame slot fi as framebufX, slot fi ^ 1 as framebufX_Prev), in the reference
+framebuffer formats (the oracle's MODE_REF).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB = os.path.join(os.path.dirname(HERE), "_ref", "librgdn_refshaders.so")
+
+_lib = None
+
+
+def load(path: str = LIB) -> C.CDLL:
+    global _lib
+    if _lib is None:
+        _lib = C.CDLL(path)
+        _lib.ref_bind.argtypes = [C.c_char_p, C.c_void_p, C.c_int, C.c_int]
+        _lib.ref_bind.restype = C.c_int
+        _lib.ref_texel_bytes.argtypes = [C.c_char_p]
+        _lib.ref_texel_bytes.restype = C.c_int
+    return _lib
+
+
+def ref_name(fb: str) -> str:
+    """The reference's image name of a framebuffer (DIFF_ACCUM_COLOR -> framebufDiffAccumColor)."""
+    return "framebuf" + "".join(w if w == "DIS" else w.capitalize() for w in fb.split("_"))
+
+
+def stage_plan(W: int, H: int, niter: int = 4):
+    """(oracle stage, iteration, reference entry point, groups) in Denoise + CalculateExposure
+    order, from the gradient a-trous on (the gradient samples are a ray-generation shader)."""
+    from raytracedgl1_gb300 import _native as N
+    gw, gh = -(-W // 3), -(-H // 3)
+    full = ((W + 15) // 16, (H + 15) // 16)
+    plan = [(N.STAGE_GRADIENT_ATROUS, i, f"CmASVGFGradientAtrous_{i}", ((gw + 15) // 16, (gh + 15) // 16)) for i in range(4)]
+    plan += [(N.STAGE_TEMPORAL_ACCUMULATION, 0, "CmSVGFTemporalAccumulation", full),
+             (N.STAGE_ANTI_FIREFLY, 0, "CmAntiFirefly", full),
+             (N.STAGE_VARIANCE_ESTIMATION, 0, "CmSVGFEstimateVariance", full)]
+    plan += [(N.STAGE_ATROUS, i, "CmSVGFAtrous_Iter0" if i == 0 else f"CmSVGFAtrous_{i}", full) for i in range(niter)]
+    plan += [(N.STAGE_LUMINANCE_HISTOGRAM, 0, "CmLuminanceHistogram", full),
+             (N.STAGE_LUMINANCE_AVG, 0, "CmLuminanceAvg", (1, 1))]
+    return plan
+
+
+class RefRun:
+    """The reference shaders' state for one frame: copies of the oracle's planes bound by name."""
+
+    def __init__(self, W: int, H: int, lib: C.CDLL | None = None):
+        self.W, self.H = W, H
+        self.lib = lib or load()
+        self.arrays: dict = {}
+
+    def bind_from(self, planes: dict, fi: int) -> None:
+        """planes: {(fb name, slot): array}; binds copies (kept in self.arrays)."""
+        self.arrays = {}
+        for (fb, slot), arr in planes.items():
+            name = ref_name(fb) + ("" if slot == fi else "_Prev")
+            if not self.lib.ref_texel_bytes(name.encode()):
+                continue
+            a = np.ascontiguousarray(arr).copy()
+            self.lib.ref_bind(name.encode(), a.ctypes.data, a.shape[1], a.shape[0])
+            self.arrays[(fb, slot)] = a
+
+    def run(self, tag: str, groups, params, tonemapping=None):
+        """Dispatches one reference shader; `tonemapping` (histogram uint32[256], avg float) is the
+        buffer's state before it, and the state after it is returned."""
+        f = getattr(self.lib, f"ref_{tag}_set_uniform", None)
+        if f is not None:
+            f(C.byref(params), C.c_float(self.W), C.c_float(self.H))
+        tm = getattr(self.lib, f"ref_{tag}_tonemapping", None)
+        ptr = None
+        if tm is not None:
+            tm.restype = C.c_void_p
+            ptr = tm()
+            h32 = np.ascontiguousarray(np.asarray(tonemapping[0], dtype=np.uint32))
+            a32 = np.array([tonemapping[1]], dtype=np.float32)
+            C.memmove(ptr, h32.ctypes.data, 1024)
+            C.memmove(ptr + 1024, a32.ctypes.data, 4)
+        getattr(self.lib, f"ref_{tag}_dispatch")(int(groups[0]), int(groups[1]))
+        if ptr is None:
+            return None
+        return (np.frombuffer(C.string_at(ptr, 1024), dtype=np.uint32).copy(),
+                float(np.frombuffer(C.string_at(ptr + 1024, 4), dtype=np.float32)[0]))
+
+
+def oracle_planes(o, fi: int) -> dict:
+    """Copies of every plane of an OracleStream: {(fb name, slot): array}, the previous-frame slot
+    only for planes that have one."""
+    from raytracedgl1_gb300 import _native as N
+    out = {}
+    for fb in N.FB_NAMES:
+        cur, prev = o.plane(fb, fi), o.plane(fb, fi ^ 1)
+        if cur is None:
+            continue
+        out[(fb, fi)] = np.ascontiguousarray(cur).copy()
+        # a plane without a previous-frame slot answers both slots with the same memory
+        if prev is not None and prev.ctypes.data != cur.ctypes.data:
+            out[(fb, fi ^ 1)] = np.ascontiguousarray(prev).copy()
+    return out
+
+
+def differing(a: dict, b: dict) -> list:
+    """[(fb, slot, texels that differ)] between two plane sets (keys of a)."""
+    bad = []
+    for key, x in a.items():
+        y = b[key]
+        if not np.array_equal(x.view(np.uint8), y.view(np.uint8)):
+            xx = x.reshape(x.shape[0], x.shape[1], -1)
+            yy = y.reshape(y.shape[0], y.shape[1], -1)
+            bad.append((key[0], key[1], int(np.count_nonzero(np.any(xx != yy, axis=-1)))))
+    return bad

@@ -5,13 +5,18 @@
 //  Only the tests, __graft_entry__.smoke() and bench.py's CPU-baseline / reference arm use
 //  it, as the checker. The product library never links, loads or calls anything here.
 //
-//  Parity status: UNPINNED against the reference itself. The reference path is GLSL for
-//  Vulkan; it cannot be compiled or run in this environment (no glslc, no Vulkan loader,
-//  no software renderer) and its own tests hold no golden vectors (Tests/RtglTest.cpp is an
-//  interactive viewer). The codecs below are pinned by known-answer tests taken from the
-//  public specs they implement (IEEE-754 binary16/bfloat16, EXT_texture_shared_exponent,
-//  the Vulkan B10G11R11 unsigned-float layout); the stage math is pinned by the
-//  closed-form known-answer tests in tests/.
+//  Parity status: PINNED to the reference's own shader sources for the compute stages. The
+//  reference path is GLSL for Vulkan, which no machine here runs; oracle/glsl_ref/ runs those
+//  GLSL sources on the CPU instead (a mechanical rewrite to C++ over a GLSL runtime written
+//  for it), dispatched as the reference dispatches them, and tests/test_ref_shaders.py
+//  requires every plane and the tonemapping buffer to equal this oracle's bit for bit after
+//  every stage: the gradient a-trous, temporal accumulation, anti-firefly, variance, the
+//  a-trous iterations with the composition, the histogram and the adaptation (committed
+//  vectors in tests/golden, and live where the reference checkout is present). The gradient
+//  samples (a ray-generation shader) and the stages beyond the reference's compute shaders
+//  stay pinned only by the codecs' known-answer tests from the public specs they implement
+//  (IEEE-754 binary16/bfloat16, EXT_texture_shared_exponent, the Vulkan B10G11R11
+//  unsigned-float layout) and the closed-form known-answer tests in tests/.
 //
 //  Conventions shared with the GPU path (each is a choice where GLSL leaves freedom):
 //   * texelFetch / imageLoad outside the image returns an all-zero texel (raw bits 0, then
@@ -1454,7 +1459,7 @@ template< class T > struct Denoise
                         }
                     const T inv = (T)1 / ws, invS = (T)1 / wsS, invI = (T)1 / wsI;
                     outDiff = outDiff * inv;
-                    outVar  = outVar * inv * inv;
+                    outVar  = outVar * ( inv * inv );   // outVariance *= invWeightSum * invWeightSum
                     outSpec = outSpec * invS;
                     outInd  = outInd * invI;
                 }

@@ -1980,7 +1980,7 @@ __device__ __forceinline__ void atrous_finish( AtrousAcc& acc, float3& outDiff, 
 {
     const float inv = 1.0f / acc.ws, invS = 1.0f / acc.wsS, invI = 1.0f / acc.wsI;
     outDiff = mul( acc.d, inv );
-    outVar  = acc.var * inv * inv;
+    outVar  = acc.var * ( inv * inv );   // outVariance *= invWeightSum * invWeightSum (CmSVGFAtrous.comp:217)
     outSpec = mul( acc.s, invS );
     outInd  = mul( acc.i, invI );
 }

@@ -1,0 +1,128 @@
+"""The oracle against the reference's own shaders.
+
+The reference's A-SVGF and tonemapping compute shaders (Source/Shaders/CmASVGFGradientAtrous.comp,
+CmSVGFTemporalAccumulation.comp, CmAntiFirefly.comp, CmSVGFEstimateVariance.comp,
+CmSVGFAtrous_Iter0.comp, CmSVGFAtrous.comp, CmLuminanceHistogram.comp, CmLuminanceAvg.comp) run on
+the CPU from their GLSL sources (oracle/glsl_ref: a mechanical rewrite to C++ over a GLSL runtime),
+dispatched as Denoiser::Denoise and Tonemapping::CalculateExposure dispatch them. Every plane of
+both frame slots and the tonemapping buffer must equal the oracle's bit for bit after every stage.
+
+- test_oracle_matches_reference_vectors: from the committed vectors (tests/golden, written by
+  tests/golden/make_ref_shader_vectors.py), wherever the oracle builds.
+- test_oracle_matches_reference_shaders_live: the same, live, at sizes with partial workgroups
+  and odd gradient images, where the reference checkout is present (it builds oracle/_ref first).
+- test_a_planted_mistake_is_caught: a texel of one input changed on the oracle's side only
+  must show up as a difference.
+"""
+import glob
+import os
+
+import numpy as np
+import pytest
+
+import oracle
+from oracle.glsl_ref import runner
+from raytracedgl1_gb300 import _native as N
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+GOLDEN = sorted(glob.glob(os.path.join(ROOT, "tests", "golden", "ref_shaders_*.npz")))
+REFERENCE = "/root/reference"
+
+
+def load_state(o, z, fi):
+    for key in z.files:
+        if key.startswith("s0/"):
+            _, fb, slot = key.split("/")
+            o.load(fb, int(slot), z[key])
+
+
+def expected_state(z, k, state):
+    for key in z.files:
+        if key.startswith(f"k{k}/") and key.count("/") == 2:
+            _, fb, slot = key.split("/")
+            state[(fb, int(slot))] = z[key]
+    return state
+
+
+@pytest.mark.parametrize("path", GOLDEN, ids=[os.path.basename(p) for p in GOLDEN])
+def test_oracle_matches_reference_vectors(path):
+    z = np.load(path)
+    W, H, fi, _ = (int(v) for v in z["meta"])
+    p = N.FrameParams.from_buffer_copy(bytes(z["params"]))
+    o = oracle.OracleStream(W, H, oracle.MODE_REF)
+    load_state(o, z, fi)
+    o.set_tonemapping(z["tm0/hist"], float(z["tm0/avg"]))
+    state = runner.oracle_planes(o, fi)
+    assert len(state) > 40
+    bad = []
+    for k, (stage, it, tag, _) in enumerate(runner.stage_plan(W, H)):
+        o.stage(stage, it, fi, p)
+        state = expected_state(z, k, state)
+        diff = runner.differing(state, runner.oracle_planes(o, fi))
+        hist, avg, _ = o.tonemapping()
+        if diff:
+            bad.append((tag, diff))
+        if not np.array_equal(hist, z[f"k{k}/hist"]) or np.float32(avg) != z[f"k{k}/avg"]:
+            bad.append((tag, "tonemapping"))
+    assert not bad, bad
+
+
+def _live_ready():
+    if not os.path.isdir(os.path.join(REFERENCE, "Source", "Shaders")):
+        return "the reference checkout is not present"
+    from oracle.glsl_ref import build
+    if not os.path.exists(build.LIB) or os.path.getmtime(build.LIB) < max(
+            os.path.getmtime(os.path.join(build.HERE, f)) for f in ("glsl.h", "glsl_rt.cpp", "build.py")):
+        try:
+            build.build(REFERENCE)
+        except Exception as e:   # no compiler or no cpp: nothing to compare against
+            return f"the reference shaders did not build: {e}"
+    return None
+
+
+def run_both(W, H, plant=None):
+    """The oracle and the reference shaders from the same state, stage by stage; returns the
+    stages whose results differ. plant(o, fi, k): a change made on the oracle's side only."""
+    from tests.golden.make_ref_shader_vectors import start_state
+    o, p, fi = start_state(W, H)
+    ref = runner.RefRun(W, H)
+    bad = []
+    for k, (stage, it, tag, groups) in enumerate(runner.stage_plan(W, H)):
+        hist, avg, _ = o.tonemapping()
+        ref.bind_from(runner.oracle_planes(o, fi), fi)
+        tm = ref.run(tag, groups, p, (hist, avg))
+        if plant:
+            plant(o, fi, k)
+        o.stage(stage, it, fi, p)
+        diff = runner.differing(ref.arrays, runner.oracle_planes(o, fi))
+        if diff:
+            bad.append((tag, diff))
+        if tm is not None:
+            h2, a2, _ = o.tonemapping()
+            if not np.array_equal(tm[0], h2) or np.float32(tm[1]) != np.float32(a2):
+                bad.append((tag, "tonemapping"))
+    return bad
+
+
+@pytest.mark.parametrize("size", [(64, 36), (98, 33), (100, 34), (130, 9), (250, 151), (16, 6)])
+def test_oracle_matches_reference_shaders_live(size):
+    why = _live_ready()
+    if why:
+        pytest.skip(why)
+    assert run_both(*size) == []
+
+
+def test_a_planted_mistake_is_caught():
+    why = _live_ready()
+    if why:
+        pytest.skip(why)
+
+    def plant(o, fi, k):
+        # before the variance stage (plan index 6), one texel of the accumulated moments changes
+        # on the oracle's side only
+        if k == 6:
+            m = o.plane("DIFF_ACCUM_MOMENTS", fi)
+            m[5, 7] = m[5, 7] + np.array(1000, dtype=m.dtype)
+
+    bad = run_both(64, 36, plant)
+    assert bad and bad[0][0] == "CmSVGFEstimateVariance", bad
