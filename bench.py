@@ -445,7 +445,10 @@ def run_reference(args, dist: Dist):
                          "sample": f"one frame of a {W}x{H} band of the workload per step (same per-pixel work)"},
         "e2e": {"value": round(mpix, 4), "unit": "Mpix/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "note": "reference GLSL/Vulkan path unavailable on this box (no graphics stack); the CPU "
-                "restatement of its shaders (oracle/) is the reference's implementation timed here",
+                "restatement of its shaders (oracle/) is the reference's implementation timed here. Its "
+                "outputs equal the reference's own shader sources run on the CPU bit for bit at every "
+                "stage (oracle/glsl_ref, tests/test_ref_shaders.py); that emulation itself runs 2.3x "
+                "slower than the restatement on one core, so the restatement is the faster CPU baseline",
     }
     print(json.dumps(line), flush=True)
 

@@ -66,18 +66,20 @@ def stage(ref: str) -> str:
     if os.path.isdir(st):
         shutil.rmtree(st)
     os.makedirs(st)
-    srcs = []
-    for d in ("Source/Shaders", "Source/Generated"):
-        for n in os.listdir(os.path.join(ref, d)):
-            if d.endswith("Shaders") and not n.endswith((".h", ".inl", ".comp")):
-                continue
-            if d.endswith("Generated") and n != "ShaderCommonGLSL.h":
-                continue
-            srcs.append(os.path.join(ref, d, n))
-    for s in srcs:
-        with open(s, encoding="utf-8", errors="replace") as f:
+    srcs = []   # (source path, path under the staging directory)
+    shaders = os.path.join(ref, "Source", "Shaders")
+    for dirpath, _, names in os.walk(shaders):
+        for n in names:
+            if n.endswith((".h", ".inl", ".comp")):
+                p = os.path.join(dirpath, n)
+                srcs.append((p, os.path.relpath(p, shaders)))
+    srcs.append((os.path.join(ref, "Source", "Generated", "ShaderCommonGLSL.h"), "ShaderCommonGLSL.h"))
+    for src, rel in srcs:
+        with open(src, encoding="utf-8", errors="replace") as f:
             lines = [ln for ln in f if not re.match(r"\s*#\s*(version|extension)\b", ln)]
-        with open(os.path.join(st, os.path.basename(s)), "w") as f:
+        dst = os.path.join(st, rel)
+        os.makedirs(os.path.dirname(dst), exist_ok=True)
+        with open(dst, "w") as f:
             f.writelines(lines)
     return st
 
