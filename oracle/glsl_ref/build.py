@@ -48,6 +48,8 @@ SHADERS = {
     "CmSVGFAtrous.comp": {"atrousIteration": [1, 2, 3, 4, 5]},
     "CmLuminanceHistogram.comp": {},
     "CmLuminanceAvg.comp": {},
+    "CmBloomDownsample.comp": {"stepIndex": list(range(8))},
+    "CmBloomUpsample.comp": {"stepIndex": list(range(8))},
 }
 
 # rgdn_frame_params fields that ShGlobalUniform has under the same name

@@ -642,6 +642,13 @@ inline void  imageStore( image2D& im, const ivec2& pix, const vec4& v ) { store_
 inline void  imageStore( uimage2D& im, const ivec2& pix, const uvec4& v ) { store_u( im.plane(), pix, v ); }
 inline vec4  texelFetch( sampler2D& s, const ivec2& pix, int ) { return load_f( s.plane(), pix ); }
 inline uvec4 texelFetch( usampler2D& s, const ivec2& pix, int ) { return load_u( s.plane(), pix ); }
+// Filtered reads: the framebuffers' sampler is bilinear with clamp-to-edge addressing. GLSL and
+// Vulkan leave the weights' precision to the device (subTexelPrecisionBits); this takes them
+// exactly in binary32: x = u w - 1/2, the texels floor(x) and floor(x) + 1 clamped to the edge,
+// the weight x - floor(x), mix(x, y, a) = x (1 - a) + y a, rows first. Only LOD 0 is read.
+vec4 bilinear( Plane& p, const vec2& uv );
+inline vec4 textureLod( sampler2D& s, const vec2& uv, float ) { return bilinear( s.plane(), uv ); }
+inline vec4 texture( sampler2D& s, const vec2& uv ) { return bilinear( s.plane(), uv ); }
 inline ivec2 imageSize( ImageBase& im ) { return ivec2( im.plane().w, im.plane().h ); }
 inline ivec2 textureSize( SamplerBase& s, int ) { return ivec2( s.plane().w, s.plane().h ); }
 

@@ -153,6 +153,20 @@ vec4 load_f( Plane& p, ivec2 pix )
     return r;
 }
 
+vec4 bilinear( Plane& p, const vec2& uv )
+{
+    if( !p.data ) return vec4( 0.0f );
+    const float x = uv.x * (float)p.w - 0.5f, y = uv.y * (float)p.h - 0.5f;
+    const float fx = std::floor( x ), fy = std::floor( y );
+    const float a = x - fx, b = y - fy;
+    const int   ix = (int)fx, iy = (int)fy;
+    auto        cl = []( int v, int n ) { return v < 0 ? 0 : v > n - 1 ? n - 1 : v; };
+    const int   x0 = cl( ix, p.w ), x1 = cl( ix + 1, p.w ), y0 = cl( iy, p.h ), y1 = cl( iy + 1, p.h );
+    const vec4  t00 = load_f( p, ivec2( x0, y0 ) ), t10 = load_f( p, ivec2( x1, y0 ) );
+    const vec4  t01 = load_f( p, ivec2( x0, y1 ) ), t11 = load_f( p, ivec2( x1, y1 ) );
+    return mix( mix( t00, t10, a ), mix( t01, t11, a ), b );
+}
+
 uvec4 load_u( Plane& p, ivec2 pix )
 {
     const uint8_t* t = texel( p, pix );

@@ -34,8 +34,13 @@ def load(path: str = LIB) -> C.CDLL:
 
 
 def ref_name(fb: str) -> str:
-    """The reference's image name of a framebuffer (DIFF_ACCUM_COLOR -> framebufDiffAccumColor)."""
-    return "framebuf" + "".join(w if w == "DIS" else w.capitalize() for w in fb.split("_"))
+    """The reference's image name of a framebuffer (DIFF_ACCUM_COLOR -> framebufDiffAccumColor,
+    BLOOM_MIP1 -> framebufBloom_Mip1)."""
+    words = fb.split("_")
+    if words[0] == "BLOOM" and len(words) > 1 and words[1] in ("MIP1", "MIP2", "MIP3", "MIP4", "MIP5", "MIP6",
+                                                               "MIP7", "MIP8", "RESULT"):
+        return "framebufBloom_" + words[1].capitalize()
+    return "framebuf" + "".join(w if w in ("DIS", "RT") else w.capitalize() for w in words)
 
 
 def stage_plan(W: int, H: int, niter: int = 4):
@@ -79,7 +84,7 @@ class RefRun:
         f = getattr(self.lib, f"ref_{tag}_set_uniform", None)
         if f is not None:
             f(C.byref(params), C.c_float(self.W), C.c_float(self.H))
-        tm = getattr(self.lib, f"ref_{tag}_tonemapping", None)
+        tm = getattr(self.lib, f"ref_{tag}_tonemapping", None) if tonemapping is not None else None
         ptr = None
         if tm is not None:
             tm.restype = C.c_void_p

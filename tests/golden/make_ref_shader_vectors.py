@@ -13,7 +13,11 @@ here). Each later stage's planes are the reference shaders' own, carried from st
   params                the frame's rgdn_frame_params bytes; meta: W, H, fi, seed
 
 Usage (where the reference checkout and a C++ compiler are present):
-  python oracle/glsl_ref/build.py && python tests/golden/make_ref_shader_vectors.py 64 36 98 33
+  python oracle/glsl_ref/build.py && python tests/golden/make_ref_shader_vectors.py 64 36 34 17
+
+It also writes tests/golden/ref_bloom_<W>x<H>.npz at the first size: bloom_input() and every bloom
+image after the reference's pyramid (Bloom::Prepare's eight downsampling and eight upsampling
+steps).
 """
 import ctypes as C
 import os
@@ -74,12 +78,54 @@ def generate(W, H, seed=SEED) -> dict:
     return out
 
 
+def bloom_input(W, H, seed=SEED) -> np.ndarray:
+    """Random B10G11R11 texels (each channel's exponent 0..29, so finite) for BLOOM_INPUT."""
+    rng = np.random.default_rng(seed)
+    r = (rng.integers(0, 30, (H, W)) << 6) | rng.integers(0, 64, (H, W))
+    g = (rng.integers(0, 30, (H, W)) << 6) | rng.integers(0, 64, (H, W))
+    b = (rng.integers(0, 30, (H, W)) << 5) | rng.integers(0, 32, (H, W))
+    return (r | (g << 11) | (b << 22)).astype(np.uint32)
+
+
+def bloom_plan(W, H):
+    """(reference entry point, groups) of Bloom::Prepare (Source/Bloom.cpp:129-187)."""
+    plan = []
+    for i in range(8):
+        w, h = -(-W // (1 << (i + 1))), -(-H // (1 << (i + 1)))
+        plan.append((f"CmBloomDownsample_{i}", ((w + 15) // 16, (h + 15) // 16)))
+    for i in range(7, -1, -1):
+        w, h = -(-W // (1 << i)), -(-H // (1 << i))
+        plan.append((f"CmBloomUpsample_{i}", ((w + 15) // 16, (h + 15) // 16)))
+    return plan
+
+
+def run_reference_bloom(W, H, inp: np.ndarray) -> dict:
+    """The reference's bloom pyramid over `inp`: {(fb, slot): plane} of every bloom image."""
+    o = oracle.OracleStream(W, H, oracle.MODE_REF)
+    o.load("BLOOM_INPUT", 0, inp)
+    ref = runner.RefRun(W, H)
+    ref.bind_from(runner.oracle_planes(o, 0), 0)
+    p = N.FrameParams()
+    for tag, groups in bloom_plan(W, H):
+        ref.run(tag, groups, p)
+    return {k: a for k, a in ref.arrays.items() if k[0].startswith("BLOOM")}
+
+
 def main(argv):
     sizes = [(int(argv[i]), int(argv[i + 1])) for i in range(0, len(argv), 2)] or [(64, 36)]
+    here = os.path.dirname(os.path.abspath(__file__))
     for W, H in sizes:
-        path = os.path.join(os.path.dirname(os.path.abspath(__file__)), f"ref_shaders_{W}x{H}.npz")
+        path = os.path.join(here, f"ref_shaders_{W}x{H}.npz")
         np.savez_compressed(path, **generate(W, H))
         print(path, os.path.getsize(path))
+    # the bloom pyramid (CmBloomDownsample / CmBloomUpsample) at the first size
+    W, H = sizes[0]
+    out = {"meta": np.array([W, H], dtype=np.int64)}
+    for (fb, slot), a in run_reference_bloom(W, H, bloom_input(W, H)).items():
+        out[f"{fb}/{slot}"] = a
+    path = os.path.join(here, f"ref_bloom_{W}x{H}.npz")
+    np.savez_compressed(path, **out)
+    print(path, os.path.getsize(path))
 
 
 if __name__ == "__main__":

@@ -2,9 +2,10 @@
 
 The reference's A-SVGF and tonemapping compute shaders (Source/Shaders/CmASVGFGradientAtrous.comp,
 CmSVGFTemporalAccumulation.comp, CmAntiFirefly.comp, CmSVGFEstimateVariance.comp,
-CmSVGFAtrous_Iter0.comp, CmSVGFAtrous.comp, CmLuminanceHistogram.comp, CmLuminanceAvg.comp) run on
-the CPU from their GLSL sources (oracle/glsl_ref: a mechanical rewrite to C++ over a GLSL runtime),
-dispatched as Denoiser::Denoise and Tonemapping::CalculateExposure dispatch them. Every plane of
+CmSVGFAtrous_Iter0.comp, CmSVGFAtrous.comp, CmLuminanceHistogram.comp, CmLuminanceAvg.comp) and its
+bloom pyramid (CmBloomDownsample.comp, CmBloomUpsample.comp) run on the CPU from their GLSL sources
+(oracle/glsl_ref: a mechanical rewrite to C++ over a GLSL runtime), dispatched as
+Denoiser::Denoise, Tonemapping::CalculateExposure and Bloom::Prepare dispatch them. Every plane of
 both frame slots and the tonemapping buffer must equal the oracle's bit for bit after every stage.
 
 - test_oracle_matches_reference_vectors: from the committed vectors (tests/golden, written by
@@ -13,6 +14,7 @@ both frame slots and the tonemapping buffer must equal the oracle's bit for bit 
   and odd gradient images, where the reference checkout is present (it builds oracle/_ref first).
 - test_a_planted_mistake_is_caught: a texel of one input changed on the oracle's side only
   must show up as a difference.
+- test_oracle_bloom_*: the bloom pyramid (every bloom image), from the committed vectors and live.
 """
 import glob
 import os
@@ -126,3 +128,44 @@ def test_a_planted_mistake_is_caught():
 
     bad = run_both(64, 36, plant)
     assert bad and bad[0][0] == "CmSVGFEstimateVariance", bad
+
+
+GOLDEN_BLOOM = sorted(glob.glob(os.path.join(ROOT, "tests", "golden", "ref_bloom_*.npz")))
+
+
+def oracle_bloom(W, H, inp):
+    """The oracle's bloom over `inp`: {(fb, slot): plane} of every bloom image."""
+    o = oracle.OracleStream(W, H, oracle.MODE_REF)
+    o.load("BLOOM_INPUT", 0, inp)
+    o.bloom(0, 1.0)
+    return {k: a for k, a in runner.oracle_planes(o, 0).items() if k[0].startswith("BLOOM")}
+
+
+@pytest.mark.parametrize("path", GOLDEN_BLOOM, ids=[os.path.basename(p) for p in GOLDEN_BLOOM])
+def test_oracle_bloom_matches_reference_vectors(path):
+    z = np.load(path)
+    W, H = (int(v) for v in z["meta"])
+    expected = {}
+    for key in z.files:
+        if key != "meta":
+            fb, slot = key.split("/")
+            expected[(fb, int(slot))] = z[key]
+    assert len(expected) == 10
+    got = oracle_bloom(W, H, expected[("BLOOM_INPUT", 0)])
+    assert runner.differing(expected, got) == []
+
+
+@pytest.mark.parametrize("size", [(64, 36), (250, 151), (1280, 720)])
+def test_oracle_bloom_matches_reference_shaders_live(size):
+    why = _live_ready()
+    if why:
+        pytest.skip(why)
+    from tests.golden.make_ref_shader_vectors import bloom_input, run_reference_bloom
+    W, H = size
+    inp = bloom_input(W, H)
+    ref = run_reference_bloom(W, H, inp)
+    # the reference writes no texel of a mip whose uv passes 1 (CmBloomDownsample.comp:123), so
+    # the smallest mips of a small frame stay empty; the input and the first mips are not
+    assert len(ref) == 10
+    assert all(np.count_nonzero(ref[(fb, 0)]) for fb in ("BLOOM_INPUT", "BLOOM_MIP1", "BLOOM_MIP2", "BLOOM_RESULT"))
+    assert runner.differing(ref, oracle_bloom(W, H, inp)) == []
