@@ -29,6 +29,7 @@
 // single-frame ones) and their large frames ran 5-13 % slower per pixel. A step with such a
 // group is launched directly rather than replayed from a graph, since that group's parameters
 // change every step; at a frame of a million pixels or more the launches stay ahead of the GPU.
+// One-frame groups alternate between the caller's stream and a second lane (enqueue_step).
 //
 // Autotuning: the first 15 steps of a storage mode time every candidate tile shape (and, for
 // the a-trous kernel, the register budget and the fusion depth) per launch on the frames being
@@ -239,6 +240,8 @@ struct BatchExec
 {
     int                        device = 0, sms = 0;
     cudaStream_t               capture = nullptr;   // private stream the graphs are captured on
+    cudaStream_t               side    = nullptr;   // second lane of one-frame groups
+    cudaEvent_t                fork = nullptr, join = nullptr;
     cudaGraphExec_t            exec[ BATCH_SLOTS ] = {};
     GraphKey                   key[ BATCH_SLOTS ];
     Config                     cfg[ 4 ];
@@ -282,6 +285,9 @@ BatchExec* create_exec( int device )
     ex->device = device;
     bool ok    = cudaDeviceGetAttribute( &ex->sms, cudaDevAttrMultiProcessorCount, device ) == cudaSuccess && ex->sms > 0;
     ok         = ok && cudaStreamCreateWithFlags( &ex->capture, cudaStreamNonBlocking ) == cudaSuccess;
+    ok         = ok && cudaStreamCreateWithFlags( &ex->side, cudaStreamNonBlocking ) == cudaSuccess;
+    ok         = ok && cudaEventCreateWithFlags( &ex->fork, cudaEventDisableTiming ) == cudaSuccess;
+    ok         = ok && cudaEventCreateWithFlags( &ex->join, cudaEventDisableTiming ) == cudaSuccess;
     for( int s = 0; s < 4; s++ )
     {
         for( int k = 0; k < BS_COUNT; k++ )
@@ -325,6 +331,9 @@ void batch_exec_free( BatchExec* ex )
     }
     for( cudaEvent_t e : ex->eventPool ) cudaEventDestroy( e );
     if( ex->capture ) cudaStreamDestroy( ex->capture );
+    if( ex->side ) cudaStreamDestroy( ex->side );
+    if( ex->fork ) cudaEventDestroy( ex->fork );
+    if( ex->join ) cudaEventDestroy( ex->join );
     delete ex;
 }
 
@@ -347,26 +356,42 @@ rgdn_status enqueue_step( rgdn_context* c, BatchExec& ex, DeviceSlots& ds, int s
     const bool tuning = !capturing && !tu.settled && tu.phase == 0;
     const bool user   = !capturing && ex.timing;
 
+    // One-frame groups run on two lanes, cs and a side stream, alternately: the frames are of
+    // different camera streams, so one frame's kernels fill the SMs the other's leave idle at its
+    // launch boundaries and wave tails. The side lane starts after everything before the step on
+    // cs and cs waits for it at the end (timed steps keep one lane, so each event brackets one frame).
+    int  singles = 0;
+    bool forked  = false;
+    for( int gi = 0; gi < key.ng; gi++ ) singles += key.g[ gi ].single;
+    const bool twoLanes = singles > 1 && !user && !capturing;
+    if( twoLanes )
+    {
+        if( cudaEventRecord( ex.fork, cs ) != cudaSuccess || cudaStreamWaitEvent( ex.side, ex.fork, 0 ) != cudaSuccess )
+            return RGDN_DEVICE_ERROR;
+        forked = true;
+    }
+    int nthSingle = 0;
     for( int gi = 0; gi < key.ng; gi++ )
     {
         const GroupKey& gk = key.g[ gi ];
         if( gk.single )
         {
             // one frame: the single-frame kernels, with its arguments as kernel parameters
-            const rgdn_job& jb = jobs[ gk.j0 ];
-            cudaEvent_t     ua = nullptr, ub = nullptr;
+            const rgdn_job&    jb   = jobs[ gk.j0 ];
+            const cudaStream_t lane = ( twoLanes && ( nthSingle++ & 1 ) ) ? ex.side : cs;
+            cudaEvent_t        ua = nullptr, ub = nullptr;
             if( user )
             {
                 ua = take_event( ex );
                 ub = take_event( ex );
                 if( !ua || !ub ) return RGDN_DEVICE_ERROR;
-                cudaEventRecord( ua, cs );
+                cudaEventRecord( ua, lane );
             }
-            rgdn_status r = run_denoise( jb.stream, jb.frameIndex, jb.params, cs );
-            if( r == RGDN_SUCCESS ) r = run_exposure( jb.stream, jb.frameIndex, jb.params, cs );
+            rgdn_status r = run_denoise( jb.stream, jb.frameIndex, jb.params, lane );
+            if( r == RGDN_SUCCESS ) r = run_exposure( jb.stream, jb.frameIndex, jb.params, lane );
             if( user )
             {
-                cudaEventRecord( ub, cs );
+                cudaEventRecord( ub, lane );
                 ex.pending.push_back( { (int)RGDN_BATCH_SINGLE_FRAME_GROUP, 0, ua, ub } );
             }
             if( r != RGDN_SUCCESS ) return r;
@@ -439,6 +464,8 @@ rgdn_status enqueue_step( rgdn_context* c, BatchExec& ex, DeviceSlots& ds, int s
         }
         if( ( r = run( -1, RGDN_STAGE_LUMINANCE_AVG, 0, 0, 0, 0 ) ) != RGDN_SUCCESS ) return r;
     }
+    if( forked && ( cudaEventRecord( ex.join, ex.side ) != cudaSuccess || cudaStreamWaitEvent( cs, ex.join, 0 ) != cudaSuccess ) )
+        return RGDN_DEVICE_ERROR;
     return RGDN_SUCCESS;
 }
 
