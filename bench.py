@@ -525,15 +525,21 @@ def run_batched(args, dist: Dist, dev: int, cs) -> dict:
             Tonemapping(s).CalculateExposure(fi, p, cs)
 
     def timed(fn, steps: int, first: int):
+        # the host enqueues every launch of a step with one-frame groups: no garbage-collection
+        # pause of this thread inside the timed region
+        import gc
         ev = [torch.cuda.Event(enable_timing=True) for _ in range(steps + 1)]
         dist.barrier()
         torch.cuda.synchronize()
+        gc.collect()
+        gc.disable()
         with torch.cuda.stream(cs):
             ev[0].record(cs)
             for k in range(steps):
                 fn(first + k)
                 ev[k + 1].record(cs)
         cs.synchronize()
+        gc.enable()
         dist.barrier()
         per = sorted(ev[k].elapsed_time(ev[k + 1]) for k in range(steps))
         return dist.max(ev[0].elapsed_time(ev[-1])), per
@@ -590,19 +596,31 @@ def run_batched(args, dist: Dist, dev: int, cs) -> dict:
                           "one_stream_per_call_mpix_s": round(vs, 1), "vs_one_frame_per_launch": round(vb / vs, 3)})
 
     per_px = stage_bytes("fp16")
+    # frames of at least singleFramePixels pixels run alone on the single-frame kernels (one timing
+    # entry per such frame for its whole chain); the rest go through the constant-table kernels
+    sizes = [s.width * s.height for s in streams]
+    alone = [n for n in sizes if cfg.singleFramePixels and n >= cfg.singleFramePixels]
+    px_alone, px_table = sum(alone), px - sum(alone)
     kern = []
     for (name, it), (n, ms) in tim.items():
-        if name == "atrous":
-            alg = kernel_bytes("atrous_fast", it, args.iters, per_px) * px
+        if name == "single_frame_group":
+            # compulsory bytes of the whole chain (every input read once, every output written once)
+            unit_px, alg = px_alone, path_bytes("fp16") * px_alone
+        elif name == "atrous":
+            pair = cfg.atrousFusionDepth >= 2 and it == 0
+            unit_px = px_table
+            alg = kernel_bytes("atrous_pair" if pair else "atrous_fast", it, args.iters, per_px) * px_table
         elif name in ("gradient_samples", "gradient_atrous"):
-            alg = per_px[name] * px
+            unit_px, alg = px_table, per_px[name] * px_table
         else:
+            unit_px = px_table
             alg = per_px.get({"temporal_accumulation": "temporal_fast_gp", "anti_firefly": "anti_firefly_fast",
-                              "variance_estimation": "variance_fast"}.get(name, name), 0.0) * px
+                              "variance_estimation": "variance_fast"}.get(name, name), 0.0) * px_table
         # 3 timed steps; a step launches each kind once per group of frames
         us_step = 1e3 * ms / 3
         kern.append({"kernel": f"batched_{name}[{it}]", "launches_per_step": round(n / 3, 2),
-                     "us_per_step": round(us_step, 2), "us_per_mpix": round(us_step / (px / 1e6), 3),
+                     "mpix_per_step": round(unit_px / 1e6, 3),
+                     "us_per_step": round(us_step, 2), "us_per_mpix": round(us_step / max(unit_px / 1e6, 1e-9), 3),
                      "alg_bytes_per_step": alg, "gbs": round(alg / (us_step / 1e6) / 1e9, 1)})
     kern.sort(key=lambda d: -d["us_per_step"])
     out = {
@@ -888,6 +906,9 @@ def run_ours(args, dist: Dist):
     ev = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
     dist.barrier()
     torch.cuda.synchronize()
+    import gc
+    gc.collect()
+    gc.disable()   # no garbage-collection pause of the launching thread in the timed region
     with torch.cuda.stream(cs):
         ev[0].record(cs)
         for k in range(args.steps):
@@ -895,6 +916,7 @@ def run_ours(args, dist: Dist):
             ev[k + 1].record(cs)
     cs.synchronize()
     torch.cuda.synchronize()
+    gc.enable()
     dist.barrier()
     launches = ctx.launch_count() - launches0
     total_ms = ev[0].elapsed_time(ev[-1])
