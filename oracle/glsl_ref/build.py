@@ -50,7 +50,50 @@ SHADERS = {
     "CmLuminanceAvg.comp": {},
     "CmBloomDownsample.comp": {"stepIndex": list(range(8))},
     "CmBloomUpsample.comp": {"stepIndex": list(range(8))},
+    # written by gradient_samples_source() from RtGradients.rgen
+    "RtGradients_main.comp": {},
 }
+
+# RtGradients.rgen is a ray-generation shader: its main() selects each stratum's sample, tests it,
+# and turns the forward-projected luminance into the temporal gradient; only the forward
+# projection itself traces rays (re-shading the previous frame's surface with this frame's
+# lights). That part is this project's boundary input RGDN_FB_GRADIENT_RESHADED (the luminance
+# pair at the previous frame's shading pixel), so the build replaces the statements that compute
+# forwardProjectedLuminance with a load of that input and runs the rest of main() as written, one
+# invocation per launch index (gl_LaunchIDEXT), over PathTracer::CalculateGradientsSamples's
+# ceil(width / 3) x ceil(height / 3) launch.
+GRADIENT_PREAMBLE = """#define DESC_SET_FRAMEBUFFERS 0
+#define DESC_SET_GLOBAL_UNIFORM 1
+#include "ShaderCommonGLSLFunc.h"
+layout(local_size_x = 1, local_size_y = 1, local_size_z = 1) in;
+layout(set = DESC_SET_FRAMEBUFFERS, binding = 1000, rg32f) uniform image2D framebufGradientReshaded;
+#define gl_LaunchIDEXT gl_GlobalInvocationID
+"""
+GRADIENT_FORWARD = "vec2 forwardProjectedLuminance = imageLoad(framebufGradientReshaded, prevShadingPix).xy;"
+
+
+def gradient_samples_source(ref: str) -> str:
+    """RtGradients.rgen's main() (from its GRADIENT_ESTIMATION_ENABLED block) behind
+    GRADIENT_PREAMBLE, with the forward projection replaced by GRADIENT_FORWARD. Every anchor must
+    be found exactly once, so a changed shader fails the build instead of building something else."""
+    with open(os.path.join(ref, "Source", "Shaders", "RtGradients.rgen"), encoding="utf-8") as f:
+        src = f.read()
+
+    def once(pat: str, text: str) -> re.Match:
+        ms = list(re.finditer(pat, text))
+        if len(ms) != 1:
+            raise RuntimeError(f"RtGradients.rgen: {pat!r} found {len(ms)} times")
+        return ms[0]
+
+    body = src[once(r"#if\s+GRADIENT_ESTIMATION_ENABLED\b", src).start():]
+    start = once(r"const\s+uint\s+oldSeed\s*=", body).start()
+    once(r"vec2\s+forwardProjectedLuminance\s*=\s*vec2\(\s*0\.0\s*\)\s*;", body[start:])
+    m = once(r"if\s*\(\s*matchedSurface\s*\)\s*\{", body[start:])
+    k, depth = start + m.end(), 1
+    while depth:
+        depth += {"{": 1, "}": -1}.get(body[k], 0)
+        k += 1
+    return GRADIENT_PREAMBLE + body[:start] + GRADIENT_FORWARD + body[k:]
 
 # rgdn_frame_params fields that ShGlobalUniform has under the same name
 UNIFORM_COPY = ["view", "viewPrev", "projection", "projectionPrev", "cameraPosition", "cameraPositionPrev",
@@ -83,6 +126,8 @@ def stage(ref: str) -> str:
         os.makedirs(os.path.dirname(dst), exist_ok=True)
         with open(dst, "w") as f:
             f.writelines(lines)
+    with open(os.path.join(st, "RtGradients_main.comp"), "w") as f:
+        f.write(gradient_samples_source(ref))
     return st
 
 

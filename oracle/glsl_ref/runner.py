@@ -5,7 +5,8 @@ infrastructure that pins the oracle to the reference.
 Each stage is dispatched the way Denoiser::Denoise and Tonemapping::CalculateExposure
 dispatch it (Source/Denoiser.cpp:92-253, Source/Tonemapping.cpp:106-165): 16x16 groups over the
 render size, the gradient a-trous over renderWidth / 3 (a float, rounded up), the luminance
-average as one group of 256. The reference's framebuffers are bound by name to copies of the
+average as one group of 256. The gradient samples before them run as
+PathTracer::CalculateGradientsSamples launches them (Source/PathTracer.cpp:196-218). The reference's framebuffers are bound by name to copies of the
 oracle's planes (frame slot fi as framebufX, slot fi ^ 1 as framebufX_Prev), in the reference
 framebuffer formats (the oracle's MODE_REF).
 """
@@ -44,12 +45,15 @@ def ref_name(fb: str) -> str:
 
 
 def stage_plan(W: int, H: int, niter: int = 4):
-    """(oracle stage, iteration, reference entry point, groups) in Denoise + CalculateExposure
-    order, from the gradient a-trous on (the gradient samples are a ray-generation shader)."""
+    """(oracle stage, iteration, reference entry point, groups) in the reference's frame order:
+    the gradient samples (RtGradients.rgen's main, launched over ceil(W / 3) x ceil(H / 3) as
+    PathTracer::CalculateGradientsSamples launches it, one invocation per group here), then
+    Denoise and CalculateExposure."""
     from raytracedgl1_gb300 import _native as N
     gw, gh = -(-W // 3), -(-H // 3)
     full = ((W + 15) // 16, (H + 15) // 16)
-    plan = [(N.STAGE_GRADIENT_ATROUS, i, f"CmASVGFGradientAtrous_{i}", ((gw + 15) // 16, (gh + 15) // 16)) for i in range(4)]
+    plan = [(N.STAGE_GRADIENT_SAMPLES, 0, "RtGradients_main", (gw, gh))]
+    plan += [(N.STAGE_GRADIENT_ATROUS, i, f"CmASVGFGradientAtrous_{i}", ((gw + 15) // 16, (gh + 15) // 16)) for i in range(4)]
     plan += [(N.STAGE_TEMPORAL_ACCUMULATION, 0, "CmSVGFTemporalAccumulation", full),
              (N.STAGE_ANTI_FIREFLY, 0, "CmAntiFirefly", full),
              (N.STAGE_VARIANCE_ESTIMATION, 0, "CmSVGFEstimateVariance", full)]
@@ -57,6 +61,14 @@ def stage_plan(W: int, H: int, niter: int = 4):
     plan += [(N.STAGE_LUMINANCE_HISTOGRAM, 0, "CmLuminanceHistogram", full),
              (N.STAGE_LUMINANCE_AVG, 0, "CmLuminanceAvg", (1, 1))]
     return plan
+
+
+# Planes the reference keeps in one image and the oracle in two frame slots: the gradient history
+# (DISGradientHistory, FRAMEBUF_FLAGS_FORCE_SIZE_1_3 without a _Prev image) is read by the gradient
+# samples before this frame's gradient a-trous overwrites it, so at that point the reference's
+# image holds the previous frame's history, which the oracle keeps in the previous frame's slot.
+# For these entry points the previous slot is bound under the reference's (current) name.
+PREV_AS_CURRENT = {"RtGradients_main": ("DIS_GRADIENT_HISTORY",)}
 
 
 class RefRun:
@@ -67,11 +79,18 @@ class RefRun:
         self.lib = lib or load()
         self.arrays: dict = {}
 
-    def bind_from(self, planes: dict, fi: int) -> None:
-        """planes: {(fb name, slot): array}; binds copies (kept in self.arrays)."""
+    def bind_from(self, planes: dict, fi: int, tag: str | None = None) -> None:
+        """planes: {(fb name, slot): array}; binds copies (kept in self.arrays) for the entry point
+        `tag` (see PREV_AS_CURRENT)."""
         self.arrays = {}
+        prev_as_current = PREV_AS_CURRENT.get(tag, ())
         for (fb, slot), arr in planes.items():
-            name = ref_name(fb) + ("" if slot == fi else "_Prev")
+            if fb in prev_as_current:
+                if slot == fi:
+                    continue
+                name = ref_name(fb)
+            else:
+                name = ref_name(fb) + ("" if slot == fi else "_Prev")
             if not self.lib.ref_texel_bytes(name.encode()):
                 continue
             a = np.ascontiguousarray(arr).copy()

@@ -10,10 +10,12 @@
 //  GLSL sources on the CPU instead (a mechanical rewrite to C++ over a GLSL runtime written
 //  for it), dispatched as the reference dispatches them, and tests/test_ref_shaders.py
 //  requires every plane and the tonemapping buffer to equal this oracle's bit for bit after
-//  every stage: the gradient a-trous, temporal accumulation, anti-firefly, variance, the
-//  a-trous iterations with the composition, the histogram and the adaptation (committed
-//  vectors in tests/golden, and live where the reference checkout is present). The gradient
-//  samples (a ray-generation shader) and the stages beyond the reference's compute shaders
+//  every stage: the gradient samples (RtGradients.rgen's main(), its ray-traced forward
+//  projection read from the boundary input RGDN_FB_GRADIENT_RESHADED), the gradient a-trous,
+//  temporal accumulation, anti-firefly, variance, the a-trous iterations with the composition,
+//  the histogram and the adaptation, and the bloom pyramid (committed vectors in tests/golden,
+//  and live where the reference checkout is present). The re-shading of the analytic scene,
+//  the final composition, the bloom's apply and the volumetric passes
 //  stay pinned only by the codecs' known-answer tests from the public specs they implement
 //  (IEEE-754 binary16/bfloat16, EXT_texture_shared_exponent, the Vulkan B10G11R11
 //  unsigned-float layout) and the closed-form known-answer tests in tests/.

@@ -4,9 +4,9 @@ from a starting state, so that the oracle can be checked against the reference w
 reference checkout is absent (tests/test_ref_shaders.py).
 
 The starting state is the oracle's, in the reference framebuffer formats, after three frames of
-the scene and the fourth frame's gradient samples (a ray-generation shader, not reproduced
-here). Each later stage's planes are the reference shaders' own, carried from stage to stage:
-  s0/<fb>/<slot>        every plane of both frame slots before the gradient a-trous
+the scene, with the fourth frame's G-buffer loaded. Each stage's planes are the reference
+shaders' own, carried from stage to stage, from the fourth frame's gradient samples on:
+  s0/<fb>/<slot>        every plane of both frame slots before the gradient samples
   k<n>/<fb>/<slot>      the planes that stage n of stage_plan() changed, after it
   k<n>/hist, k<n>/avg   the tonemapping buffer after stage n (histogram, average luminance)
   tm0/hist, tm0/avg     the tonemapping buffer before the first stage
@@ -38,7 +38,7 @@ WARM = 3
 
 
 def start_state(W, H, seed=SEED):
-    """The oracle after WARM frames and the next frame's gradient samples: (stream, params, fi)."""
+    """The oracle after WARM frames, with the next frame's G-buffer loaded: (stream, params, fi)."""
     sc = Scene(W, H, seed=seed, lightFlickerFrom=1.0)
     o = oracle.OracleStream(W, H, oracle.MODE_REF)
     for f in range(WARM + 1):
@@ -50,7 +50,6 @@ def start_state(W, H, seed=SEED):
         if f < WARM:
             o.denoise(fi, p)
             o.calculate_exposure(fi, p)
-    o.stage(N.STAGE_GRADIENT_SAMPLES, 0, fi, p)
     return o, p, fi
 
 
@@ -65,7 +64,7 @@ def generate(W, H, seed=SEED) -> dict:
     ref = runner.RefRun(W, H)
     tm = (hist, avg)
     for k, (stage, it, tag, groups) in enumerate(runner.stage_plan(W, H)):
-        ref.bind_from(planes, fi)
+        ref.bind_from(planes, fi, tag)
         r = ref.run(tag, groups, p, tm)
         for key, a in ref.arrays.items():
             if not np.array_equal(a.view(np.uint8), planes[key].view(np.uint8)):

@@ -2,18 +2,22 @@
 
 The reference's A-SVGF and tonemapping compute shaders (Source/Shaders/CmASVGFGradientAtrous.comp,
 CmSVGFTemporalAccumulation.comp, CmAntiFirefly.comp, CmSVGFEstimateVariance.comp,
-CmSVGFAtrous_Iter0.comp, CmSVGFAtrous.comp, CmLuminanceHistogram.comp, CmLuminanceAvg.comp) and its
-bloom pyramid (CmBloomDownsample.comp, CmBloomUpsample.comp) run on the CPU from their GLSL sources
+CmSVGFAtrous_Iter0.comp, CmSVGFAtrous.comp, CmLuminanceHistogram.comp, CmLuminanceAvg.comp), the
+main() of its gradient-sample shader (RtGradients.rgen, with the ray-traced forward projection
+read from the boundary input RGDN_FB_GRADIENT_RESHADED) and its bloom pyramid
+(CmBloomDownsample.comp, CmBloomUpsample.comp) run on the CPU from their GLSL sources
 (oracle/glsl_ref: a mechanical rewrite to C++ over a GLSL runtime), dispatched as
-Denoiser::Denoise, Tonemapping::CalculateExposure and Bloom::Prepare dispatch them. Every plane of
-both frame slots and the tonemapping buffer must equal the oracle's bit for bit after every stage.
+PathTracer::CalculateGradientsSamples, Denoiser::Denoise, Tonemapping::CalculateExposure and
+Bloom::Prepare dispatch them. Every plane of both frame slots and the tonemapping buffer must equal
+the oracle's bit for bit after every stage.
 
 - test_oracle_matches_reference_vectors: from the committed vectors (tests/golden, written by
   tests/golden/make_ref_shader_vectors.py), wherever the oracle builds.
 - test_oracle_matches_reference_shaders_live: the same, live, at sizes with partial workgroups
   and odd gradient images, where the reference checkout is present (it builds oracle/_ref first).
-- test_a_planted_mistake_is_caught: a texel of one input changed on the oracle's side only
-  must show up as a difference.
+- test_a_planted_mistake_is_caught: an input changed on the oracle's side only (a moments texel
+  before the variance pass; the forward-projected luminance before the gradient samples) must
+  show up as a difference at that stage.
 - test_oracle_bloom_*: the bloom pyramid (every bloom image), from the committed vectors and live.
 """
 import glob
@@ -91,7 +95,7 @@ def run_both(W, H, plant=None):
     bad = []
     for k, (stage, it, tag, groups) in enumerate(runner.stage_plan(W, H)):
         hist, avg, _ = o.tonemapping()
-        ref.bind_from(runner.oracle_planes(o, fi), fi)
+        ref.bind_from(runner.oracle_planes(o, fi), fi, tag)
         tm = ref.run(tag, groups, p, (hist, avg))
         if plant:
             plant(o, fi, k)
@@ -114,20 +118,29 @@ def test_oracle_matches_reference_shaders_live(size):
     assert run_both(*size) == []
 
 
-def test_a_planted_mistake_is_caught():
+def _plant_moments(o, fi, k):
+    # before the variance stage (plan index 7), one texel of the accumulated moments changes
+    if k == 7:
+        m = o.plane("DIFF_ACCUM_MOMENTS", fi)
+        m[5, 7] = m[5, 7] + np.array(1000, dtype=m.dtype)
+
+
+def _plant_reshaded(o, fi, k):
+    # before the gradient samples (plan index 0), the forward-projected luminance doubles
+    if k == 0:
+        r = o.plane("GRADIENT_RESHADED", fi)
+        r[...] = r * np.float32(2)
+
+
+@pytest.mark.parametrize("plant,first", [(_plant_moments, "CmSVGFEstimateVariance"),
+                                         (_plant_reshaded, "RtGradients_main")])
+def test_a_planted_mistake_is_caught(plant, first):
+    """A change made on the oracle's side only shows up at the stage that reads it."""
     why = _live_ready()
     if why:
         pytest.skip(why)
-
-    def plant(o, fi, k):
-        # before the variance stage (plan index 6), one texel of the accumulated moments changes
-        # on the oracle's side only
-        if k == 6:
-            m = o.plane("DIFF_ACCUM_MOMENTS", fi)
-            m[5, 7] = m[5, 7] + np.array(1000, dtype=m.dtype)
-
     bad = run_both(64, 36, plant)
-    assert bad and bad[0][0] == "CmSVGFEstimateVariance", bad
+    assert bad and bad[0][0] == first, bad
 
 
 GOLDEN_BLOOM = sorted(glob.glob(os.path.join(ROOT, "tests", "golden", "ref_bloom_*.npz")))
