@@ -52,7 +52,14 @@ SHADERS = {
     "CmBloomUpsample.comp": {"stepIndex": list(range(8))},
     # written by gradient_samples_source() from RtGradients.rgen
     "RtGradients_main.comp": {},
+    "CmCheckerboard.comp": {},
+    "CmPrepareFinal.comp": {},
 }
+
+# rgdn_final_params fields that ShGlobalUniform has under the same name (ImageComposition's
+# uniform inputs of CmPrepareFinal.comp)
+FINAL_COPY = ["luminanceWhitePoint", "emissionMaxScreenColor", "bloomEmissionMultiplier", "bloomThreshold",
+              "lightmapScreenCoverage"]
 
 # RtGradients.rgen is a ray-generation shader: its main() selects each stratum's sample, tests it,
 # and turns the forward-projected luminance into the temporal gradient; only the forward
@@ -276,8 +283,14 @@ def translation_unit(shader: str, body: str, info: dict, tag: str) -> str:
         sets = [f"std::memcpy(&u.{f}, &p->{f}, sizeof(p->{f}));" for f in UNIFORM_COPY]
         lines.append(f"void ref_{tag}_set_uniform(const rgdn_frame_params* p, float rw, float rh) {{ "
                      f"auto& u = {ns}::globalUniform; {' '.join(sets)} u.renderWidth = rw; u.renderHeight = rh; }}")
+        sets = [f"std::memcpy(&u.{f}, &p->{f}, sizeof(p->{f}));" for f in FINAL_COPY]
+        lines.append(f"void ref_{tag}_set_final(const rgdn_final_params* p) {{ "
+                     f"auto& u = {ns}::globalUniform; {' '.join(sets)} }}")
     if info["tonemapping"]:
         lines.append(f"void* ref_{tag}_tonemapping() {{ return &{ns}::tonemapping; }}")
+    if re.search(r"\bstatic\s+uvec4\s+g_lpmParams\s*\[", body):
+        # the LPM control block (LpmParams_BT), filled from ref_lpm_setup
+        lines.append(f"void* ref_{tag}_lpm() {{ return &{ns}::g_lpmParams; }}")
     lines.append("}")
     return "\n".join(lines) + "\n"
 
@@ -302,7 +315,7 @@ def build(ref: str, jobs: int | None = None) -> str:
                 f.write(translation_unit(shader, body, info, tag))
             units.append(path)
     flags = ["g++", "-std=c++17", "-O1", "-fPIC", "-ffp-contract=off", "-fno-fast-math", "-w",
-             "-I", HERE, "-I", os.path.join(ROOT, "include")]
+             "-I", HERE, "-I", os.path.join(ROOT, "include"), "-I", os.path.join(ref, "Source", "Shaders", "LPM")]
     objs = []
 
     def cc(src):
@@ -313,7 +326,7 @@ def build(ref: str, jobs: int | None = None) -> str:
             raise RuntimeError(f"compile {src}:\n{r.stderr[-6000:]}")
         return obj
 
-    srcs = units + [os.path.join(HERE, "glsl_rt.cpp")]
+    srcs = units + [os.path.join(HERE, "glsl_rt.cpp"), os.path.join(HERE, "lpm_setup_ref.cpp")]
     with ThreadPoolExecutor(max_workers=jobs or min(len(srcs), os.cpu_count() or 4)) as ex:
         objs = list(ex.map(cc, srcs))
     r = subprocess.run(["g++", "-shared", "-o", LIB] + objs, capture_output=True, text=True)

@@ -410,6 +410,12 @@ template< int N > inline vec< float, N > mod( const vec< float, N >& a, float y 
     for( int i = 0; i < N; i++ ) r.v[ i ] = mod( a.v[ i ], y );
     return r;
 }
+template< int N > inline vec< float, N > mod( const vec< float, N >& a, const vec< float, N >& y )
+{
+    vec< float, N > r;
+    for( int i = 0; i < N; i++ ) r.v[ i ] = mod( a.v[ i ], y.v[ i ] );
+    return r;
+}
 
 // min / max / clamp: the common type of scalars (GLSL converts int literals to the float type)
 template< class A, class B > using common = typename std::common_type< A, B >::type;
@@ -514,6 +520,12 @@ template< int N > inline vec< bool, N > isnan( const vec< float, N >& a )
     for( int i = 0; i < N; i++ ) r.v[ i ] = std::isnan( a.v[ i ] );
     return r;
 }
+template< int N > inline vec< bool, N > isinf( const vec< float, N >& a )
+{
+    vec< bool, N > r;
+    for( int i = 0; i < N; i++ ) r.v[ i ] = std::isinf( a.v[ i ] );
+    return r;
+}
 template< int N > inline bool any( const vec< bool, N >& a )
 {
     for( int i = 0; i < N; i++ )
@@ -545,6 +557,18 @@ inline uint  floatBitsToUint( float f ) { uint u; std::memcpy( &u, &f, 4 ); retu
 inline int   floatBitsToInt( float f ) { int u; std::memcpy( &u, &f, 4 ); return u; }
 inline float uintBitsToFloat( uint u ) { float f; std::memcpy( &f, &u, 4 ); return f; }
 inline float intBitsToFloat( int u ) { float f; std::memcpy( &f, &u, 4 ); return f; }
+template< int N > inline vec< uint, N > floatBitsToUint( const vec< float, N >& a )
+{
+    vec< uint, N > r;
+    for( int i = 0; i < N; i++ ) r.v[ i ] = floatBitsToUint( a.v[ i ] );
+    return r;
+}
+template< int N > inline vec< float, N > uintBitsToFloat( const vec< uint, N >& a )
+{
+    vec< float, N > r;
+    for( int i = 0; i < N; i++ ) r.v[ i ] = uintBitsToFloat( a.v[ i ] );
+    return r;
+}
 
 // binary16 <-> binary32, round to nearest even (packHalf2x16, the 16-bit float formats)
 uint16_t f32_to_f16( float f );
@@ -562,6 +586,11 @@ inline vec4 unpackUnorm4x8( uint u )
     return vec4( ( u & 0xFFu ) / 255.0f, ( ( u >> 8 ) & 0xFFu ) / 255.0f, ( ( u >> 16 ) & 0xFFu ) / 255.0f, ( u >> 24 ) / 255.0f );
 }
 inline uint bitfieldExtract( uint v, int off, int bits ) { return bits == 32 ? v : ( v >> off ) & ( ( 1u << bits ) - 1u ); }
+inline uint bitfieldInsert( uint base, uint ins, int off, int bits )
+{
+    const uint m = bits == 32 ? 0xFFFFFFFFu : ( ( 1u << bits ) - 1u ) << off;
+    return ( base & ~m ) | ( ( ins << off ) & m );
+}
 
 // atomics on buffer and shared memory (one invocation runs at a time)
 template< class T, class U > inline T atomicAdd( T& mem, U v )

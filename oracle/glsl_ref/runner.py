@@ -145,3 +145,35 @@ def differing(a: dict, b: dict) -> list:
             yy = y.reshape(y.shape[0], y.shape[1], -1)
             bad.append((key[0], key[1], int(np.count_nonzero(np.any(xx != yy, axis=-1)))))
     return bad
+
+
+def run_reference_final(W: int, H: int, planes: dict, fi: int, params, final, avg_luminance: float,
+                        lib: C.CDLL | None = None) -> dict:
+    """ImageComposition::PrepareForRaster + Finalize as the reference records them
+    (Source/ImageComposition.cpp:87-155): CmCheckerboard over the render size, the LPM control
+    block from ImageComposition::SetupLpmParams's LpmSetup call (lpm_setup_ref.cpp), then
+    CmPrepareFinal, both in 16x16 groups. `planes` are the oracle's {(fb, slot): array} in the
+    reference formats; SCREEN_EMISSION, which the oracle's single pass keeps on chip, is a scratch
+    B10G11R11 image here. Returns the reference's planes after both shaders."""
+    lib = lib or load()
+    run = RefRun(W, H, lib)
+    planes = dict(planes)
+    planes[("SCREEN_EMISSION", fi)] = np.zeros((H, W), dtype=np.uint32)
+    run.bind_from(planes, fi)
+    groups = ((W + 15) // 16, (H + 15) // 16)
+    ctl = np.zeros(96, dtype=np.uint32)
+    sat = np.array(final.saturation[:], dtype=np.float32)
+    ct = np.array(final.crosstalk[:], dtype=np.float32)
+    lib.ref_lpm_setup(sat.ctypes.data_as(C.c_void_p), ct.ctypes.data_as(C.c_void_p), ctl.ctypes.data_as(C.c_void_p))
+    for tag in ("CmCheckerboard", "CmPrepareFinal"):
+        getattr(lib, f"ref_{tag}_set_uniform")(C.byref(params), C.c_float(W), C.c_float(H))
+        getattr(lib, f"ref_{tag}_set_final")(C.byref(final))
+    for name, data in (("lpm", ctl), ("tonemapping", np.array([avg_luminance], dtype=np.float32))):
+        f = getattr(lib, f"ref_CmPrepareFinal_{name}")
+        f.restype = C.c_void_p
+        # the tonemapping buffer: 256 histogram words, then avgLuminance
+        C.memmove(f() + (1024 if name == "tonemapping" else 0), data.ctypes.data, data.nbytes)
+    for tag in ("CmCheckerboard", "CmPrepareFinal"):
+        getattr(lib, f"ref_{tag}_dispatch")(int(groups[0]), int(groups[1]))
+    return run.arrays
+

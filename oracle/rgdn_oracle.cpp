@@ -13,9 +13,10 @@
 //  every stage: the gradient samples (RtGradients.rgen's main(), its ray-traced forward
 //  projection read from the boundary input RGDN_FB_GRADIENT_RESHADED), the gradient a-trous,
 //  temporal accumulation, anti-firefly, variance, the a-trous iterations with the composition,
-//  the histogram and the adaptation, and the bloom pyramid (committed vectors in tests/golden,
-//  and live where the reference checkout is present). The re-shading of the analytic scene,
-//  the final composition, the bloom's apply and the volumetric passes
+//  the histogram and the adaptation, the bloom pyramid, and the final composition
+//  (CmCheckerboard + CmPrepareFinal, the LPM control block from the reference's own CPU-side
+//  LpmSetup) (committed vectors in tests/golden, and live where the reference checkout is
+//  present). The re-shading of the analytic scene, the bloom's apply and the volumetric passes
 //  stay pinned only by the codecs' known-answer tests from the public specs they implement
 //  (IEEE-754 binary16/bfloat16, EXT_texture_shared_exponent, the Vulkan B10G11R11
 //  unsigned-float layout) and the closed-form known-answer tests in tests/.
@@ -543,6 +544,15 @@ struct Plane
         }
     }
     void store_u8( int x, int y, uint32_t v ) { if( inside( x, y ) ) *at( x, y ) = (uint8_t)v; }
+    // v stored in this plane's format and read back
+    template< class T > V3< T > requant( V3< T > v ) const
+    {
+        Plane one;
+        one.init( 1, 1, fmt );
+        one.store< T >( 0, 0, { v.x, v.y, v.z, (T)0 } );
+        const V4< T > r = one.fetch< T >( 0, 0 );
+        return { r.x, r.y, r.z };
+    }
 
     static uint8_t unorm8( float f )
     {
@@ -1724,8 +1734,11 @@ template< class T > void prepare_final( Stream& s, uint32_t fi, const rgdn_final
             V3< T >   emis = xyz( emisP.fetch< T >( x, y ) );
             if( thr.fetch< T >( cbx, y ).w > K( 0.5 ) )   // wasSplit
             {
-                hdr  = resolve( pre, x, y, cbx, hdr );
-                emis = resolve( emisP, x, y, cbx, emis );
+                // CmCheckerboard stores the resolved values into Final (PreFinal's format) and
+                // ScreenEmission (ScreenEmisRT's format), and CmPrepareFinal reads them back
+                // (CmCheckerboard.comp:66-76, CmPrepareFinal.comp:147-150)
+                hdr  = outF.requant< T >( resolve( pre, x, y, cbx, hdr ) );
+                emis = emisP.requant< T >( resolve( emisP, x, y, cbx, emis ) );
             }
             if( p.flags & RGDN_FINAL_APPLY_SCATTERING )
             {

@@ -249,6 +249,12 @@ template<> struct Sto< MODE_REF >
         const rgdn::f3 c = decode_b10g11r11( static_cast< const uint32_t* >( p )[ i ] );
         return make_float3( c.x, c.y, c.z );
     }
+    // a value stored in PreFinal's format and read back
+    __device__ static float3 qpre( float3 v )
+    {
+        const rgdn::f3 c = decode_b10g11r11( encode_b10g11r11( v.x, v.y, v.z ) );
+        return make_float3( c.x, c.y, c.z );
+    }
 };
 
 template<> struct Sto< MODE_F32 >
@@ -268,6 +274,7 @@ template<> struct Sto< MODE_F32 >
     __device__ static void   st1( void* p, size_t i, float v ) { static_cast< float* >( p )[ i ] = v; }
     __device__ static void   stpre( void* p, size_t i, float3 v ) { static_cast< float4* >( p )[ i ] = make_float4( v.x, v.y, v.z, 0.0f ); }
     __device__ static float3 ldpre( const void* p, size_t i ) { float4 v = static_cast< const float4* >( p )[ i ]; return f3( v.x, v.y, v.z ); }
+    __device__ static float3 qpre( float3 v ) { return v; }
 };
 
 // 16-bit colour / history with FP32 moments, FP32 variance planes, FP32 prefiltered variance
@@ -318,6 +325,7 @@ template< bool BF > struct Sto16
         const ushort4 h = static_cast< const ushort4* >( p )[ i ];
         return f3( h2f( h.x ), h2f( h.y ), h2f( h.z ) );
     }
+    __device__ static float3 qpre( float3 v ) { return f3( h2f( f32_to_f16( v.x ) ), h2f( f32_to_f16( v.y ) ), h2f( f32_to_f16( v.z ) ) ); }
 };
 template<> struct Sto< MODE_F16 > : Sto16< false > {};
 template<> struct Sto< MODE_BF16 > : Sto16< true > {};
@@ -3143,12 +3151,18 @@ template< int M, bool FAST > __global__ void __launch_bounds__( 256 ) k_prepare_
     const int cbx = odd * sep + x / 2;
     float3    hdr = S::ldpre( f.preFinal, (size_t)i );
     float3    emis = decode_b10g11r11_bits( f.screenEmis[ i ] );
-    // needResolveCheckerboard: wasSplit(Throughput.a) (ShaderCommonGLSLFunc.h:435-444)
+    // needResolveCheckerboard: wasSplit(Throughput.a) (ShaderCommonGLSLFunc.h:435-444). CmCheckerboard
+    // stores the resolved values into Final and ScreenEmission (CmCheckerboard.comp:66-76), which
+    // CmPrepareFinal reads back, so they pass through those formats: Final has PreFinal's,
+    // ScreenEmission ScreenEmisRT's B10G11R11. Values that were not resolved came from those
+    // formats and pass through unchanged.
     if( h2f( f.throughput[ y * f.W + cbx ].w ) > 0.5f )
     {
         auto inImg = [ & ]( int qx, int qy ) { return qx >= 0 && qy >= 0 && qx < f.W && qy < f.H; };
         hdr  = cb_resolve( f, [ & ]( int qx, int qy ) { return inImg( qx, qy ) ? S::ldpre( f.preFinal, (size_t)( qy * f.W + qx ) ) : f3( 0, 0, 0 ); }, x, y, cbx, hdr );
         emis = cb_resolve( f, [ & ]( int qx, int qy ) { return inImg( qx, qy ) ? decode_b10g11r11_bits( f.screenEmis[ qy * f.W + qx ] ) : f3( 0, 0, 0 ); }, x, y, cbx, emis );
+        hdr  = S::qpre( hdr );
+        emis = decode_b10g11r11_bits( encode_b10g11r11( emis.x, emis.y, emis.z ) );
     }
     if( f.flags & RGDN_FINAL_APPLY_SCATTERING )
     {

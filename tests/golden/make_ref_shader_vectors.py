@@ -15,9 +15,11 @@ shaders' own, carried from stage to stage, from the fourth frame's gradient samp
 Usage (where the reference checkout and a C++ compiler are present):
   python oracle/glsl_ref/build.py && python tests/golden/make_ref_shader_vectors.py 64 36 34 17
 
-It also writes tests/golden/ref_bloom_<W>x<H>.npz at the first size: bloom_input() and every bloom
-image after the reference's pyramid (Bloom::Prepare's eight downsampling and eight upsampling
-steps).
+It also writes, at the first size, tests/golden/ref_bloom_<W>x<H>.npz: bloom_input() and every
+bloom image after the reference's pyramid (Bloom::Prepare's eight downsampling and eight upsampling
+steps); and tests/golden/ref_final_<W>x<H>.npz: two final_case() states (the inputs FINAL_INPUTS,
+the frame and final parameters, the adapted average luminance) and FINAL and BLOOM_INPUT after the
+reference's CmCheckerboard + CmPrepareFinal.
 """
 import ctypes as C
 import os
@@ -110,6 +112,51 @@ def run_reference_bloom(W, H, inp: np.ndarray) -> dict:
     return {k: a for k, a in ref.arrays.items() if k[0].startswith("BLOOM")}
 
 
+def final_case(W, H, seed=SEED, saturation=(0.0, 0.0, 0.0), crosstalk=(1.0, 1.0, 1.0), coverage=0.25,
+               scattering=True):
+    """The oracle after start_state's frame is denoised and exposed, ready for the final
+    composition, with inputs the scene leaves trivial made varied (seeded): 40 % of the pixels
+    split by the checkerboard (THROUGHPUT.a = 1 at their checkerboard position), screen emission
+    on 20 % of the pixels, a volumetric SCATTERING image (rgb in [0, 0.05), a in [0.6, 1)).
+    Returns (stream, frame params, final params, fi)."""
+    o, p, fi = start_state(W, H, seed)
+    o.denoise(fi, p)
+    o.calculate_exposure(fi, p)
+    rng = np.random.default_rng(seed + 17)
+    thr = o.plane("THROUGHPUT", fi)
+    a = thr[..., 3].view(np.float16)
+    a[...] = np.where(rng.random((H, W)) < 0.4, np.float16(1.0), a)
+    r = (rng.integers(0, 15, (H, W)) << 6) | rng.integers(0, 64, (H, W))
+    g = (rng.integers(0, 15, (H, W)) << 6) | rng.integers(0, 64, (H, W))
+    b = (rng.integers(0, 15, (H, W)) << 5) | rng.integers(0, 32, (H, W))
+    o.plane("SCREEN_EMIS_RT", fi)[...] = (r | (g << 11) | (b << 22)).astype(np.uint32) * (rng.random((H, W)) < 0.2)
+    v = np.empty((H, W, 4), np.float32)
+    v[..., :3] = rng.uniform(0.0, 0.05, (H, W, 3))
+    v[..., 3] = rng.uniform(0.6, 1.0, (H, W))
+    if not scattering:
+        v[...] = (0.0, 0.0, 0.0, 1.0)
+    o.plane("SCATTERING", fi)[...] = v.astype(np.float16).view(np.uint16)
+    f = N.FinalParams.defaults()
+    f.saturation[:] = saturation
+    f.crosstalk[:] = crosstalk
+    f.lightmapScreenCoverage = coverage
+    # the reference always applies the scattering image; without the flag it holds (0, 0, 0, 1)
+    f.flags = N.FINAL_APPLY_SCATTERING if scattering else 0
+    return o, p, f, fi
+
+
+FINAL_INPUTS = ("PRE_FINAL", "SCREEN_EMIS_RT", "THROUGHPUT", "SCATTERING")
+FINAL_OUTPUTS = ("FINAL", "BLOOM_INPUT")
+
+
+def run_reference_final_case(o, p, f, fi) -> dict:
+    """The reference's CmCheckerboard + CmPrepareFinal over the oracle's state: {fb: plane} of
+    FINAL and BLOOM_INPUT."""
+    _, avg, _ = o.tonemapping()
+    ref = runner.run_reference_final(o.width, o.height, runner.oracle_planes(o, fi), fi, p, f, avg)
+    return {fb: ref[(fb, fi)] for fb in FINAL_OUTPUTS}
+
+
 def main(argv):
     sizes = [(int(argv[i]), int(argv[i + 1])) for i in range(0, len(argv), 2)] or [(64, 36)]
     here = os.path.dirname(os.path.abspath(__file__))
@@ -123,6 +170,23 @@ def main(argv):
     for (fb, slot), a in run_reference_bloom(W, H, bloom_input(W, H)).items():
         out[f"{fb}/{slot}"] = a
     path = os.path.join(here, f"ref_bloom_{W}x{H}.npz")
+    np.savez_compressed(path, **out)
+    print(path, os.path.getsize(path))
+    # the final composition (CmCheckerboard + CmPrepareFinal) at the first size, default and
+    # non-default LPM saturation / crosstalk
+    out = {"meta": np.array([W, H], dtype=np.int64)}
+    for c, (sat, ct) in enumerate([((0.0, 0.0, 0.0), (1.0, 1.0, 1.0)), ((0.3, -0.2, 0.1), (1.0, 0.5, 0.25))]):
+        o, p, f, fi = final_case(W, H, saturation=sat, crosstalk=ct)
+        _, avg, _ = o.tonemapping()
+        out[f"c{c}/params"] = np.frombuffer(bytes(p), dtype=np.uint8)
+        out[f"c{c}/final"] = np.frombuffer(bytes(f), dtype=np.uint8)
+        out[f"c{c}/avg"] = np.float32(avg)
+        out[f"c{c}/fi"] = np.int64(fi)
+        for fb in FINAL_INPUTS:
+            out[f"c{c}/in/{fb}"] = o.plane(fb, fi).copy()
+        for fb, a in run_reference_final_case(o, p, f, fi).items():
+            out[f"c{c}/out/{fb}"] = a
+    path = os.path.join(here, f"ref_final_{W}x{H}.npz")
     np.savez_compressed(path, **out)
     print(path, os.path.getsize(path))
 

@@ -19,6 +19,10 @@ the oracle's bit for bit after every stage.
   before the variance pass; the forward-projected luminance before the gradient samples) must
   show up as a difference at that stage.
 - test_oracle_bloom_*: the bloom pyramid (every bloom image), from the committed vectors and live.
+- test_oracle_final_*: the final composition, CmCheckerboard + CmPrepareFinal (the LPM control
+  block from the reference's own CPU-side LpmSetup), with split checkerboard pixels, classic
+  shading on part of the image, screen emission, scattering, non-default saturation and
+  crosstalk; from the committed vectors and live.
 """
 import glob
 import os
@@ -182,3 +186,64 @@ def test_oracle_bloom_matches_reference_shaders_live(size):
     assert len(ref) == 10
     assert all(np.count_nonzero(ref[(fb, 0)]) for fb in ("BLOOM_INPUT", "BLOOM_MIP1", "BLOOM_MIP2", "BLOOM_RESULT"))
     assert runner.differing(ref, oracle_bloom(W, H, inp)) == []
+
+
+GOLDEN_FINAL = sorted(glob.glob(os.path.join(ROOT, "tests", "golden", "ref_final_*.npz")))
+
+
+@pytest.mark.parametrize("path", GOLDEN_FINAL, ids=[os.path.basename(p) for p in GOLDEN_FINAL])
+def test_oracle_final_matches_reference_vectors(path):
+    """The oracle's prepare_final (CmCheckerboard + CmPrepareFinal with the LPM filter) against the
+    reference's outputs for the same inputs: FINAL and BLOOM_INPUT bit for bit."""
+    z = np.load(path)
+    W, H = (int(v) for v in z["meta"])
+    cases = sorted({k.split("/")[0] for k in z.files if k != "meta"})
+    assert len(cases) == 2
+    for c in cases:
+        p = N.FrameParams.from_buffer_copy(bytes(z[f"{c}/params"]))
+        f = N.FinalParams.from_buffer_copy(bytes(z[f"{c}/final"]))
+        fi = int(z[f"{c}/fi"])
+        o = oracle.OracleStream(W, H, oracle.MODE_REF)
+        for key in z.files:
+            if key.startswith(f"{c}/in/"):
+                o.load(key.split("/")[2], fi, z[key])
+        o.set_tonemapping(np.zeros(256, dtype=np.uint32), float(z[f"{c}/avg"]))
+        o.prepare_final(fi, f)
+        for fb in ("FINAL", "BLOOM_INPUT"):
+            exp = z[f"{c}/out/{fb}"]
+            assert np.count_nonzero(exp) > exp.size // 2
+            assert np.array_equal(o.plane(fb, fi), exp), (c, fb)
+
+
+@pytest.mark.parametrize("size,sat,ct,scat", [
+    ((64, 36), (0.0, 0.0, 0.0), (1.0, 1.0, 1.0), True),
+    ((98, 33), (0.3, -0.2, 0.1), (1.0, 0.5, 0.25), True),
+    ((130, 9), (-0.5, 0.0, 0.5), (0.25, 1.0, 0.5), False),
+    ((250, 151), (0.0, 0.0, 0.0), (1.0, 1.0, 1.0), True),
+])
+def test_oracle_final_matches_reference_shaders_live(size, sat, ct, scat):
+    why = _live_ready()
+    if why:
+        pytest.skip(why)
+    from tests.golden.make_ref_shader_vectors import final_case, run_reference_final_case
+    o, p, f, fi = final_case(*size, saturation=sat, crosstalk=ct, scattering=scat)
+    ref = run_reference_final_case(o, p, f, fi)
+    o.prepare_final(fi, f)
+    got = {fb: o.plane(fb, fi) for fb in ref}
+    assert runner.differing({(fb, 0): a for fb, a in ref.items()}, {(fb, 0): a for fb, a in got.items()}) == []
+
+
+def test_final_planted_mistake_is_caught():
+    """A PRE_FINAL texel at a split pixel's neighbour changed on the oracle's side only moves the
+    resolved pixels beside it."""
+    why = _live_ready()
+    if why:
+        pytest.skip(why)
+    from tests.golden.make_ref_shader_vectors import final_case, run_reference_final_case
+    o, p, f, fi = final_case(64, 36)
+    ref = run_reference_final_case(o, p, f, fi)
+    pre = o.plane("PRE_FINAL", fi)
+    pre[10, 30] = pre[10, 30] ^ np.uint32(1 << 12)
+    o.prepare_final(fi, f)
+    assert not np.array_equal(o.plane("FINAL", fi), ref["FINAL"])
+
