@@ -54,7 +54,14 @@ SHADERS = {
     "RtGradients_main.comp": {},
     "CmCheckerboard.comp": {},
     "CmPrepareFinal.comp": {},
+    "CmVolumetricProcess.comp": {},
+    "CmScatterAccum.comp": {},
 }
+
+# rgdn_volumetric_params fields that ShGlobalUniform has under the same name (Volumetric's
+# uniform inputs of CmVolumetricProcess.comp and CmScatterAccum.comp)
+VOLUME_COPY = ["invView", "invProjection", "volumeViewProj", "cameraPosition", "volumeCameraNear",
+               "volumeCameraFar", "volumeAmbient", "volumeScattering", "volumeEnableType", "frameId"]
 
 # rgdn_final_params fields that ShGlobalUniform has under the same name (ImageComposition's
 # uniform inputs of CmPrepareFinal.comp)
@@ -201,10 +208,11 @@ def rewrite(flat: str, spec: dict) -> tuple[str, dict]:
             pos = close + 1 + mm.end()
             continue
         # image / sampler
-        mm = re.match(r"\s*" + quals + r"uniform\s+" + quals + r"([iu]?)(image2D|sampler2D)\s+(\w+)\s*;", rest)
+        mm = re.match(r"\s*" + quals + r"uniform\s+" + quals +
+                      r"([iu]?)(image2D|sampler2D|image3D|sampler3D|texture2DArray)\s+(\w+)\s*;", rest)
         if mm:
             typ, name = mm.group(1) + mm.group(2), mm.group(3)
-            if mm.group(2) == "image2D":
+            if mm.group(2) in ("image2D", "image3D"):
                 fmt = [k for k, v in args.items() if v is None]
                 if len(fmt) != 1:
                     raise RuntimeError(f"image {name}: format not found in layout({args})")
@@ -286,6 +294,12 @@ def translation_unit(shader: str, body: str, info: dict, tag: str) -> str:
         sets = [f"std::memcpy(&u.{f}, &p->{f}, sizeof(p->{f}));" for f in FINAL_COPY]
         lines.append(f"void ref_{tag}_set_final(const rgdn_final_params* p) {{ "
                      f"auto& u = {ns}::globalUniform; {' '.join(sets)} }}")
+        sets = [f"std::memcpy(&u.{f}, &p->{f}, sizeof(p->{f}));" for f in VOLUME_COPY]
+        lines.append(f"void ref_{tag}_set_volumetric(const rgdn_volumetric_params* p) {{ "
+                     f"auto& u = {ns}::globalUniform; {' '.join(sets)} }}")
+    if re.search(r"\}\s*push\s*;", body):
+        # the push-constant block
+        lines.append(f"void* ref_{tag}_push() {{ return &{ns}::push; }}")
     if info["tonemapping"]:
         lines.append(f"void* ref_{tag}_tonemapping() {{ return &{ns}::tonemapping; }}")
     if re.search(r"\bstatic\s+uvec4\s+g_lpmParams\s*\[", body):

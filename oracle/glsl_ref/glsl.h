@@ -620,6 +620,7 @@ struct Plane
 {
     uint8_t* data = nullptr;
     int      w = 0, h = 0, fmt = FMT_none;
+    int      d = 1;   // depth of a 3-D image: slices of w x h texels, z-major
 };
 std::map< std::string, Plane >& planes();   // by image name, shared by every shader of the library
 std::map< std::string, int >&   formats();  // the format each image is declared with
@@ -658,6 +659,10 @@ struct SamplerBase
 struct sampler2D : SamplerBase { using SamplerBase::SamplerBase; };
 struct usampler2D : SamplerBase { using SamplerBase::SamplerBase; };
 struct isampler2D : SamplerBase { using SamplerBase::SamplerBase; };
+struct image3D : ImageBase { using ImageBase::ImageBase; };
+struct sampler3D : SamplerBase { using SamplerBase::SamplerBase; };
+// declared for the blue-noise array of Random.h, which the shaders run here do not read
+struct texture2DArray : SamplerBase { using SamplerBase::SamplerBase; };
 
 // texel load / store in the plane's format (outside the plane: zero on load, dropped on store)
 vec4  load_f( Plane& p, ivec2 pix );
@@ -677,6 +682,17 @@ inline uvec4 texelFetch( usampler2D& s, const ivec2& pix, int ) { return load_u(
 // the weight x - floor(x), mix(x, y, a) = x (1 - a) + y a, rows first. Only LOD 0 is read.
 vec4 bilinear( Plane& p, const vec2& uv );
 inline vec4 textureLod( sampler2D& s, const vec2& uv, float ) { return bilinear( s.plane(), uv ); }
+// 3-D images: texel (x, y, z) of a w x h x d image; outside it, zero on load and dropped on store
+vec4 load_f3( Plane& p, ivec3 c );
+void store_f3( Plane& p, ivec3 c, const vec4& v );
+inline vec4 imageLoad( image3D& im, const ivec3& c ) { return load_f3( im.plane(), c ); }
+inline void imageStore( image3D& im, const ivec3& c, const vec4& v ) { store_f3( im.plane(), c, v ); }
+inline vec4 texelFetch( sampler3D& s, const ivec3& c, int ) { return load_f3( s.plane(), c ); }
+inline vec4 texelFetch( texture2DArray&, const ivec3&, int ) { return vec4( 0.0f ); }
+// Linear filtering of a 3-D image with clamp-to-edge addressing, the weights exactly in
+// binary32 as bilinear() takes them: along x, then y, then z.
+vec4 trilinear( Plane& p, const vec3& uvw );
+inline vec4 textureLod( sampler3D& s, const vec3& uvw, float ) { return trilinear( s.plane(), uvw ); }
 inline vec4 texture( sampler2D& s, const vec2& uv ) { return bilinear( s.plane(), uv ); }
 inline ivec2 imageSize( ImageBase& im ) { return ivec2( im.plane().w, im.plane().h ); }
 inline ivec2 textureSize( SamplerBase& s, int ) { return ivec2( s.plane().w, s.plane().h ); }

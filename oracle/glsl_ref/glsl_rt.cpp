@@ -167,6 +167,59 @@ vec4 bilinear( Plane& p, const vec2& uv )
     return mix( mix( t00, t10, a ), mix( t01, t11, a ), b );
 }
 
+// a 3-D image's texel as a texel of the w x (h d) plane of its slices
+static bool slice_pix( const Plane& p, const ivec3& c, ivec2& pix )
+{
+    if( !p.data || c.x < 0 || c.y < 0 || c.z < 0 || c.x >= p.w || c.y >= p.h || c.z >= p.d ) return false;
+    pix = ivec2( c.x, c.z * p.h + c.y );
+    return true;
+}
+static Plane slices( const Plane& p )
+{
+    Plane q = p;
+    q.h     = p.h * p.d;
+    q.d     = 1;
+    return q;
+}
+vec4 load_f3( Plane& p, ivec3 c )
+{
+    ivec2 pix;
+    if( !slice_pix( p, c, pix ) ) return vec4( 0.0f );
+    Plane q = slices( p );
+    return load_f( q, pix );
+}
+void store_f3( Plane& p, ivec3 c, const vec4& v )
+{
+    ivec2 pix;
+    if( !slice_pix( p, c, pix ) ) return;
+    Plane q = slices( p );
+    store_f( q, pix, v );
+}
+
+vec4 trilinear( Plane& p, const vec3& uvw )
+{
+    if( !p.data ) return vec4( 0.0f );
+    const int n[ 3 ] = { p.w, p.h, p.d };
+    int       i0[ 3 ], i1[ 3 ];
+    float     f[ 3 ];
+    for( int k = 0; k < 3; k++ )
+    {
+        const float x  = uvw.v[ k ] * (float)n[ k ] - 0.5f;
+        const float fx = std::floor( x );
+        // NaN to 0; beyond the int range saturated
+        const int ix = fx == fx ? (int)std::min( std::max( fx, -1073741824.0f ), 1073741824.0f ) : 0;
+        i0[ k ] = std::min( std::max( ix, 0 ), n[ k ] - 1 );
+        i1[ k ] = std::min( std::max( ix, -1 ) + 1, n[ k ] - 1 );
+        f[ k ]  = x - fx;
+    }
+    auto t = [ & ]( int x, int y, int z ) { return load_f3( p, ivec3( x, y, z ) ); };
+    const vec4 c00 = mix( t( i0[ 0 ], i0[ 1 ], i0[ 2 ] ), t( i1[ 0 ], i0[ 1 ], i0[ 2 ] ), f[ 0 ] );
+    const vec4 c10 = mix( t( i0[ 0 ], i1[ 1 ], i0[ 2 ] ), t( i1[ 0 ], i1[ 1 ], i0[ 2 ] ), f[ 0 ] );
+    const vec4 c01 = mix( t( i0[ 0 ], i0[ 1 ], i1[ 2 ] ), t( i1[ 0 ], i0[ 1 ], i1[ 2 ] ), f[ 0 ] );
+    const vec4 c11 = mix( t( i0[ 0 ], i1[ 1 ], i1[ 2 ] ), t( i1[ 0 ], i1[ 1 ], i1[ 2 ] ), f[ 0 ] );
+    return mix( mix( c00, c10, f[ 1 ] ), mix( c01, c11, f[ 1 ] ), f[ 2 ] );
+}
+
 uvec4 load_u( Plane& p, ivec2 pix )
 {
     const uint8_t* t = texel( p, pix );
@@ -327,6 +380,27 @@ int ref_bind( const char* name, void* data, int w, int h )
     p.data         = static_cast< uint8_t* >( data );
     p.w            = w;
     p.h            = h;
+    p.d            = 1;
+    p.fmt          = it->second;
+    return glsl::fmt_bytes( p.fmt );
+}
+// Binds a 3-D image (d slices of w x h texels) to `name` and the samplers named after it. A name
+// that only samplers use (such as a _Sampler_Prev) takes the format `fmt`; a declared image keeps
+// its declared format. Returns the texel size, 0 if the format is unknown.
+int ref_bind3d( const char* name, void* data, int w, int h, int d, int fmt )
+{
+    auto it = glsl::formats().find( name );
+    if( it == glsl::formats().end() )
+    {
+        if( fmt < 0 || fmt >= glsl::FMT_none ) return 0;
+        glsl::formats()[ name ] = fmt;
+        it                      = glsl::formats().find( name );
+    }
+    glsl::Plane& p = glsl::planes()[ name ];
+    p.data         = static_cast< uint8_t* >( data );
+    p.w            = w;
+    p.h            = h;
+    p.d            = d;
     p.fmt          = it->second;
     return glsl::fmt_bytes( p.fmt );
 }

@@ -177,3 +177,41 @@ def run_reference_final(W: int, H: int, planes: dict, fi: int, params, final, av
         getattr(lib, f"ref_{tag}_dispatch")(int(groups[0]), int(groups[1]))
     return run.arrays
 
+
+FMT_RGBA16F = 5   # glsl::FMT_rgba16f
+
+
+def run_reference_scattering(W: int, H: int, planes: dict, fi: int, params, vparams, lib: C.CDLL | None = None) -> dict:
+    """Volumetric::ProcessScattering as the reference records it (Source/Volumetric.cpp:71-190):
+    CmVolumetricProcess over the froxel columns (the volume integrated in place), then
+    CmScatterAccum over the render size with maxHistoryLength as its push constant. The oracle's
+    SCATTER_VOLUME planes (X x (Y Z) texels, z-major) are bound as the 3-D images g_volumetric
+    (this frame) and g_volumetric_Prev (the previous frame's, read through
+    g_volumetric_Sampler_Prev). Returns the reference's planes after both shaders."""
+    from raytracedgl1_gb300 import _native as N
+    lib = lib or load()
+    lib.ref_bind3d.argtypes = [C.c_char_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int]
+    lib.ref_bind3d.restype = C.c_int
+    run = RefRun(W, H, lib)
+    planes = dict(planes)
+    vols = {slot: planes.pop(("SCATTER_VOLUME", slot)) for slot in (fi, fi ^ 1) if ("SCATTER_VOLUME", slot) in planes}
+    run.bind_from(planes, fi)
+    X, Y, Z = N.VOLUME_SIZE
+    for slot, vol in vols.items():
+        a = np.ascontiguousarray(vol).copy()
+        name = b"g_volumetric" if slot == fi else b"g_volumetric_Prev"
+        if not lib.ref_bind3d(name, a.ctypes.data, X, Y, Z, FMT_RGBA16F):
+            raise RuntimeError(f"ref_bind3d {name!r}")
+        run.arrays[("SCATTER_VOLUME", slot)] = a
+    for tag in ("CmVolumetricProcess", "CmScatterAccum"):
+        getattr(lib, f"ref_{tag}_set_uniform")(C.byref(params), C.c_float(W), C.c_float(H))
+        getattr(lib, f"ref_{tag}_set_volumetric")(C.byref(vparams))
+    push = lib.ref_CmScatterAccum_push
+    push.restype = C.c_void_p
+    C.memmove(push(), np.array([vparams.maxHistoryLength], dtype=np.float32).ctypes.data, 4)
+    for tag, (w, h) in (("CmVolumetricProcess", (X, Y)), ("CmScatterAccum", (W, H))):
+        local = (C.c_uint * 3)()
+        getattr(lib, f"ref_{tag}_local")(local)
+        getattr(lib, f"ref_{tag}_dispatch")(-(-w // local[0]), -(-h // local[1]))
+    return run.arrays
+

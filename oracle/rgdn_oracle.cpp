@@ -13,10 +13,11 @@
 //  every stage: the gradient samples (RtGradients.rgen's main(), its ray-traced forward
 //  projection read from the boundary input RGDN_FB_GRADIENT_RESHADED), the gradient a-trous,
 //  temporal accumulation, anti-firefly, variance, the a-trous iterations with the composition,
-//  the histogram and the adaptation, the bloom pyramid, and the final composition
-//  (CmCheckerboard + CmPrepareFinal, the LPM control block from the reference's own CPU-side
-//  LpmSetup) (committed vectors in tests/golden, and live where the reference checkout is
-//  present). The re-shading of the analytic scene, the bloom's apply and the volumetric passes
+//  the histogram and the adaptation, the bloom pyramid, the volumetric scattering
+//  (CmVolumetricProcess + CmScatterAccum) and the final composition (CmCheckerboard +
+//  CmPrepareFinal, the LPM control block from the reference's own CPU-side LpmSetup)
+//  (committed vectors in tests/golden, and live where the reference checkout is present).
+//  The re-shading of the analytic scene and the bloom's apply
 //  stay pinned only by the codecs' known-answer tests from the public specs they implement
 //  (IEEE-754 binary16/bfloat16, EXT_texture_shared_exponent, the Vulkan B10G11R11
 //  unsigned-float layout) and the closed-form known-answer tests in tests/.

@@ -157,6 +157,74 @@ def run_reference_final_case(o, p, f, fi) -> dict:
     return {fb: ref[(fb, fi)] for fb in FINAL_OUTPUTS}
 
 
+def volume_input(seed: int) -> np.ndarray:
+    """A SCATTER_VOLUME plane ((Y Z) x X texels of RGBA16F) from an integer hash of the texel
+    index (the same bits on every machine): rgb in [0, 0.5), a in [0, 0.1)."""
+    X, Y, Z = N.VOLUME_SIZE
+    i = np.arange(Y * Z * X * 4, dtype=np.uint32) + np.uint32(seed * 0x9E3779B9 & 0xFFFFFFFF)
+    h = i
+    h = h ^ (h >> np.uint32(16)); h = h * np.uint32(0x7feb352d)
+    h = h ^ (h >> np.uint32(15)); h = h * np.uint32(0x846ca68b)
+    h = h ^ (h >> np.uint32(16))
+    u = (h >> np.uint32(8)).astype(np.float32) * np.float32(1.0 / 16777216.0)
+    u = u.reshape(Y * Z, X, 4)
+    u[..., :3] *= np.float32(0.5)
+    u[..., 3] *= np.float32(0.1)
+    return u.astype(np.float16).view(np.uint16)
+
+
+SCATTER_INPUTS = (("NORMAL", 0), ("NORMAL", 1), ("DEPTH_WORLD", 0), ("DEPTH_WORLD", 1), ("MOTION", 1),
+                  ("DEPTH_NDC", 1), ("SCATTERING", 0), ("SCATTERING_HISTORY", 0))
+
+
+def volumetric_params(mode: int, frame_id: int):
+    """Matrices that place every pixel's world position inside the froxel volume: world = NDC
+    through a slightly skewed inverse view-projection, a volume projection with a small
+    perspective term, the camera behind the screen."""
+    p = N.VolumetricParams()
+    iv = np.eye(4, dtype=np.float32)
+    iv[3, 0] = 0.05
+    ip = np.eye(4, dtype=np.float32)
+    ip[1, 0] = 0.02
+    vp = np.eye(4, dtype=np.float32)
+    vp[2, 3] = 0.1
+    p.invView[:] = iv.reshape(-1)          # rows of these arrays are GLSL columns
+    p.invProjection[:] = ip.reshape(-1)
+    p.volumeViewProj[:] = vp.reshape(-1)
+    p.cameraPosition[:] = (0.0, 0.0, -1.0, 0.0)
+    p.volumeCameraNear, p.volumeCameraFar = 0.5, 3.0
+    p.volumeAmbient[:] = (0.2, 0.4, 0.8)
+    p.volumeScattering = 300.0
+    p.maxHistoryLength = 6.0
+    p.volumeEnableType = mode
+    p.frameId = frame_id
+    return p
+
+
+def scattering_case(W, H, mode, seed=SEED):
+    """The oracle ready for the second frame's Volumetric::ProcessScattering: frame 0's scattering
+    processed over a random history, frame 1's G-buffer and NDC depth loaded, both volumes from
+    volume_input(). Returns (stream, frame params, volumetric params, fi = 1)."""
+    rng = np.random.default_rng(seed + 31 * mode)
+    sc = Scene(W, H, seed=seed + mode)
+    o = oracle.OracleStream(W, H, oracle.MODE_REF)
+    for fi in (0, 1):
+        o.load("SCATTER_VOLUME", fi, volume_input(seed * 2 + fi))
+    prev = np.concatenate([rng.uniform(0, 1, (H, W, 3)), rng.uniform(0.2, 1, (H, W, 1))], axis=2)
+    o.load("SCATTERING", 1, prev.astype(np.float16).view(np.uint16))
+    o.load("SCATTERING_HISTORY", 1, rng.uniform(1, 5, (H, W)).astype(np.float16).view(np.uint16))
+    for f in range(2):
+        fi = f & 1
+        bufs, p = sc.generate(f)
+        for k in ("NORMAL", "DEPTH_WORLD", "MOTION"):
+            o.load(k, fi, np.ascontiguousarray(bufs[k]))
+        o.load("DEPTH_NDC", fi, rng.uniform(0.1, 0.9, (H, W)).astype(np.float32))
+        vp = volumetric_params(mode, 100 + f)
+        if f == 0:
+            o.process_scattering(fi, vp)
+    return o, p, vp, 1
+
+
 def main(argv):
     sizes = [(int(argv[i]), int(argv[i + 1])) for i in range(0, len(argv), 2)] or [(64, 36)]
     here = os.path.dirname(os.path.abspath(__file__))
@@ -187,6 +255,25 @@ def main(argv):
         for fb, a in run_reference_final_case(o, p, f, fi).items():
             out[f"c{c}/out/{fb}"] = a
     path = os.path.join(here, f"ref_final_{W}x{H}.npz")
+    np.savez_compressed(path, **out)
+    print(path, os.path.getsize(path))
+    # Volumetric::ProcessScattering in each volume mode at the first size: the 2-D inputs and
+    # outputs, this frame's volume by its volume_input() seed (the previous frame's is not read:
+    # CmVolumetricProcess's temporal weight is 0) and the processed volume by its SHA-256
+    import hashlib
+    out = {"meta": np.array([W, H], dtype=np.int64)}
+    for mode in (N.VOLUME_ENABLE_NONE, N.VOLUME_ENABLE_SIMPLE, N.VOLUME_ENABLE_VOLUMETRIC):
+        o, p, vp, fi = scattering_case(W, H, mode)
+        out[f"m{mode}/params"] = np.frombuffer(bytes(p), dtype=np.uint8)
+        out[f"m{mode}/vparams"] = np.frombuffer(bytes(vp), dtype=np.uint8)
+        for fb, slot in SCATTER_INPUTS:
+            out[f"m{mode}/in/{fb}/{slot}"] = o.plane(fb, slot).copy()
+        ref = runner.run_reference_scattering(W, H, runner.oracle_planes(o, fi), fi, p, vp)
+        for fb in ("SCATTERING", "SCATTERING_HISTORY"):
+            out[f"m{mode}/out/{fb}"] = ref[(fb, fi)]
+        out[f"m{mode}/out/SCATTER_VOLUME_sha256"] = np.frombuffer(
+            hashlib.sha256(ref[("SCATTER_VOLUME", fi)].tobytes()).digest(), dtype=np.uint8)
+    path = os.path.join(here, f"ref_scattering_{W}x{H}.npz")
     np.savez_compressed(path, **out)
     print(path, os.path.getsize(path))
 

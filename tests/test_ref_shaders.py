@@ -19,6 +19,8 @@ the oracle's bit for bit after every stage.
   before the variance pass; the forward-projected luminance before the gradient samples) must
   show up as a difference at that stage.
 - test_oracle_bloom_*: the bloom pyramid (every bloom image), from the committed vectors and live.
+- test_oracle_scattering_*: Volumetric::ProcessScattering (CmVolumetricProcess + CmScatterAccum)
+  in the three volume modes, the froxel volume bound as a 3-D image.
 - test_oracle_final_*: the final composition, CmCheckerboard + CmPrepareFinal (the LPM control
   block from the reference's own CPU-side LpmSetup), with split checkerboard pixels, classic
   shading on part of the image, screen emission, scattering, non-default saturation and
@@ -246,4 +248,50 @@ def test_final_planted_mistake_is_caught():
     pre[10, 30] = pre[10, 30] ^ np.uint32(1 << 12)
     o.prepare_final(fi, f)
     assert not np.array_equal(o.plane("FINAL", fi), ref["FINAL"])
+
+
+GOLDEN_SCATTER = sorted(glob.glob(os.path.join(ROOT, "tests", "golden", "ref_scattering_*.npz")))
+
+
+@pytest.mark.parametrize("path", GOLDEN_SCATTER, ids=[os.path.basename(p) for p in GOLDEN_SCATTER])
+def test_oracle_scattering_matches_reference_vectors(path):
+    """The oracle's process_scattering (CmVolumetricProcess + CmScatterAccum) against the
+    reference's outputs in the three volume modes: SCATTERING and SCATTERING_HISTORY bit for bit,
+    the processed volume by its SHA-256."""
+    import hashlib
+    from tests.golden.make_ref_shader_vectors import SEED, volume_input
+    z = np.load(path)
+    W, H = (int(v) for v in z["meta"])
+    modes = sorted({k.split("/")[0] for k in z.files if k != "meta"})
+    assert len(modes) == 3
+    for m in modes:
+        p = N.FrameParams.from_buffer_copy(bytes(z[f"{m}/params"]))
+        vp = N.VolumetricParams.from_buffer_copy(bytes(z[f"{m}/vparams"]))
+        o = oracle.OracleStream(W, H, oracle.MODE_REF)
+        o.load("SCATTER_VOLUME", 1, volume_input(SEED * 2 + 1))
+        for key in z.files:
+            if key.startswith(f"{m}/in/"):
+                _, _, fb, slot = key.split("/")
+                o.load(fb, int(slot), z[key])
+        o.process_scattering(1, vp)
+        for fb in ("SCATTERING", "SCATTERING_HISTORY"):
+            assert np.array_equal(o.plane(fb, 1), z[f"{m}/out/{fb}"]), (m, fb)
+        digest = hashlib.sha256(o.plane("SCATTER_VOLUME", 1).tobytes()).digest()
+        assert digest == bytes(z[f"{m}/out/SCATTER_VOLUME_sha256"]), m
+
+
+@pytest.mark.parametrize("size", [(64, 36), (50, 23), (250, 151)])
+@pytest.mark.parametrize("mode", [N.VOLUME_ENABLE_NONE, N.VOLUME_ENABLE_SIMPLE, N.VOLUME_ENABLE_VOLUMETRIC])
+def test_oracle_scattering_matches_reference_shaders_live(size, mode):
+    why = _live_ready()
+    if why:
+        pytest.skip(why)
+    from tests.golden.make_ref_shader_vectors import scattering_case
+    W, H = size
+    o, p, vp, fi = scattering_case(W, H, mode)
+    ref = runner.run_reference_scattering(W, H, runner.oracle_planes(o, fi), fi, p, vp)
+    o.process_scattering(fi, vp)
+    got = runner.oracle_planes(o, fi)
+    keys = [("SCATTER_VOLUME", fi), ("SCATTERING", fi), ("SCATTERING_HISTORY", fi)]
+    assert runner.differing({k: ref[k] for k in keys}, got) == []
 
