@@ -582,6 +582,30 @@ def test_prepare_final_parity(ctx, mode_name, mode, size, exact):
     s.close()
 
 
+@pytest.mark.parametrize("mode_name,mode", MODES)
+def test_prepare_final_classic_exact_is_bit_exact(ctx, mode_name, mode):
+    """With classic shading over the whole width and RGDN_FINAL_EXACT_MATH, FINAL is uncharted2
+    of the (resolved) HDR colour in IEEE arithmetic on both sides, so it must equal the oracle's
+    bit for bit, split pixels included: the resolved colour passes through FINAL's format between
+    CmCheckerboard and CmPrepareFinal on both."""
+    W, H = 50, 23
+    o = _final_inputs(W, H, mode, seed=7)
+    split = o.plane("THROUGHPUT", 0)[..., 3].view(np.float16) > 0.5
+    assert split.sum() > 100
+    s = Stream(ctx, W, H, mode)
+    for name in ("PRE_FINAL", "SCREEN_EMIS_RT", "SCATTERING", "THROUGHPUT"):
+        s.upload(name, 0, o.plane(name, 0))
+    s.set_tonemapping(None, 0.35)
+    o.set_tonemapping(None, 0.35)
+    p = N.FinalParams.defaults()
+    p.lightmapScreenCoverage = 1.0
+    p.flags = N.FINAL_EXACT_MATH
+    ImageComposition(s).Finalize(0, p)
+    o.prepare_final(0, p)
+    assert np.array_equal(s.download("FINAL", 0), o.plane("FINAL", 0))
+    s.close()
+
+
 def _encode_pre(rgb: np.ndarray, fmt: int) -> np.ndarray:
     """HDR colours as the bytes of a pre-tonemapping plane of the given storage format."""
     H, W, _ = rgb.shape
