@@ -563,6 +563,17 @@ typedef struct rgdn_server_create_info
 
 /* G-buffer source of a request: planes RGDN_FB_ALBEDO .. RGDN_FB_GRADIENT_RESHADED */
 #define RGDN_GBUFFER_PLANES 15
+
+/* Copies `count` (1 .. RGDN_GBUFFER_PLANES) host ranges src[k] of bytes[k] into device memory
+ * dst[k], asynchronously on cudaStream, the way a served frame's planes reach the device: with
+ * RGDN_HOST_COPY_SM the ranges in pinned, device-mapped host memory with 16-byte aligned
+ * addresses and sizes are loaded by one kernel (32 blocks) over the host link, and the others go
+ * through cudaMemcpyAsync; with RGDN_HOST_COPY_ENGINE every range goes through cudaMemcpyAsync.
+ * For a renderer that streams its G-buffer from host memory into device planes it binds with
+ * rgdn_stream_bind_framebuffer. The reference has no counterpart: its G-buffer is written on the
+ * device by its ray-tracing pipeline. */
+rgdn_status rgdn_copy_host_planes( void* const* dst, const void* const* src, const size_t* bytes, uint32_t count,
+                                   uint32_t hostCopy, rgdn_cuda_stream cudaStream );
 #define RGDN_REQUEST_COPY 0u   /* gbuffer[] are host (pinned or pageable) or device pointers; copied
                                   into the stream's planes inside the step */
 #define RGDN_REQUEST_BIND 1u   /* gbuffer[] are device pointers used in place (no copy); they must

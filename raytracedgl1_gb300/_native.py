@@ -259,6 +259,7 @@ SIGNATURES = [
     ("rgdn_server_stats_get", _I, [_VP, C.POINTER(ServerStats)]),
     ("rgdn_server_stats_reset", _I, [_VP]),
     ("rgdn_server_get_stream", _I, [_VP, _U32, C.POINTER(_VP)]),
+    ("rgdn_copy_host_planes", _I, [C.POINTER(_VP), C.POINTER(_VP), C.POINTER(_SZ), _U32, _U32, _VP]),
 ]
 
 STAGE_NAMES = ["gradient_samples", "gradient_atrous", "temporal_accumulation", "anti_firefly",

@@ -233,6 +233,28 @@ const void* mapped_host( const void* p )
     return at.type == cudaMemoryTypeHost ? at.devicePointer : nullptr;
 }
 
+// Adds dst <- src (bytes) to the gather list when the SM loader can take it (device-mapped
+// pinned host memory, 16-byte aligned addresses and size); false otherwise
+bool gather_add( GatherList& gl, void* dst, const void* src, size_t bytes )
+{
+    if( gl.count >= RGDN_GBUFFER_PLANES || bytes == 0 || bytes % 16 != 0 || ( (uintptr_t)dst & 15 ) != 0 ) return false;
+    const void* m = mapped_host( src );
+    if( !m || ( (uintptr_t)m & 15 ) != 0 ) return false;
+    const int c       = gl.count++;
+    gl.src[ c ]       = static_cast< const uint4* >( m );
+    gl.dst[ c ]       = static_cast< uint4* >( dst );
+    gl.n16[ c ]       = bytes / 16;
+    gl.first[ c + 1 ] = gl.first[ c ] + (uint32_t)( ( bytes + kChunkBytes - 1 ) / kChunkBytes );
+    return true;
+}
+
+cudaError_t gather_launch( const GatherList& gl, cudaStream_t cs )
+{
+    if( !gl.count ) return cudaSuccess;
+    k_gather_host<<< std::min( gl.first[ gl.count ], kGatherBlocks ), kGatherThreads, 0, cs >>>( gl );
+    return cudaGetLastError();
+}
+
 void record_done( rgdn_server* sv, ServeReq& r, uint32_t state, double t )
 {
     r.state = state;
@@ -272,25 +294,12 @@ rgdn_status enqueue_step( rgdn_server* sv, StepRec& rec, std::vector< rgdn_job >
             rgdn_status r = rgdn_stream_get_framebuffer( sts[ k ], fb, jobs[ k ].frameIndex, &img );
             if( r != RGDN_SUCCESS ) return r;
             const size_t bytes = (size_t)img.pitch_bytes * img.height;
-            if( sv->info.hostCopy == RGDN_HOST_COPY_SM && bytes % 16 == 0 && ( (uintptr_t)img.data & 15 ) == 0 )
-            {
-                const void* m = mapped_host( q.gbuffer[ fb ] );
-                if( m && ( (uintptr_t)m & 15 ) == 0 )
-                {
-                    const int c = gl.count++;
-                    gl.src[ c ]       = static_cast< const uint4* >( m );
-                    gl.dst[ c ]       = static_cast< uint4* >( img.data );
-                    gl.n16[ c ]       = bytes / 16;
-                    gl.first[ c + 1 ] = gl.first[ c ] + (uint32_t)( ( bytes + kChunkBytes - 1 ) / kChunkBytes );
-                    continue;
-                }
-            }
+            if( sv->info.hostCopy == RGDN_HOST_COPY_SM && gather_add( gl, img.data, q.gbuffer[ fb ], bytes ) ) continue;
             if( cudaMemcpyAsync( img.data, q.gbuffer[ fb ], bytes, cudaMemcpyDefault, cs ) != cudaSuccess ) return RGDN_DEVICE_ERROR;
         }
         if( gl.count )
         {
-            k_gather_host<<< std::min( gl.first[ gl.count ], kGatherBlocks ), kGatherThreads, 0, cs >>>( gl );
-            if( cudaGetLastError() != cudaSuccess ) return RGDN_DEVICE_ERROR;
+            if( gather_launch( gl, cs ) != cudaSuccess ) return RGDN_DEVICE_ERROR;
             sv->ctx->launches.fetch_add( 1, std::memory_order_relaxed );
         }
     }
@@ -722,6 +731,24 @@ rgdn_status rgdn_server_get_stream( rgdn_server* sv, uint32_t id, rgdn_stream** 
     if( it == sv->streams.end() ) return RGDN_WRONG_FUNCTION_ARGUMENT;
     *out = it->second.s;
     return RGDN_SUCCESS;
+}
+
+rgdn_status rgdn_copy_host_planes( void* const* dst, const void* const* src, const size_t* bytes, uint32_t count, uint32_t hostCopy,
+                                   rgdn_cuda_stream cudaStream )
+{
+    if( !dst || !src || !bytes || count == 0 || count > RGDN_GBUFFER_PLANES ) return RGDN_WRONG_FUNCTION_ARGUMENT;
+    if( hostCopy != RGDN_HOST_COPY_ENGINE && hostCopy != RGDN_HOST_COPY_SM ) return RGDN_WRONG_FUNCTION_ARGUMENT;
+    for( uint32_t k = 0; k < count; k++ )
+        if( !dst[ k ] || !src[ k ] ) return RGDN_WRONG_FUNCTION_ARGUMENT;
+    const cudaStream_t cs = (cudaStream_t)cudaStream;
+    GatherList         gl;
+    memset( &gl, 0, sizeof( gl ) );
+    for( uint32_t k = 0; k < count; k++ )
+    {
+        if( hostCopy == RGDN_HOST_COPY_SM && gather_add( gl, dst[ k ], src[ k ], bytes[ k ] ) ) continue;
+        if( bytes[ k ] && cudaMemcpyAsync( dst[ k ], src[ k ], bytes[ k ], cudaMemcpyDefault, cs ) != cudaSuccess ) return RGDN_DEVICE_ERROR;
+    }
+    return gather_launch( gl, cs ) == cudaSuccess ? RGDN_SUCCESS : RGDN_DEVICE_ERROR;
 }
 
 }  // extern "C"

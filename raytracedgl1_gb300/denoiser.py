@@ -338,6 +338,18 @@ def histogram_bin_table(min_log: float, max_log: float) -> np.ndarray:
     return out
 
 
+def copy_host_planes(copies, host_copy: int = N.HOST_COPY_SM, cuda_stream=None) -> None:
+    """rgdn_copy_host_planes: copies [(device pointer, host pointer, bytes), ...] (at most
+    RGDN_GBUFFER_PLANES) asynchronously on cuda_stream, pinned device-mapped ranges by one SM
+    kernel with HOST_COPY_SM, the others (and all with HOST_COPY_ENGINE) by cudaMemcpyAsync."""
+    lib = N.load()
+    n = len(copies)
+    dst = (C.c_void_p * n)(*[c[0] for c in copies])
+    src = (C.c_void_p * n)(*[c[1] for c in copies])
+    nb = (C.c_size_t * n)(*[c[2] for c in copies])
+    N.check(lib.rgdn_copy_host_planes(dst, src, nb, n, host_copy, _stream_handle(cuda_stream)), "rgdn_copy_host_planes")
+
+
 class Server:
     """rgdn_server: continuous batching of frame requests from many camera streams, each
     stream's history resident on the device, admission under the context's memory budget."""

@@ -178,3 +178,29 @@ def test_sm_host_copy_equals_copy_engine():
         assert np.array_equal(ha, hb) and aa == ab, f"frame {f}: tonemapping differs"
     assert launches[N.HOST_COPY_SM] - launches[N.HOST_COPY_ENGINE] == len(frames)
     ctx.close()
+
+
+@pytest.mark.parametrize("host_copy", [N.HOST_COPY_SM, N.HOST_COPY_ENGINE])
+def test_copy_host_planes(host_copy):
+    """rgdn_copy_host_planes: pinned (device-mapped) ranges, one of a size that is not a multiple
+    of 16 and one in pageable memory (both of which take cudaMemcpyAsync), all land byte for byte;
+    bad arguments are refused before any copy."""
+    torch = pytest.importorskip("torch")
+    from raytracedgl1_gb300.denoiser import copy_host_planes
+    rng = np.random.default_rng(3 + host_copy)
+    sizes = [1 << 20, (3 << 20) + 16, 4096 + 8, 777 * 16]
+    srcs = [torch.from_numpy(rng.integers(0, 256, n, dtype=np.uint8)).pin_memory() for n in sizes[:3]]
+    pageable = rng.integers(0, 256, sizes[3], dtype=np.uint8)
+    dsts = [torch.zeros(n, dtype=torch.uint8, device="cuda:0") for n in sizes]
+    s = torch.cuda.Stream()
+    copies = [(d.data_ptr(), h.data_ptr(), n) for d, h, n in zip(dsts[:3], srcs, sizes[:3])]
+    copies.append((dsts[3].data_ptr(), pageable.ctypes.data, sizes[3]))
+    copy_host_planes(copies, host_copy, s)
+    s.synchronize()
+    for d, h in zip(dsts[:3], srcs):
+        assert torch.equal(d.cpu(), h)
+    assert np.array_equal(dsts[3].cpu().numpy(), pageable)
+    with pytest.raises(N.RgdnError):
+        copy_host_planes([(0, srcs[0].data_ptr(), 16)], host_copy, s)
+    with pytest.raises(N.RgdnError):
+        copy_host_planes([(dsts[0].data_ptr(), srcs[0].data_ptr(), 16)], 7, s)
