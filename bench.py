@@ -56,10 +56,11 @@ def parse():
     ap.add_argument("--e2e-steps", type=int, default=120)
     ap.add_argument("--e2e-host-copy", choices=["sm", "engine"], default="sm",
                     help="how the streamed end-to-end uploads reach the device (rgdn_copy_host_planes)")
-    ap.add_argument("--path", default="fused", choices=["fused", "plain", "tma", "pair"],
+    ap.add_argument("--path", default="fused", choices=["fused", "plain", "tma", "pair", "afvar"],
                     help="fused: the default kernels; plain: one kernel per reference dispatch; "
                          "tma: the default kernels with TMA-staged a-trous; pair: the default kernels with "
-                         "a-trous iterations 0 and 1 in one launch")
+                         "a-trous iterations 0 and 1 in one launch; afvar: the default kernels with "
+                         "anti-firefly and variance in one launch")
     ap.add_argument("--no-cpu-baseline", action="store_true", help="skip the CPU oracle (baseline and parity)")
     ap.add_argument("--parity-frames", type=int, default=8, help="frames run on GPU and oracle for the parity figures")
     ap.add_argument("--no-batched", action="store_true", help="skip the 32-stream batched measurement")
@@ -215,6 +216,9 @@ def stage_bytes(storage: str) -> dict:
         b[k] = b["temporal_accumulation"]
     b["anti_firefly_fast"] = b["anti_firefly"]
     b["variance_fast"] = b["variance_exact_geom"] = b["variance_estimation"]
+    # anti-firefly + variance in one launch: the variance's read of the clamped diffuse colour
+    # stays on chip
+    b["af_variance_fast"] = b["af_variance_exact"] = b["anti_firefly"] + b["variance_estimation"] - col3
     return b
 
 
@@ -875,6 +879,8 @@ def run_ours(args, dist: Dist):
             p.flags |= N.FLAG_TMA_STAGING
         elif args.path == "pair":
             p.flags |= N.FLAG_ATROUS_PAIR
+        elif args.path == "afvar":
+            p.flags |= N.FLAG_AF_VARIANCE_FUSED
         dev_bufs = {}
         for name, arr in bufs.items():
             t = torch.from_numpy(np.ascontiguousarray(arr).view(np.uint8).reshape(-1)).to(f"cuda:{dev}")

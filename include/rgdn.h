@@ -218,6 +218,11 @@ typedef struct rgdn_frame_params
 #define RGDN_FLAG_TMA_STAGING        0x8u /* a-trous taps staged in shared memory by the Tensor
                                              Memory Accelerator (widths divisible by 4, up to 5
                                              iterations); the same results as the default kernels */
+#define RGDN_FLAG_AF_VARIANCE_FUSED  0x20u /* anti-firefly and variance estimation in one launch: each
+                                             block keeps its tile's clamped diffuse colours (and
+                                             their one-pixel ring) in shared memory for the
+                                             variance's 3x3; the same results bit for bit (on
+                                             GB300 about 8 % slower than the two launches) */
 #define RGDN_FLAG_ATROUS_PAIR        0x40u /* a-trous iterations 0 and 1 in one launch (fusion depth 2,
                                              with 3 or more iterations): iteration 0 over the tile
                                              widened by 2 in shared memory, then iteration 1; the

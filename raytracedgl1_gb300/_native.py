@@ -51,6 +51,7 @@ STAGE_LUMINANCE_HISTOGRAM, STAGE_LUMINANCE_AVG = 6, 7
 
 FLAG_PLAIN, FLAG_SKIP_GRADIENTS, FLAG_EXACT_MATH, FLAG_TMA_STAGING, FLAG_STAGE_DEFAULT = 0x1, 0x2, 0x4, 0x8, 0x10
 FLAG_ATROUS_PAIR = 0x40
+FLAG_AF_VARIANCE_FUSED = 0x20
 FLAG_TEST_TMA_TIMEOUT = 0x80000000
 
 
@@ -271,7 +272,8 @@ KERNEL_NAMES.update({100: "atrous_fast", 101: "atrous_fast_hist", 102: "temporal
                      107: "atrous_exact", 108: "temporal_exact_geom", 109: "variance_exact_geom",
                      110: "temporal_fast_gp", 111: "temporal_exact_geom_gp", 112: "atrous_tma",
                      113: "atrous_tma_hist", 114: "prepare_final", 115: "bloom",
-                     117: "process_scattering", 122: "atrous_pair",
+                     117: "process_scattering", 122: "atrous_pair", 123: "af_variance_fast",
+                     124: "af_variance_exact",
                      200: "single_frame_group"})
 
 _lib = None

@@ -512,8 +512,12 @@ rgdn_status run_denoise_fused( rgdn_stream* s, uint32_t fi, const rgdn_frame_par
         for( int i = 0; i < 4; i++ )
             if( ( r = launch_default_stage( s, a, fi, p, RGDN_STAGE_GRADIENT_ATROUS, i, cs ) ) != RGDN_SUCCESS ) return r;
     }
-    for( int stage : { (int)RGDN_STAGE_TEMPORAL_ACCUMULATION, (int)RGDN_STAGE_ANTI_FIREFLY, (int)RGDN_STAGE_VARIANCE_ESTIMATION } )
-        if( ( r = launch_default_stage( s, a, fi, p, stage, 0, cs ) ) != RGDN_SUCCESS ) return r;
+    if( ( r = launch_default_stage( s, a, fi, p, RGDN_STAGE_TEMPORAL_ACCUMULATION, 0, cs ) ) != RGDN_SUCCESS ) return r;
+    if( p->flags & RGDN_FLAG_AF_VARIANCE_FUSED )
+        r = launch( s, a, ( p->flags & RGDN_FLAG_EXACT_MATH ) ? KF_AF_VARIANCE_EXACT : KF_AF_VARIANCE_FAST, 0, cs );
+    else if( ( r = launch_default_stage( s, a, fi, p, RGDN_STAGE_ANTI_FIREFLY, 0, cs ) ) == RGDN_SUCCESS )
+        r = launch_default_stage( s, a, fi, p, RGDN_STAGE_VARIANCE_ESTIMATION, 0, cs );
+    if( r != RGDN_SUCCESS ) return r;
     // iterations 0 and 1 in one launch when asked for, with the FAST shared-memory kernels and at
     // least one more iteration after them
     const bool pairOk = ( p->flags & RGDN_FLAG_ATROUS_PAIR ) && a.u.niter >= 3 &&

@@ -231,6 +231,8 @@ enum FusedKernel : int
     KF_BLOOM               = 115,  // the bloom pyramid and its application (timing label)
     KF_SCATTER_ACCUM       = 117,  // volume integration + screen-space accumulation (timing label)
     KF_ATROUS_PAIR01       = 122,  // a-trous iterations 0 and 1 in one launch (fusion depth 2)
+    KF_AF_VARIANCE_FAST    = 123,  // anti-firefly + variance in one launch, FAST variance weights
+    KF_AF_VARIANCE_EXACT   = 124,  // anti-firefly + variance in one launch, IEEE math
 };
 
 // Launches one stage for one frame. Returns the CUDA error of the launch.
@@ -314,7 +316,8 @@ cudaError_t launch_atrous_tma_bf16( const FrameArgs& a, int iter, bool hist, con
 int atrous_tma_smem( int storage, int iter );
 inline bool is_fast_kernel( int stage )
 {
-    return stage == KF_ATROUS_FAST || stage == KF_ATROUS_FAST_HIST || stage == KF_VARIANCE_FAST || stage == KF_ATROUS_PAIR01;
+    return stage == KF_ATROUS_FAST || stage == KF_ATROUS_FAST_HIST || stage == KF_VARIANCE_FAST || stage == KF_ATROUS_PAIR01 ||
+           stage == KF_AF_VARIANCE_FAST || stage == KF_AF_VARIANCE_EXACT;
 }
 
 // ------------------------------------------------------------------------------------------

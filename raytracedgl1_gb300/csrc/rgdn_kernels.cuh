@@ -1576,10 +1576,49 @@ __device__ __forceinline__ void af_column( const Uniform& u, const void* src, co
     }
 }
 
-template< int M > __device__ __forceinline__ void antifirefly_fast_tile( const FrameArgs& a, int bx, int by, AfShared< M >& sh )
+// One signal of the tile (every thread of the block takes part): rows r0 .. r0 + RP - 1 of
+// column x clamped into dst; keep (when non-null) receives the clamped texels of the rows
+// inside the image.
+template< int M >
+__device__ __forceinline__ void af_tile_signal( const Uniform& u, const void* src, void* dst, const int bx, const int x, const int r0,
+                                                AfShared< M >& sh, typename AfOps< M >::V* keep )
 {
     using O          = AfOps< M >;
     using V          = typename O::V;
+    constexpr int RP = AfShared< M >::RP;
+    const int     tx = threadIdx.x, ty = threadIdx.y;
+    V             c[ RP ];
+    AfPair< M >   v4[ RP ];
+    af_column< M >( u, src, x, r0, sh, ty * RP, tx + 2, c, v4 );
+    // the halo columns: local 0, 1 (x0 - 2, x0 - 1) and 34, 35 (x0 + 32, x0 + 33)
+    if( tx < 4 )
+    {
+        const int lc = tx < 2 ? tx : 32 + tx;
+        af_column< M >( u, src, bx * 32 - 2 + lc, r0, sh, ty * RP, lc, nullptr, nullptr );
+    }
+    __syncthreads();
+    if( x < u.W )
+    {
+#pragma unroll
+        for( int r = 0; r < RP; r++ )
+        {
+            if( r0 + r >= u.H ) break;
+            const AfPair< M >* row = &sh.v5[ ty * RP + r ][ tx ];
+            V mn = O::mn( O::mn( row[ 0 ].mn, row[ 1 ].mn ), O::mn( row[ 3 ].mn, row[ 4 ].mn ) );
+            V mx = O::mx( O::mx( row[ 0 ].mx, row[ 1 ].mx ), O::mx( row[ 3 ].mx, row[ 4 ].mx ) );
+            mn   = O::mn( mn, v4[ r ].mn );
+            mx   = O::mx( mx, v4[ r ].mx );
+            const V v = O::mn( O::mx( c[ r ], mn ), mx );
+            O::st( dst, ( r0 + r ) * u.W + x, v );
+            if( keep ) keep[ r ] = v;
+        }
+    }
+    __syncthreads();   // the next signal reuses the v5 rows
+}
+
+template< int M > __device__ __forceinline__ void antifirefly_fast_tile( const FrameArgs& a, int bx, int by, AfShared< M >& sh )
+{
+    using O          = AfOps< M >;
     using SH         = AfShared< M >;
     constexpr int RP = SH::RP;
     const Uniform& u = a.u;
@@ -1605,31 +1644,7 @@ template< int M > __device__ __forceinline__ void antifirefly_fast_tile( const F
     {
         const void* src = k == 0 ? a.diffTemp : k == 1 ? a.specAccum : a.indirAccum;
         void*       dst = k == 0 ? a.diffAccumColor : k == 1 ? a.specPing : a.indirPing;
-        V           c[ RP ];
-        AfPair< M > v4[ RP ];
-        af_column< M >( u, src, x, r0, sh, ty * RP, tx + 2, c, v4 );
-        // the halo columns: local 0, 1 (x0 - 2, x0 - 1) and 34, 35 (x0 + 32, x0 + 33)
-        if( tx < 4 )
-        {
-            const int lc = tx < 2 ? tx : 32 + tx;
-            af_column< M >( u, src, bx * 32 - 2 + lc, r0, sh, ty * RP, lc, nullptr, nullptr );
-        }
-        __syncthreads();
-        if( x < u.W )
-        {
-#pragma unroll
-            for( int r = 0; r < RP; r++ )
-            {
-                if( r0 + r >= u.H ) break;
-                const AfPair< M >* row = &sh.v5[ ty * RP + r ][ tx ];
-                V mn = O::mn( O::mn( row[ 0 ].mn, row[ 1 ].mn ), O::mn( row[ 3 ].mn, row[ 4 ].mn ) );
-                V mx = O::mx( O::mx( row[ 0 ].mx, row[ 1 ].mx ), O::mx( row[ 3 ].mx, row[ 4 ].mx ) );
-                mn   = O::mn( mn, v4[ r ].mn );
-                mx   = O::mx( mx, v4[ r ].mx );
-                O::st( dst, ( r0 + r ) * u.W + x, O::mn( O::mx( c[ r ], mn ), mx ) );
-            }
-        }
-        __syncthreads();   // the next signal reuses the v5 rows
+        af_tile_signal< M >( u, src, dst, bx, x, r0, sh, nullptr );
     }
 }
 
@@ -1660,6 +1675,147 @@ template< int M, bool FAST > __global__ void __launch_bounds__( 256, 8 ) k_varia
     pdl_launch_dependents();
     pdl_wait();
     variance_geo_tile< M, FAST >( a, blockIdx.x, blockIdx.y );
+}
+
+// ------------------------------------------------------------------------------------------
+// Anti-firefly and variance in one launch (RGDN_FLAG_AF_VARIANCE_FUSED). The block clamps its
+// 32 x 32 tile as antifirefly_fast_tile does and keeps the diffuse results, together with those
+// of the tile's one-pixel ring (each clamped here from its own 5 x 5 neighbourhood), in shared
+// memory as the texels DIFF_ACCUM_COLOR stores. The variance estimate of the tile's pixels then
+// reads its 3 x 3 colours there (CmSVGFEstimateVariance.comp:168-205) instead of from memory.
+// min and max are exact and the colours are the stored texels, so the results are those of
+// k_antifirefly_fast followed by k_variance_geo, bit for bit.
+// ------------------------------------------------------------------------------------------
+// the texel DIFF_ACCUM_COLOR stores for a clamped value of AfOps< M >, and its decoded colour
+// (Sto< M >::ld3 of that texel)
+template< int M > struct AfRaw;
+template<> struct AfRaw< MODE_REF >
+{
+    using R = uint32_t;
+    __device__ static R      raw( float3 v ) { return encode_e5( v.x, v.y, v.z ); }
+    __device__ static R      zero() { return 0u; }
+    __device__ static float3 col( R r ) { return e5( r ); }
+};
+template<> struct AfRaw< MODE_F32 >
+{
+    using R = float3;
+    __device__ static R      raw( float3 v ) { return v; }
+    __device__ static R      zero() { return f3( 0, 0, 0 ); }
+    __device__ static float3 col( R r ) { return r; }
+};
+template< bool BF > struct AfRaw16
+{
+    using R = uint2;
+    __device__ static R     raw( uint2 v ) { return v; }
+    __device__ static R     zero() { return make_uint2( 0u, 0u ); }
+    __device__ static float cv( uint32_t h ) { return BF ? b2f( (uint16_t)h ) : h2f( (uint16_t)h ); }
+    __device__ static float3 col( R r ) { return f3( cv( r.x & 0xFFFFu ), cv( r.x >> 16 ), cv( r.y & 0xFFFFu ) ); }
+};
+template<> struct AfRaw< MODE_F16 > : AfRaw16< false > {};
+template<> struct AfRaw< MODE_BF16 > : AfRaw16< true > {};
+
+template< int M > struct AfVarShared
+{
+    AfShared< M >           af;
+    typename AfRaw< M >::R d[ AfShared< M >::TH + 2 ][ 34 ];   // rows / columns -1 .. 32 of the tile
+};
+
+template< int M, bool FAST > __device__ __forceinline__ void af_variance_tile( const FrameArgs& a, int bx, int by, AfVarShared< M >& sh )
+{
+    using O          = AfOps< M >;
+    using V          = typename O::V;
+    using RW         = AfRaw< M >;
+    using S          = Sto< M >;
+    constexpr int RP = AfShared< M >::RP, TH = AfShared< M >::TH;
+    const Uniform& u = a.u;
+    const int      tx = threadIdx.x, ty = threadIdx.y;
+    const int      x  = bx * 32 + tx;
+    const int      r0 = by * TH + ty * RP;
+    V              keep[ RP ];
+    if( u.antiFirefly == 0 )
+    {
+        if( x < u.W )
+        {
+#pragma unroll
+            for( int r = 0; r < RP; r++ )
+            {
+                if( r0 + r >= u.H ) break;
+                const int i = ( r0 + r ) * u.W + x;
+                keep[ r ]   = O::ld( a.diffTemp, i );
+                O::st( a.diffAccumColor, i, keep[ r ] );
+                O::st( a.specPing, i, O::ld( a.specAccum, i ) );
+                O::st( a.indirPing, i, O::ld( a.indirAccum, i ) );
+            }
+        }
+    }
+    else
+    {
+        af_tile_signal< M >( u, a.specAccum, a.specPing, bx, x, r0, sh.af, nullptr );
+        af_tile_signal< M >( u, a.indirAccum, a.indirPing, bx, x, r0, sh.af, nullptr );
+        af_tile_signal< M >( u, a.diffTemp, a.diffAccumColor, bx, x, r0, sh.af, keep );
+    }
+#pragma unroll
+    for( int r = 0; r < RP; r++ )
+        sh.d[ ty * RP + r + 1 ][ tx + 1 ] = ( x < u.W && r0 + r < u.H ) ? RW::raw( keep[ r ] ) : RW::zero();
+    // the ring: rows -1 and TH (34 texels each), then columns -1 and 32 (TH texels each)
+    const int t = ty * 32 + tx;
+    if( t < 2 * 34 + 2 * TH )
+    {
+        int lx, ly;
+        if( t < 68 ) { lx = t % 34; ly = t < 34 ? 0 : TH + 1; }
+        else { lx = t < 68 + TH ? 0 : 33; ly = 1 + ( t - 68 ) % TH; }
+        const int gx = bx * 32 - 1 + lx, gy = by * TH - 1 + ly;
+        typename RW::R v = RW::zero();
+        if( gx >= 0 && gy >= 0 && gx < u.W && gy < u.H )
+        {
+            V c = O::ld( a.diffTemp, gy * u.W + gx );
+            if( u.antiFirefly != 0 )
+            {
+                // the 24-tap clamp of af_signal, zeros outside the image
+                V    mn = c, mx = c;
+                bool first = true;
+#pragma unroll
+                for( int oy = -2; oy <= 2; oy++ )
+                {
+#pragma unroll
+                    for( int ox = -2; ox <= 2; ox++ )
+                    {
+                        if( ox == 0 && oy == 0 ) continue;
+                        const int qx = gx + ox, qy = gy + oy;
+                        const V   q  = inside( u, qx, qy ) ? O::ld( a.diffTemp, qy * u.W + qx ) : O::zero();
+                        mn           = first ? q : O::mn( mn, q );
+                        mx           = first ? q : O::mx( mx, q );
+                        first        = false;
+                    }
+                }
+                c = O::mn( O::mx( c, mn ), mx );
+            }
+            v = RW::raw( c );
+        }
+        sh.d[ ly ][ lx ] = v;
+    }
+    __syncthreads();
+    if( x >= u.W ) return;
+#pragma unroll 1
+    for( int r = 0; r < RP; r++ )
+    {
+        const int y = r0 + r;
+        if( y >= u.H ) break;
+        const int i = y * u.W + x;
+        float3    c;
+        float     var;
+        variance_px< M, FAST, true >( a, x, y, i, [ & ]( int dx, int dy ) { return RW::col( sh.d[ ty * RP + r + 1 + dy ][ tx + 1 + dx ] ); }, c, var );
+        S::stcv( a.diffPing, a.varPing, (size_t)i, c, var );
+    }
+}
+
+template< int M, bool FAST >
+__global__ void __launch_bounds__( 256, ( M == MODE_F16 || M == MODE_BF16 ) ? 4 : 3 ) k_af_variance( const FrameArgs a )
+{
+    __shared__ AfVarShared< M > sh;
+    pdl_launch_dependents();
+    pdl_wait();
+    af_variance_tile< M, FAST >( a, blockIdx.x, blockIdx.y, sh );
 }
 
 // ==========================================================================================
@@ -3880,6 +4036,14 @@ template< int M > cudaError_t launch_fast_t( const FrameArgs& a, int stage, int 
         case KF_ATROUS_FAST_HIST: e = launch_atrous_fast< M, true >( a, iter, s ); break;
         case KF_VARIANCE_FAST: e = launch_pdl( dev::k_variance_geo< M, true >, grid, blk, 0, s, a ); break;
         case KF_ATROUS_PAIR01: e = launch_atrous_pair01< M >( a, s ); break;
+        case KF_AF_VARIANCE_FAST:
+        case KF_AF_VARIANCE_EXACT:
+        {
+            const dim3 g( grid.x, ( a.u.H + dev::AfShared< M >::TH - 1 ) / dev::AfShared< M >::TH );
+            e = stage == KF_AF_VARIANCE_FAST ? launch_pdl( dev::k_af_variance< M, true >, g, blk, 0, s, a )
+                                             : launch_pdl( dev::k_af_variance< M, false >, g, blk, 0, s, a );
+            break;
+        }
         default: return cudaErrorInvalidValue;
     }
     return e != cudaSuccess ? e : cudaGetLastError();

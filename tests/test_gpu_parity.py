@@ -395,6 +395,40 @@ def test_atrous_pair_equals_single(ctx, mode_name, mode, size):
     b.close()
 
 
+@pytest.mark.parametrize("mode_name,mode", MODES)
+@pytest.mark.parametrize("size", [(64, 36), (50, 23), (98, 65)])
+def test_af_variance_fused_equals_separate(ctx, mode_name, mode, size):
+    """Anti-firefly and variance in one launch (RGDN_FLAG_AF_VARIANCE_FUSED: the tile's clamped
+    diffuse colours and their one-pixel ring kept in shared memory for the variance's 3x3) give
+    the two kernels' planes bit for bit: partial tiles on the right and bottom edges, tiles whose
+    ring crosses the image edge, anti-firefly off on one frame, default and IEEE math."""
+    W, H = size
+    sc = Scene(W, H, seed=31, lightFlickerFrom=2.0)
+    a = Stream(ctx, W, H, mode)
+    b = Stream(ctx, W, H, mode)
+    for f in range(6):
+        fi = f & 1
+        bufs, p = sc.generate(f)
+        if f == 3:
+            p.antiFireflyEnabled = 0
+        if f >= 4:
+            p.flags |= N.FLAG_EXACT_MATH
+        upload_frame(a, None, bufs, fi)
+        upload_frame(b, None, bufs, fi)
+        pa = p.copy()
+        pa.flags |= N.FLAG_AF_VARIANCE_FUSED
+        for s, q in ((a, pa), (b, p)):
+            Denoiser(s).Denoise(fi, q)
+            Tonemapping(s).CalculateExposure(fi, q)
+        ga, gb = gpu_planes(a), gpu_planes(b)
+        for key in ga:
+            assert np.array_equal(ga[key][0], gb[key][0]), f"frame {f}: {key} differs"
+        ta, tb = a.tonemapping(), b.tonemapping()
+        assert np.array_equal(ta[0], tb[0]) and ta[1] == tb[1]
+    a.close()
+    b.close()
+
+
 def reshade_bind(s, o, sc, f):
     """Frame f's re-shading scene: device copies bound to GPU stream s, host arrays to the oracle
     o (None to skip). Returns the device buffers, which must outlive the frames that use them."""
