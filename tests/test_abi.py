@@ -107,3 +107,19 @@ def test_struct_layouts_match_the_header(tmp_path):
         if got != int(value):
             bad.append(f"{cname}.{field}: C {value}, ctypes {got}")
     assert not bad, bad
+
+
+def test_copy_host_planes_validates_before_any_copy():
+    """rgdn_copy_host_planes refuses a bad count, null arrays or pointers and an unknown copy
+    mode before it touches a device."""
+    lib = N.load()
+    vp3 = (C.c_void_p * 3)(1, 2, 3)
+    nb = (C.c_size_t * 3)(16, 16, 16)
+    bad = N.WRONG_FUNCTION_ARGUMENT
+    assert lib.rgdn_copy_host_planes(vp3, vp3, nb, 0, N.HOST_COPY_SM, None) == bad
+    assert lib.rgdn_copy_host_planes(vp3, vp3, nb, 16, N.HOST_COPY_SM, None) == bad
+    assert lib.rgdn_copy_host_planes(None, vp3, nb, 3, N.HOST_COPY_SM, None) == bad
+    assert lib.rgdn_copy_host_planes(vp3, vp3, None, 3, N.HOST_COPY_SM, None) == bad
+    assert lib.rgdn_copy_host_planes(vp3, vp3, nb, 3, 2, None) == bad
+    holes = (C.c_void_p * 3)(1, None, 3)
+    assert lib.rgdn_copy_host_planes(holes, vp3, nb, 3, N.HOST_COPY_ENGINE, None) == bad
