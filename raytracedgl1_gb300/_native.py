@@ -273,7 +273,7 @@ KERNEL_NAMES.update({100: "atrous_fast", 101: "atrous_fast_hist", 102: "temporal
                      110: "temporal_fast_gp", 111: "temporal_exact_geom_gp", 112: "atrous_tma",
                      113: "atrous_tma_hist", 114: "prepare_final", 115: "bloom",
                      117: "process_scattering", 122: "atrous_pair", 123: "af_variance_fast",
-                     124: "af_variance_exact",
+                     124: "af_variance_exact", 125: "temporal_fast", 126: "temporal_fast_gp",
                      200: "single_frame_group"})
 
 _lib = None

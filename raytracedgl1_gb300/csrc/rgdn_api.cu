@@ -446,7 +446,7 @@ rgdn_status run_denoise( rgdn_stream* s, uint32_t fi, const rgdn_frame_params* p
 // itself is then empty. The caller has filled `a` for frame slot `fi` and made the bin table
 // current.
 rgdn_status launch_default_stage( rgdn_stream* s, const FrameArgs& a, uint32_t fi, const rgdn_frame_params* p, int stage, int iter,
-                                  cudaStream_t cs, bool pairOk = false )
+                                  cudaStream_t cs, bool pairOk = false, bool afterGradients = false )
 {
     const bool exact = ( p->flags & RGDN_FLAG_EXACT_MATH ) != 0;
     switch( stage )
@@ -456,7 +456,10 @@ rgdn_status launch_default_stage( rgdn_stream* s, const FrameArgs& a, uint32_t f
         case RGDN_STAGE_TEMPORAL_ACCUMULATION:
         {
             const bool  gp = s->geomValid[ fi ^ 1u ];
-            const int   ta = exact ? ( gp ? KF_TEMPORAL_EXACT_GEOM_GP : KF_TEMPORAL_EXACT_GEOM ) : ( gp ? KF_TEMPORAL_FAST_GP : KF_TEMPORAL_FAST );
+            // directly after this frame's gradient chain, the FAST pass reads all but the
+            // gradient before it waits for the chain (k_temporal, EARLY)
+            const int   tf = afterGradients ? ( gp ? KF_TEMPORAL_FAST_GP_EARLY : KF_TEMPORAL_FAST_EARLY ) : ( gp ? KF_TEMPORAL_FAST_GP : KF_TEMPORAL_FAST );
+            const int   ta = exact ? ( gp ? KF_TEMPORAL_EXACT_GEOM_GP : KF_TEMPORAL_EXACT_GEOM ) : tf;
             rgdn_status r  = launch( s, a, ta, 0, cs );
             if( r == RGDN_SUCCESS ) s->geomValid[ fi ] = true;
             return r;
@@ -512,7 +515,8 @@ rgdn_status run_denoise_fused( rgdn_stream* s, uint32_t fi, const rgdn_frame_par
         for( int i = 0; i < 4; i++ )
             if( ( r = launch_default_stage( s, a, fi, p, RGDN_STAGE_GRADIENT_ATROUS, i, cs ) ) != RGDN_SUCCESS ) return r;
     }
-    if( ( r = launch_default_stage( s, a, fi, p, RGDN_STAGE_TEMPORAL_ACCUMULATION, 0, cs ) ) != RGDN_SUCCESS ) return r;
+    const bool afterGradients = !( p->flags & RGDN_FLAG_SKIP_GRADIENTS );
+    if( ( r = launch_default_stage( s, a, fi, p, RGDN_STAGE_TEMPORAL_ACCUMULATION, 0, cs, false, afterGradients ) ) != RGDN_SUCCESS ) return r;
     if( p->flags & RGDN_FLAG_AF_VARIANCE_FUSED )
         r = launch( s, a, ( p->flags & RGDN_FLAG_EXACT_MATH ) ? KF_AF_VARIANCE_EXACT : KF_AF_VARIANCE_FAST, 0, cs );
     else if( ( r = launch_default_stage( s, a, fi, p, RGDN_STAGE_ANTI_FIREFLY, 0, cs ) ) == RGDN_SUCCESS )

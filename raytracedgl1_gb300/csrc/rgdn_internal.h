@@ -233,6 +233,8 @@ enum FusedKernel : int
     KF_ATROUS_PAIR01       = 122,  // a-trous iterations 0 and 1 in one launch (fusion depth 2)
     KF_AF_VARIANCE_FAST    = 123,  // anti-firefly + variance in one launch, FAST variance weights
     KF_AF_VARIANCE_EXACT   = 124,  // anti-firefly + variance in one launch, IEEE math
+    KF_TEMPORAL_FAST_EARLY    = 125,  // KF_TEMPORAL_FAST reading all but the gradient before its wait
+    KF_TEMPORAL_FAST_GP_EARLY = 126,  // KF_TEMPORAL_FAST_GP likewise
 };
 
 // Launches one stage for one frame. Returns the CUDA error of the launch.

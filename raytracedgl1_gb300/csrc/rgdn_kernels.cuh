@@ -777,12 +777,15 @@ __device__ __forceinline__ void gradient_atrous_tile( const FrameArgs& a, int it
     gradient_atrous_px( a, gx, gy, iter, u8 );
 }
 
+// The first kernel of a frame lets its dependents launch only after its own wait: every kernel
+// enqueued before the frame has then completed, so the temporal pass that follows the gradient
+// chain may read the frame's inputs and history before its own wait (k_temporal, EARLY).
 template< int M > __global__ void __launch_bounds__( 256, 6 ) k_gradient_samples( const FrameArgs a, uint32_t* dst )
 {
     __shared__ float u8[ 256 ];
-    pdl_launch_dependents();
     fill_u8( u8, threadIdx.y * blockDim.x + threadIdx.x );
     pdl_wait();
+    pdl_launch_dependents();
     __syncthreads();
     gradient_samples_tile< M >( a, dst, blockIdx.x, blockIdx.y, u8 );
 }
@@ -849,7 +852,7 @@ constexpr bool kTemporalEarlySurfPos = false;
 constexpr bool kTemporalL2Prefetch = true;
 // the temporal pass reads this frame's unfiltered colours and view ray before its taps
 constexpr bool kTemporalEarlyInputs = true;
-template< int M, bool FAST, bool GEOM, bool GEOMPREV >
+template< int M, bool FAST, bool GEOM, bool GEOMPREV, bool EARLY = false >
 __device__ __forceinline__ void temporal_tile( const FrameArgs& a, int bx, int by, const float* u8 )
 {
     using S          = Sto< M >;
@@ -1007,6 +1010,8 @@ __device__ __forceinline__ void temporal_tile( const FrameArgs& a, int bx, int b
 
     // the filtered gradients (unorm8) and, FAST, their history-length decay from the table
     float aD = 0.0f, aI = 0.0f, aS = 0.0f, decD = 1.0f, decI = 1.0f;
+    // EARLY: the gradient chain that writes them is the only work this pass waits for
+    if( EARLY ) pdl_wait();
     if( !( u.flags & RGDN_FLAG_SKIP_GRADIENTS ) )
     {
         const int      gx = px / STRATA, gy = py / STRATA;
@@ -1258,16 +1263,20 @@ __device__ __forceinline__ void temporal_tile( const FrameArgs& a, int bx, int b
     S::st3( a.indirAccum, i, indirAccum );
 }
 
-// NT threads per block (32 x NT/32 tiles), MINB resident blocks per SM
-template< int M, bool FAST, bool GEOM, bool GEOMPREV, int NT = 256, int MINB = 1 >
+// NT threads per block (32 x NT/32 tiles), MINB resident blocks per SM. EARLY (only directly after
+// the gradient chain, whose first kernel releases its dependents after its own wait): everything
+// but the filtered gradient is read before this grid waits for the chain, so the reprojection
+// and the taps overlap the chain's last kernels. The gradient chain writes nothing else this
+// pass reads, and reads nothing this pass writes.
+template< int M, bool FAST, bool GEOM, bool GEOMPREV, int NT = 256, int MINB = 1, bool EARLY = false >
 __global__ void __launch_bounds__( NT, MINB ) k_temporal( const FrameArgs a )
 {
     __shared__ float u8[ 256 ];
     pdl_launch_dependents();
     for( int k = threadIdx.y * blockDim.x + threadIdx.x; k < 256; k += NT ) fill_u8( u8, k );
-    pdl_wait();
+    if( !EARLY ) pdl_wait();
     __syncthreads();
-    temporal_tile< M, FAST, GEOM, GEOMPREV >( a, blockIdx.x, blockIdx.y, u8 );
+    temporal_tile< M, FAST, GEOM, GEOMPREV, EARLY >( a, blockIdx.x, blockIdx.y, u8 );
 }
 
 // ==========================================================================================
@@ -3920,6 +3929,12 @@ template< int M > cudaError_t launch_stage_t( const FrameArgs& a, int stage, int
             break;
         case KF_TEMPORAL_FAST_GP:
             e = launch_pdl( dev::k_temporal< M, true, true, true, 128, 8 >, dim3( grid.x, ( a.u.H + 3 ) / 4 ), dim3( 32, 4 ), 0, s, a );
+            break;
+        case KF_TEMPORAL_FAST_EARLY:
+            e = launch_pdl( dev::k_temporal< M, true, true, false, 128, 8, true >, dim3( grid.x, ( a.u.H + 3 ) / 4 ), dim3( 32, 4 ), 0, s, a );
+            break;
+        case KF_TEMPORAL_FAST_GP_EARLY:
+            e = launch_pdl( dev::k_temporal< M, true, true, true, 128, 8, true >, dim3( grid.x, ( a.u.H + 3 ) / 4 ), dim3( 32, 4 ), 0, s, a );
             break;
         case KF_ANTI_FIREFLY_FAST:
             e = launch_pdl( dev::k_antifirefly_fast< M >, dim3( grid.x, ( a.u.H + dev::AfShared< M >::TH - 1 ) / dev::AfShared< M >::TH ), blk, 0, s, a );
