@@ -32,6 +32,10 @@ import subprocess
 import sys
 from concurrent.futures import ThreadPoolExecutor
 
+# where the reference checkout lies on the machine that builds the checker (the GPU machines have
+# none: there the committed vectors stand in for it)
+REFERENCE = "/root/reference"
+
 HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE = os.path.dirname(HERE)
 ROOT = os.path.dirname(ORACLE)
@@ -351,7 +355,7 @@ def build(ref: str, jobs: int | None = None) -> str:
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--reference", default="/root/reference")
+    ap.add_argument("--reference", default=REFERENCE)
     ap.add_argument("-j", type=int, default=None)
     a = ap.parse_args()
     if not os.path.isdir(os.path.join(a.reference, "Source", "Shaders")):

@@ -38,7 +38,7 @@ from raytracedgl1_gb300 import _native as N
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 GOLDEN = sorted(glob.glob(os.path.join(ROOT, "tests", "golden", "ref_shaders_*.npz")))
-REFERENCE = "/root/reference"
+from oracle.glsl_ref.build import REFERENCE  # noqa: E402
 
 
 def load_state(o, z, fi):
