@@ -58,6 +58,7 @@ SHADERS = {
     "RtGradients_main.comp": {},
     "CmCheckerboard.comp": {},
     "CmPrepareFinal.comp": {},
+    "CmBloomApply.comp": {"isSourcePing": [1]},
     "CmVolumetricProcess.comp": {},
     "CmScatterAccum.comp": {},
 }
@@ -71,6 +72,10 @@ VOLUME_COPY = ["invView", "invProjection", "volumeViewProj", "cameraPosition", "
 # uniform inputs of CmPrepareFinal.comp)
 FINAL_COPY = ["luminanceWhitePoint", "emissionMaxScreenColor", "bloomEmissionMultiplier", "bloomThreshold",
               "lightmapScreenCoverage"]
+
+# rgdn_bloom_params fields that ShGlobalUniform has under the same name (Bloom::Apply's uniform
+# inputs of CmBloomApply.comp; the lens-dirt term, which this path leaves out, is set to 0)
+BLOOM_COPY = ["bloomIntensity"]
 
 # RtGradients.rgen is a ray-generation shader: its main() selects each stratum's sample, tests it,
 # and turns the forward-projected luminance into the temporal gradient; only the forward
@@ -225,6 +230,12 @@ def rewrite(flat: str, spec: dict) -> tuple[str, dict]:
                 out.append(f"GLSL_SAMPLER({typ}, {name});")
             pos = close + 1 + mm.end()
             continue
+        # unsized array of samplers (the texture table): every element unbound
+        mm = re.match(r"\s*" + quals + r"uniform\s+" + quals + r"(sampler2D)\s+(\w+)\s*\[\s*\]\s*;", rest)
+        if mm:
+            out.append(f"static glsl::SamplerTable {mm.group(2)};")
+            pos = close + 1 + mm.end()
+            continue
         # uniform / buffer block
         mm = re.match(r"\s*" + quals + r"(uniform|buffer)\s+" + quals + r"(\w+)\s*\{", rest)
         if mm:
@@ -298,6 +309,10 @@ def translation_unit(shader: str, body: str, info: dict, tag: str) -> str:
         sets = [f"std::memcpy(&u.{f}, &p->{f}, sizeof(p->{f}));" for f in FINAL_COPY]
         lines.append(f"void ref_{tag}_set_final(const rgdn_final_params* p) {{ "
                      f"auto& u = {ns}::globalUniform; {' '.join(sets)} }}")
+        if re.search(r"\blensDirtIntensity\b", body):
+            sets = [f"std::memcpy(&u.{f}, &p->{f}, sizeof(p->{f}));" for f in BLOOM_COPY]
+            lines.append(f"void ref_{tag}_set_bloom(const rgdn_bloom_params* p) {{ "
+                         f"auto& u = {ns}::globalUniform; {' '.join(sets)} u.lensDirtIntensity = 0.0f; }}")
         sets = [f"std::memcpy(&u.{f}, &p->{f}, sizeof(p->{f}));" for f in VOLUME_COPY]
         lines.append(f"void ref_{tag}_set_volumetric(const rgdn_volumetric_params* p) {{ "
                      f"auto& u = {ns}::globalUniform; {' '.join(sets)} }}")

@@ -242,6 +242,24 @@ GLSL_BINOP( ^ )
 GLSL_BINOP( << )
 GLSL_BINOP( >> )
 #undef GLSL_BINOP
+// a float vector with an integer vector: the integer one converts to float (GLSL's implicit
+// conversion)
+#define GLSL_MIXOP( OP )                                                                                \
+    template< int N, class I, typename std::enable_if< std::is_integral< I >::value, int >::type = 0 >   \
+    vec< float, N > operator OP( const vec< float, N >& a, const vec< I, N >& b )                         \
+    {                                                                                                     \
+        return a OP vec< float, N >( b );                                                                 \
+    }                                                                                                     \
+    template< int N, class I, typename std::enable_if< std::is_integral< I >::value, int >::type = 0 >   \
+    vec< float, N > operator OP( const vec< I, N >& a, const vec< float, N >& b )                         \
+    {                                                                                                     \
+        return vec< float, N >( a ) OP b;                                                                 \
+    }
+GLSL_MIXOP( + )
+GLSL_MIXOP( - )
+GLSL_MIXOP( * )
+GLSL_MIXOP( / )
+#undef GLSL_MIXOP
 
 template< class T, int N > vec< T, N > operator-( const vec< T, N >& a )
 {
@@ -663,6 +681,14 @@ struct image3D : ImageBase { using ImageBase::ImageBase; };
 struct sampler3D : SamplerBase { using SamplerBase::SamplerBase; };
 // declared for the blue-noise array of Random.h, which the shaders run here do not read
 struct texture2DArray : SamplerBase { using SamplerBase::SamplerBase; };
+// the texture table (globalTextures[]): every element an unbound sampler (zero texels, size 0)
+struct SamplerTable
+{
+    sampler2D none{ "" };
+    sampler2D& operator[]( uint ) { return none; }
+    sampler2D& operator[]( int ) { return none; }
+};
+template< class T > inline T nonuniformEXT( T i ) { return i; }
 
 // texel load / store in the plane's format (outside the plane: zero on load, dropped on store)
 vec4  load_f( Plane& p, ivec2 pix );
@@ -682,6 +708,8 @@ inline uvec4 texelFetch( usampler2D& s, const ivec2& pix, int ) { return load_u(
 // the weight x - floor(x), mix(x, y, a) = x (1 - a) + y a, rows first. Only LOD 0 is read.
 vec4 bilinear( Plane& p, const vec2& uv );
 inline vec4 textureLod( sampler2D& s, const vec2& uv, float ) { return bilinear( s.plane(), uv ); }
+// the images here have one mip level, so an explicit gradient selects LOD 0 as well
+inline vec4 textureGrad( sampler2D& s, const vec2& uv, const vec2&, const vec2& ) { return bilinear( s.plane(), uv ); }
 // 3-D images: texel (x, y, z) of a w x h x d image; outside it, zero on load and dropped on store
 vec4 load_f3( Plane& p, ivec3 c );
 void store_f3( Plane& p, ivec3 c, const vec4& v );

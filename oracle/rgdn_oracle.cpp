@@ -16,8 +16,8 @@
 //  the histogram and the adaptation, the bloom pyramid, the volumetric scattering
 //  (CmVolumetricProcess + CmScatterAccum) and the final composition (CmCheckerboard +
 //  CmPrepareFinal, the LPM control block from the reference's own CPU-side LpmSetup)
-//  (committed vectors in tests/golden, and live where the reference checkout is present).
-//  The re-shading of the analytic scene and the bloom's apply
+//  and the bloom's application (committed vectors in tests/golden, and live where the
+//  reference checkout is present). The re-shading of the analytic scene
 //  stay pinned only by the codecs' known-answer tests from the public specs they implement
 //  (IEEE-754 binary16/bfloat16, EXT_texture_shared_exponent, the Vulkan B10G11R11
 //  unsigned-float layout) and the closed-form known-answer tests in tests/.

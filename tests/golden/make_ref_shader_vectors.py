@@ -17,7 +17,7 @@ Usage (where the reference checkout and a C++ compiler are present):
 
 It also writes, at the first size, tests/golden/ref_bloom_<W>x<H>.npz: bloom_input() and every
 bloom image after the reference's pyramid (Bloom::Prepare's eight downsampling and eight upsampling
-steps); and tests/golden/ref_final_<W>x<H>.npz: two final_case() states (the inputs FINAL_INPUTS,
+steps), and FINAL after Bloom::Apply over a second bloom_input() as the source image; and tests/golden/ref_final_<W>x<H>.npz: two final_case() states (the inputs FINAL_INPUTS,
 the frame and final parameters, the adapted average luminance) and FINAL and BLOOM_INPUT after the
 reference's CmCheckerboard + CmPrepareFinal.
 """
@@ -100,8 +100,14 @@ def bloom_plan(W, H):
     return plan
 
 
-def run_reference_bloom(W, H, inp: np.ndarray) -> dict:
-    """The reference's bloom pyramid over `inp`: {(fb, slot): plane} of every bloom image."""
+BLOOM_INTENSITY = 0.7
+
+
+def run_reference_bloom(W, H, inp: np.ndarray, final: np.ndarray) -> dict:
+    """The reference's bloom over `inp`: the pyramid (Bloom::Prepare), then Bloom::Apply
+    (Source/Bloom.cpp:194-240, CmBloomApply with the effect source UpscaledPing = `final` and the
+    target UpscaledPong, intensity BLOOM_INTENSITY, no lens dirt). Returns {(fb, slot): plane} of
+    every bloom image and ("FINAL", 0), the applied target."""
     o = oracle.OracleStream(W, H, oracle.MODE_REF)
     o.load("BLOOM_INPUT", 0, inp)
     ref = runner.RefRun(W, H)
@@ -109,7 +115,21 @@ def run_reference_bloom(W, H, inp: np.ndarray) -> dict:
     p = N.FrameParams()
     for tag, groups in bloom_plan(W, H):
         ref.run(tag, groups, p)
-    return {k: a for k, a in ref.arrays.items() if k[0].startswith("BLOOM")}
+    out = {k: a for k, a in ref.arrays.items() if k[0].startswith("BLOOM")}
+    lib = ref.lib
+    src = np.ascontiguousarray(final, dtype=np.uint32).copy()
+    dst = np.zeros((H, W), dtype=np.uint32)
+    lib.ref_bind(b"framebufUpscaledPing", src.ctypes.data, W, H)
+    lib.ref_bind(b"framebufUpscaledPong", dst.ctypes.data, W, H)
+    bp = N.BloomParams()
+    bp.bloomIntensity = BLOOM_INTENSITY
+    lib.ref_CmBloomApply_1_set_uniform(C.byref(p), C.c_float(W), C.c_float(H))
+    lib.ref_CmBloomApply_1_set_bloom(C.byref(bp))
+    local = (C.c_uint * 3)()
+    lib.ref_CmBloomApply_1_local(local)
+    lib.ref_CmBloomApply_1_dispatch(-(-W // local[0]), -(-H // local[1]))
+    out[("FINAL", 0)] = dst
+    return out
 
 
 def final_case(W, H, seed=SEED, saturation=(0.0, 0.0, 0.0), crosstalk=(1.0, 1.0, 1.0), coverage=0.25,
@@ -235,7 +255,7 @@ def main(argv):
     # the bloom pyramid (CmBloomDownsample / CmBloomUpsample) at the first size
     W, H = sizes[0]
     out = {"meta": np.array([W, H], dtype=np.int64)}
-    for (fb, slot), a in run_reference_bloom(W, H, bloom_input(W, H)).items():
+    for (fb, slot), a in run_reference_bloom(W, H, bloom_input(W, H), bloom_input(W, H, seed=SEED + 1)).items():
         out[f"{fb}/{slot}"] = a
     path = os.path.join(here, f"ref_bloom_{W}x{H}.npz")
     np.savez_compressed(path, **out)

@@ -18,7 +18,9 @@ the oracle's bit for bit after every stage.
 - test_a_planted_mistake_is_caught: an input changed on the oracle's side only (a moments texel
   before the variance pass; the forward-projected luminance before the gradient samples) must
   show up as a difference at that stage.
-- test_oracle_bloom_*: the bloom pyramid (every bloom image), from the committed vectors and live.
+- test_oracle_bloom_*: the bloom pyramid (every bloom image) and its application onto FINAL
+  (CmBloomApply through the effect framework's UpscaledPing/UpscaledPong images), from the
+  committed vectors and live.
 - test_oracle_scattering_*: Volumetric::ProcessScattering (CmVolumetricProcess + CmScatterAccum)
   in the three volume modes, the froxel volume bound as a 3-D image.
 - test_oracle_final_*: the final composition, CmCheckerboard + CmPrepareFinal (the LPM control
@@ -152,12 +154,15 @@ def test_a_planted_mistake_is_caught(plant, first):
 GOLDEN_BLOOM = sorted(glob.glob(os.path.join(ROOT, "tests", "golden", "ref_bloom_*.npz")))
 
 
-def oracle_bloom(W, H, inp):
-    """The oracle's bloom over `inp`: {(fb, slot): plane} of every bloom image."""
+def oracle_bloom(W, H, inp, final):
+    """The oracle's bloom over `inp`, applied onto `final`: {(fb, slot): plane} of every bloom
+    image and FINAL."""
+    from tests.golden.make_ref_shader_vectors import BLOOM_INTENSITY
     o = oracle.OracleStream(W, H, oracle.MODE_REF)
     o.load("BLOOM_INPUT", 0, inp)
-    o.bloom(0, 1.0)
-    return {k: a for k, a in runner.oracle_planes(o, 0).items() if k[0].startswith("BLOOM")}
+    o.load("FINAL", 0, final)
+    o.bloom(0, BLOOM_INTENSITY)
+    return {k: a for k, a in runner.oracle_planes(o, 0).items() if k[0].startswith("BLOOM") or k[0] == "FINAL"}
 
 
 @pytest.mark.parametrize("path", GOLDEN_BLOOM, ids=[os.path.basename(p) for p in GOLDEN_BLOOM])
@@ -169,8 +174,9 @@ def test_oracle_bloom_matches_reference_vectors(path):
         if key != "meta":
             fb, slot = key.split("/")
             expected[(fb, int(slot))] = z[key]
-    assert len(expected) == 10
-    got = oracle_bloom(W, H, expected[("BLOOM_INPUT", 0)])
+    assert len(expected) == 11
+    from tests.golden.make_ref_shader_vectors import SEED, bloom_input
+    got = oracle_bloom(W, H, expected[("BLOOM_INPUT", 0)], bloom_input(W, H, seed=SEED + 1))
     assert runner.differing(expected, got) == []
 
 
@@ -179,15 +185,16 @@ def test_oracle_bloom_matches_reference_shaders_live(size):
     why = _live_ready()
     if why:
         pytest.skip(why)
-    from tests.golden.make_ref_shader_vectors import bloom_input, run_reference_bloom
+    from tests.golden.make_ref_shader_vectors import SEED, bloom_input, run_reference_bloom
     W, H = size
-    inp = bloom_input(W, H)
-    ref = run_reference_bloom(W, H, inp)
+    inp, fin = bloom_input(W, H), bloom_input(W, H, seed=SEED + 1)
+    ref = run_reference_bloom(W, H, inp, fin)
     # the reference writes no texel of a mip whose uv passes 1 (CmBloomDownsample.comp:123), so
     # the smallest mips of a small frame stay empty; the input and the first mips are not
-    assert len(ref) == 10
-    assert all(np.count_nonzero(ref[(fb, 0)]) for fb in ("BLOOM_INPUT", "BLOOM_MIP1", "BLOOM_MIP2", "BLOOM_RESULT"))
-    assert runner.differing(ref, oracle_bloom(W, H, inp)) == []
+    assert len(ref) == 11
+    assert all(np.count_nonzero(ref[(fb, 0)]) for fb in ("BLOOM_INPUT", "BLOOM_MIP1", "BLOOM_MIP2", "BLOOM_RESULT", "FINAL"))
+    assert not np.array_equal(ref[("FINAL", 0)], fin)
+    assert runner.differing(ref, oracle_bloom(W, H, inp, fin)) == []
 
 
 GOLDEN_FINAL = sorted(glob.glob(os.path.join(ROOT, "tests", "golden", "ref_final_*.npz")))
