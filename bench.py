@@ -183,6 +183,12 @@ class ClockSampler:
 # algorithmic bytes per pixel of each kernel (each distinct texel read once, each output
 # written once), from the framebuffer formats of the storage mode
 # ------------------------------------------------------------------------------------------
+def quantile(sorted_values: list, q: float):
+    """The nearest-rank q-quantile (0 < q <= 1) of an ascending list."""
+    import math
+    return sorted_values[min(len(sorted_values) - 1, max(0, math.ceil(q * len(sorted_values)) - 1))]
+
+
 def stage_bytes(storage: str) -> dict:
     col3 = {"ref": 4, "fp32": 16, "fp16": 8, "bf16": 8}[storage]
     cv = {"ref": 8, "fp32": 16, "fp16": 12, "bf16": 12}[storage]        # colour + variance
@@ -442,7 +448,7 @@ def run_reference(args, dist: Dist):
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": round(1e3 * total / len(times), 3), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "p50_ms": round(1e3 * times[len(times) // 2], 3), "p99_ms": round(1e3 * times[int(0.99 * (len(times) - 1))], 3),
+        "p50_ms": round(1e3 * quantile(times, 0.5), 3), "p99_ms": round(1e3 * quantile(times, 0.99), 3),
         "config": dict(config_dict(args), band=f"{W}x{H}",
                        sample=f"each step times one {W}x{H} frame (a band of the {args.width}x{args.height} "
                               f"workload's width, from the same generator and stages, so the same per-pixel "
@@ -636,7 +642,7 @@ def run_batched(args, dist: Dist, dev: int, cs) -> dict:
         "mpix_per_step": round(px / 1e6, 3),
         "value": round(px * args.batch_steps * dist.world / (t_b / 1e3) / 1e6, 1), "unit": "Mpix/s",
         "ms_per_step": round(t_b / args.batch_steps, 3),
-        "p50_ms": round(per_b[len(per_b) // 2], 3), "p99_ms": round(per_b[int(0.99 * (len(per_b) - 1))], 3),
+        "p50_ms": round(quantile(per_b, 0.5), 3), "p99_ms": round(quantile(per_b, 0.99), 3),
         "steps": args.batch_steps, "gpu_launches": int(launches),
         "one_stream_per_call_mpix_s": round(px * steps_cmp * dist.world / (t_s / 1e3) / 1e6, 1),
         "plain_path_mpix_s": round(px * steps_cmp * dist.world / (t_p / 1e3) / 1e6, 1),
@@ -758,7 +764,7 @@ def run_serving(args, dist: Dist, dev: int) -> dict:
 
         def pct(v, q):
             v = sorted(v)
-            return round(v[int(q * (len(v) - 1))], 3) if v else None
+            return round(quantile(v, q), 3) if v else None
         offered = sum(res[i][0] * res[i][1] for _, i in arrivals)
         sv.close()
         return {"per_stream_hz": hz, "steps_in_flight": inflight, "seconds": round(elapsed, 3), "requests": len(arrivals),
@@ -768,7 +774,7 @@ def run_serving(args, dist: Dist, dev: int) -> dict:
                 "p50_ms": round(st["p50Ms"], 3), "p99_ms": round(st["p99Ms"], 3), "max_ms": round(st["maxMs"], 3),
                 "p99_all_requests_ms": (round(st["p99AllMs"], 3) if st["p99AllMs"] != float("inf") else "inf"),
                 "drop_rate": round(st["dropRate"], 4),
-                "p99_ms_1080p": round(lat_1080[int(0.99 * (len(lat_1080) - 1))], 3) if lat_1080 else None,
+                "p99_ms_1080p": round(pct(lat_1080, 0.99), 3) if lat_1080 else None,
                 "queue_p50_ms": pct(queue, 0.5), "queue_p99_ms": pct(queue, 0.99),
                 "service_p50_ms": pct(service, 0.5), "service_p99_ms": pct(service, 0.99),
                 "feeder_late_p99_ms": pct(late, 0.99),
@@ -1147,7 +1153,7 @@ def run_ours(args, dist: Dist):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(total_ms_max / args.steps, 4),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32", "data": "synthetic (seeded analytic scene; see bench.py docstring)",
-        "p50_ms": round(step_ms[len(step_ms) // 2], 4), "p99_ms": round(step_ms[int(0.99 * (len(step_ms) - 1))], 4),
+        "p50_ms": round(quantile(step_ms, 0.5), 4), "p99_ms": round(quantile(step_ms, 0.99), 4),
         "config": config_dict(args),
         "gpu_launches": int(launches),
         "roofline": {"bound": "hbm", "kernel": top["kernel"], "achieved": round(top["gbs"], 1),
@@ -1179,8 +1185,8 @@ def run_ours(args, dist: Dist):
                 ("engine_mpix_s" if hc_main == N.HOST_COPY_SM else "sm_mpix_s"):
                     round(W * H * args.e2e_steps * dist.world / e2e_other_s / 1e6, 2),
                 "synchronous_mpix_s": round(W * H * args.e2e_steps * dist.world / e2e_sync_s / 1e6, 2),
-                "synchronous_p50_ms": round(1e3 * lat[len(lat) // 2], 3),
-                "synchronous_p99_ms": round(1e3 * lat[int(0.99 * (len(lat) - 1))], 3),
+                "synchronous_p50_ms": round(1e3 * quantile(lat, 0.5), 3),
+                "synchronous_p99_ms": round(1e3 * quantile(lat, 0.99), 3),
                 "host_link": link, "link_bound_mpix_s": round(link_bound, 1),
                 "link_frac": round(e2e_value / link_bound, 4)},
         "clocks": clk,
