@@ -118,7 +118,9 @@ def run_both(W, H, plant=None):
     return bad
 
 
-@pytest.mark.parametrize("size", [(64, 36), (98, 33), (100, 34), (130, 9), (250, 151), (16, 6)])
+# partial workgroups and odd gradient images, and the benchmark's 640x360 and 1920x1080 frames
+# (the last about a minute)
+@pytest.mark.parametrize("size", [(64, 36), (98, 33), (100, 34), (130, 9), (250, 151), (16, 6), (640, 360), (1920, 1080)])
 def test_oracle_matches_reference_shaders_live(size):
     why = _live_ready()
     if why:
