@@ -429,6 +429,54 @@ def test_af_variance_fused_equals_separate(ctx, mode_name, mode, size):
     b.close()
 
 
+def test_inputs_written_by_a_kernel_just_before_denoise(ctx):
+    """The frame's G-buffer written by a kernel enqueued on the same CUDA stream right before
+    rgdn_denoise (a renderer's last pass) is what the frame reads: the temporal pass reads its
+    inputs before it waits for the gradient chain, which is safe only because the chain's first
+    kernel releases its dependents after every earlier kernel has completed. At 1920x1080 the
+    copy of the 164 MB G-buffer takes long enough that an early read would see stale planes; the
+    planes must equal a stream whose inputs were copied and synchronised before each frame."""
+    torch = pytest.importorskip("torch")
+    W, H = 1920, 1080
+    sc = Scene(W, H, seed=37, lightFlickerFrom=2.0)
+    a = Stream(ctx, W, H, N.STORAGE_FP16)
+    b = Stream(ctx, W, H, N.STORAGE_FP16)
+    cs = torch.cuda.Stream()
+    frames = []
+    for f in range(4):
+        bufs, p = sc.generate(f)
+        frames.append(({k: torch.from_numpy(np.ascontiguousarray(v).view(np.uint8).reshape(-1)).cuda() for k, v in bufs.items()}, p))
+    # each stream reads two device G-buffer sets, bound for the frame's slot before each frame (a
+    # plane without a previous-frame slot has one binding, so it follows the current set): a's set
+    # refilled on cs right before its frame, b's refilled and synchronised
+    sets = {s: [{k: torch.zeros_like(t) for k, t in frames[0][0].items()} for _ in range(2)] for s in ("a", "b")}
+    zero = torch.zeros(1, dtype=torch.uint8, device="cuda:0")
+    torch.cuda.synchronize()
+    for f, (bufs, p) in enumerate(frames):
+        fi = f & 1
+        for name, st in (("a", a), ("b", b)):
+            for k, t in sets[name][fi].items():
+                st.bind(k, fi, t.data_ptr())
+        with torch.cuda.stream(cs):
+            for k, t in bufs.items():
+                # the producer's pass: a kernel (not a copy-engine copy), not synchronised
+                torch.bitwise_or(t, zero, out=sets["a"][fi][k])
+        Denoiser(a).Denoise(fi, p, cs)
+        Tonemapping(a).CalculateExposure(fi, p, cs)
+        for k, t in bufs.items():
+            sets["b"][fi][k].copy_(t)
+        torch.cuda.synchronize()
+        Denoiser(b).Denoise(fi, p)
+        Tonemapping(b).CalculateExposure(fi, p)
+        torch.cuda.synchronize()
+        for name in ("PRE_FINAL", "DIFF_TEMPORARY", "ACCUM_HISTORY_LENGTH", "DIFF_COLOR_HISTORY", "SPEC_ACCUM_COLOR"):
+            assert np.array_equal(a.download(name, fi), b.download(name, fi)), f"frame {f}: {name} differs"
+        ta, tb = a.tonemapping(), b.tonemapping()
+        assert np.array_equal(ta[0], tb[0]) and ta[1] == tb[1]
+    a.close()
+    b.close()
+
+
 def reshade_bind(s, o, sc, f):
     """Frame f's re-shading scene: device copies bound to GPU stream s, host arrays to the oracle
     o (None to skip). Returns the device buffers, which must outlive the frames that use them."""
