@@ -301,7 +301,7 @@ rgdn_status rgdn_stream_get_framebuffer( rgdn_stream* stream, uint32_t fb, uint3
  * RGDN_FB_SCREEN_EMIS_RT, RGDN_FB_SCATTERING, RGDN_FB_DEPTH_NDC, RGDN_FB_SCATTER_VOLUME) of slot frameIndex at caller-owned device memory (dense rows, 16-byte aligned). An image
  * without a previous-frame slot (no _Prev in the reference) has one binding whatever frameIndex
  * says, so a caller that alternates buffers binds it again before each frame. This lets a renderer
- * that already holds its G-buffer in HBM hands it over without a copy — the role of the
+ * that already holds its G-buffer in HBM hand it over without a copy — the role of the
  * reference's shared Framebuffers images (PathTracer writes, Denoiser reads). NULL restores
  * the stream's own plane. The memory must stay valid while work using it is in flight. */
 rgdn_status rgdn_stream_bind_framebuffer( rgdn_stream* stream, uint32_t fb, uint32_t frameIndex, void* devicePtr );
