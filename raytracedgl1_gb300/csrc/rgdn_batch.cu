@@ -29,7 +29,7 @@
 // single-frame ones) and their large frames ran 5-13 % slower per pixel. A step with such a
 // group is launched directly rather than replayed from a graph, since that group's parameters
 // change every step; at a frame of a million pixels or more the launches stay ahead of the GPU.
-// One-frame groups alternate between the caller's stream and a second lane (enqueue_step).
+// One-frame groups take turns on the caller's stream and kSideLanes more (enqueue_step).
 //
 // Autotuning: the first 15 steps of a storage mode time every candidate tile shape (and, for
 // the a-trous kernel, the register budget and the fusion depth) per launch on the frames being
@@ -236,12 +236,16 @@ int ceil_div( int a, int b ) { return ( a + b - 1 ) / b; }
 
 }  // namespace
 
+// one-frame groups run on the caller's stream and kSideLanes more: on GB300 the 32-stream mix
+// ran 4152 Mpix/s with one side lane, 4199-4203 with two and 4204-4207 with three
+constexpr int kSideLanes = 2;
+
 struct BatchExec
 {
     int                        device = 0, sms = 0;
     cudaStream_t               capture = nullptr;   // private stream the graphs are captured on
-    cudaStream_t               side    = nullptr;   // second lane of one-frame groups
-    cudaEvent_t                fork = nullptr, join = nullptr;
+    cudaStream_t               side[ kSideLanes ] = {};   // lanes of one-frame groups beside the caller's
+    cudaEvent_t                fork = nullptr, join[ kSideLanes ] = {};
     cudaGraphExec_t            exec[ BATCH_SLOTS ] = {};
     GraphKey                   key[ BATCH_SLOTS ];
     Config                     cfg[ 4 ];
@@ -285,9 +289,12 @@ BatchExec* create_exec( int device )
     ex->device = device;
     bool ok    = cudaDeviceGetAttribute( &ex->sms, cudaDevAttrMultiProcessorCount, device ) == cudaSuccess && ex->sms > 0;
     ok         = ok && cudaStreamCreateWithFlags( &ex->capture, cudaStreamNonBlocking ) == cudaSuccess;
-    ok         = ok && cudaStreamCreateWithFlags( &ex->side, cudaStreamNonBlocking ) == cudaSuccess;
+    for( int l = 0; l < kSideLanes; l++ )
+    {
+        ok = ok && cudaStreamCreateWithFlags( &ex->side[ l ], cudaStreamNonBlocking ) == cudaSuccess;
+        ok = ok && cudaEventCreateWithFlags( &ex->join[ l ], cudaEventDisableTiming ) == cudaSuccess;
+    }
     ok         = ok && cudaEventCreateWithFlags( &ex->fork, cudaEventDisableTiming ) == cudaSuccess;
-    ok         = ok && cudaEventCreateWithFlags( &ex->join, cudaEventDisableTiming ) == cudaSuccess;
     for( int s = 0; s < 4; s++ )
     {
         for( int k = 0; k < BS_COUNT; k++ )
@@ -331,9 +338,12 @@ void batch_exec_free( BatchExec* ex )
     }
     for( cudaEvent_t e : ex->eventPool ) cudaEventDestroy( e );
     if( ex->capture ) cudaStreamDestroy( ex->capture );
-    if( ex->side ) cudaStreamDestroy( ex->side );
+    for( int l = 0; l < kSideLanes; l++ )
+    {
+        if( ex->side[ l ] ) cudaStreamDestroy( ex->side[ l ] );
+        if( ex->join[ l ] ) cudaEventDestroy( ex->join[ l ] );
+    }
     if( ex->fork ) cudaEventDestroy( ex->fork );
-    if( ex->join ) cudaEventDestroy( ex->join );
     delete ex;
 }
 
@@ -356,18 +366,21 @@ rgdn_status enqueue_step( rgdn_context* c, BatchExec& ex, DeviceSlots& ds, int s
     const bool tuning = !capturing && !tu.settled && tu.phase == 0;
     const bool user   = !capturing && ex.timing;
 
-    // One-frame groups run on two lanes, cs and a side stream, alternately: the frames are of
-    // different camera streams, so one frame's kernels fill the SMs the other's leave idle at its
-    // launch boundaries and wave tails. The side lane starts after everything before the step on
-    // cs and cs waits for it at the end (timed steps keep one lane, so each event brackets one frame).
+    // One-frame groups take turns on up to 1 + kSideLanes lanes, cs and side streams: the frames
+    // are of different camera streams, so one frame's kernels fill the SMs the others leave idle
+    // at their launch boundaries and wave tails. The side lanes start after everything before the
+    // step on cs and cs waits for them at the end (timed steps keep one lane, so each event
+    // brackets one frame).
     int  singles = 0;
     bool forked  = false;
     for( int gi = 0; gi < key.ng; gi++ ) singles += key.g[ gi ].single;
     const bool twoLanes = singles > 1 && !user && !capturing;
+    const int lanes = twoLanes ? std::min( singles, 1 + kSideLanes ) : 1;
     if( twoLanes )
     {
-        if( cudaEventRecord( ex.fork, cs ) != cudaSuccess || cudaStreamWaitEvent( ex.side, ex.fork, 0 ) != cudaSuccess )
-            return RGDN_DEVICE_ERROR;
+        if( cudaEventRecord( ex.fork, cs ) != cudaSuccess ) return RGDN_DEVICE_ERROR;
+        for( int l = 0; l + 1 < lanes; l++ )
+            if( cudaStreamWaitEvent( ex.side[ l ], ex.fork, 0 ) != cudaSuccess ) return RGDN_DEVICE_ERROR;
         forked = true;
     }
     int nthSingle = 0;
@@ -378,7 +391,8 @@ rgdn_status enqueue_step( rgdn_context* c, BatchExec& ex, DeviceSlots& ds, int s
         {
             // one frame: the single-frame kernels, with its arguments as kernel parameters
             const rgdn_job&    jb   = jobs[ gk.j0 ];
-            const cudaStream_t lane = ( twoLanes && ( nthSingle++ & 1 ) ) ? ex.side : cs;
+            const int          li   = twoLanes ? nthSingle++ % lanes : 0;
+            const cudaStream_t lane = li ? ex.side[ li - 1 ] : cs;
             cudaEvent_t        ua = nullptr, ub = nullptr;
             if( user )
             {
@@ -464,8 +478,10 @@ rgdn_status enqueue_step( rgdn_context* c, BatchExec& ex, DeviceSlots& ds, int s
         }
         if( ( r = run( -1, RGDN_STAGE_LUMINANCE_AVG, 0, 0, 0, 0 ) ) != RGDN_SUCCESS ) return r;
     }
-    if( forked && ( cudaEventRecord( ex.join, ex.side ) != cudaSuccess || cudaStreamWaitEvent( cs, ex.join, 0 ) != cudaSuccess ) )
-        return RGDN_DEVICE_ERROR;
+    if( forked )
+        for( int l = 0; l + 1 < lanes; l++ )
+            if( cudaEventRecord( ex.join[ l ], ex.side[ l ] ) != cudaSuccess || cudaStreamWaitEvent( cs, ex.join[ l ], 0 ) != cudaSuccess )
+                return RGDN_DEVICE_ERROR;
     return RGDN_SUCCESS;
 }
 
