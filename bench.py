@@ -496,7 +496,8 @@ def run_batched(args, dist: Dist, dev: int, cs) -> dict:
     from raytracedgl1_gb300.denoiser import Context, Denoiser, Stream, Tonemapping
     from raytracedgl1_gb300.scene import Scene
 
-    ctx = Context(dev)
+    # frames side by side on several lanes: no L2 set-aside (measured about 1 % faster without)
+    ctx = Context(dev, flags=N.CONTEXT_NO_L2_PERSIST)
     storage = STORAGE["fp16"]
     streams, seqs = [], []
     for r, (W, H) in enumerate(BATCH_MIX):
@@ -687,7 +688,7 @@ def run_serving(args, dist: Dist, dev: int) -> dict:
     from raytracedgl1_gb300.scene import Scene
 
     storage = STORAGE["fp16"]
-    ctx = Context(dev, memory_budget_bytes=120 * (1 << 30))
+    ctx = Context(dev, memory_budget_bytes=120 * (1 << 30), flags=N.CONTEXT_NO_L2_PERSIST)
     rng = np.random.default_rng(7 + dist.rank)
     res = [SERVE_RES[i] for i in rng.integers(0, len(SERVE_RES), size=64)]
     frames, host = {}, {}

@@ -150,7 +150,10 @@ class Image(C.Structure):
 
 
 class ContextCreateInfo(C.Structure):
-    _fields_ = [("device", C.c_int), ("memoryBudgetBytes", C.c_uint64)]
+    _fields_ = [("device", C.c_int), ("memoryBudgetBytes", C.c_uint64), ("flags", C.c_uint32)]
+
+
+CONTEXT_NO_L2_PERSIST = 0x1
 
 
 class StreamCreateInfo(C.Structure):

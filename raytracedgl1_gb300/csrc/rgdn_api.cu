@@ -27,6 +27,9 @@
 
 using namespace rgdn;
 
+// the default path marks the frame's geometry record persisting in L2
+constexpr bool kGeomL2Persist = true;
+
 namespace
 {
 // cuTensorMapEncodeTiled through the runtime's driver entry point (no libcuda link)
@@ -509,6 +512,20 @@ rgdn_status run_denoise_fused( rgdn_stream* s, uint32_t fi, const rgdn_frame_par
     if( r != RGDN_SUCCESS ) return r;
     FrameArgs a;
     fill_args( s, fi, p, a );
+    // the frame's geometry record persists in L2 for the launches of this frame
+    struct WindowScope
+    {
+        WindowScope( const rgdn_stream* s, const FrameArgs& a )
+        {
+            const size_t bytes = (size_t)s->W * s->H * 16;
+            if( kGeomL2Persist && s->ctx->l2Persist && a.geom && !tl_l2windowOff )
+            {
+                tl_l2window = { (void*)a.geom, bytes, std::min( 1.0f, (float)s->ctx->l2Persist / (float)bytes ) };
+                s->ctx->l2Dirty.store( true, std::memory_order_relaxed );
+            }
+        }
+        ~WindowScope() { tl_l2window = L2Window{}; }
+    } window( s, a );
     if( !( p->flags & RGDN_FLAG_SKIP_GRADIENTS ) )
     {
         if( ( r = launch_default_stage( s, a, fi, p, RGDN_STAGE_GRADIENT_SAMPLES, 0, cs ) ) != RGDN_SUCCESS ) return r;
@@ -753,6 +770,17 @@ rgdn_status rgdn_context_create( const rgdn_context_create_info* info, rgdn_cont
     if( !c ) return RGDN_INTERNAL_ERROR;
     c->device = info->device;
     c->budget = info->memoryBudgetBytes;
+    if( kGeomL2Persist && !( info->flags & RGDN_CONTEXT_NO_L2_PERSIST ) )
+    {
+        // L2 set aside for the geometry record (a limit of this process's context)
+        int maxPersist = 0;
+        if( cudaDeviceGetAttribute( &maxPersist, cudaDevAttrMaxPersistingL2CacheSize, info->device ) == cudaSuccess && maxPersist > 0 )
+        {
+            const size_t want = std::min< size_t >( (size_t)maxPersist, 48ull << 20 );
+            if( cudaDeviceSetLimit( cudaLimitPersistingL2CacheSize, want ) == cudaSuccess ) c->l2Persist = want;
+        }
+        cudaGetLastError();
+    }
     // normal decode tables: the correctly rounded sin/cos of the FP32 angles of Utils.h:132-133
     std::vector< float2 > ph( 65536 ), th( 65536 );
     for( uint32_t j = 0; j < 65536u; j++ )
@@ -794,6 +822,13 @@ rgdn_status rgdn_context_destroy( rgdn_context* c )
     cudaFree( c->phiTab );
     cudaFree( c->thetaTab );
     cudaFree( c->decayTab );
+    if( c->l2Persist )
+    {
+        // the set-aside ends with the rgdn context that made it
+        cudaCtxResetPersistingL2Cache();
+        cudaDeviceSetLimit( cudaLimitPersistingL2CacheSize, 0 );
+        cudaGetLastError();
+    }
     c->magic = 0;
     delete c;
     return RGDN_SUCCESS;

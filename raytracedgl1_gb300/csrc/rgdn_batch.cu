@@ -376,6 +376,16 @@ rgdn_status enqueue_step( rgdn_context* c, BatchExec& ex, DeviceSlots& ds, int s
     for( int gi = 0; gi < key.ng; gi++ ) singles += key.g[ gi ].single;
     const bool twoLanes = singles > 1 && !user && !capturing;
     const int lanes = twoLanes ? std::min( singles, 1 + kSideLanes ) : 1;
+    // frames side by side keep no persisting L2 window (rgdn_api.cu, run_denoise_fused), and
+    // unless the step is one frame alone, the lines earlier frames left persisting return to
+    // normal first, so the whole L2 serves the step
+    struct NoWindow
+    {
+        explicit NoWindow( bool on ) { tl_l2windowOff = on; }
+        ~NoWindow() { tl_l2windowOff = false; }
+    } noWindow( lanes > 1 );
+    const bool alone = key.ng == 1 && key.g[ 0 ].single;   // one frame, alone on the GPU
+    if( !alone && c->l2Dirty.exchange( false ) ) cudaCtxResetPersistingL2Cache();
     if( twoLanes )
     {
         if( cudaEventRecord( ex.fork, cs ) != cudaSuccess ) return RGDN_DEVICE_ERROR;

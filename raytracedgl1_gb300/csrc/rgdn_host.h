@@ -29,6 +29,8 @@ struct rgdn_context
     float2*                 phiTab   = nullptr;   // (sin phi_j, cos phi_j)
     float2*                 thetaTab = nullptr;   // (cos theta_k, sin theta_k)
     float*                  decayTab = nullptr;   // pow(1 - k/255, 10), k = 0..255
+    size_t                  l2Persist = 0;        // the L2 set aside for persisting accesses
+    std::atomic< bool >     l2Dirty{ false };     // a frame marked lines persisting since the last reset
     std::atomic< uint64_t > launches{ 0 };
     std::mutex              batchMtx;              // guards `batch`
     rgdn::BatchExec*        batch = nullptr;       // created by the first batched submission

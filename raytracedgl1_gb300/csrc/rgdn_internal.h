@@ -237,6 +237,19 @@ enum FusedKernel : int
     KF_TEMPORAL_FAST_GP_EARLY = 126,  // KF_TEMPORAL_FAST_GP likewise
 };
 
+// An address range the launches of this thread mark persisting in L2 while it is set (the
+// default path sets it to the frame's geometry record, which every later pass reads per tap)
+struct L2Window
+{
+    void*  ptr   = nullptr;
+    size_t bytes = 0;
+    float  hit   = 0.0f;
+};
+inline thread_local L2Window tl_l2window;
+// set while a batched step runs frames side by side on several lanes: their windows would
+// compete for the same set-aside L2, which measured slower than none
+inline thread_local bool tl_l2windowOff = false;
+
 // Launches one stage for one frame. Returns the CUDA error of the launch.
 typedef cudaError_t ( *StageLauncher )( const FrameArgs& a, int stage, int iter, cudaStream_t s );
 

@@ -33,11 +33,21 @@ cudaError_t launch_pdl( void ( *kernel )( KP... ), dim3 grid, dim3 block, size_t
     cfg.blockDim           = block;
     cfg.dynamicSmemBytes   = smem;
     cfg.stream             = s;
-    cudaLaunchAttribute at;
-    at.id                                         = cudaLaunchAttributeProgrammaticStreamSerialization;
-    at.val.programmaticStreamSerializationAllowed = 1;
-    cfg.attrs                                     = &at;
-    cfg.numAttrs                                  = 1;
+    cudaLaunchAttribute at[ 2 ];
+    at[ 0 ].id                                         = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[ 0 ].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs                                          = at;
+    cfg.numAttrs                                       = 1;
+    if( tl_l2window.ptr )
+    {
+        at[ 1 ].id                                 = cudaLaunchAttributeAccessPolicyWindow;
+        at[ 1 ].val.accessPolicyWindow.base_ptr    = tl_l2window.ptr;
+        at[ 1 ].val.accessPolicyWindow.num_bytes   = tl_l2window.bytes;
+        at[ 1 ].val.accessPolicyWindow.hitRatio    = tl_l2window.hit;
+        at[ 1 ].val.accessPolicyWindow.hitProp     = cudaAccessPropertyPersisting;
+        at[ 1 ].val.accessPolicyWindow.missProp    = cudaAccessPropertyStreaming;
+        cfg.numAttrs                               = 2;
+    }
     return cudaLaunchKernelEx( &cfg, kernel, std::forward< A >( args )... );
 }
 

@@ -49,9 +49,10 @@ def _stream_handle(cuda_stream) -> Optional[int]:
 class Context:
     """One CUDA device, its normal-decode tables and the streams' memory budget."""
 
-    def __init__(self, device: int = 0, memory_budget_bytes: int = 0):
+    def __init__(self, device: int = 0, memory_budget_bytes: int = 0, flags: int = 0):
+        """flags: CONTEXT_* (CONTEXT_NO_L2_PERSIST for contexts that run frames side by side)."""
         self.lib = N.load()
-        info = N.ContextCreateInfo(device, memory_budget_bytes)
+        info = N.ContextCreateInfo(device, memory_budget_bytes, flags)
         h = C.c_void_p()
         N.check(self.lib.rgdn_context_create(C.byref(info), C.byref(h)), "rgdn_context_create")
         self.handle = h
