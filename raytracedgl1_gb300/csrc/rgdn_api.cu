@@ -27,8 +27,14 @@
 
 using namespace rgdn;
 
-// the default path marks the frame's geometry record persisting in L2
-constexpr bool kGeomL2Persist = true;
+// the default path marks the frame's geometry record persisting in L2 (kGeomBothSlots: both
+// frame slots' records, so the temporal pass's previous-frame taps hit as well), with up to
+// kL2PersistMB of L2 set aside. On GB300 at 1080p: 0.5065 ms per frame with 48 MB and the
+// current slot, 0.5068 with 34 MB, 0.5786 with 80 MB and both slots (too little L2 left for the
+// passes' other planes), 0.517 without the window.
+constexpr bool   kGeomL2Persist = true;
+constexpr bool   kGeomBothSlots = false;
+constexpr size_t kL2PersistMB   = 48;
 
 namespace
 {
@@ -517,10 +523,12 @@ rgdn_status run_denoise_fused( rgdn_stream* s, uint32_t fi, const rgdn_frame_par
     {
         WindowScope( const rgdn_stream* s, const FrameArgs& a )
         {
-            const size_t bytes = (size_t)s->W * s->H * 16;
+            const size_t one   = (size_t)s->W * s->H * 16;
+            void*        base  = kGeomBothSlots ? (void*)s->geom[ 0 ] : (void*)a.geom;
+            const size_t bytes = kGeomBothSlots ? (size_t)( (uint8_t*)s->geom[ 1 ] - (uint8_t*)s->geom[ 0 ] ) + one : one;
             if( kGeomL2Persist && s->ctx->l2Persist && a.geom && !tl_l2windowOff )
             {
-                tl_l2window = { (void*)a.geom, bytes, std::min( 1.0f, (float)s->ctx->l2Persist / (float)bytes ) };
+                tl_l2window = { base, bytes, std::min( 1.0f, (float)s->ctx->l2Persist / (float)bytes ) };
                 s->ctx->l2Dirty.store( true, std::memory_order_relaxed );
             }
         }
@@ -776,7 +784,7 @@ rgdn_status rgdn_context_create( const rgdn_context_create_info* info, rgdn_cont
         int maxPersist = 0;
         if( cudaDeviceGetAttribute( &maxPersist, cudaDevAttrMaxPersistingL2CacheSize, info->device ) == cudaSuccess && maxPersist > 0 )
         {
-            const size_t want = std::min< size_t >( (size_t)maxPersist, 48ull << 20 );
+            const size_t want = std::min< size_t >( (size_t)maxPersist, kL2PersistMB << 20 );
             if( cudaDeviceSetLimit( cudaLimitPersistingL2CacheSize, want ) == cudaSuccess ) c->l2Persist = want;
         }
         cudaGetLastError();
