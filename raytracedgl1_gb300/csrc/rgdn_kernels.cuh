@@ -757,9 +757,25 @@ __device__ __forceinline__ void gradient_atrous_px( const FrameArgs& a, const in
     gradient_atrous_core( a.u, src, dst, a.disHist, gx, gy, iter, u8 );
 }
 
+// u / 255 for the 256 unorm8 codes, each the correctly rounded binary32 quotient: folded at
+// compile time (IEEE division, as the device's) into a table in global memory, so a block fills
+// its shared copy with loads instead of 256 divisions
+struct U8Table
+{
+    float v[ 256 ];
+};
+constexpr U8Table make_u8_table()
+{
+    U8Table t{};
+    for( int k = 0; k < 256; k++ ) t.v[ k ] = (float)k / 255.0f;
+    return t;
+}
+static __device__ const U8Table g_u8 = make_u8_table();
+__device__ __forceinline__ float u8_value( int k ) { return __ldg( &g_u8.v[ k ] ); }
+
 __device__ __forceinline__ void fill_u8( float* u8, int t )
 {
-    u8[ t ] = (float)t / 255.0f;
+    u8[ t ] = u8_value( t );
 }
 
 // Programmatic dependent launch. Every kernel of the path lets its successor's blocks be
@@ -2282,7 +2298,7 @@ __global__ void __launch_bounds__( NT, MINB ) k_atrous( const FrameArgs a, const
 #pragma unroll
     for( int k = t; k < 256; k += NT )
     {
-        u8[ k ] = (float)k / 255.0f;
+        u8[ k ] = u8_value( k );
         if( HIST ) hist[ k ] = 0u;
     }
     pdl_wait();
@@ -2550,7 +2566,7 @@ __global__ void __launch_bounds__( 256, MINB ) k_atrous_pair01( const FrameArgs 
     __shared__ float         u8[ 256 ];
     const int                t = threadIdx.y * 32 + threadIdx.x;
     pdl_launch_dependents();
-    u8[ t ] = (float)t / 255.0f;
+    u8[ t ] = u8_value( t );
     pdl_wait();
     __syncthreads();
     atrous_pair_tile< M >( a, blockIdx.x, blockIdx.y, smem, u8 );
@@ -2790,7 +2806,7 @@ __global__ void __launch_bounds__( 256, 3 ) k_atrous_tma( const FrameArgs a, con
         mbar_init( &bar[ 1 ], 1 );
         fence_async_shared();
     }
-    u8[ t ] = (float)t / 255.0f;
+    u8[ t ] = u8_value( t );
     if( HIST ) hist[ t ] = 0u;
     __syncthreads();
     const int first = (int)blockIdx.x;
@@ -3128,7 +3144,7 @@ __global__ void __launch_bounds__( 256, MINB ) kb_atrous( const int sarg, const 
     __shared__ float    u8[ 256 ];
     __shared__ uint32_t hist[ HM ? 256 : 1 ];
     const int t = threadIdx.y * blockDim.x + threadIdx.x;
-    u8[ t ]     = (float)t / 255.0f;
+    u8[ t ]     = u8_value( t );
     if( HM ) hist[ t ] = 0u;
     pdl_wait();
     __syncthreads();
@@ -3167,7 +3183,7 @@ template< int M, int HM > __global__ void __launch_bounds__( 128, 7 ) kt_atrous(
     pdl_launch_dependents();
     for( int k = t; k < 256; k += 128 )
     {
-        u8[ k ] = (float)k / 255.0f;
+        u8[ k ] = u8_value( k );
         if( HM ) hist[ k ] = 0u;
     }
     int        j = 0, bx = 0, by = 0;
@@ -3194,7 +3210,7 @@ template< int M > __global__ void __launch_bounds__( 256, 3 ) kt_atrous_pair01( 
     __shared__ float         u8[ 256 ];
     const int                t = threadIdx.y * 32 + threadIdx.x;
     pdl_launch_dependents();
-    u8[ t ] = (float)t / 255.0f;
+    u8[ t ] = u8_value( t );
     int        j = 0, bx = 0, by = 0;
     const bool has = batch_tile_of_block< false >( sarg, BS_ATROUS0, j, bx, by );
     pdl_wait();
@@ -3901,7 +3917,7 @@ __device__ __forceinline__ float4 scatter_pixel( const ScatterArgs& a, int cx, i
 template< int M, bool FAST > __global__ void __launch_bounds__( 256, 6 ) k_scatter_accum( const ScatterArgs a )
 {
     __shared__ float inv255[ 256 ];
-    for( int t = threadIdx.y * blockDim.x + threadIdx.x; t < 256; t += blockDim.x * blockDim.y ) inv255[ t ] = (float)t / 255.0f;
+    for( int t = threadIdx.y * blockDim.x + threadIdx.x; t < 256; t += blockDim.x * blockDim.y ) inv255[ t ] = u8_value( t );
     __syncthreads();
     const int cx = blockIdx.x * blockDim.x + threadIdx.x, cy = blockIdx.y * blockDim.y + threadIdx.y;
     pdl_launch_dependents();
