@@ -2107,15 +2107,15 @@ __device__ __forceinline__ void atrous_terms_r( AtrousCtr& c, AtrousAcc& acc, co
                                                 const int iter )
 {
     c.l             = Wm< FAST >::lum( acc.d );
-    c.wLumMul       = ( FAST ? kLog2e : 1.0f ) / ( 4.0f * prefVar + 0.00001f );
+    c.wLumMul       = FAST ? kLog2e * rcp_approx( 4.0f * prefVar + 0.00001f ) : 1.0f / ( 4.0f * prefVar + 0.00001f );
     c.roughness     = roughness;
     c.wRoughMul     = gclamp( c.roughness * 30.0f - (float)iter, 0.0f, 1.0f );
     const float nws = gclamp( hS / 8.0f, 0.0f, 1.0f );
     c.nwSpec        = gclamp( spec_power( c.roughness * c.roughness ), 8.0f, 1024.0f ) * nws;
     // FAST: one reciprocal per tap distance class (|x|+|y| = 1 or 2), scaled for the exponent
     // domain
-    c.rz1  = FAST ? kSqrtLog2e / fmaxf( c.gradDepth * 1.0f, 0.01f ) : 0.0f;
-    c.rz2  = FAST ? kSqrtLog2e / fmaxf( c.gradDepth * 2.0f, 0.01f ) : 0.0f;
+    c.rz1  = FAST ? kSqrtLog2e * rcp_approx( fmaxf( c.gradDepth * 1.0f, 0.01f ) ) : 0.0f;
+    c.rz2  = FAST ? kSqrtLog2e * rcp_approx( fmaxf( c.gradDepth * 2.0f, 0.01f ) ) : 0.0f;
     acc.ws = acc.wsS = acc.wsI = 1.0f;
 }
 template< bool FAST >
@@ -2175,9 +2175,13 @@ __device__ __forceinline__ bool atrous_centre( const FrameArgs& a, const AtrousI
     return true;
 }
 
+// FAST: the hardware reciprocals of the weight sums (each sum is at least the centre weight 1)
+template< bool FAST >
 __device__ __forceinline__ void atrous_finish( AtrousAcc& acc, float3& outDiff, float& outVar, float3& outSpec, float3& outInd )
 {
-    const float inv = 1.0f / acc.ws, invS = 1.0f / acc.wsS, invI = 1.0f / acc.wsI;
+    const float inv  = FAST ? rcp_approx( acc.ws ) : 1.0f / acc.ws;
+    const float invS = FAST ? rcp_approx( acc.wsS ) : 1.0f / acc.wsS;
+    const float invI = FAST ? rcp_approx( acc.wsI ) : 1.0f / acc.wsI;
     outDiff = mul( acc.d, inv );
     outVar  = acc.var * ( inv * inv );   // outVariance *= invWeightSum * invWeightSum (CmSVGFAtrous.comp:217)
     outSpec = mul( acc.s, invS );
@@ -2230,7 +2234,7 @@ __device__ __forceinline__ void atrous_px( const FrameArgs& a, const AtrousIO& i
             atrous_accum< FAST, INTERIOR >( c, acc, xx, yy, qx, qy, rq, nq, zq, cvq, sq, iq );
         }
     }
-    atrous_finish( acc, outDiff, outVar, outSpec, outInd );
+    atrous_finish< FAST >( acc, outDiff, outVar, outSpec, outInd );
 }
 
 // The tile of one a-trous iteration. HIST adds the bins of this tile's HistogramInput values
@@ -2419,7 +2423,7 @@ __device__ __forceinline__ AtrousOut atrous_sm_px( const FrameArgs& a, const int
     };
     if( interior ) taps( std::true_type() );
     else taps( std::false_type() );
-    atrous_finish( acc, o.d, o.var, o.s, o.i );
+    atrous_finish< true >( acc, o.d, o.var, o.s, o.i );
     return o;
 }
 
@@ -2742,7 +2746,7 @@ __device__ __forceinline__ void atrous_px_tma( const FrameArgs& a, const AtrousI
                                             L::col( bSp, k ), L::col( bIn, k ) );
         }
     }
-    atrous_finish( acc, outDiff, outVar, outSpec, outInd );
+    atrous_finish< FAST >( acc, outDiff, outVar, outSpec, outInd );
 }
 
 // Issues the TMA copies of tile (x0, y0)'s footprint into one stage (thread 0 only).
