@@ -1857,7 +1857,11 @@ __global__ void __launch_bounds__( 256, ( M == MODE_F16 || M == MODE_BF16 ) ? 4 
 // CmSVGFAtrous_Iter0.comp:158-335 and CmSVGFAtrous.comp:71-349 — one a-trous iteration;
 // the last one composes PreFinal and HistogramInput instead of storing ping/pong.
 // ==========================================================================================
-__device__ __forceinline__ float spec_power( float alpha ) { return fmaxf( 0.01f, 2.0f / ( alpha * alpha + 1e-4f ) - 2.0f ); }
+// FAST: the hardware reciprocal (the power is an exponent of a continuous weight)
+template< bool FAST = false > __device__ __forceinline__ float spec_power( float alpha )
+{
+    return fmaxf( 0.01f, ( FAST ? 2.0f * rcp_approx( alpha * alpha + 1e-4f ) : 2.0f / ( alpha * alpha + 1e-4f ) ) - 2.0f );
+}
 
 struct AtrousIO
 {
@@ -2111,7 +2115,7 @@ __device__ __forceinline__ void atrous_terms_r( AtrousCtr& c, AtrousAcc& acc, co
     c.roughness     = roughness;
     c.wRoughMul     = gclamp( c.roughness * 30.0f - (float)iter, 0.0f, 1.0f );
     const float nws = gclamp( hS / 8.0f, 0.0f, 1.0f );
-    c.nwSpec        = gclamp( spec_power( c.roughness * c.roughness ), 8.0f, 1024.0f ) * nws;
+    c.nwSpec        = gclamp( spec_power< FAST >( c.roughness * c.roughness ), 8.0f, 1024.0f ) * nws;
     // FAST: one reciprocal per tap distance class (|x|+|y| = 1 or 2), scaled for the exponent
     // domain
     c.rz1  = FAST ? kSqrtLog2e * rcp_approx( fmaxf( c.gradDepth * 1.0f, 0.01f ) ) : 0.0f;
@@ -2166,7 +2170,7 @@ __device__ __forceinline__ bool atrous_centre( const FrameArgs& a, const AtrousI
             for( int xx = -1; xx <= 1; xx++ )
                 r = r + ldcvz< M >( a, io.diffSrc, io.varSrc, px + xx, py + yy ).w * g[ xx < 0 ? -xx : xx ][ yy < 0 ? -yy : yy ];
         }
-        r = sqrtf( fmaxf( r, 0.0f ) );
+        r = FAST ? sqrt_approx( fmaxf( r, 0.0f ) ) : sqrtf( fmaxf( r, 0.0f ) );
         S::st1( a.filtVar, (size_t)i, r );
         prefVar = r;
     }
@@ -2400,7 +2404,7 @@ __device__ __forceinline__ AtrousOut atrous_sm_px( const FrameArgs& a, const int
             for( int xx = -1; xx <= 1; xx++ )
                 r = r + C[ cc + yy * RC + xx ].w * gw[ xx < 0 ? -xx : xx ][ yy < 0 ? -yy : yy ];
         }
-        prefVar = sqrtf( fmaxf( r, 0.0f ) );
+        prefVar = sqrt_approx( fmaxf( r, 0.0f ) );   // the FAST form of atrous_centre
         o.pref  = true;
     }
     o.prefVar = prefVar;
@@ -2723,7 +2727,7 @@ __device__ __forceinline__ void atrous_px_tma( const FrameArgs& a, const AtrousI
 #pragma unroll
             for( int xx = -1; xx <= 1; xx++ ) r = r + L::cv( bCv, bVar, kidx( xx, yy ) ).w * gk[ xx < 0 ? -xx : xx ][ yy < 0 ? -yy : yy ];
         }
-        r = sqrtf( fmaxf( r, 0.0f ) );
+        r = FAST ? sqrt_approx( fmaxf( r, 0.0f ) ) : sqrtf( fmaxf( r, 0.0f ) );
         S::st1( a.filtVar, (size_t)i, r );
         prefVar = r;
     }
