@@ -874,8 +874,10 @@ __device__ __forceinline__ float parallax( const Uniform& u, float3 pos, float3 
 constexpr bool kTemporalEarlyHistory = true;
 // the temporal pass reads the surface positions before the taps rather than where they are used
 constexpr bool kTemporalEarlySurfPos = false;
-// the temporal pass prefetches the history rows under its bilinear footprint into L2
-constexpr bool kTemporalL2Prefetch = true;
+// the temporal pass prefetches the history rows under its bilinear footprint into L2 (once
+// 4 % faster; with the geometry record persisting in L2 and the other later changes the pass ran
+// 98.8 us without the prefetch against 102.4 with it, A/B/A/B on GB300)
+constexpr bool kTemporalL2Prefetch = false;
 // the temporal pass reads this frame's unfiltered colours and view ray before its taps
 constexpr bool kTemporalEarlyInputs = true;
 template< int M, bool FAST, bool GEOM, bool GEOMPREV, bool EARLY = false >
